@@ -1,0 +1,161 @@
+/* sray_gpu.h -- C-ABI of the GB300 rendering path (libsray_gpu.so).
+ *
+ * This library replaces the rendering hot path of S-ray: the per-frame
+ * entry point render() and everything below it (octree traversal, the
+ * triangle/sphere/cylinder intersectors, photon emission and tracing, the
+ * photon-map gathers, Phong shading with reflection/refraction and the
+ * final gather, adaptive supersampling and the tpool block scheduler).
+ * The scene stays in S-ray's XML format and its meaning is unchanged.
+ *
+ * Conventions: every entry point returns 0 on success and a negative
+ * SRAY_E* code on failure; sray_gpu_last_error() then returns a message.
+ * No C++ types or exceptions cross this boundary.  One renderer context
+ * per process, bound to the CUDA device current at sray_gpu_init().
+ * Functions that take a `stream` argument enqueue on that CUDA stream
+ * (NULL = the legacy default stream) and return once the result is
+ * available unless stated otherwise.
+ */
+#ifndef SRAY_GPU_H_
+#define SRAY_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SRAY_RAY_MAGNITUDE 10000.0   /* src/opt.h:21 */
+
+enum {
+	SRAY_OK = 0,
+	SRAY_EINVAL = -1,      /* bad argument */
+	SRAY_ELOAD = -2,       /* scene file missing or malformed */
+	SRAY_ECUDA = -3,       /* CUDA runtime error */
+	SRAY_ESTATE = -4,      /* call out of order (e.g. render before load) */
+	SRAY_EDEVICE = -5,     /* a kernel raised its error word (queue overflow, bounded wait expired) */
+	SRAY_ENOMEM = -6
+};
+
+/* Render options.  Field meanings and defaults follow the reference's
+ * struct options (src/opt.h:38-62, defaults src/opt.c:357-388); fields
+ * after `meshoct_max_items` are extensions of this library. */
+typedef struct sray_opts {
+	int width, height;             /* -s WxH                  (640x480) */
+	int min_samples, max_samples;  /* -r min[-max]            (1-1) */
+	float max_var;                 /* -d max sample variance  (0.005) */
+	float min_energy;              /* -e ray energy cut-off   (0.0001) */
+	int shadow_samples;            /* -shadowrays             (1) */
+	int diffuse_samples;           /* -diffuserays            (1) */
+	int threads;                   /* -t host threads of the CPU path (0 = all) */
+	int blk_sz;                    /* -b tile size            (48) */
+	int iter;                      /* -i max recursion depth  (7) */
+	int fps;                       /* -f                      (30) */
+	int mblur;                     /* -m motion blur          (0) */
+	int shutter;                   /* -u shutter ms           (0) */
+	int time_start, time_end;      /* -a range                (0-0) */
+	int caust_photons, gi_photons; /* -c, -g                  (0, 0) */
+	float gather_dist;             /* -gatherdisc, fraction of the scene diagonal (0.001) */
+	float photon_energy;           /* -photonenergy           (300) */
+	int scnoct_max_depth, scnoct_max_items;   /* -soctdepth/-soctitems (5/5) */
+	int meshoct_max_depth, meshoct_max_items; /* -moctdepth/-moctitems (7/14) */
+	/* ---- extensions ---- */
+	int caust_k;                   /* >0: k-nearest caustic gather instead of the fixed-radius range */
+	int gi_k;                      /* >0: k-nearest global gather */
+	float gather_rcap;             /* radius cap of the k-nearest gathers (scene units) */
+	int rng_paths;                 /* 1: shading draws keyed by the ray's path in the shading tree */
+	uint64_t seed;                 /* Philox key of every random stream */
+	int reserved[8];
+} sray_opts;
+
+/* Fill `o` with the reference defaults (src/opt.c:357-388). */
+void sray_default_opts(sray_opts *o);
+
+/* Create the renderer context on the current CUDA device.
+ * Replaces rend_init(Image*) (src/render.cc:22-32): the framebuffer is
+ * passed to sray_gpu_render() instead of being bound here. */
+int sray_gpu_init(const sray_opts *opt);
+
+/* Change options after init (e.g. photon counts, sample counts). */
+int sray_gpu_set_opts(const sray_opts *opt);
+
+/* Load an S-ray XML scene.  Replaces Scene::load(const char*)
+ * (src/scene.cc:93-183): materials first, then env/object/light/camera,
+ * meshes built with the mesh octree options (src/meshload.cc:55-157). */
+int sray_gpu_load_scene(const char *xml_path);
+
+/* Same, from an in-memory XML document of `len` bytes. */
+int sray_gpu_load_scene_mem(const char *xml, size_t len);
+
+/* Scene summary: counts of objects, lights, materials, triangles (summed
+ * over mesh objects), unique device meshes. */
+int sray_gpu_scene_info(int *n_objects, int *n_lights, int *n_materials,
+		int64_t *n_triangles, int *n_unique_meshes);
+
+/* Build the acceleration structures for the shutter interval [t0, t1]
+ * (ms).  Replaces Scene::build_tree (src/scene.cc:353-390). */
+int sray_gpu_build(long t0, long t1);
+
+/* Shoot the caustic and global photon maps for [t0, t1] and build the
+ * device photon maps.  Replaces shoot_photons (src/render.cc:67-122),
+ * Scene::build_caustics_map/build_global_map (src/scene.cc:445-534) and
+ * PhotonMap::add_photon/scale_photon_power (src/pmap.cc:73-100).
+ * The stored counts are returned through the optional pointers. */
+int sray_gpu_shoot_photons(long t0, long t1, int *caust_stored, int *gi_stored, void *stream);
+
+/* Render frame `msec` into an RGBA float32 framebuffer of width*height*4
+ * floats (row-major, as the reference's Image, src/render.cc:210-243).
+ * `fb_is_device` = 0: `fb` is host memory and is written on return;
+ * 1: `fb` is device memory on this context's device.
+ * Replaces render(long msec) (src/render.cc:34-55) including the accel
+ * build and photon shooting of that frame. */
+int sray_gpu_render(long msec, float *fb, int fb_is_device, void *stream);
+
+/* Render only (acceleration structures and photon maps already built by
+ * sray_gpu_build / sray_gpu_shoot_photons for the frame containing `msec`):
+ * the block loop of render_frame (src/render.cc:124-244). */
+int sray_gpu_render_pixels(long msec, float *fb, int fb_is_device, void *stream);
+
+/* Closest hit of `n` rays given in world space (origin xyz, dir xyz with
+ * the segment parameter t in [eps, 1], integer time) -- the GPU form of
+ * Scene::cast_ray (src/scene.cc:764-794).  All arrays are device pointers.
+ * Outputs: object index (-1 = miss), primitive index (triangle index of the
+ * object's mesh, 0 for spheres/cylinders), the hit parameter t, and a flag
+ * byte that is 1 when another primitive was found at exactly the same t. */
+int sray_gpu_cast_rays(int n, const float *orig, const float *dir, const int *time,
+		int *obj, int *prim, float *t, unsigned char *tie, void *stream);
+
+/* Primary rays of frame `msec`, sample 0, and their closest hits: per pixel
+ * object index, primitive index, t and tie flag (device pointers of
+ * width*height entries).  Parity probe for src/camera.cc:119-142 + cast_ray. */
+int sray_gpu_primary_hits(long msec, int *obj, int *prim, float *t, unsigned char *tie, void *stream);
+
+/* Copy the stored photons of map `which` (0 = caustic, 1 = global) to host
+ * memory as 16 floats each: pos xyz, dir xyz, norm xyz, power rgba, and
+ * three unused.  `cap` is the capacity in photons; returns the count through
+ * `n_out`.  Photons are in Morton order. */
+int sray_gpu_get_photons(int which, float *out, int cap, int *n_out);
+
+/* Device-side statistics of the last render: rays traced per kind. */
+typedef struct sray_stats {
+	int64_t primary_rays, shadow_rays, secondary_rays, gather_rays;
+	int64_t photons_emitted, photons_stored, gathers;
+	int64_t samples;               /* pixel samples taken (adaptive) */
+	int64_t node_visits, prim_tests;  /* traversal work (when counting is on) */
+	int kernel_launches;           /* kernels launched by the last render */
+	int reserved[7];
+} sray_stats;
+
+int sray_gpu_get_stats(sray_stats *st);
+
+/* Copy the last error message (NUL-terminated, truncated to `cap`). */
+int sray_gpu_last_error(char *buf, size_t cap);
+
+/* Release every device buffer and the context. */
+void sray_gpu_shutdown(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SRAY_GPU_H_ */

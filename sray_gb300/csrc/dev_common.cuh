@@ -1,0 +1,638 @@
+/* dev_common.cuh -- device routines shared by the render and photon kernels:
+ * the scene descriptor, float intersection tests written in the reference's
+ * operation order, the two-level octree traversal (closest hit and any
+ * hit), surface-point reconstruction and light sampling.
+ *
+ * All files that include this are compiled with -fmad=false (no FMA
+ * contraction) and IEEE division/square root, so every float operation
+ * below rounds exactly like the CPU oracle's float path.
+ */
+#ifndef SRAY_DEV_COMMON_CUH_
+#define SRAY_DEV_COMMON_CUH_
+
+#include <stdint.h>
+#include <float.h>
+#include <cuda_runtime.h>
+#include "sray_device.h"
+#include "sray_rng.h"
+
+namespace sray {
+
+/* photon map on the device: photons in Morton order of their grid cell,
+ * a dense table of (first, count) per cell */
+struct DPhotonMap {
+	const DevPhoton *ph;
+	const uint2 *cells;       /* per linear cell: first photon, count */
+	int n;
+	int dims[3];
+	float org[3];
+	float cell;
+	int k;                    /* 0 = fixed-radius range gather, >0 = k nearest */
+	double range;             /* query radius as the kd-tree sees it (float-rounded) */
+	float inv_area;           /* range mode: 1 / (pi r^2) of the unrounded radius */
+};
+
+struct DScene {
+	const DevNode *snodes;    /* top-level octree (world space) */
+	const int *sslots;
+	int has_scene;
+	const DevNode *mnodes;    /* mesh octrees (object space) */
+	const DevTri *mtris;
+	const int *mprim;
+	const DevObj *objs;
+	int nobj;
+	const float *xf;          /* per object per time, XF_STRIDE floats */
+	int tlo, nt;
+	const float *tri_pos;     /* 9 floats per unique-mesh triangle */
+	const float *tri_attr;    /* 24 floats per unique-mesh triangle */
+	const DevMat *mats;
+	DevMat defmat;
+	const DevLight *lights;
+	int nlights;
+	const float *light_pos;   /* 4 floats per light per time */
+	const uint32_t *projbits; /* per light: 64 words global map + 64 words caustic map */
+	const float *coverage;    /* per light: global, caustic */
+	const float *cam_m;       /* 12 floats per time */
+	float cam_f, cam_xsz, cam_ysz, cam_maxd;
+	float env_col[4], env_amb[4];
+	float eps, xsmall;
+	float min_energy;
+	int iter, diffuse_samples, shadow_samples;
+	int gi_on, caust_on;
+	int width, height;
+	int mblur, shutter;
+	int t0, t1;
+	uint64_t seed;
+	float photon_energy;
+	float max_cos;
+	DPhotonMap caust, gi;
+};
+
+/* ---------------- float3 helpers (no contraction: built with -fmad=false) */
+struct V3 { float x, y, z; };
+__device__ __forceinline__ V3 mk(float x, float y, float z) { V3 v; v.x = x; v.y = y; v.z = z; return v; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ V3 operator-(V3 a) { return mk(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ V3 operator*(V3 a, float s) { return mk(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ V3 operator/(V3 a, float s) { return mk(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V3 cross(V3 a, V3 b) { return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+__device__ __forceinline__ float len(V3 a) { return sqrtf(dot(a, a)); }
+__device__ __forceinline__ V3 normalized(V3 a) { float l = len(a); return mk(a.x / l, a.y / l, a.z / l); }
+/* reflection of a vector travelling towards the surface */
+__device__ __forceinline__ V3 reflection(V3 v, V3 n) { return v - n * (2.0f * dot(v, n)); }
+__device__ __forceinline__ V3 refraction(V3 v, V3 n, float ior)
+{
+	float cos_inc = dot(v, -n);
+	float radical = 1.0f + (ior * ior) * (cos_inc * cos_inc - 1.0f);
+	if(radical < 0.0f) return reflection(v, n);
+	float beta = ior * cos_inc - sqrtf(radical);
+	return v * ior + n * beta;
+}
+
+__device__ __forceinline__ V3 mul_pt(const float *m, V3 p)
+{
+	return mk(m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3],
+			m[4] * p.x + m[5] * p.y + m[6] * p.z + m[7],
+			m[8] * p.x + m[9] * p.y + m[10] * p.z + m[11]);
+}
+__device__ __forceinline__ V3 mul_dir(const float *m, V3 p)
+{
+	return mk(m[0] * p.x + m[1] * p.y + m[2] * p.z,
+			m[4] * p.x + m[5] * p.y + m[6] * p.z,
+			m[8] * p.x + m[9] * p.y + m[10] * p.z);
+}
+__device__ __forceinline__ V3 mul_n(const float *m, V3 p)
+{
+	return mk(m[0] * p.x + m[1] * p.y + m[2] * p.z,
+			m[3] * p.x + m[4] * p.y + m[5] * p.z,
+			m[6] * p.x + m[7] * p.y + m[8] * p.z);
+}
+
+__device__ __forceinline__ int time_index(const DScene &S, int time)
+{
+	int ti = time - S.tlo;
+	return ti < 0 ? 0 : (ti >= S.nt ? S.nt - 1 : ti);
+}
+
+__device__ __forceinline__ const float *obj_xf(const DScene &S, int obj, int ti)
+{
+	return S.xf + ((size_t)obj * S.nt + ti) * XF_STRIDE;
+}
+
+/* ---------------- random draws (float) ---------------- */
+__device__ __forceinline__ float frand(sray_rng *s, float range) { return range * sray_rng_uniform_f(s); }
+__device__ __forceinline__ V3 sphrand(sray_rng *s, float rad)
+{
+	float u0 = sray_rng_uniform_f(s);
+	float u1 = sray_rng_uniform_f(s);
+	float z = 2.0f * u1 - 1.0f;
+	float sxy = sqrtf(1.0f - z * z);
+	float sn, cs;
+	sray_sincos_turns_f(u0, &sn, &cs);
+	return mk(rad * cs * sxy, rad * sn * sxy, rad * z);
+}
+
+/* ---------------- intersection tests ---------------- */
+struct RayT {
+	V3 o, d, inv;
+};
+
+/* AABox::intersect (src/aabb.cc:81-125); also returns the entry parameter */
+__device__ __forceinline__ bool box_hit(const float *mn, const float *mx, const RayT &r, float &tentry)
+{
+	int xs = r.d.x < 0.0f;
+	float tmin = ((xs ? mx[0] : mn[0]) - r.o.x) * r.inv.x;
+	float tmax = ((xs ? mn[0] : mx[0]) - r.o.x) * r.inv.x;
+	int ys = r.d.y < 0.0f;
+	float tymin = ((ys ? mx[1] : mn[1]) - r.o.y) * r.inv.y;
+	float tymax = ((ys ? mn[1] : mx[1]) - r.o.y) * r.inv.y;
+	if((tmin > tymax) || (tymin > tmax)) return false;
+	if(tymin > tmin) tmin = tymin;
+	if(tymax < tmax) tmax = tymax;
+	int zs = r.d.z < 0.0f;
+	float tzmin = ((zs ? mx[2] : mn[2]) - r.o.z) * r.inv.z;
+	float tzmax = ((zs ? mn[2] : mx[2]) - r.o.z) * r.inv.z;
+	if((tmin > tzmax) || (tzmin > tmax)) return false;
+	if(tzmin > tmin) tmin = tzmin;
+	if(tzmax < tmax) tmax = tzmax;
+	tentry = tmin;
+	return (tmin < 1.0f) && (tmax > 0.0f);
+}
+
+/* Triangle::intersect (src/mesh.cc:117-165) without the surface point;
+ * `limit` lets the caller skip the edge tests of candidates that cannot win */
+__device__ __forceinline__ bool tri_hit(const float4 a, const float4 b, const float4 c, const RayT &r, float eps,
+		float limit, float &t)
+{
+	V3 n = mk(a.w, b.w, c.w);
+	float ndd = dot(n, r.d);
+	if(fabsf(ndd) < eps) return false;
+	V3 v0 = mk(a.x, a.y, a.z);
+	V3 vo = r.o - v0;
+	t = -dot(n, vo) / ndd;
+	if(t < eps || t > 1.0f) return false;
+	if(t > limit) return false;
+	V3 v1 = mk(b.x, b.y, b.z), v2 = mk(c.x, c.y, c.z);
+	V3 pos = r.o + r.d * t;
+	if(!(dot(cross(v1 - v0, pos - v0), n) >= 0.0f)) return false;
+	if(!(dot(cross(v2 - v1, pos - v1), n) >= 0.0f)) return false;
+	if(!(dot(cross(v0 - v2, pos - v2), n) >= 0.0f)) return false;
+	return true;
+}
+
+/* Sphere::intersect (src/sphere.cc:85-131), object space */
+__device__ __forceinline__ bool sphere_hit(const RayT &r, float rad, float eps, float &dist)
+{
+	float a = dot(r.d, r.d);
+	float b = 2.0f * r.d.x * r.o.x + 2.0f * r.d.y * r.o.y + 2.0f * r.d.z * r.o.z;
+	float c = dot(r.o, r.o) - rad * rad;
+	float d = b * b - 4.0f * a * c;
+	if(d < 0.0f) return false;
+	float sq = sqrtf(d);
+	float t1 = (-b + sq) / (2.0f * a);
+	float t2 = (-b - sq) / (2.0f * a);
+	if((t1 < eps && t2 < eps) || (t1 > 1.0f && t2 > 1.0f)) return false;
+	if(t1 < eps) t1 = t2;
+	if(t2 < eps) t2 = t1;
+	dist = t1 < t2 ? t1 : t2;
+	return true;
+}
+
+/* Cylinder::intersect (src/cylinder.cc:125-185), object space */
+__device__ __forceinline__ bool cylinder_hit(const RayT &r, float rad, float start, float end, float eps, float &dist)
+{
+	float a = r.d.x * r.d.x + r.d.z * r.d.z;
+	float b = 2.0f * r.d.x * r.o.x + 2.0f * r.d.z * r.o.z;
+	float c = r.o.x * r.o.x + r.o.z * r.o.z - rad * rad;
+	float d = b * b - 4.0f * a * c;
+	if(d < 0.0f) return false;
+	float sq = sqrtf(d);
+	float t1 = (-b + sq) / (2.0f * a);
+	float t2 = (-b - sq) / (2.0f * a);
+	if((t1 < eps && t2 < eps) || (t1 > 1.0f && t2 > 1.0f)) return false;
+	V3 p1 = r.o + r.d * t1;
+	V3 p2 = r.o + r.d * t2;
+	bool v0 = true, v1 = true;
+	if(t1 < eps || p1.y < start || p1.y >= end) { v0 = false; t1 = t2; }
+	if(t2 < eps || p2.y < start || p2.y >= end) { v1 = false; t2 = t1; }
+	if(!v0 && !v1) return false;
+	dist = t1 < t2 ? t1 : t2;
+	return true;
+}
+
+__device__ __forceinline__ RayT make_ray(V3 o, V3 d)
+{
+	RayT r;
+	r.o = o;
+	r.d = d;
+	r.inv = mk(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+	return r;
+}
+
+struct Hit {
+	float t;
+	int obj, prim, tie;
+};
+
+/* candidate update: strict '<' keeps the first hit found among equals, as the
+ * reference's octree does; a different primitive at exactly the same t is
+ * flagged as a tie */
+__device__ __forceinline__ void consider(Hit &h, float t, int obj, int prim)
+{
+	if(t < h.t) {
+		h.t = t;
+		h.obj = obj;
+		h.prim = prim;
+		h.tie = 0;
+	} else if(t == h.t && (obj != h.obj || prim != h.prim)) {
+		h.tie = 1;
+	}
+}
+
+/* pruning slack: a node is skipped only when its entry lies clearly behind
+ * the best hit, so rounding differences between a hit point and the box that
+ * contains it can never hide a candidate the exhaustive search would find */
+#define SRAY_PRUNE(te, best) ((te) > (best) * 1.00001f + 1e-30f)
+
+#define SRAY_MESH_STACK 96
+#define SRAY_SCENE_STACK 96
+
+struct TraceCounters {
+	unsigned long long nodes, prims;
+};
+
+template <bool COUNT>
+__device__ __forceinline__ void mesh_closest(const DScene &S, int root, int obj, const RayT &r, Hit &h,
+		TraceCounters *tc, int *overflow)
+{
+	int stk[SRAY_MESH_STACK];
+	float stt[SRAY_MESH_STACK];
+	int sp = 0;
+	float te;
+	const DevNode &rn = S.mnodes[root];
+	if(COUNT) tc->nodes++;
+	if(!box_hit(rn.mn, rn.mx, r, te)) return;
+	stk[sp] = root;
+	stt[sp] = te;
+	sp++;
+	while(sp > 0) {
+		sp--;
+		int ni = stk[sp];
+		if(SRAY_PRUNE(stt[sp], h.t)) continue;
+		const float4 *np = reinterpret_cast<const float4 *>(S.mnodes + ni);
+		float4 n1 = __ldg(np + 1);
+		int count = __float_as_int(n1.w);
+		if(count < 0) {
+			int first = __float_as_int(__ldg(np).w);
+			/* the 8 children: test, keep the hit ones, push far to near */
+			int ci[8];
+			float ct[8];
+			int nc = 0;
+			for(int k = 0; k < 8; k++) {
+				const float4 *cp = reinterpret_cast<const float4 *>(S.mnodes + first + k);
+				float4 c0 = __ldg(cp), c1 = __ldg(cp + 1);
+				if(__float_as_int(c1.w) == 0) continue;
+				float mn[3] = {c0.x, c0.y, c0.z}, mx[3] = {c1.x, c1.y, c1.z};
+				if(COUNT) tc->nodes++;
+				float tk;
+				if(box_hit(mn, mx, r, tk) && !SRAY_PRUNE(tk, h.t)) {
+					int j = nc++;
+					while(j > 0 && ct[j - 1] < tk) { ct[j] = ct[j - 1]; ci[j] = ci[j - 1]; j--; }
+					ct[j] = tk;
+					ci[j] = first + k;
+				}
+			}
+			if(sp + nc > SRAY_MESH_STACK) { *overflow = 1; nc = SRAY_MESH_STACK - sp; }
+			for(int k = 0; k < nc; k++) { stk[sp] = ci[k]; stt[sp] = ct[k]; sp++; }
+		} else {
+			int first = __float_as_int(__ldg(np).w);
+			const float4 *tp = reinterpret_cast<const float4 *>(S.mtris + first);
+			for(int s = 0; s < count; s++) {
+				float4 a = __ldg(tp + 3 * s), b = __ldg(tp + 3 * s + 1), c = __ldg(tp + 3 * s + 2);
+				if(COUNT) tc->prims++;
+				float t;
+				if(tri_hit(a, b, c, r, S.eps, h.t, t)) consider(h, t, obj, __ldg(S.mprim + first + s));
+			}
+		}
+	}
+}
+
+template <bool COUNT>
+__device__ __forceinline__ void object_closest(const DScene &S, int oi, int ti, V3 wo, V3 wd, Hit &h,
+		TraceCounters *tc, int *overflow)
+{
+	const DevObj ob = S.objs[oi];
+	const float *m = obj_xf(S, oi, ti);
+	const float *inv = m + 12;
+	RayT r = make_ray(mul_pt(inv, wo), mul_dir(inv, wd));
+	if(ob.type == 2) {
+		if(ob.mesh_root >= 0) mesh_closest<COUNT>(S, ob.mesh_root, oi, r, h, tc, overflow);
+		return;
+	}
+	if(COUNT) tc->prims++;
+	float t;
+	bool hit = ob.type == 0 ? sphere_hit(r, ob.rad, S.eps, t) : cylinder_hit(r, ob.rad, ob.start, ob.end, S.eps, t);
+	if(hit) consider(h, t, oi, 0);
+}
+
+/* closest hit of a world-space segment (Scene::cast_ray, src/scene.cc:764-794),
+ * front-to-back over the top-level octree with the pruning above */
+template <bool COUNT>
+__device__ inline void trace_closest(const DScene &S, V3 wo, V3 wd, int time, Hit &h, TraceCounters *tc, int *overflow)
+{
+	h.t = FLT_MAX;
+	h.obj = -1;
+	h.prim = -1;
+	h.tie = 0;
+	if(!S.has_scene) return;
+	int ti = time_index(S, time);
+	RayT r = make_ray(wo, wd);
+	int stk[SRAY_SCENE_STACK];
+	float stt[SRAY_SCENE_STACK];
+	int sp = 0;
+	float te;
+	if(COUNT) tc->nodes++;
+	if(!box_hit(S.snodes[0].mn, S.snodes[0].mx, r, te)) return;
+	stk[sp] = 0;
+	stt[sp] = te;
+	sp++;
+	while(sp > 0) {
+		sp--;
+		int ni = stk[sp];
+		if(SRAY_PRUNE(stt[sp], h.t)) continue;
+		const DevNode nd = S.snodes[ni];
+		if(nd.count < 0) {
+			int ci[8];
+			float ct[8];
+			int nc = 0;
+			for(int k = 0; k < 8; k++) {
+				const DevNode ch = S.snodes[nd.first + k];
+				if(ch.count == 0) continue;
+				if(COUNT) tc->nodes++;
+				float tk;
+				if(box_hit(ch.mn, ch.mx, r, tk) && !SRAY_PRUNE(tk, h.t)) {
+					int j = nc++;
+					while(j > 0 && ct[j - 1] < tk) { ct[j] = ct[j - 1]; ci[j] = ci[j - 1]; j--; }
+					ct[j] = tk;
+					ci[j] = nd.first + k;
+				}
+			}
+			if(sp + nc > SRAY_SCENE_STACK) { *overflow = 1; nc = SRAY_SCENE_STACK - sp; }
+			for(int k = 0; k < nc; k++) { stk[sp] = ci[k]; stt[sp] = ct[k]; sp++; }
+		} else {
+			for(int s = 0; s < nd.count; s++) object_closest<COUNT>(S, S.sslots[nd.first + s], ti, wo, wd, h, tc, overflow);
+		}
+	}
+}
+
+/* any hit: the reference's shadow test is cast_ray(shadow_ray) != 0
+ * (src/shader.cc:266), i.e. whether any candidate intersection exists */
+__device__ inline bool mesh_any(const DScene &S, int root, const RayT &r, int *overflow)
+{
+	int stk[SRAY_MESH_STACK];
+	int sp = 0;
+	float te;
+	const DevNode &rn = S.mnodes[root];
+	if(!box_hit(rn.mn, rn.mx, r, te)) return false;
+	stk[sp++] = root;
+	while(sp > 0) {
+		int ni = stk[--sp];
+		const float4 *np = reinterpret_cast<const float4 *>(S.mnodes + ni);
+		float4 n0 = __ldg(np), n1 = __ldg(np + 1);
+		int count = __float_as_int(n1.w), first = __float_as_int(n0.w);
+		if(count < 0) {
+			for(int k = 7; k >= 0; k--) {
+				const float4 *cp = reinterpret_cast<const float4 *>(S.mnodes + first + k);
+				float4 c0 = __ldg(cp), c1 = __ldg(cp + 1);
+				if(__float_as_int(c1.w) == 0) continue;
+				float mn[3] = {c0.x, c0.y, c0.z}, mx[3] = {c1.x, c1.y, c1.z};
+				float tk;
+				if(box_hit(mn, mx, r, tk)) {
+					if(sp >= SRAY_MESH_STACK) { *overflow = 1; return false; }
+					stk[sp++] = first + k;
+				}
+			}
+		} else {
+			const float4 *tp = reinterpret_cast<const float4 *>(S.mtris + first);
+			for(int s = 0; s < count; s++) {
+				float4 a = __ldg(tp + 3 * s), b = __ldg(tp + 3 * s + 1), c = __ldg(tp + 3 * s + 2);
+				float t;
+				if(tri_hit(a, b, c, r, S.eps, FLT_MAX, t)) return true;
+			}
+		}
+	}
+	return false;
+}
+
+__device__ inline bool trace_any(const DScene &S, V3 wo, V3 wd, int time, int *overflow)
+{
+	if(!S.has_scene) return false;
+	int ti = time_index(S, time);
+	RayT r = make_ray(wo, wd);
+	int stk[SRAY_SCENE_STACK];
+	int sp = 0;
+	float te;
+	if(!box_hit(S.snodes[0].mn, S.snodes[0].mx, r, te)) return false;
+	stk[sp++] = 0;
+	while(sp > 0) {
+		int ni = stk[--sp];
+		const DevNode nd = S.snodes[ni];
+		if(nd.count < 0) {
+			for(int k = 7; k >= 0; k--) {
+				const DevNode ch = S.snodes[nd.first + k];
+				if(ch.count == 0) continue;
+				float tk;
+				if(box_hit(ch.mn, ch.mx, r, tk)) {
+					if(sp >= SRAY_SCENE_STACK) { *overflow = 1; return false; }
+					stk[sp++] = nd.first + k;
+				}
+			}
+		} else {
+			for(int s = 0; s < nd.count; s++) {
+				int oi = S.sslots[nd.first + s];
+				const DevObj ob = S.objs[oi];
+				const float *inv = obj_xf(S, oi, ti) + 12;
+				RayT orr = make_ray(mul_pt(inv, wo), mul_dir(inv, wd));
+				float t;
+				if(ob.type == 2) {
+					if(ob.mesh_root >= 0 && mesh_any(S, ob.mesh_root, orr, overflow)) return true;
+				} else if(ob.type == 0) {
+					if(sphere_hit(orr, ob.rad, S.eps, t)) return true;
+				} else {
+					if(cylinder_hit(orr, ob.rad, ob.start, ob.end, S.eps, t)) return true;
+				}
+			}
+		}
+	}
+	return false;
+}
+
+/* ---------------- surface point ---------------- */
+struct Surf {
+	V3 pos, normal;
+	float tex[2];
+};
+
+/* interp_face (src/mesh.cc:321-445): bilinear-patch inversion after Haines */
+__device__ inline void interp_face(const float *P, const float *A, V3 ispos, V3 normal, float xsmall, V3 *onorm, float *otex, bool want_tex)
+{
+	V3 p00 = mk(P[0], P[1], P[2]), p10 = mk(P[3], P[4], P[5]), p01 = mk(P[6], P[7], P[8]), p11 = p01;
+	V3 pa = (p00 - p10) + (p11 - p01);
+	V3 pb = p10 - p00;
+	V3 pc = p01 - p00;
+	V3 pd = p00;
+	V3 na = cross(pa, normal), nb = cross(pb, normal), nc = cross(pc, normal);
+	float du0 = dot(nc, pd);
+	float du1 = dot(na, pd) + dot(nc, pb);
+	float du2 = dot(na, pb);
+	float dv0 = dot(nb, pd);
+	float dv1 = dot(na, pd) + dot(nb, pc);
+	float dv2 = dot(na, pc);
+	float rx, ry;
+	if(fabsf(du2) <= xsmall) {
+		float divisor = du1 - dot(na, ispos);
+		rx = fabsf(divisor) > xsmall ? ((dot(nc, ispos) - du0) / divisor) : 0.0f;
+	} else {
+		V3 qux = na / (2.0f * du2);
+		V3 quy = -nc / du2;
+		float dux = -du1 / (2.0f * du2);
+		float duy = du0 / du2;
+		float ka = dux + dot(qux, ispos);
+		float kb = duy + dot(quy, ispos);
+		float u0 = ka - sqrtf(ka * ka - kb);
+		float u1 = ka + sqrtf(ka * ka - kb);
+		rx = (u0 < 0.0f || u0 > 1.0f) ? u1 : u0;
+	}
+	if(fabsf(dv2) <= xsmall) {
+		float divisor = dv1 - dot(na, ispos);
+		ry = fabsf(divisor) > xsmall ? ((dot(nb, ispos) - dv0) / divisor) : 0.0f;
+	} else {
+		V3 qvx = na / (2.0f * dv2);
+		V3 qvy = -nb / dv2;
+		float dvx = -dv1 / (2.0f * dv2);
+		float dvy = dv0 / dv2;
+		float ka = dvx + dot(qvx, ispos);
+		float kb = dvy + dot(qvy, ispos);
+		float v0 = ka - sqrtf(ka * ka - kb);
+		float v1 = ka + sqrtf(ka * ka - kb);
+		ry = (v0 < 0.0f || v0 > 1.0f) ? v1 : v0;
+	}
+#define DLERP(a, b, t) ((a) + ((b) - (a)) * (t))
+	float nn[3];
+	for(int k = 0; k < 3; k++) {
+		float n0 = DLERP(A[0 * 3 + k], A[2 * 3 + k], ry);
+		float n1 = DLERP(A[1 * 3 + k], A[2 * 3 + k], ry);
+		nn[k] = DLERP(n0, n1, rx);
+	}
+	*onorm = mk(nn[0], nn[1], nn[2]);
+	if(want_tex) {
+		for(int k = 0; k < 2; k++) {
+			float s0 = DLERP(A[18 + 0 * 2 + k], A[18 + 2 * 2 + k], ry);
+			float s1 = DLERP(A[18 + 1 * 2 + k], A[18 + 2 * 2 + k], ry);
+			otex[k] = DLERP(s0, s1, rx);
+		}
+	}
+#undef DLERP
+}
+
+__device__ __forceinline__ void sph_tex(V3 p, float *tex, bool cyl)
+{
+	double th = atan2((double)p.z, (double)p.x) + 3.14159265358979323846;
+	double r = sqrt((double)p.x * p.x + (double)p.y * p.y + (double)p.z * p.z);
+	double ph = acos((double)p.y / r);
+	tex[0] = (float)(th / (2.0 * 3.14159265358979323846));
+	tex[1] = cyl ? p.y : (float)(ph / 3.14159265358979323846);
+}
+
+/* world-space surface point of a hit, as the intersectors fill SurfPoint
+ * (object-space position and normal, then forward / inverse-transpose) */
+__device__ inline void surface_point(const DScene &S, const Hit &h, V3 wo, V3 wd, int time, Surf &sp, bool want_tex)
+{
+	int ti = time_index(S, time);
+	const DevObj ob = S.objs[h.obj];
+	const float *m = obj_xf(S, h.obj, ti);
+	const float *inv = m + 12, *it = m + 24;
+	V3 o = mul_pt(inv, wo), d = mul_dir(inv, wd);
+	V3 pos = o + d * h.t;
+	V3 nrm;
+	sp.tex[0] = sp.tex[1] = 0.0f;
+	if(ob.type == 0) {
+		nrm = pos / ob.rad;
+		if(want_tex) sph_tex(pos, sp.tex, false);
+		sp.pos = mul_pt(m, pos);
+		sp.normal = mul_n(it, nrm);
+	} else if(ob.type == 1) {
+		nrm = mk(1.0f * pos.x, 0.0f * pos.y, 1.0f * pos.z) / ob.rad;
+		if(want_tex) sph_tex(pos, sp.tex, true);
+		sp.pos = mul_pt(m, pos);
+		sp.normal = mul_n(it, nrm);
+	} else {
+		const float *P = S.tri_pos + (size_t)(ob.tri_base + h.prim) * 9;
+		const float *A = S.tri_attr + (size_t)(ob.tri_base + h.prim) * 24;
+		V3 v0 = mk(P[0], P[1], P[2]), v1 = mk(P[3], P[4], P[5]), v2 = mk(P[6], P[7], P[8]);
+		V3 fn = cross(v1 - v0, v2 - v0);
+		V3 in;
+		interp_face(P, A, pos, fn, S.xsmall, &in, sp.tex, want_tex);
+		nrm = dot(in, in) < S.xsmall ? fn : in;
+		sp.pos = mul_pt(m, pos);
+		sp.normal = normalized(mul_n(it, nrm));
+	}
+}
+
+/* ---------------- lights ---------------- */
+/* Light::get_point / SphLight::get_point / BoxLight::get_point (src/light.cc:107, 272, 346) */
+__device__ __forceinline__ V3 light_point(const DScene &S, int li, int time, sray_rng *s)
+{
+	const DevLight &L = S.lights[li];
+	const float *p = S.light_pos + ((size_t)li * S.nt + time_index(S, time)) * 4;
+	V3 pos = mk(p[0], p[1], p[2]);
+	if(L.type == 1) return pos + sphrand(s, L.radius);
+	if(L.type == 2) {
+		V3 v;
+		v.x = frand(s, L.dim[0]) - 0.5f * L.dim[0];
+		v.y = frand(s, L.dim[1]) - 0.5f * L.dim[1];
+		v.z = frand(s, L.dim[2]) - 0.5f * L.dim[2];
+		return mul_pt(L.box_m, v);
+	}
+	return pos;
+}
+
+__device__ __forceinline__ const DevMat &mat_of(const DScene &S, int obj)
+{
+	int m = S.objs[obj].mat;
+	return m >= 0 ? S.mats[m] : S.defmat;
+}
+
+__device__ __forceinline__ float fresnel(float r, float cosa)
+{
+	float inv = 1.0f - cosa;
+	float inv_sq = inv * inv;
+	return r + (1.0f - r) * inv_sq * inv_sq * inv;
+}
+
+/* ray IOR stack (depth 4): enter / leave / calc_ior */
+struct IorStack {
+	float ior;
+	float stk[4];
+	int sp;
+	__device__ void enter(float n) { ior = n; if(sp < 4) stk[sp++] = n; }
+	__device__ void leave()
+	{
+		if(sp == 0) return;
+		sp--;
+		ior = sp ? stk[sp - 1] : 1.0f;
+	}
+	__device__ float calc_ior(bool entering, float mat_ior) const
+	{
+		if(entering) return ior / mat_ior;
+		IorStack t = *this;
+		t.leave();
+		return ior / t.ior;
+	}
+};
+
+}  // namespace sray
+
+#endif

@@ -1,0 +1,529 @@
+/* photon.cu -- photon emission and tracing, and the device photon map.
+ *
+ *   k_photon        Light::gen_photon (src/light.cc:111-148) with ProjMap::gen_dir
+ *                   (src/projmap.cc:193-209), Scene::trace_caustics_photon /
+ *                   trace_global_photon (src/scene.cc:571-760); one thread per
+ *                   photon, each on its own Philox stream, so photon j of light i
+ *                   is the same photon the CPU oracle shoots
+ *   compaction      keeps stored photons in emission order
+ *   k_rs_*          stable LSD radix sort of the photons by the Morton code of
+ *                   their grid cell
+ *   k_cells         (first, end) of every occupied cell
+ * PhotonMap::add_photon / scale_photon_power (src/pmap.cc:73-100) become the
+ * per-light power scale applied at store time.  The kd-tree of the reference
+ * (kd_insert3f, kd_nearest_range3f) is replaced by the Morton-ordered grid:
+ * a range query visits the cells overlapping the query cube and tests every
+ * photon in them with the kd-tree's distance rule, so the photon set of each
+ * gather is the same.
+ */
+#include <math.h>
+#include <string.h>
+#include <algorithm>
+#include "renderer.h"
+
+namespace sray {
+
+enum { CAUST_PHOTON = 1, GI_PHOTON = 2, DIRECT_PHOTON = 0 };
+
+struct PRay {
+	V3 o, d;
+	int time, iter;
+	IorStack st;
+};
+
+struct PState {
+	float col[3];
+	int type;
+	V3 pos, dir, norm;
+};
+
+__device__ __forceinline__ bool photon_hit(const DScene &S, const PRay &r, Hit &h, Surf &sp, int *overflow)
+{
+	trace_closest<false>(S, r.o, r.d, r.time, h, nullptr, overflow);
+	if(h.obj < 0) return false;
+	surface_point(S, h, r.o, r.d, r.time, sp, false);
+	return true;
+}
+
+__device__ __forceinline__ void refract_ray(PRay &r, V3 n, float mat_ior, bool entering, float ray_mag)
+{
+	float ior = r.st.calc_ior(entering, mat_ior);
+	if(entering) r.st.enter(mat_ior);
+	else r.st.leave();
+	r.d = refraction(r.d / ray_mag, n, ior) * ray_mag;
+	if(dot(r.d, n) > 0.0f) {
+		if(entering) r.st.leave();
+		else r.st.enter(mat_ior);
+	}
+}
+
+/* Scene::trace_caustics_photon (src/scene.cc:571-647), loop form */
+__device__ bool trace_caust(const DScene &S, PRay r, PState &ph, sray_rng *s, int *overflow)
+{
+	for(int guard = 0; guard < 4096; guard++) {
+		if(r.iter <= 0) return false;
+		Hit h;
+		Surf sp;
+		if(!photon_hit(S, r, h, sp, overflow)) return false;
+		const DevMat &m = mat_of(S, h.obj);
+		float refl = m.refl, refr = m.refr, mat_ior = m.ior;
+		bool entering;
+		V3 normal;
+		float ray_mag = len(r.d);
+		if(dot(r.d, sp.normal) > 0.0f) { normal = -sp.normal; entering = false; }
+		else { normal = sp.normal; entering = true; }
+		float ior = r.st.calc_ior(entering, mat_ior);
+		float ray_dot_n = dot(-r.d / ray_mag, normal);
+		float sf0 = refr > 0.0f ? (ior - 1.0f) / (ior + 1.0f) : 1.0f;
+		float fres = fresnel(sf0 * sf0, ray_dot_n);
+		refl = fres * refl;
+		refr = (1.0f - fres) * refr;
+		float rnum = frand(s, 1.0f);
+		if(rnum < refl) {
+			r.d = reflection(r.d, normal);
+			r.iter--;
+			r.o = sp.pos;
+			ph.type = CAUST_PHOTON;
+			for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * m.ks[k];
+		} else if(rnum < refr) {
+			refract_ray(r, normal, mat_ior, entering, ray_mag);
+			r.o = sp.pos;
+			ph.type = CAUST_PHOTON;
+			for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * m.ks[k];
+		} else {
+			ph.dir = normalized(r.d);
+			ph.pos = sp.pos;
+			ph.norm = normal;
+			return true;
+		}
+	}
+	return false;
+}
+
+/* Scene::trace_global_photon (src/scene.cc:650-760), loop form */
+__device__ bool trace_global(const DScene &S, PRay r, PState &ph, sray_rng *s, int *overflow)
+{
+	for(int guard = 0; guard < 4096; guard++) {
+		if(r.iter <= 0) return false;
+		V3 incident = normalized(r.d);
+		Hit h;
+		Surf sp;
+		if(!photon_hit(S, r, h, sp, overflow)) return false;
+		V3 normal;
+		bool entering;
+		float ray_mag = len(r.d);
+		if(dot(r.d, sp.normal) > 0.0f) { normal = -sp.normal; entering = false; }
+		else { normal = sp.normal; entering = true; }
+		const DevMat &m = mat_of(S, h.obj);
+		float diff_avg = (m.kd[0] + m.kd[1] + m.kd[2]) / 3.0f;
+		float spec_avg = (m.ks[0] + m.ks[1] + m.ks[2]) / 3.0f;
+		float rnum = frand(s, 1.0f);
+		if(rnum < diff_avg) {
+			V3 dir = sphrand(s, 1.0f);
+			if(dot(dir, normal) < 0.0f) dir = -dir;
+			float ndotl = dot(-incident, normal);
+			r.d = dir * (float)SRAY_RAY_MAGNITUDE;
+			r.iter--;
+			r.o = sp.pos;
+			ph.type = GI_PHOTON;
+			for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * (ndotl * (m.kd[k] / diff_avg));
+		} else if(rnum < diff_avg + spec_avg) {
+			float refl = m.refl, refr = m.refr, mat_ior = m.ior;
+			float ior = r.st.calc_ior(entering, mat_ior);
+			float ray_dot_n = dot(-r.d / ray_mag, normal);
+			float sf0 = refr > 0.0f ? (ior - 1.0f) / (ior + 1.0f) : 1.0f;
+			float fres = fresnel(sf0 * sf0, ray_dot_n);
+			refl = fres * refl;
+			refr = (1.0f - fres) * refr;
+			float rn2 = frand(s, 1.0f);
+			if(rn2 < refl) {
+				r.d = reflection(r.d, normal);
+				r.iter--;
+				r.o = sp.pos;
+				ph.type = CAUST_PHOTON;
+				for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * m.ks[k];
+				return trace_caust(S, r, ph, s, overflow);
+			} else if(rn2 < refr) {
+				refract_ray(r, normal, mat_ior, entering, ray_mag);
+				r.o = sp.pos;
+				ph.type = CAUST_PHOTON;
+				for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * m.ks[k];
+				return trace_caust(S, r, ph, s, overflow);
+			}
+			return false;
+		} else {
+			ph.dir = incident;
+			ph.pos = sp.pos;
+			ph.norm = normal;
+			return true;
+		}
+	}
+	return false;
+}
+
+/* ProjMap::gen_dir(true) with cell_from_dir in deterministic float math;
+ * gives up (photon lost, error word set) after a bounded number of tries */
+__device__ bool gen_dir(const uint32_t *bits, sray_rng *s, V3 *out)
+{
+	for(int it = 0; it < (1 << 20); it++) {
+		V3 v = sphrand(s, 1.0f);
+		float theta = sray_atan2_f(v.z, v.x);
+		float phi = sray_atan2_f(sqrtf(v.x * v.x + v.z * v.z), v.y);
+		if(theta < 0.0f) theta = SRAY_TWO_PI_F + theta;
+		float u = theta / SRAY_TWO_PI_F, w = phi / SRAY_PI_F;
+		int uc = (int)(u * 64.0f), vc = (int)(w * 32.0f);
+		uc = uc < 0 ? 0 : (uc > 63 ? 63 : uc);
+		vc = vc < 0 ? 0 : (vc > 31 ? 31 : vc);
+		int idx = vc * 64 + uc;
+		if(bits[idx >> 5] & (1u << (idx & 31))) { *out = v; return true; }
+	}
+	return false;
+}
+
+__global__ void __launch_bounds__(128) k_photon(DScene S, int global, const int *prefix, const float *scale, int nlights,
+		int total, DevPhoton *out, int *valid, DevCounters *ctr)
+{
+	int overflow = 0, gfail = 0;
+	for(int gid = blockIdx.x * blockDim.x + threadIdx.x; gid < total; gid += gridDim.x * blockDim.x) {
+		int li = 0;
+		while(li + 1 < nlights && prefix[li + 1] <= gid) li++;
+		int j = gid - prefix[li];
+		sray_rng s;
+		sray_rng_init(&s, S.seed, global ? SRAY_DOM_GLOBAL : SRAY_DOM_CAUST, (uint32_t)j, (uint32_t)li);
+		int ms = S.t0 == S.t1 ? S.t0 : (sray_rng_int(&s) % (S.t1 - S.t0) + S.t0);
+		const DevLight &L = S.lights[li];
+		PState ph;
+		V3 pos = light_point(S, li, ms, &s);
+		float cov = S.coverage[li * 2 + (global ? 0 : 1)];
+		const uint32_t *bits = S.projbits + (size_t)li * 128 + (global ? 0 : 64);
+		for(int k = 0; k < 3; k++) ph.col[k] = L.col[k] * S.photon_energy;
+		for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * cov;
+		ph.type = DIRECT_PHOTON;
+		bool proj = true;
+		if(cov == 0.0f) {
+			proj = false;
+			for(int k = 0; k < 3; k++) ph.col[k] = L.col[k] * S.photon_energy;
+		}
+		V3 dir;
+		bool ok = true;
+		if(proj) {
+			ok = gen_dir(bits, &s, &dir);
+			if(!ok) gfail = 1;
+		} else {
+			dir = sphrand(&s, 1.0f);
+		}
+		bool stored = false;
+		if(ok) {
+			PRay r;
+			r.o = pos;
+			r.d = dir * (float)SRAY_RAY_MAGNITUDE;
+			r.time = ms;
+			r.iter = S.iter;
+			r.st.ior = 1.0f;
+			r.st.sp = 0;
+			if(global) stored = trace_global(S, r, ph, &s, &overflow);
+			else stored = trace_caust(S, r, ph, &s, &overflow) && ph.type == CAUST_PHOTON;
+		}
+		valid[gid] = stored ? 1 : 0;
+		if(stored) {
+			float sc = scale[li];
+			DevPhoton p;
+			p.p[0] = ph.pos.x; p.p[1] = ph.pos.y; p.p[2] = ph.pos.z; p.p[3] = ph.col[0] * sc;
+			p.d[0] = ph.dir.x; p.d[1] = ph.dir.y; p.d[2] = ph.dir.z; p.d[3] = ph.col[1] * sc;
+			p.n[0] = ph.norm.x; p.n[1] = ph.norm.y; p.n[2] = ph.norm.z; p.n[3] = ph.col[2] * sc;
+			out[gid] = p;
+		}
+	}
+	if(overflow) atomicOr(&ctr->overflow, 1);
+	if(gfail) atomicOr(&ctr->gen_dir_fail, 1);
+}
+
+/* ---------------- scan / compaction ---------------- */
+#define TILE 2048
+
+__global__ void k_count_valid(const int *valid, int n, unsigned *bcount)
+{
+	__shared__ int s;
+	if(threadIdx.x == 0) s = 0;
+	__syncthreads();
+	int base = blockIdx.x * TILE, c = 0;
+	for(int i = base + threadIdx.x; i < base + TILE && i < n; i += blockDim.x) c += valid[i];
+	atomicAdd(&s, c);
+	__syncthreads();
+	if(threadIdx.x == 0) bcount[blockIdx.x] = s;
+}
+
+/* exclusive scan of m entries by one block of 1024 threads; total -> *total */
+__global__ void k_scan_excl(unsigned *data, int m, unsigned *total)
+{
+	__shared__ unsigned part[1024];
+	int t = threadIdx.x;
+	int chunk = (m + 1023) / 1024;
+	int b = t * chunk, e = min(b + chunk, m);
+	unsigned s = 0;
+	for(int i = b; i < e; i++) s += data[i];
+	part[t] = s;
+	__syncthreads();
+	for(int off = 1; off < 1024; off <<= 1) {
+		unsigned v = t >= off ? part[t - off] : 0;
+		__syncthreads();
+		part[t] += v;
+		__syncthreads();
+	}
+	unsigned run = part[t] - s;
+	for(int i = b; i < e; i++) {
+		unsigned v = data[i];
+		data[i] = run;
+		run += v;
+	}
+	if(t == 1023 && total) *total = part[1023];
+}
+
+/* order-preserving compaction of one tile per block */
+__global__ void k_compact(const int *valid, const DevPhoton *in, int n, const unsigned *boffs, DevPhoton *out)
+{
+	__shared__ int wsum[8];
+	__shared__ int run;
+	int base = blockIdx.x * TILE;
+	int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+	if(threadIdx.x == 0) run = (int)boffs[blockIdx.x];
+	__syncthreads();
+	for(int r = 0; r < TILE / 256; r++) {
+		int i = base + r * 256 + threadIdx.x;
+		int v = (i < n) ? valid[i] : 0;
+		unsigned bal = __ballot_sync(0xffffffffu, v);
+		int wpre = __popc(bal & ((1u << lane) - 1u));
+		if(lane == 0) wsum[w] = __popc(bal);
+		__syncthreads();
+		int off = run;
+		for(int k = 0; k < w; k++) off += wsum[k];
+		if(v) out[off + wpre] = in[i];
+		__syncthreads();
+		if(threadIdx.x == 0) {
+			int t = 0;
+			for(int k = 0; k < 8; k++) t += wsum[k];
+			run += t;
+		}
+		__syncthreads();
+	}
+}
+
+/* ---------------- grid keys and radix sort ---------------- */
+__device__ __forceinline__ unsigned spread3(unsigned v)
+{
+	v &= 0x3ff;
+	v = (v | (v << 16)) & 0x030000FF;
+	v = (v | (v << 8)) & 0x0300F00F;
+	v = (v | (v << 4)) & 0x030C30C3;
+	v = (v | (v << 2)) & 0x09249249;
+	return v;
+}
+
+__global__ void k_keys(const DevPhoton *ph, int n, DPhotonMap M, int morton, unsigned *keys, unsigned *vals, unsigned *lin)
+{
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		int c[3];
+		for(int a = 0; a < 3; a++) {
+			double v = floor(((double)ph[i].p[a] - (double)M.org[a]) / (double)M.cell);
+			c[a] = v < 0.0 ? 0 : (v > (double)(M.dims[a] - 1) ? M.dims[a] - 1 : (int)v);
+		}
+		unsigned l = (unsigned)(((size_t)c[2] * M.dims[1] + c[1]) * M.dims[0] + c[0]);
+		keys[i] = morton ? (spread3(c[0]) | (spread3(c[1]) << 1) | (spread3(c[2]) << 2)) : l;
+		vals[i] = (unsigned)i;
+		lin[i] = l;
+	}
+}
+
+#define RS_THREADS 256
+
+__global__ void k_rs_hist(const unsigned *keys, int n, int shift, unsigned *hist, int nblocks)
+{
+	__shared__ unsigned h[256];
+	h[threadIdx.x] = 0;
+	__syncthreads();
+	int base = blockIdx.x * TILE;
+	for(int i = base + threadIdx.x; i < base + TILE && i < n; i += RS_THREADS) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+	__syncthreads();
+	hist[(size_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+/* stable scatter: tile items in order, ranks within a round from warp match masks */
+__global__ void k_rs_scatter(const unsigned *keys, const unsigned *vals, int n, int shift, const unsigned *offs, int nblocks,
+		unsigned *okeys, unsigned *ovals)
+{
+	__shared__ unsigned base[256];
+	__shared__ unsigned wcnt[RS_THREADS / 32][257];
+	int t = threadIdx.x, lane = t & 31, w = t >> 5;
+	base[t] = offs[(size_t)t * nblocks + blockIdx.x];
+	int tile = blockIdx.x * TILE;
+	for(int r = 0; r < TILE / RS_THREADS; r++) {
+		for(int k = 0; k < RS_THREADS / 32; k++) wcnt[k][t] = 0;
+		if(t == 0) for(int k = 0; k < RS_THREADS / 32; k++) wcnt[k][256] = 0;
+		__syncthreads();
+		int i = tile + r * RS_THREADS + t;
+		bool v = i < n;
+		unsigned key = v ? keys[i] : 0u;
+		unsigned d = v ? ((key >> shift) & 255u) : 256u;
+		unsigned peers = __match_any_sync(0xffffffffu, d);
+		int rank = __popc(peers & ((1u << lane) - 1u));
+		if(lane == __ffs(peers) - 1) wcnt[w][d] = __popc(peers);
+		__syncthreads();
+		if(v) {
+			unsigned pos = base[d] + rank;
+			for(int k = 0; k < w; k++) pos += wcnt[k][d];
+			okeys[pos] = key;
+			ovals[pos] = vals[i];
+		}
+		__syncthreads();
+		unsigned add = 0;
+		for(int k = 0; k < RS_THREADS / 32; k++) add += wcnt[k][t];
+		base[t] += add;
+		__syncthreads();
+	}
+}
+
+__global__ void k_permute(const DevPhoton *in, const unsigned *vals, const unsigned *lin_in, int n, DevPhoton *out, unsigned *lin_out)
+{
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		unsigned v = vals[i];
+		out[i] = in[v];
+		lin_out[i] = lin_in[v];
+	}
+}
+
+__global__ void k_cells(const unsigned *lin, int n, uint2 *cells)
+{
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		unsigned l = lin[i];
+		if(i == 0 || lin[i - 1] != l) cells[l].x = (unsigned)i;
+		if(i == n - 1 || lin[i + 1] != l) cells[l].y = (unsigned)(i + 1);
+	}
+}
+
+static int grid_n(int n, int block)
+{
+	int g = (n + block - 1) / block;
+	if(g > 152 * 16) g = 152 * 16;
+	return g < 1 ? 1 : g;
+}
+
+#define PCK(call, where) do { cudaError_t e_ = (call); if(e_ != cudaSuccess) return R.cuda_fail(e_, where); } while(0)
+
+int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored)
+{
+	PhotonBufs &P = global ? R.gi : R.caust;
+	const sray_opts &opt = R.opt;
+	int num = global ? opt.gi_photons : opt.caust_photons;
+	int nl = (int)R.sc.lights.size();
+	P.map.n = 0;
+	*stored = 0;
+	/* photon split by mean light intensity (src/render.cc:87-110) */
+	std::vector<double> inten(nl);
+	double accp = 0.0;
+	for(int i = 0; i < nl; i++) {
+		const double *c = R.sc.lights[i].col;
+		inten[i] = (c[0] + c[1] + c[2]) / 3.0;
+		accp += inten[i];
+	}
+	std::vector<int> prefix(nl + 1, 0);
+	std::vector<float> scale(nl, 0.0f);
+	for(int i = 0; i < nl; i++) {
+		int nphot = (int)ceil((double)num * (inten[i] / accp));
+		prefix[i + 1] = prefix[i] + nphot;
+		scale[i] = nphot ? (float)(1.0 / (double)nphot) : 0.0f;
+	}
+	int total = prefix[nl];
+	if(total <= 0) return 0;
+	DevBuf pre, scl;
+	PCK(pre.upload(prefix, s), "photon prefix");
+	PCK(scl.upload(scale, s), "photon scale");
+	PCK(P.tmp_ph.ensure((size_t)total * sizeof(DevPhoton)), "photon buffer");
+	PCK(P.valid.ensure((size_t)total * sizeof(int)), "photon flags");
+	PCK(R.ctr.ensure(sizeof(DevCounters)), "counters");
+	PCK(cudaMemsetAsync(R.ctr.p, 0, sizeof(DevCounters), s), "counters");
+	k_photon<<<grid_n(total, 128), 128, 0, s>>>(R.S, global, pre.as<int>(), scl.as<float>(), nl, total, P.tmp_ph.as<DevPhoton>(),
+			P.valid.as<int>(), R.ctr.as<DevCounters>());
+	/* compaction in emission order */
+	int nb = (total + TILE - 1) / TILE;
+	PCK(P.scan.ensure((size_t)(nb + 4) * sizeof(unsigned)), "scan");
+	unsigned *bc = P.scan.as<unsigned>();
+	k_count_valid<<<nb, 256, 0, s>>>(P.valid.as<int>(), total, bc);
+	k_scan_excl<<<1, 1024, 0, s>>>(bc, nb, bc + nb);
+	unsigned h_n = 0;
+	PCK(cudaMemcpyAsync(&h_n, bc + nb, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "stored count");
+	PCK(cudaStreamSynchronize(s), "photon trace");
+	DevCounters hc;
+	PCK(cudaMemcpy(&hc, R.ctr.p, sizeof hc, cudaMemcpyDeviceToHost), "counters");
+	if(hc.overflow) return R.fail(SRAY_EDEVICE, "traversal stack overflow while tracing photons");
+	if(hc.gen_dir_fail) return R.fail(SRAY_EDEVICE, "projection-map sampling found no covered cell");
+	int n = (int)h_n;
+	*stored = n;
+	if(n == 0) return 0;
+	PCK(P.ph.ensure((size_t)n * sizeof(DevPhoton)), "photon map");
+	k_compact<<<nb, 256, 0, s>>>(P.valid.as<int>(), P.tmp_ph.as<DevPhoton>(), total, bc, P.ph.as<DevPhoton>());
+	/* grid over the scene bounds: cells of the gather radius */
+	const Box &rb = R.sc.oct.nodes[0].box;
+	int k = global ? opt.gi_k : opt.caust_k;
+	double rad = k > 0 ? (double)opt.gather_rcap : R.sc.gather_dist;
+	double cell = rad > 0.0 ? rad : 1.0;
+	double ext[3];
+	for(int a = 0; a < 3; a++) ext[a] = rb.mx[a] - rb.mn[a];
+	int dims[3];
+	for(;;) {
+		double total_cells = 1.0;
+		for(int a = 0; a < 3; a++) {
+			dims[a] = (int)floor(ext[a] / cell) + 1;
+			total_cells *= dims[a];
+		}
+		if(total_cells <= (double)(1 << 26)) break;
+		cell *= 1.25;
+	}
+	DPhotonMap &M = P.map;
+	M.n = n;
+	M.k = k;
+	M.cell = (float)cell;
+	while((double)M.cell < cell) M.cell = nextafterf(M.cell, INFINITY);
+	for(int a = 0; a < 3; a++) { M.dims[a] = dims[a]; M.org[a] = (float)rb.mn[a]; }
+	for(int a = 0; a < 3; a++) while((double)M.org[a] > rb.mn[a]) M.org[a] = nextafterf(M.org[a], -INFINITY);
+	M.range = (double)(float)rad;
+	M.inv_area = (float)(1.0 / (M_PI * (rad * rad)));
+	bool morton = dims[0] <= 1024 && dims[1] <= 1024 && dims[2] <= 1024;
+	size_t ncells = (size_t)dims[0] * dims[1] * dims[2];
+	PCK(P.keys.ensure((size_t)n * 4), "keys");
+	PCK(P.keys2.ensure((size_t)n * 4), "keys");
+	PCK(P.vals.ensure((size_t)n * 4), "vals");
+	PCK(P.vals2.ensure((size_t)n * 4), "vals");
+	PCK(P.lin.ensure((size_t)n * 8), "cell ids");
+	PCK(P.cells.ensure(ncells * sizeof(uint2)), "cell table");
+	unsigned *keys = P.keys.as<unsigned>(), *keys2 = P.keys2.as<unsigned>();
+	unsigned *vals = P.vals.as<unsigned>(), *vals2 = P.vals2.as<unsigned>();
+	unsigned *lin = P.lin.as<unsigned>(), *lin2 = lin + n;
+	k_keys<<<grid_n(n, 256), 256, 0, s>>>(P.ph.as<DevPhoton>(), n, M, morton ? 1 : 0, keys, vals, lin);
+	unsigned maxkey = morton ? (1u << 30) - 1u : (unsigned)(ncells - 1);
+	int bits = 0;
+	while(bits < 32 && (maxkey >> bits)) bits++;
+	int passes = (bits + 7) / 8;
+	int nbr = (n + TILE - 1) / TILE;
+	PCK(P.hist.ensure((size_t)256 * nbr * sizeof(unsigned) + 16), "radix histogram");
+	for(int ps = 0; ps < passes; ps++) {
+		int shift = ps * 8;
+		k_rs_hist<<<nbr, RS_THREADS, 0, s>>>(keys, n, shift, P.hist.as<unsigned>(), nbr);
+		k_scan_excl<<<1, 1024, 0, s>>>(P.hist.as<unsigned>(), 256 * nbr, nullptr);
+		k_rs_scatter<<<nbr, RS_THREADS, 0, s>>>(keys, vals, n, shift, P.hist.as<unsigned>(), nbr, keys2, vals2);
+		std::swap(keys, keys2);
+		std::swap(vals, vals2);
+	}
+	PCK(P.tmp_ph.ensure((size_t)n * sizeof(DevPhoton)), "photon buffer");
+	k_permute<<<grid_n(n, 256), 256, 0, s>>>(P.ph.as<DevPhoton>(), vals, lin, n, P.tmp_ph.as<DevPhoton>(), lin2);
+	PCK(cudaMemsetAsync(P.cells.p, 0, ncells * sizeof(uint2), s), "cell table");
+	k_cells<<<grid_n(n, 256), 256, 0, s>>>(lin2, n, P.cells.as<uint2>());
+	std::swap(P.ph, P.tmp_ph);
+	M.ph = P.ph.as<DevPhoton>();
+	M.cells = P.cells.as<uint2>();
+	PCK(cudaStreamSynchronize(s), "photon map build");
+	pre.release();
+	scl.release();
+	return 0;
+}
+
+}  // namespace sray

@@ -1,0 +1,1247 @@
+/* render.cu -- wavefront rendering kernels, the frame driver and the C-ABI.
+ *
+ * One pixel sample of every active pixel is rendered per pass:
+ *   k_camera    primary rays            Camera::get_primary_ray (src/camera.cc:119-142)
+ *   k_trace     closest hits            Scene::cast_ray / Octree::intersect (src/scene.cc:764,
+ *                                        src/octree.inl:201-241) with the intersectors
+ *   k_shade     Phong + shadows + spawn shade_phong / calc_lighting / shade_undef
+ *                                        (src/shader.cc:36-283)
+ *   k_gather    photon-map estimates    PhotonMap::irradiance_est / radiance_est (src/pmap.cc:109-178)
+ *   k_finish    adaptive supersampling  render_block / variance (src/render.cc:194-270)
+ * The recursion of trace_ray is unrolled into bounces over SoA ray queues:
+ * every ray carries the product of the weights that the reference's nested
+ * return expression (src/shader.cc:246) applies to its radiance, and adds
+ * its local terms to the pixel sample directly.
+ */
+#include <math.h>
+#include <string.h>
+#include <stdio.h>
+#include <algorithm>
+#include <mutex>
+#include <cooperative_groups.h>
+#include <cooperative_groups/scan.h>
+#include "renderer.h"
+
+namespace cg = cooperative_groups;
+
+namespace sray {
+
+#define DIFFUSE_ITER 0x7fffffff   /* INT_MAX marks a final-gather ray (src/shader.cc:78-81) */
+
+static __device__ __forceinline__ int warp_alloc(int *counter, int n)
+{
+	cg::coalesced_group g = cg::coalesced_threads();
+	int excl = cg::exclusive_scan(g, n);
+	int base = 0;
+	if(g.thread_rank() == g.size() - 1) base = atomicAdd(counter, excl + n);
+	base = g.shfl(base, g.size() - 1);
+	return base + excl;
+}
+
+/* ---------------------------------------------------------------- */
+__global__ void k_camera(DScene S, const int *active, const int *n_active_p, int sample, RayQueue q, float4 *acc,
+		DevCounters *ctr)
+{
+	int n = *n_active_p;
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		int p = active ? active[i] : i;
+		int x = p % S.width, y = p / S.width;
+		sray_rng s;
+		sray_rng_init(&s, S.seed, SRAY_DOM_PIXEL, (uint32_t)p, (uint32_t)sample);
+		float px = ((float)x / (float)S.width) * S.cam_xsz - S.cam_xsz / 2.0f;
+		float py = 1.0f - ((float)y / (float)S.height) * S.cam_ysz;
+		if(sample > 0) {
+			px = px + S.cam_xsz * (frand(&s, 1.0f) - 0.5f) / (float)S.width;
+			py = py + S.cam_ysz * (frand(&s, 1.0f) - 0.5f) / (float)S.height;
+		}
+		V3 d = mk(px, py, S.cam_f) * S.cam_maxd;
+		int time = S.t0;
+		if(S.mblur && sample > 0 && S.shutter > 0) time += sray_rng_int(&s) % S.shutter - S.shutter / 2;
+		const float *m = S.cam_m + (size_t)time_index(S, time) * 12;
+		V3 o = mul_pt(m, mk(0.0f, 0.0f, 0.0f));
+		d = mul_dir(m, d);
+		q.o[i] = make_float4(o.x, o.y, o.z, 1.0f);
+		q.d[i] = make_float4(d.x, d.y, d.z, 1.0f);
+		q.w[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+		q.meta[i] = make_int4(p, S.iter, 1, time);
+		q.stk[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+		q.ext[i] = make_int2(sample, 0);
+		acc[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+	}
+	if(blockIdx.x == 0 && threadIdx.x == 0) {
+		*q.count = n;
+		atomicAdd(&ctr->rays[0], (unsigned long long)n);
+	}
+}
+
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_trace(DScene S, RayQueue q, int4 *hits, DevCounters *ctr)
+{
+	int n = *q.count;
+	TraceCounters tc = {0, 0};
+	int overflow = 0;
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		float4 o = q.o[i], d = q.d[i];
+		int time = q.meta[i].w;
+		Hit h;
+		trace_closest<COUNT>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), time, h, &tc, &overflow);
+		hits[i] = make_int4(__float_as_int(h.t), h.obj, h.prim, h.tie);
+	}
+	if(overflow) atomicOr(&ctr->overflow, 1);
+	if(COUNT) {
+		atomicAdd(&ctr->nodes, tc.nodes);
+		atomicAdd(&ctr->prims, tc.prims);
+	}
+}
+
+__device__ __forceinline__ void acc_add(float4 *acc, int p, float r, float g, float b)
+{
+	atomicAdd(&acc[p].x, r);
+	atomicAdd(&acc[p].y, g);
+	atomicAdd(&acc[p].z, b);
+}
+
+struct Child {
+	V3 o, d;
+	float energy;
+	int iter, path, dsub;
+	float wr, wg, wb;
+	IorStack st;
+};
+
+__device__ __forceinline__ void push_ray(RayQueue &q, int slot, const Child &c, int pixel, int sample, int time)
+{
+	q.o[slot] = make_float4(c.o.x, c.o.y, c.o.z, c.energy);
+	q.d[slot] = make_float4(c.d.x, c.d.y, c.d.z, c.st.ior);
+	q.w[slot] = make_float4(c.wr, c.wg, c.wb, 0.0f);
+	q.meta[slot] = make_int4(pixel, c.iter, c.path, time);
+	q.stk[slot] = make_float4(c.st.stk[0], c.st.stk[1], c.st.stk[2], c.st.stk[3]);
+	q.ext[slot] = make_int2(sample | (c.dsub << 16), c.st.sp);
+}
+
+__device__ __forceinline__ float maxf_ref(float a, float b) { return a > b ? a : b; }
+
+#define MAX_DS 8
+
+/* shade one bounce: env colour for misses, shade_phong / shade_undef for hits */
+__global__ void __launch_bounds__(128) k_shade(DScene S, RayQueue qi, const int4 *hits, RayQueue qo, GatherReq *gq,
+		int *gq_count, int gq_cap, float4 *acc, int depth, DevCounters *ctr)
+{
+	int n = *qi.count;
+	int overflow = 0;
+	unsigned long long shadow_rays = 0;
+	for(int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+		int i = base + threadIdx.x;
+		bool live = i < n;
+		int nchild = 0, ngather = 0;
+		Child ch[2 + MAX_DS];
+		GatherReq gr;
+		int pixel = 0, sample = 0, time = 0;
+		if(live) {
+			float4 o4 = qi.o[i], d4 = qi.d[i], w4 = qi.w[i], st4 = qi.stk[i];
+			int4 meta = qi.meta[i];
+			int2 ext = qi.ext[i];
+			int4 hv = hits[i];
+			pixel = meta.x;
+			int iter = meta.y, path = meta.z;
+			time = meta.w;
+			sample = ext.x & 0xffff;
+			int dsub = ext.x >> 16;
+			V3 ro = mk(o4.x, o4.y, o4.z), rd = mk(d4.x, d4.y, d4.z);
+			float energy = o4.w;
+			IorStack st;
+			st.ior = d4.w;
+			st.stk[0] = st4.x; st.stk[1] = st4.y; st.stk[2] = st4.z; st.stk[3] = st4.w;
+			st.sp = ext.y;
+			Hit h;
+			h.t = __int_as_float(hv.x);
+			h.obj = hv.y;
+			h.prim = hv.z;
+			h.tie = hv.w;
+			if(h.obj < 0) {
+				acc_add(acc, pixel, w4.x * S.env_col[0], w4.y * S.env_col[1], w4.z * S.env_col[2]);
+				if(depth == 0) acc[pixel].w = S.env_col[3];
+			} else {
+				if(depth == 0) acc[pixel].w = 1.0f;
+				const DevMat &mat = mat_of(S, h.obj);
+				Surf sp;
+				surface_point(S, h, ro, rd, time, sp, !mat.phong);
+				if(!mat.phong) {
+					/* shade_undef (src/shader.cc:36-73) */
+					sray_rng rng;
+					sray_rng_init(&rng, S.seed, SRAY_DOM_PIXEL | ((uint32_t)path << 4), (uint32_t)pixel, (uint32_t)(sample | (dsub << 16)));
+					int tx = (int)(sp.tex[0] * 20.0f), ty = (int)(sp.tex[1] * 10.0f);
+					bool even = (tx % 2) == (ty % 2);
+					float tc[3] = {even ? 1.0f : 0.2f, 0.3f, even ? 0.2f : 1.0f};
+					float df[3] = {0.1f, 0.1f, 0.1f}, sf[3] = {0.0f, 0.0f, 0.0f};
+					for(int li = 0; li < S.nlights; li++) {
+						const DevLight &L = S.lights[li];
+						V3 lpos = light_point(S, li, time, &rng);
+						V3 ldir = lpos - sp.pos;
+						float ldist = len(ldir);
+						V3 sdir = ldir;
+						ldir = ldir / ldist;
+						V3 vdir = -normalized(rd);
+						V3 hdir = normalized(ldir + vdir);
+						shadow_rays++;
+						if(!trace_any(S, sp.pos, sdir, time, &overflow)) {
+							float ndotl = maxf_ref(dot(sp.normal, ldir), 0.0f);
+							float ndoth = maxf_ref(dot(sp.normal, hdir), 0.0f);
+							float pw = powf(ndoth, 50.0f);
+							for(int k = 0; k < 3; k++) {
+								df[k] = df[k] + ndotl * L.col[k] * 1.0f;
+								sf[k] = sf[k] + pw * L.col[k] * 1.0f;
+							}
+						}
+					}
+					acc_add(acc, pixel, w4.x * (df[0] * tc[0] + sf[0]), w4.y * (df[1] * tc[1] + sf[1]), w4.z * (df[2] * tc[2] + sf[2]));
+				} else {
+					/* shade_phong (src/shader.cc:83-247) */
+					bool entering;
+					V3 normal;
+					if(dot(rd, sp.normal) > 0.0f) { normal = -sp.normal; entering = false; }
+					else { normal = sp.normal; entering = true; }
+					float ray_mag = len(rd);
+					V3 incident = rd / ray_mag;
+					const float *kd = mat.kd, *ks = mat.ks;
+					if(iter == DIFFUSE_ITER) {
+						/* final-gather ray: radiance_est(...) * kd */
+						gr.a = make_float4(sp.pos.x, sp.pos.y, sp.pos.z, __int_as_float(1));
+						gr.b = make_float4(normal.x, normal.y, normal.z, __int_as_float(pixel));
+						gr.w = make_float4(w4.x * kd[0], w4.y * kd[1], w4.z * kd[2], 0.0f);
+						ngather = 1;
+					} else {
+						sray_rng rng;
+						sray_rng_init(&rng, S.seed, SRAY_DOM_PIXEL | ((uint32_t)path << 4), (uint32_t)pixel, (uint32_t)sample);
+						float refl_fact = mat.refl, trans_fact = mat.refr, mat_ior = mat.ior;
+						float ior = st.calc_ior(entering, mat_ior);
+						float diff[3], spec[3] = {0.0f, 0.0f, 0.0f};
+						for(int k = 0; k < 3; k++) diff[k] = S.env_amb[k] * kd[k];
+						for(int li = 0; li < S.nlights; li++) {
+							const DevLight &L = S.lights[li];
+							int ns = L.type != 0 ? S.shadow_samples : 1;
+							float dl[3] = {0.0f, 0.0f, 0.0f}, sl[3] = {0.0f, 0.0f, 0.0f};
+							for(int si = 0; si < ns; si++) {
+								V3 lpos = light_point(S, li, time, &rng);
+								V3 ldir = lpos - sp.pos;
+								float ldist = len(ldir);
+								V3 sdir = ldir;
+								ldir = ldir / ldist;
+								shadow_rays++;
+								if(!trace_any(S, sp.pos, sdir, time, &overflow)) {
+									V3 vref = reflection(incident, normal);
+									float ndotl = maxf_ref(dot(normal, ldir), 0.0f);
+									float rdotl = maxf_ref(dot(vref, ldir), 0.0f);
+									float pw = powf(rdotl, mat.shin);
+									for(int k = 0; k < 3; k++) {
+										float lc = L.col[k] * 1.0f;
+										dl[k] = dl[k] + ndotl * lc;
+										sl[k] = sl[k] + pw * lc;
+									}
+								}
+							}
+							if(ns > 1) {
+								float scale = 1.0f / (float)ns;
+								for(int k = 0; k < 3; k++) { dl[k] = dl[k] * scale; sl[k] = sl[k] * scale; }
+							}
+							for(int k = 0; k < 3; k++) { diff[k] = diff[k] + dl[k]; spec[k] = spec[k] + sl[k]; }
+						}
+						/* final gather: diffuse rays end at their next hit (src/shader.cc:154-187) */
+						if(S.gi_on) {
+							int ds = S.diffuse_samples < MAX_DS ? S.diffuse_samples : MAX_DS;
+							for(int k = 0; k < ds; k++) {
+								V3 dir = sphrand(&rng, 1.0f);
+								float ndotl;
+								if((ndotl = dot(dir, normal)) < 0.0f) dir = -dir;
+								float diff_energy = ndotl * energy;
+								if(diff_energy > S.min_energy) {
+									Child &c = ch[nchild++];
+									c.o = sp.pos;
+									c.d = dir * ray_mag;
+									c.energy = diff_energy;
+									c.iter = DIFFUSE_ITER;
+									c.path = path * 4 + 2;
+									c.dsub = k;
+									c.st = st;
+									float g = S.diffuse_samples > 1 ? ndotl / (float)S.diffuse_samples : ndotl;
+									c.wr = w4.x * kd[0] * g;
+									c.wg = w4.y * kd[1] * g;
+									c.wb = w4.z * kd[2] * g;
+								}
+							}
+						}
+						float ray_dot_n = dot(-rd / ray_mag, normal);
+						float sf0 = trans_fact > 0.0f ? (ior - 1.0f) / (ior + 1.0f) : 1.0f;
+						float fres = fresnel(sf0 * sf0, ray_dot_n);
+						float refl_energy = refl_fact * energy;
+						if(refl_energy > S.min_energy && iter > 0) {
+							Child &c = ch[nchild++];
+							c.o = sp.pos;
+							c.d = reflection(rd, normal);
+							c.energy = refl_energy;
+							c.iter = iter - 1;
+							c.path = path * 4;
+							c.dsub = 0;
+							c.st = st;
+							float g = refl_fact * fres;
+							c.wr = w4.x * ks[0] * g;
+							c.wg = w4.y * ks[1] * g;
+							c.wb = w4.z * ks[2] * g;
+						}
+						float trans_energy = trans_fact * energy;
+						if(trans_energy > S.min_energy && iter > 0) {
+							Child &c = ch[nchild++];
+							c.st = st;
+							if(entering) c.st.enter(mat_ior);
+							else c.st.leave();
+							c.o = sp.pos;
+							c.d = refraction(rd / ray_mag, normal, ior) * ray_mag;
+							if(dot(c.d, normal) > 0.0f) {
+								if(entering) c.st.leave();
+								else c.st.enter(mat_ior);
+							}
+							c.energy = trans_energy;
+							c.iter = iter - 1;
+							c.path = path * 4 + 1;
+							c.dsub = 0;
+							float g = trans_fact * (1.0f - fres);
+							c.wr = w4.x * ks[0] * g;
+							c.wg = w4.y * ks[1] * g;
+							c.wb = w4.z * ks[2] * g;
+						}
+						if(S.caust_on) {
+							gr.a = make_float4(sp.pos.x, sp.pos.y, sp.pos.z, __int_as_float(0));
+							gr.b = make_float4(normal.x, normal.y, normal.z, __int_as_float(pixel));
+							gr.w = make_float4(w4.x, w4.y, w4.z, 0.0f);
+							ngather = 1;
+						}
+						acc_add(acc, pixel, w4.x * (diff[0] * kd[0] + spec[0] * ks[0]),
+								w4.y * (diff[1] * kd[1] + spec[1] * ks[1]),
+								w4.z * (diff[2] * kd[2] + spec[2] * ks[2]));
+					}
+				}
+			}
+		}
+		if(nchild > 0) {
+			int slot = warp_alloc(qo.count, nchild);
+			if(slot + nchild > qo.cap) {
+				overflow = 1;
+			} else {
+				for(int k = 0; k < nchild; k++) push_ray(qo, slot + k, ch[k], pixel, sample, time);
+			}
+		}
+		if(ngather > 0) {
+			int slot = warp_alloc(gq_count, 1);
+			if(slot >= gq_cap) overflow = 1;
+			else gq[slot] = gr;
+		}
+	}
+	if(overflow) atomicOr(&ctr->overflow, 1);
+	if(shadow_rays) atomicAdd(&ctr->rays[2], shadow_rays);
+}
+
+/* ---------------------------------------------------------------- */
+/* photon-map gathers, one warp per query                             */
+/* ---------------------------------------------------------------- */
+#define GATHER_WARPS 8
+#define KEY_CAP 512
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+	for(int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+	return v;
+}
+__device__ __forceinline__ int warp_sumi(int v)
+{
+	for(int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+	return v;
+}
+__device__ __forceinline__ unsigned warp_maxu(unsigned v)
+{
+	for(int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+	return v;
+}
+
+struct GatherCells {
+	int lo[3], hi[3];
+};
+
+__device__ __forceinline__ void gather_cells(const DPhotonMap &M, const double q[3], double range, GatherCells &gc)
+{
+	for(int a = 0; a < 3; a++) {
+		double lo = floor((q[a] - range - (double)M.org[a]) / (double)M.cell);
+		double hi = floor((q[a] + range - (double)M.org[a]) / (double)M.cell);
+		int l = lo < 0.0 ? 0 : (lo > (double)(M.dims[a] - 1) ? M.dims[a] - 1 : (int)lo);
+		int h = hi < 0.0 ? 0 : (hi > (double)(M.dims[a] - 1) ? M.dims[a] - 1 : (int)hi);
+		gc.lo[a] = l;
+		gc.hi[a] = h;
+	}
+}
+
+/* squared distance in double between a float photon position and the
+ * float-rounded query point (kd_nearest_range3f semantics) */
+__device__ __forceinline__ double dist2(const float4 &p, const double q[3])
+{
+	double dx = (double)p.x - q[0], dy = (double)p.y - q[1], dz = (double)p.z - q[2];
+	return dx * dx + dy * dy + dz * dz;
+}
+
+/* Iterate the photons in range of q; f(photon index, d2) for each. */
+template <class F>
+__device__ __forceinline__ void for_range(const DPhotonMap &M, const GatherCells &gc, const double q[3], double r2, int lane, F f)
+{
+	for(int z = gc.lo[2]; z <= gc.hi[2]; z++)
+	for(int y = gc.lo[1]; y <= gc.hi[1]; y++)
+	for(int x = gc.lo[0]; x <= gc.hi[0]; x++) {
+		uint2 c = M.cells[((size_t)z * M.dims[1] + y) * M.dims[0] + x];
+		for(unsigned j = c.x + lane; j < c.y; j += 32) {
+			float4 p = __ldg(reinterpret_cast<const float4 *>(M.ph + j));
+			double d2 = dist2(p, q);
+			if(d2 <= r2) f(j, d2);
+		}
+	}
+}
+
+__device__ __forceinline__ void photon_term(const DevPhoton *ph, int j, int kind, V3 n, float max_cos, float *sum)
+{
+	const float4 *pp = reinterpret_cast<const float4 *>(ph + j);
+	float4 p = __ldg(pp), d = __ldg(pp + 1), nn = __ldg(pp + 2);
+	V3 dir = mk(d.x, d.y, d.z);
+	if(kind == 0) {
+		if(dot(dir, n) < 0.0f) { sum[0] += p.w; sum[1] += d.w; sum[2] += nn.w; }
+	} else {
+		float ndotl = dot(-dir, n);
+		if(ndotl > 0.0f && dot(mk(nn.x, nn.y, nn.z), n) > max_cos) {
+			sum[0] += p.w * ndotl; sum[1] += d.w * ndotl; sum[2] += nn.w * ndotl;
+		}
+	}
+}
+
+/* estimate of one query by one full warp; returns the rgb estimate in all lanes */
+__device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *keys, float out[3])
+{
+	const DPhotonMap &M = kind == 0 ? S.caust : S.gi;
+	int lane = threadIdx.x & 31;
+	out[0] = out[1] = out[2] = 0.0f;
+	if(M.n == 0) return;
+	double q[3] = {(double)pos.x, (double)pos.y, (double)pos.z};
+	double r2 = M.range * M.range;
+	GatherCells gc;
+	gather_cells(M, q, M.range, gc);
+	float sum[3] = {0.0f, 0.0f, 0.0f};
+	int cnt = 0;
+	float inv_area = M.inv_area;
+	if(M.k <= 0) {
+		for_range(M, gc, q, r2, lane, [&](int j, double) {
+			cnt++;
+			photon_term(M.ph, j, kind, n, S.max_cos, sum);
+		});
+		cnt = warp_sumi(cnt);
+	} else {
+		/* k nearest within the radius cap: select the k-th smallest
+		 * float-rounded squared distance by a bitwise radix search */
+		__shared__ int kcount[GATHER_WARPS];
+		int w = threadIdx.x >> 5;
+		if(lane == 0) kcount[w] = 0;
+		__syncwarp();
+		unsigned maxkey = 0;
+		int ncand = 0;
+		for_range(M, gc, q, r2, lane, [&](int, double d2) {
+			unsigned key = __float_as_uint((float)d2);
+			maxkey = key > maxkey ? key : maxkey;
+			ncand++;
+			int slot = atomicAdd(&kcount[w], 1);
+			if(slot < KEY_CAP) keys[slot] = key;
+		});
+		__syncwarp();
+		ncand = warp_sumi(ncand);
+		maxkey = warp_maxu(maxkey);
+		unsigned kth = maxkey;
+		if(ncand > M.k) {
+			bool cached = ncand <= KEY_CAP;
+			unsigned prefix = 0;
+			int remaining = M.k;
+			for(int bit = 31; bit >= 0; bit--) {
+				unsigned hmask = ~((1u << bit) - 1u) & 0xffffffffu;
+				if(bit == 31) hmask = 0x80000000u;
+				int c0 = 0;
+				if(cached) {
+					for(int j = lane; j < ncand; j += 32) if((keys[j] & hmask) == prefix) c0++;
+				} else {
+					for_range(M, gc, q, r2, lane, [&](int, double d2) {
+						if((__float_as_uint((float)d2) & hmask) == prefix) c0++;
+					});
+				}
+				c0 = warp_sumi(c0);
+				if(c0 < remaining) {
+					remaining -= c0;
+					prefix |= (1u << bit);
+				}
+			}
+			kth = prefix;
+		}
+		for_range(M, gc, q, r2, lane, [&](int j, double d2) {
+			if(__float_as_uint((float)d2) <= kth) {
+				cnt++;
+				photon_term(M.ph, j, kind, n, S.max_cos, sum);
+			}
+		});
+		cnt = warp_sumi(cnt);
+		inv_area = (float)(1.0 / (3.14159265358979323846 * (double)__uint_as_float(kth)));
+	}
+	sum[0] = warp_sum(sum[0]);
+	sum[1] = warp_sum(sum[1]);
+	sum[2] = warp_sum(sum[2]);
+	if(kind == 0 && cnt < 8) return;
+	if(kind == 1 && cnt <= 0) return;
+	out[0] = sum[0] * inv_area;
+	out[1] = sum[1] * inv_area;
+	out[2] = sum[2] * inv_area;
+}
+
+__global__ void __launch_bounds__(GATHER_WARPS * 32) k_gather(DScene S, const GatherReq *gq, const int *gq_count,
+		float4 *acc, DevCounters *ctr)
+{
+	__shared__ unsigned keys[GATHER_WARPS][KEY_CAP];
+	int n = *gq_count;
+	int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	int gw = blockIdx.x * GATHER_WARPS + w, nw = gridDim.x * GATHER_WARPS;
+	for(int r = gw; r < n; r += nw) {
+		GatherReq g = gq[r];
+		int kind = __float_as_int(g.a.w);
+		int pixel = __float_as_int(g.b.w);
+		float est[3];
+		gather_one(S, kind, mk(g.a.x, g.a.y, g.a.z), mk(g.b.x, g.b.y, g.b.z), keys[w], est);
+		if(lane == 0) acc_add(acc, pixel, g.w.x * est[0], g.w.y * est[1], g.w.z * est[2]);
+		__syncwarp();
+	}
+	if(blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctr->rays[3], (unsigned long long)n);
+}
+
+/* end of a sample pass: variance test and framebuffer write (src/render.cc:199-244) */
+__global__ void k_finish(const int *active, const int *n_active_p, int sample, const float4 *acc, float4 *hist,
+		float4 *sums, int max_samples, int min_samples, float max_var, int *next, int *next_count, float4 *fb, int *spp)
+{
+	int n = *n_active_p;
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		int p = active ? active[i] : i;
+		float4 s = acc[p];
+		float4 sum = sample == 0 ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : sums[p];
+		sum.x = sum.x + s.x;
+		sum.y = sum.y + s.y;
+		sum.z = sum.z + s.z;
+		sum.w = sum.w + s.w;
+		int i1 = sample + 1;
+		bool done = i1 >= max_samples;
+		if(max_samples > 1) hist[(size_t)p * max_samples + sample] = s;
+		if(!done && i1 >= min_samples && i1 > 1) {
+			float rcp = (float)(1.0 / (double)i1);
+			float4 mean = make_float4(sum.x * rcp, sum.y * rcp, sum.z * rcp, sum.w * rcp);
+			float sq = 0.0f;
+			for(int j = 0; j < i1; j++) {
+				float4 h = hist[(size_t)p * max_samples + j];
+				float dx = mean.x - h.x, dy = mean.y - h.y, dz = mean.z - h.z, dw = mean.w - h.w;
+				sq = sq + (dx * dx + dy * dy + dz * dz + dw * dw);
+			}
+			float v = sq * rcp;
+			if(v < max_var) done = true;
+		}
+		if(done) {
+			double r = 1.0 / (double)i1;
+			fb[p] = make_float4((float)((double)sum.x * r), (float)((double)sum.y * r), (float)((double)sum.z * r),
+					(float)((double)sum.w * r));
+			if(spp) spp[p] = i1;
+		} else {
+			sums[p] = sum;
+			int slot = warp_alloc(next_count, 1);
+			next[slot] = p;
+		}
+	}
+}
+
+/* closest hits of caller-supplied world rays (sray_gpu_cast_rays) */
+__global__ void k_cast(DScene S, int n, const float *orig, const float *dir, const int *time, int *obj, int *prim, float *t,
+		unsigned char *tie, DevCounters *ctr)
+{
+	int overflow = 0;
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		Hit h;
+		trace_closest<false>(S, mk(orig[i * 3], orig[i * 3 + 1], orig[i * 3 + 2]), mk(dir[i * 3], dir[i * 3 + 1], dir[i * 3 + 2]),
+				time ? time[i] : S.t0, h, nullptr, &overflow);
+		obj[i] = h.obj;
+		prim[i] = h.obj >= 0 ? h.prim : -1;
+		t[i] = h.obj >= 0 ? h.t : 0.0f;
+		tie[i] = (unsigned char)h.tie;
+	}
+	if(overflow) atomicOr(&ctr->overflow, 1);
+}
+
+__global__ void k_primary_hits(DScene S, RayQueue q, const int4 *hits, int *obj, int *prim, float *t, unsigned char *tie)
+{
+	int n = *q.count;
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		int4 h = hits[i];
+		int p = q.meta[i].x;
+		obj[p] = h.y;
+		prim[p] = h.y >= 0 ? h.z : -1;
+		t[p] = h.y >= 0 ? __int_as_float(h.x) : 0.0f;
+		tie[p] = (unsigned char)h.w;
+	}
+}
+
+/* ================================================================ */
+/* host side                                                          */
+/* ================================================================ */
+static int grid_for(int n, int block)
+{
+	int sms = 152;
+	int g = (n + block - 1) / block;
+	int cap = sms * 16;
+	if(g > cap) g = cap;
+	return g < 1 ? 1 : g;
+}
+
+#define CK(call, where) do { cudaError_t e_ = (call); if(e_ != cudaSuccess) return cuda_fail(e_, where); } while(0)
+
+void Renderer::fill_scene_desc()
+{
+	DScene &D = S;
+	D.snodes = snodes.as<DevNode>();
+	D.sslots = sslots.as<int>();
+	D.has_scene = built && !sc.oct.nodes.empty() && !sc.objs.empty();
+	D.mnodes = mnodes.as<DevNode>();
+	D.mtris = mtris.as<DevTri>();
+	D.mprim = mprim.as<int>();
+	D.objs = objs.as<DevObj>();
+	D.nobj = (int)sc.objs.size();
+	D.xf = xf.as<float>();
+	D.tlo = tlo;
+	D.nt = nt;
+	D.tri_pos = tri_pos.as<float>();
+	D.tri_attr = tri_attr.as<float>();
+	D.mats = mats.as<DevMat>();
+	memset(&D.defmat, 0, sizeof D.defmat);
+	for(int k = 0; k < 4; k++) { D.defmat.kd[k] = (float)sc.defmat.kd[k]; D.defmat.ks[k] = (float)sc.defmat.ks[k]; }
+	D.defmat.shin = (float)sc.defmat.shin;
+	D.defmat.refl = (float)sc.defmat.refl;
+	D.defmat.refr = (float)sc.defmat.refr;
+	D.defmat.ior = (float)sc.defmat.ior;
+	D.defmat.phong = 0;
+	D.lights = lights.as<DevLight>();
+	D.nlights = (int)sc.lights.size();
+	D.light_pos = light_pos.as<float>();
+	D.projbits = projbits.as<uint32_t>();
+	D.coverage = coverage.as<float>();
+	D.cam_m = cam_m.as<float>();
+	D.cam_f = (float)(1.0 / tan(0.5 * sc.cam.vfov));
+	D.cam_xsz = (float)(sc.cam.aspect * 2.0);
+	D.cam_ysz = 2.0f;
+	D.cam_maxd = (float)sc.cam.max_dist;
+	for(int k = 0; k < 4; k++) { D.env_col[k] = (float)sc.env_col[k]; D.env_amb[k] = (float)sc.env_amb[k]; }
+	D.eps = (float)1e-6;
+	D.xsmall = (float)1e-8;
+	D.min_energy = opt.min_energy;
+	D.iter = opt.iter;
+	D.diffuse_samples = opt.diffuse_samples;
+	D.shadow_samples = opt.shadow_samples;
+	D.gi_on = opt.gi_photons != 0;
+	D.caust_on = opt.caust_photons != 0;
+	D.width = opt.width;
+	D.height = opt.height;
+	D.mblur = opt.mblur;
+	D.shutter = sc.cam.shutter;
+	D.t0 = t0;
+	D.t1 = t1;
+	D.seed = opt.seed;
+	D.photon_energy = opt.photon_energy;
+	D.max_cos = (float)cos(M_PI / 2.5);
+	D.caust = caust.map;
+	D.gi = gi.map;
+}
+
+static void pack_xf(const double m[4][4], float *dst)
+{
+	double inv[4][4];
+	mat_inverse(inv, m);
+	for(int i = 0; i < 3; i++) for(int j = 0; j < 4; j++) dst[i * 4 + j] = (float)m[i][j];
+	for(int i = 0; i < 3; i++) for(int j = 0; j < 4; j++) dst[12 + i * 4 + j] = (float)inv[i][j];
+	/* inverse transpose, 3x3: it[r][c] = inv[c][r] */
+	for(int r = 0; r < 3; r++) for(int c = 0; c < 3; c++) dst[24 + r * 3 + c] = (float)inv[c][r];
+	for(int k = 33; k < XF_STRIDE; k++) dst[k] = 0.0f;
+}
+
+int Renderer::upload_scene(cudaStream_t s)
+{
+	std::vector<DevNode> nodes;
+	std::vector<int> slots;
+	std::vector<DevTri> tris;
+	std::vector<int> prim;
+	std::vector<float> tp, ta;
+	int tri_cursor = 0;
+	for(size_t u = 0; u < sc.meshes.size(); u++) {
+		Mesh &m = sc.meshes[u];
+		m.node_base = (int)nodes.size();
+		m.tri_base = tri_cursor;
+		size_t s0 = slots.size();
+		flatten_octree(m.oct, nodes, slots);
+		size_t nf = m.pos.size() / 9;
+		for(size_t k = s0; k < slots.size(); k++) {
+			int f = slots[k];
+			const float *P = &m.pos[(size_t)f * 9];
+			DevTri t;
+			/* unnormalised face normal cross(v1 - v0, v2 - v0), float ops as the test computes it */
+			float e1[3] = {P[3] - P[0], P[4] - P[1], P[5] - P[2]};
+			float e2[3] = {P[6] - P[0], P[7] - P[1], P[8] - P[2]};
+			float n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+			for(int c = 0; c < 3; c++) { t.a[c] = P[c]; t.b[c] = P[3 + c]; t.c[c] = P[6 + c]; }
+			t.a[3] = n[0]; t.b[3] = n[1]; t.c[3] = n[2];
+			tris.push_back(t);
+			prim.push_back(f);
+		}
+		/* leaf slot indices become positions in the triangle-record array */
+		tp.insert(tp.end(), m.pos.begin(), m.pos.end());
+		ta.insert(ta.end(), m.attr.begin(), m.attr.end());
+		tri_cursor += (int)nf;
+		std::vector<BuildOctree::Node>().swap(m.oct.nodes);   /* build form no longer needed */
+	}
+	/* the leaf 'first' fields index `slots`, which coincide with the record array */
+	std::vector<DevObj> dobj(sc.objs.size());
+	for(size_t i = 0; i < sc.objs.size(); i++) {
+		const Object &o = sc.objs[i];
+		DevObj &d = dobj[i];
+		memset(&d, 0, sizeof d);
+		d.type = o.type;
+		d.mat = o.mat;
+		d.rad = (float)o.rad;
+		d.start = (float)o.start;
+		d.end = (float)o.end;
+		d.mesh_root = -1;
+		if(o.type == OBJ_MESH) {
+			const Mesh &m = sc.meshes[o.mesh];
+			d.mesh_root = (m.pos.empty()) ? -1 : m.node_base;
+			d.tri_base = m.tri_base;
+		}
+	}
+	std::vector<DevMat> dm(sc.mats.size());
+	for(size_t i = 0; i < sc.mats.size(); i++) {
+		const Material &m = sc.mats[i];
+		DevMat &d = dm[i];
+		memset(&d, 0, sizeof d);
+		for(int k = 0; k < 4; k++) { d.kd[k] = (float)m.kd[k]; d.ks[k] = (float)m.ks[k]; }
+		/* Material::get_value returns float (src/material.cc:193-196) */
+		d.shin = (float)m.shin;
+		d.refl = (float)m.refl;
+		d.refr = (float)m.refr;
+		d.ior = (float)m.ior;
+		d.phong = m.phong;
+	}
+	std::vector<DevLight> dl(sc.lights.size());
+	for(size_t i = 0; i < sc.lights.size(); i++) {
+		const Light &l = sc.lights[i];
+		DevLight &d = dl[i];
+		memset(&d, 0, sizeof d);
+		d.type = l.type;
+		d.radius = l.radius;
+		for(int k = 0; k < 4; k++) d.col[k] = (float)l.col[k];
+		d.dim[0] = (float)l.dim.x; d.dim[1] = (float)l.dim.y; d.dim[2] = (float)l.dim.z;
+		double m0[4][4];
+		l.xf.matrix(0, m0);
+		for(int r = 0; r < 3; r++) for(int c = 0; c < 4; c++) d.box_m[r * 4 + c] = (float)m0[r][c];
+	}
+	CK(mnodes.upload(nodes, s), "upload mesh nodes");
+	CK(mtris.upload(tris, s), "upload mesh triangles");
+	CK(mprim.upload(prim, s), "upload mesh primitive ids");
+	CK(tri_pos.upload(tp, s), "upload triangle positions");
+	CK(tri_attr.upload(ta, s), "upload triangle attributes");
+	CK(objs.upload(dobj, s), "upload objects");
+	CK(mats.upload(dm, s), "upload materials");
+	CK(lights.upload(dl, s), "upload lights");
+	CK(cudaStreamSynchronize(s), "upload scene");
+	return 0;
+}
+
+int Renderer::build_frame(long bt0, long bt1, cudaStream_t s)
+{
+	if(!loaded) return fail(SRAY_ESTATE, "no scene loaded");
+	t0 = (int)bt0;
+	t1 = (int)bt1;
+	sc.build_tree(t0, t1, opt);
+	std::vector<DevNode> nodes;
+	std::vector<int> slots;
+	flatten_octree(sc.oct, nodes, slots);
+	int shutter = sc.cam.shutter;
+	tlo = t0 - shutter - 2;
+	int thi = t1 + shutter + 2;
+	nt = thi - tlo + 1;
+	std::vector<float> xfs((size_t)sc.objs.size() * nt * XF_STRIDE);
+	for(size_t i = 0; i < sc.objs.size(); i++) {
+		for(int t = 0; t < nt; t++) {
+			double m[4][4];
+			sc.objs[i].xf.matrix(tlo + t, m);
+			pack_xf(m, &xfs[((size_t)i * nt + t) * XF_STRIDE]);
+		}
+	}
+	std::vector<float> lp((size_t)sc.lights.size() * nt * 4);
+	for(size_t i = 0; i < sc.lights.size(); i++) {
+		for(int t = 0; t < nt; t++) {
+			Vec3 p = sc.lights[i].xf.position(tlo + t);
+			float *d = &lp[((size_t)i * nt + t) * 4];
+			d[0] = (float)p.x; d[1] = (float)p.y; d[2] = (float)p.z; d[3] = 0.0f;
+		}
+	}
+	std::vector<float> cm((size_t)nt * 12);
+	for(int t = 0; t < nt; t++) {
+		double m[4][4];
+		sc.cam.matrix(tlo + t, m);
+		for(int r = 0; r < 3; r++) for(int c = 0; c < 4; c++) cm[(size_t)t * 12 + r * 4 + c] = (float)m[r][c];
+	}
+	CK(snodes.upload(nodes, s), "upload scene nodes");
+	CK(sslots.upload(slots, s), "upload scene slots");
+	CK(xf.upload(xfs, s), "upload transforms");
+	CK(light_pos.upload(lp, s), "upload light positions");
+	CK(cam_m.upload(cm, s), "upload camera");
+	CK(cudaStreamSynchronize(s), "build frame");
+	built = true;
+	photons_ready = false;
+	caust.map.n = 0;
+	gi.map.n = 0;
+	fill_scene_desc();
+	return 0;
+}
+
+int Renderer::shoot(cudaStream_t s, int *nc, int *ng)
+{
+	if(!built) return fail(SRAY_ESTATE, "acceleration structures not built");
+	caust.map.n = 0;
+	gi.map.n = 0;
+	int c = 0, g = 0;
+	if((opt.caust_photons || opt.gi_photons) && !sc.lights.empty()) {
+		/* projection maps (src/render.cc:87-103) */
+		sc.build_projmaps(t0, t1, opt.seed);
+		std::vector<uint32_t> bits(sc.lights.size() * 128, 0u);
+		std::vector<float> cov(sc.lights.size() * 2);
+		for(size_t i = 0; i < sc.lights.size(); i++) {
+			const Light &L = sc.lights[i];
+			for(int k = 0; k < 2048; k++) {
+				if(L.pm.cells[k]) bits[i * 128 + (k >> 5)] |= 1u << (k & 31);
+				if(L.spm.cells[k]) bits[i * 128 + 64 + (k >> 5)] |= 1u << (k & 31);
+			}
+			cov[i * 2] = (float)L.pm.get_coverage();
+			cov[i * 2 + 1] = (float)L.spm.get_coverage();
+		}
+		CK(projbits.upload(bits, s), "upload projection maps");
+		CK(coverage.upload(cov, s), "upload coverage");
+		fill_scene_desc();
+		int r;
+		if(opt.caust_photons && (r = photon_shoot_map(*this, 0, s, &c))) return r;
+		if(opt.gi_photons && (r = photon_shoot_map(*this, 1, s, &g))) return r;
+	}
+	photons_ready = true;
+	fill_scene_desc();
+	if(nc) *nc = c;
+	if(ng) *ng = g;
+	return 0;
+}
+
+int Renderer::ensure_queue(int which, int cap)
+{
+	if(cap <= qcap[which]) return 0;
+	size_t per = 16 * 5 + 8;
+	size_t bytes = (size_t)cap * per + 1024;
+	CK(qbuf[which].ensure(bytes), "allocate ray queue");
+	char *b = qbuf[which].as<char>();
+	RayQueue &Q = q[which];
+	Q.o = (float4 *)b; b += (size_t)cap * 16;
+	Q.d = (float4 *)b; b += (size_t)cap * 16;
+	Q.w = (float4 *)b; b += (size_t)cap * 16;
+	Q.meta = (int4 *)b; b += (size_t)cap * 16;
+	Q.stk = (float4 *)b; b += (size_t)cap * 16;
+	Q.ext = (int2 *)b; b += (size_t)cap * 8;
+	Q.cap = cap;
+	qcap[which] = cap;
+	return 0;
+}
+
+int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t s)
+{
+	(void)msec;
+	if(!built || !photons_ready) return fail(SRAY_ESTATE, "frame not prepared (build and shoot photons first)");
+	int npix = opt.width * opt.height;
+	int ds = opt.diffuse_samples < 0 ? 0 : (opt.diffuse_samples > MAX_DS ? MAX_DS : opt.diffuse_samples);
+	int maxs = opt.max_samples < 1 ? 1 : opt.max_samples;
+	CK(ctr.ensure(sizeof(DevCounters)), "counters");
+	CK(counts.ensure(64 * sizeof(int)), "counts");
+	CK(acc.ensure((size_t)npix * 16), "accumulator");
+	CK(sums.ensure((size_t)npix * 16), "sums");
+	CK(spp.ensure((size_t)npix * 4), "spp");
+	if(maxs > 1) {
+		CK(hist.ensure((size_t)npix * maxs * 16), "sample history");
+		CK(active[0].ensure((size_t)npix * 4), "active list");
+		CK(active[1].ensure((size_t)npix * 4), "active list");
+	}
+	float4 *fbd;
+	if(fb_is_device) fbd = (float4 *)fb;
+	else {
+		CK(fbdev.ensure((size_t)npix * 16), "framebuffer");
+		fbd = fbdev.as<float4>();
+	}
+	int per_ray_children = 2 + (opt.gi_photons ? ds : 0);
+	if(ensure_queue(0, npix)) return SRAY_ECUDA;
+	CK(hits.ensure((size_t)npix * 16), "hits");
+	CK(gq.ensure((size_t)npix * sizeof(GatherReq)), "gather queue");
+	int *cnt = counts.as<int>();
+	/* cnt[0]: queue 0 count, cnt[1]: queue 1 count, cnt[2]: gather count, cnt[3]/cnt[4]: active counts */
+	CK(cudaMemsetAsync(ctr.p, 0, sizeof(DevCounters), s), "reset counters");
+	CK(cudaMemsetAsync(counts.p, 0, 64 * sizeof(int), s), "reset counts");
+	int h_n = npix;
+	CK(cudaMemcpyAsync(cnt + 3, &h_n, sizeof(int), cudaMemcpyHostToDevice, s), "active count");
+	int launches = 0;
+	memset(&stats, 0, sizeof stats);
+	int n_active = npix;
+	for(int sample = 0; sample < maxs && n_active > 0; sample++) {
+		int cur_act = sample & 1;
+		const int *act = (maxs > 1 && sample > 0) ? active[cur_act].as<int>() : nullptr;
+		int *act_count = cnt + 3 + cur_act;
+		int *next_count = cnt + 3 + (cur_act ^ 1);
+		q[0].count = cnt + 0;
+		q[1].count = cnt + 1;
+		k_camera<<<grid_for(n_active, 256), 256, 0, s>>>(S, act, act_count, sample, q[0], acc.as<float4>(), ctr.as<DevCounters>());
+		launches++;
+		int n_rays = n_active;
+		int cur = 0;
+		for(int depth = 0; n_rays > 0; depth++) {
+			int need = n_rays * per_ray_children;
+			if(need < n_rays) need = n_rays;
+			int r = ensure_queue(cur ^ 1, need);
+			if(r) return r;
+			CK(hits.ensure((size_t)n_rays * 16), "hits");
+			CK(gq.ensure((size_t)n_rays * sizeof(GatherReq)), "gather queue");
+			q[0].count = cnt + 0;
+			q[1].count = cnt + 1;
+			CK(cudaMemsetAsync(q[cur ^ 1].count, 0, sizeof(int), s), "reset queue");
+			CK(cudaMemsetAsync(cnt + 2, 0, sizeof(int), s), "reset gather queue");
+			k_trace<false><<<grid_for(n_rays, 128), 128, 0, s>>>(S, q[cur], hits.as<int4>(), ctr.as<DevCounters>());
+			k_shade<<<grid_for(n_rays, 128), 128, 0, s>>>(S, q[cur], hits.as<int4>(), q[cur ^ 1], gq.as<GatherReq>(), cnt + 2,
+					n_rays, acc.as<float4>(), depth, ctr.as<DevCounters>());
+			k_gather<<<grid_for(n_rays, GATHER_WARPS) , GATHER_WARPS * 32, 0, s>>>(S, gq.as<GatherReq>(), cnt + 2, acc.as<float4>(),
+					ctr.as<DevCounters>());
+			launches += 3;
+			stats.secondary_rays += depth ? n_rays : 0;
+			int h_cnt = 0;
+			CK(cudaMemcpyAsync(&h_cnt, q[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "read queue count");
+			CK(cudaStreamSynchronize(s), "bounce");
+			n_rays = h_cnt;
+			cur ^= 1;
+		}
+		CK(cudaMemsetAsync(next_count, 0, sizeof(int), s), "reset next active");
+		k_finish<<<grid_for(n_active, 256), 256, 0, s>>>(act, act_count, sample, acc.as<float4>(), hist.as<float4>(), sums.as<float4>(),
+				maxs, opt.min_samples, opt.max_var, active[cur_act ^ 1].as<int>(), next_count, fbd, spp.as<int>());
+		launches++;
+		stats.samples += n_active;
+		int h_next = 0;
+		CK(cudaMemcpyAsync(&h_next, next_count, sizeof(int), cudaMemcpyDeviceToHost, s), "read active count");
+		CK(cudaStreamSynchronize(s), "sample pass");
+		n_active = h_next;
+	}
+	DevCounters hc;
+	CK(cudaMemcpyAsync(&hc, ctr.p, sizeof hc, cudaMemcpyDeviceToHost, s), "read counters");
+	if(!fb_is_device) CK(cudaMemcpyAsync(fb, fbd, (size_t)npix * 16, cudaMemcpyDeviceToHost, s), "copy framebuffer");
+	CK(cudaStreamSynchronize(s), "render");
+	stats.primary_rays = (int64_t)hc.rays[0];
+	stats.shadow_rays = (int64_t)hc.rays[2];
+	stats.gathers = (int64_t)hc.rays[3];
+	stats.kernel_launches = launches;
+	if(hc.overflow) return fail(SRAY_EDEVICE, "device queue or traversal stack overflow");
+	return 0;
+}
+
+static Renderer *g_R = nullptr;
+static std::string g_err;
+static std::mutex g_mu;
+
+static cudaStream_t as_stream(void *s) { return (cudaStream_t)s; }
+
+}  // namespace sray
+
+using namespace sray;
+
+#define NEED_CTX() do { if(!g_R) { g_err = "sray_gpu_init has not been called"; return SRAY_ESTATE; } } while(0)
+
+extern "C" {
+
+void sray_default_opts(sray_opts *o)
+{
+	memset(o, 0, sizeof *o);
+	o->width = 640; o->height = 480;
+	o->min_samples = 1; o->max_samples = 1;
+	o->max_var = 0.005f;
+	o->min_energy = 0.0001f;
+	o->shadow_samples = 1;
+	o->diffuse_samples = 1;
+	o->blk_sz = 48;
+	o->iter = 7;
+	o->fps = 30;
+	o->gather_dist = 0.001f;
+	o->photon_energy = 300.0f;
+	o->scnoct_max_depth = 5; o->scnoct_max_items = 5;
+	o->meshoct_max_depth = 7; o->meshoct_max_items = 14;
+	o->gather_rcap = 0.5f;
+	o->rng_paths = 1;
+	o->seed = 0x5EED0001ull;
+}
+
+static int check_opts(const sray_opts *o)
+{
+	if(!o) { g_err = "null options"; return SRAY_EINVAL; }
+	if(o->width <= 0 || o->height <= 0 || (int64_t)o->width * o->height > (1 << 27)) { g_err = "bad image size"; return SRAY_EINVAL; }
+	if(o->max_samples < 1 || o->max_samples > 64 || o->min_samples < 0) { g_err = "bad sample counts (1..64)"; return SRAY_EINVAL; }
+	if(o->diffuse_samples < 0 || o->diffuse_samples > MAX_DS) { g_err = "diffuse samples must be 0..8"; return SRAY_EINVAL; }
+	if(o->shadow_samples < 1) { g_err = "shadow samples must be >= 1"; return SRAY_EINVAL; }
+	if(o->iter < 0 || o->iter > 13) { g_err = "iter must be 0..13"; return SRAY_EINVAL; }
+	if(o->caust_photons < 0 || o->gi_photons < 0) { g_err = "negative photon count"; return SRAY_EINVAL; }
+	if(o->caust_k < 0 || o->gi_k < 0) { g_err = "negative k"; return SRAY_EINVAL; }
+	return 0;
+}
+
+int sray_gpu_init(const sray_opts *opt)
+{
+	std::lock_guard<std::mutex> lk(g_mu);
+	int r = check_opts(opt);
+	if(r) return r;
+	if(g_R) { delete g_R; g_R = nullptr; }
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if(e != cudaSuccess) { g_err = std::string("no CUDA device: ") + cudaGetErrorString(e); return SRAY_ECUDA; }
+	g_R = new Renderer;
+	g_R->opt = *opt;
+	g_R->device = dev;
+	memset(&g_R->stats, 0, sizeof g_R->stats);
+	return 0;
+}
+
+int sray_gpu_set_opts(const sray_opts *opt)
+{
+	NEED_CTX();
+	int r = check_opts(opt);
+	if(r) return r;
+	bool geom = opt->meshoct_max_depth != g_R->opt.meshoct_max_depth || opt->meshoct_max_items != g_R->opt.meshoct_max_items;
+	if(geom && g_R->loaded) { g_err = "mesh octree options change needs a scene reload"; return SRAY_ESTATE; }
+	g_R->opt = *opt;
+	g_R->photons_ready = false;
+	if(g_R->built) g_R->fill_scene_desc();
+	return 0;
+}
+
+int sray_gpu_load_scene_mem(const char *xml, size_t len)
+{
+	NEED_CTX();
+	Renderer &R = *g_R;
+	R.loaded = false;
+	R.built = false;
+	R.photons_ready = false;
+	if(!xml) { g_err = "null document"; return SRAY_EINVAL; }
+	std::string err;
+	if(!R.sc.load(xml, len, R.opt, err)) { g_err = err; return SRAY_ELOAD; }
+	int r = R.upload_scene(0);
+	if(r) { g_err = R.err; return r; }
+	R.loaded = true;
+	return 0;
+}
+
+int sray_gpu_load_scene(const char *path)
+{
+	NEED_CTX();
+	if(!path) { g_err = "null path"; return SRAY_EINVAL; }
+	FILE *fp = fopen(path, "rb");
+	if(!fp) { g_err = std::string("failed to open file: ") + path; return SRAY_ELOAD; }
+	fseek(fp, 0, SEEK_END);
+	long sz = ftell(fp);
+	fseek(fp, 0, SEEK_SET);
+	std::string buf(sz > 0 ? (size_t)sz : 0, '\0');
+	size_t rd = sz > 0 ? fread(&buf[0], 1, (size_t)sz, fp) : 0;
+	fclose(fp);
+	return sray_gpu_load_scene_mem(buf.data(), rd);
+}
+
+int sray_gpu_scene_info(int *n_objects, int *n_lights, int *n_materials, int64_t *n_triangles, int *n_unique_meshes)
+{
+	NEED_CTX();
+	Renderer &R = *g_R;
+	if(!R.loaded) { g_err = "no scene loaded"; return SRAY_ESTATE; }
+	if(n_objects) *n_objects = (int)R.sc.objs.size();
+	if(n_lights) *n_lights = (int)R.sc.lights.size();
+	if(n_materials) *n_materials = (int)R.sc.mats.size();
+	if(n_triangles) *n_triangles = R.sc.n_tris;
+	if(n_unique_meshes) *n_unique_meshes = (int)R.sc.meshes.size();
+	return 0;
+}
+
+int sray_gpu_build(long t0, long t1)
+{
+	NEED_CTX();
+	int r = g_R->build_frame(t0, t1, 0);
+	if(r) g_err = g_R->err;
+	return r;
+}
+
+int sray_gpu_shoot_photons(long t0, long t1, int *caust_stored, int *gi_stored, void *stream)
+{
+	NEED_CTX();
+	Renderer &R = *g_R;
+	if(!R.built || R.t0 != (int)t0 || R.t1 != (int)t1) {
+		int r = R.build_frame(t0, t1, as_stream(stream));
+		if(r) { g_err = R.err; return r; }
+	}
+	int r = R.shoot(as_stream(stream), caust_stored, gi_stored);
+	if(r) g_err = R.err;
+	return r;
+}
+
+static void frame_interval(const Renderer &R, long msec, long *t0, long *t1)
+{
+	long shutter = R.sc.cam.shutter;
+	*t0 = msec - shutter / 2;
+	*t1 = *t0 + shutter;
+}
+
+int sray_gpu_render_pixels(long msec, float *fb, int fb_is_device, void *stream)
+{
+	NEED_CTX();
+	if(!fb) { g_err = "null framebuffer"; return SRAY_EINVAL; }
+	int r = g_R->render_pixels(msec, fb, fb_is_device, as_stream(stream));
+	if(r) g_err = g_R->err;
+	return r;
+}
+
+int sray_gpu_render(long msec, float *fb, int fb_is_device, void *stream)
+{
+	NEED_CTX();
+	Renderer &R = *g_R;
+	if(!R.loaded) { g_err = "no scene loaded"; return SRAY_ESTATE; }
+	if(!fb) { g_err = "null framebuffer"; return SRAY_EINVAL; }
+	long t0, t1;
+	frame_interval(R, msec, &t0, &t1);
+	int r = R.build_frame(t0, t1, as_stream(stream));
+	if(!r) r = R.shoot(as_stream(stream), nullptr, nullptr);
+	if(!r) r = R.render_pixels(msec, fb, fb_is_device, as_stream(stream));
+	if(r) g_err = R.err;
+	return r;
+}
+
+int sray_gpu_cast_rays(int n, const float *orig, const float *dir, const int *time, int *obj, int *prim, float *t,
+		unsigned char *tie, void *stream)
+{
+	NEED_CTX();
+	Renderer &R = *g_R;
+	if(!R.built) { g_err = "acceleration structures not built"; return SRAY_ESTATE; }
+	if(n < 0 || (n > 0 && (!orig || !dir || !obj || !prim || !t || !tie))) { g_err = "bad arguments"; return SRAY_EINVAL; }
+	if(n == 0) return 0;
+	cudaStream_t s = as_stream(stream);
+	cudaError_t e = R.ctr.ensure(sizeof(DevCounters));
+	if(e == cudaSuccess) e = cudaMemsetAsync(R.ctr.p, 0, sizeof(DevCounters), s);
+	if(e != cudaSuccess) { g_err = cudaGetErrorString(e); return SRAY_ECUDA; }
+	k_cast<<<grid_for(n, 128), 128, 0, s>>>(R.S, n, orig, dir, time, obj, prim, t, tie, R.ctr.as<DevCounters>());
+	DevCounters hc;
+	e = cudaMemcpyAsync(&hc, R.ctr.p, sizeof hc, cudaMemcpyDeviceToHost, s);
+	if(e == cudaSuccess) e = cudaStreamSynchronize(s);
+	if(e != cudaSuccess) { g_err = cudaGetErrorString(e); return SRAY_ECUDA; }
+	if(hc.overflow) { g_err = "traversal stack overflow"; return SRAY_EDEVICE; }
+	return 0;
+}
+
+int sray_gpu_primary_hits(long msec, int *obj, int *prim, float *t, unsigned char *tie, void *stream)
+{
+	NEED_CTX();
+	Renderer &R = *g_R;
+	if(!R.loaded) { g_err = "no scene loaded"; return SRAY_ESTATE; }
+	if(!obj || !prim || !t || !tie) { g_err = "bad arguments"; return SRAY_EINVAL; }
+	cudaStream_t s = as_stream(stream);
+	long t0, t1;
+	frame_interval(R, msec, &t0, &t1);
+	if(!R.built || R.t0 != (int)t0 || R.t1 != (int)t1) {
+		int r = R.build_frame(t0, t1, s);
+		if(r) { g_err = R.err; return r; }
+	}
+	int npix = R.opt.width * R.opt.height;
+	if(R.ensure_queue(0, npix)) { g_err = R.err; return SRAY_ECUDA; }
+	cudaError_t e = R.hits.ensure((size_t)npix * 16);
+	if(e == cudaSuccess) e = R.ctr.ensure(sizeof(DevCounters));
+	if(e == cudaSuccess) e = R.counts.ensure(64 * sizeof(int));
+	if(e == cudaSuccess) e = cudaMemsetAsync(R.ctr.p, 0, sizeof(DevCounters), s);
+	if(e == cudaSuccess) e = R.acc.ensure((size_t)npix * 16);
+	if(e != cudaSuccess) { g_err = cudaGetErrorString(e); return SRAY_ECUDA; }
+	int *cnt = R.counts.as<int>();
+	e = cudaMemcpyAsync(cnt + 3, &npix, sizeof(int), cudaMemcpyHostToDevice, s);
+	if(e != cudaSuccess) { g_err = cudaGetErrorString(e); return SRAY_ECUDA; }
+	R.q[0].count = cnt + 0;
+	k_camera<<<grid_for(npix, 256), 256, 0, s>>>(R.S, nullptr, cnt + 3, 0, R.q[0], R.acc.as<float4>(), R.ctr.as<DevCounters>());
+	k_trace<false><<<grid_for(npix, 128), 128, 0, s>>>(R.S, R.q[0], R.hits.as<int4>(), R.ctr.as<DevCounters>());
+	k_primary_hits<<<grid_for(npix, 256), 256, 0, s>>>(R.S, R.q[0], R.hits.as<int4>(), obj, prim, t, tie);
+	DevCounters hc;
+	e = cudaMemcpyAsync(&hc, R.ctr.p, sizeof hc, cudaMemcpyDeviceToHost, s);
+	if(e == cudaSuccess) e = cudaStreamSynchronize(s);
+	if(e != cudaSuccess) { g_err = cudaGetErrorString(e); return SRAY_ECUDA; }
+	if(hc.overflow) { g_err = "traversal stack overflow"; return SRAY_EDEVICE; }
+	return 0;
+}
+
+int sray_gpu_get_photons(int which, float *out, int cap, int *n_out)
+{
+	NEED_CTX();
+	Renderer &R = *g_R;
+	const PhotonBufs &P = which ? R.gi : R.caust;
+	int n = P.map.n;
+	if(n_out) *n_out = n;
+	if(!out || cap <= 0 || n == 0) return 0;
+	int m = n < cap ? n : cap;
+	std::vector<DevPhoton> h(m);
+	cudaError_t e = cudaMemcpy(h.data(), P.ph.p, (size_t)m * sizeof(DevPhoton), cudaMemcpyDeviceToHost);
+	if(e != cudaSuccess) { g_err = cudaGetErrorString(e); return SRAY_ECUDA; }
+	for(int i = 0; i < m; i++) {
+		float *f = out + (size_t)i * 16;
+		f[0] = h[i].p[0]; f[1] = h[i].p[1]; f[2] = h[i].p[2];
+		f[3] = h[i].d[0]; f[4] = h[i].d[1]; f[5] = h[i].d[2];
+		f[6] = h[i].n[0]; f[7] = h[i].n[1]; f[8] = h[i].n[2];
+		f[9] = h[i].p[3]; f[10] = h[i].d[3]; f[11] = h[i].n[3]; f[12] = 0.0f;
+		f[13] = f[14] = f[15] = 0.0f;
+	}
+	return 0;
+}
+
+int sray_gpu_get_stats(sray_stats *st)
+{
+	NEED_CTX();
+	if(!st) { g_err = "null stats"; return SRAY_EINVAL; }
+	*st = g_R->stats;
+	st->photons_stored = (int64_t)g_R->caust.map.n + g_R->gi.map.n;
+	return 0;
+}
+
+int sray_gpu_last_error(char *buf, size_t cap)
+{
+	if(!buf || cap == 0) return SRAY_EINVAL;
+	size_t n = g_err.size() < cap - 1 ? g_err.size() : cap - 1;
+	memcpy(buf, g_err.data(), n);
+	buf[n] = 0;
+	return 0;
+}
+
+void sray_gpu_shutdown(void)
+{
+	std::lock_guard<std::mutex> lk(g_mu);
+	if(!g_R) return;
+	Renderer &R = *g_R;
+	DevBuf *bufs[] = {&R.mnodes, &R.mtris, &R.mprim, &R.tri_pos, &R.tri_attr, &R.objs, &R.mats, &R.lights, &R.snodes, &R.sslots,
+		&R.xf, &R.light_pos, &R.cam_m, &R.projbits, &R.coverage, &R.qbuf[0], &R.qbuf[1], &R.hits, &R.gq, &R.acc, &R.hist, &R.sums,
+		&R.active[0], &R.active[1], &R.spp, &R.fbdev, &R.ctr, &R.counts};
+	for(DevBuf *b : bufs) b->release();
+	PhotonBufs *pb[] = {&R.caust, &R.gi};
+	for(PhotonBufs *p : pb) {
+		DevBuf *pbufs[] = {&p->ph, &p->cells, &p->tmp_ph, &p->valid, &p->keys, &p->keys2, &p->vals, &p->vals2, &p->lin, &p->hist, &p->scan};
+		for(DevBuf *b : pbufs) b->release();
+	}
+	delete g_R;
+	g_R = nullptr;
+}
+
+}  /* extern "C" */

@@ -1,0 +1,121 @@
+/* renderer.h -- host-side state of the GPU renderer behind the C-ABI. */
+#ifndef SRAY_RENDERER_H_
+#define SRAY_RENDERER_H_
+
+#include <string>
+#include <vector>
+#include <cuda_runtime.h>
+#include "sray_gpu.h"
+#include "scene_host.h"
+#include "dev_common.cuh"
+
+namespace sray {
+
+/* a device allocation that only grows */
+struct DevBuf {
+	void *p = nullptr;
+	size_t bytes = 0;
+	cudaError_t ensure(size_t n)
+	{
+		if(n <= bytes) return cudaSuccess;
+		if(p) cudaFree(p);
+		p = nullptr;
+		bytes = 0;
+		cudaError_t e = cudaMalloc(&p, n < 256 ? 256 : n);
+		if(e == cudaSuccess) bytes = n < 256 ? 256 : n;
+		return e;
+	}
+	template <class T> cudaError_t upload(const std::vector<T> &v, cudaStream_t s)
+	{
+		cudaError_t e = ensure(v.size() * sizeof(T) + 16);
+		if(e != cudaSuccess || v.empty()) return e;
+		return cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+	}
+	void release()
+	{
+		if(p) cudaFree(p);
+		p = nullptr;
+		bytes = 0;
+	}
+	template <class T> T *as() const { return (T *)p; }
+};
+
+/* structure-of-arrays ray queue */
+struct RayQueue {
+	float4 *o;      /* origin xyz, energy */
+	float4 *d;      /* direction xyz, current ior */
+	float4 *w;      /* throughput weight rgb, unused */
+	int4 *meta;     /* pixel, iter, path, time */
+	float4 *stk;    /* ior stack */
+	int2 *ext;      /* sample | diffuse index << 16, stack depth */
+	int *count;
+	int cap;
+};
+
+/* a pending photon-map gather: pos + kind, normal + pixel, weight */
+struct GatherReq {
+	float4 a;
+	float4 b;
+	float4 w;
+};
+
+/* device-side error and work counters */
+struct DevCounters {
+	int overflow;        /* traversal stack or queue overflow */
+	int gen_dir_fail;    /* projection-map rejection sampling gave up */
+	int pad[2];
+	unsigned long long rays[4];   /* primary, secondary, shadow, gather */
+	unsigned long long nodes, prims;
+};
+
+struct PhotonBufs {
+	DevBuf ph, cells, tmp_ph, valid, keys, keys2, vals, vals2, lin, hist, scan;
+	DPhotonMap map;
+	int n = 0;
+};
+
+struct Renderer {
+	sray_opts opt;
+	int device = 0;
+	HostScene sc;
+	bool loaded = false;
+	std::string err;
+
+	/* scene tables (per load) */
+	DevBuf mnodes, mtris, mprim, tri_pos, tri_attr, objs, mats, lights;
+	/* frame tables (per build) */
+	DevBuf snodes, sslots, xf, light_pos, cam_m, projbits, coverage;
+	bool built = false;
+	int t0 = 0, t1 = 0, tlo = 0, nt = 1;
+	long frame_msec = 0;
+	bool photons_ready = false;
+	PhotonBufs caust, gi;
+	DScene S;
+
+	/* render buffers */
+	DevBuf qbuf[2], hits, gq, acc, hist, sums, active[2], spp, fbdev, ctr, counts;
+	RayQueue q[2];
+	int qcap[2] = {0, 0};
+	sray_stats stats;
+
+	int fail(int code, const std::string &msg) { err = msg; return code; }
+	int cuda_fail(cudaError_t e, const char *where)
+	{
+		err = std::string(where) + ": " + cudaGetErrorString(e);
+		return SRAY_ECUDA;
+	}
+
+	int upload_scene(cudaStream_t s);
+	int build_frame(long t0, long t1, cudaStream_t s);
+	int shoot(cudaStream_t s, int *nc, int *ng);
+	int render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t s);
+	int ensure_queue(int which, int cap);
+	void fill_scene_desc();
+};
+
+/* photon.cu */
+int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored);
+
+}  // namespace sray
+
+#endif

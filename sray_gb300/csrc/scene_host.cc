@@ -1,0 +1,1090 @@
+/* scene_host.cc -- S-ray scene database on the host (see scene_host.h).
+ *
+ * Reference behaviour reproduced here:
+ *   XML attribute typing            src/xmltree.c:51-95
+ *   scene loading order             src/scene.cc:93-183
+ *   materials and defaults          src/material.cc:68-111
+ *   objects / meshes                src/object.cc:28-58, src/meshload.cc:55-157
+ *   lights                          src/light.cc:38-63, 255-275, 326-350
+ *   cameras                         src/camera.cc:16-66, 161-234
+ *   keyframe tracks and transforms  src/anim.inl:70-263, src/anim.cc:68-121, 391-427
+ *   octree build                    src/octree.inl:119-191
+ *   scene octree                    src/scene.cc:353-390
+ *   projection maps                 src/projmap.cc:25-160, src/light.cc:151-200, 392-432
+ */
+#include <math.h>
+#include <float.h>
+#include <limits.h>
+#include <stdlib.h>
+#include <string.h>
+#include <algorithm>
+#include <thread>
+#include "scene_host.h"
+#include "sray_rng.h"
+
+namespace sray {
+
+/* ------------------------------------------------------------------ */
+/* flat XML DOM: names and values are views into the document buffer   */
+/* ------------------------------------------------------------------ */
+namespace {
+
+struct XAttr {
+	const char *name;
+	const char *val;
+	int nlen, vlen;
+};
+
+struct XNode {
+	const char *name;
+	int nlen;
+	int attr0, nattr;
+	int first_child = -1, last_child = -1, next = -1;
+};
+
+struct Typed {
+	int type;        /* 0 str, 1 int, 2 flt, 3 vec */
+	int ival;
+	double fval;
+	double vval[4];
+	std::string str;
+};
+
+enum { T_STR, T_INT, T_FLT, T_VEC };
+
+struct Doc {
+	std::vector<XNode> nodes;
+	std::vector<XAttr> attrs;
+	std::string err;
+
+	static bool eq(const char *s, int n, const char *lit)
+	{
+		int l = (int)strlen(lit);
+		return l == n && memcmp(s, lit, n) == 0;
+	}
+	bool is(int node, const char *lit) const { return eq(nodes[node].name, nodes[node].nlen, lit); }
+
+	const XAttr *attr(int node, const char *name) const
+	{
+		const XNode &n = nodes[node];
+		for(int i = 0; i < n.nattr; i++) {
+			const XAttr &a = attrs[n.attr0 + i];
+			if(eq(a.name, a.nlen, name)) return &a;
+		}
+		return 0;
+	}
+
+	static std::string decode(const char *v, int n)
+	{
+		std::string s(v, n);
+		if(s.find('&') == std::string::npos) return s;
+		std::string o;
+		for(size_t i = 0; i < s.size(); i++) {
+			if(s[i] == '&') {
+				size_t semi = s.find(';', i);
+				if(semi != std::string::npos) {
+					std::string e = s.substr(i + 1, semi - i - 1);
+					const char *r = e == "lt" ? "<" : e == "gt" ? ">" : e == "amp" ? "&" : e == "quot" ? "\"" : e == "apos" ? "'" : 0;
+					if(r) { o += r; i = semi; continue; }
+				}
+			}
+			o += s[i];
+		}
+		return o;
+	}
+
+	/* xml_create_attr typing (src/xmltree.c:75-93) */
+	static bool typed(const XAttr *a, Typed *t)
+	{
+		if(!a) return false;
+		t->str = decode(a->val, a->vlen);
+		const char *val = t->str.c_str();
+		t->type = T_STR;
+		t->ival = 0;
+		t->fval = 0.0;
+		t->vval[0] = t->vval[1] = t->vval[2] = t->vval[3] = 0.0;
+		if(isdigit((unsigned char)val[0]) || ((val[0] == '+' || val[0] == '-') && isdigit((unsigned char)val[1]))) {
+			t->type = strchr(val, '.') ? T_FLT : T_INT;
+			t->ival = atoi(val);
+			t->fval = strtod(val, 0);
+			t->vval[0] = t->vval[1] = t->vval[2] = t->vval[3] = 1.0;
+			int i;
+			for(i = 0; i < 4; i++) {
+				if(!*val) break;
+				t->vval[i] = strtod(val, 0);
+				while(*val && !isspace((unsigned char)*val)) val++;
+				while(*val && isspace((unsigned char)*val)) val++;
+			}
+			if(i > 1) t->type = T_VEC;
+		}
+		return true;
+	}
+
+	/* fast path for the mesh elements: integer attribute (id / vref indices) */
+	static bool int_attr(const XAttr *a, int *out)
+	{
+		if(!a || a->vlen <= 0) return false;
+		const char *v = a->val;
+		if(!(isdigit((unsigned char)v[0]) || ((v[0] == '+' || v[0] == '-') && a->vlen > 1 && isdigit((unsigned char)v[1])))) return false;
+		for(int i = 0; i < a->vlen; i++) {
+			if(v[i] == '.') return false;
+			if(isspace((unsigned char)v[i])) {
+				/* more than one number makes it a vector */
+				for(int j = i; j < a->vlen; j++) if(!isspace((unsigned char)v[j])) return false;
+				break;
+			}
+		}
+		*out = atoi(v);
+		return true;
+	}
+
+	bool parse(const char *p, size_t len)
+	{
+		const char *end = p + len;
+		std::vector<int> stack;
+		nodes.reserve(len / 48 + 16);
+		attrs.reserve(len / 40 + 16);
+		while(p < end) {
+			while(p < end && *p != '<') p++;
+			if(p >= end) break;
+			if(p + 3 < end && p[1] == '!' && p[2] == '-' && p[3] == '-') {
+				const char *e = p + 4;
+				while(e + 2 < end && !(e[0] == '-' && e[1] == '-' && e[2] == '>')) e++;
+				if(e + 2 >= end) { err = "unterminated comment"; return false; }
+				p = e + 3;
+				continue;
+			}
+			if(p + 1 < end && (p[1] == '?' || p[1] == '!')) {
+				while(p < end && *p != '>') p++;
+				p++;
+				continue;
+			}
+			if(p + 1 < end && p[1] == '/') {
+				p += 2;
+				const char *ns = p;
+				while(p < end && *p != '>' && !isspace((unsigned char)*p)) p++;
+				if(stack.empty()) { err = "unbalanced closing tag"; return false; }
+				const XNode &top = nodes[stack.back()];
+				if(top.nlen != (int)(p - ns) || memcmp(top.name, ns, top.nlen) != 0) {
+					err = "mismatched closing tag </" + std::string(ns, p - ns) + ">";
+					return false;
+				}
+				while(p < end && *p != '>') p++;
+				p++;
+				stack.pop_back();
+				continue;
+			}
+			p++;
+			XNode n;
+			n.name = p;
+			while(p < end && !isspace((unsigned char)*p) && *p != '/' && *p != '>') p++;
+			n.nlen = (int)(p - n.name);
+			n.attr0 = (int)attrs.size();
+			n.nattr = 0;
+			bool selfclose = false;
+			for(;;) {
+				while(p < end && isspace((unsigned char)*p)) p++;
+				if(p >= end) { err = "unexpected end of document in a tag"; return false; }
+				if(*p == '/') {
+					if(p + 1 < end && p[1] == '>') { p += 2; selfclose = true; break; }
+					err = "malformed tag";
+					return false;
+				}
+				if(*p == '>') { p++; break; }
+				XAttr a;
+				a.name = p;
+				while(p < end && *p != '=' && !isspace((unsigned char)*p)) p++;
+				a.nlen = (int)(p - a.name);
+				while(p < end && isspace((unsigned char)*p)) p++;
+				if(p >= end || *p != '=') { err = "attribute without value"; return false; }
+				p++;
+				while(p < end && isspace((unsigned char)*p)) p++;
+				if(p >= end || (*p != '"' && *p != '\'')) { err = "unquoted attribute value"; return false; }
+				char q = *p++;
+				a.val = p;
+				while(p < end && *p != q) p++;
+				if(p >= end) { err = "unterminated attribute value"; return false; }
+				a.vlen = (int)(p - a.val);
+				p++;
+				attrs.push_back(a);
+				n.nattr++;
+			}
+			int id = (int)nodes.size();
+			nodes.push_back(n);
+			if(!stack.empty()) {
+				XNode &par = nodes[stack.back()];
+				if(par.last_child < 0) par.first_child = id;
+				else nodes[par.last_child].next = id;
+				par.last_child = id;
+			} else if(id != 0) {
+				err = "more than one root element";
+				return false;
+			}
+			if(!selfclose) stack.push_back(id);
+		}
+		if(nodes.empty()) { err = "no root element"; return false; }
+		if(!stack.empty()) { err = "unexpected end of document"; return false; }
+		return true;
+	}
+};
+
+}  // namespace
+
+/* ------------------------------------------------------------------ */
+/* keyframe tracks (src/anim.inl:70-263)                                */
+/* ------------------------------------------------------------------ */
+template <class T> static int nearest_key(const Track<T> &tr, int s, int e, int time)
+{
+	while(true) {
+		if(s == e) return s;
+		if(e - s == 1) return abs(time - tr.time[s]) < abs(tr.time[e] - time) ? s : e;
+		int mid = (s + e) / 2;
+		if(time < tr.time[mid]) e = mid;
+		else if(time > tr.time[mid]) s = mid + 1;
+		else return mid;
+	}
+}
+
+template <class T> static void set_key(Track<T> &tr, int time, const T &v)
+{
+	if(!tr.time.empty()) {
+		int n = nearest_key(tr, 0, (int)tr.time.size() - 1, time);
+		if(tr.time[n] == time) { tr.val[n] = v; return; }
+	}
+	size_t pos = std::upper_bound(tr.time.begin(), tr.time.end(), time) - tr.time.begin();
+	tr.time.insert(tr.time.begin() + pos, time);
+	tr.val.insert(tr.val.begin() + pos, v);
+}
+
+static Vec3 mix(const Vec3 &a, const Vec3 &b, double t)
+{
+	return Vec3(a.x + (b.x - a.x) * t, a.y + (b.y - a.y) * t, a.z + (b.z - a.z) * t);
+}
+static Quat mix(const Quat &a, const Quat &b, double t)
+{
+	Quat r = {a.s + (b.s - a.s) * t, a.x + (b.x - a.x) * t, a.y + (b.y - a.y) * t, a.z + (b.z - a.z) * t};
+	return r;
+}
+static Vec3 spline(const Vec3 &v0, const Vec3 &v1, const Vec3 &v2, const Vec3 &v3, double t)
+{
+	double t2 = t * t, t3 = t2 * t;
+	Vec3 r;
+	for(int i = 0; i < 3; i++) {
+		double a = v0[i], b = v1[i], c = v2[i], d = v3[i];
+		double v = (b * 2.0 + (c - a) * t + (a * 2.0 - b * 5.0 + c * 4.0 - d) * t2 + (b * 3.0 - a - c * 3.0 + d) * t3) * 0.5;
+		if(i == 0) r.x = v; else if(i == 1) r.y = v; else r.z = v;
+	}
+	return r;
+}
+static Quat spline(const Quat &, const Quat &a, const Quat &b, const Quat &, double t)
+{
+	/* catmull_rom_spline on quaternions is a slerp of the middle keys (src/anim.inl:268-273) */
+	double d = a.s * b.s + a.x * b.x + a.y * b.y + a.z * b.z;
+	Quat bb = b;
+	if(d < 0.0) { d = -d; bb.s = -bb.s; bb.x = -bb.x; bb.y = -bb.y; bb.z = -bb.z; }
+	double wa, wb;
+	if(d > 0.9999) { wa = 1.0 - t; wb = t; }
+	else {
+		double ang = acos(d), sn = sin(ang);
+		wa = sin((1.0 - t) * ang) / sn;
+		wb = sin(t * ang) / sn;
+	}
+	Quat r = {a.s * wa + bb.s * wb, a.x * wa + bb.x * wb, a.y * wa + bb.y * wb, a.z * wa + bb.z * wb};
+	return r;
+}
+
+template <class T> static T eval(const Track<T> &tr, int time)
+{
+	size_t n = tr.time.size();
+	if(!n) return tr.def;
+	if(n > 1) {
+		int first = tr.time[0], last = tr.time[n - 1];
+		if(first != last && (time < first || time > last) && tr.extrap == EXTRAP_REPEAT) {
+			while(time < first) time += last - first;
+			time = (time - first) % (last - first) + first;
+		}
+	}
+	int k = nearest_key(tr, 0, (int)n - 1, time);
+	int s = k, e = -1;
+	if(time < tr.time[k] && tr.time[k] != tr.time[0]) { s = k - 1; e = k; }
+	else if(time > tr.time[k] && tr.time[k] != tr.time[n - 1]) { s = k; e = k + 1; }
+	if(e < 0 || tr.interp == INTERP_STEP) return tr.val[s];
+	double t = (double)(time - tr.time[s]) / (double)(tr.time[e] - tr.time[s]);
+	if(tr.interp == INTERP_LINEAR) return mix(tr.val[s], tr.val[e], t);
+	if(tr.interp == INTERP_CUBIC) {
+		const T &v0 = tr.val[s > 0 ? s - 1 : s];
+		const T &v3 = tr.val[e < (int)n - 1 ? e + 1 : e];
+		return spline(v0, tr.val[s], tr.val[e], v3, t);
+	}
+	return tr.val[s];
+}
+
+/* ------------------------------------------------------------------ */
+/* 4x4 matrices (row-major, column vectors)                             */
+/* ------------------------------------------------------------------ */
+static void m_ident(double m[4][4]) { memset(m, 0, 16 * sizeof(double)); m[0][0] = m[1][1] = m[2][2] = m[3][3] = 1.0; }
+static void m_mul(double o[4][4], const double a[4][4], const double b[4][4])
+{
+	double r[4][4];
+	for(int i = 0; i < 4; i++)
+		for(int j = 0; j < 4; j++)
+			r[i][j] = a[i][0] * b[0][j] + a[i][1] * b[1][j] + a[i][2] * b[2][j] + a[i][3] * b[3][j];
+	memcpy(o, r, sizeof r);
+}
+static void m_quat(double m[4][4], const Quat &q)
+{
+	m_ident(m);
+	double s = q.s, x = q.x, y = q.y, z = q.z;
+	m[0][0] = 1.0 - 2.0 * y * y - 2.0 * z * z;
+	m[0][1] = 2.0 * x * y - 2.0 * s * z;
+	m[0][2] = 2.0 * z * x + 2.0 * s * y;
+	m[1][0] = 2.0 * x * y + 2.0 * s * z;
+	m[1][1] = 1.0 - 2.0 * x * x - 2.0 * z * z;
+	m[1][2] = 2.0 * y * z - 2.0 * s * x;
+	m[2][0] = 2.0 * z * x - 2.0 * s * y;
+	m[2][1] = 2.0 * y * z + 2.0 * s * x;
+	m[2][2] = 1.0 - 2.0 * x * x - 2.0 * y * y;
+}
+static double det3(double a, double b, double c, double d, double e, double f, double g, double h, double i)
+{
+	return a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
+}
+void mat_inverse(double out[4][4], const double m[4][4])
+{
+	double cof[4][4];
+	for(int i = 0; i < 4; i++) {
+		for(int j = 0; j < 4; j++) {
+			double s[9];
+			int k = 0;
+			for(int r = 0; r < 4; r++) {
+				if(r == i) continue;
+				for(int c = 0; c < 4; c++) if(c != j) s[k++] = m[r][c];
+			}
+			double mn = det3(s[0], s[1], s[2], s[3], s[4], s[5], s[6], s[7], s[8]);
+			cof[i][j] = ((i + j) & 1) ? -mn : mn;
+		}
+	}
+	double det = m[0][0] * cof[0][0] + m[0][1] * cof[0][1] + m[0][2] * cof[0][2] + m[0][3] * cof[0][3];
+	for(int i = 0; i < 4; i++)
+		for(int j = 0; j < 4; j++)
+			out[i][j] = cof[j][i] / det;
+}
+static Vec3 m_pt(const double m[4][4], const Vec3 &p)
+{
+	return Vec3(m[0][0] * p.x + m[0][1] * p.y + m[0][2] * p.z + m[0][3],
+			m[1][0] * p.x + m[1][1] * p.y + m[1][2] * p.z + m[1][3],
+			m[2][0] * p.x + m[2][1] * p.y + m[2][2] * p.z + m[2][3]);
+}
+
+XForm::XForm()
+{
+	pos.def = Vec3(0, 0, 0);
+	scale.def = Vec3(1, 1, 1);
+	Quat id = {1, 0, 0, 0};
+	rot.def = id;
+}
+Vec3 XForm::position(int t) const { return eval(pos, t); }
+Vec3 XForm::scaling(int t) const { return eval(scale, t); }
+
+/* XFormNode::get_xform_matrix: pivot * T * R * S * -pivot (src/anim.cc:391-419) */
+void XForm::matrix(int t, double m[4][4]) const
+{
+	Vec3 p = eval(pos, t), s = eval(scale, t);
+	Quat q = eval(rot, t);
+	double pm[4][4], npm[4][4], tm[4][4], rm[4][4], sm[4][4], a[4][4];
+	m_ident(pm); pm[0][3] = pivot.x; pm[1][3] = pivot.y; pm[2][3] = pivot.z;
+	m_ident(npm); npm[0][3] = -pivot.x; npm[1][3] = -pivot.y; npm[2][3] = -pivot.z;
+	m_ident(tm); tm[0][3] = p.x; tm[1][3] = p.y; tm[2][3] = p.z;
+	m_quat(rm, q);
+	m_ident(sm); sm[0][0] = s.x; sm[1][1] = s.y; sm[2][2] = s.z;
+	m_mul(a, pm, tm);
+	m_mul(a, a, rm);
+	m_mul(a, a, sm);
+	m_mul(m, a, npm);
+}
+
+static double v_len(const Vec3 &v) { return sqrt(v.x * v.x + v.y * v.y + v.z * v.z); }
+static Vec3 v_cross(const Vec3 &a, const Vec3 &b)
+{
+	return Vec3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+static Vec3 v_norm(const Vec3 &v) { double l = v_len(v); return Vec3(v.x / l, v.y / l, v.z / l); }
+
+/* TargetCamera::get_matrix (src/camera.cc:216-234) */
+void Camera::matrix(int t, double m[4][4]) const
+{
+	if(!target) {
+		xf.matrix(t, m);
+		return;
+	}
+	Vec3 p = xf.position(t), tg = txf.position(t);
+	Vec3 up(0, 1, 0);
+	Vec3 dir = v_norm(Vec3(tg.x - p.x, tg.y - p.y, tg.z - p.z));
+	Vec3 right = v_norm(v_cross(up, dir));
+	up = v_cross(dir, right);
+	double roll = txf.scaling(t).x;
+	double half = roll * 0.5, sn = sin(half);
+	Quat q = {cos(half), dir.x * sn, dir.y * sn, dir.z * sn};
+	double rm[4][4];
+	m_quat(rm, q);
+	Vec3 u(rm[0][0] * up.x + rm[0][1] * up.y + rm[0][2] * up.z, rm[1][0] * up.x + rm[1][1] * up.y + rm[1][2] * up.z,
+			rm[2][0] * up.x + rm[2][1] * up.y + rm[2][2] * up.z);
+	Vec3 r(rm[0][0] * right.x + rm[0][1] * right.y + rm[0][2] * right.z, rm[1][0] * right.x + rm[1][1] * right.y + rm[1][2] * right.z,
+			rm[2][0] * right.x + rm[2][1] * right.y + rm[2][2] * right.z);
+	m_ident(m);
+	m[0][0] = r.x; m[0][1] = u.x; m[0][2] = dir.x; m[0][3] = p.x;
+	m[1][0] = r.y; m[1][1] = u.y; m[1][2] = dir.y; m[1][3] = p.y;
+	m[2][0] = r.z; m[2][1] = u.z; m[2][2] = dir.z; m[2][3] = p.z;
+}
+
+/* ------------------------------------------------------------------ */
+/* bounds and octree                                                     */
+/* ------------------------------------------------------------------ */
+Box Object::bounds(const std::vector<Mesh> &meshes, int t) const
+{
+	Box b;
+	double m[4][4];
+	xf.matrix(t, m);
+	if(type == OBJ_SPHERE) {
+		Vec3 c = m_pt(m, Vec3(0, 0, 0));
+		for(int i = 0; i < 3; i++) { b.mn[i] = c[i] - rad; b.mx[i] = c[i] + rad; }
+	} else if(type == OBJ_CYLINDER) {
+		Vec3 s1 = m_pt(m, Vec3(0, start, 0)), s2 = m_pt(m, Vec3(0, end, 0));
+		for(int i = 0; i < 3; i++) {
+			double a0 = s1[i] - rad, a1 = s2[i] - rad, c0 = s1[i] + rad, c1 = s2[i] + rad;
+			b.mn[i] = a0 < a1 ? a0 : a1;
+			b.mx[i] = c0 > c1 ? c0 : c1;
+		}
+	} else {
+		for(int i = 0; i < 3; i++) { b.mn[i] = FLT_MAX; b.mx[i] = -FLT_MAX; }
+		const Mesh &me = meshes[mesh];
+		size_t nv = me.posd.size() / 3;
+		for(size_t v = 0; v < nv; v++) {
+			Vec3 p = m_pt(m, Vec3(me.posd[v * 3], me.posd[v * 3 + 1], me.posd[v * 3 + 2]));
+			for(int i = 0; i < 3; i++) {
+				if(p[i] < b.mn[i]) b.mn[i] = p[i];
+				if(p[i] > b.mx[i]) b.mx[i] = p[i];
+			}
+		}
+	}
+	return b;
+}
+
+static inline bool overlap(const Box &a, const Box &b)
+{
+	for(int i = 0; i < 3; i++) if(a.mn[i] > b.mx[i] || b.mn[i] > a.mx[i]) return false;
+	return true;
+}
+
+namespace {
+struct OctBuilder {
+	BuildOctree *o;
+	const std::vector<Box> *boxes;
+	int max_depth, max_items;
+
+	void subdivide(int ni, int lvl)
+	{
+		if((int)o->nodes[ni].items.size() <= max_items || lvl >= max_depth) return;
+		Box b = o->nodes[ni].box;
+		double c[3];
+		for(int i = 0; i < 3; i++) c[i] = (b.mn[i] + b.mx[i]) * 0.5;
+		/* child layout of src/octree.inl:160-168 */
+		static const int hi[8][3] = {{0,0,0},{1,0,0},{1,1,0},{0,1,0},{0,0,1},{1,0,1},{1,1,1},{0,1,1}};
+		int first = (int)o->nodes.size();
+		o->nodes.resize(first + 8);
+		o->nodes[ni].child = first;
+		for(int k = 0; k < 8; k++) {
+			BuildOctree::Node &ch = o->nodes[first + k];
+			for(int i = 0; i < 3; i++) {
+				ch.box.mn[i] = hi[k][i] ? c[i] : b.mn[i];
+				ch.box.mx[i] = hi[k][i] ? b.mx[i] : c[i];
+			}
+			const std::vector<int> &pit = o->nodes[ni].items;
+			std::vector<int> it;
+			for(size_t j = 0; j < pit.size(); j++) if(overlap((*boxes)[pit[j]], ch.box)) it.push_back(pit[j]);
+			o->nodes[first + k].items.swap(it);
+			subdivide(first + k, lvl + 1);
+		}
+		std::vector<int>().swap(o->nodes[ni].items);
+	}
+};
+}  // namespace
+
+void BuildOctree::build(const std::vector<Box> &boxes, int max_depth, int max_items)
+{
+	nodes.clear();
+	Box bounds;
+	for(int i = 0; i < 3; i++) { bounds.mn[i] = FLT_MAX; bounds.mx[i] = -FLT_MAX; }
+	for(size_t k = 0; k < boxes.size(); k++) {
+		for(int i = 0; i < 3; i++) {
+			if(boxes[k].mn[i] < bounds.mn[i]) bounds.mn[i] = boxes[k].mn[i];
+			if(boxes[k].mx[i] > bounds.mx[i]) bounds.mx[i] = boxes[k].mx[i];
+		}
+	}
+	nodes.resize(1);
+	nodes[0].box = bounds;
+	nodes[0].items.resize(boxes.size());
+	for(size_t k = 0; k < boxes.size(); k++) nodes[0].items[k] = (int)k;
+	OctBuilder b;
+	b.o = this;
+	b.boxes = &boxes;
+	b.max_depth = max_depth;
+	b.max_items = max_items;
+	if((int)boxes.size() > max_items) b.subdivide(0, 0);
+}
+
+void flatten_octree(const BuildOctree &oct, std::vector<DevNode> &out, std::vector<int> &slots)
+{
+	size_t base = out.size();
+	if(oct.nodes.empty()) return;
+	/* breadth-first renumbering: children of a node stay consecutive */
+	std::vector<int> order;
+	order.reserve(oct.nodes.size());
+	std::vector<int> newidx(oct.nodes.size(), -1);
+	order.push_back(0);
+	newidx[0] = 0;
+	for(size_t q = 0; q < order.size(); q++) {
+		int n = order[q];
+		int c = oct.nodes[n].child;
+		if(c >= 0) {
+			for(int k = 0; k < 8; k++) {
+				newidx[c + k] = (int)order.size();
+				order.push_back(c + k);
+			}
+		}
+	}
+	out.resize(base + order.size());
+	for(size_t q = 0; q < order.size(); q++) {
+		const BuildOctree::Node &n = oct.nodes[order[q]];
+		DevNode &d = out[base + q];
+		for(int i = 0; i < 3; i++) { d.mn[i] = (float)n.box.mn[i]; d.mx[i] = (float)n.box.mx[i]; }
+		if(n.child >= 0) {
+			d.first = (int)base + newidx[n.child];
+			d.count = -1;
+		} else {
+			d.first = (int)slots.size();
+			d.count = (int)n.items.size();
+			slots.insert(slots.end(), n.items.begin(), n.items.end());
+		}
+	}
+}
+
+/* ------------------------------------------------------------------ */
+/* projection maps                                                       */
+/* ------------------------------------------------------------------ */
+ProjMap::ProjMap()
+{
+	cells.assign(udiv * vdiv, 0);
+	cell_area.resize(udiv * vdiv);
+	total_area = 0.0;
+	for(int i = 0; i < udiv * vdiv; i++) {
+		int uc = i % udiv, vc = i / udiv;
+		double c[4][3];
+		for(int j = 0; j < 4; j++) corner_dir(uc, vc, j, c[j]);
+		Vec3 v0(c[0][0], c[0][1], c[0][2]), v1(c[1][0], c[1][1], c[1][2]);
+		Vec3 v2(c[2][0], c[2][1], c[2][2]), v3(c[3][0], c[3][1], c[3][2]);
+		Vec3 e1(v1.x - v0.x, v1.y - v0.y, v1.z - v0.z), e2(v2.x - v0.x, v2.y - v0.y, v2.z - v0.z);
+		Vec3 e3(v3.x - v0.x, v3.y - v0.y, v3.z - v0.z);
+		double area = v_len(v_cross(e1, e2)) * 0.5;
+		area += v_len(v_cross(e2, e3)) * 0.5;
+		cell_area[i] = area;
+		total_area += area;
+	}
+}
+
+void ProjMap::corner_dir(int uc, int vc, int corner, double out[3]) const
+{
+	static const int offs[4][2] = {{0, 0}, {1, 0}, {1, 1}, {0, 1}};
+	double du = 1.0 / udiv, dv = 1.0 / vdiv;
+	double u = (uc + offs[corner][0]) * du, v = (vc + offs[corner][1]) * dv;
+	double theta = u * M_PI * 2.0, phi = v * M_PI;
+	out[0] = 1.0 * cos(theta) * sin(phi);
+	out[1] = 1.0 * cos(phi);
+	out[2] = 1.0 * sin(theta) * sin(phi);
+}
+
+void ProjMap::cell_from_dir(const double d[3], int *uc, int *vc) const
+{
+	double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+	double theta = atan2(d[2], d[0]);
+	double phi = acos(d[1] / r);
+	if(theta < 0.0) theta = M_PI * 2.0 + theta;
+	double u = theta / (M_PI * 2.0), v = phi / M_PI;
+	int a = (int)(u * udiv), b = (int)(v * vdiv);
+	*uc = a < 0 ? 0 : (a >= udiv ? udiv - 1 : a);
+	*vc = b < 0 ? 0 : (b >= vdiv ? vdiv - 1 : b);
+}
+
+void ProjMap::set_cell(int uc, int vc, bool val)
+{
+	int idx = vc * udiv + uc;
+	if((bool)cells[idx] != val) {
+		double change = cell_area[idx] / total_area;
+		coverage += val ? change : -change;
+	}
+	cells[idx] = val;
+}
+
+void ProjMap::set_all(bool v) { std::fill(cells.begin(), cells.end(), v ? 1 : 0); coverage = v ? 1.0 : 0.0; }
+void ProjMap::clear() { set_all(false); }
+double ProjMap::get_coverage() const { return coverage < 0.0 ? 0.0 : (coverage > 1.0 ? 1.0 : coverage); }
+
+static void project_boxes(ProjMap *map, const Vec3 &lpos, const std::vector<Box> &boxes)
+{
+	for(size_t i = 0; i < boxes.size(); i++) {
+		const Box &b = boxes[i];
+		if(lpos.x >= b.mn[0] && lpos.y >= b.mn[1] && lpos.z >= b.mn[2] && lpos.x < b.mx[0] && lpos.y < b.mx[1] && lpos.z < b.mx[2]) {
+			map->set_all(true);
+			return;
+		}
+		Vec3 ctr((b.mn[0] + b.mx[0]) / 2.0, (b.mn[1] + b.mx[1]) / 2.0, (b.mn[2] + b.mx[2]) / 2.0);
+		Vec3 dm(b.mn[0] - ctr.x, b.mn[1] - ctr.y, b.mn[2] - ctr.z);
+		double rad_sq = dm.x * dm.x + dm.y * dm.y + dm.z * dm.z;
+		double v[3] = {ctr.x - lpos.x, ctr.y - lpos.y, ctr.z - lpos.z};
+		double objdist = sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+		int uc, vc;
+		map->cell_from_dir(v, &uc, &vc);
+		map->set_cell(uc, vc, true);
+		int num = map->udiv * map->vdiv;
+		for(int j = 0; j < num; j++) {
+			uc = j % map->udiv;
+			vc = j / map->udiv;
+			for(int k = 0; k < 4; k++) {
+				double cd[3];
+				map->corner_dir(uc, vc, k, cd);
+				double px = lpos.x + cd[0] * objdist, py = lpos.y + cd[1] * objdist, pz = lpos.z + cd[2] * objdist;
+				double dx = px - ctr.x, dy = py - ctr.y, dz = pz - ctr.z;
+				if(dx * dx + dy * dy + dz * dz <= rad_sq) {
+					map->set_cell(uc, vc, true);
+					break;
+				}
+			}
+		}
+	}
+}
+
+/* Light::build_proj_intern (src/light.cc:151-200); light samples on the
+ * projection-map stream of the light */
+void HostScene::build_projmaps(int t0, int t1, uint64_t seed)
+{
+	for(size_t li = 0; li < lights.size(); li++) {
+		Light &L = lights[li];
+		L.pm.clear();
+		L.spm.clear();
+		if(objs.empty()) continue;
+		int tm[3] = {t0, t1, -1};
+		if(t0 == t1) tm[1] = -1;
+		int samples = L.type == LT_SPHERE ? 8 : 1;
+		for(int ti = 0; ti < 2 && tm[ti] != -1; ti++) {
+			std::vector<Box> boxes(objs.size()), cboxes;
+			for(size_t i = 0; i < objs.size(); i++) {
+				const Material &m = objs[i].mat >= 0 ? mats[objs[i].mat] : defmat;
+				boxes[i] = objs[i].bounds(meshes, tm[ti]);
+				if(m.refl > 0.0 || m.refr > 0.0) cboxes.push_back(boxes[i]);
+			}
+			sray_rng s;
+			sray_rng_init(&s, seed, SRAY_DOM_PROJMAP, (uint32_t)li, (uint32_t)ti);
+			for(int k = 0; k < samples; k++) {
+				Vec3 lp = L.xf.position(tm[ti]);
+				if(L.type == LT_SPHERE) {
+					double u0 = sray_rng_uniform_d(&s), u1 = sray_rng_uniform_d(&s);
+					double z = 2.0 * u1 - 1.0, sxy = sqrt(1.0 - z * z), ang = 2.0 * M_PI * u0;
+					double r = (double)L.radius;
+					lp = Vec3(lp.x + r * cos(ang) * sxy, lp.y + r * sin(ang) * sxy, lp.z + r * z);
+				} else if(L.type == LT_BOX) {
+					double m0[4][4];
+					L.xf.matrix(0, m0);
+					Vec3 v;
+					v.x = L.dim.x * sray_rng_uniform_d(&s) - 0.5 * L.dim.x;
+					v.y = L.dim.y * sray_rng_uniform_d(&s) - 0.5 * L.dim.y;
+					v.z = L.dim.z * sray_rng_uniform_d(&s) - 0.5 * L.dim.z;
+					lp = m_pt(m0, v);
+				}
+				project_boxes(&L.pm, lp, boxes);
+				project_boxes(&L.spm, lp, cboxes);
+			}
+		}
+	}
+}
+
+/* Scene::build_tree (src/scene.cc:353-390) */
+void HostScene::build_tree(int t0, int t1, const sray_opts &opt)
+{
+	std::vector<Box> boxes(objs.size());
+	for(size_t i = 0; i < objs.size(); i++) {
+		Box s = objs[i].bounds(meshes, t0), e = t1 == t0 ? s : objs[i].bounds(meshes, t1);
+		for(int k = 0; k < 3; k++) {
+			boxes[i].mn[k] = s.mn[k] < e.mn[k] ? s.mn[k] : e.mn[k];
+			boxes[i].mx[k] = s.mx[k] > e.mx[k] ? s.mx[k] : e.mx[k];
+		}
+	}
+	oct.build(boxes, opt.scnoct_max_depth, opt.scnoct_max_items);
+	const Box &rb = oct.nodes[0].box;
+	double dx = rb.mx[0] - rb.mn[0], dy = rb.mx[1] - rb.mn[1], dz = rb.mx[2] - rb.mn[2];
+	gather_dist = sqrt(dx * dx + dy * dy + dz * dz) * opt.gather_dist;
+}
+
+/* ------------------------------------------------------------------ */
+/* loading                                                               */
+/* ------------------------------------------------------------------ */
+static uint64_t fnv(const void *p, size_t n, uint64_t h)
+{
+	const unsigned char *c = (const unsigned char *)p;
+	for(size_t i = 0; i < n; i++) { h ^= c[i]; h *= 0x100000001b3ull; }
+	return h;
+}
+
+namespace {
+struct Loader {
+	const Doc &d;
+	HostScene &sc;
+	const sray_opts &opt;
+	std::string &err;
+
+	void load_xform(int n, XForm &xf)
+	{
+		Typed t;
+		int msec = 0;
+		if(Doc::typed(d.attr(n, "interpolate"), &t)) {
+			int v = t.str == "linear" ? INTERP_LINEAR : t.str == "step" ? INTERP_STEP : t.str == "cubic" ? INTERP_CUBIC : -1;
+			if(v >= 0) xf.pos.interp = xf.rot.interp = xf.scale.interp = v;
+		}
+		if(Doc::typed(d.attr(n, "extrapolate"), &t)) {
+			int v = t.str == "clamp" ? EXTRAP_CLAMP : t.str == "repeat" ? EXTRAP_REPEAT : t.str == "pingpong" ? EXTRAP_PINGPONG : -1;
+			if(v >= 0) xf.pos.extrap = xf.rot.extrap = xf.scale.extrap = v;
+		}
+		if(Doc::typed(d.attr(n, "time"), &t) && t.type == T_INT) msec = t.ival;
+		if(Doc::typed(d.attr(n, "pos"), &t) && t.type == T_VEC) set_key(xf.pos, msec, Vec3(t.vval[0], t.vval[1], t.vval[2]));
+		if(Doc::typed(d.attr(n, "rot"), &t) && t.type == T_VEC) {
+			Quat q = {t.vval[0], t.vval[1], t.vval[2], t.vval[3]};
+			double l = sqrt(q.s * q.s + q.x * q.x + q.y * q.y + q.z * q.z);
+			if(l > 0.0) { q.s /= l; q.x /= l; q.y /= l; q.z /= l; }
+			set_key(xf.rot, msec, q);
+		}
+		if(Doc::typed(d.attr(n, "axisrot"), &t) && t.type == T_VEC) {
+			double ang = t.vval[0] * (M_PI / 180.0), half = ang * 0.5, sn = sin(half);
+			Quat q = {cos(half), t.vval[1] * sn, t.vval[2] * sn, t.vval[3] * sn};
+			set_key(xf.rot, msec, q);
+		}
+		if(Doc::typed(d.attr(n, "scale"), &t) && t.type == T_VEC) set_key(xf.scale, msec, Vec3(t.vval[0], t.vval[1], t.vval[2]));
+		if(Doc::typed(d.attr(n, "pivot"), &t) && t.type == T_VEC) xf.pivot = Vec3(t.vval[0], t.vval[1], t.vval[2]);
+	}
+
+	bool load_material(int n)
+	{
+		Material m;
+		Typed t;
+		if(!Doc::typed(d.attr(n, "name"), &t)) { err = "invalid material: name attribute not found"; return false; }
+		m.name = t.str;
+		if(Doc::typed(d.attr(n, "shader"), &t)) m.phong = t.str == "phong";
+		for(int c = d.nodes[n].first_child; c >= 0; c = d.nodes[c].next) {
+			if(!d.is(c, "mattr")) continue;
+			Typed an, av;
+			if(!Doc::typed(d.attr(c, "name"), &an) || !Doc::typed(d.attr(c, "value"), &av)) continue;
+			double col[4];
+			if(av.type == T_VEC) { col[0] = av.vval[0]; col[1] = av.vval[1]; col[2] = av.vval[2]; col[3] = 1.0; }
+			else if(av.type == T_FLT || av.type == T_INT) { col[0] = col[1] = col[2] = av.fval; col[3] = 1.0; }
+			else continue;
+			if(an.str == "diffuse") memcpy(m.kd, col, sizeof col);
+			else if(an.str == "specular") memcpy(m.ks, col, sizeof col);
+			else if(an.str == "shininess") m.shin = col[0];
+			else if(an.str == "reflect") m.refl = col[0];
+			else if(an.str == "refract") m.refr = col[0];
+			else if(an.str == "ior") m.ior = col[0];
+		}
+		sc.mats.push_back(m);
+		return true;
+	}
+
+	bool read_vec(int n, double v[3])
+	{
+		const XAttr *a = d.attr(n, "val");
+		if(!a) return false;
+		/* numeric vector: at least two numbers (src/xmltree.c:75-93) */
+		const char *p = a->val, *e = a->val + a->vlen;
+		if(!(isdigit((unsigned char)p[0]) || ((p[0] == '+' || p[0] == '-') && isdigit((unsigned char)p[1])))) return false;
+		double vv[4] = {1, 1, 1, 1};
+		int i;
+		char buf[128];
+		int len = a->vlen < 127 ? a->vlen : 127;
+		memcpy(buf, p, len);
+		buf[len] = 0;
+		const char *q = buf;
+		for(i = 0; i < 4; i++) {
+			if(!*q) break;
+			vv[i] = strtod(q, 0);
+			while(*q && !isspace((unsigned char)*q)) q++;
+			while(*q && isspace((unsigned char)*q)) q++;
+		}
+		(void)e;
+		if(i < 2) return false;
+		v[0] = vv[0]; v[1] = vv[1]; v[2] = vv[2];
+		return true;
+	}
+
+	/* Mesh::load_xml (src/meshload.cc:55-157) */
+	bool load_mesh(int objn, Object &o)
+	{
+		int mn = -1;
+		for(int c = d.nodes[objn].first_child; c >= 0; c = d.nodes[c].next) if(d.is(c, "mesh")) { mn = c; break; }
+		if(mn < 0) { err = "<mesh> not found in mesh object " + o.name; return false; }
+		static const char *ename[4] = {"vertex", "normal", "texcoord", "tangent"};
+		struct Elem { double v[3]; int id; };
+		std::vector<Elem> el[4];
+		bool ordered[4] = {true, true, true, true};
+		int cur[4] = {0, 0, 0, 0};
+		std::vector<int> fr;   /* 12 ints per face: vertex, normal, tangent, texcoord x3 */
+		for(int c = d.nodes[mn].first_child; c >= 0; c = d.nodes[c].next) {
+			int e = -1;
+			for(int k = 0; k < 4; k++) if(d.is(c, ename[k])) { e = k; break; }
+			if(e >= 0) {
+				Elem x;
+				if(!Doc::int_attr(d.attr(c, "id"), &x.id)) x.id = cur[e];
+				x.v[0] = x.v[1] = x.v[2] = 0.0;
+				read_vec(c, x.v);
+				if(x.id != cur[e]++) ordered[e] = false;
+				el[e].push_back(x);
+			} else if(d.is(c, "face")) {
+				int f[12] = {0};
+				int k = 0;
+				for(int vr = d.nodes[c].first_child; vr >= 0 && k < 3; vr = d.nodes[vr].next) {
+					if(!d.is(vr, "vref")) continue;
+					int v;
+					f[k * 4 + 0] = Doc::int_attr(d.attr(vr, "vertex"), &v) ? v : 0;
+					f[k * 4 + 1] = Doc::int_attr(d.attr(vr, "normal"), &v) ? v : 0;
+					f[k * 4 + 2] = Doc::int_attr(d.attr(vr, "tangent"), &v) ? v : 0;
+					f[k * 4 + 3] = Doc::int_attr(d.attr(vr, "texcoord"), &v) ? v : 0;
+					k++;
+				}
+				fr.insert(fr.end(), f, f + 12);
+			}
+		}
+		for(int e = 0; e < 4; e++) {
+			if(!ordered[e]) std::stable_sort(el[e].begin(), el[e].end(), [](const Elem &a, const Elem &b) { return a.id < b.id; });
+			if(!el[e].empty() && el[e].back().id != (int)el[e].size() - 1) {
+				err = "error loading mesh " + o.name + ": missing vertex elements";
+				return false;
+			}
+		}
+		size_t nf = fr.size() / 12;
+		Mesh m;
+		m.pos.resize(nf * 9);
+		m.posd.resize(nf * 9);
+		m.attr.assign(nf * 24, 0.0f);
+		for(size_t i = 0; i < nf; i++) {
+			for(int j = 0; j < 3; j++) {
+				int vi = fr[i * 12 + j * 4], ni = fr[i * 12 + j * 4 + 1], gi = fr[i * 12 + j * 4 + 2], ti = fr[i * 12 + j * 4 + 3];
+				if(vi < 0 || vi >= (int)el[0].size()) { err = "face vertex index out of range in " + o.name; return false; }
+				for(int k = 0; k < 3; k++) {
+					m.posd[i * 9 + j * 3 + k] = el[0][vi].v[k];
+					m.pos[i * 9 + j * 3 + k] = (float)el[0][vi].v[k];
+				}
+				if(!el[1].empty()) {
+					if(ni < 0 || ni >= (int)el[1].size()) { err = "normal index out of range in " + o.name; return false; }
+					for(int k = 0; k < 3; k++) m.attr[i * 24 + j * 3 + k] = (float)el[1][ni].v[k];
+				}
+				if(!el[3].empty()) {
+					if(gi < 0 || gi >= (int)el[3].size()) { err = "tangent index out of range in " + o.name; return false; }
+					for(int k = 0; k < 3; k++) m.attr[i * 24 + 9 + j * 3 + k] = (float)el[3][gi].v[k];
+				}
+				if(!el[2].empty()) {
+					if(ti < 0 || ti >= (int)el[2].size()) { err = "texcoord index out of range in " + o.name; return false; }
+					m.attr[i * 24 + 18 + j * 2] = (float)el[2][ti].v[0];
+					m.attr[i * 24 + 18 + j * 2 + 1] = (float)el[2][ti].v[1];
+				}
+			}
+		}
+		/* identical meshes share one device copy */
+		uint64_t h = fnv(m.posd.data(), m.posd.size() * sizeof(double), 0xcbf29ce484222325ull);
+		h = fnv(m.attr.data(), m.attr.size() * sizeof(float), h);
+		for(size_t u = 0; u < sc.meshes.size(); u++) {
+			if(sc.meshes[u].hash == h && sc.meshes[u].posd == m.posd && sc.meshes[u].attr == m.attr) {
+				o.mesh = (int)u;
+				sc.n_tris += (int64_t)nf;
+				return true;
+			}
+		}
+		m.hash = h;
+		o.mesh = (int)sc.meshes.size();
+		sc.meshes.push_back(std::move(m));
+		sc.n_tris += (int64_t)nf;
+		return true;
+	}
+
+	bool load_object(int n)
+	{
+		Typed t;
+		if(!Doc::typed(d.attr(n, "type"), &t)) { err = "invalid object: no type attribute."; return false; }
+		Object o;
+		if(t.str == "sphere") o.type = OBJ_SPHERE;
+		else if(t.str == "cylinder") o.type = OBJ_CYLINDER;
+		else if(t.str == "mesh") o.type = OBJ_MESH;
+		else { err = "invalid object: unknown type: " + t.str; return false; }
+		if(Doc::typed(d.attr(n, "name"), &t)) o.name = t.str;
+		bool have_shape = false;
+		for(int c = d.nodes[n].first_child; c >= 0; c = d.nodes[c].next) {
+			if(d.is(c, "matref")) {
+				if(!Doc::typed(d.attr(c, "name"), &t)) { err = "invalid material reference in object " + o.name; return false; }
+				int found = -1;
+				for(size_t m = 0; m < sc.mats.size(); m++) if(sc.mats[m].name == t.str) { found = (int)m; break; }
+				if(found < 0) { err = "material " + t.str + " referenced by object " + o.name + " does not exist"; return false; }
+				o.mat = found;
+			} else if(d.is(c, "xform")) {
+				load_xform(c, o.xf);
+			} else if(o.type == OBJ_SPHERE && d.is(c, "sphere")) {
+				if(Doc::typed(d.attr(c, "rad"), &t)) o.rad = t.fval;
+				have_shape = true;
+			} else if(o.type == OBJ_CYLINDER && d.is(c, "cylinder")) {
+				if(Doc::typed(d.attr(c, "rad"), &t)) o.rad = t.fval;
+				if(Doc::typed(d.attr(c, "start"), &t)) o.start = t.fval;
+				if(Doc::typed(d.attr(c, "end"), &t)) o.end = t.fval;
+				have_shape = true;
+			}
+		}
+		if(o.type == OBJ_MESH) {
+			if(!load_mesh(n, o)) return false;
+		} else if(!have_shape) {
+			err = std::string(o.type == OBJ_SPHERE ? "sphere" : "cylinder") + " object " + o.name + " has no shape element";
+			return false;
+		}
+		sc.objs.push_back(o);
+		return true;
+	}
+
+	bool load_light(int n)
+	{
+		Typed t;
+		if(!Doc::typed(d.attr(n, "type"), &t)) { err = "invalid light: no type attribute."; return false; }
+		Light l;
+		if(t.str == "point") l.type = LT_POINT;
+		else if(t.str == "sphere") l.type = LT_SPHERE;
+		else if(t.str == "box") l.type = LT_BOX;
+		else { err = "invalid light: unknown type: " + t.str; return false; }
+		if(Doc::typed(d.attr(n, "color"), &t)) {
+			if(t.type == T_VEC) { l.col[0] = t.vval[0]; l.col[1] = t.vval[1]; l.col[2] = t.vval[2]; l.col[3] = 1.0; }
+			else if(t.type == T_INT || t.type == T_FLT) { l.col[0] = l.col[1] = l.col[2] = t.fval; l.col[3] = 1.0; }
+		}
+		for(int c = d.nodes[n].first_child; c >= 0; c = d.nodes[c].next) {
+			if(d.is(c, "xform")) load_xform(c, l.xf);
+			else if(l.type == LT_SPHERE && d.is(c, "sphere")) {
+				if(!Doc::typed(d.attr(c, "rad"), &t)) { err = "sphere light without rad"; return false; }
+				l.radius = (float)t.fval;
+			} else if(l.type == LT_BOX && d.is(c, "aabox")) {
+				Typed a, b;
+				if(!Doc::typed(d.attr(c, "min"), &a) || a.type != T_VEC || !Doc::typed(d.attr(c, "max"), &b) || b.type != T_VEC) {
+					err = "invalid aabox in box light";
+					return false;
+				}
+				l.dim = Vec3(b.vval[0] - a.vval[0], b.vval[1] - a.vval[1], b.vval[2] - a.vval[2]);
+			}
+		}
+		sc.lights.push_back(l);
+		return true;
+	}
+
+	bool load_camera(int n, bool &have)
+	{
+		Typed t;
+		if(!Doc::typed(d.attr(n, "type"), &t)) { err = "invalid camera: no type attribute."; return false; }
+		Camera c;
+		c.aspect = (double)opt.width / (double)opt.height;
+		c.shutter = opt.shutter;
+		if(t.str == "free") c.target = 0;
+		else if(t.str == "target") {
+			c.target = 1;
+			set_key(c.xf.pos, 0, Vec3(0, 5, 10));
+			set_key(c.txf.pos, 0, Vec3(0, 0, 0));
+			set_key(c.txf.scale, 0, Vec3(0, 0, 0));
+		} else { err = "invalid camera: unknown type: " + t.str; return false; }
+		if(Doc::typed(d.attr(n, "shutter"), &t)) c.shutter = (int)t.fval;
+		if(Doc::typed(d.attr(n, "fov"), &t) && (t.type == T_FLT || t.type == T_INT)) c.vfov = t.fval * (M_PI / 180.0);
+		int target = -1;
+		for(int ch = d.nodes[n].first_child; ch >= 0; ch = d.nodes[ch].next) {
+			if(d.is(ch, "xform")) load_xform(ch, c.xf);
+			else if(d.is(ch, "target") && target < 0) target = ch;
+		}
+		if(c.target) {
+			if(target < 0) { err = "failed to load target camera, no <target> child"; return false; }
+			for(int ch = d.nodes[target].first_child; ch >= 0; ch = d.nodes[ch].next) if(d.is(ch, "xform")) load_xform(ch, c.txf);
+		}
+		if(!have) {
+			sc.cam = c;
+			have = true;
+		}
+		return true;
+	}
+
+	bool run()
+	{
+		int root = 0;
+		for(int n = d.nodes[root].first_child; n >= 0; n = d.nodes[n].next) {
+			if(d.is(n, "material") && !load_material(n)) return false;
+		}
+		bool have_cam = false;
+		for(int n = d.nodes[root].first_child; n >= 0; n = d.nodes[n].next) {
+			Typed t;
+			if(d.is(n, "env")) {
+				if(Doc::typed(d.attr(n, "ambient"), &t)) {
+					if(t.type == T_VEC) { sc.env_amb[0] = t.vval[0]; sc.env_amb[1] = t.vval[1]; sc.env_amb[2] = t.vval[2]; sc.env_amb[3] = 1.0; }
+					else if(t.type == T_INT || t.type == T_FLT) { sc.env_amb[0] = sc.env_amb[1] = sc.env_amb[2] = t.fval; sc.env_amb[3] = 1.0; }
+				}
+				if(Doc::typed(d.attr(n, "bgcolor"), &t) && t.type == T_VEC) {
+					sc.env_col[0] = t.vval[0]; sc.env_col[1] = t.vval[1]; sc.env_col[2] = t.vval[2]; sc.env_col[3] = 1.0;
+				}
+				if(Doc::typed(d.attr(n, "ior"), &t) && t.type == T_FLT) sc.env_ior = t.fval;
+			} else if(d.is(n, "object")) {
+				if(!load_object(n)) return false;
+			} else if(d.is(n, "light")) {
+				if(!load_light(n)) return false;
+			} else if(d.is(n, "camera")) {
+				if(!load_camera(n, have_cam)) return false;
+			}
+		}
+		if(!have_cam) {
+			sc.cam = Camera();
+			sc.cam.aspect = (double)opt.width / (double)opt.height;
+			sc.cam.shutter = opt.shutter;
+		}
+		return true;
+	}
+};
+}  // namespace
+
+bool HostScene::load(const char *text, size_t len, const sray_opts &opt, std::string &err)
+{
+	Doc d;
+	if(!d.parse(text, len)) { err = "xml: " + d.err; return false; }
+	*this = HostScene();
+	Loader ld = {d, *this, opt, err};
+	if(!ld.run()) return false;
+	/* mesh octrees in object space (Mesh::build_tree, src/mesh.cc:210-226),
+	 * one per unique mesh, built on all host cores */
+	std::vector<std::thread> th;
+	size_t nm = meshes.size();
+	unsigned nth = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), (unsigned)nm));
+	for(unsigned w = 0; w < nth; w++) {
+		th.push_back(std::thread([this, &opt, w, nth, nm]() {
+			for(size_t u = w; u < nm; u += nth) {
+				Mesh &m = meshes[u];
+				size_t nf = m.posd.size() / 9;
+				std::vector<Box> boxes(nf);
+				for(size_t i = 0; i < nf; i++) {
+					Box &b = boxes[i];
+					for(int k = 0; k < 3; k++) { b.mn[k] = FLT_MAX; b.mx[k] = -FLT_MAX; }
+					for(int v = 0; v < 3; v++) {
+						for(int k = 0; k < 3; k++) {
+							double c = m.posd[i * 9 + v * 3 + k];
+							if(c < b.mn[k]) b.mn[k] = c;
+							if(c > b.mx[k]) b.mx[k] = c;
+						}
+					}
+				}
+				m.oct.build(boxes, opt.meshoct_max_depth, opt.meshoct_max_items);
+			}
+		}));
+	}
+	for(auto &t : th) t.join();
+	return true;
+}
+
+}  // namespace sray

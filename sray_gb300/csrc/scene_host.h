@@ -1,0 +1,149 @@
+/* scene_host.h -- host side of the GB300 renderer: the S-ray scene database
+ * (XML loader, transforms, materials, objects, lights, camera), the octree
+ * builds and their flattening into the device layouts.
+ *
+ * Everything here runs once per scene load (meshes) or once per frame
+ * (top-level octree, per-time matrices, projection maps) in double
+ * precision, exactly as the reference computes it, and is rounded to float
+ * only when written into the device tables.
+ */
+#ifndef SRAY_SCENE_HOST_H_
+#define SRAY_SCENE_HOST_H_
+
+#include <stdint.h>
+#include <string>
+#include <vector>
+#include "sray_gpu.h"
+#include "sray_device.h"
+
+namespace sray {
+
+enum { INTERP_STEP, INTERP_LINEAR, INTERP_CUBIC };
+enum { EXTRAP_CLAMP, EXTRAP_REPEAT, EXTRAP_PINGPONG };
+
+struct Vec3 {
+	double x, y, z;
+	Vec3() : x(0), y(0), z(0) {}
+	Vec3(double a, double b, double c) : x(a), y(b), z(c) {}
+	double operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+
+struct Quat { double s, x, y, z; };
+
+template <class T> struct Track {
+	T def;
+	std::vector<int> time;
+	std::vector<T> val;
+	int interp = INTERP_LINEAR, extrap = EXTRAP_CLAMP;
+};
+
+struct XForm {
+	Track<Vec3> pos, scale;
+	Track<Quat> rot;
+	Vec3 pivot;
+	XForm();
+	Vec3 position(int t) const;
+	Vec3 scaling(int t) const;
+	void matrix(int t, double m[4][4]) const;
+};
+
+struct Material {
+	std::string name;
+	int phong = 0;
+	double kd[4] = {1, 1, 1, 0}, ks[4] = {0, 0, 0, 0};
+	double shin = 1.0, refl = 0.0, refr = 0.0, ior = 1.5;
+};
+
+enum { OBJ_SPHERE = 0, OBJ_CYLINDER = 1, OBJ_MESH = 2 };
+enum { LT_POINT = 0, LT_SPHERE = 1, LT_BOX = 2 };
+
+struct Box { double mn[3], mx[3]; };
+
+/* an octree in build form: children of a node are 8 consecutive entries */
+struct BuildOctree {
+	struct Node { Box box; std::vector<int> items; int child = -1; };
+	std::vector<Node> nodes;
+	void build(const std::vector<Box> &item_boxes, int max_depth, int max_items);
+};
+
+/* one unique triangle mesh (identical meshes of several objects share it) */
+struct Mesh {
+	std::vector<float> pos;    /* 9 floats per face: the three vertices (object space) */
+	std::vector<double> posd;  /* same, as parsed */
+	std::vector<float> attr;   /* 24 floats per face: normals 9, tangents 9, texcoords 6 */
+	uint64_t hash = 0;
+	BuildOctree oct;
+	int node_base = 0;         /* first node in the device mesh-node array */
+	int tri_base = 0;          /* first face in the device attribute table */
+};
+
+struct Object {
+	int type = OBJ_SPHERE;
+	std::string name;
+	int mat = -1;
+	XForm xf;
+	double rad = 1.0, start = -1.0, end = 1.0;
+	int mesh = -1;
+	Box bounds(const std::vector<Mesh> &meshes, int t) const;
+};
+
+struct ProjMap {
+	int udiv = 64, vdiv = 32;
+	std::vector<char> cells;
+	std::vector<double> cell_area;
+	double total_area = 0.0, coverage = 0.0;
+	ProjMap();
+	void corner_dir(int uc, int vc, int corner, double out[3]) const;
+	void cell_from_dir(const double d[3], int *uc, int *vc) const;
+	void set_cell(int uc, int vc, bool v);
+	void set_all(bool v);
+	void clear();
+	double get_coverage() const;
+};
+
+struct Light {
+	int type = LT_POINT;
+	double col[4] = {1, 1, 1, 1};
+	XForm xf;
+	float radius = 1.0f;
+	Vec3 dim = Vec3(1, 1, 1);
+	ProjMap pm, spm;
+};
+
+struct Camera {
+	int target = 0;
+	XForm xf, txf;
+	double vfov = 0.78539816339744830962, aspect = 1.0, max_dist = SRAY_RAY_MAGNITUDE;
+	int shutter = 0;
+	void matrix(int t, double m[4][4]) const;
+};
+
+struct HostScene {
+	std::vector<Material> mats;
+	Material defmat;
+	std::vector<Object> objs;
+	std::vector<Light> lights;
+	std::vector<Mesh> meshes;
+	Camera cam;
+	double env_ior = 1.0, env_col[4] = {0, 0, 0, 0}, env_amb[4] = {0, 0, 0, 0};
+	int64_t n_tris = 0;
+
+	/* per-frame state */
+	BuildOctree oct;
+	double gather_dist = 0.0;
+
+	bool load(const char *text, size_t len, const sray_opts &opt, std::string &err);
+	void build_tree(int t0, int t1, const sray_opts &opt);
+	void build_projmaps(int t0, int t1, uint64_t seed);
+};
+
+/* general 4x4 inverse by the adjugate */
+void mat_inverse(double out[4][4], const double m[4][4]);
+
+/* Flatten an octree breadth first into device nodes; leaf items are
+ * appended to `slots` (their indices into the item array). */
+void flatten_octree(const BuildOctree &oct, std::vector<DevNode> &nodes, std::vector<int> &slots);
+
+}  // namespace sray
+
+#endif

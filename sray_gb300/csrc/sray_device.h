@@ -1,0 +1,77 @@
+/* sray_device.h -- device-resident scene layout shared by the host builder
+ * and the CUDA kernels (plain structs, no CUDA types).
+ *
+ * HBM layout (all arrays 16-byte aligned):
+ *   mesh_nodes   DevNode[ ]  octree nodes of every unique mesh, breadth first,
+ *                            the 8 children of a node consecutive (32 B each)
+ *   mesh_tris    DevTri[ ]   one 48 B record per leaf slot: the triangle's three
+ *                            object-space vertices and its unnormalised normal
+ *                            cross(v1-v0, v2-v0), duplicated into every leaf
+ *                            the triangle overlaps, so a leaf is one
+ *                            contiguous, 16 B-vector-loadable run
+ *   mesh_prim    int[ ]      triangle index of each slot (read on a hit only)
+ *   tri_pos/attr float[ ]    per unique-mesh triangle: vertices (9 floats) and
+ *                            normals/tangents/texcoords (24 floats), read once
+ *                            per shaded hit for the attribute interpolation
+ *   scene_nodes/scene_slots  top-level octree over objects (rebuilt per frame)
+ *   objs         DevObj[ ]   type, material, mesh root, xform table index
+ *   xf           float[ ]    per object per integer time: forward 3x4,
+ *                            inverse 3x4, inverse-transpose 3x3 (36 floats)
+ */
+#ifndef SRAY_DEVICE_H_
+#define SRAY_DEVICE_H_
+
+#include <stdint.h>
+
+namespace sray {
+
+struct alignas(16) DevNode {
+	float mn[3];
+	int first;      /* inner: index of child 0; leaf: first slot */
+	float mx[3];
+	int count;      /* inner: -1; leaf: number of slots */
+};
+
+struct alignas(16) DevTri {
+	float a[4];     /* v0.xyz, n.x */
+	float b[4];     /* v1.xyz, n.y */
+	float c[4];     /* v2.xyz, n.z */
+};
+
+struct alignas(16) DevObj {
+	int type;       /* 0 sphere, 1 cylinder, 2 mesh */
+	int mat;        /* material index, -1 = default material */
+	int mesh_root;  /* mesh: root node in mesh_nodes, -1 if the mesh is empty */
+	int tri_base;   /* mesh: first triangle of its unique mesh in tri_pos/tri_attr */
+	float rad, start, end;
+	int pad;
+};
+
+struct alignas(16) DevMat {
+	float kd[4], ks[4];
+	float shin, refl, refr, ior;
+	int phong;
+	int pad[3];
+};
+
+struct alignas(16) DevLight {
+	int type;       /* 0 point, 1 sphere, 2 box */
+	float radius;
+	float pad0[2];
+	float col[4];
+	float dim[4];
+	float box_m[12];   /* transform at time 0 (BoxLight::get_point) */
+};
+
+enum { XF_STRIDE = 36 };
+
+/* photon record: 48 B */
+struct alignas(16) DevPhoton {
+	float p[4];     /* pos.xyz, power.r */
+	float d[4];     /* dir.xyz, power.g */
+	float n[4];     /* norm.xyz, power.b */
+};
+
+}  // namespace sray
+
+#endif

@@ -1,0 +1,176 @@
+"""ctypes binding of libsray_gpu.so (include/sray_gpu.h).
+
+There is no CPU fallback: if the native library is missing or no CUDA
+device is present, every call raises.  Device buffers can be torch CUDA
+tensors (passed by data_ptr) or raw device pointers.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .options import SrayOpts, make_opts
+
+_LIB = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libsray_gpu.so")
+_lib = None
+
+EXPORTS = ["sray_default_opts", "sray_gpu_init", "sray_gpu_set_opts", "sray_gpu_load_scene", "sray_gpu_load_scene_mem",
+           "sray_gpu_scene_info", "sray_gpu_build", "sray_gpu_shoot_photons", "sray_gpu_render",
+           "sray_gpu_render_pixels", "sray_gpu_cast_rays", "sray_gpu_primary_hits", "sray_gpu_get_photons",
+           "sray_gpu_get_stats", "sray_gpu_last_error", "sray_gpu_shutdown"]
+
+
+class SrayStats(ctypes.Structure):
+    _fields_ = [("primary_rays", ctypes.c_int64), ("shadow_rays", ctypes.c_int64),
+                ("secondary_rays", ctypes.c_int64), ("gather_rays", ctypes.c_int64),
+                ("photons_emitted", ctypes.c_int64), ("photons_stored", ctypes.c_int64),
+                ("gathers", ctypes.c_int64), ("samples", ctypes.c_int64),
+                ("node_visits", ctypes.c_int64), ("prim_tests", ctypes.c_int64),
+                ("kernel_launches", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
+
+
+class SrayError(RuntimeError):
+    pass
+
+
+def lib_path():
+    return _LIB
+
+
+def load_library():
+    """Load the native library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB):
+        raise SrayError("libsray_gpu.so not built: run sray_gb300.build.build() (%s)" % _LIB)
+    L = ctypes.CDLL(_LIB)
+    vp, ip, lp = ctypes.c_void_p, ctypes.c_int, ctypes.c_long
+    L.sray_default_opts.argtypes = [ctypes.POINTER(SrayOpts)]
+    L.sray_gpu_init.argtypes = [ctypes.POINTER(SrayOpts)]
+    L.sray_gpu_set_opts.argtypes = [ctypes.POINTER(SrayOpts)]
+    L.sray_gpu_load_scene.argtypes = [ctypes.c_char_p]
+    L.sray_gpu_load_scene_mem.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    L.sray_gpu_scene_info.argtypes = [vp, vp, vp, vp, vp]
+    L.sray_gpu_build.argtypes = [lp, lp]
+    L.sray_gpu_shoot_photons.argtypes = [lp, lp, vp, vp, vp]
+    L.sray_gpu_render.argtypes = [lp, vp, ip, vp]
+    L.sray_gpu_render_pixels.argtypes = [lp, vp, ip, vp]
+    L.sray_gpu_cast_rays.argtypes = [ip, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.sray_gpu_primary_hits.argtypes = [lp, vp, vp, vp, vp, vp]
+    L.sray_gpu_get_photons.argtypes = [ip, vp, ip, vp]
+    L.sray_gpu_get_stats.argtypes = [ctypes.POINTER(SrayStats)]
+    L.sray_gpu_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    L.sray_gpu_shutdown.argtypes = []
+    L.sray_gpu_shutdown.restype = None
+    _lib = L
+    return L
+
+
+def _ptr(x):
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return ctypes.c_void_p(x)
+    if hasattr(x, "data_ptr"):
+        return ctypes.c_void_p(x.data_ptr())
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data_as(ctypes.c_void_p)
+    raise TypeError("unsupported buffer %r" % type(x))
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    if hasattr(stream, "cuda_stream"):
+        return ctypes.c_void_p(stream.cuda_stream)
+    return ctypes.c_void_p(int(stream))
+
+
+class GpuRenderer:
+    """The GPU renderer context (one per process)."""
+
+    def __init__(self, opts=None, **kw):
+        self.L = load_library()
+        self.opts = opts if isinstance(opts, SrayOpts) else make_opts(**(opts or {}), **kw)
+        self._chk(self.L.sray_gpu_init(ctypes.byref(self.opts)))
+
+    def _chk(self, r):
+        if r != 0:
+            buf = ctypes.create_string_buffer(1024)
+            self.L.sray_gpu_last_error(buf, 1024)
+            raise SrayError("%s (code %d)" % (buf.value.decode(errors="replace"), r))
+        return r
+
+    def set_opts(self, **kw):
+        for k, v in kw.items():
+            setattr(self.opts, k, v)
+        self._chk(self.L.sray_gpu_set_opts(ctypes.byref(self.opts)))
+
+    def load(self, path):
+        self._chk(self.L.sray_gpu_load_scene(path.encode()))
+
+    def load_xml(self, xml):
+        b = xml.encode() if isinstance(xml, str) else xml
+        self._chk(self.L.sray_gpu_load_scene_mem(b, len(b)))
+
+    def scene_info(self):
+        a, b, c, e = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        d = ctypes.c_int64()
+        self._chk(self.L.sray_gpu_scene_info(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(d),
+                                             ctypes.byref(e)))
+        return dict(objects=a.value, lights=b.value, materials=c.value, triangles=d.value, unique_meshes=e.value)
+
+    def build(self, t0=0, t1=0):
+        self._chk(self.L.sray_gpu_build(t0, t1))
+
+    def shoot_photons(self, t0=0, t1=0, stream=None):
+        c, g = ctypes.c_int(), ctypes.c_int()
+        self._chk(self.L.sray_gpu_shoot_photons(t0, t1, ctypes.byref(c), ctypes.byref(g), _stream(stream)))
+        return c.value, g.value
+
+    def render(self, msec=0, fb=None, stream=None):
+        """Full frame (accel build + photons + pixels).  fb: None -> returns a
+        host numpy [h, w, 4]; a CUDA tensor / device pointer -> written in place."""
+        if fb is None:
+            out = np.zeros((self.opts.height, self.opts.width, 4), np.float32)
+            self._chk(self.L.sray_gpu_render(msec, _ptr(out), 0, _stream(stream)))
+            return out
+        if isinstance(fb, np.ndarray):
+            self._chk(self.L.sray_gpu_render(msec, _ptr(fb), 0, _stream(stream)))
+            return fb
+        self._chk(self.L.sray_gpu_render(msec, _ptr(fb), 1, _stream(stream)))
+        return fb
+
+    def render_pixels(self, msec=0, fb=None, stream=None):
+        if fb is None:
+            out = np.zeros((self.opts.height, self.opts.width, 4), np.float32)
+            self._chk(self.L.sray_gpu_render_pixels(msec, _ptr(out), 0, _stream(stream)))
+            return out
+        dev = 0 if isinstance(fb, np.ndarray) else 1
+        self._chk(self.L.sray_gpu_render_pixels(msec, _ptr(fb), dev, _stream(stream)))
+        return fb
+
+    def primary_hits(self, obj, prim, t, tie, msec=0, stream=None):
+        """Device buffers of width*height entries (int32, int32, float32, uint8)."""
+        self._chk(self.L.sray_gpu_primary_hits(msec, _ptr(obj), _ptr(prim), _ptr(t), _ptr(tie), _stream(stream)))
+
+    def cast_rays(self, orig, dirs, times, obj, prim, t, tie, stream=None):
+        n = int(orig.shape[0])
+        self._chk(self.L.sray_gpu_cast_rays(n, _ptr(orig), _ptr(dirs), _ptr(times), _ptr(obj), _ptr(prim), _ptr(t),
+                                            _ptr(tie), _stream(stream)))
+
+    def photons(self, which):
+        n = ctypes.c_int()
+        self._chk(self.L.sray_gpu_get_photons(which, None, 0, ctypes.byref(n)))
+        out = np.zeros((max(n.value, 1), 16), np.float32)
+        self._chk(self.L.sray_gpu_get_photons(which, _ptr(out), n.value, ctypes.byref(n)))
+        return out[:n.value]
+
+    def stats(self):
+        st = SrayStats()
+        self._chk(self.L.sray_gpu_get_stats(ctypes.byref(st)))
+        return {f[0]: getattr(st, f[0]) for f in SrayStats._fields_ if f[0] != "reserved"}
+
+    def close(self):
+        self.L.sray_gpu_shutdown()

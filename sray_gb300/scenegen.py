@@ -1,0 +1,294 @@
+"""Seeded synthetic S-ray scenes in the reference's XML format.
+
+The reference ships no scenes and no benchmark data, so the benchmark scenes
+are generated: the small scene (512x512, ground plane, 16 spheres, one
+subdivision-4 icosphere, a cylinder, one point light, 100k caustic photons)
+and the production scene (1920x1080, 1,000,000-triangle displaced-grid
+terrain, 200 instanced subdivision-3 icospheres, 3 sphere lights, 2M global
+and 500k caustic photons).  Everything is drawn from a numpy Generator
+seeded from the scene seed, vertex data is float32 written with nine
+significant digits (so parsing it back and rounding to float32 is exact).
+
+The XML follows the reference's loader: <material> with <mattr>,
+<env>, <object type="sphere|cylinder|mesh"> with <matref>/<xform>/<sphere>/
+<cylinder>/<mesh>, <light type="point|sphere">, <camera type="target">
+(src/scene.cc:93-183, src/meshload.cc:55-157, src/anim.cc:68-121).
+Numbers always start with a digit or a sign, as the attribute typing of
+src/xmltree.c:75-93 requires.
+"""
+import hashlib
+import os
+
+import numpy as np
+
+__all__ = ["icosphere", "value_noise_height", "small_scene", "production_scene",
+           "scene_opts", "write_scene", "CONFIGS"]
+
+
+def _f(x):
+    return "%.9g" % float(np.float32(x))
+
+
+def _vec(v):
+    return " ".join(_f(c) for c in v)
+
+
+def icosphere(subdiv):
+    """Unit icosphere: (vertices float32 [n,3], faces int32 [m,3])."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t),
+         (0, -1, -t), (0, 1, -t), (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4),
+         (11, 10, 2), (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8),
+         (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    verts = [np.array(p, dtype=np.float64) / np.linalg.norm(p) for p in v]
+    faces = list(f)
+    for _ in range(subdiv):
+        cache = {}
+
+        def mid(a, b):
+            key = (a, b) if a < b else (b, a)
+            if key not in cache:
+                m = verts[a] + verts[b]
+                verts.append(m / np.linalg.norm(m))
+                cache[key] = len(verts) - 1
+            return cache[key]
+
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    return np.array(verts, dtype=np.float32), np.array(faces, dtype=np.int32)
+
+
+def _lattice(rng, size):
+    return rng.random((size, size), dtype=np.float64)
+
+
+def value_noise_height(x, z, seed, octaves=6, amplitude=2.0, base_freq=0.05):
+    """Seeded value noise, `octaves` octaves, smoothstep-interpolated lattice,
+    normalised to [-amplitude/2, amplitude/2] * 2 (peak-to-peak ~amplitude*2)."""
+    rng = np.random.default_rng(seed)
+    h = np.zeros_like(x, dtype=np.float64)
+    norm = 0.0
+    size = 256
+    for o in range(octaves):
+        lat = _lattice(rng, size)
+        freq = base_freq * (2.0 ** o)
+        fx = x * freq + 1000.0
+        fz = z * freq + 1000.0
+        ix = np.floor(fx).astype(np.int64)
+        iz = np.floor(fz).astype(np.int64)
+        tx = fx - ix
+        tz = fz - iz
+        tx = tx * tx * (3 - 2 * tx)
+        tz = tz * tz * (3 - 2 * tz)
+        x0, x1 = ix % size, (ix + 1) % size
+        z0, z1 = iz % size, (iz + 1) % size
+        a = lat[x0, z0] * (1 - tx) + lat[x1, z0] * tx
+        b = lat[x0, z1] * (1 - tx) + lat[x1, z1] * tx
+        w = 0.5 ** o
+        h += (a * (1 - tz) + b * tz - 0.5) * w
+        norm += w
+    return amplitude * 2.0 * h / norm
+
+
+def _mesh_xml(out, name, mat, verts, faces, normals=None, xform=None):
+    out.append('<object type="mesh" name="%s">\n<matref name="%s"/>\n' % (name, mat))
+    if xform:
+        out.append(xform)
+    out.append("<mesh>\n")
+    vs = np.char.mod("%.9g", verts.astype(np.float32).astype(np.float64))
+    ids = np.arange(len(verts))
+    out.append("".join('<vertex id="%d" val="%s %s %s"/>\n' % (i, a, b, c)
+                       for i, (a, b, c) in zip(ids, vs)))
+    if normals is not None:
+        ns = np.char.mod("%.9g", normals.astype(np.float32).astype(np.float64))
+        out.append("".join('<normal id="%d" val="%s %s %s"/>\n' % (i, a, b, c)
+                           for i, (a, b, c) in zip(ids, ns)))
+        out.append("".join(
+            '<face><vref vertex="%d" normal="%d"/><vref vertex="%d" normal="%d"/>'
+            '<vref vertex="%d" normal="%d"/></face>\n' % (a, a, b, b, c, c)
+            for a, b, c in faces.tolist()))
+    else:
+        out.append("".join(
+            '<face><vref vertex="%d"/><vref vertex="%d"/><vref vertex="%d"/></face>\n' % (a, b, c)
+            for a, b, c in faces.tolist()))
+    out.append("</mesh>\n</object>\n")
+
+
+def _material(out, name, kd, ks=0.3, shin=30.0, refl=None, refr=None, ior=None):
+    out.append('<material name="%s" shader="phong">\n' % name)
+    out.append('<mattr name="diffuse" value="%s"/>\n' % _vec(kd))
+    if np.ndim(ks) == 0:
+        ks = (ks, ks, ks)
+    out.append('<mattr name="specular" value="%s"/>\n' % _vec(ks))
+    out.append('<mattr name="shininess" value="%s"/>\n' % ("%.1f" % shin))
+    if refl is not None:
+        out.append('<mattr name="reflect" value="%.3f"/>\n' % refl)
+    if refr is not None:
+        out.append('<mattr name="refract" value="%.3f"/>\n' % refr)
+    if ior is not None:
+        out.append('<mattr name="ior" value="%.3f"/>\n' % ior)
+    out.append("</material>\n")
+
+
+def _xform(pos=None, scale=None, axisrot=None, time=None):
+    s = "<xform"
+    if time is not None:
+        s += ' time="%d"' % time
+    if pos is not None:
+        s += ' pos="%s"' % _vec(pos)
+    if scale is not None:
+        s += ' scale="%s"' % _vec(scale)
+    if axisrot is not None:
+        s += ' axisrot="%s"' % _vec(axisrot)
+    return s + "/>\n"
+
+
+def small_scene(seed=0x5EED0001):
+    """The 512x512 scene: ground quad, 16 spheres, icosphere(4), cylinder, point light."""
+    rng = np.random.default_rng(seed)
+    out = ["<?xml version=\"1.0\"?>\n<scene>\n"]
+    out.append('<env ambient="0.05 0.05 0.05" bgcolor="0.1 0.12 0.18"/>\n')
+    _material(out, "ground", (0.6, 0.6, 0.55), ks=0.1, shin=10.0)
+    n_sph = 16
+    centres = np.stack([rng.uniform(-5, 5, n_sph), rng.uniform(0.5, 3.0, n_sph),
+                        rng.uniform(-5, 5, n_sph)], axis=1)
+    radii = rng.uniform(0.3, 1.0, n_sph)
+    kinds = np.array(["phong"] * n_sph, dtype=object)
+    order = rng.permutation(n_sph)
+    kinds[order[:2]] = "glass"
+    kinds[order[2:6]] = "mirror"            # 4 of 16 = 25% mirrors
+    for i in range(n_sph):
+        kd = rng.uniform(0.1, 0.9, 3)
+        if kinds[i] == "glass":
+            _material(out, "m%d" % i, kd * 0.1, ks=1.0, shin=80.0, refr=1.0, ior=1.5)
+        elif kinds[i] == "mirror":
+            _material(out, "m%d" % i, kd, ks=1.0, shin=60.0, refl=0.8)
+        else:
+            _material(out, "m%d" % i, kd, ks=0.4, shin=30.0)
+    _material(out, "ico", rng.uniform(0.1, 0.9, 3), ks=0.5, shin=40.0)
+    _material(out, "cyl", rng.uniform(0.1, 0.9, 3), ks=0.3, shin=20.0)
+    g = 20.0
+    gv = np.array([[-g, 0, -g], [g, 0, -g], [g, 0, g], [-g, 0, g]], dtype=np.float32)
+    gf = np.array([[0, 2, 1], [0, 3, 2]], dtype=np.int32)
+    _mesh_xml(out, "ground", "ground", gv, gf)
+    for i in range(n_sph):
+        out.append('<object type="sphere" name="s%d">\n<matref name="m%d"/>\n%s<sphere rad="%s"/>\n</object>\n'
+                   % (i, i, _xform(pos=centres[i]), "%.6f" % radii[i]))
+    iv, ifc = icosphere(4)
+    _mesh_xml(out, "ico", "ico", iv, ifc, normals=iv,
+              xform=_xform(pos=(2.5, 1.3, 6.0), scale=(1.3, 1.3, 1.3)))
+    out.append('<object type="cylinder" name="cyl">\n<matref name="cyl"/>\n%s'
+               '<cylinder rad="0.5" start="0.0" end="2.0"/>\n</object>\n' % _xform(pos=(-6.5, 0.0, -2.0)))
+    out.append('<light type="point" color="1.0">\n%s</light>\n' % _xform(pos=(0.0, 8.0, 0.0)))
+    out.append('<camera type="target" fov="50.0">\n%s<target>\n%s</target>\n</camera>\n'
+               % (_xform(pos=(0.5, 7.0, 16.0)), _xform(pos=(0.0, 0.8, 0.0))))
+    out.append("</scene>\n")
+    return "".join(out)
+
+
+def production_scene(seed=0x5EED0002, grid=(1000, 500), extent=(100.0, 50.0), n_inst=200):
+    """The 1080p scene: displaced-grid terrain of 2*grid[0]*grid[1] triangles
+    (6-octave value noise, amplitude 2), n_inst subdivision-3 icosphere
+    instances with seeded transforms, 3 sphere lights."""
+    rng = np.random.default_rng(seed)
+    nx, nz = grid
+    ex, ez = extent
+    out = ["<?xml version=\"1.0\"?>\n<scene>\n"]
+    out.append('<env ambient="0.04 0.04 0.05" bgcolor="0.35 0.45 0.6"/>\n')
+    _material(out, "terrain", (0.45, 0.5, 0.32), ks=0.05, shin=8.0)
+    n_mirror = n_inst // 4
+    n_glass = n_inst // 10
+    kinds = np.array(["phong"] * n_inst, dtype=object)
+    order = rng.permutation(n_inst)
+    kinds[order[:n_glass]] = "glass"
+    kinds[order[n_glass:n_glass + n_mirror]] = "mirror"
+    for i in range(n_inst):
+        kd = rng.uniform(0.1, 0.9, 3)
+        if kinds[i] == "glass":
+            _material(out, "m%d" % i, kd * 0.1, ks=1.0, shin=80.0, refr=1.0, ior=1.5)
+        elif kinds[i] == "mirror":
+            _material(out, "m%d" % i, kd, ks=1.0, shin=60.0, refl=0.8)
+        else:
+            _material(out, "m%d" % i, kd, ks=0.4, shin=30.0)
+    # terrain
+    xs = np.linspace(-ex / 2, ex / 2, nx + 1)
+    zs = np.linspace(-ez / 2, ez / 2, nz + 1)
+    X, Z = np.meshgrid(xs, zs, indexing="ij")
+    hseed = int(rng.integers(1 << 31))
+    H = value_noise_height(X, Z, hseed)
+    verts = np.stack([X, H, Z], axis=-1).reshape(-1, 3).astype(np.float32)
+    dx = ex / nx
+    dz = ez / nz
+    Hp = np.pad(H, 1, mode="edge")
+    gx = (Hp[2:, 1:-1] - Hp[:-2, 1:-1]) / (2 * dx)
+    gz = (Hp[1:-1, 2:] - Hp[1:-1, :-2]) / (2 * dz)
+    nrm = np.stack([-gx, np.ones_like(gx), -gz], axis=-1)
+    nrm /= np.linalg.norm(nrm, axis=-1, keepdims=True)
+    nrm = nrm.reshape(-1, 3).astype(np.float32)
+    idx = np.arange((nx + 1) * (nz + 1)).reshape(nx + 1, nz + 1)
+    a = idx[:-1, :-1].ravel()
+    b = idx[1:, :-1].ravel()
+    c = idx[1:, 1:].ravel()
+    d = idx[:-1, 1:].ravel()
+    faces = np.empty((a.size * 2, 3), dtype=np.int64)
+    faces[0::2] = np.stack([a, d, c], axis=1)
+    faces[1::2] = np.stack([a, c, b], axis=1)
+    _mesh_xml(out, "terrain", "terrain", verts, faces, normals=nrm)
+    # instances
+    iv, ifc = icosphere(3)
+    px = rng.uniform(-0.4 * ex, 0.4 * ex, n_inst)
+    pz = rng.uniform(-0.4 * ez, 0.4 * ez, n_inst)
+    sc = rng.uniform(0.4, 1.5, n_inst)
+    lift = rng.uniform(0.0, 2.0, n_inst)
+    hy = value_noise_height(px, pz, hseed)
+    axes = rng.normal(size=(n_inst, 3))
+    axes /= np.linalg.norm(axes, axis=1, keepdims=True)
+    angles = rng.uniform(0, 360, n_inst)
+    for i in range(n_inst):
+        xf = _xform(pos=(px[i], hy[i] + sc[i] + lift[i], pz[i]), scale=(sc[i],) * 3,
+                    axisrot=(angles[i], axes[i][0], axes[i][1], axes[i][2]))
+        _mesh_xml(out, "inst%d" % i, "m%d" % i, iv, ifc, normals=iv, xform=xf)
+    for i, (lx, lz) in enumerate([(-20.0, 5.0), (15.0, -8.0), (5.0, 15.0)]):
+        out.append('<light type="sphere" color="0.7">\n%s<sphere rad="0.8"/>\n</light>\n'
+                   % _xform(pos=(lx, 18.0 + 2.0 * i, lz)))
+    out.append('<camera type="target" fov="50.0">\n%s<target>\n%s</target>\n</camera>\n'
+               % (_xform(pos=(0.7, 14.0, 42.0)), _xform(pos=(0.0, 0.0, -4.0))))
+    out.append("</scene>\n")
+    return "".join(out)
+
+
+# option sets (sray_opts fields) of the benchmark configurations
+CONFIGS = {
+    "small": dict(width=512, height=512, min_samples=1, max_samples=1, iter=5,
+                  caust_photons=100000, gi_photons=0, caust_k=50, gi_k=0, gather_rcap=0.5,
+                  scnoct_max_depth=8, scnoct_max_items=8, meshoct_max_depth=8, meshoct_max_items=8),
+    "production": dict(width=1920, height=1080, min_samples=1, max_samples=16, max_var=0.05, iter=8,
+                       caust_photons=500000, gi_photons=2000000, caust_k=100, gi_k=100, gather_rcap=0.5,
+                       scnoct_max_depth=8, scnoct_max_items=8, meshoct_max_depth=10, meshoct_max_items=8),
+}
+
+
+def scene_opts(name, **over):
+    d = dict(CONFIGS[name])
+    d.update(over)
+    return d
+
+
+def write_scene(name, cache_dir=None, **kw):
+    """Generate (or reuse from cache_dir) the XML of scene `name`; returns the path."""
+    gen = {"small": small_scene, "production": production_scene}[name]
+    key = hashlib.sha1(repr((name, sorted(kw.items()), 3)).encode()).hexdigest()[:12]
+    cache_dir = cache_dir or os.environ.get("SRAY_SCENE_CACHE", "/tmp/sray_scenes")
+    os.makedirs(cache_dir, exist_ok=True)
+    path = os.path.join(cache_dir, "%s_%s.xml" % (name, key))
+    if not os.path.exists(path):
+        xml = gen(**kw)
+        tmp = path + ".tmp%d" % os.getpid()
+        with open(tmp, "w") as f:
+            f.write(xml)
+        os.replace(tmp, path)
+    return path
