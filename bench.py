@@ -1,0 +1,367 @@
+#!/usr/bin/env python
+"""Frame benchmark of the GB300 renderer on the seeded production scene.
+
+A step is one full frame through the renderer's own entry point
+(sray_gpu_render: top-level octree build, projection maps, caustic and
+global photon maps traced and sorted on the device, then the adaptive
+<=16 spp wavefront render) with the scene resident in HBM.
+
+Reported value: Mrays/s = every segment traced through cast_ray (primary,
+secondary incl. final-gather rays, shadow rays) per second of frame time,
+with ms/frame beside it.  The JSON line also carries:
+  e2e          the same metric through the C-ABI with a HOST framebuffer
+               (device->host copy and per-frame table uploads inside the timing)
+  roofline     live CUDA-event time of the dominant kernel against its
+               algorithmic bytes (counted in an untimed pass) and the
+               measured HBM peak
+  cpu_baseline the CPU restatement of the reference's path, FP64, all host
+               threads, on a bounded sample of the same frame (see `sample`)
+  clocks       nvidia-smi samples taken during the timed region
+
+--impl reference times that CPU path alone, on the same metric.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s & ms/frame at equal RMSE vs FP64 oracle: NRC vs plain gather, 1 GB300"
+PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="production", choices=["production", "small"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-rows", type=int, default=24, help="rows of the CPU baseline sample")
+    ap.add_argument("--cpu-photon-frac", type=float, default=1.0)
+    return ap.parse_args()
+
+
+def workload_desc(cfg):
+    if cfg == "production":
+        return ("production: 1920x1080, adaptive 1-16 spp (variance 0.05), depth 8, 1M-triangle displaced-grid "
+                "terrain + 200 instanced icospheres (256k tris), 3 sphere lights, 2M global + 500k caustic photons, "
+                "k=100 nearest-photon gathers within r<=0.5")
+    return ("small: 512x512, 1 spp, depth 5, ground + 16 spheres + icosphere(4) + cylinder, point light, "
+            "100k caustic photons, k=50 gather")
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) of SM clock, max clock and throttle reasons."""
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+
+        def rd():
+            for line in self.proc.stdout:
+                self.samples.append([x.strip() for x in line.split(",")])
+        self.thread = threading.Thread(target=rd, daemon=True)
+        self.thread.start()
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[1]))
+                mx.append(float(s[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, nm in enumerate(names):
+                if len(s) > 5 + k and s[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(PEAKS_PATH) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM, "fallback"
+
+
+def rays_of(st):
+    return st["primary_rays"] + st["secondary_rays"] + st["shadow_rays"]
+
+
+def cpu_baseline(cfg, path, opts, rows, photon_frac, threads=0):
+    """The CPU restatement (FP64, all host threads) on a bounded sample of the
+    frame: the full photon maps (scaled by photon_frac) and a band of `rows`
+    image rows through the middle of the frame; extrapolated to the frame."""
+    from oracle.oracle import Oracle
+    o_opts = dict(opts)
+    o_opts["caust_photons"] = int(opts["caust_photons"] * photon_frac)
+    o_opts["gi_photons"] = int(opts["gi_photons"] * photon_frac)
+    o_opts["threads"] = threads
+    orc = Oracle(fp64=True, rng_mode=1, **o_opts)
+    orc.load(path)
+    t0 = time.perf_counter()
+    orc.prepare(0)
+    t_prep = time.perf_counter() - t0
+    h = opts["height"]
+    rows = min(rows, h)
+    y0 = (h - rows) // 2
+    t0 = time.perf_counter()
+    orc.render(0, rows=(y0, y0 + rows), nthreads=threads)
+    t_rows = time.perf_counter() - t0
+    c = orc.counters()
+    scale_rows = h / rows
+    t_frame = t_prep / max(photon_frac, 1e-9) + t_rows * scale_rows
+    rays_frame = c["rays"] * scale_rows
+    cores = threads if threads > 0 else (os.cpu_count() or 1)
+    return {
+        "value": rays_frame / t_frame / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
+        "ms_per_frame": t_frame * 1e3,
+        "sample": "rows %d-%d of %d at full spp and the photon maps at %g of full size (%.1f s build+photons, "
+                  "%.1f s rows), extrapolated to the frame; CPU restatement of the reference's path in FP64"
+                  % (y0, y0 + rows, h, photon_frac, t_prep, t_rows),
+        "wall_s": t_prep + t_rows,
+    }
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from sray_gb300 import scenegen
+    from oracle import oracle as orc_mod
+    orc_mod.build()
+    opts = scenegen.scene_opts(args.config)
+    path = scenegen.write_scene(args.config)
+    rows = max(4, args.cpu_rows // 2)
+    frac = 0.05 if args.config == "production" else 1.0
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(args.config, path, opts, rows, frac)
+        if i >= args.warmup:
+            vals.append(r)
+    v = sum(r["value"] for r in vals) / len(vals)
+    ms = sum(r["ms_per_frame"] for r in vals) / len(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scene)",
+        "config": {"workload": workload_desc(args.config), "method": "plain gather"},
+        "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": vals[0]["cores"], "kind": "port",
+                         "sample": vals[0]["sample"]},
+        "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    from sray_gb300 import build as gbuild, gpu, scenegen
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+    if rank == 0:
+        gbuild.build()
+    if ws > 1:
+        dist.barrier()
+    opts = scenegen.scene_opts(args.config)
+    path = scenegen.write_scene(args.config)
+    g = gpu.GpuRenderer(**opts)
+    t0 = time.perf_counter()
+    g.load(path)
+    t_load = time.perf_counter() - t0
+    info = g.scene_info()
+    H, W = opts["height"], opts["width"]
+    fb = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup):
+        g.render(0, fb, stream=stream)
+    torch.cuda.synchronize()
+
+    # untimed pass: traversal work of the closest-hit kernel (algorithmic bytes)
+    g.set_profiling(time_kernels=True, count_work=True)
+    g.kernel_times(reset=True)
+    g.render(0, fb, stream=stream)
+    torch.cuda.synchronize()
+    st_count = g.stats()
+    kt_count = g.kernel_times(reset=True)
+    trace_launches = max(kt_count.get("trace", (0.0, 1))[1], 1)
+    rays_traced = st_count["primary_rays"] + st_count["secondary_rays"]
+    trace_bytes = rays_traced * (48 + 16) + st_count["node_visits"] * 32 + st_count["prim_tests"] * 48
+
+    # timed region: K frames, device timing on the launch stream, kernel events live
+    g.set_profiling(time_kernels=True, count_work=False)
+    g.kernel_times(reset=True)
+    clocks = ClockSampler(dev)
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    rays = 0
+    launches = 0
+    for _ in range(args.steps):
+        g.render(0, fb, stream=stream)
+        st = g.stats()
+        rays += rays_of(st)
+        launches += st["kernel_launches"]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_total = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    kt = g.kernel_times(reset=True)
+    st_last = st
+    ms_step = ms_total / args.steps
+
+    # end to end through the C-ABI with a host framebuffer
+    g.set_profiling(False, False)
+    host_fb = np.zeros((H, W, 4), np.float32)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_rays = 0
+    h2d = d2h = 0
+    for _ in range(args.steps):
+        g.render(0, host_fb)
+        st = g.stats()
+        e2e_rays += rays_of(st)
+        h2d += st["h2d_bytes"]
+        d2h += st["d2h_bytes"]
+    e2e_s = time.perf_counter() - t0
+
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms_total, rays, e2e_s, e2e_rays], dtype=torch.float64, device="cuda")
+        tmax = t.clone()
+        dist.all_reduce(tmax[0:1], op=dist.ReduceOp.MAX)
+        dist.all_reduce(tmax[2:3], op=dist.ReduceOp.MAX)
+        dist.all_reduce(tmax[1:2], op=dist.ReduceOp.SUM)
+        dist.all_reduce(tmax[3:4], op=dist.ReduceOp.SUM)
+        ms_total, rays, e2e_s, e2e_rays = [float(x) for x in tmax.tolist()]
+        ms_step = ms_total / args.steps
+    value = rays / (ms_total / 1e3) / 1e6
+    e2e_value = e2e_rays / e2e_s / 1e6
+
+    # dominant kernel and its roofline
+    dom = max(kt.items(), key=lambda kv: kv[1][0])
+    hbm, src = peaks()
+    tr_ms, tr_n = kt.get("trace", (0.0, 1))
+    tr_avg_s = tr_ms / max(tr_n, 1) / 1e3
+    bytes_per_launch = trace_bytes / trace_launches
+    achieved = bytes_per_launch / tr_avg_s / 1e9 if tr_avg_s > 0 else 0.0
+    traffic = None
+    tf_path = os.path.join(ROOT, "profiles", "trace_traffic.json")
+    if os.path.exists(tf_path):
+        try:
+            with open(tf_path) as f:
+                traffic = json.load(f).get("bytes_per_launch")
+        except (OSError, ValueError):
+            traffic = None
+    roof = {"kernel": "k_trace (closest hit)", "bound": "hbm", "achieved": achieved, "peak": hbm,
+            "unit": "GB/s", "frac": achieved / hbm, "peak_source": src, "traffic": traffic,
+            "algorithmic_bytes_per_launch": bytes_per_launch,
+            "avg_launch_ms": tr_avg_s * 1e3, "dominant_kernel": dom[0],
+            "note": "algorithmic bytes = rays*64 + node visits*32 + primitive tests*48 (counted pass)",
+            "node_visits_per_ray": st_count["node_visits"] / max(rays_traced, 1),
+            "prim_tests_per_ray": st_count["prim_tests"] / max(rays_traced, 1)}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            frac = 0.05 if args.config == "production" else 1.0
+            cb = cpu_baseline(args.config, path, opts, args.cpu_rows, frac)
+            cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        except Exception as exc:  # the CPU baseline is a report, not the measurement
+            cpu = {"value": None, "unit": "Mrays/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": "failed: %s" % exc}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator, no dataset)",
+            "config": {"workload": workload_desc(args.config), "method": "plain gather",
+                       "parallelism": "replicas" if ws > 1 else "single",
+                       "l2": "inputs larger than L2: %.0f MB of triangle records + photon maps rebuilt every frame"
+                             % (info["triangles"] * 48 / 1e6),
+                       "scene": info},
+            "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": h2d // args.steps,
+                    "d2h_bytes_per_step": d2h // args.steps, "ms_per_step": e2e_s / args.steps * 1e3},
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "gpu_launches": launches,
+            "clocks": clk,
+            "kernels_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in kt.items()},
+            "frame": {"rays": rays_of(st_last), "primary": st_last["primary_rays"],
+                      "secondary": st_last["secondary_rays"], "shadow": st_last["shadow_rays"],
+                      "gathers": st_last["gathers"], "samples": st_last["samples"],
+                      "photons_stored": st_last["photons_stored"], "load_s": t_load},
+        }
+        print(json.dumps(line))
+    g.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -143,10 +143,24 @@ typedef struct sray_stats {
 	int64_t samples;               /* pixel samples taken (adaptive) */
 	int64_t node_visits, prim_tests;  /* traversal work (when counting is on) */
 	int kernel_launches;           /* kernels launched by the last render */
-	int reserved[7];
+	int pad;
+	int64_t h2d_bytes, d2h_bytes;  /* host<->device bytes copied by the last render */
+	int reserved[2];
 } sray_stats;
 
 int sray_gpu_get_stats(sray_stats *st);
+
+/* Profiling (extension, no reference counterpart).  flags bit 0: time every
+ * kernel launch with CUDA events recorded on the launch stream; bit 1: count
+ * octree node visits and primitive tests in the closest-hit kernel (slower;
+ * reported through sray_stats.node_visits / prim_tests). */
+int sray_gpu_set_profiling(int flags);
+
+/* Accumulated kernel times since the last call with reset = 1: for up to
+ * `max` kernel kinds, the name (NUL-separated in `names`), total ms and
+ * launch count.  Returns the number of kinds through `n_out`. */
+int sray_gpu_kernel_times(char *names, size_t names_cap, double *ms, int64_t *launches, int max,
+		int *n_out, int reset);
 
 /* Copy the last error message (NUL-terminated, truncated to `cap`). */
 int sray_gpu_last_error(char *buf, size_t cap);

@@ -2179,27 +2179,42 @@ template <class R> struct Frame : FrameBase {
 	{
 		std::vector<Photon<R> > &map = global ? gi : caust;
 		int num = global ? opt.gi_photons : opt.caust_photons;
-		Counters c;
+		int nthreads = opt.threads > 0 ? opt.threads : (int)std::thread::hardware_concurrency();
+		if(nthreads <= 0) nthreads = 1;
 		for(size_t li = 0; li < lights.size(); li++) {
 			int nphot = (int)ceil((double)num * power[li]);
 			size_t first = map.size();
-			for(int j = 0; j < nphot; j++) {
-				sray_rng s;
-				sray_rng_init(&s, opt.seed, global ? SRAY_DOM_GLOBAL : SRAY_DOM_CAUST, (uint32_t)j, (uint32_t)li);
-				int ms = t0 == t1 ? t0 : (sray_rng_int(&s) % (t1 - t0) + t0);
-				Photon<R> p;
-				if(!gen_photon((int)li, ms, global ? 1 : 2, &s, &p)) continue;
-				Ray<R> ray;
-				ray.o = p.p;
-				ray.d = p.dir;
-				ray.time = ms;
-				ray.iter = opt.iter;
-				if(global) {
-					if(trace_global(ray, &p, &s, c)) map.push_back(p);
-				} else {
-					if(trace_caust(ray, &p, &s, c) && p.type == CAUST_PHOTON) map.push_back(p);
+			/* photons are independent (each on its own stream): trace them on
+			 * all threads, keep the stored ones in emission order */
+			std::vector<Photon<R> > res(nphot > 0 ? nphot : 0);
+			std::vector<char> ok(nphot > 0 ? nphot : 0, 0);
+			std::atomic<int> next(0);
+			auto work = [&]() {
+				Counters c;
+				for(;;) {
+					int j0 = next.fetch_add(256);
+					if(j0 >= nphot) break;
+					for(int j = j0; j < j0 + 256 && j < nphot; j++) {
+						sray_rng s;
+						sray_rng_init(&s, opt.seed, global ? SRAY_DOM_GLOBAL : SRAY_DOM_CAUST, (uint32_t)j, (uint32_t)li);
+						int ms = t0 == t1 ? t0 : (sray_rng_int(&s) % (t1 - t0) + t0);
+						Photon<R> &p = res[j];
+						if(!gen_photon((int)li, ms, global ? 1 : 2, &s, &p)) continue;
+						Ray<R> ray;
+						ray.o = p.p;
+						ray.d = p.dir;
+						ray.time = ms;
+						ray.iter = opt.iter;
+						if(global) ok[j] = trace_global(ray, &p, &s, c);
+						else ok[j] = trace_caust(ray, &p, &s, c) && p.type == CAUST_PHOTON;
+					}
 				}
-			}
+			};
+			std::vector<std::thread> th;
+			for(int t = 1; t < nthreads; t++) th.push_back(std::thread(work));
+			work();
+			for(auto &t : th) t.join();
+			for(int j = 0; j < nphot; j++) if(ok[j]) map.push_back(res[j]);
 			if(nphot) {
 				double scale = 1.0 / (double)nphot;
 				for(size_t i = first; i < map.size(); i++) {

@@ -257,6 +257,7 @@ __device__ __forceinline__ void consider(Hit &h, float t, int obj, int prim)
 #define SRAY_PRUNE(te, best) ((te) > (best) * 1.00001f + 1e-30f)
 
 #define SRAY_MESH_STACK 96
+#define SRAY_MAILBOX 8
 #define SRAY_SCENE_STACK 96
 
 struct TraceCounters {
@@ -353,6 +354,9 @@ __device__ inline void trace_closest(const DScene &S, V3 wo, V3 wd, int time, Hi
 	float stt[SRAY_SCENE_STACK];
 	int sp = 0;
 	float te;
+	int mbox[SRAY_MAILBOX];
+	for(int k = 0; k < SRAY_MAILBOX; k++) mbox[k] = -1;
+	int mb_next = 0;
 	if(COUNT) tc->nodes++;
 	if(!box_hit(S.snodes[0].mn, S.snodes[0].mx, r, te)) return;
 	stk[sp] = 0;
@@ -382,7 +386,17 @@ __device__ inline void trace_closest(const DScene &S, V3 wo, V3 wd, int time, Hi
 			if(sp + nc > SRAY_SCENE_STACK) { *overflow = 1; nc = SRAY_SCENE_STACK - sp; }
 			for(int k = 0; k < nc; k++) { stk[sp] = ci[k]; stt[sp] = ct[k]; sp++; }
 		} else {
-			for(int s = 0; s < nd.count; s++) object_closest<COUNT>(S, S.sslots[nd.first + s], ti, wo, wd, h, tc, overflow);
+			for(int s = 0; s < nd.count; s++) {
+				int oi = S.sslots[nd.first + s];
+				/* an object straddling several leaves gives the same closest hit
+				 * every time: test it once per ray */
+				bool seen = false;
+				for(int k = 0; k < SRAY_MAILBOX; k++) seen |= mbox[k] == oi;
+				if(seen) continue;
+				mbox[mb_next] = oi;
+				mb_next = (mb_next + 1) & (SRAY_MAILBOX - 1);
+				object_closest<COUNT>(S, oi, ti, wo, wd, h, tc, overflow);
+			}
 		}
 	}
 }
@@ -433,6 +447,9 @@ __device__ inline bool trace_any(const DScene &S, V3 wo, V3 wd, int time, int *o
 	RayT r = make_ray(wo, wd);
 	int stk[SRAY_SCENE_STACK];
 	int sp = 0;
+	int mbox[SRAY_MAILBOX];
+	for(int k = 0; k < SRAY_MAILBOX; k++) mbox[k] = -1;
+	int mb_next = 0;
 	float te;
 	if(!box_hit(S.snodes[0].mn, S.snodes[0].mx, r, te)) return false;
 	stk[sp++] = 0;
@@ -452,6 +469,11 @@ __device__ inline bool trace_any(const DScene &S, V3 wo, V3 wd, int time, int *o
 		} else {
 			for(int s = 0; s < nd.count; s++) {
 				int oi = S.sslots[nd.first + s];
+				bool seen = false;
+				for(int k = 0; k < SRAY_MAILBOX; k++) seen |= mbox[k] == oi;
+				if(seen) continue;
+				mbox[mb_next] = oi;
+				mb_next = (mb_next + 1) & (SRAY_MAILBOX - 1);
 				const DevObj ob = S.objs[oi];
 				const float *inv = obj_xf(S, oi, ti) + 12;
 				RayT orr = make_ray(mul_pt(inv, wo), mul_dir(inv, wd));

@@ -437,21 +437,24 @@ int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored)
 	DevBuf pre, scl;
 	PCK(pre.upload(prefix, s), "photon prefix");
 	PCK(scl.upload(scale, s), "photon scale");
+	R.h2d += (int64_t)(prefix.size() * 4 + scale.size() * 4);
 	PCK(P.tmp_ph.ensure((size_t)total * sizeof(DevPhoton)), "photon buffer");
 	PCK(P.valid.ensure((size_t)total * sizeof(int)), "photon flags");
 	PCK(R.ctr.ensure(sizeof(DevCounters)), "counters");
 	PCK(cudaMemsetAsync(R.ctr.p, 0, sizeof(DevCounters), s), "counters");
-	k_photon<<<grid_n(total, 128), 128, 0, s>>>(R.S, global, pre.as<int>(), scl.as<float>(), nl, total, P.tmp_ph.as<DevPhoton>(),
-			P.valid.as<int>(), R.ctr.as<DevCounters>());
+	LAUNCH(R, "photon_trace", s, k_photon<<<grid_n(total, 128), 128, 0, s>>>(R.S, global, pre.as<int>(), scl.as<float>(), nl, total,
+			P.tmp_ph.as<DevPhoton>(), P.valid.as<int>(), R.ctr.as<DevCounters>()));
 	/* compaction in emission order */
 	int nb = (total + TILE - 1) / TILE;
 	PCK(P.scan.ensure((size_t)(nb + 4) * sizeof(unsigned)), "scan");
 	unsigned *bc = P.scan.as<unsigned>();
-	k_count_valid<<<nb, 256, 0, s>>>(P.valid.as<int>(), total, bc);
-	k_scan_excl<<<1, 1024, 0, s>>>(bc, nb, bc + nb);
+	LAUNCH(R, "photon_compact", s, k_count_valid<<<nb, 256, 0, s>>>(P.valid.as<int>(), total, bc));
+	LAUNCH(R, "photon_compact", s, k_scan_excl<<<1, 1024, 0, s>>>(bc, nb, bc + nb));
 	unsigned h_n = 0;
 	PCK(cudaMemcpyAsync(&h_n, bc + nb, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "stored count");
 	PCK(cudaStreamSynchronize(s), "photon trace");
+	R.d2h += sizeof(unsigned) + sizeof(DevCounters);
+	R.prof_collect();
 	DevCounters hc;
 	PCK(cudaMemcpy(&hc, R.ctr.p, sizeof hc, cudaMemcpyDeviceToHost), "counters");
 	if(hc.overflow) return R.fail(SRAY_EDEVICE, "traversal stack overflow while tracing photons");
@@ -460,7 +463,7 @@ int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored)
 	*stored = n;
 	if(n == 0) return 0;
 	PCK(P.ph.ensure((size_t)n * sizeof(DevPhoton)), "photon map");
-	k_compact<<<nb, 256, 0, s>>>(P.valid.as<int>(), P.tmp_ph.as<DevPhoton>(), total, bc, P.ph.as<DevPhoton>());
+	LAUNCH(R, "photon_compact", s, k_compact<<<nb, 256, 0, s>>>(P.valid.as<int>(), P.tmp_ph.as<DevPhoton>(), total, bc, P.ph.as<DevPhoton>()));
 	/* grid over the scene bounds: cells of the gather radius */
 	const Box &rb = R.sc.oct.nodes[0].box;
 	int k = global ? opt.gi_k : opt.caust_k;
@@ -498,7 +501,7 @@ int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored)
 	unsigned *keys = P.keys.as<unsigned>(), *keys2 = P.keys2.as<unsigned>();
 	unsigned *vals = P.vals.as<unsigned>(), *vals2 = P.vals2.as<unsigned>();
 	unsigned *lin = P.lin.as<unsigned>(), *lin2 = lin + n;
-	k_keys<<<grid_n(n, 256), 256, 0, s>>>(P.ph.as<DevPhoton>(), n, M, morton ? 1 : 0, keys, vals, lin);
+	LAUNCH(R, "photon_sort", s, k_keys<<<grid_n(n, 256), 256, 0, s>>>(P.ph.as<DevPhoton>(), n, M, morton ? 1 : 0, keys, vals, lin));
 	unsigned maxkey = morton ? (1u << 30) - 1u : (unsigned)(ncells - 1);
 	int bits = 0;
 	while(bits < 32 && (maxkey >> bits)) bits++;
@@ -507,20 +510,21 @@ int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored)
 	PCK(P.hist.ensure((size_t)256 * nbr * sizeof(unsigned) + 16), "radix histogram");
 	for(int ps = 0; ps < passes; ps++) {
 		int shift = ps * 8;
-		k_rs_hist<<<nbr, RS_THREADS, 0, s>>>(keys, n, shift, P.hist.as<unsigned>(), nbr);
-		k_scan_excl<<<1, 1024, 0, s>>>(P.hist.as<unsigned>(), 256 * nbr, nullptr);
-		k_rs_scatter<<<nbr, RS_THREADS, 0, s>>>(keys, vals, n, shift, P.hist.as<unsigned>(), nbr, keys2, vals2);
+		LAUNCH(R, "photon_sort", s, k_rs_hist<<<nbr, RS_THREADS, 0, s>>>(keys, n, shift, P.hist.as<unsigned>(), nbr));
+		LAUNCH(R, "photon_sort", s, k_scan_excl<<<1, 1024, 0, s>>>(P.hist.as<unsigned>(), 256 * nbr, nullptr));
+		LAUNCH(R, "photon_sort", s, k_rs_scatter<<<nbr, RS_THREADS, 0, s>>>(keys, vals, n, shift, P.hist.as<unsigned>(), nbr, keys2, vals2));
 		std::swap(keys, keys2);
 		std::swap(vals, vals2);
 	}
 	PCK(P.tmp_ph.ensure((size_t)n * sizeof(DevPhoton)), "photon buffer");
-	k_permute<<<grid_n(n, 256), 256, 0, s>>>(P.ph.as<DevPhoton>(), vals, lin, n, P.tmp_ph.as<DevPhoton>(), lin2);
+	LAUNCH(R, "photon_sort", s, k_permute<<<grid_n(n, 256), 256, 0, s>>>(P.ph.as<DevPhoton>(), vals, lin, n, P.tmp_ph.as<DevPhoton>(), lin2));
 	PCK(cudaMemsetAsync(P.cells.p, 0, ncells * sizeof(uint2), s), "cell table");
-	k_cells<<<grid_n(n, 256), 256, 0, s>>>(lin2, n, P.cells.as<uint2>());
+	LAUNCH(R, "photon_sort", s, k_cells<<<grid_n(n, 256), 256, 0, s>>>(lin2, n, P.cells.as<uint2>()));
 	std::swap(P.ph, P.tmp_ph);
 	M.ph = P.ph.as<DevPhoton>();
 	M.cells = P.cells.as<uint2>();
 	PCK(cudaStreamSynchronize(s), "photon map build");
+	R.prof_collect();
 	pre.release();
 	scl.release();
 	return 0;

@@ -101,243 +101,223 @@ __device__ __forceinline__ void acc_add(float4 *acc, int p, float r, float g, fl
 	atomicAdd(&acc[p].z, b);
 }
 
-struct Child {
-	V3 o, d;
-	float energy;
-	int iter, path, dsub;
-	float wr, wg, wb;
-	IorStack st;
-};
-
-__device__ __forceinline__ void push_ray(RayQueue &q, int slot, const Child &c, int pixel, int sample, int time)
-{
-	q.o[slot] = make_float4(c.o.x, c.o.y, c.o.z, c.energy);
-	q.d[slot] = make_float4(c.d.x, c.d.y, c.d.z, c.st.ior);
-	q.w[slot] = make_float4(c.wr, c.wg, c.wb, 0.0f);
-	q.meta[slot] = make_int4(pixel, c.iter, c.path, time);
-	q.stk[slot] = make_float4(c.st.stk[0], c.st.stk[1], c.st.stk[2], c.st.stk[3]);
-	q.ext[slot] = make_int2(sample | (c.dsub << 16), c.st.sp);
-}
-
 __device__ __forceinline__ float maxf_ref(float a, float b) { return a > b ? a : b; }
 
 #define MAX_DS 8
 
-/* shade one bounce: env colour for misses, shade_phong / shade_undef for hits */
-__global__ void __launch_bounds__(128) k_shade(DScene S, RayQueue qi, const int4 *hits, RayQueue qo, GatherReq *gq,
-		int *gq_count, int gq_cap, float4 *acc, int depth, DevCounters *ctr)
+struct ShadeOut {
+	RayQueue qo;
+	GatherReq *gq;
+	int *gq_count;
+	int gq_cap;
+	ShadowReq *sq;
+	int *sq_count;
+	int sq_cap;
+};
+
+__device__ __forceinline__ void push_child(ShadeOut &out, V3 o, V3 d, float energy, int iter, int path, int dsub,
+		const IorStack &st, float wr, float wg, float wb, int pixel, int sample, int time, int *overflow)
+{
+	int slot = warp_alloc(out.qo.count, 1);
+	if(slot >= out.qo.cap) { *overflow = 1; return; }
+	RayQueue &q = out.qo;
+	q.o[slot] = make_float4(o.x, o.y, o.z, energy);
+	q.d[slot] = make_float4(d.x, d.y, d.z, st.ior);
+	q.w[slot] = make_float4(wr, wg, wb, 0.0f);
+	q.meta[slot] = make_int4(pixel, iter, path, time);
+	q.stk[slot] = make_float4(st.stk[0], st.stk[1], st.stk[2], st.stk[3]);
+	q.ext[slot] = make_int2(sample | (dsub << 16), st.sp);
+}
+
+__device__ __forceinline__ void push_gather(ShadeOut &out, V3 pos, V3 n, int kind, int pixel, float wr, float wg, float wb,
+		int *overflow)
+{
+	int slot = warp_alloc(out.gq_count, 1);
+	if(slot >= out.gq_cap) { *overflow = 1; return; }
+	GatherReq g;
+	g.a = make_float4(pos.x, pos.y, pos.z, __int_as_float(kind));
+	g.b = make_float4(n.x, n.y, n.z, __int_as_float(pixel));
+	g.w = make_float4(wr, wg, wb, 0.0f);
+	out.gq[slot] = g;
+}
+
+/* a shadow ray and the light contribution it carries if unoccluded */
+__device__ __forceinline__ void push_shadow(ShadeOut &out, V3 o, V3 d, int time, int pixel, float wr, float wg, float wb,
+		int *overflow)
+{
+	int slot = warp_alloc(out.sq_count, 1);
+	if(slot >= out.sq_cap) { *overflow = 1; return; }
+	ShadowReq r;
+	r.a = make_float4(o.x, o.y, o.z, __int_as_float(time));
+	r.b = make_float4(d.x, d.y, d.z, __int_as_float(pixel));
+	r.w = make_float4(wr, wg, wb, 0.0f);
+	out.sq[slot] = r;
+}
+
+/* shade one bounce: env colour for misses, shade_phong / shade_undef for hits.
+ * Light samples become shadow requests carrying their contribution; children
+ * (reflection, refraction, final-gather rays) and photon gathers are queued. */
+__global__ void __launch_bounds__(128) k_shade(DScene S, RayQueue qi, const int4 *hits, ShadeOut out, float4 *acc, int depth,
+		DevCounters *ctr)
 {
 	int n = *qi.count;
 	int overflow = 0;
-	unsigned long long shadow_rays = 0;
-	for(int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
-		int i = base + threadIdx.x;
-		bool live = i < n;
-		int nchild = 0, ngather = 0;
-		Child ch[2 + MAX_DS];
-		GatherReq gr;
-		int pixel = 0, sample = 0, time = 0;
-		if(live) {
-			float4 o4 = qi.o[i], d4 = qi.d[i], w4 = qi.w[i], st4 = qi.stk[i];
-			int4 meta = qi.meta[i];
-			int2 ext = qi.ext[i];
-			int4 hv = hits[i];
-			pixel = meta.x;
-			int iter = meta.y, path = meta.z;
-			time = meta.w;
-			sample = ext.x & 0xffff;
-			int dsub = ext.x >> 16;
-			V3 ro = mk(o4.x, o4.y, o4.z), rd = mk(d4.x, d4.y, d4.z);
-			float energy = o4.w;
-			IorStack st;
-			st.ior = d4.w;
-			st.stk[0] = st4.x; st.stk[1] = st4.y; st.stk[2] = st4.z; st.stk[3] = st4.w;
-			st.sp = ext.y;
-			Hit h;
-			h.t = __int_as_float(hv.x);
-			h.obj = hv.y;
-			h.prim = hv.z;
-			h.tie = hv.w;
-			if(h.obj < 0) {
-				acc_add(acc, pixel, w4.x * S.env_col[0], w4.y * S.env_col[1], w4.z * S.env_col[2]);
-				if(depth == 0) acc[pixel].w = S.env_col[3];
-			} else {
-				if(depth == 0) acc[pixel].w = 1.0f;
-				const DevMat &mat = mat_of(S, h.obj);
-				Surf sp;
-				surface_point(S, h, ro, rd, time, sp, !mat.phong);
-				if(!mat.phong) {
-					/* shade_undef (src/shader.cc:36-73) */
-					sray_rng rng;
-					sray_rng_init(&rng, S.seed, SRAY_DOM_PIXEL | ((uint32_t)path << 4), (uint32_t)pixel, (uint32_t)(sample | (dsub << 16)));
-					int tx = (int)(sp.tex[0] * 20.0f), ty = (int)(sp.tex[1] * 10.0f);
-					bool even = (tx % 2) == (ty % 2);
-					float tc[3] = {even ? 1.0f : 0.2f, 0.3f, even ? 0.2f : 1.0f};
-					float df[3] = {0.1f, 0.1f, 0.1f}, sf[3] = {0.0f, 0.0f, 0.0f};
-					for(int li = 0; li < S.nlights; li++) {
-						const DevLight &L = S.lights[li];
-						V3 lpos = light_point(S, li, time, &rng);
-						V3 ldir = lpos - sp.pos;
-						float ldist = len(ldir);
-						V3 sdir = ldir;
-						ldir = ldir / ldist;
-						V3 vdir = -normalized(rd);
-						V3 hdir = normalized(ldir + vdir);
-						shadow_rays++;
-						if(!trace_any(S, sp.pos, sdir, time, &overflow)) {
-							float ndotl = maxf_ref(dot(sp.normal, ldir), 0.0f);
-							float ndoth = maxf_ref(dot(sp.normal, hdir), 0.0f);
-							float pw = powf(ndoth, 50.0f);
-							for(int k = 0; k < 3; k++) {
-								df[k] = df[k] + ndotl * L.col[k] * 1.0f;
-								sf[k] = sf[k] + pw * L.col[k] * 1.0f;
-							}
-						}
-					}
-					acc_add(acc, pixel, w4.x * (df[0] * tc[0] + sf[0]), w4.y * (df[1] * tc[1] + sf[1]), w4.z * (df[2] * tc[2] + sf[2]));
-				} else {
-					/* shade_phong (src/shader.cc:83-247) */
-					bool entering;
-					V3 normal;
-					if(dot(rd, sp.normal) > 0.0f) { normal = -sp.normal; entering = false; }
-					else { normal = sp.normal; entering = true; }
-					float ray_mag = len(rd);
-					V3 incident = rd / ray_mag;
-					const float *kd = mat.kd, *ks = mat.ks;
-					if(iter == DIFFUSE_ITER) {
-						/* final-gather ray: radiance_est(...) * kd */
-						gr.a = make_float4(sp.pos.x, sp.pos.y, sp.pos.z, __int_as_float(1));
-						gr.b = make_float4(normal.x, normal.y, normal.z, __int_as_float(pixel));
-						gr.w = make_float4(w4.x * kd[0], w4.y * kd[1], w4.z * kd[2], 0.0f);
-						ngather = 1;
-					} else {
-						sray_rng rng;
-						sray_rng_init(&rng, S.seed, SRAY_DOM_PIXEL | ((uint32_t)path << 4), (uint32_t)pixel, (uint32_t)sample);
-						float refl_fact = mat.refl, trans_fact = mat.refr, mat_ior = mat.ior;
-						float ior = st.calc_ior(entering, mat_ior);
-						float diff[3], spec[3] = {0.0f, 0.0f, 0.0f};
-						for(int k = 0; k < 3; k++) diff[k] = S.env_amb[k] * kd[k];
-						for(int li = 0; li < S.nlights; li++) {
-							const DevLight &L = S.lights[li];
-							int ns = L.type != 0 ? S.shadow_samples : 1;
-							float dl[3] = {0.0f, 0.0f, 0.0f}, sl[3] = {0.0f, 0.0f, 0.0f};
-							for(int si = 0; si < ns; si++) {
-								V3 lpos = light_point(S, li, time, &rng);
-								V3 ldir = lpos - sp.pos;
-								float ldist = len(ldir);
-								V3 sdir = ldir;
-								ldir = ldir / ldist;
-								shadow_rays++;
-								if(!trace_any(S, sp.pos, sdir, time, &overflow)) {
-									V3 vref = reflection(incident, normal);
-									float ndotl = maxf_ref(dot(normal, ldir), 0.0f);
-									float rdotl = maxf_ref(dot(vref, ldir), 0.0f);
-									float pw = powf(rdotl, mat.shin);
-									for(int k = 0; k < 3; k++) {
-										float lc = L.col[k] * 1.0f;
-										dl[k] = dl[k] + ndotl * lc;
-										sl[k] = sl[k] + pw * lc;
-									}
-								}
-							}
-							if(ns > 1) {
-								float scale = 1.0f / (float)ns;
-								for(int k = 0; k < 3; k++) { dl[k] = dl[k] * scale; sl[k] = sl[k] * scale; }
-							}
-							for(int k = 0; k < 3; k++) { diff[k] = diff[k] + dl[k]; spec[k] = spec[k] + sl[k]; }
-						}
-						/* final gather: diffuse rays end at their next hit (src/shader.cc:154-187) */
-						if(S.gi_on) {
-							int ds = S.diffuse_samples < MAX_DS ? S.diffuse_samples : MAX_DS;
-							for(int k = 0; k < ds; k++) {
-								V3 dir = sphrand(&rng, 1.0f);
-								float ndotl;
-								if((ndotl = dot(dir, normal)) < 0.0f) dir = -dir;
-								float diff_energy = ndotl * energy;
-								if(diff_energy > S.min_energy) {
-									Child &c = ch[nchild++];
-									c.o = sp.pos;
-									c.d = dir * ray_mag;
-									c.energy = diff_energy;
-									c.iter = DIFFUSE_ITER;
-									c.path = path * 4 + 2;
-									c.dsub = k;
-									c.st = st;
-									float g = S.diffuse_samples > 1 ? ndotl / (float)S.diffuse_samples : ndotl;
-									c.wr = w4.x * kd[0] * g;
-									c.wg = w4.y * kd[1] * g;
-									c.wb = w4.z * kd[2] * g;
-								}
-							}
-						}
-						float ray_dot_n = dot(-rd / ray_mag, normal);
-						float sf0 = trans_fact > 0.0f ? (ior - 1.0f) / (ior + 1.0f) : 1.0f;
-						float fres = fresnel(sf0 * sf0, ray_dot_n);
-						float refl_energy = refl_fact * energy;
-						if(refl_energy > S.min_energy && iter > 0) {
-							Child &c = ch[nchild++];
-							c.o = sp.pos;
-							c.d = reflection(rd, normal);
-							c.energy = refl_energy;
-							c.iter = iter - 1;
-							c.path = path * 4;
-							c.dsub = 0;
-							c.st = st;
-							float g = refl_fact * fres;
-							c.wr = w4.x * ks[0] * g;
-							c.wg = w4.y * ks[1] * g;
-							c.wb = w4.z * ks[2] * g;
-						}
-						float trans_energy = trans_fact * energy;
-						if(trans_energy > S.min_energy && iter > 0) {
-							Child &c = ch[nchild++];
-							c.st = st;
-							if(entering) c.st.enter(mat_ior);
-							else c.st.leave();
-							c.o = sp.pos;
-							c.d = refraction(rd / ray_mag, normal, ior) * ray_mag;
-							if(dot(c.d, normal) > 0.0f) {
-								if(entering) c.st.leave();
-								else c.st.enter(mat_ior);
-							}
-							c.energy = trans_energy;
-							c.iter = iter - 1;
-							c.path = path * 4 + 1;
-							c.dsub = 0;
-							float g = trans_fact * (1.0f - fres);
-							c.wr = w4.x * ks[0] * g;
-							c.wg = w4.y * ks[1] * g;
-							c.wb = w4.z * ks[2] * g;
-						}
-						if(S.caust_on) {
-							gr.a = make_float4(sp.pos.x, sp.pos.y, sp.pos.z, __int_as_float(0));
-							gr.b = make_float4(normal.x, normal.y, normal.z, __int_as_float(pixel));
-							gr.w = make_float4(w4.x, w4.y, w4.z, 0.0f);
-							ngather = 1;
-						}
-						acc_add(acc, pixel, w4.x * (diff[0] * kd[0] + spec[0] * ks[0]),
-								w4.y * (diff[1] * kd[1] + spec[1] * ks[1]),
-								w4.z * (diff[2] * kd[2] + spec[2] * ks[2]));
-					}
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		float4 o4 = qi.o[i], d4 = qi.d[i], w4 = qi.w[i];
+		int4 meta = qi.meta[i];
+		int2 ext = qi.ext[i];
+		int4 hv = hits[i];
+		int pixel = meta.x;
+		int iter = meta.y, path = meta.z, time = meta.w;
+		int sample = ext.x & 0xffff;
+		int dsub = ext.x >> 16;
+		V3 rd = mk(d4.x, d4.y, d4.z);
+		Hit h;
+		h.t = __int_as_float(hv.x);
+		h.obj = hv.y;
+		h.prim = hv.z;
+		h.tie = hv.w;
+		if(h.obj < 0) {
+			acc_add(acc, pixel, w4.x * S.env_col[0], w4.y * S.env_col[1], w4.z * S.env_col[2]);
+			if(depth == 0) acc[pixel].w = S.env_col[3];
+			continue;
+		}
+		if(depth == 0) acc[pixel].w = 1.0f;
+		const DevMat &mat = mat_of(S, h.obj);
+		Surf sp;
+		surface_point(S, h, mk(o4.x, o4.y, o4.z), rd, time, sp, !mat.phong);
+		if(!mat.phong) {
+			/* shade_undef (src/shader.cc:36-73) */
+			sray_rng rng;
+			sray_rng_init(&rng, S.seed, SRAY_DOM_PIXEL | ((uint32_t)path << 4), (uint32_t)pixel, (uint32_t)(sample | (dsub << 16)));
+			int tx = (int)(sp.tex[0] * 20.0f), ty = (int)(sp.tex[1] * 10.0f);
+			bool even = (tx % 2) == (ty % 2);
+			float tc[3] = {even ? 1.0f : 0.2f, 0.3f, even ? 0.2f : 1.0f};
+			acc_add(acc, pixel, w4.x * (0.1f * tc[0]), w4.y * (0.1f * tc[1]), w4.z * (0.1f * tc[2]));
+			for(int li = 0; li < S.nlights; li++) {
+				const DevLight &L = S.lights[li];
+				V3 lpos = light_point(S, li, time, &rng);
+				V3 ldir = lpos - sp.pos;
+				float ldist = len(ldir);
+				V3 sdir = ldir;
+				ldir = ldir / ldist;
+				V3 vdir = -normalized(rd);
+				V3 hdir = normalized(ldir + vdir);
+				float ndotl = maxf_ref(dot(sp.normal, ldir), 0.0f);
+				float ndoth = maxf_ref(dot(sp.normal, hdir), 0.0f);
+				float pw = powf(ndoth, 50.0f);
+				push_shadow(out, sp.pos, sdir, time, pixel, w4.x * (ndotl * L.col[0] * tc[0] + pw * L.col[0]),
+						w4.y * (ndotl * L.col[1] * tc[1] + pw * L.col[1]), w4.z * (ndotl * L.col[2] * tc[2] + pw * L.col[2]),
+						&overflow);
+			}
+			continue;
+		}
+		/* shade_phong (src/shader.cc:83-247) */
+		bool entering;
+		V3 normal;
+		if(dot(rd, sp.normal) > 0.0f) { normal = -sp.normal; entering = false; }
+		else { normal = sp.normal; entering = true; }
+		float ray_mag = len(rd);
+		V3 incident = rd / ray_mag;
+		const float *kd = mat.kd, *ks = mat.ks;
+		if(iter == DIFFUSE_ITER) {
+			/* final-gather ray: radiance_est(...) * kd */
+			push_gather(out, sp.pos, normal, 1, pixel, w4.x * kd[0], w4.y * kd[1], w4.z * kd[2], &overflow);
+			continue;
+		}
+		float energy = o4.w;
+		float4 st4 = qi.stk[i];
+		IorStack st;
+		st.ior = d4.w;
+		st.stk[0] = st4.x; st.stk[1] = st4.y; st.stk[2] = st4.z; st.stk[3] = st4.w;
+		st.sp = ext.y;
+		sray_rng rng;
+		sray_rng_init(&rng, S.seed, SRAY_DOM_PIXEL | ((uint32_t)path << 4), (uint32_t)pixel, (uint32_t)sample);
+		float refl_fact = mat.refl, trans_fact = mat.refr, mat_ior = mat.ior;
+		float ior = st.calc_ior(entering, mat_ior);
+		/* ambient: (env_ambient * kd) * kd */
+		acc_add(acc, pixel, w4.x * (S.env_amb[0] * kd[0] * kd[0]), w4.y * (S.env_amb[1] * kd[1] * kd[1]),
+				w4.z * (S.env_amb[2] * kd[2] * kd[2]));
+		V3 vref = reflection(incident, normal);
+		for(int li = 0; li < S.nlights; li++) {
+			const DevLight &L = S.lights[li];
+			int ns = L.type != 0 ? S.shadow_samples : 1;
+			float scale = ns > 1 ? 1.0f / (float)ns : 1.0f;
+			for(int si = 0; si < ns; si++) {
+				V3 lpos = light_point(S, li, time, &rng);
+				V3 ldir = lpos - sp.pos;
+				float ldist = len(ldir);
+				V3 sdir = ldir;
+				ldir = ldir / ldist;
+				float ndotl = maxf_ref(dot(normal, ldir), 0.0f);
+				float rdotl = maxf_ref(dot(vref, ldir), 0.0f);
+				float pw = powf(rdotl, mat.shin);
+				float c[3];
+				for(int k = 0; k < 3; k++) {
+					float lc = L.col[k] * 1.0f;
+					c[k] = ((ndotl * lc) * scale) * kd[k] + ((pw * lc) * scale) * ks[k];
+				}
+				if(c[0] != 0.0f || c[1] != 0.0f || c[2] != 0.0f)
+					push_shadow(out, sp.pos, sdir, time, pixel, w4.x * c[0], w4.y * c[1], w4.z * c[2], &overflow);
+			}
+		}
+		/* final gather: diffuse rays end at their next hit (src/shader.cc:154-187) */
+		if(S.gi_on) {
+			int ds = S.diffuse_samples < MAX_DS ? S.diffuse_samples : MAX_DS;
+			for(int k = 0; k < ds; k++) {
+				V3 dir = sphrand(&rng, 1.0f);
+				float ndotl;
+				if((ndotl = dot(dir, normal)) < 0.0f) dir = -dir;
+				float diff_energy = ndotl * energy;
+				if(diff_energy > S.min_energy) {
+					float g = S.diffuse_samples > 1 ? ndotl / (float)S.diffuse_samples : ndotl;
+					push_child(out, sp.pos, dir * ray_mag, diff_energy, DIFFUSE_ITER, path * 4 + 2, k, st,
+							w4.x * kd[0] * g, w4.y * kd[1] * g, w4.z * kd[2] * g, pixel, sample, time, &overflow);
 				}
 			}
 		}
-		if(nchild > 0) {
-			int slot = warp_alloc(qo.count, nchild);
-			if(slot + nchild > qo.cap) {
-				overflow = 1;
-			} else {
-				for(int k = 0; k < nchild; k++) push_ray(qo, slot + k, ch[k], pixel, sample, time);
+		float ray_dot_n = dot(-rd / ray_mag, normal);
+		float sf0 = trans_fact > 0.0f ? (ior - 1.0f) / (ior + 1.0f) : 1.0f;
+		float fres = fresnel(sf0 * sf0, ray_dot_n);
+		float refl_energy = refl_fact * energy;
+		if(refl_energy > S.min_energy && iter > 0) {
+			float g = refl_fact * fres;
+			push_child(out, sp.pos, reflection(rd, normal), refl_energy, iter - 1, path * 4, 0, st,
+					w4.x * ks[0] * g, w4.y * ks[1] * g, w4.z * ks[2] * g, pixel, sample, time, &overflow);
+		}
+		float trans_energy = trans_fact * energy;
+		if(trans_energy > S.min_energy && iter > 0) {
+			IorStack cs = st;
+			if(entering) cs.enter(mat_ior);
+			else cs.leave();
+			V3 td = refraction(rd / ray_mag, normal, ior) * ray_mag;
+			if(dot(td, normal) > 0.0f) {
+				if(entering) cs.leave();
+				else cs.enter(mat_ior);
 			}
+			float g = trans_fact * (1.0f - fres);
+			push_child(out, sp.pos, td, trans_energy, iter - 1, path * 4 + 1, 0, cs,
+					w4.x * ks[0] * g, w4.y * ks[1] * g, w4.z * ks[2] * g, pixel, sample, time, &overflow);
 		}
-		if(ngather > 0) {
-			int slot = warp_alloc(gq_count, 1);
-			if(slot >= gq_cap) overflow = 1;
-			else gq[slot] = gr;
-		}
+		if(S.caust_on) push_gather(out, sp.pos, normal, 0, pixel, w4.x, w4.y, w4.z, &overflow);
 	}
 	if(overflow) atomicOr(&ctr->overflow, 1);
-	if(shadow_rays) atomicAdd(&ctr->rays[2], shadow_rays);
+}
+
+/* shadow rays: the reference tests visibility with cast_ray(shadow_ray)
+ * (src/shader.cc:266), a hit anywhere on the segment [eps, 1] blocks */
+__global__ void __launch_bounds__(128) k_shadow(DScene S, const ShadowReq *sq, const int *sq_count, float4 *acc, DevCounters *ctr)
+{
+	int n = *sq_count;
+	int overflow = 0;
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		ShadowReq r = sq[i];
+		int time = __float_as_int(r.a.w), pixel = __float_as_int(r.b.w);
+		if(!trace_any(S, mk(r.a.x, r.a.y, r.a.z), mk(r.b.x, r.b.y, r.b.z), time, &overflow))
+			acc_add(acc, pixel, r.w.x, r.w.y, r.w.z);
+	}
+	if(overflow) atomicOr(&ctr->overflow, 1);
+	if(blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctr->rays[2], (unsigned long long)n);
 }
 
 /* ---------------------------------------------------------------- */
@@ -601,6 +581,52 @@ static int grid_for(int n, int block)
 	return g < 1 ? 1 : g;
 }
 
+int Renderer::kind_of(const char *name)
+{
+	for(size_t i = 0; i < ktimes.size(); i++) if(ktimes[i].name == name) return (int)i;
+	KTime k;
+	k.name = name;
+	ktimes.push_back(k);
+	return (int)ktimes.size() - 1;
+}
+
+void Renderer::prof_begin(int kind, cudaStream_t s, Pending *p)
+{
+	p->kind = kind;
+	p->a = p->b = nullptr;
+	launch_count++;
+	if(!(prof_flags & 1)) return;
+	for(int i = 0; i < 2; i++) {
+		cudaEvent_t e;
+		if(!event_pool.empty()) { e = event_pool.back(); event_pool.pop_back(); }
+		else cudaEventCreate(&e);
+		(i ? p->b : p->a) = e;
+	}
+	cudaEventRecord(p->a, s);
+}
+
+void Renderer::prof_end(Pending *p, cudaStream_t s)
+{
+	if(!(prof_flags & 1)) return;
+	cudaEventRecord(p->b, s);
+	pending.push_back(*p);
+}
+
+/* called after a stream synchronisation: every pending pair has completed */
+void Renderer::prof_collect()
+{
+	for(size_t i = 0; i < pending.size(); i++) {
+		float ms = 0.0f;
+		if(cudaEventElapsedTime(&ms, pending[i].a, pending[i].b) == cudaSuccess) {
+			ktimes[pending[i].kind].ms += ms;
+			ktimes[pending[i].kind].launches++;
+		}
+		event_pool.push_back(pending[i].a);
+		event_pool.push_back(pending[i].b);
+	}
+	pending.clear();
+}
+
 #define CK(call, where) do { cudaError_t e_ = (call); if(e_ != cudaSuccess) return cuda_fail(e_, where); } while(0)
 
 void Renderer::fill_scene_desc()
@@ -800,6 +826,7 @@ int Renderer::build_frame(long bt0, long bt1, cudaStream_t s)
 	CK(xf.upload(xfs, s), "upload transforms");
 	CK(light_pos.upload(lp, s), "upload light positions");
 	CK(cam_m.upload(cm, s), "upload camera");
+	h2d += (int64_t)(nodes.size() * sizeof(DevNode) + slots.size() * 4 + xfs.size() * 4 + lp.size() * 4 + cm.size() * 4);
 	CK(cudaStreamSynchronize(s), "build frame");
 	built = true;
 	photons_ready = false;
@@ -831,6 +858,7 @@ int Renderer::shoot(cudaStream_t s, int *nc, int *ng)
 		}
 		CK(projbits.upload(bits, s), "upload projection maps");
 		CK(coverage.upload(cov, s), "upload coverage");
+		h2d += (int64_t)(bits.size() * 4 + cov.size() * 4);
 		fill_scene_desc();
 		int r;
 		if(opt.caust_photons && (r = photon_shoot_map(*this, 0, s, &c))) return r;
@@ -886,6 +914,9 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 		fbd = fbdev.as<float4>();
 	}
 	int per_ray_children = 2 + (opt.gi_photons ? ds : 0);
+	int shadow_per_ray = 0;
+	for(size_t li = 0; li < sc.lights.size(); li++) shadow_per_ray += sc.lights[li].type != LT_POINT ? opt.shadow_samples : 1;
+	if(shadow_per_ray < 1) shadow_per_ray = 1;
 	if(ensure_queue(0, npix)) return SRAY_ECUDA;
 	CK(hits.ensure((size_t)npix * 16), "hits");
 	CK(gq.ensure((size_t)npix * sizeof(GatherReq)), "gather queue");
@@ -895,7 +926,8 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 	CK(cudaMemsetAsync(counts.p, 0, 64 * sizeof(int), s), "reset counts");
 	int h_n = npix;
 	CK(cudaMemcpyAsync(cnt + 3, &h_n, sizeof(int), cudaMemcpyHostToDevice, s), "active count");
-	int launches = 0;
+	h2d += sizeof(int);
+	long long l0 = launch_count;
 	memset(&stats, 0, sizeof stats);
 	int n_active = npix;
 	for(int sample = 0; sample < maxs && n_active > 0; sample++) {
@@ -905,8 +937,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 		int *next_count = cnt + 3 + (cur_act ^ 1);
 		q[0].count = cnt + 0;
 		q[1].count = cnt + 1;
-		k_camera<<<grid_for(n_active, 256), 256, 0, s>>>(S, act, act_count, sample, q[0], acc.as<float4>(), ctr.as<DevCounters>());
-		launches++;
+		LAUNCH(*this, "camera", s, k_camera<<<grid_for(n_active, 256), 256, 0, s>>>(S, act, act_count, sample, q[0], acc.as<float4>(), ctr.as<DevCounters>()));
 		int n_rays = n_active;
 		int cur = 0;
 		for(int depth = 0; n_rays > 0; depth++) {
@@ -920,37 +951,59 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			q[1].count = cnt + 1;
 			CK(cudaMemsetAsync(q[cur ^ 1].count, 0, sizeof(int), s), "reset queue");
 			CK(cudaMemsetAsync(cnt + 2, 0, sizeof(int), s), "reset gather queue");
-			k_trace<false><<<grid_for(n_rays, 128), 128, 0, s>>>(S, q[cur], hits.as<int4>(), ctr.as<DevCounters>());
-			k_shade<<<grid_for(n_rays, 128), 128, 0, s>>>(S, q[cur], hits.as<int4>(), q[cur ^ 1], gq.as<GatherReq>(), cnt + 2,
-					n_rays, acc.as<float4>(), depth, ctr.as<DevCounters>());
-			k_gather<<<grid_for(n_rays, GATHER_WARPS) , GATHER_WARPS * 32, 0, s>>>(S, gq.as<GatherReq>(), cnt + 2, acc.as<float4>(),
-					ctr.as<DevCounters>());
-			launches += 3;
+			CK(cudaMemsetAsync(cnt + 5, 0, sizeof(int), s), "reset shadow queue");
+			CK(sq.ensure((size_t)n_rays * shadow_per_ray * sizeof(ShadowReq)), "shadow queue");
+			if(prof_flags & 2)
+				LAUNCH(*this, "trace", s, k_trace<true><<<grid_for(n_rays, 128), 128, 0, s>>>(S, q[cur], hits.as<int4>(), ctr.as<DevCounters>()));
+			else
+				LAUNCH(*this, "trace", s, k_trace<false><<<grid_for(n_rays, 128), 128, 0, s>>>(S, q[cur], hits.as<int4>(), ctr.as<DevCounters>()));
+			ShadeOut so;
+			so.qo = q[cur ^ 1];
+			so.gq = gq.as<GatherReq>();
+			so.gq_count = cnt + 2;
+			so.gq_cap = n_rays;
+			so.sq = sq.as<ShadowReq>();
+			so.sq_count = cnt + 5;
+			so.sq_cap = n_rays * shadow_per_ray;
+			LAUNCH(*this, "shade", s, k_shade<<<grid_for(n_rays, 128), 128, 0, s>>>(S, q[cur], hits.as<int4>(), so, acc.as<float4>(), depth,
+					ctr.as<DevCounters>()));
+			LAUNCH(*this, "shadow", s, k_shadow<<<grid_for(n_rays * 2, 128), 128, 0, s>>>(S, sq.as<ShadowReq>(), cnt + 5, acc.as<float4>(),
+					ctr.as<DevCounters>()));
+			LAUNCH(*this, "gather", s, k_gather<<<grid_for(n_rays, GATHER_WARPS), GATHER_WARPS * 32, 0, s>>>(S, gq.as<GatherReq>(), cnt + 2,
+					acc.as<float4>(), ctr.as<DevCounters>()));
 			stats.secondary_rays += depth ? n_rays : 0;
 			int h_cnt = 0;
 			CK(cudaMemcpyAsync(&h_cnt, q[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "read queue count");
 			CK(cudaStreamSynchronize(s), "bounce");
+			d2h += sizeof(int);
+			prof_collect();
 			n_rays = h_cnt;
 			cur ^= 1;
 		}
 		CK(cudaMemsetAsync(next_count, 0, sizeof(int), s), "reset next active");
-		k_finish<<<grid_for(n_active, 256), 256, 0, s>>>(act, act_count, sample, acc.as<float4>(), hist.as<float4>(), sums.as<float4>(),
-				maxs, opt.min_samples, opt.max_var, active[cur_act ^ 1].as<int>(), next_count, fbd, spp.as<int>());
-		launches++;
+		LAUNCH(*this, "finish", s, k_finish<<<grid_for(n_active, 256), 256, 0, s>>>(act, act_count, sample, acc.as<float4>(), hist.as<float4>(),
+				sums.as<float4>(), maxs, opt.min_samples, opt.max_var, active[cur_act ^ 1].as<int>(), next_count, fbd, spp.as<int>()));
 		stats.samples += n_active;
 		int h_next = 0;
 		CK(cudaMemcpyAsync(&h_next, next_count, sizeof(int), cudaMemcpyDeviceToHost, s), "read active count");
 		CK(cudaStreamSynchronize(s), "sample pass");
+		d2h += sizeof(int);
+		prof_collect();
 		n_active = h_next;
 	}
 	DevCounters hc;
 	CK(cudaMemcpyAsync(&hc, ctr.p, sizeof hc, cudaMemcpyDeviceToHost, s), "read counters");
 	if(!fb_is_device) CK(cudaMemcpyAsync(fb, fbd, (size_t)npix * 16, cudaMemcpyDeviceToHost, s), "copy framebuffer");
 	CK(cudaStreamSynchronize(s), "render");
+	d2h += sizeof hc + (fb_is_device ? 0 : (int64_t)npix * 16);
 	stats.primary_rays = (int64_t)hc.rays[0];
 	stats.shadow_rays = (int64_t)hc.rays[2];
 	stats.gathers = (int64_t)hc.rays[3];
-	stats.kernel_launches = launches;
+	stats.kernel_launches = (int)(launch_count - l0);
+	stats.h2d_bytes = h2d;
+	stats.d2h_bytes = d2h;
+	stats.node_visits = (int64_t)hc.nodes;
+	stats.prim_tests = (int64_t)hc.prims;
 	if(hc.overflow) return fail(SRAY_EDEVICE, "device queue or traversal stack overflow");
 	return 0;
 }
@@ -1108,6 +1161,7 @@ int sray_gpu_render_pixels(long msec, float *fb, int fb_is_device, void *stream)
 {
 	NEED_CTX();
 	if(!fb) { g_err = "null framebuffer"; return SRAY_EINVAL; }
+	g_R->h2d = g_R->d2h = 0;
 	int r = g_R->render_pixels(msec, fb, fb_is_device, as_stream(stream));
 	if(r) g_err = g_R->err;
 	return r;
@@ -1121,10 +1175,13 @@ int sray_gpu_render(long msec, float *fb, int fb_is_device, void *stream)
 	if(!fb) { g_err = "null framebuffer"; return SRAY_EINVAL; }
 	long t0, t1;
 	frame_interval(R, msec, &t0, &t1);
+	long long l0 = R.launch_count;
+	R.h2d = R.d2h = 0;
 	int r = R.build_frame(t0, t1, as_stream(stream));
 	if(!r) r = R.shoot(as_stream(stream), nullptr, nullptr);
 	if(!r) r = R.render_pixels(msec, fb, fb_is_device, as_stream(stream));
 	if(r) g_err = R.err;
+	else R.stats.kernel_launches = (int)(R.launch_count - l0);
 	return r;
 }
 
@@ -1217,6 +1274,35 @@ int sray_gpu_get_stats(sray_stats *st)
 	return 0;
 }
 
+int sray_gpu_set_profiling(int flags)
+{
+	NEED_CTX();
+	g_R->prof_flags = flags;
+	return 0;
+}
+
+int sray_gpu_kernel_times(char *names, size_t names_cap, double *ms, int64_t *launches, int max, int *n_out, int reset)
+{
+	NEED_CTX();
+	Renderer &R = *g_R;
+	int n = (int)R.ktimes.size();
+	if(n_out) *n_out = n;
+	size_t off = 0;
+	for(int i = 0; i < n && i < max; i++) {
+		if(ms) ms[i] = R.ktimes[i].ms;
+		if(launches) launches[i] = R.ktimes[i].launches;
+		if(names) {
+			const std::string &nm = R.ktimes[i].name;
+			if(off + nm.size() + 1 <= names_cap) {
+				memcpy(names + off, nm.c_str(), nm.size() + 1);
+				off += nm.size() + 1;
+			}
+		}
+	}
+	if(reset) for(auto &k : R.ktimes) { k.ms = 0.0; k.launches = 0; }
+	return 0;
+}
+
 int sray_gpu_last_error(char *buf, size_t cap)
 {
 	if(!buf || cap == 0) return SRAY_EINVAL;
@@ -1232,7 +1318,7 @@ void sray_gpu_shutdown(void)
 	if(!g_R) return;
 	Renderer &R = *g_R;
 	DevBuf *bufs[] = {&R.mnodes, &R.mtris, &R.mprim, &R.tri_pos, &R.tri_attr, &R.objs, &R.mats, &R.lights, &R.snodes, &R.sslots,
-		&R.xf, &R.light_pos, &R.cam_m, &R.projbits, &R.coverage, &R.qbuf[0], &R.qbuf[1], &R.hits, &R.gq, &R.acc, &R.hist, &R.sums,
+		&R.xf, &R.light_pos, &R.cam_m, &R.projbits, &R.coverage, &R.qbuf[0], &R.qbuf[1], &R.hits, &R.gq, &R.sq, &R.acc, &R.hist, &R.sums,
 		&R.active[0], &R.active[1], &R.spp, &R.fbdev, &R.ctr, &R.counts};
 	for(DevBuf *b : bufs) b->release();
 	PhotonBufs *pb[] = {&R.caust, &R.gi};

@@ -59,6 +59,13 @@ struct GatherReq {
 	float4 w;
 };
 
+/* a shadow ray: origin + time, direction + pixel, contribution if unoccluded */
+struct ShadowReq {
+	float4 a;
+	float4 b;
+	float4 w;
+};
+
 /* device-side error and work counters */
 struct DevCounters {
 	int overflow;        /* traversal stack or queue overflow */
@@ -93,10 +100,24 @@ struct Renderer {
 	DScene S;
 
 	/* render buffers */
-	DevBuf qbuf[2], hits, gq, acc, hist, sums, active[2], spp, fbdev, ctr, counts;
+	DevBuf qbuf[2], hits, gq, sq, acc, hist, sums, active[2], spp, fbdev, ctr, counts;
 	RayQueue q[2];
 	int qcap[2] = {0, 0};
 	sray_stats stats;
+
+	/* profiling: event pairs per launch, resolved after each synchronisation */
+	int prof_flags = 0;
+	long long launch_count = 0;
+	int64_t h2d = 0, d2h = 0;     /* host<->device bytes since the last reset */
+	struct KTime { std::string name; double ms = 0.0; long long launches = 0; };
+	std::vector<KTime> ktimes;
+	struct Pending { int kind; cudaEvent_t a, b; };
+	std::vector<Pending> pending;
+	std::vector<cudaEvent_t> event_pool;
+	int kind_of(const char *name);
+	void prof_begin(int kind, cudaStream_t s, Pending *p);
+	void prof_end(Pending *p, cudaStream_t s);
+	void prof_collect();
 
 	int fail(int code, const std::string &msg) { err = msg; return code; }
 	int cuda_fail(cudaError_t e, const char *where)
@@ -112,6 +133,14 @@ struct Renderer {
 	int ensure_queue(int which, int cap);
 	void fill_scene_desc();
 };
+
+#define LAUNCH(R_, kname_, s_, ...) do { \
+		static thread_local int kind_ = -1; \
+		if(kind_ < 0 || kind_ >= (int)(R_).ktimes.size() || (R_).ktimes[kind_].name != kname_) kind_ = (R_).kind_of(kname_); \
+		Renderer::Pending pend_; (R_).prof_begin(kind_, s_, &pend_); \
+		__VA_ARGS__; \
+		(R_).prof_end(&pend_, s_); \
+	} while(0)
 
 /* photon.cu */
 int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored);

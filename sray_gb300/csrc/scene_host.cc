@@ -592,7 +592,9 @@ ProjMap::ProjMap()
 	}
 }
 
-void ProjMap::corner_dir(int uc, int vc, int corner, double out[3]) const
+/* ProjMap::cell_corner_dir (src/projmap.cc:124-140); the 64x32 grid's corner
+ * directions are computed once and reused (same values every call) */
+static void corner_dir_eval(int udiv, int vdiv, int uc, int vc, int corner, double out[3])
 {
 	static const int offs[4][2] = {{0, 0}, {1, 0}, {1, 1}, {0, 1}};
 	double du = 1.0 / udiv, dv = 1.0 / vdiv;
@@ -601,6 +603,31 @@ void ProjMap::corner_dir(int uc, int vc, int corner, double out[3]) const
 	out[0] = 1.0 * cos(theta) * sin(phi);
 	out[1] = 1.0 * cos(phi);
 	out[2] = 1.0 * sin(theta) * sin(phi);
+}
+
+struct CornerTable {
+	double d[64 * 32][4][3];
+	CornerTable()
+	{
+		for(int i = 0; i < 64 * 32; i++)
+			for(int k = 0; k < 4; k++) corner_dir_eval(64, 32, i % 64, i / 64, k, d[i][k]);
+	}
+};
+
+static const CornerTable &corner_table()
+{
+	static const CornerTable *t = new CornerTable();
+	return *t;
+}
+
+void ProjMap::corner_dir(int uc, int vc, int corner, double out[3]) const
+{
+	if(udiv == 64 && vdiv == 32) {
+		const double *c = corner_table().d[vc * 64 + uc][corner];
+		out[0] = c[0]; out[1] = c[1]; out[2] = c[2];
+		return;
+	}
+	corner_dir_eval(udiv, vdiv, uc, vc, corner, out);
 }
 
 void ProjMap::cell_from_dir(const double d[3], int *uc, int *vc) const

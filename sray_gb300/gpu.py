@@ -17,7 +17,8 @@ _lib = None
 EXPORTS = ["sray_default_opts", "sray_gpu_init", "sray_gpu_set_opts", "sray_gpu_load_scene", "sray_gpu_load_scene_mem",
            "sray_gpu_scene_info", "sray_gpu_build", "sray_gpu_shoot_photons", "sray_gpu_render",
            "sray_gpu_render_pixels", "sray_gpu_cast_rays", "sray_gpu_primary_hits", "sray_gpu_get_photons",
-           "sray_gpu_get_stats", "sray_gpu_last_error", "sray_gpu_shutdown"]
+           "sray_gpu_get_stats", "sray_gpu_set_profiling", "sray_gpu_kernel_times", "sray_gpu_last_error",
+           "sray_gpu_shutdown"]
 
 
 class SrayStats(ctypes.Structure):
@@ -26,7 +27,8 @@ class SrayStats(ctypes.Structure):
                 ("photons_emitted", ctypes.c_int64), ("photons_stored", ctypes.c_int64),
                 ("gathers", ctypes.c_int64), ("samples", ctypes.c_int64),
                 ("node_visits", ctypes.c_int64), ("prim_tests", ctypes.c_int64),
-                ("kernel_launches", ctypes.c_int), ("reserved", ctypes.c_int * 7)]
+                ("kernel_launches", ctypes.c_int), ("pad", ctypes.c_int),
+                ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64), ("reserved", ctypes.c_int * 2)]
 
 
 class SrayError(RuntimeError):
@@ -60,6 +62,8 @@ def load_library():
     L.sray_gpu_primary_hits.argtypes = [lp, vp, vp, vp, vp, vp]
     L.sray_gpu_get_photons.argtypes = [ip, vp, ip, vp]
     L.sray_gpu_get_stats.argtypes = [ctypes.POINTER(SrayStats)]
+    L.sray_gpu_set_profiling.argtypes = [ip]
+    L.sray_gpu_kernel_times.argtypes = [ctypes.c_char_p, ctypes.c_size_t, vp, vp, ip, vp, ip]
     L.sray_gpu_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     L.sray_gpu_shutdown.argtypes = []
     L.sray_gpu_shutdown.restype = None
@@ -170,7 +174,20 @@ class GpuRenderer:
     def stats(self):
         st = SrayStats()
         self._chk(self.L.sray_gpu_get_stats(ctypes.byref(st)))
-        return {f[0]: getattr(st, f[0]) for f in SrayStats._fields_ if f[0] != "reserved"}
+        return {f[0]: getattr(st, f[0]) for f in SrayStats._fields_ if f[0] not in ("reserved", "pad")}
+
+    def set_profiling(self, time_kernels=False, count_work=False):
+        self._chk(self.L.sray_gpu_set_profiling((1 if time_kernels else 0) | (2 if count_work else 0)))
+
+    def kernel_times(self, reset=True):
+        """{kernel kind: (total ms, launches)} accumulated since the last reset."""
+        names = ctypes.create_string_buffer(4096)
+        ms = np.zeros(64, np.float64)
+        ln = np.zeros(64, np.int64)
+        n = ctypes.c_int()
+        self._chk(self.L.sray_gpu_kernel_times(names, 4096, _ptr(ms), _ptr(ln), 64, ctypes.byref(n), int(reset)))
+        keys = names.raw.split(b"\0")[:n.value]
+        return {k.decode(): (float(ms[i]), int(ln[i])) for i, k in enumerate(keys)}
 
     def close(self):
         self.L.sray_gpu_shutdown()
