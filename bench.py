@@ -45,8 +45,21 @@ def parse():
     ap.add_argument("--config", default="production", choices=["production", "small"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-rows", type=int, default=24, help="rows of the CPU baseline sample")
-    ap.add_argument("--cpu-photon-frac", type=float, default=1.0)
+    ap.add_argument("--res", default=None, help="WxH override (profiling runs on a reduced case)")
+    ap.add_argument("--photon-scale", type=float, default=1.0, help="photon count multiplier (profiling)")
     return ap.parse_args()
+
+
+def config_opts(args):
+    from sray_gb300 import scenegen
+    opts = scenegen.scene_opts(args.config)
+    if args.res:
+        w, h = args.res.lower().split("x")
+        opts["width"], opts["height"] = int(w), int(h)
+    if args.photon_scale != 1.0:
+        opts["caust_photons"] = int(opts["caust_photons"] * args.photon_scale)
+        opts["gi_photons"] = int(opts["gi_photons"] * args.photon_scale)
+    return opts
 
 
 def workload_desc(cfg):
@@ -172,7 +185,7 @@ def run_reference(args):
     from sray_gb300 import scenegen
     from oracle import oracle as orc_mod
     orc_mod.build()
-    opts = scenegen.scene_opts(args.config)
+    opts = config_opts(args)
     path = scenegen.write_scene(args.config)
     rows = max(4, args.cpu_rows // 2)
     frac = 0.05 if args.config == "production" else 1.0
@@ -213,8 +226,9 @@ def run_ours(args):
         gbuild.build()
     if ws > 1:
         dist.barrier()
-    opts = scenegen.scene_opts(args.config)
+    opts = config_opts(args)
     path = scenegen.write_scene(args.config)
+    free0 = torch.cuda.mem_get_info()[0]
     g = gpu.GpuRenderer(**opts)
     t0 = time.perf_counter()
     g.load(path)
@@ -227,6 +241,7 @@ def run_ours(args):
     for _ in range(args.warmup):
         g.render(0, fb, stream=stream)
     torch.cuda.synchronize()
+    device_mb = (free0 - torch.cuda.mem_get_info()[0]) / 1e6
 
     # untimed pass: traversal work of the closest-hit kernel (algorithmic bytes)
     g.set_profiling(time_kernels=True, count_work=True)
@@ -331,7 +346,9 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator, no dataset)",
-            "config": {"workload": workload_desc(args.config), "method": "plain gather",
+            "config": {"workload": workload_desc(args.config) + ("" if not args.res and args.photon_scale == 1.0 else
+                                                                  " [reduced: %s, photons x%g]" % (args.res, args.photon_scale)),
+                       "method": "plain gather",
                        "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "inputs larger than L2: %.0f MB of triangle records + photon maps rebuilt every frame"
                              % (info["triangles"] * 48 / 1e6),
@@ -346,7 +363,7 @@ def run_ours(args):
             "frame": {"rays": rays_of(st_last), "primary": st_last["primary_rays"],
                       "secondary": st_last["secondary_rays"], "shadow": st_last["shadow_rays"],
                       "gathers": st_last["gathers"], "samples": st_last["samples"],
-                      "photons_stored": st_last["photons_stored"], "load_s": t_load},
+                      "photons_stored": st_last["photons_stored"], "load_s": t_load, "device_mb": device_mb},
         }
         print(json.dumps(line))
     g.close()

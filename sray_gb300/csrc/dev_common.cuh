@@ -36,6 +36,7 @@ struct DScene {
 	const DevNode *snodes;    /* top-level octree (world space) */
 	const int *sslots;
 	int has_scene;
+	int sroot;                /* root node index in snodes */
 	const DevNode *mnodes;    /* mesh octrees (object space) */
 	const DevTri *mtris;
 	const int *mprim;
@@ -256,59 +257,75 @@ __device__ __forceinline__ void consider(Hit &h, float t, int obj, int prim)
  * contains it can never hide a candidate the exhaustive search would find */
 #define SRAY_PRUNE(te, best) ((te) > (best) * 1.00001f + 1e-30f)
 
-#define SRAY_MESH_STACK 96
+#define SRAY_STACK 112
 #define SRAY_MAILBOX 8
-#define SRAY_SCENE_STACK 96
 
 struct TraceCounters {
 	unsigned long long nodes, prims;
 };
 
+/* octant of the ray direction: children are stored in slot order
+ * x | y << 1 | z << 2, so visiting slots (k ^ octant) for k = 0..7 goes
+ * front to back along the ray */
+__device__ __forceinline__ int octant(const RayT &r)
+{
+	return (r.d.x < 0.0f ? 1 : 0) | (r.d.y < 0.0f ? 2 : 0) | (r.d.z < 0.0f ? 4 : 0);
+}
+
+struct TStack {
+	int node[SRAY_STACK];
+	float te[SRAY_STACK];
+};
+
+/* test the 8 children of an inner node and push the hit ones far to near */
 template <bool COUNT>
-__device__ __forceinline__ void mesh_closest(const DScene &S, int root, int obj, const RayT &r, Hit &h,
+__device__ __forceinline__ int push_children(const DevNode *nodes, int first, int oct, const RayT &r, float best, TStack &st,
+		int sp, int limit, TraceCounters *tc, int *overflow)
+{
+	#pragma unroll
+	for(int k = 7; k >= 0; k--) {
+		int c = first + (k ^ oct);
+		const float4 *cp = reinterpret_cast<const float4 *>(nodes + c);
+		float4 c1 = __ldg(cp + 1);
+		if(__float_as_int(c1.w) == 0) continue;
+		float4 c0 = __ldg(cp);
+		float mn[3] = {c0.x, c0.y, c0.z}, mx[3] = {c1.x, c1.y, c1.z};
+		if(COUNT) tc->nodes++;
+		float tk;
+		if(box_hit(mn, mx, r, tk) && !SRAY_PRUNE(tk, best)) {
+			if(sp >= limit) { *overflow = 1; continue; }
+			st.node[sp] = c;
+			st.te[sp] = tk;
+			sp++;
+		}
+	}
+	return sp;
+}
+
+/* closest hit inside one mesh (object space), sharing the best hit so far */
+template <bool COUNT>
+__device__ __forceinline__ void mesh_closest(const DScene &S, int root, int obj, const RayT &r, Hit &h, TStack &st, int base,
 		TraceCounters *tc, int *overflow)
 {
-	int stk[SRAY_MESH_STACK];
-	float stt[SRAY_MESH_STACK];
-	int sp = 0;
+	int sp = base;
 	float te;
 	const DevNode &rn = S.mnodes[root];
 	if(COUNT) tc->nodes++;
 	if(!box_hit(rn.mn, rn.mx, r, te)) return;
-	stk[sp] = root;
-	stt[sp] = te;
+	int oct = octant(r);
+	st.node[sp] = root;
+	st.te[sp] = te;
 	sp++;
-	while(sp > 0) {
+	while(sp > base) {
 		sp--;
-		int ni = stk[sp];
-		if(SRAY_PRUNE(stt[sp], h.t)) continue;
+		int ni = st.node[sp];
+		if(SRAY_PRUNE(st.te[sp], h.t)) continue;
 		const float4 *np = reinterpret_cast<const float4 *>(S.mnodes + ni);
-		float4 n1 = __ldg(np + 1);
-		int count = __float_as_int(n1.w);
+		float4 n0 = __ldg(np), n1 = __ldg(np + 1);
+		int count = __float_as_int(n1.w), first = __float_as_int(n0.w);
 		if(count < 0) {
-			int first = __float_as_int(__ldg(np).w);
-			/* the 8 children: test, keep the hit ones, push far to near */
-			int ci[8];
-			float ct[8];
-			int nc = 0;
-			for(int k = 0; k < 8; k++) {
-				const float4 *cp = reinterpret_cast<const float4 *>(S.mnodes + first + k);
-				float4 c0 = __ldg(cp), c1 = __ldg(cp + 1);
-				if(__float_as_int(c1.w) == 0) continue;
-				float mn[3] = {c0.x, c0.y, c0.z}, mx[3] = {c1.x, c1.y, c1.z};
-				if(COUNT) tc->nodes++;
-				float tk;
-				if(box_hit(mn, mx, r, tk) && !SRAY_PRUNE(tk, h.t)) {
-					int j = nc++;
-					while(j > 0 && ct[j - 1] < tk) { ct[j] = ct[j - 1]; ci[j] = ci[j - 1]; j--; }
-					ct[j] = tk;
-					ci[j] = first + k;
-				}
-			}
-			if(sp + nc > SRAY_MESH_STACK) { *overflow = 1; nc = SRAY_MESH_STACK - sp; }
-			for(int k = 0; k < nc; k++) { stk[sp] = ci[k]; stt[sp] = ct[k]; sp++; }
+			sp = push_children<COUNT>(S.mnodes, first, oct, r, h.t, st, sp, SRAY_STACK, tc, overflow);
 		} else {
-			int first = __float_as_int(__ldg(np).w);
 			const float4 *tp = reinterpret_cast<const float4 *>(S.mtris + first);
 			for(int s = 0; s < count; s++) {
 				float4 a = __ldg(tp + 3 * s), b = __ldg(tp + 3 * s + 1), c = __ldg(tp + 3 * s + 2);
@@ -321,7 +338,7 @@ __device__ __forceinline__ void mesh_closest(const DScene &S, int root, int obj,
 }
 
 template <bool COUNT>
-__device__ __forceinline__ void object_closest(const DScene &S, int oi, int ti, V3 wo, V3 wd, Hit &h,
+__device__ __forceinline__ void object_closest(const DScene &S, int oi, int ti, V3 wo, V3 wd, Hit &h, TStack &st, int base,
 		TraceCounters *tc, int *overflow)
 {
 	const DevObj ob = S.objs[oi];
@@ -329,7 +346,7 @@ __device__ __forceinline__ void object_closest(const DScene &S, int oi, int ti, 
 	const float *inv = m + 12;
 	RayT r = make_ray(mul_pt(inv, wo), mul_dir(inv, wd));
 	if(ob.type == 2) {
-		if(ob.mesh_root >= 0) mesh_closest<COUNT>(S, ob.mesh_root, oi, r, h, tc, overflow);
+		if(ob.mesh_root >= 0) mesh_closest<COUNT>(S, ob.mesh_root, oi, r, h, st, base, tc, overflow);
 		return;
 	}
 	if(COUNT) tc->prims++;
@@ -338,8 +355,22 @@ __device__ __forceinline__ void object_closest(const DScene &S, int oi, int ti, 
 	if(hit) consider(h, t, oi, 0);
 }
 
-/* closest hit of a world-space segment (Scene::cast_ray, src/scene.cc:764-794),
- * front-to-back over the top-level octree with the pruning above */
+__device__ __forceinline__ bool mailbox_seen(int *mbox, int &mb_next, int oi)
+{
+	bool seen = false;
+	#pragma unroll
+	for(int k = 0; k < SRAY_MAILBOX; k++) seen |= mbox[k] == oi;
+	if(!seen) {
+		mbox[mb_next] = oi;
+		mb_next = (mb_next + 1) & (SRAY_MAILBOX - 1);
+	}
+	return seen;
+}
+
+/* closest hit of a world-space segment (Scene::cast_ray, src/scene.cc:764-794):
+ * front to back over the top-level octree with the pruning above; an object
+ * straddling several leaves gives the same closest hit every time, so each
+ * object is tested once per ray */
 template <bool COUNT>
 __device__ inline void trace_closest(const DScene &S, V3 wo, V3 wd, int time, Hit &h, TraceCounters *tc, int *overflow)
 {
@@ -350,52 +381,34 @@ __device__ inline void trace_closest(const DScene &S, V3 wo, V3 wd, int time, Hi
 	if(!S.has_scene) return;
 	int ti = time_index(S, time);
 	RayT r = make_ray(wo, wd);
-	int stk[SRAY_SCENE_STACK];
-	float stt[SRAY_SCENE_STACK];
+	int oct = octant(r);
+	TStack st;
 	int sp = 0;
 	float te;
 	int mbox[SRAY_MAILBOX];
+	#pragma unroll
 	for(int k = 0; k < SRAY_MAILBOX; k++) mbox[k] = -1;
 	int mb_next = 0;
 	if(COUNT) tc->nodes++;
-	if(!box_hit(S.snodes[0].mn, S.snodes[0].mx, r, te)) return;
-	stk[sp] = 0;
-	stt[sp] = te;
+	const DevNode &root = S.snodes[S.sroot];
+	if(!box_hit(root.mn, root.mx, r, te)) return;
+	st.node[sp] = S.sroot;
+	st.te[sp] = te;
 	sp++;
 	while(sp > 0) {
 		sp--;
-		int ni = stk[sp];
-		if(SRAY_PRUNE(stt[sp], h.t)) continue;
-		const DevNode nd = S.snodes[ni];
-		if(nd.count < 0) {
-			int ci[8];
-			float ct[8];
-			int nc = 0;
-			for(int k = 0; k < 8; k++) {
-				const DevNode ch = S.snodes[nd.first + k];
-				if(ch.count == 0) continue;
-				if(COUNT) tc->nodes++;
-				float tk;
-				if(box_hit(ch.mn, ch.mx, r, tk) && !SRAY_PRUNE(tk, h.t)) {
-					int j = nc++;
-					while(j > 0 && ct[j - 1] < tk) { ct[j] = ct[j - 1]; ci[j] = ci[j - 1]; j--; }
-					ct[j] = tk;
-					ci[j] = nd.first + k;
-				}
-			}
-			if(sp + nc > SRAY_SCENE_STACK) { *overflow = 1; nc = SRAY_SCENE_STACK - sp; }
-			for(int k = 0; k < nc; k++) { stk[sp] = ci[k]; stt[sp] = ct[k]; sp++; }
+		int ni = st.node[sp];
+		if(SRAY_PRUNE(st.te[sp], h.t)) continue;
+		const float4 *np = reinterpret_cast<const float4 *>(S.snodes + ni);
+		float4 n0 = __ldg(np), n1 = __ldg(np + 1);
+		int count = __float_as_int(n1.w), first = __float_as_int(n0.w);
+		if(count < 0) {
+			sp = push_children<COUNT>(S.snodes, first, oct, r, h.t, st, sp, SRAY_STACK / 2, tc, overflow);
 		} else {
-			for(int s = 0; s < nd.count; s++) {
-				int oi = S.sslots[nd.first + s];
-				/* an object straddling several leaves gives the same closest hit
-				 * every time: test it once per ray */
-				bool seen = false;
-				for(int k = 0; k < SRAY_MAILBOX; k++) seen |= mbox[k] == oi;
-				if(seen) continue;
-				mbox[mb_next] = oi;
-				mb_next = (mb_next + 1) & (SRAY_MAILBOX - 1);
-				object_closest<COUNT>(S, oi, ti, wo, wd, h, tc, overflow);
+			for(int s = 0; s < count; s++) {
+				int oi = __ldg(S.sslots + first + s);
+				if(mailbox_seen(mbox, mb_next, oi)) continue;
+				object_closest<COUNT>(S, oi, ti, wo, wd, h, st, sp, tc, overflow);
 			}
 		}
 	}
@@ -403,31 +416,21 @@ __device__ inline void trace_closest(const DScene &S, V3 wo, V3 wd, int time, Hi
 
 /* any hit: the reference's shadow test is cast_ray(shadow_ray) != 0
  * (src/shader.cc:266), i.e. whether any candidate intersection exists */
-__device__ inline bool mesh_any(const DScene &S, int root, const RayT &r, int *overflow)
+__device__ inline bool mesh_any(const DScene &S, int root, const RayT &r, TStack &st, int base, int *overflow)
 {
-	int stk[SRAY_MESH_STACK];
-	int sp = 0;
+	int sp = base;
 	float te;
 	const DevNode &rn = S.mnodes[root];
 	if(!box_hit(rn.mn, rn.mx, r, te)) return false;
-	stk[sp++] = root;
-	while(sp > 0) {
-		int ni = stk[--sp];
+	int oct = octant(r);
+	st.node[sp++] = root;
+	while(sp > base) {
+		int ni = st.node[--sp];
 		const float4 *np = reinterpret_cast<const float4 *>(S.mnodes + ni);
 		float4 n0 = __ldg(np), n1 = __ldg(np + 1);
 		int count = __float_as_int(n1.w), first = __float_as_int(n0.w);
 		if(count < 0) {
-			for(int k = 7; k >= 0; k--) {
-				const float4 *cp = reinterpret_cast<const float4 *>(S.mnodes + first + k);
-				float4 c0 = __ldg(cp), c1 = __ldg(cp + 1);
-				if(__float_as_int(c1.w) == 0) continue;
-				float mn[3] = {c0.x, c0.y, c0.z}, mx[3] = {c1.x, c1.y, c1.z};
-				float tk;
-				if(box_hit(mn, mx, r, tk)) {
-					if(sp >= SRAY_MESH_STACK) { *overflow = 1; return false; }
-					stk[sp++] = first + k;
-				}
-			}
+			sp = push_children<false>(S.mnodes, first, oct, r, FLT_MAX, st, sp, SRAY_STACK, nullptr, overflow);
 		} else {
 			const float4 *tp = reinterpret_cast<const float4 *>(S.mtris + first);
 			for(int s = 0; s < count; s++) {
@@ -445,41 +448,34 @@ __device__ inline bool trace_any(const DScene &S, V3 wo, V3 wd, int time, int *o
 	if(!S.has_scene) return false;
 	int ti = time_index(S, time);
 	RayT r = make_ray(wo, wd);
-	int stk[SRAY_SCENE_STACK];
+	int oct = octant(r);
+	TStack st;
 	int sp = 0;
 	int mbox[SRAY_MAILBOX];
+	#pragma unroll
 	for(int k = 0; k < SRAY_MAILBOX; k++) mbox[k] = -1;
 	int mb_next = 0;
 	float te;
-	if(!box_hit(S.snodes[0].mn, S.snodes[0].mx, r, te)) return false;
-	stk[sp++] = 0;
+	const DevNode &root = S.snodes[S.sroot];
+	if(!box_hit(root.mn, root.mx, r, te)) return false;
+	st.node[sp++] = S.sroot;
 	while(sp > 0) {
-		int ni = stk[--sp];
-		const DevNode nd = S.snodes[ni];
-		if(nd.count < 0) {
-			for(int k = 7; k >= 0; k--) {
-				const DevNode ch = S.snodes[nd.first + k];
-				if(ch.count == 0) continue;
-				float tk;
-				if(box_hit(ch.mn, ch.mx, r, tk)) {
-					if(sp >= SRAY_SCENE_STACK) { *overflow = 1; return false; }
-					stk[sp++] = nd.first + k;
-				}
-			}
+		int ni = st.node[--sp];
+		const float4 *np = reinterpret_cast<const float4 *>(S.snodes + ni);
+		float4 n0 = __ldg(np), n1 = __ldg(np + 1);
+		int count = __float_as_int(n1.w), first = __float_as_int(n0.w);
+		if(count < 0) {
+			sp = push_children<false>(S.snodes, first, oct, r, FLT_MAX, st, sp, SRAY_STACK / 2, nullptr, overflow);
 		} else {
-			for(int s = 0; s < nd.count; s++) {
-				int oi = S.sslots[nd.first + s];
-				bool seen = false;
-				for(int k = 0; k < SRAY_MAILBOX; k++) seen |= mbox[k] == oi;
-				if(seen) continue;
-				mbox[mb_next] = oi;
-				mb_next = (mb_next + 1) & (SRAY_MAILBOX - 1);
+			for(int s = 0; s < count; s++) {
+				int oi = __ldg(S.sslots + first + s);
+				if(mailbox_seen(mbox, mb_next, oi)) continue;
 				const DevObj ob = S.objs[oi];
 				const float *inv = obj_xf(S, oi, ti) + 12;
 				RayT orr = make_ray(mul_pt(inv, wo), mul_dir(inv, wd));
 				float t;
 				if(ob.type == 2) {
-					if(ob.mesh_root >= 0 && mesh_any(S, ob.mesh_root, orr, overflow)) return true;
+					if(ob.mesh_root >= 0 && mesh_any(S, ob.mesh_root, orr, st, sp, overflow)) return true;
 				} else if(ob.type == 0) {
 					if(sphere_hit(orr, ob.rad, S.eps, t)) return true;
 				} else {

@@ -635,6 +635,7 @@ void Renderer::fill_scene_desc()
 	D.snodes = snodes.as<DevNode>();
 	D.sslots = sslots.as<int>();
 	D.has_scene = built && !sc.oct.nodes.empty() && !sc.objs.empty();
+	D.sroot = scene_root;
 	D.mnodes = mnodes.as<DevNode>();
 	D.mtris = mtris.as<DevTri>();
 	D.mprim = mprim.as<int>();
@@ -706,10 +707,10 @@ int Renderer::upload_scene(cudaStream_t s)
 	int tri_cursor = 0;
 	for(size_t u = 0; u < sc.meshes.size(); u++) {
 		Mesh &m = sc.meshes[u];
-		m.node_base = (int)nodes.size();
 		m.tri_base = tri_cursor;
 		size_t s0 = slots.size();
 		flatten_octree(m.oct, nodes, slots);
+		m.node_base = m.oct.nodes.empty() ? -1 : (int)(nodes.size() - m.oct.nodes.size());
 		size_t nf = m.pos.size() / 9;
 		for(size_t k = s0; k < slots.size(); k++) {
 			int f = slots[k];
@@ -744,7 +745,7 @@ int Renderer::upload_scene(cudaStream_t s)
 		d.mesh_root = -1;
 		if(o.type == OBJ_MESH) {
 			const Mesh &m = sc.meshes[o.mesh];
-			d.mesh_root = (m.pos.empty()) ? -1 : m.node_base;
+			d.mesh_root = (m.pos.empty() || m.node_base < 0) ? -1 : m.node_base;
 			d.tri_base = m.tri_base;
 		}
 	}
@@ -795,6 +796,7 @@ int Renderer::build_frame(long bt0, long bt1, cudaStream_t s)
 	std::vector<DevNode> nodes;
 	std::vector<int> slots;
 	flatten_octree(sc.oct, nodes, slots);
+	scene_root = sc.oct.nodes.empty() ? 0 : (int)(nodes.size() - sc.oct.nodes.size());
 	int shutter = sc.cam.shutter;
 	tlo = t0 - shutter - 2;
 	int thi = t1 + shutter + 2;

@@ -94,6 +94,7 @@ struct Renderer {
 	DevBuf snodes, sslots, xf, light_pos, cam_m, projbits, coverage;
 	bool built = false;
 	int t0 = 0, t1 = 0, tlo = 0, nt = 1;
+	int scene_root = 0;
 	long frame_msec = 0;
 	bool photons_ready = false;
 	PhotonBufs caust, gi;

@@ -442,6 +442,7 @@ void Camera::matrix(int t, double m[4][4]) const
 /* ------------------------------------------------------------------ */
 Box Object::bounds(const std::vector<Mesh> &meshes, int t) const
 {
+	if(is_static) return static_box;
 	Box b;
 	double m[4][4];
 	xf.matrix(t, m);
@@ -533,10 +534,21 @@ void BuildOctree::build(const std::vector<Box> &boxes, int max_depth, int max_it
 	if((int)boxes.size() > max_items) b.subdivide(0, 0);
 }
 
+/* device child slot of the reference's child k (src/octree.inl:160-168):
+ * slot bits are x | y << 1 | z << 2 of the child's half-space */
+static const int child_slot[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+
 void flatten_octree(const BuildOctree &oct, std::vector<DevNode> &out, std::vector<int> &slots)
 {
-	size_t base = out.size();
 	if(oct.nodes.empty()) return;
+	/* pad so the root sits at index 3 mod 4: every group of 8 siblings then
+	 * starts on a 128-byte line */
+	while((out.size() & 3) != 3) {
+		DevNode pad;
+		memset(&pad, 0, sizeof pad);
+		out.push_back(pad);
+	}
+	size_t base = out.size();
 	/* breadth-first renumbering: children of a node stay consecutive */
 	std::vector<int> order;
 	order.reserve(oct.nodes.size());
@@ -547,9 +559,11 @@ void flatten_octree(const BuildOctree &oct, std::vector<DevNode> &out, std::vect
 		int n = order[q];
 		int c = oct.nodes[n].child;
 		if(c >= 0) {
+			size_t g = order.size();
+			order.resize(g + 8);
 			for(int k = 0; k < 8; k++) {
-				newidx[c + k] = (int)order.size();
-				order.push_back(c + k);
+				newidx[c + k] = (int)(g + child_slot[k]);
+				order[g + child_slot[k]] = c + k;
 			}
 		}
 	}
@@ -694,11 +708,19 @@ static void project_boxes(ProjMap *map, const Vec3 &lpos, const std::vector<Box>
  * projection-map stream of the light */
 void HostScene::build_projmaps(int t0, int t1, uint64_t seed)
 {
-	for(size_t li = 0; li < lights.size(); li++) {
+	/* each light's maps depend only on its own random stream: one thread per light */
+	std::vector<std::thread> th;
+	for(size_t li = 0; li < lights.size(); li++) th.push_back(std::thread([this, li, t0, t1, seed]() { build_light_projmaps(li, t0, t1, seed); }));
+	for(auto &t : th) t.join();
+}
+
+void HostScene::build_light_projmaps(size_t li, int t0, int t1, uint64_t seed)
+{
+	{
 		Light &L = lights[li];
 		L.pm.clear();
 		L.spm.clear();
-		if(objs.empty()) continue;
+		if(objs.empty()) return;
 		int tm[3] = {t0, t1, -1};
 		if(t0 == t1) tm[1] = -1;
 		int samples = L.type == LT_SPHERE ? 8 : 1;
@@ -706,7 +728,7 @@ void HostScene::build_projmaps(int t0, int t1, uint64_t seed)
 			std::vector<Box> boxes(objs.size()), cboxes;
 			for(size_t i = 0; i < objs.size(); i++) {
 				const Material &m = objs[i].mat >= 0 ? mats[objs[i].mat] : defmat;
-				boxes[i] = objs[i].bounds(meshes, tm[ti]);
+				boxes[i] = object_bounds(i, tm[ti]);
 				if(m.refl > 0.0 || m.refr > 0.0) cboxes.push_back(boxes[i]);
 			}
 			sray_rng s;
@@ -734,12 +756,27 @@ void HostScene::build_projmaps(int t0, int t1, uint64_t seed)
 	}
 }
 
+Box HostScene::object_bounds(size_t i, int t) const
+{
+	if(t == bt0 && i < box_t0.size()) return box_t0[i];
+	if(t == bt1 && i < box_t1.size()) return box_t1[i];
+	return objs[i].bounds(meshes, t);
+}
+
 /* Scene::build_tree (src/scene.cc:353-390) */
 void HostScene::build_tree(int t0, int t1, const sray_opts &opt)
 {
 	std::vector<Box> boxes(objs.size());
+	bt0 = t0;
+	bt1 = t1;
+	box_t0.resize(objs.size());
+	box_t1.resize(objs.size());
 	for(size_t i = 0; i < objs.size(); i++) {
-		Box s = objs[i].bounds(meshes, t0), e = t1 == t0 ? s : objs[i].bounds(meshes, t1);
+		box_t0[i] = objs[i].bounds(meshes, t0);
+		box_t1[i] = t1 == t0 ? box_t0[i] : objs[i].bounds(meshes, t1);
+	}
+	for(size_t i = 0; i < objs.size(); i++) {
+		Box s = box_t0[i], e = box_t1[i];
 		for(int k = 0; k < 3; k++) {
 			boxes[i].mn[k] = s.mn[k] < e.mn[k] ? s.mn[k] : e.mn[k];
 			boxes[i].mx[k] = s.mx[k] > e.mx[k] ? s.mx[k] : e.mx[k];
@@ -1111,6 +1148,15 @@ bool HostScene::load(const char *text, size_t len, const sray_opts &opt, std::st
 		}));
 	}
 	for(auto &t : th) t.join();
+	/* objects with at most one key per transform track have time-independent bounds */
+	for(size_t i = 0; i < objs.size(); i++) {
+		Object &o = objs[i];
+		o.is_static = false;
+		if(o.xf.pos.time.size() <= 1 && o.xf.rot.time.size() <= 1 && o.xf.scale.time.size() <= 1) {
+			o.static_box = o.bounds(meshes, 0);
+			o.is_static = true;
+		}
+	}
 	return true;
 }
 

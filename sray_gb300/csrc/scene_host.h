@@ -84,6 +84,8 @@ struct Object {
 	XForm xf;
 	double rad = 1.0, start = -1.0, end = 1.0;
 	int mesh = -1;
+	bool is_static = false;    /* every transform track has at most one key */
+	Box static_box;
 	Box bounds(const std::vector<Mesh> &meshes, int t) const;
 };
 
@@ -131,10 +133,14 @@ struct HostScene {
 	/* per-frame state */
 	BuildOctree oct;
 	double gather_dist = 0.0;
+	int bt0 = 0, bt1 = 0;
+	std::vector<Box> box_t0, box_t1;   /* object bounds at the frame's t0 / t1 */
+	Box object_bounds(size_t i, int t) const;
 
 	bool load(const char *text, size_t len, const sray_opts &opt, std::string &err);
 	void build_tree(int t0, int t1, const sray_opts &opt);
 	void build_projmaps(int t0, int t1, uint64_t seed);
+	void build_light_projmaps(size_t li, int t0, int t1, uint64_t seed);
 };
 
 /* general 4x4 inverse by the adjugate */
