@@ -39,12 +39,16 @@ static __device__ __forceinline__ int warp_alloc(int *counter, int n)
 }
 
 /* ---------------------------------------------------------------- */
-__global__ void k_camera(DScene S, const int *active, const int *n_active_p, int sample, RayQueue q, float4 *acc,
+/* primary rays of samples [s0, s0 + width) of every active pixel; the ray's
+ * accumulator slot is (active index * width + sample - s0) */
+__global__ void k_camera(DScene S, const int *active, const int *n_active_p, int s0, int width, RayQueue q, float4 *acc,
 		DevCounters *ctr)
 {
-	int n = *n_active_p;
+	int n = *n_active_p * width;
 	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		int p = active ? active[i] : i;
+		int a = i / width, j = i - a * width;
+		int p = active ? active[a] : a;
+		int sample = s0 + j;
 		int x = p % S.width, y = p / S.width;
 		sray_rng s;
 		sray_rng_init(&s, S.seed, SRAY_DOM_PIXEL, (uint32_t)p, (uint32_t)sample);
@@ -62,11 +66,11 @@ __global__ void k_camera(DScene S, const int *active, const int *n_active_p, int
 		d = mul_dir(m, d);
 		q.o[i] = make_float4(o.x, o.y, o.z, 1.0f);
 		q.d[i] = make_float4(d.x, d.y, d.z, 1.0f);
-		q.w[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-		q.meta[i] = make_int4(p, S.iter, 1, time);
+		q.w[i] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(p));
+		q.meta[i] = make_int4(i, S.iter, 1, time);
 		q.stk[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 		q.ext[i] = make_int2(sample, 0);
-		acc[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+		acc[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 	}
 	if(blockIdx.x == 0 && threadIdx.x == 0) {
 		*q.count = n;
@@ -116,15 +120,15 @@ struct ShadeOut {
 };
 
 __device__ __forceinline__ void push_child(ShadeOut &out, V3 o, V3 d, float energy, int iter, int path, int dsub,
-		const IorStack &st, float wr, float wg, float wb, int pixel, int sample, int time, int *overflow)
+		const IorStack &st, float wr, float wg, float wb, int pixel, int aslot, int sample, int time, int *overflow)
 {
 	int slot = warp_alloc(out.qo.count, 1);
 	if(slot >= out.qo.cap) { *overflow = 1; return; }
 	RayQueue &q = out.qo;
 	q.o[slot] = make_float4(o.x, o.y, o.z, energy);
 	q.d[slot] = make_float4(d.x, d.y, d.z, st.ior);
-	q.w[slot] = make_float4(wr, wg, wb, 0.0f);
-	q.meta[slot] = make_int4(pixel, iter, path, time);
+	q.w[slot] = make_float4(wr, wg, wb, __int_as_float(pixel));
+	q.meta[slot] = make_int4(aslot, iter, path, time);
 	q.stk[slot] = make_float4(st.stk[0], st.stk[1], st.stk[2], st.stk[3]);
 	q.ext[slot] = make_int2(sample | (dsub << 16), st.sp);
 }
@@ -167,7 +171,8 @@ __global__ void __launch_bounds__(128) k_shade(DScene S, RayQueue qi, const int4
 		int4 meta = qi.meta[i];
 		int2 ext = qi.ext[i];
 		int4 hv = hits[i];
-		int pixel = meta.x;
+		int aslot = meta.x;
+		int pixel = __float_as_int(w4.w);
 		int iter = meta.y, path = meta.z, time = meta.w;
 		int sample = ext.x & 0xffff;
 		int dsub = ext.x >> 16;
@@ -178,11 +183,11 @@ __global__ void __launch_bounds__(128) k_shade(DScene S, RayQueue qi, const int4
 		h.prim = hv.z;
 		h.tie = hv.w;
 		if(h.obj < 0) {
-			acc_add(acc, pixel, w4.x * S.env_col[0], w4.y * S.env_col[1], w4.z * S.env_col[2]);
-			if(depth == 0) acc[pixel].w = S.env_col[3];
+			acc_add(acc, aslot, w4.x * S.env_col[0], w4.y * S.env_col[1], w4.z * S.env_col[2]);
+			if(depth == 0) acc[aslot].w = S.env_col[3];
 			continue;
 		}
-		if(depth == 0) acc[pixel].w = 1.0f;
+		if(depth == 0) acc[aslot].w = 1.0f;
 		const DevMat &mat = mat_of(S, h.obj);
 		Surf sp;
 		surface_point(S, h, mk(o4.x, o4.y, o4.z), rd, time, sp, !mat.phong);
@@ -193,7 +198,7 @@ __global__ void __launch_bounds__(128) k_shade(DScene S, RayQueue qi, const int4
 			int tx = (int)(sp.tex[0] * 20.0f), ty = (int)(sp.tex[1] * 10.0f);
 			bool even = (tx % 2) == (ty % 2);
 			float tc[3] = {even ? 1.0f : 0.2f, 0.3f, even ? 0.2f : 1.0f};
-			acc_add(acc, pixel, w4.x * (0.1f * tc[0]), w4.y * (0.1f * tc[1]), w4.z * (0.1f * tc[2]));
+			acc_add(acc, aslot, w4.x * (0.1f * tc[0]), w4.y * (0.1f * tc[1]), w4.z * (0.1f * tc[2]));
 			for(int li = 0; li < S.nlights; li++) {
 				const DevLight &L = S.lights[li];
 				V3 lpos = light_point(S, li, time, &rng);
@@ -206,7 +211,7 @@ __global__ void __launch_bounds__(128) k_shade(DScene S, RayQueue qi, const int4
 				float ndotl = maxf_ref(dot(sp.normal, ldir), 0.0f);
 				float ndoth = maxf_ref(dot(sp.normal, hdir), 0.0f);
 				float pw = powf(ndoth, 50.0f);
-				push_shadow(out, sp.pos, sdir, time, pixel, w4.x * (ndotl * L.col[0] * tc[0] + pw * L.col[0]),
+				push_shadow(out, sp.pos, sdir, time, aslot, w4.x * (ndotl * L.col[0] * tc[0] + pw * L.col[0]),
 						w4.y * (ndotl * L.col[1] * tc[1] + pw * L.col[1]), w4.z * (ndotl * L.col[2] * tc[2] + pw * L.col[2]),
 						&overflow);
 			}
@@ -222,7 +227,7 @@ __global__ void __launch_bounds__(128) k_shade(DScene S, RayQueue qi, const int4
 		const float *kd = mat.kd, *ks = mat.ks;
 		if(iter == DIFFUSE_ITER) {
 			/* final-gather ray: radiance_est(...) * kd */
-			push_gather(out, sp.pos, normal, 1, pixel, w4.x * kd[0], w4.y * kd[1], w4.z * kd[2], &overflow);
+			push_gather(out, sp.pos, normal, 1, aslot, w4.x * kd[0], w4.y * kd[1], w4.z * kd[2], &overflow);
 			continue;
 		}
 		float energy = o4.w;
@@ -236,7 +241,7 @@ __global__ void __launch_bounds__(128) k_shade(DScene S, RayQueue qi, const int4
 		float refl_fact = mat.refl, trans_fact = mat.refr, mat_ior = mat.ior;
 		float ior = st.calc_ior(entering, mat_ior);
 		/* ambient: (env_ambient * kd) * kd */
-		acc_add(acc, pixel, w4.x * (S.env_amb[0] * kd[0] * kd[0]), w4.y * (S.env_amb[1] * kd[1] * kd[1]),
+		acc_add(acc, aslot, w4.x * (S.env_amb[0] * kd[0] * kd[0]), w4.y * (S.env_amb[1] * kd[1] * kd[1]),
 				w4.z * (S.env_amb[2] * kd[2] * kd[2]));
 		V3 vref = reflection(incident, normal);
 		for(int li = 0; li < S.nlights; li++) {
@@ -258,7 +263,7 @@ __global__ void __launch_bounds__(128) k_shade(DScene S, RayQueue qi, const int4
 					c[k] = ((ndotl * lc) * scale) * kd[k] + ((pw * lc) * scale) * ks[k];
 				}
 				if(c[0] != 0.0f || c[1] != 0.0f || c[2] != 0.0f)
-					push_shadow(out, sp.pos, sdir, time, pixel, w4.x * c[0], w4.y * c[1], w4.z * c[2], &overflow);
+					push_shadow(out, sp.pos, sdir, time, aslot, w4.x * c[0], w4.y * c[1], w4.z * c[2], &overflow);
 			}
 		}
 		/* final gather: diffuse rays end at their next hit (src/shader.cc:154-187) */
@@ -272,7 +277,7 @@ __global__ void __launch_bounds__(128) k_shade(DScene S, RayQueue qi, const int4
 				if(diff_energy > S.min_energy) {
 					float g = S.diffuse_samples > 1 ? ndotl / (float)S.diffuse_samples : ndotl;
 					push_child(out, sp.pos, dir * ray_mag, diff_energy, DIFFUSE_ITER, path * 4 + 2, k, st,
-							w4.x * kd[0] * g, w4.y * kd[1] * g, w4.z * kd[2] * g, pixel, sample, time, &overflow);
+							w4.x * kd[0] * g, w4.y * kd[1] * g, w4.z * kd[2] * g, pixel, aslot, sample, time, &overflow);
 				}
 			}
 		}
@@ -283,7 +288,7 @@ __global__ void __launch_bounds__(128) k_shade(DScene S, RayQueue qi, const int4
 		if(refl_energy > S.min_energy && iter > 0) {
 			float g = refl_fact * fres;
 			push_child(out, sp.pos, reflection(rd, normal), refl_energy, iter - 1, path * 4, 0, st,
-					w4.x * ks[0] * g, w4.y * ks[1] * g, w4.z * ks[2] * g, pixel, sample, time, &overflow);
+					w4.x * ks[0] * g, w4.y * ks[1] * g, w4.z * ks[2] * g, pixel, aslot, sample, time, &overflow);
 		}
 		float trans_energy = trans_fact * energy;
 		if(trans_energy > S.min_energy && iter > 0) {
@@ -297,9 +302,9 @@ __global__ void __launch_bounds__(128) k_shade(DScene S, RayQueue qi, const int4
 			}
 			float g = trans_fact * (1.0f - fres);
 			push_child(out, sp.pos, td, trans_energy, iter - 1, path * 4 + 1, 0, cs,
-					w4.x * ks[0] * g, w4.y * ks[1] * g, w4.z * ks[2] * g, pixel, sample, time, &overflow);
+					w4.x * ks[0] * g, w4.y * ks[1] * g, w4.z * ks[2] * g, pixel, aslot, sample, time, &overflow);
 		}
-		if(S.caust_on) push_gather(out, sp.pos, normal, 0, pixel, w4.x, w4.y, w4.z, &overflow);
+		if(S.caust_on) push_gather(out, sp.pos, normal, 0, aslot, w4.x, w4.y, w4.z, &overflow);
 	}
 	if(overflow) atomicOr(&ctr->overflow, 1);
 }
@@ -498,33 +503,41 @@ __global__ void __launch_bounds__(GATHER_WARPS * 32) k_gather(DScene S, const Ga
 	if(blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctr->rays[3], (unsigned long long)n);
 }
 
-/* end of a sample pass: variance test and framebuffer write (src/render.cc:199-244) */
-__global__ void k_finish(const int *active, const int *n_active_p, int sample, const float4 *acc, float4 *hist,
+/* end of a sample batch: the reference's stop rule applied sample by sample
+ * (src/render.cc:199-244): after sample i (counting from 1), if i >= min
+ * and i > 1 and the sample variance is below max_var the pixel stops; later
+ * samples of the batch were speculative and are discarded */
+__global__ void k_finish(const int *active, const int *n_active_p, int s0, int width, const float4 *acc, float4 *hist,
 		float4 *sums, int max_samples, int min_samples, float max_var, int *next, int *next_count, float4 *fb, int *spp)
 {
 	int n = *n_active_p;
-	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		int p = active ? active[i] : i;
-		float4 s = acc[p];
-		float4 sum = sample == 0 ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : sums[p];
-		sum.x = sum.x + s.x;
-		sum.y = sum.y + s.y;
-		sum.z = sum.z + s.z;
-		sum.w = sum.w + s.w;
-		int i1 = sample + 1;
-		bool done = i1 >= max_samples;
-		if(max_samples > 1) hist[(size_t)p * max_samples + sample] = s;
-		if(!done && i1 >= min_samples && i1 > 1) {
-			float rcp = (float)(1.0 / (double)i1);
-			float4 mean = make_float4(sum.x * rcp, sum.y * rcp, sum.z * rcp, sum.w * rcp);
-			float sq = 0.0f;
-			for(int j = 0; j < i1; j++) {
-				float4 h = hist[(size_t)p * max_samples + j];
-				float dx = mean.x - h.x, dy = mean.y - h.y, dz = mean.z - h.z, dw = mean.w - h.w;
-				sq = sq + (dx * dx + dy * dy + dz * dz + dw * dw);
+	for(int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
+		int p = active ? active[a] : a;
+		float4 sum = s0 == 0 ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : sums[p];
+		bool done = false;
+		int i1 = s0;
+		for(int j = 0; j < width && !done; j++) {
+			int sample = s0 + j;
+			float4 s = acc[(size_t)a * width + j];
+			sum.x = sum.x + s.x;
+			sum.y = sum.y + s.y;
+			sum.z = sum.z + s.z;
+			sum.w = sum.w + s.w;
+			i1 = sample + 1;
+			if(max_samples > 1) hist[(size_t)p * max_samples + sample] = s;
+			if(i1 >= max_samples) { done = true; break; }
+			if(i1 >= min_samples && i1 > 1) {
+				float rcp = (float)(1.0 / (double)i1);
+				float4 mean = make_float4(sum.x * rcp, sum.y * rcp, sum.z * rcp, sum.w * rcp);
+				float sq = 0.0f;
+				for(int k = 0; k < i1; k++) {
+					float4 h = hist[(size_t)p * max_samples + k];
+					float dx = mean.x - h.x, dy = mean.y - h.y, dz = mean.z - h.z, dw = mean.w - h.w;
+					sq = sq + (dx * dx + dy * dy + dz * dz + dw * dw);
+				}
+				float v = sq * rcp;
+				if(v < max_var) done = true;
 			}
-			float v = sq * rcp;
-			if(v < max_var) done = true;
 		}
 		if(done) {
 			double r = 1.0 / (double)i1;
@@ -561,7 +574,7 @@ __global__ void k_primary_hits(DScene S, RayQueue q, const int4 *hits, int *obj,
 	int n = *q.count;
 	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 		int4 h = hits[i];
-		int p = q.meta[i].x;
+		int p = __float_as_int(q.w[i].w);
 		obj[p] = h.y;
 		prim[p] = h.y >= 0 ? h.z : -1;
 		t[p] = h.y >= 0 ? __int_as_float(h.x) : 0.0f;
@@ -923,7 +936,8 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 	CK(hits.ensure((size_t)npix * 16), "hits");
 	CK(gq.ensure((size_t)npix * sizeof(GatherReq)), "gather queue");
 	int *cnt = counts.as<int>();
-	/* cnt[0]: queue 0 count, cnt[1]: queue 1 count, cnt[2]: gather count, cnt[3]/cnt[4]: active counts */
+	/* cnt[0]/cnt[1]: ray queue counts, cnt[2]: gather count, cnt[3]: pixels of the first batch,
+	 * cnt[5]: shadow count, cnt[6]: pixels still running after the first batch */
 	CK(cudaMemsetAsync(ctr.p, 0, sizeof(DevCounters), s), "reset counters");
 	CK(cudaMemsetAsync(counts.p, 0, 64 * sizeof(int), s), "reset counts");
 	int h_n = npix;
@@ -932,15 +946,27 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 	long long l0 = launch_count;
 	memset(&stats, 0, sizeof stats);
 	int n_active = npix;
-	for(int sample = 0; sample < maxs && n_active > 0; sample++) {
-		int cur_act = sample & 1;
-		const int *act = (maxs > 1 && sample > 0) ? active[cur_act].as<int>() : nullptr;
-		int *act_count = cnt + 3 + cur_act;
-		int *next_count = cnt + 3 + (cur_act ^ 1);
+	/* sample batches: the first covers the samples every pixel takes before
+	 * its first variance test, the second all the remaining samples of the
+	 * pixels still running (rendered speculatively, cut by k_finish) */
+	int w0 = opt.min_samples > 2 ? opt.min_samples : 2;
+	if(w0 > maxs) w0 = maxs;
+	int batch_s0[2] = {0, w0};
+	int batch_w[2] = {w0, maxs - w0};
+	for(int b = 0; b < 2 && n_active > 0 && batch_w[b] > 0; b++) {
+		int s0 = batch_s0[b], width = batch_w[b];
+		const int *act = b > 0 ? active[0].as<int>() : nullptr;
+		int *act_count = b == 0 ? cnt + 3 : cnt + 6;
+		int *next_count = b == 0 ? cnt + 6 : cnt + 7;
+		int *next_list = active[b].as<int>();
+		int n_prim = n_active * width;
+		if(ensure_queue(0, n_prim)) return SRAY_ECUDA;
+		CK(acc.ensure((size_t)n_prim * 16), "accumulator");
 		q[0].count = cnt + 0;
 		q[1].count = cnt + 1;
-		LAUNCH(*this, "camera", s, k_camera<<<grid_for(n_active, 256), 256, 0, s>>>(S, act, act_count, sample, q[0], acc.as<float4>(), ctr.as<DevCounters>()));
-		int n_rays = n_active;
+		LAUNCH(*this, "camera", s, k_camera<<<grid_for(n_prim, 256), 256, 0, s>>>(S, act, act_count, s0, width, q[0], acc.as<float4>(),
+				ctr.as<DevCounters>()));
+		int n_rays = n_prim;
 		int cur = 0;
 		for(int depth = 0; n_rays > 0; depth++) {
 			int need = n_rays * per_ray_children;
@@ -983,9 +1009,10 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			cur ^= 1;
 		}
 		CK(cudaMemsetAsync(next_count, 0, sizeof(int), s), "reset next active");
-		LAUNCH(*this, "finish", s, k_finish<<<grid_for(n_active, 256), 256, 0, s>>>(act, act_count, sample, acc.as<float4>(), hist.as<float4>(),
-				sums.as<float4>(), maxs, opt.min_samples, opt.max_var, active[cur_act ^ 1].as<int>(), next_count, fbd, spp.as<int>()));
-		stats.samples += n_active;
+		LAUNCH(*this, "finish", s, k_finish<<<grid_for(n_active, 256), 256, 0, s>>>(act, act_count, s0, width, acc.as<float4>(),
+				hist.as<float4>(), sums.as<float4>(), maxs, opt.min_samples, opt.max_var, next_list, next_count, fbd,
+				spp.as<int>()));
+		stats.samples += (int64_t)n_active * width;
 		int h_next = 0;
 		CK(cudaMemcpyAsync(&h_next, next_count, sizeof(int), cudaMemcpyDeviceToHost, s), "read active count");
 		CK(cudaStreamSynchronize(s), "sample pass");
@@ -1233,7 +1260,7 @@ int sray_gpu_primary_hits(long msec, int *obj, int *prim, float *t, unsigned cha
 	e = cudaMemcpyAsync(cnt + 3, &npix, sizeof(int), cudaMemcpyHostToDevice, s);
 	if(e != cudaSuccess) { g_err = cudaGetErrorString(e); return SRAY_ECUDA; }
 	R.q[0].count = cnt + 0;
-	k_camera<<<grid_for(npix, 256), 256, 0, s>>>(R.S, nullptr, cnt + 3, 0, R.q[0], R.acc.as<float4>(), R.ctr.as<DevCounters>());
+	k_camera<<<grid_for(npix, 256), 256, 0, s>>>(R.S, nullptr, cnt + 3, 0, 1, R.q[0], R.acc.as<float4>(), R.ctr.as<DevCounters>());
 	k_trace<false><<<grid_for(npix, 128), 128, 0, s>>>(R.S, R.q[0], R.hits.as<int4>(), R.ctr.as<DevCounters>());
 	k_primary_hits<<<grid_for(npix, 256), 256, 0, s>>>(R.S, R.q[0], R.hits.as<int4>(), obj, prim, t, tie);
 	DevCounters hc;

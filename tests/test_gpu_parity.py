@@ -91,3 +91,33 @@ def test_image_reference_range_gather(small_pair):
     img_g = g.render(0)
     img_o = o.render(0)
     assert _compare(img_g, img_o, "small 192^2 range") <= 1e-3
+
+
+def test_image_adaptive_supersampling(small_pair):
+    # jittered samples, variance stop rule evaluated sample by sample
+    g, o = small_pair(width=128, height=128, max_samples=8, max_var=0.0005)
+    img_g = g.render(0)
+    img_o = o.render(0)
+    assert _compare(img_g, img_o, "small 128^2 1-8 spp") <= 1e-3
+
+
+@pytest.fixture(scope="module")
+def production_pair(gpu_lib, oracle_lib):
+    def make(**over):
+        opts = scenegen.scene_opts("production")
+        opts.update(over)
+        path = scenegen.write_scene("production")
+        g = gpu_lib.GpuRenderer(**opts)
+        g.load(path)
+        o = oracle_lib.Oracle(fp64=False, rng_mode=1, **opts)
+        o.load(path)
+        return g, o
+    return make
+
+
+def test_image_production_reduced(production_pair):
+    # terrain + instanced icospheres, sphere lights, global and caustic k-nearest gathers
+    g, o = production_pair(width=192, height=108, caust_photons=50000, gi_photons=200000, max_samples=4)
+    img_g = g.render(0)
+    img_o = o.render(0)
+    assert _compare(img_g, img_o, "production 192x108 1-4 spp") <= 1e-3
