@@ -371,15 +371,20 @@ __device__ __forceinline__ double dist2(const float4 &p, const double q[3])
 	return dx * dx + dy * dy + dz * dz;
 }
 
-/* Iterate the photons in range of q; f(photon index, d2) for each. */
+/* The (at most 3x3x3) cells overlapping the query cube are dealt one per
+ * lane; each lane visits the photons of its cell and calls f(photon, d2)
+ * for those within range. */
 template <class F>
 __device__ __forceinline__ void for_range(const DPhotonMap &M, const GatherCells &gc, const double q[3], double r2, int lane, F f)
 {
-	for(int z = gc.lo[2]; z <= gc.hi[2]; z++)
-	for(int y = gc.lo[1]; y <= gc.hi[1]; y++)
-	for(int x = gc.lo[0]; x <= gc.hi[0]; x++) {
-		uint2 c = M.cells[((size_t)z * M.dims[1] + y) * M.dims[0] + x];
-		for(unsigned j = c.x + lane; j < c.y; j += 32) {
+	int nx = gc.hi[0] - gc.lo[0] + 1, ny = gc.hi[1] - gc.lo[1] + 1, nz = gc.hi[2] - gc.lo[2] + 1;
+	int ncell = nx * ny * nz;
+	for(int c = lane; c < ncell; c += 32) {
+		int cx = c % nx, t = c / nx;
+		int cy = t % ny, cz = t / ny;
+		uint2 cr = __ldg(reinterpret_cast<const uint2 *>(M.cells) +
+				((size_t)(gc.lo[2] + cz) * M.dims[1] + (gc.lo[1] + cy)) * M.dims[0] + (gc.lo[0] + cx));
+		for(unsigned j = cr.x; j < cr.y; j++) {
 			float4 p = __ldg(reinterpret_cast<const float4 *>(M.ph + j));
 			double d2 = dist2(p, q);
 			if(d2 <= r2) f(j, d2);
@@ -403,7 +408,7 @@ __device__ __forceinline__ void photon_term(const DevPhoton *ph, int j, int kind
 }
 
 /* estimate of one query by one full warp; returns the rgb estimate in all lanes */
-__device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *keys, float out[3])
+__device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *keys, int *kcount, float out[3])
 {
 	const DPhotonMap &M = kind == 0 ? S.caust : S.gi;
 	int lane = threadIdx.x & 31;
@@ -425,9 +430,7 @@ __device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *ke
 	} else {
 		/* k nearest within the radius cap: select the k-th smallest
 		 * float-rounded squared distance by a bitwise radix search */
-		__shared__ int kcount[GATHER_WARPS];
-		int w = threadIdx.x >> 5;
-		if(lane == 0) kcount[w] = 0;
+		if(lane == 0) *kcount = 0;
 		__syncwarp();
 		unsigned maxkey = 0;
 		int ncand = 0;
@@ -435,7 +438,7 @@ __device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *ke
 			unsigned key = __float_as_uint((float)d2);
 			maxkey = key > maxkey ? key : maxkey;
 			ncand++;
-			int slot = atomicAdd(&kcount[w], 1);
+			int slot = atomicAdd(kcount, 1);
 			if(slot < KEY_CAP) keys[slot] = key;
 		});
 		__syncwarp();
@@ -447,8 +450,7 @@ __device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *ke
 			unsigned prefix = 0;
 			int remaining = M.k;
 			for(int bit = 31; bit >= 0; bit--) {
-				unsigned hmask = ~((1u << bit) - 1u) & 0xffffffffu;
-				if(bit == 31) hmask = 0x80000000u;
+				unsigned hmask = bit == 31 ? 0x80000000u : (~((1u << bit) - 1u));
 				int c0 = 0;
 				if(cached) {
 					for(int j = lane; j < ncand; j += 32) if((keys[j] & hmask) == prefix) c0++;
@@ -488,6 +490,7 @@ __global__ void __launch_bounds__(GATHER_WARPS * 32) k_gather(DScene S, const Ga
 		float4 *acc, DevCounters *ctr)
 {
 	__shared__ unsigned keys[GATHER_WARPS][KEY_CAP];
+	__shared__ int kcount[GATHER_WARPS];
 	int n = *gq_count;
 	int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	int gw = blockIdx.x * GATHER_WARPS + w, nw = gridDim.x * GATHER_WARPS;
@@ -496,7 +499,7 @@ __global__ void __launch_bounds__(GATHER_WARPS * 32) k_gather(DScene S, const Ga
 		int kind = __float_as_int(g.a.w);
 		int pixel = __float_as_int(g.b.w);
 		float est[3];
-		gather_one(S, kind, mk(g.a.x, g.a.y, g.a.z), mk(g.b.x, g.b.y, g.b.z), keys[w], est);
+		gather_one(S, kind, mk(g.a.x, g.a.y, g.a.z), mk(g.b.x, g.b.y, g.b.z), keys[w], &kcount[w], est);
 		if(lane == 0) acc_add(acc, pixel, g.w.x * est[0], g.w.y * est[1], g.w.z * est[2]);
 		__syncwarp();
 	}

@@ -670,6 +670,48 @@ void ProjMap::set_all(bool v) { std::fill(cells.begin(), cells.end(), v ? 1 : 0)
 void ProjMap::clear() { set_all(false); }
 double ProjMap::get_coverage() const { return coverage < 0.0 ? 0.0 : (coverage > 1.0 ? 1.0 : coverage); }
 
+/* Candidate columns/rows of the 64x32 grid for one box: every cell with a
+ * corner inside the box's bounding sphere (seen from the light) lies in the
+ * spherical cap of angular radius t around the sphere's direction, since the
+ * corner test |lpos + c d - ctr|^2 <= r^2 with |c| = 1, d = |ctr - lpos| is
+ * c . v^ >= 1 - r^2 / (2 d^2).  The cap is bounded in colatitude by t and in
+ * azimuth by asin(sin t / sin phi); one cell and 0.02 rad of margin are added,
+ * and the exact corner test of the reference decides inside the candidates. */
+static bool cap_candidates(const double v[3], double objdist, double rad_sq, int *vc0, int *vc1, bool cols[64])
+{
+	double cos_t = 1.0 - rad_sq / (2.0 * objdist * objdist);
+	if(cos_t <= -1.0 + 1e-9) return false;
+	double t = acos(cos_t < 1.0 ? cos_t : 1.0) + 0.02;
+	double phi0 = acos(v[1] / objdist);
+	double theta0 = atan2(v[2], v[0]);
+	if(theta0 < 0.0) theta0 += 2.0 * M_PI;
+	double dv = M_PI / 32.0, du = 2.0 * M_PI / 64.0;
+	double plo = phi0 - t, phi_hi = phi0 + t;
+	int a = (int)floor(plo / dv) - 1, b = (int)floor(phi_hi / dv) + 1;
+	*vc0 = a < 0 ? 0 : a;
+	*vc1 = b > 31 ? 31 : b;
+	if(plo <= 0.0 || phi_hi >= M_PI) {
+		for(int k = 0; k < 64; k++) cols[k] = true;
+		return true;
+	}
+	double smin = sin(plo) < sin(phi_hi) ? sin(plo) : sin(phi_hi);
+	double st = sin(t);
+	if(st >= smin) {
+		for(int k = 0; k < 64; k++) cols[k] = true;
+		return true;
+	}
+	double dmax = asin(st / smin) + 0.02;
+	for(int k = 0; k < 64; k++) cols[k] = false;
+	int u0 = (int)floor((theta0 - dmax) / du) - 1, u1 = (int)floor((theta0 + dmax) / du) + 1;
+	if(u1 - u0 >= 63) {
+		for(int k = 0; k < 64; k++) cols[k] = true;
+		return true;
+	}
+	for(int u = u0; u <= u1; u++) cols[((u % 64) + 64) % 64] = true;
+	return true;
+}
+
+/* ::build_projmap (src/light.cc:392-432) */
 static void project_boxes(ProjMap *map, const Vec3 &lpos, const std::vector<Box> &boxes)
 {
 	for(size_t i = 0; i < boxes.size(); i++) {
@@ -686,18 +728,21 @@ static void project_boxes(ProjMap *map, const Vec3 &lpos, const std::vector<Box>
 		int uc, vc;
 		map->cell_from_dir(v, &uc, &vc);
 		map->set_cell(uc, vc, true);
-		int num = map->udiv * map->vdiv;
-		for(int j = 0; j < num; j++) {
-			uc = j % map->udiv;
-			vc = j / map->udiv;
-			for(int k = 0; k < 4; k++) {
-				double cd[3];
-				map->corner_dir(uc, vc, k, cd);
-				double px = lpos.x + cd[0] * objdist, py = lpos.y + cd[1] * objdist, pz = lpos.z + cd[2] * objdist;
-				double dx = px - ctr.x, dy = py - ctr.y, dz = pz - ctr.z;
-				if(dx * dx + dy * dy + dz * dz <= rad_sq) {
-					map->set_cell(uc, vc, true);
-					break;
+		int vc0 = 0, vc1 = map->vdiv - 1;
+		bool cols[64];
+		bool limited = map->udiv == 64 && map->vdiv == 32 && objdist > 0.0 && cap_candidates(v, objdist, rad_sq, &vc0, &vc1, cols);
+		for(int row = vc0; row <= vc1; row++) {
+			for(int col = 0; col < map->udiv; col++) {
+				if(limited && !cols[col]) continue;
+				for(int k = 0; k < 4; k++) {
+					double cd[3];
+					map->corner_dir(col, row, k, cd);
+					double px = lpos.x + cd[0] * objdist, py = lpos.y + cd[1] * objdist, pz = lpos.z + cd[2] * objdist;
+					double dx = px - ctr.x, dy = py - ctr.y, dz = pz - ctr.z;
+					if(dx * dx + dy * dy + dz * dz <= rad_sq) {
+						map->set_cell(col, row, true);
+						break;
+					}
 				}
 			}
 		}
