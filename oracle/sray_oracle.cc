@@ -116,7 +116,8 @@ struct XNode {
 
 /* src/xmltree.c:51-95: a value starting with a digit (or sign + digit) is
  * numeric: FLT if it contains '.', else INT; with more than one
- * whitespace-separated number it becomes a VEC, padded with 1.0 */
+ * whitespace-separated number it becomes a VEC, padded with 1.0.  The
+ * numbers are kept as float (struct xml_attr, src/xmltree.h:31-33). */
 static void type_attr(XAttr &a)
 {
 	const char *val = a.str.c_str();
@@ -127,12 +128,12 @@ static void type_attr(XAttr &a)
 	if(isdigit((unsigned char)val[0]) || ((val[0] == '+' || val[0] == '-') && isdigit((unsigned char)val[1]))) {
 		a.type = strchr(val, '.') ? AT_FLT : AT_INT;
 		a.ival = atoi(val);
-		a.fval = atof(val);
+		a.fval = (float)atof(val);
 		a.vval[0] = a.vval[1] = a.vval[2] = a.vval[3] = 1.0;
 		int i;
 		for(i = 0; i < 4; i++) {
 			if(!*val) break;
-			a.vval[i] = atof(val);
+			a.vval[i] = (float)atof(val);
 			while(*val && !isspace((unsigned char)*val)) val++;
 			while(*val && isspace((unsigned char)*val)) val++;
 		}

@@ -93,7 +93,8 @@ struct Doc {
 		return o;
 	}
 
-	/* xml_create_attr typing (src/xmltree.c:75-93) */
+	/* xml_create_attr typing (src/xmltree.c:75-93); numbers are stored as
+	 * float, as struct xml_attr holds them (src/xmltree.h:31-33) */
 	static bool typed(const XAttr *a, Typed *t)
 	{
 		if(!a) return false;
@@ -106,12 +107,12 @@ struct Doc {
 		if(isdigit((unsigned char)val[0]) || ((val[0] == '+' || val[0] == '-') && isdigit((unsigned char)val[1]))) {
 			t->type = strchr(val, '.') ? T_FLT : T_INT;
 			t->ival = atoi(val);
-			t->fval = strtod(val, 0);
+			t->fval = (float)strtod(val, 0);
 			t->vval[0] = t->vval[1] = t->vval[2] = t->vval[3] = 1.0;
 			int i;
 			for(i = 0; i < 4; i++) {
 				if(!*val) break;
-				t->vval[i] = strtod(val, 0);
+				t->vval[i] = (float)strtod(val, 0);
 				while(*val && !isspace((unsigned char)*val)) val++;
 				while(*val && isspace((unsigned char)*val)) val++;
 			}
@@ -921,7 +922,7 @@ struct Loader {
 		const char *q = buf;
 		for(i = 0; i < 4; i++) {
 			if(!*q) break;
-			vv[i] = strtod(q, 0);
+			vv[i] = (float)strtod(q, 0);
 			while(*q && !isspace((unsigned char)*q)) q++;
 			while(*q && isspace((unsigned char)*q)) q++;
 		}
