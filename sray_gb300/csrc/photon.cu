@@ -468,7 +468,8 @@ int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored)
 	const Box &rb = R.sc.oct.nodes[0].box;
 	int k = global ? opt.gi_k : opt.caust_k;
 	double rad = k > 0 ? (double)opt.gather_rcap : R.sc.gather_dist;
-	double cell = rad > 0.0 ? rad : 1.0;
+	/* cells twice the gather radius: a query cube overlaps at most 2x2x2 */
+	double cell = rad > 0.0 ? 2.0 * rad : 1.0;
 	double ext[3];
 	for(int a = 0; a < 3; a++) ext[a] = rb.mx[a] - rb.mn[a];
 	int dims[3];

@@ -371,23 +371,53 @@ __device__ __forceinline__ double dist2(const float4 &p, const double q[3])
 	return dx * dx + dy * dy + dz * dz;
 }
 
-/* The (at most 3x3x3) cells overlapping the query cube are dealt one per
- * lane; each lane visits the photons of its cell and calls f(photon, d2)
- * for those within range. */
+/* The cells overlapping the query cube (at most 2x2x2: cells are twice the
+ * gather radius) are looked up by the first lanes; the warp then strides
+ * over the concatenation of their photon runs, so every lane tests one
+ * photon per step whatever the cell occupancy.  f(photon, d2) is called for
+ * the photons within range. */
 template <class F>
 __device__ __forceinline__ void for_range(const DPhotonMap &M, const GatherCells &gc, const double q[3], double r2, int lane, F f)
 {
 	int nx = gc.hi[0] - gc.lo[0] + 1, ny = gc.hi[1] - gc.lo[1] + 1, nz = gc.hi[2] - gc.lo[2] + 1;
 	int ncell = nx * ny * nz;
-	for(int c = lane; c < ncell; c += 32) {
-		int cx = c % nx, t = c / nx;
-		int cy = t % ny, cz = t / ny;
-		uint2 cr = __ldg(reinterpret_cast<const uint2 *>(M.cells) +
-				((size_t)(gc.lo[2] + cz) * M.dims[1] + (gc.lo[1] + cy)) * M.dims[0] + (gc.lo[0] + cx));
-		for(unsigned j = cr.x; j < cr.y; j++) {
-			float4 p = __ldg(reinterpret_cast<const float4 *>(M.ph + j));
-			double d2 = dist2(p, q);
-			if(d2 <= r2) f(j, d2);
+	for(int c0 = 0; c0 < ncell; c0 += 32) {
+		int c = c0 + lane;
+		unsigned first = 0, cnt = 0;
+		if(c < ncell) {
+			int cx = c % nx, t = c / nx;
+			int cy = t % ny, cz = t / ny;
+			uint2 cr = __ldg(reinterpret_cast<const uint2 *>(M.cells) +
+					((size_t)(gc.lo[2] + cz) * M.dims[1] + (gc.lo[1] + cy)) * M.dims[0] + (gc.lo[0] + cx));
+			first = cr.x;
+			cnt = cr.y - cr.x;
+		}
+		/* inclusive prefix of the run lengths over the lanes */
+		unsigned incl = cnt;
+		for(int o = 1; o < 32; o <<= 1) {
+			unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
+			if(lane >= o) incl += v;
+		}
+		unsigned total = __shfl_sync(0xffffffffu, incl, 31);
+		unsigned excl = incl - cnt;
+		int nl = min(32, ncell - c0);
+		for(unsigned base = 0; base < total; base += 32) {
+			unsigned v = base + lane;
+			/* run holding virtual index v: the last lane whose exclusive prefix <= v
+			 * (all lanes take part in the shuffles, so the loop stays uniform) */
+			int owner = 0;
+			for(int k = 1; k < nl; k++) {
+				unsigned ek = __shfl_sync(0xffffffffu, excl, k);
+				if(ek <= v) owner = k;
+			}
+			unsigned fo = __shfl_sync(0xffffffffu, first, owner);
+			unsigned eo = __shfl_sync(0xffffffffu, excl, owner);
+			if(v < total) {
+				unsigned j = fo + (v - eo);
+				float4 p = __ldg(reinterpret_cast<const float4 *>(M.ph + j));
+				double d2 = dist2(p, q);
+				if(d2 <= r2) f(j, d2);
+			}
 		}
 	}
 }
