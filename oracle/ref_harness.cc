@@ -27,6 +27,7 @@
 #include "sray_rng.h"
 
 void shim_rng_select(sray_rng *s);
+extern "C" int shim_rand(void);   /* rand() of the reference's sources */
 
 static uint64_t g_seed;
 
@@ -102,7 +103,7 @@ int main(int argc, char **argv)
 					sray_rng s;
 					sray_rng_init(&s, g_seed, global ? SRAY_DOM_GLOBAL : SRAY_DOM_CAUST, (uint32_t)j, (uint32_t)li);
 					shim_rng_select(&s);
-					int ms = t0 == t1 ? (int)t0 : (int)(rand() % (t1 - t0) + t0);
+					int ms = t0 == t1 ? (int)t0 : (int)(shim_rand() % (t1 - t0) + t0);
 					Photon p = lights[li]->gen_photon(ms, global ? SAMPLE_OBJ : SAMPLE_SPEC_OBJ);
 					Ray ray;
 					ray.origin = p.pos;

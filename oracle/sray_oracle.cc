@@ -404,7 +404,7 @@ struct XForm {
 			rtrack.set_key(msec, q);
 		}
 		if((a = node.get("axisrot")) && a->type == AT_VEC) {
-			double ang = a->vval[0] * (M_PI / 180.0);
+			double ang = (a->vval[0] * M_PI) / 180.0;
 			double axis[3] = {a->vval[1], a->vval[2], a->vval[3]};
 			Quat q;
 			vmc_quat_axis_angle(q.q, axis, ang);
@@ -999,7 +999,7 @@ static bool load_scene(Scene &sc, const sray_opts &opt, const char *text, size_t
 				c.txf.strack.set_key(0, V3d(0, 0, 0));
 			} else { err = "invalid camera: unknown type: " + a->str; return false; }
 			if((a = n.get("shutter"))) c.shutter = (int)a->fval;
-			if((a = n.get("fov")) && (a->type == AT_FLT || a->type == AT_INT)) c.vfov = a->fval * (M_PI / 180.0);
+			if((a = n.get("fov")) && (a->type == AT_FLT || a->type == AT_INT)) c.vfov = (a->fval * M_PI) / 180.0;
 			bool have_target = false;
 			for(size_t j = 0; j < n.chld.size(); j++) {
 				const XNode &ch = n.chld[j];
@@ -2144,6 +2144,9 @@ template <class R> struct Frame : FrameBase {
 		L.pm.clear();
 		L.spm.clear();
 		int samples = L.type == LT_SPHERE ? 8 : 1;
+		/* one stream per light, drawn in order over both shutter ends */
+		sray_rng s;
+		sray_rng_init(&s, opt.seed, SRAY_DOM_PROJMAP, (uint32_t)li, 0);
 		for(int tidx = 0; tm[tidx] != -1 && tidx < 2; tidx++) {
 			std::vector<Box> boxes(msc.objs.size()), cboxes;
 			for(size_t i = 0; i < msc.objs.size(); i++) {
@@ -2153,8 +2156,6 @@ template <class R> struct Frame : FrameBase {
 				boxes[i] = o.bounds(tm[tidx]);
 				if(spec) cboxes.push_back(boxes[i]);
 			}
-			sray_rng s;
-			sray_rng_init(&s, opt.seed, SRAY_DOM_PROJMAP, (uint32_t)li, (uint32_t)tidx);
 			for(int k = 0; k < samples; k++) {
 				V3d lpos = L.xf.position(tm[tidx]);
 				if(L.type == LT_SPHERE) {

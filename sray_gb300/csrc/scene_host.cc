@@ -770,6 +770,9 @@ void HostScene::build_light_projmaps(size_t li, int t0, int t1, uint64_t seed)
 		int tm[3] = {t0, t1, -1};
 		if(t0 == t1) tm[1] = -1;
 		int samples = L.type == LT_SPHERE ? 8 : 1;
+		/* one stream per light, drawn in order over both shutter ends */
+		sray_rng s;
+		sray_rng_init(&s, seed, SRAY_DOM_PROJMAP, (uint32_t)li, 0);
 		for(int ti = 0; ti < 2 && tm[ti] != -1; ti++) {
 			std::vector<Box> boxes(objs.size()), cboxes;
 			for(size_t i = 0; i < objs.size(); i++) {
@@ -777,8 +780,6 @@ void HostScene::build_light_projmaps(size_t li, int t0, int t1, uint64_t seed)
 				boxes[i] = object_bounds(i, tm[ti]);
 				if(m.refl > 0.0 || m.refr > 0.0) cboxes.push_back(boxes[i]);
 			}
-			sray_rng s;
-			sray_rng_init(&s, seed, SRAY_DOM_PROJMAP, (uint32_t)li, (uint32_t)ti);
 			for(int k = 0; k < samples; k++) {
 				Vec3 lp = L.xf.position(tm[ti]);
 				if(L.type == LT_SPHERE) {
@@ -872,7 +873,7 @@ struct Loader {
 			set_key(xf.rot, msec, q);
 		}
 		if(Doc::typed(d.attr(n, "axisrot"), &t) && t.type == T_VEC) {
-			double ang = t.vval[0] * (M_PI / 180.0), half = ang * 0.5, sn = sin(half);
+			double ang = (t.vval[0] * M_PI) / 180.0, half = ang * 0.5, sn = sin(half);
 			Quat q = {cos(half), t.vval[1] * sn, t.vval[2] * sn, t.vval[3] * sn};
 			set_key(xf.rot, msec, q);
 		}
@@ -1107,7 +1108,7 @@ struct Loader {
 			set_key(c.txf.scale, 0, Vec3(0, 0, 0));
 		} else { err = "invalid camera: unknown type: " + t.str; return false; }
 		if(Doc::typed(d.attr(n, "shutter"), &t)) c.shutter = (int)t.fval;
-		if(Doc::typed(d.attr(n, "fov"), &t) && (t.type == T_FLT || t.type == T_INT)) c.vfov = t.fval * (M_PI / 180.0);
+		if(Doc::typed(d.attr(n, "fov"), &t) && (t.type == T_FLT || t.type == T_INT)) c.vfov = (t.fval * M_PI) / 180.0;
 		int target = -1;
 		for(int ch = d.nodes[n].first_child; ch >= 0; ch = d.nodes[ch].next) {
 			if(d.is(ch, "xform")) load_xform(ch, c.xf);

@@ -21,7 +21,7 @@ import os
 
 import numpy as np
 
-__all__ = ["icosphere", "value_noise_height", "small_scene", "production_scene",
+__all__ = ["icosphere", "value_noise_height", "small_scene", "production_scene", "feature_scene",
            "scene_opts", "write_scene", "CONFIGS"]
 
 
@@ -261,6 +261,44 @@ def production_scene(seed=0x5EED0002, grid=(1000, 500), extent=(100.0, 50.0), n_
     return "".join(out)
 
 
+def feature_scene(seed=0x5EED0003):
+    """A small scene touching the reference's less common paths: sphere and
+    box lights, a default (shade_undef) material, a cylinder, a mirror and a
+    glass sphere, a two-key linear motion track, a target camera."""
+    rng = np.random.default_rng(seed)
+    out = ["<?xml version=\"1.0\"?>\n<scene>\n"]
+    out.append('<env ambient="0.1" bgcolor="0.2 0.25 0.3" ior="1.0"/>\n')
+    _material(out, "floor", (0.7, 0.65, 0.6), ks=0.2, shin=12.0)
+    _material(out, "mirror", (0.2, 0.2, 0.2), ks=1.0, shin=90.0, refl=0.9)
+    _material(out, "glass", (0.05, 0.05, 0.05), ks=1.0, shin=90.0, refr=1.0, ior=1.45)
+    _material(out, "red", (0.8, 0.2, 0.15), ks=0.5, shin=25.0)
+    out.append('<material name="plain"/>\n')
+    g = 8.0
+    gv = np.array([[-g, 0, -g], [g, 0, -g], [g, 0, g], [-g, 0, g]], dtype=np.float32)
+    gf = np.array([[0, 2, 1], [0, 3, 2]], dtype=np.int32)
+    _mesh_xml(out, "floor", "floor", gv, gf)
+    out.append('<object type="sphere" name="m">\n<matref name="mirror"/>\n%s<sphere rad="1.0"/>\n</object>\n'
+               % _xform(pos=(-1.5, 1.0, 0.0)))
+    out.append('<object type="sphere" name="g">\n<matref name="glass"/>\n%s<sphere rad="0.8"/>\n</object>\n'
+               % _xform(pos=(1.2, 0.8, 1.0)))
+    out.append('<object type="sphere" name="mover">\n<matref name="red"/>\n%s%s<sphere rad="0.5"/>\n</object>\n'
+               % (_xform(pos=(0.0, 0.5, -2.0), time=0), _xform(pos=(0.6, 0.5, -2.0), time=40)))
+    out.append('<object type="cylinder" name="c">\n<matref name="plain"/>\n%s'
+               '<cylinder rad="0.4" start="0.0" end="1.5"/>\n</object>\n' % _xform(pos=(2.5, 0.0, -1.5)))
+    iv, ifc = icosphere(2)
+    _mesh_xml(out, "ico", "red", iv, ifc, normals=iv,
+              xform=_xform(pos=(-2.6, 0.7, 2.2), scale=(0.7, 0.7, 0.7), axisrot=(30.0, 0.0, 1.0, 0.0)))
+    out.append('<light type="sphere" color="0.8 0.75 0.7">\n%s<sphere rad="0.6"/>\n</light>\n'
+               % _xform(pos=(0.5, 6.0, 2.0)))
+    out.append('<light type="box" color="0.3">\n%s<aabox min="-0.5 -0.1 -0.5" max="0.5 0.1 0.5"/>\n</light>\n'
+               % _xform(pos=(-3.0, 5.0, -1.0)))
+    out.append('<camera type="target" fov="45.0">\n%s<target>\n%s</target>\n</camera>\n'
+               % (_xform(pos=(0.3, 4.5, 9.0)), _xform(pos=(0.0, 0.6, 0.0))))
+    out.append("</scene>\n")
+    del rng
+    return "".join(out)
+
+
 # option sets (sray_opts fields) of the benchmark configurations
 CONFIGS = {
     "small": dict(width=512, height=512, min_samples=1, max_samples=1, iter=5,
@@ -280,7 +318,7 @@ def scene_opts(name, **over):
 
 def write_scene(name, cache_dir=None, **kw):
     """Generate (or reuse from cache_dir) the XML of scene `name`; returns the path."""
-    gen = {"small": small_scene, "production": production_scene}[name]
+    gen = {"small": small_scene, "production": production_scene, "feature": feature_scene}[name]
     key = hashlib.sha1(repr((name, sorted(kw.items()), 3)).encode()).hexdigest()[:12]
     cache_dir = cache_dir or os.environ.get("SRAY_SCENE_CACHE", "/tmp/sray_scenes")
     os.makedirs(cache_dir, exist_ok=True)
