@@ -130,6 +130,14 @@ int sray_gpu_cast_rays(int n, const float *orig, const float *dir, const int *ti
  * width*height entries).  Parity probe for src/camera.cc:119-142 + cast_ray. */
 int sray_gpu_primary_hits(long msec, int *obj, int *prim, float *t, unsigned char *tie, void *stream);
 
+/* Photon-map estimates at `n` caller-given points of the current frame's
+ * maps: which = 0 is PhotonMap::irradiance_est on the caustic map
+ * (src/pmap.cc:109-139), 1 is PhotonMap::radiance_est on the global map
+ * (src/pmap.cc:143-178), with the gather radius / k-nearest options of the
+ * frame.  pos and norm are device arrays of n*3 floats, out receives n*3
+ * floats (rgb).  The maps must have been built (sray_gpu_shoot_photons). */
+int sray_gpu_photon_gather(int which, int n, const float *pos, const float *norm, float *out, void *stream);
+
 /* Copy the stored photons of map `which` (0 = caustic, 1 = global) to host
  * memory as 16 floats each: pos xyz, dir xyz, norm xyz, power rgba, and
  * three unused.  `cap` is the capacity in photons; returns the count through

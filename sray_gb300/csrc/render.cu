@@ -536,6 +536,40 @@ __global__ void __launch_bounds__(GATHER_WARPS * 32) k_gather(DScene S, const Ga
 	if(blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctr->rays[3], (unsigned long long)n);
 }
 
+/* gathers at caller-given points: requests packed from the caller's arrays,
+ * one warp per request, the estimate written to out[3 * i] */
+__global__ void k_pack_gather(int kind, int n, const float *pos, const float *norm, GatherReq *gq)
+{
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		GatherReq g;
+		g.a = make_float4(pos[i * 3], pos[i * 3 + 1], pos[i * 3 + 2], __int_as_float(kind));
+		g.b = make_float4(norm[i * 3], norm[i * 3 + 1], norm[i * 3 + 2], __int_as_float(i));
+		g.w = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+		gq[i] = g;
+	}
+}
+
+__global__ void __launch_bounds__(GATHER_WARPS * 32) k_gather_points(DScene S, const GatherReq *gq, int n, float *out)
+{
+	__shared__ unsigned keys[GATHER_WARPS][KEY_CAP];
+	__shared__ int kcount[GATHER_WARPS];
+	int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	int gw = blockIdx.x * GATHER_WARPS + w, nw = gridDim.x * GATHER_WARPS;
+	for(int r = gw; r < n; r += nw) {
+		GatherReq g = gq[r];
+		int kind = __float_as_int(g.a.w);
+		int idx = __float_as_int(g.b.w);
+		float est[3];
+		gather_one(S, kind, mk(g.a.x, g.a.y, g.a.z), mk(g.b.x, g.b.y, g.b.z), keys[w], &kcount[w], est);
+		if(lane == 0) {
+			out[idx * 3] = est[0];
+			out[idx * 3 + 1] = est[1];
+			out[idx * 3 + 2] = est[2];
+		}
+		__syncwarp();
+	}
+}
+
 /* end of a sample batch: the reference's stop rule applied sample by sample
  * (src/render.cc:199-244): after sample i (counting from 1), if i >= min
  * and i > 1 and the sample variance is below max_var the pixel stops; later
@@ -1301,6 +1335,24 @@ int sray_gpu_primary_hits(long msec, int *obj, int *prim, float *t, unsigned cha
 	if(e == cudaSuccess) e = cudaStreamSynchronize(s);
 	if(e != cudaSuccess) { g_err = cudaGetErrorString(e); return SRAY_ECUDA; }
 	if(hc.overflow) { g_err = "traversal stack overflow"; return SRAY_EDEVICE; }
+	return 0;
+}
+
+int sray_gpu_photon_gather(int which, int n, const float *pos, const float *norm, float *out, void *stream)
+{
+	NEED_CTX();
+	Renderer &R = *g_R;
+	if(!R.photons_ready) { g_err = "photon maps not built"; return SRAY_ESTATE; }
+	if((which != 0 && which != 1) || n < 0 || (n > 0 && (!pos || !norm || !out))) { g_err = "bad arguments"; return SRAY_EINVAL; }
+	if(n == 0) return 0;
+	cudaStream_t s = as_stream(stream);
+	cudaError_t e = R.gq.ensure((size_t)n * sizeof(GatherReq));
+	if(e != cudaSuccess) { g_err = cudaGetErrorString(e); return SRAY_ECUDA; }
+	k_pack_gather<<<grid_for(n, 256), 256, 0, s>>>(which, n, pos, norm, R.gq.as<GatherReq>());
+	k_gather_points<<<grid_for(n, GATHER_WARPS), GATHER_WARPS * 32, 0, s>>>(R.S, R.gq.as<GatherReq>(), n, out);
+	e = cudaStreamSynchronize(s);
+	if(e == cudaSuccess) e = cudaGetLastError();
+	if(e != cudaSuccess) { g_err = cudaGetErrorString(e); return SRAY_ECUDA; }
 	return 0;
 }
 

@@ -121,3 +121,69 @@ def test_image_production_reduced(production_pair):
     img_g = g.render(0)
     img_o = o.render(0)
     assert _compare(img_g, img_o, "production 192x108 1-4 spp") <= 1e-3
+
+
+def test_cast_rays_kats(gpu_lib, oracle_lib):
+    import kat_scene
+    g = gpu_lib.GpuRenderer(width=32, height=32)
+    g.load_xml(kat_scene.XML)
+    g.build(0, 0)
+    orig, dirs = kat_scene.rays()
+    n = len(orig)
+    o_t = torch.tensor(orig, dtype=torch.float32, device="cuda")
+    d_t = torch.tensor(dirs, dtype=torch.float32, device="cuda")
+    tm = torch.zeros(n, dtype=torch.int32, device="cuda")
+    obj = torch.empty(n, dtype=torch.int32, device="cuda")
+    prim = torch.empty(n, dtype=torch.int32, device="cuda")
+    t = torch.empty(n, dtype=torch.float32, device="cuda")
+    tie = torch.empty(n, dtype=torch.uint8, device="cuda")
+    g.cast_rays(o_t, d_t, tm, obj, prim, t, tie)
+    torch.cuda.synchronize()
+    bad = kat_scene.check(obj.cpu().numpy(), prim.cpu().numpy(), t.cpu().numpy(), tie.cpu().numpy(), 1e-6)
+    assert not bad, bad
+    # and bit-exact against the FP32 oracle on the same rays
+    o = oracle_lib.Oracle(fp64=False, rng_mode=1, width=32, height=32)
+    o.load_xml(kat_scene.XML)
+    oo, op, ot, _ = o.cast_rays(orig.astype(np.float32).astype(np.float64), dirs.astype(np.float32).astype(np.float64))
+    assert np.array_equal(oo, obj.cpu().numpy()) and np.array_equal(op, prim.cpu().numpy())
+    assert np.array_equal(ot.astype(np.float32), t.cpu().numpy())
+
+
+def test_feature_scene_motion_blur_area_lights(gpu_lib, oracle_lib):
+    # sphere + box lights with 2 shadow samples, global photons with 2 final-gather
+    # rays, shade_undef material, motion blur over a 40 ms shutter, 1-4 spp
+    opts = dict(width=96, height=72, min_samples=1, max_samples=4, max_var=0.01, caust_photons=20000,
+                gi_photons=30000, iter=6, shadow_samples=2, diffuse_samples=2, mblur=1, shutter=40, gather_dist=0.02)
+    path = scenegen.write_scene("feature")
+    g = gpu_lib.GpuRenderer(**opts)
+    g.load(path)
+    o = oracle_lib.Oracle(fp64=False, rng_mode=1, **opts)
+    o.load(path)
+    img_g = g.render(0)
+    img_o = o.render(0)
+    assert _compare(img_g, img_o, "feature 96x72 mblur") <= 1e-3
+
+
+@pytest.mark.parametrize("k", [0, 50])
+def test_photon_gather_points(small_pair, k):
+    # irradiance_est / radiance_est at given points: fixed-radius (k=0, the
+    # reference) and k-nearest within the radius cap
+    g, o = small_pair(width=32, height=32, caust_k=k, gi_k=k, gi_photons=40000, gather_dist=0.004)
+    nc, ng = g.shoot_photons(0, 0)
+    o.prepare(0)
+    ph = o.photons(0)
+    rng = np.random.default_rng(7)
+    pts = ph[rng.choice(len(ph), 4000), :3].astype(np.float64) + rng.normal(0, 0.01, (4000, 3))
+    nrm = np.tile([0.0, 1.0, 0.0], (4000, 1))
+    pts32 = pts.astype(np.float32)
+    for which in (0, 1):
+        out = torch.empty((4000, 3), dtype=torch.float32, device="cuda")
+        g.photon_gather(which, torch.tensor(pts32, device="cuda"), torch.tensor(nrm, dtype=torch.float32, device="cuda"), out)
+        torch.cuda.synchronize()
+        est_g = out.cpu().numpy().astype(np.float64)
+        est_o = o.gather(which, pts32.astype(np.float64), nrm)[:, :3]
+        rel = np.abs(est_g - est_o) / np.maximum(np.abs(est_o), 1e-6)
+        nz = (est_o != 0).any(axis=1).sum()
+        print("gather which=%d k=%d: %d nonzero, max rel %.3g" % (which, k, nz, rel.max()))
+        assert nz > 100
+        assert (rel.max(axis=1) > 1e-4).mean() <= 1e-3
