@@ -138,6 +138,27 @@ int sray_gpu_primary_hits(long msec, int *obj, int *prim, float *t, unsigned cha
  * floats (rgb).  The maps must have been built (sray_gpu_shoot_photons). */
 int sray_gpu_photon_gather(int which, int n, const float *pos, const float *norm, float *out, void *stream);
 
+/* Allocation-free form of sray_gpu_photon_gather.  This entry point has no
+ * counterpart in the reference.  It is for callers that must not allocate
+ * device memory while they run: an application that hands all device memory
+ * to its own pooling allocator (a cudaMalloc from inside the frame can fail
+ * or fragment that pool), or an interactive loop that cannot afford the
+ * device-wide synchronisation a cudaMalloc or cudaFree implies.  The request
+ * staging that sray_gpu_photon_gather allocates lives instead in a fixed
+ * array compiled into the library: SRAY_NOALLOC_MAX_POINTS requests (3 MiB,
+ * held on every GPU that loads the library until the process exits).
+ *  - n > SRAY_NOALLOC_MAX_POINTS is rejected with SRAY_EINVAL.
+ *  - The first call on a device looks up the array's device address on that
+ *    device; make that first call before any stream capture.
+ *  - All calls share the one array and it keeps the previous call's
+ *    requests; each call writes all the requests it reads, so nothing needs
+ *    clearing, but calls that overlap on the GPU (several host threads or
+ *    streams at once) race on it.
+ * Arguments, results and errors are those of sray_gpu_photon_gather; the
+ * call returns when `out` is written. */
+#define SRAY_NOALLOC_MAX_POINTS 65536
+int sray_gpu_photon_gather_noalloc(int which, int n, const float *pos, const float *norm, float *out, void *stream);
+
 /* Copy the stored photons of map `which` (0 = caustic, 1 = global) to host
  * memory as 16 floats each: pos xyz, dir xyz, norm xyz, power rgba, and
  * three unused.  `cap` is the capacity in photons; returns the count through

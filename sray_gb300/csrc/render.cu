@@ -1356,6 +1356,59 @@ int sray_gpu_photon_gather(int which, int n, const float *pos, const float *norm
 	return 0;
 }
 
+/* Fixed staging for sray_gpu_photon_gather_noalloc.  Host code must not
+ * take this symbol as a device address: the device address is looked up
+ * once per device with cudaGetSymbolAddress while that device is current. */
+static __device__ __align__(256) GatherReq g_noalloc_req[SRAY_NOALLOC_MAX_POINTS];
+static GatherReq *g_noalloc_addr[64];
+static std::mutex g_noalloc_mu;
+
+static int noalloc_requests(GatherReq **out)
+{
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if(e != cudaSuccess) { g_err = std::string("cudaGetDevice: ") + cudaGetErrorString(e); return SRAY_ECUDA; }
+	if(dev < 0 || dev >= 64) { g_err = "device index out of range for the fixed gather staging"; return SRAY_EINVAL; }
+	std::lock_guard<std::mutex> lk(g_noalloc_mu);
+	if(!g_noalloc_addr[dev]) {
+		void *p = nullptr;
+		e = cudaGetSymbolAddress(&p, g_noalloc_req);
+		if(e != cudaSuccess || !p) {
+			g_err = std::string("cudaGetSymbolAddress of the gather staging: ") + cudaGetErrorString(e);
+			return SRAY_ECUDA;
+		}
+		g_noalloc_addr[dev] = (GatherReq *)p;
+	}
+	*out = g_noalloc_addr[dev];
+	return 0;
+}
+
+int sray_gpu_photon_gather_noalloc(int which, int n, const float *pos, const float *norm, float *out, void *stream)
+{
+	NEED_CTX();
+	Renderer &R = *g_R;
+	if(!R.photons_ready) { g_err = "photon maps not built"; return SRAY_ESTATE; }
+	if((which != 0 && which != 1) || n < 0 || (n > 0 && (!pos || !norm || !out))) { g_err = "bad arguments"; return SRAY_EINVAL; }
+	if(n > SRAY_NOALLOC_MAX_POINTS) {
+		char msg[160];
+		snprintf(msg, sizeof msg, "sray_gpu_photon_gather_noalloc: %d points exceed its fixed capacity of %d; split the call",
+				n, SRAY_NOALLOC_MAX_POINTS);
+		g_err = msg;
+		return SRAY_EINVAL;
+	}
+	if(n == 0) return 0;
+	GatherReq *req = nullptr;
+	int r = noalloc_requests(&req);
+	if(r) return r;
+	cudaStream_t s = as_stream(stream);
+	k_pack_gather<<<grid_for(n, 256), 256, 0, s>>>(which, n, pos, norm, req);
+	k_gather_points<<<grid_for(n, GATHER_WARPS), GATHER_WARPS * 32, 0, s>>>(R.S, req, n, out);
+	cudaError_t e = cudaStreamSynchronize(s);
+	if(e == cudaSuccess) e = cudaGetLastError();
+	if(e != cudaSuccess) { g_err = cudaGetErrorString(e); return SRAY_ECUDA; }
+	return 0;
+}
+
 int sray_gpu_get_photons(int which, float *out, int cap, int *n_out)
 {
 	NEED_CTX();

@@ -16,7 +16,8 @@ _lib = None
 
 EXPORTS = ["sray_default_opts", "sray_gpu_init", "sray_gpu_set_opts", "sray_gpu_load_scene", "sray_gpu_load_scene_mem",
            "sray_gpu_scene_info", "sray_gpu_build", "sray_gpu_shoot_photons", "sray_gpu_render",
-           "sray_gpu_render_pixels", "sray_gpu_cast_rays", "sray_gpu_primary_hits", "sray_gpu_photon_gather", "sray_gpu_get_photons",
+           "sray_gpu_render_pixels", "sray_gpu_cast_rays", "sray_gpu_primary_hits", "sray_gpu_photon_gather", "sray_gpu_photon_gather_noalloc",
+           "sray_gpu_get_photons",
            "sray_gpu_get_stats", "sray_gpu_set_profiling", "sray_gpu_kernel_times", "sray_gpu_last_error",
            "sray_gpu_shutdown"]
 
@@ -61,6 +62,7 @@ def load_library():
     L.sray_gpu_cast_rays.argtypes = [ip, vp, vp, vp, vp, vp, vp, vp, vp]
     L.sray_gpu_primary_hits.argtypes = [lp, vp, vp, vp, vp, vp]
     L.sray_gpu_photon_gather.argtypes = [ip, ip, vp, vp, vp, vp]
+    L.sray_gpu_photon_gather_noalloc.argtypes = [ip, ip, vp, vp, vp, vp]
     L.sray_gpu_get_photons.argtypes = [ip, vp, ip, vp]
     L.sray_gpu_get_stats.argtypes = [ctypes.POINTER(SrayStats)]
     L.sray_gpu_set_profiling.argtypes = [ip]
@@ -169,6 +171,13 @@ class GpuRenderer:
         """Estimates at caller points (device arrays n*3 float32)."""
         n = int(pos.shape[0])
         self._chk(self.L.sray_gpu_photon_gather(which, n, _ptr(pos), _ptr(norm), _ptr(out), _stream(stream)))
+        return out
+
+    def photon_gather_noalloc(self, which, pos, norm, out, stream=None):
+        """Same estimates as photon_gather without any device allocation (at
+        most SRAY_NOALLOC_MAX_POINTS = 65536 points per call)."""
+        n = int(pos.shape[0])
+        self._chk(self.L.sray_gpu_photon_gather_noalloc(which, n, _ptr(pos), _ptr(norm), _ptr(out), _stream(stream)))
         return out
 
     def photons(self, which):
