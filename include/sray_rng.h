@@ -96,6 +96,21 @@ SRAY_HD uint32_t sray_rng_u32(sray_rng *s)
 	return s->buf[lane];
 }
 
+/* continue a stream after `n` draws (the state of a stream is its address
+ * and its draw count) */
+SRAY_HD void sray_rng_seek(sray_rng *s, uint32_t n)
+{
+	s->n = n;
+	if(n & 3u) {
+		uint32_t ctr[4];
+		ctr[0] = n >> 2;
+		ctr[1] = s->c1;
+		ctr[2] = s->c2;
+		ctr[3] = s->c3;
+		sray_philox4x32_10(ctr, s->k0, s->k1, s->buf);
+	}
+}
+
 /* uniform in [0, 1 - 2^-24], exact in float and double */
 SRAY_HD float sray_rng_uniform_f(sray_rng *s)
 {

@@ -1,10 +1,12 @@
 /* photon.cu -- photon emission and tracing, and the device photon map.
  *
- *   k_photon        Light::gen_photon (src/light.cc:111-148) with ProjMap::gen_dir
- *                   (src/projmap.cc:193-209), Scene::trace_caustics_photon /
- *                   trace_global_photon (src/scene.cc:571-760); one thread per
- *                   photon, each on its own Philox stream, so photon j of light i
- *                   is the same photon the CPU oracle shoots
+ *   k_photon_emit   Light::gen_photon (src/light.cc:111-148) with ProjMap::gen_dir
+ *                   (src/projmap.cc:193-209), one thread per photon, each on its
+ *                   own Philox stream, so photon j of light i is the same photon
+ *                   the CPU oracle shoots
+ *   k_photon_bounce Scene::trace_caustics_photon / trace_global_photon
+ *                   (src/scene.cc:571-760), one interaction per pass; the
+ *                   renderer's k_trace finds the hits in between
  *   compaction      keeps stored photons in emission order
  *   k_rs_*          stable LSD radix sort of the photons by the Morton code of
  *                   their grid cell
@@ -19,7 +21,10 @@
 #include <math.h>
 #include <string.h>
 #include <algorithm>
+#include <cooperative_groups.h>
 #include "renderer.h"
+
+namespace cg = cooperative_groups;
 
 namespace sray {
 
@@ -37,13 +42,8 @@ struct PState {
 	V3 pos, dir, norm;
 };
 
-__device__ __forceinline__ bool photon_hit(const DScene &S, const PRay &r, Hit &h, Surf &sp, int *overflow)
-{
-	trace_closest<false>(S, r.o, r.d, r.time, h, nullptr, overflow);
-	if(h.obj < 0) return false;
-	surface_point(S, h, r.o, r.d, r.time, sp, false);
-	return true;
-}
+/* outcome of one photon-surface interaction */
+enum { P_DROP = 0, P_STORE = 1, P_CONT = 2, P_TO_CAUST = 3 };
 
 __device__ __forceinline__ void refract_ray(PRay &r, V3 n, float mat_ior, bool entering, float ray_mag)
 {
@@ -57,108 +57,105 @@ __device__ __forceinline__ void refract_ray(PRay &r, V3 n, float mat_ior, bool e
 	}
 }
 
-/* Scene::trace_caustics_photon (src/scene.cc:571-647), loop form */
-__device__ bool trace_caust(const DScene &S, PRay r, PState &ph, sray_rng *s, int *overflow)
+/* one iteration of Scene::trace_caustics_photon (src/scene.cc:571-647) at
+ * the hit h: reflect or refract (P_CONT) or absorb and store (P_STORE) */
+__device__ int caust_step(const DScene &S, PRay &r, PState &ph, const Hit &h, sray_rng *s)
 {
-	for(int guard = 0; guard < 4096; guard++) {
-		if(r.iter <= 0) return false;
-		Hit h;
-		Surf sp;
-		if(!photon_hit(S, r, h, sp, overflow)) return false;
-		const DevMat &m = mat_of(S, h.obj);
+	Surf sp;
+	surface_point(S, h, r.o, r.d, r.time, sp, false);
+	const DevMat &m = mat_of(S, h.obj);
+	float refl = m.refl, refr = m.refr, mat_ior = m.ior;
+	bool entering;
+	V3 normal;
+	float ray_mag = len(r.d);
+	if(dot(r.d, sp.normal) > 0.0f) { normal = -sp.normal; entering = false; }
+	else { normal = sp.normal; entering = true; }
+	float ior = r.st.calc_ior(entering, mat_ior);
+	float ray_dot_n = dot(-r.d / ray_mag, normal);
+	float sf0 = refr > 0.0f ? (ior - 1.0f) / (ior + 1.0f) : 1.0f;
+	float fres = fresnel(sf0 * sf0, ray_dot_n);
+	refl = fres * refl;
+	refr = (1.0f - fres) * refr;
+	float rnum = frand(s, 1.0f);
+	if(rnum < refl) {
+		r.d = reflection(r.d, normal);
+		r.iter--;
+		r.o = sp.pos;
+		ph.type = CAUST_PHOTON;
+		for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * m.ks[k];
+		return P_CONT;
+	}
+	if(rnum < refr) {
+		refract_ray(r, normal, mat_ior, entering, ray_mag);
+		r.o = sp.pos;
+		ph.type = CAUST_PHOTON;
+		for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * m.ks[k];
+		return P_CONT;
+	}
+	ph.dir = normalized(r.d);
+	ph.pos = sp.pos;
+	ph.norm = normal;
+	return P_STORE;
+}
+
+/* one iteration of Scene::trace_global_photon (src/scene.cc:650-760) at the
+ * hit h: diffuse bounce (P_CONT), specular bounce that hands the photon to
+ * the caustic rules (P_TO_CAUST), absorption (P_DROP) or storage (P_STORE) */
+__device__ int global_step(const DScene &S, PRay &r, PState &ph, const Hit &h, sray_rng *s)
+{
+	V3 incident = normalized(r.d);
+	Surf sp;
+	surface_point(S, h, r.o, r.d, r.time, sp, false);
+	V3 normal;
+	bool entering;
+	float ray_mag = len(r.d);
+	if(dot(r.d, sp.normal) > 0.0f) { normal = -sp.normal; entering = false; }
+	else { normal = sp.normal; entering = true; }
+	const DevMat &m = mat_of(S, h.obj);
+	float diff_avg = (m.kd[0] + m.kd[1] + m.kd[2]) / 3.0f;
+	float spec_avg = (m.ks[0] + m.ks[1] + m.ks[2]) / 3.0f;
+	float rnum = frand(s, 1.0f);
+	if(rnum < diff_avg) {
+		V3 dir = sphrand(s, 1.0f);
+		if(dot(dir, normal) < 0.0f) dir = -dir;
+		float ndotl = dot(-incident, normal);
+		r.d = dir * (float)SRAY_RAY_MAGNITUDE;
+		r.iter--;
+		r.o = sp.pos;
+		ph.type = GI_PHOTON;
+		for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * (ndotl * (m.kd[k] / diff_avg));
+		return P_CONT;
+	}
+	if(rnum < diff_avg + spec_avg) {
 		float refl = m.refl, refr = m.refr, mat_ior = m.ior;
-		bool entering;
-		V3 normal;
-		float ray_mag = len(r.d);
-		if(dot(r.d, sp.normal) > 0.0f) { normal = -sp.normal; entering = false; }
-		else { normal = sp.normal; entering = true; }
 		float ior = r.st.calc_ior(entering, mat_ior);
 		float ray_dot_n = dot(-r.d / ray_mag, normal);
 		float sf0 = refr > 0.0f ? (ior - 1.0f) / (ior + 1.0f) : 1.0f;
 		float fres = fresnel(sf0 * sf0, ray_dot_n);
 		refl = fres * refl;
 		refr = (1.0f - fres) * refr;
-		float rnum = frand(s, 1.0f);
-		if(rnum < refl) {
+		float rn2 = frand(s, 1.0f);
+		if(rn2 < refl) {
 			r.d = reflection(r.d, normal);
 			r.iter--;
 			r.o = sp.pos;
 			ph.type = CAUST_PHOTON;
 			for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * m.ks[k];
-		} else if(rnum < refr) {
+			return P_TO_CAUST;
+		}
+		if(rn2 < refr) {
 			refract_ray(r, normal, mat_ior, entering, ray_mag);
 			r.o = sp.pos;
 			ph.type = CAUST_PHOTON;
 			for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * m.ks[k];
-		} else {
-			ph.dir = normalized(r.d);
-			ph.pos = sp.pos;
-			ph.norm = normal;
-			return true;
+			return P_TO_CAUST;
 		}
+		return P_DROP;
 	}
-	return false;
-}
-
-/* Scene::trace_global_photon (src/scene.cc:650-760), loop form */
-__device__ bool trace_global(const DScene &S, PRay r, PState &ph, sray_rng *s, int *overflow)
-{
-	for(int guard = 0; guard < 4096; guard++) {
-		if(r.iter <= 0) return false;
-		V3 incident = normalized(r.d);
-		Hit h;
-		Surf sp;
-		if(!photon_hit(S, r, h, sp, overflow)) return false;
-		V3 normal;
-		bool entering;
-		float ray_mag = len(r.d);
-		if(dot(r.d, sp.normal) > 0.0f) { normal = -sp.normal; entering = false; }
-		else { normal = sp.normal; entering = true; }
-		const DevMat &m = mat_of(S, h.obj);
-		float diff_avg = (m.kd[0] + m.kd[1] + m.kd[2]) / 3.0f;
-		float spec_avg = (m.ks[0] + m.ks[1] + m.ks[2]) / 3.0f;
-		float rnum = frand(s, 1.0f);
-		if(rnum < diff_avg) {
-			V3 dir = sphrand(s, 1.0f);
-			if(dot(dir, normal) < 0.0f) dir = -dir;
-			float ndotl = dot(-incident, normal);
-			r.d = dir * (float)SRAY_RAY_MAGNITUDE;
-			r.iter--;
-			r.o = sp.pos;
-			ph.type = GI_PHOTON;
-			for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * (ndotl * (m.kd[k] / diff_avg));
-		} else if(rnum < diff_avg + spec_avg) {
-			float refl = m.refl, refr = m.refr, mat_ior = m.ior;
-			float ior = r.st.calc_ior(entering, mat_ior);
-			float ray_dot_n = dot(-r.d / ray_mag, normal);
-			float sf0 = refr > 0.0f ? (ior - 1.0f) / (ior + 1.0f) : 1.0f;
-			float fres = fresnel(sf0 * sf0, ray_dot_n);
-			refl = fres * refl;
-			refr = (1.0f - fres) * refr;
-			float rn2 = frand(s, 1.0f);
-			if(rn2 < refl) {
-				r.d = reflection(r.d, normal);
-				r.iter--;
-				r.o = sp.pos;
-				ph.type = CAUST_PHOTON;
-				for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * m.ks[k];
-				return trace_caust(S, r, ph, s, overflow);
-			} else if(rn2 < refr) {
-				refract_ray(r, normal, mat_ior, entering, ray_mag);
-				r.o = sp.pos;
-				ph.type = CAUST_PHOTON;
-				for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * m.ks[k];
-				return trace_caust(S, r, ph, s, overflow);
-			}
-			return false;
-		} else {
-			ph.dir = incident;
-			ph.pos = sp.pos;
-			ph.norm = normal;
-			return true;
-		}
-	}
-	return false;
+	ph.dir = incident;
+	ph.pos = sp.pos;
+	ph.norm = normal;
+	return P_STORE;
 }
 
 /* ProjMap::gen_dir(true) with cell_from_dir in deterministic float math;
@@ -180,10 +177,50 @@ __device__ bool gen_dir(const uint32_t *bits, sray_rng *s, V3 *out)
 	return false;
 }
 
-__global__ void __launch_bounds__(128) k_photon(DScene S, int global, const int *prefix, const float *scale, int nlights,
-		int total, DevPhoton *out, int *valid, DevCounters *ctr)
+/* The reference traces one photon to its end with recursive calls.  Here the
+ * photons of a map advance together, one surface interaction per pass, over
+ * ray queues that the renderer's closest-hit kernel traces:
+ *   k_photon_emit    Light::gen_photon (src/light.cc:111-148) with
+ *                    ProjMap::gen_dir (src/projmap.cc:193-209) -> queue
+ *   k_trace          closest hits of the queue (render.cu)
+ *   k_photon_bounce  one trace_caustics_photon / trace_global_photon step
+ *                    per photon -> stored photon, next queue, or loss
+ * A photon keeps its own Philox stream: the queue carries its stream address
+ * (light, index) and draw count, so photon j of light i takes the same draws
+ * and the same path as the CPU oracle's recursive tracer.
+ *
+ * Photon queue entry (RayQueue fields):
+ *   o = origin, colour r     d = direction, colour g
+ *   w = colour b, ior, interactions in this phase, photon id
+ *   meta = light, iter, phase | type << 4, time
+ *   stk = ior stack          ext = draws taken, stack depth
+ * Phase 0 follows the global rules, phase 1 the caustic rules. */
+
+#define PHOTON_GUARD 4096   /* interactions per phase (loop bound of the oracle's tracer) */
+
+__device__ __forceinline__ void push_photon(const RayQueue &q, int slot, const PRay &r, const PState &ph, int guard, int gid,
+		int li, int phase, uint32_t draws)
 {
-	int overflow = 0, gfail = 0;
+	q.o[slot] = make_float4(r.o.x, r.o.y, r.o.z, ph.col[0]);
+	q.d[slot] = make_float4(r.d.x, r.d.y, r.d.z, ph.col[1]);
+	q.w[slot] = make_float4(ph.col[2], r.st.ior, __int_as_float(guard), __int_as_float(gid));
+	q.meta[slot] = make_int4(li, r.iter, phase | (ph.type << 4), r.time);
+	q.stk[slot] = make_float4(r.st.stk[0], r.st.stk[1], r.st.stk[2], r.st.stk[3]);
+	q.ext[slot] = make_int2((int)draws, r.st.sp);
+}
+
+static __device__ __forceinline__ int photon_slot(int *counter)
+{
+	cg::coalesced_group g = cg::coalesced_threads();
+	int base = 0;
+	if(g.thread_rank() == 0) base = atomicAdd(counter, (int)g.size());
+	return g.shfl(base, 0) + (int)g.thread_rank();
+}
+
+__global__ void __launch_bounds__(128) k_photon_emit(DScene S, int global, const int *prefix, int nlights, int total,
+		RayQueue q, int *valid, DevCounters *ctr)
+{
+	int gfail = 0;
 	for(int gid = blockIdx.x * blockDim.x + threadIdx.x; gid < total; gid += gridDim.x * blockDim.x) {
 		int li = 0;
 		while(li + 1 < nlights && prefix[li + 1] <= gid) li++;
@@ -212,8 +249,8 @@ __global__ void __launch_bounds__(128) k_photon(DScene S, int global, const int 
 		} else {
 			dir = sphrand(&s, 1.0f);
 		}
-		bool stored = false;
-		if(ok) {
+		valid[gid] = 0;
+		if(ok && S.iter > 0) {
 			PRay r;
 			r.o = pos;
 			r.d = dir * (float)SRAY_RAY_MAGNITUDE;
@@ -221,21 +258,69 @@ __global__ void __launch_bounds__(128) k_photon(DScene S, int global, const int 
 			r.iter = S.iter;
 			r.st.ior = 1.0f;
 			r.st.sp = 0;
-			if(global) stored = trace_global(S, r, ph, &s, &overflow);
-			else stored = trace_caust(S, r, ph, &s, &overflow) && ph.type == CAUST_PHOTON;
+			for(int k = 0; k < 4; k++) r.st.stk[k] = 0.0f;
+			int slot = photon_slot(q.count);
+			push_photon(q, slot, r, ph, 0, gid, li, global ? 0 : 1, s.n);
 		}
-		valid[gid] = stored ? 1 : 0;
-		if(stored) {
+	}
+	if(gfail) atomicOr(&ctr->gen_dir_fail, 1);
+}
+
+__global__ void __launch_bounds__(128) k_photon_bounce(DScene S, int global, const int *prefix, const float *scale, RayQueue qi,
+		const int4 *hits, RayQueue qo, DevPhoton *out, int *valid)
+{
+	int n = *qi.count;
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		int4 hv = hits[i];
+		if(hv.y < 0) continue;                       /* photon left the scene */
+		Hit h;
+		h.t = __int_as_float(hv.x);
+		h.obj = hv.y;
+		h.prim = hv.z;
+		h.tie = hv.w;
+		float4 o4 = qi.o[i], d4 = qi.d[i], w4 = qi.w[i], k4 = qi.stk[i];
+		int4 meta = qi.meta[i];
+		int2 ext = qi.ext[i];
+		int li = meta.x, phase = meta.z & 15;
+		int guard = __float_as_int(w4.z), gid = __float_as_int(w4.w);
+		PRay r;
+		r.o = mk(o4.x, o4.y, o4.z);
+		r.d = mk(d4.x, d4.y, d4.z);
+		r.time = meta.w;
+		r.iter = meta.y;
+		r.st.ior = w4.y;
+		r.st.stk[0] = k4.x; r.st.stk[1] = k4.y; r.st.stk[2] = k4.z; r.st.stk[3] = k4.w;
+		r.st.sp = ext.y;
+		PState ph;
+		ph.col[0] = o4.w; ph.col[1] = d4.w; ph.col[2] = w4.x;
+		ph.type = meta.z >> 4;
+		sray_rng s;
+		sray_rng_init(&s, S.seed, global ? SRAY_DOM_GLOBAL : SRAY_DOM_CAUST, (uint32_t)(gid - prefix[li]), (uint32_t)li);
+		sray_rng_seek(&s, (uint32_t)ext.x);
+		int res = phase == 0 ? global_step(S, r, ph, h, &s) : caust_step(S, r, ph, h, &s);
+		if(res == P_STORE) {
+			if(!global && ph.type != CAUST_PHOTON) continue;
 			float sc = scale[li];
 			DevPhoton p;
 			p.p[0] = ph.pos.x; p.p[1] = ph.pos.y; p.p[2] = ph.pos.z; p.p[3] = ph.col[0] * sc;
 			p.d[0] = ph.dir.x; p.d[1] = ph.dir.y; p.d[2] = ph.dir.z; p.d[3] = ph.col[1] * sc;
 			p.n[0] = ph.norm.x; p.n[1] = ph.norm.y; p.n[2] = ph.norm.z; p.n[3] = ph.col[2] * sc;
 			out[gid] = p;
+			valid[gid] = 1;
+			continue;
 		}
+		if(res == P_DROP) continue;
+		if(res == P_TO_CAUST) {
+			phase = 1;
+			guard = 0;
+		} else if(++guard >= PHOTON_GUARD) {
+			continue;
+		}
+		if(r.iter <= 0) continue;
+		int slot = photon_slot(qo.count);
+		if(slot >= qo.cap) continue;                 /* cannot happen: a photon has one successor */
+		push_photon(qo, slot, r, ph, guard, gid, li, phase, s.n);
 	}
-	if(overflow) atomicOr(&ctr->overflow, 1);
-	if(gfail) atomicOr(&ctr->gen_dir_fail, 1);
 }
 
 /* ---------------- scan / compaction ---------------- */
@@ -441,9 +526,30 @@ int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored)
 	PCK(P.tmp_ph.ensure((size_t)total * sizeof(DevPhoton)), "photon buffer");
 	PCK(P.valid.ensure((size_t)total * sizeof(int)), "photon flags");
 	PCK(R.ctr.ensure(sizeof(DevCounters)), "counters");
+	PCK(R.counts.ensure(64 * sizeof(int)), "counts");
 	PCK(cudaMemsetAsync(R.ctr.p, 0, sizeof(DevCounters), s), "counters");
-	LAUNCH(R, "photon_trace", s, k_photon<<<grid_n(total, 128), 128, 0, s>>>(R.S, global, pre.as<int>(), scl.as<float>(), nl, total,
-			P.tmp_ph.as<DevPhoton>(), P.valid.as<int>(), R.ctr.as<DevCounters>()));
+	PCK(cudaMemsetAsync(R.counts.p, 0, 2 * sizeof(int), s), "photon queue counts");
+	if(R.ensure_queue(0, total) || R.ensure_queue(1, total)) return SRAY_ECUDA;
+	PCK(R.hits.ensure((size_t)total * 16), "photon hits");
+	int *cnt = R.counts.as<int>();
+	R.q[0].count = cnt + 0;
+	R.q[1].count = cnt + 1;
+	LAUNCH(R, "photon_emit", s, k_photon_emit<<<grid_n(total, 128), 128, 0, s>>>(R.S, global, pre.as<int>(), nl, total, R.q[0],
+			P.valid.as<int>(), R.ctr.as<DevCounters>()));
+	int cur = 0;
+	int n_live = total;   /* upper bound until the first count is read */
+	for(int pass = 0; n_live > 0; pass++) {
+		if(pass >= 2 * PHOTON_GUARD + 2) return R.fail(SRAY_EDEVICE, "photon paths did not terminate");
+		PCK(cudaMemsetAsync(R.q[cur ^ 1].count, 0, sizeof(int), s), "reset photon queue");
+		launch_trace(R, R.q[cur], n_live, "photon_trace", s);
+		LAUNCH(R, "photon_bounce", s, k_photon_bounce<<<grid_n(n_live, 128), 128, 0, s>>>(R.S, global, pre.as<int>(),
+				scl.as<float>(), R.q[cur], R.hits.as<int4>(), R.q[cur ^ 1], P.tmp_ph.as<DevPhoton>(), P.valid.as<int>()));
+		PCK(cudaMemcpyAsync(&n_live, R.q[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "photon queue count");
+		PCK(cudaStreamSynchronize(s), "photon pass");
+		R.d2h += sizeof(int);
+		R.prof_collect();
+		cur ^= 1;
+	}
 	/* compaction in emission order */
 	int nb = (total + TILE - 1) / TILE;
 	PCK(P.scan.ensure((size_t)(nb + 4) * sizeof(unsigned)), "scan");

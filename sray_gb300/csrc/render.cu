@@ -1104,6 +1104,11 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 	return 0;
 }
 
+void launch_trace(Renderer &R, const RayQueue &q, int n, const char *name, cudaStream_t s)
+{
+	LAUNCH(R, name, s, k_trace<false><<<grid_for(n, 128), 128, 0, s>>>(R.S, q, R.hits.as<int4>(), R.ctr.as<DevCounters>()));
+}
+
 static Renderer *g_R = nullptr;
 static std::string g_err;
 static std::mutex g_mu;

@@ -143,6 +143,9 @@ struct Renderer {
 		(R_).prof_end(&pend_, s_); \
 	} while(0)
 
+/* render.cu: closest hits of the first n rays of q into R.hits */
+void launch_trace(Renderer &R, const RayQueue &q, int n, const char *name, cudaStream_t s);
+
 /* photon.cu */
 int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored);
 
