@@ -170,7 +170,8 @@ typedef struct sray_stats {
 	int64_t primary_rays, shadow_rays, secondary_rays, gather_rays;
 	int64_t photons_emitted, photons_stored, gathers;
 	int64_t samples;               /* pixel samples taken (adaptive) */
-	int64_t node_visits, prim_tests;  /* traversal work (when counting is on) */
+	int64_t node_visits, prim_tests;  /* traversal work (when counting is on): octree
+	                                     node records read, primitive tests */
 	int kernel_launches;           /* kernels launched by the last render */
 	int pad;
 	int64_t h2d_bytes, d2h_bytes;  /* host<->device bytes copied by the last render */
@@ -181,7 +182,7 @@ int sray_gpu_get_stats(sray_stats *st);
 
 /* Profiling (extension, no reference counterpart).  flags bit 0: time every
  * kernel launch with CUDA events recorded on the launch stream; bit 1: count
- * octree node visits and primitive tests in the closest-hit kernel (slower;
+ * octree node records read and primitive tests in the closest-hit kernel (slower;
  * reported through sray_stats.node_visits / prim_tests). */
 int sray_gpu_set_profiling(int flags);
 

@@ -277,29 +277,67 @@ struct TStack {
 	float te[SRAY_STACK];
 };
 
-/* test the 8 children of an inner node and push the hit ones far to near */
+/* test the children of an inner node and push the hit ones far to near.
+ * A child's box is one octant of the node's box split at `mid`, so its slab
+ * parameters are three of the nine plane parameters (mn, mid, mx per axis)
+ * computed once here; each child's test then makes exactly the comparisons
+ * of box_hit on exactly the values box_hit would compute from its box. */
+__device__ __forceinline__ void half_planes(float lo, float mid, float hi, float o, float inv, bool neg, float &n0, float &f0,
+		float &n1, float &f1)
+{
+	float ta = (lo - o) * inv, tm = (mid - o) * inv, tb = (hi - o) * inv;
+	/* lower half [lo, mid], upper half [mid, hi]; a negative direction
+	 * enters through the upper plane */
+	n0 = neg ? tm : ta;
+	f0 = neg ? ta : tm;
+	n1 = neg ? tb : tm;
+	f1 = neg ? tm : tb;
+}
+
 template <bool COUNT>
-__device__ __forceinline__ int push_children(const DevNode *nodes, int first, int oct, const RayT &r, float best, TStack &st,
+__device__ __forceinline__ int push_children(float4 n0, float4 n1, float4 n2, int oct, const RayT &r, float best, TStack &st,
 		int sp, int limit, TraceCounters *tc, int *overflow)
 {
+	int first = __float_as_int(n0.w);
+	unsigned mask = __float_as_uint(n2.w);
+	float nx0, fx0, nx1, fx1, ny0, fy0, ny1, fy1, nz0, fz0, nz1, fz1;
+	half_planes(n0.x, n2.x, n1.x, r.o.x, r.inv.x, r.d.x < 0.0f, nx0, fx0, nx1, fx1);
+	half_planes(n0.y, n2.y, n1.y, r.o.y, r.inv.y, r.d.y < 0.0f, ny0, fy0, ny1, fy1);
+	half_planes(n0.z, n2.z, n1.z, r.o.z, r.inv.z, r.d.z < 0.0f, nz0, fz0, nz1, fz1);
 	#pragma unroll
 	for(int k = 7; k >= 0; k--) {
-		int c = first + (k ^ oct);
-		const float4 *cp = reinterpret_cast<const float4 *>(nodes + c);
-		float4 c1 = __ldg(cp + 1);
-		if(__float_as_int(c1.w) == 0) continue;
-		float4 c0 = __ldg(cp);
-		float mn[3] = {c0.x, c0.y, c0.z}, mx[3] = {c1.x, c1.y, c1.z};
-		if(COUNT) tc->nodes++;
-		float tk;
-		if(box_hit(mn, mx, r, tk) && !SRAY_PRUNE(tk, best)) {
-			if(sp >= limit) { *overflow = 1; continue; }
-			st.node[sp] = c;
-			st.te[sp] = tk;
-			sp++;
-		}
+		int c = k ^ oct;
+		if(!((mask >> c) & 1u)) continue;
+		float tmin = (c & 1) ? nx1 : nx0, tmax = (c & 1) ? fx1 : fx0;
+		float tymin = (c & 2) ? ny1 : ny0, tymax = (c & 2) ? fy1 : fy0;
+		float tzmin = (c & 4) ? nz1 : nz0, tzmax = (c & 4) ? fz1 : fz0;
+		if((tmin > tymax) || (tymin > tmax)) continue;
+		if(tymin > tmin) tmin = tymin;
+		if(tymax < tmax) tmax = tymax;
+		if((tmin > tzmax) || (tzmin > tmax)) continue;
+		if(tzmin > tmin) tmin = tzmin;
+		if(tzmax < tmax) tmax = tzmax;
+		if(!((tmin < 1.0f) && (tmax > 0.0f)) || SRAY_PRUNE(tmin, best)) continue;
+		if(sp >= limit) { *overflow = 1; continue; }
+		st.node[sp] = first + c;
+		st.te[sp] = tmin;
+		sp++;
 	}
 	return sp;
+}
+
+/* a node record: n0 = mn + first, n1 = mx + count, n2 = mid + child mask
+ * (the third part is read for inner nodes only) */
+__device__ __forceinline__ void load_node(const DevNode *nodes, int ni, float4 &n0, float4 &n1)
+{
+	const float4 *np = reinterpret_cast<const float4 *>(nodes + ni);
+	n0 = __ldg(np);
+	n1 = __ldg(np + 1);
+}
+
+__device__ __forceinline__ float4 load_split(const DevNode *nodes, int ni)
+{
+	return __ldg(reinterpret_cast<const float4 *>(nodes + ni) + 2);
 }
 
 /* closest hit inside one mesh (object space), sharing the best hit so far */
@@ -310,7 +348,6 @@ __device__ __forceinline__ void mesh_closest(const DScene &S, int root, int obj,
 	int sp = base;
 	float te;
 	const DevNode &rn = S.mnodes[root];
-	if(COUNT) tc->nodes++;
 	if(!box_hit(rn.mn, rn.mx, r, te)) return;
 	int oct = octant(r);
 	st.node[sp] = root;
@@ -320,11 +357,12 @@ __device__ __forceinline__ void mesh_closest(const DScene &S, int root, int obj,
 		sp--;
 		int ni = st.node[sp];
 		if(SRAY_PRUNE(st.te[sp], h.t)) continue;
-		const float4 *np = reinterpret_cast<const float4 *>(S.mnodes + ni);
-		float4 n0 = __ldg(np), n1 = __ldg(np + 1);
+		if(COUNT) tc->nodes++;
+		float4 n0, n1;
+		load_node(S.mnodes, ni, n0, n1);
 		int count = __float_as_int(n1.w), first = __float_as_int(n0.w);
 		if(count < 0) {
-			sp = push_children<COUNT>(S.mnodes, first, oct, r, h.t, st, sp, SRAY_STACK, tc, overflow);
+			sp = push_children<COUNT>(n0, n1, load_split(S.mnodes, ni), oct, r, h.t, st, sp, SRAY_STACK, tc, overflow);
 		} else {
 			const float4 *tp = reinterpret_cast<const float4 *>(S.mtris + first);
 			for(int s = 0; s < count; s++) {
@@ -389,7 +427,6 @@ __device__ inline void trace_closest(const DScene &S, V3 wo, V3 wd, int time, Hi
 	#pragma unroll
 	for(int k = 0; k < SRAY_MAILBOX; k++) mbox[k] = -1;
 	int mb_next = 0;
-	if(COUNT) tc->nodes++;
 	const DevNode &root = S.snodes[S.sroot];
 	if(!box_hit(root.mn, root.mx, r, te)) return;
 	st.node[sp] = S.sroot;
@@ -399,11 +436,12 @@ __device__ inline void trace_closest(const DScene &S, V3 wo, V3 wd, int time, Hi
 		sp--;
 		int ni = st.node[sp];
 		if(SRAY_PRUNE(st.te[sp], h.t)) continue;
-		const float4 *np = reinterpret_cast<const float4 *>(S.snodes + ni);
-		float4 n0 = __ldg(np), n1 = __ldg(np + 1);
+		if(COUNT) tc->nodes++;
+		float4 n0, n1;
+		load_node(S.snodes, ni, n0, n1);
 		int count = __float_as_int(n1.w), first = __float_as_int(n0.w);
 		if(count < 0) {
-			sp = push_children<COUNT>(S.snodes, first, oct, r, h.t, st, sp, SRAY_STACK / 2, tc, overflow);
+			sp = push_children<COUNT>(n0, n1, load_split(S.snodes, ni), oct, r, h.t, st, sp, SRAY_STACK / 2, tc, overflow);
 		} else {
 			for(int s = 0; s < count; s++) {
 				int oi = __ldg(S.sslots + first + s);
@@ -426,11 +464,11 @@ __device__ inline bool mesh_any(const DScene &S, int root, const RayT &r, TStack
 	st.node[sp++] = root;
 	while(sp > base) {
 		int ni = st.node[--sp];
-		const float4 *np = reinterpret_cast<const float4 *>(S.mnodes + ni);
-		float4 n0 = __ldg(np), n1 = __ldg(np + 1);
+		float4 n0, n1;
+		load_node(S.mnodes, ni, n0, n1);
 		int count = __float_as_int(n1.w), first = __float_as_int(n0.w);
 		if(count < 0) {
-			sp = push_children<false>(S.mnodes, first, oct, r, FLT_MAX, st, sp, SRAY_STACK, nullptr, overflow);
+			sp = push_children<false>(n0, n1, load_split(S.mnodes, ni), oct, r, FLT_MAX, st, sp, SRAY_STACK, nullptr, overflow);
 		} else {
 			const float4 *tp = reinterpret_cast<const float4 *>(S.mtris + first);
 			for(int s = 0; s < count; s++) {
@@ -461,11 +499,11 @@ __device__ inline bool trace_any(const DScene &S, V3 wo, V3 wd, int time, int *o
 	st.node[sp++] = S.sroot;
 	while(sp > 0) {
 		int ni = st.node[--sp];
-		const float4 *np = reinterpret_cast<const float4 *>(S.snodes + ni);
-		float4 n0 = __ldg(np), n1 = __ldg(np + 1);
+		float4 n0, n1;
+		load_node(S.snodes, ni, n0, n1);
 		int count = __float_as_int(n1.w), first = __float_as_int(n0.w);
 		if(count < 0) {
-			sp = push_children<false>(S.snodes, first, oct, r, FLT_MAX, st, sp, SRAY_STACK / 2, nullptr, overflow);
+			sp = push_children<false>(n0, n1, load_split(S.snodes, ni), oct, r, FLT_MAX, st, sp, SRAY_STACK / 2, nullptr, overflow);
 		} else {
 			for(int s = 0; s < count; s++) {
 				int oi = __ldg(S.sslots + first + s);

@@ -542,9 +542,9 @@ static const int child_slot[8] = {0, 1, 3, 2, 4, 5, 7, 6};
 void flatten_octree(const BuildOctree &oct, std::vector<DevNode> &out, std::vector<int> &slots)
 {
 	if(oct.nodes.empty()) return;
-	/* pad so the root sits at index 3 mod 4: every group of 8 siblings then
-	 * starts on a 128-byte line */
-	while((out.size() & 3) != 3) {
+	/* pad so the root sits at index 7 mod 8: every group of 8 siblings
+	 * (384 bytes) then starts on a 128-byte line */
+	while((out.size() & 7) != 7) {
 		DevNode pad;
 		memset(&pad, 0, sizeof pad);
 		out.push_back(pad);
@@ -572,10 +572,18 @@ void flatten_octree(const BuildOctree &oct, std::vector<DevNode> &out, std::vect
 	for(size_t q = 0; q < order.size(); q++) {
 		const BuildOctree::Node &n = oct.nodes[order[q]];
 		DevNode &d = out[base + q];
-		for(int i = 0; i < 3; i++) { d.mn[i] = (float)n.box.mn[i]; d.mx[i] = (float)n.box.mx[i]; }
+		for(int i = 0; i < 3; i++) { d.mn[i] = (float)n.box.mn[i]; d.mx[i] = (float)n.box.mx[i]; d.mid[i] = 0.0f; }
+		d.mask = 0;
 		if(n.child >= 0) {
 			d.first = (int)base + newidx[n.child];
 			d.count = -1;
+			/* the children's bounds are mn/centre/mx of this box, rounded the
+			 * same way as the boxes the builder gave them */
+			for(int i = 0; i < 3; i++) d.mid[i] = (float)((n.box.mn[i] + n.box.mx[i]) * 0.5);
+			for(int k = 0; k < 8; k++) {
+				const BuildOctree::Node &c = oct.nodes[n.child + k];
+				if(c.child >= 0 || !c.items.empty()) d.mask |= 1u << child_slot[k];
+			}
 		} else {
 			d.first = (int)slots.size();
 			d.count = (int)n.items.size();

@@ -25,11 +25,15 @@
 
 namespace sray {
 
+/* an octree node; the children of an inner node are the octants of its box
+ * split at `mid`, so their boxes are not stored */
 struct alignas(16) DevNode {
 	float mn[3];
-	int first;      /* inner: index of child 0; leaf: first slot */
+	int first;      /* inner: index of child slot 0; leaf: first slot */
 	float mx[3];
 	int count;      /* inner: -1; leaf: number of slots */
+	float mid[3];   /* inner: split point (the reference's box centre) */
+	unsigned mask;  /* inner: bit k set when child slot k holds items */
 };
 
 struct alignas(16) DevTri {
