@@ -371,16 +371,32 @@ __device__ __forceinline__ double dist2(const float4 &p, const double q[3])
 	return dx * dx + dy * dy + dz * dz;
 }
 
+/* Screening bound for the in-range test.  The float squared distance
+ * d2f = fl(fl(fl(dx)^2 + fl(dy)^2) + fl(dz)^2), with dx = p.x - q.x from
+ * float operands, is within 6 units in the last place of the exact sum of
+ * squares (each of the five roundings adds at most 2^-24 relative error and
+ * all terms are non-negative), which the double computation reproduces to
+ * 2^-50.  So a photon whose d2f exceeds r2 (1 + 2^-20) is out of range
+ * exactly as the double test would find; the others are decided in double. */
+__device__ __forceinline__ float screen_threshold(double r2)
+{
+	return (float)(r2 * (1.0 + 1.0 / 1048576.0));
+}
+
 /* The cells overlapping the query cube (at most 2x2x2: cells are twice the
  * gather radius) are looked up by the first lanes; the warp then strides
  * over the concatenation of their photon runs, so every lane tests one
- * photon per step whatever the cell occupancy.  f(photon, d2) is called for
- * the photons within range. */
+ * photon per step whatever the cell occupancy.  f(in, photon, d2) is called
+ * by every lane at every step (so it may use warp collectives); `in` tells
+ * whether the lane holds a photon within range, d2 its exact squared
+ * distance. */
 template <class F>
 __device__ __forceinline__ void for_range(const DPhotonMap &M, const GatherCells &gc, const double q[3], double r2, int lane, F f)
 {
 	int nx = gc.hi[0] - gc.lo[0] + 1, ny = gc.hi[1] - gc.lo[1] + 1, nz = gc.hi[2] - gc.lo[2] + 1;
 	int ncell = nx * ny * nz;
+	float qx = (float)q[0], qy = (float)q[1], qz = (float)q[2];
+	float thr = screen_threshold(r2);
 	for(int c0 = 0; c0 < ncell; c0 += 32) {
 		int c = c0 + lane;
 		unsigned first = 0, cnt = 0;
@@ -412,12 +428,20 @@ __device__ __forceinline__ void for_range(const DPhotonMap &M, const GatherCells
 			}
 			unsigned fo = __shfl_sync(0xffffffffu, first, owner);
 			unsigned eo = __shfl_sync(0xffffffffu, excl, owner);
+			bool in = false;
+			unsigned j = 0;
+			double d2 = 0.0;
 			if(v < total) {
-				unsigned j = fo + (v - eo);
+				j = fo + (v - eo);
 				float4 p = __ldg(reinterpret_cast<const float4 *>(M.ph + j));
-				double d2 = dist2(p, q);
-				if(d2 <= r2) f(j, d2);
+				float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
+				float d2f = dx * dx + dy * dy + dz * dz;
+				if(!(d2f > thr)) {
+					d2 = dist2(p, q);
+					in = d2 <= r2;
+				}
 			}
+			f(in, (int)j, d2);
 		}
 	}
 }
@@ -437,11 +461,14 @@ __device__ __forceinline__ void photon_term(const DevPhoton *ph, int j, int kind
 	}
 }
 
-/* estimate of one query by one full warp; returns the rgb estimate in all lanes */
-__device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *keys, int *kcount, float out[3])
+/* estimate of one query by one full warp; returns the rgb estimate in all
+ * lanes.  keys/idx: KEY_CAP entries of this warp's shared memory, holding the
+ * candidates (photons within range) in the order the warp visits them. */
+__device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *keys, int *idx, float out[3])
 {
 	const DPhotonMap &M = kind == 0 ? S.caust : S.gi;
 	int lane = threadIdx.x & 31;
+	unsigned lt_mask = (1u << lane) - 1u;
 	out[0] = out[1] = out[2] = 0.0f;
 	if(M.n == 0) return;
 	double q[3] = {(double)pos.x, (double)pos.y, (double)pos.z};
@@ -452,41 +479,44 @@ __device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *ke
 	int cnt = 0;
 	float inv_area = M.inv_area;
 	if(M.k <= 0) {
-		for_range(M, gc, q, r2, lane, [&](int j, double) {
-			cnt++;
-			photon_term(M.ph, j, kind, n, S.max_cos, sum);
+		for_range(M, gc, q, r2, lane, [&](bool in, int j, double) {
+			if(in) {
+				cnt++;
+				photon_term(M.ph, j, kind, n, S.max_cos, sum);
+			}
 		});
 		cnt = warp_sumi(cnt);
 	} else {
-		/* k nearest within the radius cap: select the k-th smallest
-		 * float-rounded squared distance by a bitwise radix search */
-		if(lane == 0) *kcount = 0;
-		__syncwarp();
+		/* k nearest within the radius cap: the k-th smallest float-rounded
+		 * squared distance, found by a bitwise radix search over the
+		 * candidates' keys */
 		unsigned maxkey = 0;
 		int ncand = 0;
-		for_range(M, gc, q, r2, lane, [&](int, double d2) {
+		for_range(M, gc, q, r2, lane, [&](bool in, int j, double d2) {
 			unsigned key = __float_as_uint((float)d2);
-			maxkey = key > maxkey ? key : maxkey;
-			ncand++;
-			int slot = atomicAdd(kcount, 1);
-			if(slot < KEY_CAP) keys[slot] = key;
+			unsigned b = __ballot_sync(0xffffffffu, in);
+			int slot = ncand + __popc(b & lt_mask);
+			if(in) {
+				maxkey = key > maxkey ? key : maxkey;
+				if(slot < KEY_CAP) { keys[slot] = key; idx[slot] = j; }
+			}
+			ncand += __popc(b);
 		});
 		__syncwarp();
-		ncand = warp_sumi(ncand);
 		maxkey = warp_maxu(maxkey);
+		bool cached = ncand <= KEY_CAP;
 		unsigned kth = maxkey;
 		if(ncand > M.k) {
-			bool cached = ncand <= KEY_CAP;
 			unsigned prefix = 0;
 			int remaining = M.k;
 			for(int bit = 31; bit >= 0; bit--) {
 				unsigned hmask = bit == 31 ? 0x80000000u : (~((1u << bit) - 1u));
 				int c0 = 0;
 				if(cached) {
-					for(int j = lane; j < ncand; j += 32) if((keys[j] & hmask) == prefix) c0++;
+					for(int c = lane; c < ncand; c += 32) if((keys[c] & hmask) == prefix) c0++;
 				} else {
-					for_range(M, gc, q, r2, lane, [&](int, double d2) {
-						if((__float_as_uint((float)d2) & hmask) == prefix) c0++;
+					for_range(M, gc, q, r2, lane, [&](bool in, int, double d2) {
+						if(in && (__float_as_uint((float)d2) & hmask) == prefix) c0++;
 					});
 				}
 				c0 = warp_sumi(c0);
@@ -497,12 +527,21 @@ __device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *ke
 			}
 			kth = prefix;
 		}
-		for_range(M, gc, q, r2, lane, [&](int j, double d2) {
-			if(__float_as_uint((float)d2) <= kth) {
-				cnt++;
-				photon_term(M.ph, j, kind, n, S.max_cos, sum);
+		if(cached) {
+			for(int c = lane; c < ncand; c += 32) {
+				if(keys[c] <= kth) {
+					cnt++;
+					photon_term(M.ph, idx[c], kind, n, S.max_cos, sum);
+				}
 			}
-		});
+		} else {
+			for_range(M, gc, q, r2, lane, [&](bool in, int j, double d2) {
+				if(in && __float_as_uint((float)d2) <= kth) {
+					cnt++;
+					photon_term(M.ph, j, kind, n, S.max_cos, sum);
+				}
+			});
+		}
 		cnt = warp_sumi(cnt);
 		inv_area = (float)(1.0 / (3.14159265358979323846 * (double)__uint_as_float(kth)));
 	}
@@ -520,7 +559,7 @@ __global__ void __launch_bounds__(GATHER_WARPS * 32) k_gather(DScene S, const Ga
 		float4 *acc, DevCounters *ctr)
 {
 	__shared__ unsigned keys[GATHER_WARPS][KEY_CAP];
-	__shared__ int kcount[GATHER_WARPS];
+	__shared__ int idx[GATHER_WARPS][KEY_CAP];
 	int n = *gq_count;
 	int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	int gw = blockIdx.x * GATHER_WARPS + w, nw = gridDim.x * GATHER_WARPS;
@@ -529,7 +568,7 @@ __global__ void __launch_bounds__(GATHER_WARPS * 32) k_gather(DScene S, const Ga
 		int kind = __float_as_int(g.a.w);
 		int pixel = __float_as_int(g.b.w);
 		float est[3];
-		gather_one(S, kind, mk(g.a.x, g.a.y, g.a.z), mk(g.b.x, g.b.y, g.b.z), keys[w], &kcount[w], est);
+		gather_one(S, kind, mk(g.a.x, g.a.y, g.a.z), mk(g.b.x, g.b.y, g.b.z), keys[w], idx[w], est);
 		if(lane == 0) acc_add(acc, pixel, g.w.x * est[0], g.w.y * est[1], g.w.z * est[2]);
 		__syncwarp();
 	}
@@ -552,19 +591,19 @@ __global__ void k_pack_gather(int kind, int n, const float *pos, const float *no
 __global__ void __launch_bounds__(GATHER_WARPS * 32) k_gather_points(DScene S, const GatherReq *gq, int n, float *out)
 {
 	__shared__ unsigned keys[GATHER_WARPS][KEY_CAP];
-	__shared__ int kcount[GATHER_WARPS];
+	__shared__ int idx[GATHER_WARPS][KEY_CAP];
 	int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	int gw = blockIdx.x * GATHER_WARPS + w, nw = gridDim.x * GATHER_WARPS;
 	for(int r = gw; r < n; r += nw) {
 		GatherReq g = gq[r];
 		int kind = __float_as_int(g.a.w);
-		int idx = __float_as_int(g.b.w);
+		int pt = __float_as_int(g.b.w);
 		float est[3];
-		gather_one(S, kind, mk(g.a.x, g.a.y, g.a.z), mk(g.b.x, g.b.y, g.b.z), keys[w], &kcount[w], est);
+		gather_one(S, kind, mk(g.a.x, g.a.y, g.a.z), mk(g.b.x, g.b.y, g.b.z), keys[w], idx[w], est);
 		if(lane == 0) {
-			out[idx * 3] = est[0];
-			out[idx * 3 + 1] = est[1];
-			out[idx * 3 + 2] = est[2];
+			out[pt * 3] = est[0];
+			out[pt * 3 + 1] = est[1];
+			out[pt * 3 + 2] = est[2];
 		}
 		__syncwarp();
 	}
