@@ -363,7 +363,11 @@ def run_ours(args):
             "frame": {"rays": rays_of(st_last), "primary": st_last["primary_rays"],
                       "secondary": st_last["secondary_rays"], "shadow": st_last["shadow_rays"],
                       "gathers": st_last["gathers"], "samples": st_last["samples"],
-                      "photons_stored": st_last["photons_stored"], "load_s": t_load, "device_mb": device_mb},
+                      "photons_stored": st_last["photons_stored"], "load_s": t_load, "device_mb": device_mb,
+                      "gather_slots_per_query": st_last["gather_tested"] / max(st_last["gathers"], 1),
+                      "gather_candidates_per_query": st_last["gather_candidates"] / max(st_last["gathers"], 1),
+                      "gather_select_frac": st_last["gather_selects"] / max(st_last["gathers"], 1),
+                      "gather_spill_frac": st_last["gather_spills"] / max(st_last["gathers"], 1)},
         }
         print(json.dumps(line))
     g.close()

@@ -175,6 +175,10 @@ typedef struct sray_stats {
 	int kernel_launches;           /* kernels launched by the last render */
 	int pad;
 	int64_t h2d_bytes, d2h_bytes;  /* host<->device bytes copied by the last render */
+	int64_t gather_tested;         /* photons whose distance a gather computed */
+	int64_t gather_candidates;     /* of those, photons within the gather radius */
+	int64_t gather_selects;        /* gathers with more candidates than k */
+	int64_t gather_spills;         /* gathers whose candidates overflowed the on-chip cache */
 	int reserved[2];
 } sray_stats;
 

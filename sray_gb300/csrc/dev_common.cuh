@@ -30,6 +30,9 @@ struct DPhotonMap {
 	int k;                    /* 0 = fixed-radius range gather, >0 = k nearest */
 	double range;             /* query radius as the kd-tree sees it (float-rounded) */
 	float inv_area;           /* range mode: 1 / (pi r^2) of the unrounded radius */
+	float range_f;            /* the same radius as a float */
+	float r2_hi, r2_lo;       /* range_f^2 exactly, as an unevaluated float sum */
+	float screen;             /* float squared distances above this are out of range */
 };
 
 struct DScene {

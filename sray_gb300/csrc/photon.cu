@@ -597,6 +597,13 @@ int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored)
 	for(int a = 0; a < 3; a++) while((double)M.org[a] > rb.mn[a]) M.org[a] = nextafterf(M.org[a], -INFINITY);
 	M.range = (double)(float)rad;
 	M.inv_area = (float)(1.0 / (M_PI * (rad * rad)));
+	M.range_f = (float)rad;
+	{
+		double r2 = (double)M.range_f * (double)M.range_f;   /* exact: 48 significant bits */
+		M.r2_hi = (float)r2;
+		M.r2_lo = (float)(r2 - (double)M.r2_hi);
+		M.screen = (float)(r2 * (1.0 + 1.0 / 1048576.0));
+	}
 	bool morton = dims[0] <= 1024 && dims[1] <= 1024 && dims[2] <= 1024;
 	size_t ncells = (size_t)dims[0] * dims[1] * dims[2];
 	PCK(P.keys.ensure((size_t)n * 4), "keys");

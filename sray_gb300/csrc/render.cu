@@ -351,52 +351,114 @@ struct GatherCells {
 	int lo[3], hi[3];
 };
 
-__device__ __forceinline__ void gather_cells(const DPhotonMap &M, const double q[3], double range, GatherCells &gc)
+/* The grid cells a query must visit: every cell that can hold a photon
+ * within the radius.  Photons were binned with floor((p - org) / cell) in
+ * double; the window is computed in float and widened by a slack that covers
+ * the float rounding (three operations, each within 2^-24 of its operands),
+ * so it always contains the exact window and at most grows by one cell where
+ * the query's edge lies within the slack of a cell boundary. */
+__device__ __forceinline__ void gather_cells(const DPhotonMap &M, V3 q, GatherCells &gc)
 {
+	float qa[3] = {q.x, q.y, q.z};
 	for(int a = 0; a < 3; a++) {
-		double lo = floor((q[a] - range - (double)M.org[a]) / (double)M.cell);
-		double hi = floor((q[a] + range - (double)M.org[a]) / (double)M.cell);
-		int l = lo < 0.0 ? 0 : (lo > (double)(M.dims[a] - 1) ? M.dims[a] - 1 : (int)lo);
-		int h = hi < 0.0 ? 0 : (hi > (double)(M.dims[a] - 1) ? M.dims[a] - 1 : (int)hi);
-		gc.lo[a] = l;
-		gc.hi[a] = h;
+		float base = qa[a] - M.org[a];
+		float lo = (base - M.range_f) / M.cell, hi = (base + M.range_f) / M.cell;
+		float slack = 1e-3f + (fabsf(base) + M.range_f) / M.cell * 1e-6f;
+		lo = floorf(lo - slack);
+		hi = floorf(hi + slack);
+		float top = (float)(M.dims[a] - 1);
+		gc.lo[a] = lo >= 0.0f ? (lo > top ? M.dims[a] - 1 : (int)lo) : 0;
+		gc.hi[a] = hi >= 0.0f ? (hi > top ? M.dims[a] - 1 : (int)hi) : 0;
 	}
 }
 
 /* squared distance in double between a float photon position and the
- * float-rounded query point (kd_nearest_range3f semantics) */
-__device__ __forceinline__ double dist2(const float4 &p, const double q[3])
+ * float query point (kd_nearest_range3f semantics) */
+__device__ __forceinline__ double dist2(const float4 &p, V3 q)
 {
-	double dx = (double)p.x - q[0], dy = (double)p.y - q[1], dz = (double)p.z - q[2];
+	double dx = (double)p.x - (double)q.x, dy = (double)p.y - (double)q.y, dz = (double)p.z - (double)q.z;
 	return dx * dx + dy * dy + dz * dz;
 }
 
-/* Screening bound for the in-range test.  The float squared distance
- * d2f = fl(fl(fl(dx)^2 + fl(dy)^2) + fl(dz)^2), with dx = p.x - q.x from
- * float operands, is within 6 units in the last place of the exact sum of
- * squares (each of the five roundings adds at most 2^-24 relative error and
- * all terms are non-negative), which the double computation reproduces to
- * 2^-50.  So a photon whose d2f exceeds r2 (1 + 2^-20) is out of range
- * exactly as the double test would find; the others are decided in double. */
-__device__ __forceinline__ float screen_threshold(double r2)
+/* ---- exact range decisions without double arithmetic ----
+ * The reference decides "within range" and orders neighbours on the double
+ * sum of squares d2 = (px-qx)^2 + (py-qy)^2 + (pz-qz)^2 rounded to float.
+ * This GPU has little double throughput, so d2 is evaluated in float-float
+ * arithmetic (Dekker's two-sum and the fma two-product): the unevaluated sum
+ * H + L is within 2^-43 of the exact value and the double evaluation within
+ * 2^-50, so with a margin of 2^-36 both the range test and the float rounding
+ * of d2 come out as the double computation gives them, unless H + L lies
+ * within the margin of the radius or of a float rounding boundary; those
+ * rare cases (and tiny or non-finite sums) are recomputed in double. */
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
 {
-	return (float)(r2 * (1.0 + 1.0 / 1048576.0));
+	s = a + b;
+	float bb = s - a;
+	e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ void fast_two_sum(float a, float b, float &s, float &e)
+{
+	s = a + b;
+	e = b - (s - a);
+}
+
+__device__ __forceinline__ void diff_sq_ff(float p, float q, float &h, float &l)
+{
+	float s, e;
+	two_sum(p, -q, s, e);     /* s + e = p - q exactly */
+	h = s * s;
+	l = __fmaf_rn(s, s, -h);  /* h + l = s^2 exactly */
+	l = l + ((2.0f * s) * e + e * e);
+}
+
+__device__ __forceinline__ void add_ff(float h1, float l1, float h2, float l2, float &h, float &l)
+{
+	float s, e;
+	two_sum(h1, h2, s, e);
+	e = e + (l1 + l2);
+	fast_two_sum(s, e, h, l);
+}
+
+/* returns false when the double computation must decide; otherwise sets
+ * `in` (d2 <= range^2 in double) and `key` (bits of (float)d2) */
+__device__ __forceinline__ bool range_ff(const DPhotonMap &M, float4 p, V3 q, bool &in, unsigned &key)
+{
+	float hx, lx, hy, ly, hz, lz, h, l;
+	diff_sq_ff(p.x, q.x, hx, lx);
+	diff_sq_ff(p.y, q.y, hy, ly);
+	diff_sq_ff(p.z, q.z, hz, lz);
+	add_ff(hx, lx, hy, ly, h, l);
+	add_ff(h, l, hz, lz, h, l);
+	if(!(h >= 8.673617e-19f && h <= 1e30f)) return false;      /* 2^-60 .. overflow-safe */
+	float delta = h * 1.4551915e-11f;                          /* 2^-36 */
+	/* range test against range^2 = r2_hi + r2_lo */
+	float diff = (h - M.r2_hi) + (l - M.r2_lo);
+	if(diff > delta) { in = false; key = 0; return true; }
+	if(!(diff < -delta)) return false;
+	in = true;
+	/* rounding of d2 to float: h unless d2 may cross half an ulp of h */
+	unsigned hb = __float_as_uint(h);
+	float ulp = __uint_as_float(hb & 0x7f800000u) * 1.1920929e-7f;   /* 2^-23 */
+	float ulp_dn = (hb & 0x007fffffu) ? ulp : 0.5f * ulp;
+	if(!(l + delta < 0.5f * ulp) || !(l - delta > -0.5f * ulp_dn)) return false;
+	key = hb;
+	return true;
 }
 
 /* The cells overlapping the query cube (at most 2x2x2: cells are twice the
  * gather radius) are looked up by the first lanes; the warp then strides
  * over the concatenation of their photon runs, so every lane tests one
- * photon per step whatever the cell occupancy.  f(in, photon, d2) is called
+ * photon per step whatever the cell occupancy.  f(in, photon, key) is called
  * by every lane at every step (so it may use warp collectives); `in` tells
- * whether the lane holds a photon within range, d2 its exact squared
- * distance. */
+ * whether the lane holds a photon within range, key the bits of its squared
+ * distance rounded to float. */
 template <class F>
-__device__ __forceinline__ void for_range(const DPhotonMap &M, const GatherCells &gc, const double q[3], double r2, int lane, F f)
+__device__ __forceinline__ void for_range(const DPhotonMap &M, const GatherCells &gc, V3 q, int lane, F f)
 {
 	int nx = gc.hi[0] - gc.lo[0] + 1, ny = gc.hi[1] - gc.lo[1] + 1, nz = gc.hi[2] - gc.lo[2] + 1;
 	int ncell = nx * ny * nz;
-	float qx = (float)q[0], qy = (float)q[1], qz = (float)q[2];
-	float thr = screen_threshold(r2);
+	float thr = M.screen;
 	for(int c0 = 0; c0 < ncell; c0 += 32) {
 		int c = c0 + lane;
 		unsigned first = 0, cnt = 0;
@@ -429,19 +491,21 @@ __device__ __forceinline__ void for_range(const DPhotonMap &M, const GatherCells
 			unsigned fo = __shfl_sync(0xffffffffu, first, owner);
 			unsigned eo = __shfl_sync(0xffffffffu, excl, owner);
 			bool in = false;
-			unsigned j = 0;
-			double d2 = 0.0;
+			unsigned j = 0, key = 0;
 			if(v < total) {
 				j = fo + (v - eo);
 				float4 p = __ldg(reinterpret_cast<const float4 *>(M.ph + j));
-				float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
+				float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
 				float d2f = dx * dx + dy * dy + dz * dz;
-				if(!(d2f > thr)) {
-					d2 = dist2(p, q);
-					in = d2 <= r2;
+				/* screen: d2f is within 6 ulp of the exact sum of squares, so
+				 * above range^2 (1 + 2^-20) the photon is out of range */
+				if(!(d2f > thr) && !range_ff(M, p, q, in, key)) {
+					double d2 = dist2(p, q);
+					in = d2 <= M.range * M.range;
+					key = __float_as_uint((float)d2);
 				}
 			}
-			f(in, (int)j, d2);
+			f(in, (int)j, key);
 		}
 	}
 }
@@ -464,22 +528,24 @@ __device__ __forceinline__ void photon_term(const DevPhoton *ph, int j, int kind
 /* estimate of one query by one full warp; returns the rgb estimate in all
  * lanes.  keys/idx: KEY_CAP entries of this warp's shared memory, holding the
  * candidates (photons within range) in the order the warp visits them. */
-__device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *keys, int *idx, float out[3])
+struct GatherWork {
+	unsigned long long tested, cand, select, spill;
+};
+
+__device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *keys, int *idx, float out[3], GatherWork &gw)
 {
 	const DPhotonMap &M = kind == 0 ? S.caust : S.gi;
 	int lane = threadIdx.x & 31;
 	unsigned lt_mask = (1u << lane) - 1u;
 	out[0] = out[1] = out[2] = 0.0f;
 	if(M.n == 0) return;
-	double q[3] = {(double)pos.x, (double)pos.y, (double)pos.z};
-	double r2 = M.range * M.range;
 	GatherCells gc;
-	gather_cells(M, q, M.range, gc);
+	gather_cells(M, pos, gc);
 	float sum[3] = {0.0f, 0.0f, 0.0f};
 	int cnt = 0;
 	float inv_area = M.inv_area;
 	if(M.k <= 0) {
-		for_range(M, gc, q, r2, lane, [&](bool in, int j, double) {
+		for_range(M, gc, pos, lane, [&](bool in, int j, unsigned) {
 			if(in) {
 				cnt++;
 				photon_term(M.ph, j, kind, n, S.max_cos, sum);
@@ -492,8 +558,8 @@ __device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *ke
 		 * candidates' keys */
 		unsigned maxkey = 0;
 		int ncand = 0;
-		for_range(M, gc, q, r2, lane, [&](bool in, int j, double d2) {
-			unsigned key = __float_as_uint((float)d2);
+		for_range(M, gc, pos, lane, [&](bool in, int j, unsigned key) {
+			gw.tested += 32;
 			unsigned b = __ballot_sync(0xffffffffu, in);
 			int slot = ncand + __popc(b & lt_mask);
 			if(in) {
@@ -505,6 +571,9 @@ __device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *ke
 		__syncwarp();
 		maxkey = warp_maxu(maxkey);
 		bool cached = ncand <= KEY_CAP;
+		gw.cand += (unsigned)ncand;
+		gw.spill += cached ? 0u : 1u;
+		gw.select += ncand > M.k ? 1u : 0u;
 		unsigned kth = maxkey;
 		if(ncand > M.k) {
 			unsigned prefix = 0;
@@ -515,8 +584,8 @@ __device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *ke
 				if(cached) {
 					for(int c = lane; c < ncand; c += 32) if((keys[c] & hmask) == prefix) c0++;
 				} else {
-					for_range(M, gc, q, r2, lane, [&](bool in, int, double d2) {
-						if(in && (__float_as_uint((float)d2) & hmask) == prefix) c0++;
+					for_range(M, gc, pos, lane, [&](bool in, int, unsigned key) {
+						if(in && (key & hmask) == prefix) c0++;
 					});
 				}
 				c0 = warp_sumi(c0);
@@ -535,15 +604,17 @@ __device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *ke
 				}
 			}
 		} else {
-			for_range(M, gc, q, r2, lane, [&](bool in, int j, double d2) {
-				if(in && __float_as_uint((float)d2) <= kth) {
+			for_range(M, gc, pos, lane, [&](bool in, int j, unsigned key) {
+				if(in && key <= kth) {
 					cnt++;
 					photon_term(M.ph, j, kind, n, S.max_cos, sum);
 				}
 			});
 		}
 		cnt = warp_sumi(cnt);
-		inv_area = (float)(1.0 / (3.14159265358979323846 * (double)__uint_as_float(kth)));
+		/* 1 / (pi d2_k) in float (the reference rounds the double quotient;
+		 * the two differ by at most two units in the last place) */
+		inv_area = 1.0f / (3.14159265358979323846f * __uint_as_float(kth));
 	}
 	sum[0] = warp_sum(sum[0]);
 	sum[1] = warp_sum(sum[1]);
@@ -555,7 +626,7 @@ __device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *ke
 	out[2] = sum[2] * inv_area;
 }
 
-__global__ void __launch_bounds__(GATHER_WARPS * 32) k_gather(DScene S, const GatherReq *gq, const int *gq_count,
+__global__ void __launch_bounds__(GATHER_WARPS * 32, 3) k_gather(DScene S, const GatherReq *gq, const int *gq_count,
 		float4 *acc, DevCounters *ctr)
 {
 	__shared__ unsigned keys[GATHER_WARPS][KEY_CAP];
@@ -563,14 +634,21 @@ __global__ void __launch_bounds__(GATHER_WARPS * 32) k_gather(DScene S, const Ga
 	int n = *gq_count;
 	int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	int gw = blockIdx.x * GATHER_WARPS + w, nw = gridDim.x * GATHER_WARPS;
+	GatherWork work = {0, 0, 0, 0};
 	for(int r = gw; r < n; r += nw) {
 		GatherReq g = gq[r];
 		int kind = __float_as_int(g.a.w);
 		int pixel = __float_as_int(g.b.w);
 		float est[3];
-		gather_one(S, kind, mk(g.a.x, g.a.y, g.a.z), mk(g.b.x, g.b.y, g.b.z), keys[w], idx[w], est);
+		gather_one(S, kind, mk(g.a.x, g.a.y, g.a.z), mk(g.b.x, g.b.y, g.b.z), keys[w], idx[w], est, work);
 		if(lane == 0) acc_add(acc, pixel, g.w.x * est[0], g.w.y * est[1], g.w.z * est[2]);
 		__syncwarp();
+	}
+	if(lane == 0 && work.tested) {
+		atomicAdd(&ctr->g_tested, work.tested);
+		atomicAdd(&ctr->g_cand, work.cand);
+		atomicAdd(&ctr->g_select, work.select);
+		atomicAdd(&ctr->g_spill, work.spill);
 	}
 	if(blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctr->rays[3], (unsigned long long)n);
 }
@@ -588,18 +666,19 @@ __global__ void k_pack_gather(int kind, int n, const float *pos, const float *no
 	}
 }
 
-__global__ void __launch_bounds__(GATHER_WARPS * 32) k_gather_points(DScene S, const GatherReq *gq, int n, float *out)
+__global__ void __launch_bounds__(GATHER_WARPS * 32, 3) k_gather_points(DScene S, const GatherReq *gq, int n, float *out)
 {
 	__shared__ unsigned keys[GATHER_WARPS][KEY_CAP];
 	__shared__ int idx[GATHER_WARPS][KEY_CAP];
 	int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	int gw = blockIdx.x * GATHER_WARPS + w, nw = gridDim.x * GATHER_WARPS;
+	GatherWork work = {0, 0, 0, 0};
 	for(int r = gw; r < n; r += nw) {
 		GatherReq g = gq[r];
 		int kind = __float_as_int(g.a.w);
 		int pt = __float_as_int(g.b.w);
 		float est[3];
-		gather_one(S, kind, mk(g.a.x, g.a.y, g.a.z), mk(g.b.x, g.b.y, g.b.z), keys[w], idx[w], est);
+		gather_one(S, kind, mk(g.a.x, g.a.y, g.a.z), mk(g.b.x, g.b.y, g.b.z), keys[w], idx[w], est, work);
 		if(lane == 0) {
 			out[pt * 3] = est[0];
 			out[pt * 3 + 1] = est[1];
@@ -1139,6 +1218,10 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 	stats.d2h_bytes = d2h;
 	stats.node_visits = (int64_t)hc.nodes;
 	stats.prim_tests = (int64_t)hc.prims;
+	stats.gather_tested = (int64_t)hc.g_tested;
+	stats.gather_candidates = (int64_t)hc.g_cand;
+	stats.gather_selects = (int64_t)hc.g_select;
+	stats.gather_spills = (int64_t)hc.g_spill;
 	if(hc.overflow) return fail(SRAY_EDEVICE, "device queue or traversal stack overflow");
 	return 0;
 }

@@ -73,6 +73,7 @@ struct DevCounters {
 	int pad[2];
 	unsigned long long rays[4];   /* primary, secondary, shadow, gather */
 	unsigned long long nodes, prims;
+	unsigned long long g_tested, g_cand, g_select, g_spill;   /* gather work */
 };
 
 struct PhotonBufs {

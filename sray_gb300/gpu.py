@@ -29,7 +29,10 @@ class SrayStats(ctypes.Structure):
                 ("gathers", ctypes.c_int64), ("samples", ctypes.c_int64),
                 ("node_visits", ctypes.c_int64), ("prim_tests", ctypes.c_int64),
                 ("kernel_launches", ctypes.c_int), ("pad", ctypes.c_int),
-                ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64), ("reserved", ctypes.c_int * 2)]
+                ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64),
+                ("gather_tested", ctypes.c_int64), ("gather_candidates", ctypes.c_int64),
+                ("gather_selects", ctypes.c_int64), ("gather_spills", ctypes.c_int64),
+                ("reserved", ctypes.c_int * 2)]
 
 
 class SrayError(RuntimeError):
