@@ -367,7 +367,8 @@ def run_ours(args):
                       "gather_slots_per_query": st_last["gather_tested"] / max(st_last["gathers"], 1),
                       "gather_candidates_per_query": st_last["gather_candidates"] / max(st_last["gathers"], 1),
                       "gather_select_frac": st_last["gather_selects"] / max(st_last["gathers"], 1),
-                      "gather_spill_frac": st_last["gather_spills"] / max(st_last["gathers"], 1)},
+                      "gather_spill_frac": st_last["gather_spills"] / max(st_last["gathers"], 1),
+                      "bvh_fallbacks": st_last["bvh_fallbacks"]},
         }
         print(json.dumps(line))
     g.close()

@@ -179,6 +179,8 @@ typedef struct sray_stats {
 	int64_t gather_candidates;     /* of those, photons within the gather radius */
 	int64_t gather_selects;        /* gathers with more candidates than k */
 	int64_t gather_spills;         /* gathers whose candidates overflowed the on-chip cache */
+	int64_t bvh_fallbacks;         /* mesh hits found through the hierarchy that the
+	                                  octree did not confirm (traced by the octree) */
 	int reserved[2];
 } sray_stats;
 

@@ -43,6 +43,13 @@ struct DScene {
 	const DevNode *mnodes;    /* mesh octrees (object space) */
 	const DevTri *mtris;
 	const int *mprim;
+	const DevBvhNode *bnodes; /* mesh hierarchies (object space) */
+	const DevTri *btris;      /* triangles in hierarchy leaf order */
+	const int *bprim;         /* their face indices */
+	const int *bhome;         /* their home nodes in the mesh octrees */
+	const DevBvhNode *tnodes; /* object hierarchy (world space), null if none */
+	const int *ohome;         /* per object: its home node in the scene octree */
+	unsigned long long *bvh_fallbacks;   /* hits the octree did not confirm */
 	const DevObj *objs;
 	int nobj;
 	const float *xf;          /* per object per time, XF_STRIDE floats */
@@ -260,7 +267,7 @@ __device__ __forceinline__ void consider(Hit &h, float t, int obj, int prim)
  * contains it can never hide a candidate the exhaustive search would find */
 #define SRAY_PRUNE(te, best) ((te) > (best) * 1.00001f + 1e-30f)
 
-#define SRAY_STACK 112
+#define SRAY_STACK 128
 #define SRAY_MAILBOX 8
 
 struct TraceCounters {
@@ -343,6 +350,37 @@ __device__ __forceinline__ float4 load_split(const DevNode *nodes, int ni)
 	return __ldg(reinterpret_cast<const float4 *>(nodes + ni) + 2);
 }
 
+/* Triangle mailbox.  A triangle whose bounds overlap several octree leaves
+ * is listed in each of them, and a ray crossing those leaves would test it
+ * again with the same result (a repeated test can neither improve the best
+ * hit nor flag a tie that the first test did not).  Each thread keeps the
+ * last triangle seen per slot of a 16-way direct-mapped table in shared
+ * memory, cleared whenever the ray enters a mesh, and skips repeats.  The
+ * traversal kernels run 128 threads per block. */
+#define SRAY_TRACE_THREADS 128
+#define SRAY_TRI_MBOX 16
+
+__device__ __forceinline__ int *tri_mailbox()
+{
+	__shared__ int mb[SRAY_TRI_MBOX * SRAY_TRACE_THREADS];
+	return mb + threadIdx.x;
+}
+
+__device__ __forceinline__ void tri_mailbox_clear(int *mb)
+{
+	#pragma unroll
+	for(int k = 0; k < SRAY_TRI_MBOX; k++) mb[k * SRAY_TRACE_THREADS] = -1;
+}
+
+/* true when `prim` was tested since the last clear; records it otherwise */
+__device__ __forceinline__ bool tri_mailbox_seen(int *mb, int prim)
+{
+	int *e = mb + (prim & (SRAY_TRI_MBOX - 1)) * SRAY_TRACE_THREADS;
+	if(*e == prim) return true;
+	*e = prim;
+	return false;
+}
+
 /* closest hit inside one mesh (object space), sharing the best hit so far */
 template <bool COUNT>
 __device__ __forceinline__ void mesh_closest(const DScene &S, int root, int obj, const RayT &r, Hit &h, TStack &st, int base,
@@ -353,6 +391,8 @@ __device__ __forceinline__ void mesh_closest(const DScene &S, int root, int obj,
 	const DevNode &rn = S.mnodes[root];
 	if(!box_hit(rn.mn, rn.mx, r, te)) return;
 	int oct = octant(r);
+	int *mb = tri_mailbox();
+	tri_mailbox_clear(mb);
 	st.node[sp] = root;
 	st.te[sp] = te;
 	sp++;
@@ -369,14 +409,18 @@ __device__ __forceinline__ void mesh_closest(const DScene &S, int root, int obj,
 		} else {
 			const float4 *tp = reinterpret_cast<const float4 *>(S.mtris + first);
 			for(int s = 0; s < count; s++) {
+				int prim = __ldg(S.mprim + first + s);
+				if(tri_mailbox_seen(mb, prim)) continue;
 				float4 a = __ldg(tp + 3 * s), b = __ldg(tp + 3 * s + 1), c = __ldg(tp + 3 * s + 2);
 				if(COUNT) tc->prims++;
 				float t;
-				if(tri_hit(a, b, c, r, S.eps, h.t, t)) consider(h, t, obj, __ldg(S.mprim + first + s));
+				if(tri_hit(a, b, c, r, S.eps, h.t, t)) consider(h, t, obj, prim);
 			}
 		}
 	}
 }
+
+/* ---------------- octree traversal (the reference's structure) ---------------- */
 
 template <bool COUNT>
 __device__ __forceinline__ void object_closest(const DScene &S, int oi, int ti, V3 wo, V3 wd, Hit &h, TStack &st, int base,
@@ -396,14 +440,51 @@ __device__ __forceinline__ void object_closest(const DScene &S, int oi, int ti, 
 	if(hit) consider(h, t, oi, 0);
 }
 
-__device__ __forceinline__ bool mailbox_seen(int *mbox, int &mb_next, int oi)
+/* Object mailbox.  An object spanning several top-level leaves gives the
+ * same closest hit each time it is tested, so it is tested once per ray.
+ * Scenes of up to SRAY_OBJ_EXACT objects keep an exact per-ray set (one bit
+ * per object in shared memory); larger scenes remember the last
+ * SRAY_MAILBOX objects. */
+#define SRAY_OBJ_EXACT 1024
+
+struct ObjMailbox {
+	unsigned *bits;
+	int ring[SRAY_MAILBOX];
+	int next;
+	bool exact;
+};
+
+__device__ __forceinline__ void obj_mailbox_init(const DScene &S, ObjMailbox &m)
 {
+	__shared__ unsigned bits[(SRAY_OBJ_EXACT / 32) * SRAY_TRACE_THREADS];
+	m.bits = bits + threadIdx.x;
+	m.exact = S.nobj <= SRAY_OBJ_EXACT;
+	m.next = 0;
+	if(m.exact) {
+		int words = (S.nobj + 31) >> 5;
+		for(int w = 0; w < words; w++) m.bits[w * SRAY_TRACE_THREADS] = 0u;
+	} else {
+		#pragma unroll
+		for(int k = 0; k < SRAY_MAILBOX; k++) m.ring[k] = -1;
+	}
+}
+
+__device__ __forceinline__ bool mailbox_seen(ObjMailbox &m, int oi)
+{
+	if(m.exact) {
+		unsigned *w = m.bits + (oi >> 5) * SRAY_TRACE_THREADS;
+		unsigned bit = 1u << (oi & 31);
+		unsigned v = *w;
+		if(v & bit) return true;
+		*w = v | bit;
+		return false;
+	}
 	bool seen = false;
 	#pragma unroll
-	for(int k = 0; k < SRAY_MAILBOX; k++) seen |= mbox[k] == oi;
+	for(int k = 0; k < SRAY_MAILBOX; k++) seen |= m.ring[k] == oi;
 	if(!seen) {
-		mbox[mb_next] = oi;
-		mb_next = (mb_next + 1) & (SRAY_MAILBOX - 1);
+		m.ring[m.next] = oi;
+		m.next = (m.next + 1) & (SRAY_MAILBOX - 1);
 	}
 	return seen;
 }
@@ -413,7 +494,8 @@ __device__ __forceinline__ bool mailbox_seen(int *mbox, int &mb_next, int oi)
  * straddling several leaves gives the same closest hit every time, so each
  * object is tested once per ray */
 template <bool COUNT>
-__device__ inline void trace_closest(const DScene &S, V3 wo, V3 wd, int time, Hit &h, TraceCounters *tc, int *overflow)
+__device__ __forceinline__ void trace_closest_octree_impl(const DScene &S, V3 wo, V3 wd, int time, Hit &h, TraceCounters *tc,
+		int *overflow)
 {
 	h.t = FLT_MAX;
 	h.obj = -1;
@@ -426,10 +508,8 @@ __device__ inline void trace_closest(const DScene &S, V3 wo, V3 wd, int time, Hi
 	TStack st;
 	int sp = 0;
 	float te;
-	int mbox[SRAY_MAILBOX];
-	#pragma unroll
-	for(int k = 0; k < SRAY_MAILBOX; k++) mbox[k] = -1;
-	int mb_next = 0;
+	ObjMailbox mbox;
+	obj_mailbox_init(S, mbox);
 	const DevNode &root = S.snodes[S.sroot];
 	if(!box_hit(root.mn, root.mx, r, te)) return;
 	st.node[sp] = S.sroot;
@@ -448,7 +528,7 @@ __device__ inline void trace_closest(const DScene &S, V3 wo, V3 wd, int time, Hi
 		} else {
 			for(int s = 0; s < count; s++) {
 				int oi = __ldg(S.sslots + first + s);
-				if(mailbox_seen(mbox, mb_next, oi)) continue;
+				if(mailbox_seen(mbox, oi)) continue;
 				object_closest<COUNT>(S, oi, ti, wo, wd, h, st, sp, tc, overflow);
 			}
 		}
@@ -464,6 +544,8 @@ __device__ inline bool mesh_any(const DScene &S, int root, const RayT &r, TStack
 	const DevNode &rn = S.mnodes[root];
 	if(!box_hit(rn.mn, rn.mx, r, te)) return false;
 	int oct = octant(r);
+	int *mb = tri_mailbox();
+	tri_mailbox_clear(mb);
 	st.node[sp++] = root;
 	while(sp > base) {
 		int ni = st.node[--sp];
@@ -475,6 +557,7 @@ __device__ inline bool mesh_any(const DScene &S, int root, const RayT &r, TStack
 		} else {
 			const float4 *tp = reinterpret_cast<const float4 *>(S.mtris + first);
 			for(int s = 0; s < count; s++) {
+				if(tri_mailbox_seen(mb, __ldg(S.mprim + first + s))) continue;
 				float4 a = __ldg(tp + 3 * s), b = __ldg(tp + 3 * s + 1), c = __ldg(tp + 3 * s + 2);
 				float t;
 				if(tri_hit(a, b, c, r, S.eps, FLT_MAX, t)) return true;
@@ -484,7 +567,7 @@ __device__ inline bool mesh_any(const DScene &S, int root, const RayT &r, TStack
 	return false;
 }
 
-__device__ inline bool trace_any(const DScene &S, V3 wo, V3 wd, int time, int *overflow)
+__device__ __forceinline__ bool trace_any_octree_impl(const DScene &S, V3 wo, V3 wd, int time, int *overflow)
 {
 	if(!S.has_scene) return false;
 	int ti = time_index(S, time);
@@ -492,10 +575,8 @@ __device__ inline bool trace_any(const DScene &S, V3 wo, V3 wd, int time, int *o
 	int oct = octant(r);
 	TStack st;
 	int sp = 0;
-	int mbox[SRAY_MAILBOX];
-	#pragma unroll
-	for(int k = 0; k < SRAY_MAILBOX; k++) mbox[k] = -1;
-	int mb_next = 0;
+	ObjMailbox mbox;
+	obj_mailbox_init(S, mbox);
 	float te;
 	const DevNode &root = S.snodes[S.sroot];
 	if(!box_hit(root.mn, root.mx, r, te)) return false;
@@ -510,7 +591,7 @@ __device__ inline bool trace_any(const DScene &S, V3 wo, V3 wd, int time, int *o
 		} else {
 			for(int s = 0; s < count; s++) {
 				int oi = __ldg(S.sslots + first + s);
-				if(mailbox_seen(mbox, mb_next, oi)) continue;
+				if(mailbox_seen(mbox, oi)) continue;
 				const DevObj ob = S.objs[oi];
 				const float *inv = obj_xf(S, oi, ti) + 12;
 				RayT orr = make_ray(mul_pt(inv, wo), mul_dir(inv, wd));
@@ -526,6 +607,307 @@ __device__ inline bool trace_any(const DScene &S, V3 wo, V3 wd, int time, int *o
 		}
 	}
 	return false;
+}
+
+/* ---------------- two-level hierarchy traversal confirmed by the octrees ----------------
+ * The octrees define the result: the closest hit among the objects listed in
+ * the top-level leaves the ray reaches, each object's own hit being the
+ * closest among the faces listed in the mesh-octree leaves the ray reaches
+ * (a leaf is reached when its box test and every ancestor's pass).
+ *
+ * Two binary hierarchies find the same hit faster: one over the objects,
+ * each boxed by the union of the top-level leaves that list it, and one per
+ * unique mesh over its faces.  Their boxes are widened per ray, so neither
+ * skips an object the octree would test or a face the triangle test accepts;
+ * the hit found is therefore the closest over a superset of the octrees'
+ * candidates.  If it is unique at its distance and both octrees reach it
+ * (the hit point's leaf lists the face, resp. the object, and that leaf's
+ * box test passes), the octrees return it too.  Otherwise -- a second hit at
+ * the same distance, or a hit an octree would not reach, both confined to
+ * rounding-level coincidences and to objects moving outside their frame
+ * bounds -- the ray is marked and traced again by the octrees alone. */
+
+/* a ray prepared for the widened box test: the inverse direction clamped to
+ * finite values, and per axis the widening in units of t.  The widening,
+ * 2^-19 of the largest coordinate the segment reaches, covers the rounding
+ * of the hit point and of the edge tests (a few units in the last place of
+ * those coordinates) with a wide margin. */
+struct RayC {
+	V3 o, inv, slack;
+};
+
+__device__ __forceinline__ RayC make_rayc(const RayT &r)
+{
+	RayC c;
+	c.o = r.o;
+	c.inv = mk(fminf(fmaxf(r.inv.x, -1e20f), 1e20f), fminf(fmaxf(r.inv.y, -1e20f), 1e20f), fminf(fmaxf(r.inv.z, -1e20f), 1e20f));
+	float om = fmaxf(fmaxf(fabsf(r.o.x), fabsf(r.o.y)), fabsf(r.o.z));
+	float dm = fmaxf(fmaxf(fabsf(r.d.x), fabsf(r.d.y)), fabsf(r.d.z));
+	float delta = (om + dm) * 1.9073486e-6f;   /* 2^-19 */
+	c.slack = mk(delta * fabsf(c.inv.x), delta * fabsf(c.inv.y), delta * fabsf(c.inv.z));
+	return c;
+}
+
+__device__ __forceinline__ bool wide_box(const RayC &c, float x0, float y0, float z0, float x1, float y1, float z1, float limit,
+		float &tn)
+{
+	float ax = (x0 - c.o.x) * c.inv.x, bx = (x1 - c.o.x) * c.inv.x;
+	float ay = (y0 - c.o.y) * c.inv.y, by = (y1 - c.o.y) * c.inv.y;
+	float az = (z0 - c.o.z) * c.inv.z, bz = (z1 - c.o.z) * c.inv.z;
+	float tnear = fmaxf(fmaxf(fminf(ax, bx) - c.slack.x, fminf(ay, by) - c.slack.y), fminf(az, bz) - c.slack.z);
+	float tfar = fminf(fminf(fmaxf(ax, bx) + c.slack.x, fmaxf(ay, by) + c.slack.y), fmaxf(az, bz) + c.slack.z);
+	tn = tnear;
+	return tnear <= tfar && tfar >= 0.0f && tnear <= limit;
+}
+
+/* Would an octree (nodes, and the item ids its leaves list) test item `id`
+ * for this ray, with best hit t?  The leaves listing the item all lie below
+ * its home node; the hit point (computed as the intersection tests compute
+ * it) picks the leaf.  The octree reaches that leaf if the leaf's own box
+ * test passes: slab parameters are monotone in the planes, so each
+ * ancestor's intervals contain the leaf's and its test (and the pruning test,
+ * its entry parameter being no larger) passes too. */
+__device__ inline bool octree_reaches(const DevNode *nodes, const int *ids, int home, const RayT &r, int id, float t, bool prune)
+{
+	V3 P = r.o + r.d * t;
+	int ni = home;
+	for(int level = 0; level < 64; level++) {
+		const float4 *np = reinterpret_cast<const float4 *>(nodes + ni);
+		float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
+		int count = __float_as_int(n1.w), first = __float_as_int(n0.w);
+		if(count >= 0) {
+			float mn[3] = {n0.x, n0.y, n0.z}, mx[3] = {n1.x, n1.y, n1.z};
+			float te;
+			if(!box_hit(mn, mx, r, te)) return false;
+			if(prune && SRAY_PRUNE(te, t)) return false;
+			for(int s = 0; s < count; s++) if(__ldg(ids + first + s) == id) return true;
+			return false;
+		}
+		int c = (P.x >= n2.x ? 1 : 0) | (P.y >= n2.y ? 2 : 0) | (P.z >= n2.z ? 4 : 0);
+		if(!((__float_as_uint(n2.w) >> c) & 1u)) return false;
+		ni = first + c;
+	}
+	return false;
+}
+
+__device__ __forceinline__ void load_bvh_node(const DevBvhNode *nodes, int i, float4 &f0, float4 &f1, float4 &f2, int4 &f3)
+{
+	const float4 *np = reinterpret_cast<const float4 *>(nodes + i);
+	f0 = __ldg(np);
+	f1 = __ldg(np + 1);
+	f2 = __ldg(np + 2);
+	f3 = __ldg(reinterpret_cast<const int4 *>(np) + 3);
+}
+
+/* the object-space ray of object o at time index ti */
+__device__ __forceinline__ RayT object_ray(const DScene &S, int o, int ti, V3 wo, V3 wd)
+{
+	const float *inv = obj_xf(S, o, ti) + 12;
+	return make_ray(mul_pt(inv, wo), mul_dir(inv, wd));
+}
+
+/* ANY = false: closest hit into h, returns false when the octrees must
+ * decide.  ANY = true: returns 1 when a hit the octrees reach exists, 0 when
+ * no hit exists, 2 when the octrees must decide. */
+template <bool COUNT, bool ANY>
+__device__ __forceinline__ int trace_two_level(const DScene &S, V3 wo, V3 wd, int time, Hit &h, TraceCounters *tc, int *overflow)
+{
+	h.t = FLT_MAX;
+	h.obj = -1;
+	h.prim = -1;
+	h.tie = 0;
+	if(!S.has_scene) return ANY ? 0 : 1;
+	if(!S.tnodes) return ANY ? 2 : 0;
+	int ti = time_index(S, time);
+	RayT wr = make_ray(wo, wd);
+	RayC wc = make_rayc(wr);
+	RayT r = wr;
+	RayC rc = wc;
+	TStack st;
+	float best = ANY ? 1.0f : FLT_MAX;
+	int bobj = -1, bprim = -1, bslot = -1;
+	bool eq = false;
+	int sp = 0, inst_base = 0, iobj = -1;
+	bool inst = false;
+	int cur = 0;   /* the object hierarchy's root */
+	for(;;) {
+		if(cur == BVH_NONE) {
+			bool found = false;
+			while(sp > 0) {
+				int k = sp - 1;
+				if(inst && k < inst_base) {   /* the instance's entries are done */
+					inst = false;
+					iobj = -1;
+					r = wr;
+					rc = wc;
+				}
+				sp = k;
+				if(ANY || st.te[k] <= best) {
+					cur = st.node[k];
+					found = true;
+					break;
+				}
+			}
+			if(!found) break;
+		}
+		if(!inst && cur < 0) {
+			/* enter object ~cur */
+			int o = ~cur;
+			cur = BVH_NONE;
+			const DevObj ob = S.objs[o];
+			RayT orr = object_ray(S, o, ti, wo, wd);
+			if(ob.type != 2) {
+				if(COUNT) tc->prims++;
+				float t;
+				bool hit = ob.type == 0 ? sphere_hit(orr, ob.rad, S.eps, t) : cylinder_hit(orr, ob.rad, ob.start, ob.end, S.eps, t);
+				if(hit && t <= best) {
+					if(ANY) {
+						bobj = o;
+						bprim = 0;
+						best = t;
+						break;
+					}
+					if(t < best) {
+						best = t;
+						bobj = o;
+						bprim = 0;
+						bslot = -1;
+						eq = false;
+					} else if(o != bobj || bprim != 0) {
+						eq = true;
+					}
+				}
+				continue;
+			}
+			if(ob.mesh_root < 0) continue;
+			if(ob.bvh_root < 0) return ANY ? 2 : 0;
+			/* the mesh octree's entry test: a mesh it would not enter gives
+			 * no candidates (nor one beating the best, when pruned) */
+			float te;
+			const DevNode &rn = S.mnodes[ob.mesh_root];
+			if(!box_hit(rn.mn, rn.mx, orr, te) || (!ANY && SRAY_PRUNE(te, best))) continue;
+			r = orr;
+			rc = make_rayc(orr);
+			inst = true;
+			inst_base = sp;
+			iobj = o;
+			cur = ob.bvh_root;
+			continue;
+		}
+		/* a node of the object hierarchy (world space) or of a mesh's */
+		float4 f0, f1, f2;
+		int4 f3;
+		load_bvh_node(inst ? S.bnodes : S.tnodes, cur, f0, f1, f2, f3);
+		if(COUNT) tc->nodes++;
+		float lim = fminf(best, 1.0f);
+		float tl = 0.0f, tr = 0.0f;
+		bool hl = f3.x != BVH_NONE && wide_box(rc, f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, lim, tl);
+		bool hr = f3.y != BVH_NONE && wide_box(rc, f1.z, f1.w, f2.x, f2.y, f2.z, f2.w, lim, tr);
+		if(inst) {
+			/* face leaves are tested here */
+			#pragma unroll
+			for(int side = 0; side < 2; side++) {
+				int ref = side ? f3.y : f3.x;
+				bool hit = side ? hr : hl;
+				if(!hit || ref >= 0) continue;
+				unsigned v = ~(unsigned)ref;
+				int start = (int)(v >> 4), cnt = (int)(v & 15u);
+				const float4 *tp = reinterpret_cast<const float4 *>(S.btris + start);
+				for(int k = 0; k < cnt; k++) {
+					float4 a = __ldg(tp + 3 * k), b = __ldg(tp + 3 * k + 1), c = __ldg(tp + 3 * k + 2);
+					if(COUNT) tc->prims++;
+					float t;
+					if(!tri_hit(a, b, c, r, S.eps, best, t)) continue;
+					int prim = __ldg(S.bprim + start + k);
+					if(ANY) {
+						bobj = iobj;
+						bprim = prim;
+						bslot = start + k;
+						best = t;
+						break;
+					}
+					if(t < best) {
+						best = t;
+						bobj = iobj;
+						bprim = prim;
+						bslot = start + k;
+						eq = false;
+					} else if(iobj != bobj || prim != bprim) {
+						eq = true;
+					}
+				}
+				if(ANY && bobj >= 0) break;
+				if(side) hr = false; else hl = false;
+			}
+			if(ANY && bobj >= 0) break;
+			if(!ANY) {
+				if(hl && tl > best) hl = false;
+				if(hr && tr > best) hr = false;
+			}
+		}
+		/* object-hierarchy leaves are objects (negative references): they
+		 * are entered like nodes */
+		if(hl && hr) {
+			int nr = f3.x, fr = f3.y;
+			float ft = tr;
+			if(tr < tl) { nr = f3.y; fr = f3.x; ft = tl; }
+			if(sp >= SRAY_STACK) { *overflow = 1; return ANY ? 0 : 1; }
+			st.node[sp] = fr;
+			st.te[sp] = ft;
+			sp++;
+			cur = nr;
+		} else if(hl) {
+			cur = f3.x;
+		} else if(hr) {
+			cur = f3.y;
+		} else {
+			cur = BVH_NONE;
+		}
+	}
+	if(bobj < 0) return ANY ? 0 : 1;
+	if(!ANY && eq) return 0;
+	/* confirm against the octrees */
+	if(bslot >= 0 && !octree_reaches(S.mnodes, S.mprim, __ldg(S.bhome + bslot), object_ray(S, bobj, ti, wo, wd), bprim, best, !ANY))
+		return ANY ? 2 : 0;
+	if(!octree_reaches(S.snodes, S.sslots, __ldg(S.ohome + bobj), wr, bobj, best, !ANY)) return ANY ? 2 : 0;
+	if(ANY) return 1;
+	h.t = best;
+	h.obj = bobj;
+	h.prim = bprim;
+	h.tie = 0;
+	return 1;
+}
+
+/* the octrees alone, kept out of line so that the hierarchy traversal's
+ * registers are not shaped by them */
+template <bool COUNT>
+static __device__ __noinline__ void trace_closest_octree(const DScene &S, V3 wo, V3 wd, int time, Hit &h, TraceCounters *tc, int *overflow)
+{
+	trace_closest_octree_impl<COUNT>(S, wo, wd, time, h, tc, overflow);
+}
+
+static __device__ __noinline__ bool trace_any_octree(const DScene &S, V3 wo, V3 wd, int time, int *overflow)
+{
+	return trace_any_octree_impl(S, wo, wd, time, overflow);
+}
+
+/* closest hit, the octrees deciding when the hierarchies cannot */
+template <bool COUNT>
+__device__ inline void trace_closest(const DScene &S, V3 wo, V3 wd, int time, Hit &h, TraceCounters *tc, int *overflow)
+{
+	if(!trace_two_level<COUNT, false>(S, wo, wd, time, h, tc, overflow)) {
+		atomicAdd(S.bvh_fallbacks, 1ull);
+		trace_closest_octree<COUNT>(S, wo, wd, time, h, tc, overflow);
+	}
+}
+
+__device__ inline bool trace_any(const DScene &S, V3 wo, V3 wd, int time, int *overflow)
+{
+	Hit h;
+	int res = trace_two_level<false, true>(S, wo, wd, time, h, nullptr, overflow);
+	if(res != 2) return res == 1;
+	atomicAdd(S.bvh_fallbacks, 1ull);
+	return trace_any_octree(S, wo, wd, time, overflow);
 }
 
 /* ---------------- surface point ---------------- */

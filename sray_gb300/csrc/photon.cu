@@ -541,7 +541,7 @@ int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored)
 	for(int pass = 0; n_live > 0; pass++) {
 		if(pass >= 2 * PHOTON_GUARD + 2) return R.fail(SRAY_EDEVICE, "photon paths did not terminate");
 		PCK(cudaMemsetAsync(R.q[cur ^ 1].count, 0, sizeof(int), s), "reset photon queue");
-		launch_trace(R, R.q[cur], n_live, "photon_trace", s);
+		if(launch_trace(R, R.q[cur], n_live, "photon_trace", s)) return SRAY_ECUDA;
 		LAUNCH(R, "photon_bounce", s, k_photon_bounce<<<grid_n(n_live, 128), 128, 0, s>>>(R.S, global, pre.as<int>(),
 				scl.as<float>(), R.q[cur], R.hits.as<int4>(), R.q[cur ^ 1], P.tmp_ph.as<DevPhoton>(), P.valid.as<int>()));
 		PCK(cudaMemcpyAsync(&n_live, R.q[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "photon queue count");

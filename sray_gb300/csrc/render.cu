@@ -14,6 +14,7 @@
  * its local terms to the pixel sample directly.
  */
 #include <math.h>
+#include <float.h>
 #include <string.h>
 #include <stdio.h>
 #include <algorithm>
@@ -78,24 +79,37 @@ __global__ void k_camera(DScene S, const int *active, const int *n_active_p, int
 	}
 }
 
-template <bool COUNT>
-__global__ void __launch_bounds__(128) k_trace(DScene S, RayQueue q, int4 *hits, DevCounters *ctr)
+/* Closest hits.  HYB = true traces through the mesh hierarchies and lists
+ * the rays whose result the octree must decide in fb (count in fb[0], ray
+ * indices from fb + 1); HYB = false traces the listed rays with the octree
+ * alone.  Keeping the two in separate kernels keeps the octree code out of
+ * the hierarchy traversal's register allocation. */
+template <bool COUNT, bool HYB>
+__global__ void __launch_bounds__(SRAY_TRACE_THREADS, 6) k_trace(DScene S, RayQueue q, int4 *hits, DevCounters *ctr, int *fb)
 {
-	int n = *q.count;
+	int n = HYB ? *q.count : fb[0];
 	TraceCounters tc = {0, 0};
 	int overflow = 0;
 	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		float4 o = q.o[i], d = q.d[i];
-		int time = q.meta[i].w;
+		int ri = HYB ? i : fb[1 + i];
+		float4 o = q.o[ri], d = q.d[ri];
+		int time = q.meta[ri].w;
 		Hit h;
-		trace_closest<COUNT>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), time, h, &tc, &overflow);
-		hits[i] = make_int4(__float_as_int(h.t), h.obj, h.prim, h.tie);
+		bool sure = true;
+		if(HYB) sure = trace_two_level<COUNT, false>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), time, h, &tc, &overflow) != 0;
+		else trace_closest_octree_impl<COUNT>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), time, h, &tc, &overflow);
+		if(HYB && !sure) {
+			fb[1 + atomicAdd(fb, 1)] = ri;
+			continue;
+		}
+		hits[ri] = make_int4(__float_as_int(h.t), h.obj, h.prim, h.tie);
 	}
 	if(overflow) atomicOr(&ctr->overflow, 1);
 	if(COUNT) {
 		atomicAdd(&ctr->nodes, tc.nodes);
 		atomicAdd(&ctr->prims, tc.prims);
 	}
+	if(!HYB && n > 0 && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctr->bvh_fallbacks, (unsigned long long)n);
 }
 
 __device__ __forceinline__ void acc_add(float4 *acc, int p, float r, float g, float b)
@@ -311,18 +325,35 @@ __global__ void __launch_bounds__(128) k_shade(DScene S, RayQueue qi, const int4
 
 /* shadow rays: the reference tests visibility with cast_ray(shadow_ray)
  * (src/shader.cc:266), a hit anywhere on the segment [eps, 1] blocks */
-__global__ void __launch_bounds__(128) k_shadow(DScene S, const ShadowReq *sq, const int *sq_count, float4 *acc, DevCounters *ctr)
+/* shadow rays; HYB and fb as for k_trace */
+template <bool HYB>
+__global__ void __launch_bounds__(SRAY_TRACE_THREADS, 6) k_shadow(DScene S, const ShadowReq *sq, const int *sq_count, float4 *acc,
+		DevCounters *ctr, int *fb)
 {
-	int n = *sq_count;
+	int n = HYB ? *sq_count : fb[0];
 	int overflow = 0;
 	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		ShadowReq r = sq[i];
+		int ri = HYB ? i : fb[1 + i];
+		ShadowReq r = sq[ri];
 		int time = __float_as_int(r.a.w), pixel = __float_as_int(r.b.w);
-		if(!trace_any(S, mk(r.a.x, r.a.y, r.a.z), mk(r.b.x, r.b.y, r.b.z), time, &overflow))
-			acc_add(acc, pixel, r.w.x, r.w.y, r.w.z);
+		int res;
+		if(HYB) {
+			Hit h;
+			res = trace_two_level<false, true>(S, mk(r.a.x, r.a.y, r.a.z), mk(r.b.x, r.b.y, r.b.z), time, h, nullptr, &overflow);
+		} else {
+			res = trace_any_octree_impl(S, mk(r.a.x, r.a.y, r.a.z), mk(r.b.x, r.b.y, r.b.z), time, &overflow) ? 1 : 0;
+		}
+		if(HYB && res == 2) {
+			fb[1 + atomicAdd(fb, 1)] = ri;
+			continue;
+		}
+		if(res == 0) acc_add(acc, pixel, r.w.x, r.w.y, r.w.z);
 	}
 	if(overflow) atomicOr(&ctr->overflow, 1);
-	if(blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctr->rays[2], (unsigned long long)n);
+	if(blockIdx.x == 0 && threadIdx.x == 0) {
+		if(HYB) atomicAdd(&ctr->rays[2], (unsigned long long)n);
+		else if(n > 0) atomicAdd(&ctr->bvh_fallbacks, (unsigned long long)n);
+	}
 }
 
 /* ---------------------------------------------------------------- */
@@ -738,7 +769,7 @@ __global__ void k_finish(const int *active, const int *n_active_p, int s0, int w
 }
 
 /* closest hits of caller-supplied world rays (sray_gpu_cast_rays) */
-__global__ void k_cast(DScene S, int n, const float *orig, const float *dir, const int *time, int *obj, int *prim, float *t,
+__global__ void __launch_bounds__(SRAY_TRACE_THREADS) k_cast(DScene S, int n, const float *orig, const float *dir, const int *time, int *obj, int *prim, float *t,
 		unsigned char *tie, DevCounters *ctr)
 {
 	int overflow = 0;
@@ -837,6 +868,13 @@ void Renderer::fill_scene_desc()
 	D.mnodes = mnodes.as<DevNode>();
 	D.mtris = mtris.as<DevTri>();
 	D.mprim = mprim.as<int>();
+	D.bnodes = bnodes.as<DevBvhNode>();
+	D.btris = btris.as<DevTri>();
+	D.bprim = bprim.as<int>();
+	D.bhome = bhome.as<int>();
+	D.tnodes = has_tlas ? tnodes.as<DevBvhNode>() : nullptr;
+	D.ohome = ohome.as<int>();
+	D.bvh_fallbacks = ctr.p ? &ctr.as<DevCounters>()->bvh_fallbacks : nullptr;
 	D.objs = objs.as<DevObj>();
 	D.nobj = (int)sc.objs.size();
 	D.xf = xf.as<float>();
@@ -902,27 +940,64 @@ int Renderer::upload_scene(cudaStream_t s)
 	std::vector<DevTri> tris;
 	std::vector<int> prim;
 	std::vector<float> tp, ta;
+	std::vector<DevBvhNode> bn;
+	std::vector<DevTri> bt;
+	std::vector<int> bp, bh;
 	int tri_cursor = 0;
+	/* the triangle record the intersection test reads */
+	auto record = [](const float *P) {
+		DevTri t;
+		/* unnormalised face normal cross(v1 - v0, v2 - v0), float ops as the test computes it */
+		float e1[3] = {P[3] - P[0], P[4] - P[1], P[5] - P[2]};
+		float e2[3] = {P[6] - P[0], P[7] - P[1], P[8] - P[2]};
+		float n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+		for(int c = 0; c < 3; c++) { t.a[c] = P[c]; t.b[c] = P[3 + c]; t.c[c] = P[6 + c]; }
+		t.a[3] = n[0]; t.b[3] = n[1]; t.c[3] = n[2];
+		return t;
+	};
 	for(size_t u = 0; u < sc.meshes.size(); u++) {
 		Mesh &m = sc.meshes[u];
 		m.tri_base = tri_cursor;
 		size_t s0 = slots.size();
-		flatten_octree(m.oct, nodes, slots);
+		std::vector<int> index_of;
+		flatten_octree(m.oct, nodes, slots, &index_of);
 		m.node_base = m.oct.nodes.empty() ? -1 : (int)(nodes.size() - m.oct.nodes.size());
 		size_t nf = m.pos.size() / 9;
 		for(size_t k = s0; k < slots.size(); k++) {
 			int f = slots[k];
-			const float *P = &m.pos[(size_t)f * 9];
-			DevTri t;
-			/* unnormalised face normal cross(v1 - v0, v2 - v0), float ops as the test computes it */
-			float e1[3] = {P[3] - P[0], P[4] - P[1], P[5] - P[2]};
-			float e2[3] = {P[6] - P[0], P[7] - P[1], P[8] - P[2]};
-			float n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
-			for(int c = 0; c < 3; c++) { t.a[c] = P[c]; t.b[c] = P[3 + c]; t.c[c] = P[6 + c]; }
-			t.a[3] = n[0]; t.b[3] = n[1]; t.c[3] = n[2];
-			tris.push_back(t);
+			tris.push_back(record(&m.pos[(size_t)f * 9]));
 			prim.push_back(f);
 		}
+		/* the hierarchy, with references made absolute */
+		m.bvh_base = -1;
+		if(!m.bvh.nodes.empty() && bt.size() + m.bvh.order.size() < ((size_t)1 << 27)) {
+			int noff = (int)bn.size(), toff = (int)bt.size();
+			m.bvh_base = noff;
+			for(const DevBvhNode &src : m.bvh.nodes) {
+				DevBvhNode d = src;
+				int *refs[2] = {&d.left, &d.right};
+				for(int k = 0; k < 2; k++) {
+					int ref = *refs[k];
+					if(ref == BVH_NONE) continue;
+					if(ref >= 0) *refs[k] = ref + noff;
+					else {
+						unsigned v = ~(unsigned)ref;
+						unsigned start = (v >> 4) + (unsigned)toff, cnt = v & 15u;
+						*refs[k] = (int)~((start << 4) | cnt);
+					}
+				}
+				bn.push_back(d);
+			}
+			std::vector<int> home;
+			octree_homes(m.oct, m.posd, index_of, home);
+			for(int f : m.bvh.order) {
+				bt.push_back(record(&m.pos[(size_t)f * 9]));
+				bp.push_back(f);
+				bh.push_back(home[f]);
+			}
+		}
+		std::vector<DevBvhNode>().swap(m.bvh.nodes);
+		std::vector<int>().swap(m.bvh.order);
 		/* leaf slot indices become positions in the triangle-record array */
 		tp.insert(tp.end(), m.pos.begin(), m.pos.end());
 		ta.insert(ta.end(), m.attr.begin(), m.attr.end());
@@ -941,10 +1016,12 @@ int Renderer::upload_scene(cudaStream_t s)
 		d.start = (float)o.start;
 		d.end = (float)o.end;
 		d.mesh_root = -1;
+		d.bvh_root = -1;
 		if(o.type == OBJ_MESH) {
 			const Mesh &m = sc.meshes[o.mesh];
 			d.mesh_root = (m.pos.empty() || m.node_base < 0) ? -1 : m.node_base;
 			d.tri_base = m.tri_base;
+			d.bvh_root = d.mesh_root >= 0 ? m.bvh_base : -1;
 		}
 	}
 	std::vector<DevMat> dm(sc.mats.size());
@@ -981,6 +1058,11 @@ int Renderer::upload_scene(cudaStream_t s)
 	CK(objs.upload(dobj, s), "upload objects");
 	CK(mats.upload(dm, s), "upload materials");
 	CK(lights.upload(dl, s), "upload lights");
+	CK(bnodes.upload(bn, s), "upload mesh hierarchies");
+	CK(btris.upload(bt, s), "upload hierarchy triangles");
+	CK(bprim.upload(bp, s), "upload hierarchy face ids");
+	CK(bhome.upload(bh, s), "upload hierarchy home nodes");
+	CK(ctr.ensure(sizeof(DevCounters)), "counters");
 	CK(cudaStreamSynchronize(s), "upload scene");
 	return 0;
 }
@@ -993,8 +1075,53 @@ int Renderer::build_frame(long bt0, long bt1, cudaStream_t s)
 	sc.build_tree(t0, t1, opt);
 	std::vector<DevNode> nodes;
 	std::vector<int> slots;
-	flatten_octree(sc.oct, nodes, slots);
+	std::vector<int> index_of;
+	flatten_octree(sc.oct, nodes, slots, &index_of);
 	scene_root = sc.oct.nodes.empty() ? 0 : (int)(nodes.size() - sc.oct.nodes.size());
+	/* the object hierarchy: each object boxed by the union of the octree
+	 * leaves that list it (so that it is entered whenever the octree would
+	 * test the object), one object per leaf */
+	std::vector<DevBvhNode> tn;
+	std::vector<int> ohome_h;
+	if(!sc.oct.nodes.empty() && !sc.objs.empty()) {
+		size_t no = sc.objs.size();
+		std::vector<Box> ub(no);
+		for(size_t i = 0; i < no; i++) for(int k = 0; k < 3; k++) { ub[i].mn[k] = DBL_MAX; ub[i].mx[k] = -DBL_MAX; }
+		for(const BuildOctree::Node &n : sc.oct.nodes) {
+			if(n.child >= 0) continue;
+			for(int it : n.items) {
+				for(int k = 0; k < 3; k++) {
+					ub[it].mn[k] = std::min(ub[it].mn[k], n.box.mn[k]);
+					ub[it].mx[k] = std::max(ub[it].mx[k], n.box.mx[k]);
+				}
+			}
+		}
+		std::vector<float> mn(no * 3), mx(no * 3);
+		for(size_t i = 0; i < no; i++) {
+			for(int k = 0; k < 3; k++) {
+				float lo = (float)ub[i].mn[k], hi = (float)ub[i].mx[k];
+				if((double)lo > ub[i].mn[k]) lo = nextafterf(lo, -INFINITY);
+				if((double)hi < ub[i].mx[k]) hi = nextafterf(hi, INFINITY);
+				if(!(ub[i].mn[k] <= ub[i].mx[k])) { lo = FLT_MAX; hi = -FLT_MAX; }   /* listed in no leaf */
+				mn[i * 3 + k] = lo;
+				mx[i * 3 + k] = hi;
+			}
+		}
+		MeshBvh tl;
+		tl.build_items(mn.data(), mx.data(), no, 1);
+		for(const DevBvhNode &src : tl.nodes) {
+			DevBvhNode d = src;
+			int *refs[2] = {&d.left, &d.right};
+			for(int k = 0; k < 2; k++) {
+				int ref = *refs[k];
+				if(ref == BVH_NONE || ref >= 0) continue;
+				unsigned v = ~(unsigned)ref;
+				*refs[k] = ~tl.order[v >> 4];   /* leaf: the object itself */
+			}
+			tn.push_back(d);
+		}
+		octree_homes_boxes(sc.oct, sc.oct_boxes, index_of, ohome_h);
+	}
 	int shutter = sc.cam.shutter;
 	tlo = t0 - shutter - 2;
 	int thi = t1 + shutter + 2;
@@ -1023,6 +1150,9 @@ int Renderer::build_frame(long bt0, long bt1, cudaStream_t s)
 	}
 	CK(snodes.upload(nodes, s), "upload scene nodes");
 	CK(sslots.upload(slots, s), "upload scene slots");
+	CK(tnodes.upload(tn, s), "upload object hierarchy");
+	CK(ohome.upload(ohome_h, s), "upload object home nodes");
+	has_tlas = !tn.empty();
 	CK(xf.upload(xfs, s), "upload transforms");
 	CK(light_pos.upload(lp, s), "upload light positions");
 	CK(cam_m.upload(cm, s), "upload camera");
@@ -1166,10 +1296,8 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			CK(cudaMemsetAsync(cnt + 2, 0, sizeof(int), s), "reset gather queue");
 			CK(cudaMemsetAsync(cnt + 5, 0, sizeof(int), s), "reset shadow queue");
 			CK(sq.ensure((size_t)n_rays * shadow_per_ray * sizeof(ShadowReq)), "shadow queue");
-			if(prof_flags & 2)
-				LAUNCH(*this, "trace", s, k_trace<true><<<grid_for(n_rays, 128), 128, 0, s>>>(S, q[cur], hits.as<int4>(), ctr.as<DevCounters>()));
-			else
-				LAUNCH(*this, "trace", s, k_trace<false><<<grid_for(n_rays, 128), 128, 0, s>>>(S, q[cur], hits.as<int4>(), ctr.as<DevCounters>()));
+			r = trace_rays(q[cur], n_rays, "trace", (prof_flags & 2) != 0, s);
+			if(r) return r;
 			ShadeOut so;
 			so.qo = q[cur ^ 1];
 			so.gq = gq.as<GatherReq>();
@@ -1180,8 +1308,12 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			so.sq_cap = n_rays * shadow_per_ray;
 			LAUNCH(*this, "shade", s, k_shade<<<grid_for(n_rays, 128), 128, 0, s>>>(S, q[cur], hits.as<int4>(), so, acc.as<float4>(), depth,
 					ctr.as<DevCounters>()));
-			LAUNCH(*this, "shadow", s, k_shadow<<<grid_for(n_rays * 2, 128), 128, 0, s>>>(S, sq.as<ShadowReq>(), cnt + 5, acc.as<float4>(),
-					ctr.as<DevCounters>()));
+			CK(fbl.ensure(((size_t)n_rays * shadow_per_ray + 1) * sizeof(int)), "fallback list");
+			CK(cudaMemsetAsync(fbl.p, 0, sizeof(int), s), "reset fallback list");
+			LAUNCH(*this, "shadow", s, k_shadow<true><<<grid_for(n_rays * 2, 128), 128, 0, s>>>(S, sq.as<ShadowReq>(), cnt + 5,
+					acc.as<float4>(), ctr.as<DevCounters>(), fbl.as<int>()));
+			LAUNCH(*this, "shadow", s, k_shadow<false><<<152, 128, 0, s>>>(S, sq.as<ShadowReq>(), cnt + 5, acc.as<float4>(),
+					ctr.as<DevCounters>(), fbl.as<int>()));
 			LAUNCH(*this, "gather", s, k_gather<<<grid_for(n_rays, GATHER_WARPS), GATHER_WARPS * 32, 0, s>>>(S, gq.as<GatherReq>(), cnt + 2,
 					acc.as<float4>(), ctr.as<DevCounters>()));
 			stats.secondary_rays += depth ? n_rays : 0;
@@ -1222,13 +1354,33 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 	stats.gather_candidates = (int64_t)hc.g_cand;
 	stats.gather_selects = (int64_t)hc.g_select;
 	stats.gather_spills = (int64_t)hc.g_spill;
+	stats.bvh_fallbacks = (int64_t)hc.bvh_fallbacks;
 	if(hc.overflow) return fail(SRAY_EDEVICE, "device queue or traversal stack overflow");
 	return 0;
 }
 
-void launch_trace(Renderer &R, const RayQueue &q, int n, const char *name, cudaStream_t s)
+/* closest hits of the first n (upper bound; the queue's count decides)
+ * rays of q into hits: the hierarchy pass, then the octree pass over the
+ * rays it listed */
+int Renderer::trace_rays(const RayQueue &qq, int n, const char *name, bool count, cudaStream_t s)
 {
-	LAUNCH(R, name, s, k_trace<false><<<grid_for(n, 128), 128, 0, s>>>(R.S, q, R.hits.as<int4>(), R.ctr.as<DevCounters>()));
+	CK(fbl.ensure(((size_t)n + 1) * sizeof(int)), "fallback list");
+	CK(cudaMemsetAsync(fbl.p, 0, sizeof(int), s), "reset fallback list");
+	if(count) {
+		LAUNCH(*this, name, s, k_trace<true, true><<<grid_for(n, 128), 128, 0, s>>>(S, qq, hits.as<int4>(), ctr.as<DevCounters>(),
+				fbl.as<int>()));
+		LAUNCH(*this, name, s, k_trace<true, false><<<152, 128, 0, s>>>(S, qq, hits.as<int4>(), ctr.as<DevCounters>(), fbl.as<int>()));
+	} else {
+		LAUNCH(*this, name, s, k_trace<false, true><<<grid_for(n, 128), 128, 0, s>>>(S, qq, hits.as<int4>(), ctr.as<DevCounters>(),
+				fbl.as<int>()));
+		LAUNCH(*this, name, s, k_trace<false, false><<<152, 128, 0, s>>>(S, qq, hits.as<int4>(), ctr.as<DevCounters>(), fbl.as<int>()));
+	}
+	return 0;
+}
+
+int launch_trace(Renderer &R, const RayQueue &q, int n, const char *name, cudaStream_t s)
+{
+	return R.trace_rays(q, n, name, false, s);
 }
 
 static Renderer *g_R = nullptr;
@@ -1455,7 +1607,7 @@ int sray_gpu_primary_hits(long msec, int *obj, int *prim, float *t, unsigned cha
 	if(e != cudaSuccess) { g_err = cudaGetErrorString(e); return SRAY_ECUDA; }
 	R.q[0].count = cnt + 0;
 	k_camera<<<grid_for(npix, 256), 256, 0, s>>>(R.S, nullptr, cnt + 3, 0, 1, R.q[0], R.acc.as<float4>(), R.ctr.as<DevCounters>());
-	k_trace<false><<<grid_for(npix, 128), 128, 0, s>>>(R.S, R.q[0], R.hits.as<int4>(), R.ctr.as<DevCounters>());
+	if(R.trace_rays(R.q[0], npix, "trace", false, s)) { g_err = R.err; return SRAY_ECUDA; }
 	k_primary_hits<<<grid_for(npix, 256), 256, 0, s>>>(R.S, R.q[0], R.hits.as<int4>(), obj, prim, t, tie);
 	DevCounters hc;
 	e = cudaMemcpyAsync(&hc, R.ctr.p, sizeof hc, cudaMemcpyDeviceToHost, s);
@@ -1613,7 +1765,8 @@ void sray_gpu_shutdown(void)
 	Renderer &R = *g_R;
 	DevBuf *bufs[] = {&R.mnodes, &R.mtris, &R.mprim, &R.tri_pos, &R.tri_attr, &R.objs, &R.mats, &R.lights, &R.snodes, &R.sslots,
 		&R.xf, &R.light_pos, &R.cam_m, &R.projbits, &R.coverage, &R.qbuf[0], &R.qbuf[1], &R.hits, &R.gq, &R.sq, &R.acc, &R.hist, &R.sums,
-		&R.active[0], &R.active[1], &R.spp, &R.fbdev, &R.ctr, &R.counts};
+		&R.active[0], &R.active[1], &R.spp, &R.fbdev, &R.ctr, &R.counts, &R.bnodes, &R.btris, &R.bprim, &R.bhome,
+		&R.fbl, &R.tnodes, &R.ohome};
 	for(DevBuf *b : bufs) b->release();
 	PhotonBufs *pb[] = {&R.caust, &R.gi};
 	for(PhotonBufs *p : pb) {

@@ -74,6 +74,7 @@ struct DevCounters {
 	unsigned long long rays[4];   /* primary, secondary, shadow, gather */
 	unsigned long long nodes, prims;
 	unsigned long long g_tested, g_cand, g_select, g_spill;   /* gather work */
+	unsigned long long bvh_fallbacks;   /* hierarchy hits the octree did not confirm */
 };
 
 struct PhotonBufs {
@@ -90,10 +91,11 @@ struct Renderer {
 	std::string err;
 
 	/* scene tables (per load) */
-	DevBuf mnodes, mtris, mprim, tri_pos, tri_attr, objs, mats, lights;
+	DevBuf mnodes, mtris, mprim, tri_pos, tri_attr, objs, mats, lights, bnodes, btris, bprim, bhome;
 	/* frame tables (per build) */
-	DevBuf snodes, sslots, xf, light_pos, cam_m, projbits, coverage;
+	DevBuf snodes, sslots, xf, light_pos, cam_m, projbits, coverage, tnodes, ohome;
 	bool built = false;
+	bool has_tlas = false;
 	int t0 = 0, t1 = 0, tlo = 0, nt = 1;
 	int scene_root = 0;
 	long frame_msec = 0;
@@ -102,7 +104,7 @@ struct Renderer {
 	DScene S;
 
 	/* render buffers */
-	DevBuf qbuf[2], hits, gq, sq, acc, hist, sums, active[2], spp, fbdev, ctr, counts;
+	DevBuf qbuf[2], hits, gq, sq, acc, hist, sums, active[2], spp, fbdev, ctr, counts, fbl;
 	RayQueue q[2];
 	int qcap[2] = {0, 0};
 	sray_stats stats;
@@ -133,6 +135,7 @@ struct Renderer {
 	int shoot(cudaStream_t s, int *nc, int *ng);
 	int render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t s);
 	int ensure_queue(int which, int cap);
+	int trace_rays(const RayQueue &q, int n, const char *name, bool count, cudaStream_t s);
 	void fill_scene_desc();
 };
 
@@ -145,7 +148,7 @@ struct Renderer {
 	} while(0)
 
 /* render.cu: closest hits of the first n rays of q into R.hits */
-void launch_trace(Renderer &R, const RayQueue &q, int n, const char *name, cudaStream_t s);
+int launch_trace(Renderer &R, const RayQueue &q, int n, const char *name, cudaStream_t s);
 
 /* photon.cu */
 int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored);

@@ -539,7 +539,7 @@ void BuildOctree::build(const std::vector<Box> &boxes, int max_depth, int max_it
  * slot bits are x | y << 1 | z << 2 of the child's half-space */
 static const int child_slot[8] = {0, 1, 3, 2, 4, 5, 7, 6};
 
-void flatten_octree(const BuildOctree &oct, std::vector<DevNode> &out, std::vector<int> &slots)
+void flatten_octree(const BuildOctree &oct, std::vector<DevNode> &out, std::vector<int> &slots, std::vector<int> *index_of)
 {
 	if(oct.nodes.empty()) return;
 	/* pad so the root sits at index 7 mod 8: every group of 8 siblings
@@ -589,6 +589,59 @@ void flatten_octree(const BuildOctree &oct, std::vector<DevNode> &out, std::vect
 			d.count = (int)n.items.size();
 			slots.insert(slots.end(), n.items.begin(), n.items.end());
 		}
+	}
+	if(index_of) {
+		index_of->assign(oct.nodes.size(), -1);
+		for(size_t q = 0; q < order.size(); q++) (*index_of)[order[q]] = (int)(base + q);
+	}
+}
+
+static int octree_home(const BuildOctree &oct, const Box &b, const std::vector<int> &index_of)
+{
+	/* descend while exactly one child takes the item (the builder's overlap
+	 * rule decides which children list it) */
+	int n = 0;
+	for(;;) {
+		int c = oct.nodes[n].child;
+		if(c < 0) break;
+		int only = -1, hits = 0;
+		for(int k = 0; k < 8; k++) {
+			if(overlap(b, oct.nodes[c + k].box)) {
+				hits++;
+				only = c + k;
+			}
+		}
+		if(hits != 1) break;
+		n = only;
+	}
+	return index_of[n];
+}
+
+void octree_homes_boxes(const BuildOctree &oct, const std::vector<Box> &boxes, const std::vector<int> &index_of,
+		std::vector<int> &home)
+{
+	home.assign(boxes.size(), -1);
+	if(oct.nodes.empty()) return;
+	for(size_t i = 0; i < boxes.size(); i++) home[i] = octree_home(oct, boxes[i], index_of);
+}
+
+void octree_homes(const BuildOctree &oct, const std::vector<double> &posd, const std::vector<int> &index_of,
+		std::vector<int> &home)
+{
+	size_t nf = posd.size() / 9;
+	home.assign(nf, -1);
+	if(oct.nodes.empty()) return;
+	for(size_t f = 0; f < nf; f++) {
+		Box b;
+		for(int k = 0; k < 3; k++) { b.mn[k] = FLT_MAX; b.mx[k] = -FLT_MAX; }
+		for(int v = 0; v < 3; v++) {
+			for(int k = 0; k < 3; k++) {
+				double c = posd[f * 9 + v * 3 + k];
+				if(c < b.mn[k]) b.mn[k] = c;
+				if(c > b.mx[k]) b.mx[k] = c;
+			}
+		}
+		home[f] = octree_home(oct, b, index_of);
 	}
 }
 
@@ -838,6 +891,7 @@ void HostScene::build_tree(int t0, int t1, const sray_opts &opt)
 		}
 	}
 	oct.build(boxes, opt.scnoct_max_depth, opt.scnoct_max_items);
+	oct_boxes = boxes;
 	const Box &rb = oct.nodes[0].box;
 	double dx = rb.mx[0] - rb.mn[0], dy = rb.mx[1] - rb.mn[1], dz = rb.mx[2] - rb.mn[2];
 	gather_dist = sqrt(dx * dx + dy * dy + dz * dz) * opt.gather_dist;
@@ -1180,10 +1234,17 @@ bool HostScene::load(const char *text, size_t len, const sray_opts &opt, std::st
 	 * one per unique mesh, built on all host cores */
 	std::vector<std::thread> th;
 	size_t nm = meshes.size();
-	unsigned nth = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), (unsigned)nm));
+	/* tasks 0 .. nm-1 build octrees, nm .. 2nm-1 hierarchies */
+	size_t ntask = 2 * nm;
+	unsigned nth = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), (unsigned)ntask));
 	for(unsigned w = 0; w < nth; w++) {
-		th.push_back(std::thread([this, &opt, w, nth, nm]() {
-			for(size_t u = w; u < nm; u += nth) {
+		th.push_back(std::thread([this, &opt, w, nth, nm, ntask]() {
+			for(size_t task = w; task < ntask; task += nth) {
+				if(task >= nm) {
+					meshes[task - nm].bvh.build(meshes[task - nm].pos);
+					continue;
+				}
+				size_t u = task;
 				Mesh &m = meshes[u];
 				size_t nf = m.posd.size() / 9;
 				std::vector<Box> boxes(nf);

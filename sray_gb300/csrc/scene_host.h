@@ -66,6 +66,19 @@ struct BuildOctree {
 	void build(const std::vector<Box> &item_boxes, int max_depth, int max_items);
 };
 
+/* A binary bounding-volume hierarchy over a mesh's triangles, built by the
+ * surface-area heuristic over 16 bins per axis.  It only speeds up finding
+ * candidates; which hit counts is still decided by the mesh octree (the
+ * traversal confirms every hit against it). */
+struct MeshBvh {
+	std::vector<DevBvhNode> nodes;   /* child references relative to this hierarchy */
+	std::vector<int> order;          /* items in leaf order */
+	int depth = 0;
+	void build(const std::vector<float> &pos);   /* over faces: 9 floats each */
+	/* over boxes (3 floats min, 3 max per item), at most leaf_max per leaf */
+	void build_items(const float *mn, const float *mx, size_t n, int leaf_max);
+};
+
 /* one unique triangle mesh (identical meshes of several objects share it) */
 struct Mesh {
 	std::vector<float> pos;    /* 9 floats per face: the three vertices (object space) */
@@ -73,7 +86,9 @@ struct Mesh {
 	std::vector<float> attr;   /* 24 floats per face: normals 9, tangents 9, texcoords 6 */
 	uint64_t hash = 0;
 	BuildOctree oct;
+	MeshBvh bvh;
 	int node_base = 0;         /* first node in the device mesh-node array */
+	int bvh_base = -1;         /* root in the device hierarchy-node array */
 	int tri_base = 0;          /* first face in the device attribute table */
 };
 
@@ -135,6 +150,7 @@ struct HostScene {
 	double gather_dist = 0.0;
 	int bt0 = 0, bt1 = 0;
 	std::vector<Box> box_t0, box_t1;   /* object bounds at the frame's t0 / t1 */
+	std::vector<Box> oct_boxes;        /* the boxes the scene octree was built from */
 	Box object_bounds(size_t i, int t) const;
 
 	bool load(const char *text, size_t len, const sray_opts &opt, std::string &err);
@@ -148,7 +164,17 @@ void mat_inverse(double out[4][4], const double m[4][4]);
 
 /* Flatten an octree breadth first into device nodes; leaf items are
  * appended to `slots` (their indices into the item array). */
-void flatten_octree(const BuildOctree &oct, std::vector<DevNode> &nodes, std::vector<int> &slots);
+void flatten_octree(const BuildOctree &oct, std::vector<DevNode> &nodes, std::vector<int> &slots,
+		std::vector<int> *index_of = nullptr);
+
+/* For every face of a mesh: the deepest node of its octree whose box holds
+ * the face's bounds (the node below which all the leaves listing the face
+ * lie), as an index into the flattened nodes (index_of from flatten_octree). */
+void octree_homes(const BuildOctree &oct, const std::vector<double> &posd, const std::vector<int> &index_of,
+		std::vector<int> &home);
+/* the same for items given by their boxes */
+void octree_homes_boxes(const BuildOctree &oct, const std::vector<Box> &boxes, const std::vector<int> &index_of,
+		std::vector<int> &home);
 
 }  // namespace sray
 

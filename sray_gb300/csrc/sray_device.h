@@ -36,6 +36,20 @@ struct alignas(16) DevNode {
 	unsigned mask;  /* inner: bit k set when child slot k holds items */
 };
 
+/* a node of a mesh's bounding-volume hierarchy: the boxes of its two
+ * children and their references.  A reference >= 0 is a node index, BVH_NONE
+ * an absent child, and any other negative value r a leaf holding the
+ * (~r) & 15 triangles that start at (~r) >> 4 in the hierarchy's triangle
+ * order. */
+#define BVH_NONE 0x7fffffff
+
+struct alignas(16) DevBvhNode {
+	float lmn[3], lmx[3];
+	float rmn[3], rmx[3];
+	int left, right;
+	int pad[2];
+};
+
 struct alignas(16) DevTri {
 	float a[4];     /* v0.xyz, n.x */
 	float b[4];     /* v1.xyz, n.y */
@@ -48,7 +62,7 @@ struct alignas(16) DevObj {
 	int mesh_root;  /* mesh: root node in mesh_nodes, -1 if the mesh is empty */
 	int tri_base;   /* mesh: first triangle of its unique mesh in tri_pos/tri_attr */
 	float rad, start, end;
-	int pad;
+	int bvh_root;   /* mesh: root node in the mesh hierarchies, -1 if none */
 };
 
 struct alignas(16) DevMat {

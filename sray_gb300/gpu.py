@@ -32,6 +32,7 @@ class SrayStats(ctypes.Structure):
                 ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64),
                 ("gather_tested", ctypes.c_int64), ("gather_candidates", ctypes.c_int64),
                 ("gather_selects", ctypes.c_int64), ("gather_spills", ctypes.c_int64),
+                ("bvh_fallbacks", ctypes.c_int64),
                 ("reserved", ctypes.c_int * 2)]
 
 
