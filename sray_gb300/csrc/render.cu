@@ -22,6 +22,7 @@
 #include <cooperative_groups.h>
 #include <cooperative_groups/scan.h>
 #include "renderer.h"
+#include "range_ff.h"
 
 namespace cg = cooperative_groups;
 
@@ -411,69 +412,14 @@ __device__ __forceinline__ double dist2(const float4 &p, V3 q)
 	return dx * dx + dy * dy + dz * dz;
 }
 
-/* ---- exact range decisions without double arithmetic ----
- * The reference decides "within range" and orders neighbours on the double
- * sum of squares d2 = (px-qx)^2 + (py-qy)^2 + (pz-qz)^2 rounded to float.
- * This GPU has little double throughput, so d2 is evaluated in float-float
- * arithmetic (Dekker's two-sum and the fma two-product): the unevaluated sum
- * H + L is within 2^-43 of the exact value and the double evaluation within
- * 2^-50, so with a margin of 2^-36 both the range test and the float rounding
- * of d2 come out as the double computation gives them, unless H + L lies
- * within the margin of the radius or of a float rounding boundary; those
- * rare cases (and tiny or non-finite sums) are recomputed in double. */
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
-{
-	s = a + b;
-	float bb = s - a;
-	e = (a - (s - bb)) + (b - bb);
-}
-
-__device__ __forceinline__ void fast_two_sum(float a, float b, float &s, float &e)
-{
-	s = a + b;
-	e = b - (s - a);
-}
-
-__device__ __forceinline__ void diff_sq_ff(float p, float q, float &h, float &l)
-{
-	float s, e;
-	two_sum(p, -q, s, e);     /* s + e = p - q exactly */
-	h = s * s;
-	l = __fmaf_rn(s, s, -h);  /* h + l = s^2 exactly */
-	l = l + ((2.0f * s) * e + e * e);
-}
-
-__device__ __forceinline__ void add_ff(float h1, float l1, float h2, float l2, float &h, float &l)
-{
-	float s, e;
-	two_sum(h1, h2, s, e);
-	e = e + (l1 + l2);
-	fast_two_sum(s, e, h, l);
-}
-
-/* returns false when the double computation must decide; otherwise sets
- * `in` (d2 <= range^2 in double) and `key` (bits of (float)d2) */
+/* exact range decisions without double arithmetic (range_ff.h) */
 __device__ __forceinline__ bool range_ff(const DPhotonMap &M, float4 p, V3 q, bool &in, unsigned &key)
 {
-	float hx, lx, hy, ly, hz, lz, h, l;
-	diff_sq_ff(p.x, q.x, hx, lx);
-	diff_sq_ff(p.y, q.y, hy, ly);
-	diff_sq_ff(p.z, q.z, hz, lz);
-	add_ff(hx, lx, hy, ly, h, l);
-	add_ff(h, l, hz, lz, h, l);
-	if(!(h >= 8.673617e-19f && h <= 1e30f)) return false;      /* 2^-60 .. overflow-safe */
-	float delta = h * 1.4551915e-11f;                          /* 2^-36 */
-	/* range test against range^2 = r2_hi + r2_lo */
-	float diff = (h - M.r2_hi) + (l - M.r2_lo);
-	if(diff > delta) { in = false; key = 0; return true; }
-	if(!(diff < -delta)) return false;
-	in = true;
-	/* rounding of d2 to float: h unless d2 may cross half an ulp of h */
-	unsigned hb = __float_as_uint(h);
-	float ulp = __uint_as_float(hb & 0x7f800000u) * 1.1920929e-7f;   /* 2^-23 */
-	float ulp_dn = (hb & 0x007fffffu) ? ulp : 0.5f * ulp;
-	if(!(l + delta < 0.5f * ulp) || !(l - delta > -0.5f * ulp_dn)) return false;
-	key = hb;
+	int inr = 0;
+	uint32_t k = 0;
+	if(!sray_range_ff(p.x, p.y, p.z, q.x, q.y, q.z, M.r2_hi, M.r2_lo, &inr, &k)) return false;
+	in = inr != 0;
+	key = k;
 	return true;
 }
 
@@ -1312,7 +1258,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			CK(cudaMemsetAsync(fbl.p, 0, sizeof(int), s), "reset fallback list");
 			LAUNCH(*this, "shadow", s, k_shadow<true><<<grid_for(n_rays * 2, 128), 128, 0, s>>>(S, sq.as<ShadowReq>(), cnt + 5,
 					acc.as<float4>(), ctr.as<DevCounters>(), fbl.as<int>()));
-			LAUNCH(*this, "shadow", s, k_shadow<false><<<152, 128, 0, s>>>(S, sq.as<ShadowReq>(), cnt + 5, acc.as<float4>(),
+			LAUNCH(*this, "octree_retrace", s, k_shadow<false><<<152, 128, 0, s>>>(S, sq.as<ShadowReq>(), cnt + 5, acc.as<float4>(),
 					ctr.as<DevCounters>(), fbl.as<int>()));
 			LAUNCH(*this, "gather", s, k_gather<<<grid_for(n_rays, GATHER_WARPS), GATHER_WARPS * 32, 0, s>>>(S, gq.as<GatherReq>(), cnt + 2,
 					acc.as<float4>(), ctr.as<DevCounters>()));
@@ -1369,11 +1315,13 @@ int Renderer::trace_rays(const RayQueue &qq, int n, const char *name, bool count
 	if(count) {
 		LAUNCH(*this, name, s, k_trace<true, true><<<grid_for(n, 128), 128, 0, s>>>(S, qq, hits.as<int4>(), ctr.as<DevCounters>(),
 				fbl.as<int>()));
-		LAUNCH(*this, name, s, k_trace<true, false><<<152, 128, 0, s>>>(S, qq, hits.as<int4>(), ctr.as<DevCounters>(), fbl.as<int>()));
+		LAUNCH(*this, "octree_retrace", s, k_trace<true, false><<<152, 128, 0, s>>>(S, qq, hits.as<int4>(), ctr.as<DevCounters>(),
+				fbl.as<int>()));
 	} else {
 		LAUNCH(*this, name, s, k_trace<false, true><<<grid_for(n, 128), 128, 0, s>>>(S, qq, hits.as<int4>(), ctr.as<DevCounters>(),
 				fbl.as<int>()));
-		LAUNCH(*this, name, s, k_trace<false, false><<<152, 128, 0, s>>>(S, qq, hits.as<int4>(), ctr.as<DevCounters>(), fbl.as<int>()));
+		LAUNCH(*this, "octree_retrace", s, k_trace<false, false><<<152, 128, 0, s>>>(S, qq, hits.as<int4>(), ctr.as<DevCounters>(),
+				fbl.as<int>()));
 	}
 	return 0;
 }
