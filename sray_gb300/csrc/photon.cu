@@ -197,6 +197,7 @@ __device__ bool gen_dir(const uint32_t *bits, sray_rng *s, V3 *out)
  * Phase 0 follows the global rules, phase 1 the caustic rules. */
 
 #define PHOTON_GUARD 4096   /* interactions per phase (loop bound of the oracle's tracer) */
+#define PHOTON_FINISH 65536 /* live photons below which the tail is traced in one launch */
 
 __device__ __forceinline__ void push_photon(const RayQueue &q, int slot, const PRay &r, const PState &ph, int guard, int gid,
 		int li, int phase, uint32_t draws)
@@ -266,6 +267,66 @@ __global__ void __launch_bounds__(128) k_photon_emit(DScene S, int global, const
 	if(gfail) atomicOr(&ctr->gen_dir_fail, 1);
 }
 
+/* a photon in flight, as the queue entry holds it */
+struct PFlight {
+	PRay r;
+	PState ph;
+	int li, gid, phase, guard;
+	uint32_t draws;
+};
+
+__device__ __forceinline__ void load_photon(const RayQueue &q, int i, PFlight &f)
+{
+	float4 o4 = q.o[i], d4 = q.d[i], w4 = q.w[i], k4 = q.stk[i];
+	int4 meta = q.meta[i];
+	int2 ext = q.ext[i];
+	f.li = meta.x;
+	f.phase = meta.z & 15;
+	f.guard = __float_as_int(w4.z);
+	f.gid = __float_as_int(w4.w);
+	f.r.o = mk(o4.x, o4.y, o4.z);
+	f.r.d = mk(d4.x, d4.y, d4.z);
+	f.r.time = meta.w;
+	f.r.iter = meta.y;
+	f.r.st.ior = w4.y;
+	f.r.st.stk[0] = k4.x; f.r.st.stk[1] = k4.y; f.r.st.stk[2] = k4.z; f.r.st.stk[3] = k4.w;
+	f.r.st.sp = ext.y;
+	f.ph.col[0] = o4.w; f.ph.col[1] = d4.w; f.ph.col[2] = w4.x;
+	f.ph.type = meta.z >> 4;
+	f.draws = (uint32_t)ext.x;
+}
+
+/* one surface interaction of a photon at hit h (h.obj >= 0): stores it
+ * (returns 1), loses it (0) or leaves it ready for its next trace (2) */
+__device__ __forceinline__ int photon_interact(const DScene &S, int global, const int *prefix, const float *scale, PFlight &f,
+		const Hit &h, DevPhoton *out, int *valid)
+{
+	sray_rng s;
+	sray_rng_init(&s, S.seed, global ? SRAY_DOM_GLOBAL : SRAY_DOM_CAUST, (uint32_t)(f.gid - prefix[f.li]), (uint32_t)f.li);
+	sray_rng_seek(&s, f.draws);
+	int res = f.phase == 0 ? global_step(S, f.r, f.ph, h, &s) : caust_step(S, f.r, f.ph, h, &s);
+	f.draws = s.n;
+	if(res == P_STORE) {
+		if(!global && f.ph.type != CAUST_PHOTON) return 0;
+		float sc = scale[f.li];
+		DevPhoton p;
+		p.p[0] = f.ph.pos.x; p.p[1] = f.ph.pos.y; p.p[2] = f.ph.pos.z; p.p[3] = f.ph.col[0] * sc;
+		p.d[0] = f.ph.dir.x; p.d[1] = f.ph.dir.y; p.d[2] = f.ph.dir.z; p.d[3] = f.ph.col[1] * sc;
+		p.n[0] = f.ph.norm.x; p.n[1] = f.ph.norm.y; p.n[2] = f.ph.norm.z; p.n[3] = f.ph.col[2] * sc;
+		out[f.gid] = p;
+		valid[f.gid] = 1;
+		return 1;
+	}
+	if(res == P_DROP) return 0;
+	if(res == P_TO_CAUST) {
+		f.phase = 1;
+		f.guard = 0;
+	} else if(++f.guard >= PHOTON_GUARD) {
+		return 0;
+	}
+	return f.r.iter <= 0 ? 0 : 2;
+}
+
 __global__ void __launch_bounds__(128) k_photon_bounce(DScene S, int global, const int *prefix, const float *scale, RayQueue qi,
 		const int4 *hits, RayQueue qo, DevPhoton *out, int *valid)
 {
@@ -278,49 +339,43 @@ __global__ void __launch_bounds__(128) k_photon_bounce(DScene S, int global, con
 		h.obj = hv.y;
 		h.prim = hv.z;
 		h.tie = hv.w;
-		float4 o4 = qi.o[i], d4 = qi.d[i], w4 = qi.w[i], k4 = qi.stk[i];
-		int4 meta = qi.meta[i];
-		int2 ext = qi.ext[i];
-		int li = meta.x, phase = meta.z & 15;
-		int guard = __float_as_int(w4.z), gid = __float_as_int(w4.w);
-		PRay r;
-		r.o = mk(o4.x, o4.y, o4.z);
-		r.d = mk(d4.x, d4.y, d4.z);
-		r.time = meta.w;
-		r.iter = meta.y;
-		r.st.ior = w4.y;
-		r.st.stk[0] = k4.x; r.st.stk[1] = k4.y; r.st.stk[2] = k4.z; r.st.stk[3] = k4.w;
-		r.st.sp = ext.y;
-		PState ph;
-		ph.col[0] = o4.w; ph.col[1] = d4.w; ph.col[2] = w4.x;
-		ph.type = meta.z >> 4;
-		sray_rng s;
-		sray_rng_init(&s, S.seed, global ? SRAY_DOM_GLOBAL : SRAY_DOM_CAUST, (uint32_t)(gid - prefix[li]), (uint32_t)li);
-		sray_rng_seek(&s, (uint32_t)ext.x);
-		int res = phase == 0 ? global_step(S, r, ph, h, &s) : caust_step(S, r, ph, h, &s);
-		if(res == P_STORE) {
-			if(!global && ph.type != CAUST_PHOTON) continue;
-			float sc = scale[li];
-			DevPhoton p;
-			p.p[0] = ph.pos.x; p.p[1] = ph.pos.y; p.p[2] = ph.pos.z; p.p[3] = ph.col[0] * sc;
-			p.d[0] = ph.dir.x; p.d[1] = ph.dir.y; p.d[2] = ph.dir.z; p.d[3] = ph.col[1] * sc;
-			p.n[0] = ph.norm.x; p.n[1] = ph.norm.y; p.n[2] = ph.norm.z; p.n[3] = ph.col[2] * sc;
-			out[gid] = p;
-			valid[gid] = 1;
-			continue;
-		}
-		if(res == P_DROP) continue;
-		if(res == P_TO_CAUST) {
-			phase = 1;
-			guard = 0;
-		} else if(++guard >= PHOTON_GUARD) {
-			continue;
-		}
-		if(r.iter <= 0) continue;
+		PFlight f;
+		load_photon(qi, i, f);
+		if(photon_interact(S, global, prefix, scale, f, h, out, valid) != 2) continue;
 		int slot = photon_slot(qo.count);
 		if(slot >= qo.cap) continue;                 /* cannot happen: a photon has one successor */
-		push_photon(qo, slot, r, ph, guard, gid, li, phase, s.n);
+		push_photon(qo, slot, f.r, f.ph, f.guard, f.gid, f.li, f.phase, f.draws);
 	}
+}
+
+/* The tail of a photon map: once few photons are left, each thread takes
+ * photons from the queue (through a shared counter) and traces every one to
+ * its end, instead of one interaction per pass; a pass costs as much as its
+ * slowest ray, and the tail is made of few photons on long paths.  Photons
+ * whose hit the octrees must decide are handed back, before that trace, to
+ * the pending queue, which the pass-wise loop finishes. */
+__global__ void __launch_bounds__(128) k_photon_finish(DScene S, int global, const int *prefix, const float *scale, RayQueue qi,
+		int *next, RayQueue qpend, DevPhoton *out, int *valid, DevCounters *ctr)
+{
+	int n = *qi.count;
+	int overflow = 0;
+	for(;;) {
+		int i = atomicAdd(next, 1);
+		if(i >= n) break;
+		PFlight f;
+		load_photon(qi, i, f);
+		for(int step = 0; step < 2 * PHOTON_GUARD + 2; step++) {
+			Hit h;
+			if(!trace_two_level<false, false>(S, f.r.o, f.r.d, f.r.time, h, nullptr, &overflow)) {
+				int slot = photon_slot(qpend.count);
+				if(slot < qpend.cap) push_photon(qpend, slot, f.r, f.ph, f.guard, f.gid, f.li, f.phase, f.draws);
+				break;
+			}
+			if(h.obj < 0) break;
+			if(photon_interact(S, global, prefix, scale, f, h, out, valid) != 2) break;
+		}
+	}
+	if(overflow) atomicOr(&ctr->overflow, 1);
 }
 
 /* ---------------- scan / compaction ---------------- */
@@ -538,9 +593,24 @@ int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored)
 			P.valid.as<int>(), R.ctr.as<DevCounters>()));
 	int cur = 0;
 	int n_live = total;   /* upper bound until the first count is read */
+	bool finished = false;
 	for(int pass = 0; n_live > 0; pass++) {
-		if(pass >= 2 * PHOTON_GUARD + 2) return R.fail(SRAY_EDEVICE, "photon paths did not terminate");
+		if(pass >= 2 * PHOTON_GUARD + 4) return R.fail(SRAY_EDEVICE, "photon paths did not terminate");
 		PCK(cudaMemsetAsync(R.q[cur ^ 1].count, 0, sizeof(int), s), "reset photon queue");
+		if(!finished && pass > 0 && n_live <= PHOTON_FINISH) {
+			/* the tail in one launch; what it hands back continues pass-wise */
+			finished = true;
+			PCK(cudaMemsetAsync(cnt + 2, 0, sizeof(int), s), "reset photon tail counter");
+			LAUNCH(R, "photon_finish", s, k_photon_finish<<<grid_n(n_live, 128), 128, 0, s>>>(R.S, global, pre.as<int>(),
+					scl.as<float>(), R.q[cur], cnt + 2, R.q[cur ^ 1], P.tmp_ph.as<DevPhoton>(), P.valid.as<int>(),
+					R.ctr.as<DevCounters>()));
+			PCK(cudaMemcpyAsync(&n_live, R.q[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "photon queue count");
+			PCK(cudaStreamSynchronize(s), "photon tail");
+			R.d2h += sizeof(int);
+			R.prof_collect();
+			cur ^= 1;
+			continue;
+		}
 		if(launch_trace(R, R.q[cur], n_live, "photon_trace", s)) return SRAY_ECUDA;
 		LAUNCH(R, "photon_bounce", s, k_photon_bounce<<<grid_n(n_live, 128), 128, 0, s>>>(R.S, global, pre.as<int>(),
 				scl.as<float>(), R.q[cur], R.hits.as<int4>(), R.q[cur ^ 1], P.tmp_ph.as<DevPhoton>(), P.valid.as<int>()));
