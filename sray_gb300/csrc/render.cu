@@ -15,6 +15,7 @@
  */
 #include <math.h>
 #include <float.h>
+#include <limits.h>
 #include <string.h>
 #include <stdio.h>
 #include <algorithm>
@@ -173,155 +174,379 @@ __device__ __forceinline__ void push_shadow(ShadeOut &out, V3 o, V3 d, int time,
 	out.sq[slot] = r;
 }
 
-/* shade one bounce: env colour for misses, shade_phong / shade_undef for hits.
- * Light samples become shadow requests carrying their contribution; children
- * (reflection, refraction, final-gather rays) and photon gathers are queued. */
+/* a ray of the shading tree, as a queue entry holds it */
+struct RayRec {
+	V3 o, d;
+	float energy;
+	IorStack st;
+	float w[3];
+	int pixel, aslot, iter, path, time, sample, dsub;
+};
+
+__device__ __forceinline__ void load_ray(const RayQueue &q, int i, RayRec &r)
+{
+	float4 o4 = q.o[i], d4 = q.d[i], w4 = q.w[i], st4 = q.stk[i];
+	int4 meta = q.meta[i];
+	int2 ext = q.ext[i];
+	r.o = mk(o4.x, o4.y, o4.z);
+	r.d = mk(d4.x, d4.y, d4.z);
+	r.energy = o4.w;
+	r.st.ior = d4.w;
+	r.st.stk[0] = st4.x; r.st.stk[1] = st4.y; r.st.stk[2] = st4.z; r.st.stk[3] = st4.w;
+	r.st.sp = ext.y;
+	r.w[0] = w4.x; r.w[1] = w4.y; r.w[2] = w4.z;
+	r.pixel = __float_as_int(w4.w);
+	r.aslot = meta.x;
+	r.iter = meta.y;
+	r.path = meta.z;
+	r.time = meta.w;
+	r.sample = ext.x & 0xffff;
+	r.dsub = ext.x >> 16;
+}
+
+__device__ __forceinline__ void store_ray(const RayQueue &q, int slot, const RayRec &r)
+{
+	q.o[slot] = make_float4(r.o.x, r.o.y, r.o.z, r.energy);
+	q.d[slot] = make_float4(r.d.x, r.d.y, r.d.z, r.st.ior);
+	q.w[slot] = make_float4(r.w[0], r.w[1], r.w[2], __int_as_float(r.pixel));
+	q.meta[slot] = make_int4(r.aslot, r.iter, r.path, r.time);
+	q.stk[slot] = make_float4(r.st.stk[0], r.st.stk[1], r.st.stk[2], r.st.stk[3]);
+	q.ext[slot] = make_int2(r.sample | (r.dsub << 16), r.st.sp);
+}
+
+__device__ __forceinline__ RayRec make_child(const RayRec &p, V3 o, V3 d, float energy, int iter, int path, int dsub, const IorStack &st,
+		float wr, float wg, float wb)
+{
+	RayRec c;
+	c.o = o;
+	c.d = d;
+	c.energy = energy;
+	c.st = st;
+	c.w[0] = wr; c.w[1] = wg; c.w[2] = wb;
+	c.pixel = p.pixel;
+	c.aslot = p.aslot;
+	c.iter = iter;
+	c.path = path;
+	c.time = p.time;
+	c.sample = p.sample;
+	c.dsub = dsub;
+	return c;
+}
+
+/* shade one hit: env colour for misses, shade_phong / shade_undef
+ * (src/shader.cc:36-283) for hits.  Light samples, children (reflection,
+ * refraction, final-gather rays) and photon gathers go to the emitter `em`:
+ * em.shadow(origin, dir, time, slot, contribution rgb) for a light sample
+ * whose contribution counts when the segment is unoccluded,
+ * em.gather(pos, normal, kind, slot, weight rgb), em.child(ray). */
+template <class E>
+__device__ __forceinline__ void shade_one(const DScene &S, const RayRec &ray, const Hit &h, int depth, float4 *acc, E &em)
+{
+	int aslot = ray.aslot;
+	int pixel = ray.pixel;
+	int iter = ray.iter, path = ray.path, time = ray.time;
+	int sample = ray.sample;
+	int dsub = ray.dsub;
+	V3 rd = ray.d;
+	const float *w = ray.w;
+	if(h.obj < 0) {
+		acc_add(acc, aslot, w[0] * S.env_col[0], w[1] * S.env_col[1], w[2] * S.env_col[2]);
+		if(depth == 0) acc[aslot].w = S.env_col[3];
+		return;
+	}
+	if(depth == 0) acc[aslot].w = 1.0f;
+	const DevMat &mat = mat_of(S, h.obj);
+	Surf sp;
+	surface_point(S, h, ray.o, rd, time, sp, !mat.phong);
+	if(!mat.phong) {
+		/* shade_undef (src/shader.cc:36-73) */
+		sray_rng rng;
+		sray_rng_init(&rng, S.seed, SRAY_DOM_PIXEL | ((uint32_t)path << 4), (uint32_t)pixel, (uint32_t)(sample | (dsub << 16)));
+		int tx = (int)(sp.tex[0] * 20.0f), ty = (int)(sp.tex[1] * 10.0f);
+		bool even = (tx % 2) == (ty % 2);
+		float tc[3] = {even ? 1.0f : 0.2f, 0.3f, even ? 0.2f : 1.0f};
+		acc_add(acc, aslot, w[0] * (0.1f * tc[0]), w[1] * (0.1f * tc[1]), w[2] * (0.1f * tc[2]));
+		for(int li = 0; li < S.nlights; li++) {
+			const DevLight &L = S.lights[li];
+			V3 lpos = light_point(S, li, time, &rng);
+			V3 ldir = lpos - sp.pos;
+			float ldist = len(ldir);
+			V3 sdir = ldir;
+			ldir = ldir / ldist;
+			V3 vdir = -normalized(rd);
+			V3 hdir = normalized(ldir + vdir);
+			float ndotl = maxf_ref(dot(sp.normal, ldir), 0.0f);
+			float ndoth = maxf_ref(dot(sp.normal, hdir), 0.0f);
+			float pw = powf(ndoth, 50.0f);
+			em.shadow(sp.pos, sdir, time, aslot, w[0] * (ndotl * L.col[0] * tc[0] + pw * L.col[0]),
+					w[1] * (ndotl * L.col[1] * tc[1] + pw * L.col[1]), w[2] * (ndotl * L.col[2] * tc[2] + pw * L.col[2]));
+		}
+		return;
+	}
+	/* shade_phong (src/shader.cc:83-247) */
+	bool entering;
+	V3 normal;
+	if(dot(rd, sp.normal) > 0.0f) { normal = -sp.normal; entering = false; }
+	else { normal = sp.normal; entering = true; }
+	float ray_mag = len(rd);
+	V3 incident = rd / ray_mag;
+	const float *kd = mat.kd, *ks = mat.ks;
+	if(iter == DIFFUSE_ITER) {
+		/* final-gather ray: radiance_est(...) * kd */
+		em.gather(sp.pos, normal, 1, aslot, w[0] * kd[0], w[1] * kd[1], w[2] * kd[2]);
+		return;
+	}
+	float energy = ray.energy;
+	const IorStack &st = ray.st;
+	sray_rng rng;
+	sray_rng_init(&rng, S.seed, SRAY_DOM_PIXEL | ((uint32_t)path << 4), (uint32_t)pixel, (uint32_t)sample);
+	float refl_fact = mat.refl, trans_fact = mat.refr, mat_ior = mat.ior;
+	float ior = st.calc_ior(entering, mat_ior);
+	/* ambient: (env_ambient * kd) * kd */
+	acc_add(acc, aslot, w[0] * (S.env_amb[0] * kd[0] * kd[0]), w[1] * (S.env_amb[1] * kd[1] * kd[1]),
+			w[2] * (S.env_amb[2] * kd[2] * kd[2]));
+	V3 vref = reflection(incident, normal);
+	for(int li = 0; li < S.nlights; li++) {
+		const DevLight &L = S.lights[li];
+		int ns = L.type != 0 ? S.shadow_samples : 1;
+		float scale = ns > 1 ? 1.0f / (float)ns : 1.0f;
+		for(int si = 0; si < ns; si++) {
+			V3 lpos = light_point(S, li, time, &rng);
+			V3 ldir = lpos - sp.pos;
+			float ldist = len(ldir);
+			V3 sdir = ldir;
+			ldir = ldir / ldist;
+			float ndotl = maxf_ref(dot(normal, ldir), 0.0f);
+			float rdotl = maxf_ref(dot(vref, ldir), 0.0f);
+			float pw = powf(rdotl, mat.shin);
+			float c[3];
+			for(int k = 0; k < 3; k++) {
+				float lc = L.col[k] * 1.0f;
+				c[k] = ((ndotl * lc) * scale) * kd[k] + ((pw * lc) * scale) * ks[k];
+			}
+			if(c[0] != 0.0f || c[1] != 0.0f || c[2] != 0.0f) em.shadow(sp.pos, sdir, time, aslot, w[0] * c[0], w[1] * c[1], w[2] * c[2]);
+		}
+	}
+	/* final gather: diffuse rays end at their next hit (src/shader.cc:154-187) */
+	if(S.gi_on) {
+		int ds = S.diffuse_samples < MAX_DS ? S.diffuse_samples : MAX_DS;
+		for(int k = 0; k < ds; k++) {
+			V3 dir = sphrand(&rng, 1.0f);
+			float ndotl;
+			if((ndotl = dot(dir, normal)) < 0.0f) dir = -dir;
+			float diff_energy = ndotl * energy;
+			if(diff_energy > S.min_energy) {
+				float g = S.diffuse_samples > 1 ? ndotl / (float)S.diffuse_samples : ndotl;
+				em.child(make_child(ray, sp.pos, dir * ray_mag, diff_energy, DIFFUSE_ITER, path * 4 + 2, k, st, w[0] * kd[0] * g,
+						w[1] * kd[1] * g, w[2] * kd[2] * g));
+			}
+		}
+	}
+	float ray_dot_n = dot(-rd / ray_mag, normal);
+	float sf0 = trans_fact > 0.0f ? (ior - 1.0f) / (ior + 1.0f) : 1.0f;
+	float fres = fresnel(sf0 * sf0, ray_dot_n);
+	float refl_energy = refl_fact * energy;
+	if(refl_energy > S.min_energy && iter > 0) {
+		float g = refl_fact * fres;
+		em.child(make_child(ray, sp.pos, reflection(rd, normal), refl_energy, iter - 1, path * 4, 0, st, w[0] * ks[0] * g,
+				w[1] * ks[1] * g, w[2] * ks[2] * g));
+	}
+	float trans_energy = trans_fact * energy;
+	if(trans_energy > S.min_energy && iter > 0) {
+		IorStack cs = st;
+		if(entering) cs.enter(mat_ior);
+		else cs.leave();
+		V3 td = refraction(rd / ray_mag, normal, ior) * ray_mag;
+		if(dot(td, normal) > 0.0f) {
+			if(entering) cs.leave();
+			else cs.enter(mat_ior);
+		}
+		float g = trans_fact * (1.0f - fres);
+		em.child(make_child(ray, sp.pos, td, trans_energy, iter - 1, path * 4 + 1, 0, cs, w[0] * ks[0] * g, w[1] * ks[1] * g,
+				w[2] * ks[2] * g));
+	}
+	if(S.caust_on) em.gather(sp.pos, normal, 0, aslot, w[0], w[1], w[2]);
+}
+
+/* the wavefront emitter: everything goes to the next pass's queues */
+struct QueueEmitter {
+	ShadeOut *out;
+	int *overflow;
+	__device__ void shadow(V3 o, V3 d, int time, int slot, float r, float g, float b) { push_shadow(*out, o, d, time, slot, r, g, b, overflow); }
+	__device__ void gather(V3 pos, V3 n, int kind, int slot, float r, float g, float b) { push_gather(*out, pos, n, kind, slot, r, g, b, overflow); }
+	__device__ void child(const RayRec &c)
+	{
+		int slot = warp_alloc(out->qo.count, 1);
+		if(slot >= out->qo.cap) { *overflow = 1; return; }
+		store_ray(out->qo, slot, c);
+	}
+};
+
 __global__ void __launch_bounds__(128) k_shade(DScene S, RayQueue qi, const int4 *hits, ShadeOut out, float4 *acc, int depth,
 		DevCounters *ctr)
 {
 	int n = *qi.count;
 	int overflow = 0;
+	QueueEmitter em;
+	em.out = &out;
+	em.overflow = &overflow;
 	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		float4 o4 = qi.o[i], d4 = qi.d[i], w4 = qi.w[i];
-		int4 meta = qi.meta[i];
-		int2 ext = qi.ext[i];
+		RayRec r;
+		load_ray(qi, i, r);
 		int4 hv = hits[i];
-		int aslot = meta.x;
-		int pixel = __float_as_int(w4.w);
-		int iter = meta.y, path = meta.z, time = meta.w;
-		int sample = ext.x & 0xffff;
-		int dsub = ext.x >> 16;
-		V3 rd = mk(d4.x, d4.y, d4.z);
 		Hit h;
 		h.t = __int_as_float(hv.x);
 		h.obj = hv.y;
 		h.prim = hv.z;
 		h.tie = hv.w;
-		if(h.obj < 0) {
-			acc_add(acc, aslot, w4.x * S.env_col[0], w4.y * S.env_col[1], w4.z * S.env_col[2]);
-			if(depth == 0) acc[aslot].w = S.env_col[3];
-			continue;
-		}
-		if(depth == 0) acc[aslot].w = 1.0f;
-		const DevMat &mat = mat_of(S, h.obj);
-		Surf sp;
-		surface_point(S, h, mk(o4.x, o4.y, o4.z), rd, time, sp, !mat.phong);
-		if(!mat.phong) {
-			/* shade_undef (src/shader.cc:36-73) */
-			sray_rng rng;
-			sray_rng_init(&rng, S.seed, SRAY_DOM_PIXEL | ((uint32_t)path << 4), (uint32_t)pixel, (uint32_t)(sample | (dsub << 16)));
-			int tx = (int)(sp.tex[0] * 20.0f), ty = (int)(sp.tex[1] * 10.0f);
-			bool even = (tx % 2) == (ty % 2);
-			float tc[3] = {even ? 1.0f : 0.2f, 0.3f, even ? 0.2f : 1.0f};
-			acc_add(acc, aslot, w4.x * (0.1f * tc[0]), w4.y * (0.1f * tc[1]), w4.z * (0.1f * tc[2]));
-			for(int li = 0; li < S.nlights; li++) {
-				const DevLight &L = S.lights[li];
-				V3 lpos = light_point(S, li, time, &rng);
-				V3 ldir = lpos - sp.pos;
-				float ldist = len(ldir);
-				V3 sdir = ldir;
-				ldir = ldir / ldist;
-				V3 vdir = -normalized(rd);
-				V3 hdir = normalized(ldir + vdir);
-				float ndotl = maxf_ref(dot(sp.normal, ldir), 0.0f);
-				float ndoth = maxf_ref(dot(sp.normal, hdir), 0.0f);
-				float pw = powf(ndoth, 50.0f);
-				push_shadow(out, sp.pos, sdir, time, aslot, w4.x * (ndotl * L.col[0] * tc[0] + pw * L.col[0]),
-						w4.y * (ndotl * L.col[1] * tc[1] + pw * L.col[1]), w4.z * (ndotl * L.col[2] * tc[2] + pw * L.col[2]),
-						&overflow);
-			}
-			continue;
-		}
-		/* shade_phong (src/shader.cc:83-247) */
-		bool entering;
-		V3 normal;
-		if(dot(rd, sp.normal) > 0.0f) { normal = -sp.normal; entering = false; }
-		else { normal = sp.normal; entering = true; }
-		float ray_mag = len(rd);
-		V3 incident = rd / ray_mag;
-		const float *kd = mat.kd, *ks = mat.ks;
-		if(iter == DIFFUSE_ITER) {
-			/* final-gather ray: radiance_est(...) * kd */
-			push_gather(out, sp.pos, normal, 1, aslot, w4.x * kd[0], w4.y * kd[1], w4.z * kd[2], &overflow);
-			continue;
-		}
-		float energy = o4.w;
-		float4 st4 = qi.stk[i];
-		IorStack st;
-		st.ior = d4.w;
-		st.stk[0] = st4.x; st.stk[1] = st4.y; st.stk[2] = st4.z; st.stk[3] = st4.w;
-		st.sp = ext.y;
-		sray_rng rng;
-		sray_rng_init(&rng, S.seed, SRAY_DOM_PIXEL | ((uint32_t)path << 4), (uint32_t)pixel, (uint32_t)sample);
-		float refl_fact = mat.refl, trans_fact = mat.refr, mat_ior = mat.ior;
-		float ior = st.calc_ior(entering, mat_ior);
-		/* ambient: (env_ambient * kd) * kd */
-		acc_add(acc, aslot, w4.x * (S.env_amb[0] * kd[0] * kd[0]), w4.y * (S.env_amb[1] * kd[1] * kd[1]),
-				w4.z * (S.env_amb[2] * kd[2] * kd[2]));
-		V3 vref = reflection(incident, normal);
-		for(int li = 0; li < S.nlights; li++) {
-			const DevLight &L = S.lights[li];
-			int ns = L.type != 0 ? S.shadow_samples : 1;
-			float scale = ns > 1 ? 1.0f / (float)ns : 1.0f;
-			for(int si = 0; si < ns; si++) {
-				V3 lpos = light_point(S, li, time, &rng);
-				V3 ldir = lpos - sp.pos;
-				float ldist = len(ldir);
-				V3 sdir = ldir;
-				ldir = ldir / ldist;
-				float ndotl = maxf_ref(dot(normal, ldir), 0.0f);
-				float rdotl = maxf_ref(dot(vref, ldir), 0.0f);
-				float pw = powf(rdotl, mat.shin);
-				float c[3];
-				for(int k = 0; k < 3; k++) {
-					float lc = L.col[k] * 1.0f;
-					c[k] = ((ndotl * lc) * scale) * kd[k] + ((pw * lc) * scale) * ks[k];
-				}
-				if(c[0] != 0.0f || c[1] != 0.0f || c[2] != 0.0f)
-					push_shadow(out, sp.pos, sdir, time, aslot, w4.x * c[0], w4.y * c[1], w4.z * c[2], &overflow);
-			}
-		}
-		/* final gather: diffuse rays end at their next hit (src/shader.cc:154-187) */
-		if(S.gi_on) {
-			int ds = S.diffuse_samples < MAX_DS ? S.diffuse_samples : MAX_DS;
-			for(int k = 0; k < ds; k++) {
-				V3 dir = sphrand(&rng, 1.0f);
-				float ndotl;
-				if((ndotl = dot(dir, normal)) < 0.0f) dir = -dir;
-				float diff_energy = ndotl * energy;
-				if(diff_energy > S.min_energy) {
-					float g = S.diffuse_samples > 1 ? ndotl / (float)S.diffuse_samples : ndotl;
-					push_child(out, sp.pos, dir * ray_mag, diff_energy, DIFFUSE_ITER, path * 4 + 2, k, st,
-							w4.x * kd[0] * g, w4.y * kd[1] * g, w4.z * kd[2] * g, pixel, aslot, sample, time, &overflow);
-				}
-			}
-		}
-		float ray_dot_n = dot(-rd / ray_mag, normal);
-		float sf0 = trans_fact > 0.0f ? (ior - 1.0f) / (ior + 1.0f) : 1.0f;
-		float fres = fresnel(sf0 * sf0, ray_dot_n);
-		float refl_energy = refl_fact * energy;
-		if(refl_energy > S.min_energy && iter > 0) {
-			float g = refl_fact * fres;
-			push_child(out, sp.pos, reflection(rd, normal), refl_energy, iter - 1, path * 4, 0, st,
-					w4.x * ks[0] * g, w4.y * ks[1] * g, w4.z * ks[2] * g, pixel, aslot, sample, time, &overflow);
-		}
-		float trans_energy = trans_fact * energy;
-		if(trans_energy > S.min_energy && iter > 0) {
-			IorStack cs = st;
-			if(entering) cs.enter(mat_ior);
-			else cs.leave();
-			V3 td = refraction(rd / ray_mag, normal, ior) * ray_mag;
-			if(dot(td, normal) > 0.0f) {
-				if(entering) cs.leave();
-				else cs.enter(mat_ior);
-			}
-			float g = trans_fact * (1.0f - fres);
-			push_child(out, sp.pos, td, trans_energy, iter - 1, path * 4 + 1, 0, cs,
-					w4.x * ks[0] * g, w4.y * ks[1] * g, w4.z * ks[2] * g, pixel, aslot, sample, time, &overflow);
-		}
-		if(S.caust_on) push_gather(out, sp.pos, normal, 0, aslot, w4.x, w4.y, w4.z, &overflow);
+		shade_one(S, r, h, depth, acc, em);
 	}
 	if(overflow) atomicOr(&ctr->overflow, 1);
+}
+
+/* The tail of the shading tree.  Past the first bounces few rays are left,
+ * on long and branching paths (chains through glass and mirrors), and a
+ * pass costs as much as its slowest ray.  k_render_pool runs the rest of the
+ * tree in one launch over a shared pool of rays: the queue's rays occupy
+ * the first slots, every thread claims the next slot, waits until a ray is
+ * there, traces and shades it and appends its children to the pool.  Light
+ * samples are traced on the spot (their contribution added when the
+ * hierarchies confirm the segment unoccluded, queued for the octree pass
+ * when they cannot decide); photon gathers are queued for the warp-per-query
+ * kernel; a ray whose closest hit the octrees must decide goes to the
+ * pending queue unshaded.
+ *
+ * Pool control words: [0] next slot to claim, [1] slots filled or reserved,
+ * [2] rays in flight (in the pool and not yet shaded), [3] error.  A slot's
+ * ready flag is set after its record is written (with a fence); records are
+ * read through L2 (__ldcg), never from a possibly stale L1 line.  A thread
+ * whose slot is beyond every reservation leaves once no ray is in flight
+ * (no more can come); every wait is bounded and sets the error word when
+ * it runs out. */
+#define RENDER_TAIL 131072        /* rays below which the rest of the tree runs in k_render_pool */
+#define POOL_SPIN_LIMIT (1 << 22) /* polls of a slot before the pool gives up (about 0.5 s) */
+#define POOL_SHADOW (-0x7ffffff0)   /* iter of a pool item that is a light sample's shadow ray */
+
+__device__ __forceinline__ void load_ray_l2(const RayQueue &q, int i, RayRec &r)
+{
+	float4 o4 = __ldcg(q.o + i), d4 = __ldcg(q.d + i), w4 = __ldcg(q.w + i), st4 = __ldcg(q.stk + i);
+	int4 meta = __ldcg(q.meta + i);
+	int2 ext = __ldcg(q.ext + i);
+	r.o = mk(o4.x, o4.y, o4.z);
+	r.d = mk(d4.x, d4.y, d4.z);
+	r.energy = o4.w;
+	r.st.ior = d4.w;
+	r.st.stk[0] = st4.x; r.st.stk[1] = st4.y; r.st.stk[2] = st4.z; r.st.stk[3] = st4.w;
+	r.st.sp = ext.y;
+	r.w[0] = w4.x; r.w[1] = w4.y; r.w[2] = w4.z;
+	r.pixel = __float_as_int(w4.w);
+	r.aslot = meta.x;
+	r.iter = meta.y;
+	r.path = meta.z;
+	r.time = meta.w;
+	r.sample = ext.x & 0xffff;
+	r.dsub = ext.x >> 16;
+}
+
+struct PoolEmitter {
+	const DScene *S;
+	ShadeOut *out;
+	RayQueue *pool;
+	int *ready, *ctl;
+	float4 *acc;
+	int *overflow;
+	unsigned long long shadows;
+	/* a light sample becomes a pool item of its own (iter = POOL_SHADOW),
+	 * traced by whichever thread claims it */
+	__device__ void shadow(V3 o, V3 d, int time, int slot, float r, float g, float b)
+	{
+		RayRec c;
+		c.o = o;
+		c.d = d;
+		c.energy = 0.0f;
+		c.st.ior = 1.0f;
+		c.st.stk[0] = c.st.stk[1] = c.st.stk[2] = c.st.stk[3] = 0.0f;
+		c.st.sp = 0;
+		c.w[0] = r; c.w[1] = g; c.w[2] = b;
+		c.pixel = 0;
+		c.aslot = slot;
+		c.iter = POOL_SHADOW;
+		c.path = 0;
+		c.time = time;
+		c.sample = 0;
+		c.dsub = 0;
+		child(c);
+	}
+	__device__ void gather(V3 pos, V3 n, int kind, int slot, float r, float g, float b) { push_gather(*out, pos, n, kind, slot, r, g, b, overflow); }
+	__device__ void child(const RayRec &c)
+	{
+		atomicAdd(&ctl[2], 1);                 /* in flight before it can be claimed */
+		int j = atomicAdd(&ctl[1], 1);
+		if(j >= pool->cap) {
+			*overflow = 1;
+			atomicSub(&ctl[2], 1);
+			return;
+		}
+		store_ray(*pool, j, c);
+		__threadfence();
+		atomicExch(&ready[j], 1);
+	}
+};
+
+__global__ void __launch_bounds__(128) k_render_pool(DScene S, RayQueue pool, int *ready, int *ctl, ShadeOut out, float4 *acc,
+		DevCounters *ctr)
+{
+	int overflow = 0;
+	PoolEmitter em;
+	em.S = &S;
+	em.out = &out;
+	em.pool = &pool;
+	em.ready = ready;
+	em.ctl = ctl;
+	em.acc = acc;
+	em.overflow = &overflow;
+	em.shadows = 0;
+	unsigned long long traced = 0;
+	volatile int *vready = ready;
+	volatile int *vctl = ctl;
+	for(;;) {
+		int i = atomicAdd(&ctl[0], 1);
+		if(i >= pool.cap) break;
+		bool have = false;
+		for(int spin = 0; spin < POOL_SPIN_LIMIT; spin++) {
+			if(vready[i]) { have = true; break; }
+			if(vctl[2] == 0) {
+				__threadfence();
+				if(vctl[1] <= i) break;   /* nothing in flight and no reservation reaches slot i */
+			}
+			__nanosleep(128);
+		}
+		if(!have) {
+			if(!(vctl[2] == 0 && vctl[1] <= i)) atomicOr(&ctl[3], 1);   /* gave up waiting */
+			break;
+		}
+		__threadfence();
+		RayRec r;
+		load_ray_l2(pool, i, r);
+		Hit h;
+		if(r.iter == POOL_SHADOW) {
+			int res = trace_two_level<false, true>(S, r.o, r.d, r.time, h, nullptr, &overflow);
+			if(res == 0) acc_add(acc, r.aslot, r.w[0], r.w[1], r.w[2]);
+			else if(res == 2) push_shadow(out, r.o, r.d, r.time, r.aslot, r.w[0], r.w[1], r.w[2], &overflow);
+			if(res != 2) em.shadows++;
+		} else if(!trace_two_level<false, false>(S, r.o, r.d, r.time, h, nullptr, &overflow)) {
+			int slot = atomicAdd(out.qo.count, 1);
+			if(slot >= out.qo.cap) overflow = 1;
+			else store_ray(out.qo, slot, r);
+		} else {
+			traced++;
+			shade_one(S, r, h, 1, acc, em);
+		}
+		atomicSub(&ctl[2], 1);   /* after its children were counted in flight */
+	}
+	if(overflow) atomicOr(&ctr->overflow, 1);
+	if(traced) atomicAdd(&ctr->rays[1], traced);
+	if(em.shadows) atomicAdd(&ctr->rays[2], em.shadows);
 }
 
 /* shadow rays: the reference tests visibility with cast_ray(shadow_ray)
@@ -1229,7 +1454,53 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 				ctr.as<DevCounters>()));
 		int n_rays = n_prim;
 		int cur = 0;
+		bool tail_done = false;
 		for(int depth = 0; n_rays > 0; depth++) {
+			if(depth >= 1 && !tail_done && n_rays <= RENDER_TAIL) {
+				/* the rest of the shading tree in one launch (k_render_pool) */
+				tail_done = true;
+				q[0].count = cnt + 0;
+				q[1].count = cnt + 1;
+				CK(cudaMemsetAsync(q[cur ^ 1].count, 0, sizeof(int), s), "reset queue");
+				CK(cudaMemsetAsync(cnt + 2, 0, sizeof(int), s), "reset gather queue");
+				CK(cudaMemsetAsync(cnt + 5, 0, sizeof(int), s), "reset shadow queue");
+				int *ctl = cnt + 8;
+				int cap = q[cur].cap;
+				CK(pool_ready.ensure((size_t)cap * sizeof(int)), "pool flags");
+				CK(cudaMemsetAsync(pool_ready.p, 1, (size_t)n_rays * sizeof(int), s), "pool flags");
+				CK(cudaMemsetAsync(pool_ready.as<int>() + n_rays, 0, (size_t)(cap - n_rays) * sizeof(int), s), "pool flags");
+				int ctl_h[4] = {0, n_rays, n_rays, 0};
+				CK(cudaMemcpyAsync(ctl, ctl_h, sizeof ctl_h, cudaMemcpyHostToDevice, s), "pool control");
+				h2d += sizeof ctl_h;
+				ShadeOut so;
+				so.qo = q[cur ^ 1];
+				so.gq = gq.as<GatherReq>();
+				so.gq_count = cnt + 2;
+				so.gq_cap = (int)std::min<size_t>(gq.bytes / sizeof(GatherReq), (size_t)INT_MAX);
+				so.sq = sq.as<ShadowReq>();
+				so.sq_count = cnt + 5;
+				so.sq_cap = (int)std::min<size_t>(sq.bytes / sizeof(ShadowReq), (size_t)INT_MAX);
+				LAUNCH(*this, "render_pool", s, k_render_pool<<<152 * 4, 128, 0, s>>>(S, q[cur], pool_ready.as<int>(), ctl, so,
+						acc.as<float4>(), ctr.as<DevCounters>()));
+				CK(fbl.ensure(((size_t)so.sq_cap + 1) * sizeof(int)), "fallback list");
+				CK(cudaMemsetAsync(fbl.p, 0, sizeof(int), s), "reset fallback list");
+				LAUNCH(*this, "shadow", s, k_shadow<true><<<grid_for(so.sq_cap, 128), 128, 0, s>>>(S, sq.as<ShadowReq>(), cnt + 5,
+						acc.as<float4>(), ctr.as<DevCounters>(), fbl.as<int>()));
+				LAUNCH(*this, "octree_retrace", s, k_shadow<false><<<152, 128, 0, s>>>(S, sq.as<ShadowReq>(), cnt + 5,
+						acc.as<float4>(), ctr.as<DevCounters>(), fbl.as<int>()));
+				LAUNCH(*this, "gather", s, k_gather<<<grid_for(so.gq_cap, GATHER_WARPS), GATHER_WARPS * 32, 0, s>>>(S,
+						gq.as<GatherReq>(), cnt + 2, acc.as<float4>(), ctr.as<DevCounters>()));
+				int h_cnt = 0, h_err = 0;
+				CK(cudaMemcpyAsync(&h_cnt, q[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "read queue count");
+				CK(cudaMemcpyAsync(&h_err, ctl + 3, sizeof(int), cudaMemcpyDeviceToHost, s), "read pool error");
+				CK(cudaStreamSynchronize(s), "shading tail");
+				d2h += 2 * sizeof(int);
+				prof_collect();
+				if(h_err) return fail(SRAY_EDEVICE, "shading pool: a wait for work ran out");
+				n_rays = h_cnt;
+				cur ^= 1;
+				continue;
+			}
 			int need = n_rays * per_ray_children;
 			if(need < n_rays) need = n_rays;
 			int r = ensure_queue(cur ^ 1, need);
@@ -1289,6 +1560,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 	CK(cudaStreamSynchronize(s), "render");
 	d2h += sizeof hc + (fb_is_device ? 0 : (int64_t)npix * 16);
 	stats.primary_rays = (int64_t)hc.rays[0];
+	stats.secondary_rays += (int64_t)hc.rays[1];
 	stats.shadow_rays = (int64_t)hc.rays[2];
 	stats.gathers = (int64_t)hc.rays[3];
 	stats.kernel_launches = (int)(launch_count - l0);
@@ -1714,7 +1986,7 @@ void sray_gpu_shutdown(void)
 	DevBuf *bufs[] = {&R.mnodes, &R.mtris, &R.mprim, &R.tri_pos, &R.tri_attr, &R.objs, &R.mats, &R.lights, &R.snodes, &R.sslots,
 		&R.xf, &R.light_pos, &R.cam_m, &R.projbits, &R.coverage, &R.qbuf[0], &R.qbuf[1], &R.hits, &R.gq, &R.sq, &R.acc, &R.hist, &R.sums,
 		&R.active[0], &R.active[1], &R.spp, &R.fbdev, &R.ctr, &R.counts, &R.bnodes, &R.btris, &R.bprim, &R.bhome,
-		&R.fbl, &R.tnodes, &R.ohome};
+		&R.fbl, &R.tnodes, &R.ohome, &R.pool_ready};
 	for(DevBuf *b : bufs) b->release();
 	PhotonBufs *pb[] = {&R.caust, &R.gi};
 	for(PhotonBufs *p : pb) {

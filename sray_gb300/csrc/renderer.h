@@ -104,7 +104,7 @@ struct Renderer {
 	DScene S;
 
 	/* render buffers */
-	DevBuf qbuf[2], hits, gq, sq, acc, hist, sums, active[2], spp, fbdev, ctr, counts, fbl;
+	DevBuf qbuf[2], hits, gq, sq, acc, hist, sums, active[2], spp, fbdev, ctr, counts, fbl, pool_ready;
 	RayQueue q[2];
 	int qcap[2] = {0, 0};
 	sray_stats stats;
