@@ -219,6 +219,82 @@ void MeshBvh::build_items(const float *mn, const float *mx, size_t n, int leaf_m
 	depth = B.max_depth;
 }
 
+namespace {
+struct Entry {
+	int ref;
+	float mn[3], mx[3];
+	double area() const
+	{
+		if(ref == BVH_NONE) return -1.0;
+		double e[3];
+		for(int a = 0; a < 3; a++) e[a] = mx[a] > mn[a] ? (double)mx[a] - (double)mn[a] : 0.0;
+		return e[0] * e[1] + e[1] * e[2] + e[2] * e[0];
+	}
+};
+
+void children_of(const DevBvhNode &n, Entry *e)
+{
+	e[0].ref = n.left;
+	e[1].ref = n.right;
+	for(int a = 0; a < 3; a++) {
+		e[0].mn[a] = n.lmn[a];
+		e[0].mx[a] = n.lmx[a];
+		e[1].mn[a] = n.rmn[a];
+		e[1].mx[a] = n.rmx[a];
+	}
+}
+
+int collapse_node(const std::vector<DevBvhNode> &b2, int n2, std::vector<DevBvh4> &out)
+{
+	Entry c[4];
+	int nc = 2;
+	children_of(b2[n2], c);
+	while(nc < 4) {
+		int best = -1;
+		double ba = -1.0;
+		for(int k = 0; k < nc; k++) {
+			if(c[k].ref < 0 || c[k].ref == BVH_NONE) continue;
+			double a = c[k].area();
+			if(a > ba) { ba = a; best = k; }
+		}
+		if(best < 0) break;
+		Entry two[2];
+		children_of(b2[c[best].ref], two);
+		c[best] = two[0];
+		c[nc++] = two[1];
+	}
+	int id = (int)out.size();
+	out.push_back(DevBvh4());
+	int refs[4];
+	for(int k = 0; k < 4; k++) {
+		if(k >= nc || c[k].ref == BVH_NONE) refs[k] = BVH_NONE;
+		else if(c[k].ref >= 0) refs[k] = collapse_node(b2, c[k].ref, out);
+		else refs[k] = c[k].ref;
+	}
+	DevBvh4 &d = out[id];
+	memset(&d, 0, sizeof d);
+	for(int k = 0; k < 4; k++) {
+		bool ok = k < nc && refs[k] != BVH_NONE;
+		d.lox[k] = ok ? c[k].mn[0] : FLT_MAX;
+		d.loy[k] = ok ? c[k].mn[1] : FLT_MAX;
+		d.loz[k] = ok ? c[k].mn[2] : FLT_MAX;
+		d.hix[k] = ok ? c[k].mx[0] : -FLT_MAX;
+		d.hiy[k] = ok ? c[k].mx[1] : -FLT_MAX;
+		d.hiz[k] = ok ? c[k].mx[2] : -FLT_MAX;
+		d.child[k] = refs[k];
+	}
+	return id;
+}
+}  // namespace
+
+void MeshBvh::collapse4(std::vector<DevBvh4> &out) const
+{
+	out.clear();
+	if(nodes.empty()) return;
+	out.reserve(nodes.size() / 2 + 1);
+	collapse_node(nodes, 0, out);
+}
+
 void MeshBvh::build(const std::vector<float> &pos)
 {
 	size_t nf = pos.size() / 9;

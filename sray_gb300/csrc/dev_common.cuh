@@ -43,11 +43,11 @@ struct DScene {
 	const DevNode *mnodes;    /* mesh octrees (object space) */
 	const DevTri *mtris;
 	const int *mprim;
-	const DevBvhNode *bnodes; /* mesh hierarchies (object space) */
+	const DevBvh4 *bnodes;    /* mesh hierarchies, 4-wide (object space) */
 	const DevTri *btris;      /* triangles in hierarchy leaf order */
 	const int *bprim;         /* their face indices */
 	const int *bhome;         /* their home nodes in the mesh octrees */
-	const DevBvhNode *tnodes; /* object hierarchy (world space), null if none */
+	const DevBvh4 *tnodes;    /* object hierarchy, 4-wide (world space), null if none */
 	const int *ohome;         /* per object: its home node in the scene octree */
 	unsigned long long *bvh_fallbacks;   /* hits the octree did not confirm */
 	const DevObj *objs;
@@ -690,15 +690,6 @@ __device__ inline bool octree_reaches(const DevNode *nodes, const int *ids, int 
 	return false;
 }
 
-__device__ __forceinline__ void load_bvh_node(const DevBvhNode *nodes, int i, float4 &f0, float4 &f1, float4 &f2, int4 &f3)
-{
-	const float4 *np = reinterpret_cast<const float4 *>(nodes + i);
-	f0 = __ldg(np);
-	f1 = __ldg(np + 1);
-	f2 = __ldg(np + 2);
-	f3 = __ldg(reinterpret_cast<const int4 *>(np) + 3);
-}
-
 /* the object-space ray of object o at time index ti */
 __device__ __forceinline__ RayT object_ray(const DScene &S, int o, int ti, V3 wo, V3 wd)
 {
@@ -794,75 +785,77 @@ __device__ __forceinline__ int trace_two_level(const DScene &S, V3 wo, V3 wd, in
 			cur = ob.bvh_root;
 			continue;
 		}
-		/* a node of the object hierarchy (world space) or of a mesh's */
-		float4 f0, f1, f2;
-		int4 f3;
-		load_bvh_node(inst ? S.bnodes : S.tnodes, cur, f0, f1, f2, f3);
+		if(inst && cur < 0) {
+			/* a leaf of the mesh hierarchy: its faces */
+			unsigned v = ~(unsigned)cur;
+			cur = BVH_NONE;
+			int start = (int)(v >> 4), cnt = (int)(v & 15u);
+			const float4 *tp = reinterpret_cast<const float4 *>(S.btris + start);
+			bool done = false;
+			for(int k = 0; k < cnt; k++) {
+				float4 a = __ldg(tp + 3 * k), b = __ldg(tp + 3 * k + 1), c = __ldg(tp + 3 * k + 2);
+				if(COUNT) tc->prims++;
+				float t;
+				if(!tri_hit(a, b, c, r, S.eps, best, t)) continue;
+				int prim = __ldg(S.bprim + start + k);
+				if(ANY) {
+					bobj = iobj;
+					bprim = prim;
+					bslot = start + k;
+					best = t;
+					done = true;
+					break;
+				}
+				if(t < best) {
+					best = t;
+					bobj = iobj;
+					bprim = prim;
+					bslot = start + k;
+					eq = false;
+				} else if(iobj != bobj || prim != bprim) {
+					eq = true;
+				}
+			}
+			if(ANY && done) break;
+			continue;
+		}
+		/* a node of the object hierarchy (world space) or of a mesh's: up to
+		 * four children in one 128-byte line; the hit ones (nodes, leaves, or
+		 * objects) are visited nearest first, each leaf and object in an
+		 * iteration of its own so that the lanes of a warp stay together */
+		const float4 *np = reinterpret_cast<const float4 *>((inst ? S.bnodes : S.tnodes) + cur);
+		float4 lx = __ldg(np), ly = __ldg(np + 1), lz = __ldg(np + 2);
+		float4 hx = __ldg(np + 3), hy = __ldg(np + 4), hz = __ldg(np + 5);
+		int4 ch = __ldg(reinterpret_cast<const int4 *>(np) + 6);
 		if(COUNT) tc->nodes++;
 		float lim = fminf(best, 1.0f);
-		float tl = 0.0f, tr = 0.0f;
-		bool hl = f3.x != BVH_NONE && wide_box(rc, f0.x, f0.y, f0.z, f0.w, f1.x, f1.y, lim, tl);
-		bool hr = f3.y != BVH_NONE && wide_box(rc, f1.z, f1.w, f2.x, f2.y, f2.z, f2.w, lim, tr);
-		if(inst) {
-			/* face leaves are tested here */
-			#pragma unroll
-			for(int side = 0; side < 2; side++) {
-				int ref = side ? f3.y : f3.x;
-				bool hit = side ? hr : hl;
-				if(!hit || ref >= 0) continue;
-				unsigned v = ~(unsigned)ref;
-				int start = (int)(v >> 4), cnt = (int)(v & 15u);
-				const float4 *tp = reinterpret_cast<const float4 *>(S.btris + start);
-				for(int k = 0; k < cnt; k++) {
-					float4 a = __ldg(tp + 3 * k), b = __ldg(tp + 3 * k + 1), c = __ldg(tp + 3 * k + 2);
-					if(COUNT) tc->prims++;
-					float t;
-					if(!tri_hit(a, b, c, r, S.eps, best, t)) continue;
-					int prim = __ldg(S.bprim + start + k);
-					if(ANY) {
-						bobj = iobj;
-						bprim = prim;
-						bslot = start + k;
-						best = t;
-						break;
-					}
-					if(t < best) {
-						best = t;
-						bobj = iobj;
-						bprim = prim;
-						bslot = start + k;
-						eq = false;
-					} else if(iobj != bobj || prim != bprim) {
-						eq = true;
-					}
-				}
-				if(ANY && bobj >= 0) break;
-				if(side) hr = false; else hl = false;
-			}
-			if(ANY && bobj >= 0) break;
-			if(!ANY) {
-				if(hl && tl > best) hl = false;
-				if(hr && tr > best) hr = false;
-			}
-		}
-		/* object-hierarchy leaves are objects (negative references): they
-		 * are entered like nodes */
-		if(hl && hr) {
-			int nr = f3.x, fr = f3.y;
-			float ft = tr;
-			if(tr < tl) { nr = f3.y; fr = f3.x; ft = tl; }
-			if(sp >= SRAY_STACK) { *overflow = 1; return ANY ? 0 : 1; }
-			st.node[sp] = fr;
-			st.te[sp] = ft;
-			sp++;
-			cur = nr;
-		} else if(hl) {
-			cur = f3.x;
-		} else if(hr) {
-			cur = f3.y;
-		} else {
+		int ref[4] = {ch.x, ch.y, ch.z, ch.w};
+		float key[4];
+		float tn;
+		key[0] = (ref[0] != BVH_NONE && wide_box(rc, lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, lim, tn)) ? tn : INFINITY;
+		key[1] = (ref[1] != BVH_NONE && wide_box(rc, lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, lim, tn)) ? tn : INFINITY;
+		key[2] = (ref[2] != BVH_NONE && wide_box(rc, lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, lim, tn)) ? tn : INFINITY;
+		key[3] = (ref[3] != BVH_NONE && wide_box(rc, lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, lim, tn)) ? tn : INFINITY;
+#define SRAY_CSWAP(i, j) do { if(key[j] < key[i]) { float tk = key[i]; key[i] = key[j]; key[j] = tk; int tr_ = ref[i]; ref[i] = ref[j]; ref[j] = tr_; } } while(0)
+		SRAY_CSWAP(0, 1);
+		SRAY_CSWAP(2, 3);
+		SRAY_CSWAP(0, 2);
+		SRAY_CSWAP(1, 3);
+		SRAY_CSWAP(1, 2);
+#undef SRAY_CSWAP
+		if(key[0] == INFINITY) {
 			cur = BVH_NONE;
+			continue;
 		}
+		#pragma unroll
+		for(int k = 3; k >= 1; k--) {
+			if(key[k] == INFINITY) continue;
+			if(sp >= SRAY_STACK) { *overflow = 1; return ANY ? 0 : 1; }
+			st.node[sp] = ref[k];
+			st.te[sp] = key[k];
+			sp++;
+		}
+		cur = ref[0];
 	}
 	if(bobj < 0) return ANY ? 0 : 1;
 	if(!ANY && eq) return 0;

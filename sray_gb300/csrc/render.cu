@@ -1039,11 +1039,11 @@ void Renderer::fill_scene_desc()
 	D.mnodes = mnodes.as<DevNode>();
 	D.mtris = mtris.as<DevTri>();
 	D.mprim = mprim.as<int>();
-	D.bnodes = bnodes.as<DevBvhNode>();
+	D.bnodes = bnodes.as<DevBvh4>();
 	D.btris = btris.as<DevTri>();
 	D.bprim = bprim.as<int>();
 	D.bhome = bhome.as<int>();
-	D.tnodes = has_tlas ? tnodes.as<DevBvhNode>() : nullptr;
+	D.tnodes = has_tlas ? tnodes.as<DevBvh4>() : nullptr;
 	D.ohome = ohome.as<int>();
 	D.bvh_fallbacks = ctr.p ? &ctr.as<DevCounters>()->bvh_fallbacks : nullptr;
 	D.objs = objs.as<DevObj>();
@@ -1111,7 +1111,7 @@ int Renderer::upload_scene(cudaStream_t s)
 	std::vector<DevTri> tris;
 	std::vector<int> prim;
 	std::vector<float> tp, ta;
-	std::vector<DevBvhNode> bn;
+	std::vector<DevBvh4> bn;
 	std::vector<DevTri> bt;
 	std::vector<int> bp, bh;
 	int tri_cursor = 0;
@@ -1144,17 +1144,18 @@ int Renderer::upload_scene(cudaStream_t s)
 		if(!m.bvh.nodes.empty() && bt.size() + m.bvh.order.size() < ((size_t)1 << 27)) {
 			int noff = (int)bn.size(), toff = (int)bt.size();
 			m.bvh_base = noff;
-			for(const DevBvhNode &src : m.bvh.nodes) {
-				DevBvhNode d = src;
-				int *refs[2] = {&d.left, &d.right};
-				for(int k = 0; k < 2; k++) {
-					int ref = *refs[k];
+			std::vector<DevBvh4> n4;
+			m.bvh.collapse4(n4);
+			for(const DevBvh4 &src : n4) {
+				DevBvh4 d = src;
+				for(int k = 0; k < 4; k++) {
+					int ref = d.child[k];
 					if(ref == BVH_NONE) continue;
-					if(ref >= 0) *refs[k] = ref + noff;
+					if(ref >= 0) d.child[k] = ref + noff;
 					else {
 						unsigned v = ~(unsigned)ref;
 						unsigned start = (v >> 4) + (unsigned)toff, cnt = v & 15u;
-						*refs[k] = (int)~((start << 4) | cnt);
+						d.child[k] = (int)~((start << 4) | cnt);
 					}
 				}
 				bn.push_back(d);
@@ -1252,7 +1253,7 @@ int Renderer::build_frame(long bt0, long bt1, cudaStream_t s)
 	/* the object hierarchy: each object boxed by the union of the octree
 	 * leaves that list it (so that it is entered whenever the octree would
 	 * test the object), one object per leaf */
-	std::vector<DevBvhNode> tn;
+	std::vector<DevBvh4> tn;
 	std::vector<int> ohome_h;
 	if(!sc.oct.nodes.empty() && !sc.objs.empty()) {
 		size_t no = sc.objs.size();
@@ -1280,16 +1281,14 @@ int Renderer::build_frame(long bt0, long bt1, cudaStream_t s)
 		}
 		MeshBvh tl;
 		tl.build_items(mn.data(), mx.data(), no, 1);
-		for(const DevBvhNode &src : tl.nodes) {
-			DevBvhNode d = src;
-			int *refs[2] = {&d.left, &d.right};
-			for(int k = 0; k < 2; k++) {
-				int ref = *refs[k];
+		tl.collapse4(tn);
+		for(DevBvh4 &d : tn) {
+			for(int k = 0; k < 4; k++) {
+				int ref = d.child[k];
 				if(ref == BVH_NONE || ref >= 0) continue;
 				unsigned v = ~(unsigned)ref;
-				*refs[k] = ~tl.order[v >> 4];   /* leaf: the object itself */
+				d.child[k] = ~tl.order[v >> 4];   /* leaf: the object itself */
 			}
-			tn.push_back(d);
 		}
 		octree_homes_boxes(sc.oct, sc.oct_boxes, index_of, ohome_h);
 	}

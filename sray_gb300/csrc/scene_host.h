@@ -77,6 +77,9 @@ struct MeshBvh {
 	void build(const std::vector<float> &pos);   /* over faces: 9 floats each */
 	/* over boxes (3 floats min, 3 max per item), at most leaf_max per leaf */
 	void build_items(const float *mn, const float *mx, size_t n, int leaf_max);
+	/* the same hierarchy with up to four children per node: each node takes
+	 * over the children of its largest inner children (by surface area) */
+	void collapse4(std::vector<DevBvh4> &out) const;
 };
 
 /* one unique triangle mesh (identical meshes of several objects share it) */

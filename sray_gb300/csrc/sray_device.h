@@ -50,6 +50,16 @@ struct alignas(16) DevBvhNode {
 	int pad[2];
 };
 
+/* a node of the 4-wide hierarchies the GPU traverses, one 128-byte line:
+ * the boxes of up to four children (planes in structure-of-arrays order)
+ * and their references, encoded as in DevBvhNode */
+struct alignas(128) DevBvh4 {
+	float lox[4], loy[4], loz[4];
+	float hix[4], hiy[4], hiz[4];
+	int child[4];
+	int pad[4];
+};
+
 struct alignas(16) DevTri {
 	float a[4];     /* v0.xyz, n.x */
 	float b[4];     /* v1.xyz, n.y */
