@@ -574,47 +574,50 @@ int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored)
 	}
 	int total = prefix[nl];
 	if(total <= 0) return 0;
-	DevBuf pre, scl;
+	DevBuf &pre = P.prefix, &scl = P.scale;
 	PCK(pre.upload(prefix, s), "photon prefix");
 	PCK(scl.upload(scale, s), "photon scale");
 	R.h2d += (int64_t)(prefix.size() * 4 + scale.size() * 4);
 	PCK(P.tmp_ph.ensure((size_t)total * sizeof(DevPhoton)), "photon buffer");
 	PCK(P.valid.ensure((size_t)total * sizeof(int)), "photon flags");
-	PCK(R.ctr.ensure(sizeof(DevCounters)), "counters");
-	PCK(R.counts.ensure(64 * sizeof(int)), "counts");
-	PCK(cudaMemsetAsync(R.ctr.p, 0, sizeof(DevCounters), s), "counters");
-	PCK(cudaMemsetAsync(R.counts.p, 0, 2 * sizeof(int), s), "photon queue counts");
-	if(R.ensure_queue(0, total) || R.ensure_queue(1, total)) return SRAY_ECUDA;
-	PCK(R.hits.ensure((size_t)total * 16), "photon hits");
-	int *cnt = R.counts.as<int>();
-	R.q[0].count = cnt + 0;
-	R.q[1].count = cnt + 1;
-	LAUNCH(R, "photon_emit", s, k_photon_emit<<<grid_n(total, 128), 128, 0, s>>>(R.S, global, pre.as<int>(), nl, total, R.q[0],
-			P.valid.as<int>(), R.ctr.as<DevCounters>()));
+	PCK(R.pctr.ensure(sizeof(DevCounters)), "counters");
+	PCK(R.pcounts.ensure(64 * sizeof(int)), "counts");
+	PCK(cudaMemsetAsync(R.pctr.p, 0, sizeof(DevCounters), s), "counters");
+	PCK(cudaMemsetAsync(R.pcounts.p, 0, 4 * sizeof(int), s), "photon queue counts");
+	int *cnt = R.pcounts.as<int>();
+	R.pq[0].count = cnt + 0;
+	R.pq[1].count = cnt + 1;
+	if(R.ensure_pqueue(0, total) || R.ensure_pqueue(1, total)) return SRAY_ECUDA;
+	PCK(R.phits.ensure((size_t)total * 16), "photon hits");
+	/* the scene as the photon kernels see it: their counters */
+	DScene PS = R.S;
+	PS.bvh_fallbacks = &R.pctr.as<DevCounters>()->bvh_fallbacks;
+	DevCounters *pctr = R.pctr.as<DevCounters>();
+	LAUNCH(R, "photon_emit", s, k_photon_emit<<<grid_n(total, 128), 128, 0, s>>>(PS, global, pre.as<int>(), nl, total, R.pq[0],
+			P.valid.as<int>(), pctr));
 	int cur = 0;
 	int n_live = total;   /* upper bound until the first count is read */
 	bool finished = false;
 	for(int pass = 0; n_live > 0; pass++) {
 		if(pass >= 2 * PHOTON_GUARD + 4) return R.fail(SRAY_EDEVICE, "photon paths did not terminate");
-		PCK(cudaMemsetAsync(R.q[cur ^ 1].count, 0, sizeof(int), s), "reset photon queue");
+		PCK(cudaMemsetAsync(R.pq[cur ^ 1].count, 0, sizeof(int), s), "reset photon queue");
 		if(!finished && pass > 0 && n_live <= PHOTON_FINISH) {
 			/* the tail in one launch; what it hands back continues pass-wise */
 			finished = true;
 			PCK(cudaMemsetAsync(cnt + 2, 0, sizeof(int), s), "reset photon tail counter");
-			LAUNCH(R, "photon_finish", s, k_photon_finish<<<grid_n(n_live, 128), 128, 0, s>>>(R.S, global, pre.as<int>(),
-					scl.as<float>(), R.q[cur], cnt + 2, R.q[cur ^ 1], P.tmp_ph.as<DevPhoton>(), P.valid.as<int>(),
-					R.ctr.as<DevCounters>()));
-			PCK(cudaMemcpyAsync(&n_live, R.q[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "photon queue count");
+			LAUNCH(R, "photon_finish", s, k_photon_finish<<<grid_n(n_live, 128), 128, 0, s>>>(PS, global, pre.as<int>(),
+					scl.as<float>(), R.pq[cur], cnt + 2, R.pq[cur ^ 1], P.tmp_ph.as<DevPhoton>(), P.valid.as<int>(), pctr));
+			PCK(cudaMemcpyAsync(&n_live, R.pq[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "photon queue count");
 			PCK(cudaStreamSynchronize(s), "photon tail");
 			R.d2h += sizeof(int);
 			R.prof_collect();
 			cur ^= 1;
 			continue;
 		}
-		if(launch_trace(R, R.q[cur], n_live, "photon_trace", s)) return SRAY_ECUDA;
-		LAUNCH(R, "photon_bounce", s, k_photon_bounce<<<grid_n(n_live, 128), 128, 0, s>>>(R.S, global, pre.as<int>(),
-				scl.as<float>(), R.q[cur], R.hits.as<int4>(), R.q[cur ^ 1], P.tmp_ph.as<DevPhoton>(), P.valid.as<int>()));
-		PCK(cudaMemcpyAsync(&n_live, R.q[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "photon queue count");
+		if(launch_trace(R, PS, R.pq[cur], n_live, "photon_trace", s)) return SRAY_ECUDA;
+		LAUNCH(R, "photon_bounce", s, k_photon_bounce<<<grid_n(n_live, 128), 128, 0, s>>>(PS, global, pre.as<int>(),
+				scl.as<float>(), R.pq[cur], R.phits.as<int4>(), R.pq[cur ^ 1], P.tmp_ph.as<DevPhoton>(), P.valid.as<int>()));
+		PCK(cudaMemcpyAsync(&n_live, R.pq[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "photon queue count");
 		PCK(cudaStreamSynchronize(s), "photon pass");
 		R.d2h += sizeof(int);
 		R.prof_collect();
@@ -627,12 +630,12 @@ int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored)
 	LAUNCH(R, "photon_compact", s, k_count_valid<<<nb, 256, 0, s>>>(P.valid.as<int>(), total, bc));
 	LAUNCH(R, "photon_compact", s, k_scan_excl<<<1, 1024, 0, s>>>(bc, nb, bc + nb));
 	unsigned h_n = 0;
+	DevCounters hc;
 	PCK(cudaMemcpyAsync(&h_n, bc + nb, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "stored count");
+	PCK(cudaMemcpyAsync(&hc, pctr, sizeof hc, cudaMemcpyDeviceToHost, s), "counters");
 	PCK(cudaStreamSynchronize(s), "photon trace");
 	R.d2h += sizeof(unsigned) + sizeof(DevCounters);
 	R.prof_collect();
-	DevCounters hc;
-	PCK(cudaMemcpy(&hc, R.ctr.p, sizeof hc, cudaMemcpyDeviceToHost), "counters");
 	if(hc.overflow) return R.fail(SRAY_EDEVICE, "traversal stack overflow while tracing photons");
 	if(hc.gen_dir_fail) return R.fail(SRAY_EDEVICE, "projection-map sampling found no covered cell");
 	int n = (int)h_n;
@@ -709,8 +712,6 @@ int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored)
 	M.cells = P.cells.as<uint2>();
 	PCK(cudaStreamSynchronize(s), "photon map build");
 	R.prof_collect();
-	pre.release();
-	scl.release();
 	return 0;
 }
 

@@ -423,7 +423,7 @@ __global__ void __launch_bounds__(128) k_shade(DScene S, RayQueue qi, const int4
  * whose slot is beyond every reservation leaves once no ray is in flight
  * (no more can come); every wait is bounded and sets the error word when
  * it runs out. */
-#define RENDER_TAIL 131072        /* rays below which the rest of the tree runs in k_render_pool */
+#define RENDER_TAIL 32768         /* rays below which the rest of the tree runs in k_render_pool */
 #define POOL_SPIN_LIMIT (1 << 22) /* polls of a slot before the pool gives up (about 0.5 s) */
 #define POOL_SHADOW (-0x7ffffff0)   /* iter of a pool item that is a light sample's shadow ray */
 
@@ -1015,7 +1015,14 @@ void Renderer::prof_end(Pending *p, cudaStream_t s)
 /* called after a stream synchronisation: every pending pair has completed */
 void Renderer::prof_collect()
 {
+	/* pairs on a stream that has not got there yet (the photon stream runs
+	 * beside the render stream) stay pending */
+	size_t keep = 0;
 	for(size_t i = 0; i < pending.size(); i++) {
+		if(cudaEventQuery(pending[i].b) != cudaSuccess) {
+			pending[keep++] = pending[i];
+			continue;
+		}
 		float ms = 0.0f;
 		if(cudaEventElapsedTime(&ms, pending[i].a, pending[i].b) == cudaSuccess) {
 			ktimes[pending[i].kind].ms += ms;
@@ -1024,7 +1031,7 @@ void Renderer::prof_collect()
 		event_pool.push_back(pending[i].a);
 		event_pool.push_back(pending[i].b);
 	}
-	pending.clear();
+	pending.resize(keep);
 }
 
 #define CK(call, where) do { cudaError_t e_ = (call); if(e_ != cudaSuccess) return cuda_fail(e_, where); } while(0)
@@ -1371,29 +1378,41 @@ int Renderer::shoot(cudaStream_t s, int *nc, int *ng)
 	return 0;
 }
 
-int Renderer::ensure_queue(int which, int cap)
+int Renderer::queue_alloc(DevBuf &buf, RayQueue &Q, int &qc, int cap)
 {
-	if(cap <= qcap[which]) return 0;
+	if(cap <= qc) return 0;
 	size_t per = 16 * 5 + 8;
 	size_t bytes = (size_t)cap * per + 1024;
-	CK(qbuf[which].ensure(bytes), "allocate ray queue");
-	char *b = qbuf[which].as<char>();
-	RayQueue &Q = q[which];
+	CK(buf.ensure(bytes), "allocate ray queue");
+	char *b = buf.as<char>();
+	int *count = Q.count;
 	Q.o = (float4 *)b; b += (size_t)cap * 16;
 	Q.d = (float4 *)b; b += (size_t)cap * 16;
 	Q.w = (float4 *)b; b += (size_t)cap * 16;
 	Q.meta = (int4 *)b; b += (size_t)cap * 16;
 	Q.stk = (float4 *)b; b += (size_t)cap * 16;
 	Q.ext = (int2 *)b; b += (size_t)cap * 8;
+	Q.count = count;
 	Q.cap = cap;
-	qcap[which] = cap;
+	qc = cap;
 	return 0;
 }
 
-int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t s)
+int Renderer::ensure_queue(int which, int cap)
+{
+	return queue_alloc(qbuf[which], q[which], qcap[which], cap);
+}
+
+int Renderer::ensure_pqueue(int which, int cap)
+{
+	return queue_alloc(pqbuf[which], pq[which], pqcap[which], cap);
+}
+
+int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t s, bool overlap_photons)
 {
 	(void)msec;
-	if(!built || !photons_ready) return fail(SRAY_ESTATE, "frame not prepared (build and shoot photons first)");
+	if(!built || (!photons_ready && !overlap_photons)) return fail(SRAY_ESTATE, "frame not prepared (build and shoot photons first)");
+	bool photons_pending = overlap_photons;
 	int npix = opt.width * opt.height;
 	int ds = opt.diffuse_samples < 0 ? 0 : (opt.diffuse_samples > MAX_DS ? MAX_DS : opt.diffuse_samples);
 	int maxs = opt.max_samples < 1 ? 1 : opt.max_samples;
@@ -1530,6 +1549,14 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 					acc.as<float4>(), ctr.as<DevCounters>(), fbl.as<int>()));
 			LAUNCH(*this, "octree_retrace", s, k_shadow<false><<<152, 128, 0, s>>>(S, sq.as<ShadowReq>(), cnt + 5, acc.as<float4>(),
 					ctr.as<DevCounters>(), fbl.as<int>()));
+			if(photons_pending) {
+				/* the first gathers need the photon maps: trace them on the
+				 * photon stream now, while this bounce's closest hits,
+				 * shading and shadow rays run, and make the render stream
+				 * wait for them */
+				photons_pending = false;
+				if((r = shoot_on_photon_stream(s))) return r;
+			}
 			LAUNCH(*this, "gather", s, k_gather<<<grid_for(n_rays, GATHER_WARPS), GATHER_WARPS * 32, 0, s>>>(S, gq.as<GatherReq>(), cnt + 2,
 					acc.as<float4>(), ctr.as<DevCounters>()));
 			stats.secondary_rays += depth ? n_rays : 0;
@@ -1552,6 +1579,10 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 		d2h += sizeof(int);
 		prof_collect();
 		n_active = h_next;
+	}
+	if(photons_pending) {
+		int r = shoot_on_photon_stream(s);
+		if(r) return r;
 	}
 	DevCounters hc;
 	CK(cudaMemcpyAsync(&hc, ctr.p, sizeof hc, cudaMemcpyDeviceToHost, s), "read counters");
@@ -1579,27 +1610,50 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 /* closest hits of the first n (upper bound; the queue's count decides)
  * rays of q into hits: the hierarchy pass, then the octree pass over the
  * rays it listed */
-int Renderer::trace_rays(const RayQueue &qq, int n, const char *name, bool count, cudaStream_t s)
+int Renderer::trace_rays_with(const DScene &D, const RayQueue &qq, int n, const char *name, bool count, cudaStream_t s,
+		int4 *hit_out, DevBuf &fb, DevCounters *c)
 {
-	CK(fbl.ensure(((size_t)n + 1) * sizeof(int)), "fallback list");
-	CK(cudaMemsetAsync(fbl.p, 0, sizeof(int), s), "reset fallback list");
+	CK(fb.ensure(((size_t)n + 1) * sizeof(int)), "fallback list");
+	CK(cudaMemsetAsync(fb.p, 0, sizeof(int), s), "reset fallback list");
 	if(count) {
-		LAUNCH(*this, name, s, k_trace<true, true><<<grid_for(n, 128), 128, 0, s>>>(S, qq, hits.as<int4>(), ctr.as<DevCounters>(),
-				fbl.as<int>()));
-		LAUNCH(*this, "octree_retrace", s, k_trace<true, false><<<152, 128, 0, s>>>(S, qq, hits.as<int4>(), ctr.as<DevCounters>(),
-				fbl.as<int>()));
+		LAUNCH(*this, name, s, k_trace<true, true><<<grid_for(n, 128), 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
+		LAUNCH(*this, "octree_retrace", s, k_trace<true, false><<<152, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
 	} else {
-		LAUNCH(*this, name, s, k_trace<false, true><<<grid_for(n, 128), 128, 0, s>>>(S, qq, hits.as<int4>(), ctr.as<DevCounters>(),
-				fbl.as<int>()));
-		LAUNCH(*this, "octree_retrace", s, k_trace<false, false><<<152, 128, 0, s>>>(S, qq, hits.as<int4>(), ctr.as<DevCounters>(),
-				fbl.as<int>()));
+		LAUNCH(*this, name, s, k_trace<false, true><<<grid_for(n, 128), 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
+		LAUNCH(*this, "octree_retrace", s, k_trace<false, false><<<152, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
 	}
 	return 0;
 }
 
-int launch_trace(Renderer &R, const RayQueue &q, int n, const char *name, cudaStream_t s)
+int Renderer::trace_rays(const RayQueue &qq, int n, const char *name, bool count, cudaStream_t s)
 {
-	return R.trace_rays(q, n, name, false, s);
+	return trace_rays_with(S, qq, n, name, count, s, hits.as<int4>(), fbl, ctr.as<DevCounters>());
+}
+
+/* photon passes: the photon buffers and counters */
+int launch_trace(Renderer &R, const DScene &D, const RayQueue &q, int n, const char *name, cudaStream_t s)
+{
+	return R.trace_rays_with(D, q, n, name, false, s, R.phits.as<int4>(), R.pfbl, R.pctr.as<DevCounters>());
+}
+
+int Renderer::photon_stream()
+{
+	if(ps) return 0;
+	CK(cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking), "photon stream");
+	CK(cudaEventCreateWithFlags(&ps_done, cudaEventDisableTiming), "photon event");
+	return 0;
+}
+
+/* photon maps on the photon stream; the render stream s waits for them */
+int Renderer::shoot_on_photon_stream(cudaStream_t s)
+{
+	int r = photon_stream();
+	if(r) return r;
+	/* the frame's tables were uploaded on s, which build_frame synchronised */
+	if((r = shoot(ps, nullptr, nullptr))) return r;
+	CK(cudaEventRecord(ps_done, ps), "photon event");
+	CK(cudaStreamWaitEvent(s, ps_done, 0), "wait for photon maps");
+	return 0;
 }
 
 static Renderer *g_R = nullptr;
@@ -1772,8 +1826,7 @@ int sray_gpu_render(long msec, float *fb, int fb_is_device, void *stream)
 	long long l0 = R.launch_count;
 	R.h2d = R.d2h = 0;
 	int r = R.build_frame(t0, t1, as_stream(stream));
-	if(!r) r = R.shoot(as_stream(stream), nullptr, nullptr);
-	if(!r) r = R.render_pixels(msec, fb, fb_is_device, as_stream(stream));
+	if(!r) r = R.render_pixels(msec, fb, fb_is_device, as_stream(stream), true);
 	if(r) g_err = R.err;
 	else R.stats.kernel_launches = (int)(R.launch_count - l0);
 	return r;
@@ -1985,13 +2038,17 @@ void sray_gpu_shutdown(void)
 	DevBuf *bufs[] = {&R.mnodes, &R.mtris, &R.mprim, &R.tri_pos, &R.tri_attr, &R.objs, &R.mats, &R.lights, &R.snodes, &R.sslots,
 		&R.xf, &R.light_pos, &R.cam_m, &R.projbits, &R.coverage, &R.qbuf[0], &R.qbuf[1], &R.hits, &R.gq, &R.sq, &R.acc, &R.hist, &R.sums,
 		&R.active[0], &R.active[1], &R.spp, &R.fbdev, &R.ctr, &R.counts, &R.bnodes, &R.btris, &R.bprim, &R.bhome,
-		&R.fbl, &R.tnodes, &R.ohome, &R.pool_ready};
+		&R.fbl, &R.tnodes, &R.ohome, &R.pool_ready, &R.pqbuf[0], &R.pqbuf[1], &R.phits, &R.pfbl, &R.pcounts, &R.pctr};
+	if(R.ps) cudaStreamSynchronize(R.ps);
 	for(DevBuf *b : bufs) b->release();
 	PhotonBufs *pb[] = {&R.caust, &R.gi};
 	for(PhotonBufs *p : pb) {
-		DevBuf *pbufs[] = {&p->ph, &p->cells, &p->tmp_ph, &p->valid, &p->keys, &p->keys2, &p->vals, &p->vals2, &p->lin, &p->hist, &p->scan};
+		DevBuf *pbufs[] = {&p->ph, &p->cells, &p->tmp_ph, &p->valid, &p->keys, &p->keys2, &p->vals, &p->vals2, &p->lin, &p->hist, &p->scan,
+			&p->prefix, &p->scale};
 		for(DevBuf *b : pbufs) b->release();
 	}
+	if(R.ps_done) cudaEventDestroy(R.ps_done);
+	if(R.ps) cudaStreamDestroy(R.ps);
 	delete g_R;
 	g_R = nullptr;
 }

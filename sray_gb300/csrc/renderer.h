@@ -78,7 +78,7 @@ struct DevCounters {
 };
 
 struct PhotonBufs {
-	DevBuf ph, cells, tmp_ph, valid, keys, keys2, vals, vals2, lin, hist, scan;
+	DevBuf ph, cells, tmp_ph, valid, keys, keys2, vals, vals2, lin, hist, scan, prefix, scale;
 	DPhotonMap map;
 	int n = 0;
 };
@@ -107,6 +107,13 @@ struct Renderer {
 	DevBuf qbuf[2], hits, gq, sq, acc, hist, sums, active[2], spp, fbdev, ctr, counts, fbl, pool_ready;
 	RayQueue q[2];
 	int qcap[2] = {0, 0};
+	/* photon tracing has buffers and a stream of its own, so that it can run
+	 * beside the first bounce of a frame */
+	DevBuf pqbuf[2], phits, pfbl, pcounts, pctr;
+	RayQueue pq[2];
+	int pqcap[2] = {0, 0};
+	cudaStream_t ps = nullptr;
+	cudaEvent_t ps_done = nullptr;
 	sray_stats stats;
 
 	/* profiling: event pairs per launch, resolved after each synchronisation */
@@ -133,9 +140,18 @@ struct Renderer {
 	int upload_scene(cudaStream_t s);
 	int build_frame(long t0, long t1, cudaStream_t s);
 	int shoot(cudaStream_t s, int *nc, int *ng);
-	int render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t s);
+	/* overlap_photons: shoot the photon maps on the photon stream while the
+	 * first bounce's closest hits, shading and shadow rays run, the gathers
+	 * waiting for them */
+	int render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t s, bool overlap_photons = false);
 	int ensure_queue(int which, int cap);
+	int ensure_pqueue(int which, int cap);
+	int queue_alloc(DevBuf &buf, RayQueue &Q, int &qc, int cap);
 	int trace_rays(const RayQueue &q, int n, const char *name, bool count, cudaStream_t s);
+	int trace_rays_with(const DScene &D, const RayQueue &q, int n, const char *name, bool count, cudaStream_t s, int4 *hit_out,
+			DevBuf &fb, DevCounters *c);
+	int photon_stream();
+	int shoot_on_photon_stream(cudaStream_t s);
 	void fill_scene_desc();
 };
 
@@ -148,7 +164,7 @@ struct Renderer {
 	} while(0)
 
 /* render.cu: closest hits of the first n rays of q into R.hits */
-int launch_trace(Renderer &R, const RayQueue &q, int n, const char *name, cudaStream_t s);
+int launch_trace(Renderer &R, const DScene &D, const RayQueue &q, int n, const char *name, cudaStream_t s);
 
 /* photon.cu */
 int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored);
