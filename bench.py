@@ -253,7 +253,7 @@ def run_ours(args):
     kt_count = g.kernel_times(reset=True)
     trace_launches = max(kt_count.get("trace", (0.0, 1))[1], 1)
     rays_traced = st_count["primary_rays"] + st_count["secondary_rays"]
-    trace_bytes = rays_traced * (48 + 16) + st_count["node_visits"] * 64 + st_count["prim_tests"] * 48
+    trace_bytes = rays_traced * (48 + 16) + st_count["node_visits"] * 128 + st_count["prim_tests"] * 48
 
     # timed region: K frames, device timing on the launch stream, kernel events live
     g.set_profiling(time_kernels=True, count_work=False)
@@ -327,7 +327,7 @@ def run_ours(args):
             "unit": "GB/s", "frac": achieved / hbm, "peak_source": src, "traffic": traffic,
             "algorithmic_bytes_per_launch": bytes_per_launch,
             "avg_launch_ms": tr_avg_s * 1e3, "dominant_kernel": dom[0],
-            "note": "algorithmic bytes = rays*64 + hierarchy nodes read*64 + triangle records read*48 (counted "
+            "note": "algorithmic bytes = rays*64 + 4-wide hierarchy nodes read*128 + triangle records read*48 (counted "
                     "pass); traffic = DRAM bytes per render launch from the committed ncu capture: the nodes and "
                     "triangles are re-read from L1/L2, so DRAM traffic is a small fraction of the algorithmic bytes",
             "node_records_per_ray": st_count["node_visits"] / max(rays_traced, 1),
