@@ -627,25 +627,40 @@ __device__ __forceinline__ bool trace_any_octree_impl(const DScene &S, V3 wo, V3
  * rounding-level coincidences and to objects moving outside their frame
  * bounds -- the ray is marked and traced again by the octrees alone. */
 
-/* a ray prepared for the widened box test: the inverse direction clamped to
- * finite values, and per axis the widening in units of t.  The widening,
- * 2^-19 of the largest coordinate the segment reaches, covers the rounding
- * of the hit point and of the edge tests (a few units in the last place of
- * those coordinates) with a wide margin. */
+/* A ray prepared for the widened box test: the inverse direction clamped to
+ * finite values, and per axis the widening in units of t.
+ *
+ * The widening must cover, for a face the triangle test accepts at t, the
+ * distance by which the segment's exact point at t can lie outside the
+ * face's box, plus the rounding of the slab parameters.  The computed hit
+ * point o + d t is within 2^-23 (|o| + |p|) of the exact one, and the edge
+ * tests accept it at most a few units in the last place of those
+ * coordinates outside the face.  A slab parameter (x - o) / d_a is rounded
+ * by at most 3 * 2^-24 of |x - o|.  Every point and plane involved lies in
+ * the hierarchy's bounds, so all of this is below 2^-20.5 (|o| + R), where
+ * R is the largest coordinate of those bounds.  The widening is 2^-17 of that
+ * (a factor of 11 over it).  It does not grow with the segment's length, which
+ * is RAY_MAGNITUDE times the unit direction (src/opt.h:21), while the scene is
+ * a few hundred units across. */
 struct RayC {
 	V3 o, inv, slack;
 };
 
-__device__ __forceinline__ RayC make_rayc(const RayT &r)
+__device__ __forceinline__ RayC make_rayc(const RayT &r, float bound)
 {
 	RayC c;
 	c.o = r.o;
 	c.inv = mk(fminf(fmaxf(r.inv.x, -1e20f), 1e20f), fminf(fmaxf(r.inv.y, -1e20f), 1e20f), fminf(fmaxf(r.inv.z, -1e20f), 1e20f));
 	float om = fmaxf(fmaxf(fabsf(r.o.x), fabsf(r.o.y)), fabsf(r.o.z));
-	float dm = fmaxf(fmaxf(fabsf(r.d.x), fabsf(r.d.y)), fabsf(r.d.z));
-	float delta = (om + dm) * 1.9073486e-6f;   /* 2^-19 */
+	float delta = (om + bound) * 7.6293945e-6f;   /* 2^-17 */
 	c.slack = mk(delta * fabsf(c.inv.x), delta * fabsf(c.inv.y), delta * fabsf(c.inv.z));
 	return c;
+}
+
+/* the largest coordinate of a box */
+__device__ __forceinline__ float box_bound(const float *mn, const float *mx)
+{
+	return fmaxf(fmaxf(fmaxf(fabsf(mn[0]), fabsf(mn[1])), fmaxf(fabsf(mn[2]), fabsf(mx[0]))), fmaxf(fabsf(mx[1]), fabsf(mx[2])));
 }
 
 __device__ __forceinline__ bool wide_box(const RayC &c, float x0, float y0, float z0, float x1, float y1, float z1, float limit,
@@ -711,7 +726,8 @@ __device__ __forceinline__ int trace_two_level(const DScene &S, V3 wo, V3 wd, in
 	if(!S.tnodes) return ANY ? 2 : 0;
 	int ti = time_index(S, time);
 	RayT wr = make_ray(wo, wd);
-	RayC wc = make_rayc(wr);
+	const DevNode &sroot = S.snodes[S.sroot];
+	RayC wc = make_rayc(wr, box_bound(sroot.mn, sroot.mx));
 	RayT r = wr;
 	RayC rc = wc;
 	TStack st;
@@ -778,7 +794,7 @@ __device__ __forceinline__ int trace_two_level(const DScene &S, V3 wo, V3 wd, in
 			const DevNode &rn = S.mnodes[ob.mesh_root];
 			if(!box_hit(rn.mn, rn.mx, orr, te) || (!ANY && SRAY_PRUNE(te, best))) continue;
 			r = orr;
-			rc = make_rayc(orr);
+			rc = make_rayc(orr, box_bound(rn.mn, rn.mx));
 			inst = true;
 			inst_base = sp;
 			iobj = o;
