@@ -177,35 +177,49 @@ __device__ bool gen_dir(const uint32_t *bits, sray_rng *s, V3 *out)
 	return false;
 }
 
-/* The reference traces one photon to its end with recursive calls.  Here the
- * photons of a map advance together, one surface interaction per pass, over
- * ray queues that the renderer's closest-hit kernel traces:
+/* The reference traces one photon to its end with recursive calls, one map
+ * after the other.  Here the photons of both maps advance together, one
+ * surface interaction per pass, over ray queues that the renderer's
+ * closest-hit kernel traces:
  *   k_photon_emit    Light::gen_photon (src/light.cc:111-148) with
  *                    ProjMap::gen_dir (src/projmap.cc:193-209) -> queue
  *   k_trace          closest hits of the queue (render.cu)
  *   k_photon_bounce  one trace_caustics_photon / trace_global_photon step
  *                    per photon -> stored photon, next queue, or loss
+ *   k_photon_finish  the last photons, each traced to its end
  * A photon keeps its own Philox stream: the queue carries its stream address
- * (light, index) and draw count, so photon j of light i takes the same draws
- * and the same path as the CPU oracle's recursive tracer.
+ * (map, light, index) and draw count, so photon j of light i takes the same
+ * draws and the same path as the CPU oracle's recursive tracer.
  *
  * Photon queue entry (RayQueue fields):
  *   o = origin, colour r     d = direction, colour g
- *   w = colour b, ior, interactions in this phase, photon id
- *   meta = light, iter, phase | type << 4, time
+ *   w = colour b, ior, interactions in this phase, photon index in its map
+ *   meta = light, iter, phase | type << 4 | map << 8, time
  *   stk = ior stack          ext = draws taken, stack depth
- * Phase 0 follows the global rules, phase 1 the caustic rules. */
+ * Phase 0 follows the global rules, phase 1 the caustic rules; map 0 is the
+ * caustic map, map 1 the global one. */
 
 #define PHOTON_GUARD 4096   /* interactions per phase (loop bound of the oracle's tracer) */
 #define PHOTON_FINISH 65536 /* live photons below which the tail is traced in one launch */
 
+/* the two maps being traced: emission counts, per-light prefix sums and
+ * power scales, and the per-photon output */
+struct PhotonSet {
+	int total[2];
+	int nlights;
+	const int *prefix[2];
+	const float *scale[2];
+	DevPhoton *out[2];
+	int *valid[2];
+};
+
 __device__ __forceinline__ void push_photon(const RayQueue &q, int slot, const PRay &r, const PState &ph, int guard, int gid,
-		int li, int phase, uint32_t draws)
+		int li, int phase, int map, uint32_t draws)
 {
 	q.o[slot] = make_float4(r.o.x, r.o.y, r.o.z, ph.col[0]);
 	q.d[slot] = make_float4(r.d.x, r.d.y, r.d.z, ph.col[1]);
 	q.w[slot] = make_float4(ph.col[2], r.st.ior, __int_as_float(guard), __int_as_float(gid));
-	q.meta[slot] = make_int4(li, r.iter, phase | (ph.type << 4), r.time);
+	q.meta[slot] = make_int4(li, r.iter, phase | (ph.type << 4) | (map << 8), r.time);
 	q.stk[slot] = make_float4(r.st.stk[0], r.st.stk[1], r.st.stk[2], r.st.stk[3]);
 	q.ext[slot] = make_int2((int)draws, r.st.sp);
 }
@@ -218,13 +232,17 @@ static __device__ __forceinline__ int photon_slot(int *counter)
 	return g.shfl(base, 0) + (int)g.thread_rank();
 }
 
-__global__ void __launch_bounds__(128) k_photon_emit(DScene S, int global, const int *prefix, int nlights, int total,
-		RayQueue q, int *valid, DevCounters *ctr)
+__global__ void __launch_bounds__(128) k_photon_emit(DScene S, PhotonSet P, RayQueue q, DevCounters *ctr)
 {
 	int gfail = 0;
-	for(int gid = blockIdx.x * blockDim.x + threadIdx.x; gid < total; gid += gridDim.x * blockDim.x) {
+	int all = P.total[0] + P.total[1];
+	for(int id = blockIdx.x * blockDim.x + threadIdx.x; id < all; id += gridDim.x * blockDim.x) {
+		int map = id >= P.total[0] ? 1 : 0;
+		int gid = map ? id - P.total[0] : id;
+		int global = map;
+		const int *prefix = P.prefix[map];
 		int li = 0;
-		while(li + 1 < nlights && prefix[li + 1] <= gid) li++;
+		while(li + 1 < P.nlights && prefix[li + 1] <= gid) li++;
 		int j = gid - prefix[li];
 		sray_rng s;
 		sray_rng_init(&s, S.seed, global ? SRAY_DOM_GLOBAL : SRAY_DOM_CAUST, (uint32_t)j, (uint32_t)li);
@@ -250,7 +268,7 @@ __global__ void __launch_bounds__(128) k_photon_emit(DScene S, int global, const
 		} else {
 			dir = sphrand(&s, 1.0f);
 		}
-		valid[gid] = 0;
+		P.valid[map][gid] = 0;
 		if(ok && S.iter > 0) {
 			PRay r;
 			r.o = pos;
@@ -261,7 +279,7 @@ __global__ void __launch_bounds__(128) k_photon_emit(DScene S, int global, const
 			r.st.sp = 0;
 			for(int k = 0; k < 4; k++) r.st.stk[k] = 0.0f;
 			int slot = photon_slot(q.count);
-			push_photon(q, slot, r, ph, 0, gid, li, global ? 0 : 1, s.n);
+			push_photon(q, slot, r, ph, 0, gid, li, global ? 0 : 1, map, s.n);
 		}
 	}
 	if(gfail) atomicOr(&ctr->gen_dir_fail, 1);
@@ -271,7 +289,7 @@ __global__ void __launch_bounds__(128) k_photon_emit(DScene S, int global, const
 struct PFlight {
 	PRay r;
 	PState ph;
-	int li, gid, phase, guard;
+	int li, gid, phase, guard, map;
 	uint32_t draws;
 };
 
@@ -282,6 +300,7 @@ __device__ __forceinline__ void load_photon(const RayQueue &q, int i, PFlight &f
 	int2 ext = q.ext[i];
 	f.li = meta.x;
 	f.phase = meta.z & 15;
+	f.map = (meta.z >> 8) & 1;
 	f.guard = __float_as_int(w4.z);
 	f.gid = __float_as_int(w4.w);
 	f.r.o = mk(o4.x, o4.y, o4.z);
@@ -292,29 +311,29 @@ __device__ __forceinline__ void load_photon(const RayQueue &q, int i, PFlight &f
 	f.r.st.stk[0] = k4.x; f.r.st.stk[1] = k4.y; f.r.st.stk[2] = k4.z; f.r.st.stk[3] = k4.w;
 	f.r.st.sp = ext.y;
 	f.ph.col[0] = o4.w; f.ph.col[1] = d4.w; f.ph.col[2] = w4.x;
-	f.ph.type = meta.z >> 4;
+	f.ph.type = (meta.z >> 4) & 15;
 	f.draws = (uint32_t)ext.x;
 }
 
 /* one surface interaction of a photon at hit h (h.obj >= 0): stores it
  * (returns 1), loses it (0) or leaves it ready for its next trace (2) */
-__device__ __forceinline__ int photon_interact(const DScene &S, int global, const int *prefix, const float *scale, PFlight &f,
-		const Hit &h, DevPhoton *out, int *valid)
+__device__ __forceinline__ int photon_interact(const DScene &S, const PhotonSet &P, PFlight &f, const Hit &h)
 {
+	int global = f.map;
 	sray_rng s;
-	sray_rng_init(&s, S.seed, global ? SRAY_DOM_GLOBAL : SRAY_DOM_CAUST, (uint32_t)(f.gid - prefix[f.li]), (uint32_t)f.li);
+	sray_rng_init(&s, S.seed, global ? SRAY_DOM_GLOBAL : SRAY_DOM_CAUST, (uint32_t)(f.gid - P.prefix[f.map][f.li]), (uint32_t)f.li);
 	sray_rng_seek(&s, f.draws);
 	int res = f.phase == 0 ? global_step(S, f.r, f.ph, h, &s) : caust_step(S, f.r, f.ph, h, &s);
 	f.draws = s.n;
 	if(res == P_STORE) {
 		if(!global && f.ph.type != CAUST_PHOTON) return 0;
-		float sc = scale[f.li];
+		float sc = P.scale[f.map][f.li];
 		DevPhoton p;
 		p.p[0] = f.ph.pos.x; p.p[1] = f.ph.pos.y; p.p[2] = f.ph.pos.z; p.p[3] = f.ph.col[0] * sc;
 		p.d[0] = f.ph.dir.x; p.d[1] = f.ph.dir.y; p.d[2] = f.ph.dir.z; p.d[3] = f.ph.col[1] * sc;
 		p.n[0] = f.ph.norm.x; p.n[1] = f.ph.norm.y; p.n[2] = f.ph.norm.z; p.n[3] = f.ph.col[2] * sc;
-		out[f.gid] = p;
-		valid[f.gid] = 1;
+		P.out[f.map][f.gid] = p;
+		P.valid[f.map][f.gid] = 1;
 		return 1;
 	}
 	if(res == P_DROP) return 0;
@@ -327,8 +346,7 @@ __device__ __forceinline__ int photon_interact(const DScene &S, int global, cons
 	return f.r.iter <= 0 ? 0 : 2;
 }
 
-__global__ void __launch_bounds__(128) k_photon_bounce(DScene S, int global, const int *prefix, const float *scale, RayQueue qi,
-		const int4 *hits, RayQueue qo, DevPhoton *out, int *valid)
+__global__ void __launch_bounds__(128) k_photon_bounce(DScene S, PhotonSet P, RayQueue qi, const int4 *hits, RayQueue qo)
 {
 	int n = *qi.count;
 	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -341,21 +359,21 @@ __global__ void __launch_bounds__(128) k_photon_bounce(DScene S, int global, con
 		h.tie = hv.w;
 		PFlight f;
 		load_photon(qi, i, f);
-		if(photon_interact(S, global, prefix, scale, f, h, out, valid) != 2) continue;
+		if(photon_interact(S, P, f, h) != 2) continue;
 		int slot = photon_slot(qo.count);
 		if(slot >= qo.cap) continue;                 /* cannot happen: a photon has one successor */
-		push_photon(qo, slot, f.r, f.ph, f.guard, f.gid, f.li, f.phase, f.draws);
+		push_photon(qo, slot, f.r, f.ph, f.guard, f.gid, f.li, f.phase, f.map, f.draws);
 	}
 }
 
-/* The tail of a photon map: once few photons are left, each thread takes
+/* The tail of the photon maps: once few photons are left, each thread takes
  * photons from the queue (through a shared counter) and traces every one to
  * its end, instead of one interaction per pass; a pass costs as much as its
  * slowest ray, and the tail is made of few photons on long paths.  Photons
  * whose hit the octrees must decide are handed back, before that trace, to
  * the pending queue, which the pass-wise loop finishes. */
-__global__ void __launch_bounds__(128) k_photon_finish(DScene S, int global, const int *prefix, const float *scale, RayQueue qi,
-		int *next, RayQueue qpend, DevPhoton *out, int *valid, DevCounters *ctr)
+__global__ void __launch_bounds__(128) k_photon_finish(DScene S, PhotonSet P, RayQueue qi, int *next, RayQueue qpend,
+		DevCounters *ctr)
 {
 	int n = *qi.count;
 	int overflow = 0;
@@ -368,11 +386,11 @@ __global__ void __launch_bounds__(128) k_photon_finish(DScene S, int global, con
 			Hit h;
 			if(!trace_two_level<false, false>(S, f.r.o, f.r.d, f.r.time, h, nullptr, &overflow)) {
 				int slot = photon_slot(qpend.count);
-				if(slot < qpend.cap) push_photon(qpend, slot, f.r, f.ph, f.guard, f.gid, f.li, f.phase, f.draws);
+				if(slot < qpend.cap) push_photon(qpend, slot, f.r, f.ph, f.guard, f.gid, f.li, f.phase, f.map, f.draws);
 				break;
 			}
 			if(h.obj < 0) break;
-			if(photon_interact(S, global, prefix, scale, f, h, out, valid) != 2) break;
+			if(photon_interact(S, P, f, h) != 2) break;
 		}
 	}
 	if(overflow) atomicOr(&ctr->overflow, 1);
@@ -549,15 +567,17 @@ static int grid_n(int n, int block)
 
 #define PCK(call, where) do { cudaError_t e_ = (call); if(e_ != cudaSuccess) return R.cuda_fail(e_, where); } while(0)
 
-int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored)
+/* emission counts of one map: photon split by mean light intensity
+ * (src/render.cc:87-110), per-light prefix sums and power scales uploaded */
+static int photon_setup(Renderer &R, int global, cudaStream_t s, int *total_out)
 {
 	PhotonBufs &P = global ? R.gi : R.caust;
 	const sray_opts &opt = R.opt;
 	int num = global ? opt.gi_photons : opt.caust_photons;
 	int nl = (int)R.sc.lights.size();
 	P.map.n = 0;
-	*stored = 0;
-	/* photon split by mean light intensity (src/render.cc:87-110) */
+	*total_out = 0;
+	if(num <= 0 || nl <= 0) return 0;
 	std::vector<double> inten(nl);
 	double accp = 0.0;
 	for(int i = 0; i < nl; i++) {
@@ -574,12 +594,37 @@ int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored)
 	}
 	int total = prefix[nl];
 	if(total <= 0) return 0;
-	DevBuf &pre = P.prefix, &scl = P.scale;
-	PCK(pre.upload(prefix, s), "photon prefix");
-	PCK(scl.upload(scale, s), "photon scale");
+	PCK(P.prefix.upload(prefix, s), "photon prefix");
+	PCK(P.scale.upload(scale, s), "photon scale");
 	R.h2d += (int64_t)(prefix.size() * 4 + scale.size() * 4);
 	PCK(P.tmp_ph.ensure((size_t)total * sizeof(DevPhoton)), "photon buffer");
 	PCK(P.valid.ensure((size_t)total * sizeof(int)), "photon flags");
+	*total_out = total;
+	return 0;
+}
+
+static int photon_finalize(Renderer &R, int global, int total, cudaStream_t s, int *stored);
+
+/* both photon maps, traced together */
+int photon_shoot_maps(Renderer &R, cudaStream_t s, int *nc, int *ng)
+{
+	*nc = *ng = 0;
+	int tot[2];
+	int r;
+	if((r = photon_setup(R, 0, s, &tot[0]))) return r;
+	if((r = photon_setup(R, 1, s, &tot[1]))) return r;
+	int all = tot[0] + tot[1];
+	if(all <= 0) return 0;
+	PhotonSet PSet;
+	PSet.nlights = (int)R.sc.lights.size();
+	for(int m = 0; m < 2; m++) {
+		PhotonBufs &P = m ? R.gi : R.caust;
+		PSet.total[m] = tot[m];
+		PSet.prefix[m] = P.prefix.as<int>();
+		PSet.scale[m] = P.scale.as<float>();
+		PSet.out[m] = P.tmp_ph.as<DevPhoton>();
+		PSet.valid[m] = P.valid.as<int>();
+	}
 	PCK(R.pctr.ensure(sizeof(DevCounters)), "counters");
 	PCK(R.pcounts.ensure(64 * sizeof(int)), "counts");
 	PCK(cudaMemsetAsync(R.pctr.p, 0, sizeof(DevCounters), s), "counters");
@@ -587,16 +632,15 @@ int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored)
 	int *cnt = R.pcounts.as<int>();
 	R.pq[0].count = cnt + 0;
 	R.pq[1].count = cnt + 1;
-	if(R.ensure_pqueue(0, total) || R.ensure_pqueue(1, total)) return SRAY_ECUDA;
-	PCK(R.phits.ensure((size_t)total * 16), "photon hits");
+	if(R.ensure_pqueue(0, all) || R.ensure_pqueue(1, all)) return SRAY_ECUDA;
+	PCK(R.phits.ensure((size_t)all * 16), "photon hits");
 	/* the scene as the photon kernels see it: their counters */
 	DScene PS = R.S;
 	PS.bvh_fallbacks = &R.pctr.as<DevCounters>()->bvh_fallbacks;
 	DevCounters *pctr = R.pctr.as<DevCounters>();
-	LAUNCH(R, "photon_emit", s, k_photon_emit<<<grid_n(total, 128), 128, 0, s>>>(PS, global, pre.as<int>(), nl, total, R.pq[0],
-			P.valid.as<int>(), pctr));
+	LAUNCH(R, "photon_emit", s, k_photon_emit<<<grid_n(all, 128), 128, 0, s>>>(PS, PSet, R.pq[0], pctr));
 	int cur = 0;
-	int n_live = total;   /* upper bound until the first count is read */
+	int n_live = all;   /* upper bound until the first count is read */
 	bool finished = false;
 	for(int pass = 0; n_live > 0; pass++) {
 		if(pass >= 2 * PHOTON_GUARD + 4) return R.fail(SRAY_EDEVICE, "photon paths did not terminate");
@@ -605,8 +649,8 @@ int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored)
 			/* the tail in one launch; what it hands back continues pass-wise */
 			finished = true;
 			PCK(cudaMemsetAsync(cnt + 2, 0, sizeof(int), s), "reset photon tail counter");
-			LAUNCH(R, "photon_finish", s, k_photon_finish<<<grid_n(n_live, 128), 128, 0, s>>>(PS, global, pre.as<int>(),
-					scl.as<float>(), R.pq[cur], cnt + 2, R.pq[cur ^ 1], P.tmp_ph.as<DevPhoton>(), P.valid.as<int>(), pctr));
+			LAUNCH(R, "photon_finish", s, k_photon_finish<<<grid_n(n_live, 128), 128, 0, s>>>(PS, PSet, R.pq[cur], cnt + 2,
+					R.pq[cur ^ 1], pctr));
 			PCK(cudaMemcpyAsync(&n_live, R.pq[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "photon queue count");
 			PCK(cudaStreamSynchronize(s), "photon tail");
 			R.d2h += sizeof(int);
@@ -615,14 +659,32 @@ int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored)
 			continue;
 		}
 		if(launch_trace(R, PS, R.pq[cur], n_live, "photon_trace", s)) return SRAY_ECUDA;
-		LAUNCH(R, "photon_bounce", s, k_photon_bounce<<<grid_n(n_live, 128), 128, 0, s>>>(PS, global, pre.as<int>(),
-				scl.as<float>(), R.pq[cur], R.phits.as<int4>(), R.pq[cur ^ 1], P.tmp_ph.as<DevPhoton>(), P.valid.as<int>()));
+		LAUNCH(R, "photon_bounce", s, k_photon_bounce<<<grid_n(n_live, 128), 128, 0, s>>>(PS, PSet, R.pq[cur], R.phits.as<int4>(),
+				R.pq[cur ^ 1]));
 		PCK(cudaMemcpyAsync(&n_live, R.pq[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "photon queue count");
 		PCK(cudaStreamSynchronize(s), "photon pass");
 		R.d2h += sizeof(int);
 		R.prof_collect();
 		cur ^= 1;
 	}
+	DevCounters hc;
+	PCK(cudaMemcpyAsync(&hc, pctr, sizeof hc, cudaMemcpyDeviceToHost, s), "counters");
+	PCK(cudaStreamSynchronize(s), "photon trace");
+	R.d2h += sizeof(DevCounters);
+	if(hc.overflow) return R.fail(SRAY_EDEVICE, "traversal stack overflow while tracing photons");
+	if(hc.gen_dir_fail) return R.fail(SRAY_EDEVICE, "projection-map sampling found no covered cell");
+	if(tot[0] && (r = photon_finalize(R, 0, tot[0], s, nc))) return r;
+	if(tot[1] && (r = photon_finalize(R, 1, tot[1], s, ng))) return r;
+	return 0;
+}
+
+/* a map's stored photons: compacted in emission order, sorted by grid cell,
+ * with the cell table */
+static int photon_finalize(Renderer &R, int global, int total, cudaStream_t s, int *stored)
+{
+	PhotonBufs &P = global ? R.gi : R.caust;
+	const sray_opts &opt = R.opt;
+	*stored = 0;
 	/* compaction in emission order */
 	int nb = (total + TILE - 1) / TILE;
 	PCK(P.scan.ensure((size_t)(nb + 4) * sizeof(unsigned)), "scan");
@@ -630,14 +692,10 @@ int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored)
 	LAUNCH(R, "photon_compact", s, k_count_valid<<<nb, 256, 0, s>>>(P.valid.as<int>(), total, bc));
 	LAUNCH(R, "photon_compact", s, k_scan_excl<<<1, 1024, 0, s>>>(bc, nb, bc + nb));
 	unsigned h_n = 0;
-	DevCounters hc;
 	PCK(cudaMemcpyAsync(&h_n, bc + nb, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "stored count");
-	PCK(cudaMemcpyAsync(&hc, pctr, sizeof hc, cudaMemcpyDeviceToHost, s), "counters");
-	PCK(cudaStreamSynchronize(s), "photon trace");
-	R.d2h += sizeof(unsigned) + sizeof(DevCounters);
+	PCK(cudaStreamSynchronize(s), "photon compaction");
+	R.d2h += sizeof(unsigned);
 	R.prof_collect();
-	if(hc.overflow) return R.fail(SRAY_EDEVICE, "traversal stack overflow while tracing photons");
-	if(hc.gen_dir_fail) return R.fail(SRAY_EDEVICE, "projection-map sampling found no covered cell");
 	int n = (int)h_n;
 	*stored = n;
 	if(n == 0) return 0;

@@ -1367,9 +1367,8 @@ int Renderer::shoot(cudaStream_t s, int *nc, int *ng)
 		CK(coverage.upload(cov, s), "upload coverage");
 		h2d += (int64_t)(bits.size() * 4 + cov.size() * 4);
 		fill_scene_desc();
-		int r;
-		if(opt.caust_photons && (r = photon_shoot_map(*this, 0, s, &c))) return r;
-		if(opt.gi_photons && (r = photon_shoot_map(*this, 1, s, &g))) return r;
+		int r = photon_shoot_maps(*this, s, &c, &g);
+		if(r) return r;
 	}
 	photons_ready = true;
 	fill_scene_desc();

@@ -167,7 +167,7 @@ struct Renderer {
 int launch_trace(Renderer &R, const DScene &D, const RayQueue &q, int n, const char *name, cudaStream_t s);
 
 /* photon.cu */
-int photon_shoot_map(Renderer &R, int global, cudaStream_t s, int *stored);
+int photon_shoot_maps(Renderer &R, cudaStream_t s, int *caust_stored, int *gi_stored);
 
 }  // namespace sray
 
