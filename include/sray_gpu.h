@@ -186,6 +186,28 @@ typedef struct sray_stats {
 
 int sray_gpu_get_stats(sray_stats *st);
 
+/* ---- Radiance cache (extension, no reference counterpart) ----
+ * A small MLP standing in for the final gather of indirect light
+ * (shade_phong's diffuse rays + PhotonMap::radiance_est, src/shader.cc:154-187,
+ * src/pmap.cc:143-178).  Inputs x[n][9]: position scaled to the scene box,
+ * unit normal, unit direction; outputs y[n][3].  12-band sin/cos encoding,
+ * 216 -> 64 -> 64 -> 64 -> 64 -> 3 (ReLU), BF16 weights on tensor cores with
+ * FP32 accumulation, relative L2 loss, Adam (lr 1e-3).  Parameters are
+ * exchanged as SRAY_NRC_PARAMS floats in the order W1 (64x216, row-major),
+ * b1, W2, b2, W3, b3, W4, b4, W5 (3x64), b5.  Pointers to x, y, targets,
+ * gradient and loss are device pointers. */
+#define SRAY_NRC_PARAMS 26563
+
+int sray_nrc_reset(uint64_t seed);
+int sray_nrc_set_params(const float *params, int n);
+int sray_nrc_get_params(float *params, int n);
+int sray_nrc_infer(int n, const float *x, float *y, void *stream);
+/* gradient of the loss over the batch (no update) */
+int sray_nrc_gradients(int n, const float *x, const float *targets, float *grad, float *loss, void *stream);
+/* one Adam step on the batch; *loss (device, optional) = the batch loss before the step */
+int sray_nrc_train(int n, const float *x, const float *targets, float *loss, void *stream);
+int sray_nrc_last_error(char *buf, size_t len);
+
 /* Profiling (extension, no reference counterpart).  flags bit 0: time every
  * kernel launch with CUDA events recorded on the launch stream; bit 1: count
  * octree node records read and primitive tests in the closest-hit kernel (slower;

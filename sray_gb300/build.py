@@ -23,8 +23,8 @@ CU_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "
             "-Xcompiler", "-fPIC,-ffp-contract=off", "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 CC_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-I/usr/local/cuda/include"]
 
-SOURCES = ["render.cu", "photon.cu", "scene_host.cc", "bvh_host.cc"]
-HEADERS = ["dev_common.cuh", "renderer.h", "scene_host.h", "sray_device.h", "range_ff.h"]
+SOURCES = ["render.cu", "photon.cu", "nrc.cu", "scene_host.cc", "bvh_host.cc"]
+HEADERS = ["dev_common.cuh", "renderer.h", "scene_host.h", "sray_device.h", "range_ff.h", "nrc.h"]
 
 
 def _deps():

@@ -1,0 +1,807 @@
+/* nrc.cu -- the radiance cache: a small MLP that stands in for the photon-map
+ * final gather of indirect light, trained online on the gather's own
+ * estimates (no counterpart in the reference; the final gather it replaces is
+ * shade_phong's diffuse rays + PhotonMap::radiance_est, src/shader.cc:154-187,
+ * src/pmap.cc:143-178).
+ *
+ * Network: 9 inputs (position scaled to the scene box, normal, direction),
+ * 12-band sin/cos encoding (216 features), 4 hidden layers of 64 ReLU units,
+ * 3 linear outputs; relative L2 loss; Adam.  Weights are kept in FP32 (the
+ * Adam master copy) and used as BF16 by warp-level tensor-core MMAs
+ * (mma.sync m16n8k16, FP32 accumulation): a warp carries 16 samples through
+ * all five layers with the activations in registers, the accumulator tile of
+ * one layer becoming the operand tile of the next.
+ *
+ *   k_nrc_forward<false>  inference: encode + 5 layers, fused
+ *   k_nrc_forward<true>   training forward: also stores the layer inputs
+ *                         (BF16) and the loss gradient of the outputs
+ *   k_nrc_backward        dZ of layers 4..1 through the transposed weights,
+ *                         bias gradients
+ *   k_nrc_wgrad<L>        weight gradients dW = dZ^T H over the batch (MMA,
+ *                         samples split over blocks, FP32 atomics)
+ *   k_nrc_adam            Adam on the FP32 master, BF16 copies refreshed
+ *
+ * The CPU restatement (checker of these kernels) is oracle/nrc.py.
+ */
+#include <math.h>
+#include <string.h>
+#include <stdint.h>
+#include <vector>
+#include <mutex>
+#include <string>
+#include <cuda_bf16.h>
+#include "sray_gpu.h"
+#include "sray_rng.h"
+#include "nrc.h"
+
+namespace sray {
+
+/* ---- parameter layout (packed FP32, the order of oracle/nrc.py) ---- */
+enum {
+	NRC_F = 216,            /* encoded features */
+	NRC_FP = 224,           /* padded to 14 k-tiles of 16 */
+	NRC_H = 64,
+	NRC_O = 3,
+	OFF_W1 = 0,
+	OFF_B1 = OFF_W1 + NRC_H * NRC_F,
+	OFF_W2 = OFF_B1 + NRC_H,
+	OFF_B2 = OFF_W2 + NRC_H * NRC_H,
+	OFF_W3 = OFF_B2 + NRC_H,
+	OFF_B3 = OFF_W3 + NRC_H * NRC_H,
+	OFF_W4 = OFF_B3 + NRC_H,
+	OFF_B4 = OFF_W4 + NRC_H * NRC_H,
+	OFF_W5 = OFF_B4 + NRC_H,
+	OFF_B5 = OFF_W5 + NRC_O * NRC_H,
+	NRC_NPARAM = OFF_B5 + NRC_O
+};
+static_assert(NRC_NPARAM == SRAY_NRC_PARAMS, "parameter count");
+
+/* shared-memory row strides (bf16 elements), padded against bank conflicts */
+enum { LD1 = 232, LDH = 72, LD5T = 24 };
+
+/* BF16 weight images in global memory, in the shared-memory layout:
+ *   w1  [64][LD1]      (in 0..215, zero up to 231)
+ *   w2-4 [64][LDH]     (out rows, in columns)
+ *   w5  [8][LDH]       (rows 3..7 zero)
+ *   w2t-w4t [64][LDH]  transposed (in rows, out columns), for the backward pass
+ *   w5t [64][LD5T]     transposed, out columns 3..23 zero
+ * plus the FP32 biases b1-b4 [64], b5 [8]. */
+struct NrcDev {
+	const __nv_bfloat16 *w1, *w2, *w3, *w4, *w5;
+	const __nv_bfloat16 *w2t, *w3t, *w4t, *w5t;
+	const float *bias;            /* 4 x 64 + 8 */
+};
+
+enum {
+	IMG_W1 = 0,
+	IMG_W2 = IMG_W1 + 64 * LD1,
+	IMG_W3 = IMG_W2 + 64 * LDH,
+	IMG_W4 = IMG_W3 + 64 * LDH,
+	IMG_W5 = IMG_W4 + 64 * LDH,
+	IMG_W2T = IMG_W5 + 8 * LDH,
+	IMG_W3T = IMG_W2T + 64 * LDH,
+	IMG_W4T = IMG_W3T + 64 * LDH,
+	IMG_W5T = IMG_W4T + 64 * LDH,
+	IMG_END = IMG_W5T + 64 * LD5T,
+	FWD_SMEM_BF16 = IMG_W2T,                /* w1..w5 */
+	BWD_SMEM_BF16 = IMG_END - IMG_W2T,      /* w2t..w5t */
+	NRC_NBIAS = 4 * 64 + 8
+};
+
+/* ---- warp-level MMA tiles ---- */
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
+{
+	asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+			: "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+			: "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
+{
+	__nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+	return *reinterpret_cast<uint32_t *>(&v);
+}
+
+__device__ __forceinline__ float bf16_lo(uint32_t v) { return __uint_as_float(v << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t v) { return __uint_as_float(v & 0xffff0000u); }
+
+/* B operand of a k16 x n8 tile whose element (k, n) is M[n0 + n][k0 + k] of
+ * a row-major shared matrix with row stride ld: two adjacent k per register */
+__device__ __forceinline__ void load_b(const __nv_bfloat16 *M, int ld, int n0, int k0, int lane, uint32_t &b0, uint32_t &b1)
+{
+	int g = lane >> 2, t = lane & 3;
+	const __nv_bfloat16 *p = M + (size_t)(n0 + g) * ld + k0 + 2 * t;
+	b0 = *reinterpret_cast<const uint32_t *>(p);
+	b1 = *reinterpret_cast<const uint32_t *>(p + 8);
+}
+
+/* a 16 x 64 activation block as accumulators: 8 n-tiles x 4 floats */
+struct Acc64 {
+	float d[8][4];
+};
+
+/* accumulators of a layer -> A operand tiles of the next (BF16): k-tile kt
+ * is made of n-tiles 2kt and 2kt+1 */
+__device__ __forceinline__ void acc_to_a(const Acc64 &z, uint32_t (&a)[4][4], bool relu)
+{
+	#pragma unroll
+	for(int kt = 0; kt < 4; kt++) {
+		const float *lo = z.d[2 * kt], *hi = z.d[2 * kt + 1];
+		float v[8] = {lo[0], lo[1], lo[2], lo[3], hi[0], hi[1], hi[2], hi[3]};
+		if(relu) {
+			#pragma unroll
+			for(int i = 0; i < 8; i++) v[i] = fmaxf(v[i], 0.0f);
+		}
+		a[kt][0] = pack_bf16(v[0], v[1]);
+		a[kt][1] = pack_bf16(v[2], v[3]);
+		a[kt][2] = pack_bf16(v[4], v[5]);
+		a[kt][3] = pack_bf16(v[6], v[7]);
+	}
+}
+
+/* 16 x 64 = A(16 x 64) W^T: W [64][LDH] (out, in) */
+__device__ __forceinline__ void layer64(const uint32_t (&a)[4][4], const __nv_bfloat16 *W, const float *bias, int lane, Acc64 &z)
+{
+	int t = lane & 3;
+	#pragma unroll
+	for(int nt = 0; nt < 8; nt++) {
+		float b0 = bias[nt * 8 + 2 * t], b1 = bias[nt * 8 + 2 * t + 1];
+		z.d[nt][0] = b0; z.d[nt][1] = b1; z.d[nt][2] = b0; z.d[nt][3] = b1;
+		#pragma unroll
+		for(int kt = 0; kt < 4; kt++) {
+			uint32_t w0, w1;
+			load_b(W, LDH, nt * 8, kt * 16, lane, w0, w1);
+			mma16816(z.d[nt], a[kt], w0, w1);
+		}
+	}
+}
+
+/* one encoded feature pair (sin, cos of pi 2^b x_v) for pair index p, 0 for padding */
+__device__ __forceinline__ uint32_t feature_pair(const float *x, int p)
+{
+	if(p >= NRC_F / 2) return 0u;
+	int v = p / 12, b = p - v * 12;
+	float s, c;
+	sincospif(x[v] * (float)(1 << b), &s, &c);
+	return pack_bf16(s, c);
+}
+
+/* the A operand of k-tile kt of the encoded inputs, rows g and g + 8 */
+__device__ __forceinline__ void encode_a(const float *xg, const float *xg8, int kt, int lane, uint32_t (&a)[4])
+{
+	int t = lane & 3;
+	int p0 = kt * 8 + t, p1 = kt * 8 + 4 + t;
+	a[0] = feature_pair(xg, p0);
+	a[1] = feature_pair(xg8, p0);
+	a[2] = feature_pair(xg, p1);
+	a[3] = feature_pair(xg8, p1);
+}
+
+__device__ __forceinline__ void copy_to_shared(__nv_bfloat16 *dst, const __nv_bfloat16 *src, int n)
+{
+	const uint4 *s = reinterpret_cast<const uint4 *>(src);
+	uint4 *d = reinterpret_cast<uint4 *>(dst);
+	for(int i = threadIdx.x; i < n / 8; i += blockDim.x) d[i] = s[i];
+}
+
+/* Forward pass, a warp per 16 samples.  x: [n][9]; y: [n][3] (inference) or
+ * unused.  TRAIN: t [n][3] targets; stores h0 [n16][NRC_FP] (encoded, BF16),
+ * h1..h4 [n16][64] (BF16), dz5 [n16][16] (BF16 loss gradient of the
+ * outputs), db5 partial sums and the loss. */
+struct TrainBufs {
+	__nv_bfloat16 *h[5];          /* h[0] encoded inputs, h[1..4] hidden */
+	__nv_bfloat16 *dz[6];         /* dz[1..4] hidden, dz[5] outputs (16 wide) */
+	float *grad;                  /* packed FP32 gradient */
+	float *loss;
+};
+
+template <bool TRAIN>
+__global__ void __launch_bounds__(128) k_nrc_forward(NrcDev net, int n, const float *x, float *y, const float *tgt, TrainBufs tb)
+{
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	__nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
+	float *sb = reinterpret_cast<float *>(sw + FWD_SMEM_BF16);
+	copy_to_shared(sw, net.w1, FWD_SMEM_BF16);
+	for(int i = threadIdx.x; i < NRC_NBIAS; i += blockDim.x) sb[i] = net.bias[i];
+	__syncthreads();
+	const __nv_bfloat16 *W1 = sw + IMG_W1, *W2 = sw + IMG_W2, *W3 = sw + IMG_W3, *W4 = sw + IMG_W4, *W5 = sw + IMG_W5;
+	int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	int g = lane >> 2, t = lane & 3;
+	int ntiles = (n + 15) >> 4;
+	float loss = 0.0f;
+	float db5[2] = {0.0f, 0.0f};
+	for(int tile = blockIdx.x * 4 + warp; tile < ntiles; tile += gridDim.x * 4) {
+		int r0 = tile * 16 + g, r1 = r0 + 8;
+		float xg[9], xg8[9];
+		#pragma unroll
+		for(int k = 0; k < 9; k++) {
+			xg[k] = r0 < n ? x[(size_t)r0 * 9 + k] : 0.0f;
+			xg8[k] = r1 < n ? x[(size_t)r1 * 9 + k] : 0.0f;
+		}
+		/* layer 1: 14 k-tiles of encoded features */
+		Acc64 z;
+		#pragma unroll
+		for(int nt = 0; nt < 8; nt++) {
+			float b0 = sb[nt * 8 + 2 * t], b1 = sb[nt * 8 + 2 * t + 1];
+			z.d[nt][0] = b0; z.d[nt][1] = b1; z.d[nt][2] = b0; z.d[nt][3] = b1;
+		}
+		for(int kt = 0; kt < NRC_FP / 16; kt++) {
+			uint32_t a[4];
+			encode_a(xg, xg8, kt, lane, a);
+			if(TRAIN) {
+				__nv_bfloat16 *h0 = tb.h[0];
+				uint32_t *p0 = reinterpret_cast<uint32_t *>(h0 + (size_t)r0 * NRC_FP + kt * 16 + 2 * t);
+				uint32_t *p1 = reinterpret_cast<uint32_t *>(h0 + (size_t)r1 * NRC_FP + kt * 16 + 2 * t);
+				p0[0] = a[0]; p1[0] = a[1]; p0[4] = a[2]; p1[4] = a[3];
+			}
+			#pragma unroll
+			for(int nt = 0; nt < 8; nt++) {
+				uint32_t w0, w1;
+				load_b(W1, LD1, nt * 8, kt * 16, lane, w0, w1);
+				mma16816(z.d[nt], a, w0, w1);
+			}
+		}
+		uint32_t a[4][4];
+		const __nv_bfloat16 *Ws[3] = {W2, W3, W4};
+		#pragma unroll
+		for(int l = 0; l < 3; l++) {
+			acc_to_a(z, a, true);
+			if(TRAIN) {
+				/* h_{l+1}: the BF16 input of layer l + 2 */
+				__nv_bfloat16 *h = tb.h[l + 1];
+				#pragma unroll
+				for(int kt = 0; kt < 4; kt++) {
+					uint32_t *p0 = reinterpret_cast<uint32_t *>(h + (size_t)r0 * 64 + kt * 16 + 2 * t);
+					uint32_t *p1 = reinterpret_cast<uint32_t *>(h + (size_t)r1 * 64 + kt * 16 + 2 * t);
+					p0[0] = a[kt][0]; p1[0] = a[kt][1]; p0[4] = a[kt][2]; p1[4] = a[kt][3];
+				}
+			}
+			layer64(a, Ws[l], sb + 64 * (l + 1), lane, z);
+		}
+		acc_to_a(z, a, true);
+		if(TRAIN) {
+			__nv_bfloat16 *h = tb.h[4];
+			#pragma unroll
+			for(int kt = 0; kt < 4; kt++) {
+				uint32_t *p0 = reinterpret_cast<uint32_t *>(h + (size_t)r0 * 64 + kt * 16 + 2 * t);
+				uint32_t *p1 = reinterpret_cast<uint32_t *>(h + (size_t)r1 * 64 + kt * 16 + 2 * t);
+				p0[0] = a[kt][0]; p1[0] = a[kt][1]; p0[4] = a[kt][2]; p1[4] = a[kt][3];
+			}
+		}
+		/* output layer: one n-tile (outputs 0..7, 3 used) */
+		float o[4];
+		o[0] = sb[256 + 2 * t]; o[1] = sb[256 + 2 * t + 1]; o[2] = o[0]; o[3] = o[1];
+		#pragma unroll
+		for(int kt = 0; kt < 4; kt++) {
+			uint32_t w0, w1;
+			load_b(W5, LDH, 0, kt * 16, lane, w0, w1);
+			mma16816(o, a[kt], w0, w1);
+		}
+		/* lane (g, t) holds outputs 2t, 2t+1 of rows g and g + 8 */
+		#pragma unroll
+		for(int half = 0; half < 2; half++) {
+			int r = half ? r1 : r0;
+			#pragma unroll
+			for(int c = 0; c < 2; c++) {
+				int col = 2 * t + c;
+				float yv = o[2 * half + c];
+				if(!TRAIN) {
+					if(r < n && col < NRC_O) y[(size_t)r * 3 + col] = yv;
+				} else {
+					float dy = 0.0f;
+					if(r < n && col < NRC_O) {
+						float tv = tgt[(size_t)r * 3 + col];
+						float den = yv * yv + 0.01f;
+						float e = yv - tv;
+						loss += e * e / den;
+						dy = 2.0f * e / den / (float)(3 * n);
+					}
+					/* dz5 row r, columns 0..15 (BF16); db5 from the FP32 value */
+					tb.dz[5][(size_t)r * 16 + col] = __float2bfloat16_rn(dy);
+					db5[c] += dy;
+					if(y && r < n && col < NRC_O) y[(size_t)r * 3 + col] = yv;
+				}
+			}
+		}
+		if(TRAIN && t < 4) {
+			/* columns 8..15 of dz5 are zero padding for the backward MMA k-tile */
+			tb.dz[5][(size_t)r0 * 16 + 8 + 2 * t] = __float2bfloat16_rn(0.0f);
+			tb.dz[5][(size_t)r0 * 16 + 9 + 2 * t] = __float2bfloat16_rn(0.0f);
+			tb.dz[5][(size_t)r1 * 16 + 8 + 2 * t] = __float2bfloat16_rn(0.0f);
+			tb.dz[5][(size_t)r1 * 16 + 9 + 2 * t] = __float2bfloat16_rn(0.0f);
+		}
+	}
+	if(TRAIN) {
+		for(int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
+		if(lane == 0 && loss != 0.0f) atomicAdd(tb.loss, loss / (float)(3 * n));
+		/* output-bias gradient: lanes with the same t hold the same columns */
+		for(int o = 4; o < 32; o <<= 1) {
+			db5[0] += __shfl_xor_sync(0xffffffffu, db5[0], o);
+			db5[1] += __shfl_xor_sync(0xffffffffu, db5[1], o);
+		}
+		if(g == 0) {
+			if(2 * t < NRC_O && db5[0] != 0.0f) atomicAdd(&tb.grad[OFF_B5 + 2 * t], db5[0]);
+			if(2 * t + 1 < NRC_O && db5[1] != 0.0f) atomicAdd(&tb.grad[OFF_B5 + 2 * t + 1], db5[1]);
+		}
+	}
+}
+
+/* Backward pass, a warp per 16 samples: dH_{l-1} = dZ_l W_l, dZ_{l-1} =
+ * dH_{l-1} where h_{l-1} > 0; stores dz[4..1] (BF16) and adds the bias
+ * gradients (from the FP32 values) to the packed gradient. */
+__global__ void __launch_bounds__(128) k_nrc_backward(NrcDev net, int n, TrainBufs tb)
+{
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	__nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
+	float *sdb = reinterpret_cast<float *>(sw + BWD_SMEM_BF16);   /* 4 x 64 bias sums of the block */
+	copy_to_shared(sw, net.w2t, BWD_SMEM_BF16);
+	for(int i = threadIdx.x; i < 256; i += blockDim.x) sdb[i] = 0.0f;
+	__syncthreads();
+	const __nv_bfloat16 *W2T = sw, *W3T = sw + (IMG_W3T - IMG_W2T), *W4T = sw + (IMG_W4T - IMG_W2T), *W5T = sw + (IMG_W5T - IMG_W2T);
+	int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	int g = lane >> 2, t = lane & 3;
+	int ntiles = (n + 15) >> 4;
+	for(int tile = blockIdx.x * 4 + warp; tile < ntiles; tile += gridDim.x * 4) {
+		int r0 = tile * 16 + g, r1 = r0 + 8;
+		/* dz5 as an A tile (k = outputs, 16 wide) */
+		uint32_t a5[4];
+		const __nv_bfloat16 *d5 = tb.dz[5];
+		a5[0] = *reinterpret_cast<const uint32_t *>(d5 + (size_t)r0 * 16 + 2 * t);
+		a5[1] = *reinterpret_cast<const uint32_t *>(d5 + (size_t)r1 * 16 + 2 * t);
+		a5[2] = *reinterpret_cast<const uint32_t *>(d5 + (size_t)r0 * 16 + 8 + 2 * t);
+		a5[3] = *reinterpret_cast<const uint32_t *>(d5 + (size_t)r1 * 16 + 8 + 2 * t);
+		Acc64 dz;
+		#pragma unroll
+		for(int nt = 0; nt < 8; nt++) {
+			dz.d[nt][0] = dz.d[nt][1] = dz.d[nt][2] = dz.d[nt][3] = 0.0f;
+			uint32_t w0, w1;
+			load_b(W5T, LD5T, nt * 8, 0, lane, w0, w1);
+			mma16816(dz.d[nt], a5, w0, w1);
+		}
+		const __nv_bfloat16 *WT[3] = {W4T, W3T, W2T};
+		for(int l = 4; l >= 1; l--) {
+			/* mask by h_l > 0, bias sums, BF16 store of dz_l */
+			const __nv_bfloat16 *h = tb.h[l];
+			__nv_bfloat16 *dzo = tb.dz[l];
+			#pragma unroll
+			for(int nt = 0; nt < 8; nt++) {
+				int col = nt * 8 + 2 * t;
+				uint32_t hv0 = *reinterpret_cast<const uint32_t *>(h + (size_t)r0 * 64 + col);
+				uint32_t hv1 = *reinterpret_cast<const uint32_t *>(h + (size_t)r1 * 64 + col);
+				if(!(bf16_lo(hv0) > 0.0f)) dz.d[nt][0] = 0.0f;
+				if(!(bf16_hi(hv0) > 0.0f)) dz.d[nt][1] = 0.0f;
+				if(!(bf16_lo(hv1) > 0.0f)) dz.d[nt][2] = 0.0f;
+				if(!(bf16_hi(hv1) > 0.0f)) dz.d[nt][3] = 0.0f;
+				*reinterpret_cast<uint32_t *>(dzo + (size_t)r0 * 64 + col) = pack_bf16(dz.d[nt][0], dz.d[nt][1]);
+				*reinterpret_cast<uint32_t *>(dzo + (size_t)r1 * 64 + col) = pack_bf16(dz.d[nt][2], dz.d[nt][3]);
+				float s0 = dz.d[nt][0] + dz.d[nt][2], s1 = dz.d[nt][1] + dz.d[nt][3];
+				for(int o = 4; o < 32; o <<= 1) {
+					s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+					s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+				}
+				if(g == 0) {
+					atomicAdd(&sdb[(l - 1) * 64 + col], s0);
+					atomicAdd(&sdb[(l - 1) * 64 + col + 1], s1);
+				}
+			}
+			if(l == 1) break;
+			uint32_t a[4][4];
+			acc_to_a(dz, a, false);
+			const __nv_bfloat16 *W = WT[4 - l];
+			#pragma unroll
+			for(int nt = 0; nt < 8; nt++) {
+				dz.d[nt][0] = dz.d[nt][1] = dz.d[nt][2] = dz.d[nt][3] = 0.0f;
+				#pragma unroll
+				for(int kt = 0; kt < 4; kt++) {
+					uint32_t w0, w1;
+					load_b(W, LDH, nt * 8, kt * 16, lane, w0, w1);
+					mma16816(dz.d[nt], a[kt], w0, w1);
+				}
+			}
+		}
+	}
+	__syncthreads();
+	const int boff[4] = {OFF_B1, OFF_B2, OFF_B3, OFF_B4};
+	for(int i = threadIdx.x; i < 256; i += blockDim.x) {
+		float v = sdb[i];
+		if(v != 0.0f) atomicAdd(&tb.grad[boff[i >> 6] + (i & 63)], v);
+	}
+}
+
+/* Weight gradient of one layer over the batch: dW[o][i] = sum_s dz[s][o] h[s][i],
+ * M outputs (rows of dz, 16-wide storage stride DZS), N inputs (h stride HS).
+ * Samples are split over blocks; each block stages 32 samples at a time,
+ * transposed, in shared memory and its 8 warps hold TPW 16x8 output tiles
+ * each; the block's sums are added to the packed gradient at OFF (only
+ * o < MO, i < NI are real). */
+template <int MT, int NT, int TPW, int DZS, int HS>
+__global__ void __launch_bounds__(256) k_nrc_wgrad(int n, const __nv_bfloat16 *dz, const __nv_bfloat16 *h, float *grad, int off,
+		int MO, int NI, int per_block)
+{
+	enum { M = MT * 16, N = NT * 8, LDS = 40 };
+	__shared__ __align__(16) __nv_bfloat16 sdz[M * LDS];
+	__shared__ __align__(16) __nv_bfloat16 sh[N * LDS];
+	int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	int g = lane >> 2, t = lane & 3;
+	float acc[TPW][4];
+	#pragma unroll
+	for(int k = 0; k < TPW; k++) acc[k][0] = acc[k][1] = acc[k][2] = acc[k][3] = 0.0f;
+	int s_begin = blockIdx.x * per_block, s_end = min(n, s_begin + per_block);
+	for(int s0 = s_begin; s0 < s_end; s0 += 32) {
+		__syncthreads();
+		/* stage dz^T [M][32] and h^T [N][32] */
+		for(int i = threadIdx.x; i < 32 * M; i += blockDim.x) {
+			int s = i / M, o = i - s * M;
+			__nv_bfloat16 v = __float2bfloat16_rn(0.0f);
+			if(s0 + s < s_end && o < DZS) v = dz[(size_t)(s0 + s) * DZS + o];
+			sdz[o * LDS + s] = v;
+		}
+		for(int i = threadIdx.x; i < 32 * N; i += blockDim.x) {
+			int s = i / N, c = i - s * N;
+			__nv_bfloat16 v = __float2bfloat16_rn(0.0f);
+			if(s0 + s < s_end && c < HS) v = h[(size_t)(s0 + s) * HS + c];
+			sh[c * LDS + s] = v;
+		}
+		__syncthreads();
+		#pragma unroll
+		for(int k = 0; k < TPW; k++) {
+			int tile = warp * TPW + k;
+			if(tile >= MT * NT) break;
+			int mt = tile / NT, nt = tile - mt * NT;
+			#pragma unroll
+			for(int ks = 0; ks < 2; ks++) {
+				uint32_t a[4];
+				const __nv_bfloat16 *pa = sdz + (mt * 16 + g) * LDS + ks * 16 + 2 * t;
+				a[0] = *reinterpret_cast<const uint32_t *>(pa);
+				a[1] = *reinterpret_cast<const uint32_t *>(pa + 8 * LDS);
+				a[2] = *reinterpret_cast<const uint32_t *>(pa + 8);
+				a[3] = *reinterpret_cast<const uint32_t *>(pa + 8 * LDS + 8);
+				uint32_t b0, b1;
+				load_b(sh, LDS, nt * 8, ks * 16, lane, b0, b1);
+				mma16816(acc[k], a, b0, b1);
+			}
+		}
+	}
+	#pragma unroll
+	for(int k = 0; k < TPW; k++) {
+		int tile = warp * TPW + k;
+		if(tile >= MT * NT) break;
+		int mt = tile / NT, nt = tile - mt * NT;
+		int rows[2] = {mt * 16 + g, mt * 16 + g + 8};
+		#pragma unroll
+		for(int half = 0; half < 2; half++) {
+			int o = rows[half];
+			#pragma unroll
+			for(int c = 0; c < 2; c++) {
+				int i = nt * 8 + 2 * t + c;
+				float v = acc[k][2 * half + c];
+				if(o < MO && i < NI && v != 0.0f) atomicAdd(&grad[off + o * NI + i], v);
+			}
+		}
+	}
+}
+
+/* Adam on the FP32 master; the BF16 images are rewritten from it */
+__global__ void k_nrc_adam(float *p, float *m, float *v, float *grad, int step, float lr)
+{
+	const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+	float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < NRC_NPARAM; i += gridDim.x * blockDim.x) {
+		float gi = grad[i];
+		grad[i] = 0.0f;
+		float mi = b1 * m[i] + (1.0f - b1) * gi;
+		float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+		m[i] = mi;
+		v[i] = vi;
+		float pi = p[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+		p[i] = pi;
+	}
+}
+
+/* the BF16 images and FP32 biases of the current master weights */
+__global__ void k_nrc_images(const float *p, __nv_bfloat16 *img, float *bias)
+{
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < IMG_END; i += gridDim.x * blockDim.x) {
+		float v = 0.0f;
+		if(i < IMG_W2) {
+			int o = i / LD1, c = i - o * LD1;
+			if(c < NRC_F) v = p[OFF_W1 + o * NRC_F + c];
+		} else if(i < IMG_W5) {
+			int l = (i - IMG_W2) / (64 * LDH), r = i - IMG_W2 - l * 64 * LDH;
+			int o = r / LDH, c = r - o * LDH;
+			const int offs[3] = {OFF_W2, OFF_W3, OFF_W4};
+			if(c < 64) v = p[offs[l] + o * 64 + c];
+		} else if(i < IMG_W2T) {
+			int r = i - IMG_W5, o = r / LDH, c = r - o * LDH;
+			if(o < NRC_O && c < 64) v = p[OFF_W5 + o * 64 + c];
+		} else if(i < IMG_W5T) {
+			int l = (i - IMG_W2T) / (64 * LDH), r = i - IMG_W2T - l * 64 * LDH;
+			int in = r / LDH, o = r - in * LDH;
+			const int offs[3] = {OFF_W2, OFF_W3, OFF_W4};
+			if(o < 64) v = p[offs[l] + o * 64 + in];
+		} else {
+			int r = i - IMG_W5T, in = r / LD5T, o = r - in * LD5T;
+			if(o < NRC_O) v = p[OFF_W5 + o * 64 + in];
+		}
+		img[i] = __float2bfloat16_rn(v);
+	}
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < NRC_NBIAS; i += gridDim.x * blockDim.x) {
+		float v = 0.0f;
+		if(i < 256) {
+			const int offs[4] = {OFF_B1, OFF_B2, OFF_B3, OFF_B4};
+			v = p[offs[i >> 6] + (i & 63)];
+		} else if(i - 256 < NRC_O) {
+			v = p[OFF_B5 + i - 256];
+		}
+		bias[i] = v;
+	}
+}
+
+/* ---------------- host side ---------------- */
+
+struct NrcState {
+	int device = -1;
+	float *p = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr, *loss = nullptr, *bias = nullptr;
+	__nv_bfloat16 *img = nullptr;
+	__nv_bfloat16 *hbuf = nullptr;   /* training activations */
+	int hcap = 0;                    /* samples the training buffers hold */
+	int step = 0;
+	bool ready = false;
+	std::string err;
+};
+
+static NrcState g_nrc;
+static std::mutex g_nrc_mu;
+
+static int nrc_fail(cudaError_t e, const char *where)
+{
+	g_nrc.err = std::string(where) + ": " + cudaGetErrorString(e);
+	return SRAY_ECUDA;
+}
+
+#define NCK(call, where) do { cudaError_t e_ = (call); if(e_ != cudaSuccess) return nrc_fail(e_, where); } while(0)
+
+static NrcDev nrc_dev()
+{
+	NrcDev d;
+	const __nv_bfloat16 *b = g_nrc.img;
+	d.w1 = b + IMG_W1; d.w2 = b + IMG_W2; d.w3 = b + IMG_W3; d.w4 = b + IMG_W4; d.w5 = b + IMG_W5;
+	d.w2t = b + IMG_W2T; d.w3t = b + IMG_W3T; d.w4t = b + IMG_W4T; d.w5t = b + IMG_W5T;
+	d.bias = g_nrc.bias;
+	return d;
+}
+
+static int nrc_alloc()
+{
+	int dev = 0;
+	NCK(cudaGetDevice(&dev), "device");
+	if(g_nrc.ready && g_nrc.device == dev) return 0;
+	NCK(cudaMalloc(&g_nrc.p, NRC_NPARAM * sizeof(float)), "radiance cache weights");
+	NCK(cudaMalloc(&g_nrc.m, NRC_NPARAM * sizeof(float)), "radiance cache moments");
+	NCK(cudaMalloc(&g_nrc.v, NRC_NPARAM * sizeof(float)), "radiance cache moments");
+	NCK(cudaMalloc(&g_nrc.grad, NRC_NPARAM * sizeof(float)), "radiance cache gradient");
+	NCK(cudaMalloc(&g_nrc.loss, sizeof(float)), "radiance cache loss");
+	NCK(cudaMalloc(&g_nrc.bias, NRC_NBIAS * sizeof(float)), "radiance cache biases");
+	NCK(cudaMalloc(&g_nrc.img, IMG_END * sizeof(__nv_bfloat16)), "radiance cache images");
+	NCK(cudaFuncSetAttribute(k_nrc_forward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4), "smem");
+	NCK(cudaFuncSetAttribute(k_nrc_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4), "smem");
+	NCK(cudaFuncSetAttribute(k_nrc_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, BWD_SMEM_BF16 * 2 + 256 * 4), "smem");
+	g_nrc.device = dev;
+	g_nrc.ready = true;
+	return 0;
+}
+
+static int nrc_set(const float *host_p, cudaStream_t s)
+{
+	NCK(cudaMemcpyAsync(g_nrc.p, host_p, NRC_NPARAM * sizeof(float), cudaMemcpyHostToDevice, s), "upload weights");
+	NCK(cudaMemsetAsync(g_nrc.m, 0, NRC_NPARAM * sizeof(float), s), "reset moments");
+	NCK(cudaMemsetAsync(g_nrc.v, 0, NRC_NPARAM * sizeof(float), s), "reset moments");
+	NCK(cudaMemsetAsync(g_nrc.grad, 0, NRC_NPARAM * sizeof(float), s), "reset gradient");
+	k_nrc_images<<<64, 256, 0, s>>>(g_nrc.p, g_nrc.img, g_nrc.bias);
+	NCK(cudaGetLastError(), "radiance cache images");
+	g_nrc.step = 0;
+	return 0;
+}
+
+/* He-uniform weights from a Philox stream, zero biases */
+static void nrc_init_host(uint64_t seed, std::vector<float> &p)
+{
+	p.assign(NRC_NPARAM, 0.0f);
+	struct L { int off, out, in; } ls[5] = {{OFF_W1, 64, NRC_F}, {OFF_W2, 64, 64}, {OFF_W3, 64, 64}, {OFF_W4, 64, 64}, {OFF_W5, 3, 64}};
+	sray_rng r;
+	sray_rng_init(&r, seed, SRAY_DOM_USER, 0x4e5243u, 0);
+	for(const L &l : ls) {
+		float lim = sqrtf(6.0f / (float)l.in);
+		for(int i = 0; i < l.out * l.in; i++) p[l.off + i] = (2.0f * sray_rng_uniform_f(&r) - 1.0f) * lim;
+	}
+}
+
+static int nrc_train_bufs(int n, TrainBufs &tb, cudaStream_t s)
+{
+	int n16 = (n + 15) & ~15;
+	if(n16 > g_nrc.hcap) {
+		if(g_nrc.hbuf) cudaFree(g_nrc.hbuf);
+		g_nrc.hbuf = nullptr;
+		g_nrc.hcap = 0;
+		size_t per = NRC_FP + 4 * 64 + 4 * 64 + 16;
+		NCK(cudaMalloc(&g_nrc.hbuf, (size_t)n16 * per * sizeof(__nv_bfloat16)), "radiance cache training buffers");
+		g_nrc.hcap = n16;
+	}
+	__nv_bfloat16 *b = g_nrc.hbuf;
+	size_t cap = (size_t)g_nrc.hcap;
+	tb.h[0] = b; b += cap * NRC_FP;
+	for(int l = 1; l <= 4; l++) { tb.h[l] = b; b += cap * 64; }
+	tb.dz[0] = nullptr;
+	for(int l = 1; l <= 4; l++) { tb.dz[l] = b; b += cap * 64; }
+	tb.dz[5] = b;
+	tb.grad = g_nrc.grad;
+	tb.loss = g_nrc.loss;
+	(void)s;
+	return 0;
+}
+
+static int nrc_grid(int n)
+{
+	int tiles = (n + 15) / 16;
+	int blocks = (tiles + 3) / 4;
+	if(blocks > 152 * 8) blocks = 152 * 8;
+	return blocks < 1 ? 1 : blocks;
+}
+
+/* gradient of the loss over a batch into g_nrc.grad (which must hold zeros) */
+static int nrc_gradient(int n, const float *x, const float *t, float *y, cudaStream_t s)
+{
+	TrainBufs tb;
+	int r = nrc_train_bufs(n, tb, s);
+	if(r) return r;
+	NCK(cudaMemsetAsync(g_nrc.loss, 0, sizeof(float), s), "reset loss");
+	NrcDev d = nrc_dev();
+	k_nrc_forward<true><<<nrc_grid(n), 128, FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4, s>>>(d, n, x, y, t, tb);
+	k_nrc_backward<<<nrc_grid(n), 128, BWD_SMEM_BF16 * 2 + 256 * 4, s>>>(d, n, tb);
+	int per = 512;
+	int blocks = (n + per - 1) / per;
+	/* layer 1: 64 x 224 (216 real), layers 2-4: 64 x 64, layer 5: 16 x 64 (3 real) */
+	k_nrc_wgrad<4, 28, 14, 64, NRC_FP><<<blocks, 256, 0, s>>>(n, tb.dz[1], tb.h[0], g_nrc.grad, OFF_W1, 64, NRC_F, per);
+	k_nrc_wgrad<4, 8, 4, 64, 64><<<blocks, 256, 0, s>>>(n, tb.dz[2], tb.h[1], g_nrc.grad, OFF_W2, 64, 64, per);
+	k_nrc_wgrad<4, 8, 4, 64, 64><<<blocks, 256, 0, s>>>(n, tb.dz[3], tb.h[2], g_nrc.grad, OFF_W3, 64, 64, per);
+	k_nrc_wgrad<4, 8, 4, 64, 64><<<blocks, 256, 0, s>>>(n, tb.dz[4], tb.h[3], g_nrc.grad, OFF_W4, 64, 64, per);
+	k_nrc_wgrad<1, 8, 1, 16, 64><<<blocks, 256, 0, s>>>(n, tb.dz[5], tb.h[4], g_nrc.grad, OFF_W5, NRC_O, 64, per);
+	NCK(cudaGetLastError(), "radiance cache gradient");
+	return 0;
+}
+
+int nrc_ensure_ready(uint64_t seed, cudaStream_t s)
+{
+	bool fresh = !g_nrc.ready;
+	int r = nrc_alloc();
+	if(r) return r;
+	if(fresh) {
+		std::vector<float> p;
+		nrc_init_host(seed, p);
+		if((r = nrc_set(p.data(), s))) return r;
+		NCK(cudaStreamSynchronize(s), "radiance cache init");
+	}
+	return 0;
+}
+
+int nrc_infer(int n, const float *x, float *y, cudaStream_t s)
+{
+	if(n <= 0) return 0;
+	k_nrc_forward<false><<<nrc_grid(n), 128, FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4, s>>>(nrc_dev(), n, x, y, nullptr, TrainBufs());
+	NCK(cudaGetLastError(), "radiance cache inference");
+	return 0;
+}
+
+int nrc_train(int n, const float *x, const float *t, float lr, cudaStream_t s)
+{
+	if(n <= 0) return 0;
+	int r = nrc_gradient(n, x, t, nullptr, s);
+	if(r) return r;
+	g_nrc.step++;
+	k_nrc_adam<<<64, 256, 0, s>>>(g_nrc.p, g_nrc.m, g_nrc.v, g_nrc.grad, g_nrc.step, lr);
+	k_nrc_images<<<64, 256, 0, s>>>(g_nrc.p, g_nrc.img, g_nrc.bias);
+	NCK(cudaGetLastError(), "radiance cache training");
+	return 0;
+}
+
+const char *nrc_error() { return g_nrc.err.c_str(); }
+
+float *nrc_loss_ptr() { return g_nrc.loss; }
+
+}  // namespace sray
+
+using namespace sray;
+
+extern "C" {
+
+static thread_local std::string t_nrc_err;
+
+static int nrc_err_ret(int r)
+{
+	if(r) t_nrc_err = g_nrc.err;
+	return r;
+}
+
+int sray_nrc_reset(uint64_t seed)
+{
+	std::lock_guard<std::mutex> lk(g_nrc_mu);
+	int r = nrc_alloc();
+	if(r) return nrc_err_ret(r);
+	std::vector<float> p;
+	nrc_init_host(seed, p);
+	r = nrc_set(p.data(), 0);
+	if(!r) { cudaError_t e = cudaStreamSynchronize(0); if(e != cudaSuccess) r = nrc_fail(e, "reset"); }
+	return nrc_err_ret(r);
+}
+
+int sray_nrc_set_params(const float *p, int n)
+{
+	std::lock_guard<std::mutex> lk(g_nrc_mu);
+	if(!p || n != NRC_NPARAM) { g_nrc.err = "expected SRAY_NRC_PARAMS parameters"; return nrc_err_ret(SRAY_EINVAL); }
+	int r = nrc_alloc();
+	if(!r) r = nrc_set(p, 0);
+	if(!r) { cudaError_t e = cudaStreamSynchronize(0); if(e != cudaSuccess) r = nrc_fail(e, "set parameters"); }
+	return nrc_err_ret(r);
+}
+
+int sray_nrc_get_params(float *p, int n)
+{
+	std::lock_guard<std::mutex> lk(g_nrc_mu);
+	if(!p || n != NRC_NPARAM) { g_nrc.err = "expected SRAY_NRC_PARAMS parameters"; return nrc_err_ret(SRAY_EINVAL); }
+	if(!g_nrc.ready) { g_nrc.err = "radiance cache not initialised"; return nrc_err_ret(SRAY_ESTATE); }
+	cudaError_t e = cudaMemcpy(p, g_nrc.p, NRC_NPARAM * sizeof(float), cudaMemcpyDeviceToHost);
+	return nrc_err_ret(e == cudaSuccess ? 0 : nrc_fail(e, "get parameters"));
+}
+
+int sray_nrc_infer(int n, const float *x, float *y, void *stream)
+{
+	std::lock_guard<std::mutex> lk(g_nrc_mu);
+	if(n < 0 || (n > 0 && (!x || !y))) { g_nrc.err = "bad arguments"; return nrc_err_ret(SRAY_EINVAL); }
+	if(!g_nrc.ready) { g_nrc.err = "radiance cache not initialised"; return nrc_err_ret(SRAY_ESTATE); }
+	cudaStream_t s = (cudaStream_t)stream;
+	int r = nrc_infer(n, x, y, s);
+	if(!r) { cudaError_t e = cudaStreamSynchronize(s); if(e != cudaSuccess) r = nrc_fail(e, "inference"); }
+	return nrc_err_ret(r);
+}
+
+int sray_nrc_gradients(int n, const float *x, const float *t, float *grad, float *loss, void *stream)
+{
+	std::lock_guard<std::mutex> lk(g_nrc_mu);
+	if(n <= 0 || !x || !t || !grad || !loss) { g_nrc.err = "bad arguments"; return nrc_err_ret(SRAY_EINVAL); }
+	if(!g_nrc.ready) { g_nrc.err = "radiance cache not initialised"; return nrc_err_ret(SRAY_ESTATE); }
+	cudaStream_t s = (cudaStream_t)stream;
+	int r = 0;
+	cudaError_t e = cudaMemsetAsync(g_nrc.grad, 0, NRC_NPARAM * sizeof(float), s);
+	if(e != cudaSuccess) r = nrc_fail(e, "reset gradient");
+	if(!r) r = nrc_gradient(n, x, t, nullptr, s);
+	if(!r) { e = cudaMemcpyAsync(grad, g_nrc.grad, NRC_NPARAM * sizeof(float), cudaMemcpyDeviceToDevice, s); if(e != cudaSuccess) r = nrc_fail(e, "copy gradient"); }
+	if(!r) { e = cudaMemcpyAsync(loss, g_nrc.loss, sizeof(float), cudaMemcpyDeviceToDevice, s); if(e != cudaSuccess) r = nrc_fail(e, "copy loss"); }
+	if(!r) { e = cudaMemsetAsync(g_nrc.grad, 0, NRC_NPARAM * sizeof(float), s); if(e != cudaSuccess) r = nrc_fail(e, "reset gradient"); }
+	if(!r) { e = cudaStreamSynchronize(s); if(e != cudaSuccess) r = nrc_fail(e, "gradients"); }
+	return nrc_err_ret(r);
+}
+
+int sray_nrc_train(int n, const float *x, const float *t, float *loss, void *stream)
+{
+	std::lock_guard<std::mutex> lk(g_nrc_mu);
+	if(n <= 0 || !x || !t) { g_nrc.err = "bad arguments"; return nrc_err_ret(SRAY_EINVAL); }
+	if(!g_nrc.ready) { g_nrc.err = "radiance cache not initialised"; return nrc_err_ret(SRAY_ESTATE); }
+	cudaStream_t s = (cudaStream_t)stream;
+	int r = nrc_train(n, x, t, 1e-3f, s);
+	if(!r && loss) { cudaError_t e = cudaMemcpyAsync(loss, g_nrc.loss, sizeof(float), cudaMemcpyDeviceToDevice, s); if(e != cudaSuccess) r = nrc_fail(e, "copy loss"); }
+	if(!r) { cudaError_t e = cudaStreamSynchronize(s); if(e != cudaSuccess) r = nrc_fail(e, "training"); }
+	return nrc_err_ret(r);
+}
+
+int sray_nrc_last_error(char *buf, size_t len)
+{
+	if(!buf || len == 0) return SRAY_EINVAL;
+	size_t n = t_nrc_err.size() < len - 1 ? t_nrc_err.size() : len - 1;
+	memcpy(buf, t_nrc_err.data(), n);
+	buf[n] = 0;
+	return 0;
+}
+
+}  /* extern "C" */

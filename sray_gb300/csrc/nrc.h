@@ -1,0 +1,22 @@
+/* nrc.h -- the radiance cache as the renderer drives it (nrc.cu). */
+#ifndef SRAY_NRC_H_
+#define SRAY_NRC_H_
+
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace sray {
+
+/* allocate and, the first time, initialise the network from `seed` */
+int nrc_ensure_ready(uint64_t seed, cudaStream_t s);
+/* y[n][3] = network(x[n][9]); x = position scaled to the scene box, normal, direction */
+int nrc_infer(int n, const float *x, float *y, cudaStream_t s);
+/* one Adam step on the batch (x[n][9], targets t[n][3]) */
+int nrc_train(int n, const float *x, const float *t, float lr, cudaStream_t s);
+/* device address of the last batch's loss */
+float *nrc_loss_ptr();
+const char *nrc_error();
+
+}  // namespace sray
+
+#endif

@@ -19,7 +19,10 @@ EXPORTS = ["sray_default_opts", "sray_gpu_init", "sray_gpu_set_opts", "sray_gpu_
            "sray_gpu_render_pixels", "sray_gpu_cast_rays", "sray_gpu_primary_hits", "sray_gpu_photon_gather", "sray_gpu_photon_gather_noalloc",
            "sray_gpu_get_photons",
            "sray_gpu_get_stats", "sray_gpu_set_profiling", "sray_gpu_kernel_times", "sray_gpu_last_error",
-           "sray_gpu_shutdown"]
+           "sray_gpu_shutdown", "sray_nrc_reset", "sray_nrc_set_params", "sray_nrc_get_params", "sray_nrc_infer",
+           "sray_nrc_gradients", "sray_nrc_train", "sray_nrc_last_error"]
+
+NRC_PARAMS = 26563
 
 
 class SrayStats(ctypes.Structure):
@@ -74,8 +77,48 @@ def load_library():
     L.sray_gpu_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     L.sray_gpu_shutdown.argtypes = []
     L.sray_gpu_shutdown.restype = None
+    L.sray_nrc_reset.argtypes = [ctypes.c_uint64]
+    L.sray_nrc_set_params.argtypes = [vp, ip]
+    L.sray_nrc_get_params.argtypes = [vp, ip]
+    L.sray_nrc_infer.argtypes = [ip, vp, vp, vp]
+    L.sray_nrc_gradients.argtypes = [ip, vp, vp, vp, vp, vp]
+    L.sray_nrc_train.argtypes = [ip, vp, vp, vp, vp]
+    L.sray_nrc_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     _lib = L
     return L
+
+
+class RadianceCache:
+    """The radiance-cache MLP through its C-ABI (inputs and outputs are CUDA
+    tensors: x [n, 9] float32, targets [n, 3])."""
+
+    def __init__(self, seed=1):
+        self.L = load_library()
+        self._chk(self.L.sray_nrc_reset(seed))
+
+    def _chk(self, r):
+        if r != 0:
+            buf = ctypes.create_string_buffer(512)
+            self.L.sray_nrc_last_error(buf, 512)
+            raise SrayError("radiance cache error %d: %s" % (r, buf.value.decode(errors="replace")))
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self._chk(self.L.sray_nrc_set_params(_ptr(p), p.size))
+
+    def params(self):
+        p = np.zeros(NRC_PARAMS, np.float32)
+        self._chk(self.L.sray_nrc_get_params(_ptr(p), p.size))
+        return p
+
+    def infer(self, x, y, stream=None):
+        self._chk(self.L.sray_nrc_infer(x.shape[0], _ptr(x), _ptr(y), _stream(stream)))
+
+    def gradients(self, x, t, grad, loss, stream=None):
+        self._chk(self.L.sray_nrc_gradients(x.shape[0], _ptr(x), _ptr(t), _ptr(grad), _ptr(loss), _stream(stream)))
+
+    def train(self, x, t, loss=None, stream=None):
+        self._chk(self.L.sray_nrc_train(x.shape[0], _ptr(x), _ptr(t), _ptr(loss), _stream(stream)))
 
 
 def _ptr(x):

@@ -1,0 +1,103 @@
+"""The radiance-cache kernels against the CPU restatement (oracle/nrc.py).
+
+Forward: the tensor-core inference equals the oracle's bfloat16-rounded
+forward pass (the kernels accumulate in FP32 in another order, so the bar is
+a relative tolerance).  Gradients: the packed gradient of the loss from the
+training kernels equals the oracle's backward pass with the same bfloat16
+roundings.  Training: Adam steps on the GPU drive the loss down on a smooth
+target and track the oracle's own training trajectory.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import nrc
+
+pytestmark = pytest.mark.gpu
+
+
+def inputs(rng, n):
+    pos = rng.uniform(0.0, 1.0, (n, 3))
+    nrm = rng.normal(size=(n, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return np.concatenate([pos, nrm, d], axis=1).astype(np.float32)
+
+
+@pytest.fixture(scope="module")
+def cache(gpu_lib):
+    return gpu_lib.RadianceCache(seed=1)
+
+
+def test_forward_matches_oracle(cache):
+    rng = np.random.default_rng(11)
+    p = nrc.init_params(21)
+    p[-3:] = (0.2, 0.5, 0.8)
+    cache.set_params(p)
+    for n in (1, 37, 4096):
+        x = inputs(rng, n)
+        y = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+        cache.infer(torch.tensor(x, device="cuda"), y)
+        ref, _ = nrc.forward(p, x)
+        got = y.cpu().numpy()
+        scale = np.sqrt(np.mean(ref ** 2)) + 1e-3
+        err = np.max(np.abs(got - ref)) / scale
+        assert err < 2e-2, (n, err)
+        assert np.sqrt(np.mean((got - ref) ** 2)) / scale < 2e-3
+
+
+def test_gradients_match_oracle(cache):
+    rng = np.random.default_rng(12)
+    p = nrc.init_params(22)
+    p[-3:] = (0.3, 0.3, 0.3)
+    cache.set_params(p)
+    n = 2048
+    x = inputs(rng, n)
+    t = rng.uniform(0.0, 1.0, (n, 3)).astype(np.float32)
+    grad = torch.zeros(nrc.N_PARAMS, dtype=torch.float32, device="cuda")
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    cache.gradients(torch.tensor(x, device="cuda"), torch.tensor(t, device="cuda"), grad, loss)
+    y, c = nrc.forward(p, x)
+    ref_loss, dy = nrc.loss_and_dy(y, t)
+    ref = nrc.backward(c, dy)
+    got = grad.cpu().numpy().astype(np.float64)
+    assert abs(loss.item() - ref_loss) <= 1e-2 * ref_loss
+    off = 0
+    for i, s in enumerate(nrc.SHAPES):
+        k = int(np.prod(s))
+        g, r = got[off:off + k], ref[off:off + k]
+        rel = np.linalg.norm(g - r) / (np.linalg.norm(r) + 1e-12)
+        assert rel < 3e-2, ("parameter block", i, rel)
+        off += k
+
+
+def test_training_tracks_oracle_and_learns(cache):
+    rng = np.random.default_rng(13)
+    p = nrc.init_params(23)
+    cache.set_params(p)
+    n = 8192
+    x = inputs(rng, n)
+    smooth = 0.4 + 0.3 * np.sin(np.pi * x[:, 0]) * np.cos(np.pi * x[:, 2]) + 0.1 * x[:, 4]
+    t = (smooth[:, None] * np.array([1.0, 0.8, 0.6])).astype(np.float32)
+    xd, td = torch.tensor(x, device="cuda"), torch.tensor(t, device="cuda")
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    q = p.astype(np.float64)
+    m = np.zeros_like(q); v = np.zeros_like(q)
+    losses = []
+    for step in range(1, 1201):
+        cache.train(xd, td, loss)
+        losses.append(loss.item())
+        if step <= 20:
+            y, c = nrc.forward(q, x)
+            l, dy = nrc.loss_and_dy(y, t)
+            q, m, v = nrc.adam_step(q, nrc.backward(c, dy), m, v, step)
+            assert abs(losses[-1] - l) <= 0.05 * l + 1e-4, (step, losses[-1], l)
+    assert losses[-1] < 0.05 * losses[0], (losses[0], losses[-1])
+    # the trained network against the best constant predictor of the targets
+    y = torch.empty((n, 3), dtype=torch.float32, device="cuda")
+    cache.infer(xd, y)
+    err_net = np.mean((y.cpu().numpy() - t) ** 2)
+    err_mean = np.mean((t.mean(axis=0) - t) ** 2)
+    print("trained mse %.5f, constant predictor mse %.5f, loss %.4f -> %.4f" % (err_net, err_mean, losses[0], losses[-1]))
+    assert err_net < 0.25 * err_mean, (err_net, err_mean)
