@@ -43,7 +43,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="production", choices=["production", "small"])
+    ap.add_argument("--config", default="production", choices=["production", "small", "learned"])
+    ap.add_argument("--no-nrc", action="store_true", help="skip the radiance-cache comparison")
+    ap.add_argument("--nrc-burn-in", type=int, default=600, help="frames of online training before the cache is timed")
+    ap.add_argument("--nrc-ladder", default="1,2,4,8,16,32,64,128",
+                    help="diffuse samples per vertex of the plain final gather, compared with the cache")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-rows", type=int, default=24, help="rows of the CPU baseline sample")
     ap.add_argument("--res", default=None, help="WxH override (profiling runs on a reduced case)")
@@ -64,6 +68,11 @@ def config_opts(args):
 
 
 def workload_desc(cfg):
+    if cfg == "learned":
+        return ("learned gather: the small scene at 1920x1080, 1 spp, depth 5, 100k caustic photons (k=50), "
+                "500k global photons (k=100 nearest within r<=0.5), final gather of indirect light by the radiance "
+                "cache (12-band encoding, 4x64 ReLU, BF16 weights, FP32 accumulation, Adam 1e-3, 65,536 training "
+                "vertices per frame, per-region fallback to the plain gather with 16 rays per vertex above 0.05 validation error) vs the plain photon gather")
     if cfg == "production":
         return ("production: 1920x1080, adaptive 1-16 spp (variance 0.05), depth 8, 1M-triangle displaced-grid "
                 "terrain + 200 instanced icospheres (256k tris), 3 sphere lights, 2M global + 500k caustic photons, "
@@ -177,6 +186,149 @@ def cpu_baseline(cfg, path, opts, rows, photon_frac, threads=0):
                   % (y0, y0 + rows, h, photon_frac, t_prep, t_rows),
         "wall_s": t_prep + t_rows,
     }
+
+
+REF_DS = 256
+REF_BANDS = 16
+
+
+def reference_bands(h, n=REF_BANDS, rows=8):
+    """Row bands (y0, y1) spread evenly over an image of h rows."""
+    step = max(h // n, rows)
+    return [(y, min(y + rows, h)) for y in range(step // 2 - rows // 2, h - rows + 1, step)][:n]
+
+
+def oracle_reference_rows(opts, path, ds=REF_DS, bands=None, threads=0):
+    """The FP64 CPU oracle's image on row bands with `ds` final-gather rays
+    per vertex: the converged reference of the final-gather estimators
+    (same scene, photon maps, lights and camera).  Returns (image, rows, s)."""
+    import numpy as np
+    from oracle.oracle import Oracle
+    o = dict(opts)
+    o["diffuse_samples"] = ds
+    o["threads"] = threads
+    h, w = opts["height"], opts["width"]
+    bands = bands or reference_bands(h)
+    t0 = time.perf_counter()
+    orc = Oracle(fp64=True, rng_mode=1, **o)
+    orc.load(path)
+    orc.prepare(0)
+    ref = np.zeros((h, w, 4), np.float64)
+    for b in bands:
+        img = np.asarray(orc.render(0, rows=b, nthreads=threads))
+        ref[b[0]:b[1]] = img[b[0]:b[1]]
+    rows = np.concatenate([np.arange(a, b) for a, b in bands])
+    return ref, rows, time.perf_counter() - t0
+
+
+def image_rmse(img, ref, rows):
+    import numpy as np
+    d = np.asarray(img, np.float64)[rows, :, :3] - ref[rows, :, :3]
+    return float(np.sqrt(np.mean(d * d)))
+
+
+def equal_rmse_time(ladder, target):
+    """Frame time of the plain method at the cache's RMSE: ladder = [(ds, ms,
+    rmse)] with rmse falling as ds grows; interpolated linearly in log rmse
+    against log ds, the time linearly in ds.  Returns (ms, ds, bracketed):
+    bracketed False means the target lies outside the ladder, and the
+    nearest end is returned (a bound, not an estimate)."""
+    import math
+    pts = sorted(ladder)
+    if not pts:
+        return None, None, False
+    if target >= pts[0][2]:
+        return pts[0][1], pts[0][0], target == pts[0][2]
+    for (d0, m0, r0), (d1, m1, r1) in zip(pts, pts[1:]):
+        if r0 >= target >= r1 and r0 > r1:
+            f = (math.log(r0) - math.log(target)) / (math.log(r0) - math.log(r1))
+            ds = math.exp(math.log(d0) + f * (math.log(d1) - math.log(d0)))
+            ms = m0 + (ds - d0) / (d1 - d0) * (m1 - m0)
+            return ms, ds, True
+    return pts[-1][1], pts[-1][0], False
+
+
+def nrc_vs_plain(args, reference):
+    """Radiance cache vs the plain final gather on the learned-gather scene:
+    the plain method's RMSE and frame time for each number of final-gather
+    rays per vertex, the cache's after `--nrc-burn-in` frames of online
+    training (timed frames keep training), and the plain frame time at the
+    cache's RMSE.  reference = (image, rows) of the FP64 oracle, or None."""
+    import numpy as np
+    import torch
+    from sray_gb300 import gpu, scenegen
+
+    opts = scenegen.scene_opts("learned")
+    path = scenegen.write_scene("learned")
+    H, W = opts["height"], opts["width"]
+    g = gpu.GpuRenderer(**opts)
+    g.load(path)
+    fb = torch.zeros((H, W, 4), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    steps = max(args.steps, 3)
+
+    def timed(n):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        rays = 0
+        for _ in range(n):
+            g.render(0, fb, stream=stream)
+            rays += rays_of(g.stats())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / n
+        return ms, rays / n / (ms / 1e3) / 1e6
+
+    def err():
+        if reference is None:
+            return None
+        return image_rmse(fb.cpu().numpy(), reference[0], reference[1])
+
+    ladder = []
+    for ds in [int(x) for x in args.nrc_ladder.split(",") if x]:
+        g.set_opts(nrc=0, diffuse_samples=ds)
+        for _ in range(2):
+            g.render(0, fb, stream=stream)
+        ms, mr = timed(steps)
+        ladder.append({"diffuse_samples": ds, "ms_per_frame": ms, "mrays_per_s": mr, "rmse": err()})
+    out = {"workload": workload_desc("learned"), "plain": ladder,
+           "reference": None if reference is None else
+           "FP64 CPU oracle, %d final-gather rays per vertex, %d rows in %d bands" % (REF_DS, len(reference[1]), REF_BANDS)}
+    g.set_opts(nrc=1, diffuse_samples=1)
+    g.nrc_reset()
+    t0 = time.perf_counter()
+    for _ in range(args.nrc_burn_in):
+        g.render(0, fb, stream=stream)
+    torch.cuda.synchronize()
+    burn_s = time.perf_counter() - t0
+    for mode, name in ((1, "cache"), (2, "cache_no_fallback")):
+        g.set_opts(nrc=mode)
+        for _ in range(3):
+            g.render(0, fb, stream=stream)
+        g.set_profiling(time_kernels=True)
+        g.kernel_times(reset=True)
+        ms, mr = timed(steps)
+        kt = g.kernel_times(reset=True)
+        g.set_profiling(False)
+        st = g.nrc_stats()
+        res = {"mode": mode, "ms_per_frame": ms, "mrays_per_s": mr, "rmse": err(),
+               "cached_vertex_frac": st["cached"] / max(st["vertices"], 1), "frames_trained": st["frames"],
+               "train_samples_per_frame": st["train_samples"], "val_samples_per_frame": st["val_samples"],
+               "regions_validated": st["regions_validated"], "regions_cached": st["regions_cached"],
+               "val_rel_err": st["val_rel_err"], "loss": st["loss"],
+               "nrc_ms_per_frame": {k: round(v[0] / steps, 3) for k, v in kt.items() if k.startswith("nrc")},
+               "gather_ms_per_frame": round(kt.get("gather", (0.0, 0))[0] / steps, 3)}
+        if res["rmse"] is not None:
+            pts = [(p["diffuse_samples"], p["ms_per_frame"], p["rmse"]) for p in ladder]
+            pms, pds, ok = equal_rmse_time(pts, res["rmse"])
+            res["plain_at_equal_rmse"] = {"ms_per_frame": pms, "diffuse_samples": pds, "bracketed": ok,
+                                          "time_ratio": ms / pms if pms else None}
+        out[name] = res
+    out["burn_in"] = {"frames": args.nrc_burn_in, "s": burn_s}
+    g.close()
+    return out
 
 
 def run_reference(args):
@@ -343,6 +495,34 @@ def run_ours(args):
             cpu = {"value": None, "unit": "Mrays/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": "failed: %s" % exc}
 
+    # photons and gathers per second: of the frame, and of their own kernels
+    ph_ms = sum(v[0] for k, v in kt.items() if k.startswith("photon")) / args.steps
+    ga_ms = kt.get("gather", (0.0, 0))[0] / args.steps
+    throughput = {"photons_per_frame": st_last["photons_emitted"], "gathers_per_frame": st_last["gathers"],
+                  "photons_per_s": st_last["photons_emitted"] / (ms_step / 1e3),
+                  "gathers_per_s": st_last["gathers"] / (ms_step / 1e3),
+                  "photon_kernels_ms": ph_ms, "gather_kernels_ms": ga_ms,
+                  "photons_per_s_of_photon_kernels": st_last["photons_emitted"] / (ph_ms / 1e3) if ph_ms else None,
+                  "gathers_per_s_of_gather_kernels": st_last["gathers"] / (ga_ms / 1e3) if ga_ms else None,
+                  "note": "photon kernels run on their own stream beside the first bounce; per-frame rates use the "
+                          "frame time, kernel rates the CUDA-event time of the photon / gather launches"}
+
+    nrc = None
+    if rank == 0 and not args.no_nrc and ws == 1 and args.res is None:
+        g.close()
+        ref = None
+        if not args.no_cpu_baseline:
+            from sray_gb300 import scenegen as sg
+            lopts = sg.scene_opts("learned")
+            img, rows, ref_s = oracle_reference_rows(lopts, sg.write_scene("learned"))
+            ref = (img, rows)
+        try:
+            nrc = nrc_vs_plain(args, ref)
+            if ref is not None:
+                nrc["reference_s"] = ref_s
+        except Exception as exc:  # reported, the headline stands on its own
+            nrc = {"error": str(exc)}
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
@@ -361,6 +541,7 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "gpu_launches": launches,
             "clocks": clk,
+            "nrc_vs_plain": nrc,
             "kernels_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in kt.items()},
             "frame": {"rays": rays_of(st_last), "primary": st_last["primary_rays"],
                       "secondary": st_last["secondary_rays"], "shadow": st_last["shadow_rays"],
@@ -371,9 +552,11 @@ def run_ours(args):
                       "gather_select_frac": st_last["gather_selects"] / max(st_last["gathers"], 1),
                       "gather_spill_frac": st_last["gather_spills"] / max(st_last["gathers"], 1),
                       "bvh_fallbacks": st_last["bvh_fallbacks"]},
+            "throughput": throughput,
         }
         print(json.dumps(line))
-    g.close()
+    if nrc is None:
+        g.close()
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()

@@ -65,7 +65,17 @@ typedef struct sray_opts {
 	float gather_rcap;             /* radius cap of the k-nearest gathers (scene units) */
 	int rng_paths;                 /* 1: shading draws keyed by the ray's path in the shading tree */
 	uint64_t seed;                 /* Philox key of every random stream */
-	int reserved[8];
+	/* radiance cache (no reference counterpart): the final gather's indirect
+	 * light from the network instead of diffuse rays + photon gathers */
+	int nrc;                       /* 0 plain final gather; 1 cache with per-region
+	                                  fallback to the plain gather; 2 cache everywhere */
+	int nrc_train_samples;         /* training vertices per frame (65536) */
+	float nrc_max_rel_err;         /* validation relative error above which a region
+	                                  falls back to the plain gather (0.05) */
+	int nrc_train_steps;           /* Adam steps per frame over the training vertices (4) */
+	int nrc_fallback_samples;      /* final-gather rays per vertex in a fallback region
+	                                  (0: diffuse_samples) */
+	int reserved[3];
 } sray_opts;
 
 /* Fill `o` with the reference defaults (src/opt.c:357-388). */
@@ -185,6 +195,28 @@ typedef struct sray_stats {
 } sray_stats;
 
 int sray_gpu_get_stats(sray_stats *st);
+
+/* Radiance-cache state of the renderer (opts.nrc != 0). */
+typedef struct sray_nrc_stats {
+	int64_t frames;                /* frames that trained the cache */
+	int64_t vertices;              /* final-gather vertices of the last frame */
+	int64_t cached;                /* of those, shaded from the network */
+	int64_t train_samples;         /* training vertices of the last frame */
+	int64_t val_samples;           /* validation vertices of the last frame */
+	int regions;                   /* spatial regions (grid cells over the scene box) */
+	int regions_validated;         /* regions with enough validation vertices */
+	int regions_cached;            /* regions the network serves (error <= threshold) */
+	float val_rel_err;             /* |sum prediction - sum target| / sum target over
+	                                  the validated regions (running sums) */
+	float loss;                    /* training loss of the last step */
+	int pad;
+	int64_t reserved[4];
+} sray_nrc_stats;
+
+int sray_gpu_nrc_stats(sray_nrc_stats *st);
+/* forget the validation history (every region back to the plain gather) and
+ * re-initialise the network from `seed` */
+int sray_gpu_nrc_reset(uint64_t seed);
 
 /* ---- Radiance cache (extension, no reference counterpart) ----
  * A small MLP standing in for the final gather of indirect light

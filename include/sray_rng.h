@@ -40,7 +40,8 @@ enum {
 	SRAY_DOM_CAUST = 2,       /* one caustic photon */
 	SRAY_DOM_GLOBAL = 3,      /* one global-illumination photon */
 	SRAY_DOM_PROJMAP = 4,     /* light sample positions used to build projection maps */
-	SRAY_DOM_USER = 5
+	SRAY_DOM_USER = 5,
+	SRAY_DOM_NRC = 6          /* final-gather directions of a radiance-cache record (keyed per frame) */
 };
 
 typedef struct sray_rng {

@@ -1082,6 +1082,7 @@ template <class R> struct Ray {
 template <class R> struct SurfPoint {
 	R dist;
 	V3<R> pos, normal, tangent;
+	V3<R> gn;         /* geometric normal (world space, unit): where float light samples start */
 	R tex[2];
 };
 
@@ -1099,6 +1100,7 @@ struct Counters {
 };
 
 template <class R> static inline R maxr(R a, R b) { return a > b ? a : b; }
+#define SHADOW_OFFSET 3.814697265625e-06   /* 2^-18 */
 template <class R> static inline R powr(R a, R b);
 template <> inline float powr(float a, float b) { return powf(a, b); }
 template <> inline double powr(double a, double b) { return pow(a, b); }
@@ -1360,6 +1362,7 @@ template <class R> struct Frame : FrameBase {
 			sp->tex[1] = tc[1];
 			sp->normal = dot(n, n) < xsmall ? normal : n;
 			sp->tangent = tg;
+			sp->gn = normal;
 		}
 		return true;
 	}
@@ -1492,14 +1495,32 @@ template <class R> struct Frame : FrameBase {
 		*tie = false;
 		if(o.type == OBJ_SPHERE) {
 			c.prims++;
+			R t1, t2;
+			if(sizeof(R) == 4) {
+				/* float: the roots in a form without cancellation (the
+				 * discriminant from the ray's closest approach to the centre,
+				 * the near root as c / q), as the GPU computes them */
+				R a = dot(ray.d, ray.d);
+				R bh = dot(ray.o, ray.d);
+				V pp = ray.o - ray.d * (bh / a);
+				R dh = o.rad * o.rad - dot(pp, pp);
+				if(dh < (R)0) return false;
+				R sq = std::sqrt(dh * a);
+				R cc = dot(ray.o, ray.o) - o.rad * o.rad;
+				R q = -(bh + (bh < (R)0 ? -sq : sq));
+				R ta = q / a, tb = q != (R)0 ? cc / q : ta;
+				t1 = ta > tb ? ta : tb;
+				t2 = ta > tb ? tb : ta;
+			} else {
 			R a = dot(ray.d, ray.d);
 			R b = (R)2 * ray.d.x * ray.o.x + (R)2 * ray.d.y * ray.o.y + (R)2 * ray.d.z * ray.o.z;
 			R cc = dot(ray.o, ray.o) - o.rad * o.rad;
 			R d = b * b - (R)4 * a * cc;
 			if(d < (R)0) return false;
 			R sq = rsqrt_<R>(d);
-			R t1 = (-b + sq) / ((R)2 * a);
-			R t2 = (-b - sq) / ((R)2 * a);
+			t1 = (-b + sq) / ((R)2 * a);
+			t2 = (-b - sq) / ((R)2 * a);
+			}
 			if((t1 < eps && t2 < eps) || (t1 > (R)1 && t2 > (R)1)) return false;
 			if(t1 < eps) t1 = t2;
 			if(t2 < eps) t2 = t1;
@@ -1510,19 +1531,34 @@ template <class R> struct Frame : FrameBase {
 			sph_tex(sp->pos, sp->tex, false);
 			sp->pos = mul_pt(m, sp->pos);
 			sp->normal = mul_n(it, sp->normal);
+			sp->gn = normalized(sp->normal);
 			sp->tangent = mul_n(it, sp->tangent);
 			return true;
 		}
 		if(o.type == OBJ_CYLINDER) {
 			c.prims++;
+			R t1, t2;
 			R a = ray.d.x * ray.d.x + ray.d.z * ray.d.z;
+			if(sizeof(R) == 4 && a > (R)0) {
+				R bh = ray.d.x * ray.o.x + ray.d.z * ray.o.z;
+				R px = ray.o.x - ray.d.x * (bh / a), pz = ray.o.z - ray.d.z * (bh / a);
+				R dh = o.rad * o.rad - (px * px + pz * pz);
+				if(dh < (R)0) return false;
+				R sq = std::sqrt(dh * a);
+				R cc = ray.o.x * ray.o.x + ray.o.z * ray.o.z - o.rad * o.rad;
+				R q = -(bh + (bh < (R)0 ? -sq : sq));
+				R ta = q / a, tb = q != (R)0 ? cc / q : ta;
+				t1 = ta > tb ? ta : tb;
+				t2 = ta > tb ? tb : ta;
+			} else {
 			R b = (R)2 * ray.d.x * ray.o.x + (R)2 * ray.d.z * ray.o.z;
 			R cc = ray.o.x * ray.o.x + ray.o.z * ray.o.z - o.rad * o.rad;
 			R d = b * b - (R)4 * a * cc;
 			if(d < (R)0) return false;
 			R sq = rsqrt_<R>(d);
-			R t1 = (-b + sq) / ((R)2 * a);
-			R t2 = (-b - sq) / ((R)2 * a);
+			t1 = (-b + sq) / ((R)2 * a);
+			t2 = (-b - sq) / ((R)2 * a);
+			}
 			if((t1 < eps && t2 < eps) || (t1 > (R)1 && t2 > (R)1)) return false;
 			V p1 = ray.o + ray.d * t1;
 			V p2 = ray.o + ray.d * t2;
@@ -1537,6 +1573,7 @@ template <class R> struct Frame : FrameBase {
 			sph_tex(sp->pos, sp->tex, true);
 			sp->pos = mul_pt(m, sp->pos);
 			sp->normal = mul_n(it, sp->normal);
+			sp->gn = normalized(sp->normal);
 			sp->tangent = mul_n(it, sp->tangent);
 			return true;
 		}
@@ -1555,6 +1592,7 @@ template <class R> struct Frame : FrameBase {
 		sp->pos = mul_pt(m, sp->pos);
 		sp->normal = normalized(mul_n(it, sp->normal));
 		sp->tangent = normalized(mul_n(it, sp->tangent));
+		sp->gn = normalized(mul_n(it, sp->gn));
 		return true;
 	}
 
@@ -1746,8 +1784,27 @@ template <class R> struct Frame : FrameBase {
 		return r + ((R)1 - r) * inv_sq * inv_sq * inv;
 	}
 
+	/* The origin of a light sample's shadow ray.  The reference starts it at
+	 * the surface point and ignores hits closer than ERROR_MARGIN (in units
+	 * of the segment); in double the surface's own hit is ~1e-15 away, in
+	 * float the point is off the surface by a few ulps and a segment leaving
+	 * at a shallow angle can hit its own surface beyond the margin.  In
+	 * float the ray therefore starts 2^-18 (|p|max + 1) off the surface
+	 * along the geometric normal, on the side it leaves to (the GPU does
+	 * the same); double keeps the reference's origin. */
+	V shadow_origin(const V &pt, const V &gn, const V &dir) const
+	{
+		if(sizeof(R) != 4) return pt;
+		R side = dot(dir, gn);
+		if(side == (R)0) return pt;
+		R off = (maxr(maxr(fabsr(pt.x), fabsr(pt.y)), fabsr(pt.z)) + (R)1) * (R)SHADOW_OFFSET;
+		if(side < (R)0) off = -off;
+		return pt + gn * off;
+	}
+
 	/* calc_lighting (src/shader.cc:250-283) */
-	void calc_lighting(C *diff, C *spec, int li, R shininess, const V &pt, const V &norm, const V &vdir, int tm, Ctx &ctx) const
+	void calc_lighting(C *diff, C *spec, int li, R shininess, const V &pt, const V &norm, const V &gn, const V &vdir, int tm,
+			Ctx &ctx) const
 	{
 		const LightR &lt = lights[li];
 		int ns = lt.type != LT_POINT ? opt.shadow_samples : 1;
@@ -1757,7 +1814,7 @@ template <class R> struct Frame : FrameBase {
 			V ldir = lpos - pt;
 			R ldist = length(ldir);
 			Ray<R> shadow;
-			shadow.o = pt;
+			shadow.o = shadow_origin(pt, gn, ldir);
 			shadow.d = ldir;
 			shadow.time = tm;
 			ldir = ldir / ldist;
@@ -1790,7 +1847,7 @@ template <class R> struct Frame : FrameBase {
 			V ldir = lpos - sp.pos;
 			R ldist = length(ldir);
 			Ray<R> shadow;
-			shadow.o = sp.pos;
+			shadow.o = shadow_origin(sp.pos, sp.gn, ldir);
 			shadow.d = ldir;
 			shadow.time = ray.time;
 			ldir = ldir / ldist;
@@ -1841,7 +1898,7 @@ template <class R> struct Frame : FrameBase {
 		C spec(0, 0, 0, (R)1);
 		for(size_t i = 0; i < lights.size(); i++) {
 			C d, s;
-			calc_lighting(&d, &s, (int)i, shininess, sp.pos, normal, incident, ray.time, ctx);
+			calc_lighting(&d, &s, (int)i, shininess, sp.pos, normal, sp.gn, incident, ray.time, ctx);
 			diff = diff + d;
 			spec = spec + s;
 		}

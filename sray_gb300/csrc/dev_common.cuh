@@ -35,6 +35,36 @@ struct DPhotonMap {
 	float screen;             /* float squared distances above this are out of range */
 };
 
+/* The radiance cache as the shading kernels see it.  At a final-gather
+ * vertex (a Phong hit with the global map on) the network's inputs are the
+ * position scaled to the scene box, the normal and the incident direction,
+ * each mapped to [0, 1]; the region of a vertex is its cell of an
+ * NRC_GRID^3 grid over the box.  A vertex in a region the network serves
+ * becomes a query (inputs, weight, accumulator slot) instead of diffuse
+ * rays; a vertex the frame's hash selects also becomes a training or
+ * validation record whose target (the plain final gather's estimate,
+ * without the vertex's weight and kd) accumulates in slot t0 + record. */
+#define NRC_GRID 8
+#define NRC_VAL_RAYS 8                /* final-gather rays (at least) of a validation record */
+#define NRC_REGIONS (NRC_GRID * NRC_GRID * NRC_GRID)
+struct DNrc {
+	int mode;                         /* 0 off, 1 cache with per-region fallback, 2 cache everywhere */
+	float lo[3], sc[3];               /* box corner and 1 / box size */
+	const unsigned char *fallback;    /* per region: 1 = plain final gather */
+	float *qx;                        /* query inputs, 9 floats each */
+	float4 *qw;                       /* query weight rgb, accumulator slot */
+	int *qcount;
+	int qcap;
+	float *tx;                        /* training records [0, tcap), validation records [tcap, tcap + vcap) */
+	int *tcount;                      /* [0] training records, [1] validation records */
+	int tcap, vcap;
+	int t0;                           /* accumulator slot of record 0 */
+	uint32_t p_train, p_val;          /* a vertex whose hash is below p_train trains, below p_train + p_val validates */
+	uint32_t key;                     /* per-frame key of the selection hash */
+	int fb_samples;                   /* final-gather rays in a fallback region (0: diffuse_samples) */
+	unsigned long long *counters;     /* [0] final-gather vertices, [1] cached */
+};
+
 struct DScene {
 	const DevNode *snodes;    /* top-level octree (world space) */
 	const int *sslots;
@@ -77,6 +107,7 @@ struct DScene {
 	float photon_energy;
 	float max_cos;
 	DPhotonMap caust, gi;
+	DNrc nrc;
 };
 
 /* ---------------- float3 helpers (no contraction: built with -fmad=false) */
@@ -194,16 +225,33 @@ __device__ __forceinline__ bool tri_hit(const float4 a, const float4 b, const fl
 }
 
 /* Sphere::intersect (src/sphere.cc:85-131), object space */
+/* The reference solves a t^2 + b t + c = 0 with the textbook formula.  In
+ * float, with the reference's ray lengths (primary rays 10^4 long) b^2 and
+ * 4ac cancel and the hit point drifts off the surface by ~1e-4, so that
+ * light samples from it hit the surface again.  These solvers compute the
+ * same roots without the cancellation: the discriminant from the ray's
+ * closest approach to the axis / centre, r^2 - |o - (o.d / d.d) d|^2, and
+ * the near root as c / q (q = -(o.d) -+ sqrt(...)).  The root selection that
+ * follows is the reference's. */
+__device__ __forceinline__ void stable_roots(float a, float bh, float dh, float c, float &t1, float &t2)
+{
+	float sq = sqrtf(dh * a);
+	float q = -(bh + (bh < 0.0f ? -sq : sq));
+	float ta = q / a, tb = q != 0.0f ? c / q : ta;
+	t1 = ta > tb ? ta : tb;
+	t2 = ta > tb ? tb : ta;
+}
+
 __device__ __forceinline__ bool sphere_hit(const RayT &r, float rad, float eps, float &dist)
 {
 	float a = dot(r.d, r.d);
-	float b = 2.0f * r.d.x * r.o.x + 2.0f * r.d.y * r.o.y + 2.0f * r.d.z * r.o.z;
+	float bh = dot(r.o, r.d);
+	V3 pp = r.o - r.d * (bh / a);
+	float dh = rad * rad - dot(pp, pp);
+	if(dh < 0.0f) return false;
 	float c = dot(r.o, r.o) - rad * rad;
-	float d = b * b - 4.0f * a * c;
-	if(d < 0.0f) return false;
-	float sq = sqrtf(d);
-	float t1 = (-b + sq) / (2.0f * a);
-	float t2 = (-b - sq) / (2.0f * a);
+	float t1, t2;
+	stable_roots(a, bh, dh, c, t1, t2);
 	if((t1 < eps && t2 < eps) || (t1 > 1.0f && t2 > 1.0f)) return false;
 	if(t1 < eps) t1 = t2;
 	if(t2 < eps) t2 = t1;
@@ -215,13 +263,24 @@ __device__ __forceinline__ bool sphere_hit(const RayT &r, float rad, float eps, 
 __device__ __forceinline__ bool cylinder_hit(const RayT &r, float rad, float start, float end, float eps, float &dist)
 {
 	float a = r.d.x * r.d.x + r.d.z * r.d.z;
-	float b = 2.0f * r.d.x * r.o.x + 2.0f * r.d.z * r.o.z;
-	float c = r.o.x * r.o.x + r.o.z * r.o.z - rad * rad;
-	float d = b * b - 4.0f * a * c;
-	if(d < 0.0f) return false;
-	float sq = sqrtf(d);
-	float t1 = (-b + sq) / (2.0f * a);
-	float t2 = (-b - sq) / (2.0f * a);
+	float t1, t2;
+	if(a > 0.0f) {
+		float bh = r.d.x * r.o.x + r.d.z * r.o.z;
+		float px = r.o.x - r.d.x * (bh / a), pz = r.o.z - r.d.z * (bh / a);
+		float dh = rad * rad - (px * px + pz * pz);
+		if(dh < 0.0f) return false;
+		float c = r.o.x * r.o.x + r.o.z * r.o.z - rad * rad;
+		stable_roots(a, bh, dh, c, t1, t2);
+	} else {
+		/* a ray parallel to the axis: the reference's formula */
+		float b = 2.0f * r.d.x * r.o.x + 2.0f * r.d.z * r.o.z;
+		float c = r.o.x * r.o.x + r.o.z * r.o.z - rad * rad;
+		float d = b * b - 4.0f * a * c;
+		if(d < 0.0f) return false;
+		float sq = sqrtf(d);
+		t1 = (-b + sq) / (2.0f * a);
+		t2 = (-b - sq) / (2.0f * a);
+	}
 	if((t1 < eps && t2 < eps) || (t1 > 1.0f && t2 > 1.0f)) return false;
 	V3 p1 = r.o + r.d * t1;
 	V3 p2 = r.o + r.d * t2;
@@ -922,8 +981,29 @@ __device__ inline bool trace_any(const DScene &S, V3 wo, V3 wd, int time, int *o
 /* ---------------- surface point ---------------- */
 struct Surf {
 	V3 pos, normal;
+	V3 gn;            /* geometric normal, unit, world space */
 	float tex[2];
 };
+
+/* The origin of a light sample's shadow ray.  The reference starts it at the
+ * surface point and ignores hits closer than ERROR_MARGIN (in units of the
+ * segment); in double the surface's own hit is ~1e-15 away, in float the
+ * point is off the surface by a few ulps and a segment leaving at a shallow
+ * angle can hit its own surface beyond the margin (dark speckles near the
+ * shadow terminator).  The ray therefore starts 2^-18 (|p|max + 1) off the
+ * surface along the geometric normal, on the side it leaves to. */
+#define SHADOW_OFFSET 3.814697265625e-06f   /* 2^-18 */
+__device__ __forceinline__ V3 shadow_origin(const Surf &sp, V3 dir)
+{
+	float side = dot(dir, sp.gn);
+	if(side == 0.0f) return sp.pos;
+	float ax = fabsf(sp.pos.x), ay = fabsf(sp.pos.y), az = fabsf(sp.pos.z);
+	float m = ax > ay ? ax : ay;
+	m = m > az ? m : az;
+	float off = (m + 1.0f) * SHADOW_OFFSET;
+	if(side < 0.0f) off = -off;
+	return sp.pos + sp.gn * off;
+}
 
 /* interp_face (src/mesh.cc:321-445): bilinear-patch inversion after Haines */
 __device__ inline void interp_face(const float *P, const float *A, V3 ispos, V3 normal, float xsmall, V3 *onorm, float *otex, bool want_tex)
@@ -1013,11 +1093,13 @@ __device__ inline void surface_point(const DScene &S, const Hit &h, V3 wo, V3 wd
 		if(want_tex) sph_tex(pos, sp.tex, false);
 		sp.pos = mul_pt(m, pos);
 		sp.normal = mul_n(it, nrm);
+		sp.gn = normalized(sp.normal);
 	} else if(ob.type == 1) {
 		nrm = mk(1.0f * pos.x, 0.0f * pos.y, 1.0f * pos.z) / ob.rad;
 		if(want_tex) sph_tex(pos, sp.tex, true);
 		sp.pos = mul_pt(m, pos);
 		sp.normal = mul_n(it, nrm);
+		sp.gn = normalized(sp.normal);
 	} else {
 		const float *P = S.tri_pos + (size_t)(ob.tri_base + h.prim) * 9;
 		const float *A = S.tri_attr + (size_t)(ob.tri_base + h.prim) * 24;
@@ -1028,6 +1110,7 @@ __device__ inline void surface_point(const DScene &S, const Hit &h, V3 wo, V3 wd
 		nrm = dot(in, in) < S.xsmall ? fn : in;
 		sp.pos = mul_pt(m, pos);
 		sp.normal = normalized(mul_n(it, nrm));
+		sp.gn = normalized(mul_n(it, fn));
 	}
 }
 

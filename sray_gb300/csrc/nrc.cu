@@ -12,8 +12,10 @@
  * all five layers with the activations in registers, the accumulator tile of
  * one layer becoming the operand tile of the next.
  *
- *   k_nrc_forward<false>  inference: encode + 5 layers, fused
- *   k_nrc_forward<true>   training forward: also stores the layer inputs
+ *   k_nrc_forward<FWD_INFER>  inference: encode + 5 layers, fused
+ *   k_nrc_forward<FWD_QUERY>  the renderer's queries: the same, the output
+ *                         weighted into the pixel's accumulator
+ *   k_nrc_forward<FWD_TRAIN>  training forward: also stores the layer inputs
  *                         (BF16) and the loss gradient of the outputs
  *   k_nrc_backward        dZ of layers 4..1 through the transposed weights,
  *                         bias gradients
@@ -195,9 +197,26 @@ struct TrainBufs {
 	float *loss;
 };
 
-template <bool TRAIN>
-__global__ void __launch_bounds__(128) k_nrc_forward(NrcDev net, int n, const float *x, float *y, const float *tgt, TrainBufs tb)
+/* queries of the renderer: inputs x [n][9]; w[i] = weight rgb and the
+ * accumulator slot; acc[slot] += w * max(y, 0); the count is read on the
+ * device (n is the capacity) */
+struct QueryOut {
+	const int *count;
+	const float4 *w;
+	float4 *acc;
+};
+
+enum { FWD_INFER = 0, FWD_TRAIN = 1, FWD_QUERY = 2 };
+
+template <int MODE>
+__global__ void __launch_bounds__(128) k_nrc_forward(NrcDev net, int n, const float *x, float *y, const float *tgt, TrainBufs tb,
+		QueryOut qo)
 {
+	constexpr bool TRAIN = MODE == FWD_TRAIN;
+	if(MODE == FWD_QUERY) {
+		int c = *qo.count;
+		n = c < n ? c : n;
+	}
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	__nv_bfloat16 *sw = reinterpret_cast<__nv_bfloat16 *>(smem_raw);
 	float *sb = reinterpret_cast<float *>(sw + FWD_SMEM_BF16);
@@ -285,7 +304,13 @@ __global__ void __launch_bounds__(128) k_nrc_forward(NrcDev net, int n, const fl
 			for(int c = 0; c < 2; c++) {
 				int col = 2 * t + c;
 				float yv = o[2 * half + c];
-				if(!TRAIN) {
+				if(MODE == FWD_QUERY) {
+					if(r < n && col < NRC_O) {
+						float4 wv = qo.w[r];
+						float wc = col == 0 ? wv.x : (col == 1 ? wv.y : wv.z);
+						atomicAdd(reinterpret_cast<float *>(qo.acc + __float_as_int(wv.w)) + col, wc * fmaxf(yv, 0.0f));
+					}
+				} else if(!TRAIN) {
 					if(r < n && col < NRC_O) y[(size_t)r * 3 + col] = yv;
 				} else {
 					float dy = 0.0f;
@@ -583,9 +608,11 @@ static int nrc_alloc()
 	NCK(cudaMalloc(&g_nrc.loss, sizeof(float)), "radiance cache loss");
 	NCK(cudaMalloc(&g_nrc.bias, NRC_NBIAS * sizeof(float)), "radiance cache biases");
 	NCK(cudaMalloc(&g_nrc.img, IMG_END * sizeof(__nv_bfloat16)), "radiance cache images");
-	NCK(cudaFuncSetAttribute(k_nrc_forward<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	NCK(cudaFuncSetAttribute(k_nrc_forward<FWD_INFER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 			FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4), "smem");
-	NCK(cudaFuncSetAttribute(k_nrc_forward<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+	NCK(cudaFuncSetAttribute(k_nrc_forward<FWD_TRAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+			FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4), "smem");
+	NCK(cudaFuncSetAttribute(k_nrc_forward<FWD_QUERY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 			FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4), "smem");
 	NCK(cudaFuncSetAttribute(k_nrc_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, BWD_SMEM_BF16 * 2 + 256 * 4), "smem");
 	g_nrc.device = dev;
@@ -658,7 +685,7 @@ static int nrc_gradient(int n, const float *x, const float *t, float *y, cudaStr
 	if(r) return r;
 	NCK(cudaMemsetAsync(g_nrc.loss, 0, sizeof(float), s), "reset loss");
 	NrcDev d = nrc_dev();
-	k_nrc_forward<true><<<nrc_grid(n), 128, FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4, s>>>(d, n, x, y, t, tb);
+	k_nrc_forward<FWD_TRAIN><<<nrc_grid(n), 128, FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4, s>>>(d, n, x, y, t, tb, QueryOut());
 	k_nrc_backward<<<nrc_grid(n), 128, BWD_SMEM_BF16 * 2 + 256 * 4, s>>>(d, n, tb);
 	int per = 512;
 	int blocks = (n + per - 1) / per;
@@ -689,8 +716,22 @@ int nrc_ensure_ready(uint64_t seed, cudaStream_t s)
 int nrc_infer(int n, const float *x, float *y, cudaStream_t s)
 {
 	if(n <= 0) return 0;
-	k_nrc_forward<false><<<nrc_grid(n), 128, FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4, s>>>(nrc_dev(), n, x, y, nullptr, TrainBufs());
+	k_nrc_forward<FWD_INFER><<<nrc_grid(n), 128, FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4, s>>>(nrc_dev(), n, x, y, nullptr, TrainBufs(),
+			QueryOut());
 	NCK(cudaGetLastError(), "radiance cache inference");
+	return 0;
+}
+
+int nrc_query(const int *count, int cap, const float *x, const float4 *w, float4 *acc, cudaStream_t s)
+{
+	if(cap <= 0) return 0;
+	QueryOut qo;
+	qo.count = count;
+	qo.w = w;
+	qo.acc = acc;
+	k_nrc_forward<FWD_QUERY><<<nrc_grid(cap), 128, FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4, s>>>(nrc_dev(), cap, x, nullptr, nullptr,
+			TrainBufs(), qo);
+	NCK(cudaGetLastError(), "radiance cache queries");
 	return 0;
 }
 

@@ -11,7 +11,11 @@ namespace sray {
 int nrc_ensure_ready(uint64_t seed, cudaStream_t s);
 /* y[n][3] = network(x[n][9]); x = position scaled to the scene box, normal, direction */
 int nrc_infer(int n, const float *x, float *y, cudaStream_t s);
-/* one Adam step on the batch (x[n][9], targets t[n][3]) */
+/* the renderer's queries: acc[slot] += w.rgb * max(network(x[i]), 0) for
+ * i < *count (at most cap), slot = the int in w[i].w */
+int nrc_query(const int *count, int cap, const float *x, const float4 *w, float4 *acc, cudaStream_t s);
+/* one Adam step on the batch (x[n][9], targets t[n][3]): NRC_TRAIN_KERNELS launches */
+#define NRC_TRAIN_KERNELS 9
 int nrc_train(int n, const float *x, const float *t, float lr, cudaStream_t s);
 /* device address of the last batch's loss */
 float *nrc_loss_ptr();

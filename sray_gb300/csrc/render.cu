@@ -17,12 +17,14 @@
 #include <float.h>
 #include <limits.h>
 #include <string.h>
+#include <stddef.h>
 #include <stdio.h>
 #include <algorithm>
 #include <mutex>
 #include <cooperative_groups.h>
 #include <cooperative_groups/scan.h>
 #include "renderer.h"
+#include "nrc.h"
 #include "range_ff.h"
 
 namespace cg = cooperative_groups;
@@ -123,7 +125,7 @@ __device__ __forceinline__ void acc_add(float4 *acc, int p, float r, float g, fl
 
 __device__ __forceinline__ float maxf_ref(float a, float b) { return a > b ? a : b; }
 
-#define MAX_DS 8
+#define MAX_DS 128
 
 struct ShadeOut {
 	RayQueue qo;
@@ -233,6 +235,61 @@ __device__ __forceinline__ RayRec make_child(const RayRec &p, V3 o, V3 d, float 
 	return c;
 }
 
+/* ---- radiance cache at a final-gather vertex ---- */
+
+/* 32-bit integer hash: the "lowbias32" finaliser of C. Wellons' hash
+ * prospector (xorshift-multiply, two rounds) */
+__device__ __forceinline__ uint32_t hash32(uint32_t x)
+{
+	x ^= x >> 16;
+	x *= 0x7feb352du;
+	x ^= x >> 15;
+	x *= 0x846ca68bu;
+	x ^= x >> 16;
+	return x;
+}
+
+/* network inputs of a vertex: position in the scene box, normal and
+ * incident direction, all mapped to [0, 1] */
+__device__ __forceinline__ void nrc_inputs(const DNrc &N, V3 pos, V3 n, V3 d, float *x)
+{
+	x[0] = (pos.x - N.lo[0]) * N.sc[0];
+	x[1] = (pos.y - N.lo[1]) * N.sc[1];
+	x[2] = (pos.z - N.lo[2]) * N.sc[2];
+	x[3] = 0.5f * (n.x + 1.0f);
+	x[4] = 0.5f * (n.y + 1.0f);
+	x[5] = 0.5f * (n.z + 1.0f);
+	x[6] = 0.5f * (d.x + 1.0f);
+	x[7] = 0.5f * (d.y + 1.0f);
+	x[8] = 0.5f * (d.z + 1.0f);
+}
+
+__device__ __forceinline__ int nrc_region(const float *x)
+{
+	int c[3];
+	#pragma unroll
+	for(int a = 0; a < 3; a++) {
+		float v = x[a] * (float)NRC_GRID;
+		int k = v > 0.0f ? (int)v : 0;
+		c[a] = k < NRC_GRID ? k : NRC_GRID - 1;
+	}
+	return (c[2] * NRC_GRID + c[1]) * NRC_GRID + c[0];
+}
+
+/* warp-aggregated count of the threads for which pred holds */
+__device__ __forceinline__ void warp_count(unsigned long long *p, bool pred)
+{
+	cg::coalesced_group g = cg::coalesced_threads();
+	unsigned int n = __popc(g.ballot(pred));
+	if(g.thread_rank() == 0 && n) atomicAdd(p, (unsigned long long)n);
+}
+
+__device__ __forceinline__ void store_x(float *dst, const float *x)
+{
+	#pragma unroll
+	for(int k = 0; k < 9; k++) dst[k] = x[k];
+}
+
 /* shade one hit: env colour for misses, shade_phong / shade_undef
  * (src/shader.cc:36-283) for hits.  Light samples, children (reflection,
  * refraction, final-gather rays) and photon gathers go to the emitter `em`:
@@ -278,7 +335,7 @@ __device__ __forceinline__ void shade_one(const DScene &S, const RayRec &ray, co
 			float ndotl = maxf_ref(dot(sp.normal, ldir), 0.0f);
 			float ndoth = maxf_ref(dot(sp.normal, hdir), 0.0f);
 			float pw = powf(ndoth, 50.0f);
-			em.shadow(sp.pos, sdir, time, aslot, w[0] * (ndotl * L.col[0] * tc[0] + pw * L.col[0]),
+			em.shadow(shadow_origin(sp, sdir), sdir, time, aslot, w[0] * (ndotl * L.col[0] * tc[0] + pw * L.col[0]),
 					w[1] * (ndotl * L.col[1] * tc[1] + pw * L.col[1]), w[2] * (ndotl * L.col[2] * tc[2] + pw * L.col[2]));
 		}
 		return;
@@ -324,21 +381,77 @@ __device__ __forceinline__ void shade_one(const DScene &S, const RayRec &ray, co
 				float lc = L.col[k] * 1.0f;
 				c[k] = ((ndotl * lc) * scale) * kd[k] + ((pw * lc) * scale) * ks[k];
 			}
-			if(c[0] != 0.0f || c[1] != 0.0f || c[2] != 0.0f) em.shadow(sp.pos, sdir, time, aslot, w[0] * c[0], w[1] * c[1], w[2] * c[2]);
+			if(c[0] != 0.0f || c[1] != 0.0f || c[2] != 0.0f) em.shadow(shadow_origin(sp, sdir), sdir, time, aslot, w[0] * c[0], w[1] * c[1], w[2] * c[2]);
 		}
 	}
 	/* final gather: diffuse rays end at their next hit (src/shader.cc:154-187) */
 	if(S.gi_on) {
 		int ds = S.diffuse_samples < MAX_DS ? S.diffuse_samples : MAX_DS;
-		for(int k = 0; k < ds; k++) {
+		bool cached = false;
+		int rec = -1;
+		if(S.nrc.mode) {
+			/* the radiance cache: a query in a region the network serves;
+			 * a training or validation record where the frame's hash
+			 * selects the vertex (its diffuse rays carry weight g alone, so
+			 * that the record's slot receives the plain estimate / (w kd)) */
+			const DNrc &N = S.nrc;
+			float x[9];
+			nrc_inputs(N, sp.pos, normal, incident, x);
+			cached = N.mode == 2 || !N.fallback[nrc_region(x)];
+			uint32_t hsel = hash32(N.key ^ hash32((uint32_t)pixel * 0x9e3779b9u ^ hash32((uint32_t)path + 0x632be5abu * (uint32_t)sample)));
+			if(hsel < N.p_train) {
+				int j = warp_alloc(N.tcount, 1);
+				if(j < N.tcap) rec = j;
+			} else if(hsel - N.p_train < N.p_val) {
+				int j = warp_alloc(N.tcount + 1, 1);
+				if(j < N.vcap) rec = N.tcap + j;
+			}
+			if(rec >= 0) store_x(N.tx + (size_t)rec * 9, x);
+			if(cached) {
+				int j = warp_alloc(N.qcount, 1);
+				if(j < N.qcap) {
+					store_x(N.qx + (size_t)j * 9, x);
+					N.qw[j] = make_float4(w[0] * kd[0], w[1] * kd[1], w[2] * kd[2], __int_as_float(aslot));
+				} else {
+					cached = false;   /* query queue full: the plain gather */
+				}
+			}
+			warp_count(N.counters, true);
+			warp_count(N.counters + 1, cached);
+		}
+		/* rays of the image's plain gather: ds, or the fallback count in a
+		 * fallback region; of a record: ds for training, NRC_VAL_RAYS (at
+		 * least) for validation, whose targets judge the network */
+		int nimg = cached ? 0 : (S.nrc.mode && S.nrc.fb_samples > 0 ? S.nrc.fb_samples : ds);
+		int nrec = rec < 0 ? 0 : (rec < S.nrc.tcap ? ds : (ds > NRC_VAL_RAYS ? ds : NRC_VAL_RAYS));
+		for(int k = 0; k < nimg; k++) {
 			V3 dir = sphrand(&rng, 1.0f);
 			float ndotl;
 			if((ndotl = dot(dir, normal)) < 0.0f) dir = -dir;
 			float diff_energy = ndotl * energy;
 			if(diff_energy > S.min_energy) {
-				float g = S.diffuse_samples > 1 ? ndotl / (float)S.diffuse_samples : ndotl;
+				float g = nimg > 1 ? ndotl / (float)nimg : ndotl;
 				em.child(make_child(ray, sp.pos, dir * ray_mag, diff_energy, DIFFUSE_ITER, path * 4 + 2, k, st, w[0] * kd[0] * g,
 						w[1] * kd[1] * g, w[2] * kd[2] * g));
+			}
+		}
+		if(nrec) {
+			/* a record's directions come from a stream keyed by the frame, so
+			 * that a vertex trained again sees a new estimate */
+			sray_rng rr;
+			sray_rng_init(&rr, S.seed ^ ((uint64_t)S.nrc.key << 32), SRAY_DOM_NRC | ((uint32_t)path << 4), (uint32_t)pixel,
+					(uint32_t)sample);
+			for(int k = 0; k < nrec; k++) {
+				V3 dir = sphrand(&rr, 1.0f);
+				float ndotl;
+				if((ndotl = dot(dir, normal)) < 0.0f) dir = -dir;
+				float diff_energy = ndotl * energy;
+				if(diff_energy > S.min_energy) {
+					float g = nrec > 1 ? ndotl / (float)nrec : ndotl;
+					RayRec c = make_child(ray, sp.pos, dir * ray_mag, diff_energy, DIFFUSE_ITER, path * 4 + 2, k, st, g, g, g);
+					c.aslot = S.nrc.t0 + rec;
+					em.child(c);
+				}
 			}
 		}
 	}
@@ -734,7 +847,75 @@ struct GatherWork {
 	unsigned long long tested, cand, select, spill;
 };
 
-__device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *keys, int *idx, float out[3], GatherWork &gw)
+/* More candidates than the on-chip list holds (a dense caustic inside the
+ * radius cap): a histogram of the candidates' keys in GATHER_BINS
+ * logarithmic bins (8 per octave of the squared distance, the top bin
+ * holding the largest key) finds the bin of the k-th nearest; a second pass
+ * lists the candidates of that bin and below, which hold the k nearest, in
+ * keys/idx.  Returns the number listed, or -1 if they do not fit either. */
+#define GATHER_BINS 256
+__device__ __noinline__ int gather_narrow(const DPhotonMap &M, const GatherCells &gc, V3 pos, int lane, unsigned &maxkey,
+		unsigned *keys, int *idx, int *hist)
+{
+	for(int i = lane; i < GATHER_BINS; i += 32) hist[i] = 0;
+	__syncwarp();
+	int base = (int)(maxkey >> 20) - (GATHER_BINS - 1);
+	for_range(M, gc, pos, lane, [&](bool in, int, unsigned key) {
+		if(in) {
+			int b = (int)(key >> 20) - base;
+			atomicAdd(&hist[b > 0 ? b : 0], 1);
+		}
+	});
+	__syncwarp();
+	/* the bin of the k-th smallest key: each lane sums 8 bins, a warp scan
+	 * finds the lane, the lane its bin */
+	int loc[GATHER_BINS / 32];
+	int ls = 0;
+	#pragma unroll
+	for(int i = 0; i < GATHER_BINS / 32; i++) {
+		loc[i] = hist[lane * (GATHER_BINS / 32) + i];
+		ls += loc[i];
+	}
+	int incl = ls;
+	for(int o = 1; o < 32; o <<= 1) {
+		int v = __shfl_up_sync(0xffffffffu, incl, o);
+		if(lane >= o) incl += v;
+	}
+	int excl = incl - ls;
+	unsigned m = __ballot_sync(0xffffffffu, excl < M.k && M.k <= incl);
+	int owner = m ? __ffs(m) - 1 : 31;
+	int bstar = GATHER_BINS - 1;
+	if(lane == owner) {
+		int c = excl;
+		#pragma unroll
+		for(int i = 0; i < GATHER_BINS / 32; i++) {
+			if(c + loc[i] >= M.k) { bstar = lane * (GATHER_BINS / 32) + i; break; }
+			c += loc[i];
+		}
+	}
+	bstar = __shfl_sync(0xffffffffu, bstar, owner);
+	int nlist = 0;
+	unsigned lt_mask = (1u << lane) - 1u;
+	unsigned kmax = 0;
+	for_range(M, gc, pos, lane, [&](bool in, int j, unsigned key) {
+		bool take = in && (int)(key >> 20) - base <= bstar;
+		unsigned b = __ballot_sync(0xffffffffu, take);
+		int slot = nlist + __popc(b & lt_mask);
+		if(take) {
+			kmax = key > kmax ? key : kmax;
+			if(slot < KEY_CAP) { keys[slot] = key; idx[slot] = j; }
+		}
+		nlist += __popc(b);
+	});
+	__syncwarp();
+	if(nlist > KEY_CAP) return -1;
+	/* the largest listed key: the k-th nearest when exactly k are listed */
+	maxkey = warp_maxu(kmax);
+	return nlist;
+}
+
+__device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *keys, int *idx, int *hist, float out[3],
+		GatherWork &gw)
 {
 	const DPhotonMap &M = kind == 0 ? S.caust : S.gi;
 	int lane = threadIdx.x & 31;
@@ -776,6 +957,13 @@ __device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *ke
 		gw.cand += (unsigned)ncand;
 		gw.spill += cached ? 0u : 1u;
 		gw.select += ncand > M.k ? 1u : 0u;
+		if(!cached && ncand > M.k) {
+			int nl = gather_narrow(M, gc, pos, lane, maxkey, keys, idx, hist);
+			if(nl >= 0) {
+				ncand = nl;
+				cached = true;
+			}
+		}
 		unsigned kth = maxkey;
 		if(ncand > M.k) {
 			unsigned prefix = 0;
@@ -833,6 +1021,7 @@ __global__ void __launch_bounds__(GATHER_WARPS * 32, 3) k_gather(DScene S, const
 {
 	__shared__ unsigned keys[GATHER_WARPS][KEY_CAP];
 	__shared__ int idx[GATHER_WARPS][KEY_CAP];
+	__shared__ int hist[GATHER_WARPS][GATHER_BINS];
 	int n = *gq_count;
 	int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	int gw = blockIdx.x * GATHER_WARPS + w, nw = gridDim.x * GATHER_WARPS;
@@ -842,7 +1031,7 @@ __global__ void __launch_bounds__(GATHER_WARPS * 32, 3) k_gather(DScene S, const
 		int kind = __float_as_int(g.a.w);
 		int pixel = __float_as_int(g.b.w);
 		float est[3];
-		gather_one(S, kind, mk(g.a.x, g.a.y, g.a.z), mk(g.b.x, g.b.y, g.b.z), keys[w], idx[w], est, work);
+		gather_one(S, kind, mk(g.a.x, g.a.y, g.a.z), mk(g.b.x, g.b.y, g.b.z), keys[w], idx[w], hist[w], est, work);
 		if(lane == 0) acc_add(acc, pixel, g.w.x * est[0], g.w.y * est[1], g.w.z * est[2]);
 		__syncwarp();
 	}
@@ -872,6 +1061,7 @@ __global__ void __launch_bounds__(GATHER_WARPS * 32, 3) k_gather_points(DScene S
 {
 	__shared__ unsigned keys[GATHER_WARPS][KEY_CAP];
 	__shared__ int idx[GATHER_WARPS][KEY_CAP];
+	__shared__ int hist[GATHER_WARPS][GATHER_BINS];
 	int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	int gw = blockIdx.x * GATHER_WARPS + w, nw = gridDim.x * GATHER_WARPS;
 	GatherWork work = {0, 0, 0, 0};
@@ -880,7 +1070,7 @@ __global__ void __launch_bounds__(GATHER_WARPS * 32, 3) k_gather_points(DScene S
 		int kind = __float_as_int(g.a.w);
 		int pt = __float_as_int(g.b.w);
 		float est[3];
-		gather_one(S, kind, mk(g.a.x, g.a.y, g.a.z), mk(g.b.x, g.b.y, g.b.z), keys[w], idx[w], est, work);
+		gather_one(S, kind, mk(g.a.x, g.a.y, g.a.z), mk(g.b.x, g.b.y, g.b.z), keys[w], idx[w], hist[w], est, work);
 		if(lane == 0) {
 			out[pt * 3] = est[0];
 			out[pt * 3 + 1] = est[1];
@@ -1407,6 +1597,259 @@ int Renderer::ensure_pqueue(int which, int cap)
 	return queue_alloc(pqbuf[which], pq[which], pqcap[which], cap);
 }
 
+/* ---------------------------------------------------------------- */
+/* radiance cache: records, validation and training (host driver below) */
+
+#define NRC_VAL_DECAY 0.98f   /* per-frame decay of a region's running validation sums */
+#define NRC_VAL_MIN 64.0f     /* running record count a region needs before it is judged */
+#define NRC_LR 1e-3f
+
+/* targets of the training records [0, n_t) and the validation records
+ * [tcap, tcap + n_v): the channels their slots accumulated */
+__global__ void k_nrc_harvest(const float4 *acc_rec, int n_t, int tcap, int n_v, float *tgt)
+{
+	int n = tcap + n_v;
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		if(i >= n_t && i < tcap) continue;
+		float4 a = acc_rec[i];
+		tgt[(size_t)i * 3 + 0] = a.x;
+		tgt[(size_t)i * 3 + 1] = a.y;
+		tgt[(size_t)i * 3 + 2] = a.z;
+	}
+}
+
+/* the frame's validation records into their regions' sums */
+__global__ void k_nrc_validate(int n, const float *x, const float *y, const float *t, NrcRegionStats *rs)
+{
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		int r = nrc_region(x + (size_t)i * 9);
+		const float *yi = y + (size_t)i * 3, *ti = t + (size_t)i * 3;
+		float ly = fmaxf(yi[0], 0.0f) + fmaxf(yi[1], 0.0f) + fmaxf(yi[2], 0.0f);
+		float lt = ti[0] + ti[1] + ti[2];
+		atomicAdd(&rs->sy[r], ly);
+		atomicAdd(&rs->st[r], lt);
+		atomicAdd(&rs->sn[r], 1.0f);
+		atomicAdd(&rs->sq[r], (ly - lt) * (ly - lt));
+	}
+}
+
+__device__ __forceinline__ float block_sum_regions(float v, float *red)
+{
+	int r = threadIdx.x;
+	red[r] = v;
+	__syncthreads();
+	for(int h = NRC_REGIONS / 2; h > 0; h >>= 1) {
+		if(r < h) red[r] += red[r + h];
+		__syncthreads();
+	}
+	float out = red[0];
+	__syncthreads();
+	return out;
+}
+
+/* one block, a thread per region: fold the frame's sums into the running
+ * sums and judge each region.  Its validation relative error is
+ * |sum prediction - sum target| / sum target over the running sums (the
+ * denominator floored at 1% of the mean target, so that dark regions are
+ * not judged on noise).  A region is judged once it has NRC_VAL_MIN records
+ * and the standard error of that estimate (from the squared differences) is
+ * at most half the threshold; the network serves it when judged and the
+ * error is at most the threshold, else the plain gather does. */
+__global__ void __launch_bounds__(NRC_REGIONS) k_nrc_regions(NrcRegionStats *rs, float decay, float max_rel, float min_n, int mode)
+{
+	__shared__ float red[NRC_REGIONS];
+	int r = threadIdx.x;
+	float ey = rs->ey[r] * decay + rs->sy[r];
+	float et = rs->et[r] * decay + rs->st[r];
+	float en = rs->en[r] * decay + rs->sn[r];
+	float eq = rs->eq[r] * decay + rs->sq[r];
+	rs->ey[r] = ey;
+	rs->et[r] = et;
+	rs->en[r] = en;
+	rs->eq[r] = eq;
+	rs->sy[r] = 0.0f;
+	rs->st[r] = 0.0f;
+	rs->sn[r] = 0.0f;
+	rs->sq[r] = 0.0f;
+	float tot_t = block_sum_regions(et, red);
+	float tot_n = block_sum_regions(en, red);
+	float mean = tot_n > 0.0f ? tot_t / tot_n : 0.0f;
+	float den = fmaxf(et, 0.01f * mean * en);
+	float err = fabsf(ey - et);
+	float var = en > 0.0f ? fmaxf(eq - (ey - et) * (ey - et) / en, 0.0f) : 0.0f;
+	bool judged = en >= min_n && den > 0.0f && sqrtf(var) <= 0.5f * max_rel * den;
+	bool ok = judged && err <= max_rel * den;
+	rs->fallback[r] = (mode == 2 || ok) ? 0 : 1;
+	float nj = block_sum_regions(judged ? 1.0f : 0.0f, red);
+	float nok = block_sum_regions(ok ? 1.0f : 0.0f, red);
+	float se = block_sum_regions(judged ? err : 0.0f, red);
+	float stt = block_sum_regions(judged ? et : 0.0f, red);
+	if(r == 0) {
+		rs->summary[0] = nj;
+		rs->summary[1] = nok;
+		rs->summary[2] = stt > 0.0f ? se / stt : 0.0f;
+		rs->summary[3] = 0.0f;
+	}
+}
+
+__global__ void k_nrc_reset_regions(NrcRegionStats *rs)
+{
+	int r = threadIdx.x;
+	rs->sy[r] = rs->st[r] = rs->sn[r] = rs->sq[r] = 0.0f;
+	rs->ey[r] = rs->et[r] = rs->en[r] = rs->eq[r] = 0.0f;
+	rs->fallback[r] = 1;
+	if(r < 4) rs->summary[r] = 0.0f;
+}
+
+int Renderer::nrc_reset_regions(cudaStream_t s)
+{
+	CK(nrc_regions.ensure(sizeof(NrcRegionStats)), "radiance cache regions");
+	k_nrc_reset_regions<<<1, NRC_REGIONS, 0, s>>>(nrc_regions.as<NrcRegionStats>());
+	CK(cudaGetLastError(), "radiance cache regions");
+	nrc_regions_ready = true;
+	return 0;
+}
+
+static uint32_t nrc_prob(double f)
+{
+	if(!(f > 0.0)) return 0u;
+	if(f >= 1.0) return 0xffffffffu;
+	return (uint32_t)(f * 4294967296.0);
+}
+
+static uint32_t nrc_mix(uint64_t v)
+{
+	v ^= v >> 33;
+	v *= 0xff51afd7ed558ccdull;
+	v ^= v >> 33;
+	v *= 0xc4ceb9fe1a85ec53ull;
+	v ^= v >> 33;
+	return (uint32_t)v;
+}
+
+/* the radiance cache's view of sample batch `batch` (n_prim primary rays):
+ * query and record buffers, the record slots past the batch's accumulator
+ * slots, and (first batch only) the selection of training and validation
+ * vertices, sized from the last frame's vertex count */
+int Renderer::nrc_setup(int batch, int n_prim, cudaStream_t s)
+{
+	DNrc &N = S.nrc;
+	N.mode = S.gi_on ? opt.nrc : 0;
+	if(!N.mode) return 0;
+	int r = nrc_ensure_ready(opt.seed, s);
+	if(r) return fail(r, std::string("radiance cache: ") + nrc_error());
+	if(!nrc_regions_ready && (r = nrc_reset_regions(s))) return r;
+	int ntrain = opt.nrc_train_samples > 0 ? opt.nrc_train_samples : 65536;
+	int nval = ntrain / 4 > 1024 ? ntrain / 4 : 1024;
+	int tcap = ntrain + ntrain / 8 + 1024;
+	int vcap = nval + nval / 8 + 1024;
+	nrc_rcap = tcap + vcap;
+	CK(nrc_rx.ensure((size_t)nrc_rcap * 9 * sizeof(float)), "radiance cache records");
+	CK(nrc_rt.ensure((size_t)nrc_rcap * 3 * sizeof(float)), "radiance cache targets");
+	CK(nrc_ry.ensure((size_t)vcap * 3 * sizeof(float)), "radiance cache predictions");
+	int64_t qc = (int64_t)n_prim * 2 + 65536;
+	if(qc > INT_MAX / 2) qc = INT_MAX / 2;
+	nrc_qcap = (int)qc;
+	CK(nrc_qx.ensure((size_t)nrc_qcap * 9 * sizeof(float)), "radiance cache queries");
+	CK(nrc_qw.ensure((size_t)nrc_qcap * sizeof(float4)), "radiance cache queries");
+	CK(acc.ensure(((size_t)n_prim + nrc_rcap) * 16), "accumulator");
+	CK(cudaMemsetAsync(acc.as<float4>() + n_prim, 0, (size_t)nrc_rcap * 16, s), "reset record slots");
+	int *cnt = counts.as<int>();
+	CK(cudaMemsetAsync(cnt + 16, 0, 3 * sizeof(int), s), "reset radiance cache counts");
+	N.qx = nrc_qx.as<float>();
+	N.qw = nrc_qw.as<float4>();
+	N.qcount = cnt + 16;
+	N.qcap = nrc_qcap;
+	N.tx = nrc_rx.as<float>();
+	N.tcount = cnt + 17;
+	N.tcap = tcap;
+	N.vcap = vcap;
+	N.t0 = n_prim;
+	N.fallback = nrc_regions.as<NrcRegionStats>()->fallback;
+	double lo[3] = {0.0, 0.0, 0.0}, hi[3] = {1.0, 1.0, 1.0};
+	if(!sc.oct.nodes.empty()) {
+		for(int k = 0; k < 3; k++) {
+			lo[k] = sc.oct.nodes[0].box.mn[k];
+			hi[k] = sc.oct.nodes[0].box.mx[k];
+		}
+	}
+	for(int k = 0; k < 3; k++) {
+		double ext = hi[k] - lo[k];
+		N.lo[k] = (float)lo[k];
+		N.sc[k] = ext > 0.0 ? (float)(1.0 / ext) : 1.0f;
+	}
+	if(batch == 0) {
+		double expect = nrc_expect > 0 ? (double)nrc_expect : (double)n_prim;
+		double ft = ntrain / expect, fv = nval / expect;
+		if(ft + fv > 1.0) {
+			/* fewer vertices than records wanted: every vertex is one, in proportion */
+			double sum = ft + fv;
+			ft /= sum;
+			fv /= sum;
+		}
+		N.p_train = nrc_prob(ft);
+		N.p_val = nrc_prob(fv);
+		if((uint64_t)N.p_train + N.p_val > 0xffffffffull) N.p_val = 0xffffffffu - N.p_train;
+	} else {
+		N.p_train = N.p_val = 0;
+	}
+	N.key = nrc_mix(opt.seed ^ ((uint64_t)nrc_frames * 0x9e3779b97f4a7c15ull) ^ 0x4e5243ull);
+	N.fb_samples = opt.nrc_fallback_samples;
+	N.counters = (unsigned long long *)(ctr.as<char>() + offsetof(DevCounters, nrc)) + 2 * (batch > 0);
+	return 0;
+}
+
+/* after the batch's shading tree: the queries' network outputs into the
+ * accumulators; after the first batch also the records' targets, the
+ * validation of the network on the validation records (before it trains
+ * on this frame), the regions' fallback flags for the next frame, and the
+ * training steps */
+int Renderer::nrc_batch_done(int batch, cudaStream_t s)
+{
+	if(!S.nrc.mode) return 0;
+	int *cnt = counts.as<int>();
+	int r = 0;
+	LAUNCH(*this, "nrc_query", s, r = nrc_query(cnt + 16, nrc_qcap, nrc_qx.as<float>(), nrc_qw.as<float4>(), acc.as<float4>(), s));
+	if(r) return fail(r, std::string("radiance cache: ") + nrc_error());
+	if(batch != 0) return 0;
+	int h[2] = {0, 0};
+	CK(cudaMemcpyAsync(h, cnt + 17, sizeof h, cudaMemcpyDeviceToHost, s), "read record counts");
+	CK(cudaStreamSynchronize(s), "record counts");
+	d2h += sizeof h;
+	prof_collect();
+	const DNrc &N = S.nrc;
+	int n_t = h[0] < N.tcap ? h[0] : N.tcap;
+	int n_v = h[1] < N.vcap ? h[1] : N.vcap;
+	float *rx = nrc_rx.as<float>(), *rt = nrc_rt.as<float>();
+	NrcRegionStats *rs = nrc_regions.as<NrcRegionStats>();
+	if(n_t + n_v > 0)
+		LAUNCH(*this, "nrc_records", s, k_nrc_harvest<<<grid_for(N.tcap + n_v, 256), 256, 0, s>>>(acc.as<float4>() + N.t0, n_t, N.tcap,
+				n_v, rt));
+	if(n_v > 0) {
+		LAUNCH(*this, "nrc_validate", s, r = nrc_infer(n_v, rx + (size_t)N.tcap * 9, nrc_ry.as<float>(), s));
+		if(r) return fail(r, std::string("radiance cache: ") + nrc_error());
+		LAUNCH(*this, "nrc_validate", s, k_nrc_validate<<<grid_for(n_v, 256), 256, 0, s>>>(n_v, rx + (size_t)N.tcap * 9,
+				nrc_ry.as<float>(), rt + (size_t)N.tcap * 3, rs));
+	}
+	float max_rel = opt.nrc_max_rel_err;
+	LAUNCH(*this, "nrc_validate", s, k_nrc_regions<<<1, NRC_REGIONS, 0, s>>>(rs, NRC_VAL_DECAY, max_rel, NRC_VAL_MIN, N.mode));
+	int steps = opt.nrc_train_steps > 0 ? opt.nrc_train_steps : 4;
+	int per = n_t / steps;
+	if(per < 16) {
+		steps = n_t >= 16 ? 1 : 0;
+		per = n_t;
+	}
+	for(int i = 0; i < steps; i++) {
+		LAUNCH(*this, "nrc_train", s, r = nrc_train(per, rx + (size_t)i * per * 9, rt + (size_t)i * per * 3, NRC_LR, s));
+		if(r) return fail(r, std::string("radiance cache: ") + nrc_error());
+		launch_count += NRC_TRAIN_KERNELS - 1;
+	}
+	nrc_last_train = n_t;
+	nrc_last_val = n_v;
+	nrc_frames++;
+	return 0;
+}
+
 int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t s, bool overlap_photons)
 {
 	(void)msec;
@@ -1431,7 +1874,15 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 		CK(fbdev.ensure((size_t)npix * 16), "framebuffer");
 		fbd = fbdev.as<float4>();
 	}
-	int per_ray_children = 2 + (opt.gi_photons ? ds : 0);
+	/* a vertex may send both its image's diffuse rays (the fallback count in
+	 * a fallback region) and a record's */
+	int img_rays = ds, rec_rays = 0;
+	if(opt.nrc) {
+		int fb = opt.nrc_fallback_samples > MAX_DS ? MAX_DS : opt.nrc_fallback_samples;
+		img_rays = fb > ds ? fb : ds;
+		rec_rays = ds > NRC_VAL_RAYS ? ds : NRC_VAL_RAYS;
+	}
+	int per_ray_children = 2 + (opt.gi_photons ? img_rays + rec_rays : 0);
 	int shadow_per_ray = 0;
 	for(size_t li = 0; li < sc.lights.size(); li++) shadow_per_ray += sc.lights[li].type != LT_POINT ? opt.shadow_samples : 1;
 	if(shadow_per_ray < 1) shadow_per_ray = 1;
@@ -1465,6 +1916,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 		int n_prim = n_active * width;
 		if(ensure_queue(0, n_prim)) return SRAY_ECUDA;
 		CK(acc.ensure((size_t)n_prim * 16), "accumulator");
+		if(int r = nrc_setup(b, n_prim, s)) return r;
 		q[0].count = cnt + 0;
 		q[1].count = cnt + 1;
 		LAUNCH(*this, "camera", s, k_camera<<<grid_for(n_prim, 256), 256, 0, s>>>(S, act, act_count, s0, width, q[0], acc.as<float4>(),
@@ -1567,6 +2019,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			n_rays = h_cnt;
 			cur ^= 1;
 		}
+		if(int r = nrc_batch_done(b, s)) return r;
 		CK(cudaMemsetAsync(next_count, 0, sizeof(int), s), "reset next active");
 		LAUNCH(*this, "finish", s, k_finish<<<grid_for(n_active, 256), 256, 0, s>>>(act, act_count, s0, width, acc.as<float4>(),
 				hist.as<float4>(), sums.as<float4>(), maxs, opt.min_samples, opt.max_var, next_list, next_count, fbd,
@@ -1602,6 +2055,12 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 	stats.gather_selects = (int64_t)hc.g_select;
 	stats.gather_spills = (int64_t)hc.g_spill;
 	stats.bvh_fallbacks = (int64_t)hc.bvh_fallbacks;
+	if(overlap_photons && !sc.lights.empty()) stats.photons_emitted = (int64_t)opt.caust_photons + opt.gi_photons;
+	if(S.nrc.mode) {
+		nrc_expect = (int64_t)hc.nrc[0];
+		nrc_last_vertices = (int64_t)(hc.nrc[0] + hc.nrc[2]);
+		nrc_last_cached = (int64_t)(hc.nrc[1] + hc.nrc[3]);
+	}
 	if(hc.overflow) return fail(SRAY_EDEVICE, "device queue or traversal stack overflow");
 	return 0;
 }
@@ -1688,6 +2147,10 @@ void sray_default_opts(sray_opts *o)
 	o->gather_rcap = 0.5f;
 	o->rng_paths = 1;
 	o->seed = 0x5EED0001ull;
+	o->nrc = 0;
+	o->nrc_train_samples = 65536;
+	o->nrc_max_rel_err = 0.05f;
+	o->nrc_train_steps = 4;
 }
 
 static int check_opts(const sray_opts *o)
@@ -1695,11 +2158,16 @@ static int check_opts(const sray_opts *o)
 	if(!o) { g_err = "null options"; return SRAY_EINVAL; }
 	if(o->width <= 0 || o->height <= 0 || (int64_t)o->width * o->height > (1 << 27)) { g_err = "bad image size"; return SRAY_EINVAL; }
 	if(o->max_samples < 1 || o->max_samples > 64 || o->min_samples < 0) { g_err = "bad sample counts (1..64)"; return SRAY_EINVAL; }
-	if(o->diffuse_samples < 0 || o->diffuse_samples > MAX_DS) { g_err = "diffuse samples must be 0..8"; return SRAY_EINVAL; }
+	if(o->diffuse_samples < 0 || o->diffuse_samples > MAX_DS) { g_err = "diffuse samples must be 0..128"; return SRAY_EINVAL; }
 	if(o->shadow_samples < 1) { g_err = "shadow samples must be >= 1"; return SRAY_EINVAL; }
 	if(o->iter < 0 || o->iter > 13) { g_err = "iter must be 0..13"; return SRAY_EINVAL; }
 	if(o->caust_photons < 0 || o->gi_photons < 0) { g_err = "negative photon count"; return SRAY_EINVAL; }
 	if(o->caust_k < 0 || o->gi_k < 0) { g_err = "negative k"; return SRAY_EINVAL; }
+	if(o->nrc < 0 || o->nrc > 2) { g_err = "nrc must be 0, 1 or 2"; return SRAY_EINVAL; }
+	if(o->nrc_train_samples < 0 || o->nrc_train_samples > (1 << 22)) { g_err = "nrc_train_samples must be 0..4194304"; return SRAY_EINVAL; }
+	if(o->nrc_train_steps < 0 || o->nrc_train_steps > 64) { g_err = "nrc_train_steps must be 0..64"; return SRAY_EINVAL; }
+	if(!(o->nrc_max_rel_err >= 0.0f)) { g_err = "nrc_max_rel_err must be >= 0"; return SRAY_EINVAL; }
+	if(o->nrc_fallback_samples < 0 || o->nrc_fallback_samples > MAX_DS) { g_err = "nrc_fallback_samples must be 0..128"; return SRAY_EINVAL; }
 	return 0;
 }
 
@@ -1991,6 +2459,49 @@ int sray_gpu_get_stats(sray_stats *st)
 	return 0;
 }
 
+int sray_gpu_nrc_stats(sray_nrc_stats *st)
+{
+	NEED_CTX();
+	if(!st) { g_err = "null stats"; return SRAY_EINVAL; }
+	Renderer &R = *g_R;
+	memset(st, 0, sizeof *st);
+	st->frames = R.nrc_frames;
+	st->vertices = R.nrc_last_vertices;
+	st->cached = R.nrc_last_cached;
+	st->train_samples = R.nrc_last_train;
+	st->val_samples = R.nrc_last_val;
+	st->regions = NRC_REGIONS;
+	if(R.nrc_regions_ready) {
+		float sm[4];
+		cudaError_t e = cudaMemcpy(sm, R.nrc_regions.as<NrcRegionStats>()->summary, sizeof sm, cudaMemcpyDeviceToHost);
+		if(e != cudaSuccess) { g_err = std::string("radiance cache stats: ") + cudaGetErrorString(e); return SRAY_ECUDA; }
+		st->regions_validated = (int)sm[0];
+		st->regions_cached = (int)sm[1];
+		st->val_rel_err = sm[2];
+		float *lp = nrc_loss_ptr();
+		if(lp && cudaMemcpy(&st->loss, lp, sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess) st->loss = -1.0f;
+	}
+	return 0;
+}
+
+int sray_gpu_nrc_reset(uint64_t seed)
+{
+	NEED_CTX();
+	Renderer &R = *g_R;
+	int r = sray_nrc_reset(seed);
+	if(r) { g_err = std::string("radiance cache: ") + nrc_error(); return r; }
+	R.nrc_frames = 0;
+	R.nrc_expect = 0;
+	R.nrc_last_train = R.nrc_last_val = 0;
+	R.nrc_last_vertices = R.nrc_last_cached = 0;
+	if(R.nrc_regions_ready) {
+		r = R.nrc_reset_regions(0);
+		if(r) { g_err = R.err; return r; }
+		if(cudaDeviceSynchronize() != cudaSuccess) { g_err = "radiance cache reset"; return SRAY_ECUDA; }
+	}
+	return 0;
+}
+
 int sray_gpu_set_profiling(int flags)
 {
 	NEED_CTX();
@@ -2037,7 +2548,8 @@ void sray_gpu_shutdown(void)
 	DevBuf *bufs[] = {&R.mnodes, &R.mtris, &R.mprim, &R.tri_pos, &R.tri_attr, &R.objs, &R.mats, &R.lights, &R.snodes, &R.sslots,
 		&R.xf, &R.light_pos, &R.cam_m, &R.projbits, &R.coverage, &R.qbuf[0], &R.qbuf[1], &R.hits, &R.gq, &R.sq, &R.acc, &R.hist, &R.sums,
 		&R.active[0], &R.active[1], &R.spp, &R.fbdev, &R.ctr, &R.counts, &R.bnodes, &R.btris, &R.bprim, &R.bhome,
-		&R.fbl, &R.tnodes, &R.ohome, &R.pool_ready, &R.pqbuf[0], &R.pqbuf[1], &R.phits, &R.pfbl, &R.pcounts, &R.pctr};
+		&R.fbl, &R.tnodes, &R.ohome, &R.pool_ready, &R.pqbuf[0], &R.pqbuf[1], &R.phits, &R.pfbl, &R.pcounts, &R.pctr,
+		&R.nrc_qx, &R.nrc_qw, &R.nrc_rx, &R.nrc_rt, &R.nrc_ry, &R.nrc_regions};
 	if(R.ps) cudaStreamSynchronize(R.ps);
 	for(DevBuf *b : bufs) b->release();
 	PhotonBufs *pb[] = {&R.caust, &R.gi};

@@ -75,6 +75,19 @@ struct DevCounters {
 	unsigned long long nodes, prims;
 	unsigned long long g_tested, g_cand, g_select, g_spill;   /* gather work */
 	unsigned long long bvh_fallbacks;   /* hierarchy hits the octree did not confirm */
+	unsigned long long nrc[4];          /* final-gather vertices, cached: sample batch 0, batch 1 */
+};
+
+/* per-region validation of the radiance cache: the frame's sums of
+ * prediction and target (channel sums), the record count and the squared
+ * prediction - target differences, their running
+ * (exponentially decayed) totals, the fallback flags the shading kernels
+ * read, and a summary [validated regions, cached regions, relative error] */
+struct NrcRegionStats {
+	float sy[NRC_REGIONS], st[NRC_REGIONS], sn[NRC_REGIONS], sq[NRC_REGIONS];
+	float ey[NRC_REGIONS], et[NRC_REGIONS], en[NRC_REGIONS], eq[NRC_REGIONS];
+	float summary[4];
+	unsigned char fallback[NRC_REGIONS];
 };
 
 struct PhotonBufs {
@@ -101,7 +114,7 @@ struct Renderer {
 	long frame_msec = 0;
 	bool photons_ready = false;
 	PhotonBufs caust, gi;
-	DScene S;
+	DScene S = {};                /* S.nrc is set per sample batch (nrc_setup) */
 
 	/* render buffers */
 	DevBuf qbuf[2], hits, gq, sq, acc, hist, sums, active[2], spp, fbdev, ctr, counts, fbl, pool_ready;
@@ -115,6 +128,19 @@ struct Renderer {
 	cudaStream_t ps = nullptr;
 	cudaEvent_t ps_done = nullptr;
 	sray_stats stats;
+
+	/* radiance cache: queries (inputs, weight + slot), training and
+	 * validation records (inputs, targets, predictions), region statistics */
+	DevBuf nrc_qx, nrc_qw, nrc_rx, nrc_rt, nrc_ry, nrc_regions;
+	int nrc_qcap = 0, nrc_rcap = 0;
+	bool nrc_regions_ready = false;
+	int64_t nrc_frames = 0;
+	int64_t nrc_expect = 0;       /* final-gather vertices of the last frame's first sample batch */
+	int nrc_last_train = 0, nrc_last_val = 0;
+	int64_t nrc_last_vertices = 0, nrc_last_cached = 0;
+	int nrc_setup(int batch, int n_prim, cudaStream_t s);
+	int nrc_batch_done(int batch, cudaStream_t s);
+	int nrc_reset_regions(cudaStream_t s);
 
 	/* profiling: event pairs per launch, resolved after each synchronisation */
 	int prof_flags = 0;

@@ -18,7 +18,7 @@ EXPORTS = ["sray_default_opts", "sray_gpu_init", "sray_gpu_set_opts", "sray_gpu_
            "sray_gpu_scene_info", "sray_gpu_build", "sray_gpu_shoot_photons", "sray_gpu_render",
            "sray_gpu_render_pixels", "sray_gpu_cast_rays", "sray_gpu_primary_hits", "sray_gpu_photon_gather", "sray_gpu_photon_gather_noalloc",
            "sray_gpu_get_photons",
-           "sray_gpu_get_stats", "sray_gpu_set_profiling", "sray_gpu_kernel_times", "sray_gpu_last_error",
+           "sray_gpu_get_stats", "sray_gpu_nrc_stats", "sray_gpu_nrc_reset", "sray_gpu_set_profiling", "sray_gpu_kernel_times", "sray_gpu_last_error",
            "sray_gpu_shutdown", "sray_nrc_reset", "sray_nrc_set_params", "sray_nrc_get_params", "sray_nrc_infer",
            "sray_nrc_gradients", "sray_nrc_train", "sray_nrc_last_error"]
 
@@ -37,6 +37,14 @@ class SrayStats(ctypes.Structure):
                 ("gather_selects", ctypes.c_int64), ("gather_spills", ctypes.c_int64),
                 ("bvh_fallbacks", ctypes.c_int64),
                 ("reserved", ctypes.c_int * 2)]
+
+
+class SrayNrcStats(ctypes.Structure):
+    _fields_ = [("frames", ctypes.c_int64), ("vertices", ctypes.c_int64), ("cached", ctypes.c_int64),
+                ("train_samples", ctypes.c_int64), ("val_samples", ctypes.c_int64),
+                ("regions", ctypes.c_int), ("regions_validated", ctypes.c_int), ("regions_cached", ctypes.c_int),
+                ("val_rel_err", ctypes.c_float), ("loss", ctypes.c_float), ("pad", ctypes.c_int),
+                ("reserved", ctypes.c_int64 * 4)]
 
 
 class SrayError(RuntimeError):
@@ -72,6 +80,8 @@ def load_library():
     L.sray_gpu_photon_gather_noalloc.argtypes = [ip, ip, vp, vp, vp, vp]
     L.sray_gpu_get_photons.argtypes = [ip, vp, ip, vp]
     L.sray_gpu_get_stats.argtypes = [ctypes.POINTER(SrayStats)]
+    L.sray_gpu_nrc_stats.argtypes = [ctypes.POINTER(SrayNrcStats)]
+    L.sray_gpu_nrc_reset.argtypes = [ctypes.c_uint64]
     L.sray_gpu_set_profiling.argtypes = [ip]
     L.sray_gpu_kernel_times.argtypes = [ctypes.c_char_p, ctypes.c_size_t, vp, vp, ip, vp, ip]
     L.sray_gpu_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
@@ -93,8 +103,11 @@ class RadianceCache:
     tensors: x [n, 9] float32, targets [n, 3])."""
 
     def __init__(self, seed=1):
+        """seed: re-initialise the network from it; None: use the network as it
+        is (the one the renderer trains)."""
         self.L = load_library()
-        self._chk(self.L.sray_nrc_reset(seed))
+        if seed is not None:
+            self._chk(self.L.sray_nrc_reset(seed))
 
     def _chk(self, r):
         if r != 0:
@@ -238,6 +251,18 @@ class GpuRenderer:
         st = SrayStats()
         self._chk(self.L.sray_gpu_get_stats(ctypes.byref(st)))
         return {f[0]: getattr(st, f[0]) for f in SrayStats._fields_ if f[0] not in ("reserved", "pad")}
+
+    def nrc_stats(self):
+        """Radiance-cache state: frames trained, the last frame's final-gather
+        vertices and how many the network served, training / validation
+        records, regions validated and served, validation relative error, loss."""
+        st = SrayNrcStats()
+        self._chk(self.L.sray_gpu_nrc_stats(ctypes.byref(st)))
+        return {f[0]: getattr(st, f[0]) for f in SrayNrcStats._fields_ if f[0] not in ("reserved", "pad")}
+
+    def nrc_reset(self, seed=None):
+        """Re-initialise the network and forget the regions' validation history."""
+        self._chk(self.L.sray_gpu_nrc_reset(self.opts.seed if seed is None else seed))
 
     def set_profiling(self, time_kernels=False, count_work=False):
         self._chk(self.L.sray_gpu_set_profiling((1 if time_kernels else 0) | (2 if count_work else 0)))

@@ -304,6 +304,12 @@ CONFIGS = {
     "small": dict(width=512, height=512, min_samples=1, max_samples=1, iter=5,
                   caust_photons=100000, gi_photons=0, caust_k=50, gi_k=0, gather_rcap=0.5,
                   scnoct_max_depth=8, scnoct_max_items=8, meshoct_max_depth=8, meshoct_max_items=8),
+    # the radiance-cache comparison: the small scene at 1080p with a global
+    # map, one final-gather ray per vertex (the plain method) or the network
+    "learned": dict(width=1920, height=1080, min_samples=1, max_samples=1, iter=5,
+                    caust_photons=100000, gi_photons=500000, caust_k=50, gi_k=100, gather_rcap=0.5,
+                    diffuse_samples=1, nrc_fallback_samples=16, scnoct_max_depth=8, scnoct_max_items=8,
+                    meshoct_max_depth=8, meshoct_max_items=8),
     "production": dict(width=1920, height=1080, min_samples=1, max_samples=16, max_var=0.05, iter=8,
                        caust_photons=500000, gi_photons=2000000, caust_k=100, gi_k=100, gather_rcap=0.5,
                        scnoct_max_depth=8, scnoct_max_items=8, meshoct_max_depth=10, meshoct_max_items=8),
@@ -318,7 +324,7 @@ def scene_opts(name, **over):
 
 def write_scene(name, cache_dir=None, **kw):
     """Generate (or reuse from cache_dir) the XML of scene `name`; returns the path."""
-    gen = {"small": small_scene, "production": production_scene, "feature": feature_scene}[name]
+    gen = {"small": small_scene, "learned": small_scene, "production": production_scene, "feature": feature_scene}[name]
     key = hashlib.sha1(repr((name, sorted(kw.items()), 3)).encode()).hexdigest()[:12]
     cache_dir = cache_dir or os.environ.get("SRAY_SCENE_CACHE", "/tmp/sray_scenes")
     os.makedirs(cache_dir, exist_ok=True)

@@ -187,3 +187,18 @@ def test_photon_gather_points(small_pair, k):
         print("gather which=%d k=%d: %d nonzero, max rel %.3g" % (which, k, nz, rel.max()))
         assert nz > 100
         assert (rel.max(axis=1) > 1e-4).mean() <= 1e-3
+
+
+def test_image_vs_fp64_reference(gpu_lib, oracle_lib, small_scene_path):
+    # the reference's own arithmetic (double): within 1e-3 relative on all but
+    # a few pixels, and the image's RMSE against it
+    opts = _opts(width=256, height=256)
+    g = gpu_lib.GpuRenderer(**opts)
+    g.load(small_scene_path)
+    img_g = g.render(0)
+    o = oracle_lib.Oracle(fp64=True, rng_mode=1, **opts)
+    o.load(small_scene_path)
+    img_o = o.render(0)
+    d = img_g[..., :3].astype(np.float64) - img_o[..., :3].astype(np.float64)
+    print("small 256^2 vs FP64 oracle: rmse %.3g" % np.sqrt(np.mean(d * d)))
+    assert _compare(img_g, img_o, "small 256^2 vs FP64") <= 1e-3
