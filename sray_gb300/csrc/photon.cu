@@ -606,7 +606,7 @@ static int photon_setup(Renderer &R, int global, cudaStream_t s, int *total_out)
 static int photon_finalize(Renderer &R, int global, int total, cudaStream_t s, int *stored);
 
 /* both photon maps, traced together */
-int photon_shoot_maps(Renderer &R, cudaStream_t s, int *nc, int *ng)
+int photon_shoot_maps(Renderer &R, const DScene &base, cudaStream_t s, int *nc, int *ng)
 {
 	*nc = *ng = 0;
 	int tot[2];
@@ -635,7 +635,7 @@ int photon_shoot_maps(Renderer &R, cudaStream_t s, int *nc, int *ng)
 	if(R.ensure_pqueue(0, all) || R.ensure_pqueue(1, all)) return SRAY_ECUDA;
 	PCK(R.phits.ensure((size_t)all * 16), "photon hits");
 	/* the scene as the photon kernels see it: their counters */
-	DScene PS = R.S;
+	DScene PS = base;
 	PS.bvh_fallbacks = &R.pctr.as<DevCounters>()->bvh_fallbacks;
 	DevCounters *pctr = R.pctr.as<DevCounters>();
 	LAUNCH(R, "photon_emit", s, k_photon_emit<<<grid_n(all, 128), 128, 0, s>>>(PS, PSet, R.pq[0], pctr));

@@ -1180,9 +1180,12 @@ int Renderer::kind_of(const char *name)
 	return (int)ktimes.size() - 1;
 }
 
-void Renderer::prof_begin(int kind, cudaStream_t s, Pending *p)
+void Renderer::prof_begin(const char *name, int *kind_cache, cudaStream_t s, Pending *p)
 {
-	p->kind = kind;
+	std::lock_guard<std::mutex> lk(prof_mu);
+	int k = *kind_cache;
+	if(k < 0 || k >= (int)ktimes.size() || ktimes[k].name != name) *kind_cache = k = kind_of(name);
+	p->kind = k;
 	p->a = p->b = nullptr;
 	launch_count++;
 	if(!(prof_flags & 1)) return;
@@ -1197,14 +1200,16 @@ void Renderer::prof_begin(int kind, cudaStream_t s, Pending *p)
 
 void Renderer::prof_end(Pending *p, cudaStream_t s)
 {
-	if(!(prof_flags & 1)) return;
+	if(!p->b) return;
 	cudaEventRecord(p->b, s);
+	std::lock_guard<std::mutex> lk(prof_mu);
 	pending.push_back(*p);
 }
 
 /* called after a stream synchronisation: every pending pair has completed */
 void Renderer::prof_collect()
 {
+	std::lock_guard<std::mutex> lk(prof_mu);
 	/* pairs on a stream that has not got there yet (the photon stream runs
 	 * beside the render stream) stay pending */
 	size_t keep = 0;
@@ -1533,33 +1538,76 @@ int Renderer::build_frame(long bt0, long bt1, cudaStream_t s)
 	return 0;
 }
 
+/* projection maps and both photon maps on stream s, with the scene view
+ * `base` (the projection-map tables are set in a copy of it); the map
+ * descriptors land in caust.map / gi.map, which fill_scene_desc() copies
+ * into S */
+int Renderer::shoot_maps(const DScene &base, cudaStream_t s, int *nc, int *ng)
+{
+	caust.map.n = 0;
+	gi.map.n = 0;
+	*nc = *ng = 0;
+	if(!(opt.caust_photons || opt.gi_photons) || sc.lights.empty()) return 0;
+	/* projection maps (src/render.cc:87-103) */
+	sc.build_projmaps(t0, t1, opt.seed);
+	std::vector<uint32_t> bits(sc.lights.size() * 128, 0u);
+	std::vector<float> cov(sc.lights.size() * 2);
+	for(size_t i = 0; i < sc.lights.size(); i++) {
+		const Light &L = sc.lights[i];
+		for(int k = 0; k < 2048; k++) {
+			if(L.pm.cells[k]) bits[i * 128 + (k >> 5)] |= 1u << (k & 31);
+			if(L.spm.cells[k]) bits[i * 128 + 64 + (k >> 5)] |= 1u << (k & 31);
+		}
+		cov[i * 2] = (float)L.pm.get_coverage();
+		cov[i * 2 + 1] = (float)L.spm.get_coverage();
+	}
+	CK(projbits.upload(bits, s), "upload projection maps");
+	CK(coverage.upload(cov, s), "upload coverage");
+	h2d += (int64_t)(bits.size() * 4 + cov.size() * 4);
+	DScene D = base;
+	D.projbits = projbits.as<uint32_t>();
+	D.coverage = coverage.as<float>();
+	return photon_shoot_maps(*this, D, s, nc, ng);
+}
+
+int Renderer::photon_job(DScene base)
+{
+	int c = 0, g = 0;
+	return shoot_maps(base, ps, &c, &g);
+}
+
+/* start tracing the photon maps on the photon stream from a host thread of
+ * their own; the render stream s has uploaded the frame's tables (build_frame
+ * synchronised it) */
+int Renderer::start_photon_job(cudaStream_t s)
+{
+	(void)s;
+	int r = photon_stream();
+	if(r) return r;
+	if(photon_thread.joinable()) return fail(SRAY_ESTATE, "photon maps already being traced");
+	photon_rc = 0;
+	DScene base = S;
+	photon_thread = std::thread([this, base]() { photon_rc = photon_job(base); });
+	return 0;
+}
+
+/* wait for the photon maps; the scene view then carries them */
+int Renderer::finish_photon_job()
+{
+	if(!photon_thread.joinable()) return 0;
+	photon_thread.join();
+	if(photon_rc) return photon_rc;
+	photons_ready = true;
+	fill_scene_desc();
+	return 0;
+}
+
 int Renderer::shoot(cudaStream_t s, int *nc, int *ng)
 {
 	if(!built) return fail(SRAY_ESTATE, "acceleration structures not built");
-	caust.map.n = 0;
-	gi.map.n = 0;
 	int c = 0, g = 0;
-	if((opt.caust_photons || opt.gi_photons) && !sc.lights.empty()) {
-		/* projection maps (src/render.cc:87-103) */
-		sc.build_projmaps(t0, t1, opt.seed);
-		std::vector<uint32_t> bits(sc.lights.size() * 128, 0u);
-		std::vector<float> cov(sc.lights.size() * 2);
-		for(size_t i = 0; i < sc.lights.size(); i++) {
-			const Light &L = sc.lights[i];
-			for(int k = 0; k < 2048; k++) {
-				if(L.pm.cells[k]) bits[i * 128 + (k >> 5)] |= 1u << (k & 31);
-				if(L.spm.cells[k]) bits[i * 128 + 64 + (k >> 5)] |= 1u << (k & 31);
-			}
-			cov[i * 2] = (float)L.pm.get_coverage();
-			cov[i * 2 + 1] = (float)L.spm.get_coverage();
-		}
-		CK(projbits.upload(bits, s), "upload projection maps");
-		CK(coverage.upload(cov, s), "upload coverage");
-		h2d += (int64_t)(bits.size() * 4 + cov.size() * 4);
-		fill_scene_desc();
-		int r = photon_shoot_maps(*this, s, &c, &g);
-		if(r) return r;
-	}
+	int r = shoot_maps(S, s, &c, &g);
+	if(r) return r;
 	photons_ready = true;
 	fill_scene_desc();
 	if(nc) *nc = c;
@@ -1900,6 +1948,31 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 	long long l0 = launch_count;
 	memset(&stats, 0, sizeof stats);
 	int n_active = npix;
+	/* the photon thread is always joined before this returns */
+	struct PhotonJoin {
+		Renderer *R;
+		~PhotonJoin() { if(R->photon_thread.joinable()) R->photon_thread.join(); }
+	} photon_join{this};
+	/* While the photon maps are traced (on the photon stream, from a host
+	 * thread of their own), the first sample batch's bounces go on and their
+	 * photon-map gathers accumulate in gq; they run in one launch once the
+	 * maps exist (before the shading tail, at the latest at the end of the
+	 * batch).  gq_upper bounds the gathers queued so far (a shaded ray asks
+	 * for at most one). */
+	bool deferring = false;
+	int64_t gq_upper = 0, gq_defer_cap = 0;
+	auto flush_gathers = [&]() -> int {
+		if(!deferring) return 0;
+		deferring = false;
+		int r = finish_photon_job();
+		if(r) return r;
+		if(gq_upper > 0)
+			LAUNCH(*this, "gather", s, k_gather<<<grid_for((int)gq_upper, GATHER_WARPS), GATHER_WARPS * 32, 0, s>>>(S,
+					gq.as<GatherReq>(), cnt + 2, acc.as<float4>(), ctr.as<DevCounters>()));
+		gq_upper = 0;
+		CK(cudaMemsetAsync(cnt + 2, 0, sizeof(int), s), "reset gather queue");
+		return 0;
+	};
 	/* sample batches: the first covers the samples every pixel takes before
 	 * its first variance test, the second all the remaining samples of the
 	 * pixels still running (rendered speculatively, cut by k_finish) */
@@ -1917,6 +1990,17 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 		if(ensure_queue(0, n_prim)) return SRAY_ECUDA;
 		CK(acc.ensure((size_t)n_prim * 16), "accumulator");
 		if(int r = nrc_setup(b, n_prim, s)) return r;
+		if(photons_pending) {
+			photons_pending = false;
+			int64_t cap = (int64_t)n_prim * 3 + 65536;
+			if(cap > INT_MAX / 2) cap = INT_MAX / 2;
+			CK(gq.ensure((size_t)cap * sizeof(GatherReq)), "gather queue");
+			CK(cudaMemsetAsync(cnt + 2, 0, sizeof(int), s), "reset gather queue");
+			if(int r = start_photon_job(s)) return r;
+			deferring = true;
+			gq_defer_cap = cap;
+			gq_upper = 0;
+		}
 		q[0].count = cnt + 0;
 		q[1].count = cnt + 1;
 		LAUNCH(*this, "camera", s, k_camera<<<grid_for(n_prim, 256), 256, 0, s>>>(S, act, act_count, s0, width, q[0], acc.as<float4>(),
@@ -1928,6 +2012,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			if(depth >= 1 && !tail_done && n_rays <= RENDER_TAIL) {
 				/* the rest of the shading tree in one launch (k_render_pool) */
 				tail_done = true;
+				if(int r = flush_gathers()) return r;
 				q[0].count = cnt + 0;
 				q[1].count = cnt + 1;
 				CK(cudaMemsetAsync(q[cur ^ 1].count, 0, sizeof(int), s), "reset queue");
@@ -1975,11 +2060,14 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			int r = ensure_queue(cur ^ 1, need);
 			if(r) return r;
 			CK(hits.ensure((size_t)n_rays * 16), "hits");
-			CK(gq.ensure((size_t)n_rays * sizeof(GatherReq)), "gather queue");
+			if(deferring && gq_upper + n_rays > gq_defer_cap && (r = flush_gathers())) return r;
+			if(!deferring) {
+				CK(gq.ensure((size_t)n_rays * sizeof(GatherReq)), "gather queue");
+				CK(cudaMemsetAsync(cnt + 2, 0, sizeof(int), s), "reset gather queue");
+			}
 			q[0].count = cnt + 0;
 			q[1].count = cnt + 1;
 			CK(cudaMemsetAsync(q[cur ^ 1].count, 0, sizeof(int), s), "reset queue");
-			CK(cudaMemsetAsync(cnt + 2, 0, sizeof(int), s), "reset gather queue");
 			CK(cudaMemsetAsync(cnt + 5, 0, sizeof(int), s), "reset shadow queue");
 			CK(sq.ensure((size_t)n_rays * shadow_per_ray * sizeof(ShadowReq)), "shadow queue");
 			r = trace_rays(q[cur], n_rays, "trace", (prof_flags & 2) != 0, s);
@@ -1988,7 +2076,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			so.qo = q[cur ^ 1];
 			so.gq = gq.as<GatherReq>();
 			so.gq_count = cnt + 2;
-			so.gq_cap = n_rays;
+			so.gq_cap = deferring ? (int)gq_defer_cap : n_rays;
 			so.sq = sq.as<ShadowReq>();
 			so.sq_count = cnt + 5;
 			so.sq_cap = n_rays * shadow_per_ray;
@@ -2000,16 +2088,11 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 					acc.as<float4>(), ctr.as<DevCounters>(), fbl.as<int>()));
 			LAUNCH(*this, "octree_retrace", s, k_shadow<false><<<152, 128, 0, s>>>(S, sq.as<ShadowReq>(), cnt + 5, acc.as<float4>(),
 					ctr.as<DevCounters>(), fbl.as<int>()));
-			if(photons_pending) {
-				/* the first gathers need the photon maps: trace them on the
-				 * photon stream now, while this bounce's closest hits,
-				 * shading and shadow rays run, and make the render stream
-				 * wait for them */
-				photons_pending = false;
-				if((r = shoot_on_photon_stream(s))) return r;
-			}
-			LAUNCH(*this, "gather", s, k_gather<<<grid_for(n_rays, GATHER_WARPS), GATHER_WARPS * 32, 0, s>>>(S, gq.as<GatherReq>(), cnt + 2,
-					acc.as<float4>(), ctr.as<DevCounters>()));
+			if(deferring)
+				gq_upper += n_rays;
+			else
+				LAUNCH(*this, "gather", s, k_gather<<<grid_for(n_rays, GATHER_WARPS), GATHER_WARPS * 32, 0, s>>>(S, gq.as<GatherReq>(),
+						cnt + 2, acc.as<float4>(), ctr.as<DevCounters>()));
 			stats.secondary_rays += depth ? n_rays : 0;
 			int h_cnt = 0;
 			CK(cudaMemcpyAsync(&h_cnt, q[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "read queue count");
@@ -2019,6 +2102,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			n_rays = h_cnt;
 			cur ^= 1;
 		}
+		if(int r = flush_gathers()) return r;
 		if(int r = nrc_batch_done(b, s)) return r;
 		CK(cudaMemsetAsync(next_count, 0, sizeof(int), s), "reset next active");
 		LAUNCH(*this, "finish", s, k_finish<<<grid_for(n_active, 256), 256, 0, s>>>(act, act_count, s0, width, acc.as<float4>(),
@@ -2033,7 +2117,8 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 		n_active = h_next;
 	}
 	if(photons_pending) {
-		int r = shoot_on_photon_stream(s);
+		/* no sample batch ran: the maps are still the frame's */
+		int r = shoot(s, nullptr, nullptr);
 		if(r) return r;
 	}
 	DevCounters hc;
@@ -2099,18 +2184,6 @@ int Renderer::photon_stream()
 	if(ps) return 0;
 	CK(cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking), "photon stream");
 	CK(cudaEventCreateWithFlags(&ps_done, cudaEventDisableTiming), "photon event");
-	return 0;
-}
-
-/* photon maps on the photon stream; the render stream s waits for them */
-int Renderer::shoot_on_photon_stream(cudaStream_t s)
-{
-	int r = photon_stream();
-	if(r) return r;
-	/* the frame's tables were uploaded on s, which build_frame synchronised */
-	if((r = shoot(ps, nullptr, nullptr))) return r;
-	CK(cudaEventRecord(ps_done, ps), "photon event");
-	CK(cudaStreamWaitEvent(s, ps_done, 0), "wait for photon maps");
 	return 0;
 }
 
@@ -2513,6 +2586,7 @@ int sray_gpu_kernel_times(char *names, size_t names_cap, double *ms, int64_t *la
 {
 	NEED_CTX();
 	Renderer &R = *g_R;
+	std::lock_guard<std::mutex> lk(R.prof_mu);
 	int n = (int)R.ktimes.size();
 	if(n_out) *n_out = n;
 	size_t off = 0;
@@ -2545,6 +2619,7 @@ void sray_gpu_shutdown(void)
 	std::lock_guard<std::mutex> lk(g_mu);
 	if(!g_R) return;
 	Renderer &R = *g_R;
+	if(R.photon_thread.joinable()) R.photon_thread.join();
 	DevBuf *bufs[] = {&R.mnodes, &R.mtris, &R.mprim, &R.tri_pos, &R.tri_attr, &R.objs, &R.mats, &R.lights, &R.snodes, &R.sslots,
 		&R.xf, &R.light_pos, &R.cam_m, &R.projbits, &R.coverage, &R.qbuf[0], &R.qbuf[1], &R.hits, &R.gq, &R.sq, &R.acc, &R.hist, &R.sums,
 		&R.active[0], &R.active[1], &R.spp, &R.fbdev, &R.ctr, &R.counts, &R.bnodes, &R.btris, &R.bprim, &R.bhome,

@@ -4,6 +4,9 @@
 
 #include <string>
 #include <vector>
+#include <atomic>
+#include <mutex>
+#include <thread>
 #include <cuda_runtime.h>
 #include "sray_gpu.h"
 #include "scene_host.h"
@@ -142,19 +145,32 @@ struct Renderer {
 	int nrc_batch_done(int batch, cudaStream_t s);
 	int nrc_reset_regions(cudaStream_t s);
 
-	/* profiling: event pairs per launch, resolved after each synchronisation */
+	/* profiling: event pairs per launch, resolved after each synchronisation.
+	 * The photon maps are traced by a host thread of their own beside the
+	 * render loop, so the bookkeeping is locked and the byte counters are
+	 * atomic. */
 	int prof_flags = 0;
 	long long launch_count = 0;
-	int64_t h2d = 0, d2h = 0;     /* host<->device bytes since the last reset */
+	std::atomic<int64_t> h2d{0}, d2h{0};   /* host<->device bytes since the last reset */
 	struct KTime { std::string name; double ms = 0.0; long long launches = 0; };
 	std::vector<KTime> ktimes;
 	struct Pending { int kind; cudaEvent_t a, b; };
 	std::vector<Pending> pending;
 	std::vector<cudaEvent_t> event_pool;
+	std::mutex prof_mu;
 	int kind_of(const char *name);
-	void prof_begin(int kind, cudaStream_t s, Pending *p);
+	void prof_begin(const char *name, int *kind_cache, cudaStream_t s, Pending *p);
 	void prof_end(Pending *p, cudaStream_t s);
 	void prof_collect();
+
+	/* the photon maps of a frame, traced by a host thread on the photon
+	 * stream while the render loop goes on; the photon-map gathers wait */
+	std::thread photon_thread;
+	int photon_rc = 0;
+	int start_photon_job(cudaStream_t s);
+	int finish_photon_job();
+	int photon_job(DScene base);
+	int shoot_maps(const DScene &base, cudaStream_t s, int *nc, int *ng);
 
 	int fail(int code, const std::string &msg) { err = msg; return code; }
 	int cuda_fail(cudaError_t e, const char *where)
@@ -177,14 +193,12 @@ struct Renderer {
 	int trace_rays_with(const DScene &D, const RayQueue &q, int n, const char *name, bool count, cudaStream_t s, int4 *hit_out,
 			DevBuf &fb, DevCounters *c);
 	int photon_stream();
-	int shoot_on_photon_stream(cudaStream_t s);
 	void fill_scene_desc();
 };
 
 #define LAUNCH(R_, kname_, s_, ...) do { \
 		static thread_local int kind_ = -1; \
-		if(kind_ < 0 || kind_ >= (int)(R_).ktimes.size() || (R_).ktimes[kind_].name != kname_) kind_ = (R_).kind_of(kname_); \
-		Renderer::Pending pend_; (R_).prof_begin(kind_, s_, &pend_); \
+		Renderer::Pending pend_; (R_).prof_begin(kname_, &kind_, s_, &pend_); \
 		__VA_ARGS__; \
 		(R_).prof_end(&pend_, s_); \
 	} while(0)
@@ -192,8 +206,8 @@ struct Renderer {
 /* render.cu: closest hits of the first n rays of q into R.hits */
 int launch_trace(Renderer &R, const DScene &D, const RayQueue &q, int n, const char *name, cudaStream_t s);
 
-/* photon.cu */
-int photon_shoot_maps(Renderer &R, cudaStream_t s, int *caust_stored, int *gi_stored);
+/* photon.cu: both maps traced with the scene view `base` */
+int photon_shoot_maps(Renderer &R, const DScene &base, cudaStream_t s, int *caust_stored, int *gi_stored);
 
 }  // namespace sray
 
