@@ -252,6 +252,36 @@ int sray_gpu_set_profiling(int flags);
 int sray_gpu_kernel_times(char *names, size_t names_cap, double *ms, int64_t *launches, int max,
 		int *n_out, int reset);
 
+/* Scheduler tuning (extension, no reference counterpart; the reference's
+ * scheduler is a thread pool over 48x48 tiles, src/tpool.cc:48-225).  The
+ * queue depths at which a wavefront's tail is handed to a persistent launch,
+ * and that launch's size. */
+typedef struct sray_tuning {
+	int render_tail;          /* rays in flight below which the rest of the shading tree
+	                             runs in the persistent pool launch (32768) */
+	int pool_blocks_per_sm;   /* 128-thread blocks per SM of the pool launch (4) */
+	int photon_tail;          /* photons in flight below which the photon tail runs in one
+	                             persistent launch (65536) */
+	int reserved[5];
+} sray_tuning;
+
+typedef struct sray_tune_trial {
+	sray_tuning tuning;
+	float ms_per_frame;       /* mean over the trial's timed frames */
+	int pad;
+} sray_tune_trial;
+
+int sray_gpu_get_tuning(sray_tuning *t);
+int sray_gpu_set_tuning(const sray_tuning *t);
+
+/* The autotuner: renders frame `msec` into the device framebuffer `fb` on
+ * `stream` under candidate tunings (coordinate descent over the fields of
+ * sray_tuning, one warm-up and `frames` timed frames each, CUDA-event
+ * timing), keeps the fastest and returns it with its time.  Every trial goes
+ * into `log` (up to `log_cap`, count through `n_log`). */
+int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tuning *best, float *best_ms,
+		sray_tune_trial *log, int log_cap, int *n_log);
+
 /* Copy the last error message (NUL-terminated, truncated to `cap`). */
 int sray_gpu_last_error(char *buf, size_t cap);
 

@@ -200,7 +200,6 @@ __device__ bool gen_dir(const uint32_t *bits, sray_rng *s, V3 *out)
  * caustic map, map 1 the global one. */
 
 #define PHOTON_GUARD 4096   /* interactions per phase (loop bound of the oracle's tracer) */
-#define PHOTON_FINISH 65536 /* live photons below which the tail is traced in one launch */
 
 /* the two maps being traced: emission counts, per-light prefix sums and
  * power scales, and the per-photon output */
@@ -645,7 +644,7 @@ int photon_shoot_maps(Renderer &R, const DScene &base, cudaStream_t s, int *nc, 
 	for(int pass = 0; n_live > 0; pass++) {
 		if(pass >= 2 * PHOTON_GUARD + 4) return R.fail(SRAY_EDEVICE, "photon paths did not terminate");
 		PCK(cudaMemsetAsync(R.pq[cur ^ 1].count, 0, sizeof(int), s), "reset photon queue");
-		if(!finished && pass > 0 && n_live <= PHOTON_FINISH) {
+		if(!finished && pass > 0 && n_live <= R.tune.photon_tail) {
 			/* the tail in one launch; what it hands back continues pass-wise */
 			finished = true;
 			PCK(cudaMemsetAsync(cnt + 2, 0, sizeof(int), s), "reset photon tail counter");

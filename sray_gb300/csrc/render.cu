@@ -517,7 +517,8 @@ __global__ void __launch_bounds__(128) k_shade(DScene S, RayQueue qi, const int4
 	if(overflow) atomicOr(&ctr->overflow, 1);
 }
 
-/* The tail of the shading tree.  Past the first bounces few rays are left,
+/* The tail of the shading tree (below tune.render_tail rays in flight).
+ * Past the first bounces few rays are left,
  * on long and branching paths (chains through glass and mirrors), and a
  * pass costs as much as its slowest ray.  k_render_pool runs the rest of the
  * tree in one launch over a shared pool of rays: the queue's rays occupy
@@ -536,8 +537,8 @@ __global__ void __launch_bounds__(128) k_shade(DScene S, RayQueue qi, const int4
  * whose slot is beyond every reservation leaves once no ray is in flight
  * (no more can come); every wait is bounded and sets the error word when
  * it runs out. */
-#define RENDER_TAIL 32768         /* rays below which the rest of the tree runs in k_render_pool */
 #define POOL_SPIN_LIMIT (1 << 22) /* polls of a slot before the pool gives up (about 0.5 s) */
+#define POOL_HEADROOM 64          /* pool slots per ray it starts with */
 #define POOL_SHADOW (-0x7ffffff0)   /* iter of a pool item that is a light sample's shadow ray */
 
 __device__ __forceinline__ void load_ray_l2(const RayQueue &q, int i, RayRec &r)
@@ -2009,7 +2010,9 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 		int cur = 0;
 		bool tail_done = false;
 		for(int depth = 0; n_rays > 0; depth++) {
-			if(depth >= 1 && !tail_done && n_rays <= RENDER_TAIL) {
+			/* the pool holds every ray of the rest of the tree: enter it only
+			 * with POOL_HEADROOM times the rays' room in the queue */
+			if(depth >= 1 && !tail_done && n_rays <= tune.render_tail && (int64_t)n_rays * POOL_HEADROOM <= q[cur].cap) {
 				/* the rest of the shading tree in one launch (k_render_pool) */
 				tail_done = true;
 				if(int r = flush_gathers()) return r;
@@ -2034,7 +2037,8 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 				so.sq = sq.as<ShadowReq>();
 				so.sq_count = cnt + 5;
 				so.sq_cap = (int)std::min<size_t>(sq.bytes / sizeof(ShadowReq), (size_t)INT_MAX);
-				LAUNCH(*this, "render_pool", s, k_render_pool<<<152 * 4, 128, 0, s>>>(S, q[cur], pool_ready.as<int>(), ctl, so,
+				LAUNCH(*this, "render_pool", s, k_render_pool<<<nsm * tune.pool_blocks_per_sm, 128, 0, s>>>(S, q[cur],
+						pool_ready.as<int>(), ctl, so,
 						acc.as<float4>(), ctr.as<DevCounters>()));
 				CK(fbl.ensure(((size_t)so.sq_cap + 1) * sizeof(int)), "fallback list");
 				CK(cudaMemsetAsync(fbl.p, 0, sizeof(int), s), "reset fallback list");
@@ -2256,6 +2260,7 @@ int sray_gpu_init(const sray_opts *opt)
 	g_R = new Renderer;
 	g_R->opt = *opt;
 	g_R->device = dev;
+	if(cudaDeviceGetAttribute(&g_R->nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || g_R->nsm <= 0) g_R->nsm = 152;
 	memset(&g_R->stats, 0, sizeof g_R->stats);
 	return 0;
 }
@@ -2355,21 +2360,126 @@ int sray_gpu_render_pixels(long msec, float *fb, int fb_is_device, void *stream)
 	return r;
 }
 
+static int render_frame(Renderer &R, long msec, float *fb, int fb_is_device, cudaStream_t s)
+{
+	long t0, t1;
+	frame_interval(R, msec, &t0, &t1);
+	long long l0 = R.launch_count;
+	R.h2d = R.d2h = 0;
+	int r = R.build_frame(t0, t1, s);
+	if(!r) r = R.render_pixels(msec, fb, fb_is_device, s, true);
+	if(r) g_err = R.err;
+	else R.stats.kernel_launches = (int)(R.launch_count - l0);
+	return r;
+}
+
 int sray_gpu_render(long msec, float *fb, int fb_is_device, void *stream)
 {
 	NEED_CTX();
 	Renderer &R = *g_R;
 	if(!R.loaded) { g_err = "no scene loaded"; return SRAY_ESTATE; }
 	if(!fb) { g_err = "null framebuffer"; return SRAY_EINVAL; }
-	long t0, t1;
-	frame_interval(R, msec, &t0, &t1);
-	long long l0 = R.launch_count;
-	R.h2d = R.d2h = 0;
-	int r = R.build_frame(t0, t1, as_stream(stream));
-	if(!r) r = R.render_pixels(msec, fb, fb_is_device, as_stream(stream), true);
-	if(r) g_err = R.err;
-	else R.stats.kernel_launches = (int)(R.launch_count - l0);
-	return r;
+	return render_frame(R, msec, fb, fb_is_device, as_stream(stream));
+}
+
+static int check_tuning(const sray_tuning *t)
+{
+	if(!t) { g_err = "null tuning"; return SRAY_EINVAL; }
+	if(t->render_tail < 0 || t->render_tail > (1 << 26)) { g_err = "render_tail must be 0..2^26"; return SRAY_EINVAL; }
+	if(t->pool_blocks_per_sm < 1 || t->pool_blocks_per_sm > 16) { g_err = "pool_blocks_per_sm must be 1..16"; return SRAY_EINVAL; }
+	if(t->photon_tail < 0 || t->photon_tail > (1 << 26)) { g_err = "photon_tail must be 0..2^26"; return SRAY_EINVAL; }
+	return 0;
+}
+
+int sray_gpu_get_tuning(sray_tuning *t)
+{
+	NEED_CTX();
+	if(!t) { g_err = "null tuning"; return SRAY_EINVAL; }
+	*t = g_R->tune;
+	return 0;
+}
+
+int sray_gpu_set_tuning(const sray_tuning *t)
+{
+	NEED_CTX();
+	int r = check_tuning(t);
+	if(r) return r;
+	g_R->tune = *t;
+	return 0;
+}
+
+/* Coordinate descent over the tunables: each field in turn takes each of
+ * its candidate values with the others at the best found so far; a trial is
+ * one warm-up frame and `frames` frames timed with CUDA events on the
+ * stream.  Trials already measured are not repeated. */
+int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tuning *best, float *best_ms,
+		sray_tune_trial *log, int log_cap, int *n_log)
+{
+	NEED_CTX();
+	Renderer &R = *g_R;
+	if(!R.loaded) { g_err = "no scene loaded"; return SRAY_ESTATE; }
+	if(!fb || frames < 1) { g_err = "bad arguments"; return SRAY_EINVAL; }
+	cudaStream_t s = as_stream(stream);
+	static const int tails[] = {8192, 32768, 131072};
+	static const int pools[] = {2, 4, 8, 16};
+	static const int ptails[] = {16384, 65536, 262144};
+	struct Knob { int sray_tuning::*field; const int *vals; int n; };
+	const Knob knobs[] = {{&sray_tuning::render_tail, tails, 3}, {&sray_tuning::pool_blocks_per_sm, pools, 4},
+		{&sray_tuning::photon_tail, ptails, 3}};
+	std::vector<sray_tune_trial> done;
+	cudaEvent_t e0, e1;
+	if(cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) { g_err = "autotune events"; return SRAY_ECUDA; }
+	auto trial = [&](const sray_tuning &t, float *ms) -> int {
+		for(const sray_tune_trial &d : done) {
+			if(d.tuning.render_tail == t.render_tail && d.tuning.pool_blocks_per_sm == t.pool_blocks_per_sm &&
+					d.tuning.photon_tail == t.photon_tail) {
+				*ms = d.ms_per_frame;
+				return 0;
+			}
+		}
+		R.tune = t;
+		int r = render_frame(R, msec, fb, 1, s);
+		if(r) return r;
+		cudaEventRecord(e0, s);
+		for(int i = 0; i < frames && !r; i++) r = render_frame(R, msec, fb, 1, s);
+		cudaEventRecord(e1, s);
+		if(r) return r;
+		if(cudaEventSynchronize(e1) != cudaSuccess) { g_err = "autotune timing"; return SRAY_ECUDA; }
+		float t_ms = 0.0f;
+		cudaEventElapsedTime(&t_ms, e0, e1);
+		sray_tune_trial tr;
+		memset(&tr, 0, sizeof tr);
+		tr.tuning = t;
+		tr.ms_per_frame = t_ms / (float)frames;
+		done.push_back(tr);
+		*ms = tr.ms_per_frame;
+		return 0;
+	};
+	sray_tuning cur = R.tune;
+	float cur_ms = 0.0f;
+	int r = trial(cur, &cur_ms);
+	for(const Knob &k : knobs) {
+		for(int i = 0; i < k.n && !r; i++) {
+			sray_tuning t = cur;
+			t.*(k.field) = k.vals[i];
+			float ms = 0.0f;
+			r = trial(t, &ms);
+			if(!r && ms < cur_ms) {
+				cur = t;
+				cur_ms = ms;
+			}
+		}
+		if(r) break;
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	R.tune = cur;
+	if(r) return r;
+	if(best) *best = cur;
+	if(best_ms) *best_ms = cur_ms;
+	if(n_log) *n_log = (int)done.size();
+	for(int i = 0; log && i < log_cap && i < (int)done.size(); i++) log[i] = done[i];
+	return 0;
 }
 
 int sray_gpu_cast_rays(int n, const float *orig, const float *dir, const int *time, int *obj, int *prim, float *t,

@@ -131,6 +131,8 @@ struct Renderer {
 	cudaStream_t ps = nullptr;
 	cudaEvent_t ps_done = nullptr;
 	sray_stats stats;
+	sray_tuning tune = {32768, 4, 65536, {0, 0, 0, 0, 0}};
+	int nsm = 0;                  /* multiprocessors of the device */
 
 	/* radiance cache: queries (inputs, weight + slot), training and
 	 * validation records (inputs, targets, predictions), region statistics */

@@ -18,7 +18,8 @@ EXPORTS = ["sray_default_opts", "sray_gpu_init", "sray_gpu_set_opts", "sray_gpu_
            "sray_gpu_scene_info", "sray_gpu_build", "sray_gpu_shoot_photons", "sray_gpu_render",
            "sray_gpu_render_pixels", "sray_gpu_cast_rays", "sray_gpu_primary_hits", "sray_gpu_photon_gather", "sray_gpu_photon_gather_noalloc",
            "sray_gpu_get_photons",
-           "sray_gpu_get_stats", "sray_gpu_nrc_stats", "sray_gpu_nrc_reset", "sray_gpu_set_profiling", "sray_gpu_kernel_times", "sray_gpu_last_error",
+           "sray_gpu_get_stats", "sray_gpu_nrc_stats", "sray_gpu_nrc_reset", "sray_gpu_get_tuning",
+           "sray_gpu_set_tuning", "sray_gpu_autotune", "sray_gpu_set_profiling", "sray_gpu_kernel_times", "sray_gpu_last_error",
            "sray_gpu_shutdown", "sray_nrc_reset", "sray_nrc_set_params", "sray_nrc_get_params", "sray_nrc_infer",
            "sray_nrc_gradients", "sray_nrc_train", "sray_nrc_last_error"]
 
@@ -45,6 +46,19 @@ class SrayNrcStats(ctypes.Structure):
                 ("regions", ctypes.c_int), ("regions_validated", ctypes.c_int), ("regions_cached", ctypes.c_int),
                 ("val_rel_err", ctypes.c_float), ("loss", ctypes.c_float), ("pad", ctypes.c_int),
                 ("reserved", ctypes.c_int64 * 4)]
+
+
+class SrayTuning(ctypes.Structure):
+    _fields_ = [("render_tail", ctypes.c_int), ("pool_blocks_per_sm", ctypes.c_int), ("photon_tail", ctypes.c_int),
+                ("reserved", ctypes.c_int * 5)]
+
+
+class SrayTuneTrial(ctypes.Structure):
+    _fields_ = [("tuning", SrayTuning), ("ms_per_frame", ctypes.c_float), ("pad", ctypes.c_int)]
+
+
+def _tuning_dict(t):
+    return {f[0]: getattr(t, f[0]) for f in SrayTuning._fields_ if f[0] != "reserved"}
 
 
 class SrayError(RuntimeError):
@@ -82,6 +96,10 @@ def load_library():
     L.sray_gpu_get_stats.argtypes = [ctypes.POINTER(SrayStats)]
     L.sray_gpu_nrc_stats.argtypes = [ctypes.POINTER(SrayNrcStats)]
     L.sray_gpu_nrc_reset.argtypes = [ctypes.c_uint64]
+    L.sray_gpu_get_tuning.argtypes = [ctypes.POINTER(SrayTuning)]
+    L.sray_gpu_set_tuning.argtypes = [ctypes.POINTER(SrayTuning)]
+    L.sray_gpu_autotune.argtypes = [lp, vp, ip, vp, ctypes.POINTER(SrayTuning), ctypes.POINTER(ctypes.c_float),
+                                    ctypes.POINTER(SrayTuneTrial), ip, ctypes.POINTER(ctypes.c_int)]
     L.sray_gpu_set_profiling.argtypes = [ip]
     L.sray_gpu_kernel_times.argtypes = [ctypes.c_char_p, ctypes.c_size_t, vp, vp, ip, vp, ip]
     L.sray_gpu_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
@@ -263,6 +281,30 @@ class GpuRenderer:
     def nrc_reset(self, seed=None):
         """Re-initialise the network and forget the regions' validation history."""
         self._chk(self.L.sray_gpu_nrc_reset(self.opts.seed if seed is None else seed))
+
+    def tuning(self):
+        t = SrayTuning()
+        self._chk(self.L.sray_gpu_get_tuning(ctypes.byref(t)))
+        return _tuning_dict(t)
+
+    def set_tuning(self, **kw):
+        t = SrayTuning()
+        self._chk(self.L.sray_gpu_get_tuning(ctypes.byref(t)))
+        for k, v in kw.items():
+            setattr(t, k, v)
+        self._chk(self.L.sray_gpu_set_tuning(ctypes.byref(t)))
+
+    def autotune(self, fb, msec=0, frames=3, stream=None):
+        """Pick the fastest tuning for frame `msec` (device framebuffer `fb`);
+        returns (tuning, ms per frame, [(tuning, ms) per trial])."""
+        best = SrayTuning()
+        ms = ctypes.c_float()
+        log = (SrayTuneTrial * 64)()
+        n = ctypes.c_int()
+        self._chk(self.L.sray_gpu_autotune(msec, _ptr(fb), frames, _stream(stream), ctypes.byref(best), ctypes.byref(ms),
+                                           log, 64, ctypes.byref(n)))
+        trials = [(_tuning_dict(log[i].tuning), log[i].ms_per_frame) for i in range(min(n.value, 64))]
+        return _tuning_dict(best), ms.value, trials
 
     def set_profiling(self, time_kernels=False, count_work=False):
         self._chk(self.L.sray_gpu_set_profiling((1 if time_kernels else 0) | (2 if count_work else 0)))

@@ -202,3 +202,23 @@ def test_image_vs_fp64_reference(gpu_lib, oracle_lib, small_scene_path):
     d = img_g[..., :3].astype(np.float64) - img_o[..., :3].astype(np.float64)
     print("small 256^2 vs FP64 oracle: rmse %.3g" % np.sqrt(np.mean(d * d)))
     assert _compare(img_g, img_o, "small 256^2 vs FP64") <= 1e-3
+
+
+def test_autotuner_keeps_the_image(gpu_lib, small_scene_path):
+    # the tunables only move work between launches: the image is the same
+    opts = _opts(width=128, height=128, max_samples=4, max_var=0.0005)
+    g = gpu_lib.GpuRenderer(**opts)
+    g.load(small_scene_path)
+    fb = torch.zeros((128, 128, 4), dtype=torch.float32, device="cuda")
+    g.render(0, fb)
+    ref = fb.cpu().numpy().copy()
+    best, ms, trials = g.autotune(fb, frames=1)
+    print("autotuner: %d trials, best %s at %.3f ms" % (len(trials), best, ms))
+    assert len(trials) >= 8 and ms > 0.0
+    assert g.tuning() == best
+    g.set_tuning(render_tail=1 << 20, pool_blocks_per_sm=1, photon_tail=0)
+    g.render(0, fb)
+    assert np.abs(fb.cpu().numpy() - ref).max() <= 1e-5
+    g.set_tuning(render_tail=0, pool_blocks_per_sm=16, photon_tail=1 << 20)
+    g.render(0, fb)
+    assert np.abs(fb.cpu().numpy() - ref).max() <= 1e-5
