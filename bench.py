@@ -45,9 +45,12 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="production", choices=["production", "small", "learned"])
     ap.add_argument("--no-nrc", action="store_true", help="skip the radiance-cache comparison")
-    ap.add_argument("--method", default="plain", choices=["plain", "cache"],
-                    help="final gather of the headline frames: the plain gather or the radiance cache")
+    ap.add_argument("--method", default="plain", choices=["plain", "cache", "cache-everywhere"],
+                    help="final gather of the headline frames: the plain gather, the radiance cache with its "
+                         "per-region fallback, or the cache in every region")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default scheduler tuning")
+    ap.add_argument("--tuning", default=None,
+                    help="render_tail,pool_blocks_per_sm,photon_tail: set the scheduler tuning instead of autotuning")
     ap.add_argument("--nrc-burn-in", type=int, default=600, help="frames of online training before the cache is timed")
     ap.add_argument("--nrc-ladder", default="1,2,4,8,16,32,64,128",
                     help="diffuse samples per vertex of the plain final gather, compared with the cache")
@@ -67,8 +70,9 @@ def config_opts(args):
     if args.photon_scale != 1.0:
         opts["caust_photons"] = int(opts["caust_photons"] * args.photon_scale)
         opts["gi_photons"] = int(opts["gi_photons"] * args.photon_scale)
-    if getattr(args, "method", "plain") == "cache":
-        opts["nrc"] = 1
+    method = getattr(args, "method", "plain")
+    if method != "plain":
+        opts["nrc"] = 1 if method == "cache" else 2
     return opts
 
 
@@ -313,6 +317,11 @@ def nrc_vs_plain(args, reference):
             return None
         return image_rmse(fb.cpu().numpy(), reference[0], reference[1])
 
+    tuning = None
+    if not args.no_autotune:
+        g.set_opts(nrc=0, diffuse_samples=1)
+        best, best_ms, _ = g.autotune(fb, frames=3, stream=stream)
+        tuning = dict(best, ms_per_frame=best_ms)
     ladder = []
     for ds in [int(x) for x in args.nrc_ladder.split(",") if x]:
         g.set_opts(nrc=0, diffuse_samples=ds)
@@ -320,7 +329,7 @@ def nrc_vs_plain(args, reference):
             g.render(0, fb, stream=stream)
         ms, mr = timed(steps)
         ladder.append({"diffuse_samples": ds, "ms_per_frame": ms, "mrays_per_s": mr, "rmse": err()})
-    out = {"workload": workload_desc("learned"), "plain": ladder,
+    out = {"workload": workload_desc("learned"), "tuning": tuning, "plain": ladder,
            "reference": None if reference is None else
            "FP64 CPU oracle, %d final-gather rays per vertex, %d rows in %d bands" % (REF_DS, len(reference[1]), REF_BANDS)}
     g.set_opts(nrc=1, diffuse_samples=1)
@@ -424,8 +433,11 @@ def run_ours(args):
     device_mb = (free0 - torch.cuda.mem_get_info()[0]) / 1e6
 
     # the library's autotuner picks the scheduler's queue depths (untimed setup)
+    if args.tuning:
+        rt, pb, pt = [int(v) for v in args.tuning.split(",")]
+        g.set_tuning(render_tail=rt, pool_blocks_per_sm=pb, photon_tail=pt)
     tuning = {"chosen": g.tuning(), "autotuned": False}
-    if not args.no_autotune:
+    if not args.no_autotune and not args.tuning:
         best, best_ms, trials = g.autotune(fb, frames=3, stream=stream)
         tuning = {"chosen": best, "autotuned": True, "best_ms_per_frame": best_ms, "frames_per_trial": 3,
                   "trials": [dict(t, ms=round(ms, 3)) for t, ms in trials]}
@@ -466,6 +478,7 @@ def run_ours(args):
     kt = g.kernel_times(reset=True)
     st_last = st
     ms_step = ms_total / args.steps
+    g_nrc_stats = g.nrc_stats() if opts.get("nrc") else None
 
     # end to end through the C-ABI with a host framebuffer
     g.set_profiling(False, False)
@@ -571,7 +584,8 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator, no dataset)",
             "config": {"workload": workload_desc(args.config) + ("" if not args.res and args.photon_scale == 1.0 else
                                                                   " [reduced: %s, photons x%g]" % (args.res, args.photon_scale)),
-                       "method": "radiance cache" if args.method == "cache" else "plain gather",
+                       "method": {"plain": "plain gather", "cache": "radiance cache with per-region fallback",
+                                  "cache-everywhere": "radiance cache in every region"}[args.method],
                        "parallelism": "replicas" if ws > 1 else "single",
                        "tuning": tuning,
                        "l2": "inputs larger than L2: %.0f MB of triangle records + photon maps rebuilt every frame"
@@ -593,7 +607,8 @@ def run_ours(args):
                       "gather_candidates_per_query": st_last["gather_candidates"] / max(st_last["gathers"], 1),
                       "gather_select_frac": st_last["gather_selects"] / max(st_last["gathers"], 1),
                       "gather_spill_frac": st_last["gather_spills"] / max(st_last["gathers"], 1),
-                      "bvh_fallbacks": st_last["bvh_fallbacks"]},
+                      "bvh_fallbacks": st_last["bvh_fallbacks"],
+                      "nrc": g_nrc_stats},
             "throughput": throughput,
             "primary_mrays_per_s": st_last["primary_rays"] / (ms_step / 1e3) / 1e6,
             "image_vs_fp64_oracle": check,

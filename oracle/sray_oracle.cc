@@ -1367,6 +1367,16 @@ template <class R> struct Frame : FrameBase {
 		return true;
 	}
 
+	/* The patch inversion's discriminant.  Where the hit lies on the patch's
+	 * fold the exact value is ~0; float rounding can make it negative, and
+	 * the reference's sqrt would give NaN (a NaN normal).  Float clamps it
+	 * to 0 (the GPU does the same); double keeps the reference's sqrt. */
+	static R root_disc(R d)
+	{
+		if(sizeof(R) == 4) d = d > (R)0 ? d : (R)0;
+		return rsqrt_<R>(d);
+	}
+
 	/* interp_face (src/mesh.cc:321-445): bilinear-patch inversion after Haines */
 	void interp_face(const TriR &tri, const V &ispos, const V &normal, V *onorm, V *otang, R *otex) const
 	{
@@ -1393,8 +1403,9 @@ template <class R> struct Frame : FrameBase {
 			R duy = du0 / du2;
 			R ka = dux + dot(qux, ispos);
 			R kb = duy + dot(quy, ispos);
-			R u0 = ka - rsqrt_<R>(ka * ka - kb);
-			R u1 = ka + rsqrt_<R>(ka * ka - kb);
+			R sq = root_disc(ka * ka - kb);
+			R u0 = ka - sq;
+			R u1 = ka + sq;
 			rx = (u0 < (R)0 || u0 > (R)1) ? u1 : u0;
 		}
 		if(fabsr(dv2) <= xsmall) {
@@ -1407,8 +1418,9 @@ template <class R> struct Frame : FrameBase {
 			R dvy = dv0 / dv2;
 			R ka = dvx + dot(qvx, ispos);
 			R kb = dvy + dot(qvy, ispos);
-			R v0 = ka - rsqrt_<R>(ka * ka - kb);
-			R v1 = ka + rsqrt_<R>(ka * ka - kb);
+			R sq = root_disc(ka * ka - kb);
+			R v0 = ka - sq;
+			R v1 = ka + sq;
 			ry = (v0 < (R)0 || v0 > (R)1) ? v1 : v0;
 		}
 #define OLERP(a, b, t) ((a) + ((b) - (a)) * (t))

@@ -1005,6 +1005,12 @@ __device__ __forceinline__ V3 shadow_origin(const Surf &sp, V3 dir)
 	return sp.pos + sp.gn * off;
 }
 
+/* The patch inversion's discriminant: ~0 where the hit lies on the patch's
+ * fold, and float rounding can make it negative, where the reference's
+ * sqrt (in double, never negative there) would give a NaN normal.  Clamped
+ * to 0. */
+__device__ __forceinline__ float root_disc(float d) { return sqrtf(d > 0.0f ? d : 0.0f); }
+
 /* interp_face (src/mesh.cc:321-445): bilinear-patch inversion after Haines */
 __device__ inline void interp_face(const float *P, const float *A, V3 ispos, V3 normal, float xsmall, V3 *onorm, float *otex, bool want_tex)
 {
@@ -1031,8 +1037,9 @@ __device__ inline void interp_face(const float *P, const float *A, V3 ispos, V3 
 		float duy = du0 / du2;
 		float ka = dux + dot(qux, ispos);
 		float kb = duy + dot(quy, ispos);
-		float u0 = ka - sqrtf(ka * ka - kb);
-		float u1 = ka + sqrtf(ka * ka - kb);
+		float sq = root_disc(ka * ka - kb);
+		float u0 = ka - sq;
+		float u1 = ka + sq;
 		rx = (u0 < 0.0f || u0 > 1.0f) ? u1 : u0;
 	}
 	if(fabsf(dv2) <= xsmall) {
@@ -1045,8 +1052,9 @@ __device__ inline void interp_face(const float *P, const float *A, V3 ispos, V3 
 		float dvy = dv0 / dv2;
 		float ka = dvx + dot(qvx, ispos);
 		float kb = dvy + dot(qvy, ispos);
-		float v0 = ka - sqrtf(ka * ka - kb);
-		float v1 = ka + sqrtf(ka * ka - kb);
+		float sq = root_disc(ka * ka - kb);
+		float v0 = ka - sq;
+		float v1 = ka + sq;
 		ry = (v0 < 0.0f || v0 > 1.0f) ? v1 : v0;
 	}
 #define DLERP(a, b, t) ((a) + ((b) - (a)) * (t))

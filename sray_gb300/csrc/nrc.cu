@@ -60,6 +60,7 @@ static_assert(NRC_NPARAM == SRAY_NRC_PARAMS, "parameter count");
 
 /* shared-memory row strides (bf16 elements), padded against bank conflicts */
 enum { LD1 = 232, LDH = 72, LD5T = 24 };
+#define NRC_FWD_THREADS 256   /* forward blocks: 8 warps share one copy of the weights in shared memory */
 
 /* BF16 weight images in global memory, in the shared-memory layout:
  *   w1  [64][LD1]      (in 0..215, zero up to 231)
@@ -209,7 +210,7 @@ struct QueryOut {
 enum { FWD_INFER = 0, FWD_TRAIN = 1, FWD_QUERY = 2 };
 
 template <int MODE>
-__global__ void __launch_bounds__(128) k_nrc_forward(NrcDev net, int n, const float *x, float *y, const float *tgt, TrainBufs tb,
+__global__ void __launch_bounds__(NRC_FWD_THREADS) k_nrc_forward(NrcDev net, int n, const float *x, float *y, const float *tgt, TrainBufs tb,
 		QueryOut qo)
 {
 	constexpr bool TRAIN = MODE == FWD_TRAIN;
@@ -229,7 +230,8 @@ __global__ void __launch_bounds__(128) k_nrc_forward(NrcDev net, int n, const fl
 	int ntiles = (n + 15) >> 4;
 	float loss = 0.0f;
 	float db5[2] = {0.0f, 0.0f};
-	for(int tile = blockIdx.x * 4 + warp; tile < ntiles; tile += gridDim.x * 4) {
+	const int wpb = NRC_FWD_THREADS / 32;
+	for(int tile = blockIdx.x * wpb + warp; tile < ntiles; tile += gridDim.x * wpb) {
 		int r0 = tile * 16 + g, r1 = r0 + 8;
 		float xg[9], xg8[9];
 		#pragma unroll
@@ -507,9 +509,10 @@ __global__ void __launch_bounds__(256) k_nrc_wgrad(int n, const __nv_bfloat16 *d
 }
 
 /* Adam on the FP32 master; the BF16 images are rewritten from it */
-__global__ void k_nrc_adam(float *p, float *m, float *v, float *grad, int step, float lr)
+__global__ void k_nrc_adam(float *p, float *m, float *v, float *grad, const int *step_dev, float lr)
 {
 	const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+	int step = *step_dev + 1;   /* the step counter lives on the device, so that a captured graph replays */
 	float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
 	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < NRC_NPARAM; i += gridDim.x * blockDim.x) {
 		float gi = grad[i];
@@ -523,9 +526,11 @@ __global__ void k_nrc_adam(float *p, float *m, float *v, float *grad, int step, 
 	}
 }
 
-/* the BF16 images and FP32 biases of the current master weights */
-__global__ void k_nrc_images(const float *p, __nv_bfloat16 *img, float *bias)
+/* the BF16 images and FP32 biases of the current master weights; after an
+ * Adam step (count_step) also the step counter */
+__global__ void k_nrc_images(const float *p, __nv_bfloat16 *img, float *bias, int *step_dev, int count_step)
 {
+	if(count_step && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(step_dev, 1);
 	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < IMG_END; i += gridDim.x * blockDim.x) {
 		float v = 0.0f;
 		if(i < IMG_W2) {
@@ -567,6 +572,14 @@ __global__ void k_nrc_images(const float *p, __nv_bfloat16 *img, float *bias)
 struct NrcState {
 	int device = -1;
 	float *p = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr, *loss = nullptr, *bias = nullptr;
+	int *step_dev = nullptr;         /* Adam steps taken (device copy of `step`) */
+	/* the per-frame training steps as a CUDA graph, replayed while the
+	 * batch shape and buffers stay the same */
+	cudaGraphExec_t graph = nullptr;
+	cudaStream_t cap = nullptr;      /* stream the graph is captured on (the caller's may be the legacy stream) */
+	int g_steps = 0, g_per = 0;
+	const float *g_x = nullptr, *g_t = nullptr;
+	float g_lr = 0.0f;
 	__nv_bfloat16 *img = nullptr;
 	__nv_bfloat16 *hbuf = nullptr;   /* training activations */
 	int hcap = 0;                    /* samples the training buffers hold */
@@ -608,6 +621,7 @@ static int nrc_alloc()
 	NCK(cudaMalloc(&g_nrc.loss, sizeof(float)), "radiance cache loss");
 	NCK(cudaMalloc(&g_nrc.bias, NRC_NBIAS * sizeof(float)), "radiance cache biases");
 	NCK(cudaMalloc(&g_nrc.img, IMG_END * sizeof(__nv_bfloat16)), "radiance cache images");
+	NCK(cudaMalloc(&g_nrc.step_dev, sizeof(int)), "radiance cache step");
 	NCK(cudaFuncSetAttribute(k_nrc_forward<FWD_INFER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 			FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4), "smem");
 	NCK(cudaFuncSetAttribute(k_nrc_forward<FWD_TRAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -626,7 +640,8 @@ static int nrc_set(const float *host_p, cudaStream_t s)
 	NCK(cudaMemsetAsync(g_nrc.m, 0, NRC_NPARAM * sizeof(float), s), "reset moments");
 	NCK(cudaMemsetAsync(g_nrc.v, 0, NRC_NPARAM * sizeof(float), s), "reset moments");
 	NCK(cudaMemsetAsync(g_nrc.grad, 0, NRC_NPARAM * sizeof(float), s), "reset gradient");
-	k_nrc_images<<<64, 256, 0, s>>>(g_nrc.p, g_nrc.img, g_nrc.bias);
+	NCK(cudaMemsetAsync(g_nrc.step_dev, 0, sizeof(int), s), "reset step");
+	k_nrc_images<<<64, 256, 0, s>>>(g_nrc.p, g_nrc.img, g_nrc.bias, g_nrc.step_dev, 0);
 	NCK(cudaGetLastError(), "radiance cache images");
 	g_nrc.step = 0;
 	return 0;
@@ -669,11 +684,14 @@ static int nrc_train_bufs(int n, TrainBufs &tb, cudaStream_t s)
 	return 0;
 }
 
-static int nrc_grid(int n)
+/* blocks for n samples at wpb warps per block (16 samples per warp); at
+ * most a few resident waves, the kernels loop over the rest */
+static int nrc_grid(int n, int wpb)
 {
 	int tiles = (n + 15) / 16;
-	int blocks = (tiles + 3) / 4;
-	if(blocks > 152 * 8) blocks = 152 * 8;
+	int blocks = (tiles + wpb - 1) / wpb;
+	int cap = 152 * 32 / wpb;
+	if(blocks > cap) blocks = cap;
 	return blocks < 1 ? 1 : blocks;
 }
 
@@ -685,9 +703,13 @@ static int nrc_gradient(int n, const float *x, const float *t, float *y, cudaStr
 	if(r) return r;
 	NCK(cudaMemsetAsync(g_nrc.loss, 0, sizeof(float), s), "reset loss");
 	NrcDev d = nrc_dev();
-	k_nrc_forward<FWD_TRAIN><<<nrc_grid(n), 128, FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4, s>>>(d, n, x, y, t, tb, QueryOut());
-	k_nrc_backward<<<nrc_grid(n), 128, BWD_SMEM_BF16 * 2 + 256 * 4, s>>>(d, n, tb);
-	int per = 512;
+	k_nrc_forward<FWD_TRAIN><<<nrc_grid(n, NRC_FWD_THREADS / 32), NRC_FWD_THREADS, FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4, s>>>(d, n, x, y, t,
+			tb, QueryOut());
+	k_nrc_backward<<<nrc_grid(n, 4), 128, BWD_SMEM_BF16 * 2 + 256 * 4, s>>>(d, n, tb);
+	/* samples per weight-gradient block: about two blocks per SM, at least
+	 * 128 (each block adds its partial dW with atomics) */
+	int per = (n + 2 * 152 - 1) / (2 * 152);
+	per = per < 128 ? 128 : (per + 31) & ~31;
 	int blocks = (n + per - 1) / per;
 	/* layer 1: 64 x 224 (216 real), layers 2-4: 64 x 64, layer 5: 16 x 64 (3 real) */
 	k_nrc_wgrad<4, 28, 14, 64, NRC_FP><<<blocks, 256, 0, s>>>(n, tb.dz[1], tb.h[0], g_nrc.grad, OFF_W1, 64, NRC_F, per);
@@ -716,7 +738,8 @@ int nrc_ensure_ready(uint64_t seed, cudaStream_t s)
 int nrc_infer(int n, const float *x, float *y, cudaStream_t s)
 {
 	if(n <= 0) return 0;
-	k_nrc_forward<FWD_INFER><<<nrc_grid(n), 128, FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4, s>>>(nrc_dev(), n, x, y, nullptr, TrainBufs(),
+	k_nrc_forward<FWD_INFER><<<nrc_grid(n, NRC_FWD_THREADS / 32), NRC_FWD_THREADS, FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4, s>>>(nrc_dev(), n,
+			x, y, nullptr, TrainBufs(),
 			QueryOut());
 	NCK(cudaGetLastError(), "radiance cache inference");
 	return 0;
@@ -729,7 +752,8 @@ int nrc_query(const int *count, int cap, const float *x, const float4 *w, float4
 	qo.count = count;
 	qo.w = w;
 	qo.acc = acc;
-	k_nrc_forward<FWD_QUERY><<<nrc_grid(cap), 128, FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4, s>>>(nrc_dev(), cap, x, nullptr, nullptr,
+	k_nrc_forward<FWD_QUERY><<<nrc_grid(cap, NRC_FWD_THREADS / 32), NRC_FWD_THREADS, FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4, s>>>(nrc_dev(), cap,
+			x, nullptr, nullptr,
 			TrainBufs(), qo);
 	NCK(cudaGetLastError(), "radiance cache queries");
 	return 0;
@@ -741,9 +765,54 @@ int nrc_train(int n, const float *x, const float *t, float lr, cudaStream_t s)
 	int r = nrc_gradient(n, x, t, nullptr, s);
 	if(r) return r;
 	g_nrc.step++;
-	k_nrc_adam<<<64, 256, 0, s>>>(g_nrc.p, g_nrc.m, g_nrc.v, g_nrc.grad, g_nrc.step, lr);
-	k_nrc_images<<<64, 256, 0, s>>>(g_nrc.p, g_nrc.img, g_nrc.bias);
+	k_nrc_adam<<<64, 256, 0, s>>>(g_nrc.p, g_nrc.m, g_nrc.v, g_nrc.grad, g_nrc.step_dev, lr);
+	k_nrc_images<<<64, 256, 0, s>>>(g_nrc.p, g_nrc.img, g_nrc.bias, g_nrc.step_dev, 1);
 	NCK(cudaGetLastError(), "radiance cache training");
+	return 0;
+}
+
+/* `steps` Adam steps over consecutive batches of `per` samples: captured
+ * once as a CUDA graph (forward, backward, weight gradients, Adam and weight
+ * images of every step: steps * NRC_TRAIN_KERNELS kernels) and replayed
+ * while the shape, buffers and rate stay the same */
+int nrc_train_steps(int steps, int per, const float *x, const float *t, float lr, cudaStream_t s)
+{
+	if(steps <= 0 || per <= 0) return 0;
+	NrcState &G = g_nrc;
+	if(!(G.graph && G.g_steps == steps && G.g_per == per && G.g_x == x && G.g_t == t && G.g_lr == lr)) {
+		if(G.graph) {
+			cudaGraphExecDestroy(G.graph);
+			G.graph = nullptr;
+		}
+		TrainBufs tb;
+		int r = nrc_train_bufs(per, tb, s);   /* allocate before the capture */
+		if(r) return r;
+		if(!G.cap) NCK(cudaStreamCreateWithFlags(&G.cap, cudaStreamNonBlocking), "capture stream");
+		cudaGraph_t g = nullptr;
+		NCK(cudaStreamBeginCapture(G.cap, cudaStreamCaptureModeThreadLocal), "capture training steps");
+		int step0 = G.step;
+		for(int i = 0; i < steps && !r; i++) r = nrc_train(per, x + (size_t)i * per * 9, t + (size_t)i * per * 3, lr, G.cap);
+		G.step = step0;
+		cudaError_t e = cudaStreamEndCapture(G.cap, &g);
+		if(r) {
+			if(g) cudaGraphDestroy(g);
+			return r;
+		}
+		if(e != cudaSuccess) return nrc_fail(e, "capture training steps");
+		e = cudaGraphInstantiate(&G.graph, g, 0);
+		cudaGraphDestroy(g);
+		if(e != cudaSuccess) {
+			G.graph = nullptr;
+			return nrc_fail(e, "instantiate training graph");
+		}
+		G.g_steps = steps;
+		G.g_per = per;
+		G.g_x = x;
+		G.g_t = t;
+		G.g_lr = lr;
+	}
+	NCK(cudaGraphLaunch(G.graph, s), "training graph");
+	G.step += steps;
 	return 0;
 }
 

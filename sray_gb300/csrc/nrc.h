@@ -17,6 +17,9 @@ int nrc_query(const int *count, int cap, const float *x, const float4 *w, float4
 /* one Adam step on the batch (x[n][9], targets t[n][3]): NRC_TRAIN_KERNELS launches */
 #define NRC_TRAIN_KERNELS 9
 int nrc_train(int n, const float *x, const float *t, float lr, cudaStream_t s);
+/* `steps` Adam steps over consecutive batches of `per` samples of (x, t),
+ * replayed from a CUDA graph while the arguments stay the same */
+int nrc_train_steps(int steps, int per, const float *x, const float *t, float lr, cudaStream_t s);
 /* device address of the last batch's loss */
 float *nrc_loss_ptr();
 const char *nrc_error();

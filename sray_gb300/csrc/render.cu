@@ -1829,7 +1829,9 @@ int Renderer::nrc_setup(int batch, int n_prim, cudaStream_t s)
 	}
 	if(batch == 0) {
 		double expect = nrc_expect > 0 ? (double)nrc_expect : (double)n_prim;
-		double ft = ntrain / expect, fv = nval / expect;
+		/* 2 % more training vertices than the batch takes, so that a frame
+		 * almost always has the full batch (and replays the training graph) */
+		double ft = ntrain * 1.02 / expect, fv = nval / expect;
 		if(ft + fv > 1.0) {
 			/* fewer vertices than records wanted: every vertex is one, in proportion */
 			double sum = ft + fv;
@@ -1883,17 +1885,20 @@ int Renderer::nrc_batch_done(int batch, cudaStream_t s)
 	float max_rel = opt.nrc_max_rel_err;
 	LAUNCH(*this, "nrc_validate", s, k_nrc_regions<<<1, NRC_REGIONS, 0, s>>>(rs, NRC_VAL_DECAY, max_rel, NRC_VAL_MIN, N.mode));
 	int steps = opt.nrc_train_steps > 0 ? opt.nrc_train_steps : 4;
-	int per = n_t / steps;
+	int ntrain = opt.nrc_train_samples > 0 ? opt.nrc_train_samples : 65536;
+	int use = n_t < ntrain ? n_t : ntrain;
+	int per = use / steps;
 	if(per < 16) {
-		steps = n_t >= 16 ? 1 : 0;
-		per = n_t;
+		steps = use >= 16 ? 1 : 0;
+		per = use;
 	}
-	for(int i = 0; i < steps; i++) {
-		LAUNCH(*this, "nrc_train", s, r = nrc_train(per, rx + (size_t)i * per * 9, rt + (size_t)i * per * 3, NRC_LR, s));
+	if(steps > 0) {
+		/* the frame's training steps: one graph launch (steps x NRC_TRAIN_KERNELS kernels) */
+		LAUNCH(*this, "nrc_train", s, r = nrc_train_steps(steps, per, rx, rt, NRC_LR, s));
 		if(r) return fail(r, std::string("radiance cache: ") + nrc_error());
-		launch_count += NRC_TRAIN_KERNELS - 1;
+		launch_count += (long long)steps * NRC_TRAIN_KERNELS - 1;
 	}
-	nrc_last_train = n_t;
+	nrc_last_train = steps * per;
 	nrc_last_val = n_v;
 	nrc_frames++;
 	return 0;
@@ -2420,12 +2425,12 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 	if(!R.loaded) { g_err = "no scene loaded"; return SRAY_ESTATE; }
 	if(!fb || frames < 1) { g_err = "bad arguments"; return SRAY_EINVAL; }
 	cudaStream_t s = as_stream(stream);
-	static const int tails[] = {8192, 32768, 131072};
+	static const int tails[] = {0, 2048, 8192, 32768, 131072};
 	static const int pools[] = {2, 4, 8, 16};
-	static const int ptails[] = {16384, 65536, 262144};
+	static const int ptails[] = {16384, 65536, 262144, 1048576};
 	struct Knob { int sray_tuning::*field; const int *vals; int n; };
-	const Knob knobs[] = {{&sray_tuning::render_tail, tails, 3}, {&sray_tuning::pool_blocks_per_sm, pools, 4},
-		{&sray_tuning::photon_tail, ptails, 3}};
+	const Knob knobs[] = {{&sray_tuning::render_tail, tails, 5}, {&sray_tuning::pool_blocks_per_sm, pools, 4},
+		{&sray_tuning::photon_tail, ptails, 4}};
 	std::vector<sray_tune_trial> done;
 	cudaEvent_t e0, e1;
 	if(cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) { g_err = "autotune events"; return SRAY_ECUDA; }
