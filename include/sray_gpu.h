@@ -97,6 +97,15 @@ int sray_gpu_load_scene(const char *xml_path);
 /* Same, from an in-memory XML document of `len` bytes. */
 int sray_gpu_load_scene_mem(const char *xml, size_t len);
 
+/* Load an XML scene with a binary side-car of its meshes (extension; the
+ * reference parses every mesh element, src/meshload.cc:55-157).  When the
+ * file at `sidecar` was written for this exact document and the same mesh
+ * octree options, the meshes, their octrees and hierarchies are read from
+ * it and the document's <mesh> elements are skipped; otherwise the document
+ * is loaded in full and the side-car is written.  *used (optional) = 1 when
+ * the side-car was used. */
+int sray_gpu_load_scene_sidecar(const char *xml_path, const char *sidecar, int *used);
+
 /* Scene summary: counts of objects, lights, materials, triangles (summed
  * over mesh objects), unique device meshes. */
 int sray_gpu_scene_info(int *n_objects, int *n_lights, int *n_materials,

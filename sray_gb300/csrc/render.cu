@@ -2283,35 +2283,61 @@ int sray_gpu_set_opts(const sray_opts *opt)
 	return 0;
 }
 
-int sray_gpu_load_scene_mem(const char *xml, size_t len)
+static int load_scene_text(const char *xml, size_t len, const char *sidecar, int *used)
 {
-	NEED_CTX();
 	Renderer &R = *g_R;
 	R.loaded = false;
 	R.built = false;
 	R.photons_ready = false;
 	if(!xml) { g_err = "null document"; return SRAY_EINVAL; }
 	std::string err;
-	if(!R.sc.load(xml, len, R.opt, err)) { g_err = err; return SRAY_ELOAD; }
+	bool u = false;
+	if(!R.sc.load(xml, len, R.opt, err, sidecar, &u)) { g_err = err; return SRAY_ELOAD; }
+	if(used) *used = u ? 1 : 0;
 	int r = R.upload_scene(0);
 	if(r) { g_err = R.err; return r; }
 	R.loaded = true;
 	return 0;
 }
 
-int sray_gpu_load_scene(const char *path)
+int sray_gpu_load_scene_mem(const char *xml, size_t len)
 {
 	NEED_CTX();
+	return load_scene_text(xml, len, nullptr, nullptr);
+}
+
+static int read_file(const char *path, std::string &buf)
+{
 	if(!path) { g_err = "null path"; return SRAY_EINVAL; }
 	FILE *fp = fopen(path, "rb");
 	if(!fp) { g_err = std::string("failed to open file: ") + path; return SRAY_ELOAD; }
 	fseek(fp, 0, SEEK_END);
 	long sz = ftell(fp);
 	fseek(fp, 0, SEEK_SET);
-	std::string buf(sz > 0 ? (size_t)sz : 0, '\0');
+	buf.assign(sz > 0 ? (size_t)sz : 0, '\0');
 	size_t rd = sz > 0 ? fread(&buf[0], 1, (size_t)sz, fp) : 0;
 	fclose(fp);
-	return sray_gpu_load_scene_mem(buf.data(), rd);
+	buf.resize(rd);
+	return 0;
+}
+
+int sray_gpu_load_scene(const char *path)
+{
+	NEED_CTX();
+	std::string buf;
+	int r = read_file(path, buf);
+	if(r) return r;
+	return load_scene_text(buf.data(), buf.size(), nullptr, nullptr);
+}
+
+int sray_gpu_load_scene_sidecar(const char *path, const char *sidecar, int *used)
+{
+	NEED_CTX();
+	if(!sidecar) { g_err = "null side-car path"; return SRAY_EINVAL; }
+	std::string buf;
+	int r = read_file(path, buf);
+	if(r) return r;
+	return load_scene_text(buf.data(), buf.size(), sidecar, used);
 }
 
 int sray_gpu_scene_info(int *n_objects, int *n_lights, int *n_materials, int64_t *n_triangles, int *n_unique_meshes)

@@ -139,6 +139,8 @@ struct Doc {
 		return true;
 	}
 
+	bool skip_mesh = false;   /* leave the children of <mesh> elements unparsed */
+
 	bool parse(const char *p, size_t len)
 	{
 		const char *end = p + len;
@@ -220,6 +222,16 @@ struct Doc {
 			} else if(id != 0) {
 				err = "more than one root element";
 				return false;
+			}
+			if(!selfclose && skip_mesh && eq(n.name, n.nlen, "mesh")) {
+				/* the mesh's elements come from the side-car: jump past </mesh> */
+				static const char close[] = "</mesh";
+				const char *c = std::search(p, end, close, close + 6);
+				if(c >= end) { err = "unterminated <mesh>"; return false; }
+				p = c + 6;
+				while(p < end && *p != '>') p++;
+				p++;
+				continue;
 			}
 			if(!selfclose) stack.push_back(id);
 		}
@@ -913,6 +925,9 @@ struct Loader {
 	HostScene &sc;
 	const sray_opts &opt;
 	std::string &err;
+	const std::vector<int> *sidecar_mesh = nullptr;   /* unique mesh of each mesh object, in document order */
+	size_t mesh_objects = 0;
+	std::vector<int> mesh_of_object;                  /* filled while loading (for writing a side-car) */
 
 	void load_xform(int n, XForm &xf)
 	{
@@ -997,6 +1012,19 @@ struct Loader {
 
 	/* Mesh::load_xml (src/meshload.cc:55-157) */
 	bool load_mesh(int objn, Object &o)
+	{
+		if(sidecar_mesh) {
+			if(mesh_objects >= sidecar_mesh->size()) { err = "side-car holds fewer meshes than the document"; return false; }
+			o.mesh = (*sidecar_mesh)[mesh_objects++];
+			sc.n_tris += (int64_t)(sc.meshes[o.mesh].posd.size() / 9);
+			return true;
+		}
+		bool ok = load_mesh_xml(objn, o);
+		if(ok) mesh_of_object.push_back(o.mesh);
+		return ok;
+	}
+
+	bool load_mesh_xml(int objn, Object &o)
 	{
 		int mn = -1;
 		for(int c = d.nodes[objn].first_child; c >= 0; c = d.nodes[c].next) if(d.is(c, "mesh")) { mn = c; break; }
@@ -1223,17 +1251,174 @@ struct Loader {
 };
 }  // namespace
 
-bool HostScene::load(const char *text, size_t len, const sray_opts &opt, std::string &err)
+/* ---- binary side-car of a document's meshes ----
+ * header: magic, format version, document size and hash, the mesh octree
+ * options; per unique mesh: faces, vertices (double, 9 per face),
+ * attributes (float, 24 per face), content hash, octree (per node: box,
+ * first child, items), binary hierarchy (nodes, leaf order, depth); then
+ * the unique mesh of every mesh object in document order. */
+static const char SIDECAR_MAGIC[8] = {'S', 'R', 'A', 'Y', 'M', 'S', 'H', '1'};
+
+static uint64_t text_hash(const char *p, size_t n)
 {
+	uint64_t h = 0x243f6a8885a308d3ull ^ (uint64_t)n;
+	size_t i = 0;
+	for(; i + 8 <= n; i += 8) {
+		uint64_t w;
+		memcpy(&w, p + i, 8);
+		h = (h ^ w) * 0x9e3779b97f4a7c15ull;
+		h ^= h >> 29;
+	}
+	uint64_t w = 0;
+	memcpy(&w, p + i, n - i);
+	h = (h ^ w) * 0x9e3779b97f4a7c15ull;
+	return h ^ (h >> 31);
+}
+
+namespace {
+struct Writer {
+	FILE *f;
+	bool ok = true;
+	void raw(const void *p, size_t n) { if(ok && n && fwrite(p, 1, n, f) != n) ok = false; }
+	template <class T> void val(const T &v) { raw(&v, sizeof v); }
+	template <class T> void vec(const std::vector<T> &v) { val((uint64_t)v.size()); raw(v.data(), v.size() * sizeof(T)); }
+};
+struct Reader {
+	const char *p, *end;
+	bool ok = true;
+	void raw(void *dst, size_t n)
+	{
+		if(!ok || (size_t)(end - p) < n) { ok = false; return; }
+		memcpy(dst, p, n);
+		p += n;
+	}
+	template <class T> void val(T &v) { raw(&v, sizeof v); }
+	template <class T> void vec(std::vector<T> &v)
+	{
+		uint64_t n = 0;
+		val(n);
+		if(!ok || n > (uint64_t)(end - p) / sizeof(T)) { ok = false; return; }
+		v.resize(n);
+		raw(v.data(), n * sizeof(T));
+	}
+};
+}  // namespace
+
+static bool write_sidecar(const char *path, const HostScene &sc, const std::vector<int> &mesh_of_object, uint64_t doc_size,
+		uint64_t doc_hash, const sray_opts &opt)
+{
+	std::string tmp = std::string(path) + ".tmp";
+	FILE *f = fopen(tmp.c_str(), "wb");
+	if(!f) return false;
+	Writer w{f};
+	w.raw(SIDECAR_MAGIC, 8);
+	w.val(doc_size);
+	w.val(doc_hash);
+	w.val((int32_t)opt.meshoct_max_depth);
+	w.val((int32_t)opt.meshoct_max_items);
+	w.val((uint64_t)sc.meshes.size());
+	for(const Mesh &m : sc.meshes) {
+		w.vec(m.posd);
+		w.vec(m.attr);
+		w.val(m.hash);
+		w.val((uint64_t)m.oct.nodes.size());
+		for(const BuildOctree::Node &n : m.oct.nodes) {
+			w.val(n.box);
+			w.val((int32_t)n.child);
+			w.vec(n.items);
+		}
+		w.vec(m.bvh.nodes);
+		w.vec(m.bvh.order);
+		w.val((int32_t)m.bvh.depth);
+	}
+	w.vec(mesh_of_object);
+	bool ok = w.ok && fclose(f) == 0;
+	if(!ok) { remove(tmp.c_str()); return false; }
+	return rename(tmp.c_str(), path) == 0;
+}
+
+/* the side-car's meshes and structures if it belongs to this document and
+ * these options, else false */
+static bool read_sidecar(const char *path, HostScene &sc, std::vector<int> &mesh_of_object, uint64_t doc_size, uint64_t doc_hash,
+		const sray_opts &opt)
+{
+	FILE *f = fopen(path, "rb");
+	if(!f) return false;
+	std::vector<char> buf;
+	if(fseek(f, 0, SEEK_END) == 0) {
+		long sz = ftell(f);
+		if(sz > 0) {
+			buf.resize((size_t)sz);
+			fseek(f, 0, SEEK_SET);
+			if(fread(buf.data(), 1, buf.size(), f) != buf.size()) buf.clear();
+		}
+	}
+	fclose(f);
+	if(buf.size() < 8 || memcmp(buf.data(), SIDECAR_MAGIC, 8) != 0) return false;
+	Reader r{buf.data() + 8, buf.data() + buf.size()};
+	uint64_t size = 0, hash = 0, nm = 0;
+	int32_t depth = 0, items = 0;
+	r.val(size);
+	r.val(hash);
+	r.val(depth);
+	r.val(items);
+	if(!r.ok || size != doc_size || hash != doc_hash || depth != opt.meshoct_max_depth || items != opt.meshoct_max_items) return false;
+	r.val(nm);
+	if(!r.ok || nm > (1u << 24)) return false;
+	std::vector<Mesh> meshes(nm);
+	for(Mesh &m : meshes) {
+		r.vec(m.posd);
+		r.vec(m.attr);
+		r.val(m.hash);
+		uint64_t nn = 0;
+		r.val(nn);
+		if(!r.ok || nn > (uint64_t)(r.end - r.p)) return false;
+		m.oct.nodes.resize(nn);
+		for(BuildOctree::Node &n : m.oct.nodes) {
+			int32_t child = 0;
+			r.val(n.box);
+			r.val(child);
+			n.child = child;
+			r.vec(n.items);
+		}
+		r.vec(m.bvh.nodes);
+		r.vec(m.bvh.order);
+		int32_t bd = 0;
+		r.val(bd);
+		m.bvh.depth = bd;
+		if(!r.ok || m.posd.size() % 9 || m.attr.size() != m.posd.size() / 9 * 24) return false;
+		m.pos.resize(m.posd.size());
+		for(size_t i = 0; i < m.posd.size(); i++) m.pos[i] = (float)m.posd[i];
+	}
+	r.vec(mesh_of_object);
+	if(!r.ok) return false;
+	for(int u : mesh_of_object) if(u < 0 || (uint64_t)u >= nm) return false;
+	sc.meshes = std::move(meshes);
+	return true;
+}
+
+bool HostScene::load(const char *text, size_t len, const sray_opts &opt, std::string &err, const char *sidecar, bool *used)
+{
+	if(used) *used = false;
+	uint64_t doc_hash = sidecar ? text_hash(text, len) : 0;
+	std::vector<int> cached_map;
+	HostScene cached;
+	bool have_sidecar = sidecar && read_sidecar(sidecar, cached, cached_map, len, doc_hash, opt);
 	Doc d;
+	d.skip_mesh = have_sidecar;
 	if(!d.parse(text, len)) { err = "xml: " + d.err; return false; }
 	*this = HostScene();
+	if(have_sidecar) meshes = std::move(cached.meshes);
 	Loader ld = {d, *this, opt, err};
+	if(have_sidecar) ld.sidecar_mesh = &cached_map;
 	if(!ld.run()) return false;
+	if(have_sidecar && ld.mesh_objects != cached_map.size()) { err = "side-car holds more meshes than the document"; return false; }
+	if(used) *used = have_sidecar;
 	/* mesh octrees in object space (Mesh::build_tree, src/mesh.cc:210-226),
-	 * one per unique mesh, built on all host cores */
+	 * one per unique mesh, built on all host cores (read from the side-car
+	 * when it had them) */
 	std::vector<std::thread> th;
-	size_t nm = meshes.size();
+	size_t nm = have_sidecar ? 0 : meshes.size();
 	/* tasks 0 .. nm-1 build octrees, nm .. 2nm-1 hierarchies */
 	size_t ntask = 2 * nm;
 	unsigned nth = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), (unsigned)ntask));
@@ -1264,6 +1449,7 @@ bool HostScene::load(const char *text, size_t len, const sray_opts &opt, std::st
 		}));
 	}
 	for(auto &t : th) t.join();
+	if(sidecar && !have_sidecar) write_sidecar(sidecar, *this, ld.mesh_of_object, len, doc_hash, opt);
 	/* objects with at most one key per transform track have time-independent bounds */
 	for(size_t i = 0; i < objs.size(); i++) {
 		Object &o = objs[i];

@@ -156,7 +156,13 @@ struct HostScene {
 	std::vector<Box> oct_boxes;        /* the boxes the scene octree was built from */
 	Box object_bounds(size_t i, int t) const;
 
-	bool load(const char *text, size_t len, const sray_opts &opt, std::string &err);
+	/* Load an S-ray XML document.  With a side-car path: when the file
+	 * there holds the meshes of this exact document (and their octrees and
+	 * hierarchies for the same mesh octree options), they are read from it
+	 * and the XML's <mesh> elements are skipped; otherwise the document is
+	 * loaded in full and the side-car is written.  *used tells which. */
+	bool load(const char *text, size_t len, const sray_opts &opt, std::string &err, const char *sidecar = nullptr,
+			bool *used = nullptr);
 	void build_tree(int t0, int t1, const sray_opts &opt);
 	void build_projmaps(int t0, int t1, uint64_t seed);
 	void build_light_projmaps(size_t li, int t0, int t1, uint64_t seed);

@@ -15,6 +15,7 @@ _LIB = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libsray
 _lib = None
 
 EXPORTS = ["sray_default_opts", "sray_gpu_init", "sray_gpu_set_opts", "sray_gpu_load_scene", "sray_gpu_load_scene_mem",
+           "sray_gpu_load_scene_sidecar",
            "sray_gpu_scene_info", "sray_gpu_build", "sray_gpu_shoot_photons", "sray_gpu_render",
            "sray_gpu_render_pixels", "sray_gpu_cast_rays", "sray_gpu_primary_hits", "sray_gpu_photon_gather", "sray_gpu_photon_gather_noalloc",
            "sray_gpu_get_photons",
@@ -83,6 +84,7 @@ def load_library():
     L.sray_gpu_set_opts.argtypes = [ctypes.POINTER(SrayOpts)]
     L.sray_gpu_load_scene.argtypes = [ctypes.c_char_p]
     L.sray_gpu_load_scene_mem.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    L.sray_gpu_load_scene_sidecar.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
     L.sray_gpu_scene_info.argtypes = [vp, vp, vp, vp, vp]
     L.sray_gpu_build.argtypes = [lp, lp]
     L.sray_gpu_shoot_photons.argtypes = [lp, lp, vp, vp, vp]
@@ -192,8 +194,16 @@ class GpuRenderer:
             setattr(self.opts, k, v)
         self._chk(self.L.sray_gpu_set_opts(ctypes.byref(self.opts)))
 
-    def load(self, path):
-        self._chk(self.L.sray_gpu_load_scene(path.encode()))
+    def load(self, path, sidecar=None):
+        """Load an XML scene; with `sidecar`, through the binary side-car of its
+        meshes (written when missing or stale).  Returns True when the side-car
+        was used."""
+        if sidecar is None:
+            self._chk(self.L.sray_gpu_load_scene(path.encode()))
+            return False
+        used = ctypes.c_int()
+        self._chk(self.L.sray_gpu_load_scene_sidecar(path.encode(), sidecar.encode(), ctypes.byref(used)))
+        return bool(used.value)
 
     def load_xml(self, xml):
         b = xml.encode() if isinstance(xml, str) else xml

@@ -222,3 +222,15 @@ def test_autotuner_keeps_the_image(gpu_lib, small_scene_path):
     g.set_tuning(render_tail=0, pool_blocks_per_sm=16, photon_tail=1 << 20)
     g.render(0, fb)
     assert np.abs(fb.cpu().numpy() - ref).max() <= 1e-5
+
+
+def test_sidecar_load_renders_the_same(gpu_lib, small_scene_path, tmp_path):
+    opts = _opts(width=96, height=96)
+    g = gpu_lib.GpuRenderer(**opts)
+    g.load(small_scene_path)
+    ref = g.render(0)
+    car = str(tmp_path / "small.srmesh")
+    assert not g.load(small_scene_path, sidecar=car)      # written
+    assert g.load(small_scene_path, sidecar=car)          # used
+    img = g.render(0)
+    assert np.abs(img - ref).max() <= 1e-6
