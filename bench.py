@@ -43,7 +43,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="production", choices=["production", "small", "learned"])
+    ap.add_argument("--config", default="production", choices=["production", "small", "learned", "stress"])
     ap.add_argument("--no-nrc", action="store_true", help="skip the radiance-cache comparison")
     ap.add_argument("--method", default="plain", choices=["plain", "cache", "cache-everywhere"],
                     help="final gather of the headline frames: the plain gather, the radiance cache with its "
@@ -77,6 +77,10 @@ def config_opts(args):
 
 
 def workload_desc(cfg):
+    if cfg == "stress":
+        return ("stress: 3840x2160, adaptive 1-16 spp (variance 0.05), depth 8, 4x4 displaced-grid terrain tiles "
+                "(10M triangles) + 2000 instanced icospheres (10% moving over a 40 ms shutter, motion blur on), "
+                "3 sphere lights, 20M global + 4M caustic photons, k=100 gathers within r<=0.5")
     if cfg == "learned":
         return ("learned gather: the small scene at 1920x1080, 1 spp, depth 5, 100k caustic photons (k=50), "
                 "500k global photons (k=100 nearest within r<=0.5), final gather of indirect light by the radiance "
@@ -533,7 +537,7 @@ def run_ours(args):
             "prim_tests_per_ray": st_count["prim_tests"] / max(rays_traced, 1)}
 
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline and args.config != "stress":
         try:
             frac = 0.05 if args.config == "production" else 1.0
             cb = cpu_baseline(args.config, path, opts, args.cpu_rows, frac)
@@ -555,14 +559,43 @@ def run_ours(args):
                           "frame time, kernel rates the CUDA-event time of the photon / gather launches"}
 
     check = None
-    if rank == 0 and not args.no_cpu_baseline:
+    if rank == 0 and not args.no_cpu_baseline and args.config != "stress":
         try:
             check = production_image_check(opts, path, fb.cpu().numpy())
         except Exception as exc:  # reported, not the measurement
             check = {"error": str(exc)}
 
+    stress_cache = None
+    if args.config == "stress" and not args.no_nrc:
+        # the same frames with the radiance cache (per-region fallback), trained online
+        g.set_opts(nrc=1)
+        free1 = torch.cuda.mem_get_info()[0]
+        burn = 30
+        for _ in range(burn):
+            g.render(0, fb, stream=stream)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        crays = 0
+        for _ in range(args.steps):
+            g.render(0, fb, stream=stream)
+            crays += rays_of(g.stats())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        cms = e0.elapsed_time(e1) / args.steps
+        st_c = g.nrc_stats()
+        stress_cache = {"ms_per_frame": cms, "mrays_per_s": crays / args.steps / (cms / 1e3) / 1e6,
+                        "plain_ms_per_frame": ms_step, "frames_trained": st_c["frames"],
+                        "cached_vertex_frac": st_c["cached"] / max(st_c["vertices"], 1),
+                        "regions_cached": st_c["regions_cached"], "val_rel_err": st_c["val_rel_err"],
+                        "device_mb_plain": device_mb,
+                        "device_mb_extra_for_cache": (free1 - torch.cuda.mem_get_info()[0]) / 1e6,
+                        "note": "RMSE against the FP64 oracle is not computed for this scene (the CPU oracle would "
+                                "trace 24M photons over 10M triangles in double)"}
+
     nrc = None
-    if rank == 0 and not args.no_nrc and ws == 1 and args.res is None:
+    if rank == 0 and not args.no_nrc and ws == 1 and args.res is None and args.config != "stress":
         g.close()
         ref = None
         if not args.no_cpu_baseline:
@@ -598,6 +631,7 @@ def run_ours(args):
             "gpu_launches": launches,
             "clocks": clk,
             "nrc_vs_plain": nrc,
+            "stress_cache_vs_plain": stress_cache,
             "kernels_ms_per_step": {k: round(v[0] / args.steps, 3) for k, v in kt.items()},
             "frame": {"rays": rays_of(st_last), "primary": st_last["primary_rays"],
                       "secondary": st_last["secondary_rays"], "shadow": st_last["shadow_rays"],

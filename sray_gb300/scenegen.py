@@ -261,6 +261,92 @@ def production_scene(seed=0x5EED0002, grid=(1000, 500), extent=(100.0, 50.0), n_
     return "".join(out)
 
 
+def stress_scene(seed=0x5EED0005, tiles=(4, 4), tile_grid=(625, 500), tile_extent=(100.0, 80.0), n_inst=2000,
+                 moving=0.1, shutter_ms=40):
+    """The stress scene, as chunks of XML: tiles[0] x tiles[1] displaced-grid
+    terrain meshes of 2 * tile_grid[0] * tile_grid[1] triangles each (one
+    continuous 6-octave value-noise height field, amplitude 2), n_inst
+    subdivision-3 icosphere instances (a `moving` fraction with a two-key
+    linear motion over the shutter), 3 sphere lights."""
+    rng = np.random.default_rng(seed)
+    tx, tz = tiles
+    gx_, gz_ = tile_grid
+    ex, ez = tile_extent
+    EX, EZ = ex * tx, ez * tz
+    out = ["<?xml version=\"1.0\"?>\n<scene>\n", '<env ambient="0.04 0.04 0.05" bgcolor="0.35 0.45 0.6"/>\n']
+    _material(out, "terrain", (0.45, 0.5, 0.32), ks=0.05, shin=8.0)
+    n_mirror, n_glass = n_inst // 4, n_inst // 10
+    kinds = np.array(["phong"] * n_inst, dtype=object)
+    order = rng.permutation(n_inst)
+    kinds[order[:n_glass]] = "glass"
+    kinds[order[n_glass:n_glass + n_mirror]] = "mirror"
+    for i in range(n_inst):
+        kd = rng.uniform(0.1, 0.9, 3)
+        if kinds[i] == "glass":
+            _material(out, "m%d" % i, kd * 0.1, ks=1.0, shin=80.0, refr=1.0, ior=1.5)
+        elif kinds[i] == "mirror":
+            _material(out, "m%d" % i, kd, ks=1.0, shin=60.0, refl=0.8)
+        else:
+            _material(out, "m%d" % i, kd, ks=0.4, shin=30.0)
+    yield "".join(out)
+    hseed = int(rng.integers(1 << 31))
+    for ti in range(tx):
+        for tj in range(tz):
+            x0, z0 = -EX / 2 + ti * ex, -EZ / 2 + tj * ez
+            xs = np.linspace(x0, x0 + ex, gx_ + 1)
+            zs = np.linspace(z0, z0 + ez, gz_ + 1)
+            X, Z = np.meshgrid(xs, zs, indexing="ij")
+            H = value_noise_height(X, Z, hseed)
+            verts = np.stack([X, H, Z], axis=-1).reshape(-1, 3).astype(np.float32)
+            d = 1e-3
+            gx = (value_noise_height(X + d, Z, hseed) - value_noise_height(X - d, Z, hseed)) / (2 * d)
+            gz = (value_noise_height(X, Z + d, hseed) - value_noise_height(X, Z - d, hseed)) / (2 * d)
+            nrm = np.stack([-gx, np.ones_like(gx), -gz], axis=-1)
+            nrm /= np.linalg.norm(nrm, axis=-1, keepdims=True)
+            nrm = nrm.reshape(-1, 3).astype(np.float32)
+            idx = np.arange((gx_ + 1) * (gz_ + 1)).reshape(gx_ + 1, gz_ + 1)
+            a, b = idx[:-1, :-1].ravel(), idx[1:, :-1].ravel()
+            c, dd = idx[1:, 1:].ravel(), idx[:-1, 1:].ravel()
+            faces = np.empty((a.size * 2, 3), dtype=np.int64)
+            faces[0::2] = np.stack([a, dd, c], axis=1)
+            faces[1::2] = np.stack([a, c, b], axis=1)
+            chunk = []
+            _mesh_xml(chunk, "terrain_%d_%d" % (ti, tj), "terrain", verts, faces, normals=nrm)
+            yield "".join(chunk)
+    iv, ifc = icosphere(3)
+    px = rng.uniform(-0.45 * EX, 0.45 * EX, n_inst)
+    pz = rng.uniform(-0.45 * EZ, 0.45 * EZ, n_inst)
+    sc = rng.uniform(0.4, 1.5, n_inst)
+    lift = rng.uniform(0.0, 2.0, n_inst)
+    hy = value_noise_height(px, pz, hseed)
+    axes = rng.normal(size=(n_inst, 3))
+    axes /= np.linalg.norm(axes, axis=1, keepdims=True)
+    angles = rng.uniform(0, 360, n_inst)
+    move = rng.uniform(0, 1, n_inst) < moving
+    vel = rng.normal(size=(n_inst, 3)) * 0.5
+    chunk = []
+    for i in range(n_inst):
+        p0 = (px[i], hy[i] + sc[i] + lift[i], pz[i])
+        if move[i]:
+            p1 = tuple(np.asarray(p0) + vel[i])
+            xf = (_xform(pos=p0, scale=(sc[i],) * 3, axisrot=(angles[i], axes[i][0], axes[i][1], axes[i][2]), time=0)
+                  + _xform(pos=p1, scale=(sc[i],) * 3, axisrot=(angles[i], axes[i][0], axes[i][1], axes[i][2]),
+                           time=shutter_ms))
+        else:
+            xf = _xform(pos=p0, scale=(sc[i],) * 3, axisrot=(angles[i], axes[i][0], axes[i][1], axes[i][2]))
+        _mesh_xml(chunk, "inst%d" % i, "m%d" % i, iv, ifc, normals=iv, xform=xf)
+        if len(chunk) > 400:
+            yield "".join(chunk)
+            chunk = []
+    for i, (lx, lz) in enumerate([(-60.0, 20.0), (45.0, -30.0), (15.0, 50.0)]):
+        chunk.append('<light type="sphere" color="0.9">\n%s<sphere rad="1.5"/>\n</light>\n'
+                     % _xform(pos=(lx, 45.0 + 4.0 * i, lz)))
+    chunk.append('<camera type="target" fov="55.0">\n%s<target>\n%s</target>\n</camera>\n'
+                 % (_xform(pos=(2.0, 40.0, 150.0)), _xform(pos=(0.0, 0.0, -10.0))))
+    chunk.append("</scene>\n")
+    yield "".join(chunk)
+
+
 def feature_scene(seed=0x5EED0003):
     """A small scene touching the reference's less common paths: sphere and
     box lights, a default (shade_undef) material, a cylinder, a mirror and a
@@ -310,6 +396,12 @@ CONFIGS = {
                     caust_photons=100000, gi_photons=500000, caust_k=50, gi_k=100, gather_rcap=0.5,
                     diffuse_samples=1, nrc_fallback_samples=16, scnoct_max_depth=8, scnoct_max_items=8,
                     meshoct_max_depth=8, meshoct_max_items=8),
+    # the stress configuration: 10M triangles (4x4 terrain tiles) + 2000
+    # instances at 3840x2160, 20M global + 4M caustic photons, motion blur
+    "stress": dict(width=3840, height=2160, min_samples=1, max_samples=16, max_var=0.05, iter=8,
+                   caust_photons=4000000, gi_photons=20000000, caust_k=100, gi_k=100, gather_rcap=0.5,
+                   mblur=1, shutter=40, time_start=0, time_end=0,
+                   scnoct_max_depth=8, scnoct_max_items=8, meshoct_max_depth=10, meshoct_max_items=8),
     "production": dict(width=1920, height=1080, min_samples=1, max_samples=16, max_var=0.05, iter=8,
                        caust_photons=500000, gi_photons=2000000, caust_k=100, gi_k=100, gather_rcap=0.5,
                        scnoct_max_depth=8, scnoct_max_items=8, meshoct_max_depth=10, meshoct_max_items=8),
@@ -324,7 +416,8 @@ def scene_opts(name, **over):
 
 def write_scene(name, cache_dir=None, **kw):
     """Generate (or reuse from cache_dir) the XML of scene `name`; returns the path."""
-    gen = {"small": small_scene, "learned": small_scene, "production": production_scene, "feature": feature_scene}[name]
+    gen = {"small": small_scene, "learned": small_scene, "production": production_scene, "feature": feature_scene,
+           "stress": stress_scene}[name]
     key = hashlib.sha1(repr((name, sorted(kw.items()), 3)).encode()).hexdigest()[:12]
     cache_dir = cache_dir or os.environ.get("SRAY_SCENE_CACHE", "/tmp/sray_scenes")
     os.makedirs(cache_dir, exist_ok=True)
@@ -333,6 +426,10 @@ def write_scene(name, cache_dir=None, **kw):
         xml = gen(**kw)
         tmp = path + ".tmp%d" % os.getpid()
         with open(tmp, "w") as f:
-            f.write(xml)
+            if isinstance(xml, str):
+                f.write(xml)
+            else:
+                for chunk in xml:      # generators write their document in pieces
+                    f.write(chunk)
         os.replace(tmp, path)
     return path
