@@ -34,7 +34,8 @@ enum {
 	SRAY_ECUDA = -3,       /* CUDA runtime error */
 	SRAY_ESTATE = -4,      /* call out of order (e.g. render before load) */
 	SRAY_EDEVICE = -5,     /* a kernel raised its error word (queue overflow, bounded wait expired) */
-	SRAY_ENOMEM = -6
+	SRAY_ENOMEM = -6,
+	SRAY_EIO = -7          /* a file could not be opened or written */
 };
 
 /* Render options.  Field meanings and defaults follow the reference's
@@ -183,6 +184,15 @@ int sray_gpu_photon_gather_noalloc(int which, int n, const float *pos, const flo
  * three unused.  `cap` is the capacity in photons; returns the count through
  * `n_out`.  Photons are in Morton order. */
 int sray_gpu_get_photons(int which, float *out, int cap, int *n_out);
+
+/* PhotonMap::dump / restore (src/pmap.cc:180-251), in the reference's text
+ * format ("energy %f", then "<pos> <dir> <norm> <col>" per photon).  Restore
+ * scales the powers by this renderer's photon_energy over the dump's and
+ * builds the map on the device over the current frame's scene bounds
+ * (after sray_gpu_build); sray_gpu_render_pixels then gathers from it.
+ * The photon count goes through n_out. */
+int sray_gpu_dump_photons(int which, const char *path);
+int sray_gpu_restore_photons(int which, const char *path, int *n_out);
 
 /* Device-side statistics of the last render: rays traced per kind. */
 typedef struct sray_stats {

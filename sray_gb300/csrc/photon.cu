@@ -700,6 +700,15 @@ static int photon_finalize(Renderer &R, int global, int total, cudaStream_t s, i
 	if(n == 0) return 0;
 	PCK(P.ph.ensure((size_t)n * sizeof(DevPhoton)), "photon map");
 	LAUNCH(R, "photon_compact", s, k_compact<<<nb, 256, 0, s>>>(P.valid.as<int>(), P.tmp_ph.as<DevPhoton>(), total, bc, P.ph.as<DevPhoton>()));
+	return photon_map_build(R, global, n, s);
+}
+
+/* the map over the n photons in P.ph: grid, Morton sort, cell table */
+int photon_map_build(Renderer &R, int global, int n, cudaStream_t s)
+{
+	PhotonBufs &P = global ? R.gi : R.caust;
+	const sray_opts &opt = R.opt;
+	if(R.sc.oct.nodes.empty()) return R.fail(SRAY_ESTATE, "no scene bounds (build the frame first)");
 	/* grid over the scene bounds: cells of the gather radius */
 	const Box &rb = R.sc.oct.nodes[0].box;
 	int k = global ? opt.gi_k : opt.caust_k;
@@ -770,6 +779,20 @@ static int photon_finalize(Renderer &R, int global, int total, cudaStream_t s, i
 	PCK(cudaStreamSynchronize(s), "photon map build");
 	R.prof_collect();
 	return 0;
+}
+
+/* map `global` from host photons (a restored dump) */
+int photon_map_restore(Renderer &R, int global, const std::vector<DevPhoton> &h, cudaStream_t s)
+{
+	PhotonBufs &P = global ? R.gi : R.caust;
+	int n = (int)h.size();
+	P.map.n = 0;
+	if(n == 0) return 0;
+	PCK(P.ph.ensure((size_t)n * sizeof(DevPhoton)), "photon map");
+	PCK(P.tmp_ph.ensure((size_t)n * sizeof(DevPhoton)), "photon buffer");
+	PCK(cudaMemcpyAsync(P.ph.p, h.data(), (size_t)n * sizeof(DevPhoton), cudaMemcpyHostToDevice, s), "upload photons");
+	R.h2d += (int64_t)n * sizeof(DevPhoton);
+	return photon_map_build(R, global, n, s);
 }
 
 }  // namespace sray

@@ -14,6 +14,7 @@
  * its local terms to the pixel sample directly.
  */
 #include <math.h>
+#include <cmath>
 #include <float.h>
 #include <limits.h>
 #include <string.h>
@@ -2661,6 +2662,80 @@ int sray_gpu_get_photons(int which, float *out, int cap, int *n_out)
 		f[9] = h[i].p[3]; f[10] = h[i].d[3]; f[11] = h[i].n[3]; f[12] = 0.0f;
 		f[13] = f[14] = f[15] = 0.0f;
 	}
+	return 0;
+}
+
+/* PhotonMap::dump (src/pmap.cc:180-205): "energy %f", then per photon
+ * "<pos> <dir> <norm> <col>" with %f components */
+int sray_gpu_dump_photons(int which, const char *path)
+{
+	NEED_CTX();
+	Renderer &R = *g_R;
+	if(!path || (which != 0 && which != 1)) { g_err = "bad arguments"; return SRAY_EINVAL; }
+	const PhotonBufs &P = which ? R.gi : R.caust;
+	int n = P.map.n;
+	std::vector<DevPhoton> h(n > 0 ? n : 0);
+	if(n > 0) {
+		cudaError_t e = cudaMemcpy(h.data(), P.ph.p, (size_t)n * sizeof(DevPhoton), cudaMemcpyDeviceToHost);
+		if(e != cudaSuccess) { g_err = cudaGetErrorString(e); return SRAY_ECUDA; }
+	}
+	FILE *fp = fopen(path, "w");
+	if(!fp) { g_err = std::string("failed to dump photon map: ") + path; return SRAY_EIO; }
+	fprintf(fp, "energy %f\n", R.opt.photon_energy);
+	for(const DevPhoton &p : h) {
+		fprintf(fp, "<%f %f %f> ", p.p[0], p.p[1], p.p[2]);
+		fprintf(fp, "<%f %f %f> ", p.d[0], p.d[1], p.d[2]);
+		fprintf(fp, "<%f %f %f> ", p.n[0], p.n[1], p.n[2]);
+		fprintf(fp, "<%f %f %f>\n", p.p[3], p.d[3], p.n[3]);
+	}
+	if(fclose(fp) != 0) { g_err = std::string("failed to write photon map: ") + path; return SRAY_EIO; }
+	return 0;
+}
+
+/* PhotonMap::restore (src/pmap.cc:207-251): powers scaled by this
+ * renderer's photon_energy over the dump's; the map is built on the device
+ * over the current frame's scene bounds (sray_gpu_build first) */
+int sray_gpu_restore_photons(int which, const char *path, int *n_out)
+{
+	NEED_CTX();
+	Renderer &R = *g_R;
+	if(!path || (which != 0 && which != 1)) { g_err = "bad arguments"; return SRAY_EINVAL; }
+	if(!R.built) { g_err = "acceleration structures not built"; return SRAY_ESTATE; }
+	FILE *fp = fopen(path, "r");
+	if(!fp) { g_err = std::string("failed to open photon dump: ") + path; return SRAY_EIO; }
+	float prev = 0.0f;
+	if(fscanf(fp, "energy %f\n", &prev) < 1 || !(prev > 0.0f)) {
+		fclose(fp);
+		g_err = std::string("failed to restore photon dump: ") + path;
+		return SRAY_ELOAD;
+	}
+	float scale = R.opt.photon_energy / prev;
+	std::vector<DevPhoton> h;
+	for(;;) {
+		float v[12];
+		int res = fscanf(fp, "<%f %f %f> <%f %f %f> <%f %f %f> <%f %f %f>\n", &v[0], &v[1], &v[2], &v[3], &v[4], &v[5], &v[6], &v[7],
+				&v[8], &v[9], &v[10], &v[11]);
+		if(res == EOF) break;
+		bool finite = res == 12;
+		for(int k = 0; k < 12 && finite; k++) finite = std::isfinite(v[k]);
+		if(!finite) {
+			fclose(fp);
+			g_err = std::string("failed to restore photon dump: ") + path;
+			return SRAY_ELOAD;
+		}
+		DevPhoton p;
+		p.p[0] = v[0]; p.p[1] = v[1]; p.p[2] = v[2]; p.p[3] = v[9] * scale;
+		p.d[0] = v[3]; p.d[1] = v[4]; p.d[2] = v[5]; p.d[3] = v[10] * scale;
+		p.n[0] = v[6]; p.n[1] = v[7]; p.n[2] = v[8]; p.n[3] = v[11] * scale;
+		h.push_back(p);
+	}
+	fclose(fp);
+	if(h.size() > (size_t)INT_MAX / 2) { g_err = "photon dump too large"; return SRAY_EINVAL; }
+	int r = photon_map_restore(R, which, h, 0);
+	if(r) { g_err = R.err; return r; }
+	R.photons_ready = true;
+	R.fill_scene_desc();
+	if(n_out) *n_out = (int)h.size();
 	return 0;
 }
 

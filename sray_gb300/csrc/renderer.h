@@ -210,6 +210,9 @@ int launch_trace(Renderer &R, const DScene &D, const RayQueue &q, int n, const c
 
 /* photon.cu: both maps traced with the scene view `base` */
 int photon_shoot_maps(Renderer &R, const DScene &base, cudaStream_t s, int *caust_stored, int *gi_stored);
+/* photon.cu: map `global` (0 caustic, 1 global) over the n photons in its buffer / from host photons */
+int photon_map_build(Renderer &R, int global, int n, cudaStream_t s);
+int photon_map_restore(Renderer &R, int global, const std::vector<DevPhoton> &h, cudaStream_t s);
 
 }  // namespace sray
 

@@ -18,7 +18,7 @@ EXPORTS = ["sray_default_opts", "sray_gpu_init", "sray_gpu_set_opts", "sray_gpu_
            "sray_gpu_load_scene_sidecar",
            "sray_gpu_scene_info", "sray_gpu_build", "sray_gpu_shoot_photons", "sray_gpu_render",
            "sray_gpu_render_pixels", "sray_gpu_cast_rays", "sray_gpu_primary_hits", "sray_gpu_photon_gather", "sray_gpu_photon_gather_noalloc",
-           "sray_gpu_get_photons",
+           "sray_gpu_get_photons", "sray_gpu_dump_photons", "sray_gpu_restore_photons",
            "sray_gpu_get_stats", "sray_gpu_nrc_stats", "sray_gpu_nrc_reset", "sray_gpu_get_tuning",
            "sray_gpu_set_tuning", "sray_gpu_autotune", "sray_gpu_set_profiling", "sray_gpu_kernel_times", "sray_gpu_last_error",
            "sray_gpu_shutdown", "sray_nrc_reset", "sray_nrc_set_params", "sray_nrc_get_params", "sray_nrc_infer",
@@ -95,6 +95,8 @@ def load_library():
     L.sray_gpu_photon_gather.argtypes = [ip, ip, vp, vp, vp, vp]
     L.sray_gpu_photon_gather_noalloc.argtypes = [ip, ip, vp, vp, vp, vp]
     L.sray_gpu_get_photons.argtypes = [ip, vp, ip, vp]
+    L.sray_gpu_dump_photons.argtypes = [ip, ctypes.c_char_p]
+    L.sray_gpu_restore_photons.argtypes = [ip, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
     L.sray_gpu_get_stats.argtypes = [ctypes.POINTER(SrayStats)]
     L.sray_gpu_nrc_stats.argtypes = [ctypes.POINTER(SrayNrcStats)]
     L.sray_gpu_nrc_reset.argtypes = [ctypes.c_uint64]
@@ -274,6 +276,16 @@ class GpuRenderer:
         out = np.zeros((max(n.value, 1), 16), np.float32)
         self._chk(self.L.sray_gpu_get_photons(which, _ptr(out), n.value, ctypes.byref(n)))
         return out[:n.value]
+
+    def dump_photons(self, which, path):
+        """Write map `which` (0 caustic, 1 global) in the reference's dump format."""
+        self._chk(self.L.sray_gpu_dump_photons(which, path.encode()))
+
+    def restore_photons(self, which, path):
+        """Rebuild map `which` from a dump (after build()); returns the photon count."""
+        n = ctypes.c_int()
+        self._chk(self.L.sray_gpu_restore_photons(which, path.encode(), ctypes.byref(n)))
+        return n.value
 
     def stats(self):
         st = SrayStats()

@@ -234,3 +234,22 @@ def test_sidecar_load_renders_the_same(gpu_lib, small_scene_path, tmp_path):
     assert g.load(small_scene_path, sidecar=car)          # used
     img = g.render(0)
     assert np.abs(img - ref).max() <= 1e-6
+
+
+def test_photon_dump_restore(small_pair, tmp_path):
+    # the reference's dump format round trip: the restored map renders the
+    # same image up to the dump's 6-decimal rounding of the photon fields
+    g, _ = small_pair(width=128, height=128)
+    g.build(0, 0)
+    g.shoot_photons(0, 0)
+    ref = g.render_pixels(0)
+    ph = g.photons(0)
+    path = str(tmp_path / "caustics.dump")
+    g.dump_photons(0, path)
+    lines = open(path).read().splitlines()
+    assert lines[0].startswith("energy ") and len(lines) == 1 + len(ph)
+    assert lines[1].startswith("<") and lines[1].count("<") == 4
+    g.build(0, 0)
+    assert g.restore_photons(0, path) == len(ph)
+    img = g.render_pixels(0)
+    assert _compare(img, ref, "restored caustic map") <= 1e-3
