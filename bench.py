@@ -570,7 +570,7 @@ def run_ours(args):
         # the same frames with the radiance cache (per-region fallback), trained online
         g.set_opts(nrc=1)
         free1 = torch.cuda.mem_get_info()[0]
-        burn = 30
+        burn = args.nrc_burn_in
         for _ in range(burn):
             g.render(0, fb, stream=stream)
         torch.cuda.synchronize()
@@ -585,7 +585,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         cms = e0.elapsed_time(e1) / args.steps
         st_c = g.nrc_stats()
-        stress_cache = {"ms_per_frame": cms, "mrays_per_s": crays / args.steps / (cms / 1e3) / 1e6,
+        stress_cache = {"ms_per_frame": cms, "mrays_per_s": crays / args.steps / (cms / 1e3) / 1e6, "burn_in_frames": burn,
                         "plain_ms_per_frame": ms_step, "frames_trained": st_c["frames"],
                         "cached_vertex_frac": st_c["cached"] / max(st_c["vertices"], 1),
                         "regions_cached": st_c["regions_cached"], "val_rel_err": st_c["val_rel_err"],
