@@ -1760,6 +1760,15 @@ int Renderer::nrc_reset_regions(cudaStream_t s)
 	return 0;
 }
 
+/* training / validation records wanted per frame and the room for them */
+static void nrc_record_caps(const sray_opts &opt, int *ntrain, int *nval, int *tcap, int *vcap)
+{
+	*ntrain = opt.nrc_train_samples > 0 ? opt.nrc_train_samples : 65536;
+	*nval = *ntrain / 4 > 1024 ? *ntrain / 4 : 1024;
+	*tcap = *ntrain + *ntrain / 8 + 1024;
+	*vcap = *nval + *nval / 8 + 1024;
+}
+
 static uint32_t nrc_prob(double f)
 {
 	if(!(f > 0.0)) return 0u;
@@ -1789,10 +1798,8 @@ int Renderer::nrc_setup(int batch, int n_prim, cudaStream_t s)
 	int r = nrc_ensure_ready(opt.seed, s);
 	if(r) return fail(r, std::string("radiance cache: ") + nrc_error());
 	if(!nrc_regions_ready && (r = nrc_reset_regions(s))) return r;
-	int ntrain = opt.nrc_train_samples > 0 ? opt.nrc_train_samples : 65536;
-	int nval = ntrain / 4 > 1024 ? ntrain / 4 : 1024;
-	int tcap = ntrain + ntrain / 8 + 1024;
-	int vcap = nval + nval / 8 + 1024;
+	int ntrain, nval, tcap, vcap;
+	nrc_record_caps(opt, &ntrain, &nval, &tcap, &vcap);
 	nrc_rcap = tcap + vcap;
 	CK(nrc_rx.ensure((size_t)nrc_rcap * 9 * sizeof(float)), "radiance cache records");
 	CK(nrc_rt.ensure((size_t)nrc_rcap * 3 * sizeof(float)), "radiance cache targets");
@@ -1929,15 +1936,20 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 		CK(fbdev.ensure((size_t)npix * 16), "framebuffer");
 		fbd = fbdev.as<float4>();
 	}
-	/* a vertex may send both its image's diffuse rays (the fallback count in
-	 * a fallback region) and a record's */
-	int img_rays = ds, rec_rays = 0;
-	if(opt.nrc) {
+	/* a vertex sends its image's diffuse rays (the fallback count in a
+	 * fallback region); the records' rays come on top, bounded by the record
+	 * count of a frame */
+	int img_rays = ds;
+	int64_t rec_extra = 0;
+	if(opt.nrc && opt.gi_photons) {
 		int fb = opt.nrc_fallback_samples > MAX_DS ? MAX_DS : opt.nrc_fallback_samples;
 		img_rays = fb > ds ? fb : ds;
-		rec_rays = ds > NRC_VAL_RAYS ? ds : NRC_VAL_RAYS;
+		int rec_rays = ds > NRC_VAL_RAYS ? ds : NRC_VAL_RAYS;
+		int ntrain, nval, tcap, vcap;
+		nrc_record_caps(opt, &ntrain, &nval, &tcap, &vcap);
+		rec_extra = (int64_t)(tcap + vcap) * rec_rays;
 	}
-	int per_ray_children = 2 + (opt.gi_photons ? img_rays + rec_rays : 0);
+	int per_ray_children = 2 + (opt.gi_photons ? img_rays : 0);
 	int shadow_per_ray = 0;
 	for(size_t li = 0; li < sc.lights.size(); li++) shadow_per_ray += sc.lights[li].type != LT_POINT ? opt.shadow_samples : 1;
 	if(shadow_per_ray < 1) shadow_per_ray = 1;
@@ -2065,7 +2077,8 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 				cur ^= 1;
 				continue;
 			}
-			int need = n_rays * per_ray_children;
+			int64_t need64 = (int64_t)n_rays * per_ray_children + rec_extra;
+			int need = need64 > INT_MAX / 2 ? INT_MAX / 2 : (int)need64;
 			if(need < n_rays) need = n_rays;
 			int r = ensure_queue(cur ^ 1, need);
 			if(r) return r;
