@@ -304,6 +304,28 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 /* Copy the last error message (NUL-terminated, truncated to `cap`). */
 int sray_gpu_last_error(char *buf, size_t cap);
 
+/* A batch of frames of the loaded scene in one wavefront (extension; the
+ * reference renders one frame per render() call, src/render.cc:34-55).
+ * Each job has its own frame time, resolution and device framebuffer
+ * (width * height * 4 floats); the jobs share the options (samples, photon
+ * counts) and the camera (its aspect is the one set at load, as for a
+ * single frame).  The acceleration structures are built once over the union of
+ * the jobs' shutter intervals, each job gets its own photon maps (shot over
+ * its own interval), and all jobs' pixels go through the same camera,
+ * closest-hit, shading, shadow and gather launches and the same adaptive
+ * sample batches.  A job's image equals the one sray_gpu_render gives for
+ * it alone, except that its random streams are keyed by its pixel's index
+ * in the batch (job j's pixels follow those of jobs 0..j-1): job 0 matches
+ * exactly. */
+typedef struct sray_job {
+	long msec;
+	int width, height;
+	float *fb;                /* device framebuffer */
+	int reserved[4];
+} sray_job;
+
+int sray_gpu_render_batch(const sray_job *jobs, int n, void *stream);
+
 /* Release every device buffer and the context. */
 void sray_gpu_shutdown(void);
 

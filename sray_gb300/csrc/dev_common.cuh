@@ -65,6 +65,13 @@ struct DNrc {
 	unsigned long long *counters;     /* [0] final-gather vertices, [1] cached */
 };
 
+/* one job of a batch (sray_gpu_render_batch): its pixels are
+ * [pix0, pix0 + width * height) of the batch's pixel space */
+struct DevJob {
+	int pix0, width, height, t0;
+	float cam_f, cam_xsz, cam_ysz, pad;
+};
+
 struct DScene {
 	const DevNode *snodes;    /* top-level octree (world space) */
 	const int *sslots;
@@ -108,7 +115,25 @@ struct DScene {
 	float max_cos;
 	DPhotonMap caust, gi;
 	DNrc nrc;
+	/* a batch of jobs (njobs > 0): the jobs and their photon maps, caustic
+	 * and global of job j at maps[2j], maps[2j + 1]; a gather request's kind
+	 * is then the map index */
+	int njobs;
+	const DevJob *jobs;
+	const DPhotonMap *maps;
 };
+
+/* the job of a pixel of the batch's pixel space */
+__device__ __forceinline__ int job_of(const DScene &S, int pixel)
+{
+	int lo = 0, hi = S.njobs - 1;
+	while(lo < hi) {
+		int mid = (lo + hi + 1) >> 1;
+		if(S.jobs[mid].pix0 <= pixel) lo = mid;
+		else hi = mid - 1;
+	}
+	return lo;
+}
 
 /* ---------------- float3 helpers (no contraction: built with -fmad=false) */
 struct V3 { float x, y, z; };

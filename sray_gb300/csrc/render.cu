@@ -55,17 +55,25 @@ __global__ void k_camera(DScene S, const int *active, const int *n_active_p, int
 		int a = i / width, j = i - a * width;
 		int p = active ? active[a] : a;
 		int sample = s0 + j;
-		int x = p % S.width, y = p / S.width;
+		int W = S.width, Hh = S.height, lp = p, t0 = S.t0;
+		float cam_f = S.cam_f, xsz = S.cam_xsz, ysz = S.cam_ysz;
+		if(S.njobs > 0) {
+			/* a batch: the job's resolution, camera aspect and frame time */
+			const DevJob &J = S.jobs[job_of(S, p)];
+			W = J.width; Hh = J.height; lp = p - J.pix0; t0 = J.t0;
+			cam_f = J.cam_f; xsz = J.cam_xsz; ysz = J.cam_ysz;
+		}
+		int x = lp % W, y = lp / W;
 		sray_rng s;
 		sray_rng_init(&s, S.seed, SRAY_DOM_PIXEL, (uint32_t)p, (uint32_t)sample);
-		float px = ((float)x / (float)S.width) * S.cam_xsz - S.cam_xsz / 2.0f;
-		float py = 1.0f - ((float)y / (float)S.height) * S.cam_ysz;
+		float px = ((float)x / (float)W) * xsz - xsz / 2.0f;
+		float py = 1.0f - ((float)y / (float)Hh) * ysz;
 		if(sample > 0) {
-			px = px + S.cam_xsz * (frand(&s, 1.0f) - 0.5f) / (float)S.width;
-			py = py + S.cam_ysz * (frand(&s, 1.0f) - 0.5f) / (float)S.height;
+			px = px + xsz * (frand(&s, 1.0f) - 0.5f) / (float)W;
+			py = py + ysz * (frand(&s, 1.0f) - 0.5f) / (float)Hh;
 		}
-		V3 d = mk(px, py, S.cam_f) * S.cam_maxd;
-		int time = S.t0;
+		V3 d = mk(px, py, cam_f) * S.cam_maxd;
+		int time = t0;
 		if(S.mblur && sample > 0 && S.shutter > 0) time += sray_rng_int(&s) % S.shutter - S.shutter / 2;
 		const float *m = S.cam_m + (size_t)time_index(S, time) * 12;
 		V3 o = mul_pt(m, mk(0.0f, 0.0f, 0.0f));
@@ -351,7 +359,7 @@ __device__ __forceinline__ void shade_one(const DScene &S, const RayRec &ray, co
 	const float *kd = mat.kd, *ks = mat.ks;
 	if(iter == DIFFUSE_ITER) {
 		/* final-gather ray: radiance_est(...) * kd */
-		em.gather(sp.pos, normal, 1, aslot, w[0] * kd[0], w[1] * kd[1], w[2] * kd[2]);
+		em.gather(sp.pos, normal, S.njobs > 0 ? 2 * job_of(S, pixel) + 1 : 1, aslot, w[0] * kd[0], w[1] * kd[1], w[2] * kd[2]);
 		return;
 	}
 	float energy = ray.energy;
@@ -479,7 +487,7 @@ __device__ __forceinline__ void shade_one(const DScene &S, const RayRec &ray, co
 		em.child(make_child(ray, sp.pos, td, trans_energy, iter - 1, path * 4 + 1, 0, cs, w[0] * ks[0] * g, w[1] * ks[1] * g,
 				w[2] * ks[2] * g));
 	}
-	if(S.caust_on) em.gather(sp.pos, normal, 0, aslot, w[0], w[1], w[2]);
+	if(S.caust_on) em.gather(sp.pos, normal, S.njobs > 0 ? 2 * job_of(S, pixel) : 0, aslot, w[0], w[1], w[2]);
 }
 
 /* the wavefront emitter: everything goes to the next pass's queues */
@@ -919,7 +927,9 @@ __device__ __noinline__ int gather_narrow(const DPhotonMap &M, const GatherCells
 __device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *keys, int *idx, int *hist, float out[3],
 		GatherWork &gw)
 {
-	const DPhotonMap &M = kind == 0 ? S.caust : S.gi;
+	/* in a batch the request's kind is the index of its job's map */
+	const DPhotonMap &M = S.maps ? S.maps[kind] : (kind == 0 ? S.caust : S.gi);
+	kind &= 1;
 	int lane = threadIdx.x & 31;
 	unsigned lt_mask = (1u << lane) - 1u;
 	out[0] = out[1] = out[2] = 0.0f;
@@ -1550,8 +1560,8 @@ int Renderer::shoot_maps(const DScene &base, cudaStream_t s, int *nc, int *ng)
 	gi.map.n = 0;
 	*nc = *ng = 0;
 	if(!(opt.caust_photons || opt.gi_photons) || sc.lights.empty()) return 0;
-	/* projection maps (src/render.cc:87-103) */
-	sc.build_projmaps(t0, t1, opt.seed);
+	/* projection maps (src/render.cc:87-103) over the photons' interval */
+	sc.build_projmaps(base.t0, base.t1, opt.seed);
 	std::vector<uint32_t> bits(sc.lights.size() * 128, 0u);
 	std::vector<float> cov(sc.lights.size() * 2);
 	for(size_t i = 0; i < sc.lights.size(); i++) {
@@ -1917,7 +1927,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 	(void)msec;
 	if(!built || (!photons_ready && !overlap_photons)) return fail(SRAY_ESTATE, "frame not prepared (build and shoot photons first)");
 	bool photons_pending = overlap_photons;
-	int npix = opt.width * opt.height;
+	int npix = batch_npix > 0 ? batch_npix : opt.width * opt.height;
 	int ds = opt.diffuse_samples < 0 ? 0 : (opt.diffuse_samples > MAX_DS ? MAX_DS : opt.diffuse_samples);
 	int maxs = opt.max_samples < 1 ? 1 : opt.max_samples;
 	CK(ctr.ensure(sizeof(DevCounters)), "counters");
@@ -2207,6 +2217,77 @@ int Renderer::photon_stream()
 	if(ps) return 0;
 	CK(cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking), "photon stream");
 	CK(cudaEventCreateWithFlags(&ps_done, cudaEventDisableTiming), "photon event");
+	return 0;
+}
+
+/* a batch of jobs in one wavefront (sray_gpu_render_batch) */
+int Renderer::render_batch(const sray_job *jobs, int n, cudaStream_t s)
+{
+	if(!loaded) return fail(SRAY_ESTATE, "no scene loaded");
+	if(!jobs || n < 1 || n > 4096) return fail(SRAY_EINVAL, "a batch holds 1 to 4096 jobs");
+	long shutter = sc.cam.shutter;
+	std::vector<DevJob> hj(n);
+	std::vector<long> f0(n), f1(n);
+	int64_t total = 0;
+	long bt0 = 0, bt1 = 0;
+	for(int j = 0; j < n; j++) {
+		const sray_job &J = jobs[j];
+		if(J.width <= 0 || J.height <= 0 || !J.fb) return fail(SRAY_EINVAL, "bad job");
+		f0[j] = J.msec - shutter / 2;
+		f1[j] = f0[j] + shutter;
+		bt0 = j ? std::min(bt0, f0[j]) : f0[j];
+		bt1 = j ? std::max(bt1, f1[j]) : f1[j];
+		DevJob &d = hj[j];
+		memset(&d, 0, sizeof d);
+		d.pix0 = (int)total;
+		d.width = J.width;
+		d.height = J.height;
+		d.t0 = (int)f0[j];
+		d.cam_f = (float)(1.0 / tan(0.5 * sc.cam.vfov));
+		d.cam_xsz = (float)(sc.cam.aspect * 2.0);   /* the camera's aspect, as for a single frame */
+		d.cam_ysz = 2.0f;
+		total += (int64_t)J.width * J.height;
+		if(total > (1 << 27)) return fail(SRAY_EINVAL, "a batch holds at most 2^27 pixels");
+	}
+	int r = build_frame(bt0, bt1, s);
+	if(r) return r;
+	/* each job's photon maps, shot over its own interval */
+	if(job_maps.size() < (size_t)n) job_maps.resize(n);   /* kept: their buffers are reused by the next batch */
+	std::vector<DPhotonMap> hm(2 * (size_t)n);
+	for(int j = 0; j < n; j++) {
+		DScene base = S;
+		base.t0 = (int)f0[j];
+		base.t1 = (int)f1[j];
+		int c = 0, g = 0;
+		if((r = shoot_maps(base, s, &c, &g))) return r;
+		std::swap(caust, job_maps[j].caust);
+		std::swap(gi, job_maps[j].gi);
+		hm[2 * j] = job_maps[j].caust.map;
+		hm[2 * j + 1] = job_maps[j].gi.map;
+	}
+	caust.map.n = 0;
+	gi.map.n = 0;
+	CK(djobs.upload(hj, s), "job table");
+	CK(dmaps.upload(hm, s), "job photon maps");
+	h2d += (int64_t)(hj.size() * sizeof(DevJob) + hm.size() * sizeof(DPhotonMap));
+	CK(fbdev.ensure((size_t)total * 16), "batch framebuffer");
+	fill_scene_desc();
+	S.njobs = n;
+	S.jobs = djobs.as<DevJob>();
+	S.maps = dmaps.as<DPhotonMap>();
+	batch_npix = (int)total;
+	photons_ready = true;
+	r = render_pixels(bt0, fbdev.as<float>(), 1, s, false);
+	S.njobs = 0;
+	S.jobs = nullptr;
+	S.maps = nullptr;
+	batch_npix = 0;
+	photons_ready = false;
+	if(r) return r;
+	for(int j = 0; j < n; j++)
+		CK(cudaMemcpyAsync(jobs[j].fb, fbdev.as<float4>() + hj[j].pix0, (size_t)hj[j].width * hj[j].height * 16,
+				cudaMemcpyDeviceToDevice, s), "job framebuffer");
+	CK(cudaStreamSynchronize(s), "batch");
 	return 0;
 }
 
@@ -2525,6 +2606,18 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 	if(n_log) *n_log = (int)done.size();
 	for(int i = 0; log && i < log_cap && i < (int)done.size(); i++) log[i] = done[i];
 	return 0;
+}
+
+int sray_gpu_render_batch(const sray_job *jobs, int n, void *stream)
+{
+	NEED_CTX();
+	Renderer &R = *g_R;
+	long long l0 = R.launch_count;
+	R.h2d = R.d2h = 0;
+	int r = R.render_batch(jobs, n, as_stream(stream));
+	if(r) g_err = R.err;
+	else R.stats.kernel_launches = (int)(R.launch_count - l0);
+	return r;
 }
 
 int sray_gpu_cast_rays(int n, const float *orig, const float *dir, const int *time, int *obj, int *prim, float *t,
@@ -2849,6 +2942,16 @@ void sray_gpu_shutdown(void)
 	if(!g_R) return;
 	Renderer &R = *g_R;
 	if(R.photon_thread.joinable()) R.photon_thread.join();
+	for(Renderer::JobMaps &jm : R.job_maps) {
+		PhotonBufs *jp[] = {&jm.caust, &jm.gi};
+		for(PhotonBufs *p : jp) {
+			DevBuf *pbufs[] = {&p->ph, &p->cells, &p->tmp_ph, &p->valid, &p->keys, &p->keys2, &p->vals, &p->vals2, &p->lin, &p->hist,
+				&p->scan, &p->prefix, &p->scale};
+			for(DevBuf *b : pbufs) b->release();
+		}
+	}
+	R.djobs.release();
+	R.dmaps.release();
 	DevBuf *bufs[] = {&R.mnodes, &R.mtris, &R.mprim, &R.tri_pos, &R.tri_attr, &R.objs, &R.mats, &R.lights, &R.snodes, &R.sslots,
 		&R.xf, &R.light_pos, &R.cam_m, &R.projbits, &R.coverage, &R.qbuf[0], &R.qbuf[1], &R.hits, &R.gq, &R.sq, &R.acc, &R.hist, &R.sums,
 		&R.active[0], &R.active[1], &R.spp, &R.fbdev, &R.ctr, &R.counts, &R.bnodes, &R.btris, &R.bprim, &R.bhome,

@@ -143,6 +143,13 @@ struct Renderer {
 	int64_t nrc_expect = 0;       /* final-gather vertices of the last frame's first sample batch */
 	int nrc_last_train = 0, nrc_last_val = 0;
 	int64_t nrc_last_vertices = 0, nrc_last_cached = 0;
+	/* a batch of jobs (render_batch): their pixel count, job table, photon
+	 * maps (caustic and global per job) */
+	struct JobMaps { PhotonBufs caust, gi; };
+	int batch_npix = 0;
+	DevBuf djobs, dmaps;
+	std::vector<JobMaps> job_maps;
+	int render_batch(const sray_job *jobs, int n, cudaStream_t s);
 	int nrc_setup(int batch, int n_prim, cudaStream_t s);
 	int nrc_batch_done(int batch, cudaStream_t s);
 	int nrc_reset_regions(cudaStream_t s);

@@ -18,7 +18,7 @@ EXPORTS = ["sray_default_opts", "sray_gpu_init", "sray_gpu_set_opts", "sray_gpu_
            "sray_gpu_load_scene_sidecar",
            "sray_gpu_scene_info", "sray_gpu_build", "sray_gpu_shoot_photons", "sray_gpu_render",
            "sray_gpu_render_pixels", "sray_gpu_cast_rays", "sray_gpu_primary_hits", "sray_gpu_photon_gather", "sray_gpu_photon_gather_noalloc",
-           "sray_gpu_get_photons", "sray_gpu_dump_photons", "sray_gpu_restore_photons",
+           "sray_gpu_get_photons", "sray_gpu_dump_photons", "sray_gpu_restore_photons", "sray_gpu_render_batch",
            "sray_gpu_get_stats", "sray_gpu_nrc_stats", "sray_gpu_nrc_reset", "sray_gpu_get_tuning",
            "sray_gpu_set_tuning", "sray_gpu_autotune", "sray_gpu_set_profiling", "sray_gpu_kernel_times", "sray_gpu_last_error",
            "sray_gpu_shutdown", "sray_nrc_reset", "sray_nrc_set_params", "sray_nrc_get_params", "sray_nrc_infer",
@@ -47,6 +47,11 @@ class SrayNrcStats(ctypes.Structure):
                 ("regions", ctypes.c_int), ("regions_validated", ctypes.c_int), ("regions_cached", ctypes.c_int),
                 ("val_rel_err", ctypes.c_float), ("loss", ctypes.c_float), ("pad", ctypes.c_int),
                 ("reserved", ctypes.c_int64 * 4)]
+
+
+class SrayJob(ctypes.Structure):
+    _fields_ = [("msec", ctypes.c_long), ("width", ctypes.c_int), ("height", ctypes.c_int), ("fb", ctypes.c_void_p),
+                ("reserved", ctypes.c_int * 4)]
 
 
 class SrayTuning(ctypes.Structure):
@@ -96,6 +101,7 @@ def load_library():
     L.sray_gpu_photon_gather_noalloc.argtypes = [ip, ip, vp, vp, vp, vp]
     L.sray_gpu_get_photons.argtypes = [ip, vp, ip, vp]
     L.sray_gpu_dump_photons.argtypes = [ip, ctypes.c_char_p]
+    L.sray_gpu_render_batch.argtypes = [ctypes.POINTER(SrayJob), ip, vp]
     L.sray_gpu_restore_photons.argtypes = [ip, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
     L.sray_gpu_get_stats.argtypes = [ctypes.POINTER(SrayStats)]
     L.sray_gpu_nrc_stats.argtypes = [ctypes.POINTER(SrayNrcStats)]
@@ -238,6 +244,16 @@ class GpuRenderer:
             return fb
         self._chk(self.L.sray_gpu_render(msec, _ptr(fb), 1, _stream(stream)))
         return fb
+
+    def render_batch(self, jobs, stream=None):
+        """Render several frames in one wavefront: jobs = [(msec, fb)], fb a
+        CUDA tensor [height, width, 4] float32 per job."""
+        arr = (SrayJob * len(jobs))()
+        for i, (msec, fb) in enumerate(jobs):
+            arr[i].msec = msec
+            arr[i].height, arr[i].width = int(fb.shape[0]), int(fb.shape[1])
+            arr[i].fb = fb.data_ptr()
+        self._chk(self.L.sray_gpu_render_batch(arr, len(jobs), _stream(stream)))
 
     def render_pixels(self, msec=0, fb=None, stream=None):
         if fb is None:

@@ -260,3 +260,24 @@ def test_photon_dump_restore(small_pair, tmp_path):
     _compare(img, ref, "restored caustic map")
     rel = np.abs(img[..., :3] - ref[..., :3]) / np.maximum(np.abs(ref[..., :3]), 1e-3)
     assert rel.max() <= 1e-2
+
+
+def test_batch_jobs_match_single_frames(gpu_lib, small_scene_path):
+    # jobs of different sizes in one wavefront; at 1 spp without global
+    # photons the small scene's image draws nothing per pixel, so each job
+    # equals its own single render (job 0 would match at any spp: its
+    # pixels keep their streams)
+    sizes = [(96, 96), (64, 48), (128, 72)]
+    g = gpu_lib.GpuRenderer(**_opts(width=96, height=96))
+    g.load(small_scene_path)
+    fbs = [torch.zeros((h, w, 4), dtype=torch.float32, device="cuda") for w, h in sizes]
+    g.render_batch([(0, fb) for fb in fbs])
+    st = g.stats()
+    for (w, h), fb in zip(sizes, fbs):
+        g.set_opts(width=w, height=h)
+        ref = torch.zeros((h, w, 4), dtype=torch.float32, device="cuda")
+        g.render(0, ref)
+        d = np.abs(fb.cpu().numpy() - ref.cpu().numpy()).max()
+        print("batch job %dx%d: max abs difference to its own frame %.3g" % (w, h, d))
+        assert d <= 1e-5
+    assert st["primary_rays"] == sum(w * h for w, h in sizes)
