@@ -43,7 +43,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="production", choices=["production", "small", "learned", "stress"])
+    ap.add_argument("--config", default="production", choices=["production", "small", "learned", "stress", "batch"])
+    ap.add_argument("--batch-jobs", type=int, default=16, help="jobs of the batch configuration")
     ap.add_argument("--no-nrc", action="store_true", help="skip the radiance-cache comparison")
     ap.add_argument("--method", default="plain", choices=["plain", "cache", "cache-everywhere"],
                     help="final gather of the headline frames: the plain gather, the radiance cache with its "
@@ -371,6 +372,82 @@ def nrc_vs_plain(args, reference):
     return out
 
 
+BATCH_SIZES = [(256, 256), (512, 512), (1280, 720), (1920, 1080)]
+
+
+def run_batch(args):
+    """Batched frames: `--batch-jobs` jobs of the production scene with
+    resolutions cycling through 256^2, 512^2, 720p and 1080p, frame times 40
+    ms apart, adaptive 1-16 spp, 200k global + 50k caustic photons per job,
+    rendered in one wavefront (sray_gpu_render_batch) against the same jobs
+    rendered one after another (sray_gpu_render)."""
+    import torch
+    from sray_gb300 import build as gbuild, gpu, scenegen
+    torch.cuda.set_device(0)
+    gbuild.build()
+    opts = scenegen.scene_opts("production", caust_photons=50000, gi_photons=200000)
+    path = scenegen.write_scene("production")
+    g = gpu.GpuRenderer(**opts)
+    g.load(path)
+    stream = torch.cuda.current_stream()
+    sizes = [BATCH_SIZES[i % len(BATCH_SIZES)] for i in range(args.batch_jobs)]
+    fbs = [torch.zeros((h, w, 4), dtype=torch.float32, device="cuda") for w, h in sizes]
+    jobs = [(40 * i, fb) for i, fb in enumerate(fbs)]
+
+    def timed(fn, n):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        rays = 0
+        for _ in range(n):
+            rays += fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n, rays / n
+
+    def batch():
+        g.render_batch(jobs, stream=stream)
+        return rays_of(g.stats())
+
+    def singles():
+        r = 0
+        for (w, h), (msec, fb) in zip(sizes, jobs):
+            g.set_opts(width=w, height=h)
+            g.render(msec, fb, stream=stream)
+            r += rays_of(g.stats())
+        return r
+
+    for _ in range(args.warmup):
+        batch()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    ms_b, rays_b = timed(batch, args.steps)
+    clk = clocks.stop()
+    launches = g.stats()["kernel_launches"]
+    singles()
+    ms_s, rays_s = timed(singles, args.steps)
+    g.close()
+    line = {
+        "metric": METRIC, "value": rays_b / (ms_b / 1e3) / 1e6, "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_b, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded scene generator, no dataset)",
+        "config": {"workload": "batch: %d jobs of the production scene (resolutions cycling 256^2, 512^2, 1280x720, "
+                               "1920x1080; frames 40 ms apart; adaptive 1-16 spp; 200k global + 50k caustic photons "
+                               "per job) in one wavefront" % args.batch_jobs,
+                   "method": "plain gather", "jobs": [list(sz) for sz in sizes]},
+        "batch_vs_single": {"batch_ms": ms_b, "single_frames_ms": ms_s, "speedup": ms_s / ms_b,
+                            "batch_mrays_per_s": rays_b / (ms_b / 1e3) / 1e6,
+                            "single_mrays_per_s": rays_s / (ms_s / 1e3) / 1e6},
+        "gpu_launches": launches, "clocks": clk,
+        "e2e": None, "roofline": None, "cpu_baseline": None,
+        "note": "a step renders every job once; e2e, roofline and the CPU baseline are reported for the "
+                "production configuration",
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -660,6 +737,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == "batch":
+        return run_batch(args)
     return run_ours(args)
 
 
