@@ -1585,7 +1585,26 @@ int Renderer::shoot_maps(const DScene &base, cudaStream_t s, int *nc, int *ng)
 int Renderer::photon_job(DScene base)
 {
 	int c = 0, g = 0;
-	return shoot_maps(base, ps, &c, &g);
+	if(batch_t0.empty()) return shoot_maps(base, ps, &c, &g);
+	/* a batch: each job's maps over its own interval, then their table */
+	size_t n = batch_t0.size();
+	std::vector<DPhotonMap> hm(2 * n);
+	for(size_t j = 0; j < n; j++) {
+		base.t0 = batch_t0[j];
+		base.t1 = batch_t1[j];
+		int r = shoot_maps(base, ps, &c, &g);
+		if(r) return r;
+		std::swap(caust, job_maps[j].caust);
+		std::swap(gi, job_maps[j].gi);
+		hm[2 * j] = job_maps[j].caust.map;
+		hm[2 * j + 1] = job_maps[j].gi.map;
+	}
+	caust.map.n = 0;
+	gi.map.n = 0;
+	CK(dmaps.upload(hm, ps), "job photon maps");
+	CK(cudaStreamSynchronize(ps), "job photon maps");
+	h2d += (int64_t)(hm.size() * sizeof(DPhotonMap));
+	return 0;
 }
 
 /* start tracing the photon maps on the photon stream from a host thread of
@@ -1611,6 +1630,7 @@ int Renderer::finish_photon_job()
 	if(photon_rc) return photon_rc;
 	photons_ready = true;
 	fill_scene_desc();
+	if(!batch_t0.empty()) S.maps = dmaps.as<DPhotonMap>();   /* the batch's map table */
 	return 0;
 }
 
@@ -2251,37 +2271,27 @@ int Renderer::render_batch(const sray_job *jobs, int n, cudaStream_t s)
 	}
 	int r = build_frame(bt0, bt1, s);
 	if(r) return r;
-	/* each job's photon maps, shot over its own interval */
+	/* each job's photon maps, shot over its own interval by the photon
+	 * thread while the batch's first bounces run (their gathers wait) */
 	if(job_maps.size() < (size_t)n) job_maps.resize(n);   /* kept: their buffers are reused by the next batch */
-	std::vector<DPhotonMap> hm(2 * (size_t)n);
-	for(int j = 0; j < n; j++) {
-		DScene base = S;
-		base.t0 = (int)f0[j];
-		base.t1 = (int)f1[j];
-		int c = 0, g = 0;
-		if((r = shoot_maps(base, s, &c, &g))) return r;
-		std::swap(caust, job_maps[j].caust);
-		std::swap(gi, job_maps[j].gi);
-		hm[2 * j] = job_maps[j].caust.map;
-		hm[2 * j + 1] = job_maps[j].gi.map;
-	}
-	caust.map.n = 0;
-	gi.map.n = 0;
+	batch_t0.assign(f0.begin(), f0.end());
+	batch_t1.assign(f1.begin(), f1.end());
 	CK(djobs.upload(hj, s), "job table");
-	CK(dmaps.upload(hm, s), "job photon maps");
-	h2d += (int64_t)(hj.size() * sizeof(DevJob) + hm.size() * sizeof(DPhotonMap));
+	CK(dmaps.ensure(2 * (size_t)n * sizeof(DPhotonMap)), "job photon maps");
+	h2d += (int64_t)(hj.size() * sizeof(DevJob));
 	CK(fbdev.ensure((size_t)total * 16), "batch framebuffer");
-	fill_scene_desc();
+	CK(cudaStreamSynchronize(s), "job table");
 	S.njobs = n;
 	S.jobs = djobs.as<DevJob>();
-	S.maps = dmaps.as<DPhotonMap>();
+	S.maps = nullptr;
 	batch_npix = (int)total;
-	photons_ready = true;
-	r = render_pixels(bt0, fbdev.as<float>(), 1, s, false);
+	r = render_pixels(bt0, fbdev.as<float>(), 1, s, true);
 	S.njobs = 0;
 	S.jobs = nullptr;
 	S.maps = nullptr;
 	batch_npix = 0;
+	batch_t0.clear();
+	batch_t1.clear();
 	photons_ready = false;
 	if(r) return r;
 	for(int j = 0; j < n; j++)

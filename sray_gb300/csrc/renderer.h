@@ -147,6 +147,7 @@ struct Renderer {
 	 * maps (caustic and global per job) */
 	struct JobMaps { PhotonBufs caust, gi; };
 	int batch_npix = 0;
+	std::vector<int> batch_t0, batch_t1;   /* jobs' shutter intervals: the photon job shoots one map pair each */
 	DevBuf djobs, dmaps;
 	std::vector<JobMaps> job_maps;
 	int render_batch(const sray_job *jobs, int n, cudaStream_t s);
