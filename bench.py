@@ -163,6 +163,14 @@ def peaks():
         return FALLBACK_HBM, "fallback"
 
 
+def bf16_peak():
+    try:
+        with open(PEAKS_PATH) as f:
+            return float(json.load(f)["bf16_tflops"])
+    except (OSError, KeyError, ValueError):
+        return 1900.0
+
+
 def rays_of(st):
     return st["primary_rays"] + st["secondary_rays"] + st["shadow_rays"]
 
@@ -361,6 +369,12 @@ def nrc_vs_plain(args, reference):
                "val_rel_err": st["val_rel_err"], "loss": st["loss"],
                "nrc_ms_per_frame": {k: round(v[0] / steps, 3) for k, v in kt.items() if k.startswith("nrc")},
                "gather_ms_per_frame": round(kt.get("gather", (0.0, 0))[0] / steps, 3)}
+        # roofline of the query kernel: 2 x 26,304 FLOP per query against the measured bf16 peak
+        q_ms = kt.get("nrc_query", (0.0, 0))[0] / steps
+        if q_ms > 0 and st["cached"] > 0:
+            tf = st["cached"] * 2 * 26304 / (q_ms / 1e3) / 1e12
+            res["query_roofline"] = {"bound": "tensor", "achieved": tf, "peak": bf16_peak(), "unit": "TFLOP/s",
+                                     "frac": tf / bf16_peak(), "queries_per_frame": st["cached"], "ms_per_frame": q_ms}
         if res["rmse"] is not None:
             pts = [(p["diffuse_samples"], p["ms_per_frame"], p["rmse"]) for p in ladder]
             pms, pds, ok = equal_rmse_time(pts, res["rmse"])
