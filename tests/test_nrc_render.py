@@ -108,3 +108,26 @@ def test_validation_catches_a_wrong_network(learned, gpu_lib):
         after["cached"] / after["vertices"]))
     assert after["regions_cached"] == 0
     assert after["cached"] <= 0.02 * after["vertices"]
+
+
+def test_cache_with_adaptive_sampling_and_two_batches(gpu_lib):
+    # the production scene (reduced): two sample batches, area lights; the
+    # cache queries both batches, records come from the first, and the
+    # frame stays finite and close to the plain gather's (same estimator in
+    # expectation; the untrained cache falls back everywhere at first)
+    opts = scenegen.scene_opts("production", width=160, height=90, caust_photons=20000, gi_photons=80000, max_samples=4)
+    g = gpu_lib.GpuRenderer(**opts)
+    g.load(scenegen.write_scene("production"))
+    plain = g.render(0)
+    g.set_opts(nrc=1)
+    g.nrc_reset(5)
+    first = g.render(0)
+    assert np.abs(first - plain).max() <= 1e-5          # nothing validated yet: the plain gather everywhere
+    g.set_opts(nrc=2)
+    for _ in range(30):
+        img = g.render(0)
+    st = g.nrc_stats()
+    assert np.isfinite(img).all() and st["cached"] == st["vertices"] > 0 and st["train_samples"] > 0
+    d = img[..., :3] - plain[..., :3]
+    print("production 160x90, cache after 30 frames: rmse against the plain gather %.4f" % np.sqrt(np.mean(d * d)))
+    g.close()
