@@ -1512,10 +1512,19 @@ int Renderer::build_frame(long bt0, long bt1, cudaStream_t s)
 	nt = thi - tlo + 1;
 	std::vector<float> xfs((size_t)sc.objs.size() * nt * XF_STRIDE);
 	for(size_t i = 0; i < sc.objs.size(); i++) {
+		float *row = &xfs[(size_t)i * nt * XF_STRIDE];
+		if(sc.objs[i].is_static) {
+			/* at most one key per track: the same matrices at every time */
+			double m[4][4];
+			sc.objs[i].xf.matrix(tlo, m);
+			pack_xf(m, row);
+			for(int t = 1; t < nt; t++) memcpy(row + (size_t)t * XF_STRIDE, row, XF_STRIDE * sizeof(float));
+			continue;
+		}
 		for(int t = 0; t < nt; t++) {
 			double m[4][4];
 			sc.objs[i].xf.matrix(tlo + t, m);
-			pack_xf(m, &xfs[((size_t)i * nt + t) * XF_STRIDE]);
+			pack_xf(m, row + (size_t)t * XF_STRIDE);
 		}
 	}
 	std::vector<float> lp((size_t)sc.lights.size() * nt * 4);
