@@ -95,6 +95,18 @@ def workload_desc(cfg):
             "100k caustic photons, k=50 gather")
 
 
+def reduce_over_ranks(ms_total, rays, e2e_s, e2e_rays, device="cpu"):
+    """Replicas: the job's time is the slowest rank's, its work the sum of
+    all ranks' (so value = all rays / max time)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms_total, rays, e2e_s, e2e_rays], dtype=torch.float64, device=device)
+    tmax, tsum = t.clone(), t.clone()
+    dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
+    return float(tmax[0]), float(tsum[1]), float(tmax[2]), float(tsum[3])
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -592,13 +604,7 @@ def run_ours(args):
 
     if ws > 1:
         import torch.distributed as dist
-        t = torch.tensor([ms_total, rays, e2e_s, e2e_rays], dtype=torch.float64, device="cuda")
-        tmax = t.clone()
-        dist.all_reduce(tmax[0:1], op=dist.ReduceOp.MAX)
-        dist.all_reduce(tmax[2:3], op=dist.ReduceOp.MAX)
-        dist.all_reduce(tmax[1:2], op=dist.ReduceOp.SUM)
-        dist.all_reduce(tmax[3:4], op=dist.ReduceOp.SUM)
-        ms_total, rays, e2e_s, e2e_rays = [float(x) for x in tmax.tolist()]
+        ms_total, rays, e2e_s, e2e_rays = reduce_over_ranks(ms_total, rays, e2e_s, e2e_rays, device="cuda")
         ms_step = ms_total / args.steps
     value = rays / (ms_total / 1e3) / 1e6
     e2e_value = e2e_rays / e2e_s / 1e6
