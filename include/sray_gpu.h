@@ -107,6 +107,16 @@ int sray_gpu_load_scene_mem(const char *xml, size_t len);
  * the side-car was used. */
 int sray_gpu_load_scene_sidecar(const char *xml_path, const char *sidecar, int *used);
 
+/* Prepend a directory to the texture search path SRAY_DATA_PATH, as
+ * add_path does (src/datapath.c:40-51); sray prepends the scene file's
+ * directory before loading it (src/sray.cc:101-112).  Textures named by a
+ * material attribute's "map" are searched in the FIRST directory of the
+ * list only, as the reference's find_file does (src/datapath.c:57-113); a
+ * texture that is not found leaves its attribute untextured
+ * (src/material.cc:64-72).  Binary PPM (P6) files are read.  Affects the
+ * next scene load. */
+int sray_gpu_add_data_path(const char *dir);
+
 /* Scene summary: counts of objects, lights, materials, triangles (summed
  * over mesh objects), unique device meshes. */
 int sray_gpu_scene_info(int *n_objects, int *n_lights, int *n_materials,

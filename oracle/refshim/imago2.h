@@ -1,6 +1,6 @@
 /* imago2.h -- TEST INFRASTRUCTURE: stand-in for libimago (image files).
- * Saving writes a portable float map; loading always fails (the scenes of
- * the test suite use no textures). */
+ * Saving writes a portable float map; loading reads binary PPM (P6) as RGBA
+ * floats (the texture test scenes use that format). */
 #ifndef SHIM_IMAGO2_H_
 #define SHIM_IMAGO2_H_
 

@@ -115,8 +115,44 @@ void *kd_res_item(struct kdres *s, double *pos)
 	return s->items[s->cur].first;
 }
 
-/* ---- imago2 ---- */
-void *img_load_pixels(const char *, int *, int *, int) { return nullptr; }
+/* ---- imago2 ----
+ * Loading reads binary PPM (P6, maxval <= 255) into RGBA floats (v / 255,
+ * alpha 1), rows top first, the subset of libimago's formats the texture
+ * tests use; other files fail to load. */
+static int ppm_token(FILE *fp)
+{
+	int c, v = 0, any = 0;
+	while((c = fgetc(fp)) != EOF) {
+		if(c == '#') { while((c = fgetc(fp)) != EOF && c != '\n') {} continue; }
+		if(c >= '0' && c <= '9') { v = v * 10 + (c - '0'); any = 1; }
+		else if(any) break;
+	}
+	return any ? v : -1;
+}
+
+void *img_load_pixels(const char *fname, int *xsz, int *ysz, int fmt)
+{
+	if(fmt != IMG_FMT_RGBAF) return nullptr;
+	FILE *fp = fopen(fname, "rb");
+	if(!fp) return nullptr;
+	char magic[2];
+	if(fread(magic, 1, 2, fp) != 2 || magic[0] != 'P' || magic[1] != '6') { fclose(fp); return nullptr; }
+	int w = ppm_token(fp), h = ppm_token(fp), maxv = ppm_token(fp);
+	if(w <= 0 || h <= 0 || maxv <= 0 || maxv > 255) { fclose(fp); return nullptr; }
+	size_t n = (size_t)w * h;
+	unsigned char *rgb = (unsigned char *)malloc(n * 3);
+	float *out = (float *)malloc(n * 4 * sizeof(float));
+	if(!rgb || !out || fread(rgb, 1, n * 3, fp) != n * 3) { free(rgb); free(out); fclose(fp); return nullptr; }
+	fclose(fp);
+	for(size_t i = 0; i < n; i++) {
+		for(int k = 0; k < 3; k++) out[i * 4 + k] = rgb[i * 3 + k] / 255.0f;
+		out[i * 4 + 3] = 1.0f;
+	}
+	free(rgb);
+	*xsz = w;
+	*ysz = h;
+	return out;
+}
 void img_free_pixels(void *p) { free(p); }
 int img_save_pixels(const char *fname, void *pix, int xsz, int ysz, int fmt)
 {

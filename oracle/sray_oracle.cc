@@ -27,6 +27,7 @@
 #include <thread>
 #include <atomic>
 #include <memory>
+#include <unistd.h>
 #include "sray_oracle.h"
 #include "sray_rng.h"
 #include "vmath_core.h"
@@ -450,6 +451,14 @@ static V3d xform_pt(const double m[4][4], const V3d &p)
 struct MatAttr {
 	std::string name;
 	double col[4];
+	int tex = -1;                /* index into Scene::texs, -1 = none */
+};
+
+/* Texture (src/texture.cc): an RGBA float image, rows top first, looked up
+ * with the 5-tap filter and repeat wrapping. */
+struct Tex {
+	int xsz = 0, ysz = 0;
+	std::vector<float> pix;
 };
 
 struct Material {
@@ -466,17 +475,20 @@ struct Material {
 		set("refract", 0.0, 0.0, 0.0, 0.0);
 		set("ior", 1.5, 0.0, 0.0, 0.0);
 	}
-	void set(const char *n, double r, double g, double b, double a)
+	/* set_attribute replaces both the colour and the texture (src/material.cc:140-151) */
+	void set(const char *n, double r, double g, double b, double a, int tex = -1)
 	{
 		for(size_t i = 0; i < attr.size(); i++) {
 			if(attr[i].name == n) {
 				attr[i].col[0] = r; attr[i].col[1] = g; attr[i].col[2] = b; attr[i].col[3] = a;
+				attr[i].tex = tex;
 				return;
 			}
 		}
 		MatAttr m;
 		m.name = n;
 		m.col[0] = r; m.col[1] = g; m.col[2] = b; m.col[3] = a;
+		m.tex = tex;
 		attr.push_back(m);
 		std::sort(attr.begin(), attr.end(), [](const MatAttr &x, const MatAttr &y) { return x.name < y.name; });
 	}
@@ -492,6 +504,11 @@ struct Material {
 		static const double def[4] = {1.0, 1.0, 1.0, 1.0};
 		const MatAttr *a = find(n);
 		return a ? a->col : def;
+	}
+	int tex_of(const char *n) const
+	{
+		const MatAttr *a = find(n);
+		return a ? a->tex : -1;
 	}
 };
 
@@ -780,6 +797,7 @@ struct Scene {
 	double env_col[4] = {0, 0, 0, 0};
 	double env_amb[4] = {0, 0, 0, 0};
 	Material default_mat;
+	std::vector<Tex> texs;
 	Octree oct;
 	double gather_dist = 0.001;
 	int64_t n_tris = 0;
@@ -892,6 +910,61 @@ static void build_mesh_tree(Object &o, int depth, int items)
 	o.oct.build(boxes, depth, items);
 }
 
+/* find_file (src/datapath.c:57-77): "<dir>/<name>" for the directories of
+ * SRAY_DATA_PATH that exist as a file.  The list parser (src/datapath.c:
+ * 79-113) writes its terminator over the first ':' and then tests that same
+ * byte, so only the first entry of the list is ever searched. */
+static bool find_data_file(const char *name, std::string &path)
+{
+	const char *env = getenv("SRAY_DATA_PATH");
+	if(!env || !*env) return false;
+	path.assign(env, strcspn(env, ":"));
+	path += "/";
+	path += name;
+	return access(path.c_str(), F_OK) == 0;
+}
+
+static int ppm_number(FILE *fp)
+{
+	int c, v = 0, any = 0;
+	while((c = fgetc(fp)) != EOF) {
+		if(c == '#') { while((c = fgetc(fp)) != EOF && c != '\n') {} continue; }
+		if(c >= '0' && c <= '9') { v = v * 10 + (c - '0'); any = 1; }
+		else if(any) break;
+	}
+	return any ? v : -1;
+}
+
+/* Texture::load (src/texture.cc:28-36) -> Image::load (src/img.cc:60-74):
+ * the image as RGBA floats.  Binary PPM (P6, maxval <= 255), channel / 255
+ * and alpha 1, is the one file format read here. */
+static bool load_texture(const char *name, Tex &t)
+{
+	std::string path;
+	if(!find_data_file(name, path)) return false;
+	FILE *fp = fopen(path.c_str(), "rb");
+	if(!fp) return false;
+	char magic[2];
+	bool ok = fread(magic, 1, 2, fp) == 2 && magic[0] == 'P' && magic[1] == '6';
+	int w = ok ? ppm_number(fp) : -1, h = ok ? ppm_number(fp) : -1, maxv = ok ? ppm_number(fp) : -1;
+	ok = ok && w > 0 && h > 0 && maxv > 0 && maxv <= 255 && (int64_t)w * h < ((int64_t)1 << 28);
+	std::vector<unsigned char> rgb;
+	if(ok) {
+		rgb.resize((size_t)w * h * 3);
+		ok = fread(rgb.data(), 1, rgb.size(), fp) == rgb.size();
+	}
+	fclose(fp);
+	if(!ok) return false;
+	t.xsz = w;
+	t.ysz = h;
+	t.pix.resize((size_t)w * h * 4);
+	for(size_t i = 0; i < (size_t)w * h; i++) {
+		for(int k = 0; k < 3; k++) t.pix[i * 4 + k] = rgb[i * 3 + k] / 255.0f;
+		t.pix[i * 4 + 3] = 1.0f;
+	}
+	return true;
+}
+
 static bool load_scene(Scene &sc, const sray_opts &opt, const char *text, size_t len, std::string &err)
 {
 	XmlParser xp;
@@ -911,8 +984,24 @@ static bool load_scene(Scene &sc, const sray_opts &opt, const char *text, size_t
 			if(c.name != "mattr") continue;
 			const XAttr *an = c.get("name"), *av = c.get("value");
 			if(!an || !av) continue;
-			if(av->type == AT_VEC) m.set(an->str.c_str(), av->vval[0], av->vval[1], av->vval[2], 1.0);
-			else if(av->type == AT_FLT || av->type == AT_INT) m.set(an->str.c_str(), av->fval, av->fval, av->fval, 1.0);
+			double col[4];
+			if(av->type == AT_VEC) { col[0] = av->vval[0]; col[1] = av->vval[1]; col[2] = av->vval[2]; }
+			else if(av->type == AT_FLT || av->type == AT_INT) col[0] = col[1] = col[2] = av->fval;
+			else continue;
+			col[3] = 1.0;
+			/* a "map" loads a texture of its own; one that fails to load
+			 * leaves the attribute untextured (src/material.cc:64-72) */
+			int tex = -1;
+			if((a = c.get("map"))) {
+				Tex t;
+				if(load_texture(a->str.c_str(), t)) {
+					tex = (int)sc.texs.size();
+					sc.texs.push_back(std::move(t));
+				} else {
+					fprintf(stderr, "failed to load texture: %s\n", a->str.c_str());
+				}
+			}
+			m.set(an->str.c_str(), col[0], col[1], col[2], col[3], tex);
 		}
 		sc.mats.push_back(m);
 	}
@@ -1138,11 +1227,16 @@ template <class R> struct Frame : FrameBase {
 	struct NodeR { R mn[3], mx[3]; };
 	std::vector<std::vector<NodeR> > mesh_boxes;
 	std::vector<NodeR> scene_boxes;
+	/* attributes that can carry a texture, in MatR::tex order */
+	enum { TA_DIFFUSE, TA_SPECULAR, TA_SHININESS, TA_REFLECT, TA_REFRACT, TA_IOR, TA_NORMAL, TA_COUNT };
 	struct MatR {
 		int phong;
 		C kd, ks;
 		R shin, refl, refr, ior;
-		bool have_spec, have_shin;
+		bool have_spec, have_shin, have_normal;
+		int tex[TA_COUNT];               /* texture per attribute, -1 = none */
+		R scol[TA_COUNT];                /* the attribute colour's x (textured scalars, bump scale) */
+		bool textured;
 	};
 	std::vector<MatR> mats;
 	MatR defmat;
@@ -1297,7 +1391,64 @@ template <class R> struct Frame : FrameBase {
 		r.refl = (R)(float)m.get("reflect")[0];
 		r.refr = (R)(float)m.get("refract")[0];
 		r.ior = (R)(float)m.get("ior")[0];
+		r.have_normal = m.have("normal");
+		static const char *names[TA_COUNT] = {"diffuse", "specular", "shininess", "reflect", "refract", "ior", "normal"};
+		r.textured = false;
+		for(int k = 0; k < TA_COUNT; k++) {
+			r.tex[k] = m.tex_of(names[k]);
+			r.scol[k] = (R)m.get(names[k])[0];
+			if(r.tex[k] >= 0) r.textured = true;
+		}
 		return r;
+	}
+
+	/* ------------------ textures ------------------ */
+	/* Texture::lookup (src/texture.cc:60-83) with the texture's identity
+	 * transform: texel (int)(tc * size), the average of it and its four
+	 * edge neighbours, each wrapped by Texture::get_texel's repeat mode
+	 * (src/texture.cc:85-101). */
+	C tex_lookup(int ti, const R tc[2]) const
+	{
+		const Tex &t = sc.texs[ti];
+		int tx = (int)(tc[0] * (R)t.xsz);
+		int ty = (int)(tc[1] * (R)t.ysz);
+		static const int off[5][2] = {{0, 0}, {1, 0}, {-1, 0}, {0, 1}, {0, -1}};
+		C sum;
+		for(int i = 0; i < 5; i++) {
+			int x = (tx + off[i][0]) % t.xsz, y = (ty + off[i][1]) % t.ysz;
+			if(x < 0) x += t.xsz;
+			if(y < 0) y += t.ysz;
+			const float *p = &t.pix[((size_t)y * t.xsz + x) * 4];
+			C c((R)p[0], (R)p[1], (R)p[2], (R)p[3]);
+			sum = i ? sum + c : c;
+		}
+		return sum / (R)5;
+	}
+	/* MatAttrib::get_color / get_value (src/material.inl:18-29) */
+	C attr_color(const MatR &m, int a, const C &col, const R tc[2]) const
+	{
+		return m.tex[a] >= 0 ? tex_lookup(m.tex[a], tc) * col : col;
+	}
+	R attr_value(const MatR &m, int a, R val, const R tc[2]) const
+	{
+		return m.tex[a] >= 0 ? (R)(float)(tex_lookup(m.tex[a], tc).x * m.scol[a]) : val;
+	}
+	/* get_bump_normal (src/shader.cc:296-318): the unflipped surface normal,
+	 * tilted by the normal map's texel in the frame (tangent, normal x
+	 * tangent, normal) when the attribute has a texture */
+	V bump_normal(const MatR &m, const SurfPoint<R> &sp) const
+	{
+		V normal = sp.normal;
+		if(m.tex[TA_NORMAL] < 0) return normal;
+		C nc = tex_lookup(m.tex[TA_NORMAL], sp.tex);
+		V n(nc.x * (R)2 - (R)1, nc.y * (R)2 - (R)1, nc.z * (R)2 - (R)1);
+		n.x = n.x * m.scol[TA_NORMAL];
+		n.y = n.y * m.scol[TA_NORMAL];
+		n = normalized(n);
+		V bitan = cross(normal, sp.tangent);
+		return V(sp.tangent.x * n.x + bitan.x * n.y + normal.x * n.z,
+				sp.tangent.y * n.x + bitan.y * n.y + normal.y * n.z,
+				sp.tangent.z * n.x + bitan.z * n.y + normal.z * n.z);
 	}
 
 	const MatR &mat_for(int obj) const
@@ -1892,19 +2043,20 @@ template <class R> struct Frame : FrameBase {
 		V incident = ray.d / ray_mag;
 		C ks(0, 0, 0, (R)1);
 		R refl_fact = 0, trans_fact = 0;
-		C kd = mat.kd;
-		if(mat.have_spec) ks = mat.ks;
-		R shininess = mat.shin;
+		C kd = attr_color(mat, TA_DIFFUSE, mat.kd, sp.tex);
+		if(mat.have_spec) ks = attr_color(mat, TA_SPECULAR, mat.ks, sp.tex);
+		R shininess = attr_value(mat, TA_SHININESS, mat.shin, sp.tex);
 
 		if(ray.iter == INT_MAX) {
 			C rad = radiance_est(sp.pos, normal, *ctx.c);
 			return rad * kd;
 		}
 		node_rng(ctx, path, 0);
-		refl_fact = mat.refl;
-		trans_fact = mat.refr;
-		R mat_ior = mat.ior;
+		refl_fact = attr_value(mat, TA_REFLECT, mat.refl, sp.tex);
+		trans_fact = attr_value(mat, TA_REFRACT, mat.refr, sp.tex);
+		R mat_ior = attr_value(mat, TA_IOR, mat.ior, sp.tex);
 		R ior = ray.calc_ior(entering, mat_ior);
+		if(mat.have_normal) normal = bump_normal(mat, sp);
 
 		C diff = env_amb * kd;
 		C spec(0, 0, 0, (R)1);
@@ -2028,14 +2180,17 @@ template <class R> struct Frame : FrameBase {
 			int obj;
 			if(!cast(ray, &sp, &obj, 0, 0, c)) return false;
 			const MatR &m = mat_for(obj);
-			C spec = m.ks;
-			R refl = m.refl, refr = m.refr, mat_ior = m.ior;
+			C spec = attr_color(m, TA_SPECULAR, m.ks, sp.tex);
+			R refl = attr_value(m, TA_REFLECT, m.refl, sp.tex);
+			R refr = attr_value(m, TA_REFRACT, m.refr, sp.tex);
+			R mat_ior = attr_value(m, TA_IOR, m.ior, sp.tex);
 			bool entering;
 			V normal;
 			R ray_mag = length(ray.d);
 			if(dot(ray.d, sp.normal) > (R)0) { normal = -sp.normal; entering = false; }
 			else { normal = sp.normal; entering = true; }
 			R ior = ray.calc_ior(entering, mat_ior);
+			if(m.have_normal) normal = bump_normal(m, sp);
 			R ray_dot_n = dot(-ray.d / ray_mag, normal);
 			R sf0 = refr > (R)0 ? (ior - (R)1) / (ior + (R)1) : (R)1;
 			R fres = fresnel(sf0 * sf0, ray_dot_n);
@@ -2099,9 +2254,9 @@ template <class R> struct Frame : FrameBase {
 			if(dot(ray.d, sp.normal) > (R)0) { normal = -sp.normal; entering = false; }
 			else { normal = sp.normal; entering = true; }
 			const MatR &m = mat_for(obj);
-			C diff = m.kd;
+			C diff = attr_color(m, TA_DIFFUSE, m.kd, sp.tex);
 			R diff_avg = (diff.x + diff.y + diff.z) / (R)3;
-			C spec = m.ks;
+			C spec = attr_color(m, TA_SPECULAR, m.ks, sp.tex);
 			R spec_avg = (spec.x + spec.y + spec.z) / (R)3;
 			R rnum = frand(s, (R)1);
 			if(rnum < diff_avg) {
@@ -2116,7 +2271,9 @@ template <class R> struct Frame : FrameBase {
 				ph->col = ph->col * (ndotl * (diff / diff_avg));
 				ray = nr;
 			} else if(rnum < diff_avg + spec_avg) {
-				R refl = m.refl, refr = m.refr, mat_ior = m.ior;
+				R refl = attr_value(m, TA_REFLECT, m.refl, sp.tex);
+				R refr = attr_value(m, TA_REFRACT, m.refr, sp.tex);
+				R mat_ior = attr_value(m, TA_IOR, m.ior, sp.tex);
 				R ior = ray.calc_ior(entering, mat_ior);
 				R ray_dot_n = dot(-ray.d / ray_mag, normal);
 				R sf0 = refr > (R)0 ? (ior - (R)1) / (ior + (R)1) : (R)1;

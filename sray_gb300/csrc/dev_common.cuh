@@ -95,6 +95,8 @@ struct DScene {
 	const float *tri_attr;    /* 24 floats per unique-mesh triangle */
 	const DevMat *mats;
 	DevMat defmat;
+	const DevTex *texs;       /* textures of the materials' attributes */
+	const float4 *texels;     /* their RGBA texels */
 	const DevLight *lights;
 	int nlights;
 	const float *light_pos;   /* 4 floats per light per time */
@@ -1007,6 +1009,7 @@ __device__ inline bool trace_any(const DScene &S, V3 wo, V3 wd, int time, int *o
 struct Surf {
 	V3 pos, normal;
 	V3 gn;            /* geometric normal, unit, world space */
+	V3 tangent;       /* filled when asked for (a normal-mapped material) */
 	float tex[2];
 };
 
@@ -1037,7 +1040,8 @@ __device__ __forceinline__ V3 shadow_origin(const Surf &sp, V3 dir)
 __device__ __forceinline__ float root_disc(float d) { return sqrtf(d > 0.0f ? d : 0.0f); }
 
 /* interp_face (src/mesh.cc:321-445): bilinear-patch inversion after Haines */
-__device__ inline void interp_face(const float *P, const float *A, V3 ispos, V3 normal, float xsmall, V3 *onorm, float *otex, bool want_tex)
+__device__ inline void interp_face(const float *P, const float *A, V3 ispos, V3 normal, float xsmall, V3 *onorm, float *otex, bool want_tex,
+		V3 *otang = nullptr)
 {
 	V3 p00 = mk(P[0], P[1], P[2]), p10 = mk(P[3], P[4], P[5]), p01 = mk(P[6], P[7], P[8]), p11 = p01;
 	V3 pa = (p00 - p10) + (p11 - p01);
@@ -1097,6 +1101,15 @@ __device__ inline void interp_face(const float *P, const float *A, V3 ispos, V3 
 			otex[k] = DLERP(s0, s1, rx);
 		}
 	}
+	if(otang) {
+		float g[3];
+		for(int k = 0; k < 3; k++) {
+			float g0 = DLERP(A[9 + 0 * 3 + k], A[9 + 2 * 3 + k], ry);
+			float g1 = DLERP(A[9 + 1 * 3 + k], A[9 + 2 * 3 + k], ry);
+			g[k] = DLERP(g0, g1, rx);
+		}
+		*otang = mk(g[0], g[1], g[2]);
+	}
 #undef DLERP
 }
 
@@ -1110,8 +1123,13 @@ __device__ __forceinline__ void sph_tex(V3 p, float *tex, bool cyl)
 }
 
 /* world-space surface point of a hit, as the intersectors fill SurfPoint
- * (object-space position and normal, then forward / inverse-transpose) */
-__device__ inline void surface_point(const DScene &S, const Hit &h, V3 wo, V3 wd, int time, Surf &sp, bool want_tex)
+ * (object-space position and normal, then forward / inverse-transpose).
+ * Texture coordinates with want_tex, the tangent with want_tan: the
+ * quadrics' (0,1,0) x normal, unnormalised (src/sphere.cc:120,
+ * src/cylinder.cc:173), a mesh's interpolated vertex tangents, normalised
+ * (src/mesh.cc:162, 302-305). */
+__device__ inline void surface_point(const DScene &S, const Hit &h, V3 wo, V3 wd, int time, Surf &sp, bool want_tex,
+		bool want_tan = false)
 {
 	int ti = time_index(S, time);
 	const DevObj ob = S.objs[h.obj];
@@ -1124,12 +1142,14 @@ __device__ inline void surface_point(const DScene &S, const Hit &h, V3 wo, V3 wd
 	if(ob.type == 0) {
 		nrm = pos / ob.rad;
 		if(want_tex) sph_tex(pos, sp.tex, false);
+		if(want_tan) sp.tangent = mul_n(it, cross(mk(0.0f, 1.0f, 0.0f), nrm));
 		sp.pos = mul_pt(m, pos);
 		sp.normal = mul_n(it, nrm);
 		sp.gn = normalized(sp.normal);
 	} else if(ob.type == 1) {
 		nrm = mk(1.0f * pos.x, 0.0f * pos.y, 1.0f * pos.z) / ob.rad;
 		if(want_tex) sph_tex(pos, sp.tex, true);
+		if(want_tan) sp.tangent = mul_n(it, cross(mk(0.0f, 1.0f, 0.0f), nrm));
 		sp.pos = mul_pt(m, pos);
 		sp.normal = mul_n(it, nrm);
 		sp.gn = normalized(sp.normal);
@@ -1138,13 +1158,85 @@ __device__ inline void surface_point(const DScene &S, const Hit &h, V3 wo, V3 wd
 		const float *A = S.tri_attr + (size_t)(ob.tri_base + h.prim) * 24;
 		V3 v0 = mk(P[0], P[1], P[2]), v1 = mk(P[3], P[4], P[5]), v2 = mk(P[6], P[7], P[8]);
 		V3 fn = cross(v1 - v0, v2 - v0);
-		V3 in;
-		interp_face(P, A, pos, fn, S.xsmall, &in, sp.tex, want_tex);
+		V3 in, tg;
+		interp_face(P, A, pos, fn, S.xsmall, &in, sp.tex, want_tex, want_tan ? &tg : nullptr);
 		nrm = dot(in, in) < S.xsmall ? fn : in;
+		if(want_tan) sp.tangent = normalized(mul_n(it, tg));
 		sp.pos = mul_pt(m, pos);
 		sp.normal = normalized(mul_n(it, nrm));
 		sp.gn = normalized(mul_n(it, fn));
 	}
+}
+
+/* ---------------- textures ---------------- */
+/* Texture::lookup (src/texture.cc:60-83), the texture's transform being the
+ * identity: texel (int)(tc * size) averaged with its four edge neighbours,
+ * each wrapped by the repeat mode of Texture::get_texel
+ * (src/texture.cc:85-101). */
+__device__ __forceinline__ float4 tex_lookup(const DScene &S, int ti, const float *tc)
+{
+	const DevTex t = S.texs[ti];
+	int tx = (int)(tc[0] * (float)t.xsz);
+	int ty = (int)(tc[1] * (float)t.ysz);
+	const int ox[5] = {0, 1, -1, 0, 0}, oy[5] = {0, 0, 0, 1, -1};
+	float4 sum = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+	#pragma unroll
+	for(int i = 0; i < 5; i++) {
+		int x = (tx + ox[i]) % t.xsz, y = (ty + oy[i]) % t.ysz;
+		if(x < 0) x += t.xsz;
+		if(y < 0) y += t.ysz;
+		float4 c = __ldg(S.texels + t.off + (long long)y * t.xsz + x);
+		if(i == 0) sum = c;
+		else { sum.x = sum.x + c.x; sum.y = sum.y + c.y; sum.z = sum.z + c.z; sum.w = sum.w + c.w; }
+	}
+	return make_float4(sum.x / 5.0f, sum.y / 5.0f, sum.z / 5.0f, sum.w / 5.0f);
+}
+
+/* a material's attributes at a surface point (MatAttrib::get_color /
+ * get_value, src/material.inl:18-29): the colour, times the texel where the
+ * attribute has a texture; a scalar is the colour's x, as float */
+struct MatVals {
+	float kd[3], ks[3];
+	float shin, refl, refr, ior;
+};
+__device__ __forceinline__ void mat_values(const DScene &S, const DevMat &m, const float *tc, MatVals &v)
+{
+	#pragma unroll
+	for(int k = 0; k < 3; k++) { v.kd[k] = m.kd[k]; v.ks[k] = m.ks[k]; }
+	v.shin = m.shin;
+	v.refl = m.refl;
+	v.refr = m.refr;
+	v.ior = m.ior;
+	if(!m.textured) return;
+	if(m.tex[TA_DIFFUSE] >= 0) {
+		float4 c = tex_lookup(S, m.tex[TA_DIFFUSE], tc);
+		v.kd[0] = c.x * m.kd[0]; v.kd[1] = c.y * m.kd[1]; v.kd[2] = c.z * m.kd[2];
+	}
+	if(m.tex[TA_SPECULAR] >= 0) {
+		float4 c = tex_lookup(S, m.tex[TA_SPECULAR], tc);
+		v.ks[0] = c.x * m.ks[0]; v.ks[1] = c.y * m.ks[1]; v.ks[2] = c.z * m.ks[2];
+	}
+	if(m.tex[TA_SHININESS] >= 0) v.shin = tex_lookup(S, m.tex[TA_SHININESS], tc).x * m.scol[TA_SHININESS];
+	if(m.tex[TA_REFLECT] >= 0) v.refl = tex_lookup(S, m.tex[TA_REFLECT], tc).x * m.scol[TA_REFLECT];
+	if(m.tex[TA_REFRACT] >= 0) v.refr = tex_lookup(S, m.tex[TA_REFRACT], tc).x * m.scol[TA_REFRACT];
+	if(m.tex[TA_IOR] >= 0) v.ior = tex_lookup(S, m.tex[TA_IOR], tc).x * m.scol[TA_IOR];
+}
+
+/* get_bump_normal (src/shader.cc:296-318): the unflipped surface normal,
+ * tilted by the normal map's texel in the frame (tangent, normal x tangent,
+ * normal) where the "normal" attribute has a texture */
+__device__ __forceinline__ V3 bump_normal(const DScene &S, const DevMat &m, const Surf &sp)
+{
+	V3 normal = sp.normal;
+	if(m.tex[TA_NORMAL] < 0) return normal;
+	float4 c = tex_lookup(S, m.tex[TA_NORMAL], sp.tex);
+	V3 n = mk(c.x * 2.0f - 1.0f, c.y * 2.0f - 1.0f, c.z * 2.0f - 1.0f);
+	n.x = n.x * m.scol[TA_NORMAL];
+	n.y = n.y * m.scol[TA_NORMAL];
+	n = normalized(n);
+	V3 bitan = cross(normal, sp.tangent);
+	return mk(sp.tangent.x * n.x + bitan.x * n.y + normal.x * n.z, sp.tangent.y * n.x + bitan.y * n.y + normal.y * n.z,
+			sp.tangent.z * n.x + bitan.z * n.y + normal.z * n.z);
 }
 
 /* ---------------- lights ---------------- */

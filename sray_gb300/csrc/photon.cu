@@ -61,16 +61,21 @@ __device__ __forceinline__ void refract_ray(PRay &r, V3 n, float mat_ior, bool e
  * the hit h: reflect or refract (P_CONT) or absorb and store (P_STORE) */
 __device__ int caust_step(const DScene &S, PRay &r, PState &ph, const Hit &h, sray_rng *s)
 {
-	Surf sp;
-	surface_point(S, h, r.o, r.d, r.time, sp, false);
 	const DevMat &m = mat_of(S, h.obj);
-	float refl = m.refl, refr = m.refr, mat_ior = m.ior;
+	Surf sp;
+	surface_point(S, h, r.o, r.d, r.time, sp, m.textured, m.textured && m.tex[TA_NORMAL] >= 0);
+	MatVals mv;
+	mat_values(S, m, sp.tex, mv);
+	float refl = mv.refl, refr = mv.refr, mat_ior = mv.ior;
 	bool entering;
 	V3 normal;
 	float ray_mag = len(r.d);
 	if(dot(r.d, sp.normal) > 0.0f) { normal = -sp.normal; entering = false; }
 	else { normal = sp.normal; entering = true; }
 	float ior = r.st.calc_ior(entering, mat_ior);
+	/* a normal map replaces the normal after the index of refraction is
+	 * known (src/scene.cc:600-605) */
+	if(m.have_normal) normal = bump_normal(S, m, sp);
 	float ray_dot_n = dot(-r.d / ray_mag, normal);
 	float sf0 = refr > 0.0f ? (ior - 1.0f) / (ior + 1.0f) : 1.0f;
 	float fres = fresnel(sf0 * sf0, ray_dot_n);
@@ -82,14 +87,14 @@ __device__ int caust_step(const DScene &S, PRay &r, PState &ph, const Hit &h, sr
 		r.iter--;
 		r.o = sp.pos;
 		ph.type = CAUST_PHOTON;
-		for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * m.ks[k];
+		for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * mv.ks[k];
 		return P_CONT;
 	}
 	if(rnum < refr) {
 		refract_ray(r, normal, mat_ior, entering, ray_mag);
 		r.o = sp.pos;
 		ph.type = CAUST_PHOTON;
-		for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * m.ks[k];
+		for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * mv.ks[k];
 		return P_CONT;
 	}
 	ph.dir = normalized(r.d);
@@ -104,16 +109,18 @@ __device__ int caust_step(const DScene &S, PRay &r, PState &ph, const Hit &h, sr
 __device__ int global_step(const DScene &S, PRay &r, PState &ph, const Hit &h, sray_rng *s)
 {
 	V3 incident = normalized(r.d);
+	const DevMat &m = mat_of(S, h.obj);
 	Surf sp;
-	surface_point(S, h, r.o, r.d, r.time, sp, false);
+	surface_point(S, h, r.o, r.d, r.time, sp, m.textured);
 	V3 normal;
 	bool entering;
 	float ray_mag = len(r.d);
 	if(dot(r.d, sp.normal) > 0.0f) { normal = -sp.normal; entering = false; }
 	else { normal = sp.normal; entering = true; }
-	const DevMat &m = mat_of(S, h.obj);
-	float diff_avg = (m.kd[0] + m.kd[1] + m.kd[2]) / 3.0f;
-	float spec_avg = (m.ks[0] + m.ks[1] + m.ks[2]) / 3.0f;
+	MatVals mv;
+	mat_values(S, m, sp.tex, mv);
+	float diff_avg = (mv.kd[0] + mv.kd[1] + mv.kd[2]) / 3.0f;
+	float spec_avg = (mv.ks[0] + mv.ks[1] + mv.ks[2]) / 3.0f;
 	float rnum = frand(s, 1.0f);
 	if(rnum < diff_avg) {
 		V3 dir = sphrand(s, 1.0f);
@@ -123,11 +130,11 @@ __device__ int global_step(const DScene &S, PRay &r, PState &ph, const Hit &h, s
 		r.iter--;
 		r.o = sp.pos;
 		ph.type = GI_PHOTON;
-		for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * (ndotl * (m.kd[k] / diff_avg));
+		for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * (ndotl * (mv.kd[k] / diff_avg));
 		return P_CONT;
 	}
 	if(rnum < diff_avg + spec_avg) {
-		float refl = m.refl, refr = m.refr, mat_ior = m.ior;
+		float refl = mv.refl, refr = mv.refr, mat_ior = mv.ior;
 		float ior = r.st.calc_ior(entering, mat_ior);
 		float ray_dot_n = dot(-r.d / ray_mag, normal);
 		float sf0 = refr > 0.0f ? (ior - 1.0f) / (ior + 1.0f) : 1.0f;
@@ -140,14 +147,14 @@ __device__ int global_step(const DScene &S, PRay &r, PState &ph, const Hit &h, s
 			r.iter--;
 			r.o = sp.pos;
 			ph.type = CAUST_PHOTON;
-			for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * m.ks[k];
+			for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * mv.ks[k];
 			return P_TO_CAUST;
 		}
 		if(rn2 < refr) {
 			refract_ray(r, normal, mat_ior, entering, ray_mag);
 			r.o = sp.pos;
 			ph.type = CAUST_PHOTON;
-			for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * m.ks[k];
+			for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * mv.ks[k];
 			return P_TO_CAUST;
 		}
 		return P_DROP;

@@ -323,7 +323,7 @@ __device__ __forceinline__ void shade_one(const DScene &S, const RayRec &ray, co
 	if(depth == 0) acc[aslot].w = 1.0f;
 	const DevMat &mat = mat_of(S, h.obj);
 	Surf sp;
-	surface_point(S, h, ray.o, rd, time, sp, !mat.phong);
+	surface_point(S, h, ray.o, rd, time, sp, !mat.phong || mat.textured, mat.textured && mat.tex[TA_NORMAL] >= 0);
 	if(!mat.phong) {
 		/* shade_undef (src/shader.cc:36-73) */
 		sray_rng rng;
@@ -356,7 +356,9 @@ __device__ __forceinline__ void shade_one(const DScene &S, const RayRec &ray, co
 	else { normal = sp.normal; entering = true; }
 	float ray_mag = len(rd);
 	V3 incident = rd / ray_mag;
-	const float *kd = mat.kd, *ks = mat.ks;
+	MatVals mv;
+	mat_values(S, mat, sp.tex, mv);
+	const float *kd = mv.kd, *ks = mv.ks;
 	if(iter == DIFFUSE_ITER) {
 		/* final-gather ray: radiance_est(...) * kd */
 		em.gather(sp.pos, normal, S.njobs > 0 ? 2 * job_of(S, pixel) + 1 : 1, aslot, w[0] * kd[0], w[1] * kd[1], w[2] * kd[2]);
@@ -366,8 +368,11 @@ __device__ __forceinline__ void shade_one(const DScene &S, const RayRec &ray, co
 	const IorStack &st = ray.st;
 	sray_rng rng;
 	sray_rng_init(&rng, S.seed, SRAY_DOM_PIXEL | ((uint32_t)path << 4), (uint32_t)pixel, (uint32_t)sample);
-	float refl_fact = mat.refl, trans_fact = mat.refr, mat_ior = mat.ior;
+	float refl_fact = mv.refl, trans_fact = mv.refr, mat_ior = mv.ior;
 	float ior = st.calc_ior(entering, mat_ior);
+	/* a normal map replaces the (flipped) normal after the index of
+	 * refraction is known (src/shader.cc:133-139) */
+	if(mat.have_normal) normal = bump_normal(S, mat, sp);
 	/* ambient: (env_ambient * kd) * kd */
 	acc_add(acc, aslot, w[0] * (S.env_amb[0] * kd[0] * kd[0]), w[1] * (S.env_amb[1] * kd[1] * kd[1]),
 			w[2] * (S.env_amb[2] * kd[2] * kd[2]));
@@ -384,7 +389,7 @@ __device__ __forceinline__ void shade_one(const DScene &S, const RayRec &ray, co
 			ldir = ldir / ldist;
 			float ndotl = maxf_ref(dot(normal, ldir), 0.0f);
 			float rdotl = maxf_ref(dot(vref, ldir), 0.0f);
-			float pw = powf(rdotl, mat.shin);
+			float pw = powf(rdotl, mv.shin);
 			float c[3];
 			for(int k = 0; k < 3; k++) {
 				float lc = L.col[k] * 1.0f;
@@ -1243,6 +1248,29 @@ void Renderer::prof_collect()
 
 #define CK(call, where) do { cudaError_t e_ = (call); if(e_ != cudaSuccess) return cuda_fail(e_, where); } while(0)
 
+/* a material's device form; Material::get_value returns float
+ * (src/material.cc:193-196) */
+static DevMat dev_material(const Material &m)
+{
+	DevMat d;
+	memset(&d, 0, sizeof d);
+	for(int k = 0; k < 4; k++) { d.kd[k] = (float)m.kd[k]; d.ks[k] = (float)m.ks[k]; }
+	d.shin = (float)m.shin;
+	d.refl = (float)m.refl;
+	d.refr = (float)m.refr;
+	d.ior = (float)m.ior;
+	d.phong = m.phong;
+	d.have_normal = m.have_normal ? 1 : 0;
+	const double scal[TA_COUNT] = {m.kd[0], m.ks[0], m.shin, m.refl, m.refr, m.ior, m.nrm_scale};
+	for(int k = 0; k < 8; k++) d.tex[k] = -1;
+	for(int k = 0; k < TA_COUNT; k++) {
+		d.tex[k] = m.tex[k];
+		d.scol[k] = (float)scal[k];
+		if(m.tex[k] >= 0) d.textured = 1;
+	}
+	return d;
+}
+
 void Renderer::fill_scene_desc()
 {
 	DScene &D = S;
@@ -1268,13 +1296,10 @@ void Renderer::fill_scene_desc()
 	D.tri_pos = tri_pos.as<float>();
 	D.tri_attr = tri_attr.as<float>();
 	D.mats = mats.as<DevMat>();
-	memset(&D.defmat, 0, sizeof D.defmat);
-	for(int k = 0; k < 4; k++) { D.defmat.kd[k] = (float)sc.defmat.kd[k]; D.defmat.ks[k] = (float)sc.defmat.ks[k]; }
-	D.defmat.shin = (float)sc.defmat.shin;
-	D.defmat.refl = (float)sc.defmat.refl;
-	D.defmat.refr = (float)sc.defmat.refr;
-	D.defmat.ior = (float)sc.defmat.ior;
+	D.defmat = dev_material(sc.defmat);
 	D.defmat.phong = 0;
+	D.texs = texs.as<DevTex>();
+	D.texels = texels.as<float4>();
 	D.lights = lights.as<DevLight>();
 	D.nlights = (int)sc.lights.size();
 	D.light_pos = light_pos.as<float>();
@@ -1411,18 +1436,18 @@ int Renderer::upload_scene(cudaStream_t s)
 		}
 	}
 	std::vector<DevMat> dm(sc.mats.size());
-	for(size_t i = 0; i < sc.mats.size(); i++) {
-		const Material &m = sc.mats[i];
-		DevMat &d = dm[i];
-		memset(&d, 0, sizeof d);
-		for(int k = 0; k < 4; k++) { d.kd[k] = (float)m.kd[k]; d.ks[k] = (float)m.ks[k]; }
-		/* Material::get_value returns float (src/material.cc:193-196) */
-		d.shin = (float)m.shin;
-		d.refl = (float)m.refl;
-		d.refr = (float)m.refr;
-		d.ior = (float)m.ior;
-		d.phong = m.phong;
+	for(size_t i = 0; i < sc.mats.size(); i++) dm[i] = dev_material(sc.mats[i]);
+	/* the texel table: every texture's RGBA texels, back to back */
+	std::vector<DevTex> dtex(sc.texs.size());
+	std::vector<float> texel;
+	for(size_t i = 0; i < sc.texs.size(); i++) {
+		dtex[i].off = (long long)(texel.size() / 4);
+		dtex[i].xsz = sc.texs[i].xsz;
+		dtex[i].ysz = sc.texs[i].ysz;
+		texel.insert(texel.end(), sc.texs[i].pix.begin(), sc.texs[i].pix.end());
 	}
+	CK(texs.upload(dtex, s), "upload textures");
+	CK(texels.upload(texel, s), "upload texels");
 	std::vector<DevLight> dl(sc.lights.size());
 	for(size_t i = 0; i < sc.lights.size(); i++) {
 		const Light &l = sc.lights[i];
@@ -2454,6 +2479,16 @@ int sray_gpu_load_scene_sidecar(const char *path, const char *sidecar, int *used
 	return load_scene_text(buf.data(), buf.size(), sidecar, used);
 }
 
+int sray_gpu_add_data_path(const char *dir)
+{
+	if(!dir) { g_err = "null directory"; return SRAY_EINVAL; }
+	const char *cur = getenv("SRAY_DATA_PATH");
+	std::string v = dir;
+	if(cur) v += std::string(":") + cur;
+	if(setenv("SRAY_DATA_PATH", v.c_str(), 1) != 0) { g_err = "setenv failed"; return SRAY_EINVAL; }
+	return 0;
+}
+
 int sray_gpu_scene_info(int *n_objects, int *n_lights, int *n_materials, int64_t *n_triangles, int *n_unique_meshes)
 {
 	NEED_CTX();
@@ -2971,7 +3006,8 @@ void sray_gpu_shutdown(void)
 	}
 	R.djobs.release();
 	R.dmaps.release();
-	DevBuf *bufs[] = {&R.mnodes, &R.mtris, &R.mprim, &R.tri_pos, &R.tri_attr, &R.objs, &R.mats, &R.lights, &R.snodes, &R.sslots,
+	DevBuf *bufs[] = {&R.mnodes, &R.mtris, &R.mprim, &R.tri_pos, &R.tri_attr, &R.objs, &R.mats, &R.texs, &R.texels, &R.lights,
+		&R.snodes, &R.sslots,
 		&R.xf, &R.light_pos, &R.cam_m, &R.projbits, &R.coverage, &R.qbuf[0], &R.qbuf[1], &R.hits, &R.gq, &R.sq, &R.acc, &R.hist, &R.sums,
 		&R.active[0], &R.active[1], &R.spp, &R.fbdev, &R.ctr, &R.counts, &R.bnodes, &R.btris, &R.bprim, &R.bhome,
 		&R.fbl, &R.tnodes, &R.ohome, &R.pool_ready, &R.pqbuf[0], &R.pqbuf[1], &R.phits, &R.pfbl, &R.pcounts, &R.pctr,

@@ -107,7 +107,7 @@ struct Renderer {
 	std::string err;
 
 	/* scene tables (per load) */
-	DevBuf mnodes, mtris, mprim, tri_pos, tri_attr, objs, mats, lights, bnodes, btris, bprim, bhome;
+	DevBuf mnodes, mtris, mprim, tri_pos, tri_attr, objs, mats, texs, texels, lights, bnodes, btris, bprim, bhome;
 	/* frame tables (per build) */
 	DevBuf snodes, sslots, xf, light_pos, cam_m, projbits, coverage, tnodes, ohome;
 	bool built = false;

@@ -17,12 +17,72 @@
 #include <limits.h>
 #include <stdlib.h>
 #include <string.h>
+#include <stdio.h>
+#include <unistd.h>
 #include <algorithm>
 #include <thread>
 #include "scene_host.h"
 #include "sray_rng.h"
 
 namespace sray {
+
+/* ------------------------------------------------------------------ */
+/* textures                                                             */
+/* ------------------------------------------------------------------ */
+namespace {
+
+/* a PPM header number: decimal digits after whitespace and '#' comments */
+int ppm_number(FILE *fp)
+{
+	int c, v = 0, any = 0;
+	while((c = fgetc(fp)) != EOF) {
+		if(c == '#') {
+			while((c = fgetc(fp)) != EOF && c != '\n') {}
+			continue;
+		}
+		if(c >= '0' && c <= '9') {
+			if(v > 100000000) return -1;
+			v = v * 10 + (c - '0');
+			any = 1;
+		} else if(any) {
+			break;
+		}
+	}
+	return any ? v : -1;
+}
+
+}  // namespace
+
+bool load_texture(const char *name, Texture &t)
+{
+	const char *env = getenv("SRAY_DATA_PATH");
+	if(!env || !*env || !name) return false;
+	std::string path(env, strcspn(env, ":"));
+	path += "/";
+	path += name;
+	if(access(path.c_str(), F_OK) != 0) return false;
+	FILE *fp = fopen(path.c_str(), "rb");
+	if(!fp) return false;
+	char magic[2];
+	bool ok = fread(magic, 1, 2, fp) == 2 && magic[0] == 'P' && magic[1] == '6';
+	int w = ok ? ppm_number(fp) : -1, h = ok ? ppm_number(fp) : -1, maxv = ok ? ppm_number(fp) : -1;
+	ok = ok && w > 0 && h > 0 && maxv > 0 && maxv <= 255 && (int64_t)w * h < ((int64_t)1 << 28);
+	std::vector<unsigned char> rgb;
+	if(ok) {
+		rgb.resize((size_t)w * h * 3);
+		ok = fread(rgb.data(), 1, rgb.size(), fp) == rgb.size();
+	}
+	fclose(fp);
+	if(!ok) return false;
+	t.xsz = w;
+	t.ysz = h;
+	t.pix.resize((size_t)w * h * 4);
+	for(size_t i = 0; i < (size_t)w * h; i++) {
+		for(int k = 0; k < 3; k++) t.pix[i * 4 + k] = (float)rgb[i * 3 + k] / 255.0f;
+		t.pix[i * 4 + 3] = 1.0f;
+	}
+	return true;
+}
 
 /* ------------------------------------------------------------------ */
 /* flat XML DOM: names and values are views into the document buffer   */
@@ -973,12 +1033,27 @@ struct Loader {
 			if(av.type == T_VEC) { col[0] = av.vval[0]; col[1] = av.vval[1]; col[2] = av.vval[2]; col[3] = 1.0; }
 			else if(av.type == T_FLT || av.type == T_INT) { col[0] = col[1] = col[2] = av.fval; col[3] = 1.0; }
 			else continue;
-			if(an.str == "diffuse") memcpy(m.kd, col, sizeof col);
-			else if(an.str == "specular") memcpy(m.ks, col, sizeof col);
-			else if(an.str == "shininess") m.shin = col[0];
-			else if(an.str == "reflect") m.refl = col[0];
-			else if(an.str == "refract") m.refr = col[0];
-			else if(an.str == "ior") m.ior = col[0];
+			/* a "map" loads a texture of its own; one that fails to load
+			 * leaves the attribute untextured (src/material.cc:64-72) */
+			int tex = -1;
+			Typed am;
+			if(Doc::typed(d.attr(c, "map"), &am)) {
+				Texture tx;
+				if(load_texture(am.str.c_str(), tx)) {
+					tex = (int)sc.texs.size();
+					sc.texs.push_back(std::move(tx));
+				} else {
+					fprintf(stderr, "failed to load texture: %s\n", am.str.c_str());
+				}
+			}
+			/* set_attribute replaces the colour and the texture (src/material.cc:140-151) */
+			if(an.str == "diffuse") { memcpy(m.kd, col, sizeof col); m.tex[TA_DIFFUSE] = tex; }
+			else if(an.str == "specular") { memcpy(m.ks, col, sizeof col); m.tex[TA_SPECULAR] = tex; }
+			else if(an.str == "shininess") { m.shin = col[0]; m.tex[TA_SHININESS] = tex; }
+			else if(an.str == "reflect") { m.refl = col[0]; m.tex[TA_REFLECT] = tex; }
+			else if(an.str == "refract") { m.refr = col[0]; m.tex[TA_REFRACT] = tex; }
+			else if(an.str == "ior") { m.ior = col[0]; m.tex[TA_IOR] = tex; }
+			else if(an.str == "normal") { m.have_normal = true; m.nrm_scale = col[0]; m.tex[TA_NORMAL] = tex; }
 		}
 		sc.mats.push_back(m);
 		return true;

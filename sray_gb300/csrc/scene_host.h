@@ -52,7 +52,22 @@ struct Material {
 	int phong = 0;
 	double kd[4] = {1, 1, 1, 0}, ks[4] = {0, 0, 0, 0};
 	double shin = 1.0, refl = 0.0, refr = 0.0, ior = 1.5;
+	bool have_normal = false;         /* a "normal" attribute is present */
+	double nrm_scale = 1.0;           /* its colour's x */
+	int tex[TA_COUNT] = {-1, -1, -1, -1, -1, -1, -1};   /* texture per attribute, -1 = none */
 };
+
+/* a texture image: RGBA floats, rows top first */
+struct Texture {
+	int xsz = 0, ysz = 0;
+	std::vector<float> pix;
+};
+
+/* Texture::load (src/texture.cc:28-36): the file found by find_file
+ * (src/datapath.c:57-77) in the first directory of SRAY_DATA_PATH (the
+ * reference's list parser stops after the first entry), read as RGBA
+ * floats.  Binary PPM (P6, maxval <= 255) is the format read. */
+bool load_texture(const char *name, Texture &t);
 
 enum { OBJ_SPHERE = 0, OBJ_CYLINDER = 1, OBJ_MESH = 2 };
 enum { LT_POINT = 0, LT_SPHERE = 1, LT_BOX = 2 };
@@ -141,6 +156,7 @@ struct Camera {
 struct HostScene {
 	std::vector<Material> mats;
 	Material defmat;
+	std::vector<Texture> texs;
 	std::vector<Object> objs;
 	std::vector<Light> lights;
 	std::vector<Mesh> meshes;

@@ -75,11 +75,25 @@ struct alignas(16) DevObj {
 	int bvh_root;   /* mesh: root node in the mesh hierarchies, -1 if none */
 };
 
+/* attributes that can carry a texture, in DevMat::tex order */
+enum { TA_DIFFUSE, TA_SPECULAR, TA_SHININESS, TA_REFLECT, TA_REFRACT, TA_IOR, TA_NORMAL, TA_COUNT };
+
 struct alignas(16) DevMat {
 	float kd[4], ks[4];
 	float shin, refl, refr, ior;
 	int phong;
-	int pad[3];
+	int textured;      /* some attribute has a texture */
+	int have_normal;   /* the material has a "normal" attribute (src/shader.cc:136-139) */
+	int pad;
+	int tex[8];        /* texture of each attribute (TA_*), -1 = none */
+	float scol[8];     /* the attribute colour's x: factor of a textured scalar, bump scale */
+};
+
+/* a texture: RGBA float texels, rows top first, at `off` (in texels) in the
+ * scene's texel table */
+struct alignas(16) DevTex {
+	long long off;
+	int xsz, ysz;
 };
 
 struct alignas(16) DevLight {

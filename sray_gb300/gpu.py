@@ -15,7 +15,7 @@ _LIB = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libsray
 _lib = None
 
 EXPORTS = ["sray_default_opts", "sray_gpu_init", "sray_gpu_set_opts", "sray_gpu_load_scene", "sray_gpu_load_scene_mem",
-           "sray_gpu_load_scene_sidecar",
+           "sray_gpu_load_scene_sidecar", "sray_gpu_add_data_path",
            "sray_gpu_scene_info", "sray_gpu_build", "sray_gpu_shoot_photons", "sray_gpu_render",
            "sray_gpu_render_pixels", "sray_gpu_cast_rays", "sray_gpu_primary_hits", "sray_gpu_photon_gather", "sray_gpu_photon_gather_noalloc",
            "sray_gpu_get_photons", "sray_gpu_dump_photons", "sray_gpu_restore_photons", "sray_gpu_render_batch",
@@ -90,6 +90,7 @@ def load_library():
     L.sray_gpu_load_scene.argtypes = [ctypes.c_char_p]
     L.sray_gpu_load_scene_mem.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     L.sray_gpu_load_scene_sidecar.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
+    L.sray_gpu_add_data_path.argtypes = [ctypes.c_char_p]
     L.sray_gpu_scene_info.argtypes = [vp, vp, vp, vp, vp]
     L.sray_gpu_build.argtypes = [lp, lp]
     L.sray_gpu_shoot_photons.argtypes = [lp, lp, vp, vp, vp]
@@ -216,6 +217,11 @@ class GpuRenderer:
     def load_xml(self, xml):
         b = xml.encode() if isinstance(xml, str) else xml
         self._chk(self.L.sray_gpu_load_scene_mem(b, len(b)))
+
+    def add_data_path(self, directory):
+        """Prepend a directory to the texture search path (SRAY_DATA_PATH);
+        textures are looked up in its first directory only."""
+        self._chk(self.L.sray_gpu_add_data_path(directory.encode()))
 
     def scene_info(self):
         a, b, c, e = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()

@@ -22,7 +22,7 @@ import os
 import numpy as np
 
 __all__ = ["icosphere", "value_noise_height", "small_scene", "production_scene", "feature_scene",
-           "scene_opts", "write_scene", "CONFIGS"]
+           "textured_scene", "textures", "write_textures", "scene_opts", "write_scene", "CONFIGS"]
 
 
 def _f(x):
@@ -94,7 +94,7 @@ def value_noise_height(x, z, seed, octaves=6, amplitude=2.0, base_freq=0.05):
     return amplitude * 2.0 * h / norm
 
 
-def _mesh_xml(out, name, mat, verts, faces, normals=None, xform=None):
+def _mesh_xml(out, name, mat, verts, faces, normals=None, xform=None, texcoords=None, tangents=None):
     out.append('<object type="mesh" name="%s">\n<matref name="%s"/>\n' % (name, mat))
     if xform:
         out.append(xform)
@@ -103,7 +103,20 @@ def _mesh_xml(out, name, mat, verts, faces, normals=None, xform=None):
     ids = np.arange(len(verts))
     out.append("".join('<vertex id="%d" val="%s %s %s"/>\n' % (i, a, b, c)
                        for i, (a, b, c) in zip(ids, vs)))
-    if normals is not None:
+    if texcoords is not None:
+        # every vertex carries a normal, a texture coordinate and a tangent
+        ns = np.char.mod("%.9g", normals.astype(np.float32).astype(np.float64))
+        ts = np.char.mod("%.9g", texcoords.astype(np.float32).astype(np.float64))
+        gs = np.char.mod("%.9g", tangents.astype(np.float32).astype(np.float64))
+        for i in ids:
+            out.append('<normal id="%d" val="%s %s %s"/>\n' % (i, *ns[i]))
+            out.append('<texcoord id="%d" val="%s %s"/>\n' % (i, *ts[i]))
+            out.append('<tangent id="%d" val="%s %s %s"/>\n' % (i, *gs[i]))
+        out.append("".join(
+            "<face>%s</face>\n" % "".join('<vref vertex="%d" normal="%d" texcoord="%d" tangent="%d"/>' % (v, v, v, v)
+                                          for v in f)
+            for f in faces.tolist()))
+    elif normals is not None:
         ns = np.char.mod("%.9g", normals.astype(np.float32).astype(np.float64))
         out.append("".join('<normal id="%d" val="%s %s %s"/>\n' % (i, a, b, c)
                            for i, (a, b, c) in zip(ids, ns)))
@@ -385,6 +398,114 @@ def feature_scene(seed=0x5EED0003):
     return "".join(out)
 
 
+def _ppm(w, h, rgb):
+    """Binary PPM (P6) bytes of an [h, w, 3] uint8 image."""
+    return b"P6\n%d %d\n255\n" % (w, h) + np.ascontiguousarray(rgb, dtype=np.uint8).tobytes()
+
+
+def textures():
+    """The images of the textured scene, {file name: PPM bytes}.  Integer
+    formulas only, so that every machine writes the same bytes."""
+    y, x = np.mgrid[0:64, 0:64].astype(np.int64)
+    blk = ((x >> 3) + (y >> 3)) & 3
+    pal = np.array([[230, 210, 180], [60, 90, 160], [200, 60, 50], [90, 170, 80]], dtype=np.int64)
+    tiles = np.clip(pal[blk] - ((x * 7 + y * 13) & 31)[..., None], 0, 255)
+    y, x = np.mgrid[0:32, 0:32].astype(np.int64)
+    dx, dy = (x & 15) - 8, (y & 15) - 8
+    bumps = np.stack([128 + dx * 12, 128 + dy * 12, np.full_like(dx, 220)], axis=-1)
+    y, x = np.mgrid[0:16, 0:16].astype(np.int64)
+    stripes = 80 + ((x + y) & 3) * 55
+    mask = np.stack([stripes, stripes, stripes], axis=-1)
+    y, x = np.mgrid[0:8, 0:8].astype(np.int64)
+    ramp = 200 + x * 7
+    iorm = np.stack([ramp, ramp, ramp], axis=-1)
+    return {"tiles.ppm": _ppm(64, 64, tiles), "bumps.ppm": _ppm(32, 32, bumps),
+            "stripes.ppm": _ppm(16, 16, mask), "ior.ppm": _ppm(8, 8, iorm)}
+
+
+def write_textures(directory):
+    """Write the textured scene's images into `directory` (the directory a
+    renderer searches through SRAY_DATA_PATH)."""
+    os.makedirs(directory, exist_ok=True)
+    for name, data in textures().items():
+        path = os.path.join(directory, name)
+        if not os.path.exists(path) or open(path, "rb").read() != data:
+            tmp = path + ".tmp%d" % os.getpid()
+            with open(tmp, "wb") as f:
+                f.write(data)
+            os.replace(tmp, path)
+
+
+def _uv_sphere_frame(v):
+    """Texture coordinates and tangents of a unit sphere's vertices, with the
+    sphere primitive's own mapping (src/sphere.cc:118-124)."""
+    th = np.arctan2(v[:, 2], v[:, 0]) + np.pi
+    ph = np.arccos(np.clip(v[:, 1], -1.0, 1.0))
+    tc = np.stack([th / (2 * np.pi), ph / np.pi], axis=1)
+    tg = np.cross(np.array([0.0, 1.0, 0.0]), v)
+    n = np.linalg.norm(tg, axis=1, keepdims=True)
+    tg = np.where(n > 1e-6, tg / np.maximum(n, 1e-12), np.array([1.0, 0.0, 0.0]))
+    return tc, tg
+
+
+def textured_scene():
+    """A small scene of textured materials (the files of textures()): a tiled
+    floor mesh with texture coordinates and tangents, a normal-mapped sphere
+    with striped specular and shininess, a normal-mapped glass sphere with a
+    textured index of refraction (caustic photons through a bumped surface),
+    a striped mirror, a tiled cylinder, a textured icosphere, one material
+    with an untextured "normal" attribute and one whose texture fails to
+    load; a point and a sphere light."""
+    out = ["<?xml version=\"1.0\"?>\n<scene>\n"]
+    out.append('<env ambient="0.08" bgcolor="0.15 0.18 0.25" ior="1.0"/>\n')
+    out.append('<material name="floor" shader="phong">\n<mattr name="diffuse" value="0.9" map="tiles.ppm"/>\n'
+               '<mattr name="specular" value="0.15"/>\n<mattr name="shininess" value="20.0"/>\n</material>\n')
+    out.append('<material name="bumpy" shader="phong">\n<mattr name="diffuse" value="0.75 0.5 0.3"/>\n'
+               '<mattr name="specular" value="0.7" map="stripes.ppm"/>\n'
+               '<mattr name="shininess" value="60.0" map="stripes.ppm"/>\n'
+               '<mattr name="normal" value="1.5" map="bumps.ppm"/>\n</material>\n')
+    out.append('<material name="glass" shader="phong">\n<mattr name="diffuse" value="0.05"/>\n'
+               '<mattr name="specular" value="1.0"/>\n<mattr name="shininess" value="80.0"/>\n'
+               '<mattr name="refract" value="1.0"/>\n<mattr name="ior" value="1.6" map="ior.ppm"/>\n'
+               '<mattr name="normal" value="0.6" map="bumps.ppm"/>\n</material>\n')
+    out.append('<material name="mirror" shader="phong">\n<mattr name="diffuse" value="0.2"/>\n'
+               '<mattr name="specular" value="1.0"/>\n<mattr name="shininess" value="90.0"/>\n'
+               '<mattr name="reflect" value="0.9" map="stripes.ppm"/>\n</material>\n')
+    out.append('<material name="pillar" shader="phong">\n<mattr name="diffuse" value="0.8 0.8 0.7" map="tiles.ppm"/>\n'
+               '<mattr name="specular" value="0.3"/>\n<mattr name="shininess" value="25.0"/>\n'
+               '<mattr name="normal" value="1.0"/>\n</material>\n')
+    out.append('<material name="lost" shader="phong">\n<mattr name="diffuse" value="0.3 0.6 0.4" map="no_such.ppm"/>\n'
+               '<mattr name="specular" value="0.4"/>\n<mattr name="shininess" value="30.0"/>\n</material>\n')
+    g = 8.0
+    gv = np.array([[-g, 0, -g], [g, 0, -g], [g, 0, g], [-g, 0, g]], dtype=np.float32)
+    gf = np.array([[0, 2, 1], [0, 3, 2]], dtype=np.int32)
+    gn = np.tile(np.array([[0.0, 1.0, 0.0]]), (4, 1))
+    gt = np.array([[0.0, 0.0], [3.0, 0.0], [3.0, 3.0], [0.0, 3.0]])     # three repeats across the floor
+    gg = np.tile(np.array([[1.0, 0.0, 0.0]]), (4, 1))
+    _mesh_xml(out, "floor", "floor", gv, gf, normals=gn, texcoords=gt, tangents=gg)
+    out.append('<object type="sphere" name="bumpy">\n<matref name="bumpy"/>\n%s<sphere rad="1.1"/>\n</object>\n'
+               % _xform(pos=(-1.6, 1.1, 0.2)))
+    out.append('<object type="sphere" name="glass">\n<matref name="glass"/>\n%s<sphere rad="0.8"/>\n</object>\n'
+               % _xform(pos=(1.3, 1.3, 1.4)))
+    out.append('<object type="sphere" name="mirror">\n<matref name="mirror"/>\n%s<sphere rad="0.9"/>\n</object>\n'
+               % _xform(pos=(1.2, 0.9, -2.2)))
+    out.append('<object type="cylinder" name="pillar">\n<matref name="pillar"/>\n%s'
+               '<cylinder rad="0.45" start="0.0" end="2.4"/>\n</object>\n' % _xform(pos=(3.2, 0.0, -0.6)))
+    iv, ifc = icosphere(2)
+    tc, tg = _uv_sphere_frame(iv.astype(np.float64))
+    _mesh_xml(out, "ico", "bumpy", iv, ifc, normals=iv, texcoords=tc, tangents=tg,
+              xform=_xform(pos=(-2.8, 0.6, 2.6), scale=(0.6, 0.6, 0.6)))
+    out.append('<object type="sphere" name="lost">\n<matref name="lost"/>\n%s<sphere rad="0.5"/>\n</object>\n'
+               % _xform(pos=(0.2, 0.5, 2.8)))
+    out.append('<light type="point" color="0.9">\n%s</light>\n' % _xform(pos=(2.0, 7.0, 3.0)))
+    out.append('<light type="sphere" color="0.4 0.38 0.35">\n%s<sphere rad="0.5"/>\n</light>\n'
+               % _xform(pos=(-3.0, 5.5, -1.0)))
+    out.append('<camera type="target" fov="50.0">\n%s<target>\n%s</target>\n</camera>\n'
+               % (_xform(pos=(0.5, 4.0, 9.0)), _xform(pos=(0.0, 0.8, 0.0))))
+    out.append("</scene>\n")
+    return "".join(out)
+
+
 # option sets (sray_opts fields) of the benchmark configurations
 CONFIGS = {
     "small": dict(width=512, height=512, min_samples=1, max_samples=1, iter=5,
@@ -402,6 +523,9 @@ CONFIGS = {
                    caust_photons=4000000, gi_photons=20000000, caust_k=100, gi_k=100, gather_rcap=0.5,
                    mblur=1, shutter=40, time_start=0, time_end=0,
                    scnoct_max_depth=8, scnoct_max_items=8, meshoct_max_depth=10, meshoct_max_items=8),
+    # textured materials and normal maps (the reference's fixed-radius gathers)
+    "textured": dict(width=128, height=96, min_samples=1, max_samples=2, max_var=0.02, iter=6,
+                     caust_photons=20000, gi_photons=30000, shadow_samples=2, diffuse_samples=2, gather_dist=0.02),
     "production": dict(width=1920, height=1080, min_samples=1, max_samples=16, max_var=0.05, iter=8,
                        caust_photons=500000, gi_photons=2000000, caust_k=100, gi_k=100, gather_rcap=0.5,
                        scnoct_max_depth=8, scnoct_max_items=8, meshoct_max_depth=10, meshoct_max_items=8),
@@ -417,7 +541,7 @@ def scene_opts(name, **over):
 def write_scene(name, cache_dir=None, **kw):
     """Generate (or reuse from cache_dir) the XML of scene `name`; returns the path."""
     gen = {"small": small_scene, "learned": small_scene, "production": production_scene, "feature": feature_scene,
-           "stress": stress_scene}[name]
+           "stress": stress_scene, "textured": textured_scene}[name]
     key = hashlib.sha1(repr((name, sorted(kw.items()), 3)).encode()).hexdigest()[:12]
     cache_dir = cache_dir or os.environ.get("SRAY_SCENE_CACHE", "/tmp/sray_scenes")
     os.makedirs(cache_dir, exist_ok=True)
@@ -432,4 +556,6 @@ def write_scene(name, cache_dir=None, **kw):
                 for chunk in xml:      # generators write their document in pieces
                     f.write(chunk)
         os.replace(tmp, path)
+    if name == "textured":
+        write_textures(cache_dir)
     return path

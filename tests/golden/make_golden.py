@@ -2,13 +2,14 @@
 
 Runs the reference's own rendering code (compiled from its unmodified
 sources by oracle/build_ref.py, with the project's libvmath/kdtree/imago
-stand-ins and a Philox stream per photon and per pixel sample) on three
-seeded scenes and stores, per case: the scene XML, the options, the
+stand-ins and a Philox stream per photon and per pixel sample) on four
+seeded scenes (the textured one reads the images of scenegen.textures()
+through SRAY_DATA_PATH) and stores, per case: the scene XML, the options, the
 primary-hit ids and t, the stored caustic and global photons, and the
 rendered image with its per-pixel sample counts.
 
 Only runs where the reference sources are present:
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 """
 import gzip
 import json
@@ -41,6 +42,10 @@ CASES = {
                  "-moctdepth", "8", "-moctitems", "8"],
                 dict(width=64, height=36, min_samples=1, max_samples=2, max_var=0.05, caust_photons=5000,
                      gi_photons=20000, iter=4, gather_dist=0.01, meshoct_max_depth=8, meshoct_max_items=8)),
+    "textured": ("textured", {}, ["-s", "64x48", "-r", "1-2", "-d", "0.02", "-c", "20000", "-g", "30000", "-i", "6",
+                                  "-shadowrays", "2", "-diffuserays", "2", "-gatherdisc", "0.02"],
+                 dict(width=64, height=48, min_samples=1, max_samples=2, max_var=0.02, caust_photons=20000,
+                      gi_photons=30000, iter=6, shadow_samples=2, diffuse_samples=2, gather_dist=0.02)),
 }
 
 
@@ -49,10 +54,13 @@ def run_case(harness, name, spec):
     gen, kw, cli, oopts = spec
     path = scenegen.write_scene(gen, **kw)
     xml = open(path, "rb").read()
+    # textures are found through the first directory of SRAY_DATA_PATH
+    env = dict(os.environ, SRAY_DATA_PATH=os.path.dirname(path))
     with tempfile.TemporaryDirectory() as td:
         prefix = os.path.join(td, name)
         h = oopts["height"]
-        subprocess.check_call([harness, path, prefix, hex(SEED), "0", str(h)] + cli, stdout=subprocess.DEVNULL)
+        subprocess.check_call([harness, path, prefix, hex(SEED), "0", str(h)] + cli, stdout=subprocess.DEVNULL,
+                              env=env)
         hits = np.fromfile(prefix + ".hits", dtype=np.dtype([("o", "<i4"), ("p", "<i4"), ("t", "<f8")]))
         caust = np.fromfile(prefix + ".caust", dtype=np.float32).reshape(-1, 16)
         gi = np.fromfile(prefix + ".gi", dtype=np.float32).reshape(-1, 16)
@@ -74,8 +82,9 @@ def main():
     if not harness:
         print("reference sources not present; nothing to do")
         return 0
-    for name, spec in CASES.items():
-        run_case(harness, name, spec)
+    names = sys.argv[1:] or list(CASES)
+    for name in names:
+        run_case(harness, name, CASES[name])
     with open(os.path.join(HERE, "MACHINE"), "w") as f:
         f.write(os.uname().machine + "\n")
     return 0

@@ -4,6 +4,8 @@ reduced resolution for speed where stated).
 Bars: primary-hit object and primitive ids bit-exact except on rays flagged
 as exact-t ties; photon maps identical as sets; per-pixel radiance within
 1e-3 relative (on 99.9% of pixels; the rest are counted and reported)."""
+import os
+
 import numpy as np
 import pytest
 import torch
@@ -147,6 +149,76 @@ def test_cast_rays_kats(gpu_lib, oracle_lib):
     oo, op, ot, _ = o.cast_rays(orig.astype(np.float32).astype(np.float64), dirs.astype(np.float32).astype(np.float64))
     assert np.array_equal(oo, obj.cpu().numpy()) and np.array_equal(op, prim.cpu().numpy())
     assert np.array_equal(ot.astype(np.float32), t.cpu().numpy())
+
+
+@pytest.fixture
+def textured_pair(gpu_lib, oracle_lib, monkeypatch, tmp_path):
+    """The textured scene, its images found through SRAY_DATA_PATH."""
+    def make(data_dir=None, **over):
+        opts = scenegen.scene_opts("textured", **over)
+        path = scenegen.write_scene("textured")
+        monkeypatch.setenv("SRAY_DATA_PATH", data_dir or os.path.dirname(path))
+        g = gpu_lib.GpuRenderer(**opts)
+        g.load(path)
+        o = oracle_lib.Oracle(fp64=False, rng_mode=1, **opts)
+        o.load(path)
+        return g, o
+    return make
+
+
+def test_textured_scene(textured_pair, tmp_path):
+    # diffuse, specular, shininess, reflect and ior textures; normal maps on a
+    # sphere, on a glass sphere (caustic photons through the bumped surface)
+    # and on a mesh with vertex tangents; an untextured "normal" attribute
+    # and a texture that fails to load
+    g, o = textured_pair()
+    o.prepare(0)
+    nc, ng = g.shoot_photons(0, 0)
+    for which, n in ((0, nc), (1, ng)):
+        ph_o, ph_g = o.photons(which), g.photons(which)
+        ko = np.lexsort(ph_o[:, :12].T[::-1])
+        kg = np.lexsort(ph_g[:, :12].T[::-1])
+        same = len(ph_o) == len(ph_g) and np.array_equal(ph_o[ko, :12], ph_g[kg, :12])
+        print("%s photons: oracle %d gpu %d identical %s" % (("caustic", "global")[which], len(ph_o), len(ph_g), same))
+        assert len(ph_g) == n
+        assert abs(len(ph_o) - len(ph_g)) <= max(2, len(ph_o) // 1000)
+    img_g = g.render(0)
+    img_o = o.render(0)
+    assert _compare(img_g, img_o, "textured 128x96") <= 1e-3
+    # the same scene with no image found: the attributes fall back to their
+    # colours, and the picture changes
+    g2, _ = textured_pair(data_dir=str(tmp_path))
+    img_u = g2.render(0)
+    changed = (np.abs(img_u[..., :3] - img_g[..., :3]).max(-1) > 1e-3).mean()
+    print("pixels changed by the textures: %.1f%%" % (100 * changed))
+    assert changed > 0.2
+
+
+def test_textured_primary_hits_match_reference(gpu_lib, monkeypatch, tmp_path):
+    # primary hits of the textured scene against the reference's own (the
+    # golden fixture the oracle is pinned to)
+    import gzip
+    import json
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    d = np.load(os.path.join(here, "textured.npz"))
+    opts = json.loads(bytes(d["opts"]).decode())
+    with gzip.open(os.path.join(here, "textured.xml.gz")) as f:
+        xml = f.read()
+    scenegen.write_textures(str(tmp_path))
+    monkeypatch.setenv("SRAY_DATA_PATH", str(tmp_path))
+    g = gpu_lib.GpuRenderer(**opts)
+    g.load_xml(xml)
+    n = opts["width"] * opts["height"]
+    obj = torch.empty(n, dtype=torch.int32, device="cuda")
+    prim = torch.empty(n, dtype=torch.int32, device="cuda")
+    t = torch.empty(n, dtype=torch.float32, device="cuda")
+    tie = torch.empty(n, dtype=torch.uint8, device="cuda")
+    g.primary_hits(obj, prim, t, tie)
+    torch.cuda.synchronize()
+    gobj, gprim = obj.cpu().numpy(), prim.cpu().numpy()
+    mism = (gobj != d["obj"]) | (gprim != d["prim"])
+    print("textured primary hits: %d mismatches of %d (ties %d)" % (mism.sum(), n, int((tie.cpu().numpy() > 0).sum())))
+    assert mism.mean() <= 1e-3
 
 
 def test_feature_scene_motion_blur_area_lights(gpu_lib, oracle_lib):

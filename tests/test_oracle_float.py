@@ -6,6 +6,8 @@ float: the quadric roots (solved without cancellation in float) and light
 samples leaving a surface at a shallow angle (started off the surface in
 float).  With those, per-pixel radiance agrees within 1e-3 relative on all
 but a few pixels (silhouettes and exact ties)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -27,9 +29,13 @@ def _agreement(oracle_lib, opts, path):
     ("small", dict(width=128, height=128)),
     ("learned", dict(width=160, height=90, gi_photons=100000)),
     ("production", dict(width=96, height=54, caust_photons=20000, gi_photons=50000, max_samples=1)),
+    ("textured", dict()),
 ])
-def test_float_mode_tracks_double(oracle_lib, name, over):
+def test_float_mode_tracks_double(oracle_lib, name, over, monkeypatch):
     opts = scenegen.scene_opts(name, **over)
-    frac, rmse = _agreement(oracle_lib, opts, scenegen.write_scene(name))
+    path = scenegen.write_scene(name)
+    if name == "textured":      # its images sit beside the scene file
+        monkeypatch.setenv("SRAY_DATA_PATH", os.path.dirname(path))
+    frac, rmse = _agreement(oracle_lib, opts, path)
     print("%s: pixels over 1e-3 relative %.4f%%, rmse %.2e" % (name, 100 * frac, rmse))
     assert frac <= 2e-3

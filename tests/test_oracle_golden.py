@@ -1,6 +1,7 @@
 """The CPU oracle against golden fixtures produced by the reference's own
 code (tests/golden/make_golden.py): primary-hit ids and t, stored photons,
-images and per-pixel sample counts of three seeded scenes.
+images and per-pixel sample counts of four seeded scenes (one of them
+textured).
 
 On the machine type the fixtures were generated on the FP64 oracle must be
 bit-exact.  Elsewhere the C library's transcendental functions may differ in
@@ -16,7 +17,7 @@ import numpy as np
 import pytest
 
 HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["small_range", "feature", "terrain"]
+CASES = ["small_range", "feature", "terrain", "textured"]
 
 
 def fixture_machine():
@@ -24,8 +25,18 @@ def fixture_machine():
         return f.read().strip()
 
 
+def use_textures(monkeypatch, tmp_path):
+    """The textured scene's images, found through SRAY_DATA_PATH as the
+    reference's find_file does."""
+    from sray_gb300 import scenegen
+    scenegen.write_textures(str(tmp_path))
+    monkeypatch.setenv("SRAY_DATA_PATH", str(tmp_path))
+
+
 @pytest.mark.parametrize("case", CASES)
-def test_oracle_matches_reference(oracle_lib, case):
+def test_oracle_matches_reference(oracle_lib, case, monkeypatch, tmp_path):
+    if case == "textured":
+        use_textures(monkeypatch, tmp_path)
     d = np.load(os.path.join(HERE, case + ".npz"))
     opts = json.loads(bytes(d["opts"]).decode())
     with gzip.open(os.path.join(HERE, case + ".xml.gz")) as f:
