@@ -291,7 +291,9 @@ typedef struct sray_tuning {
 	int pool_blocks_per_sm;   /* 128-thread blocks per SM of the pool launch (4) */
 	int photon_tail;          /* photons in flight below which the photon tail runs in one
 	                             persistent launch (65536) */
-	int reserved[5];
+	int shadow_order;         /* any-hit traversal of light samples: 0 visits a node's hit
+	                             children nearest first, 1 in the node's order (0) */
+	int reserved[4];
 } sray_tuning;
 
 typedef struct sray_tune_trial {

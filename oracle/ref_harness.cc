@@ -66,7 +66,9 @@ int main(int argc, char **argv)
 	if(!scn->load(scene_path)) return 1;
 	if(!scn->get_camera()) scn->set_camera(new Camera);
 	Camera *cam = scn->get_camera();
-	long msec = 0;
+	/* the frame time (default 0): SRAY_REF_MSEC */
+	const char *ms_env = getenv("SRAY_REF_MSEC");
+	long msec = ms_env ? atol(ms_env) : 0;
 	long shutter = cam->get_shutter();
 	long t0 = msec - shutter / 2, t1 = t0 + shutter;
 

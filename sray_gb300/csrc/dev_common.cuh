@@ -800,8 +800,10 @@ __device__ __forceinline__ RayT object_ray(const DScene &S, int o, int ti, V3 wo
 
 /* ANY = false: closest hit into h, returns false when the octrees must
  * decide.  ANY = true: returns 1 when a hit the octrees reach exists, 0 when
- * no hit exists, 2 when the octrees must decide. */
-template <bool COUNT, bool ANY>
+ * no hit exists, 2 when the octrees must decide.  SORT: a node's hit
+ * children are visited nearest first (always for closest hits); an any-hit
+ * query may visit them in the node's order instead. */
+template <bool COUNT, bool ANY, bool SORT = true>
 __device__ __forceinline__ int trace_two_level(const DScene &S, V3 wo, V3 wd, int time, Hit &h, TraceCounters *tc, int *overflow)
 {
 	h.t = FLT_MAX;
@@ -938,6 +940,22 @@ __device__ __forceinline__ int trace_two_level(const DScene &S, V3 wo, V3 wd, in
 		key[1] = (ref[1] != BVH_NONE && wide_box(rc, lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, lim, tn)) ? tn : INFINITY;
 		key[2] = (ref[2] != BVH_NONE && wide_box(rc, lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, lim, tn)) ? tn : INFINITY;
 		key[3] = (ref[3] != BVH_NONE && wide_box(rc, lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, lim, tn)) ? tn : INFINITY;
+		if(ANY && !SORT) {
+			/* the hit children in node order: the first is next, the rest
+			 * are stacked so that they pop in order */
+			int nxt = BVH_NONE;
+			#pragma unroll
+			for(int k = 3; k >= 0; k--) {
+				if(key[k] == INFINITY) continue;
+				if(nxt != BVH_NONE) {
+					if(sp >= SRAY_STACK) { *overflow = 1; return 0; }
+					st.node[sp++] = nxt;
+				}
+				nxt = ref[k];
+			}
+			cur = nxt;
+			continue;
+		}
 #define SRAY_CSWAP(i, j) do { if(key[j] < key[i]) { float tk = key[i]; key[i] = key[j]; key[j] = tk; int tr_ = ref[i]; ref[i] = ref[j]; ref[j] = tr_; } } while(0)
 		SRAY_CSWAP(0, 1);
 		SRAY_CSWAP(2, 3);
@@ -954,7 +972,7 @@ __device__ __forceinline__ int trace_two_level(const DScene &S, V3 wo, V3 wd, in
 			if(key[k] == INFINITY) continue;
 			if(sp >= SRAY_STACK) { *overflow = 1; return ANY ? 0 : 1; }
 			st.node[sp] = ref[k];
-			st.te[sp] = key[k];
+			if(!ANY) st.te[sp] = key[k];   /* any hit visits every entry */
 			sp++;
 		}
 		cur = ref[0];

@@ -680,7 +680,7 @@ __global__ void __launch_bounds__(128) k_render_pool(DScene S, RayQueue pool, in
 /* shadow rays: the reference tests visibility with cast_ray(shadow_ray)
  * (src/shader.cc:266), a hit anywhere on the segment [eps, 1] blocks */
 /* shadow rays; HYB and fb as for k_trace */
-template <bool HYB>
+template <bool HYB, bool SORT = true>
 __global__ void __launch_bounds__(SRAY_TRACE_THREADS, 6) k_shadow(DScene S, const ShadowReq *sq, const int *sq_count, float4 *acc,
 		DevCounters *ctr, int *fb)
 {
@@ -693,7 +693,7 @@ __global__ void __launch_bounds__(SRAY_TRACE_THREADS, 6) k_shadow(DScene S, cons
 		int res;
 		if(HYB) {
 			Hit h;
-			res = trace_two_level<false, true>(S, mk(r.a.x, r.a.y, r.a.z), mk(r.b.x, r.b.y, r.b.z), time, h, nullptr, &overflow);
+			res = trace_two_level<false, true, SORT>(S, mk(r.a.x, r.a.y, r.a.z), mk(r.b.x, r.b.y, r.b.z), time, h, nullptr, &overflow);
 		} else {
 			res = trace_any_octree_impl(S, mk(r.a.x, r.a.y, r.a.z), mk(r.b.x, r.b.y, r.b.z), time, &overflow) ? 1 : 0;
 		}
@@ -1332,15 +1332,65 @@ void Renderer::fill_scene_desc()
 	D.gi = gi.map;
 }
 
-static void pack_xf(const double m[4][4], float *dst)
+
+/* The frame's transform table on the device: thread (i, t) evaluates the
+ * keyframe tracks of object i at time tlo + t and writes its record
+ * (forward, inverse, inverse transpose; XF_STRIDE floats), or, past the
+ * objects, light i's position (4 floats).  The evaluation is anim_eval.h's,
+ * the same code the host runs for object bounds and projection maps. */
+__global__ void k_xforms(const DevAnim *anims, const int *kt, const double *kv, int nobj, int nlights, int tlo, int nt, float *xf,
+		float *lpos)
 {
-	double inv[4][4];
-	mat_inverse(inv, m);
-	for(int i = 0; i < 3; i++) for(int j = 0; j < 4; j++) dst[i * 4 + j] = (float)m[i][j];
-	for(int i = 0; i < 3; i++) for(int j = 0; j < 4; j++) dst[12 + i * 4 + j] = (float)inv[i][j];
-	/* inverse transpose, 3x3: it[r][c] = inv[c][r] */
-	for(int r = 0; r < 3; r++) for(int c = 0; c < 3; c++) dst[24 + r * 3 + c] = (float)inv[c][r];
-	for(int k = 33; k < XF_STRIDE; k++) dst[k] = 0.0f;
+	long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= (long long)(nobj + nlights) * nt) return;
+	int ai = (int)(i / nt), t = (int)(i % nt);
+	const DevAnim &a = anims[ai];
+	KeyView kp = {kt + a.toff[0], kv + a.voff[0], a.def, a.n[0], 3, a.interp[0], a.extrap[0]};
+	double p[3];
+	key_eval(kp, tlo + t, p);
+	if(ai >= nobj) {
+		float *d = lpos + ((size_t)(ai - nobj) * nt + t) * 4;
+		d[0] = (float)p[0];
+		d[1] = (float)p[1];
+		d[2] = (float)p[2];
+		d[3] = 0.0f;
+		return;
+	}
+	KeyView kr = {kt + a.toff[1], kv + a.voff[1], a.def + 3, a.n[1], 4, a.interp[1], a.extrap[1]};
+	KeyView ks = {kt + a.toff[2], kv + a.voff[2], a.def + 7, a.n[2], 3, a.interp[2], a.extrap[2]};
+	double q[4], sc[3], m[4][4];
+	key_eval(kr, tlo + t, q);
+	key_eval(ks, tlo + t, sc);
+	node_matrix(p, q, sc, a.pivot, m);
+	pack_transform(m, xf + ((size_t)ai * nt + t) * XF_STRIDE, XF_STRIDE);
+}
+
+/* a node's tracks appended to the key tables */
+template <class T> static void add_track(const Track<T> &tr, int k, DevAnim &a, std::vector<int> &kt, std::vector<double> &kv)
+{
+	a.toff[k] = (int)kt.size();
+	a.voff[k] = (int)kv.size();
+	a.n[k] = (int)tr.time.size();
+	a.interp[k] = tr.interp;
+	a.extrap[k] = tr.extrap;
+	kt.insert(kt.end(), tr.time.begin(), tr.time.end());
+	const double *v = reinterpret_cast<const double *>(tr.val.data());
+	kv.insert(kv.end(), v, v + tr.val.size() * (sizeof(T) / sizeof(double)));
+}
+static DevAnim dev_anim(const XForm &xf, bool position_only, std::vector<int> &kt, std::vector<double> &kv)
+{
+	DevAnim a;
+	memset(&a, 0, sizeof a);
+	add_track(xf.pos, 0, a, kt, kv);
+	if(!position_only) {
+		add_track(xf.rot, 1, a, kt, kv);
+		add_track(xf.scale, 2, a, kt, kv);
+	}
+	a.pivot[0] = xf.pivot.x; a.pivot[1] = xf.pivot.y; a.pivot[2] = xf.pivot.z;
+	a.def[0] = xf.pos.def.x; a.def[1] = xf.pos.def.y; a.def[2] = xf.pos.def.z;
+	a.def[3] = xf.rot.def.s; a.def[4] = xf.rot.def.x; a.def[5] = xf.rot.def.y; a.def[6] = xf.rot.def.z;
+	a.def[7] = xf.scale.def.x; a.def[8] = xf.scale.def.y; a.def[9] = xf.scale.def.z;
+	return a;
 }
 
 int Renderer::upload_scene(cudaStream_t s)
@@ -1469,6 +1519,15 @@ int Renderer::upload_scene(cudaStream_t s)
 	CK(objs.upload(dobj, s), "upload objects");
 	CK(mats.upload(dm, s), "upload materials");
 	CK(lights.upload(dl, s), "upload lights");
+	/* keyframe tracks: the objects', then the lights' positions */
+	std::vector<DevAnim> da;
+	std::vector<int> kt;
+	std::vector<double> kv;
+	for(const Object &o : sc.objs) da.push_back(dev_anim(o.xf, false, kt, kv));
+	for(const Light &l : sc.lights) da.push_back(dev_anim(l.xf, true, kt, kv));
+	CK(anims.upload(da, s), "upload keyframe tracks");
+	CK(key_t.upload(kt, s), "upload key times");
+	CK(key_v.upload(kv, s), "upload key values");
 	CK(bnodes.upload(bn, s), "upload mesh hierarchies");
 	CK(btris.upload(bt, s), "upload hierarchy triangles");
 	CK(bprim.upload(bp, s), "upload hierarchy face ids");
@@ -1535,30 +1594,16 @@ int Renderer::build_frame(long bt0, long bt1, cudaStream_t s)
 	tlo = t0 - shutter - 2;
 	int thi = t1 + shutter + 2;
 	nt = thi - tlo + 1;
-	std::vector<float> xfs((size_t)sc.objs.size() * nt * XF_STRIDE);
-	for(size_t i = 0; i < sc.objs.size(); i++) {
-		float *row = &xfs[(size_t)i * nt * XF_STRIDE];
-		if(sc.objs[i].is_static) {
-			/* at most one key per track: the same matrices at every time */
-			double m[4][4];
-			sc.objs[i].xf.matrix(tlo, m);
-			pack_xf(m, row);
-			for(int t = 1; t < nt; t++) memcpy(row + (size_t)t * XF_STRIDE, row, XF_STRIDE * sizeof(float));
-			continue;
-		}
-		for(int t = 0; t < nt; t++) {
-			double m[4][4];
-			sc.objs[i].xf.matrix(tlo + t, m);
-			pack_xf(m, row + (size_t)t * XF_STRIDE);
-		}
-	}
-	std::vector<float> lp((size_t)sc.lights.size() * nt * 4);
-	for(size_t i = 0; i < sc.lights.size(); i++) {
-		for(int t = 0; t < nt; t++) {
-			Vec3 p = sc.lights[i].xf.position(tlo + t);
-			float *d = &lp[((size_t)i * nt + t) * 4];
-			d[0] = (float)p.x; d[1] = (float)p.y; d[2] = (float)p.z; d[3] = 0.0f;
-		}
+	/* object transforms and light positions for every time the frame can
+	 * touch, evaluated from the keyframe tracks on the device */
+	size_t nobj = sc.objs.size(), nlt = sc.lights.size();
+	CK(xf.ensure(nobj * nt * XF_STRIDE * sizeof(float) + 16), "transform table");
+	CK(light_pos.ensure(nlt * nt * 4 * sizeof(float) + 16), "light positions");
+	size_t nthr = (nobj + nlt) * (size_t)nt;
+	if(nthr) {
+		LAUNCH(*this, "xforms", s, k_xforms<<<(unsigned)((nthr + 127) / 128), 128, 0, s>>>(anims.as<DevAnim>(), key_t.as<int>(),
+				key_v.as<double>(), (int)nobj, (int)nlt, tlo, nt, xf.as<float>(), light_pos.as<float>()));
+		CK(cudaGetLastError(), "transform table");
 	}
 	std::vector<float> cm((size_t)nt * 12);
 	for(int t = 0; t < nt; t++) {
@@ -1571,10 +1616,8 @@ int Renderer::build_frame(long bt0, long bt1, cudaStream_t s)
 	CK(tnodes.upload(tn, s), "upload object hierarchy");
 	CK(ohome.upload(ohome_h, s), "upload object home nodes");
 	has_tlas = !tn.empty();
-	CK(xf.upload(xfs, s), "upload transforms");
-	CK(light_pos.upload(lp, s), "upload light positions");
 	CK(cam_m.upload(cm, s), "upload camera");
-	h2d += (int64_t)(nodes.size() * sizeof(DevNode) + slots.size() * 4 + xfs.size() * 4 + lp.size() * 4 + cm.size() * 4);
+	h2d += (int64_t)(nodes.size() * sizeof(DevNode) + slots.size() * 4 + cm.size() * 4);
 	CK(cudaStreamSynchronize(s), "build frame");
 	built = true;
 	photons_ready = false;
@@ -2124,8 +2167,12 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 						acc.as<float4>(), ctr.as<DevCounters>()));
 				CK(fbl.ensure(((size_t)so.sq_cap + 1) * sizeof(int)), "fallback list");
 				CK(cudaMemsetAsync(fbl.p, 0, sizeof(int), s), "reset fallback list");
-				LAUNCH(*this, "shadow", s, k_shadow<true><<<grid_for(so.sq_cap, 128), 128, 0, s>>>(S, sq.as<ShadowReq>(), cnt + 5,
-						acc.as<float4>(), ctr.as<DevCounters>(), fbl.as<int>()));
+				if(tune.shadow_order)
+					LAUNCH(*this, "shadow", s, k_shadow<true, false><<<grid_for(so.sq_cap, 128), 128, 0, s>>>(S, sq.as<ShadowReq>(),
+							cnt + 5, acc.as<float4>(), ctr.as<DevCounters>(), fbl.as<int>()));
+				else
+					LAUNCH(*this, "shadow", s, k_shadow<true><<<grid_for(so.sq_cap, 128), 128, 0, s>>>(S, sq.as<ShadowReq>(), cnt + 5,
+							acc.as<float4>(), ctr.as<DevCounters>(), fbl.as<int>()));
 				LAUNCH(*this, "octree_retrace", s, k_shadow<false><<<152, 128, 0, s>>>(S, sq.as<ShadowReq>(), cnt + 5,
 						acc.as<float4>(), ctr.as<DevCounters>(), fbl.as<int>()));
 				LAUNCH(*this, "gather", s, k_gather<<<grid_for(so.gq_cap, GATHER_WARPS), GATHER_WARPS * 32, 0, s>>>(S,
@@ -2171,8 +2218,12 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 					ctr.as<DevCounters>()));
 			CK(fbl.ensure(((size_t)n_rays * shadow_per_ray + 1) * sizeof(int)), "fallback list");
 			CK(cudaMemsetAsync(fbl.p, 0, sizeof(int), s), "reset fallback list");
-			LAUNCH(*this, "shadow", s, k_shadow<true><<<grid_for(n_rays * 2, 128), 128, 0, s>>>(S, sq.as<ShadowReq>(), cnt + 5,
-					acc.as<float4>(), ctr.as<DevCounters>(), fbl.as<int>()));
+			if(tune.shadow_order)
+				LAUNCH(*this, "shadow", s, k_shadow<true, false><<<grid_for(n_rays * 2, 128), 128, 0, s>>>(S, sq.as<ShadowReq>(),
+						cnt + 5, acc.as<float4>(), ctr.as<DevCounters>(), fbl.as<int>()));
+			else
+				LAUNCH(*this, "shadow", s, k_shadow<true><<<grid_for(n_rays * 2, 128), 128, 0, s>>>(S, sq.as<ShadowReq>(), cnt + 5,
+						acc.as<float4>(), ctr.as<DevCounters>(), fbl.as<int>()));
 			LAUNCH(*this, "octree_retrace", s, k_shadow<false><<<152, 128, 0, s>>>(S, sq.as<ShadowReq>(), cnt + 5, acc.as<float4>(),
 					ctr.as<DevCounters>(), fbl.as<int>()));
 			if(deferring)
@@ -2568,6 +2619,7 @@ static int check_tuning(const sray_tuning *t)
 	if(t->render_tail < 0 || t->render_tail > (1 << 26)) { g_err = "render_tail must be 0..2^26"; return SRAY_EINVAL; }
 	if(t->pool_blocks_per_sm < 1 || t->pool_blocks_per_sm > 16) { g_err = "pool_blocks_per_sm must be 1..16"; return SRAY_EINVAL; }
 	if(t->photon_tail < 0 || t->photon_tail > (1 << 26)) { g_err = "photon_tail must be 0..2^26"; return SRAY_EINVAL; }
+	if(t->shadow_order != 0 && t->shadow_order != 1) { g_err = "shadow_order must be 0 or 1"; return SRAY_EINVAL; }
 	return 0;
 }
 
@@ -2603,16 +2655,17 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 	static const int tails[] = {0, 2048, 8192, 32768, 131072};
 	static const int pools[] = {2, 4, 8, 16};
 	static const int ptails[] = {16384, 65536, 262144, 1048576};
+	static const int orders[] = {0, 1};
 	struct Knob { int sray_tuning::*field; const int *vals; int n; };
 	const Knob knobs[] = {{&sray_tuning::render_tail, tails, 5}, {&sray_tuning::pool_blocks_per_sm, pools, 4},
-		{&sray_tuning::photon_tail, ptails, 4}};
+		{&sray_tuning::photon_tail, ptails, 4}, {&sray_tuning::shadow_order, orders, 2}};
 	std::vector<sray_tune_trial> done;
 	cudaEvent_t e0, e1;
 	if(cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) { g_err = "autotune events"; return SRAY_ECUDA; }
 	auto trial = [&](const sray_tuning &t, float *ms) -> int {
 		for(const sray_tune_trial &d : done) {
 			if(d.tuning.render_tail == t.render_tail && d.tuning.pool_blocks_per_sm == t.pool_blocks_per_sm &&
-					d.tuning.photon_tail == t.photon_tail) {
+					d.tuning.photon_tail == t.photon_tail && d.tuning.shadow_order == t.shadow_order) {
 				*ms = d.ms_per_frame;
 				return 0;
 			}
@@ -3007,6 +3060,7 @@ void sray_gpu_shutdown(void)
 	R.djobs.release();
 	R.dmaps.release();
 	DevBuf *bufs[] = {&R.mnodes, &R.mtris, &R.mprim, &R.tri_pos, &R.tri_attr, &R.objs, &R.mats, &R.texs, &R.texels, &R.lights,
+		&R.anims, &R.key_t, &R.key_v,
 		&R.snodes, &R.sslots,
 		&R.xf, &R.light_pos, &R.cam_m, &R.projbits, &R.coverage, &R.qbuf[0], &R.qbuf[1], &R.hits, &R.gq, &R.sq, &R.acc, &R.hist, &R.sums,
 		&R.active[0], &R.active[1], &R.spp, &R.fbdev, &R.ctr, &R.counts, &R.bnodes, &R.btris, &R.bprim, &R.bhome,

@@ -108,6 +108,7 @@ struct Renderer {
 
 	/* scene tables (per load) */
 	DevBuf mnodes, mtris, mprim, tri_pos, tri_attr, objs, mats, texs, texels, lights, bnodes, btris, bprim, bhome;
+	DevBuf anims, key_t, key_v;   /* keyframe tracks of the objects, then the lights */
 	/* frame tables (per build) */
 	DevBuf snodes, sslots, xf, light_pos, cam_m, projbits, coverage, tnodes, ohome;
 	bool built = false;
@@ -131,7 +132,7 @@ struct Renderer {
 	cudaStream_t ps = nullptr;
 	cudaEvent_t ps_done = nullptr;
 	sray_stats stats;
-	sray_tuning tune = {32768, 4, 65536, {0, 0, 0, 0, 0}};
+	sray_tuning tune = {32768, 4, 65536, 0, {0, 0, 0, 0}};
 	int nsm = 0;                  /* multiprocessors of the device */
 
 	/* radiance cache: queries (inputs, weight + slot), training and

@@ -306,22 +306,26 @@ struct Doc {
 /* ------------------------------------------------------------------ */
 /* keyframe tracks (src/anim.inl:70-263)                                */
 /* ------------------------------------------------------------------ */
-template <class T> static int nearest_key(const Track<T> &tr, int s, int e, int time)
+static_assert(sizeof(Vec3) == 3 * sizeof(double) && sizeof(Quat) == 4 * sizeof(double), "track values are packed doubles");
+
+/* a track as the flat view the shared evaluator reads */
+template <class T> static KeyView key_view(const Track<T> &tr)
 {
-	while(true) {
-		if(s == e) return s;
-		if(e - s == 1) return abs(time - tr.time[s]) < abs(tr.time[e] - time) ? s : e;
-		int mid = (s + e) / 2;
-		if(time < tr.time[mid]) e = mid;
-		else if(time > tr.time[mid]) s = mid + 1;
-		else return mid;
-	}
+	KeyView k;
+	k.time = tr.time.data();
+	k.val = reinterpret_cast<const double *>(tr.val.data());
+	k.def = reinterpret_cast<const double *>(&tr.def);
+	k.n = (int)tr.time.size();
+	k.dim = (int)(sizeof(T) / sizeof(double));
+	k.interp = tr.interp;
+	k.extrap = tr.extrap;
+	return k;
 }
 
 template <class T> static void set_key(Track<T> &tr, int time, const T &v)
 {
 	if(!tr.time.empty()) {
-		int n = nearest_key(tr, 0, (int)tr.time.size() - 1, time);
+		int n = key_nearest(tr.time.data(), 0, (int)tr.time.size() - 1, time);
 		if(tr.time[n] == time) { tr.val[n] = v; return; }
 	}
 	size_t pos = std::upper_bound(tr.time.begin(), tr.time.end(), time) - tr.time.begin();
@@ -329,119 +333,17 @@ template <class T> static void set_key(Track<T> &tr, int time, const T &v)
 	tr.val.insert(tr.val.begin() + pos, v);
 }
 
-static Vec3 mix(const Vec3 &a, const Vec3 &b, double t)
+static Vec3 eval_vec(const Track<Vec3> &tr, int t)
 {
-	return Vec3(a.x + (b.x - a.x) * t, a.y + (b.y - a.y) * t, a.z + (b.z - a.z) * t);
-}
-static Quat mix(const Quat &a, const Quat &b, double t)
-{
-	Quat r = {a.s + (b.s - a.s) * t, a.x + (b.x - a.x) * t, a.y + (b.y - a.y) * t, a.z + (b.z - a.z) * t};
-	return r;
-}
-static Vec3 spline(const Vec3 &v0, const Vec3 &v1, const Vec3 &v2, const Vec3 &v3, double t)
-{
-	double t2 = t * t, t3 = t2 * t;
-	Vec3 r;
-	for(int i = 0; i < 3; i++) {
-		double a = v0[i], b = v1[i], c = v2[i], d = v3[i];
-		double v = (b * 2.0 + (c - a) * t + (a * 2.0 - b * 5.0 + c * 4.0 - d) * t2 + (b * 3.0 - a - c * 3.0 + d) * t3) * 0.5;
-		if(i == 0) r.x = v; else if(i == 1) r.y = v; else r.z = v;
-	}
-	return r;
-}
-static Quat spline(const Quat &, const Quat &a, const Quat &b, const Quat &, double t)
-{
-	/* catmull_rom_spline on quaternions is a slerp of the middle keys (src/anim.inl:268-273) */
-	double d = a.s * b.s + a.x * b.x + a.y * b.y + a.z * b.z;
-	Quat bb = b;
-	if(d < 0.0) { d = -d; bb.s = -bb.s; bb.x = -bb.x; bb.y = -bb.y; bb.z = -bb.z; }
-	double wa, wb;
-	if(d > 0.9999) { wa = 1.0 - t; wb = t; }
-	else {
-		double ang = acos(d), sn = sin(ang);
-		wa = sin((1.0 - t) * ang) / sn;
-		wb = sin(t * ang) / sn;
-	}
-	Quat r = {a.s * wa + bb.s * wb, a.x * wa + bb.x * wb, a.y * wa + bb.y * wb, a.z * wa + bb.z * wb};
-	return r;
-}
-
-template <class T> static T eval(const Track<T> &tr, int time)
-{
-	size_t n = tr.time.size();
-	if(!n) return tr.def;
-	if(n > 1) {
-		int first = tr.time[0], last = tr.time[n - 1];
-		if(first != last && (time < first || time > last) && tr.extrap == EXTRAP_REPEAT) {
-			while(time < first) time += last - first;
-			time = (time - first) % (last - first) + first;
-		}
-	}
-	int k = nearest_key(tr, 0, (int)n - 1, time);
-	int s = k, e = -1;
-	if(time < tr.time[k] && tr.time[k] != tr.time[0]) { s = k - 1; e = k; }
-	else if(time > tr.time[k] && tr.time[k] != tr.time[n - 1]) { s = k; e = k + 1; }
-	if(e < 0 || tr.interp == INTERP_STEP) return tr.val[s];
-	double t = (double)(time - tr.time[s]) / (double)(tr.time[e] - tr.time[s]);
-	if(tr.interp == INTERP_LINEAR) return mix(tr.val[s], tr.val[e], t);
-	if(tr.interp == INTERP_CUBIC) {
-		const T &v0 = tr.val[s > 0 ? s - 1 : s];
-		const T &v3 = tr.val[e < (int)n - 1 ? e + 1 : e];
-		return spline(v0, tr.val[s], tr.val[e], v3, t);
-	}
-	return tr.val[s];
+	double o[3];
+	key_eval(key_view(tr), t, o);
+	return Vec3(o[0], o[1], o[2]);
 }
 
 /* ------------------------------------------------------------------ */
 /* 4x4 matrices (row-major, column vectors)                             */
 /* ------------------------------------------------------------------ */
-static void m_ident(double m[4][4]) { memset(m, 0, 16 * sizeof(double)); m[0][0] = m[1][1] = m[2][2] = m[3][3] = 1.0; }
-static void m_mul(double o[4][4], const double a[4][4], const double b[4][4])
-{
-	double r[4][4];
-	for(int i = 0; i < 4; i++)
-		for(int j = 0; j < 4; j++)
-			r[i][j] = a[i][0] * b[0][j] + a[i][1] * b[1][j] + a[i][2] * b[2][j] + a[i][3] * b[3][j];
-	memcpy(o, r, sizeof r);
-}
-static void m_quat(double m[4][4], const Quat &q)
-{
-	m_ident(m);
-	double s = q.s, x = q.x, y = q.y, z = q.z;
-	m[0][0] = 1.0 - 2.0 * y * y - 2.0 * z * z;
-	m[0][1] = 2.0 * x * y - 2.0 * s * z;
-	m[0][2] = 2.0 * z * x + 2.0 * s * y;
-	m[1][0] = 2.0 * x * y + 2.0 * s * z;
-	m[1][1] = 1.0 - 2.0 * x * x - 2.0 * z * z;
-	m[1][2] = 2.0 * y * z - 2.0 * s * x;
-	m[2][0] = 2.0 * z * x - 2.0 * s * y;
-	m[2][1] = 2.0 * y * z + 2.0 * s * x;
-	m[2][2] = 1.0 - 2.0 * x * x - 2.0 * y * y;
-}
-static double det3(double a, double b, double c, double d, double e, double f, double g, double h, double i)
-{
-	return a * (e * i - f * h) - b * (d * i - f * g) + c * (d * h - e * g);
-}
-void mat_inverse(double out[4][4], const double m[4][4])
-{
-	double cof[4][4];
-	for(int i = 0; i < 4; i++) {
-		for(int j = 0; j < 4; j++) {
-			double s[9];
-			int k = 0;
-			for(int r = 0; r < 4; r++) {
-				if(r == i) continue;
-				for(int c = 0; c < 4; c++) if(c != j) s[k++] = m[r][c];
-			}
-			double mn = det3(s[0], s[1], s[2], s[3], s[4], s[5], s[6], s[7], s[8]);
-			cof[i][j] = ((i + j) & 1) ? -mn : mn;
-		}
-	}
-	double det = m[0][0] * cof[0][0] + m[0][1] * cof[0][1] + m[0][2] * cof[0][2] + m[0][3] * cof[0][3];
-	for(int i = 0; i < 4; i++)
-		for(int j = 0; j < 4; j++)
-			out[i][j] = cof[j][i] / det;
-}
+void mat_inverse(double out[4][4], const double m[4][4]) { m4_inverse(out, m); }
 static Vec3 m_pt(const double m[4][4], const Vec3 &p)
 {
 	return Vec3(m[0][0] * p.x + m[0][1] * p.y + m[0][2] * p.z + m[0][3],
@@ -456,24 +358,17 @@ XForm::XForm()
 	Quat id = {1, 0, 0, 0};
 	rot.def = id;
 }
-Vec3 XForm::position(int t) const { return eval(pos, t); }
-Vec3 XForm::scaling(int t) const { return eval(scale, t); }
+Vec3 XForm::position(int t) const { return eval_vec(pos, t); }
+Vec3 XForm::scaling(int t) const { return eval_vec(scale, t); }
 
 /* XFormNode::get_xform_matrix: pivot * T * R * S * -pivot (src/anim.cc:391-419) */
 void XForm::matrix(int t, double m[4][4]) const
 {
-	Vec3 p = eval(pos, t), s = eval(scale, t);
-	Quat q = eval(rot, t);
-	double pm[4][4], npm[4][4], tm[4][4], rm[4][4], sm[4][4], a[4][4];
-	m_ident(pm); pm[0][3] = pivot.x; pm[1][3] = pivot.y; pm[2][3] = pivot.z;
-	m_ident(npm); npm[0][3] = -pivot.x; npm[1][3] = -pivot.y; npm[2][3] = -pivot.z;
-	m_ident(tm); tm[0][3] = p.x; tm[1][3] = p.y; tm[2][3] = p.z;
-	m_quat(rm, q);
-	m_ident(sm); sm[0][0] = s.x; sm[1][1] = s.y; sm[2][2] = s.z;
-	m_mul(a, pm, tm);
-	m_mul(a, a, rm);
-	m_mul(a, a, sm);
-	m_mul(m, a, npm);
+	double p[3], q[4], s[3], pv[3] = {pivot.x, pivot.y, pivot.z};
+	key_eval(key_view(pos), t, p);
+	key_eval(key_view(rot), t, q);
+	key_eval(key_view(scale), t, s);
+	node_matrix(p, q, s, pv, m);
 }
 
 static double v_len(const Vec3 &v) { return sqrt(v.x * v.x + v.y * v.y + v.z * v.z); }
@@ -497,14 +392,14 @@ void Camera::matrix(int t, double m[4][4]) const
 	up = v_cross(dir, right);
 	double roll = txf.scaling(t).x;
 	double half = roll * 0.5, sn = sin(half);
-	Quat q = {cos(half), dir.x * sn, dir.y * sn, dir.z * sn};
+	double q[4] = {cos(half), dir.x * sn, dir.y * sn, dir.z * sn};
 	double rm[4][4];
-	m_quat(rm, q);
+	m4_quat(rm, q);
 	Vec3 u(rm[0][0] * up.x + rm[0][1] * up.y + rm[0][2] * up.z, rm[1][0] * up.x + rm[1][1] * up.y + rm[1][2] * up.z,
 			rm[2][0] * up.x + rm[2][1] * up.y + rm[2][2] * up.z);
 	Vec3 r(rm[0][0] * right.x + rm[0][1] * right.y + rm[0][2] * right.z, rm[1][0] * right.x + rm[1][1] * right.y + rm[1][2] * right.z,
 			rm[2][0] * right.x + rm[2][1] * right.y + rm[2][2] * right.z);
-	m_ident(m);
+	m4_ident(m);
 	m[0][0] = r.x; m[0][1] = u.x; m[0][2] = dir.x; m[0][3] = p.x;
 	m[1][0] = r.y; m[1][1] = u.y; m[1][2] = dir.y; m[1][3] = p.y;
 	m[2][0] = r.z; m[2][1] = u.z; m[2][2] = dir.z; m[2][3] = p.z;

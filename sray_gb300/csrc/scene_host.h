@@ -15,11 +15,10 @@
 #include <vector>
 #include "sray_gpu.h"
 #include "sray_device.h"
+#include "anim_eval.h"
 
 namespace sray {
 
-enum { INTERP_STEP, INTERP_LINEAR, INTERP_CUBIC };
-enum { EXTRAP_CLAMP, EXTRAP_REPEAT, EXTRAP_PINGPONG };
 
 struct Vec3 {
 	double x, y, z;

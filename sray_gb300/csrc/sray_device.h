@@ -107,6 +107,18 @@ struct alignas(16) DevLight {
 
 enum { XF_STRIDE = 36 };
 
+/* the keyframe tracks of an object (or a light: position only) on the
+ * device: per track (position, rotation, scale) its first key time in the
+ * key-time table, its first value in the key-value table (3 doubles per
+ * position / scale key, 4 per rotation key), its key count, interpolation
+ * and extrapolation; the pivot; the defaults of empty tracks */
+struct alignas(16) DevAnim {
+	int toff[3], voff[3], n[3], interp[3], extrap[3];
+	int pad;
+	double pivot[3];
+	double def[10];   /* position 0-2, rotation 3-6, scale 7-9 */
+};
+
 /* photon record: 48 B */
 struct alignas(16) DevPhoton {
 	float p[4];     /* pos.xyz, power.r */

@@ -22,7 +22,7 @@ import os
 import numpy as np
 
 __all__ = ["icosphere", "value_noise_height", "small_scene", "production_scene", "feature_scene",
-           "textured_scene", "textures", "write_textures", "scene_opts", "write_scene", "CONFIGS"]
+           "textured_scene", "animated_scene", "textures", "write_textures", "scene_opts", "write_scene", "CONFIGS"]
 
 
 def _f(x):
@@ -506,6 +506,69 @@ def textured_scene():
     return "".join(out)
 
 
+def animated_scene():
+    """Keyframed objects in every interpolation and extrapolation mode of
+    the reference's tracks (src/anim.cc:68-121, src/anim.inl:189-273):
+    linear position keys repeated past the last key, cubic (Catmull-Rom)
+    position keys, step keys, rotations by axis-angle and by quaternion with
+    slerp (cubic) and component-wise lerp (linear), scale keys about a pivot,
+    a moving point light; rendered at a time between or past the keys."""
+    def xf(time, interp=None, extrap=None, **kw):
+        s = '<xform time="%d"' % time
+        if interp:
+            s += ' interpolate="%s"' % interp
+        if extrap:
+            s += ' extrapolate="%s"' % extrap
+        for k, v in kw.items():
+            s += ' %s="%s"' % (k, _vec(v))
+        return s + "/>\n"
+    out = ["<?xml version=\"1.0\"?>\n<scene>\n"]
+    out.append('<env ambient="0.1" bgcolor="0.2 0.2 0.25" ior="1.0"/>\n')
+    _material(out, "floor", (0.6, 0.6, 0.55), ks=0.2, shin=15.0)
+    _material(out, "a", (0.8, 0.3, 0.2), ks=0.5, shin=30.0)
+    _material(out, "b", (0.2, 0.7, 0.3), ks=0.5, shin=30.0)
+    _material(out, "c", (0.3, 0.4, 0.9), ks=0.4, shin=20.0)
+    _material(out, "d", (0.8, 0.8, 0.2), ks=0.6, shin=50.0)
+    _material(out, "glass", (0.05, 0.05, 0.05), ks=1.0, shin=80.0, refr=1.0, ior=1.5)
+    g = 8.0
+    gv = np.array([[-g, 0, -g], [g, 0, -g], [g, 0, g], [-g, 0, g]], dtype=np.float32)
+    gf = np.array([[0, 2, 1], [0, 3, 2]], dtype=np.int32)
+    _mesh_xml(out, "floor", "floor", gv, gf)
+    # linear, repeated: keys at 0, 500, 1000
+    out.append('<object type="sphere" name="rep">\n<matref name="a"/>\n%s%s%s<sphere rad="0.7"/>\n</object>\n'
+               % (xf(0, "linear", "repeat", pos=(-3.0, 0.7, 0.0)), xf(500, pos=(-1.0, 1.5, -1.0)),
+                  xf(1000, pos=(-3.0, 0.7, 0.0))))
+    # cubic positions: keys at 0, 300, 600, 900
+    out.append('<object type="sphere" name="cub">\n<matref name="glass"/>\n%s%s%s%s<sphere rad="0.6"/>\n</object>\n'
+               % (xf(0, "cubic", pos=(0.0, 0.6, 2.0)), xf(300, pos=(0.8, 1.4, 1.5)), xf(600, pos=(1.6, 0.9, 2.2)),
+                  xf(900, pos=(2.2, 0.6, 1.0))))
+    # step keys
+    out.append('<object type="cylinder" name="stp">\n<matref name="c"/>\n%s%s%s'
+               '<cylinder rad="0.4" start="0.0" end="1.8"/>\n</object>\n'
+               % (xf(0, "step", pos=(2.5, 0.0, -2.0)), xf(400, pos=(3.0, 0.0, -1.5)), xf(800, pos=(3.5, 0.0, -1.0))))
+    # axis-angle rotation keys (cubic: slerp), scale keys, a pivot
+    iv, ifc = icosphere(2)
+    rot_xml = (xf(0, "cubic", pos=(-1.0, 1.0, -3.0), axisrot=(0.0, 0.0, 1.0, 0.0), scale=(0.8, 0.8, 0.8),
+                  pivot=(0.3, 0.0, 0.0))
+               + xf(700, axisrot=(120.0, 0.3, 1.0, 0.2), scale=(1.0, 0.6, 1.2))
+               + xf(1400, axisrot=(250.0, 0.0, 1.0, 0.5), scale=(0.7, 0.9, 0.8)))
+    _mesh_xml(out, "spin", "d", iv, ifc, normals=iv, xform=rot_xml)
+    # quaternion keys, linear (component-wise lerp)
+    box = np.array([[-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1], [-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1]],
+                   dtype=np.float32) * 0.5
+    bf = np.array([[0, 2, 1], [0, 3, 2], [4, 5, 6], [4, 6, 7], [0, 1, 5], [0, 5, 4], [2, 3, 7], [2, 7, 6],
+                   [1, 2, 6], [1, 6, 5], [0, 4, 7], [0, 7, 3]], dtype=np.int32)
+    quat_xml = (xf(0, "linear", pos=(1.0, 0.6, -0.5), rot=(1.0, 0.0, 0.0, 0.0))
+                + xf(600, rot=(0.7, 0.2, 0.6, 0.3)) + xf(1200, rot=(0.3, 0.5, 0.1, 0.8)))
+    _mesh_xml(out, "tumble", "b", box, bf, xform=quat_xml)
+    out.append('<light type="point" color="1.0">\n%s%s</light>\n'
+               % (xf(0, pos=(0.0, 7.0, 2.0)), xf(1000, pos=(3.0, 6.0, 4.0))))
+    out.append('<camera type="target" fov="50.0">\n%s<target>\n%s</target>\n</camera>\n'
+               % (_xform(pos=(0.5, 5.0, 9.5)), _xform(pos=(0.0, 0.8, 0.0))))
+    out.append("</scene>\n")
+    return "".join(out)
+
+
 # option sets (sray_opts fields) of the benchmark configurations
 CONFIGS = {
     "small": dict(width=512, height=512, min_samples=1, max_samples=1, iter=5,
@@ -541,7 +604,7 @@ def scene_opts(name, **over):
 def write_scene(name, cache_dir=None, **kw):
     """Generate (or reuse from cache_dir) the XML of scene `name`; returns the path."""
     gen = {"small": small_scene, "learned": small_scene, "production": production_scene, "feature": feature_scene,
-           "stress": stress_scene, "textured": textured_scene}[name]
+           "stress": stress_scene, "textured": textured_scene, "animated": animated_scene}[name]
     key = hashlib.sha1(repr((name, sorted(kw.items()), 3)).encode()).hexdigest()[:12]
     cache_dir = cache_dir or os.environ.get("SRAY_SCENE_CACHE", "/tmp/sray_scenes")
     os.makedirs(cache_dir, exist_ok=True)

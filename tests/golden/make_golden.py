@@ -2,9 +2,9 @@
 
 Runs the reference's own rendering code (compiled from its unmodified
 sources by oracle/build_ref.py, with the project's libvmath/kdtree/imago
-stand-ins and a Philox stream per photon and per pixel sample) on four
+stand-ins and a Philox stream per photon and per pixel sample) on five
 seeded scenes (the textured one reads the images of scenegen.textures()
-through SRAY_DATA_PATH) and stores, per case: the scene XML, the options, the
+through SRAY_DATA_PATH; the animated one is rendered at 1350 ms) and stores, per case: the scene XML, the options, the
 primary-hit ids and t, the stored caustic and global photons, and the
 rendered image with its per-pixel sample counts.
 
@@ -46,16 +46,21 @@ CASES = {
                                   "-shadowrays", "2", "-diffuserays", "2", "-gatherdisc", "0.02"],
                  dict(width=64, height=48, min_samples=1, max_samples=2, max_var=0.02, caust_photons=20000,
                       gi_photons=30000, iter=6, shadow_samples=2, diffuse_samples=2, gather_dist=0.02)),
+    # keyframes in every interpolation / extrapolation mode, rendered at 1350 ms
+    "animated": ("animated", {}, ["-s", "64x48", "-c", "20000", "-i", "5"],
+                 dict(width=64, height=48, caust_photons=20000, iter=5), 1350),
 }
 
 
 def run_case(harness, name, spec):
     from sray_gb300 import scenegen
-    gen, kw, cli, oopts = spec
+    gen, kw, cli, oopts = spec[:4]
+    msec = spec[4] if len(spec) > 4 else 0
     path = scenegen.write_scene(gen, **kw)
     xml = open(path, "rb").read()
-    # textures are found through the first directory of SRAY_DATA_PATH
-    env = dict(os.environ, SRAY_DATA_PATH=os.path.dirname(path))
+    # textures are found through the first directory of SRAY_DATA_PATH; the
+    # frame time is SRAY_REF_MSEC
+    env = dict(os.environ, SRAY_DATA_PATH=os.path.dirname(path), SRAY_REF_MSEC=str(msec))
     with tempfile.TemporaryDirectory() as td:
         prefix = os.path.join(td, name)
         h = oopts["height"]
@@ -67,7 +72,7 @@ def run_case(harness, name, spec):
         img = np.fromfile(prefix + ".img", dtype=np.float32).reshape(h, oopts["width"], 5)
     out = os.path.join(HERE, name + ".npz")
     np.savez_compressed(out, obj=hits["o"], prim=hits["p"], t=hits["t"], caust=caust[:, :13], gi=gi[:, :13],
-                        img=img[..., :4], spp=img[..., 4].astype(np.int32),
+                        img=img[..., :4], spp=img[..., 4].astype(np.int32), msec=np.int64(msec),
                         opts=np.frombuffer(json.dumps(oopts).encode(), dtype=np.uint8),
                         cli=np.frombuffer(json.dumps(cli).encode(), dtype=np.uint8))
     with gzip.open(os.path.join(HERE, name + ".xml.gz"), "wb") as f:

@@ -87,6 +87,15 @@ def test_image_small_scene(small_pair):
     assert _compare(img_g, img_o, "small 256^2 knn") <= 1e-3
 
 
+def test_shadow_order_keeps_the_image(small_pair):
+    # light samples' any-hit traversal in node order instead of nearest first
+    g, o = small_pair(width=192, height=192)
+    g.set_tuning(shadow_order=1)
+    img_g = g.render(0)
+    img_o = o.render(0)
+    assert _compare(img_g, img_o, "small 192^2 shadow rays in node order") <= 1e-3
+
+
 def test_image_reference_range_gather(small_pair):
     # the reference's own gather: fixed radius (gather_dist of the scene diagonal), no k
     g, o = small_pair(width=192, height=192, caust_k=0, gather_dist=0.004)
@@ -218,6 +227,56 @@ def test_textured_primary_hits_match_reference(gpu_lib, monkeypatch, tmp_path):
     gobj, gprim = obj.cpu().numpy(), prim.cpu().numpy()
     mism = (gobj != d["obj"]) | (gprim != d["prim"])
     print("textured primary hits: %d mismatches of %d (ties %d)" % (mism.sum(), n, int((tie.cpu().numpy() > 0).sum())))
+    assert mism.mean() <= 1e-3
+
+
+def _hits(g, n, msec):
+    obj = torch.empty(n, dtype=torch.int32, device="cuda")
+    prim = torch.empty(n, dtype=torch.int32, device="cuda")
+    t = torch.empty(n, dtype=torch.float32, device="cuda")
+    tie = torch.empty(n, dtype=torch.uint8, device="cuda")
+    g.primary_hits(obj, prim, t, tie, msec=msec)
+    torch.cuda.synchronize()
+    return obj.cpu().numpy(), prim.cpu().numpy(), t.cpu().numpy(), tie.cpu().numpy()
+
+
+@pytest.mark.parametrize("msec", [0, 350, 1350])
+def test_animated_scene(gpu_lib, oracle_lib, msec):
+    # transforms evaluated on the device from the keyframe tracks: linear
+    # keys repeated past the last one, Catmull-Rom positions, step keys,
+    # slerped and lerped rotations, scale about a pivot, a moving light
+    opts = dict(width=96, height=72, caust_photons=20000, iter=5)
+    path = scenegen.write_scene("animated")
+    g = gpu_lib.GpuRenderer(**opts)
+    g.load(path)
+    o = oracle_lib.Oracle(fp64=False, rng_mode=1, **opts)
+    o.load(path)
+    n = opts["width"] * opts["height"]
+    gobj, gprim, gt, gtie = _hits(g, n, msec)
+    oobj, oprim, ot, otie = o.primary_hits(msec)
+    mism = ((gobj != oobj) | (gprim != oprim)) & ~((gtie > 0) | (otie > 0))
+    print("animated %d ms: %d hits, %d unflagged mismatches" % (msec, int((oobj >= 0).sum()), mism.sum()))
+    assert mism.sum() == 0
+    img_g = g.render(msec)
+    img_o = o.render(msec)
+    assert _compare(img_g, img_o, "animated 96x72 at %d ms" % msec) <= 1e-3
+
+
+def test_animated_primary_hits_match_reference(gpu_lib):
+    # primary hits at 1350 ms against the reference's own (golden fixture)
+    import gzip
+    import json
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    d = np.load(os.path.join(here, "animated.npz"))
+    opts = json.loads(bytes(d["opts"]).decode())
+    with gzip.open(os.path.join(here, "animated.xml.gz")) as f:
+        xml = f.read()
+    g = gpu_lib.GpuRenderer(**opts)
+    g.load_xml(xml)
+    n = opts["width"] * opts["height"]
+    gobj, gprim, gt, gtie = _hits(g, n, int(d["msec"]))
+    mism = (gobj != d["obj"]) | (gprim != d["prim"])
+    print("animated primary hits vs reference: %d mismatches of %d" % (mism.sum(), n))
     assert mism.mean() <= 1e-3
 
 

@@ -1,7 +1,8 @@
 """The CPU oracle against golden fixtures produced by the reference's own
 code (tests/golden/make_golden.py): primary-hit ids and t, stored photons,
-images and per-pixel sample counts of four seeded scenes (one of them
-textured).
+images and per-pixel sample counts of five seeded scenes (one of them
+textured, one keyframed in every interpolation and extrapolation mode and
+rendered at 1350 ms).
 
 On the machine type the fixtures were generated on the FP64 oracle must be
 bit-exact.  Elsewhere the C library's transcendental functions may differ in
@@ -17,7 +18,7 @@ import numpy as np
 import pytest
 
 HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["small_range", "feature", "terrain", "textured"]
+CASES = ["small_range", "feature", "terrain", "textured", "animated"]
 
 
 def fixture_machine():
@@ -41,11 +42,13 @@ def test_oracle_matches_reference(oracle_lib, case, monkeypatch, tmp_path):
     opts = json.loads(bytes(d["opts"]).decode())
     with gzip.open(os.path.join(HERE, case + ".xml.gz")) as f:
         xml = f.read()
+    msec = int(d["msec"]) if "msec" in d.files else 0
     o = oracle_lib.Oracle(fp64=True, rng_mode=0, **opts)
     o.load_xml(xml)
-    obj, prim, t, _ = o.primary_hits()
+    obj, prim, t, _ = o.primary_hits(msec)
+    o.prepare(msec)
     caust, gi = o.photons(0)[:, :13], o.photons(1)[:, :13]
-    img, spp = o.render(0, want_spp=True)
+    img, spp = o.render(msec, want_spp=True)
     exact = platform.machine() == fixture_machine()
     print("%s: %d hits, %d/%d photons, exact=%s" % (case, int((obj >= 0).sum()), len(caust), len(gi), exact))
     if exact:
