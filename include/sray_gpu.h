@@ -293,7 +293,11 @@ typedef struct sray_tuning {
 	                             persistent launch (65536) */
 	int shadow_order;         /* any-hit traversal of light samples: 0 visits a node's hit
 	                             children nearest first, 1 in the node's order (0) */
-	int reserved[4];
+	int stream_priority;      /* which of the two concurrent streams gets the device's
+	                             greatest priority: 0 neither, 1 the photon stream, 2 the
+	                             render work (on an internal stream ordered after and
+	                             before the caller's) (0) */
+	int reserved[3];
 } sray_tuning;
 
 typedef struct sray_tune_trial {

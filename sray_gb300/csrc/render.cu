@@ -2319,9 +2319,30 @@ int launch_trace(Renderer &R, const DScene &D, const RayQueue &q, int n, const c
 
 int Renderer::photon_stream()
 {
-	if(ps) return 0;
-	CK(cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking), "photon stream");
-	CK(cudaEventCreateWithFlags(&ps_done, cudaEventDisableTiming), "photon event");
+	int want = tune.stream_priority == 1 ? 1 : 0;
+	if(ps && ps_priority == want) return 0;
+	if(ps) {
+		/* no photon work is in flight between frames */
+		CK(cudaStreamSynchronize(ps), "photon stream");
+		CK(cudaStreamDestroy(ps), "photon stream");
+		ps = nullptr;
+	}
+	int least = 0, greatest = 0;
+	CK(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
+	CK(cudaStreamCreateWithPriority(&ps, cudaStreamNonBlocking, want ? greatest : least), "photon stream");
+	ps_priority = want;
+	if(!ps_done) CK(cudaEventCreateWithFlags(&ps_done, cudaEventDisableTiming), "photon event");
+	return 0;
+}
+
+int Renderer::priority_stream()
+{
+	if(hs) return 0;
+	int least = 0, greatest = 0;
+	CK(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
+	CK(cudaStreamCreateWithPriority(&hs, cudaStreamNonBlocking, greatest), "priority stream");
+	CK(cudaEventCreateWithFlags(&hs_fork, cudaEventDisableTiming), "priority stream event");
+	CK(cudaEventCreateWithFlags(&hs_join, cudaEventDisableTiming), "priority stream event");
 	return 0;
 }
 
@@ -2597,8 +2618,21 @@ static int render_frame(Renderer &R, long msec, float *fb, int fb_is_device, cud
 	frame_interval(R, msec, &t0, &t1);
 	long long l0 = R.launch_count;
 	R.h2d = R.d2h = 0;
-	int r = R.build_frame(t0, t1, s);
-	if(!r) r = R.render_pixels(msec, fb, fb_is_device, s, true);
+	/* stream_priority 2: the frame runs on an internal stream of the
+	 * greatest priority, after the caller's stream's earlier work and
+	 * before its later work */
+	cudaStream_t rs = s;
+	int r = 0;
+	if(R.tune.stream_priority == 2) {
+		r = R.priority_stream();
+		if(!r && (cudaEventRecord(R.hs_fork, s) != cudaSuccess || cudaStreamWaitEvent(R.hs, R.hs_fork, 0) != cudaSuccess))
+			r = R.fail(SRAY_ECUDA, "priority stream fork");
+		rs = R.hs;
+	}
+	if(!r) r = R.build_frame(t0, t1, rs);
+	if(!r) r = R.render_pixels(msec, fb, fb_is_device, rs, true);
+	if(rs != s && (cudaEventRecord(R.hs_join, rs) != cudaSuccess || cudaStreamWaitEvent(s, R.hs_join, 0) != cudaSuccess) && !r)
+		r = R.fail(SRAY_ECUDA, "priority stream join");
 	if(r) g_err = R.err;
 	else R.stats.kernel_launches = (int)(R.launch_count - l0);
 	return r;
@@ -2620,6 +2654,7 @@ static int check_tuning(const sray_tuning *t)
 	if(t->pool_blocks_per_sm < 1 || t->pool_blocks_per_sm > 16) { g_err = "pool_blocks_per_sm must be 1..16"; return SRAY_EINVAL; }
 	if(t->photon_tail < 0 || t->photon_tail > (1 << 26)) { g_err = "photon_tail must be 0..2^26"; return SRAY_EINVAL; }
 	if(t->shadow_order != 0 && t->shadow_order != 1) { g_err = "shadow_order must be 0 or 1"; return SRAY_EINVAL; }
+	if(t->stream_priority < 0 || t->stream_priority > 2) { g_err = "stream_priority must be 0, 1 or 2"; return SRAY_EINVAL; }
 	return 0;
 }
 
@@ -2655,17 +2690,18 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 	static const int tails[] = {0, 2048, 8192, 32768, 131072};
 	static const int pools[] = {2, 4, 8, 16};
 	static const int ptails[] = {16384, 65536, 262144, 1048576};
-	static const int orders[] = {0, 1};
+	static const int binary[] = {0, 1}, prios[] = {0, 1, 2};
 	struct Knob { int sray_tuning::*field; const int *vals; int n; };
 	const Knob knobs[] = {{&sray_tuning::render_tail, tails, 5}, {&sray_tuning::pool_blocks_per_sm, pools, 4},
-		{&sray_tuning::photon_tail, ptails, 4}, {&sray_tuning::shadow_order, orders, 2}};
+		{&sray_tuning::photon_tail, ptails, 4}, {&sray_tuning::shadow_order, binary, 2}, {&sray_tuning::stream_priority, prios, 3}};
 	std::vector<sray_tune_trial> done;
 	cudaEvent_t e0, e1;
 	if(cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) { g_err = "autotune events"; return SRAY_ECUDA; }
 	auto trial = [&](const sray_tuning &t, float *ms) -> int {
 		for(const sray_tune_trial &d : done) {
 			if(d.tuning.render_tail == t.render_tail && d.tuning.pool_blocks_per_sm == t.pool_blocks_per_sm &&
-					d.tuning.photon_tail == t.photon_tail && d.tuning.shadow_order == t.shadow_order) {
+					d.tuning.photon_tail == t.photon_tail && d.tuning.shadow_order == t.shadow_order &&
+					d.tuning.stream_priority == t.stream_priority) {
 				*ms = d.ms_per_frame;
 				return 0;
 			}
@@ -3076,6 +3112,12 @@ void sray_gpu_shutdown(void)
 	}
 	if(R.ps_done) cudaEventDestroy(R.ps_done);
 	if(R.ps) cudaStreamDestroy(R.ps);
+	if(R.hs) {
+		cudaStreamSynchronize(R.hs);
+		cudaStreamDestroy(R.hs);
+		cudaEventDestroy(R.hs_fork);
+		cudaEventDestroy(R.hs_join);
+	}
 	delete g_R;
 	g_R = nullptr;
 }

@@ -130,9 +130,13 @@ struct Renderer {
 	RayQueue pq[2];
 	int pqcap[2] = {0, 0};
 	cudaStream_t ps = nullptr;
+	int ps_priority = -1;      /* 1 when ps has the greatest priority */
+	cudaStream_t hs = nullptr; /* the frame's stream under stream_priority 2 */
+	cudaEvent_t hs_fork = nullptr, hs_join = nullptr;
+	int priority_stream();
 	cudaEvent_t ps_done = nullptr;
 	sray_stats stats;
-	sray_tuning tune = {32768, 4, 65536, 0, {0, 0, 0, 0}};
+	sray_tuning tune = {32768, 4, 65536, 0, 0, {0, 0, 0}};
 	int nsm = 0;                  /* multiprocessors of the device */
 
 	/* radiance cache: queries (inputs, weight + slot), training and

@@ -87,13 +87,20 @@ def test_image_small_scene(small_pair):
     assert _compare(img_g, img_o, "small 256^2 knn") <= 1e-3
 
 
-def test_shadow_order_keeps_the_image(small_pair):
-    # light samples' any-hit traversal in node order instead of nearest first
+@pytest.mark.parametrize("tuning", [dict(shadow_order=1), dict(stream_priority=1), dict(stream_priority=2)])
+def test_tuning_keeps_the_image(small_pair, tuning):
+    # light samples' any-hit traversal in node order instead of nearest
+    # first; the photon stream or the frame's own stream given priority
     g, o = small_pair(width=192, height=192)
-    g.set_tuning(shadow_order=1)
+    g.set_tuning(**tuning)
     img_g = g.render(0)
     img_o = o.render(0)
-    assert _compare(img_g, img_o, "small 192^2 shadow rays in node order") <= 1e-3
+    assert _compare(img_g, img_o, "small 192^2 %s" % tuning) <= 1e-3
+    fb = torch.empty((192, 192, 4), dtype=torch.float32, device="cuda")
+    stream = torch.cuda.Stream()
+    g.render(0, fb=fb, stream=stream)      # device framebuffer on a caller's stream
+    stream.synchronize()
+    assert _compare(fb.cpu().numpy(), img_o, "small 192^2 %s, device framebuffer" % tuning) <= 1e-3
 
 
 def test_image_reference_range_gather(small_pair):
