@@ -87,12 +87,21 @@ def test_image_small_scene(small_pair):
     assert _compare(img_g, img_o, "small 256^2 knn") <= 1e-3
 
 
-@pytest.mark.parametrize("tuning", [dict(shadow_order=1), dict(stream_priority=1), dict(stream_priority=2)])
+@pytest.mark.parametrize("tuning", [dict(shadow_order=1), dict(stream_priority=1), dict(stream_priority=2),
+                                    dict(trace_fetch=1), dict(trace_fetch=1, shadow_order=1)])
 def test_tuning_keeps_the_image(small_pair, tuning):
     # light samples' any-hit traversal in node order instead of nearest
-    # first; the photon stream or the frame's own stream given priority
+    # first; the photon stream or the frame's own stream given priority;
+    # traversals with a lane taking its next ray as soon as its own ends
     g, o = small_pair(width=192, height=192)
     g.set_tuning(**tuning)
+    n = 192 * 192
+    gobj, gprim, gt, gtie = _hits(g, n, 0)
+    oobj, oprim, ot, otie = o.primary_hits(0)
+    mism = ((gobj != oobj) | (gprim != oprim)) & ~((gtie > 0) | (otie > 0))
+    assert mism.sum() == 0
+    hit = (oobj >= 0) & (gobj == oobj) & (gprim == oprim)
+    assert np.array_equal(gt[hit], ot[hit].astype(np.float32))
     img_g = g.render(0)
     img_o = o.render(0)
     assert _compare(img_g, img_o, "small 192^2 %s" % tuning) <= 1e-3
