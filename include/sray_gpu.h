@@ -297,10 +297,7 @@ typedef struct sray_tuning {
 	                             greatest priority: 0 neither, 1 the photon stream, 2 the
 	                             render work (on an internal stream ordered after and
 	                             before the caller's) (0) */
-	int trace_fetch;          /* closest-hit and light-sample traversal: 0 a lane holds one
-	                             ray until its warp's rays all end, 1 a lane takes its next
-	                             ray as soon as its own ends (0) */
-	int reserved[2];
+	int reserved[3];
 } sray_tuning;
 
 typedef struct sray_tune_trial {

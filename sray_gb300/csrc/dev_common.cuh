@@ -440,28 +440,25 @@ __device__ __forceinline__ float4 load_split(const DevNode *nodes, int ni)
  * is listed in each of them, and a ray crossing those leaves would test it
  * again with the same result (a repeated test can neither improve the best
  * hit nor flag a tie that the first test did not).  Each thread keeps the
- * last triangle seen per slot of a 16-way direct-mapped table in shared
- * memory, cleared whenever the ray enters a mesh, and skips repeats.  The
- * traversal kernels run 128 threads per block. */
+ * last triangle seen per slot of a 16-way direct-mapped table, cleared
+ * whenever the ray enters a mesh, and skips repeats.  The table is the
+ * thread's own (local memory), not shared memory: the octree-only kernels
+ * run between the hierarchy kernels, which use no shared memory, and a
+ * kernel that needs shared memory waits for SMs to drain the other
+ * stream's blocks before it can start. */
 #define SRAY_TRACE_THREADS 128
 #define SRAY_TRI_MBOX 16
-
-__device__ __forceinline__ int *tri_mailbox()
-{
-	__shared__ int mb[SRAY_TRI_MBOX * SRAY_TRACE_THREADS];
-	return mb + threadIdx.x;
-}
 
 __device__ __forceinline__ void tri_mailbox_clear(int *mb)
 {
 	#pragma unroll
-	for(int k = 0; k < SRAY_TRI_MBOX; k++) mb[k * SRAY_TRACE_THREADS] = -1;
+	for(int k = 0; k < SRAY_TRI_MBOX; k++) mb[k] = -1;
 }
 
 /* true when `prim` was tested since the last clear; records it otherwise */
 __device__ __forceinline__ bool tri_mailbox_seen(int *mb, int prim)
 {
-	int *e = mb + (prim & (SRAY_TRI_MBOX - 1)) * SRAY_TRACE_THREADS;
+	int *e = mb + (prim & (SRAY_TRI_MBOX - 1));
 	if(*e == prim) return true;
 	*e = prim;
 	return false;
@@ -477,7 +474,7 @@ __device__ __forceinline__ void mesh_closest(const DScene &S, int root, int obj,
 	const DevNode &rn = S.mnodes[root];
 	if(!box_hit(rn.mn, rn.mx, r, te)) return;
 	int oct = octant(r);
-	int *mb = tri_mailbox();
+	int mb[SRAY_TRI_MBOX];
 	tri_mailbox_clear(mb);
 	st.node[sp] = root;
 	st.te[sp] = te;
@@ -529,12 +526,12 @@ __device__ __forceinline__ void object_closest(const DScene &S, int oi, int ti, 
 /* Object mailbox.  An object spanning several top-level leaves gives the
  * same closest hit each time it is tested, so it is tested once per ray.
  * Scenes of up to SRAY_OBJ_EXACT objects keep an exact per-ray set (one bit
- * per object in shared memory); larger scenes remember the last
- * SRAY_MAILBOX objects. */
+ * per object, in the thread's local memory as the triangle mailbox); larger
+ * scenes remember the last SRAY_MAILBOX objects. */
 #define SRAY_OBJ_EXACT 1024
 
 struct ObjMailbox {
-	unsigned *bits;
+	unsigned bits[SRAY_OBJ_EXACT / 32];
 	int ring[SRAY_MAILBOX];
 	int next;
 	bool exact;
@@ -542,13 +539,11 @@ struct ObjMailbox {
 
 __device__ __forceinline__ void obj_mailbox_init(const DScene &S, ObjMailbox &m)
 {
-	__shared__ unsigned bits[(SRAY_OBJ_EXACT / 32) * SRAY_TRACE_THREADS];
-	m.bits = bits + threadIdx.x;
 	m.exact = S.nobj <= SRAY_OBJ_EXACT;
 	m.next = 0;
 	if(m.exact) {
 		int words = (S.nobj + 31) >> 5;
-		for(int w = 0; w < words; w++) m.bits[w * SRAY_TRACE_THREADS] = 0u;
+		for(int w = 0; w < words; w++) m.bits[w] = 0u;
 	} else {
 		#pragma unroll
 		for(int k = 0; k < SRAY_MAILBOX; k++) m.ring[k] = -1;
@@ -558,7 +553,7 @@ __device__ __forceinline__ void obj_mailbox_init(const DScene &S, ObjMailbox &m)
 __device__ __forceinline__ bool mailbox_seen(ObjMailbox &m, int oi)
 {
 	if(m.exact) {
-		unsigned *w = m.bits + (oi >> 5) * SRAY_TRACE_THREADS;
+		unsigned *w = m.bits + (oi >> 5);
 		unsigned bit = 1u << (oi & 31);
 		unsigned v = *w;
 		if(v & bit) return true;
@@ -630,7 +625,7 @@ __device__ inline bool mesh_any(const DScene &S, int root, const RayT &r, TStack
 	const DevNode &rn = S.mnodes[root];
 	if(!box_hit(rn.mn, rn.mx, r, te)) return false;
 	int oct = octant(r);
-	int *mb = tri_mailbox();
+	int mb[SRAY_TRI_MBOX];
 	tri_mailbox_clear(mb);
 	st.node[sp++] = root;
 	while(sp > base) {
@@ -796,226 +791,6 @@ __device__ __forceinline__ RayT object_ray(const DScene &S, int o, int ti, V3 wo
 {
 	const float *inv = obj_xf(S, o, ti) + 12;
 	return make_ray(mul_pt(inv, wo), mul_dir(inv, wd));
-}
-
-/* One ray's two-level traversal (the same steps as trace_two_level below)
- * as resumable state, so that a kernel can advance it one step at a time
- * (trav_begin, trav_step until it stops, trav_finish) and give a lane a new
- * ray as soon as its own ends (k_trace_dyn, k_shadow_dyn). */
-struct Trav {
-	V3 wo, wd;
-	int ti;
-	RayT wr, r;
-	RayC wc, rc;
-	float best;
-	int bobj, bprim, bslot;
-	bool eq, inst;
-	int sp, inst_base, iobj, cur;
-	int res;          /* the result when the traversal ends early (TRAV_RESULT) */
-};   /* the node stack is kept apart, so that these stay in registers */
-enum { TRAV_RUN = 0, TRAV_DONE = 1, TRAV_RESULT = 2 };
-
-template <bool ANY>
-__device__ __forceinline__ int trav_begin(const DScene &S, V3 wo, V3 wd, int time, Trav &T)
-{
-	if(!S.has_scene) { T.res = ANY ? 0 : 1; return TRAV_RESULT; }
-	if(!S.tnodes) { T.res = ANY ? 2 : 0; return TRAV_RESULT; }
-	T.wo = wo;
-	T.wd = wd;
-	T.ti = time_index(S, time);
-	T.wr = make_ray(wo, wd);
-	const DevNode &sroot = S.snodes[S.sroot];
-	T.wc = make_rayc(T.wr, box_bound(sroot.mn, sroot.mx));
-	T.r = T.wr;
-	T.rc = T.wc;
-	T.best = ANY ? 1.0f : FLT_MAX;
-	T.bobj = T.bprim = T.bslot = -1;
-	T.eq = false;
-	T.inst = false;
-	T.sp = 0;
-	T.inst_base = 0;
-	T.iobj = -1;
-	T.cur = 0;   /* the object hierarchy's root */
-	return TRAV_RUN;
-}
-
-/* one step: pop the next entry if there is none in hand, then enter an
- * object, test a leaf's faces, or open a node.  TRAV_DONE when the
- * traversal is over (trav_finish decides), TRAV_RESULT when it ended early
- * with T.res. */
-template <bool COUNT, bool ANY, bool SORT>
-__device__ __forceinline__ int trav_step(const DScene &S, Trav &T, TStack &st, TraceCounters *tc, int *overflow)
-{
-	if(T.cur == BVH_NONE) {
-		bool found = false;
-		while(T.sp > 0) {
-			int k = T.sp - 1;
-			if(T.inst && k < T.inst_base) {   /* the instance's entries are done */
-				T.inst = false;
-				T.iobj = -1;
-				T.r = T.wr;
-				T.rc = T.wc;
-			}
-			T.sp = k;
-			if(ANY || st.te[k] <= T.best) {
-				T.cur = st.node[k];
-				found = true;
-				break;
-			}
-		}
-		if(!found) return TRAV_DONE;
-	}
-	if(!T.inst && T.cur < 0) {
-		/* enter object ~cur */
-		int o = ~T.cur;
-		T.cur = BVH_NONE;
-		const DevObj ob = S.objs[o];
-		RayT orr = object_ray(S, o, T.ti, T.wo, T.wd);
-		if(ob.type != 2) {
-			if(COUNT) tc->prims++;
-			float t;
-			bool hit = ob.type == 0 ? sphere_hit(orr, ob.rad, S.eps, t) : cylinder_hit(orr, ob.rad, ob.start, ob.end, S.eps, t);
-			if(hit && t <= T.best) {
-				if(ANY) {
-					T.bobj = o;
-					T.bprim = 0;
-					T.best = t;
-					return TRAV_DONE;
-				}
-				if(t < T.best) {
-					T.best = t;
-					T.bobj = o;
-					T.bprim = 0;
-					T.bslot = -1;
-					T.eq = false;
-				} else if(o != T.bobj || T.bprim != 0) {
-					T.eq = true;
-				}
-			}
-			return TRAV_RUN;
-		}
-		if(ob.mesh_root < 0) return TRAV_RUN;
-		if(ob.bvh_root < 0) { T.res = ANY ? 2 : 0; return TRAV_RESULT; }
-		/* the mesh octree's entry test: a mesh it would not enter gives
-		 * no candidates (nor one beating the best, when pruned) */
-		float te;
-		const DevNode &rn = S.mnodes[ob.mesh_root];
-		if(!box_hit(rn.mn, rn.mx, orr, te) || (!ANY && SRAY_PRUNE(te, T.best))) return TRAV_RUN;
-		T.r = orr;
-		T.rc = make_rayc(orr, box_bound(rn.mn, rn.mx));
-		T.inst = true;
-		T.inst_base = T.sp;
-		T.iobj = o;
-		T.cur = ob.bvh_root;
-		return TRAV_RUN;
-	}
-	if(T.inst && T.cur < 0) {
-		/* a leaf of the mesh hierarchy: its faces */
-		unsigned v = ~(unsigned)T.cur;
-		T.cur = BVH_NONE;
-		int start = (int)(v >> 4), cnt = (int)(v & 15u);
-		const float4 *tp = reinterpret_cast<const float4 *>(S.btris + start);
-		for(int k = 0; k < cnt; k++) {
-			float4 a = __ldg(tp + 3 * k), b = __ldg(tp + 3 * k + 1), c = __ldg(tp + 3 * k + 2);
-			if(COUNT) tc->prims++;
-			float t;
-			if(!tri_hit(a, b, c, T.r, S.eps, T.best, t)) continue;
-			int prim = __ldg(S.bprim + start + k);
-			if(ANY) {
-				T.bobj = T.iobj;
-				T.bprim = prim;
-				T.bslot = start + k;
-				T.best = t;
-				return TRAV_DONE;
-			}
-			if(t < T.best) {
-				T.best = t;
-				T.bobj = T.iobj;
-				T.bprim = prim;
-				T.bslot = start + k;
-				T.eq = false;
-			} else if(T.iobj != T.bobj || prim != T.bprim) {
-				T.eq = true;
-			}
-		}
-		return TRAV_RUN;
-	}
-	/* a node of the object hierarchy (world space) or of a mesh's: up to
-	 * four children in one 128-byte line; the hit ones (nodes, leaves, or
-	 * objects) are visited nearest first, each leaf and object in a step of
-	 * its own so that the lanes of a warp stay together */
-	const float4 *np = reinterpret_cast<const float4 *>((T.inst ? S.bnodes : S.tnodes) + T.cur);
-	float4 lx = __ldg(np), ly = __ldg(np + 1), lz = __ldg(np + 2);
-	float4 hx = __ldg(np + 3), hy = __ldg(np + 4), hz = __ldg(np + 5);
-	int4 ch = __ldg(reinterpret_cast<const int4 *>(np) + 6);
-	if(COUNT) tc->nodes++;
-	float lim = fminf(T.best, 1.0f);
-	int ref[4] = {ch.x, ch.y, ch.z, ch.w};
-	float key[4];
-	float tn;
-	const RayC &rc = T.rc;
-	key[0] = (ref[0] != BVH_NONE && wide_box(rc, lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, lim, tn)) ? tn : INFINITY;
-	key[1] = (ref[1] != BVH_NONE && wide_box(rc, lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, lim, tn)) ? tn : INFINITY;
-	key[2] = (ref[2] != BVH_NONE && wide_box(rc, lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, lim, tn)) ? tn : INFINITY;
-	key[3] = (ref[3] != BVH_NONE && wide_box(rc, lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, lim, tn)) ? tn : INFINITY;
-	if(ANY && !SORT) {
-		/* the hit children in node order: the first is next, the rest
-		 * are stacked so that they pop in order */
-		int nxt = BVH_NONE;
-		#pragma unroll
-		for(int k = 3; k >= 0; k--) {
-			if(key[k] == INFINITY) continue;
-			if(nxt != BVH_NONE) {
-				if(T.sp >= SRAY_STACK) { *overflow = 1; T.res = 0; return TRAV_RESULT; }
-				st.node[T.sp++] = nxt;
-			}
-			nxt = ref[k];
-		}
-		T.cur = nxt;
-		return TRAV_RUN;
-	}
-#define SRAY_CSWAP(i, j) do { if(key[j] < key[i]) { float tk = key[i]; key[i] = key[j]; key[j] = tk; int tr_ = ref[i]; ref[i] = ref[j]; ref[j] = tr_; } } while(0)
-	SRAY_CSWAP(0, 1);
-	SRAY_CSWAP(2, 3);
-	SRAY_CSWAP(0, 2);
-	SRAY_CSWAP(1, 3);
-	SRAY_CSWAP(1, 2);
-#undef SRAY_CSWAP
-	if(key[0] == INFINITY) {
-		T.cur = BVH_NONE;
-		return TRAV_RUN;
-	}
-	#pragma unroll
-	for(int k = 3; k >= 1; k--) {
-		if(key[k] == INFINITY) continue;
-		if(T.sp >= SRAY_STACK) { *overflow = 1; T.res = ANY ? 0 : 1; return TRAV_RESULT; }
-		st.node[T.sp] = ref[k];
-		if(!ANY) st.te[T.sp] = key[k];   /* any hit visits every entry */
-		T.sp++;
-	}
-	T.cur = ref[0];
-	return TRAV_RUN;
-}
-
-/* the end of a traversal: the hit, confirmed against the octrees.  ANY =
- * false: the closest hit into h (h empty on entry), returns 0 when the
- * octrees must decide.  ANY = true: returns 1 when a hit the octrees reach
- * exists, 0 when no hit exists, 2 when the octrees must decide. */
-template <bool ANY>
-__device__ __forceinline__ int trav_finish(const DScene &S, const Trav &T, Hit &h)
-{
-	if(T.bobj < 0) return ANY ? 0 : 1;
-	if(!ANY && T.eq) return 0;
-	if(T.bslot >= 0 && !octree_reaches(S.mnodes, S.mprim, __ldg(S.bhome + T.bslot), object_ray(S, T.bobj, T.ti, T.wo, T.wd), T.bprim,
-			T.best, !ANY))
-		return ANY ? 2 : 0;
-	if(!octree_reaches(S.snodes, S.sslots, __ldg(S.ohome + T.bobj), T.wr, T.bobj, T.best, !ANY)) return ANY ? 2 : 0;
-	if(ANY) return 1;
-	h.t = T.best;
-	h.obj = T.bobj;
-	h.prim = T.bprim;
-	h.tie = 0;
-	return 1;
 }
 
 /* ANY = false: closest hit into h, returns false when the octrees must

@@ -125,50 +125,6 @@ __global__ void __launch_bounds__(SRAY_TRACE_THREADS, 6) k_trace(DScene S, RayQu
 	if(!HYB && n > 0 && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctr->bvh_fallbacks, (unsigned long long)n);
 }
 
-/* Closest hits as k_trace computes them, but a lane takes its next ray as
- * soon as its own traversal ends (persistent threads with per-lane fetch):
- * the lanes of a warp keep stepping traversals, each one node, leaf or
- * object per step, instead of idling until the warp's longest ray ends.
- * Rays are taken in grid-stride order. */
-template <bool COUNT>
-__global__ void __launch_bounds__(SRAY_TRACE_THREADS, 6) k_trace_dyn(DScene S, RayQueue q, int4 *hits, DevCounters *ctr, int *fb)
-{
-	int n = *q.count;
-	TraceCounters tc = {0, 0};
-	int overflow = 0;
-	int stride = gridDim.x * blockDim.x;
-	int next = blockIdx.x * blockDim.x + threadIdx.x;
-	Trav T;
-	TStack st;
-	int ri = -1, status = TRAV_DONE;
-	for(;;) {
-		if(ri < 0) {
-			if(next >= n) break;
-			ri = next;
-			next += stride;
-			float4 o = q.o[ri], d = q.d[ri];
-			status = trav_begin<false>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), q.meta[ri].w, T);
-		}
-		if(status == TRAV_RUN) status = trav_step<COUNT, false, true>(S, T, st, &tc, &overflow);
-		if(status != TRAV_RUN) {
-			Hit h;
-			h.t = FLT_MAX;
-			h.obj = -1;
-			h.prim = -1;
-			h.tie = 0;
-			int res = status == TRAV_RESULT ? T.res : trav_finish<false>(S, T, h);
-			if(res) hits[ri] = make_int4(__float_as_int(h.t), h.obj, h.prim, h.tie);
-			else fb[1 + atomicAdd(fb, 1)] = ri;
-			ri = -1;
-		}
-	}
-	if(overflow) atomicOr(&ctr->overflow, 1);
-	if(COUNT) {
-		atomicAdd(&ctr->nodes, tc.nodes);
-		atomicAdd(&ctr->prims, tc.prims);
-	}
-}
-
 __device__ __forceinline__ void acc_add(float4 *acc, int p, float r, float g, float b)
 {
 	atomicAdd(&acc[p].x, r);
@@ -752,43 +708,6 @@ __global__ void __launch_bounds__(SRAY_TRACE_THREADS, 6) k_shadow(DScene S, cons
 		if(HYB) atomicAdd(&ctr->rays[2], (unsigned long long)n);
 		else if(n > 0) atomicAdd(&ctr->bvh_fallbacks, (unsigned long long)n);
 	}
-}
-
-/* light samples as k_shadow<true, SORT> tests them, a lane taking its next
- * request as soon as its own traversal ends (as k_trace_dyn) */
-template <bool SORT>
-__global__ void __launch_bounds__(SRAY_TRACE_THREADS, 6) k_shadow_dyn(DScene S, const ShadowReq *sq, const int *sq_count, float4 *acc,
-		DevCounters *ctr, int *fb)
-{
-	int n = *sq_count;
-	int overflow = 0;
-	int stride = gridDim.x * blockDim.x;
-	int next = blockIdx.x * blockDim.x + threadIdx.x;
-	Trav T;
-	TStack st;
-	int ri = -1, status = TRAV_DONE, pixel = 0;
-	float4 w = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-	for(;;) {
-		if(ri < 0) {
-			if(next >= n) break;
-			ri = next;
-			next += stride;
-			ShadowReq r = sq[ri];
-			pixel = __float_as_int(r.b.w);
-			w = r.w;
-			status = trav_begin<true>(S, mk(r.a.x, r.a.y, r.a.z), mk(r.b.x, r.b.y, r.b.z), __float_as_int(r.a.w), T);
-		}
-		if(status == TRAV_RUN) status = trav_step<false, true, SORT>(S, T, st, nullptr, &overflow);
-		if(status != TRAV_RUN) {
-			Hit h;
-			int res = status == TRAV_RESULT ? T.res : trav_finish<true>(S, T, h);
-			if(res == 2) fb[1 + atomicAdd(fb, 1)] = ri;
-			else if(res == 0) acc_add(acc, pixel, w.x, w.y, w.z);
-			ri = -1;
-		}
-	}
-	if(overflow) atomicOr(&ctr->overflow, 1);
-	if(blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctr->rays[2], (unsigned long long)n);
 }
 
 /* ---------------------------------------------------------------- */
@@ -2361,16 +2280,10 @@ int Renderer::trace_rays_with(const DScene &D, const RayQueue &qq, int n, const 
 	CK(cudaMemsetAsync(fb.p, 0, sizeof(int), s), "reset fallback list");
 	int g = grid_for(n, 128);
 	if(count) {
-		if(tune.trace_fetch)
-			LAUNCH(*this, name, s, k_trace_dyn<true><<<g, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
-		else
-			LAUNCH(*this, name, s, k_trace<true, true><<<g, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
+		LAUNCH(*this, name, s, k_trace<true, true><<<g, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
 		LAUNCH(*this, "octree_retrace", s, k_trace<true, false><<<152, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
 	} else {
-		if(tune.trace_fetch)
-			LAUNCH(*this, name, s, k_trace_dyn<false><<<g, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
-		else
-			LAUNCH(*this, name, s, k_trace<false, true><<<g, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
+		LAUNCH(*this, name, s, k_trace<false, true><<<g, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
 		LAUNCH(*this, "octree_retrace", s, k_trace<false, false><<<152, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
 	}
 	return 0;
@@ -2388,11 +2301,7 @@ int Renderer::shadow_rays(int cap, cudaStream_t s)
 	float4 *a = acc.as<float4>();
 	DevCounters *c = ctr.as<DevCounters>();
 	int *f = fbl.as<int>();
-	if(tune.trace_fetch && tune.shadow_order)
-		LAUNCH(*this, "shadow", s, k_shadow_dyn<false><<<g, 128, 0, s>>>(S, q, cnt + 5, a, c, f));
-	else if(tune.trace_fetch)
-		LAUNCH(*this, "shadow", s, k_shadow_dyn<true><<<g, 128, 0, s>>>(S, q, cnt + 5, a, c, f));
-	else if(tune.shadow_order)
+	if(tune.shadow_order)
 		LAUNCH(*this, "shadow", s, k_shadow<true, false><<<g, 128, 0, s>>>(S, q, cnt + 5, a, c, f));
 	else
 		LAUNCH(*this, "shadow", s, k_shadow<true><<<g, 128, 0, s>>>(S, q, cnt + 5, a, c, f));
@@ -2749,7 +2658,6 @@ static int check_tuning(const sray_tuning *t)
 	if(t->photon_tail < 0 || t->photon_tail > (1 << 26)) { g_err = "photon_tail must be 0..2^26"; return SRAY_EINVAL; }
 	if(t->shadow_order != 0 && t->shadow_order != 1) { g_err = "shadow_order must be 0 or 1"; return SRAY_EINVAL; }
 	if(t->stream_priority < 0 || t->stream_priority > 2) { g_err = "stream_priority must be 0, 1 or 2"; return SRAY_EINVAL; }
-	if(t->trace_fetch != 0 && t->trace_fetch != 1) { g_err = "trace_fetch must be 0 or 1"; return SRAY_EINVAL; }
 	return 0;
 }
 
@@ -2788,8 +2696,7 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 	static const int binary[] = {0, 1}, prios[] = {0, 1, 2};
 	struct Knob { int sray_tuning::*field; const int *vals; int n; };
 	const Knob knobs[] = {{&sray_tuning::render_tail, tails, 5}, {&sray_tuning::pool_blocks_per_sm, pools, 4},
-		{&sray_tuning::photon_tail, ptails, 4}, {&sray_tuning::shadow_order, binary, 2}, {&sray_tuning::stream_priority, prios, 3},
-		{&sray_tuning::trace_fetch, binary, 2}};
+		{&sray_tuning::photon_tail, ptails, 4}, {&sray_tuning::shadow_order, binary, 2}, {&sray_tuning::stream_priority, prios, 3}};
 	std::vector<sray_tune_trial> done;
 	cudaEvent_t e0, e1;
 	if(cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) { g_err = "autotune events"; return SRAY_ECUDA; }
@@ -2797,7 +2704,7 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 		for(const sray_tune_trial &d : done) {
 			if(d.tuning.render_tail == t.render_tail && d.tuning.pool_blocks_per_sm == t.pool_blocks_per_sm &&
 					d.tuning.photon_tail == t.photon_tail && d.tuning.shadow_order == t.shadow_order &&
-					d.tuning.stream_priority == t.stream_priority && d.tuning.trace_fetch == t.trace_fetch) {
+					d.tuning.stream_priority == t.stream_priority) {
 				*ms = d.ms_per_frame;
 				return 0;
 			}
