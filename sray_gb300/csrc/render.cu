@@ -2260,10 +2260,6 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 	stats.gather_selects = (int64_t)hc.g_select;
 	stats.gather_spills = (int64_t)hc.g_spill;
 	stats.bvh_fallbacks = (int64_t)hc.bvh_fallbacks;
-	/* the next frames' octree retraces: a few blocks while fallbacks are
-	 * rare (they then start as soon as a few SMs have room beside the
-	 * photon stream's blocks), a full wave otherwise */
-	retrace_grid = stats.bvh_fallbacks > RETRACE_FEW ? nsm : RETRACE_SMALL_GRID;
 	if(overlap_photons && !sc.lights.empty()) stats.photons_emitted = (int64_t)opt.caust_photons + opt.gi_photons;
 	if(S.nrc.mode) {
 		nrc_expect = (int64_t)hc.nrc[0];
@@ -2285,10 +2281,10 @@ int Renderer::trace_rays_with(const DScene &D, const RayQueue &qq, int n, const 
 	int g = grid_for(n, 128);
 	if(count) {
 		LAUNCH(*this, name, s, k_trace<true, true><<<g, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
-		LAUNCH(*this, "octree_retrace", s, k_trace<true, false><<<retrace_grid, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
+		LAUNCH(*this, "octree_retrace", s, k_trace<true, false><<<152, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
 	} else {
 		LAUNCH(*this, name, s, k_trace<false, true><<<g, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
-		LAUNCH(*this, "octree_retrace", s, k_trace<false, false><<<retrace_grid, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
+		LAUNCH(*this, "octree_retrace", s, k_trace<false, false><<<152, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
 	}
 	return 0;
 }
@@ -2309,7 +2305,7 @@ int Renderer::shadow_rays(int cap, cudaStream_t s)
 		LAUNCH(*this, "shadow", s, k_shadow<true, false><<<g, 128, 0, s>>>(S, q, cnt + 5, a, c, f));
 	else
 		LAUNCH(*this, "shadow", s, k_shadow<true><<<g, 128, 0, s>>>(S, q, cnt + 5, a, c, f));
-	LAUNCH(*this, "octree_retrace", s, k_shadow<false><<<retrace_grid, 128, 0, s>>>(S, q, cnt + 5, a, c, f));
+	LAUNCH(*this, "octree_retrace", s, k_shadow<false><<<152, 128, 0, s>>>(S, q, cnt + 5, a, c, f));
 	return 0;
 }
 

@@ -135,10 +135,7 @@ struct Renderer {
 	cudaEvent_t hs_fork = nullptr, hs_join = nullptr;
 	int priority_stream();
 	int shadow_rays(int cap, cudaStream_t s);
-	/* blocks of the octree-retrace launches, from the last frame's count
-	 * of rays the hierarchies left to the octrees */
-	int retrace_grid = 152;
-	enum { RETRACE_FEW = 65536, RETRACE_SMALL_GRID = 16 };
+
 	cudaEvent_t ps_done = nullptr;
 	sray_stats stats;
 	sray_tuning tune = {32768, 4, 65536, 0, 0, {0, 0, 0}};
