@@ -297,11 +297,7 @@ typedef struct sray_tuning {
 	                             greatest priority: 0 neither, 1 the photon stream, 2 the
 	                             render work (on an internal stream ordered after and
 	                             before the caller's) (0) */
-	int smem_carveout;        /* shared-memory carveout (percent of the SM's L1/shared
-	                             memory) preferred by the kernels that use no shared
-	                             memory, so that the gathers' blocks find it configured
-	                             beside them; 0 leaves the driver's choice (0) */
-	int reserved[2];
+	int reserved[3];
 } sray_tuning;
 
 typedef struct sray_tune_trial {

@@ -802,14 +802,4 @@ int photon_map_restore(Renderer &R, int global, const std::vector<DevPhoton> &h,
 	return photon_map_build(R, global, n, s);
 }
 
-cudaError_t photon_carveout(int value)
-{
-	const void *k[] = {(const void *)k_photon_emit, (const void *)k_photon_bounce, (const void *)k_photon_finish};
-	for(const void *f : k) {
-		cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, value);
-		if(e != cudaSuccess) return e;
-	}
-	return cudaSuccess;
-}
-
 }  // namespace sray

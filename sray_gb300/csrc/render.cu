@@ -2338,22 +2338,6 @@ int Renderer::photon_stream()
 	return 0;
 }
 
-/* The kernels that use no shared memory prefer the tuning's carveout (the
- * driver's choice for 0), so that SMs running them already have room for
- * the gathers' shared memory instead of draining first. */
-int Renderer::apply_carveout()
-{
-	if(tune.smem_carveout == carveout_applied) return 0;
-	int v = tune.smem_carveout ? tune.smem_carveout : (int)cudaSharedmemCarveoutDefault;
-	const void *k[] = {(const void *)k_trace<true, true>, (const void *)k_trace<false, true>, (const void *)k_trace<true, false>,
-		(const void *)k_trace<false, false>, (const void *)k_shadow<true, true>, (const void *)k_shadow<true, false>,
-		(const void *)k_shadow<false, true>, (const void *)k_shade, (const void *)k_camera, (const void *)k_finish};
-	for(const void *f : k) CK(cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, v), "carveout");
-	CK(photon_carveout(v), "carveout");
-	carveout_applied = tune.smem_carveout;
-	return 0;
-}
-
 int Renderer::priority_stream()
 {
 	if(hs) return 0;
@@ -2641,8 +2625,8 @@ static int render_frame(Renderer &R, long msec, float *fb, int fb_is_device, cud
 	 * greatest priority, after the caller's stream's earlier work and
 	 * before its later work */
 	cudaStream_t rs = s;
-	int r = R.apply_carveout();
-	if(!r && R.tune.stream_priority == 2) {
+	int r = 0;
+	if(R.tune.stream_priority == 2) {
 		r = R.priority_stream();
 		if(!r && (cudaEventRecord(R.hs_fork, s) != cudaSuccess || cudaStreamWaitEvent(R.hs, R.hs_fork, 0) != cudaSuccess))
 			r = R.fail(SRAY_ECUDA, "priority stream fork");
@@ -2674,7 +2658,6 @@ static int check_tuning(const sray_tuning *t)
 	if(t->photon_tail < 0 || t->photon_tail > (1 << 26)) { g_err = "photon_tail must be 0..2^26"; return SRAY_EINVAL; }
 	if(t->shadow_order != 0 && t->shadow_order != 1) { g_err = "shadow_order must be 0 or 1"; return SRAY_EINVAL; }
 	if(t->stream_priority < 0 || t->stream_priority > 2) { g_err = "stream_priority must be 0, 1 or 2"; return SRAY_EINVAL; }
-	if(t->smem_carveout < 0 || t->smem_carveout > 100) { g_err = "smem_carveout must be 0..100"; return SRAY_EINVAL; }
 	return 0;
 }
 
@@ -2710,11 +2693,10 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 	static const int tails[] = {0, 2048, 8192, 32768, 131072};
 	static const int pools[] = {2, 4, 8, 16};
 	static const int ptails[] = {16384, 65536, 262144, 1048576};
-	static const int binary[] = {0, 1}, prios[] = {0, 1, 2}, carve[] = {0, 25, 50};
+	static const int binary[] = {0, 1}, prios[] = {0, 1, 2};
 	struct Knob { int sray_tuning::*field; const int *vals; int n; };
 	const Knob knobs[] = {{&sray_tuning::render_tail, tails, 5}, {&sray_tuning::pool_blocks_per_sm, pools, 4},
-		{&sray_tuning::photon_tail, ptails, 4}, {&sray_tuning::shadow_order, binary, 2}, {&sray_tuning::stream_priority, prios, 3},
-		{&sray_tuning::smem_carveout, carve, 3}};
+		{&sray_tuning::photon_tail, ptails, 4}, {&sray_tuning::shadow_order, binary, 2}, {&sray_tuning::stream_priority, prios, 3}};
 	std::vector<sray_tune_trial> done;
 	cudaEvent_t e0, e1;
 	if(cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) { g_err = "autotune events"; return SRAY_ECUDA; }
@@ -2722,7 +2704,7 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 		for(const sray_tune_trial &d : done) {
 			if(d.tuning.render_tail == t.render_tail && d.tuning.pool_blocks_per_sm == t.pool_blocks_per_sm &&
 					d.tuning.photon_tail == t.photon_tail && d.tuning.shadow_order == t.shadow_order &&
-					d.tuning.stream_priority == t.stream_priority && d.tuning.smem_carveout == t.smem_carveout) {
+					d.tuning.stream_priority == t.stream_priority) {
 				*ms = d.ms_per_frame;
 				return 0;
 			}

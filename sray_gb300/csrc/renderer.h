@@ -135,12 +135,10 @@ struct Renderer {
 	cudaEvent_t hs_fork = nullptr, hs_join = nullptr;
 	int priority_stream();
 	int shadow_rays(int cap, cudaStream_t s);
-	int carveout_applied = 0;   /* the smem_carveout the kernels were last given */
-	int apply_carveout();
 
 	cudaEvent_t ps_done = nullptr;
 	sray_stats stats;
-	sray_tuning tune = {32768, 4, 65536, 0, 0, 0, {0, 0}};
+	sray_tuning tune = {32768, 4, 65536, 0, 0, {0, 0, 0}};
 	int nsm = 0;                  /* multiprocessors of the device */
 
 	/* radiance cache: queries (inputs, weight + slot), training and
@@ -223,9 +221,6 @@ struct Renderer {
 	} while(0)
 
 /* render.cu: closest hits of the first n rays of q into R.hits */
-/* the preferred shared-memory carveout of the photon kernels that use
- * none (cudaFuncAttributePreferredSharedMemoryCarveout value) */
-cudaError_t photon_carveout(int value);
 int launch_trace(Renderer &R, const DScene &D, const RayQueue &q, int n, const char *name, cudaStream_t s);
 
 /* photon.cu: both maps traced with the scene view `base` */
