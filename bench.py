@@ -51,7 +51,7 @@ def parse():
                          "per-region fallback, or the cache in every region")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default scheduler tuning")
     ap.add_argument("--tuning", default=None,
-                    help="render_tail,pool_blocks_per_sm,photon_tail[,shadow_order[,stream_priority]]: "
+                    help="render_tail,pool_blocks_per_sm,photon_tail[,shadow_order[,stream_priority[,warp_rays]]]: "
                          "set the "
                          "scheduler tuning instead "
                          "of autotuning")
@@ -545,8 +545,8 @@ def run_ours(args):
     # the library's autotuner picks the scheduler's queue depths (untimed setup)
     if args.tuning:
         vals = [int(v) for v in args.tuning.split(",")]
-        g.set_tuning(**dict(zip(("render_tail", "pool_blocks_per_sm", "photon_tail", "shadow_order", "stream_priority"),
-                                vals)))
+        g.set_tuning(**dict(zip(("render_tail", "pool_blocks_per_sm", "photon_tail", "shadow_order", "stream_priority",
+                                 "warp_rays"), vals)))
     tuning = {"chosen": g.tuning(), "autotuned": False}
     if not args.no_autotune and not args.tuning:
         best, best_ms, trials = g.autotune(fb, frames=3, stream=stream)

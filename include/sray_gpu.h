@@ -297,7 +297,9 @@ typedef struct sray_tuning {
 	                             greatest priority: 0 neither, 1 the photon stream, 2 the
 	                             render work (on an internal stream ordered after and
 	                             before the caller's) (0) */
-	int reserved[3];
+	int warp_rays;            /* closest-hit passes of at most this many rays trace one
+	                             ray per warp instead of one per thread (0: never) (0) */
+	int reserved[2];
 } sray_tuning;
 
 typedef struct sray_tune_trial {

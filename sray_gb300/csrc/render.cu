@@ -125,6 +125,200 @@ __global__ void __launch_bounds__(SRAY_TRACE_THREADS, 6) k_trace(DScene S, RayQu
 	if(!HYB && n > 0 && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctr->bvh_fallbacks, (unsigned long long)n);
 }
 
+/* Closest hits with one warp per ray, for passes of few rays (the tails of
+ * the shading tree: long mirror and glass chains, grazing rays), whose
+ * launches otherwise last as long as one thread's chain of dependent node
+ * fetches.  The warp keeps the ray's stack in shared memory and takes up to
+ * eight entries per step: four lanes per entry test a node's four children,
+ * a leaf's faces, or an object.  The hit children are sorted across the
+ * warp and stacked nearest on top.  The result is the thread-per-ray
+ * traversal's: the closest candidate over every entry whose box is reached
+ * within the best distance so far, with a tie where two different faces or
+ * objects share it (the candidates at the final distance are reached in any
+ * order), confirmed against the octrees; a ray it cannot decide (a tie, an
+ * unconfirmed hit, a full stack) goes to the octree retrace. */
+#define WR_CAP 512
+#define WR_POP 8
+
+__device__ __forceinline__ float lane_pick(float4 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); }
+
+__global__ void __launch_bounds__(128) k_trace_warp(DScene S, RayQueue q, int4 *hits, int *fb)
+{
+	__shared__ int s_ref[4][WR_CAP];
+	__shared__ int s_obj[4][WR_CAP];
+	__shared__ float s_te[4][WR_CAP];
+	const unsigned FULL = 0xffffffffu;
+	int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+	int g = lane >> 2, sub = lane & 3;
+	int n = *q.count;
+	for(int ri = blockIdx.x * 4 + w; ri < n; ri += gridDim.x * 4) {
+		float4 o4 = q.o[ri], d4 = q.d[ri];
+		int time = q.meta[ri].w;
+		V3 wo = mk(o4.x, o4.y, o4.z), wd = mk(d4.x, d4.y, d4.z);
+		int res = 1;
+		float best = FLT_MAX;
+		int bobj = -1, bprim = -1, bslot = -1;
+		if(!S.has_scene) {
+			res = 1;
+		} else if(!S.tnodes) {
+			res = 0;
+		} else {
+			int ti = time_index(S, time);
+			RayT wr = make_ray(wo, wd);
+			const DevNode &sroot = S.snodes[S.sroot];
+			RayC wc = make_rayc(wr, box_bound(sroot.mn, sroot.mx));
+			bool eq = false, bail = false;
+			if(lane == 0) {
+				s_ref[w][0] = 0;   /* the object hierarchy's root */
+				s_obj[w][0] = -1;
+				s_te[w][0] = -INFINITY;
+			}
+			int sp = 1;
+			__syncwarp();
+			while(sp > 0 && !bail) {
+				int npop = sp < WR_POP ? sp : WR_POP;
+				int base = sp - npop;
+				bool active = g < npop;
+				int eref = 0, eobj = -1;
+				if(active) {
+					eref = s_ref[w][base + g];
+					eobj = s_obj[w][base + g];
+					active = s_te[w][base + g] <= best;
+				}
+				__syncwarp();
+				sp = base;
+				float ct = INFINITY;
+				int cobj = -1, cprim = -1, cslot = -1;
+				bool ceq = false, push = false, lbail = false;
+				int pref = 0, pobj = -1;
+				float pte = 0.0f;
+				if(active) {
+					if(eobj < 0 && eref < 0) {
+						/* an object of the object hierarchy */
+						if(sub == 0) {
+							int o = ~eref;
+							const DevObj ob = S.objs[o];
+							RayT orr = object_ray(S, o, ti, wo, wd);
+							if(ob.type != 2) {
+								float t;
+								bool hit = ob.type == 0 ? sphere_hit(orr, ob.rad, S.eps, t) : cylinder_hit(orr, ob.rad, ob.start, ob.end, S.eps, t);
+								if(hit && t <= best) { ct = t; cobj = o; cprim = 0; cslot = -1; }
+							} else if(ob.mesh_root >= 0) {
+								if(ob.bvh_root < 0) {
+									lbail = true;
+								} else {
+									float te;
+									const DevNode &rn = S.mnodes[ob.mesh_root];
+									if(box_hit(rn.mn, rn.mx, orr, te) && !SRAY_PRUNE(te, best)) {
+										push = true;
+										pref = ob.bvh_root;
+										pobj = o;
+										pte = te;
+									}
+								}
+							}
+						}
+					} else if(eref < 0) {
+						/* a leaf of object eobj's mesh hierarchy: faces sub, sub + 4, ... */
+						unsigned v = ~(unsigned)eref;
+						int start = (int)(v >> 4), cnt = (int)(v & 15u);
+						RayT orr = object_ray(S, eobj, ti, wo, wd);
+						const float4 *tp = reinterpret_cast<const float4 *>(S.btris + start);
+						for(int k = sub; k < cnt; k += 4) {
+							float4 a = __ldg(tp + 3 * k), b = __ldg(tp + 3 * k + 1), c = __ldg(tp + 3 * k + 2);
+							float t;
+							if(!tri_hit(a, b, c, orr, S.eps, best, t)) continue;
+							int prim = __ldg(S.bprim + start + k);
+							if(t < ct) { ct = t; cobj = eobj; cprim = prim; cslot = start + k; ceq = false; }
+							else if(t == ct) ceq = true;
+						}
+					} else {
+						/* a node: child `sub` */
+						const float4 *np = reinterpret_cast<const float4 *>((eobj >= 0 ? S.bnodes : S.tnodes) + eref);
+						RayC rc = wc;
+						if(eobj >= 0) {
+							const DevNode &rn = S.mnodes[S.objs[eobj].mesh_root];
+							rc = make_rayc(object_ray(S, eobj, ti, wo, wd), box_bound(rn.mn, rn.mx));
+						}
+						int ch = __ldg(reinterpret_cast<const int *>(np + 6) + sub);
+						float tn;
+						if(ch != BVH_NONE && wide_box(rc, lane_pick(__ldg(np), sub), lane_pick(__ldg(np + 1), sub), lane_pick(__ldg(np + 2), sub),
+								lane_pick(__ldg(np + 3), sub), lane_pick(__ldg(np + 4), sub), lane_pick(__ldg(np + 5), sub), fminf(best, 1.0f), tn)) {
+							push = true;
+							pref = ch;
+							pobj = eobj;
+							pte = tn;
+						}
+					}
+				}
+				if(__any_sync(FULL, lbail)) { bail = true; break; }
+				/* the step's closest candidate */
+				float m = ct;
+				for(int off = 16; off > 0; off >>= 1) m = fminf(m, __shfl_xor_sync(FULL, m, off));
+				if(m < INFINITY && m <= best) {
+					unsigned at = __ballot_sync(FULL, ct == m);
+					int src = __ffs(at) - 1;
+					int mobj = __shfl_sync(FULL, cobj, src), mprim = __shfl_sync(FULL, cprim, src), mslot = __shfl_sync(FULL, cslot, src);
+					bool other = __any_sync(FULL, ct == m && (ceq || cobj != mobj || cprim != mprim));
+					if(m < best) {
+						best = m;
+						bobj = mobj;
+						bprim = mprim;
+						bslot = mslot;
+						eq = other;
+					} else if(other || mobj != bobj || mprim != bprim) {
+						eq = true;
+					}
+				}
+				/* stack the hit children, farthest first so that the nearest pop first */
+				unsigned pm = __ballot_sync(FULL, push);
+				int cnt = __popc(pm);
+				if(sp + cnt > WR_CAP) { bail = true; break; }
+				float key = push ? pte : -INFINITY;
+				int idx = lane;
+				for(int k = 2; k <= 32; k <<= 1) {
+					for(int j = k >> 1; j > 0; j >>= 1) {
+						float ok = __shfl_xor_sync(FULL, key, j);
+						int oi = __shfl_xor_sync(FULL, idx, j);
+						bool desc = (lane & k) == 0;         /* descending runs first: a descending sort overall */
+						bool lower = (lane & j) == 0;
+						bool take = lower == desc ? (ok > key || (ok == key && oi < idx)) : (ok < key || (ok == key && oi > idx));
+						if(take) { key = ok; idx = oi; }
+					}
+				}
+				int sref = __shfl_sync(FULL, pref, idx), sobj = __shfl_sync(FULL, pobj, idx);
+				float ste = __shfl_sync(FULL, pte, idx);
+				if(lane < cnt) {
+					s_ref[w][sp + lane] = sref;
+					s_obj[w][sp + lane] = sobj;
+					s_te[w][sp + lane] = ste;
+				}
+				sp += cnt;
+				__syncwarp();
+			}
+			if(bail) res = 0;
+			else if(bobj < 0) res = 1;
+			else if(eq) res = 0;
+			else {
+				int ok = 1;
+				if(lane == 0) {
+					if(bslot >= 0 && !octree_reaches(S.mnodes, S.mprim, __ldg(S.bhome + bslot), object_ray(S, bobj, ti, wo, wd), bprim, best, true))
+						ok = 0;
+					else if(!octree_reaches(S.snodes, S.sslots, __ldg(S.ohome + bobj), wr, bobj, best, true))
+						ok = 0;
+				}
+				res = __shfl_sync(FULL, ok, 0);
+			}
+		}
+		if(lane == 0) {
+			if(!res) fb[1 + atomicAdd(fb, 1)] = ri;
+			else if(bobj >= 0) hits[ri] = make_int4(__float_as_int(best), bobj, bprim, 0);
+			else hits[ri] = make_int4(__float_as_int(FLT_MAX), -1, -1, 0);
+		}
+		__syncwarp();
+	}
+}
+
 __device__ __forceinline__ void acc_add(float4 *acc, int p, float r, float g, float b)
 {
 	atomicAdd(&acc[p].x, r);
@@ -2279,6 +2473,12 @@ int Renderer::trace_rays_with(const DScene &D, const RayQueue &qq, int n, const 
 	CK(fb.ensure(((size_t)n + 1) * sizeof(int)), "fallback list");
 	CK(cudaMemsetAsync(fb.p, 0, sizeof(int), s), "reset fallback list");
 	int g = grid_for(n, 128);
+	if(!count && n <= tune.warp_rays) {
+		/* a pass of few rays: one warp per ray */
+		LAUNCH(*this, name, s, k_trace_warp<<<grid_for(n, 4), 128, 0, s>>>(D, qq, hit_out, fb.as<int>()));
+		LAUNCH(*this, "octree_retrace", s, k_trace<false, false><<<152, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
+		return 0;
+	}
 	if(count) {
 		LAUNCH(*this, name, s, k_trace<true, true><<<g, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
 		LAUNCH(*this, "octree_retrace", s, k_trace<true, false><<<152, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
@@ -2658,6 +2858,7 @@ static int check_tuning(const sray_tuning *t)
 	if(t->photon_tail < 0 || t->photon_tail > (1 << 26)) { g_err = "photon_tail must be 0..2^26"; return SRAY_EINVAL; }
 	if(t->shadow_order != 0 && t->shadow_order != 1) { g_err = "shadow_order must be 0 or 1"; return SRAY_EINVAL; }
 	if(t->stream_priority < 0 || t->stream_priority > 2) { g_err = "stream_priority must be 0, 1 or 2"; return SRAY_EINVAL; }
+	if(t->warp_rays < 0 || t->warp_rays > (1 << 24)) { g_err = "warp_rays must be 0..2^24"; return SRAY_EINVAL; }
 	return 0;
 }
 
@@ -2693,10 +2894,11 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 	static const int tails[] = {0, 2048, 8192, 32768, 131072};
 	static const int pools[] = {2, 4, 8, 16};
 	static const int ptails[] = {16384, 65536, 262144, 1048576};
-	static const int binary[] = {0, 1}, prios[] = {0, 1, 2};
+	static const int binary[] = {0, 1}, prios[] = {0, 1, 2}, wrays[] = {0, 1024, 4096, 16384};
 	struct Knob { int sray_tuning::*field; const int *vals; int n; };
 	const Knob knobs[] = {{&sray_tuning::render_tail, tails, 5}, {&sray_tuning::pool_blocks_per_sm, pools, 4},
-		{&sray_tuning::photon_tail, ptails, 4}, {&sray_tuning::shadow_order, binary, 2}, {&sray_tuning::stream_priority, prios, 3}};
+		{&sray_tuning::photon_tail, ptails, 4}, {&sray_tuning::shadow_order, binary, 2}, {&sray_tuning::stream_priority, prios, 3},
+		{&sray_tuning::warp_rays, wrays, 4}};
 	std::vector<sray_tune_trial> done;
 	cudaEvent_t e0, e1;
 	if(cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) { g_err = "autotune events"; return SRAY_ECUDA; }
@@ -2704,7 +2906,7 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 		for(const sray_tune_trial &d : done) {
 			if(d.tuning.render_tail == t.render_tail && d.tuning.pool_blocks_per_sm == t.pool_blocks_per_sm &&
 					d.tuning.photon_tail == t.photon_tail && d.tuning.shadow_order == t.shadow_order &&
-					d.tuning.stream_priority == t.stream_priority) {
+					d.tuning.stream_priority == t.stream_priority && d.tuning.warp_rays == t.warp_rays) {
 				*ms = d.ms_per_frame;
 				return 0;
 			}

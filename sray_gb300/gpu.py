@@ -56,7 +56,8 @@ class SrayJob(ctypes.Structure):
 
 class SrayTuning(ctypes.Structure):
     _fields_ = [("render_tail", ctypes.c_int), ("pool_blocks_per_sm", ctypes.c_int), ("photon_tail", ctypes.c_int),
-                ("shadow_order", ctypes.c_int), ("stream_priority", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+                ("shadow_order", ctypes.c_int), ("stream_priority", ctypes.c_int), ("warp_rays", ctypes.c_int),
+                ("reserved", ctypes.c_int * 2)]
 
 
 class SrayTuneTrial(ctypes.Structure):

@@ -87,10 +87,12 @@ def test_image_small_scene(small_pair):
     assert _compare(img_g, img_o, "small 256^2 knn") <= 1e-3
 
 
-@pytest.mark.parametrize("tuning", [dict(shadow_order=1), dict(stream_priority=1), dict(stream_priority=2)])
+@pytest.mark.parametrize("tuning", [dict(shadow_order=1), dict(stream_priority=1), dict(stream_priority=2),
+                                    dict(warp_rays=1 << 24)])
 def test_tuning_keeps_the_image(small_pair, tuning):
     # light samples' any-hit traversal in node order instead of nearest
-    # first; the photon stream or the frame's own stream given priority
+    # first; the photon stream or the frame's own stream given priority;
+    # every closest-hit pass traced one ray per warp
     g, o = small_pair(width=192, height=192)
     g.set_tuning(**tuning)
     n = 192 * 192
