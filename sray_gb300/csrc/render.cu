@@ -142,174 +142,192 @@ __global__ void __launch_bounds__(SRAY_TRACE_THREADS, 6) k_trace(DScene S, RayQu
 
 __device__ __forceinline__ float lane_pick(float4 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); }
 
+/* One ray's two-level traversal by the calling warp (all 32 lanes, the
+ * same arguments), with the warp's stack st_*.  ANY = false: returns 1 with
+ * the closest hit in best / bobj / bprim (bobj -1: none), 0 when the
+ * octrees must decide.  ANY = true (a light sample, segment [eps, 1]):
+ * returns 1 when a hit the octrees reach exists, 0 when none exists, 2 when
+ * the octrees must decide. */
+template <bool ANY>
+__device__ __forceinline__ int warp_trace(const DScene &S, V3 wo, V3 wd, int time, int *st_ref, int *st_obj, float *st_te, float &best,
+		int &bobj, int &bprim)
+{
+	const unsigned FULL = 0xffffffffu;
+	int lane = threadIdx.x & 31;
+	int g = lane >> 2, sub = lane & 3;
+	best = ANY ? 1.0f : FLT_MAX;
+	bobj = -1;
+	bprim = -1;
+	if(!S.has_scene) return ANY ? 0 : 1;
+	if(!S.tnodes) return ANY ? 2 : 0;
+	int bslot = -1;
+	int ti = time_index(S, time);
+	RayT wr = make_ray(wo, wd);
+	const DevNode &sroot = S.snodes[S.sroot];
+	RayC wc = make_rayc(wr, box_bound(sroot.mn, sroot.mx));
+	bool eq = false;
+	if(lane == 0) {
+		st_ref[0] = 0;   /* the object hierarchy's root */
+		st_obj[0] = -1;
+		st_te[0] = -INFINITY;
+	}
+	int sp = 1;
+	__syncwarp();
+	while(sp > 0) {
+		int npop = sp < WR_POP ? sp : WR_POP;
+		int base = sp - npop;
+		bool active = g < npop;
+		int eref = 0, eobj = -1;
+		if(active) {
+			eref = st_ref[base + g];
+			eobj = st_obj[base + g];
+			active = ANY || st_te[base + g] <= best;
+		}
+		__syncwarp();
+		sp = base;
+		float ct = INFINITY;
+		int cobj = -1, cprim = -1, cslot = -1;
+		bool ceq = false, push = false, lbail = false;
+		int pref = 0, pobj = -1;
+		float pte = 0.0f;
+		if(active) {
+			if(eobj < 0 && eref < 0) {
+				/* an object of the object hierarchy */
+				if(sub == 0) {
+					int o = ~eref;
+					const DevObj ob = S.objs[o];
+					RayT orr = object_ray(S, o, ti, wo, wd);
+					if(ob.type != 2) {
+						float t;
+						bool hit = ob.type == 0 ? sphere_hit(orr, ob.rad, S.eps, t) : cylinder_hit(orr, ob.rad, ob.start, ob.end, S.eps, t);
+						if(hit && t <= best) { ct = t; cobj = o; cprim = 0; cslot = -1; }
+					} else if(ob.mesh_root >= 0) {
+						if(ob.bvh_root < 0) {
+							lbail = true;
+						} else {
+							float te;
+							const DevNode &rn = S.mnodes[ob.mesh_root];
+							if(box_hit(rn.mn, rn.mx, orr, te) && (ANY || !SRAY_PRUNE(te, best))) {
+								push = true;
+								pref = ob.bvh_root;
+								pobj = o;
+								pte = te;
+							}
+						}
+					}
+				}
+			} else if(eref < 0) {
+				/* a leaf of object eobj's mesh hierarchy: faces sub, sub + 4, ... */
+				unsigned v = ~(unsigned)eref;
+				int start = (int)(v >> 4), cnt = (int)(v & 15u);
+				RayT orr = object_ray(S, eobj, ti, wo, wd);
+				const float4 *tp = reinterpret_cast<const float4 *>(S.btris + start);
+				for(int k = sub; k < cnt; k += 4) {
+					float4 a = __ldg(tp + 3 * k), b = __ldg(tp + 3 * k + 1), c = __ldg(tp + 3 * k + 2);
+					float t;
+					if(!tri_hit(a, b, c, orr, S.eps, best, t)) continue;
+					int prim = __ldg(S.bprim + start + k);
+					if(t < ct) { ct = t; cobj = eobj; cprim = prim; cslot = start + k; ceq = false; }
+					else if(t == ct) ceq = true;
+				}
+			} else {
+				/* a node: child `sub` */
+				const float4 *np = reinterpret_cast<const float4 *>((eobj >= 0 ? S.bnodes : S.tnodes) + eref);
+				RayC rc = wc;
+				if(eobj >= 0) {
+					const DevNode &rn = S.mnodes[S.objs[eobj].mesh_root];
+					rc = make_rayc(object_ray(S, eobj, ti, wo, wd), box_bound(rn.mn, rn.mx));
+				}
+				int ch = __ldg(reinterpret_cast<const int *>(np + 6) + sub);
+				float tn;
+				if(ch != BVH_NONE && wide_box(rc, lane_pick(__ldg(np), sub), lane_pick(__ldg(np + 1), sub), lane_pick(__ldg(np + 2), sub),
+						lane_pick(__ldg(np + 3), sub), lane_pick(__ldg(np + 4), sub), lane_pick(__ldg(np + 5), sub), fminf(best, 1.0f), tn)) {
+					push = true;
+					pref = ch;
+					pobj = eobj;
+					pte = tn;
+				}
+			}
+		}
+		if(__any_sync(FULL, lbail)) return ANY ? 2 : 0;
+		/* the step's closest candidate */
+		float m = ct;
+		for(int off = 16; off > 0; off >>= 1) m = fminf(m, __shfl_xor_sync(FULL, m, off));
+		if(m < INFINITY && m <= best) {
+			unsigned at = __ballot_sync(FULL, ct == m);
+			int src = __ffs(at) - 1;
+			int mobj = __shfl_sync(FULL, cobj, src), mprim = __shfl_sync(FULL, cprim, src), mslot = __shfl_sync(FULL, cslot, src);
+			if(ANY) {
+				best = m;
+				bobj = mobj;
+				bprim = mprim;
+				bslot = mslot;
+				break;
+			}
+			bool other = __any_sync(FULL, ct == m && (ceq || cobj != mobj || cprim != mprim));
+			if(m < best) {
+				best = m;
+				bobj = mobj;
+				bprim = mprim;
+				bslot = mslot;
+				eq = other;
+			} else if(other || mobj != bobj || mprim != bprim) {
+				eq = true;
+			}
+		}
+		/* stack the hit children, farthest first so that the nearest pop first */
+		unsigned pm = __ballot_sync(FULL, push);
+		int cnt = __popc(pm);
+		if(sp + cnt > WR_CAP) return ANY ? 2 : 0;
+		float key = push ? pte : -INFINITY;
+		int idx = lane;
+		for(int k = 2; k <= 32; k <<= 1) {
+			for(int j = k >> 1; j > 0; j >>= 1) {
+				float ok = __shfl_xor_sync(FULL, key, j);
+				int oi = __shfl_xor_sync(FULL, idx, j);
+				bool desc = (lane & k) == 0;         /* descending runs first: a descending sort overall */
+				bool lower = (lane & j) == 0;
+				bool take = lower == desc ? (ok > key || (ok == key && oi < idx)) : (ok < key || (ok == key && oi > idx));
+				if(take) { key = ok; idx = oi; }
+			}
+		}
+		int sref = __shfl_sync(FULL, pref, idx), sobj = __shfl_sync(FULL, pobj, idx);
+		float ste = __shfl_sync(FULL, pte, idx);
+		if(lane < cnt) {
+			st_ref[sp + lane] = sref;
+			st_obj[sp + lane] = sobj;
+			st_te[sp + lane] = ste;
+		}
+		sp += cnt;
+		__syncwarp();
+	}
+	if(bobj < 0) return ANY ? 0 : 1;
+	if(!ANY && eq) return 0;
+	int ok = 1;
+	if(lane == 0) {
+		if(bslot >= 0 && !octree_reaches(S.mnodes, S.mprim, __ldg(S.bhome + bslot), object_ray(S, bobj, ti, wo, wd), bprim, best, !ANY))
+			ok = 0;
+		else if(!octree_reaches(S.snodes, S.sslots, __ldg(S.ohome + bobj), wr, bobj, best, !ANY))
+			ok = 0;
+	}
+	ok = __shfl_sync(FULL, ok, 0);
+	if(ANY) return ok ? 1 : 2;
+	return ok;
+}
+
 __global__ void __launch_bounds__(128) k_trace_warp(DScene S, RayQueue q, int4 *hits, int *fb)
 {
 	__shared__ int s_ref[4][WR_CAP];
 	__shared__ int s_obj[4][WR_CAP];
 	__shared__ float s_te[4][WR_CAP];
-	const unsigned FULL = 0xffffffffu;
 	int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-	int g = lane >> 2, sub = lane & 3;
 	int n = *q.count;
 	for(int ri = blockIdx.x * 4 + w; ri < n; ri += gridDim.x * 4) {
 		float4 o4 = q.o[ri], d4 = q.d[ri];
-		int time = q.meta[ri].w;
-		V3 wo = mk(o4.x, o4.y, o4.z), wd = mk(d4.x, d4.y, d4.z);
-		int res = 1;
-		float best = FLT_MAX;
-		int bobj = -1, bprim = -1, bslot = -1;
-		if(!S.has_scene) {
-			res = 1;
-		} else if(!S.tnodes) {
-			res = 0;
-		} else {
-			int ti = time_index(S, time);
-			RayT wr = make_ray(wo, wd);
-			const DevNode &sroot = S.snodes[S.sroot];
-			RayC wc = make_rayc(wr, box_bound(sroot.mn, sroot.mx));
-			bool eq = false, bail = false;
-			if(lane == 0) {
-				s_ref[w][0] = 0;   /* the object hierarchy's root */
-				s_obj[w][0] = -1;
-				s_te[w][0] = -INFINITY;
-			}
-			int sp = 1;
-			__syncwarp();
-			while(sp > 0 && !bail) {
-				int npop = sp < WR_POP ? sp : WR_POP;
-				int base = sp - npop;
-				bool active = g < npop;
-				int eref = 0, eobj = -1;
-				if(active) {
-					eref = s_ref[w][base + g];
-					eobj = s_obj[w][base + g];
-					active = s_te[w][base + g] <= best;
-				}
-				__syncwarp();
-				sp = base;
-				float ct = INFINITY;
-				int cobj = -1, cprim = -1, cslot = -1;
-				bool ceq = false, push = false, lbail = false;
-				int pref = 0, pobj = -1;
-				float pte = 0.0f;
-				if(active) {
-					if(eobj < 0 && eref < 0) {
-						/* an object of the object hierarchy */
-						if(sub == 0) {
-							int o = ~eref;
-							const DevObj ob = S.objs[o];
-							RayT orr = object_ray(S, o, ti, wo, wd);
-							if(ob.type != 2) {
-								float t;
-								bool hit = ob.type == 0 ? sphere_hit(orr, ob.rad, S.eps, t) : cylinder_hit(orr, ob.rad, ob.start, ob.end, S.eps, t);
-								if(hit && t <= best) { ct = t; cobj = o; cprim = 0; cslot = -1; }
-							} else if(ob.mesh_root >= 0) {
-								if(ob.bvh_root < 0) {
-									lbail = true;
-								} else {
-									float te;
-									const DevNode &rn = S.mnodes[ob.mesh_root];
-									if(box_hit(rn.mn, rn.mx, orr, te) && !SRAY_PRUNE(te, best)) {
-										push = true;
-										pref = ob.bvh_root;
-										pobj = o;
-										pte = te;
-									}
-								}
-							}
-						}
-					} else if(eref < 0) {
-						/* a leaf of object eobj's mesh hierarchy: faces sub, sub + 4, ... */
-						unsigned v = ~(unsigned)eref;
-						int start = (int)(v >> 4), cnt = (int)(v & 15u);
-						RayT orr = object_ray(S, eobj, ti, wo, wd);
-						const float4 *tp = reinterpret_cast<const float4 *>(S.btris + start);
-						for(int k = sub; k < cnt; k += 4) {
-							float4 a = __ldg(tp + 3 * k), b = __ldg(tp + 3 * k + 1), c = __ldg(tp + 3 * k + 2);
-							float t;
-							if(!tri_hit(a, b, c, orr, S.eps, best, t)) continue;
-							int prim = __ldg(S.bprim + start + k);
-							if(t < ct) { ct = t; cobj = eobj; cprim = prim; cslot = start + k; ceq = false; }
-							else if(t == ct) ceq = true;
-						}
-					} else {
-						/* a node: child `sub` */
-						const float4 *np = reinterpret_cast<const float4 *>((eobj >= 0 ? S.bnodes : S.tnodes) + eref);
-						RayC rc = wc;
-						if(eobj >= 0) {
-							const DevNode &rn = S.mnodes[S.objs[eobj].mesh_root];
-							rc = make_rayc(object_ray(S, eobj, ti, wo, wd), box_bound(rn.mn, rn.mx));
-						}
-						int ch = __ldg(reinterpret_cast<const int *>(np + 6) + sub);
-						float tn;
-						if(ch != BVH_NONE && wide_box(rc, lane_pick(__ldg(np), sub), lane_pick(__ldg(np + 1), sub), lane_pick(__ldg(np + 2), sub),
-								lane_pick(__ldg(np + 3), sub), lane_pick(__ldg(np + 4), sub), lane_pick(__ldg(np + 5), sub), fminf(best, 1.0f), tn)) {
-							push = true;
-							pref = ch;
-							pobj = eobj;
-							pte = tn;
-						}
-					}
-				}
-				if(__any_sync(FULL, lbail)) { bail = true; break; }
-				/* the step's closest candidate */
-				float m = ct;
-				for(int off = 16; off > 0; off >>= 1) m = fminf(m, __shfl_xor_sync(FULL, m, off));
-				if(m < INFINITY && m <= best) {
-					unsigned at = __ballot_sync(FULL, ct == m);
-					int src = __ffs(at) - 1;
-					int mobj = __shfl_sync(FULL, cobj, src), mprim = __shfl_sync(FULL, cprim, src), mslot = __shfl_sync(FULL, cslot, src);
-					bool other = __any_sync(FULL, ct == m && (ceq || cobj != mobj || cprim != mprim));
-					if(m < best) {
-						best = m;
-						bobj = mobj;
-						bprim = mprim;
-						bslot = mslot;
-						eq = other;
-					} else if(other || mobj != bobj || mprim != bprim) {
-						eq = true;
-					}
-				}
-				/* stack the hit children, farthest first so that the nearest pop first */
-				unsigned pm = __ballot_sync(FULL, push);
-				int cnt = __popc(pm);
-				if(sp + cnt > WR_CAP) { bail = true; break; }
-				float key = push ? pte : -INFINITY;
-				int idx = lane;
-				for(int k = 2; k <= 32; k <<= 1) {
-					for(int j = k >> 1; j > 0; j >>= 1) {
-						float ok = __shfl_xor_sync(FULL, key, j);
-						int oi = __shfl_xor_sync(FULL, idx, j);
-						bool desc = (lane & k) == 0;         /* descending runs first: a descending sort overall */
-						bool lower = (lane & j) == 0;
-						bool take = lower == desc ? (ok > key || (ok == key && oi < idx)) : (ok < key || (ok == key && oi > idx));
-						if(take) { key = ok; idx = oi; }
-					}
-				}
-				int sref = __shfl_sync(FULL, pref, idx), sobj = __shfl_sync(FULL, pobj, idx);
-				float ste = __shfl_sync(FULL, pte, idx);
-				if(lane < cnt) {
-					s_ref[w][sp + lane] = sref;
-					s_obj[w][sp + lane] = sobj;
-					s_te[w][sp + lane] = ste;
-				}
-				sp += cnt;
-				__syncwarp();
-			}
-			if(bail) res = 0;
-			else if(bobj < 0) res = 1;
-			else if(eq) res = 0;
-			else {
-				int ok = 1;
-				if(lane == 0) {
-					if(bslot >= 0 && !octree_reaches(S.mnodes, S.mprim, __ldg(S.bhome + bslot), object_ray(S, bobj, ti, wo, wd), bprim, best, true))
-						ok = 0;
-					else if(!octree_reaches(S.snodes, S.sslots, __ldg(S.ohome + bobj), wr, bobj, best, true))
-						ok = 0;
-				}
-				res = __shfl_sync(FULL, ok, 0);
-			}
-		}
+		float best;
+		int bobj, bprim;
+		int res = warp_trace<false>(S, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), q.meta[ri].w, s_ref[w], s_obj[w], s_te[w], best, bobj,
+				bprim);
 		if(lane == 0) {
 			if(!res) fb[1 + atomicAdd(fb, 1)] = ri;
 			else if(bobj >= 0) hits[ri] = make_int4(__float_as_int(best), bobj, bprim, 0);
@@ -902,6 +920,31 @@ __global__ void __launch_bounds__(SRAY_TRACE_THREADS, 6) k_shadow(DScene S, cons
 		if(HYB) atomicAdd(&ctr->rays[2], (unsigned long long)n);
 		else if(n > 0) atomicAdd(&ctr->bvh_fallbacks, (unsigned long long)n);
 	}
+}
+
+/* light samples with one warp per segment (as k_trace_warp), for passes of
+ * few samples */
+__global__ void __launch_bounds__(128) k_shadow_warp(DScene S, const ShadowReq *sq, const int *sq_count, float4 *acc, DevCounters *ctr,
+		int *fb)
+{
+	__shared__ int s_ref[4][WR_CAP];
+	__shared__ int s_obj[4][WR_CAP];
+	__shared__ float s_te[4][WR_CAP];
+	int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+	int n = *sq_count;
+	for(int ri = blockIdx.x * 4 + w; ri < n; ri += gridDim.x * 4) {
+		ShadowReq r = sq[ri];
+		float best;
+		int bobj, bprim;
+		int res = warp_trace<true>(S, mk(r.a.x, r.a.y, r.a.z), mk(r.b.x, r.b.y, r.b.z), __float_as_int(r.a.w), s_ref[w], s_obj[w], s_te[w],
+				best, bobj, bprim);
+		if(lane == 0) {
+			if(res == 2) fb[1 + atomicAdd(fb, 1)] = ri;
+			else if(res == 0) acc_add(acc, __float_as_int(r.b.w), r.w.x, r.w.y, r.w.z);
+		}
+		__syncwarp();
+	}
+	if(blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctr->rays[2], (unsigned long long)n);
 }
 
 /* ---------------------------------------------------------------- */
@@ -2501,7 +2544,9 @@ int Renderer::shadow_rays(int cap, cudaStream_t s)
 	float4 *a = acc.as<float4>();
 	DevCounters *c = ctr.as<DevCounters>();
 	int *f = fbl.as<int>();
-	if(tune.shadow_order)
+	if(cap <= tune.warp_rays)
+		LAUNCH(*this, "shadow", s, k_shadow_warp<<<grid_for(cap, 4), 128, 0, s>>>(S, q, cnt + 5, a, c, f));
+	else if(tune.shadow_order)
 		LAUNCH(*this, "shadow", s, k_shadow<true, false><<<g, 128, 0, s>>>(S, q, cnt + 5, a, c, f));
 	else
 		LAUNCH(*this, "shadow", s, k_shadow<true><<<g, 128, 0, s>>>(S, q, cnt + 5, a, c, f));
@@ -2894,11 +2939,11 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 	static const int tails[] = {0, 2048, 8192, 32768, 131072};
 	static const int pools[] = {2, 4, 8, 16};
 	static const int ptails[] = {16384, 65536, 262144, 1048576};
-	static const int binary[] = {0, 1}, prios[] = {0, 1, 2}, wrays[] = {0, 1024, 4096, 16384};
+	static const int binary[] = {0, 1}, prios[] = {0, 1, 2}, wrays[] = {0, 4096, 16384, 65536, 262144};
 	struct Knob { int sray_tuning::*field; const int *vals; int n; };
 	const Knob knobs[] = {{&sray_tuning::render_tail, tails, 5}, {&sray_tuning::pool_blocks_per_sm, pools, 4},
 		{&sray_tuning::photon_tail, ptails, 4}, {&sray_tuning::shadow_order, binary, 2}, {&sray_tuning::stream_priority, prios, 3},
-		{&sray_tuning::warp_rays, wrays, 4}};
+		{&sray_tuning::warp_rays, wrays, 5}};
 	std::vector<sray_tune_trial> done;
 	cudaEvent_t e0, e1;
 	if(cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) { g_err = "autotune events"; return SRAY_ECUDA; }
