@@ -284,10 +284,12 @@ int sray_gpu_kernel_times(char *names, size_t names_cap, double *ms, int64_t *la
 /* Scheduler tuning (extension, no reference counterpart; the reference's
  * scheduler is a thread pool over 48x48 tiles, src/tpool.cc:48-225).  The
  * queue depths at which a wavefront's tail is handed to a persistent launch,
- * and that launch's size. */
+ * that launch's size, thread- or warp-per-ray traversal by pass size, the
+ * any-hit child order and the streams' priorities.  The defaults are the
+ * autotuner's choice on the 1080p production frame. */
 typedef struct sray_tuning {
 	int render_tail;          /* rays in flight below which the rest of the shading tree
-	                             runs in the persistent pool launch (32768) */
+	                             runs in the persistent pool launch (0: none) */
 	int pool_blocks_per_sm;   /* 128-thread blocks per SM of the pool launch (4) */
 	int photon_tail;          /* photons in flight below which the photon tail runs in one
 	                             persistent launch (65536) */
@@ -296,9 +298,10 @@ typedef struct sray_tuning {
 	int stream_priority;      /* which of the two concurrent streams gets the device's
 	                             greatest priority: 0 neither, 1 the photon stream, 2 the
 	                             render work (on an internal stream ordered after and
-	                             before the caller's) (0) */
-	int warp_rays;            /* closest-hit passes of at most this many rays trace one
-	                             ray per warp instead of one per thread (0: never) (0) */
+	                             before the caller's) (2) */
+	int warp_rays;            /* closest-hit and light-sample passes of at most this many
+	                             rays trace one ray per warp instead of one per thread
+	                             (0: never) (16384) */
 	int reserved[2];
 } sray_tuning;
 
