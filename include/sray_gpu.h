@@ -299,10 +299,11 @@ typedef struct sray_tuning {
 	                             greatest priority: 0 neither, 1 the photon stream, 2 the
 	                             render work (on an internal stream ordered after and
 	                             before the caller's) (2) */
-	int warp_rays;            /* closest-hit and light-sample passes of at most this many
-	                             rays trace one ray per warp instead of one per thread
-	                             (0: never) (16384) */
-	int reserved[2];
+	int warp_rays;            /* closest-hit passes of at most this many rays trace one
+	                             ray per warp instead of one per thread (0: never) (16384) */
+	int warp_segments;        /* the same for light-sample passes of at most this many
+	                             segments (16384) */
+	int reserved[1];
 } sray_tuning;
 
 typedef struct sray_tune_trial {

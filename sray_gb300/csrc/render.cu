@@ -2544,7 +2544,7 @@ int Renderer::shadow_rays(int cap, cudaStream_t s)
 	float4 *a = acc.as<float4>();
 	DevCounters *c = ctr.as<DevCounters>();
 	int *f = fbl.as<int>();
-	if(cap <= tune.warp_rays)
+	if(cap <= tune.warp_segments)
 		LAUNCH(*this, "shadow", s, k_shadow_warp<<<grid_for(cap, 4), 128, 0, s>>>(S, q, cnt + 5, a, c, f));
 	else if(tune.shadow_order)
 		LAUNCH(*this, "shadow", s, k_shadow<true, false><<<g, 128, 0, s>>>(S, q, cnt + 5, a, c, f));
@@ -2904,6 +2904,7 @@ static int check_tuning(const sray_tuning *t)
 	if(t->shadow_order != 0 && t->shadow_order != 1) { g_err = "shadow_order must be 0 or 1"; return SRAY_EINVAL; }
 	if(t->stream_priority < 0 || t->stream_priority > 2) { g_err = "stream_priority must be 0, 1 or 2"; return SRAY_EINVAL; }
 	if(t->warp_rays < 0 || t->warp_rays > (1 << 24)) { g_err = "warp_rays must be 0..2^24"; return SRAY_EINVAL; }
+	if(t->warp_segments < 0 || t->warp_segments > (1 << 24)) { g_err = "warp_segments must be 0..2^24"; return SRAY_EINVAL; }
 	return 0;
 }
 
@@ -2943,7 +2944,7 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 	struct Knob { int sray_tuning::*field; const int *vals; int n; };
 	const Knob knobs[] = {{&sray_tuning::render_tail, tails, 5}, {&sray_tuning::pool_blocks_per_sm, pools, 4},
 		{&sray_tuning::photon_tail, ptails, 4}, {&sray_tuning::shadow_order, binary, 2}, {&sray_tuning::stream_priority, prios, 3},
-		{&sray_tuning::warp_rays, wrays, 5}};
+		{&sray_tuning::warp_rays, wrays, 5}, {&sray_tuning::warp_segments, wrays, 5}};
 	std::vector<sray_tune_trial> done;
 	cudaEvent_t e0, e1;
 	if(cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) { g_err = "autotune events"; return SRAY_ECUDA; }
@@ -2951,7 +2952,8 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 		for(const sray_tune_trial &d : done) {
 			if(d.tuning.render_tail == t.render_tail && d.tuning.pool_blocks_per_sm == t.pool_blocks_per_sm &&
 					d.tuning.photon_tail == t.photon_tail && d.tuning.shadow_order == t.shadow_order &&
-					d.tuning.stream_priority == t.stream_priority && d.tuning.warp_rays == t.warp_rays) {
+					d.tuning.stream_priority == t.stream_priority && d.tuning.warp_rays == t.warp_rays &&
+					d.tuning.warp_segments == t.warp_segments) {
 				*ms = d.ms_per_frame;
 				return 0;
 			}

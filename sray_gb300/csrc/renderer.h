@@ -139,7 +139,7 @@ struct Renderer {
 	cudaEvent_t ps_done = nullptr;
 	sray_stats stats;
 	/* the autotuner's choice on the production frame */
-	sray_tuning tune = {0, 4, 65536, 0, 2, 16384, {0, 0}};
+	sray_tuning tune = {0, 4, 65536, 0, 2, 16384, 16384, {0}};
 	int nsm = 0;                  /* multiprocessors of the device */
 
 	/* radiance cache: queries (inputs, weight + slot), training and
