@@ -303,7 +303,9 @@ typedef struct sray_tuning {
 	                             ray per warp instead of one per thread (0: never) (16384) */
 	int warp_segments;        /* the same for light-sample passes of at most this many
 	                             segments (16384) */
-	int reserved[1];
+	int side_gather;          /* 1: the first sample batch's photon-map gathers start as
+	                             soon as the maps exist, on a stream of their own beside
+	                             the remaining bounces (0) */
 } sray_tuning;
 
 typedef struct sray_tune_trial {

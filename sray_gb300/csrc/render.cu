@@ -1932,7 +1932,11 @@ int Renderer::start_photon_job(cudaStream_t s)
 	if(photon_thread.joinable()) return fail(SRAY_ESTATE, "photon maps already being traced");
 	photon_rc = 0;
 	DScene base = S;
-	photon_thread = std::thread([this, base]() { photon_rc = photon_job(base); });
+	photon_finished.store(false);
+	photon_thread = std::thread([this, base]() {
+		photon_rc = photon_job(base);
+		photon_finished.store(true);
+	});
 	return 0;
 }
 
@@ -2324,16 +2328,43 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 	 * for at most one). */
 	bool deferring = false;
 	int64_t gq_upper = 0, gq_defer_cap = 0;
+	/* side_gather: the accumulated gathers run on the gather stream from a
+	 * copy of their requests, beside the batch's remaining bounces, and the
+	 * batch waits for them before its accumulators are read */
+	bool side_pending = false;
+	struct SideJoin {
+		Renderer *R;
+		bool *pending;
+		~SideJoin() { if(*pending) cudaStreamSynchronize(R->gs); }
+	} side_join{this, &side_pending};
 	auto flush_gathers = [&]() -> int {
 		if(!deferring) return 0;
 		deferring = false;
 		int r = finish_photon_job();
 		if(r) return r;
-		if(gq_upper > 0)
+		if(gq_upper > 0 && tune.side_gather) {
+			if(int r2 = gather_stream()) return r2;
+			CK(gq_side.ensure((size_t)gq_upper * sizeof(GatherReq)), "side gather queue");
+			CK(cudaMemcpyAsync(gq_side.p, gq.p, (size_t)gq_upper * sizeof(GatherReq), cudaMemcpyDeviceToDevice, s), "side gathers");
+			CK(cudaMemcpyAsync(cnt + 24, cnt + 2, sizeof(int), cudaMemcpyDeviceToDevice, s), "side gather count");
+			CK(cudaEventRecord(gs_fork, s), "side gather fork");
+			CK(cudaStreamWaitEvent(gs, gs_fork, 0), "side gather fork");
+			LAUNCH(*this, "gather", gs, k_gather<<<grid_for((int)gq_upper, GATHER_WARPS), GATHER_WARPS * 32, 0, gs>>>(S,
+					gq_side.as<GatherReq>(), cnt + 24, acc.as<float4>(), ctr.as<DevCounters>()));
+			CK(cudaEventRecord(gs_done, gs), "side gather done");
+			side_pending = true;
+		} else if(gq_upper > 0) {
 			LAUNCH(*this, "gather", s, k_gather<<<grid_for((int)gq_upper, GATHER_WARPS), GATHER_WARPS * 32, 0, s>>>(S,
 					gq.as<GatherReq>(), cnt + 2, acc.as<float4>(), ctr.as<DevCounters>()));
+		}
 		gq_upper = 0;
 		CK(cudaMemsetAsync(cnt + 2, 0, sizeof(int), s), "reset gather queue");
+		return 0;
+	};
+	auto join_side = [&]() -> int {
+		if(!side_pending) return 0;
+		side_pending = false;
+		CK(cudaStreamWaitEvent(s, gs_done, 0), "side gather join");
 		return 0;
 	};
 	/* sample batches: the first covers the samples every pixel takes before
@@ -2372,6 +2403,10 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 		int cur = 0;
 		bool tail_done = false;
 		for(int depth = 0; n_rays > 0; depth++) {
+			/* side_gather: once the photon maps exist, the gathers queued so
+			 * far go out at the next bounce instead of the batch's end */
+			if(deferring && tune.side_gather && photon_finished.load())
+				if(int r = flush_gathers()) return r;
 			/* the pool holds every ray of the rest of the tree: enter it only
 			 * with POOL_HEADROOM times the rays' room in the queue */
 			if(depth >= 1 && !tail_done && n_rays <= tune.render_tail && (int64_t)n_rays * POOL_HEADROOM <= q[cur].cap) {
@@ -2460,6 +2495,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			cur ^= 1;
 		}
 		if(int r = flush_gathers()) return r;
+		if(int r = join_side()) return r;
 		if(int r = nrc_batch_done(b, s)) return r;
 		CK(cudaMemsetAsync(next_count, 0, sizeof(int), s), "reset next active");
 		LAUNCH(*this, "finish", s, k_finish<<<grid_for(n_active, 256), 256, 0, s>>>(act, act_count, s0, width, acc.as<float4>(),
@@ -2580,6 +2616,17 @@ int Renderer::photon_stream()
 	CK(cudaStreamCreateWithPriority(&ps, cudaStreamNonBlocking, want ? greatest : least), "photon stream");
 	ps_priority = want;
 	if(!ps_done) CK(cudaEventCreateWithFlags(&ps_done, cudaEventDisableTiming), "photon event");
+	return 0;
+}
+
+int Renderer::gather_stream()
+{
+	if(gs) return 0;
+	int least = 0, greatest = 0;
+	CK(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
+	CK(cudaStreamCreateWithPriority(&gs, cudaStreamNonBlocking, least), "gather stream");
+	CK(cudaEventCreateWithFlags(&gs_fork, cudaEventDisableTiming), "gather stream event");
+	CK(cudaEventCreateWithFlags(&gs_done, cudaEventDisableTiming), "gather stream event");
 	return 0;
 }
 
@@ -2905,6 +2952,7 @@ static int check_tuning(const sray_tuning *t)
 	if(t->stream_priority < 0 || t->stream_priority > 2) { g_err = "stream_priority must be 0, 1 or 2"; return SRAY_EINVAL; }
 	if(t->warp_rays < 0 || t->warp_rays > (1 << 24)) { g_err = "warp_rays must be 0..2^24"; return SRAY_EINVAL; }
 	if(t->warp_segments < 0 || t->warp_segments > (1 << 24)) { g_err = "warp_segments must be 0..2^24"; return SRAY_EINVAL; }
+	if(t->side_gather != 0 && t->side_gather != 1) { g_err = "side_gather must be 0 or 1"; return SRAY_EINVAL; }
 	return 0;
 }
 
@@ -2944,7 +2992,7 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 	struct Knob { int sray_tuning::*field; const int *vals; int n; };
 	const Knob knobs[] = {{&sray_tuning::render_tail, tails, 5}, {&sray_tuning::pool_blocks_per_sm, pools, 4},
 		{&sray_tuning::photon_tail, ptails, 4}, {&sray_tuning::shadow_order, binary, 2}, {&sray_tuning::stream_priority, prios, 3},
-		{&sray_tuning::warp_rays, wrays, 5}, {&sray_tuning::warp_segments, wrays, 5}};
+		{&sray_tuning::warp_rays, wrays, 5}, {&sray_tuning::warp_segments, wrays, 5}, {&sray_tuning::side_gather, binary, 2}};
 	std::vector<sray_tune_trial> done;
 	cudaEvent_t e0, e1;
 	if(cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) { g_err = "autotune events"; return SRAY_ECUDA; }
@@ -2953,7 +3001,7 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 			if(d.tuning.render_tail == t.render_tail && d.tuning.pool_blocks_per_sm == t.pool_blocks_per_sm &&
 					d.tuning.photon_tail == t.photon_tail && d.tuning.shadow_order == t.shadow_order &&
 					d.tuning.stream_priority == t.stream_priority && d.tuning.warp_rays == t.warp_rays &&
-					d.tuning.warp_segments == t.warp_segments) {
+					d.tuning.warp_segments == t.warp_segments && d.tuning.side_gather == t.side_gather) {
 				*ms = d.ms_per_frame;
 				return 0;
 			}
@@ -3364,6 +3412,13 @@ void sray_gpu_shutdown(void)
 	}
 	if(R.ps_done) cudaEventDestroy(R.ps_done);
 	if(R.ps) cudaStreamDestroy(R.ps);
+	if(R.gs) {
+		cudaStreamSynchronize(R.gs);
+		cudaStreamDestroy(R.gs);
+		cudaEventDestroy(R.gs_fork);
+		cudaEventDestroy(R.gs_done);
+	}
+	R.gq_side.release();
 	if(R.hs) {
 		cudaStreamSynchronize(R.hs);
 		cudaStreamDestroy(R.hs);

@@ -132,6 +132,11 @@ struct Renderer {
 	cudaStream_t ps = nullptr;
 	int ps_priority = -1;      /* 1 when ps has the greatest priority */
 	cudaStream_t hs = nullptr; /* the frame's stream under stream_priority 2 */
+	cudaStream_t gs = nullptr; /* the gather stream under side_gather */
+	cudaEvent_t gs_fork = nullptr, gs_done = nullptr;
+	DevBuf gq_side;            /* its copy of the accumulated gather requests */
+	std::atomic<bool> photon_finished{false};   /* the photon thread has returned */
+	int gather_stream();
 	cudaEvent_t hs_fork = nullptr, hs_join = nullptr;
 	int priority_stream();
 	int shadow_rays(int cap, cudaStream_t s);
@@ -139,7 +144,7 @@ struct Renderer {
 	cudaEvent_t ps_done = nullptr;
 	sray_stats stats;
 	/* the autotuner's choice on the production frame */
-	sray_tuning tune = {0, 4, 65536, 0, 2, 16384, 16384, {0}};
+	sray_tuning tune = {0, 4, 65536, 0, 2, 16384, 16384, 0};
 	int nsm = 0;                  /* multiprocessors of the device */
 
 	/* radiance cache: queries (inputs, weight + slot), training and

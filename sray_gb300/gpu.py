@@ -57,7 +57,7 @@ class SrayJob(ctypes.Structure):
 class SrayTuning(ctypes.Structure):
     _fields_ = [("render_tail", ctypes.c_int), ("pool_blocks_per_sm", ctypes.c_int), ("photon_tail", ctypes.c_int),
                 ("shadow_order", ctypes.c_int), ("stream_priority", ctypes.c_int), ("warp_rays", ctypes.c_int),
-                ("warp_segments", ctypes.c_int), ("reserved", ctypes.c_int * 1)]
+                ("warp_segments", ctypes.c_int), ("side_gather", ctypes.c_int)]
 
 
 class SrayTuneTrial(ctypes.Structure):
