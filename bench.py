@@ -58,7 +58,10 @@ def parse():
     ap.add_argument("--nrc-ladder", default="1,2,4,8,16,32,64,128",
                     help="diffuse samples per vertex of the plain final gather, compared with the cache")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-rows", type=int, default=24, help="rows of the CPU baseline sample")
+    ap.add_argument("--cpu-rows", type=int, default=4, help="rows per band of the CPU baseline sample (16 bands)")
+    ap.add_argument("--cpu-full-frame", action="store_true",
+                    help="reference arm: also render one whole frame on the CPU and compare it with the projection")
+    ap.add_argument("--no-parity", action="store_true", help="skip the untimed parity leg against the FP32 oracle")
     ap.add_argument("--res", default=None, help="WxH override (profiling runs on a reduced case)")
     ap.add_argument("--photon-scale", type=float, default=1.0, help="photon count multiplier (profiling)")
     return ap.parse_args()
@@ -189,42 +192,130 @@ def rays_of(st):
     return st["primary_rays"] + st["secondary_rays"] + st["shadow_rays"]
 
 
-def cpu_baseline(cfg, path, opts, rows, photon_frac, threads=0):
-    """The CPU restatement (FP64, all host threads) on a bounded sample of the
-    frame: the full photon maps (scaled by photon_frac) and a band of `rows`
-    image rows through the middle of the frame; extrapolated to the frame."""
-    from oracle.oracle import Oracle
-    o_opts = dict(opts)
-    o_opts["caust_photons"] = int(opts["caust_photons"] * photon_frac)
-    o_opts["gi_photons"] = int(opts["gi_photons"] * photon_frac)
-    o_opts["threads"] = threads
-    orc = Oracle(fp64=True, rng_mode=1, **o_opts)
-    orc.load(path)
+CPU_BANDS = 16
+
+
+def band_rows(h, n=CPU_BANDS, rows=4):
+    """n bands of `rows` image rows spread evenly over an image of h rows."""
+    step = max(h // n, rows)
+    return [(y, min(y + rows, h)) for y in range(step // 2 - rows // 2, h - rows + 1, step)][:n]
+
+
+def cpu_sample(orc, h, bands, threads=0):
+    """One bounded sample of the frame on the CPU restatement: prepare the
+    frame (scene tree, projection maps, photon maps at the oracle's photon
+    counts) and render the row bands.  Returns the phase times (s), the
+    rays traced on the bands and their image."""
+    import numpy as np
     t0 = time.perf_counter()
     orc.prepare(0)
     t_prep = time.perf_counter() - t0
-    h = opts["height"]
-    rows = min(rows, h)
-    y0 = (h - rows) // 2
+    ph = orc.phase_ms()
+    rows = [y for b0, b1 in bands for y in range(b0, b1)]
     t0 = time.perf_counter()
-    orc.render(0, rows=(y0, y0 + rows), nthreads=threads)
+    img = orc.render_rows(rows, nthreads=threads)
     t_rows = time.perf_counter() - t0
-    c = orc.counters()
-    scale_rows = h / rows
-    t_frame = t_prep / max(photon_frac, 1e-9) + t_rows * scale_rows
-    rays_frame = c["rays"] * scale_rows
+    rays = orc.counters()["rays"]
+    return {"prepare_s": t_prep, "build_s": ph["build"] / 1e3, "projmaps_s": ph["projmaps"] / 1e3,
+            "photons_s": ph["photons"] / 1e3, "rows_s": t_rows, "rays": rays,
+            "rows": sum(b1 - b0 for b0, b1 in bands), "image": img}
+
+
+def cpu_baseline(opts, path, bands, threads=0):
+    """The CPU restatement of the reference's path (FP64, all host threads)
+    on a bounded sample of the frame: the frame's full preparation (scene
+    tree, projection maps, both photon maps at full size: measured, not
+    extrapolated) and the rows of `bands` spread over the image; the frame
+    time is the preparation plus the rows' time scaled by the image's rows.
+    Also returns the FP64 image of the bands (the RMSE reference)."""
+    from oracle.oracle import Oracle
+    o_opts = dict(opts)
+    o_opts["threads"] = threads
+    orc = Oracle(fp64=True, rng_mode=1, **o_opts)
+    orc.load(path)
+    h = opts["height"]
+    smp = cpu_sample(orc, h, bands, threads)
+    scale_rows = h / smp["rows"]
+    t_frame = smp["prepare_s"] + smp["rows_s"] * scale_rows
+    rays_frame = smp["rays"] * scale_rows
     cores = threads if threads > 0 else (os.cpu_count() or 1)
     return {
         "value": rays_frame / t_frame / 1e6, "unit": "Mrays/s", "cores": cores, "kind": "port",
         "ms_per_frame": t_frame * 1e3,
-        "sample": "rows %d-%d of %d at full spp and the photon maps at %g of full size (%.1f s build+photons, "
-                  "%.1f s rows), extrapolated to the frame; CPU restatement of the reference's path in FP64"
-                  % (y0, y0 + rows, h, photon_frac, t_prep, t_rows),
-        "wall_s": t_prep + t_rows,
-    }
+        "sample": "the frame's full preparation measured (%.1f s: scene tree %.1f, projection maps %.1f, %d+%d photons "
+                  "traced and stored %.1f) and %d rows in %d bands spread over the %d-row image (%.1f s), the rows "
+                  "scaled to the image; CPU restatement of the reference's path in FP64"
+                  % (smp["prepare_s"], smp["build_s"], smp["projmaps_s"], opts["caust_photons"], opts["gi_photons"],
+                     smp["photons_s"], smp["rows"], len(bands), h, smp["rows_s"]),
+        "wall_s": smp["prepare_s"] + smp["rows_s"],
+        "phases_s": {k: round(smp[k], 3) for k in ("build_s", "projmaps_s", "photons_s", "rows_s")},
+    }, smp["image"]
+
+
+def fp64_image_check(img, ref, bands):
+    """The GPU frame's RMSE against the FP64 oracle (the reference's
+    arithmetic, same seeds and photon counts) on the row bands, and the
+    share of those pixels over 1e-3 relative."""
+    import numpy as np
+    rows = np.concatenate([np.arange(a, b) for a, b in bands])
+    a = np.asarray(img, np.float64)[rows, :, :3]
+    r = np.asarray(ref, np.float64)[rows, :, :3]
+    rel = np.abs(a - r) / np.maximum(np.abs(r), 1e-3)
+    return {"rmse": float(np.sqrt(np.mean((a - r) ** 2))), "pixels_over_1e-3": float((rel.max(-1) > 1e-3).mean()),
+            "rows": len(rows), "bands": [list(b) for b in bands],
+            "reference": "FP64 CPU oracle, same seeds and photon counts"}
+
+
+def parity_leg(opts, path, g, img, bands):
+    """Parity of the headline frame against the FP32 oracle (the GPU's
+    arithmetic, same seeds and photon counts), untimed: primary-hit ids of
+    every pixel (bit-exact except rays either side flags as an exact-t tie),
+    both photon maps as sets, and the image within 1e-3 relative on the row
+    bands."""
+    import numpy as np
+    import torch
+    from oracle.oracle import Oracle
+    H, W = opts["height"], opts["width"]
+    t_start = time.perf_counter()
+    o = Oracle(fp64=False, rng_mode=1, **opts)
+    o.load(path)
+    n = W * H
+    obj = torch.empty(n, dtype=torch.int32, device="cuda")
+    prim = torch.empty(n, dtype=torch.int32, device="cuda")
+    t = torch.empty(n, dtype=torch.float32, device="cuda")
+    tie = torch.empty(n, dtype=torch.uint8, device="cuda")
+    g.primary_hits(obj, prim, t, tie)
+    torch.cuda.synchronize()
+    gobj, gprim, gt, gtie = obj.cpu().numpy(), prim.cpu().numpy(), t.cpu().numpy(), tie.cpu().numpy()
+    oobj, oprim, ot, otie = o.primary_hits(0)
+    flagged = (gtie > 0) | (otie > 0)
+    mism = (gobj != oobj) | (gprim != oprim)
+    same_t = (oobj >= 0) & ~mism & ~flagged
+    maps = {}
+    for which, name in ((0, "caustic"), (1, "global")):
+        pg, po = g.photons(which), o.photons(which)
+        same = len(pg) == len(po) and np.array_equal(po[np.lexsort(po[:, :12].T[::-1]), :12],
+                                                      pg[np.lexsort(pg[:, :12].T[::-1]), :12])
+        maps[name] = {"gpu": int(len(pg)), "oracle": int(len(po)), "identical": bool(same)}
+    rows = np.concatenate([np.arange(a, b) for a, b in bands])
+    ref = o.render_rows(rows)
+    a = np.asarray(img, np.float64)[rows, :, :3]
+    r = ref[rows, :, :3].astype(np.float64)
+    rel = np.abs(a - r) / np.maximum(np.abs(r), 1e-3)
+    over = rel.max(-1) > 1e-3
+    return {"reference": "FP32 CPU oracle (the GPU's float arithmetic and path-keyed streams), same seeds and photon counts",
+            "pixels": int(n), "primary_hits": int((oobj >= 0).sum()),
+            "primary_mismatches": int(mism.sum()), "primary_unflagged_mismatches": int((mism & ~flagged).sum()),
+            "ties": int(flagged.sum()), "primary_t_bit_exact": bool(np.array_equal(gt[same_t], ot[same_t].astype(np.float32))),
+            "photon_maps": maps,
+            "image_rows": int(len(rows)), "image_bands": len(bands),
+            "image_pixels_over_1e-3": float(over.mean()), "image_max_rel": float(rel.max()),
+            "pass": bool((mism & ~flagged).sum() == 0 and over.mean() <= 1e-3),
+            "s": time.perf_counter() - t_start}
 
 
 REF_DS = 256
+REF_PHOTON_FRAC = 0.1
 REF_BANDS = 16
 
 
@@ -255,28 +346,6 @@ def oracle_reference_rows(opts, path, ds=REF_DS, bands=None, threads=0):
         ref[b[0]:b[1]] = img[b[0]:b[1]]
     rows = np.concatenate([np.arange(a, b) for a, b in bands])
     return ref, rows, time.perf_counter() - t0
-
-
-def production_image_check(opts, path, img, rows=16, threads=0):
-    """The frame's RMSE against the FP64 oracle (the reference's arithmetic,
-    same seeds, full photon maps) on a band of rows through the middle, and
-    the share of those pixels over 1e-3 relative."""
-    import numpy as np
-    from oracle.oracle import Oracle
-    o = dict(opts)
-    o["threads"] = threads
-    h = opts["height"]
-    y0 = (h - rows) // 2
-    t0 = time.perf_counter()
-    orc = Oracle(fp64=True, rng_mode=1, **o)
-    orc.load(path)
-    orc.prepare(0)
-    ref = np.asarray(orc.render(0, rows=(y0, y0 + rows), nthreads=threads), np.float64)[y0:y0 + rows, :, :3]
-    a = np.asarray(img, np.float64)[y0:y0 + rows, :, :3]
-    rel = np.abs(a - ref) / np.maximum(np.abs(ref), 1e-3)
-    return {"rmse": float(np.sqrt(np.mean((a - ref) ** 2))), "pixels_over_1e-3": float((rel.max(-1) > 1e-3).mean()),
-            "rows": [y0, y0 + rows], "s": time.perf_counter() - t0,
-            "reference": "FP64 CPU oracle, same seeds and photon counts"}
 
 
 def image_rmse(img, ref, rows):
@@ -477,32 +546,97 @@ def run_batch(args):
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of the reference's path (FP64,
+    every host thread) on the same workload.  A step is one bounded sample
+    of the frame: the frame's preparation (scene tree, projection maps and
+    both photon maps at REF_PHOTON_FRAC of full size) and one row from each
+    of 16 bands spread over the image.  The full frame's time is projected
+    from each step: the tree and projection maps as measured, the photon
+    phase from a line a + b * fraction fitted in the warm-up (photon maps at
+    two fractions), the rows scaled to the image.  ms_per_step is the
+    measured sample, projected_ms_per_frame the frame."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
     from sray_gb300 import scenegen
     from oracle import oracle as orc_mod
+    from oracle.oracle import Oracle
     orc_mod.build()
     opts = config_opts(args)
     path = scenegen.write_scene(args.config)
-    rows = max(4, args.cpu_rows // 2)
-    frac = 0.05 if args.config == "production" else 1.0
-    vals = []
+    H = opts["height"]
+    bands = band_rows(H, CPU_BANDS, 2)
+    cores = os.cpu_count() or 1
+    orc = Oracle(fp64=True, rng_mode=1, **dict(opts, threads=0))
+    t0 = time.perf_counter()
+    orc.load(path)
+    load_s = time.perf_counter() - t0
+    full = (opts["caust_photons"], opts["gi_photons"])
+    sampled = args.config in ("production", "stress")
+    f = REF_PHOTON_FRAC if sampled else 1.0
+
+    def at(frac):
+        orc.set_opts(caust_photons=int(round(full[0] * frac)), gi_photons=int(round(full[1] * frac)))
+
+    fit = None
+    if sampled:
+        # the photon phase against the photon count: two fractions, warm-up
+        pts = []
+        for frac in (f, 3 * f):
+            at(frac)
+            orc.prepare(0)
+            pts.append((frac, orc.phase_ms()["photons"] / 1e3))
+        b = (pts[1][1] - pts[0][1]) / (pts[1][0] - pts[0][0])
+        fit = {"photon_s_per_full_map": b, "photon_s_fixed": pts[0][1] - b * pts[0][0],
+               "points": [[round(x, 4), round(y, 4)] for x, y in pts]}
+    steps = []
+    t_run = time.perf_counter()
     for i in range(args.warmup + args.steps):
-        r = cpu_baseline(args.config, path, opts, rows, frac)
+        at(f)
+        t0 = time.perf_counter()
+        smp = cpu_sample(orc, H, bands)
+        wall = time.perf_counter() - t0
+        photons_full = smp["photons_s"] + (fit["photon_s_per_full_map"] * (1.0 - f) if fit else 0.0)
+        frame_s = smp["build_s"] + smp["projmaps_s"] + photons_full + smp["rows_s"] * H / smp["rows"]
+        rays = smp["rays"] * H / smp["rows"]
         if i >= args.warmup:
-            vals.append(r)
-    v = sum(r["value"] for r in vals) / len(vals)
-    ms = sum(r["ms_per_frame"] for r in vals) / len(vals)
+            steps.append({"wall_s": wall, "frame_s": frame_s, "rays": rays, "smp": smp})
+    run_s = time.perf_counter() - t_run
+    frame_ms = sum(x["frame_s"] for x in steps) / len(steps) * 1e3
+    v = sum(x["rays"] for x in steps) / sum(x["frame_s"] for x in steps) / 1e6
+    step_ms = sum(x["wall_s"] for x in steps) / len(steps) * 1e3
+    last = steps[-1]["smp"]
+    sample = ("each step: the frame's preparation with the photon maps at %g of full size (%d+%d photons) and %d rows "
+              "from %d bands spread over the %d-row image; the frame's time projected from it (scene tree and "
+              "projection maps as measured, the photon phase from a line fitted over photon maps at %g and %g of full "
+              "size, the rows scaled to the image); CPU restatement of the reference's path in FP64 on %d threads"
+              % (f, int(round(full[0] * f)), int(round(full[1] * f)), last["rows"], len(bands), H, f, 3 * f, cores)
+              if sampled else
+              "each step: the whole frame's preparation and %d rows from %d bands spread over the %d-row image, the rows "
+              "scaled to the image; CPU restatement of the reference's path in FP64 on %d threads"
+              % (last["rows"], len(bands), H, cores))
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "Mrays/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded scene)",
         "config": {"workload": workload_desc(args.config), "method": "plain gather"},
-        "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": vals[0]["cores"], "kind": "port",
-                         "sample": vals[0]["sample"]},
+        "projected_ms_per_frame": frame_ms,
+        "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "photon_fit": fit, "load_s": load_s, "timed_steps_s": run_s,
+        "phases_s_last_step": {k: round(last[k], 3) for k in ("build_s", "projmaps_s", "photons_s", "rows_s")},
+        "note": "ms_per_step is the measured sample of each step; value and projected_ms_per_frame are the whole frame "
+                "projected from it",
     }
+    if args.cpu_full_frame:
+        # the check of the projection: one whole frame (full photon maps, every row)
+        at(1.0)
+        t0 = time.perf_counter()
+        orc.prepare(0)
+        orc.render(0)
+        full_s = time.perf_counter() - t0
+        line["full_frame_check"] = {"measured_ms": full_s * 1e3, "projected_ms": frame_ms,
+                                    "projected_over_measured": frame_ms / (full_s * 1e3)}
     print(json.dumps(line))
     return 0
 
@@ -639,14 +773,22 @@ def run_ours(args):
             "prim_tests_per_ray": st_count["prim_tests"] / max(rays_traced, 1)}
 
     cpu = None
+    check = None
+    bands = band_rows(H, CPU_BANDS, args.cpu_rows)
     if rank == 0 and not args.no_cpu_baseline and args.config != "stress":
         try:
-            frac = 0.05 if args.config == "production" else 1.0
-            cb = cpu_baseline(args.config, path, opts, args.cpu_rows, frac)
-            cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+            cb, ref64 = cpu_baseline(opts, path, bands)
+            cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "ms_per_frame", "phases_s")}
+            check = fp64_image_check(host_fb, ref64, bands)
         except Exception as exc:  # the CPU baseline is a report, not the measurement
             cpu = {"value": None, "unit": "Mrays/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": "failed: %s" % exc}
+    parity = None
+    if rank == 0 and not args.no_parity and args.config in ("production", "small") and ws == 1:
+        try:
+            parity = parity_leg(opts, path, g, host_fb, band_rows(H, CPU_BANDS, 8))
+        except Exception as exc:  # reported beside the measurement
+            parity = {"error": str(exc)}
 
     # photons and gathers per second: of the frame, and of their own kernels
     ph_ms = sum(v[0] for k, v in kt.items() if k.startswith("photon")) / args.steps
@@ -659,13 +801,6 @@ def run_ours(args):
                   "gathers_per_s_of_gather_kernels": st_last["gathers"] / (ga_ms / 1e3) if ga_ms else None,
                   "note": "photon kernels run on their own stream beside the first bounce; per-frame rates use the "
                           "frame time, kernel rates the CUDA-event time of the photon / gather launches"}
-
-    check = None
-    if rank == 0 and not args.no_cpu_baseline and args.config != "stress":
-        try:
-            check = production_image_check(opts, path, fb.cpu().numpy())
-        except Exception as exc:  # reported, not the measurement
-            check = {"error": str(exc)}
 
     stress_cache = None
     if args.config == "stress" and not args.no_nrc:
@@ -748,6 +883,7 @@ def run_ours(args):
             "throughput": throughput,
             "primary_mrays_per_s": st_last["primary_rays"] / (ms_step / 1e3) / 1e6,
             "image_vs_fp64_oracle": check,
+            "parity": parity,
         }
         print(json.dumps(line))
     if nrc is None:

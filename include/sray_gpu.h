@@ -10,7 +10,8 @@
  * Conventions: every entry point returns 0 on success and a negative
  * SRAY_E* code on failure; sray_gpu_last_error() then returns a message.
  * No C++ types or exceptions cross this boundary.  One renderer context
- * per process, bound to the CUDA device current at sray_gpu_init().
+ * per process, bound to the CUDA device current at sray_gpu_init(); a call
+ * made while another device is current returns SRAY_ESTATE.
  * Functions that take a `stream` argument enqueue on that CUDA stream
  * (NULL = the legacy default stream) and return once the result is
  * available unless stated otherwise.
@@ -179,13 +180,15 @@ int sray_gpu_photon_gather(int which, int n, const float *pos, const float *norm
  * held on every GPU that loads the library until the process exits).
  *  - n > SRAY_NOALLOC_MAX_POINTS is rejected with SRAY_EINVAL.
  *  - The first call on a device looks up the array's device address on that
- *    device; make that first call before any stream capture.
+ *    device (the renderer's, which must be current); make that first call
+ *    before any stream capture.
  *  - All calls share the one array and it keeps the previous call's
  *    requests; each call writes all the requests it reads, so nothing needs
  *    clearing, but calls that overlap on the GPU (several host threads or
  *    streams at once) race on it.
- * Arguments, results and errors are those of sray_gpu_photon_gather; the
- * call returns when `out` is written. */
+ * Arguments, results and errors are those of sray_gpu_photon_gather.  Like
+ * it, the call waits for `stream` to finish its work (cudaStreamSynchronize)
+ * before it returns, so `out` is written on return. */
 #define SRAY_NOALLOC_MAX_POINTS 65536
 int sray_gpu_photon_gather_noalloc(int which, int n, const float *pos, const float *norm, float *out, void *stream);
 
@@ -305,7 +308,9 @@ typedef struct sray_tuning {
 	                             segments (16384) */
 	int side_gather;          /* 1: the first sample batch's photon-map gathers start as
 	                             soon as the maps exist, on a stream of their own beside
-	                             the remaining bounces (0) */
+	                             the remaining bounces; 2: the same, the render loop
+	                             waiting for the maps at the second bounce (a check of
+	                             that path independent of timing) (0) */
 } sray_tuning;
 
 typedef struct sray_tune_trial {

@@ -63,6 +63,10 @@ def lib():
         L.orc_cast_rays.argtypes = [vp, ip, vp, vp, vp, vp, vp, vp, vp]
         L.orc_gather.argtypes = [vp, ip, ip, vp, vp, vp]
         L.orc_counters.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.orc_set_pixel_base.argtypes = [vp, ip]
+        L.orc_render_row_list.argtypes = [vp, ctypes.c_long, ip, vp, vp, ip, ip, vp]
+        L.orc_set_opts.argtypes = [vp, ctypes.POINTER(SrayOpts)]
+        L.orc_phase_ms.argtypes = [vp, vp]
         _lib = L
     return _lib
 
@@ -131,6 +135,14 @@ class Oracle:
         self._chk(self.L.orc_render_rows(self.h, msec, y0, y1, _p(fb), nthreads, int(quirk_sum), _p(spp)))
         return (fb, spp) if want_spp else fb
 
+    def render_rows(self, rows, msec=0, nthreads=0, quirk_sum=False):
+        """The listed image rows (the rest of the returned image is zero)."""
+        o = self.opts
+        fb = np.zeros((o.height, o.width, 4), dtype=np.float32)
+        r = np.ascontiguousarray(rows, np.int32)
+        self._chk(self.L.orc_render_row_list(self.h, msec, len(r), _p(r), _p(fb), nthreads, int(quirk_sum), None))
+        return fb
+
     def primary_hits(self, msec=0):
         o = self.opts
         n = o.width * o.height
@@ -159,6 +171,24 @@ class Oracle:
         out = np.zeros((len(pos), 4), np.float64)
         self._chk(self.L.orc_gather(self.h, which, len(pos), _p(pos), _p(norm), _p(out)))
         return out
+
+    def set_opts(self, **kw):
+        """Change options of the loaded scene (photon counts, samples...);
+        the next call prepares the frame again."""
+        for k, v in kw.items():
+            setattr(self.opts, k, v)
+        self._chk(self.L.orc_set_opts(self.h, ctypes.byref(self.opts)))
+
+    def set_pixel_base(self, base):
+        """Key pixel p's streams as pixel base + p (a job of a GPU batch)."""
+        self._chk(self.L.orc_set_pixel_base(self.h, int(base)))
+
+    def phase_ms(self):
+        """(scene tree + frame tables, projection maps, photons) of the last
+        prepare, wall ms."""
+        ms = np.zeros(3, np.float64)
+        self._chk(self.L.orc_phase_ms(self.h, _p(ms)))
+        return dict(build=float(ms[0]), projmaps=float(ms[1]), photons=float(ms[2]))
 
     def counters(self):
         v = [ctypes.c_int64() for _ in range(5)]

@@ -9,6 +9,7 @@
  * (src/render.cc:194-244); everything they call is the reference's code.
  *
  * usage: ref_harness scene.xml out_prefix seed y0 y1 [reference options...]
+ *        ref_harness --time scene.xml reps [reference options...]
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -22,6 +23,9 @@
 #include "camera.h"
 #include "light.h"
 #include "opt.h"
+#include "img.h"
+#include "render.h"
+#include "timer.h"
 #undef private
 #undef protected
 #include "sray_rng.h"
@@ -45,8 +49,48 @@ static void dump_photons(const char *fname, PhotonMap &pm)
 	fclose(fp);
 }
 
+/* --time scene.xml reps [reference options...]: the reference's own frame
+ * entry point, rend_init + render(msec) (src/render.cc:22-55: build_accel,
+ * shoot_photons and render_frame on its pthread tpool), timed with its own
+ * get_msec (src/timer.c:13-25), reps times.  Prints one JSON line. */
+static int time_render(int argc, char **argv)
+{
+	const char *scene_path = argv[2];
+	int reps = atoi(argv[3]);
+	std::vector<char *> av;
+	av.push_back(argv[0]);
+	for(int i = 4; i < argc; i++) av.push_back(argv[i]);
+	av.push_back((char *)scene_path);
+	av.push_back(0);
+	if(parse_opt((int)av.size() - 1, av.data()) == -1) return 1;
+	opt.verb = -1;
+	Scene *scn = new Scene;
+	if(!scn->load(scene_path)) return 1;
+	if(!scn->get_camera()) scn->set_camera(new Camera);
+	set_scene(scn);
+	Image fb;
+	if(!fb.create(opt.width, opt.height)) return 1;
+	if(!rend_init(&fb)) return 1;
+	const char *ms_env = getenv("SRAY_REF_MSEC");
+	long msec = ms_env ? atol(ms_env) : 0;
+	std::vector<unsigned long> ms;
+	for(int i = 0; i < reps; i++) {
+		unsigned long t0 = get_msec();
+		render(msec);
+		ms.push_back(get_msec() - t0);
+	}
+	double sum = 0.0;
+	for(int i = 0; i < opt.width * opt.height * 4; i++) sum += fb.pixels[i];
+	/* on a line of its own: render() prints debug lines on stdout */
+	printf("\n{\"threads\": %d, \"width\": %d, \"height\": %d, \"render_ms\": [", opt.threads, opt.width, opt.height);
+	for(size_t i = 0; i < ms.size(); i++) printf("%s%lu", i ? ", " : "", ms[i]);
+	printf("], \"pixel_sum\": %.6g}\n", sum);
+	return 0;
+}
+
 int main(int argc, char **argv)
 {
+	if(argc >= 4 && strcmp(argv[1], "--time") == 0) return time_render(argc, argv);
 	if(argc < 6) {
 		fprintf(stderr, "usage: %s scene.xml out_prefix seed y0 y1 [options]\n", argv[0]);
 		return 1;

@@ -5,6 +5,8 @@
 #include <stdlib.h>
 #include <string.h>
 #include <algorithm>
+#include <atomic>
+#include <mutex>
 #include <utility>
 #include <vector>
 #include "vmath/vmath.h"
@@ -33,11 +35,18 @@ extern "C" int shim_rand(void) { return sray_rng_int(shim_rng_current()); }
 
 /* ---- kdtree ---- */
 struct kdpoint { float pos[3]; void *data; };
+/* The index (points sorted by the cell of the query radius) is built by the
+ * first query and reused while the radius stays the same.  Queries come from
+ * the reference's tpool workers at once (the real library's queries only
+ * read the tree), so the build runs under a lock and the others wait for it;
+ * a query with another radius rebuilds, which the reference never does
+ * while others query (each map has one gather radius per frame). */
 struct kdtree {
 	std::vector<kdpoint> pts;
 	void (*destr)(void *) = nullptr;
-	bool built = false;
+	std::atomic<bool> built{false};
 	double cell = 0.0;
+	std::mutex mu;
 	std::vector<std::pair<unsigned long long, int> > keys;
 };
 struct kdres {
@@ -50,6 +59,20 @@ static unsigned long long pack_key(long long x, long long y, long long z)
 	return ((unsigned long long)(x & 0x1fffff) << 42) | ((unsigned long long)(y & 0x1fffff) << 21) | (unsigned long long)(z & 0x1fffff);
 }
 
+static void build_index(struct kdtree *t, double cell)
+{
+	t->built.store(false, std::memory_order_release);
+	t->cell = cell;
+	t->keys.resize(t->pts.size());
+	for(size_t i = 0; i < t->pts.size(); i++) {
+		long long c[3];
+		for(int k = 0; k < 3; k++) c[k] = (long long)floor((double)t->pts[i].pos[k] / t->cell);
+		t->keys[i] = std::make_pair(pack_key(c[0], c[1], c[2]), (int)i);
+	}
+	std::sort(t->keys.begin(), t->keys.end());
+	t->built.store(true, std::memory_order_release);
+}
+
 extern "C" {
 
 struct kdtree *kd_create(int k) { return k == 3 ? new kdtree : nullptr; }
@@ -58,7 +81,7 @@ void kd_clear(struct kdtree *t)
 	if(t->destr) for(auto &p : t->pts) t->destr(p.data);
 	t->pts.clear();
 	t->keys.clear();
-	t->built = false;
+	t->built.store(false);
 }
 void kd_free(struct kdtree *t) { if(t) { kd_clear(t); delete t; } }
 void kd_data_destructor(struct kdtree *t, void (*d)(void *)) { t->destr = d; }
@@ -68,7 +91,7 @@ int kd_insert3f(struct kdtree *t, float x, float y, float z, void *data)
 	p.pos[0] = x; p.pos[1] = y; p.pos[2] = z;
 	p.data = data;
 	t->pts.push_back(p);
-	t->built = false;
+	t->built.store(false);
 	return 0;
 }
 
@@ -76,18 +99,13 @@ struct kdres *kd_nearest_range3f(struct kdtree *t, float x, float y, float z, fl
 {
 	kdres *r = new kdres;
 	double q[3] = {x, y, z}, rg = range, r2 = rg * rg;
-	if(!t->built || t->cell != rg) {
-		t->cell = rg > 0.0 ? rg : 1.0;
-		t->keys.resize(t->pts.size());
-		for(size_t i = 0; i < t->pts.size(); i++) {
-			long long c[3];
-			for(int k = 0; k < 3; k++) c[k] = (long long)floor((double)t->pts[i].pos[k] / t->cell);
-			t->keys[i] = std::make_pair(pack_key(c[0], c[1], c[2]), (int)i);
-		}
-		std::sort(t->keys.begin(), t->keys.end());
-		t->built = true;
+	double want = rg > 0.0 ? rg : 1.0;
+	if(!t->built.load(std::memory_order_acquire) || t->cell != want) {
+		std::lock_guard<std::mutex> lk(t->mu);
+		if(!t->built.load(std::memory_order_acquire) || t->cell != want) build_index(t, want);
 	}
 	long long lo[3], hi[3];
+
 	for(int k = 0; k < 3; k++) { lo[k] = (long long)floor((q[k] - rg) / t->cell); hi[k] = (long long)floor((q[k] + rg) / t->cell); }
 	for(long long a = lo[0]; a <= hi[0]; a++)
 	for(long long b = lo[1]; b <= hi[1]; b++)

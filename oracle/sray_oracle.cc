@@ -15,6 +15,7 @@
  * float-rounded radius), behind a uniform grid instead of a kd-tree, since
  * only the set of photons in range matters for the sums.
  */
+#include <chrono>
 #include <math.h>
 #include <float.h>
 #include <limits.h>
@@ -1198,6 +1199,7 @@ template <class R> static inline R fabsr(R a) { return a < (R)0 ? -a : a; }
 struct FrameBase {
 	virtual ~FrameBase() {}
 	virtual int render_rows(int y0, int y1, float *fb, int nthreads, int quirk, int *spp) = 0;
+	virtual int render_row_list(int n, const int *rows, float *fb, int nthreads, int quirk, int *spp) = 0;
 	virtual int primary_hits(int *obj, int *prim, double *t, unsigned char *tie) = 0;
 	virtual int cast_rays(int n, const double *o, const double *d, const int *tm, int *obj, int *prim, double *t, unsigned char *tie) = 0;
 	virtual int photons(int which, float *out, int cap) = 0;
@@ -1205,6 +1207,12 @@ struct FrameBase {
 	virtual int gather(int which, int n, const double *pos, const double *norm, double *out) = 0;
 	Counters ctr;
 	std::string err;
+	/* pixel index added to every pixel's stream key (a job of a batch keys
+	 * its pixels by their place in the batch's pixel space) */
+	uint32_t pix_base = 0;
+	/* wall time of the phases of the last prepare, ms: scene tree and
+	 * frame tables, projection maps, photon tracing and map build */
+	double ms_build = 0.0, ms_proj = 0.0, ms_photons = 0.0;
 };
 
 template <class R> struct Frame : FrameBase {
@@ -2343,6 +2351,8 @@ template <class R> struct Frame : FrameBase {
 	 * (src/scene.cc:445-534); every photon on its own stream */
 	void shoot(Scene &msc)
 	{
+		auto t_shoot = std::chrono::steady_clock::now();
+		ms_proj = ms_photons = 0.0;
 		caust.clear();
 		gi.clear();
 		if(!opt.caust_photons && !opt.gi_photons) return;
@@ -2356,9 +2366,12 @@ template <class R> struct Frame : FrameBase {
 			acc += intensity[i];
 			if(!msc.objs.empty()) build_proj(msc, i);
 		}
+		auto tp = std::chrono::steady_clock::now();
+		ms_proj = std::chrono::duration<double, std::milli>(tp - t_shoot).count();
 		for(int i = 0; i < nl; i++) power[i] = intensity[i] / acc;
 		shoot_map(0, power);
 		shoot_map(1, power);
+		ms_photons = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tp).count();
 	}
 
 	/* Light::build_proj_intern (src/light.cc:151-200) */
@@ -2479,7 +2492,7 @@ template <class R> struct Frame : FrameBase {
 			float *img = fb + ((size_t)py * opt.width + xs) * 4;
 			for(int x = 0; x < xsz; x++) {
 				int px = xs + x;
-				uint32_t pix = (uint32_t)(py * opt.width + px);
+				uint32_t lpix = (uint32_t)(py * opt.width + px), pix = pix_base + lpix;
 				img[x * 4] = img[x * 4 + 1] = img[x * 4 + 2] = img[x * 4 + 3] = 0.0f;
 				int i = 0;
 				C pixel;
@@ -2502,7 +2515,7 @@ template <class R> struct Frame : FrameBase {
 						if(v < opt.max_var) break;
 					}
 				}
-				if(spp) spp[pix] = i;
+				if(spp) spp[lpix] = i;
 				double rcp = 1.0 / (double)i;
 				if(quirk) {
 					img[x] = (float)(img[x] * rcp);
@@ -2543,6 +2556,40 @@ template <class R> struct Frame : FrameBase {
 		return 0;
 	}
 
+	/* the listed rows, one task per row and tile column (a thin sample of
+	 * rows spread over the image keeps every thread busy) */
+	int render_row_list(int n, const int *rows, float *fb, int nthreads, int quirk, int *spp) override
+	{
+		int bsz = opt.blk_sz > 0 ? opt.blk_sz : 48;
+		int xb = (opt.width + bsz - 1) / bsz;
+		std::vector<std::pair<int, int> > tasks;
+		for(int i = 0; i < n; i++) {
+			if(rows[i] < 0 || rows[i] >= opt.height) return SRAY_EINVAL;
+			for(int bx = 0; bx < xb; bx++) tasks.push_back(std::make_pair(bx, rows[i]));
+		}
+		if(nthreads <= 0) nthreads = (int)std::thread::hardware_concurrency();
+		if(nthreads <= 0) nthreads = 1;
+		std::atomic<size_t> next(0);
+		std::vector<Counters> cs(nthreads);
+		auto work = [&](int tid) {
+			for(;;) {
+				size_t k = next.fetch_add(1);
+				if(k >= tasks.size()) break;
+				int y = tasks[k].second;
+				render_block(tasks[k].first, y / bsz, y, y + 1, fb, quirk, spp, cs[tid]);
+			}
+		};
+		std::vector<std::thread> th;
+		for(int i = 1; i < nthreads; i++) th.push_back(std::thread(work, i));
+		work(0);
+		for(auto &t : th) t.join();
+		ctr = Counters();
+		for(auto &c : cs) {
+			ctr.rays += c.rays; ctr.nodes += c.nodes; ctr.prims += c.prims; ctr.shadow += c.shadow; ctr.gathers += c.gathers;
+		}
+		return 0;
+	}
+
 	int primary_hits(int *obj, int *prim, double *t, unsigned char *tie) override
 	{
 		ctr = Counters();
@@ -2558,7 +2605,7 @@ template <class R> struct Frame : FrameBase {
 				for(int x = 0; x < opt.width; x++) {
 					int i = row * opt.width + x;
 					sray_rng s;
-					sray_rng_init(&s, opt.seed, SRAY_DOM_PIXEL, (uint32_t)i, 0);
+					sray_rng_init(&s, opt.seed, SRAY_DOM_PIXEL, pix_base + (uint32_t)i, 0);
 					Ray<R> ray = primary(x, row, 0, t0, &s);
 					SurfPoint<R> sp;
 					int o = -1, p = -1;
@@ -2689,6 +2736,7 @@ struct Oracle {
 	bool loaded = false;
 	std::unique_ptr<FrameBase> frame;
 	long frame_msec = LONG_MIN;
+	uint32_t pix_base = 0;
 	std::string err;
 };
 
@@ -2698,18 +2746,21 @@ static int prepare(Oracle *o, long msec)
 	if(o->frame && o->frame_msec == msec) return 0;
 	int shutter = o->sc.cam.shutter;
 	int t0 = (int)(msec - shutter / 2), t1 = t0 + shutter;
+	auto tb = std::chrono::steady_clock::now();
 	build_scene_tree(o->sc, o->opt, t0, t1);
 	int lo = t0 - shutter - 2, hi = t1 + shutter + 2;
 	if(o->fp64) {
 		Frame<double> *f = new Frame<double>(o->sc, o->opt, o->rng_mode, msec);
 		f->t0 = t0; f->t1 = t1;
 		f->setup(lo, hi);
+		f->ms_build = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb).count();
 		f->shoot(o->sc);
 		o->frame.reset(f);
 	} else {
 		Frame<float> *f = new Frame<float>(o->sc, o->opt, o->rng_mode, msec);
 		f->t0 = t0; f->t1 = t1;
 		f->setup(lo, hi);
+		f->ms_build = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb).count();
 		f->shoot(o->sc);
 		o->frame.reset(f);
 	}
@@ -2792,7 +2843,17 @@ int orc_render_rows(void *h, long msec, int y0, int y1, float *fb, int nthreads,
 	Oracle *o = (Oracle *)h;
 	int r = prepare(o, msec);
 	if(r) return r;
+	o->frame->pix_base = o->pix_base;
 	return o->frame->render_rows(y0, y1, fb, nthreads, quirk_sum, spp_out);
+}
+
+int orc_render_row_list(void *h, long msec, int n, const int *rows, float *fb, int nthreads, int quirk_sum, int *spp_out)
+{
+	Oracle *o = (Oracle *)h;
+	int r = prepare(o, msec);
+	if(r) return r;
+	o->frame->pix_base = o->pix_base;
+	return o->frame->render_row_list(n, rows, fb, nthreads, quirk_sum, spp_out);
 }
 
 int orc_primary_hits(void *h, long msec, int *obj, int *prim, double *t, unsigned char *tie)
@@ -2800,7 +2861,39 @@ int orc_primary_hits(void *h, long msec, int *obj, int *prim, double *t, unsigne
 	Oracle *o = (Oracle *)h;
 	int r = prepare(o, msec);
 	if(r) return r;
+	o->frame->pix_base = o->pix_base;
 	return o->frame->primary_hits(obj, prim, t, tie);
+}
+
+int orc_set_opts(void *h, const sray_opts *opt)
+{
+	Oracle *o = (Oracle *)h;
+	if(o->loaded && (opt->meshoct_max_depth != o->opt.meshoct_max_depth || opt->meshoct_max_items != o->opt.meshoct_max_items)) {
+		o->err = "mesh octree options change needs a scene reload";
+		return SRAY_ESTATE;
+	}
+	o->opt = *opt;
+	o->frame.reset();
+	o->frame_msec = LONG_MIN;
+	return 0;
+}
+
+int orc_set_pixel_base(void *h, int base)
+{
+	Oracle *o = (Oracle *)h;
+	if(base < 0) { o->err = "negative pixel base"; return SRAY_EINVAL; }
+	o->pix_base = (uint32_t)base;
+	return 0;
+}
+
+int orc_phase_ms(void *h, double *ms)
+{
+	Oracle *o = (Oracle *)h;
+	if(!o->frame) { o->err = "no frame prepared"; return SRAY_ESTATE; }
+	ms[0] = o->frame->ms_build;
+	ms[1] = o->frame->ms_proj;
+	ms[2] = o->frame->ms_photons;
+	return 0;
 }
 
 int orc_cast_rays(void *h, int n, const double *orig, const double *dir, const int *time,

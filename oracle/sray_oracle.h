@@ -47,6 +47,10 @@ int orc_get_photons(void *h, int which, float *out, int cap);
 int orc_render_rows(void *h, long msec, int y0, int y1, float *fb, int nthreads,
 		int quirk_sum, int *spp_out);
 
+/* The same for the n listed rows (any order, each in [0, height)). */
+int orc_render_row_list(void *h, long msec, int n, const int *rows, float *fb, int nthreads,
+		int quirk_sum, int *spp_out);
+
 /* Primary ray (sample 0) closest hits of the prepared frame. */
 int orc_primary_hits(void *h, long msec, int *obj, int *prim, double *t, unsigned char *tie);
 
@@ -57,6 +61,20 @@ int orc_cast_rays(void *h, int n, const double *orig, const double *dir, const i
 /* Gathers at arbitrary points of the prepared frame: which = 0 caustic
  * irradiance_est, 1 global radiance_est.  out: n*4 doubles. */
 int orc_gather(void *h, int which, int n, const double *pos, const double *norm, double *out);
+
+/* Replace the options of a loaded oracle (photon counts, samples, ...; not
+ * the mesh octree options, which shape the loaded meshes).  The next call
+ * prepares the frame again. */
+int orc_set_opts(void *h, const sray_opts *opt);
+
+/* Offset added to every pixel index in the pixel sample streams' keys of
+ * later orc_render_rows / orc_primary_hits calls (a job of a GPU batch keys
+ * its pixels by their place in the batch).  Default 0. */
+int orc_set_pixel_base(void *h, int base);
+
+/* Wall time of the last frame preparation's phases, ms: ms[0] scene tree and
+ * frame tables, ms[1] projection maps, ms[2] photon tracing and map build. */
+int orc_phase_ms(void *h, double *ms);
 
 /* Work counters of the last orc_render_rows / orc_primary_hits call. */
 int orc_counters(void *h, int64_t *rays, int64_t *node_visits, int64_t *prim_tests,

@@ -719,7 +719,8 @@ int photon_map_build(Renderer &R, int global, int n, cudaStream_t s)
 	/* grid over the scene bounds: cells of the gather radius */
 	const Box &rb = R.sc.oct.nodes[0].box;
 	int k = global ? opt.gi_k : opt.caust_k;
-	double rad = k > 0 ? (double)opt.gather_rcap : R.sc.gather_dist;
+	/* a job of a batch gathers with the radius of its own interval */
+	double rad = k > 0 ? (double)opt.gather_rcap : (R.map_gather_dist >= 0.0 ? R.map_gather_dist : R.sc.gather_dist);
 	/* cells twice the gather radius: a query cube overlaps at most 2x2x2 */
 	double cell = rad > 0.0 ? 2.0 * rad : 1.0;
 	double ext[3];

@@ -1906,7 +1906,11 @@ int Renderer::photon_job(DScene base)
 	for(size_t j = 0; j < n; j++) {
 		base.t0 = batch_t0[j];
 		base.t1 = batch_t1[j];
+		/* the radius Scene::build_tree gives the job's own frame: the batch's
+		 * tree spans every job's interval */
+		map_gather_dist = sc.gather_dist_at(batch_t0[j], batch_t1[j], opt);
 		int r = shoot_maps(base, ps, &c, &g);
+		map_gather_dist = -1.0;
 		if(r) return r;
 		std::swap(caust, job_maps[j].caust);
 		std::swap(gi, job_maps[j].gi);
@@ -2404,8 +2408,10 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 		bool tail_done = false;
 		for(int depth = 0; n_rays > 0; depth++) {
 			/* side_gather: once the photon maps exist, the gathers queued so
-			 * far go out at the next bounce instead of the batch's end */
-			if(deferring && tune.side_gather && photon_finished.load())
+			 * far go out at the next bounce instead of the batch's end;
+			 * side_gather 2 waits for the maps at the second bounce, so that
+			 * this mid-batch path runs whatever the timing */
+			if(deferring && tune.side_gather && (photon_finished.load() || (tune.side_gather == 2 && depth >= 1)))
 				if(int r = flush_gathers()) return r;
 			/* the pool holds every ray of the rest of the tree: enter it only
 			 * with POOL_HEADROOM times the rays' room in the queue */
@@ -2712,7 +2718,28 @@ static cudaStream_t as_stream(void *s) { return (cudaStream_t)s; }
 
 using namespace sray;
 
-#define NEED_CTX() do { if(!g_R) { g_err = "sray_gpu_init has not been called"; return SRAY_ESTATE; } } while(0)
+/* The context belongs to the device that was current at sray_gpu_init:
+ * its buffers, streams and tables live there.  A call made while another
+ * device is current is refused instead of launching on the wrong one. */
+static int check_ctx_device()
+{
+	int dev = -1;
+	cudaError_t e = cudaGetDevice(&dev);
+	if(e != cudaSuccess) { g_err = std::string("cudaGetDevice: ") + cudaGetErrorString(e); return SRAY_ECUDA; }
+	if(dev != g_R->device) {
+		char msg[160];
+		snprintf(msg, sizeof msg, "CUDA device %d is current but the renderer was initialised on device %d; make it current first",
+				dev, g_R->device);
+		g_err = msg;
+		return SRAY_ESTATE;
+	}
+	return 0;
+}
+
+#define NEED_CTX() do { \
+		if(!g_R) { g_err = "sray_gpu_init has not been called"; return SRAY_ESTATE; } \
+		if(int r_dev_ = check_ctx_device()) return r_dev_; \
+	} while(0)
 
 extern "C" {
 
@@ -2952,7 +2979,7 @@ static int check_tuning(const sray_tuning *t)
 	if(t->stream_priority < 0 || t->stream_priority > 2) { g_err = "stream_priority must be 0, 1 or 2"; return SRAY_EINVAL; }
 	if(t->warp_rays < 0 || t->warp_rays > (1 << 24)) { g_err = "warp_rays must be 0..2^24"; return SRAY_EINVAL; }
 	if(t->warp_segments < 0 || t->warp_segments > (1 << 24)) { g_err = "warp_segments must be 0..2^24"; return SRAY_EINVAL; }
-	if(t->side_gather != 0 && t->side_gather != 1) { g_err = "side_gather must be 0 or 1"; return SRAY_EINVAL; }
+	if(t->side_gather < 0 || t->side_gather > 2) { g_err = "side_gather must be 0, 1 or 2"; return SRAY_EINVAL; }
 	return 0;
 }
 
@@ -3145,16 +3172,15 @@ static __device__ __align__(256) GatherReq g_noalloc_req[SRAY_NOALLOC_MAX_POINTS
 static GatherReq *g_noalloc_addr[64];
 static std::mutex g_noalloc_mu;
 
-static int noalloc_requests(GatherReq **out)
+/* the staging's address on the renderer's device (which the caller has
+ * made current: NEED_CTX refuses calls from another device) */
+static int noalloc_requests(int dev, GatherReq **out)
 {
-	int dev = 0;
-	cudaError_t e = cudaGetDevice(&dev);
-	if(e != cudaSuccess) { g_err = std::string("cudaGetDevice: ") + cudaGetErrorString(e); return SRAY_ECUDA; }
 	if(dev < 0 || dev >= 64) { g_err = "device index out of range for the fixed gather staging"; return SRAY_EINVAL; }
 	std::lock_guard<std::mutex> lk(g_noalloc_mu);
 	if(!g_noalloc_addr[dev]) {
 		void *p = nullptr;
-		e = cudaGetSymbolAddress(&p, g_noalloc_req);
+		cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_req);
 		if(e != cudaSuccess || !p) {
 			g_err = std::string("cudaGetSymbolAddress of the gather staging: ") + cudaGetErrorString(e);
 			return SRAY_ECUDA;
@@ -3180,7 +3206,7 @@ int sray_gpu_photon_gather_noalloc(int which, int n, const float *pos, const flo
 	}
 	if(n == 0) return 0;
 	GatherReq *req = nullptr;
-	int r = noalloc_requests(&req);
+	int r = noalloc_requests(R.device, &req);
 	if(r) return r;
 	cudaStream_t s = as_stream(stream);
 	k_pack_gather<<<grid_for(n, 256), 256, 0, s>>>(which, n, pos, norm, req);

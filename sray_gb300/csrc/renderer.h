@@ -161,6 +161,7 @@ struct Renderer {
 	struct JobMaps { PhotonBufs caust, gi; };
 	int batch_npix = 0;
 	std::vector<int> batch_t0, batch_t1;   /* jobs' shutter intervals: the photon job shoots one map pair each */
+	double map_gather_dist = -1.0;         /* >= 0: the range radius of the maps being built (a batch job's) */
 	DevBuf djobs, dmaps;
 	std::vector<JobMaps> job_maps;
 	int render_batch(const sray_job *jobs, int n, cudaStream_t s);

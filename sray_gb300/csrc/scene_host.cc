@@ -864,6 +864,24 @@ void HostScene::build_tree(int t0, int t1, const sray_opts &opt)
 	gather_dist = sqrt(dx * dx + dy * dy + dz * dz) * opt.gather_dist;
 }
 
+/* gather_dist of Scene::build_tree(t0, t1) (src/scene.cc:384-387): the
+ * diagonal of the union of every object's bounds at t0 and t1 (the scene
+ * octree's root box) times the option */
+double HostScene::gather_dist_at(int t0, int t1, const sray_opts &opt) const
+{
+	double mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+	for(size_t i = 0; i < objs.size(); i++) {
+		Box b[2] = {objs[i].bounds(meshes, t0), t1 == t0 ? objs[i].bounds(meshes, t0) : objs[i].bounds(meshes, t1)};
+		for(int j = 0; j < 2; j++)
+			for(int k = 0; k < 3; k++) {
+				if(b[j].mn[k] < mn[k]) mn[k] = b[j].mn[k];
+				if(b[j].mx[k] > mx[k]) mx[k] = b[j].mx[k];
+			}
+	}
+	double dx = mx[0] - mn[0], dy = mx[1] - mn[1], dz = mx[2] - mn[2];
+	return sqrt(dx * dx + dy * dy + dz * dz) * opt.gather_dist;
+}
+
 /* ------------------------------------------------------------------ */
 /* loading                                                               */
 /* ------------------------------------------------------------------ */

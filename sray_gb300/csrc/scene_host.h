@@ -179,6 +179,8 @@ struct HostScene {
 	bool load(const char *text, size_t len, const sray_opts &opt, std::string &err, const char *sidecar = nullptr,
 			bool *used = nullptr);
 	void build_tree(int t0, int t1, const sray_opts &opt);
+	/* the gather radius build_tree(t0, t1) would set, without building */
+	double gather_dist_at(int t0, int t1, const sray_opts &opt) const;
 	void build_projmaps(int t0, int t1, uint64_t seed);
 	void build_light_projmaps(size_t li, int t0, int t1, uint64_t seed);
 };

@@ -56,17 +56,27 @@ def test_primary_hits_bit_exact(small_pair):
     assert np.array_equal(gt[hit], ot[hit].astype(np.float32))
 
 
-def test_photon_maps_identical(small_pair):
-    g, o = small_pair()
-    o.prepare(0)
-    nc, ng = g.shoot_photons(0, 0)
-    ph_o = o.photons(0)
-    ph_g = g.photons(0)
-    print("caustic photons: oracle %d gpu %d" % (len(ph_o), len(ph_g)))
-    assert len(ph_o) == len(ph_g) == nc
+def _same_photons(ph_o, ph_g):
+    if len(ph_o) != len(ph_g):
+        return False
     ko = np.lexsort(ph_o[:, :12].T[::-1])
     kg = np.lexsort(ph_g[:, :12].T[::-1])
-    assert np.array_equal(ph_o[ko, :12], ph_g[kg, :12])
+    return np.array_equal(ph_o[ko, :12], ph_g[kg, :12])
+
+
+def test_photon_maps_identical(small_pair):
+    # caustic and global maps: the same photons (position, direction,
+    # normal, power) as sets
+    g, o = small_pair(gi_photons=60000)
+    o.prepare(0)
+    nc, ng = g.shoot_photons(0, 0)
+    for which, n in ((0, nc), (1, ng)):
+        ph_o = o.photons(which)
+        ph_g = g.photons(which)
+        same = _same_photons(ph_o, ph_g)
+        print("%s photons: oracle %d gpu %d identical %s" % (("caustic", "global")[which], len(ph_o), len(ph_g), same))
+        assert len(ph_g) == n > 0
+        assert same
 
 
 def _compare(img_g, img_o, label):
@@ -89,7 +99,7 @@ def test_image_small_scene(small_pair):
 
 @pytest.mark.parametrize("tuning", [dict(shadow_order=1), dict(stream_priority=1), dict(stream_priority=2),
                                     dict(warp_rays=1 << 24, warp_segments=1 << 24), dict(warp_rays=0, warp_segments=0),
-                                    dict(side_gather=1)])
+                                    dict(side_gather=1), dict(side_gather=2)])
 def test_tuning_keeps_the_image(small_pair, tuning):
     # light samples' any-hit traversal in node order instead of nearest
     # first; the photon stream or the frame's own stream given priority;
@@ -202,12 +212,10 @@ def test_textured_scene(textured_pair, tmp_path):
     nc, ng = g.shoot_photons(0, 0)
     for which, n in ((0, nc), (1, ng)):
         ph_o, ph_g = o.photons(which), g.photons(which)
-        ko = np.lexsort(ph_o[:, :12].T[::-1])
-        kg = np.lexsort(ph_g[:, :12].T[::-1])
-        same = len(ph_o) == len(ph_g) and np.array_equal(ph_o[ko, :12], ph_g[kg, :12])
+        same = _same_photons(ph_o, ph_g)
         print("%s photons: oracle %d gpu %d identical %s" % (("caustic", "global")[which], len(ph_o), len(ph_g), same))
         assert len(ph_g) == n
-        assert abs(len(ph_o) - len(ph_g)) <= max(2, len(ph_o) // 1000)
+        assert same
     img_g = g.render(0)
     img_o = o.render(0)
     assert _compare(img_g, img_o, "textured 128x96") <= 1e-3
@@ -429,3 +437,29 @@ def test_batch_jobs_match_single_frames(gpu_lib, small_scene_path):
         print("batch job %dx%d: max abs difference to its own frame %.3g" % (w, h, d))
         assert d <= 1e-5
     assert st["primary_rays"] == sum(w * h for w, h in sizes)
+
+
+def test_batch_jobs_match_oracle_mblur_gi_spp(gpu_lib, oracle_lib):
+    # a batch of the feature scene (motion blur over a 40 ms shutter, sphere
+    # and box lights with 2 samples, global photons with 2 final-gather rays,
+    # 1-4 adaptive jittered samples): jobs at different frame times and
+    # resolutions, each against the FP32 oracle's frame at its time with its
+    # pixels keyed by their place in the batch and its own photon maps
+    opts = dict(width=96, height=72, min_samples=1, max_samples=4, max_var=0.01, caust_photons=20000,
+                gi_photons=30000, iter=6, shadow_samples=2, diffuse_samples=2, mblur=1, shutter=40, gather_dist=0.02)
+    path = scenegen.write_scene("feature")
+    jobs = [(0, 96, 72), (40, 64, 48), (100, 128, 96)]    # the loaded aspect (4:3)
+    g = gpu_lib.GpuRenderer(**opts)
+    g.load(path)
+    fbs = [torch.zeros((h, w, 4), dtype=torch.float32, device="cuda") for _, w, h in jobs]
+    g.render_batch([(ms, fb) for (ms, _, _), fb in zip(jobs, fbs)])
+    st = g.stats()
+    assert st["samples"] > sum(w * h for _, w, h in jobs)          # some pixels took more than one sample
+    base = 0
+    for (ms, w, h), fb in zip(jobs, fbs):
+        o = oracle_lib.Oracle(fp64=False, rng_mode=1, **dict(opts, width=w, height=h))
+        o.load(path)
+        o.set_pixel_base(base)
+        img_o = o.render(ms)
+        assert _compare(fb.cpu().numpy(), img_o, "batch job %dx%d at %d ms (pixel base %d)" % (w, h, ms, base)) <= 1e-3
+        base += w * h
