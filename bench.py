@@ -188,6 +188,41 @@ def bf16_peak():
         return 1900.0
 
 
+def algorithmic_bytes(st):
+    """Algorithmic bytes of a frame per kernel kind, from the counted pass:
+    (bytes, units, unit name, description)."""
+    rays = st["primary_rays"] + st["secondary_rays"]
+    return {
+        "trace": (rays * (48 + 16) + st["node_visits"] * 128 + st["prim_tests"] * 48, rays, "rays",
+                  "48 B ray + 16 B hit per ray, 128 B per 4-wide node read, 48 B per triangle tested"),
+        "shadow": (st["shadow_rays"] * (48 + 16) + st["shadow_node_visits"] * 128 + st["shadow_prim_tests"] * 48,
+                   st["shadow_rays"], "segments",
+                   "48 B request + 16 B accumulator per light-sample segment, 128 B per node read, 48 B per triangle tested"),
+        "gather": (st["gathers"] * (48 + 16 + 64) + st["gather_tested"] * 16 + st["gather_candidates"] * 32,
+                   st["gathers"], "queries",
+                   "48 B request + 16 B accumulator + 8 cells x 8 B per query, 16 B position per photon tested, "
+                   "32 B more per photon within range"),
+    }
+
+
+PROFILE_TABLE = os.path.join(ROOT, "profiles", "roofline_kernels_960x540.md")
+
+
+def committed_profile(kind):
+    """Figures of the committed ncu capture for a kernel kind: machine-read
+    lines `<kind>.<figure>: <value>` in the profile summary."""
+    out = {"source": None}
+    try:
+        text = open(PROFILE_TABLE).read()
+    except OSError:
+        return out
+    out["source"] = os.path.relpath(PROFILE_TABLE, ROOT)
+    for key in ("dram_bytes_per_unit", "threads_per_instruction", "issue_active"):
+        m = re.search(r"^%s\.%s:\s*([0-9.eE+-]+)" % (re.escape(kind), key), text, re.M)
+        out[key] = float(m.group(1)) if m else None
+    return out
+
+
 def rays_of(st):
     return st["primary_rays"] + st["secondary_rays"] + st["shadow_rays"]
 
@@ -686,16 +721,14 @@ def run_ours(args):
         tuning = {"chosen": best, "autotuned": True, "best_ms_per_frame": best_ms, "frames_per_trial": 3,
                   "trials": [dict(t, ms=round(ms, 3)) for t, ms in trials]}
 
-    # untimed pass: traversal work of the closest-hit kernel (algorithmic bytes)
+    # untimed pass: traversal and gather work of the frame (algorithmic bytes)
     g.set_profiling(time_kernels=True, count_work=True)
     g.kernel_times(reset=True)
     g.render(0, fb, stream=stream)
     torch.cuda.synchronize()
     st_count = g.stats()
-    kt_count = g.kernel_times(reset=True)
-    trace_launches = max(kt_count.get("trace", (0.0, 1))[1], 1)
-    rays_traced = st_count["primary_rays"] + st_count["secondary_rays"]
-    trace_bytes = rays_traced * (48 + 16) + st_count["node_visits"] * 128 + st_count["prim_tests"] * 48
+    g.kernel_times(reset=True)
+    alg = algorithmic_bytes(st_count)
 
     # timed region: K frames, device timing on the launch stream, kernel events live
     g.set_profiling(time_kernels=True, count_work=False)
@@ -746,31 +779,44 @@ def run_ours(args):
     value = rays / (ms_total / 1e3) / 1e6
     e2e_value = e2e_rays / e2e_s / 1e6
 
-    # dominant kernel of the frame's own stream and its roofline (the photon
-    # kernels run beside it on a stream of lower priority: their event
-    # times include waiting for SM slots)
+    # the roofline of the kernels that bound the frame's own stream (the
+    # photon kernels run beside it on a stream of lower priority: their event
+    # times include waiting for SM slots); `roofline` is the dominant one's
     dom = max(((k, v) for k, v in kt.items() if not k.startswith("photon")), key=lambda kv: kv[1][0])
     hbm, src = peaks()
-    tr_ms, tr_n = kt.get("trace", (0.0, 1))
-    tr_avg_s = tr_ms / max(tr_n, 1) / 1e3
-    bytes_per_launch = trace_bytes / trace_launches
-    achieved = bytes_per_launch / tr_avg_s / 1e9 if tr_avg_s > 0 else 0.0
-    traffic = None
-    tf_path = os.path.join(ROOT, "profiles", "k_trace_traffic_production_1080p.md")
-    if os.path.exists(tf_path) and args.res is None and args.photon_scale == 1.0 and args.config == "production":
-        # DRAM bytes per render launch of this kernel from the committed ncu capture
-        with open(tf_path) as f:
-            m = re.search(r"render_dram_bytes_per_launch:\s*([0-9]+)", f.read())
-        traffic = int(m.group(1)) if m else None
-    roof = {"kernel": "k_trace (closest hit)", "bound": "hbm", "achieved": achieved, "peak": hbm,
-            "unit": "GB/s", "frac": achieved / hbm, "peak_source": src, "traffic": traffic,
-            "algorithmic_bytes_per_launch": bytes_per_launch,
-            "avg_launch_ms": tr_avg_s * 1e3, "dominant_kernel": dom[0],
-            "note": "algorithmic bytes = rays*64 + 4-wide hierarchy nodes read*128 + triangle records read*48 (counted "
-                    "pass); traffic = DRAM bytes per render launch from the committed ncu capture: the nodes and "
-                    "triangles are re-read from L1/L2, so DRAM traffic is a small fraction of the algorithmic bytes",
-            "node_records_per_ray": st_count["node_visits"] / max(rays_traced, 1),
-            "prim_tests_per_ray": st_count["prim_tests"] / max(rays_traced, 1)}
+    scaled = args.res is None and args.photon_scale == 1.0 and args.config == "production"
+    kernels = {}
+    for name, (bytes_frame, units, unit_name, desc) in alg.items():
+        k_ms, k_n = kt.get(name, (0.0, 0))
+        ms_frame = k_ms / args.steps
+        achieved = bytes_frame / (ms_frame / 1e3) / 1e9 if ms_frame > 0 else 0.0
+        launches_frame = k_n / args.steps
+        prof = committed_profile(name)
+        traffic = None
+        if prof.get("dram_bytes_per_unit") is not None and launches_frame > 0:
+            # DRAM bytes per unit of work from the committed small-case capture,
+            # scaled to this frame's units per launch
+            traffic = prof["dram_bytes_per_unit"] * units / launches_frame
+        kernels[name] = {
+            "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "peak_source": src, "traffic": traffic,
+            "algorithmic_bytes_per_launch": bytes_frame / launches_frame if launches_frame else None,
+            "avg_launch_ms": ms_frame / launches_frame if launches_frame else None,
+            "ms_per_frame": ms_frame, "launches_per_frame": launches_frame, unit_name + "_per_frame": units,
+            "algorithmic_bytes": desc,
+            "threads_per_instruction": prof.get("threads_per_instruction"), "issue_active": prof.get("issue_active"),
+            "profile": prof.get("source")}
+    dom_name = dom[0] if dom[0] in kernels else max(kernels, key=lambda k: kernels[k]["ms_per_frame"])
+    roof = dict(kernels[dom_name], kernel=dom_name, dominant_kernel=dom[0], kernels=kernels,
+                note="achieved = algorithmic bytes of the frame's launches (counted in an untimed pass) over their "
+                     "CUDA-event time in the timed frames; traffic = DRAM bytes per unit from the committed ncu capture "
+                     "of a smaller frame, times this frame's units per launch: the hierarchies and photon maps are "
+                     "re-read from L1/L2, so DRAM traffic is a small fraction of the algorithmic bytes and the kernels "
+                     "are bound by instruction issue at the SIMT efficiency beside each")
+    roof["node_records_per_ray"] = st_count["node_visits"] / max(st_count["primary_rays"] + st_count["secondary_rays"], 1)
+    roof["prim_tests_per_ray"] = st_count["prim_tests"] / max(st_count["primary_rays"] + st_count["secondary_rays"], 1)
+    if not scaled:
+        roof["note"] += " (reduced case: traffic from the capture is not scaled)"
 
     cpu = None
     check = None

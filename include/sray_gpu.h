@@ -223,7 +223,8 @@ typedef struct sray_stats {
 	int64_t gather_spills;         /* gathers whose candidates overflowed the on-chip cache */
 	int64_t bvh_fallbacks;         /* mesh hits found through the hierarchy that the
 	                                  octree did not confirm (traced by the octree) */
-	int reserved[2];
+	int64_t shadow_node_visits;    /* the same traversal work of the light samples' */
+	int64_t shadow_prim_tests;     /* any-hit passes (when counting is on) */
 } sray_stats;
 
 int sray_gpu_get_stats(sray_stats *st);
@@ -329,6 +330,30 @@ int sray_gpu_set_tuning(const sray_tuning *t);
  * into `log` (up to `log_cap`, count through `n_log`). */
 int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tuning *best, float *best_ms,
 		sray_tune_trial *log, int log_cap, int *n_log);
+
+/* Host-side fault injection for tests (extension, no reference
+ * counterpart; the reference's only failure handling is its signal
+ * handlers, src/sray.cc:85-89).  Nothing here makes a kernel fault, trap or
+ * hang: the injected conditions are ones the library already detects and
+ * reports, made to happen on demand.  Settings hold until changed (all zero
+ * but fail_alloc_after = -1 turns injection off).
+ *  - fail_alloc_after >= 0: that many more device allocations succeed, then
+ *    every one fails as out of memory; the call that needed it returns
+ *    SRAY_ENOMEM and the context stays usable.
+ *  - queue_cap > 0: the shading tree's child ray queue takes at most that
+ *    many rays; a frame that makes more returns SRAY_EDEVICE.
+ *  - pool_spin_limit > 0: polls of a slot before the persistent shading
+ *    pool (sray_tuning.render_tail) gives up waiting for work (default
+ *    about half a second); a frame whose wait runs out returns
+ *    SRAY_EDEVICE. */
+typedef struct sray_faults {
+	int fail_alloc_after;
+	int queue_cap;
+	int pool_spin_limit;
+	int reserved[5];
+} sray_faults;
+
+int sray_gpu_set_faults(const sray_faults *f);
 
 /* Copy the last error message (NUL-terminated, truncated to `cap`). */
 int sray_gpu_last_error(char *buf, size_t cap);

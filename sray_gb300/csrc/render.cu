@@ -763,7 +763,8 @@ __global__ void __launch_bounds__(128) k_shade(DScene S, RayQueue qi, const int4
  * whose slot is beyond every reservation leaves once no ray is in flight
  * (no more can come); every wait is bounded and sets the error word when
  * it runs out. */
-#define POOL_SPIN_LIMIT (1 << 22) /* polls of a slot before the pool gives up (about 0.5 s) */
+#define POOL_SPIN_LIMIT (1 << 22) /* polls of a slot before the pool gives up (about 0.5 s; a
+                                     sray_gpu_set_faults test lowers it) */
 #define POOL_HEADROOM 64          /* pool slots per ray it starts with */
 #define POOL_SHADOW (-0x7ffffff0)   /* iter of a pool item that is a light sample's shadow ray */
 
@@ -834,7 +835,7 @@ struct PoolEmitter {
 };
 
 __global__ void __launch_bounds__(128) k_render_pool(DScene S, RayQueue pool, int *ready, int *ctl, ShadeOut out, float4 *acc,
-		DevCounters *ctr)
+		DevCounters *ctr, int spin_limit)
 {
 	int overflow = 0;
 	PoolEmitter em;
@@ -853,7 +854,7 @@ __global__ void __launch_bounds__(128) k_render_pool(DScene S, RayQueue pool, in
 		int i = atomicAdd(&ctl[0], 1);
 		if(i >= pool.cap) break;
 		bool have = false;
-		for(int spin = 0; spin < POOL_SPIN_LIMIT; spin++) {
+		for(int spin = 0; spin < spin_limit; spin++) {
 			if(vready[i]) { have = true; break; }
 			if(vctl[2] == 0) {
 				__threadfence();
@@ -892,12 +893,13 @@ __global__ void __launch_bounds__(128) k_render_pool(DScene S, RayQueue pool, in
 /* shadow rays: the reference tests visibility with cast_ray(shadow_ray)
  * (src/shader.cc:266), a hit anywhere on the segment [eps, 1] blocks */
 /* shadow rays; HYB and fb as for k_trace */
-template <bool HYB, bool SORT = true>
+template <bool HYB, bool SORT = true, bool COUNT = false>
 __global__ void __launch_bounds__(SRAY_TRACE_THREADS, 6) k_shadow(DScene S, const ShadowReq *sq, const int *sq_count, float4 *acc,
 		DevCounters *ctr, int *fb)
 {
 	int n = HYB ? *sq_count : fb[0];
 	int overflow = 0;
+	TraceCounters tc = {0, 0};
 	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 		int ri = HYB ? i : fb[1 + i];
 		ShadowReq r = sq[ri];
@@ -905,7 +907,7 @@ __global__ void __launch_bounds__(SRAY_TRACE_THREADS, 6) k_shadow(DScene S, cons
 		int res;
 		if(HYB) {
 			Hit h;
-			res = trace_two_level<false, true, SORT>(S, mk(r.a.x, r.a.y, r.a.z), mk(r.b.x, r.b.y, r.b.z), time, h, nullptr, &overflow);
+			res = trace_two_level<COUNT, true, SORT>(S, mk(r.a.x, r.a.y, r.a.z), mk(r.b.x, r.b.y, r.b.z), time, h, &tc, &overflow);
 		} else {
 			res = trace_any_octree_impl(S, mk(r.a.x, r.a.y, r.a.z), mk(r.b.x, r.b.y, r.b.z), time, &overflow) ? 1 : 0;
 		}
@@ -916,6 +918,10 @@ __global__ void __launch_bounds__(SRAY_TRACE_THREADS, 6) k_shadow(DScene S, cons
 		if(res == 0) acc_add(acc, pixel, r.w.x, r.w.y, r.w.z);
 	}
 	if(overflow) atomicOr(&ctr->overflow, 1);
+	if(COUNT) {
+		atomicAdd(&ctr->snodes, tc.nodes);
+		atomicAdd(&ctr->sprims, tc.prims);
+	}
 	if(blockIdx.x == 0 && threadIdx.x == 0) {
 		if(HYB) atomicAdd(&ctr->rays[2], (unsigned long long)n);
 		else if(n > 0) atomicAdd(&ctr->bvh_fallbacks, (unsigned long long)n);
@@ -2434,6 +2440,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 				h2d += sizeof ctl_h;
 				ShadeOut so;
 				so.qo = q[cur ^ 1];
+				so.qo.cap = child_cap(so.qo.cap);
 				so.gq = gq.as<GatherReq>();
 				so.gq_count = cnt + 2;
 				so.gq_cap = (int)std::min<size_t>(gq.bytes / sizeof(GatherReq), (size_t)INT_MAX);
@@ -2442,7 +2449,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 				so.sq_cap = (int)std::min<size_t>(sq.bytes / sizeof(ShadowReq), (size_t)INT_MAX);
 				LAUNCH(*this, "render_pool", s, k_render_pool<<<nsm * tune.pool_blocks_per_sm, 128, 0, s>>>(S, q[cur],
 						pool_ready.as<int>(), ctl, so,
-						acc.as<float4>(), ctr.as<DevCounters>()));
+						acc.as<float4>(), ctr.as<DevCounters>(), g_faults.spin_limit.load() > 0 ? g_faults.spin_limit.load() : POOL_SPIN_LIMIT));
 				if(int r = shadow_rays(so.sq_cap, s)) return r;
 				LAUNCH(*this, "gather", s, k_gather<<<grid_for(so.gq_cap, GATHER_WARPS), GATHER_WARPS * 32, 0, s>>>(S,
 						gq.as<GatherReq>(), cnt + 2, acc.as<float4>(), ctr.as<DevCounters>()));
@@ -2453,6 +2460,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 				d2h += 2 * sizeof(int);
 				prof_collect();
 				if(h_err) return fail(SRAY_EDEVICE, "shading pool: a wait for work ran out");
+				if(h_cnt > so.qo.cap) return queue_overflow(h_cnt, so.qo.cap);
 				n_rays = h_cnt;
 				cur ^= 1;
 				continue;
@@ -2477,6 +2485,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			if(r) return r;
 			ShadeOut so;
 			so.qo = q[cur ^ 1];
+			so.qo.cap = child_cap(so.qo.cap);
 			so.gq = gq.as<GatherReq>();
 			so.gq_count = cnt + 2;
 			so.gq_cap = deferring ? (int)gq_defer_cap : n_rays;
@@ -2497,6 +2506,9 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			CK(cudaStreamSynchronize(s), "bounce");
 			d2h += sizeof(int);
 			prof_collect();
+			/* children beyond the queue were dropped (the count kept going):
+			 * the frame stops here rather than trace entries never written */
+			if(h_cnt > so.qo.cap) return queue_overflow(h_cnt, so.qo.cap);
 			n_rays = h_cnt;
 			cur ^= 1;
 		}
@@ -2534,11 +2546,14 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 	stats.d2h_bytes = d2h;
 	stats.node_visits = (int64_t)hc.nodes;
 	stats.prim_tests = (int64_t)hc.prims;
+	stats.shadow_node_visits = (int64_t)hc.snodes;
+	stats.shadow_prim_tests = (int64_t)hc.sprims;
 	stats.gather_tested = (int64_t)hc.g_tested;
 	stats.gather_candidates = (int64_t)hc.g_cand;
 	stats.gather_selects = (int64_t)hc.g_select;
 	stats.gather_spills = (int64_t)hc.g_spill;
 	stats.bvh_fallbacks = (int64_t)hc.bvh_fallbacks;
+	retrace_hint = stats.bvh_fallbacks;
 	if(overlap_photons && !sc.lights.empty()) stats.photons_emitted = (int64_t)opt.caust_photons + opt.gi_photons;
 	if(S.nrc.mode) {
 		nrc_expect = (int64_t)hc.nrc[0];
@@ -2547,6 +2562,21 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 	}
 	if(hc.overflow) return fail(SRAY_EDEVICE, "device queue or traversal stack overflow");
 	return 0;
+}
+
+/* the child queue's capacity as the emitters see it (an injected cap for
+ * the fault tests, else the allocation's) */
+int Renderer::child_cap(int cap) const
+{
+	int f = g_faults.queue_cap.load();
+	return f > 0 && f < cap ? f : cap;
+}
+
+int Renderer::queue_overflow(int count, int cap)
+{
+	char msg[160];
+	snprintf(msg, sizeof msg, "device ray queue overflow: %d child rays for a queue of %d", count, cap);
+	return fail(SRAY_EDEVICE, msg);
 }
 
 /* closest hits of the first n (upper bound; the queue's count decides)
@@ -2561,15 +2591,15 @@ int Renderer::trace_rays_with(const DScene &D, const RayQueue &qq, int n, const 
 	if(!count && n <= tune.warp_rays) {
 		/* a pass of few rays: one warp per ray */
 		LAUNCH(*this, name, s, k_trace_warp<<<grid_for(n, 4), 128, 0, s>>>(D, qq, hit_out, fb.as<int>()));
-		LAUNCH(*this, "octree_retrace", s, k_trace<false, false><<<152, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
+		LAUNCH(*this, "octree_retrace", s, k_trace<false, false><<<retrace_grid(), 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
 		return 0;
 	}
 	if(count) {
 		LAUNCH(*this, name, s, k_trace<true, true><<<g, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
-		LAUNCH(*this, "octree_retrace", s, k_trace<true, false><<<152, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
+		LAUNCH(*this, "octree_retrace", s, k_trace<true, false><<<retrace_grid(), 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
 	} else {
 		LAUNCH(*this, name, s, k_trace<false, true><<<g, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
-		LAUNCH(*this, "octree_retrace", s, k_trace<false, false><<<152, 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
+		LAUNCH(*this, "octree_retrace", s, k_trace<false, false><<<retrace_grid(), 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
 	}
 	return 0;
 }
@@ -2586,13 +2616,15 @@ int Renderer::shadow_rays(int cap, cudaStream_t s)
 	float4 *a = acc.as<float4>();
 	DevCounters *c = ctr.as<DevCounters>();
 	int *f = fbl.as<int>();
-	if(cap <= tune.warp_segments)
+	if(prof_flags & 2)   /* counting the traversal work: every pass thread per segment */
+		LAUNCH(*this, "shadow", s, k_shadow<true, true, true><<<g, 128, 0, s>>>(S, q, cnt + 5, a, c, f));
+	else if(cap <= tune.warp_segments)
 		LAUNCH(*this, "shadow", s, k_shadow_warp<<<grid_for(cap, 4), 128, 0, s>>>(S, q, cnt + 5, a, c, f));
 	else if(tune.shadow_order)
 		LAUNCH(*this, "shadow", s, k_shadow<true, false><<<g, 128, 0, s>>>(S, q, cnt + 5, a, c, f));
 	else
 		LAUNCH(*this, "shadow", s, k_shadow<true><<<g, 128, 0, s>>>(S, q, cnt + 5, a, c, f));
-	LAUNCH(*this, "octree_retrace", s, k_shadow<false><<<152, 128, 0, s>>>(S, q, cnt + 5, a, c, f));
+	LAUNCH(*this, "octree_retrace", s, k_shadow<false><<<retrace_grid(), 128, 0, s>>>(S, q, cnt + 5, a, c, f));
 	return 0;
 }
 
@@ -2708,6 +2740,7 @@ int Renderer::render_batch(const sray_job *jobs, int n, cudaStream_t s)
 	return 0;
 }
 
+FaultState g_faults;
 static Renderer *g_R = nullptr;
 static std::string g_err;
 static std::mutex g_mu;
@@ -3393,6 +3426,16 @@ int sray_gpu_kernel_times(char *names, size_t names_cap, double *ms, int64_t *la
 		}
 	}
 	if(reset) for(auto &k : R.ktimes) { k.ms = 0.0; k.launches = 0; }
+	return 0;
+}
+
+int sray_gpu_set_faults(const sray_faults *f)
+{
+	if(!f) { g_err = "null fault settings"; return SRAY_EINVAL; }
+	if(f->fail_alloc_after < -1 || f->queue_cap < 0 || f->pool_spin_limit < 0) { g_err = "bad fault settings"; return SRAY_EINVAL; }
+	g_faults.alloc_left.store(f->fail_alloc_after);
+	g_faults.queue_cap.store(f->queue_cap);
+	g_faults.spin_limit.store(f->pool_spin_limit);
 	return 0;
 }
 

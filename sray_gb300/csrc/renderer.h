@@ -14,6 +14,25 @@
 
 namespace sray {
 
+/* Host-side fault injection (sray_gpu_set_faults): the device allocations
+ * left before they fail as out of memory (-1: off), a cap on the shading
+ * tree's child queue, and the persistent pool's wait limit.  Nothing here
+ * makes a kernel fault, trap or hang. */
+struct FaultState {
+	std::atomic<int> alloc_left{-1};
+	std::atomic<int> queue_cap{0};
+	std::atomic<int> spin_limit{0};
+};
+extern FaultState g_faults;
+
+/* one device allocation under the injected failure count */
+static inline bool fault_alloc_fails()
+{
+	int left = g_faults.alloc_left.load();
+	while(left > 0 && !g_faults.alloc_left.compare_exchange_weak(left, left - 1)) {}
+	return left == 0;
+}
+
 /* a device allocation that only grows */
 struct DevBuf {
 	void *p = nullptr;
@@ -24,6 +43,7 @@ struct DevBuf {
 		if(p) cudaFree(p);
 		p = nullptr;
 		bytes = 0;
+		if(fault_alloc_fails()) return cudaErrorMemoryAllocation;
 		cudaError_t e = cudaMalloc(&p, n < 256 ? 256 : n);
 		if(e == cudaSuccess) bytes = n < 256 ? 256 : n;
 		return e;
@@ -78,6 +98,7 @@ struct DevCounters {
 	unsigned long long nodes, prims;
 	unsigned long long g_tested, g_cand, g_select, g_spill;   /* gather work */
 	unsigned long long bvh_fallbacks;   /* hierarchy hits the octree did not confirm */
+	unsigned long long snodes, sprims;  /* node records read and primitive tests of light samples */
 	unsigned long long nrc[4];          /* final-gather vertices, cached: sample batch 0, batch 1 */
 };
 
@@ -146,6 +167,18 @@ struct Renderer {
 	/* the autotuner's choice on the production frame */
 	sray_tuning tune = {0, 4, 65536, 0, 2, 16384, 16384, 0};
 	int nsm = 0;                  /* multiprocessors of the device */
+	/* Octree retraces follow every hierarchy pass and nearly always find no
+	 * ray listed (a couple a frame).  Their grid-stride launches are sized
+	 * from the last frame's count: one block when it was small, so that an
+	 * empty launch needs a single free slot instead of one on every SM
+	 * (beside the photon stream's blocks, a full-width launch waited for
+	 * SMs to drain).  Any count is traced correctly, only more slowly. */
+	std::atomic<int64_t> retrace_hint{0};   /* also read by the photon thread */
+	int retrace_grid() const
+	{
+		int64_t b = (retrace_hint.load(std::memory_order_relaxed) + 127) / 128;
+		return b < 1 ? 1 : (b > nsm ? nsm : (int)b);
+	}
 
 	/* radiance cache: queries (inputs, weight + slot), training and
 	 * validation records (inputs, targets, predictions), region statistics */
@@ -200,7 +233,7 @@ struct Renderer {
 	int cuda_fail(cudaError_t e, const char *where)
 	{
 		err = std::string(where) + ": " + cudaGetErrorString(e);
-		return SRAY_ECUDA;
+		return e == cudaErrorMemoryAllocation ? SRAY_ENOMEM : SRAY_ECUDA;
 	}
 
 	int upload_scene(cudaStream_t s);
@@ -211,6 +244,8 @@ struct Renderer {
 	 * waiting for them */
 	int render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t s, bool overlap_photons = false);
 	int ensure_queue(int which, int cap);
+	int child_cap(int cap) const;
+	int queue_overflow(int count, int cap);
 	int ensure_pqueue(int which, int cap);
 	int queue_alloc(DevBuf &buf, RayQueue &Q, int &qc, int cap);
 	int trace_rays(const RayQueue &q, int n, const char *name, bool count, cudaStream_t s);

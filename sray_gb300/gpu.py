@@ -21,7 +21,7 @@ EXPORTS = ["sray_default_opts", "sray_gpu_init", "sray_gpu_set_opts", "sray_gpu_
            "sray_gpu_get_photons", "sray_gpu_dump_photons", "sray_gpu_restore_photons", "sray_gpu_render_batch",
            "sray_gpu_get_stats", "sray_gpu_nrc_stats", "sray_gpu_nrc_reset", "sray_gpu_get_tuning",
            "sray_gpu_set_tuning", "sray_gpu_autotune", "sray_gpu_set_profiling", "sray_gpu_kernel_times", "sray_gpu_last_error",
-           "sray_gpu_shutdown", "sray_nrc_reset", "sray_nrc_set_params", "sray_nrc_get_params", "sray_nrc_infer",
+           "sray_gpu_shutdown", "sray_gpu_set_faults", "sray_nrc_reset", "sray_nrc_set_params", "sray_nrc_get_params", "sray_nrc_infer",
            "sray_nrc_gradients", "sray_nrc_train", "sray_nrc_last_error"]
 
 NRC_PARAMS = 26563
@@ -38,7 +38,7 @@ class SrayStats(ctypes.Structure):
                 ("gather_tested", ctypes.c_int64), ("gather_candidates", ctypes.c_int64),
                 ("gather_selects", ctypes.c_int64), ("gather_spills", ctypes.c_int64),
                 ("bvh_fallbacks", ctypes.c_int64),
-                ("reserved", ctypes.c_int * 2)]
+                ("shadow_node_visits", ctypes.c_int64), ("shadow_prim_tests", ctypes.c_int64)]
 
 
 class SrayNrcStats(ctypes.Structure):
@@ -52,6 +52,11 @@ class SrayNrcStats(ctypes.Structure):
 class SrayJob(ctypes.Structure):
     _fields_ = [("msec", ctypes.c_long), ("width", ctypes.c_int), ("height", ctypes.c_int), ("fb", ctypes.c_void_p),
                 ("reserved", ctypes.c_int * 4)]
+
+
+class SrayFaults(ctypes.Structure):
+    _fields_ = [("fail_alloc_after", ctypes.c_int), ("queue_cap", ctypes.c_int), ("pool_spin_limit", ctypes.c_int),
+                ("reserved", ctypes.c_int * 5)]
 
 
 class SrayTuning(ctypes.Structure):
@@ -69,7 +74,15 @@ def _tuning_dict(t):
 
 
 class SrayError(RuntimeError):
-    pass
+    """A failed call: the library's message and its SRAY_E* code."""
+
+    def __init__(self, msg, code=None):
+        super().__init__(msg)
+        self.code = code
+
+
+# the library's status codes (include/sray_gpu.h)
+SRAY_EINVAL, SRAY_ELOAD, SRAY_ECUDA, SRAY_ESTATE, SRAY_EDEVICE, SRAY_ENOMEM, SRAY_EIO = -1, -2, -3, -4, -5, -6, -7
 
 
 def lib_path():
@@ -115,6 +128,7 @@ def load_library():
     L.sray_gpu_set_profiling.argtypes = [ip]
     L.sray_gpu_kernel_times.argtypes = [ctypes.c_char_p, ctypes.c_size_t, vp, vp, ip, vp, ip]
     L.sray_gpu_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    L.sray_gpu_set_faults.argtypes = [ctypes.POINTER(SrayFaults)]
     L.sray_gpu_shutdown.argtypes = []
     L.sray_gpu_shutdown.restype = None
     L.sray_nrc_reset.argtypes = [ctypes.c_uint64]
@@ -196,7 +210,7 @@ class GpuRenderer:
         if r != 0:
             buf = ctypes.create_string_buffer(1024)
             self.L.sray_gpu_last_error(buf, 1024)
-            raise SrayError("%s (code %d)" % (buf.value.decode(errors="replace"), r))
+            raise SrayError("%s (code %d)" % (buf.value.decode(errors="replace"), r), r)
         return r
 
     def set_opts(self, **kw):
@@ -326,6 +340,12 @@ class GpuRenderer:
     def nrc_reset(self, seed=None):
         """Re-initialise the network and forget the regions' validation history."""
         self._chk(self.L.sray_gpu_nrc_reset(self.opts.seed if seed is None else seed))
+
+    def set_faults(self, fail_alloc_after=-1, queue_cap=0, pool_spin_limit=0):
+        """Host-side fault injection for tests (sray_gpu_set_faults); the
+        defaults turn it off."""
+        f = SrayFaults(fail_alloc_after, queue_cap, pool_spin_limit)
+        self._chk(self.L.sray_gpu_set_faults(ctypes.byref(f)))
 
     def tuning(self):
         t = SrayTuning()

@@ -203,6 +203,13 @@ def small_scene(seed=0x5EED0001):
     return "".join(out)
 
 
+def small_xml_without_specular(seed=0x5EED0001):
+    """The small scene with no reflective or refractive material: a light's
+    projection map of specular objects is empty (coverage 0)."""
+    return "".join(line for line in small_scene(seed).splitlines(True)
+                   if 'name="reflect"' not in line and 'name="refract"' not in line)
+
+
 def production_scene(seed=0x5EED0002, grid=(1000, 500), extent=(100.0, 50.0), n_inst=200):
     """The 1080p scene: displaced-grid terrain of 2*grid[0]*grid[1] triangles
     (6-octave value noise, amplitude 2), n_inst subdivision-3 icosphere

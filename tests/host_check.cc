@@ -8,6 +8,9 @@
  *   keyframes XForm::matrix at the key times equals the node matrix of the
  *             keys; linear keys repeated past the last key are periodic;
  *             step keys hold between keys; clamped tracks hold the end keys
+ *   documents malformed or inconsistent scene documents (empty, truncated,
+ *             unbalanced tags, unknown types, dangling references, face
+ *             indices out of range) are refused with a message
  * Usage: host_check <scratch dir> <animated scene xml> */
 #include <math.h>
 #include <stdio.h>
@@ -186,6 +189,41 @@ static void check_keyframes(const char *scene)
 	CHECK(checked > 10);
 }
 
+/* malformed documents: every one is refused with a message, none crashes
+ * (the reference's loader prints and returns false, src/scene.cc:79-90) */
+static void check_bad_documents(const char *good_path)
+{
+	std::string good = slurp(good_path);
+	CHECK(good.size() > 200);
+	struct Case { const char *what; std::string text; const char *needle; };
+	std::vector<Case> cases = {
+		{"empty", "", "no root element"},
+		{"not xml", "this is not a scene", "no root element"},
+		{"truncated", good.substr(0, good.size() / 2), "end of document"},
+		{"unclosed", "<scene><material name=\"m\"></scene>", "mismatched closing tag"},
+		{"bad attribute", "<scene><material name=m/></scene>", "unquoted attribute value"},
+		{"unknown object", "<scene><object name=\"o\" type=\"torus\"/></scene>", "unknown type"},
+		{"missing material", "<scene><object name=\"o\" type=\"sphere\"><matref name=\"nope\"/><sphere rad=\"1.0\"/></object></scene>",
+			"does not exist"},
+		{"face index", "<scene><object name=\"m\" type=\"mesh\"><mesh><vertex id=\"0\" val=\"0 0 0\"/>"
+			"<vertex id=\"1\" val=\"1 0 0\"/><vertex id=\"2\" val=\"0 1 0\"/>"
+			"<face><vref vertex=\"0\"/><vref vertex=\"1\"/><vref vertex=\"7\"/></face></mesh></object></scene>",
+			"out of range"},
+		{"light type", "<scene><light type=\"spot\"/></scene>", "unknown type"},
+	};
+	for(const Case &c : cases) {
+		HostScene sc;
+		std::string err;
+		bool ok = sc.load(c.text.data(), c.text.size(), host_opts(), err);
+		printf("bad document (%s): %s\n", c.what, ok ? "LOADED" : err.c_str());
+		CHECK(!ok);
+		CHECK(err.find(c.needle) != std::string::npos);
+	}
+	HostScene sc;
+	std::string err;
+	CHECK(sc.load(good.data(), good.size(), host_opts(), err));
+}
+
 int main(int argc, char **argv)
 {
 	if(argc < 3) {
@@ -194,6 +232,7 @@ int main(int argc, char **argv)
 	}
 	check_textures(argv[1]);
 	check_keyframes(argv[2]);
+	check_bad_documents(argv[2]);
 	if(failures) {
 		printf("%d failures\n", failures);
 		return 1;

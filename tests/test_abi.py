@@ -28,9 +28,9 @@ def test_struct_layouts_match_header(tmp_path):
     """The ctypes mirrors have the header's sizes and field offsets."""
     import subprocess
     from sray_gb300.options import SrayOpts
-    from sray_gb300.gpu import SrayStats, SrayNrcStats, SrayTuning, SrayTuneTrial, SrayJob
+    from sray_gb300.gpu import SrayStats, SrayNrcStats, SrayTuning, SrayTuneTrial, SrayJob, SrayFaults
     mirrors = {"sray_opts": SrayOpts, "sray_stats": SrayStats, "sray_nrc_stats": SrayNrcStats, "sray_tuning": SrayTuning,
-               "sray_tune_trial": SrayTuneTrial, "sray_job": SrayJob}
+               "sray_tune_trial": SrayTuneTrial, "sray_job": SrayJob, "sray_faults": SrayFaults}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "sray_gpu.h"', "int main(void) {"]
     for cname, py in mirrors.items():
         lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
