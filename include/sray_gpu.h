@@ -108,6 +108,108 @@ int sray_gpu_load_scene_mem(const char *xml, size_t len);
  * the side-car was used. */
 int sray_gpu_load_scene_sidecar(const char *xml_path, const char *sidecar, int *used);
 
+/* ---- A scene given as tables (instead of an XML document) ----
+ * The scene classes of the reference -- Scene (src/scene.h:36-130), Object
+ * with Sphere / Cylinder / Mesh (src/object.h:40-85, src/sphere.h,
+ * src/cylinder.h, src/mesh.h:25-62), Material with its attributes
+ * (src/material.h:29-101), Light with SphLight / BoxLight (src/light.h:42-121),
+ * Camera / TargetCamera (src/camera.h:26-90) and the keyframe tracks of
+ * XFormNode (src/anim.h) -- flattened into plain arrays, so that a scene built
+ * or changed in memory reaches the GPU without an XML round trip.  All
+ * pointers are host memory, read during the call only. */
+
+/* One keyframe track (src/anim.h Track<T>): key times (ms, ascending) and
+ * values (3 doubles per key for position and scale, 4 for rotation as a
+ * quaternion s, x, y, z); interpolation 0 step, 1 linear, 2 cubic;
+ * extrapolation 0 clamp, 1 repeat.  nkeys = 0: the track's default
+ * (position 0, identity rotation, unit scale). */
+typedef struct sray_track_desc {
+	int nkeys;
+	int interp, extrap;
+	const int *time;
+	const double *val;
+} sray_track_desc;
+
+/* An XFormNode: position, rotation and scale tracks and the pivot
+ * (src/anim.cc:391-419 builds pivot * T * R * S * -pivot from them). */
+typedef struct sray_xform_desc {
+	sray_track_desc pos, rot, scale;
+	double pivot[3];
+} sray_xform_desc;
+
+/* material attributes, in the order of sray_material_desc.attr */
+enum { SRAY_ATTR_DIFFUSE, SRAY_ATTR_SPECULAR, SRAY_ATTR_SHININESS, SRAY_ATTR_REFLECT, SRAY_ATTR_REFRACT,
+	SRAY_ATTR_IOR, SRAY_ATTR_NORMAL, SRAY_ATTR_COUNT };
+
+/* A texture image: RGBA floats, rows top first (src/img.h Image). */
+typedef struct sray_texture_desc {
+	int width, height;
+	const float *pixels;
+} sray_texture_desc;
+
+typedef struct sray_material_desc {
+	const char *name;
+	int phong;                      /* 1: shade_phong; 0: shade_undef (src/shader.cc:36-73) */
+	struct {
+		int present;                /* the material has this attribute (Material::have_attribute) */
+		double col[4];              /* its colour (MatAttrib::col; scalars in x) */
+		int texture;                /* index into sray_scene_desc.textures, -1: none */
+	} attr[SRAY_ATTR_COUNT];
+} sray_material_desc;
+
+enum { SRAY_OBJ_SPHERE = 0, SRAY_OBJ_CYLINDER = 1, SRAY_OBJ_MESH = 2 };
+
+typedef struct sray_object_desc {
+	const char *name;
+	int type;                       /* SRAY_OBJ_* */
+	int material;                   /* index into sray_scene_desc.materials, -1: the default */
+	sray_xform_desc xform;
+	double rad, start, end;         /* sphere radius; cylinder radius and y range [start, end) */
+	int nfaces;                     /* mesh: triangles, each with its own three vertices
+	                                   (src/mesh.h:30-41 Triangle::v) in object space */
+	const double *pos;              /* nfaces * 9 */
+	const double *normal;           /* nfaces * 9, NULL: zero */
+	const double *tangent;          /* nfaces * 9, NULL: zero */
+	const double *texcoord;         /* nfaces * 6, NULL: zero */
+} sray_object_desc;
+
+enum { SRAY_LIGHT_POINT = 0, SRAY_LIGHT_SPHERE = 1, SRAY_LIGHT_BOX = 2 };
+
+typedef struct sray_light_desc {
+	int type;                       /* SRAY_LIGHT_* */
+	double color[4];
+	sray_xform_desc xform;
+	double radius;                  /* sphere light */
+	double dim[3];                  /* box light: extent of its box */
+} sray_light_desc;
+
+typedef struct sray_camera_desc {
+	int target;                     /* 1: TargetCamera, aimed at target_xform's position,
+	                                   rolled by its scale track's x (src/camera.cc:216-234) */
+	double vfov;                    /* vertical field of view, radians */
+	int shutter;                    /* ms */
+	sray_xform_desc xform, target_xform;
+} sray_camera_desc;
+
+typedef struct sray_scene_desc {
+	int n_materials, n_objects, n_lights, n_textures;
+	const sray_material_desc *materials;
+	const sray_object_desc *objects;
+	const sray_light_desc *lights;
+	const sray_texture_desc *textures;
+	const sray_camera_desc *camera;    /* NULL: the default camera */
+	double env_ambient[4], env_color[4], env_ior;
+	int reserved[4];
+} sray_scene_desc;
+
+/* Load a scene given as tables.  Replaces Scene::load (src/scene.cc:93-183)
+ * for a scene that exists in memory: the meshes get their octrees
+ * (src/mesh.cc:210-226) and hierarchies, identical meshes share one device
+ * copy, and everything after it (sray_gpu_build, _render, ...) is as for
+ * sray_gpu_load_scene.  Returns SRAY_EINVAL with a message for a malformed
+ * description (bad type, material, texture or face data). */
+int sray_gpu_upload_scene(const sray_scene_desc *desc);
+
 /* Prepend a directory to the texture search path SRAY_DATA_PATH, as
  * add_path does (src/datapath.c:40-51); sray prepends the scene file's
  * directory before loading it (src/sray.cc:101-112).  Textures named by a

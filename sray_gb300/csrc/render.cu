@@ -2866,6 +2866,22 @@ static int load_scene_text(const char *xml, size_t len, const char *sidecar, int
 	return 0;
 }
 
+int sray_gpu_upload_scene(const sray_scene_desc *desc)
+{
+	NEED_CTX();
+	Renderer &R = *g_R;
+	R.loaded = false;
+	R.built = false;
+	R.photons_ready = false;
+	if(!desc) { g_err = "null scene description"; return SRAY_EINVAL; }
+	std::string err;
+	if(!R.sc.from_desc(*desc, R.opt, err)) { g_err = err; return SRAY_EINVAL; }
+	int r = R.upload_scene(0);
+	if(r) { g_err = R.err; return r; }
+	R.loaded = true;
+	return 0;
+}
+
 int sray_gpu_load_scene_mem(const char *xml, size_t len)
 {
 	NEED_CTX();

@@ -1402,11 +1402,19 @@ bool HostScene::load(const char *text, size_t len, const sray_opts &opt, std::st
 	if(!ld.run()) return false;
 	if(have_sidecar && ld.mesh_objects != cached_map.size()) { err = "side-car holds more meshes than the document"; return false; }
 	if(used) *used = have_sidecar;
-	/* mesh octrees in object space (Mesh::build_tree, src/mesh.cc:210-226),
-	 * one per unique mesh, built on all host cores (read from the side-car
-	 * when it had them) */
+	finish_load(opt, !have_sidecar);
+	if(sidecar && !have_sidecar) write_sidecar(sidecar, *this, ld.mesh_of_object, len, doc_hash, opt);
+	return true;
+}
+
+/* after the scene's contents are in: the mesh octrees in object space
+ * (Mesh::build_tree, src/mesh.cc:210-226) and hierarchies, one per unique
+ * mesh, built on all host cores (unless they came from a side-car), and
+ * the static objects' bounds */
+void HostScene::finish_load(const sray_opts &opt, bool build_meshes)
+{
 	std::vector<std::thread> th;
-	size_t nm = have_sidecar ? 0 : meshes.size();
+	size_t nm = build_meshes ? meshes.size() : 0;
 	/* tasks 0 .. nm-1 build octrees, nm .. 2nm-1 hierarchies */
 	size_t ntask = 2 * nm;
 	unsigned nth = std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), (unsigned)ntask));
@@ -1437,7 +1445,6 @@ bool HostScene::load(const char *text, size_t len, const sray_opts &opt, std::st
 		}));
 	}
 	for(auto &t : th) t.join();
-	if(sidecar && !have_sidecar) write_sidecar(sidecar, *this, ld.mesh_of_object, len, doc_hash, opt);
 	/* objects with at most one key per transform track have time-independent bounds */
 	for(size_t i = 0; i < objs.size(); i++) {
 		Object &o = objs[i];
@@ -1447,6 +1454,144 @@ bool HostScene::load(const char *text, size_t len, const sray_opts &opt, std::st
 			o.is_static = true;
 		}
 	}
+}
+
+/* ---- a scene given as tables ---- */
+template <class T> static bool desc_track(const sray_track_desc &d, int width, Track<T> &tr, const char *what, std::string &err,
+		T (*make)(const double *))
+{
+	if(d.nkeys < 0 || (d.nkeys > 0 && (!d.time || !d.val))) { err = std::string("bad ") + what + " track"; return false; }
+	if(d.interp < INTERP_STEP || d.interp > INTERP_CUBIC || d.extrap < EXTRAP_CLAMP || d.extrap > EXTRAP_PINGPONG) {
+		err = std::string("bad interpolation or extrapolation of a ") + what + " track";
+		return false;
+	}
+	tr.interp = d.interp;
+	tr.extrap = d.extrap;
+	for(int k = 0; k < d.nkeys; k++) set_key(tr, d.time[k], make(d.val + (size_t)k * width));
+	return true;
+}
+
+static Vec3 make_vec3(const double *v) { return Vec3(v[0], v[1], v[2]); }
+static Quat make_quat(const double *v) { Quat q = {v[0], v[1], v[2], v[3]}; return q; }
+
+static bool desc_xform(const sray_xform_desc &d, XForm &xf, std::string &err)
+{
+	if(!desc_track(d.pos, 3, xf.pos, "position", err, make_vec3)) return false;
+	if(!desc_track(d.rot, 4, xf.rot, "rotation", err, make_quat)) return false;
+	if(!desc_track(d.scale, 3, xf.scale, "scale", err, make_vec3)) return false;
+	xf.pivot = Vec3(d.pivot[0], d.pivot[1], d.pivot[2]);
+	return true;
+}
+
+bool HostScene::from_desc(const sray_scene_desc &d, const sray_opts &opt, std::string &err)
+{
+	*this = HostScene();
+	if(d.n_materials < 0 || d.n_objects < 0 || d.n_lights < 0 || d.n_textures < 0 ||
+			(d.n_materials && !d.materials) || (d.n_objects && !d.objects) || (d.n_lights && !d.lights) ||
+			(d.n_textures && !d.textures)) {
+		err = "bad scene description: negative count or missing table";
+		return false;
+	}
+	for(int i = 0; i < d.n_textures; i++) {
+		const sray_texture_desc &t = d.textures[i];
+		if(t.width <= 0 || t.height <= 0 || !t.pixels) { err = "bad texture " + std::to_string(i); return false; }
+		Texture tx;
+		tx.xsz = t.width;
+		tx.ysz = t.height;
+		tx.pix.assign(t.pixels, t.pixels + (size_t)t.width * t.height * 4);
+		texs.push_back(std::move(tx));
+	}
+	for(int i = 0; i < d.n_materials; i++) {
+		const sray_material_desc &md = d.materials[i];
+		Material m;
+		m.name = md.name ? md.name : "";
+		m.phong = md.phong ? 1 : 0;
+		for(int a = 0; a < SRAY_ATTR_COUNT; a++) {
+			if(!md.attr[a].present) continue;
+			const double *col = md.attr[a].col;
+			int tex = md.attr[a].texture;
+			if(tex < -1 || tex >= d.n_textures) { err = "material " + m.name + ": texture index out of range"; return false; }
+			switch(a) {
+			case SRAY_ATTR_DIFFUSE: memcpy(m.kd, col, sizeof m.kd); m.tex[TA_DIFFUSE] = tex; break;
+			case SRAY_ATTR_SPECULAR: memcpy(m.ks, col, sizeof m.ks); m.tex[TA_SPECULAR] = tex; break;
+			case SRAY_ATTR_SHININESS: m.shin = col[0]; m.tex[TA_SHININESS] = tex; break;
+			case SRAY_ATTR_REFLECT: m.refl = col[0]; m.tex[TA_REFLECT] = tex; break;
+			case SRAY_ATTR_REFRACT: m.refr = col[0]; m.tex[TA_REFRACT] = tex; break;
+			case SRAY_ATTR_IOR: m.ior = col[0]; m.tex[TA_IOR] = tex; break;
+			case SRAY_ATTR_NORMAL: m.have_normal = true; m.nrm_scale = col[0]; m.tex[TA_NORMAL] = tex; break;
+			}
+		}
+		mats.push_back(m);
+	}
+	for(int i = 0; i < d.n_objects; i++) {
+		const sray_object_desc &od = d.objects[i];
+		Object o;
+		o.name = od.name ? od.name : "";
+		if(od.type < SRAY_OBJ_SPHERE || od.type > SRAY_OBJ_MESH) { err = "object " + o.name + ": unknown type"; return false; }
+		o.type = od.type;
+		if(od.material < -1 || od.material >= d.n_materials) { err = "object " + o.name + ": material index out of range"; return false; }
+		o.mat = od.material;
+		if(!desc_xform(od.xform, o.xf, err)) { err = "object " + o.name + ": " + err; return false; }
+		o.rad = od.rad;
+		o.start = od.start;
+		o.end = od.end;
+		if(o.type == OBJ_MESH) {
+			if(od.nfaces < 0 || (od.nfaces > 0 && !od.pos)) { err = "mesh " + o.name + ": no vertex data"; return false; }
+			size_t nf = (size_t)od.nfaces;
+			Mesh m;
+			m.posd.assign(od.pos, od.pos + nf * 9);
+			m.pos.resize(nf * 9);
+			for(size_t k = 0; k < nf * 9; k++) m.pos[k] = (float)m.posd[k];
+			m.attr.assign(nf * 24, 0.0f);
+			for(size_t f = 0; f < nf; f++) {
+				for(int k = 0; k < 9; k++) {
+					if(od.normal) m.attr[f * 24 + k] = (float)od.normal[f * 9 + k];
+					if(od.tangent) m.attr[f * 24 + 9 + k] = (float)od.tangent[f * 9 + k];
+				}
+				if(od.texcoord) for(int k = 0; k < 6; k++) m.attr[f * 24 + 18 + k] = (float)od.texcoord[f * 6 + k];
+			}
+			/* identical meshes share one device copy */
+			uint64_t h = fnv(m.posd.data(), m.posd.size() * sizeof(double), 0xcbf29ce484222325ull);
+			h = fnv(m.attr.data(), m.attr.size() * sizeof(float), h);
+			o.mesh = -1;
+			for(size_t u = 0; u < meshes.size(); u++)
+				if(meshes[u].hash == h && meshes[u].posd == m.posd && meshes[u].attr == m.attr) { o.mesh = (int)u; break; }
+			if(o.mesh < 0) {
+				m.hash = h;
+				o.mesh = (int)meshes.size();
+				meshes.push_back(std::move(m));
+			}
+			n_tris += (int64_t)nf;
+		}
+		objs.push_back(o);
+	}
+	for(int i = 0; i < d.n_lights; i++) {
+		const sray_light_desc &ld = d.lights[i];
+		Light l;
+		if(ld.type < SRAY_LIGHT_POINT || ld.type > SRAY_LIGHT_BOX) { err = "light " + std::to_string(i) + ": unknown type"; return false; }
+		l.type = ld.type;
+		memcpy(l.col, ld.color, sizeof l.col);
+		if(!desc_xform(ld.xform, l.xf, err)) { err = "light " + std::to_string(i) + ": " + err; return false; }
+		l.radius = (float)ld.radius;
+		l.dim = Vec3(ld.dim[0], ld.dim[1], ld.dim[2]);
+		lights.push_back(l);
+	}
+	cam = Camera();
+	cam.aspect = (double)opt.width / (double)opt.height;
+	cam.shutter = opt.shutter;
+	if(d.camera) {
+		cam.target = d.camera->target ? 1 : 0;
+		cam.vfov = d.camera->vfov;
+		cam.shutter = d.camera->shutter;
+		if(!desc_xform(d.camera->xform, cam.xf, err) || !desc_xform(d.camera->target_xform, cam.txf, err)) {
+			err = "camera: " + err;
+			return false;
+		}
+	}
+	memcpy(env_amb, d.env_ambient, sizeof env_amb);
+	memcpy(env_col, d.env_color, sizeof env_col);
+	env_ior = d.env_ior;
+	finish_load(opt, true);
 	return true;
 }
 

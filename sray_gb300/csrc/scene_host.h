@@ -178,6 +178,9 @@ struct HostScene {
 	 * loaded in full and the side-car is written.  *used tells which. */
 	bool load(const char *text, size_t len, const sray_opts &opt, std::string &err, const char *sidecar = nullptr,
 			bool *used = nullptr);
+	/* Load a scene given as tables (sray_gpu_upload_scene). */
+	bool from_desc(const sray_scene_desc &d, const sray_opts &opt, std::string &err);
+	void finish_load(const sray_opts &opt, bool build_meshes);
 	void build_tree(int t0, int t1, const sray_opts &opt);
 	/* the gather radius build_tree(t0, t1) would set, without building */
 	double gather_dist_at(int t0, int t1, const sray_opts &opt) const;

@@ -21,7 +21,7 @@ EXPORTS = ["sray_default_opts", "sray_gpu_init", "sray_gpu_set_opts", "sray_gpu_
            "sray_gpu_get_photons", "sray_gpu_dump_photons", "sray_gpu_restore_photons", "sray_gpu_render_batch",
            "sray_gpu_get_stats", "sray_gpu_nrc_stats", "sray_gpu_nrc_reset", "sray_gpu_get_tuning",
            "sray_gpu_set_tuning", "sray_gpu_autotune", "sray_gpu_set_profiling", "sray_gpu_kernel_times", "sray_gpu_last_error",
-           "sray_gpu_shutdown", "sray_gpu_set_faults", "sray_nrc_reset", "sray_nrc_set_params", "sray_nrc_get_params", "sray_nrc_infer",
+           "sray_gpu_shutdown", "sray_gpu_set_faults", "sray_gpu_upload_scene", "sray_nrc_reset", "sray_nrc_set_params", "sray_nrc_get_params", "sray_nrc_infer",
            "sray_nrc_gradients", "sray_nrc_train", "sray_nrc_last_error"]
 
 NRC_PARAMS = 26563
@@ -129,6 +129,8 @@ def load_library():
     L.sray_gpu_kernel_times.argtypes = [ctypes.c_char_p, ctypes.c_size_t, vp, vp, ip, vp, ip]
     L.sray_gpu_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     L.sray_gpu_set_faults.argtypes = [ctypes.POINTER(SrayFaults)]
+    from .scene_desc import SceneDescC
+    L.sray_gpu_upload_scene.argtypes = [ctypes.POINTER(SceneDescC)]
     L.sray_gpu_shutdown.argtypes = []
     L.sray_gpu_shutdown.restype = None
     L.sray_nrc_reset.argtypes = [ctypes.c_uint64]
@@ -228,6 +230,11 @@ class GpuRenderer:
         used = ctypes.c_int()
         self._chk(self.L.sray_gpu_load_scene_sidecar(path.encode(), sidecar.encode(), ctypes.byref(used)))
         return bool(used.value)
+
+    def upload_scene(self, desc):
+        """Load a scene given as tables (sray_gb300.scene_desc.SceneDesc)."""
+        c = desc.c()
+        self._chk(self.L.sray_gpu_upload_scene(ctypes.byref(c)))
 
     def load_xml(self, xml):
         b = xml.encode() if isinstance(xml, str) else xml

@@ -32,7 +32,8 @@ def _raises(code, fn, *a, **kw):
 def test_malformed_scene_documents(gpu_lib, small_scene_path):
     g = gpu_lib.GpuRenderer(**_opts())
     good = open(small_scene_path, "rb").read()
-    assert "end of document" in _raises(gpu.SRAY_ELOAD, g.load_xml, good[:len(good) // 2])
+    assert "xml:" in _raises(gpu.SRAY_ELOAD, g.load_xml, good[:len(good) // 2])      # cut inside a tag
+    assert "end of document" in _raises(gpu.SRAY_ELOAD, g.load_xml, good[:good.rindex(b"</scene>")])
     assert "root element" in _raises(gpu.SRAY_ELOAD, g.load_xml, b"not a scene")
     assert "unknown type" in _raises(gpu.SRAY_ELOAD, g.load_xml, b'<scene><object name="o" type="torus"/></scene>')
     assert _raises(gpu.SRAY_ELOAD, g.load, "/nonexistent/scene.xml")
