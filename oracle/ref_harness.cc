@@ -10,6 +10,7 @@
  *
  * usage: ref_harness scene.xml out_prefix seed y0 y1 [reference options...]
  *        ref_harness --time scene.xml reps [reference options...]
+ *        ref_harness --restore dump.txt out.bin [reference options...]
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -88,9 +89,29 @@ static int time_render(int argc, char **argv)
 	return 0;
 }
 
+/* --restore dump.txt out.bin [reference options...]: PhotonMap::restore
+ * (src/pmap.cc:207-251) of a dump file, its photons written as 16 floats
+ * each (pos, dir, norm, col, type) -- the reference reading a dump another
+ * program wrote. */
+static int restore_dump(int argc, char **argv)
+{
+	std::vector<char *> av;
+	av.push_back(argv[0]);
+	for(int i = 4; i < argc; i++) av.push_back(argv[i]);
+	av.push_back((char *)"none.xml");
+	av.push_back(0);
+	if(parse_opt((int)av.size() - 1, av.data()) == -1) return 1;
+	opt.verb = -1;
+	PhotonMap pm;
+	if(!pm.restore(argv[2])) return 1;
+	dump_photons(argv[3], pm);
+	return 0;
+}
+
 int main(int argc, char **argv)
 {
 	if(argc >= 4 && strcmp(argv[1], "--time") == 0) return time_render(argc, argv);
+	if(argc >= 4 && strcmp(argv[1], "--restore") == 0) return restore_dump(argc, argv);
 	if(argc < 6) {
 		fprintf(stderr, "usage: %s scene.xml out_prefix seed y0 y1 [options]\n", argv[0]);
 		return 1;
@@ -172,6 +193,12 @@ int main(int argc, char **argv)
 	dump_photons(fname, scn->caust_map);
 	snprintf(fname, sizeof fname, "%s.gi", prefix);
 	dump_photons(fname, scn->gi_map);
+	/* the maps in the reference's own text format (PhotonMap::dump,
+	 * src/pmap.cc:180-205) */
+	snprintf(fname, sizeof fname, "%s.caust.dump", prefix);
+	scn->caust_map.dump(fname);
+	snprintf(fname, sizeof fname, "%s.gi.dump", prefix);
+	scn->gi_map.dump(fname);
 
 	/* primary hits: object index, triangle index of meshes, t */
 	int W = opt.width, H = opt.height;

@@ -6,7 +6,8 @@ stand-ins and a Philox stream per photon and per pixel sample) on five
 seeded scenes (the textured one reads the images of scenegen.textures()
 through SRAY_DATA_PATH; the animated one is rendered at 1350 ms) and stores, per case: the scene XML, the options, the
 primary-hit ids and t, the stored caustic and global photons, and the
-rendered image with its per-pixel sample counts.
+rendered image with its per-pixel sample counts; for the feature scene
+also both photon maps as the reference's PhotonMap::dump writes them.
 
 Only runs where the reference sources are present:
     python tests/golden/make_golden.py [case ...]
@@ -52,6 +53,10 @@ CASES = {
 }
 
 
+# cases whose photon maps are also stored as the reference's dump files
+DUMP_CASES = {"feature"}
+
+
 def run_case(harness, name, spec):
     from sray_gb300 import scenegen
     gen, kw, cli, oopts = spec[:4]
@@ -70,6 +75,11 @@ def run_case(harness, name, spec):
         caust = np.fromfile(prefix + ".caust", dtype=np.float32).reshape(-1, 16)
         gi = np.fromfile(prefix + ".gi", dtype=np.float32).reshape(-1, 16)
         img = np.fromfile(prefix + ".img", dtype=np.float32).reshape(h, oopts["width"], 5)
+        if name in DUMP_CASES:
+            # the maps in the reference's own dump format (PhotonMap::dump)
+            for which in ("caust", "gi"):
+                with open(prefix + ".%s.dump" % which, "rb") as f, gzip.open(os.path.join(HERE, "%s.%s.dump.gz" % (name, which)), "wb") as g:
+                    g.write(f.read())
     out = os.path.join(HERE, name + ".npz")
     np.savez_compressed(out, obj=hits["o"], prim=hits["p"], t=hits["t"], caust=caust[:, :13], gi=gi[:, :13],
                         img=img[..., :4], spp=img[..., 4].astype(np.int32), msec=np.int64(msec),

@@ -463,3 +463,49 @@ def test_batch_jobs_match_oracle_mblur_gi_spp(gpu_lib, oracle_lib):
         img_o = o.render(ms)
         assert _compare(fb.cpu().numpy(), img_o, "batch job %dx%d at %d ms (pixel base %d)" % (w, h, ms, base)) <= 1e-3
         base += w * h
+
+
+def _read_dump(text):
+    """Photons of a dump in the reference's format: energy, then
+    <pos> <dir> <norm> <col> per line (src/pmap.cc:180-205)."""
+    lines = text.splitlines()
+    assert lines[0].startswith("energy ")
+    rows = [[float(v) for v in ln.replace("<", " ").replace(">", " ").split()] for ln in lines[1:] if ln.strip()]
+    return float(lines[0].split()[1]), np.array(rows, np.float64).reshape(-1, 12)
+
+
+def test_gpu_restores_reference_dumps(gpu_lib, tmp_path):
+    # photon maps the reference itself dumped (PhotonMap::dump, compiled
+    # from its sources): the GPU restores every photon, within the format's
+    # six decimals, and renders from them as from the reference's photons
+    import gzip
+    import json
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    d = np.load(os.path.join(here, "feature.npz"))
+    opts = json.loads(bytes(d["opts"]).decode())
+    with gzip.open(os.path.join(here, "feature.xml.gz")) as f:
+        xml = f.read()
+    g = gpu_lib.GpuRenderer(**opts)
+    g.load_xml(xml)
+    shutter = opts["shutter"]
+    g.build(-(shutter // 2), shutter - shutter // 2)
+    from scipy.spatial import cKDTree
+    for which, name in ((0, "caust"), (1, "gi")):
+        path = str(tmp_path / ("%s.dump" % name))
+        with gzip.open(os.path.join(here, "feature.%s.dump.gz" % name), "rt") as f:
+            text = f.read()
+        with open(path, "w") as f:
+            f.write(text)
+        energy, rows = _read_dump(text)
+        n = g.restore_photons(which, path)
+        back = g.photons(which).astype(np.float64)
+        ref = d[name].astype(np.float64)          # the reference's photons in full precision
+        assert n == len(rows) == len(ref) == len(back)
+        _, j = cKDTree(back[:, :3]).query(rows[:, :3])
+        assert len(np.unique(j)) == len(rows)
+        fmt = np.abs(back[j, :12] - rows[:, :12]).max()
+        _, k = cKDTree(back[:, :3]).query(ref[:, :3])
+        full = np.abs(back[k, :12] - ref[:, :12]).max()
+        print("restored %s: %d photons (energy %g); against the dump's text %.2g, against the reference's values %.2g"
+              % (name, n, energy, fmt, full))
+        assert fmt <= 1e-6 and full <= 1.5e-6
