@@ -409,6 +409,9 @@ typedef struct sray_tuning {
 	                             ray per warp instead of one per thread (0: never) (16384) */
 	int warp_segments;        /* the same for light-sample passes of at most this many
 	                             segments (16384) */
+	int queue_depth;          /* primary rays per wave: a sample batch's pixels go through
+	                             the shading tree in waves of at most this many primary
+	                             rays, each wave finished before the next (0: one wave) (0) */
 	int side_gather;          /* 1: the first sample batch's photon-map gathers start as
 	                             soon as the maps exist, on a stream of their own beside
 	                             the remaining bounces; 2: the same, the render loop
@@ -460,11 +463,22 @@ int sray_gpu_set_faults(const sray_faults *f);
 /* Copy the last error message (NUL-terminated, truncated to `cap`). */
 int sray_gpu_last_error(char *buf, size_t cap);
 
+/* The autotuner for batches (sray_gpu_render_batch): the queue depth
+ * (65,536, 262,144 or 1,048,576 primary rays per wave) against the
+ * traversal mode (thread per ray; one warp per ray in passes of at most
+ * 16,384 rays or segments; one warp per ray in every pass), each trial
+ * timed over `frames` batches after one warm-up.  Keeps and returns the
+ * fastest; trials go into `log` as for sray_gpu_autotune. */
+struct sray_job;
+int sray_gpu_autotune_batch(const struct sray_job *jobs, int n, int frames, void *stream, sray_tuning *best, float *best_ms,
+		sray_tune_trial *log, int log_cap, int *n_log);
+
 /* A batch of frames of the loaded scene in one wavefront (extension; the
  * reference renders one frame per render() call, src/render.cc:34-55).
  * Each job has its own frame time, resolution and device framebuffer
- * (width * height * 4 floats); the jobs share the options (samples, photon
- * counts) and the camera (its aspect is the one set at load, as for a
+ * (width * height * 4 floats), its scene (in a scene set) and optionally its
+ * own photon counts; the jobs share the other options (samples, depth) and
+ * use their scene's camera (its aspect is the one set at load, as for a
  * single frame).  The acceleration structures are built once over the union of
  * the jobs' shutter intervals, each job gets its own photon maps (shot over
  * its own interval), and all jobs' pixels go through the same camera,
@@ -477,10 +491,25 @@ typedef struct sray_job {
 	long msec;
 	int width, height;
 	float *fb;                /* device framebuffer */
-	int reserved[4];
+	int scene;                /* its scene in a scene set (sray_gpu_load_scene_set); 0 otherwise */
+	int caust_photons;        /* its photon counts (0: the options') */
+	int gi_photons;
+	int reserved;
 } sray_job;
 
 int sray_gpu_render_batch(const sray_job *jobs, int n, void *stream);
+
+/* Load several scene documents as one scene set (extension; the reference
+ * holds one scene, src/scene.h:32-33): batches can then mix jobs of
+ * different scenes (sray_job.scene = the index into xml_paths), each
+ * rendered as sray_gpu_render would render it alone with the same random
+ * streams, keyed by its pixels' place in the batch.  The scenes' meshes,
+ * materials, lights and cameras live side by side in one set of device
+ * tables; each frame builds every scene's octree and object hierarchy, and
+ * a ray finds its scene through its job.  A scene set renders through
+ * sray_gpu_render_batch only (nrc = 0); one document makes an ordinary
+ * scene. */
+int sray_gpu_load_scene_set(const char *const *xml_paths, int n);
 
 /* Release every device buffer and the context. */
 void sray_gpu_shutdown(void);

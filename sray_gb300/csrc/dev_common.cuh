@@ -69,7 +69,18 @@ struct DNrc {
  * [pix0, pix0 + width * height) of the batch's pixel space */
 struct DevJob {
 	int pix0, width, height, t0;
-	float cam_f, cam_xsz, cam_ysz, pad;
+	float cam_f, cam_xsz, cam_ysz;
+	int scene;                /* its scene in a scene set (0 otherwise) */
+	int cam_base;             /* first time slot of its scene's camera in cam_m */
+	int pad[3];
+};
+
+/* one scene of a scene set: the roots of its scene octree and object
+ * hierarchy in the set's tables, its lights and environment */
+struct DevSceneRef {
+	int sroot, troot;         /* troot < 0: no objects */
+	int light0, nlights;
+	float env_col[4], env_amb[4];
 };
 
 struct DScene {
@@ -123,6 +134,12 @@ struct DScene {
 	int njobs;
 	const DevJob *jobs;
 	const DPhotonMap *maps;
+	/* the object hierarchy's root (0 for one scene; a batch job's photon
+	 * view points it, sroot and the light tables at its scene's) */
+	int troot;
+	/* a scene set (nscenes > 1): a ray's scene is its job's */
+	int nscenes;
+	const DevSceneRef *scenes;
 };
 
 /* the job of a pixel of the batch's pixel space */
@@ -570,19 +587,32 @@ __device__ __forceinline__ bool mailbox_seen(ObjMailbox &m, int oi)
 	return seen;
 }
 
+/* The roots a traversal starts from: those of scene `scene` of a scene set
+ * (scene >= 0), else the view's own.  x: the scene octree's root (< 0: no
+ * scene), y: the object hierarchy's (< 0: none, the octree decides). */
+__device__ __forceinline__ int2 scene_roots(const DScene &S, int scene)
+{
+	if(scene >= 0) {
+		const DevSceneRef &R = S.scenes[scene];
+		return make_int2(S.has_scene ? R.sroot : -1, R.troot);
+	}
+	return make_int2(S.has_scene ? S.sroot : -1, S.tnodes ? S.troot : -1);
+}
+
 /* closest hit of a world-space segment (Scene::cast_ray, src/scene.cc:764-794):
  * front to back over the top-level octree with the pruning above; an object
  * straddling several leaves gives the same closest hit every time, so each
  * object is tested once per ray */
 template <bool COUNT>
 __device__ __forceinline__ void trace_closest_octree_impl(const DScene &S, V3 wo, V3 wd, int time, Hit &h, TraceCounters *tc,
-		int *overflow)
+		int *overflow, int scene = -1)
 {
+	const int sroot_i = scene_roots(S, scene).x;
 	h.t = FLT_MAX;
 	h.obj = -1;
 	h.prim = -1;
 	h.tie = 0;
-	if(!S.has_scene) return;
+	if(sroot_i < 0) return;
 	int ti = time_index(S, time);
 	RayT r = make_ray(wo, wd);
 	int oct = octant(r);
@@ -591,9 +621,9 @@ __device__ __forceinline__ void trace_closest_octree_impl(const DScene &S, V3 wo
 	float te;
 	ObjMailbox mbox;
 	obj_mailbox_init(S, mbox);
-	const DevNode &root = S.snodes[S.sroot];
+	const DevNode &root = S.snodes[sroot_i];
 	if(!box_hit(root.mn, root.mx, r, te)) return;
-	st.node[sp] = S.sroot;
+	st.node[sp] = sroot_i;
 	st.te[sp] = te;
 	sp++;
 	while(sp > 0) {
@@ -648,9 +678,10 @@ __device__ inline bool mesh_any(const DScene &S, int root, const RayT &r, TStack
 	return false;
 }
 
-__device__ __forceinline__ bool trace_any_octree_impl(const DScene &S, V3 wo, V3 wd, int time, int *overflow)
+__device__ __forceinline__ bool trace_any_octree_impl(const DScene &S, V3 wo, V3 wd, int time, int *overflow, int scene = -1)
 {
-	if(!S.has_scene) return false;
+	const int sroot_i = scene_roots(S, scene).x;
+	if(sroot_i < 0) return false;
 	int ti = time_index(S, time);
 	RayT r = make_ray(wo, wd);
 	int oct = octant(r);
@@ -659,9 +690,9 @@ __device__ __forceinline__ bool trace_any_octree_impl(const DScene &S, V3 wo, V3
 	ObjMailbox mbox;
 	obj_mailbox_init(S, mbox);
 	float te;
-	const DevNode &root = S.snodes[S.sroot];
+	const DevNode &root = S.snodes[sroot_i];
 	if(!box_hit(root.mn, root.mx, r, te)) return false;
-	st.node[sp++] = S.sroot;
+	st.node[sp++] = sroot_i;
 	while(sp > 0) {
 		int ni = st.node[--sp];
 		float4 n0, n1;
@@ -799,17 +830,19 @@ __device__ __forceinline__ RayT object_ray(const DScene &S, int o, int ti, V3 wo
  * children are visited nearest first (always for closest hits); an any-hit
  * query may visit them in the node's order instead. */
 template <bool COUNT, bool ANY, bool SORT = true>
-__device__ __forceinline__ int trace_two_level(const DScene &S, V3 wo, V3 wd, int time, Hit &h, TraceCounters *tc, int *overflow)
+__device__ __forceinline__ int trace_two_level(const DScene &S, V3 wo, V3 wd, int time, Hit &h, TraceCounters *tc, int *overflow,
+		int scene = -1)
 {
 	h.t = FLT_MAX;
 	h.obj = -1;
 	h.prim = -1;
 	h.tie = 0;
-	if(!S.has_scene) return ANY ? 0 : 1;
-	if(!S.tnodes) return ANY ? 2 : 0;
+	const int2 roots = scene_roots(S, scene);
+	if(roots.x < 0) return ANY ? 0 : 1;
+	if(roots.y < 0) return ANY ? 2 : 0;
 	int ti = time_index(S, time);
 	RayT wr = make_ray(wo, wd);
-	const DevNode &sroot = S.snodes[S.sroot];
+	const DevNode &sroot = S.snodes[roots.x];
 	RayC wc = make_rayc(wr, box_bound(sroot.mn, sroot.mx));
 	RayT r = wr;
 	RayC rc = wc;
@@ -819,7 +852,7 @@ __device__ __forceinline__ int trace_two_level(const DScene &S, V3 wo, V3 wd, in
 	bool eq = false;
 	int sp = 0, inst_base = 0, iobj = -1;
 	bool inst = false;
-	int cur = 0;   /* the object hierarchy's root */
+	int cur = roots.y;   /* the object hierarchy's root */
 	for(;;) {
 		if(cur == BVH_NONE) {
 			bool found = false;

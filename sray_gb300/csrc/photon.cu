@@ -579,15 +579,16 @@ static int photon_setup(Renderer &R, int global, cudaStream_t s, int *total_out)
 {
 	PhotonBufs &P = global ? R.gi : R.caust;
 	const sray_opts &opt = R.opt;
-	int num = global ? opt.gi_photons : opt.caust_photons;
-	int nl = (int)R.sc.lights.size();
+	/* a batch job's own photon count and its scene's lights */
+	int num = R.map_counts[global] >= 0 ? R.map_counts[global] : (global ? opt.gi_photons : opt.caust_photons);
+	int nl = R.map_nlight >= 0 ? R.map_nlight : (int)R.sc.lights.size();
 	P.map.n = 0;
 	*total_out = 0;
 	if(num <= 0 || nl <= 0) return 0;
 	std::vector<double> inten(nl);
 	double accp = 0.0;
 	for(int i = 0; i < nl; i++) {
-		const double *c = R.sc.lights[i].col;
+		const double *c = R.sc.lights[R.map_light0 + i].col;
 		inten[i] = (c[0] + c[1] + c[2]) / 3.0;
 		accp += inten[i];
 	}
@@ -622,7 +623,7 @@ int photon_shoot_maps(Renderer &R, const DScene &base, cudaStream_t s, int *nc, 
 	int all = tot[0] + tot[1];
 	if(all <= 0) return 0;
 	PhotonSet PSet;
-	PSet.nlights = (int)R.sc.lights.size();
+	PSet.nlights = base.nlights;
 	for(int m = 0; m < 2; m++) {
 		PhotonBufs &P = m ? R.gi : R.caust;
 		PSet.total[m] = tot[m];

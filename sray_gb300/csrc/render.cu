@@ -44,24 +44,33 @@ static __device__ __forceinline__ int warp_alloc(int *counter, int n)
 	return base + excl;
 }
 
+/* the scene of a batch pixel in a scene set (-1: the view's own scene) */
+__device__ __forceinline__ int pixel_scene(const DScene &S, int pixel)
+{
+	return S.nscenes > 1 && S.njobs > 0 ? S.jobs[job_of(S, pixel)].scene : -1;
+}
+
 /* ---------------------------------------------------------------- */
 /* primary rays of samples [s0, s0 + width) of every active pixel; the ray's
  * accumulator slot is (active index * width + sample - s0) */
-__global__ void k_camera(DScene S, const int *active, const int *n_active_p, int s0, int width, RayQueue q, float4 *acc,
+__global__ void k_camera(DScene S, const int *active, int a0, int na, int s0, int width, RayQueue q, float4 *acc,
 		DevCounters *ctr)
 {
-	int n = *n_active_p * width;
+	/* a wave: active pixels [a0, a0 + na); queue entry i is accumulator slot a0 * width + i */
+	int n = na * width;
 	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		int a = i / width, j = i - a * width;
+		int a = a0 + i / width, j = i - (i / width) * width;
+		int slot = a0 * width + i;
 		int p = active ? active[a] : a;
 		int sample = s0 + j;
-		int W = S.width, Hh = S.height, lp = p, t0 = S.t0;
+		int W = S.width, Hh = S.height, lp = p, t0 = S.t0, cam_base = 0;
 		float cam_f = S.cam_f, xsz = S.cam_xsz, ysz = S.cam_ysz;
 		if(S.njobs > 0) {
-			/* a batch: the job's resolution, camera aspect and frame time */
+			/* a batch: the job's resolution, camera (its scene's) and frame time */
 			const DevJob &J = S.jobs[job_of(S, p)];
 			W = J.width; Hh = J.height; lp = p - J.pix0; t0 = J.t0;
 			cam_f = J.cam_f; xsz = J.cam_xsz; ysz = J.cam_ysz;
+			cam_base = J.cam_base;
 		}
 		int x = lp % W, y = lp / W;
 		sray_rng s;
@@ -75,16 +84,16 @@ __global__ void k_camera(DScene S, const int *active, const int *n_active_p, int
 		V3 d = mk(px, py, cam_f) * S.cam_maxd;
 		int time = t0;
 		if(S.mblur && sample > 0 && S.shutter > 0) time += sray_rng_int(&s) % S.shutter - S.shutter / 2;
-		const float *m = S.cam_m + (size_t)time_index(S, time) * 12;
+		const float *m = S.cam_m + ((size_t)cam_base + time_index(S, time)) * 12;
 		V3 o = mul_pt(m, mk(0.0f, 0.0f, 0.0f));
 		d = mul_dir(m, d);
 		q.o[i] = make_float4(o.x, o.y, o.z, 1.0f);
 		q.d[i] = make_float4(d.x, d.y, d.z, 1.0f);
 		q.w[i] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(p));
-		q.meta[i] = make_int4(i, S.iter, 1, time);
+		q.meta[i] = make_int4(slot, S.iter, 1, time);
 		q.stk[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 		q.ext[i] = make_int2(sample, 0);
-		acc[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+		acc[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 	}
 	if(blockIdx.x == 0 && threadIdx.x == 0) {
 		*q.count = n;
@@ -107,10 +116,11 @@ __global__ void __launch_bounds__(SRAY_TRACE_THREADS, 6) k_trace(DScene S, RayQu
 		int ri = HYB ? i : fb[1 + i];
 		float4 o = q.o[ri], d = q.d[ri];
 		int time = q.meta[ri].w;
+		int scene = S.nscenes > 1 ? pixel_scene(S, __float_as_int(q.w[ri].w)) : -1;
 		Hit h;
 		bool sure = true;
-		if(HYB) sure = trace_two_level<COUNT, false>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), time, h, &tc, &overflow) != 0;
-		else trace_closest_octree_impl<COUNT>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), time, h, &tc, &overflow);
+		if(HYB) sure = trace_two_level<COUNT, false>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), time, h, &tc, &overflow, scene) != 0;
+		else trace_closest_octree_impl<COUNT>(S, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), time, h, &tc, &overflow, scene);
 		if(HYB && !sure) {
 			fb[1 + atomicAdd(fb, 1)] = ri;
 			continue;
@@ -150,7 +160,7 @@ __device__ __forceinline__ float lane_pick(float4 v, int k) { return k == 0 ? v.
  * the octrees must decide. */
 template <bool ANY>
 __device__ __forceinline__ int warp_trace(const DScene &S, V3 wo, V3 wd, int time, int *st_ref, int *st_obj, float *st_te, float &best,
-		int &bobj, int &bprim)
+		int &bobj, int &bprim, int scene)
 {
 	const unsigned FULL = 0xffffffffu;
 	int lane = threadIdx.x & 31;
@@ -158,16 +168,17 @@ __device__ __forceinline__ int warp_trace(const DScene &S, V3 wo, V3 wd, int tim
 	best = ANY ? 1.0f : FLT_MAX;
 	bobj = -1;
 	bprim = -1;
-	if(!S.has_scene) return ANY ? 0 : 1;
-	if(!S.tnodes) return ANY ? 2 : 0;
+	const int2 roots = scene_roots(S, scene);
+	if(roots.x < 0) return ANY ? 0 : 1;
+	if(roots.y < 0) return ANY ? 2 : 0;
 	int bslot = -1;
 	int ti = time_index(S, time);
 	RayT wr = make_ray(wo, wd);
-	const DevNode &sroot = S.snodes[S.sroot];
+	const DevNode &sroot = S.snodes[roots.x];
 	RayC wc = make_rayc(wr, box_bound(sroot.mn, sroot.mx));
 	bool eq = false;
 	if(lane == 0) {
-		st_ref[0] = 0;   /* the object hierarchy's root */
+		st_ref[0] = roots.y;   /* the object hierarchy's root */
 		st_obj[0] = -1;
 		st_te[0] = -INFINITY;
 	}
@@ -326,8 +337,9 @@ __global__ void __launch_bounds__(128) k_trace_warp(DScene S, RayQueue q, int4 *
 		float4 o4 = q.o[ri], d4 = q.d[ri];
 		float best;
 		int bobj, bprim;
+		int scene = S.nscenes > 1 ? pixel_scene(S, __float_as_int(q.w[ri].w)) : -1;
 		int res = warp_trace<false>(S, mk(o4.x, o4.y, o4.z), mk(d4.x, d4.y, d4.z), q.meta[ri].w, s_ref[w], s_obj[w], s_te[w], best, bobj,
-				bprim);
+				bprim, scene);
 		if(lane == 0) {
 			if(!res) fb[1 + atomicAdd(fb, 1)] = ri;
 			else if(bobj >= 0) hits[ri] = make_int4(__float_as_int(best), bobj, bprim, 0);
@@ -386,14 +398,14 @@ __device__ __forceinline__ void push_gather(ShadeOut &out, V3 pos, V3 n, int kin
 
 /* a shadow ray and the light contribution it carries if unoccluded */
 __device__ __forceinline__ void push_shadow(ShadeOut &out, V3 o, V3 d, int time, int pixel, float wr, float wg, float wb,
-		int *overflow)
+		int *overflow, int scene = -1)
 {
 	int slot = warp_alloc(out.sq_count, 1);
 	if(slot >= out.sq_cap) { *overflow = 1; return; }
 	ShadowReq r;
 	r.a = make_float4(o.x, o.y, o.z, __int_as_float(time));
 	r.b = make_float4(d.x, d.y, d.z, __int_as_float(pixel));
-	r.w = make_float4(wr, wg, wb, 0.0f);
+	r.w = make_float4(wr, wg, wb, __int_as_float(scene));
 	out.sq[slot] = r;
 }
 
@@ -527,9 +539,23 @@ __device__ __forceinline__ void shade_one(const DScene &S, const RayRec &ray, co
 	int dsub = ray.dsub;
 	V3 rd = ray.d;
 	const float *w = ray.w;
+	/* the ray's scene: its lights and environment (a scene set's, or the view's) */
+	const int scene = pixel_scene(S, pixel);
+	int l0 = 0, nl = S.nlights;
+	/* (values, not pointers: the address of a kernel parameter would copy
+	 * the scene view to local memory) */
+	float4 env_col = make_float4(S.env_col[0], S.env_col[1], S.env_col[2], S.env_col[3]);
+	float4 env_amb = make_float4(S.env_amb[0], S.env_amb[1], S.env_amb[2], S.env_amb[3]);
+	if(scene >= 0) {
+		const DevSceneRef &SR = S.scenes[scene];
+		l0 = SR.light0;
+		nl = SR.nlights;
+		env_col = make_float4(SR.env_col[0], SR.env_col[1], SR.env_col[2], SR.env_col[3]);
+		env_amb = make_float4(SR.env_amb[0], SR.env_amb[1], SR.env_amb[2], SR.env_amb[3]);
+	}
 	if(h.obj < 0) {
-		acc_add(acc, aslot, w[0] * S.env_col[0], w[1] * S.env_col[1], w[2] * S.env_col[2]);
-		if(depth == 0) acc[aslot].w = S.env_col[3];
+		acc_add(acc, aslot, w[0] * env_col.x, w[1] * env_col.y, w[2] * env_col.z);
+		if(depth == 0) acc[aslot].w = env_col.w;
 		return;
 	}
 	if(depth == 0) acc[aslot].w = 1.0f;
@@ -544,7 +570,7 @@ __device__ __forceinline__ void shade_one(const DScene &S, const RayRec &ray, co
 		bool even = (tx % 2) == (ty % 2);
 		float tc[3] = {even ? 1.0f : 0.2f, 0.3f, even ? 0.2f : 1.0f};
 		acc_add(acc, aslot, w[0] * (0.1f * tc[0]), w[1] * (0.1f * tc[1]), w[2] * (0.1f * tc[2]));
-		for(int li = 0; li < S.nlights; li++) {
+		for(int li = l0; li < l0 + nl; li++) {
 			const DevLight &L = S.lights[li];
 			V3 lpos = light_point(S, li, time, &rng);
 			V3 ldir = lpos - sp.pos;
@@ -557,7 +583,7 @@ __device__ __forceinline__ void shade_one(const DScene &S, const RayRec &ray, co
 			float ndoth = maxf_ref(dot(sp.normal, hdir), 0.0f);
 			float pw = powf(ndoth, 50.0f);
 			em.shadow(shadow_origin(sp, sdir), sdir, time, aslot, w[0] * (ndotl * L.col[0] * tc[0] + pw * L.col[0]),
-					w[1] * (ndotl * L.col[1] * tc[1] + pw * L.col[1]), w[2] * (ndotl * L.col[2] * tc[2] + pw * L.col[2]));
+					w[1] * (ndotl * L.col[1] * tc[1] + pw * L.col[1]), w[2] * (ndotl * L.col[2] * tc[2] + pw * L.col[2]), scene);
 		}
 		return;
 	}
@@ -586,10 +612,10 @@ __device__ __forceinline__ void shade_one(const DScene &S, const RayRec &ray, co
 	 * refraction is known (src/shader.cc:133-139) */
 	if(mat.have_normal) normal = bump_normal(S, mat, sp);
 	/* ambient: (env_ambient * kd) * kd */
-	acc_add(acc, aslot, w[0] * (S.env_amb[0] * kd[0] * kd[0]), w[1] * (S.env_amb[1] * kd[1] * kd[1]),
-			w[2] * (S.env_amb[2] * kd[2] * kd[2]));
+	acc_add(acc, aslot, w[0] * (env_amb.x * kd[0] * kd[0]), w[1] * (env_amb.y * kd[1] * kd[1]),
+			w[2] * (env_amb.z * kd[2] * kd[2]));
 	V3 vref = reflection(incident, normal);
-	for(int li = 0; li < S.nlights; li++) {
+	for(int li = l0; li < l0 + nl; li++) {
 		const DevLight &L = S.lights[li];
 		int ns = L.type != 0 ? S.shadow_samples : 1;
 		float scale = ns > 1 ? 1.0f / (float)ns : 1.0f;
@@ -607,7 +633,8 @@ __device__ __forceinline__ void shade_one(const DScene &S, const RayRec &ray, co
 				float lc = L.col[k] * 1.0f;
 				c[k] = ((ndotl * lc) * scale) * kd[k] + ((pw * lc) * scale) * ks[k];
 			}
-			if(c[0] != 0.0f || c[1] != 0.0f || c[2] != 0.0f) em.shadow(shadow_origin(sp, sdir), sdir, time, aslot, w[0] * c[0], w[1] * c[1], w[2] * c[2]);
+			if(c[0] != 0.0f || c[1] != 0.0f || c[2] != 0.0f)
+				em.shadow(shadow_origin(sp, sdir), sdir, time, aslot, w[0] * c[0], w[1] * c[1], w[2] * c[2], scene);
 		}
 	}
 	/* final gather: diffuse rays end at their next hit (src/shader.cc:154-187) */
@@ -711,7 +738,10 @@ __device__ __forceinline__ void shade_one(const DScene &S, const RayRec &ray, co
 struct QueueEmitter {
 	ShadeOut *out;
 	int *overflow;
-	__device__ void shadow(V3 o, V3 d, int time, int slot, float r, float g, float b) { push_shadow(*out, o, d, time, slot, r, g, b, overflow); }
+	__device__ void shadow(V3 o, V3 d, int time, int slot, float r, float g, float b, int scene)
+	{
+		push_shadow(*out, o, d, time, slot, r, g, b, overflow, scene);
+	}
 	__device__ void gather(V3 pos, V3 n, int kind, int slot, float r, float g, float b) { push_gather(*out, pos, n, kind, slot, r, g, b, overflow); }
 	__device__ void child(const RayRec &c)
 	{
@@ -799,8 +829,9 @@ struct PoolEmitter {
 	unsigned long long shadows;
 	/* a light sample becomes a pool item of its own (iter = POOL_SHADOW),
 	 * traced by whichever thread claims it */
-	__device__ void shadow(V3 o, V3 d, int time, int slot, float r, float g, float b)
+	__device__ void shadow(V3 o, V3 d, int time, int slot, float r, float g, float b, int scene)
 	{
+		(void)scene;   /* scene sets render without the pool */
 		RayRec c;
 		c.o = o;
 		c.d = d;
@@ -905,11 +936,13 @@ __global__ void __launch_bounds__(SRAY_TRACE_THREADS, 6) k_shadow(DScene S, cons
 		ShadowReq r = sq[ri];
 		int time = __float_as_int(r.a.w), pixel = __float_as_int(r.b.w);
 		int res;
+		int scene = S.nscenes > 1 ? __float_as_int(r.w.w) : -1;
 		if(HYB) {
 			Hit h;
-			res = trace_two_level<COUNT, true, SORT>(S, mk(r.a.x, r.a.y, r.a.z), mk(r.b.x, r.b.y, r.b.z), time, h, &tc, &overflow);
+			res = trace_two_level<COUNT, true, SORT>(S, mk(r.a.x, r.a.y, r.a.z), mk(r.b.x, r.b.y, r.b.z), time, h, &tc, &overflow,
+					scene);
 		} else {
-			res = trace_any_octree_impl(S, mk(r.a.x, r.a.y, r.a.z), mk(r.b.x, r.b.y, r.b.z), time, &overflow) ? 1 : 0;
+			res = trace_any_octree_impl(S, mk(r.a.x, r.a.y, r.a.z), mk(r.b.x, r.b.y, r.b.z), time, &overflow, scene) ? 1 : 0;
 		}
 		if(HYB && res == 2) {
 			fb[1 + atomicAdd(fb, 1)] = ri;
@@ -943,7 +976,7 @@ __global__ void __launch_bounds__(128) k_shadow_warp(DScene S, const ShadowReq *
 		float best;
 		int bobj, bprim;
 		int res = warp_trace<true>(S, mk(r.a.x, r.a.y, r.a.z), mk(r.b.x, r.b.y, r.b.z), __float_as_int(r.a.w), s_ref[w], s_obj[w], s_te[w],
-				best, bobj, bprim);
+				best, bobj, bprim, S.nscenes > 1 ? __float_as_int(r.w.w) : -1);
 		if(lane == 0) {
 			if(res == 2) fb[1 + atomicAdd(fb, 1)] = ri;
 			else if(res == 0) acc_add(acc, __float_as_int(r.b.w), r.w.x, r.w.y, r.w.z);
@@ -1521,6 +1554,9 @@ void Renderer::fill_scene_desc()
 	D.sslots = sslots.as<int>();
 	D.has_scene = built && !sc.oct.nodes.empty() && !sc.objs.empty();
 	D.sroot = scene_root;
+	D.troot = 0;
+	D.nscenes = (int)scene_refs.size();
+	D.scenes = scene_refs.empty() ? nullptr : dscenes.as<DevSceneRef>();
 	D.mnodes = mnodes.as<DevNode>();
 	D.mtris = mtris.as<DevTri>();
 	D.mprim = mprim.as<int>();
@@ -1780,9 +1816,144 @@ int Renderer::upload_scene(cudaStream_t s)
 	return 0;
 }
 
+/* the object hierarchy over items [0, n): each boxed by the union of the
+ * octree leaves that list it (so that it is entered whenever the octree
+ * would test it), one item per leaf; node references offset by tbase, an
+ * item i becomes object ~(obj0 + i) */
+static void object_hierarchy(const BuildOctree &oct, size_t no, int obj0, int tbase, std::vector<DevBvh4> &tn)
+{
+	std::vector<Box> ub(no);
+	for(size_t i = 0; i < no; i++) for(int k = 0; k < 3; k++) { ub[i].mn[k] = DBL_MAX; ub[i].mx[k] = -DBL_MAX; }
+	for(const BuildOctree::Node &n : oct.nodes) {
+		if(n.child >= 0) continue;
+		for(int it : n.items) {
+			for(int k = 0; k < 3; k++) {
+				ub[it].mn[k] = std::min(ub[it].mn[k], n.box.mn[k]);
+				ub[it].mx[k] = std::max(ub[it].mx[k], n.box.mx[k]);
+			}
+		}
+	}
+	std::vector<float> mn(no * 3), mx(no * 3);
+	for(size_t i = 0; i < no; i++) {
+		for(int k = 0; k < 3; k++) {
+			float lo = (float)ub[i].mn[k], hi = (float)ub[i].mx[k];
+			if((double)lo > ub[i].mn[k]) lo = nextafterf(lo, -INFINITY);
+			if((double)hi < ub[i].mx[k]) hi = nextafterf(hi, INFINITY);
+			if(!(ub[i].mn[k] <= ub[i].mx[k])) { lo = FLT_MAX; hi = -FLT_MAX; }   /* listed in no leaf */
+			mn[i * 3 + k] = lo;
+			mx[i * 3 + k] = hi;
+		}
+	}
+	MeshBvh tl;
+	tl.build_items(mn.data(), mx.data(), no, 1);
+	std::vector<DevBvh4> part;
+	tl.collapse4(part);
+	for(DevBvh4 &d : part) {
+		for(int k = 0; k < 4; k++) {
+			int ref = d.child[k];
+			if(ref == BVH_NONE) continue;
+			if(ref >= 0) {
+				d.child[k] = ref + tbase;
+				continue;
+			}
+			unsigned v = ~(unsigned)ref;
+			d.child[k] = ~(obj0 + tl.order[v >> 4]);   /* leaf: the object itself */
+		}
+	}
+	tn.insert(tn.end(), part.begin(), part.end());
+}
+
+/* A scene set's frame: every scene's octree over its own objects (the
+ * reference's Scene::build_tree, src/scene.cc:353-390, per scene) and object
+ * hierarchy, side by side in one node table; their roots, lights and
+ * environments in the scene descriptors; the cameras' matrices per scene */
+int Renderer::build_frame_set(long bt0, long bt1, cudaStream_t s)
+{
+	t0 = (int)bt0;
+	t1 = (int)bt1;
+	sc.build_tree(t0, t1, opt);   /* over every object: the union's box (photon grids, object bounds cache) */
+	int ns = (int)sc.ranges.size();
+	std::vector<DevNode> nodes;
+	std::vector<int> slots, ohome_h(sc.objs.size(), 0);
+	std::vector<DevBvh4> tn;
+	scene_refs.assign(ns, DevSceneRef());
+	int shutter = 0;
+	for(int k = 0; k < ns; k++) {
+		const SceneRange &rg = sc.ranges[k];
+		DevSceneRef &R = scene_refs[k];
+		memset(&R, 0, sizeof R);
+		R.sroot = R.troot = -1;
+		R.light0 = rg.light0;
+		R.nlights = rg.nlight;
+		for(int c = 0; c < 4; c++) { R.env_col[c] = (float)rg.env_col[c]; R.env_amb[c] = (float)rg.env_amb[c]; }
+		if(rg.cam.shutter > shutter) shutter = rg.cam.shutter;
+		if(rg.nobj == 0) continue;
+		std::vector<Box> boxes(rg.nobj);
+		for(int i = 0; i < rg.nobj; i++) {
+			Box a = sc.object_bounds(rg.obj0 + i, t0), b = t1 == t0 ? a : sc.object_bounds(rg.obj0 + i, t1);
+			for(int c = 0; c < 3; c++) {
+				boxes[i].mn[c] = a.mn[c] < b.mn[c] ? a.mn[c] : b.mn[c];
+				boxes[i].mx[c] = a.mx[c] > b.mx[c] ? a.mx[c] : b.mx[c];
+			}
+		}
+		BuildOctree oct;
+		oct.build(boxes, opt.scnoct_max_depth, opt.scnoct_max_items);
+		size_t slot0 = slots.size();
+		std::vector<int> index_of, hm;
+		flatten_octree(oct, nodes, slots, &index_of);
+		for(size_t q = slot0; q < slots.size(); q++) slots[q] += rg.obj0;
+		R.sroot = (int)(nodes.size() - oct.nodes.size());
+		R.troot = (int)tn.size();
+		object_hierarchy(oct, (size_t)rg.nobj, rg.obj0, R.troot, tn);
+		octree_homes_boxes(oct, boxes, index_of, hm);
+		for(int i = 0; i < rg.nobj; i++) ohome_h[rg.obj0 + i] = hm[i];
+	}
+	scene_root = ns > 0 ? scene_refs[0].sroot : 0;
+	tlo = t0 - shutter - 2;
+	int thi = t1 + shutter + 2;
+	nt = thi - tlo + 1;
+	size_t nobj = sc.objs.size(), nlt = sc.lights.size();
+	CK(xf.ensure(nobj * nt * XF_STRIDE * sizeof(float) + 16), "transform table");
+	CK(light_pos.ensure(nlt * nt * 4 * sizeof(float) + 16), "light positions");
+	size_t nthr = (nobj + nlt) * (size_t)nt;
+	if(nthr) {
+		LAUNCH(*this, "xforms", s, k_xforms<<<(unsigned)((nthr + 127) / 128), 128, 0, s>>>(anims.as<DevAnim>(), key_t.as<int>(),
+				key_v.as<double>(), (int)nobj, (int)nlt, tlo, nt, xf.as<float>(), light_pos.as<float>()));
+		CK(cudaGetLastError(), "transform table");
+	}
+	std::vector<float> cm((size_t)ns * nt * 12);
+	for(int k = 0; k < ns; k++) {
+		for(int t = 0; t < nt; t++) {
+			double m[4][4];
+			sc.ranges[k].cam.matrix(tlo + t, m);
+			for(int r = 0; r < 3; r++) for(int c = 0; c < 4; c++) cm[((size_t)k * nt + t) * 12 + r * 4 + c] = (float)m[r][c];
+		}
+	}
+	CK(snodes.upload(nodes, s), "upload scene nodes");
+	CK(sslots.upload(slots, s), "upload scene slots");
+	CK(tnodes.upload(tn, s), "upload object hierarchies");
+	CK(ohome.upload(ohome_h, s), "upload object home nodes");
+	CK(dscenes.upload(scene_refs, s), "upload scene descriptors");
+	has_tlas = !tn.empty();
+	CK(cam_m.upload(cm, s), "upload cameras");
+	h2d += (int64_t)(nodes.size() * sizeof(DevNode) + slots.size() * 4 + cm.size() * 4 + tn.size() * sizeof(DevBvh4));
+	CK(cudaStreamSynchronize(s), "build frame");
+	built = true;
+	photons_ready = false;
+	caust.map.n = 0;
+	gi.map.n = 0;
+	fill_scene_desc();
+	return 0;
+}
+
 int Renderer::build_frame(long bt0, long bt1, cudaStream_t s)
 {
 	if(!loaded) return fail(SRAY_ESTATE, "no scene loaded");
+	if(sc.ranges.size() > 1) {
+		if(!in_batch) return fail(SRAY_ESTATE, "a scene set renders through sray_gpu_render_batch");
+		return build_frame_set(bt0, bt1, s);
+	}
+	scene_refs.clear();
 	t0 = (int)bt0;
 	t1 = (int)bt1;
 	sc.build_tree(t0, t1, opt);
@@ -1879,13 +2050,17 @@ int Renderer::shoot_maps(const DScene &base, cudaStream_t s, int *nc, int *ng)
 	caust.map.n = 0;
 	gi.map.n = 0;
 	*nc = *ng = 0;
-	if(!(opt.caust_photons || opt.gi_photons) || sc.lights.empty()) return 0;
+	/* the lights and objects of the maps' scene (a batch job's in a scene set) */
+	int l0 = map_light0, nl = map_nlight >= 0 ? map_nlight : (int)sc.lights.size();
+	int o0 = map_obj0, no = map_nobj >= 0 ? map_nobj : (int)sc.objs.size();
+	int cp = map_counts[0] >= 0 ? map_counts[0] : opt.caust_photons, gp = map_counts[1] >= 0 ? map_counts[1] : opt.gi_photons;
+	if(!(cp || gp) || nl == 0) return 0;
 	/* projection maps (src/render.cc:87-103) over the photons' interval */
-	sc.build_projmaps(base.t0, base.t1, opt.seed);
-	std::vector<uint32_t> bits(sc.lights.size() * 128, 0u);
-	std::vector<float> cov(sc.lights.size() * 2);
-	for(size_t i = 0; i < sc.lights.size(); i++) {
-		const Light &L = sc.lights[i];
+	sc.build_projmaps(base.t0, base.t1, opt.seed, l0, nl, o0, no);
+	std::vector<uint32_t> bits((size_t)nl * 128, 0u);
+	std::vector<float> cov((size_t)nl * 2);
+	for(size_t i = 0; i < (size_t)nl; i++) {
+		const Light &L = sc.lights[l0 + i];
 		for(int k = 0; k < 2048; k++) {
 			if(L.pm.cells[k]) bits[i * 128 + (k >> 5)] |= 1u << (k & 31);
 			if(L.spm.cells[k]) bits[i * 128 + 64 + (k >> 5)] |= 1u << (k & 31);
@@ -1909,14 +2084,41 @@ int Renderer::photon_job(DScene base)
 	/* a batch: each job's maps over its own interval, then their table */
 	size_t n = batch_t0.size();
 	std::vector<DPhotonMap> hm(2 * n);
+	const DScene base0 = base;
 	for(size_t j = 0; j < n; j++) {
+		base = base0;
 		base.t0 = batch_t0[j];
 		base.t1 = batch_t1[j];
+		int o0 = 0, no = (int)sc.objs.size();
+		if(!scene_refs.empty()) {
+			/* a scene set: the view of the job's scene (its roots and lights),
+			 * its own photon counts */
+			int k = batch_scene[j];
+			const SceneRange &rg = sc.ranges[k];
+			const DevSceneRef &ref = scene_refs[k];
+			base.sroot = ref.sroot;
+			base.troot = ref.troot;
+			base.has_scene = base0.has_scene && ref.sroot >= 0;
+			base.lights = base0.lights + rg.light0;
+			base.nlights = rg.nlight;
+			base.light_pos = base0.light_pos + (size_t)rg.light0 * nt * 4;
+			base.nscenes = 0;
+			base.scenes = nullptr;
+			map_light0 = rg.light0;
+			map_nlight = rg.nlight;
+			map_obj0 = o0 = rg.obj0;
+			map_nobj = no = rg.nobj;
+		}
+		map_counts[0] = batch_caust[j] > 0 ? batch_caust[j] : -1;
+		map_counts[1] = batch_gi[j] > 0 ? batch_gi[j] : -1;
 		/* the radius Scene::build_tree gives the job's own frame: the batch's
 		 * tree spans every job's interval */
-		map_gather_dist = sc.gather_dist_at(batch_t0[j], batch_t1[j], opt);
+		map_gather_dist = sc.gather_dist_at(batch_t0[j], batch_t1[j], opt, o0, no);
 		int r = shoot_maps(base, ps, &c, &g);
 		map_gather_dist = -1.0;
+		map_light0 = map_obj0 = 0;
+		map_nlight = map_nobj = -1;
+		map_counts[0] = map_counts[1] = -1;
 		if(r) return r;
 		std::swap(caust, job_maps[j].caust);
 		std::swap(gi, job_maps[j].gi);
@@ -2391,12 +2593,23 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 		int *next_count = b == 0 ? cnt + 6 : cnt + 7;
 		int *next_list = active[b].as<int>();
 		int n_prim = n_active * width;
-		if(ensure_queue(0, n_prim)) return SRAY_ECUDA;
+		/* waves: at most tune.queue_depth primary rays (whole pixels) per
+		 * wave, each traced to the end of its shading tree before the next
+		 * starts; the queues are sized for a wave, the accumulators for the
+		 * batch */
+		int wave_pix = n_active;
+		if(tune.queue_depth > 0) {
+			wave_pix = tune.queue_depth / width;
+			if(wave_pix < 1) wave_pix = 1;
+			if(wave_pix > n_active) wave_pix = n_active;
+		}
+		int wave_rays = wave_pix * width;
+		if(ensure_queue(0, wave_rays)) return SRAY_ECUDA;
 		CK(acc.ensure((size_t)n_prim * 16), "accumulator");
 		if(int r = nrc_setup(b, n_prim, s)) return r;
 		if(photons_pending) {
 			photons_pending = false;
-			int64_t cap = (int64_t)n_prim * 3 + 65536;
+			int64_t cap = (int64_t)wave_rays * 3 + 65536;
 			if(cap > INT_MAX / 2) cap = INT_MAX / 2;
 			CK(gq.ensure((size_t)cap * sizeof(GatherReq)), "gather queue");
 			CK(cudaMemsetAsync(cnt + 2, 0, sizeof(int), s), "reset gather queue");
@@ -2405,11 +2618,14 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			gq_defer_cap = cap;
 			gq_upper = 0;
 		}
+		for(int a0 = 0; a0 < n_active; a0 += wave_pix) {
+		int na = n_active - a0 < wave_pix ? n_active - a0 : wave_pix;
+		int n_wave = na * width;
 		q[0].count = cnt + 0;
 		q[1].count = cnt + 1;
-		LAUNCH(*this, "camera", s, k_camera<<<grid_for(n_prim, 256), 256, 0, s>>>(S, act, act_count, s0, width, q[0], acc.as<float4>(),
+		LAUNCH(*this, "camera", s, k_camera<<<grid_for(n_wave, 256), 256, 0, s>>>(S, act, a0, na, s0, width, q[0], acc.as<float4>(),
 				ctr.as<DevCounters>()));
-		int n_rays = n_prim;
+		int n_rays = n_wave;
 		int cur = 0;
 		bool tail_done = false;
 		for(int depth = 0; n_rays > 0; depth++) {
@@ -2421,7 +2637,8 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 				if(int r = flush_gathers()) return r;
 			/* the pool holds every ray of the rest of the tree: enter it only
 			 * with POOL_HEADROOM times the rays' room in the queue */
-			if(depth >= 1 && !tail_done && n_rays <= tune.render_tail && (int64_t)n_rays * POOL_HEADROOM <= q[cur].cap) {
+			if(depth >= 1 && !tail_done && n_rays <= tune.render_tail && (int64_t)n_rays * POOL_HEADROOM <= q[cur].cap &&
+					S.nscenes <= 1) {
 				/* the rest of the shading tree in one launch (k_render_pool) */
 				tail_done = true;
 				if(int r = flush_gathers()) return r;
@@ -2512,8 +2729,10 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			n_rays = h_cnt;
 			cur ^= 1;
 		}
+		/* the wave's gathers (the first wave's wait for the photon maps) */
 		if(int r = flush_gathers()) return r;
 		if(int r = join_side()) return r;
+		}
 		if(int r = nrc_batch_done(b, s)) return r;
 		CK(cudaMemsetAsync(next_count, 0, sizeof(int), s), "reset next active");
 		LAUNCH(*this, "finish", s, k_finish<<<grid_for(n_active, 256), 256, 0, s>>>(act, act_count, s0, width, acc.as<float4>(),
@@ -2684,14 +2903,25 @@ int Renderer::render_batch(const sray_job *jobs, int n, cudaStream_t s)
 {
 	if(!loaded) return fail(SRAY_ESTATE, "no scene loaded");
 	if(!jobs || n < 1 || n > 4096) return fail(SRAY_EINVAL, "a batch holds 1 to 4096 jobs");
-	long shutter = sc.cam.shutter;
+	int nsc = sc.ranges.empty() ? 1 : (int)sc.ranges.size();
+	if(nsc > 1 && opt.nrc) return fail(SRAY_EINVAL, "the radiance cache serves one scene: a scene set renders with nrc = 0");
 	std::vector<DevJob> hj(n);
 	std::vector<long> f0(n), f1(n);
 	int64_t total = 0;
 	long bt0 = 0, bt1 = 0;
+	batch_scene.assign(n, 0);
+	batch_caust.assign(n, 0);
+	batch_gi.assign(n, 0);
 	for(int j = 0; j < n; j++) {
 		const sray_job &J = jobs[j];
 		if(J.width <= 0 || J.height <= 0 || !J.fb) return fail(SRAY_EINVAL, "bad job");
+		if(J.scene < 0 || J.scene >= nsc) return fail(SRAY_EINVAL, "job scene out of range");
+		if(J.caust_photons < 0 || J.gi_photons < 0) return fail(SRAY_EINVAL, "negative job photon count");
+		const Camera &cam = nsc > 1 ? sc.ranges[J.scene].cam : sc.cam;
+		long shutter = cam.shutter;
+		batch_scene[j] = J.scene;
+		batch_caust[j] = J.caust_photons;
+		batch_gi[j] = J.gi_photons;
 		f0[j] = J.msec - shutter / 2;
 		f1[j] = f0[j] + shutter;
 		bt0 = j ? std::min(bt0, f0[j]) : f0[j];
@@ -2702,14 +2932,18 @@ int Renderer::render_batch(const sray_job *jobs, int n, cudaStream_t s)
 		d.width = J.width;
 		d.height = J.height;
 		d.t0 = (int)f0[j];
-		d.cam_f = (float)(1.0 / tan(0.5 * sc.cam.vfov));
-		d.cam_xsz = (float)(sc.cam.aspect * 2.0);   /* the camera's aspect, as for a single frame */
+		d.cam_f = (float)(1.0 / tan(0.5 * cam.vfov));
+		d.cam_xsz = (float)(cam.aspect * 2.0);   /* the camera's aspect, as for a single frame */
 		d.cam_ysz = 2.0f;
+		d.scene = J.scene;
 		total += (int64_t)J.width * J.height;
 		if(total > (1 << 27)) return fail(SRAY_EINVAL, "a batch holds at most 2^27 pixels");
 	}
+	in_batch = true;
 	int r = build_frame(bt0, bt1, s);
+	in_batch = false;
 	if(r) return r;
+	for(int j = 0; j < n; j++) hj[j].cam_base = hj[j].scene * nt;   /* its scene's camera in the frame's table */
 	/* each job's photon maps, shot over its own interval by the photon
 	 * thread while the batch's first bounces run (their gathers wait) */
 	if(job_maps.size() < (size_t)n) job_maps.resize(n);   /* kept: their buffers are reused by the next batch */
@@ -2772,6 +3006,11 @@ static int check_ctx_device()
 #define NEED_CTX() do { \
 		if(!g_R) { g_err = "sray_gpu_init has not been called"; return SRAY_ESTATE; } \
 		if(int r_dev_ = check_ctx_device()) return r_dev_; \
+	} while(0)
+
+/* entry points of a single scene: a scene set renders through batches */
+#define NEED_SINGLE() do { \
+		if(g_R->sc.ranges.size() > 1) { g_err = "a scene set renders through sray_gpu_render_batch"; return SRAY_ESTATE; } \
 	} while(0)
 
 extern "C" {
@@ -2922,6 +3161,32 @@ int sray_gpu_load_scene_sidecar(const char *path, const char *sidecar, int *used
 	return load_scene_text(buf.data(), buf.size(), sidecar, used);
 }
 
+int sray_gpu_load_scene_set(const char *const *xml_paths, int n)
+{
+	NEED_CTX();
+	Renderer &R = *g_R;
+	if(!xml_paths || n < 1 || n > 4096) { g_err = "a scene set holds 1 to 4096 documents"; return SRAY_EINVAL; }
+	R.loaded = false;
+	R.built = false;
+	R.photons_ready = false;
+	HostScene set;
+	for(int k = 0; k < n; k++) {
+		if(!xml_paths[k]) { g_err = "null document path"; return SRAY_EINVAL; }
+		std::string buf, err;
+		int r = read_file(xml_paths[k], buf);
+		if(r) return r;
+		HostScene one;
+		if(!one.load(buf.data(), buf.size(), R.opt, err)) { g_err = std::string(xml_paths[k]) + ": " + err; return SRAY_ELOAD; }
+		if(k == 0) set = std::move(one);
+		else set.append_scene(std::move(one));
+	}
+	R.sc = std::move(set);
+	int r = R.upload_scene(0);
+	if(r) { g_err = R.err; return r; }
+	R.loaded = true;
+	return 0;
+}
+
 int sray_gpu_add_data_path(const char *dir)
 {
 	if(!dir) { g_err = "null directory"; return SRAY_EINVAL; }
@@ -2948,6 +3213,7 @@ int sray_gpu_scene_info(int *n_objects, int *n_lights, int *n_materials, int64_t
 int sray_gpu_build(long t0, long t1)
 {
 	NEED_CTX();
+	NEED_SINGLE();
 	int r = g_R->build_frame(t0, t1, 0);
 	if(r) g_err = g_R->err;
 	return r;
@@ -2956,6 +3222,7 @@ int sray_gpu_build(long t0, long t1)
 int sray_gpu_shoot_photons(long t0, long t1, int *caust_stored, int *gi_stored, void *stream)
 {
 	NEED_CTX();
+	NEED_SINGLE();
 	Renderer &R = *g_R;
 	if(!R.built || R.t0 != (int)t0 || R.t1 != (int)t1) {
 		int r = R.build_frame(t0, t1, as_stream(stream));
@@ -2976,6 +3243,7 @@ static void frame_interval(const Renderer &R, long msec, long *t0, long *t1)
 int sray_gpu_render_pixels(long msec, float *fb, int fb_is_device, void *stream)
 {
 	NEED_CTX();
+	NEED_SINGLE();
 	if(!fb) { g_err = "null framebuffer"; return SRAY_EINVAL; }
 	g_R->h2d = g_R->d2h = 0;
 	int r = g_R->render_pixels(msec, fb, fb_is_device, as_stream(stream));
@@ -3012,6 +3280,7 @@ static int render_frame(Renderer &R, long msec, float *fb, int fb_is_device, cud
 int sray_gpu_render(long msec, float *fb, int fb_is_device, void *stream)
 {
 	NEED_CTX();
+	NEED_SINGLE();
 	Renderer &R = *g_R;
 	if(!R.loaded) { g_err = "no scene loaded"; return SRAY_ESTATE; }
 	if(!fb) { g_err = "null framebuffer"; return SRAY_EINVAL; }
@@ -3029,6 +3298,10 @@ static int check_tuning(const sray_tuning *t)
 	if(t->warp_rays < 0 || t->warp_rays > (1 << 24)) { g_err = "warp_rays must be 0..2^24"; return SRAY_EINVAL; }
 	if(t->warp_segments < 0 || t->warp_segments > (1 << 24)) { g_err = "warp_segments must be 0..2^24"; return SRAY_EINVAL; }
 	if(t->side_gather < 0 || t->side_gather > 2) { g_err = "side_gather must be 0, 1 or 2"; return SRAY_EINVAL; }
+	if(t->queue_depth != 0 && (t->queue_depth < 1024 || t->queue_depth > (1 << 27))) {
+		g_err = "queue_depth must be 0 or 1024..2^27";
+		return SRAY_EINVAL;
+	}
 	return 0;
 }
 
@@ -3057,6 +3330,7 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 		sray_tune_trial *log, int log_cap, int *n_log)
 {
 	NEED_CTX();
+	NEED_SINGLE();
 	Renderer &R = *g_R;
 	if(!R.loaded) { g_err = "no scene loaded"; return SRAY_ESTATE; }
 	if(!fb || frames < 1) { g_err = "bad arguments"; return SRAY_EINVAL; }
@@ -3065,19 +3339,18 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 	static const int pools[] = {2, 4, 8, 16};
 	static const int ptails[] = {16384, 65536, 262144, 1048576};
 	static const int binary[] = {0, 1}, prios[] = {0, 1, 2}, wrays[] = {0, 4096, 16384, 65536, 262144};
+	static const int depths[] = {0, 1 << 16, 1 << 18, 1 << 20};
 	struct Knob { int sray_tuning::*field; const int *vals; int n; };
 	const Knob knobs[] = {{&sray_tuning::render_tail, tails, 5}, {&sray_tuning::pool_blocks_per_sm, pools, 4},
 		{&sray_tuning::photon_tail, ptails, 4}, {&sray_tuning::shadow_order, binary, 2}, {&sray_tuning::stream_priority, prios, 3},
-		{&sray_tuning::warp_rays, wrays, 5}, {&sray_tuning::warp_segments, wrays, 5}, {&sray_tuning::side_gather, binary, 2}};
+		{&sray_tuning::warp_rays, wrays, 5}, {&sray_tuning::warp_segments, wrays, 5}, {&sray_tuning::queue_depth, depths, 4},
+		{&sray_tuning::side_gather, binary, 2}};
 	std::vector<sray_tune_trial> done;
 	cudaEvent_t e0, e1;
 	if(cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) { g_err = "autotune events"; return SRAY_ECUDA; }
 	auto trial = [&](const sray_tuning &t, float *ms) -> int {
 		for(const sray_tune_trial &d : done) {
-			if(d.tuning.render_tail == t.render_tail && d.tuning.pool_blocks_per_sm == t.pool_blocks_per_sm &&
-					d.tuning.photon_tail == t.photon_tail && d.tuning.shadow_order == t.shadow_order &&
-					d.tuning.stream_priority == t.stream_priority && d.tuning.warp_rays == t.warp_rays &&
-					d.tuning.warp_segments == t.warp_segments && d.tuning.side_gather == t.side_gather) {
+			if(memcmp(&d.tuning, &t, sizeof t) == 0) {
 				*ms = d.ms_per_frame;
 				return 0;
 			}
@@ -3127,6 +3400,60 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 	return 0;
 }
 
+int sray_gpu_autotune_batch(const sray_job *jobs, int n, int frames, void *stream, sray_tuning *best, float *best_ms,
+		sray_tune_trial *log, int log_cap, int *n_log)
+{
+	NEED_CTX();
+	Renderer &R = *g_R;
+	if(!R.loaded) { g_err = "no scene loaded"; return SRAY_ESTATE; }
+	if(!jobs || n < 1 || frames < 1) { g_err = "bad arguments"; return SRAY_EINVAL; }
+	cudaStream_t s = as_stream(stream);
+	static const int depths[] = {1 << 16, 1 << 18, 1 << 20};
+	/* thread per ray; warp per ray in the tails; warp per ray everywhere */
+	static const int modes[] = {0, 16384, 1 << 24};
+	std::vector<sray_tune_trial> done;
+	cudaEvent_t e0, e1;
+	if(cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) { g_err = "autotune events"; return SRAY_ECUDA; }
+	sray_tuning base = R.tune, cur = R.tune;
+	float cur_ms = 0.0f;
+	int r = 0;
+	for(int di = 0; di < 3 && !r; di++) {
+		for(int mi = 0; mi < 3 && !r; mi++) {
+			sray_tuning t = base;
+			t.queue_depth = depths[di];
+			t.warp_rays = t.warp_segments = modes[mi];
+			R.tune = t;
+			r = R.render_batch(jobs, n, s);
+			if(r) { g_err = R.err; break; }
+			cudaEventRecord(e0, s);
+			for(int i = 0; i < frames && !r; i++) r = R.render_batch(jobs, n, s);
+			cudaEventRecord(e1, s);
+			if(r) { g_err = R.err; break; }
+			if(cudaEventSynchronize(e1) != cudaSuccess) { g_err = "autotune timing"; r = SRAY_ECUDA; break; }
+			float t_ms = 0.0f;
+			cudaEventElapsedTime(&t_ms, e0, e1);
+			sray_tune_trial tr;
+			memset(&tr, 0, sizeof tr);
+			tr.tuning = t;
+			tr.ms_per_frame = t_ms / (float)frames;
+			done.push_back(tr);
+			if(done.size() == 1 || tr.ms_per_frame < cur_ms) {
+				cur = t;
+				cur_ms = tr.ms_per_frame;
+			}
+		}
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	R.tune = r ? base : cur;
+	if(r) return r;
+	if(best) *best = cur;
+	if(best_ms) *best_ms = cur_ms;
+	if(n_log) *n_log = (int)done.size();
+	for(int i = 0; log && i < log_cap && i < (int)done.size(); i++) log[i] = done[i];
+	return 0;
+}
+
 int sray_gpu_render_batch(const sray_job *jobs, int n, void *stream)
 {
 	NEED_CTX();
@@ -3143,6 +3470,7 @@ int sray_gpu_cast_rays(int n, const float *orig, const float *dir, const int *ti
 		unsigned char *tie, void *stream)
 {
 	NEED_CTX();
+	NEED_SINGLE();
 	Renderer &R = *g_R;
 	if(!R.built) { g_err = "acceleration structures not built"; return SRAY_ESTATE; }
 	if(n < 0 || (n > 0 && (!orig || !dir || !obj || !prim || !t || !tie))) { g_err = "bad arguments"; return SRAY_EINVAL; }
@@ -3163,6 +3491,7 @@ int sray_gpu_cast_rays(int n, const float *orig, const float *dir, const int *ti
 int sray_gpu_primary_hits(long msec, int *obj, int *prim, float *t, unsigned char *tie, void *stream)
 {
 	NEED_CTX();
+	NEED_SINGLE();
 	Renderer &R = *g_R;
 	if(!R.loaded) { g_err = "no scene loaded"; return SRAY_ESTATE; }
 	if(!obj || !prim || !t || !tie) { g_err = "bad arguments"; return SRAY_EINVAL; }
@@ -3185,7 +3514,7 @@ int sray_gpu_primary_hits(long msec, int *obj, int *prim, float *t, unsigned cha
 	e = cudaMemcpyAsync(cnt + 3, &npix, sizeof(int), cudaMemcpyHostToDevice, s);
 	if(e != cudaSuccess) { g_err = cudaGetErrorString(e); return SRAY_ECUDA; }
 	R.q[0].count = cnt + 0;
-	k_camera<<<grid_for(npix, 256), 256, 0, s>>>(R.S, nullptr, cnt + 3, 0, 1, R.q[0], R.acc.as<float4>(), R.ctr.as<DevCounters>());
+	k_camera<<<grid_for(npix, 256), 256, 0, s>>>(R.S, nullptr, 0, npix, 0, 1, R.q[0], R.acc.as<float4>(), R.ctr.as<DevCounters>());
 	if(R.trace_rays(R.q[0], npix, "trace", false, s)) { g_err = R.err; return SRAY_ECUDA; }
 	k_primary_hits<<<grid_for(npix, 256), 256, 0, s>>>(R.S, R.q[0], R.hits.as<int4>(), obj, prim, t, tie);
 	DevCounters hc;

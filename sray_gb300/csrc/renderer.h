@@ -165,7 +165,7 @@ struct Renderer {
 	cudaEvent_t ps_done = nullptr;
 	sray_stats stats;
 	/* the autotuner's choice on the production frame */
-	sray_tuning tune = {0, 4, 65536, 0, 2, 16384, 16384, 0};
+	sray_tuning tune = {0, 4, 65536, 0, 2, 16384, 16384, 0, 0};
 	int nsm = 0;                  /* multiprocessors of the device */
 	/* Octree retraces follow every hierarchy pass and nearly always find no
 	 * ray listed (a couple a frame).  Their grid-stride launches are sized
@@ -195,6 +195,14 @@ struct Renderer {
 	int batch_npix = 0;
 	std::vector<int> batch_t0, batch_t1;   /* jobs' shutter intervals: the photon job shoots one map pair each */
 	double map_gather_dist = -1.0;         /* >= 0: the range radius of the maps being built (a batch job's) */
+	/* the photon job of a batch job: its scene's lights and its photon counts (-1: all lights, the options') */
+	int map_light0 = 0, map_nlight = -1, map_counts[2] = {-1, -1}, map_obj0 = 0, map_nobj = -1;
+	std::vector<int> batch_scene, batch_caust, batch_gi;   /* jobs' scenes and photon counts (0: the options') */
+	/* a scene set: its scene descriptors on the device */
+	DevBuf dscenes;
+	std::vector<DevSceneRef> scene_refs;
+	bool in_batch = false;
+	int build_frame_set(long t0, long t1, cudaStream_t s);
 	DevBuf djobs, dmaps;
 	std::vector<JobMaps> job_maps;
 	int render_batch(const sray_job *jobs, int n, cudaStream_t s);

@@ -780,33 +780,37 @@ static void project_boxes(ProjMap *map, const Vec3 &lpos, const std::vector<Box>
 
 /* Light::build_proj_intern (src/light.cc:151-200); light samples on the
  * projection-map stream of the light */
-void HostScene::build_projmaps(int t0, int t1, uint64_t seed)
+void HostScene::build_projmaps(int t0, int t1, uint64_t seed, int light0, int nlight, int obj0, int nobj)
 {
+	if(nlight < 0) nlight = (int)lights.size() - light0;
+	if(nobj < 0) nobj = (int)objs.size() - obj0;
 	/* each light's maps depend only on its own random stream: one thread per light */
 	std::vector<std::thread> th;
-	for(size_t li = 0; li < lights.size(); li++) th.push_back(std::thread([this, li, t0, t1, seed]() { build_light_projmaps(li, t0, t1, seed); }));
+	for(int k = 0; k < nlight; k++)
+		th.push_back(std::thread([this, light0, k, t0, t1, seed, obj0, nobj]() { build_light_projmaps(light0 + k, t0, t1, seed, k, obj0, nobj); }));
 	for(auto &t : th) t.join();
 }
 
-void HostScene::build_light_projmaps(size_t li, int t0, int t1, uint64_t seed)
+void HostScene::build_light_projmaps(size_t li, int t0, int t1, uint64_t seed, int key, int obj0, int nobj)
 {
 	{
 		Light &L = lights[li];
 		L.pm.clear();
 		L.spm.clear();
-		if(objs.empty()) return;
+		if(nobj <= 0) return;
 		int tm[3] = {t0, t1, -1};
 		if(t0 == t1) tm[1] = -1;
 		int samples = L.type == LT_SPHERE ? 8 : 1;
 		/* one stream per light, drawn in order over both shutter ends */
 		sray_rng s;
-		sray_rng_init(&s, seed, SRAY_DOM_PROJMAP, (uint32_t)li, 0);
+		sray_rng_init(&s, seed, SRAY_DOM_PROJMAP, (uint32_t)key, 0);
 		for(int ti = 0; ti < 2 && tm[ti] != -1; ti++) {
-			std::vector<Box> boxes(objs.size()), cboxes;
-			for(size_t i = 0; i < objs.size(); i++) {
+			std::vector<Box> boxes((size_t)nobj), cboxes;
+			for(int j = 0; j < nobj; j++) {
+				size_t i = (size_t)(obj0 + j);
 				const Material &m = objs[i].mat >= 0 ? mats[objs[i].mat] : defmat;
-				boxes[i] = object_bounds(i, tm[ti]);
-				if(m.refl > 0.0 || m.refr > 0.0) cboxes.push_back(boxes[i]);
+				boxes[j] = object_bounds(i, tm[ti]);
+				if(m.refl > 0.0 || m.refr > 0.0) cboxes.push_back(boxes[j]);
 			}
 			for(int k = 0; k < samples; k++) {
 				Vec3 lp = L.xf.position(tm[ti]);
@@ -867,10 +871,11 @@ void HostScene::build_tree(int t0, int t1, const sray_opts &opt)
 /* gather_dist of Scene::build_tree(t0, t1) (src/scene.cc:384-387): the
  * diagonal of the union of every object's bounds at t0 and t1 (the scene
  * octree's root box) times the option */
-double HostScene::gather_dist_at(int t0, int t1, const sray_opts &opt) const
+double HostScene::gather_dist_at(int t0, int t1, const sray_opts &opt, int obj0, int nobj) const
 {
+	if(nobj < 0) nobj = (int)objs.size() - obj0;
 	double mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
-	for(size_t i = 0; i < objs.size(); i++) {
+	for(size_t i = (size_t)obj0; i < (size_t)(obj0 + nobj); i++) {
 		Box b[2] = {objs[i].bounds(meshes, t0), t1 == t0 ? objs[i].bounds(meshes, t0) : objs[i].bounds(meshes, t1)};
 		for(int j = 0; j < 2; j++)
 			for(int k = 0; k < 3; k++) {
@@ -1454,6 +1459,45 @@ void HostScene::finish_load(const sray_opts &opt, bool build_meshes)
 			o.is_static = true;
 		}
 	}
+}
+
+/* ---- a scene set ---- */
+void HostScene::append_scene(HostScene &&o)
+{
+	if(ranges.empty()) {
+		SceneRange r0;
+		r0.nobj = (int)objs.size();
+		r0.nlight = (int)lights.size();
+		r0.cam = cam;
+		r0.env_ior = env_ior;
+		memcpy(r0.env_col, env_col, sizeof env_col);
+		memcpy(r0.env_amb, env_amb, sizeof env_amb);
+		ranges.push_back(r0);
+	}
+	SceneRange r;
+	r.obj0 = (int)objs.size();
+	r.nobj = (int)o.objs.size();
+	r.light0 = (int)lights.size();
+	r.nlight = (int)o.lights.size();
+	r.cam = o.cam;
+	r.env_ior = o.env_ior;
+	memcpy(r.env_col, o.env_col, sizeof env_col);
+	memcpy(r.env_amb, o.env_amb, sizeof env_amb);
+	int tex0 = (int)texs.size(), mat0 = (int)mats.size(), mesh0 = (int)meshes.size();
+	for(Texture &t : o.texs) texs.push_back(std::move(t));
+	for(Material m : o.mats) {
+		for(int k = 0; k < TA_COUNT; k++) if(m.tex[k] >= 0) m.tex[k] += tex0;
+		mats.push_back(m);
+	}
+	for(Mesh &m : o.meshes) meshes.push_back(std::move(m));
+	for(Object ob : o.objs) {
+		if(ob.mat >= 0) ob.mat += mat0;
+		if(ob.mesh >= 0) ob.mesh += mesh0;
+		objs.push_back(ob);
+	}
+	for(const Light &l : o.lights) lights.push_back(l);
+	n_tris += o.n_tris;
+	ranges.push_back(r);
 }
 
 /* ---- a scene given as tables ---- */

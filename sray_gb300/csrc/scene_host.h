@@ -152,6 +152,14 @@ struct Camera {
 	void matrix(int t, double m[4][4]) const;
 };
 
+/* one scene of a scene set: its objects and lights (index ranges into the
+ * set's tables), camera and environment */
+struct SceneRange {
+	int obj0 = 0, nobj = 0, light0 = 0, nlight = 0;
+	Camera cam;
+	double env_ior = 1.0, env_col[4] = {0, 0, 0, 0}, env_amb[4] = {0, 0, 0, 0};
+};
+
 struct HostScene {
 	std::vector<Material> mats;
 	Material defmat;
@@ -162,6 +170,13 @@ struct HostScene {
 	Camera cam;
 	double env_ior = 1.0, env_col[4] = {0, 0, 0, 0}, env_amb[4] = {0, 0, 0, 0};
 	int64_t n_tris = 0;
+
+	/* a scene set (several documents loaded together for batches whose jobs
+	 * render different scenes): one range per scene; empty for one scene */
+	std::vector<SceneRange> ranges;
+	/* append `other` as the set's next scene (materials, textures, meshes,
+	 * objects and lights re-indexed) */
+	void append_scene(HostScene &&other);
 
 	/* per-frame state */
 	BuildOctree oct;
@@ -183,9 +198,12 @@ struct HostScene {
 	void finish_load(const sray_opts &opt, bool build_meshes);
 	void build_tree(int t0, int t1, const sray_opts &opt);
 	/* the gather radius build_tree(t0, t1) would set, without building */
-	double gather_dist_at(int t0, int t1, const sray_opts &opt) const;
-	void build_projmaps(int t0, int t1, uint64_t seed);
-	void build_light_projmaps(size_t li, int t0, int t1, uint64_t seed);
+	double gather_dist_at(int t0, int t1, const sray_opts &opt, int obj0 = 0, int nobj = -1) const;
+	/* the projection maps of lights [light0, light0 + nlight) over objects
+	 * [obj0, obj0 + nobj) (all by default); a light's stream is keyed by its
+	 * index within that range */
+	void build_projmaps(int t0, int t1, uint64_t seed, int light0 = 0, int nlight = -1, int obj0 = 0, int nobj = -1);
+	void build_light_projmaps(size_t li, int t0, int t1, uint64_t seed, int key, int obj0, int nobj);
 };
 
 /* general 4x4 inverse by the adjugate */

@@ -21,7 +21,8 @@ EXPORTS = ["sray_default_opts", "sray_gpu_init", "sray_gpu_set_opts", "sray_gpu_
            "sray_gpu_get_photons", "sray_gpu_dump_photons", "sray_gpu_restore_photons", "sray_gpu_render_batch",
            "sray_gpu_get_stats", "sray_gpu_nrc_stats", "sray_gpu_nrc_reset", "sray_gpu_get_tuning",
            "sray_gpu_set_tuning", "sray_gpu_autotune", "sray_gpu_set_profiling", "sray_gpu_kernel_times", "sray_gpu_last_error",
-           "sray_gpu_shutdown", "sray_gpu_set_faults", "sray_gpu_upload_scene", "sray_nrc_reset", "sray_nrc_set_params", "sray_nrc_get_params", "sray_nrc_infer",
+           "sray_gpu_shutdown", "sray_gpu_set_faults", "sray_gpu_upload_scene", "sray_gpu_load_scene_set",
+           "sray_gpu_autotune_batch", "sray_nrc_reset", "sray_nrc_set_params", "sray_nrc_get_params", "sray_nrc_infer",
            "sray_nrc_gradients", "sray_nrc_train", "sray_nrc_last_error"]
 
 NRC_PARAMS = 26563
@@ -51,7 +52,8 @@ class SrayNrcStats(ctypes.Structure):
 
 class SrayJob(ctypes.Structure):
     _fields_ = [("msec", ctypes.c_long), ("width", ctypes.c_int), ("height", ctypes.c_int), ("fb", ctypes.c_void_p),
-                ("reserved", ctypes.c_int * 4)]
+                ("scene", ctypes.c_int), ("caust_photons", ctypes.c_int), ("gi_photons", ctypes.c_int),
+                ("reserved", ctypes.c_int)]
 
 
 class SrayFaults(ctypes.Structure):
@@ -62,7 +64,7 @@ class SrayFaults(ctypes.Structure):
 class SrayTuning(ctypes.Structure):
     _fields_ = [("render_tail", ctypes.c_int), ("pool_blocks_per_sm", ctypes.c_int), ("photon_tail", ctypes.c_int),
                 ("shadow_order", ctypes.c_int), ("stream_priority", ctypes.c_int), ("warp_rays", ctypes.c_int),
-                ("warp_segments", ctypes.c_int), ("side_gather", ctypes.c_int)]
+                ("warp_segments", ctypes.c_int), ("queue_depth", ctypes.c_int), ("side_gather", ctypes.c_int)]
 
 
 class SrayTuneTrial(ctypes.Structure):
@@ -117,6 +119,10 @@ def load_library():
     L.sray_gpu_get_photons.argtypes = [ip, vp, ip, vp]
     L.sray_gpu_dump_photons.argtypes = [ip, ctypes.c_char_p]
     L.sray_gpu_render_batch.argtypes = [ctypes.POINTER(SrayJob), ip, vp]
+    L.sray_gpu_load_scene_set.argtypes = [ctypes.POINTER(ctypes.c_char_p), ip]
+    L.sray_gpu_autotune_batch.argtypes = [ctypes.POINTER(SrayJob), ip, ip, vp, ctypes.POINTER(SrayTuning),
+                                          ctypes.POINTER(ctypes.c_float), ctypes.POINTER(SrayTuneTrial), ip,
+                                          ctypes.POINTER(ctypes.c_int)]
     L.sray_gpu_restore_photons.argtypes = [ip, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]
     L.sray_gpu_get_stats.argtypes = [ctypes.POINTER(SrayStats)]
     L.sray_gpu_nrc_stats.argtypes = [ctypes.POINTER(SrayNrcStats)]
@@ -273,15 +279,42 @@ class GpuRenderer:
         self._chk(self.L.sray_gpu_render(msec, _ptr(fb), 1, _stream(stream)))
         return fb
 
-    def render_batch(self, jobs, stream=None):
-        """Render several frames in one wavefront: jobs = [(msec, fb)], fb a
-        CUDA tensor [height, width, 4] float32 per job."""
+    @staticmethod
+    def _jobs(jobs):
         arr = (SrayJob * len(jobs))()
-        for i, (msec, fb) in enumerate(jobs):
+        for i, job in enumerate(jobs):
+            msec, fb = job[0], job[1]
+            extra = job[2] if len(job) > 2 else {}
             arr[i].msec = msec
             arr[i].height, arr[i].width = int(fb.shape[0]), int(fb.shape[1])
             arr[i].fb = fb.data_ptr()
-        self._chk(self.L.sray_gpu_render_batch(arr, len(jobs), _stream(stream)))
+            arr[i].scene = int(extra.get("scene", 0))
+            arr[i].caust_photons = int(extra.get("caust_photons", 0))
+            arr[i].gi_photons = int(extra.get("gi_photons", 0))
+        return arr
+
+    def render_batch(self, jobs, stream=None):
+        """Render several frames in one wavefront: jobs = [(msec, fb)] or
+        [(msec, fb, {"scene": k, "caust_photons": c, "gi_photons": g})], fb a
+        CUDA tensor [height, width, 4] float32 per job."""
+        self._chk(self.L.sray_gpu_render_batch(self._jobs(jobs), len(jobs), _stream(stream)))
+
+    def load_scene_set(self, paths):
+        """Load several documents as one scene set (jobs pick theirs by index)."""
+        arr = (ctypes.c_char_p * len(paths))(*[p.encode() for p in paths])
+        self._chk(self.L.sray_gpu_load_scene_set(arr, len(paths)))
+
+    def autotune_batch(self, jobs, frames=2, stream=None):
+        """The batch autotuner: queue depth x traversal mode; returns (tuning,
+        ms per batch, [(tuning, ms) per trial])."""
+        best = SrayTuning()
+        ms = ctypes.c_float()
+        log = (SrayTuneTrial * 16)()
+        n = ctypes.c_int()
+        self._chk(self.L.sray_gpu_autotune_batch(self._jobs(jobs), len(jobs), frames, _stream(stream), ctypes.byref(best),
+                                                 ctypes.byref(ms), log, 16, ctypes.byref(n)))
+        trials = [(_tuning_dict(log[i].tuning), log[i].ms_per_frame) for i in range(min(n.value, 16))]
+        return _tuning_dict(best), ms.value, trials
 
     def render_pixels(self, msec=0, fb=None, stream=None):
         if fb is None:

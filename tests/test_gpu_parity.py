@@ -99,7 +99,8 @@ def test_image_small_scene(small_pair):
 
 @pytest.mark.parametrize("tuning", [dict(shadow_order=1), dict(stream_priority=1), dict(stream_priority=2),
                                     dict(warp_rays=1 << 24, warp_segments=1 << 24), dict(warp_rays=0, warp_segments=0),
-                                    dict(side_gather=1), dict(side_gather=2)])
+                                    dict(side_gather=1), dict(side_gather=2), dict(queue_depth=4096),
+                                    dict(queue_depth=1024, warp_rays=1 << 24, warp_segments=1 << 24)])
 def test_tuning_keeps_the_image(small_pair, tuning):
     # light samples' any-hit traversal in node order instead of nearest
     # first; the photon stream or the frame's own stream given priority;
@@ -509,3 +510,32 @@ def test_gpu_restores_reference_dumps(gpu_lib, tmp_path):
         print("restored %s: %d photons (energy %g); against the dump's text %.2g, against the reference's values %.2g"
               % (name, n, energy, fmt, full))
         assert fmt <= 1e-6 and full <= 1.5e-6
+
+
+def test_scene_set_batch_matches_oracle(gpu_lib, oracle_lib):
+    # a scene set (three documents: the small scene, the feature scene with
+    # moving objects and area lights, a terrain with instances) and one
+    # batch mixing their jobs at different times, resolutions and photon
+    # counts, in waves of 4096 primary rays: each job is its scene's own
+    # frame (FP32 oracle, pixels keyed by their place in the batch)
+    opts = dict(width=96, height=72, min_samples=1, max_samples=3, max_var=0.01, caust_photons=10000, gi_photons=20000,
+                iter=5, shadow_samples=2, diffuse_samples=1, mblur=1, shutter=40, gather_dist=0.02)
+    paths = [scenegen.write_scene("small"), scenegen.write_scene("feature"),
+             scenegen.write_scene("production", grid=(60, 30), n_inst=12)]
+    jobs = [(0, 96, 72, 0, {}), (40, 64, 48, 1, dict(caust_photons=5000, gi_photons=30000)),
+            (0, 64, 48, 2, dict(gi_photons=15000)), (100, 96, 72, 1, {}), (0, 48, 36, 0, dict(caust_photons=20000))]
+    g = gpu_lib.GpuRenderer(**opts)
+    g.load_scene_set(paths)
+    g.set_tuning(queue_depth=4096)
+    fbs = [torch.zeros((h, w, 4), dtype=torch.float32, device="cuda") for _, w, h, _, _ in jobs]
+    g.render_batch([(ms, fb, dict(extra, scene=k)) for (ms, _, _, k, extra), fb in zip(jobs, fbs)])
+    with pytest.raises(gpu_lib.SrayError):
+        g.render(0)                                  # a scene set renders through batches only
+    base = 0
+    for (ms, w, h, k, extra), fb in zip(jobs, fbs):
+        o = oracle_lib.Oracle(fp64=False, rng_mode=1, **dict(opts, width=w, height=h, **extra))
+        o.load(paths[k])
+        o.set_pixel_base(base)
+        img_o = o.render(ms)
+        assert _compare(fb.cpu().numpy(), img_o, "scene %d job %dx%d at %d ms (pixel base %d)" % (k, w, h, ms, base)) <= 1e-3
+        base += w * h
