@@ -44,7 +44,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="production", choices=["production", "small", "learned", "stress", "batch"])
-    ap.add_argument("--batch-jobs", type=int, default=16, help="jobs of the batch configuration")
+    ap.add_argument("--batch-jobs", type=int, default=64, help="jobs of the batch configuration")
+    ap.add_argument("--batch-scenes", type=int, default=16, help="scenes of the batch configuration's scene set")
     ap.add_argument("--no-nrc", action="store_true", help="skip the radiance-cache comparison")
     ap.add_argument("--method", default="plain", choices=["plain", "cache", "cache-everywhere"],
                     help="final gather of the headline frames: the plain gather, the radiance cache with its "
@@ -507,24 +508,48 @@ def nrc_vs_plain(args, reference):
 BATCH_SIZES = [(256, 256), (512, 512), (1280, 720), (1920, 1080)]
 
 
+def batch_workload(n_jobs, n_scenes, seed=0x5EED0B):
+    """The batched configuration: n_scenes seeded terrain-plus-moving-spheres
+    scenes with triangle counts log-uniform in [10k, 2M]; n_jobs jobs, job j
+    rendering scene j mod n_scenes at animation frame j div n_scenes (40 ms
+    apart), its resolution drawn from 256^2, 512^2, 720p and 1080p, its
+    photon count log-uniform in [100k, 2M] (a fifth caustic)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    tris = np.exp(rng.uniform(np.log(1e4), np.log(2e6), n_scenes)).astype(int)
+    sizes = [BATCH_SIZES[int(k)] for k in rng.integers(0, len(BATCH_SIZES), n_jobs)]
+    photons = np.exp(rng.uniform(np.log(1e5), np.log(2e6), n_jobs)).astype(int)
+    jobs = [dict(scene=j % n_scenes, msec=40 * (j // n_scenes), width=sizes[j][0], height=sizes[j][1],
+                 caust_photons=int(photons[j] // 5), gi_photons=int(photons[j] - photons[j] // 5)) for j in range(n_jobs)]
+    return [int(t) for t in tris], jobs
+
+
 def run_batch(args):
-    """Batched frames: `--batch-jobs` jobs of the production scene with
-    resolutions cycling through 256^2, 512^2, 720p and 1080p, frame times 40
-    ms apart, adaptive 1-16 spp, 200k global + 50k caustic photons per job,
-    rendered in one wavefront (sray_gpu_render_batch) against the same jobs
-    rendered one after another (sray_gpu_render)."""
+    """Batched rendering: `--batch-jobs` jobs over a scene set of
+    `--batch-scenes` scenes (batch_workload), motion blur over an 8 ms shutter
+    (8 time samples), adaptive 1-16 spp, in one wavefront per batch
+    (sray_gpu_render_batch) after the batch autotuner has picked the queue
+    depth (65,536 / 262,144 / 1,048,576 primary rays per wave) and the
+    traversal mode (thread per ray / warp per ray in the tails / warp per ray
+    everywhere); against the same jobs rendered one at a time."""
     import torch
     from sray_gb300 import build as gbuild, gpu, scenegen
     torch.cuda.set_device(0)
     gbuild.build()
-    opts = scenegen.scene_opts("production", caust_photons=50000, gi_photons=200000)
-    path = scenegen.write_scene("production")
+    tris, jobs = batch_workload(args.batch_jobs, args.batch_scenes)
+    t0 = time.perf_counter()
+    paths = [scenegen.write_scene("batch", seed=1000 + k, tris=t) for k, t in enumerate(tris)]
+    gen_s = time.perf_counter() - t0
+    opts = scenegen.scene_opts("production", mblur=1, shutter=8)
     g = gpu.GpuRenderer(**opts)
-    g.load(path)
+    t0 = time.perf_counter()
+    g.load_scene_set(paths)
+    load_s = time.perf_counter() - t0
     stream = torch.cuda.current_stream()
-    sizes = [BATCH_SIZES[i % len(BATCH_SIZES)] for i in range(args.batch_jobs)]
-    fbs = [torch.zeros((h, w, 4), dtype=torch.float32, device="cuda") for w, h in sizes]
-    jobs = [(40 * i, fb) for i, fb in enumerate(fbs)]
+    fbs = [torch.zeros((J["height"], J["width"], 4), dtype=torch.float32, device="cuda") for J in jobs]
+    spec = [(J["msec"], fb, dict(scene=J["scene"], caust_photons=J["caust_photons"], gi_photons=J["gi_photons"]))
+            for J, fb in zip(jobs, fbs)]
+    free0 = torch.cuda.mem_get_info()[0]
 
     def timed(fn, n):
         e0 = torch.cuda.Event(enable_timing=True)
@@ -539,42 +564,55 @@ def run_batch(args):
         return e0.elapsed_time(e1) / n, rays / n
 
     def batch():
-        g.render_batch(jobs, stream=stream)
+        g.render_batch(spec, stream=stream)
         return rays_of(g.stats())
 
     def singles():
         r = 0
-        for (w, h), (msec, fb) in zip(sizes, jobs):
-            g.set_opts(width=w, height=h)
-            g.render(msec, fb, stream=stream)
+        for job in spec:
+            g.render_batch([job], stream=stream)
             r += rays_of(g.stats())
         return r
 
+    g.set_tuning(queue_depth=1 << 20)      # bounded queues from the first batch on
+    batch()
+    tuning = None
+    if not args.no_autotune:
+        best, best_ms, trials = g.autotune_batch(spec, frames=1, stream=stream)
+        tuning = {"chosen": best, "ms_per_batch": best_ms,
+                  "trials": [dict(queue_depth=t["queue_depth"], warp_rays=t["warp_rays"], ms=round(ms, 2)) for t, ms in trials]}
     for _ in range(args.warmup):
         batch()
+    device_mb = (free0 - torch.cuda.mem_get_info()[0]) / 1e6
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
     ms_b, rays_b = timed(batch, args.steps)
     clk = clocks.stop()
-    launches = g.stats()["kernel_launches"]
-    singles()
-    ms_s, rays_s = timed(singles, args.steps)
+    st = g.stats()
+    ms_s, rays_s = timed(singles, 1)
     g.close()
     line = {
         "metric": METRIC, "value": rays_b / (ms_b / 1e3) / 1e6, "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_b, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded scene generator, no dataset)",
-        "config": {"workload": "batch: %d jobs of the production scene (resolutions cycling 256^2, 512^2, 1280x720, "
-                               "1920x1080; frames 40 ms apart; adaptive 1-16 spp; 200k global + 50k caustic photons "
-                               "per job) in one wavefront" % args.batch_jobs,
-                   "method": "plain gather", "jobs": [list(sz) for sz in sizes]},
-        "batch_vs_single": {"batch_ms": ms_b, "single_frames_ms": ms_s, "speedup": ms_s / ms_b,
+        "config": {"workload": "batch: %d jobs over %d scenes (terrain + 24 moving spheres, %d to %d triangles, %.1fM in "
+                               "all), each job a scene at its own animation frame, resolution from 256^2, 512^2, 1280x720, "
+                               "1920x1080, 100k-2M photons, motion blur over an 8 ms shutter (8 time samples), adaptive "
+                               "1-16 spp, depth 8, k=100 gathers within r<=0.5; one wavefront per batch"
+                               % (len(jobs), len(tris), min(tris), max(tris), sum(tris) / 1e6),
+                   "method": "plain gather", "tuning": tuning,
+                   "pixels": sum(J["width"] * J["height"] for J in jobs),
+                   "photons": sum(J["caust_photons"] + J["gi_photons"] for J in jobs)},
+        "batch_vs_single": {"batch_ms": ms_b, "jobs_one_at_a_time_ms": ms_s, "speedup": ms_s / ms_b,
                             "batch_mrays_per_s": rays_b / (ms_b / 1e3) / 1e6,
                             "single_mrays_per_s": rays_s / (ms_s / 1e3) / 1e6},
-        "gpu_launches": launches, "clocks": clk,
+        "frame": {"rays": rays_of(st), "primary": st["primary_rays"], "samples": st["samples"],
+                  "photons_stored": st["photons_stored"], "device_mb": device_mb, "load_s": load_s, "scene_gen_s": gen_s},
+        "gpu_launches": st["kernel_launches"], "clocks": clk,
         "e2e": None, "roofline": None, "cpu_baseline": None,
-        "note": "a step renders every job once; e2e, roofline and the CPU baseline are reported for the "
-                "production configuration",
+        "note": "a step renders every job once; e2e, roofline and the CPU baseline are reported for the production "
+                "configuration; per-job parity of scene-set batches against the FP32 oracle is "
+                "tests/test_gpu_parity.py::test_scene_set_batch_matches_oracle",
     }
     print(json.dumps(line))
     return 0

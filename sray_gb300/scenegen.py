@@ -17,6 +17,7 @@ Numbers always start with a digit or a sign, as the attribute typing of
 src/xmltree.c:75-93 requires.
 """
 import hashlib
+import math
 import os
 
 import numpy as np
@@ -234,7 +235,79 @@ def production_scene(seed=0x5EED0002, grid=(1000, 500), extent=(100.0, 50.0), n_
             _material(out, "m%d" % i, kd, ks=1.0, shin=60.0, refl=0.8)
         else:
             _material(out, "m%d" % i, kd, ks=0.4, shin=30.0)
-    # terrain
+    hseed = _terrain(out, rng, nx, nz, ex, ez)
+    # instances
+    iv, ifc = icosphere(3)
+    px = rng.uniform(-0.4 * ex, 0.4 * ex, n_inst)
+    pz = rng.uniform(-0.4 * ez, 0.4 * ez, n_inst)
+    sc = rng.uniform(0.4, 1.5, n_inst)
+    lift = rng.uniform(0.0, 2.0, n_inst)
+    hy = value_noise_height(px, pz, hseed)
+    axes = rng.normal(size=(n_inst, 3))
+    axes /= np.linalg.norm(axes, axis=1, keepdims=True)
+    angles = rng.uniform(0, 360, n_inst)
+    for i in range(n_inst):
+        xf = _xform(pos=(px[i], hy[i] + sc[i] + lift[i], pz[i]), scale=(sc[i],) * 3,
+                    axisrot=(angles[i], axes[i][0], axes[i][1], axes[i][2]))
+        _mesh_xml(out, "inst%d" % i, "m%d" % i, iv, ifc, normals=iv, xform=xf)
+    for i, (lx, lz) in enumerate([(-20.0, 5.0), (15.0, -8.0), (5.0, 15.0)]):
+        out.append('<light type="sphere" color="0.7">\n%s<sphere rad="0.8"/>\n</light>\n'
+                   % _xform(pos=(lx, 18.0 + 2.0 * i, lz)))
+    out.append('<camera type="target" fov="50.0">\n%s<target>\n%s</target>\n</camera>\n'
+               % (_xform(pos=(0.7, 14.0, 42.0)), _xform(pos=(0.0, 0.0, -4.0))))
+    out.append("</scene>\n")
+    return "".join(out)
+
+
+def batch_scene(seed=0x5EED0007, tris=100000, n_movers=24):
+    """A job of the batched configuration: a displaced-grid terrain of about
+    `tris` triangles (2:1 grid, 6-octave value noise) and `n_movers` spheres
+    moving on linear keyframes (two keys 1 s apart: under an 8 ms shutter
+    each sample of a pixel sees one of 8 integer times), 2 sphere lights; a
+    quarter of the spheres are mirrors and two are glass."""
+    rng = np.random.default_rng(seed)
+    nz = max(2, int(round(math.sqrt(tris / 4.0))))
+    nx = 2 * nz
+    ex, ez = 80.0, 40.0
+    out = ["<?xml version=\"1.0\"?>\n<scene>\n"]
+    out.append('<env ambient="0.04 0.04 0.05" bgcolor="0.35 0.45 0.6"/>\n')
+    _material(out, "terrain", (0.45, 0.5, 0.32), ks=0.05, shin=8.0)
+    kinds = np.array(["phong"] * n_movers, dtype=object)
+    order = rng.permutation(n_movers)
+    kinds[order[:2]] = "glass"
+    kinds[order[2:2 + n_movers // 4]] = "mirror"
+    for i in range(n_movers):
+        kd = rng.uniform(0.1, 0.9, 3)
+        if kinds[i] == "glass":
+            _material(out, "m%d" % i, kd * 0.1, ks=1.0, shin=80.0, refr=1.0, ior=1.5)
+        elif kinds[i] == "mirror":
+            _material(out, "m%d" % i, kd, ks=1.0, shin=60.0, refl=0.8)
+        else:
+            _material(out, "m%d" % i, kd, ks=0.4, shin=30.0)
+    hseed = _terrain(out, rng, nx, nz, ex, ez)
+    px = rng.uniform(-0.35 * ex, 0.35 * ex, n_movers)
+    pz = rng.uniform(-0.35 * ez, 0.35 * ez, n_movers)
+    rad = rng.uniform(0.5, 1.8, n_movers)
+    hy = value_noise_height(px, pz, hseed)
+    vel = rng.uniform(-4.0, 4.0, (n_movers, 2))      # scene units per second
+    for i in range(n_movers):
+        y = hy[i] + rad[i] + 0.3
+        out.append('<object type="sphere" name="s%d">\n<matref name="m%d"/>\n' % (i, i))
+        out.append(_xform(pos=(px[i], y, pz[i]), time=0).replace("<xform", '<xform interpolate="linear"'))
+        out.append(_xform(pos=(px[i] + vel[i][0], y, pz[i] + vel[i][1]), time=1000))
+        out.append('<sphere rad="%.4f"/>\n</object>\n' % rad[i])
+    for i, (lx, lz) in enumerate([(-18.0, 4.0), (14.0, -6.0)]):
+        out.append('<light type="sphere" color="0.8">\n%s<sphere rad="0.8"/>\n</light>\n'
+                   % _xform(pos=(lx, 18.0 + 2.0 * i, lz)))
+    out.append('<camera type="target" fov="50.0">\n%s<target>\n%s</target>\n</camera>\n'
+               % (_xform(pos=(0.7, 14.0, 38.0)), _xform(pos=(0.0, 0.0, -4.0))))
+    out.append("</scene>\n")
+    return "".join(out)
+
+
+def _terrain(out, rng, nx, nz, ex, ez):
+    """A displaced-grid terrain mesh of 2 nx nz triangles over ex x ez;
+    returns the height seed."""
     xs = np.linspace(-ex / 2, ex / 2, nx + 1)
     zs = np.linspace(-ez / 2, ez / 2, nz + 1)
     X, Z = np.meshgrid(xs, zs, indexing="ij")
@@ -258,27 +331,7 @@ def production_scene(seed=0x5EED0002, grid=(1000, 500), extent=(100.0, 50.0), n_
     faces[0::2] = np.stack([a, d, c], axis=1)
     faces[1::2] = np.stack([a, c, b], axis=1)
     _mesh_xml(out, "terrain", "terrain", verts, faces, normals=nrm)
-    # instances
-    iv, ifc = icosphere(3)
-    px = rng.uniform(-0.4 * ex, 0.4 * ex, n_inst)
-    pz = rng.uniform(-0.4 * ez, 0.4 * ez, n_inst)
-    sc = rng.uniform(0.4, 1.5, n_inst)
-    lift = rng.uniform(0.0, 2.0, n_inst)
-    hy = value_noise_height(px, pz, hseed)
-    axes = rng.normal(size=(n_inst, 3))
-    axes /= np.linalg.norm(axes, axis=1, keepdims=True)
-    angles = rng.uniform(0, 360, n_inst)
-    for i in range(n_inst):
-        xf = _xform(pos=(px[i], hy[i] + sc[i] + lift[i], pz[i]), scale=(sc[i],) * 3,
-                    axisrot=(angles[i], axes[i][0], axes[i][1], axes[i][2]))
-        _mesh_xml(out, "inst%d" % i, "m%d" % i, iv, ifc, normals=iv, xform=xf)
-    for i, (lx, lz) in enumerate([(-20.0, 5.0), (15.0, -8.0), (5.0, 15.0)]):
-        out.append('<light type="sphere" color="0.7">\n%s<sphere rad="0.8"/>\n</light>\n'
-                   % _xform(pos=(lx, 18.0 + 2.0 * i, lz)))
-    out.append('<camera type="target" fov="50.0">\n%s<target>\n%s</target>\n</camera>\n'
-               % (_xform(pos=(0.7, 14.0, 42.0)), _xform(pos=(0.0, 0.0, -4.0))))
-    out.append("</scene>\n")
-    return "".join(out)
+    return hseed
 
 
 def stress_scene(seed=0x5EED0005, tiles=(4, 4), tile_grid=(625, 500), tile_extent=(100.0, 80.0), n_inst=2000,
@@ -611,7 +664,7 @@ def scene_opts(name, **over):
 def write_scene(name, cache_dir=None, **kw):
     """Generate (or reuse from cache_dir) the XML of scene `name`; returns the path."""
     gen = {"small": small_scene, "learned": small_scene, "production": production_scene, "feature": feature_scene,
-           "stress": stress_scene, "textured": textured_scene, "animated": animated_scene}[name]
+           "stress": stress_scene, "textured": textured_scene, "animated": animated_scene, "batch": batch_scene}[name]
     key = hashlib.sha1(repr((name, sorted(kw.items()), 3)).encode()).hexdigest()[:12]
     cache_dir = cache_dir or os.environ.get("SRAY_SCENE_CACHE", "/tmp/sray_scenes")
     os.makedirs(cache_dir, exist_ok=True)
