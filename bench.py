@@ -43,7 +43,9 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="production", choices=["production", "small", "learned", "stress", "batch"])
+    ap.add_argument("--config", default="production",
+                    choices=["production", "small", "learned", "stress", "batch", "stress-batch"])
+    ap.add_argument("--batch-frames", type=int, default=16, help="frames per batch of the stress-batch configuration")
     ap.add_argument("--batch-jobs", type=int, default=64, help="jobs of the batch configuration")
     ap.add_argument("--batch-scenes", type=int, default=16, help="scenes of the batch configuration's scene set")
     ap.add_argument("--no-nrc", action="store_true", help="skip the radiance-cache comparison")
@@ -376,11 +378,8 @@ def oracle_reference_rows(opts, path, ds=REF_DS, bands=None, threads=0):
     orc = Oracle(fp64=True, rng_mode=1, **o)
     orc.load(path)
     orc.prepare(0)
-    ref = np.zeros((h, w, 4), np.float64)
-    for b in bands:
-        img = np.asarray(orc.render(0, rows=b, nthreads=threads))
-        ref[b[0]:b[1]] = img[b[0]:b[1]]
     rows = np.concatenate([np.arange(a, b) for a, b in bands])
+    ref = np.asarray(orc.render_rows(rows, nthreads=threads), np.float64)
     return ref, rows, time.perf_counter() - t0
 
 
@@ -531,7 +530,8 @@ def run_batch(args):
     (sray_gpu_render_batch) after the batch autotuner has picked the queue
     depth (65,536 / 262,144 / 1,048,576 primary rays per wave) and the
     traversal mode (thread per ray / warp per ray in the tails / warp per ray
-    everywhere); against the same jobs rendered one at a time."""
+    everywhere); against the same jobs rendered one frame at a time with
+    sray_gpu_render, each scene loaded alone."""
     import torch
     from sray_gb300 import build as gbuild, gpu, scenegen
     torch.cuda.set_device(0)
@@ -567,12 +567,6 @@ def run_batch(args):
         g.render_batch(spec, stream=stream)
         return rays_of(g.stats())
 
-    def singles():
-        r = 0
-        for job in spec:
-            g.render_batch([job], stream=stream)
-            r += rays_of(g.stats())
-        return r
 
     g.set_tuning(queue_depth=1 << 20)      # bounded queues from the first batch on
     batch()
@@ -589,8 +583,36 @@ def run_batch(args):
     ms_b, rays_b = timed(batch, args.steps)
     clk = clocks.stop()
     st = g.stats()
-    ms_s, rays_s = timed(singles, 1)
+    # where a batch's time goes: kernel event times of one more batch
+    g.set_profiling(time_kernels=True)
+    g.kernel_times(reset=True)
+    batch()
+    kt = g.kernel_times(reset=True)
+    g.set_profiling(False)
     g.close()
+    # the same jobs one frame at a time, as the reference renders them: each
+    # scene loaded alone (untimed), its jobs rendered with sray_gpu_render
+    ms_s, rays_s = 0.0, 0
+    for k, p in enumerate(paths):
+        mine = [J for J in jobs if J["scene"] == k]
+        if not mine:
+            continue
+        g1 = gpu.GpuRenderer(**opts)
+        g1.load(p)
+        fb = torch.zeros((1080, 1920, 4), dtype=torch.float32, device="cuda")
+        for J in mine:
+            g1.set_opts(width=J["width"], height=J["height"], caust_photons=J["caust_photons"], gi_photons=J["gi_photons"])
+            view = fb.view(-1)[:J["width"] * J["height"] * 4].view(J["height"], J["width"], 4)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            g1.render(J["msec"], view, stream=stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms_s += e0.elapsed_time(e1)
+            rays_s += rays_of(g1.stats())
+        g1.close()
     line = {
         "metric": METRIC, "value": rays_b / (ms_b / 1e3) / 1e6, "unit": "Mrays/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_b, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -603,16 +625,119 @@ def run_batch(args):
                    "method": "plain gather", "tuning": tuning,
                    "pixels": sum(J["width"] * J["height"] for J in jobs),
                    "photons": sum(J["caust_photons"] + J["gi_photons"] for J in jobs)},
+        "kernels_ms_per_batch": {k: round(v[0], 2) for k, v in kt.items()},
         "batch_vs_single": {"batch_ms": ms_b, "jobs_one_at_a_time_ms": ms_s, "speedup": ms_s / ms_b,
                             "batch_mrays_per_s": rays_b / (ms_b / 1e3) / 1e6,
                             "single_mrays_per_s": rays_s / (ms_s / 1e3) / 1e6},
         "frame": {"rays": rays_of(st), "primary": st["primary_rays"], "samples": st["samples"],
-                  "photons_stored": st["photons_stored"], "device_mb": device_mb, "load_s": load_s, "scene_gen_s": gen_s},
+                  "device_mb": device_mb, "load_s": load_s, "scene_gen_s": gen_s},
         "gpu_launches": st["kernel_launches"], "clocks": clk,
         "e2e": None, "roofline": None, "cpu_baseline": None,
         "note": "a step renders every job once; e2e, roofline and the CPU baseline are reported for the production "
                 "configuration; per-job parity of scene-set batches against the FP32 oracle is "
                 "tests/test_gpu_parity.py::test_scene_set_batch_matches_oracle",
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_stress_batch(args):
+    """The combined stress configuration: the stress scene (10M triangles,
+    2,000 instances, 24M photons, 3840x2160, adaptive 1-16 spp, motion blur)
+    as batches of `--batch-frames` motion-blurred frames 2 ms apart, each
+    batch one wavefront (waves of 4M primary rays), first with the plain
+    gather, then with the radiance cache trained online across the batches:
+    ms/frame, Mrays/s and device memory of both, and both images' RMSE
+    against the FP64 oracle's converged final gather (64 rays per vertex) on
+    row bands of frame 0, all at the full photon counts."""
+    import numpy as np
+    import torch
+    from sray_gb300 import build as gbuild, gpu, scenegen
+    torch.cuda.set_device(0)
+    gbuild.build()
+    opts = scenegen.scene_opts("stress")
+    t0 = time.perf_counter()
+    path = scenegen.write_scene("stress")
+    gen_s = time.perf_counter() - t0
+    H, W = opts["height"], opts["width"]
+    free_start = torch.cuda.mem_get_info()[0]
+    g = gpu.GpuRenderer(**opts)
+    t0 = time.perf_counter()
+    g.load(path)
+    load_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream()
+    nf = args.batch_frames
+    fbs = [torch.zeros((H, W, 4), dtype=torch.float32, device="cuda") for _ in range(nf)]
+    jobs = [(2 * j, fb) for j, fb in enumerate(fbs)]
+    g.set_tuning(queue_depth=1 << 22)
+
+    def timed(n):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        rays = 0
+        for _ in range(n):
+            g.render_batch(jobs, stream=stream)
+            rays += rays_of(g.stats())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / n
+        return ms, rays / n
+
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(args.warmup):
+        g.render_batch(jobs, stream=stream)
+    torch.cuda.synchronize()
+    mem_plain = (free_start - torch.cuda.mem_get_info()[0]) / 1e6
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    ms_plain, rays_plain = timed(args.steps)
+    clk = clocks.stop()
+    launches = g.stats()["kernel_launches"]
+    img_plain = fbs[0].cpu().numpy().copy()
+    g.set_opts(nrc=1)
+    g.nrc_reset()
+    t0 = time.perf_counter()
+    for _ in range(args.nrc_burn_in):
+        g.render_batch(jobs, stream=stream)
+    torch.cuda.synchronize()
+    burn_s = time.perf_counter() - t0
+    mem_cache = (free_start - torch.cuda.mem_get_info()[0]) / 1e6
+    ms_cache, rays_cache = timed(args.steps)
+    st = g.nrc_stats()
+    img_cache = fbs[0].cpu().numpy().copy()
+    g.close()
+    del fbs
+    ref_info = None
+    if not args.no_cpu_baseline:
+        bands = band_rows(H, 8, 2)
+        ref, rows, ref_s = oracle_reference_rows(opts, path, ds=64, bands=bands)
+        ref_info = {"rmse_plain": image_rmse(img_plain, ref, rows), "rmse_cache": image_rmse(img_cache, ref, rows),
+                    "rows": int(len(rows)), "bands": [list(b) for b in bands], "s": ref_s,
+                    "reference": "FP64 CPU oracle of frame 0 (same seeds, full photon counts), 64 final-gather rays per "
+                                 "vertex (the converged plain estimator)"}
+    line = {
+        "metric": METRIC, "value": rays_cache / (ms_cache / 1e3) / 1e6, "unit": "Mrays/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_cache, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator, no dataset)",
+        "config": {"workload": workload_desc("stress") + "; %d frames 2 ms apart per batch, one wavefront per batch "
+                                                         "(waves of 4M primary rays)" % nf,
+                   "method": "radiance cache with per-region fallback, trained online across batches"},
+        "stress_batch": {"frames_per_batch": nf,
+                         "plain": {"ms_per_batch": ms_plain, "ms_per_frame": ms_plain / nf,
+                                   "mrays_per_s": rays_plain / (ms_plain / 1e3) / 1e6, "device_mb": mem_plain},
+                         "cache": {"ms_per_batch": ms_cache, "ms_per_frame": ms_cache / nf,
+                                   "mrays_per_s": rays_cache / (ms_cache / 1e3) / 1e6, "device_mb": mem_cache,
+                                   "burn_in_batches": args.nrc_burn_in, "burn_in_s": burn_s, "frames_trained": st["frames"],
+                                   "cached_vertex_frac": st["cached"] / max(st["vertices"], 1),
+                                   "regions_cached": st["regions_cached"], "val_rel_err": st["val_rel_err"]},
+                         "cache_over_plain_time": ms_cache / ms_plain,
+                         "image_vs_fp64_oracle": ref_info,
+                         "scene_gen_s": gen_s, "load_s": load_s},
+        "gpu_launches": launches, "clocks": clk, "e2e": None, "roofline": None, "cpu_baseline": None,
+        "note": "a step is one batch of frames; e2e, roofline and the CPU baseline are reported for the production "
+                "configuration",
     }
     print(json.dumps(line))
     return 0
@@ -984,6 +1109,8 @@ def main():
         return run_reference(args)
     if args.config == "batch":
         return run_batch(args)
+    if args.config == "stress-batch":
+        return run_stress_batch(args)
     return run_ours(args)
 
 

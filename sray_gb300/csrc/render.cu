@@ -2350,7 +2350,7 @@ static uint32_t nrc_mix(uint64_t v)
  * query and record buffers, the record slots past the batch's accumulator
  * slots, and (first batch only) the selection of training and validation
  * vertices, sized from the last frame's vertex count */
-int Renderer::nrc_setup(int batch, int n_prim, cudaStream_t s)
+int Renderer::nrc_setup(int batch, int n_prim, int wave_rays, cudaStream_t s)
 {
 	DNrc &N = S.nrc;
 	N.mode = S.gi_on ? opt.nrc : 0;
@@ -2364,7 +2364,8 @@ int Renderer::nrc_setup(int batch, int n_prim, cudaStream_t s)
 	CK(nrc_rx.ensure((size_t)nrc_rcap * 9 * sizeof(float)), "radiance cache records");
 	CK(nrc_rt.ensure((size_t)nrc_rcap * 3 * sizeof(float)), "radiance cache targets");
 	CK(nrc_ry.ensure((size_t)vcap * 3 * sizeof(float)), "radiance cache predictions");
-	int64_t qc = (int64_t)n_prim * 2 + 65536;
+	/* queries are answered after each wave (nrc_wave_done) */
+	int64_t qc = (int64_t)wave_rays * 2 + 65536;
 	if(qc > INT_MAX / 2) qc = INT_MAX / 2;
 	nrc_qcap = (int)qc;
 	CK(nrc_qx.ensure((size_t)nrc_qcap * 9 * sizeof(float)), "radiance cache queries");
@@ -2418,18 +2419,27 @@ int Renderer::nrc_setup(int batch, int n_prim, cudaStream_t s)
 	return 0;
 }
 
-/* after the batch's shading tree: the queries' network outputs into the
- * accumulators; after the first batch also the records' targets, the
- * validation of the network on the validation records (before it trains
- * on this frame), the regions' fallback flags for the next frame, and the
- * training steps */
-int Renderer::nrc_batch_done(int batch, cudaStream_t s)
+/* the wave's queries: the network's outputs into their accumulators, the
+ * query queue emptied for the next wave */
+int Renderer::nrc_wave_done(cudaStream_t s)
 {
 	if(!S.nrc.mode) return 0;
 	int *cnt = counts.as<int>();
 	int r = 0;
 	LAUNCH(*this, "nrc_query", s, r = nrc_query(cnt + 16, nrc_qcap, nrc_qx.as<float>(), nrc_qw.as<float4>(), acc.as<float4>(), s));
 	if(r) return fail(r, std::string("radiance cache: ") + nrc_error());
+	CK(cudaMemsetAsync(cnt + 16, 0, sizeof(int), s), "reset radiance cache queries");
+	return 0;
+}
+
+/* after the first sample batch: the records' targets, the validation of
+ * the network on the validation records (before it trains on this frame),
+ * the regions' fallback flags for the next frame, and the training steps */
+int Renderer::nrc_batch_done(int batch, cudaStream_t s)
+{
+	if(!S.nrc.mode) return 0;
+	int *cnt = counts.as<int>();
+	int r = 0;
 	if(batch != 0) return 0;
 	int h[2] = {0, 0};
 	CK(cudaMemcpyAsync(h, cnt + 17, sizeof h, cudaMemcpyDeviceToHost, s), "read record counts");
@@ -2606,7 +2616,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 		int wave_rays = wave_pix * width;
 		if(ensure_queue(0, wave_rays)) return SRAY_ECUDA;
 		CK(acc.ensure((size_t)n_prim * 16), "accumulator");
-		if(int r = nrc_setup(b, n_prim, s)) return r;
+		if(int r = nrc_setup(b, n_prim, wave_rays, s)) return r;
 		if(photons_pending) {
 			photons_pending = false;
 			int64_t cap = (int64_t)wave_rays * 3 + 65536;
@@ -2729,9 +2739,11 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			n_rays = h_cnt;
 			cur ^= 1;
 		}
-		/* the wave's gathers (the first wave's wait for the photon maps) */
+		/* the wave's gathers (the first wave's wait for the photon maps) and
+		 * radiance-cache queries */
 		if(int r = flush_gathers()) return r;
 		if(int r = join_side()) return r;
+		if(int r = nrc_wave_done(s)) return r;
 		}
 		if(int r = nrc_batch_done(b, s)) return r;
 		CK(cudaMemsetAsync(next_count, 0, sizeof(int), s), "reset next active");

@@ -206,7 +206,8 @@ struct Renderer {
 	DevBuf djobs, dmaps;
 	std::vector<JobMaps> job_maps;
 	int render_batch(const sray_job *jobs, int n, cudaStream_t s);
-	int nrc_setup(int batch, int n_prim, cudaStream_t s);
+	int nrc_setup(int batch, int n_prim, int wave_rays, cudaStream_t s);
+	int nrc_wave_done(cudaStream_t s);
 	int nrc_batch_done(int batch, cudaStream_t s);
 	int nrc_reset_regions(cudaStream_t s);
 

@@ -133,3 +133,35 @@ def test_cache_with_adaptive_sampling_and_two_batches(gpu_lib):
     d = img[..., :3] - plain[..., :3]
     print("production 160x90, cache after 30 frames: rmse against the plain gather %.4f" % np.sqrt(np.mean(d * d)))
     g.close()
+
+
+def test_cache_in_a_batch(gpu_lib):
+    # the cache inside a batch of frames (one wavefront over the jobs): the
+    # first batch, nothing validated, is the plain gather's batch; trained
+    # online across batches, every job is served by the network and stays
+    # close to its plain-gather frame
+    opts = scenegen.scene_opts("production", width=160, height=90, caust_photons=20000, gi_photons=80000, max_samples=4)
+    g = gpu_lib.GpuRenderer(**opts)
+    g.load(scenegen.write_scene("production"))
+    sizes = [(160, 90), (96, 54), (128, 72)]
+    fbs = [torch.zeros((h, w, 4), dtype=torch.float32, device="cuda") for w, h in sizes]
+    jobs = [(40 * i, fb) for i, fb in enumerate(fbs)]
+    g.render_batch(jobs)
+    plain = [fb.cpu().numpy().copy() for fb in fbs]
+    g.set_opts(nrc=1)
+    g.nrc_reset(5)
+    g.render_batch(jobs)
+    for fb, p in zip(fbs, plain):
+        assert (np.abs(fb.cpu().numpy() - p).max(-1) > 1e-5).mean() <= 1e-3
+    g.set_opts(nrc=2)
+    for _ in range(30):
+        g.render_batch(jobs)
+    st = g.nrc_stats()
+    assert st["frames"] == 31 and st["cached"] == st["vertices"] > 0
+    for (w, h), fb, p in zip(sizes, fbs, plain):
+        img = fb.cpu().numpy()
+        d = img[..., :3] - p[..., :3]
+        e = float(np.sqrt(np.mean(d * d)))
+        print("batch job %dx%d, cache after 30 batches: rmse against the plain gather %.4f" % (w, h, e))
+        assert np.isfinite(img).all() and e < 0.1
+    g.close()
