@@ -587,7 +587,8 @@ def run_batch(args):
     g.set_profiling(time_kernels=True)
     g.kernel_times(reset=True)
     batch()
-    kt = g.kernel_times(reset=True)
+    kt_all = g.kernel_times(reset=True, host=True)
+    kt = {k: v for k, v in kt_all.items() if not k.startswith("host.")}
     g.set_profiling(False)
     g.close()
     # the same jobs one frame at a time, as the reference renders them: each
@@ -626,6 +627,7 @@ def run_batch(args):
                    "pixels": sum(J["width"] * J["height"] for J in jobs),
                    "photons": sum(J["caust_photons"] + J["gi_photons"] for J in jobs)},
         "kernels_ms_per_batch": {k: round(v[0], 2) for k, v in kt.items()},
+        "host_ms_per_batch": {k[5:]: [round(v[0], 2), v[1]] for k, v in kt_all.items() if k.startswith("host.")},
         "batch_vs_single": {"batch_ms": ms_b, "jobs_one_at_a_time_ms": ms_s, "speedup": ms_s / ms_b,
                             "batch_mrays_per_s": rays_b / (ms_b / 1e3) / 1e6,
                             "single_mrays_per_s": rays_s / (ms_s / 1e3) / 1e6},

@@ -383,7 +383,10 @@ int sray_gpu_set_profiling(int flags);
 
 /* Accumulated kernel times since the last call with reset = 1: for up to
  * `max` kernel kinds, the name (NUL-separated in `names`), total ms and
- * launch count.  Returns the number of kinds through `n_out`. */
+ * launch count.  Returns the number of kinds through `n_out`.  Kinds named
+ * "host.<phase>" are host wall-clock phases timed beside the kernels (a
+ * batch's frame build, the photon thread, waits for the photon maps and for
+ * each bounce's queue count); their count is the times the phase ran. */
 int sray_gpu_kernel_times(char *names, size_t names_cap, double *ms, int64_t *launches, int max,
 		int *n_out, int reset);
 

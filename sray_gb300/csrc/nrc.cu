@@ -12,11 +12,14 @@
  * all five layers with the activations in registers, the accumulator tile of
  * one layer becoming the operand tile of the next.
  *
- *   k_nrc_forward<FWD_INFER>  inference: encode + 5 layers, fused
- *   k_nrc_forward<FWD_QUERY>  the renderer's queries: the same, the output
+ *   k_nrc_forward_tc<FWD_INFER>  inference: encode + 5 layers on the
+ *                         5th-generation tensor cores (tcgen05.mma, TMEM
+ *                         accumulators), a 128-sample tile per MMA
+ *   k_nrc_forward_tc<FWD_QUERY>  the renderer's queries: the same, the output
  *                         weighted into the pixel's accumulator
- *   k_nrc_forward<FWD_TRAIN>  training forward: also stores the layer inputs
- *                         (BF16) and the loss gradient of the outputs
+ *   k_nrc_forward<FWD_TRAIN>  training forward (warp-level MMA): also stores
+ *                         the layer inputs (BF16) and the loss gradient of
+ *                         the outputs
  *   k_nrc_backward        dZ of layers 4..1 through the transposed weights,
  *                         bias gradients
  *   k_nrc_wgrad<L>        weight gradients dW = dZ^T H over the batch (MMA,
@@ -353,6 +356,273 @@ __global__ void __launch_bounds__(NRC_FWD_THREADS) k_nrc_forward(NrcDev net, int
 	}
 }
 
+/* ---- The inference and query forward on the 5th-generation tensor cores ----
+ * tcgen05.mma with the operands in shared memory and the accumulators in
+ * tensor memory (TMEM).  A CTA of 256 threads is two groups of four warps;
+ * each group carries a tile of 128 samples through the five layers: its
+ * threads write the tile's encoded inputs (one sample per thread) into
+ * shared memory, one elected thread issues the layer's MMAs (M = 128,
+ * N = 64, K = 16 each; 14 for the 224-wide first layer, 4 for the others,
+ * N = 16 for the output layer) and commits them to the group's mbarrier,
+ * and the threads read their rows of the accumulator back from TMEM
+ * (tcgen05.ld, 32x32b: a warp its 32 lanes) for the bias, ReLU and BF16
+ * rounding that make the next layer's operand.  The two groups of a CTA
+ * interleave, so one group's encoding and epilogues overlap the other's
+ * MMAs.  The weights (BF16, 54 KB) are copied once per CTA into the
+ * canonical K-major layout without swizzle: 8-row x 16-byte core matrices,
+ * the two of a K = 16 step 128 bytes apart (leading byte offset), 8-row
+ * groups K/8 x 128 bytes apart (stride byte offset).  Every wait on an
+ * mbarrier is bounded; one that runs out sets the error word and the group
+ * stops (TMEM is released as usual). */
+#define TC_THREADS 256
+#define TC_WAIT_LIMIT (1 << 20)
+
+enum {
+	TC_W1 = 0,                          /* 64 x 224: 8 row groups x 28 K-chunks x 128 B */
+	TC_W2 = TC_W1 + 64 * NRC_FP * 2,
+	TC_W3 = TC_W2 + 64 * 64 * 2,
+	TC_W4 = TC_W3 + 64 * 64 * 2,
+	TC_W5 = TC_W4 + 64 * 64 * 2,        /* 16 x 64 (rows 3..15 zero) */
+	TC_BIAS = TC_W5 + 16 * 64 * 2,      /* FP32: 4 x 64 + 8 */
+	TC_GROUP0 = (TC_BIAS + NRC_NBIAS * 4 + 127) & ~127,
+	TC_A1 = 0,                          /* per group: 128 x 224 encoded inputs */
+	TC_H = TC_A1 + 128 * NRC_FP * 2,    /* 128 x 64 hidden activations */
+	TC_MBAR = TC_H + 128 * 64 * 2,
+	TC_GROUP_BYTES = TC_MBAR + 128,
+	TC_TMEM_SLOT = TC_GROUP0 + 2 * TC_GROUP_BYTES,
+	TC_SMEM = TC_TMEM_SLOT + 16,
+	TC_TMEM_COLS = 256                  /* per group: 64 hidden + 16 output columns, at 128 g */
+};
+
+/* byte offset of element row r, 8-element K-chunk c in the canonical layout of a tile with kc chunks */
+__device__ __forceinline__ uint32_t tc_canon(int r, int c, int kc) { return (uint32_t)(((r >> 3) * kc + c) * 128 + (r & 7) * 16); }
+
+/* shared-memory matrix descriptor: start, leading and stride byte offsets, the
+ * descriptor version of sm_100, no swizzle */
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+	uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+	d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+	d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+	d |= (uint64_t)1 << 46;
+	return d;
+}
+
+/* instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, M x N */
+__device__ __forceinline__ uint32_t tc_idesc(int m, int n)
+{
+	return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, int accumulate)
+{
+	asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+			"tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+			:: "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate) : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar)
+{
+	asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(mbar) : "memory");
+}
+
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity)
+{
+	for(int i = 0; i < TC_WAIT_LIMIT; i++) {
+		uint32_t done;
+		asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.b32 %0, 1, 0, p;\n\t}\n"
+				: "=r"(done) : "r"(mbar), "r"(parity) : "memory");
+		if(done) return true;
+	}
+	return false;
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void group_sync(int g) { asm volatile("bar.sync %0, 128;" :: "r"(1 + g) : "memory"); }
+
+/* true when v holds in every thread of group g (its named barrier): a wait
+ * that ran out in one thread stops the whole group together */
+__device__ __forceinline__ bool group_all(int g, bool v)
+{
+	uint32_t r;
+	asm volatile("{\n\t.reg .pred q, p;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.and.pred p, %2, 128, q;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+			: "=r"(r) : "r"((uint32_t)v), "r"(1 + g) : "memory");
+	return r != 0;
+}
+
+/* 64 columns of the calling thread's accumulator row (its warp's 32 lanes) */
+__device__ __forceinline__ void tc_ld64(uint32_t taddr, float (&v)[64])
+{
+	uint32_t r[64];
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x64.b32 "
+			"{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,"
+			"%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];"
+			: "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+			  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+			  "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+			  "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
+			  "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
+			  "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
+			  "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]),
+			  "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+			: "r"(taddr) : "memory");
+	asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+	#pragma unroll
+	for(int i = 0; i < 64; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16])
+{
+	uint32_t r[16];
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+			: "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+			  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+			: "r"(taddr) : "memory");
+	asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+	#pragma unroll
+	for(int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+/* a weight image [rows][ld] (BF16) into the canonical layout of kc K-chunks,
+ * rows beyond `rows` up to `rows_pad` zero */
+__device__ __forceinline__ void tc_weights(unsigned char *dst, const __nv_bfloat16 *src, int rows, int rows_pad, int ld, int kc)
+{
+	for(int i = threadIdx.x; i < rows_pad * kc; i += blockDim.x) {
+		int r = i / kc, c = i - r * kc;
+		uint4 v = make_uint4(0u, 0u, 0u, 0u);
+		if(r < rows) v = *reinterpret_cast<const uint4 *>(src + (size_t)r * ld + c * 8);
+		*reinterpret_cast<uint4 *>(dst + tc_canon(r, c, kc)) = v;
+	}
+}
+
+/* the hidden activations of the calling thread's row: bias, ReLU, BF16, canonical layout (8 K-chunks) */
+__device__ __forceinline__ void tc_hidden(unsigned char *H, int row, const float (&v)[64], const float *b)
+{
+	#pragma unroll
+	for(int c = 0; c < 8; c++) {
+		uint4 q;
+		q.x = pack_bf16(fmaxf(v[8 * c + 0] + b[8 * c + 0], 0.0f), fmaxf(v[8 * c + 1] + b[8 * c + 1], 0.0f));
+		q.y = pack_bf16(fmaxf(v[8 * c + 2] + b[8 * c + 2], 0.0f), fmaxf(v[8 * c + 3] + b[8 * c + 3], 0.0f));
+		q.z = pack_bf16(fmaxf(v[8 * c + 4] + b[8 * c + 4], 0.0f), fmaxf(v[8 * c + 5] + b[8 * c + 5], 0.0f));
+		q.w = pack_bf16(fmaxf(v[8 * c + 6] + b[8 * c + 6], 0.0f), fmaxf(v[8 * c + 7] + b[8 * c + 7], 0.0f));
+		*reinterpret_cast<uint4 *>(H + tc_canon(row, c, 8)) = q;
+	}
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(TC_THREADS, 1) k_nrc_forward_tc(NrcDev net, int n, const float *x, float *y, QueryOut qo,
+		unsigned *err)
+{
+	if(MODE == FWD_QUERY) {
+		int c = *qo.count;
+		n = c < n ? c : n;
+	}
+	extern __shared__ __align__(1024) unsigned char tsm[];
+	const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(tsm);
+	tc_weights(tsm + TC_W1, net.w1, 64, 64, LD1, NRC_FP / 8);
+	tc_weights(tsm + TC_W2, net.w2, 64, 64, LDH, 8);
+	tc_weights(tsm + TC_W3, net.w3, 64, 64, LDH, 8);
+	tc_weights(tsm + TC_W4, net.w4, 64, 64, LDH, 8);
+	tc_weights(tsm + TC_W5, net.w5, NRC_O, 16, LDH, 8);
+	float *sb = reinterpret_cast<float *>(tsm + TC_BIAS);
+	for(int i = threadIdx.x; i < NRC_NBIAS; i += blockDim.x) sb[i] = net.bias[i];
+	const int warp = threadIdx.x >> 5, g = warp >> 2, tid = threadIdx.x & 127;
+	unsigned char *gbase = tsm + TC_GROUP0 + g * TC_GROUP_BYTES;
+	const uint32_t mbar = sbase + TC_GROUP0 + g * TC_GROUP_BYTES + TC_MBAR;
+	uint32_t *tslot = reinterpret_cast<uint32_t *>(tsm + TC_TMEM_SLOT);
+	if(tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(mbar) : "memory");
+	if(warp == 0) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+				:: "r"(sbase + TC_TMEM_SLOT), "r"((uint32_t)TC_TMEM_COLS) : "memory");
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+	}
+	/* the weights are read by the tensor cores (async proxy) */
+	proxy_fence();
+	tc_fence_before();
+	__syncthreads();
+	tc_fence_after();
+	const uint32_t tmem = *tslot;
+	const uint32_t tD = tmem + (uint32_t)(g * 128), tO = tD + 64;
+	const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
+	const uint32_t sA1 = sbase + TC_GROUP0 + g * TC_GROUP_BYTES + TC_A1, sH = sA1 + (TC_H - TC_A1);
+	const uint32_t sW1 = sbase + TC_W1, sWh[3] = {sbase + TC_W2, sbase + TC_W3, sbase + TC_W4}, sW5 = sbase + TC_W5;
+	unsigned char *A1 = gbase + TC_A1, *H = gbase + TC_H;
+	const uint32_t id64 = tc_idesc(128, 64), id16 = tc_idesc(128, 16);
+	uint32_t phase = 0;
+	bool ok = true;
+	int ntiles = (n + 127) >> 7;
+	for(int tile = blockIdx.x * 2 + g; tile < ntiles && ok; tile += gridDim.x * 2) {
+		int row = tile * 128 + tid;
+		/* encoded inputs of this thread's sample: 28 chunks of 4 (sin, cos) pairs */
+		float xv[9];
+		#pragma unroll
+		for(int k = 0; k < 9; k++) xv[k] = row < n ? x[(size_t)row * 9 + k] : 0.0f;
+		for(int c = 0; c < NRC_FP / 8; c++) {
+			uint4 q;
+			q.x = feature_pair(xv, 4 * c);
+			q.y = feature_pair(xv, 4 * c + 1);
+			q.z = feature_pair(xv, 4 * c + 2);
+			q.w = feature_pair(xv, 4 * c + 3);
+			*reinterpret_cast<uint4 *>(A1 + tc_canon(tid, c, NRC_FP / 8)) = q;
+		}
+		/* five layers: MMAs by one thread, epilogues by all */
+		for(int l = 0; l < 5 && ok; l++) {
+			proxy_fence();
+			tc_fence_before();
+			group_sync(g);
+			if(tid == 0) {
+				tc_fence_after();
+				if(l == 0) {
+					for(int j = 0; j < NRC_FP / 16; j++)
+						tc_mma(tD, tc_desc(sA1 + j * 256, 128, (NRC_FP / 8) * 128), tc_desc(sW1 + j * 256, 128, (NRC_FP / 8) * 128), id64, j);
+				} else if(l < 4) {
+					for(int j = 0; j < 4; j++) tc_mma(tD, tc_desc(sH + j * 256, 128, 1024), tc_desc(sWh[l - 1] + j * 256, 128, 1024), id64, j);
+				} else {
+					for(int j = 0; j < 4; j++) tc_mma(tO, tc_desc(sH + j * 256, 128, 1024), tc_desc(sW5 + j * 256, 128, 1024), id16, j);
+				}
+				tc_commit(mbar);
+			}
+			ok = group_all(g, tc_wait(mbar, phase));
+			phase ^= 1u;
+			if(!ok) break;
+			tc_fence_after();
+			if(l < 4) {
+				float v[64];
+				tc_ld64(tD + lane_off, v);
+				tc_hidden(H, tid, v, sb + 64 * l);
+			} else {
+				float v[16];
+				tc_ld16(tO + lane_off, v);
+				if(row < n) {
+					float o[3] = {v[0] + sb[256], v[1] + sb[257], v[2] + sb[258]};
+					if(MODE == FWD_QUERY) {
+						float4 wv = qo.w[row];
+						float *a = reinterpret_cast<float *>(qo.acc + __float_as_int(wv.w));
+						atomicAdd(a, wv.x * fmaxf(o[0], 0.0f));
+						atomicAdd(a + 1, wv.y * fmaxf(o[1], 0.0f));
+						atomicAdd(a + 2, wv.z * fmaxf(o[2], 0.0f));
+					} else {
+						y[(size_t)row * 3] = o[0];
+						y[(size_t)row * 3 + 1] = o[1];
+						y[(size_t)row * 3 + 2] = o[2];
+					}
+				}
+			}
+		}
+	}
+	if(!ok) {
+		atomicOr(err, 1u);
+		/* what was committed may still be running: a last bounded wait */
+		tc_wait(mbar, phase);
+	}
+	tc_fence_before();
+	__syncthreads();
+	tc_fence_after();
+	if(warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" :: "r"(tmem), "r"((uint32_t)TC_TMEM_COLS) : "memory");
+}
+
 /* Backward pass, a warp per 16 samples: dH_{l-1} = dZ_l W_l, dZ_{l-1} =
  * dH_{l-1} where h_{l-1} > 0; stores dz[4..1] (BF16) and adds the bias
  * gradients (from the FP32 values) to the packed gradient. */
@@ -573,6 +843,8 @@ struct NrcState {
 	int device = -1;
 	float *p = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr, *loss = nullptr, *bias = nullptr;
 	int *step_dev = nullptr;         /* Adam steps taken (device copy of `step`) */
+	unsigned *tc_err = nullptr;      /* set when a tensor-core forward's bounded wait ran out */
+	int nsm = 0;
 	/* the per-frame training steps as a CUDA graph, replayed while the
 	 * batch shape and buffers stay the same */
 	cudaGraphExec_t graph = nullptr;
@@ -622,11 +894,12 @@ static int nrc_alloc()
 	NCK(cudaMalloc(&g_nrc.bias, NRC_NBIAS * sizeof(float)), "radiance cache biases");
 	NCK(cudaMalloc(&g_nrc.img, IMG_END * sizeof(__nv_bfloat16)), "radiance cache images");
 	NCK(cudaMalloc(&g_nrc.step_dev, sizeof(int)), "radiance cache step");
-	NCK(cudaFuncSetAttribute(k_nrc_forward<FWD_INFER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-			FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4), "smem");
+	NCK(cudaMalloc(&g_nrc.tc_err, sizeof(unsigned)), "radiance cache error word");
+	NCK(cudaMemset(g_nrc.tc_err, 0, sizeof(unsigned)), "radiance cache error word");
+	NCK(cudaDeviceGetAttribute(&g_nrc.nsm, cudaDevAttrMultiProcessorCount, dev), "multiprocessors");
+	NCK(cudaFuncSetAttribute(k_nrc_forward_tc<FWD_INFER>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM), "smem");
+	NCK(cudaFuncSetAttribute(k_nrc_forward_tc<FWD_QUERY>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM), "smem");
 	NCK(cudaFuncSetAttribute(k_nrc_forward<FWD_TRAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-			FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4), "smem");
-	NCK(cudaFuncSetAttribute(k_nrc_forward<FWD_QUERY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 			FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4), "smem");
 	NCK(cudaFuncSetAttribute(k_nrc_backward, cudaFuncAttributeMaxDynamicSharedMemorySize, BWD_SMEM_BF16 * 2 + 256 * 4), "smem");
 	g_nrc.device = dev;
@@ -735,13 +1008,36 @@ int nrc_ensure_ready(uint64_t seed, cudaStream_t s)
 	return 0;
 }
 
+/* CTAs of the tensor-core forward for up to n samples: one per SM at
+ * most, two 128-sample tiles in flight each */
+static int tc_grid(int n)
+{
+	int tiles = (n + 127) / 128;
+	int blocks = (tiles + 1) / 2;
+	int cap = g_nrc.nsm > 0 ? g_nrc.nsm : 152;
+	if(blocks > cap) blocks = cap;
+	return blocks < 1 ? 1 : blocks;
+}
+
 int nrc_infer(int n, const float *x, float *y, cudaStream_t s)
 {
 	if(n <= 0) return 0;
-	k_nrc_forward<FWD_INFER><<<nrc_grid(n, NRC_FWD_THREADS / 32), NRC_FWD_THREADS, FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4, s>>>(nrc_dev(), n,
-			x, y, nullptr, TrainBufs(),
-			QueryOut());
+	k_nrc_forward_tc<FWD_INFER><<<tc_grid(n), TC_THREADS, TC_SMEM, s>>>(nrc_dev(), n, x, y, QueryOut(), g_nrc.tc_err);
 	NCK(cudaGetLastError(), "radiance cache inference");
+	return 0;
+}
+
+int nrc_device_error(cudaStream_t s)
+{
+	if(!g_nrc.ready) return 0;
+	unsigned h = 0;
+	NCK(cudaMemcpyAsync(&h, g_nrc.tc_err, sizeof h, cudaMemcpyDeviceToHost, s), "radiance cache error word");
+	NCK(cudaStreamSynchronize(s), "radiance cache error word");
+	if(h) {
+		g_nrc.err = "radiance cache: a tensor-core wait ran out";
+		NCK(cudaMemsetAsync(g_nrc.tc_err, 0, sizeof(unsigned), s), "radiance cache error word");
+		return SRAY_EDEVICE;
+	}
 	return 0;
 }
 
@@ -752,9 +1048,7 @@ int nrc_query(const int *count, int cap, const float *x, const float4 *w, float4
 	qo.count = count;
 	qo.w = w;
 	qo.acc = acc;
-	k_nrc_forward<FWD_QUERY><<<nrc_grid(cap, NRC_FWD_THREADS / 32), NRC_FWD_THREADS, FWD_SMEM_BF16 * 2 + NRC_NBIAS * 4, s>>>(nrc_dev(), cap,
-			x, nullptr, nullptr,
-			TrainBufs(), qo);
+	k_nrc_forward_tc<FWD_QUERY><<<tc_grid(cap), TC_THREADS, TC_SMEM, s>>>(nrc_dev(), cap, x, nullptr, qo, g_nrc.tc_err);
 	NCK(cudaGetLastError(), "radiance cache queries");
 	return 0;
 }
@@ -873,6 +1167,7 @@ int sray_nrc_infer(int n, const float *x, float *y, void *stream)
 	cudaStream_t s = (cudaStream_t)stream;
 	int r = nrc_infer(n, x, y, s);
 	if(!r) { cudaError_t e = cudaStreamSynchronize(s); if(e != cudaSuccess) r = nrc_fail(e, "inference"); }
+	if(!r) r = nrc_device_error(s);
 	return nrc_err_ret(r);
 }
 

@@ -20,6 +20,9 @@ int nrc_train(int n, const float *x, const float *t, float lr, cudaStream_t s);
 /* `steps` Adam steps over consecutive batches of `per` samples of (x, t),
  * replayed from a CUDA graph while the arguments stay the same */
 int nrc_train_steps(int steps, int per, const float *x, const float *t, float lr, cudaStream_t s);
+/* SRAY_EDEVICE (and the error word cleared) when a tensor-core forward's
+ * bounded wait ran out since the last call; waits for stream s */
+int nrc_device_error(cudaStream_t s);
 /* device address of the last batch's loss */
 float *nrc_loss_ptr();
 const char *nrc_error();

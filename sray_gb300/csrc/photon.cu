@@ -717,8 +717,9 @@ int photon_map_build(Renderer &R, int global, int n, cudaStream_t s)
 	PhotonBufs &P = global ? R.gi : R.caust;
 	const sray_opts &opt = R.opt;
 	if(R.sc.oct.nodes.empty()) return R.fail(SRAY_ESTATE, "no scene bounds (build the frame first)");
-	/* grid over the scene bounds: cells of the gather radius */
-	const Box &rb = R.sc.oct.nodes[0].box;
+	/* grid over the scene bounds (a batch job's: its scene over its own
+	 * interval, the box its frame alone would have): cells of the gather radius */
+	const Box &rb = R.map_has_box ? R.map_box : R.sc.oct.nodes[0].box;
 	int k = global ? opt.gi_k : opt.caust_k;
 	/* a job of a batch gathers with the radius of its own interval */
 	double rad = k > 0 ? (double)opt.gather_rcap : (R.map_gather_dist >= 0.0 ? R.map_gather_dist : R.sc.gather_dist);

@@ -1455,6 +1455,9 @@ __global__ void k_primary_hits(DScene S, RayQueue q, const int4 *hits, int *obj,
 /* ================================================================ */
 /* host side                                                          */
 /* ================================================================ */
+/* at most this many gather requests wait for the photon maps across waves */
+#define DEFER_MAX_REQS ((int64_t)1 << 28)
+
 static int grid_for(int n, int block)
 {
 	int sms = 152;
@@ -1471,6 +1474,16 @@ int Renderer::kind_of(const char *name)
 	k.name = name;
 	ktimes.push_back(k);
 	return (int)ktimes.size() - 1;
+}
+
+void Renderer::host_time(const char *name, double t0)
+{
+	if(!(prof_flags & 1)) return;
+	double ms = host_now_ms() - t0;
+	std::lock_guard<std::mutex> lk(prof_mu);
+	KTime &k = ktimes[kind_of(name)];
+	k.ms += ms;
+	k.launches++;
 }
 
 void Renderer::prof_begin(const char *name, int *kind_cache, cudaStream_t s, Pending *p)
@@ -1871,7 +1884,7 @@ int Renderer::build_frame_set(long bt0, long bt1, cudaStream_t s)
 {
 	t0 = (int)bt0;
 	t1 = (int)bt1;
-	sc.build_tree(t0, t1, opt);   /* over every object: the union's box (photon grids, object bounds cache) */
+	sc.bound_objects(t0, t1, opt);   /* the object bounds cache and the union's box; the scenes' octrees follow */
 	int ns = (int)sc.ranges.size();
 	std::vector<DevNode> nodes;
 	std::vector<int> slots, ohome_h(sc.objs.size(), 0);
@@ -2041,6 +2054,60 @@ int Renderer::build_frame(long bt0, long bt1, cudaStream_t s)
 	return 0;
 }
 
+/* a light's projection maps as the photon kernels read them: 2048 cell bits
+ * of the map, then of the caustic map; their coverages */
+static void pack_projmaps(const ProjMap &pm, const ProjMap &spm, uint32_t *bits, float *cov)
+{
+	for(int k = 0; k < 128; k++) bits[k] = 0u;
+	for(int k = 0; k < 2048; k++) {
+		if(pm.cells[k]) bits[k >> 5] |= 1u << (k & 31);
+		if(spm.cells[k]) bits[64 + (k >> 5)] |= 1u << (k & 31);
+	}
+	cov[0] = (float)pm.get_coverage();
+	cov[1] = (float)spm.get_coverage();
+}
+
+/* every job's projection maps of a batch, on all host cores: each light of a
+ * job is one task (its own random stream, its own output) */
+void Renderer::batch_projmaps(std::vector<std::vector<uint32_t>> &bits, std::vector<std::vector<float>> &cov)
+{
+	size_t n = batch_t0.size();
+	bits.assign(n, std::vector<uint32_t>());
+	cov.assign(n, std::vector<float>());
+	struct Task { size_t job; int light; };
+	std::vector<Task> tasks;
+	std::vector<int> l0(n, 0), o0(n, 0), no(n, (int)sc.objs.size());
+	for(size_t j = 0; j < n; j++) {
+		int nl = (int)sc.lights.size();
+		if(!scene_refs.empty()) {
+			const SceneRange &rg = sc.ranges[batch_scene[j]];
+			l0[j] = rg.light0;
+			nl = rg.nlight;
+			o0[j] = rg.obj0;
+			no[j] = rg.nobj;
+		}
+		bits[j].assign((size_t)nl * 128, 0u);
+		cov[j].assign((size_t)nl * 2, 0.0f);
+		for(int k = 0; k < nl; k++) tasks.push_back(Task{j, k});
+	}
+	std::atomic<size_t> next{0};
+	auto work = [&]() {
+		for(size_t i; (i = next.fetch_add(1)) < tasks.size();) {
+			const Task &T = tasks[i];
+			ProjMap pm, spm;
+			sc.light_projmaps((size_t)(l0[T.job] + T.light), (int)batch_t0[T.job], (int)batch_t1[T.job], opt.seed, T.light, o0[T.job],
+					no[T.job], pm, spm);
+			pack_projmaps(pm, spm, &bits[T.job][(size_t)T.light * 128], &cov[T.job][(size_t)T.light * 2]);
+		}
+	};
+	unsigned hw = std::thread::hardware_concurrency();
+	size_t nth = std::min<size_t>(tasks.size(), hw ? hw : 4);
+	std::vector<std::thread> th;
+	for(size_t t = 1; t < nth; t++) th.push_back(std::thread(work));
+	work();
+	for(auto &t : th) t.join();
+}
+
 /* projection maps and both photon maps on stream s, with the scene view
  * `base` (the projection-map tables are set in a copy of it); the map
  * descriptors land in caust.map / gi.map, which fill_scene_desc() copies
@@ -2055,22 +2122,25 @@ int Renderer::shoot_maps(const DScene &base, cudaStream_t s, int *nc, int *ng)
 	int o0 = map_obj0, no = map_nobj >= 0 ? map_nobj : (int)sc.objs.size();
 	int cp = map_counts[0] >= 0 ? map_counts[0] : opt.caust_photons, gp = map_counts[1] >= 0 ? map_counts[1] : opt.gi_photons;
 	if(!(cp || gp) || nl == 0) return 0;
-	/* projection maps (src/render.cc:87-103) over the photons' interval */
-	sc.build_projmaps(base.t0, base.t1, opt.seed, l0, nl, o0, no);
-	std::vector<uint32_t> bits((size_t)nl * 128, 0u);
-	std::vector<float> cov((size_t)nl * 2);
-	for(size_t i = 0; i < (size_t)nl; i++) {
-		const Light &L = sc.lights[l0 + i];
-		for(int k = 0; k < 2048; k++) {
-			if(L.pm.cells[k]) bits[i * 128 + (k >> 5)] |= 1u << (k & 31);
-			if(L.spm.cells[k]) bits[i * 128 + 64 + (k >> 5)] |= 1u << (k & 31);
-		}
-		cov[i * 2] = (float)L.pm.get_coverage();
-		cov[i * 2 + 1] = (float)L.spm.get_coverage();
+	/* projection maps (src/render.cc:87-103) over the photons' interval:
+	 * a batch job's were built beforehand (map_bits / map_cov) */
+	std::vector<uint32_t> own_bits;
+	std::vector<float> own_cov;
+	const std::vector<uint32_t> *bits = map_bits;
+	const std::vector<float> *cov = map_cov;
+	if(!bits || !cov) {
+		double tp = host_now_ms();
+		sc.build_projmaps(base.t0, base.t1, opt.seed, l0, nl, o0, no);
+		own_bits.assign((size_t)nl * 128, 0u);
+		own_cov.assign((size_t)nl * 2, 0.0f);
+		for(size_t i = 0; i < (size_t)nl; i++) pack_projmaps(sc.lights[l0 + i].pm, sc.lights[l0 + i].spm, &own_bits[i * 128], &own_cov[i * 2]);
+		host_time("host.projmaps", tp);
+		bits = &own_bits;
+		cov = &own_cov;
 	}
-	CK(projbits.upload(bits, s), "upload projection maps");
-	CK(coverage.upload(cov, s), "upload coverage");
-	h2d += (int64_t)(bits.size() * 4 + cov.size() * 4);
+	CK(projbits.upload(*bits, s), "upload projection maps");
+	CK(coverage.upload(*cov, s), "upload coverage");
+	h2d += (int64_t)(bits->size() * 4 + cov->size() * 4);
 	DScene D = base;
 	D.projbits = projbits.as<uint32_t>();
 	D.coverage = coverage.as<float>();
@@ -2085,6 +2155,11 @@ int Renderer::photon_job(DScene base)
 	size_t n = batch_t0.size();
 	std::vector<DPhotonMap> hm(2 * n);
 	const DScene base0 = base;
+	std::vector<std::vector<uint32_t>> jbits;
+	std::vector<std::vector<float>> jcov;
+	double tp = host_now_ms();
+	batch_projmaps(jbits, jcov);
+	host_time("host.projmaps", tp);
 	for(size_t j = 0; j < n; j++) {
 		base = base0;
 		base.t0 = batch_t0[j];
@@ -2114,8 +2189,15 @@ int Renderer::photon_job(DScene base)
 		/* the radius Scene::build_tree gives the job's own frame: the batch's
 		 * tree spans every job's interval */
 		map_gather_dist = sc.gather_dist_at(batch_t0[j], batch_t1[j], opt, o0, no);
+		map_box = sc.box_at(batch_t0[j], batch_t1[j], o0, no);
+		map_has_box = true;
+		map_bits = &jbits[j];
+		map_cov = &jcov[j];
 		int r = shoot_maps(base, ps, &c, &g);
 		map_gather_dist = -1.0;
+		map_has_box = false;
+		map_bits = nullptr;
+		map_cov = nullptr;
 		map_light0 = map_obj0 = 0;
 		map_nlight = map_nobj = -1;
 		map_counts[0] = map_counts[1] = -1;
@@ -2146,7 +2228,9 @@ int Renderer::start_photon_job(cudaStream_t s)
 	DScene base = S;
 	photon_finished.store(false);
 	photon_thread = std::thread([this, base]() {
+		double t0 = host_now_ms();
 		photon_rc = photon_job(base);
+		host_time("host.photon_thread", t0);
 		photon_finished.store(true);
 	});
 	return 0;
@@ -2156,7 +2240,9 @@ int Renderer::start_photon_job(cudaStream_t s)
 int Renderer::finish_photon_job()
 {
 	if(!photon_thread.joinable()) return 0;
+	double t0 = host_now_ms();
 	photon_thread.join();
+	host_time("host.photon_wait", t0);
 	if(photon_rc) return photon_rc;
 	photons_ready = true;
 	fill_scene_desc();
@@ -2583,6 +2669,41 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 		CK(cudaMemsetAsync(cnt + 2, 0, sizeof(int), s), "reset gather queue");
 		return 0;
 	};
+	/* While the photon maps are still being traced the accumulated gathers
+	 * outlive a wave: their queue grows (its requests copied over) up to a
+	 * quarter of the free device memory and DEFER_MAX_REQS requests, rather
+	 * than the render stream waiting for the maps.  The queues it grew out of
+	 * are freed once the stream has passed them. */
+	struct Retired {
+		std::vector<DevBuf> bufs;
+		cudaStream_t s;
+		~Retired()
+		{
+			if(bufs.empty()) return;
+			cudaStreamSynchronize(s);
+			for(DevBuf &b : bufs) b.release();
+		}
+	} retired{{}, s};
+	auto grow_deferred = [&](int64_t need) -> bool {
+		int64_t cap = std::max<int64_t>(need, 2 * gq_defer_cap);
+		if(cap > DEFER_MAX_REQS) cap = DEFER_MAX_REQS;
+		if(cap < need) return false;
+		size_t fr = 0, tot = 0;
+		if(cudaMemGetInfo(&fr, &tot) != cudaSuccess || (size_t)cap * sizeof(GatherReq) > fr / 4) return false;
+		DevBuf nb;
+		if(nb.ensure((size_t)cap * sizeof(GatherReq)) != cudaSuccess) {
+			cudaGetLastError();
+			return false;
+		}
+		if(gq_upper > 0 && cudaMemcpyAsync(nb.p, gq.p, (size_t)gq_upper * sizeof(GatherReq), cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+			nb.release();
+			return false;
+		}
+		retired.bufs.push_back(gq);
+		gq = nb;
+		gq_defer_cap = cap;
+		return true;
+	};
 	auto join_side = [&]() -> int {
 		if(!side_pending) return 0;
 		side_pending = false;
@@ -2698,7 +2819,10 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			int r = ensure_queue(cur ^ 1, need);
 			if(r) return r;
 			CK(hits.ensure((size_t)n_rays * 16), "hits");
-			if(deferring && gq_upper + n_rays > gq_defer_cap && (r = flush_gathers())) return r;
+			if(deferring && gq_upper + n_rays > gq_defer_cap) {
+				bool grown = !photon_finished.load() && !S.nrc.mode && grow_deferred(gq_upper + n_rays);
+				if(!grown && (r = flush_gathers())) return r;
+			}
 			if(!deferring) {
 				CK(gq.ensure((size_t)n_rays * sizeof(GatherReq)), "gather queue");
 				CK(cudaMemsetAsync(cnt + 2, 0, sizeof(int), s), "reset gather queue");
@@ -2730,7 +2854,9 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			stats.secondary_rays += depth ? n_rays : 0;
 			int h_cnt = 0;
 			CK(cudaMemcpyAsync(&h_cnt, q[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "read queue count");
+			double tw = host_now_ms();
 			CK(cudaStreamSynchronize(s), "bounce");
+			host_time("host.bounce_wait", tw);
 			d2h += sizeof(int);
 			prof_collect();
 			/* children beyond the queue were dropped (the count kept going):
@@ -2739,12 +2865,18 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			n_rays = h_cnt;
 			cur ^= 1;
 		}
-		/* the wave's gathers (the first wave's wait for the photon maps) and
-		 * radiance-cache queries */
-		if(int r = flush_gathers()) return r;
+		/* the wave's gathers and radiance-cache queries; while the photon
+		 * maps are still being traced and more waves follow, the gathers stay
+		 * queued (the radiance cache, whose records are gather estimates,
+		 * takes them wave by wave) */
+		bool more_waves = a0 + wave_pix < n_active;
+		if(!(deferring && more_waves && !S.nrc.mode && !photon_finished.load()))
+			if(int r = flush_gathers()) return r;
 		if(int r = join_side()) return r;
 		if(int r = nrc_wave_done(s)) return r;
 		}
+		if(int r = flush_gathers()) return r;
+		if(int r = join_side()) return r;
 		if(int r = nrc_batch_done(b, s)) return r;
 		CK(cudaMemsetAsync(next_count, 0, sizeof(int), s), "reset next active");
 		LAUNCH(*this, "finish", s, k_finish<<<grid_for(n_active, 256), 256, 0, s>>>(act, act_count, s0, width, acc.as<float4>(),
@@ -2792,6 +2924,8 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 		nrc_last_cached = (int64_t)(hc.nrc[1] + hc.nrc[3]);
 	}
 	if(hc.overflow) return fail(SRAY_EDEVICE, "device queue or traversal stack overflow");
+	int r_nrc = 0;
+	if(S.nrc.mode && (r_nrc = nrc_device_error(s)) != 0) return fail(r_nrc, nrc_error());
 	return 0;
 }
 
@@ -2952,7 +3086,9 @@ int Renderer::render_batch(const sray_job *jobs, int n, cudaStream_t s)
 		if(total > (1 << 27)) return fail(SRAY_EINVAL, "a batch holds at most 2^27 pixels");
 	}
 	in_batch = true;
+	double tb = host_now_ms();
 	int r = build_frame(bt0, bt1, s);
+	host_time("host.build", tb);
 	in_batch = false;
 	if(r) return r;
 	for(int j = 0; j < n; j++) hj[j].cam_base = hj[j].scene * nt;   /* its scene's camera in the frame's table */
@@ -2970,7 +3106,9 @@ int Renderer::render_batch(const sray_job *jobs, int n, cudaStream_t s)
 	S.jobs = djobs.as<DevJob>();
 	S.maps = nullptr;
 	batch_npix = (int)total;
+	double tr = host_now_ms();
 	r = render_pixels(bt0, fbdev.as<float>(), 1, s, true);
+	host_time("host.render", tr);
 	S.njobs = 0;
 	S.jobs = nullptr;
 	S.maps = nullptr;

@@ -7,6 +7,7 @@
 #include <atomic>
 #include <mutex>
 #include <thread>
+#include <chrono>
 #include <cuda_runtime.h>
 #include "sray_gpu.h"
 #include "scene_host.h"
@@ -195,6 +196,11 @@ struct Renderer {
 	int batch_npix = 0;
 	std::vector<int> batch_t0, batch_t1;   /* jobs' shutter intervals: the photon job shoots one map pair each */
 	double map_gather_dist = -1.0;         /* >= 0: the range radius of the maps being built (a batch job's) */
+	bool map_has_box = false;              /* the grid box of the maps being built (a batch job's scene */
+	Box map_box;                           /* over its own interval), else the frame octree's root box */
+	const std::vector<uint32_t> *map_bits = nullptr;   /* a batch job's projection maps, built beforehand */
+	const std::vector<float> *map_cov = nullptr;
+	void batch_projmaps(std::vector<std::vector<uint32_t>> &bits, std::vector<std::vector<float>> &cov);
 	/* the photon job of a batch job: its scene's lights and its photon counts (-1: all lights, the options') */
 	int map_light0 = 0, map_nlight = -1, map_counts[2] = {-1, -1}, map_obj0 = 0, map_nobj = -1;
 	std::vector<int> batch_scene, batch_caust, batch_gi;   /* jobs' scenes and photon counts (0: the options') */
@@ -225,6 +231,13 @@ struct Renderer {
 	std::vector<cudaEvent_t> event_pool;
 	std::mutex prof_mu;
 	int kind_of(const char *name);
+	/* host time of a phase since t0 (host_now_ms), kept beside the kernels'
+	 * under its name ("host.<phase>") while kernel timing is on */
+	void host_time(const char *name, double t0);
+	static double host_now_ms()
+	{
+		return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+	}
 	void prof_begin(const char *name, int *kind_cache, cudaStream_t s, Pending *p);
 	void prof_end(Pending *p, cudaStream_t s);
 	void prof_collect();

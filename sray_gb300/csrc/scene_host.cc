@@ -793,10 +793,15 @@ void HostScene::build_projmaps(int t0, int t1, uint64_t seed, int light0, int nl
 
 void HostScene::build_light_projmaps(size_t li, int t0, int t1, uint64_t seed, int key, int obj0, int nobj)
 {
+	light_projmaps(li, t0, t1, seed, key, obj0, nobj, lights[li].pm, lights[li].spm);
+}
+
+void HostScene::light_projmaps(size_t li, int t0, int t1, uint64_t seed, int key, int obj0, int nobj, ProjMap &pm, ProjMap &spm) const
+{
 	{
-		Light &L = lights[li];
-		L.pm.clear();
-		L.spm.clear();
+		const Light &L = lights[li];
+		pm.clear();
+		spm.clear();
 		if(nobj <= 0) return;
 		int tm[3] = {t0, t1, -1};
 		if(t0 == t1) tm[1] = -1;
@@ -828,8 +833,8 @@ void HostScene::build_light_projmaps(size_t li, int t0, int t1, uint64_t seed, i
 					v.z = L.dim.z * sray_rng_uniform_d(&s) - 0.5 * L.dim.z;
 					lp = m_pt(m0, v);
 				}
-				project_boxes(&L.pm, lp, boxes);
-				project_boxes(&L.spm, lp, cboxes);
+				project_boxes(&pm, lp, boxes);
+				project_boxes(&spm, lp, cboxes);
 			}
 		}
 	}
@@ -868,22 +873,52 @@ void HostScene::build_tree(int t0, int t1, const sray_opts &opt)
 	gather_dist = sqrt(dx * dx + dy * dy + dz * dz) * opt.gather_dist;
 }
 
-/* gather_dist of Scene::build_tree(t0, t1) (src/scene.cc:384-387): the
- * diagonal of the union of every object's bounds at t0 and t1 (the scene
- * octree's root box) times the option */
-double HostScene::gather_dist_at(int t0, int t1, const sray_opts &opt, int obj0, int nobj) const
+void HostScene::bound_objects(int t0, int t1, const sray_opts &opt)
+{
+	bt0 = t0;
+	bt1 = t1;
+	box_t0.resize(objs.size());
+	box_t1.resize(objs.size());
+	oct_boxes.resize(objs.size());
+	for(size_t i = 0; i < objs.size(); i++) {
+		box_t0[i] = objs[i].bounds(meshes, t0);
+		box_t1[i] = t1 == t0 ? box_t0[i] : objs[i].bounds(meshes, t1);
+		for(int k = 0; k < 3; k++) {
+			oct_boxes[i].mn[k] = std::min(box_t0[i].mn[k], box_t1[i].mn[k]);
+			oct_boxes[i].mx[k] = std::max(box_t0[i].mx[k], box_t1[i].mx[k]);
+		}
+	}
+	oct.nodes.assign(1, BuildOctree::Node());
+	oct.nodes[0].box = box_at(t0, t1);
+	const Box &rb = oct.nodes[0].box;
+	double dx = rb.mx[0] - rb.mn[0], dy = rb.mx[1] - rb.mn[1], dz = rb.mx[2] - rb.mn[2];
+	gather_dist = sqrt(dx * dx + dy * dy + dz * dz) * opt.gather_dist;
+}
+
+/* the root box of Scene::build_tree(t0, t1) (src/scene.cc:353-390): the
+ * union of every object's bounds at t0 and t1 */
+Box HostScene::box_at(int t0, int t1, int obj0, int nobj) const
 {
 	if(nobj < 0) nobj = (int)objs.size() - obj0;
-	double mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+	Box u;
+	for(int k = 0; k < 3; k++) { u.mn[k] = FLT_MAX; u.mx[k] = -FLT_MAX; }
 	for(size_t i = (size_t)obj0; i < (size_t)(obj0 + nobj); i++) {
-		Box b[2] = {objs[i].bounds(meshes, t0), t1 == t0 ? objs[i].bounds(meshes, t0) : objs[i].bounds(meshes, t1)};
+		Box b[2] = {object_bounds(i, t0), t1 == t0 ? object_bounds(i, t0) : object_bounds(i, t1)};
 		for(int j = 0; j < 2; j++)
 			for(int k = 0; k < 3; k++) {
-				if(b[j].mn[k] < mn[k]) mn[k] = b[j].mn[k];
-				if(b[j].mx[k] > mx[k]) mx[k] = b[j].mx[k];
+				if(b[j].mn[k] < u.mn[k]) u.mn[k] = b[j].mn[k];
+				if(b[j].mx[k] > u.mx[k]) u.mx[k] = b[j].mx[k];
 			}
 	}
-	double dx = mx[0] - mn[0], dy = mx[1] - mn[1], dz = mx[2] - mn[2];
+	return u;
+}
+
+/* gather_dist of Scene::build_tree(t0, t1) (src/scene.cc:384-387): the
+ * diagonal of the root box times the option */
+double HostScene::gather_dist_at(int t0, int t1, const sray_opts &opt, int obj0, int nobj) const
+{
+	Box b = box_at(t0, t1, obj0, nobj);
+	double dx = b.mx[0] - b.mn[0], dy = b.mx[1] - b.mn[1], dz = b.mx[2] - b.mn[2];
 	return sqrt(dx * dx + dy * dy + dz * dz) * opt.gather_dist;
 }
 

@@ -197,13 +197,21 @@ struct HostScene {
 	bool from_desc(const sray_scene_desc &d, const sray_opts &opt, std::string &err);
 	void finish_load(const sray_opts &opt, bool build_meshes);
 	void build_tree(int t0, int t1, const sray_opts &opt);
-	/* the gather radius build_tree(t0, t1) would set, without building */
+	/* build_tree's object bounds cache, root box and gather radius without
+	 * the octree (a scene set's scenes have octrees of their own): oct keeps
+	 * its root node only */
+	void bound_objects(int t0, int t1, const sray_opts &opt);
+	/* the root box and gather radius build_tree(t0, t1) would give the
+	 * objects obj0 .. obj0 + nobj, without building */
+	Box box_at(int t0, int t1, int obj0 = 0, int nobj = -1) const;
 	double gather_dist_at(int t0, int t1, const sray_opts &opt, int obj0 = 0, int nobj = -1) const;
 	/* the projection maps of lights [light0, light0 + nlight) over objects
 	 * [obj0, obj0 + nobj) (all by default); a light's stream is keyed by its
 	 * index within that range */
 	void build_projmaps(int t0, int t1, uint64_t seed, int light0 = 0, int nlight = -1, int obj0 = 0, int nobj = -1);
 	void build_light_projmaps(size_t li, int t0, int t1, uint64_t seed, int key, int obj0, int nobj);
+	/* the same maps of light li into pm / spm (the light's own are untouched) */
+	void light_projmaps(size_t li, int t0, int t1, uint64_t seed, int key, int obj0, int nobj, ProjMap &pm, ProjMap &spm) const;
 };
 
 /* general 4x4 inverse by the adjugate */

@@ -414,15 +414,18 @@ class GpuRenderer:
     def set_profiling(self, time_kernels=False, count_work=False):
         self._chk(self.L.sray_gpu_set_profiling((1 if time_kernels else 0) | (2 if count_work else 0)))
 
-    def kernel_times(self, reset=True):
-        """{kernel kind: (total ms, launches)} accumulated since the last reset."""
+    def kernel_times(self, reset=True, host=False):
+        """{kernel kind: (total ms, launches)} accumulated since the last reset;
+        with host=True also the host phases ("host.<phase>": total ms, times
+        entered) timed beside them."""
         names = ctypes.create_string_buffer(4096)
         ms = np.zeros(64, np.float64)
         ln = np.zeros(64, np.int64)
         n = ctypes.c_int()
         self._chk(self.L.sray_gpu_kernel_times(names, 4096, _ptr(ms), _ptr(ln), 64, ctypes.byref(n), int(reset)))
         keys = names.raw.split(b"\0")[:n.value]
-        return {k.decode(): (float(ms[i]), int(ln[i])) for i, k in enumerate(keys)}
+        out = {k.decode(): (float(ms[i]), int(ln[i])) for i, k in enumerate(keys)}
+        return out if host else {k: v for k, v in out.items() if not k.startswith("host.")}
 
     def close(self):
         self.L.sray_gpu_shutdown()

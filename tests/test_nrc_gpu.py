@@ -1,6 +1,6 @@
 """The radiance-cache kernels against the CPU restatement (oracle/nrc.py).
 
-Forward: the tensor-core inference equals the oracle's bfloat16-rounded
+Forward: the tcgen05 inference equals the oracle's bfloat16-rounded
 forward pass (the kernels accumulate in FP32 in another order, so the bar is
 a relative tolerance).  Gradients: the packed gradient of the loss from the
 training kernels equals the oracle's backward pass with the same bfloat16
@@ -35,7 +35,7 @@ def test_forward_matches_oracle(cache):
     p = nrc.init_params(21)
     p[-3:] = (0.2, 0.5, 0.8)
     cache.set_params(p)
-    for n in (1, 37, 4096):
+    for n in (1, 37, 4096, 100003):      # 100003: several 128-sample tiles per group of every CTA
         x = inputs(rng, n)
         y = torch.empty((n, 3), dtype=torch.float32, device="cuda")
         cache.infer(torch.tensor(x, device="cuda"), y)
