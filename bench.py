@@ -574,7 +574,7 @@ def run_batch(args):
     if not args.no_autotune:
         best, best_ms, trials = g.autotune_batch(spec, frames=1, stream=stream)
         tuning = {"chosen": best, "ms_per_batch": best_ms,
-                  "trials": [dict(queue_depth=t["queue_depth"], warp_rays=t["warp_rays"], ms=round(ms, 2)) for t, ms in trials]}
+                  "trials": [dict(queue_depth=t["queue_depth"], warp_rays=t["warp_rays"], render_tail=t["render_tail"], ms=round(ms, 2)) for t, ms in trials]}
     for _ in range(args.warmup):
         batch()
     device_mb = (free0 - torch.cuda.mem_get_info()[0]) / 1e6
@@ -698,7 +698,9 @@ def run_stress_batch(args):
     clk = clocks.stop()
     launches = g.stats()["kernel_launches"]
     img_plain = fbs[0].cpu().numpy().copy()
-    g.set_opts(nrc=1)
+    # the learned configuration's training rate per frame (65,536 records, 4
+    # Adam steps), so a batch of nf frames trains on nf times as many
+    g.set_opts(nrc=1, nrc_train_samples=min(65536 * nf, 1 << 20), nrc_train_steps=4 * nf)
     g.nrc_reset()
     t0 = time.perf_counter()
     for _ in range(args.nrc_burn_in):
@@ -732,6 +734,7 @@ def run_stress_batch(args):
                          "cache": {"ms_per_batch": ms_cache, "ms_per_frame": ms_cache / nf,
                                    "mrays_per_s": rays_cache / (ms_cache / 1e3) / 1e6, "device_mb": mem_cache,
                                    "burn_in_batches": args.nrc_burn_in, "burn_in_s": burn_s, "frames_trained": st["frames"],
+                                   "train_samples_per_batch": st["train_samples"], "val_samples_per_batch": st["val_samples"],
                                    "cached_vertex_frac": st["cached"] / max(st["vertices"], 1),
                                    "regions_cached": st["regions_cached"], "val_rel_err": st["val_rel_err"]},
                          "cache_over_plain_time": ms_cache / ms_plain,

@@ -469,9 +469,11 @@ int sray_gpu_last_error(char *buf, size_t cap);
 /* The autotuner for batches (sray_gpu_render_batch): the queue depth
  * (65,536, 262,144 or 1,048,576 primary rays per wave) against the
  * traversal mode (thread per ray; one warp per ray in passes of at most
- * 16,384 rays or segments; one warp per ray in every pass), each trial
- * timed over `frames` batches after one warm-up.  Keeps and returns the
- * fastest; trials go into `log` as for sray_gpu_autotune. */
+ * 16,384 rays or segments; one warp per ray in every pass), then the best
+ * pair with the shading tree's tail in the persistent pool launch (below
+ * 32,768 and 131,072 rays in flight); each trial timed over `frames`
+ * batches after one warm-up.  Keeps and returns the fastest; trials go into
+ * `log` as for sray_gpu_autotune. */
 struct sray_job;
 int sray_gpu_autotune_batch(const struct sray_job *jobs, int n, int frames, void *stream, sray_tuning *best, float *best_ms,
 		sray_tune_trial *log, int log_cap, int *n_log);

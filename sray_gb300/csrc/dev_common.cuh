@@ -755,17 +755,42 @@ __device__ __forceinline__ bool trace_any_octree_impl(const DScene &S, V3 wo, V3
  * is RAY_MAGNITUDE times the unit direction (src/opt.h:21), while the scene is
  * a few hundred units across. */
 struct RayC {
-	V3 o, inv, slack;
+	V3 inv;
+	V3 cn, cf;            /* slab constants of the entry / exit planes: -(o inv) -/+ slack */
+	unsigned neg;         /* bit a: the direction's axis a is negative (the entry plane
+	                         is the box's upper bound) */
 };
+
+/* a 4-wide node's six bound vectors (lo x, y, z, hi x, y, z) as entry planes
+ * (n) and exit planes (f) of the ray */
+struct NodePlanes {
+	float4 nx, ny, nz, fx, fy, fz;
+};
+
+__device__ __forceinline__ NodePlanes node_planes(const float4 *np, const RayC &c)
+{
+	int sx = (c.neg & 1u) ? 3 : 0, sy = (c.neg & 2u) ? 3 : 0, sz = (c.neg & 4u) ? 3 : 0;
+	NodePlanes p;
+	p.nx = __ldg(np + sx);
+	p.ny = __ldg(np + 1 + sy);
+	p.nz = __ldg(np + 2 + sz);
+	p.fx = __ldg(np + 3 - sx);
+	p.fy = __ldg(np + 4 - sy);
+	p.fz = __ldg(np + 5 - sz);
+	return p;
+}
 
 __device__ __forceinline__ RayC make_rayc(const RayT &r, float bound)
 {
 	RayC c;
-	c.o = r.o;
 	c.inv = mk(fminf(fmaxf(r.inv.x, -1e20f), 1e20f), fminf(fmaxf(r.inv.y, -1e20f), 1e20f), fminf(fmaxf(r.inv.z, -1e20f), 1e20f));
 	float om = fmaxf(fmaxf(fabsf(r.o.x), fabsf(r.o.y)), fabsf(r.o.z));
 	float delta = (om + bound) * 7.6293945e-6f;   /* 2^-17 */
-	c.slack = mk(delta * fabsf(c.inv.x), delta * fabsf(c.inv.y), delta * fabsf(c.inv.z));
+	V3 sl = mk(delta * fabsf(c.inv.x), delta * fabsf(c.inv.y), delta * fabsf(c.inv.z));
+	V3 oi = mk(r.o.x * c.inv.x, r.o.y * c.inv.y, r.o.z * c.inv.z);
+	c.cn = mk(-oi.x - sl.x, -oi.y - sl.y, -oi.z - sl.z);
+	c.cf = mk(sl.x - oi.x, sl.y - oi.y, sl.z - oi.z);
+	c.neg = (c.inv.x < 0.0f ? 1u : 0u) | (c.inv.y < 0.0f ? 2u : 0u) | (c.inv.z < 0.0f ? 4u : 0u);
 	return c;
 }
 
@@ -775,14 +800,19 @@ __device__ __forceinline__ float box_bound(const float *mn, const float *mx)
 	return fmaxf(fmaxf(fmaxf(fabsf(mn[0]), fabsf(mn[1])), fmaxf(fabsf(mn[2]), fabsf(mx[0]))), fmaxf(fabsf(mx[1]), fabsf(mx[2])));
 }
 
-__device__ __forceinline__ bool wide_box(const RayC &c, float x0, float y0, float z0, float x1, float y1, float z1, float limit,
+/* The widened box test with the entry planes (nx, ny, nz) and exit planes
+ * (fx, fy, fz) picked by the direction's signs: each slab parameter is one
+ * FMA, x inv + c, with the widening in c.  Against (x - o) inv - slack this
+ * moves each parameter by a few units in the last place of o inv (and by
+ * the cancellation when x is near o, also of order ulp(o inv)); the slack is
+ * 2^-17 (|o| + R) |inv| >= 2^-17 |o inv|, over a hundred times that, so the
+ * test stays a superset of the octrees' candidates.  A box with its bounds
+ * swapped (an object no leaf lists) gives an empty interval. */
+__device__ __forceinline__ bool wide_box(const RayC &c, float nx, float ny, float nz, float fx, float fy, float fz, float limit,
 		float &tn)
 {
-	float ax = (x0 - c.o.x) * c.inv.x, bx = (x1 - c.o.x) * c.inv.x;
-	float ay = (y0 - c.o.y) * c.inv.y, by = (y1 - c.o.y) * c.inv.y;
-	float az = (z0 - c.o.z) * c.inv.z, bz = (z1 - c.o.z) * c.inv.z;
-	float tnear = fmaxf(fmaxf(fminf(ax, bx) - c.slack.x, fminf(ay, by) - c.slack.y), fminf(az, bz) - c.slack.z);
-	float tfar = fminf(fminf(fmaxf(ax, bx) + c.slack.x, fmaxf(ay, by) + c.slack.y), fmaxf(az, bz) + c.slack.z);
+	float tnear = fmaxf(fmaxf(fmaf(nx, c.inv.x, c.cn.x), fmaf(ny, c.inv.y, c.cn.y)), fmaf(nz, c.inv.z, c.cn.z));
+	float tfar = fminf(fminf(fmaf(fx, c.inv.x, c.cf.x), fmaf(fy, c.inv.y, c.cf.y)), fmaf(fz, c.inv.z, c.cf.z));
 	tn = tnear;
 	return tnear <= tfar && tfar >= 0.0f && tnear <= limit;
 }
@@ -956,18 +986,18 @@ __device__ __forceinline__ int trace_two_level(const DScene &S, V3 wo, V3 wd, in
 		 * objects) are visited nearest first, each leaf and object in an
 		 * iteration of its own so that the lanes of a warp stay together */
 		const float4 *np = reinterpret_cast<const float4 *>((inst ? S.bnodes : S.tnodes) + cur);
-		float4 lx = __ldg(np), ly = __ldg(np + 1), lz = __ldg(np + 2);
-		float4 hx = __ldg(np + 3), hy = __ldg(np + 4), hz = __ldg(np + 5);
+		const NodePlanes pl = node_planes(np, rc);
+		const float4 &nx = pl.nx, &ny = pl.ny, &nz = pl.nz, &fx = pl.fx, &fy = pl.fy, &fz = pl.fz;
 		int4 ch = __ldg(reinterpret_cast<const int4 *>(np) + 6);
 		if(COUNT) tc->nodes++;
 		float lim = fminf(best, 1.0f);
 		int ref[4] = {ch.x, ch.y, ch.z, ch.w};
 		float key[4];
 		float tn;
-		key[0] = (ref[0] != BVH_NONE && wide_box(rc, lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, lim, tn)) ? tn : INFINITY;
-		key[1] = (ref[1] != BVH_NONE && wide_box(rc, lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, lim, tn)) ? tn : INFINITY;
-		key[2] = (ref[2] != BVH_NONE && wide_box(rc, lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, lim, tn)) ? tn : INFINITY;
-		key[3] = (ref[3] != BVH_NONE && wide_box(rc, lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, lim, tn)) ? tn : INFINITY;
+		key[0] = (ref[0] != BVH_NONE && wide_box(rc, nx.x, ny.x, nz.x, fx.x, fy.x, fz.x, lim, tn)) ? tn : INFINITY;
+		key[1] = (ref[1] != BVH_NONE && wide_box(rc, nx.y, ny.y, nz.y, fx.y, fy.y, fz.y, lim, tn)) ? tn : INFINITY;
+		key[2] = (ref[2] != BVH_NONE && wide_box(rc, nx.z, ny.z, nz.z, fx.z, fy.z, fz.z, lim, tn)) ? tn : INFINITY;
+		key[3] = (ref[3] != BVH_NONE && wide_box(rc, nx.w, ny.w, nz.w, fx.w, fy.w, fz.w, lim, tn)) ? tn : INFINITY;
 		if(ANY && !SORT) {
 			/* the hit children in node order: the first is next, the rest
 			 * are stacked so that they pop in order */

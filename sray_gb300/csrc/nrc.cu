@@ -358,15 +358,16 @@ __global__ void __launch_bounds__(NRC_FWD_THREADS) k_nrc_forward(NrcDev net, int
 
 /* ---- The inference and query forward on the 5th-generation tensor cores ----
  * tcgen05.mma with the operands in shared memory and the accumulators in
- * tensor memory (TMEM).  A CTA of 256 threads is two groups of four warps;
- * each group carries a tile of 128 samples through the five layers: its
- * threads write the tile's encoded inputs (one sample per thread) into
- * shared memory, one elected thread issues the layer's MMAs (M = 128,
- * N = 64, K = 16 each; 14 for the 224-wide first layer, 4 for the others,
- * N = 16 for the output layer) and commits them to the group's mbarrier,
- * and the threads read their rows of the accumulator back from TMEM
- * (tcgen05.ld, 32x32b: a warp its 32 lanes) for the bias, ReLU and BF16
- * rounding that make the next layer's operand.  The two groups of a CTA
+ * tensor memory (TMEM).  A CTA of 512 threads is two groups of eight warps;
+ * each group carries a tile of 128 samples through the five layers, two
+ * threads per sample (row): its threads write the tile's encoded inputs
+ * (half of a row's features each) into shared memory, one elected thread
+ * issues the layer's MMAs (M = 128, N = 64, K = 16 each; 14 for the
+ * 224-wide first layer, 4 for the others, N = 16 for the output layer) and
+ * commits them to the group's mbarrier, and the threads read their rows of
+ * the accumulator back from TMEM (tcgen05.ld, 32x32b: warp w its lanes
+ * 32 (w mod 4) on; the two warps of a lane quarter take 32 columns each) for
+ * the bias, ReLU and BF16 rounding that make the next layer's operand.  The two groups of a CTA
  * interleave, so one group's encoding and epilogues overlap the other's
  * MMAs.  The weights (BF16, 54 KB) are copied once per CTA into the
  * canonical K-major layout without swizzle: 8-row x 16-byte core matrices,
@@ -374,7 +375,8 @@ __global__ void __launch_bounds__(NRC_FWD_THREADS) k_nrc_forward(NrcDev net, int
  * groups K/8 x 128 bytes apart (stride byte offset).  Every wait on an
  * mbarrier is bounded; one that runs out sets the error word and the group
  * stops (TMEM is released as usual). */
-#define TC_THREADS 256
+#define TC_THREADS 512
+#define TC_GROUP_THREADS 256
 #define TC_WAIT_LIMIT (1 << 20)
 
 enum {
@@ -440,37 +442,32 @@ __device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity)
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void group_sync(int g) { asm volatile("bar.sync %0, 128;" :: "r"(1 + g) : "memory"); }
+__device__ __forceinline__ void group_sync(int g) { asm volatile("bar.sync %0, %1;" :: "r"(1 + g), "n"(TC_GROUP_THREADS) : "memory"); }
 
 /* true when v holds in every thread of group g (its named barrier): a wait
  * that ran out in one thread stops the whole group together */
 __device__ __forceinline__ bool group_all(int g, bool v)
 {
 	uint32_t r;
-	asm volatile("{\n\t.reg .pred q, p;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.and.pred p, %2, 128, q;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
-			: "=r"(r) : "r"((uint32_t)v), "r"(1 + g) : "memory");
+	asm volatile("{\n\t.reg .pred q, p;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.and.pred p, %2, %3, q;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+			: "=r"(r) : "r"((uint32_t)v), "r"(1 + g), "n"(TC_GROUP_THREADS) : "memory");
 	return r != 0;
 }
 
-/* 64 columns of the calling thread's accumulator row (its warp's 32 lanes) */
-__device__ __forceinline__ void tc_ld64(uint32_t taddr, float (&v)[64])
+/* 32 columns of the calling thread's accumulator row (its warp's 32 lanes) */
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32])
 {
-	uint32_t r[64];
-	asm volatile("tcgen05.ld.sync.aligned.32x32b.x64.b32 "
-			"{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,"
-			"%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];"
+	uint32_t r[32];
+	asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+			"{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
 			: "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
 			  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
 			  "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-			  "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]),
-			  "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]),
-			  "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]),
-			  "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]),
-			  "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+			  "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
 			: "r"(taddr) : "memory");
 	asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 	#pragma unroll
-	for(int i = 0; i < 64; i++) v[i] = __uint_as_float(r[i]);
+	for(int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
 __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16])
@@ -485,6 +482,29 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16])
 	for(int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
+/* K-chunk c of a sample's encoded inputs: the (sin, cos) pairs of bands
+ * 4k .. 4k + 3 of input v (c = 3v + k; chunk 27 is padding).  Band 4k is
+ * evaluated (sincospif, exact argument scaling), the next three by angle
+ * doubling, sin 2a = 2 sin a cos a and cos 2a = 1 - 2 sin^2 a: a few units in
+ * the last place of FP32 after three steps, below the BF16 rounding that
+ * follows. */
+__device__ __forceinline__ uint4 tc_encode_chunk(const float *xv, int c)
+{
+	if(c >= NRC_F / 8) return make_uint4(0u, 0u, 0u, 0u);   /* 9 inputs x 3 chunks */
+	int v = c / 3, k = c - 3 * v;
+	float sn, cs;
+	sincospif(xv[v] * (float)(1 << (4 * k)), &sn, &cs);
+	uint32_t q[4];
+	#pragma unroll
+	for(int b = 0; b < 4; b++) {
+		q[b] = pack_bf16(sn, cs);
+		float s2 = 2.0f * (sn * cs);
+		cs = fmaf(-2.0f * sn, sn, 1.0f);
+		sn = s2;
+	}
+	return make_uint4(q[0], q[1], q[2], q[3]);
+}
+
 /* a weight image [rows][ld] (BF16) into the canonical layout of kc K-chunks,
  * rows beyond `rows` up to `rows_pad` zero */
 __device__ __forceinline__ void tc_weights(unsigned char *dst, const __nv_bfloat16 *src, int rows, int rows_pad, int ld, int kc)
@@ -497,17 +517,18 @@ __device__ __forceinline__ void tc_weights(unsigned char *dst, const __nv_bfloat
 	}
 }
 
-/* the hidden activations of the calling thread's row: bias, ReLU, BF16, canonical layout (8 K-chunks) */
-__device__ __forceinline__ void tc_hidden(unsigned char *H, int row, const float (&v)[64], const float *b)
+/* half `hf` (32 columns) of the hidden activations of the calling thread's
+ * row: bias, ReLU, BF16, canonical layout (8 K-chunks, this half's 4) */
+__device__ __forceinline__ void tc_hidden(unsigned char *H, int row, int hf, const float (&v)[32], const float *b)
 {
 	#pragma unroll
-	for(int c = 0; c < 8; c++) {
+	for(int c = 0; c < 4; c++) {
 		uint4 q;
 		q.x = pack_bf16(fmaxf(v[8 * c + 0] + b[8 * c + 0], 0.0f), fmaxf(v[8 * c + 1] + b[8 * c + 1], 0.0f));
 		q.y = pack_bf16(fmaxf(v[8 * c + 2] + b[8 * c + 2], 0.0f), fmaxf(v[8 * c + 3] + b[8 * c + 3], 0.0f));
 		q.z = pack_bf16(fmaxf(v[8 * c + 4] + b[8 * c + 4], 0.0f), fmaxf(v[8 * c + 5] + b[8 * c + 5], 0.0f));
 		q.w = pack_bf16(fmaxf(v[8 * c + 6] + b[8 * c + 6], 0.0f), fmaxf(v[8 * c + 7] + b[8 * c + 7], 0.0f));
-		*reinterpret_cast<uint4 *>(H + tc_canon(row, c, 8)) = q;
+		*reinterpret_cast<uint4 *>(H + tc_canon(row, hf * 4 + c, 8)) = q;
 	}
 }
 
@@ -528,11 +549,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_nrc_forward_tc(NrcDev net, in
 	tc_weights(tsm + TC_W5, net.w5, NRC_O, 16, LDH, 8);
 	float *sb = reinterpret_cast<float *>(tsm + TC_BIAS);
 	for(int i = threadIdx.x; i < NRC_NBIAS; i += blockDim.x) sb[i] = net.bias[i];
-	const int warp = threadIdx.x >> 5, g = warp >> 2, tid = threadIdx.x & 127;
+	/* group g: warps 8g .. 8g + 7; a warp's lane quarter (warp mod 4) gives
+	 * its rows, its half (hf) the features and accumulator columns it takes */
+	const int warp = threadIdx.x >> 5, g = warp >> 3, hf = (warp >> 2) & 1;
+	const int tid = ((warp & 3) << 5) | (threadIdx.x & 31);
+	const bool leader = (threadIdx.x & (TC_GROUP_THREADS - 1)) == 0;
 	unsigned char *gbase = tsm + TC_GROUP0 + g * TC_GROUP_BYTES;
 	const uint32_t mbar = sbase + TC_GROUP0 + g * TC_GROUP_BYTES + TC_MBAR;
 	uint32_t *tslot = reinterpret_cast<uint32_t *>(tsm + TC_TMEM_SLOT);
-	if(tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(mbar) : "memory");
+	if(leader) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(mbar) : "memory");
 	if(warp == 0) {
 		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
 				:: "r"(sbase + TC_TMEM_SLOT), "r"((uint32_t)TC_TMEM_COLS) : "memory");
@@ -547,52 +572,61 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_nrc_forward_tc(NrcDev net, in
 	const uint32_t tD = tmem + (uint32_t)(g * 128), tO = tD + 64;
 	const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
 	const uint32_t sA1 = sbase + TC_GROUP0 + g * TC_GROUP_BYTES + TC_A1, sH = sA1 + (TC_H - TC_A1);
-	const uint32_t sW1 = sbase + TC_W1, sWh[3] = {sbase + TC_W2, sbase + TC_W3, sbase + TC_W4}, sW5 = sbase + TC_W5;
+	const uint32_t sW1 = sbase + TC_W1, sW5 = sbase + TC_W5;
 	unsigned char *A1 = gbase + TC_A1, *H = gbase + TC_H;
 	const uint32_t id64 = tc_idesc(128, 64), id16 = tc_idesc(128, 16);
 	uint32_t phase = 0;
 	bool ok = true;
 	int ntiles = (n + 127) >> 7;
+	/* the inputs of this thread's sample in its group's next tile, loaded one
+	 * tile ahead so that the loads wait under the current tile's layers */
+	float xn[9];
+	{
+		int row = (blockIdx.x * 2 + g) * 128 + tid;
+		#pragma unroll
+		for(int k = 0; k < 9; k++) xn[k] = row < n ? x[(size_t)row * 9 + k] : 0.0f;
+	}
 	for(int tile = blockIdx.x * 2 + g; tile < ntiles && ok; tile += gridDim.x * 2) {
 		int row = tile * 128 + tid;
-		/* encoded inputs of this thread's sample: 28 chunks of 4 (sin, cos) pairs */
 		float xv[9];
 		#pragma unroll
-		for(int k = 0; k < 9; k++) xv[k] = row < n ? x[(size_t)row * 9 + k] : 0.0f;
-		for(int c = 0; c < NRC_FP / 8; c++) {
-			uint4 q;
-			q.x = feature_pair(xv, 4 * c);
-			q.y = feature_pair(xv, 4 * c + 1);
-			q.z = feature_pair(xv, 4 * c + 2);
-			q.w = feature_pair(xv, 4 * c + 3);
-			*reinterpret_cast<uint4 *>(A1 + tc_canon(tid, c, NRC_FP / 8)) = q;
+		for(int k = 0; k < 9; k++) xv[k] = xn[k];
+		{
+			int nrow = row + gridDim.x * 2 * 128;
+			#pragma unroll
+			for(int k = 0; k < 9; k++) xn[k] = nrow < n ? x[(size_t)nrow * 9 + k] : 0.0f;
 		}
+		/* encoded inputs of this thread's sample: its half of the 28 chunks
+		 * of 4 (sin, cos) pairs */
+		for(int c = hf * (NRC_FP / 16); c < (hf + 1) * (NRC_FP / 16); c++)
+			*reinterpret_cast<uint4 *>(A1 + tc_canon(tid, c, NRC_FP / 8)) = tc_encode_chunk(xv, c);
 		/* five layers: MMAs by one thread, epilogues by all */
 		for(int l = 0; l < 5 && ok; l++) {
 			proxy_fence();
 			tc_fence_before();
 			group_sync(g);
-			if(tid == 0) {
+			if(leader) {
 				tc_fence_after();
 				if(l == 0) {
 					for(int j = 0; j < NRC_FP / 16; j++)
 						tc_mma(tD, tc_desc(sA1 + j * 256, 128, (NRC_FP / 8) * 128), tc_desc(sW1 + j * 256, 128, (NRC_FP / 8) * 128), id64, j);
 				} else if(l < 4) {
-					for(int j = 0; j < 4; j++) tc_mma(tD, tc_desc(sH + j * 256, 128, 1024), tc_desc(sWh[l - 1] + j * 256, 128, 1024), id64, j);
+					const uint32_t sW = sbase + TC_W2 + (uint32_t)(l - 1) * (TC_W3 - TC_W2);   /* W2, W3, W4 back to back */
+					for(int j = 0; j < 4; j++) tc_mma(tD, tc_desc(sH + j * 256, 128, 1024), tc_desc(sW + j * 256, 128, 1024), id64, j);
 				} else {
 					for(int j = 0; j < 4; j++) tc_mma(tO, tc_desc(sH + j * 256, 128, 1024), tc_desc(sW5 + j * 256, 128, 1024), id16, j);
 				}
 				tc_commit(mbar);
 			}
 			ok = group_all(g, tc_wait(mbar, phase));
+			if(!ok) break;      /* phase stays the one still outstanding */
 			phase ^= 1u;
-			if(!ok) break;
 			tc_fence_after();
 			if(l < 4) {
-				float v[64];
-				tc_ld64(tD + lane_off, v);
-				tc_hidden(H, tid, v, sb + 64 * l);
-			} else {
+				float v[32];
+				tc_ld32(tD + lane_off + (uint32_t)(hf * 32), v);
+				tc_hidden(H, tid, hf, v, sb + 64 * l + hf * 32);
+			} else if(hf == 0) {
 				float v[16];
 				tc_ld16(tO + lane_off, v);
 				if(row < n) {

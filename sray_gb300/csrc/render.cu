@@ -150,7 +150,6 @@ __global__ void __launch_bounds__(SRAY_TRACE_THREADS, 6) k_trace(DScene S, RayQu
 #define WR_CAP 512
 #define WR_POP 8
 
-__device__ __forceinline__ float lane_pick(float4 v, int k) { return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w)); }
 
 /* One ray's two-level traversal by the calling warp (all 32 lanes, the
  * same arguments), with the warp's stack st_*.  ANY = false: returns 1 with
@@ -251,8 +250,11 @@ __device__ __forceinline__ int warp_trace(const DScene &S, V3 wo, V3 wd, int tim
 				}
 				int ch = __ldg(reinterpret_cast<const int *>(np + 6) + sub);
 				float tn;
-				if(ch != BVH_NONE && wide_box(rc, lane_pick(__ldg(np), sub), lane_pick(__ldg(np + 1), sub), lane_pick(__ldg(np + 2), sub),
-						lane_pick(__ldg(np + 3), sub), lane_pick(__ldg(np + 4), sub), lane_pick(__ldg(np + 5), sub), fminf(best, 1.0f), tn)) {
+				/* this lane's child in each bound vector, entry and exit planes by the direction's signs */
+				const float *nf = reinterpret_cast<const float *>(np) + sub;
+				int sx = (rc.neg & 1u) ? 12 : 0, sy = (rc.neg & 2u) ? 12 : 0, sz = (rc.neg & 4u) ? 12 : 0;
+				if(ch != BVH_NONE && wide_box(rc, __ldg(nf + sx), __ldg(nf + 4 + sy), __ldg(nf + 8 + sz), __ldg(nf + 12 - sx),
+						__ldg(nf + 16 - sy), __ldg(nf + 20 - sz), fminf(best, 1.0f), tn)) {
 					push = true;
 					pref = ch;
 					pobj = eobj;
@@ -827,11 +829,10 @@ struct PoolEmitter {
 	float4 *acc;
 	int *overflow;
 	unsigned long long shadows;
-	/* a light sample becomes a pool item of its own (iter = POOL_SHADOW),
-	 * traced by whichever thread claims it */
+	/* a light sample becomes a pool item of its own (iter = POOL_SHADOW, its
+	 * scene in path), traced by whichever thread claims it */
 	__device__ void shadow(V3 o, V3 d, int time, int slot, float r, float g, float b, int scene)
 	{
-		(void)scene;   /* scene sets render without the pool */
 		RayRec c;
 		c.o = o;
 		c.d = d;
@@ -843,7 +844,7 @@ struct PoolEmitter {
 		c.pixel = 0;
 		c.aslot = slot;
 		c.iter = POOL_SHADOW;
-		c.path = 0;
+		c.path = scene;
 		c.time = time;
 		c.sample = 0;
 		c.dsub = 0;
@@ -902,11 +903,11 @@ __global__ void __launch_bounds__(128) k_render_pool(DScene S, RayQueue pool, in
 		load_ray_l2(pool, i, r);
 		Hit h;
 		if(r.iter == POOL_SHADOW) {
-			int res = trace_two_level<false, true>(S, r.o, r.d, r.time, h, nullptr, &overflow);
+			int res = trace_two_level<false, true>(S, r.o, r.d, r.time, h, nullptr, &overflow, r.path);
 			if(res == 0) acc_add(acc, r.aslot, r.w[0], r.w[1], r.w[2]);
-			else if(res == 2) push_shadow(out, r.o, r.d, r.time, r.aslot, r.w[0], r.w[1], r.w[2], &overflow);
+			else if(res == 2) push_shadow(out, r.o, r.d, r.time, r.aslot, r.w[0], r.w[1], r.w[2], &overflow, r.path);
 			if(res != 2) em.shadows++;
-		} else if(!trace_two_level<false, false>(S, r.o, r.d, r.time, h, nullptr, &overflow)) {
+		} else if(!trace_two_level<false, false>(S, r.o, r.d, r.time, h, nullptr, &overflow, pixel_scene(S, r.pixel))) {
 			int slot = atomicAdd(out.qo.count, 1);
 			if(slot >= out.qo.cap) overflow = 1;
 			else store_ray(out.qo, slot, r);
@@ -2768,8 +2769,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 				if(int r = flush_gathers()) return r;
 			/* the pool holds every ray of the rest of the tree: enter it only
 			 * with POOL_HEADROOM times the rays' room in the queue */
-			if(depth >= 1 && !tail_done && n_rays <= tune.render_tail && (int64_t)n_rays * POOL_HEADROOM <= q[cur].cap &&
-					S.nscenes <= 1) {
+			if(depth >= 1 && !tail_done && n_rays <= tune.render_tail && (int64_t)n_rays * POOL_HEADROOM <= q[cur].cap) {
 				/* the rest of the shading tree in one launch (k_render_pool) */
 				tail_done = true;
 				if(int r = flush_gathers()) return r;
@@ -3567,30 +3567,37 @@ int sray_gpu_autotune_batch(const sray_job *jobs, int n, int frames, void *strea
 	sray_tuning base = R.tune, cur = R.tune;
 	float cur_ms = 0.0f;
 	int r = 0;
-	for(int di = 0; di < 3 && !r; di++) {
-		for(int mi = 0; mi < 3 && !r; mi++) {
-			sray_tuning t = base;
-			t.queue_depth = depths[di];
-			t.warp_rays = t.warp_segments = modes[mi];
-			R.tune = t;
-			r = R.render_batch(jobs, n, s);
-			if(r) { g_err = R.err; break; }
-			cudaEventRecord(e0, s);
-			for(int i = 0; i < frames && !r; i++) r = R.render_batch(jobs, n, s);
-			cudaEventRecord(e1, s);
-			if(r) { g_err = R.err; break; }
-			if(cudaEventSynchronize(e1) != cudaSuccess) { g_err = "autotune timing"; r = SRAY_ECUDA; break; }
-			float t_ms = 0.0f;
-			cudaEventElapsedTime(&t_ms, e0, e1);
-			sray_tune_trial tr;
-			memset(&tr, 0, sizeof tr);
-			tr.tuning = t;
-			tr.ms_per_frame = t_ms / (float)frames;
-			done.push_back(tr);
-			if(done.size() == 1 || tr.ms_per_frame < cur_ms) {
-				cur = t;
-				cur_ms = tr.ms_per_frame;
-			}
+	/* the nine pairs, then the best pair with the shading tree's tail in the
+	 * persistent pool launch (below 32k and 128k rays in flight) */
+	static const int tails[] = {1 << 15, 1 << 17};
+	for(int k = 0; k < 9 + 2 && !r; k++) {
+		sray_tuning t = base;
+		if(k < 9) {
+			t.queue_depth = depths[k / 3];
+			t.warp_rays = t.warp_segments = modes[k % 3];
+			t.render_tail = 0;
+		} else {
+			t = cur;
+			t.render_tail = tails[k - 9];
+		}
+		R.tune = t;
+		r = R.render_batch(jobs, n, s);
+		if(r) { g_err = R.err; break; }
+		cudaEventRecord(e0, s);
+		for(int i = 0; i < frames && !r; i++) r = R.render_batch(jobs, n, s);
+		cudaEventRecord(e1, s);
+		if(r) { g_err = R.err; break; }
+		if(cudaEventSynchronize(e1) != cudaSuccess) { g_err = "autotune timing"; r = SRAY_ECUDA; break; }
+		float t_ms = 0.0f;
+		cudaEventElapsedTime(&t_ms, e0, e1);
+		sray_tune_trial tr;
+		memset(&tr, 0, sizeof tr);
+		tr.tuning = t;
+		tr.ms_per_frame = t_ms / (float)frames;
+		done.push_back(tr);
+		if(done.size() == 1 || tr.ms_per_frame < cur_ms) {
+			cur = t;
+			cur_ms = tr.ms_per_frame;
 		}
 	}
 	cudaEventDestroy(e0);

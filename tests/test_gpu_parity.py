@@ -512,12 +512,15 @@ def test_gpu_restores_reference_dumps(gpu_lib, tmp_path):
         assert fmt <= 1e-6 and full <= 1.5e-6
 
 
-def test_scene_set_batch_matches_oracle(gpu_lib, oracle_lib):
+@pytest.mark.parametrize("tuning", [dict(queue_depth=4096), dict(queue_depth=8192, render_tail=1 << 20)],
+                         ids=["waves", "waves+pool"])
+def test_scene_set_batch_matches_oracle(gpu_lib, oracle_lib, tuning):
     # a scene set (three documents: the small scene, the feature scene with
     # moving objects and area lights, a terrain with instances) and one
     # batch mixing their jobs at different times, resolutions and photon
-    # counts, in waves of 4096 primary rays: each job is its scene's own
-    # frame (FP32 oracle, pixels keyed by their place in the batch)
+    # counts, in waves of 4096 primary rays, or of 8192 with each wave's
+    # shading tail in the persistent pool launch: each job is its scene's
+    # own frame (FP32 oracle, pixels keyed by their place in the batch)
     opts = dict(width=96, height=72, min_samples=1, max_samples=3, max_var=0.01, caust_photons=10000, gi_photons=20000,
                 iter=5, shadow_samples=2, diffuse_samples=1, mblur=1, shutter=40, gather_dist=0.02)
     paths = [scenegen.write_scene("small"), scenegen.write_scene("feature"),
@@ -526,9 +529,14 @@ def test_scene_set_batch_matches_oracle(gpu_lib, oracle_lib):
             (0, 64, 48, 2, dict(gi_photons=15000)), (100, 96, 72, 1, {}), (0, 48, 36, 0, dict(caust_photons=20000))]
     g = gpu_lib.GpuRenderer(**opts)
     g.load_scene_set(paths)
-    g.set_tuning(queue_depth=4096)
+    g.set_tuning(**tuning)
     fbs = [torch.zeros((h, w, 4), dtype=torch.float32, device="cuda") for _, w, h, _, _ in jobs]
+    g.set_profiling(time_kernels=True)
+    g.kernel_times(reset=True)
     g.render_batch([(ms, fb, dict(extra, scene=k)) for (ms, _, _, k, extra), fb in zip(jobs, fbs)])
+    pool_launches = g.kernel_times(reset=True).get("render_pool", (0.0, 0))[1]
+    g.set_profiling(False)
+    assert (pool_launches > 0) == ("render_tail" in tuning), pool_launches
     with pytest.raises(gpu_lib.SrayError):
         g.render(0)                                  # a scene set renders through batches only
     base = 0

@@ -1,8 +1,13 @@
 """The radiance-cache kernels against the CPU restatement (oracle/nrc.py).
 
 Forward: the tcgen05 inference equals the oracle's bfloat16-rounded
-forward pass (the kernels accumulate in FP32 in another order, so the bar is
-a relative tolerance).  Gradients: the packed gradient of the loss from the
+forward pass (the kernels accumulate in FP32 in another order and evaluate
+the encoding's higher bands by angle doubling, so the bar is a relative
+tolerance).  A bfloat16 network amplifies a one-ulp difference in a feature
+or hidden activation: in the oracle itself, moving 0.01 % of the features
+by one bfloat16 ulp moves the largest of 100,003 outputs by 2.1 % of the
+outputs' RMS while the RMS difference stays 3e-4.  So the RMS bar is 2e-3
+and the bar on the single worst sample 3e-2.  Gradients: the packed gradient of the loss from the
 training kernels equals the oracle's backward pass with the same bfloat16
 roundings.  Training: Adam steps on the GPU drive the loss down on a smooth
 target and track the oracle's own training trajectory.
@@ -43,7 +48,7 @@ def test_forward_matches_oracle(cache):
         got = y.cpu().numpy()
         scale = np.sqrt(np.mean(ref ** 2)) + 1e-3
         err = np.max(np.abs(got - ref)) / scale
-        assert err < 2e-2, (n, err)
+        assert err < 3e-2, (n, err)
         assert np.sqrt(np.mean((got - ref) ** 2)) / scale < 2e-3
 
 
