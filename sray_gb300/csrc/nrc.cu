@@ -380,16 +380,16 @@ __global__ void __launch_bounds__(NRC_FWD_THREADS) k_nrc_forward(NrcDev net, int
 #define TC_WAIT_LIMIT (1 << 20)
 
 enum {
+	TC_KH = 80,                         /* K of layers 2-5: 64 activations, the bias pair, zeros */
 	TC_W1 = 0,                          /* 64 x 224: 8 row groups x 28 K-chunks x 128 B */
-	TC_W2 = TC_W1 + 64 * NRC_FP * 2,
-	TC_W3 = TC_W2 + 64 * 64 * 2,
-	TC_W4 = TC_W3 + 64 * 64 * 2,
-	TC_W5 = TC_W4 + 64 * 64 * 2,        /* 16 x 64 (rows 3..15 zero) */
-	TC_BIAS = TC_W5 + 16 * 64 * 2,      /* FP32: 4 x 64 + 8 */
-	TC_GROUP0 = (TC_BIAS + NRC_NBIAS * 4 + 127) & ~127,
+	TC_W2 = TC_W1 + 64 * NRC_FP * 2,    /* 64 x 80 each */
+	TC_W3 = TC_W2 + 64 * TC_KH * 2,
+	TC_W4 = TC_W3 + 64 * TC_KH * 2,
+	TC_W5 = TC_W4 + 64 * TC_KH * 2,     /* 16 x 80 (rows 3..15 zero) */
+	TC_GROUP0 = (TC_W5 + 16 * TC_KH * 2 + 127) & ~127,
 	TC_A1 = 0,                          /* per group: 128 x 224 encoded inputs */
-	TC_H = TC_A1 + 128 * NRC_FP * 2,    /* 128 x 64 hidden activations */
-	TC_MBAR = TC_H + 128 * 64 * 2,
+	TC_H = TC_A1 + 128 * NRC_FP * 2,    /* 128 x 80 hidden activations */
+	TC_MBAR = TC_H + 128 * TC_KH * 2,
 	TC_GROUP_BYTES = TC_MBAR + 128,
 	TC_TMEM_SLOT = TC_GROUP0 + 2 * TC_GROUP_BYTES,
 	TC_SMEM = TC_TMEM_SLOT + 16,
@@ -490,7 +490,8 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16])
  * follows. */
 __device__ __forceinline__ uint4 tc_encode_chunk(const float *xv, int c)
 {
-	if(c >= NRC_F / 8) return make_uint4(0u, 0u, 0u, 0u);   /* 9 inputs x 3 chunks */
+	/* 9 inputs x 3 chunks; chunk 27 the constant pair (1, 1) of the bias */
+	if(c >= NRC_F / 8) return make_uint4(pack_bf16(1.0f, 1.0f), 0u, 0u, 0u);
 	int v = c / 3, k = c - 3 * v;
 	float sn, cs;
 	sincospif(xv[v] * (float)(1 << (4 * k)), &sn, &cs);
@@ -505,30 +506,47 @@ __device__ __forceinline__ uint4 tc_encode_chunk(const float *xv, int c)
 	return make_uint4(q[0], q[1], q[2], q[3]);
 }
 
-/* a weight image [rows][ld] (BF16) into the canonical layout of kc K-chunks,
- * rows beyond `rows` up to `rows_pad` zero */
-__device__ __forceinline__ void tc_weights(unsigned char *dst, const __nv_bfloat16 *src, int rows, int rows_pad, int ld, int kc)
+/* a weight image [rows][ld] (BF16) into the canonical layout of kc K-chunks:
+ * its first ks chunks, then in chunk ks the row's bias as a BF16 pair (hi,
+ * lo: b = hi + lo to 2^-17) that multiplies the operand's constant pair
+ * (1, 1), the rest zero; rows beyond `rows` up to `rows_pad` zero */
+__device__ __forceinline__ void tc_weights(unsigned char *dst, const __nv_bfloat16 *src, int rows, int rows_pad, int ld, int ks, int kc,
+		const float *bias)
 {
 	for(int i = threadIdx.x; i < rows_pad * kc; i += blockDim.x) {
 		int r = i / kc, c = i - r * kc;
 		uint4 v = make_uint4(0u, 0u, 0u, 0u);
-		if(r < rows) v = *reinterpret_cast<const uint4 *>(src + (size_t)r * ld + c * 8);
+		if(r < rows && c < ks) v = *reinterpret_cast<const uint4 *>(src + (size_t)r * ld + c * 8);
+		if(r < rows && c == ks) {
+			float b = bias[r];
+			__nv_bfloat16 hi = __float2bfloat16_rn(b);
+			v.x = pack_bf16(__bfloat162float(hi), b - __bfloat162float(hi));
+		}
 		*reinterpret_cast<uint4 *>(dst + tc_canon(r, c, kc)) = v;
 	}
 }
 
+/* two accumulator values as a BF16 pair after ReLU (lo in the low half) */
+__device__ __forceinline__ uint32_t relu_bf16x2(float lo, float hi)
+{
+	uint32_t d;
+	asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+	return d;
+}
+
 /* half `hf` (32 columns) of the hidden activations of the calling thread's
- * row: bias, ReLU, BF16, canonical layout (8 K-chunks, this half's 4) */
-__device__ __forceinline__ void tc_hidden(unsigned char *H, int row, int hf, const float (&v)[32], const float *b)
+ * row (the bias came with the product): ReLU, BF16, canonical layout (10
+ * K-chunks, this half's 4) */
+__device__ __forceinline__ void tc_hidden(unsigned char *H, int row, int hf, const float (&v)[32])
 {
 	#pragma unroll
 	for(int c = 0; c < 4; c++) {
 		uint4 q;
-		q.x = pack_bf16(fmaxf(v[8 * c + 0] + b[8 * c + 0], 0.0f), fmaxf(v[8 * c + 1] + b[8 * c + 1], 0.0f));
-		q.y = pack_bf16(fmaxf(v[8 * c + 2] + b[8 * c + 2], 0.0f), fmaxf(v[8 * c + 3] + b[8 * c + 3], 0.0f));
-		q.z = pack_bf16(fmaxf(v[8 * c + 4] + b[8 * c + 4], 0.0f), fmaxf(v[8 * c + 5] + b[8 * c + 5], 0.0f));
-		q.w = pack_bf16(fmaxf(v[8 * c + 6] + b[8 * c + 6], 0.0f), fmaxf(v[8 * c + 7] + b[8 * c + 7], 0.0f));
-		*reinterpret_cast<uint4 *>(H + tc_canon(row, hf * 4 + c, 8)) = q;
+		q.x = relu_bf16x2(v[8 * c + 0], v[8 * c + 1]);
+		q.y = relu_bf16x2(v[8 * c + 2], v[8 * c + 3]);
+		q.z = relu_bf16x2(v[8 * c + 4], v[8 * c + 5]);
+		q.w = relu_bf16x2(v[8 * c + 6], v[8 * c + 7]);
+		*reinterpret_cast<uint4 *>(H + tc_canon(row, hf * 4 + c, TC_KH / 8)) = q;
 	}
 }
 
@@ -542,13 +560,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_nrc_forward_tc(NrcDev net, in
 	}
 	extern __shared__ __align__(1024) unsigned char tsm[];
 	const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(tsm);
-	tc_weights(tsm + TC_W1, net.w1, 64, 64, LD1, NRC_FP / 8);
-	tc_weights(tsm + TC_W2, net.w2, 64, 64, LDH, 8);
-	tc_weights(tsm + TC_W3, net.w3, 64, 64, LDH, 8);
-	tc_weights(tsm + TC_W4, net.w4, 64, 64, LDH, 8);
-	tc_weights(tsm + TC_W5, net.w5, NRC_O, 16, LDH, 8);
-	float *sb = reinterpret_cast<float *>(tsm + TC_BIAS);
-	for(int i = threadIdx.x; i < NRC_NBIAS; i += blockDim.x) sb[i] = net.bias[i];
+	tc_weights(tsm + TC_W1, net.w1, 64, 64, LD1, NRC_F / 8, NRC_FP / 8, net.bias);
+	tc_weights(tsm + TC_W2, net.w2, 64, 64, LDH, 8, TC_KH / 8, net.bias + 64);
+	tc_weights(tsm + TC_W3, net.w3, 64, 64, LDH, 8, TC_KH / 8, net.bias + 128);
+	tc_weights(tsm + TC_W4, net.w4, 64, 64, LDH, 8, TC_KH / 8, net.bias + 192);
+	tc_weights(tsm + TC_W5, net.w5, NRC_O, 16, LDH, 8, TC_KH / 8, net.bias + 256);
 	/* group g: warps 8g .. 8g + 7; a warp's lane quarter (warp mod 4) gives
 	 * its rows, its half (hf) the features and accumulator columns it takes */
 	const int warp = threadIdx.x >> 5, g = warp >> 3, hf = (warp >> 2) & 1;
@@ -558,6 +574,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_nrc_forward_tc(NrcDev net, in
 	const uint32_t mbar = sbase + TC_GROUP0 + g * TC_GROUP_BYTES + TC_MBAR;
 	uint32_t *tslot = reinterpret_cast<uint32_t *>(tsm + TC_TMEM_SLOT);
 	if(leader) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(mbar) : "memory");
+	/* the hidden operand's chunks 8 and 9: the bias pair (1, 1), then zeros */
+	*reinterpret_cast<uint4 *>(gbase + TC_H + tc_canon(tid, 8 + hf, TC_KH / 8)) =
+			make_uint4(hf ? 0u : pack_bf16(1.0f, 1.0f), 0u, 0u, 0u);
 	if(warp == 0) {
 		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
 				:: "r"(sbase + TC_TMEM_SLOT), "r"((uint32_t)TC_TMEM_COLS) : "memory");
@@ -612,9 +631,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_nrc_forward_tc(NrcDev net, in
 						tc_mma(tD, tc_desc(sA1 + j * 256, 128, (NRC_FP / 8) * 128), tc_desc(sW1 + j * 256, 128, (NRC_FP / 8) * 128), id64, j);
 				} else if(l < 4) {
 					const uint32_t sW = sbase + TC_W2 + (uint32_t)(l - 1) * (TC_W3 - TC_W2);   /* W2, W3, W4 back to back */
-					for(int j = 0; j < 4; j++) tc_mma(tD, tc_desc(sH + j * 256, 128, 1024), tc_desc(sW + j * 256, 128, 1024), id64, j);
+					for(int j = 0; j < TC_KH / 16; j++)
+						tc_mma(tD, tc_desc(sH + j * 256, 128, TC_KH / 8 * 128), tc_desc(sW + j * 256, 128, TC_KH / 8 * 128), id64, j);
 				} else {
-					for(int j = 0; j < 4; j++) tc_mma(tO, tc_desc(sH + j * 256, 128, 1024), tc_desc(sW5 + j * 256, 128, 1024), id16, j);
+					for(int j = 0; j < TC_KH / 16; j++)
+						tc_mma(tO, tc_desc(sH + j * 256, 128, TC_KH / 8 * 128), tc_desc(sW5 + j * 256, 128, TC_KH / 8 * 128), id16, j);
 				}
 				tc_commit(mbar);
 			}
@@ -625,12 +646,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_nrc_forward_tc(NrcDev net, in
 			if(l < 4) {
 				float v[32];
 				tc_ld32(tD + lane_off + (uint32_t)(hf * 32), v);
-				tc_hidden(H, tid, hf, v, sb + 64 * l + hf * 32);
+				tc_hidden(H, tid, hf, v);
 			} else if(hf == 0) {
 				float v[16];
 				tc_ld16(tO + lane_off, v);
 				if(row < n) {
-					float o[3] = {v[0] + sb[256], v[1] + sb[257], v[2] + sb[258]};
+					const float *o = v;   /* the bias came with the product */
 					if(MODE == FWD_QUERY) {
 						float4 wv = qo.w[row];
 						float *a = reinterpret_cast<float *>(qo.acc + __float_as_int(wv.w));

@@ -107,7 +107,7 @@ __global__ void k_camera(DScene S, const int *active, int a0, int na, int s0, in
  * alone.  Keeping the two in separate kernels keeps the octree code out of
  * the hierarchy traversal's register allocation. */
 template <bool COUNT, bool HYB>
-__global__ void __launch_bounds__(SRAY_TRACE_THREADS, 6) k_trace(DScene S, RayQueue q, int4 *hits, DevCounters *ctr, int *fb)
+__global__ void __launch_bounds__(SRAY_TRACE_THREADS, 8) k_trace(DScene S, RayQueue q, int4 *hits, DevCounters *ctr, int *fb)
 {
 	int n = HYB ? *q.count : fb[0];
 	TraceCounters tc = {0, 0};
@@ -926,7 +926,7 @@ __global__ void __launch_bounds__(128) k_render_pool(DScene S, RayQueue pool, in
  * (src/shader.cc:266), a hit anywhere on the segment [eps, 1] blocks */
 /* shadow rays; HYB and fb as for k_trace */
 template <bool HYB, bool SORT = true, bool COUNT = false>
-__global__ void __launch_bounds__(SRAY_TRACE_THREADS, 6) k_shadow(DScene S, const ShadowReq *sq, const int *sq_count, float4 *acc,
+__global__ void __launch_bounds__(SRAY_TRACE_THREADS, 8) k_shadow(DScene S, const ShadowReq *sq, const int *sq_count, float4 *acc,
 		DevCounters *ctr, int *fb)
 {
 	int n = HYB ? *sq_count : fb[0];
