@@ -111,8 +111,6 @@ struct DScene {
 	const DevLight *lights;
 	int nlights;
 	const float *light_pos;   /* 4 floats per light per time */
-	const uint32_t *projbits; /* per light: 64 words global map + 64 words caustic map */
-	const float *coverage;    /* per light: global, caustic */
 	const float *cam_m;       /* 12 floats per time */
 	float cam_f, cam_xsz, cam_ysz, cam_maxd;
 	float env_col[4], env_amb[4];
@@ -152,6 +150,12 @@ __device__ __forceinline__ int job_of(const DScene &S, int pixel)
 		else hi = mid - 1;
 	}
 	return lo;
+}
+
+/* the scene of a batch pixel in a scene set (-1: the view's own scene) */
+__device__ __forceinline__ int pixel_scene(const DScene &S, int pixel)
+{
+	return S.nscenes > 1 && S.njobs > 0 ? S.jobs[job_of(S, pixel)].scene : -1;
 }
 
 /* ---------------- float3 helpers (no contraction: built with -fmad=false) */

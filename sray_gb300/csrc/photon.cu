@@ -208,24 +208,51 @@ __device__ bool gen_dir(const uint32_t *bits, sray_rng *s, V3 *out)
 
 #define PHOTON_GUARD 4096   /* interactions per phase (loop bound of the oracle's tracer) */
 
-/* the two maps being traced: emission counts, per-light prefix sums and
- * power scales, and the per-photon output */
-struct PhotonSet {
+/* A job of the photon wavefront: one frame's two maps (a batch traces the
+ * maps of all its jobs in one wavefront).  Its photons are the global
+ * indices [base, base + total[0]) (caustic map) and then total[1] more
+ * (global map); each keeps the stream address of its frame's own photon
+ * (map, light within the scene, index within the light). */
+struct PJob {
+	int base;
 	int total[2];
-	int nlights;
-	const int *prefix[2];
-	const float *scale[2];
-	DevPhoton *out[2];
-	int *valid[2];
+	int light0, nlights;  /* its scene's lights in the light table */
+	int prefix0;          /* per-light prefix sums at prefix + prefix0: the caustic
+	                         map's nlights + 1, then the global map's */
+	int scale0;           /* per-light power scales at scale + scale0: caustic, then global */
+	int proj0;            /* its first light's projection maps (128 words) and coverages (2) */
+	int t0, t1;           /* the frame's interval */
 };
 
+struct PhotonSet {
+	int njobs, total;
+	const PJob *jobs;
+	const int *prefix;
+	const float *scale;
+	const uint32_t *projbits;
+	const float *coverage;
+	DevPhoton *out;       /* per global index: the stored photon and its flag */
+	int *valid;
+};
+
+__device__ __forceinline__ int pjob_of(const PhotonSet &P, int id)
+{
+	int lo = 0, hi = P.njobs - 1;
+	while(lo < hi) {
+		int mid = (lo + hi + 1) >> 1;
+		if(P.jobs[mid].base <= id) lo = mid;
+		else hi = mid - 1;
+	}
+	return lo;
+}
+
 __device__ __forceinline__ void push_photon(const RayQueue &q, int slot, const PRay &r, const PState &ph, int guard, int gid,
-		int li, int phase, int map, uint32_t draws)
+		int li, int job, int phase, int map, uint32_t draws)
 {
 	q.o[slot] = make_float4(r.o.x, r.o.y, r.o.z, ph.col[0]);
 	q.d[slot] = make_float4(r.d.x, r.d.y, r.d.z, ph.col[1]);
 	q.w[slot] = make_float4(ph.col[2], r.st.ior, __int_as_float(guard), __int_as_float(gid));
-	q.meta[slot] = make_int4(li, r.iter, phase | (ph.type << 4) | (map << 8), r.time);
+	q.meta[slot] = make_int4(li | (job << 16), r.iter, phase | (ph.type << 4) | (map << 8), r.time);
 	q.stk[slot] = make_float4(r.st.stk[0], r.st.stk[1], r.st.stk[2], r.st.stk[3]);
 	q.ext[slot] = make_int2((int)draws, r.st.sp);
 }
@@ -241,23 +268,26 @@ static __device__ __forceinline__ int photon_slot(int *counter)
 __global__ void __launch_bounds__(128) k_photon_emit(DScene S, PhotonSet P, RayQueue q, DevCounters *ctr)
 {
 	int gfail = 0;
-	int all = P.total[0] + P.total[1];
-	for(int id = blockIdx.x * blockDim.x + threadIdx.x; id < all; id += gridDim.x * blockDim.x) {
-		int map = id >= P.total[0] ? 1 : 0;
-		int gid = map ? id - P.total[0] : id;
+	for(int id = blockIdx.x * blockDim.x + threadIdx.x; id < P.total; id += gridDim.x * blockDim.x) {
+		int job = pjob_of(P, id);
+		const PJob &J = P.jobs[job];
+		int local = id - J.base;
+		int map = local >= J.total[0] ? 1 : 0;
+		int gid = map ? local - J.total[0] : local;
 		int global = map;
-		const int *prefix = P.prefix[map];
+		const int *prefix = P.prefix + J.prefix0 + map * (J.nlights + 1);
 		int li = 0;
-		while(li + 1 < P.nlights && prefix[li + 1] <= gid) li++;
+		while(li + 1 < J.nlights && prefix[li + 1] <= gid) li++;
 		int j = gid - prefix[li];
 		sray_rng s;
 		sray_rng_init(&s, S.seed, global ? SRAY_DOM_GLOBAL : SRAY_DOM_CAUST, (uint32_t)j, (uint32_t)li);
-		int ms = S.t0 == S.t1 ? S.t0 : (sray_rng_int(&s) % (S.t1 - S.t0) + S.t0);
-		const DevLight &L = S.lights[li];
+		int ms = J.t0 == J.t1 ? J.t0 : (sray_rng_int(&s) % (J.t1 - J.t0) + J.t0);
+		int lg = J.light0 + li;
+		const DevLight &L = S.lights[lg];
 		PState ph;
-		V3 pos = light_point(S, li, ms, &s);
-		float cov = S.coverage[li * 2 + (global ? 0 : 1)];
-		const uint32_t *bits = S.projbits + (size_t)li * 128 + (global ? 0 : 64);
+		V3 pos = light_point(S, lg, ms, &s);
+		float cov = P.coverage[(J.proj0 + li) * 2 + (global ? 0 : 1)];
+		const uint32_t *bits = P.projbits + (size_t)(J.proj0 + li) * 128 + (global ? 0 : 64);
 		for(int k = 0; k < 3; k++) ph.col[k] = L.col[k] * S.photon_energy;
 		for(int k = 0; k < 3; k++) ph.col[k] = ph.col[k] * cov;
 		ph.type = DIRECT_PHOTON;
@@ -274,7 +304,7 @@ __global__ void __launch_bounds__(128) k_photon_emit(DScene S, PhotonSet P, RayQ
 		} else {
 			dir = sphrand(&s, 1.0f);
 		}
-		P.valid[map][gid] = 0;
+		P.valid[id] = 0;
 		if(ok && S.iter > 0) {
 			PRay r;
 			r.o = pos;
@@ -285,7 +315,7 @@ __global__ void __launch_bounds__(128) k_photon_emit(DScene S, PhotonSet P, RayQ
 			r.st.sp = 0;
 			for(int k = 0; k < 4; k++) r.st.stk[k] = 0.0f;
 			int slot = photon_slot(q.count);
-			push_photon(q, slot, r, ph, 0, gid, li, global ? 0 : 1, map, s.n);
+			push_photon(q, slot, r, ph, 0, id, li, job, global ? 0 : 1, map, s.n);
 		}
 	}
 	if(gfail) atomicOr(&ctr->gen_dir_fail, 1);
@@ -295,7 +325,7 @@ __global__ void __launch_bounds__(128) k_photon_emit(DScene S, PhotonSet P, RayQ
 struct PFlight {
 	PRay r;
 	PState ph;
-	int li, gid, phase, guard, map;
+	int li, job, gid, phase, guard, map;   /* gid: the photon's global index */
 	uint32_t draws;
 };
 
@@ -304,7 +334,8 @@ __device__ __forceinline__ void load_photon(const RayQueue &q, int i, PFlight &f
 	float4 o4 = q.o[i], d4 = q.d[i], w4 = q.w[i], k4 = q.stk[i];
 	int4 meta = q.meta[i];
 	int2 ext = q.ext[i];
-	f.li = meta.x;
+	f.li = meta.x & 0xffff;
+	f.job = meta.x >> 16;
 	f.phase = meta.z & 15;
 	f.map = (meta.z >> 8) & 1;
 	f.guard = __float_as_int(w4.z);
@@ -326,20 +357,23 @@ __device__ __forceinline__ void load_photon(const RayQueue &q, int i, PFlight &f
 __device__ __forceinline__ int photon_interact(const DScene &S, const PhotonSet &P, PFlight &f, const Hit &h)
 {
 	int global = f.map;
+	const PJob &J = P.jobs[f.job];
+	int gid = f.gid - J.base - (f.map ? J.total[0] : 0);   /* within its frame's map */
 	sray_rng s;
-	sray_rng_init(&s, S.seed, global ? SRAY_DOM_GLOBAL : SRAY_DOM_CAUST, (uint32_t)(f.gid - P.prefix[f.map][f.li]), (uint32_t)f.li);
+	sray_rng_init(&s, S.seed, global ? SRAY_DOM_GLOBAL : SRAY_DOM_CAUST,
+			(uint32_t)(gid - P.prefix[J.prefix0 + f.map * (J.nlights + 1) + f.li]), (uint32_t)f.li);
 	sray_rng_seek(&s, f.draws);
 	int res = f.phase == 0 ? global_step(S, f.r, f.ph, h, &s) : caust_step(S, f.r, f.ph, h, &s);
 	f.draws = s.n;
 	if(res == P_STORE) {
 		if(!global && f.ph.type != CAUST_PHOTON) return 0;
-		float sc = P.scale[f.map][f.li];
+		float sc = P.scale[J.scale0 + f.map * J.nlights + f.li];
 		DevPhoton p;
 		p.p[0] = f.ph.pos.x; p.p[1] = f.ph.pos.y; p.p[2] = f.ph.pos.z; p.p[3] = f.ph.col[0] * sc;
 		p.d[0] = f.ph.dir.x; p.d[1] = f.ph.dir.y; p.d[2] = f.ph.dir.z; p.d[3] = f.ph.col[1] * sc;
 		p.n[0] = f.ph.norm.x; p.n[1] = f.ph.norm.y; p.n[2] = f.ph.norm.z; p.n[3] = f.ph.col[2] * sc;
-		P.out[f.map][f.gid] = p;
-		P.valid[f.map][f.gid] = 1;
+		P.out[f.gid] = p;
+		P.valid[f.gid] = 1;
 		return 1;
 	}
 	if(res == P_DROP) return 0;
@@ -368,7 +402,7 @@ __global__ void __launch_bounds__(128) k_photon_bounce(DScene S, PhotonSet P, Ra
 		if(photon_interact(S, P, f, h) != 2) continue;
 		int slot = photon_slot(qo.count);
 		if(slot >= qo.cap) continue;                 /* cannot happen: a photon has one successor */
-		push_photon(qo, slot, f.r, f.ph, f.guard, f.gid, f.li, f.phase, f.map, f.draws);
+		push_photon(qo, slot, f.r, f.ph, f.guard, f.gid, f.li, f.job, f.phase, f.map, f.draws);
 	}
 }
 
@@ -390,9 +424,9 @@ __global__ void __launch_bounds__(128) k_photon_finish(DScene S, PhotonSet P, Ra
 		load_photon(qi, i, f);
 		for(int step = 0; step < 2 * PHOTON_GUARD + 2; step++) {
 			Hit h;
-			if(!trace_two_level<false, false>(S, f.r.o, f.r.d, f.r.time, h, nullptr, &overflow)) {
+			if(!trace_two_level<false, false>(S, f.r.o, f.r.d, f.r.time, h, nullptr, &overflow, pixel_scene(S, f.gid))) {
 				int slot = photon_slot(qpend.count);
-				if(slot < qpend.cap) push_photon(qpend, slot, f.r, f.ph, f.guard, f.gid, f.li, f.phase, f.map, f.draws);
+				if(slot < qpend.cap) push_photon(qpend, slot, f.r, f.ph, f.guard, f.gid, f.li, f.job, f.phase, f.map, f.draws);
 				break;
 			}
 			if(h.obj < 0) break;
@@ -573,65 +607,97 @@ static int grid_n(int n, int block)
 
 #define PCK(call, where) do { cudaError_t e_ = (call); if(e_ != cudaSuccess) return R.cuda_fail(e_, where); } while(0)
 
-/* emission counts of one map: photon split by mean light intensity
- * (src/render.cc:87-110), per-light prefix sums and power scales uploaded */
-static int photon_setup(Renderer &R, int global, cudaStream_t s, int *total_out)
+/* emission counts of one map of a frame: photons split by mean light
+ * intensity (src/render.cc:87-110); appends the per-light prefix sums
+ * (nl + 1) and power scales (nl), returns the map's total */
+static int split_photons(const Renderer &R, int light0, int nl, int num, std::vector<int> &prefix, std::vector<float> &scale)
 {
-	PhotonBufs &P = global ? R.gi : R.caust;
-	const sray_opts &opt = R.opt;
-	/* a batch job's own photon count and its scene's lights */
-	int num = R.map_counts[global] >= 0 ? R.map_counts[global] : (global ? opt.gi_photons : opt.caust_photons);
-	int nl = R.map_nlight >= 0 ? R.map_nlight : (int)R.sc.lights.size();
-	P.map.n = 0;
-	*total_out = 0;
+	size_t p0 = prefix.size();
+	prefix.resize(p0 + nl + 1, 0);
+	scale.resize(scale.size() + nl, 0.0f);
+	size_t s0 = scale.size() - nl;
 	if(num <= 0 || nl <= 0) return 0;
 	std::vector<double> inten(nl);
 	double accp = 0.0;
 	for(int i = 0; i < nl; i++) {
-		const double *c = R.sc.lights[R.map_light0 + i].col;
+		const double *c = R.sc.lights[light0 + i].col;
 		inten[i] = (c[0] + c[1] + c[2]) / 3.0;
 		accp += inten[i];
 	}
-	std::vector<int> prefix(nl + 1, 0);
-	std::vector<float> scale(nl, 0.0f);
 	for(int i = 0; i < nl; i++) {
 		int nphot = (int)ceil((double)num * (inten[i] / accp));
-		prefix[i + 1] = prefix[i] + nphot;
-		scale[i] = nphot ? (float)(1.0 / (double)nphot) : 0.0f;
+		prefix[p0 + i + 1] = prefix[p0 + i] + nphot;
+		scale[s0 + i] = nphot ? (float)(1.0 / (double)nphot) : 0.0f;
 	}
-	int total = prefix[nl];
-	if(total <= 0) return 0;
-	PCK(P.prefix.upload(prefix, s), "photon prefix");
-	PCK(P.scale.upload(scale, s), "photon scale");
-	R.h2d += (int64_t)(prefix.size() * 4 + scale.size() * 4);
-	PCK(P.tmp_ph.ensure((size_t)total * sizeof(DevPhoton)), "photon buffer");
-	PCK(P.valid.ensure((size_t)total * sizeof(int)), "photon flags");
-	*total_out = total;
-	return 0;
+	return prefix[p0 + nl];
 }
 
-static int photon_finalize(Renderer &R, int global, int total, cudaStream_t s, int *stored);
-
-/* both photon maps, traced together */
-int photon_shoot_maps(Renderer &R, const DScene &base, cudaStream_t s, int *nc, int *ng)
+/* Both photon maps of every job, traced as one wavefront on stream s: the
+ * emission of all jobs' photons in one launch, then passes of closest hits
+ * and interactions over one queue (each photon finds its job, and through
+ * it its scene, lights, interval and projection maps), then the tail.  The
+ * stored photons and their flags stay in R.pw_out / R.pw_valid by global
+ * index; jobs[j].base and total[] locate each job's two segments. */
+int photon_trace_jobs(Renderer &R, const DScene &base, const std::vector<PhotonJobSpec> &spec, std::vector<PJobOut> &out,
+		cudaStream_t s)
 {
-	*nc = *ng = 0;
-	int tot[2];
-	int r;
-	if((r = photon_setup(R, 0, s, &tot[0]))) return r;
-	if((r = photon_setup(R, 1, s, &tot[1]))) return r;
-	int all = tot[0] + tot[1];
-	if(all <= 0) return 0;
-	PhotonSet PSet;
-	PSet.nlights = base.nlights;
-	for(int m = 0; m < 2; m++) {
-		PhotonBufs &P = m ? R.gi : R.caust;
-		PSet.total[m] = tot[m];
-		PSet.prefix[m] = P.prefix.as<int>();
-		PSet.scale[m] = P.scale.as<float>();
-		PSet.out[m] = P.tmp_ph.as<DevPhoton>();
-		PSet.valid[m] = P.valid.as<int>();
+	int n = (int)spec.size();
+	out.assign(n, PJobOut());
+	std::vector<PJob> jobs(n);
+	std::vector<int> prefix;
+	std::vector<float> scale, cov;
+	std::vector<uint32_t> bits;
+	std::vector<DevJob> pj(n);
+	int64_t all = 0;
+	for(int j = 0; j < n; j++) {
+		const PhotonJobSpec &J = spec[j];
+		PJob &d = jobs[j];
+		memset(&d, 0, sizeof d);
+		d.base = (int)all;
+		d.light0 = J.light0;
+		d.nlights = J.nlights;
+		d.prefix0 = (int)prefix.size();
+		d.scale0 = (int)scale.size();
+		d.proj0 = (int)(cov.size() / 2);
+		d.t0 = J.t0;
+		d.t1 = J.t1;
+		for(int m = 0; m < 2; m++) d.total[m] = split_photons(R, J.light0, J.nlights, J.num[m], prefix, scale);
+		if(J.nlights > 0) {
+			if(!J.bits || !J.cov || J.bits->size() < (size_t)J.nlights * 128 || J.cov->size() < (size_t)J.nlights * 2)
+				return R.fail(SRAY_ESTATE, "photon job without its projection maps");
+			bits.insert(bits.end(), J.bits->begin(), J.bits->begin() + (size_t)J.nlights * 128);
+			cov.insert(cov.end(), J.cov->begin(), J.cov->begin() + (size_t)J.nlights * 2);
+		}
+		memset(&pj[j], 0, sizeof pj[j]);
+		pj[j].pix0 = d.base;
+		pj[j].scene = J.scene;
+		out[j].base = d.base;
+		out[j].total[0] = d.total[0];
+		out[j].total[1] = d.total[1];
+		all += (int64_t)d.total[0] + d.total[1];
+		if(all > INT_MAX / 2) return R.fail(SRAY_EINVAL, "too many photons in one wavefront");
 	}
+	if(all == 0) return 0;
+	PCK(R.pw_jobs.upload(jobs, s), "photon jobs");
+	PCK(R.pw_prefix.upload(prefix, s), "photon prefix");
+	PCK(R.pw_scale.upload(scale, s), "photon scale");
+	PCK(R.pw_bits.upload(bits, s), "projection maps");
+	PCK(R.pw_cov.upload(cov, s), "coverage");
+	PCK(R.pw_pix.upload(pj, s), "photon job table");
+	R.h2d += (int64_t)(jobs.size() * sizeof(PJob) + prefix.size() * 4 + scale.size() * 4 + bits.size() * 4 + cov.size() * 4 +
+			pj.size() * sizeof(DevJob));
+	PCK(R.pw_out.ensure((size_t)all * sizeof(DevPhoton)), "photon buffer");
+	PCK(R.pw_valid.ensure((size_t)all * sizeof(int)), "photon flags");
+	PhotonSet PSet;
+	PSet.njobs = n;
+	PSet.total = (int)all;
+	PSet.jobs = R.pw_jobs.as<PJob>();
+	PSet.prefix = R.pw_prefix.as<int>();
+	PSet.scale = R.pw_scale.as<float>();
+	PSet.projbits = R.pw_bits.as<uint32_t>();
+	PSet.coverage = R.pw_cov.as<float>();
+	PSet.out = R.pw_out.as<DevPhoton>();
+	PSet.valid = R.pw_valid.as<int>();
 	PCK(R.pctr.ensure(sizeof(DevCounters)), "counters");
 	PCK(R.pcounts.ensure(64 * sizeof(int)), "counts");
 	PCK(cudaMemsetAsync(R.pctr.p, 0, sizeof(DevCounters), s), "counters");
@@ -639,15 +705,19 @@ int photon_shoot_maps(Renderer &R, const DScene &base, cudaStream_t s, int *nc, 
 	int *cnt = R.pcounts.as<int>();
 	R.pq[0].count = cnt + 0;
 	R.pq[1].count = cnt + 1;
-	if(R.ensure_pqueue(0, all) || R.ensure_pqueue(1, all)) return SRAY_ECUDA;
+	if(R.ensure_pqueue(0, (int)all) || R.ensure_pqueue(1, (int)all)) return SRAY_ECUDA;
 	PCK(R.phits.ensure((size_t)all * 16), "photon hits");
-	/* the scene as the photon kernels see it: their counters */
+	/* the scene as the photon kernels see it: their counters, and in a scene
+	 * set the photon job table, through which a photon's global index finds
+	 * its scene (the render's pixel table is not theirs) */
 	DScene PS = base;
 	PS.bvh_fallbacks = &R.pctr.as<DevCounters>()->bvh_fallbacks;
+	PS.jobs = PS.nscenes > 1 ? R.pw_pix.as<DevJob>() : nullptr;
+	PS.njobs = PS.nscenes > 1 ? n : 0;
 	DevCounters *pctr = R.pctr.as<DevCounters>();
-	LAUNCH(R, "photon_emit", s, k_photon_emit<<<grid_n(all, 128), 128, 0, s>>>(PS, PSet, R.pq[0], pctr));
+	LAUNCH(R, "photon_emit", s, k_photon_emit<<<grid_n((int)all, 128), 128, 0, s>>>(PS, PSet, R.pq[0], pctr));
 	int cur = 0;
-	int n_live = all;   /* upper bound until the first count is read */
+	int n_live = (int)all;   /* upper bound until the first count is read */
 	bool finished = false;
 	for(int pass = 0; n_live > 0; pass++) {
 		if(pass >= 2 * PHOTON_GUARD + 4) return R.fail(SRAY_EDEVICE, "photon paths did not terminate");
@@ -680,23 +750,23 @@ int photon_shoot_maps(Renderer &R, const DScene &base, cudaStream_t s, int *nc, 
 	R.d2h += sizeof(DevCounters);
 	if(hc.overflow) return R.fail(SRAY_EDEVICE, "traversal stack overflow while tracing photons");
 	if(hc.gen_dir_fail) return R.fail(SRAY_EDEVICE, "projection-map sampling found no covered cell");
-	if(tot[0] && (r = photon_finalize(R, 0, tot[0], s, nc))) return r;
-	if(tot[1] && (r = photon_finalize(R, 1, tot[1], s, ng))) return r;
 	return 0;
 }
 
-/* a map's stored photons: compacted in emission order, sorted by grid cell,
- * with the cell table */
-static int photon_finalize(Renderer &R, int global, int total, cudaStream_t s, int *stored)
+/* a map's stored photons from its segment of the wavefront's output
+ * (flags `valid`, photons `in`, `total` of them): compacted in emission
+ * order, sorted by grid cell, with the cell table */
+int photon_finalize(Renderer &R, int global, const int *valid, const DevPhoton *in, int total, cudaStream_t s, int *stored)
 {
 	PhotonBufs &P = global ? R.gi : R.caust;
-	const sray_opts &opt = R.opt;
 	*stored = 0;
+	P.map.n = 0;
+	if(total <= 0) return 0;
 	/* compaction in emission order */
 	int nb = (total + TILE - 1) / TILE;
 	PCK(P.scan.ensure((size_t)(nb + 4) * sizeof(unsigned)), "scan");
 	unsigned *bc = P.scan.as<unsigned>();
-	LAUNCH(R, "photon_compact", s, k_count_valid<<<nb, 256, 0, s>>>(P.valid.as<int>(), total, bc));
+	LAUNCH(R, "photon_compact", s, k_count_valid<<<nb, 256, 0, s>>>(valid, total, bc));
 	LAUNCH(R, "photon_compact", s, k_scan_excl<<<1, 1024, 0, s>>>(bc, nb, bc + nb));
 	unsigned h_n = 0;
 	PCK(cudaMemcpyAsync(&h_n, bc + nb, sizeof(unsigned), cudaMemcpyDeviceToHost, s), "stored count");
@@ -707,8 +777,37 @@ static int photon_finalize(Renderer &R, int global, int total, cudaStream_t s, i
 	*stored = n;
 	if(n == 0) return 0;
 	PCK(P.ph.ensure((size_t)n * sizeof(DevPhoton)), "photon map");
-	LAUNCH(R, "photon_compact", s, k_compact<<<nb, 256, 0, s>>>(P.valid.as<int>(), P.tmp_ph.as<DevPhoton>(), total, bc, P.ph.as<DevPhoton>()));
+	LAUNCH(R, "photon_compact", s, k_compact<<<nb, 256, 0, s>>>(valid, in, total, bc, P.ph.as<DevPhoton>()));
 	return photon_map_build(R, global, n, s);
+}
+
+/* both photon maps of the frame (one job): the wavefront, then each map from
+ * its segment */
+int photon_shoot_maps(Renderer &R, const DScene &base, const std::vector<uint32_t> &bits, const std::vector<float> &cov,
+		cudaStream_t s, int *nc, int *ng)
+{
+	*nc = *ng = 0;
+	R.caust.map.n = 0;
+	R.gi.map.n = 0;
+	std::vector<PhotonJobSpec> spec(1);
+	PhotonJobSpec &J = spec[0];
+	J.num[0] = R.opt.caust_photons;
+	J.num[1] = R.opt.gi_photons;
+	J.light0 = 0;
+	J.nlights = (int)R.sc.lights.size();
+	J.t0 = base.t0;
+	J.t1 = base.t1;
+	J.scene = -1;
+	J.bits = &bits;
+	J.cov = &cov;
+	std::vector<PJobOut> out;
+	int r = photon_trace_jobs(R, base, spec, out, s);
+	if(r) return r;
+	const DevPhoton *ph = R.pw_out.as<DevPhoton>();
+	const int *valid = R.pw_valid.as<int>();
+	if((r = photon_finalize(R, 0, valid, ph, out[0].total[0], s, nc))) return r;
+	int o1 = out[0].total[0];
+	return photon_finalize(R, 1, valid + o1, ph + o1, out[0].total[1], s, ng);
 }
 
 /* the map over the n photons in P.ph: grid, Morton sort, cell table */

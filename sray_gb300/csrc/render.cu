@@ -44,12 +44,6 @@ static __device__ __forceinline__ int warp_alloc(int *counter, int n)
 	return base + excl;
 }
 
-/* the scene of a batch pixel in a scene set (-1: the view's own scene) */
-__device__ __forceinline__ int pixel_scene(const DScene &S, int pixel)
-{
-	return S.nscenes > 1 && S.njobs > 0 ? S.jobs[job_of(S, pixel)].scene : -1;
-}
-
 /* ---------------------------------------------------------------- */
 /* primary rays of samples [s0, s0 + width) of every active pixel; the ray's
  * accumulator slot is (active index * width + sample - s0) */
@@ -1596,8 +1590,6 @@ void Renderer::fill_scene_desc()
 	D.lights = lights.as<DevLight>();
 	D.nlights = (int)sc.lights.size();
 	D.light_pos = light_pos.as<float>();
-	D.projbits = projbits.as<uint32_t>();
-	D.coverage = coverage.as<float>();
 	D.cam_m = cam_m.as<float>();
 	D.cam_f = (float)(1.0 / tan(0.5 * sc.cam.vfov));
 	D.cam_xsz = (float)(sc.cam.aspect * 2.0);
@@ -2118,93 +2110,74 @@ int Renderer::shoot_maps(const DScene &base, cudaStream_t s, int *nc, int *ng)
 	caust.map.n = 0;
 	gi.map.n = 0;
 	*nc = *ng = 0;
-	/* the lights and objects of the maps' scene (a batch job's in a scene set) */
-	int l0 = map_light0, nl = map_nlight >= 0 ? map_nlight : (int)sc.lights.size();
-	int o0 = map_obj0, no = map_nobj >= 0 ? map_nobj : (int)sc.objs.size();
-	int cp = map_counts[0] >= 0 ? map_counts[0] : opt.caust_photons, gp = map_counts[1] >= 0 ? map_counts[1] : opt.gi_photons;
-	if(!(cp || gp) || nl == 0) return 0;
-	/* projection maps (src/render.cc:87-103) over the photons' interval:
-	 * a batch job's were built beforehand (map_bits / map_cov) */
-	std::vector<uint32_t> own_bits;
-	std::vector<float> own_cov;
-	const std::vector<uint32_t> *bits = map_bits;
-	const std::vector<float> *cov = map_cov;
-	if(!bits || !cov) {
-		double tp = host_now_ms();
-		sc.build_projmaps(base.t0, base.t1, opt.seed, l0, nl, o0, no);
-		own_bits.assign((size_t)nl * 128, 0u);
-		own_cov.assign((size_t)nl * 2, 0.0f);
-		for(size_t i = 0; i < (size_t)nl; i++) pack_projmaps(sc.lights[l0 + i].pm, sc.lights[l0 + i].spm, &own_bits[i * 128], &own_cov[i * 2]);
-		host_time("host.projmaps", tp);
-		bits = &own_bits;
-		cov = &own_cov;
-	}
-	CK(projbits.upload(*bits, s), "upload projection maps");
-	CK(coverage.upload(*cov, s), "upload coverage");
-	h2d += (int64_t)(bits->size() * 4 + cov->size() * 4);
-	DScene D = base;
-	D.projbits = projbits.as<uint32_t>();
-	D.coverage = coverage.as<float>();
-	return photon_shoot_maps(*this, D, s, nc, ng);
+	int nl = (int)sc.lights.size();
+	if(!(opt.caust_photons || opt.gi_photons) || nl == 0) return 0;
+	/* projection maps (src/render.cc:87-103) over the photons' interval */
+	double tp = host_now_ms();
+	sc.build_projmaps(base.t0, base.t1, opt.seed);
+	std::vector<uint32_t> bits((size_t)nl * 128, 0u);
+	std::vector<float> cov((size_t)nl * 2, 0.0f);
+	for(size_t i = 0; i < (size_t)nl; i++) pack_projmaps(sc.lights[i].pm, sc.lights[i].spm, &bits[i * 128], &cov[i * 2]);
+	host_time("host.projmaps", tp);
+	return photon_shoot_maps(*this, base, bits, cov, s, nc, ng);
 }
 
 int Renderer::photon_job(DScene base)
 {
 	int c = 0, g = 0;
 	if(batch_t0.empty()) return shoot_maps(base, ps, &c, &g);
-	/* a batch: each job's maps over its own interval, then their table */
+	/* a batch: every job's two maps over its own interval, with its own
+	 * photon counts and its scene's lights, in one photon wavefront; then
+	 * each map from its segment, and their table */
 	size_t n = batch_t0.size();
 	std::vector<DPhotonMap> hm(2 * n);
-	const DScene base0 = base;
 	std::vector<std::vector<uint32_t>> jbits;
 	std::vector<std::vector<float>> jcov;
 	double tp = host_now_ms();
 	batch_projmaps(jbits, jcov);
 	host_time("host.projmaps", tp);
+	std::vector<PhotonJobSpec> spec(n);
+	std::vector<int> o0(n, 0), no(n, (int)sc.objs.size());
 	for(size_t j = 0; j < n; j++) {
-		base = base0;
-		base.t0 = batch_t0[j];
-		base.t1 = batch_t1[j];
-		int o0 = 0, no = (int)sc.objs.size();
+		PhotonJobSpec &J = spec[j];
+		J.light0 = 0;
+		J.nlights = (int)sc.lights.size();
 		if(!scene_refs.empty()) {
-			/* a scene set: the view of the job's scene (its roots and lights),
-			 * its own photon counts */
-			int k = batch_scene[j];
-			const SceneRange &rg = sc.ranges[k];
-			const DevSceneRef &ref = scene_refs[k];
-			base.sroot = ref.sroot;
-			base.troot = ref.troot;
-			base.has_scene = base0.has_scene && ref.sroot >= 0;
-			base.lights = base0.lights + rg.light0;
-			base.nlights = rg.nlight;
-			base.light_pos = base0.light_pos + (size_t)rg.light0 * nt * 4;
-			base.nscenes = 0;
-			base.scenes = nullptr;
-			map_light0 = rg.light0;
-			map_nlight = rg.nlight;
-			map_obj0 = o0 = rg.obj0;
-			map_nobj = no = rg.nobj;
+			const SceneRange &rg = sc.ranges[batch_scene[j]];
+			J.light0 = rg.light0;
+			J.nlights = rg.nlight;
+			J.scene = batch_scene[j];
+			o0[j] = rg.obj0;
+			no[j] = rg.nobj;
 		}
-		map_counts[0] = batch_caust[j] > 0 ? batch_caust[j] : -1;
-		map_counts[1] = batch_gi[j] > 0 ? batch_gi[j] : -1;
-		/* the radius Scene::build_tree gives the job's own frame: the batch's
-		 * tree spans every job's interval */
-		map_gather_dist = sc.gather_dist_at(batch_t0[j], batch_t1[j], opt, o0, no);
-		map_box = sc.box_at(batch_t0[j], batch_t1[j], o0, no);
+		J.num[0] = batch_caust[j] > 0 ? batch_caust[j] : opt.caust_photons;
+		J.num[1] = batch_gi[j] > 0 ? batch_gi[j] : opt.gi_photons;
+		J.t0 = (int)batch_t0[j];
+		J.t1 = (int)batch_t1[j];
+		J.bits = &jbits[j];
+		J.cov = &jcov[j];
+	}
+	std::vector<PJobOut> out;
+	int r = photon_trace_jobs(*this, base, spec, out, ps);
+	if(r) return r;
+	const DevPhoton *ph = pw_out.as<DevPhoton>();
+	const int *valid = pw_valid.as<int>();
+	for(size_t j = 0; j < n; j++) {
+		/* the radius and grid box Scene::build_tree gives the job's own
+		 * frame: the batch's tree spans every job's interval */
+		map_gather_dist = sc.gather_dist_at(batch_t0[j], batch_t1[j], opt, o0[j], no[j]);
+		map_box = sc.box_at(batch_t0[j], batch_t1[j], o0[j], no[j]);
 		map_has_box = true;
-		map_bits = &jbits[j];
-		map_cov = &jcov[j];
-		int r = shoot_maps(base, ps, &c, &g);
-		map_gather_dist = -1.0;
-		map_has_box = false;
-		map_bits = nullptr;
-		map_cov = nullptr;
-		map_light0 = map_obj0 = 0;
-		map_nlight = map_nobj = -1;
-		map_counts[0] = map_counts[1] = -1;
-		if(r) return r;
 		std::swap(caust, job_maps[j].caust);
 		std::swap(gi, job_maps[j].gi);
+		int b = out[j].base, t0 = out[j].total[0];
+		r = photon_finalize(*this, 0, valid + b, ph + b, t0, ps, &c);
+		if(!r) r = photon_finalize(*this, 1, valid + b + t0, ph + b + t0, out[j].total[1], ps, &g);
+		std::swap(caust, job_maps[j].caust);
+		std::swap(gi, job_maps[j].gi);
+		map_gather_dist = -1.0;
+		map_has_box = false;
+		if(r) return r;
 		hm[2 * j] = job_maps[j].caust.map;
 		hm[2 * j + 1] = job_maps[j].gi.map;
 	}
@@ -3959,8 +3932,7 @@ void sray_gpu_shutdown(void)
 	for(Renderer::JobMaps &jm : R.job_maps) {
 		PhotonBufs *jp[] = {&jm.caust, &jm.gi};
 		for(PhotonBufs *p : jp) {
-			DevBuf *pbufs[] = {&p->ph, &p->cells, &p->tmp_ph, &p->valid, &p->keys, &p->keys2, &p->vals, &p->vals2, &p->lin, &p->hist,
-				&p->scan, &p->prefix, &p->scale};
+			DevBuf *pbufs[] = {&p->ph, &p->cells, &p->tmp_ph, &p->keys, &p->keys2, &p->vals, &p->vals2, &p->lin, &p->hist, &p->scan};
 			for(DevBuf *b : pbufs) b->release();
 		}
 	}
@@ -3969,16 +3941,16 @@ void sray_gpu_shutdown(void)
 	DevBuf *bufs[] = {&R.mnodes, &R.mtris, &R.mprim, &R.tri_pos, &R.tri_attr, &R.objs, &R.mats, &R.texs, &R.texels, &R.lights,
 		&R.anims, &R.key_t, &R.key_v,
 		&R.snodes, &R.sslots,
-		&R.xf, &R.light_pos, &R.cam_m, &R.projbits, &R.coverage, &R.qbuf[0], &R.qbuf[1], &R.hits, &R.gq, &R.sq, &R.acc, &R.hist, &R.sums,
+		&R.xf, &R.light_pos, &R.cam_m, &R.qbuf[0], &R.qbuf[1], &R.hits, &R.gq, &R.sq, &R.acc, &R.hist, &R.sums,
 		&R.active[0], &R.active[1], &R.spp, &R.fbdev, &R.ctr, &R.counts, &R.bnodes, &R.btris, &R.bprim, &R.bhome,
 		&R.fbl, &R.tnodes, &R.ohome, &R.pool_ready, &R.pqbuf[0], &R.pqbuf[1], &R.phits, &R.pfbl, &R.pcounts, &R.pctr,
+		&R.pw_jobs, &R.pw_prefix, &R.pw_scale, &R.pw_bits, &R.pw_cov, &R.pw_pix, &R.pw_out, &R.pw_valid,
 		&R.nrc_qx, &R.nrc_qw, &R.nrc_rx, &R.nrc_rt, &R.nrc_ry, &R.nrc_regions};
 	if(R.ps) cudaStreamSynchronize(R.ps);
 	for(DevBuf *b : bufs) b->release();
 	PhotonBufs *pb[] = {&R.caust, &R.gi};
 	for(PhotonBufs *p : pb) {
-		DevBuf *pbufs[] = {&p->ph, &p->cells, &p->tmp_ph, &p->valid, &p->keys, &p->keys2, &p->vals, &p->vals2, &p->lin, &p->hist, &p->scan,
-			&p->prefix, &p->scale};
+		DevBuf *pbufs[] = {&p->ph, &p->cells, &p->tmp_ph, &p->keys, &p->keys2, &p->vals, &p->vals2, &p->lin, &p->hist, &p->scan};
 		for(DevBuf *b : pbufs) b->release();
 	}
 	if(R.ps_done) cudaEventDestroy(R.ps_done);

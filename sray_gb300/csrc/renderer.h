@@ -116,7 +116,7 @@ struct NrcRegionStats {
 };
 
 struct PhotonBufs {
-	DevBuf ph, cells, tmp_ph, valid, keys, keys2, vals, vals2, lin, hist, scan, prefix, scale;
+	DevBuf ph, cells, tmp_ph, keys, keys2, vals, vals2, lin, hist, scan;
 	DPhotonMap map;
 	int n = 0;
 };
@@ -132,7 +132,7 @@ struct Renderer {
 	DevBuf mnodes, mtris, mprim, tri_pos, tri_attr, objs, mats, texs, texels, lights, bnodes, btris, bprim, bhome;
 	DevBuf anims, key_t, key_v;   /* keyframe tracks of the objects, then the lights */
 	/* frame tables (per build) */
-	DevBuf snodes, sslots, xf, light_pos, cam_m, projbits, coverage, tnodes, ohome;
+	DevBuf snodes, sslots, xf, light_pos, cam_m, tnodes, ohome;
 	bool built = false;
 	bool has_tlas = false;
 	int t0 = 0, t1 = 0, tlo = 0, nt = 1;
@@ -198,11 +198,11 @@ struct Renderer {
 	double map_gather_dist = -1.0;         /* >= 0: the range radius of the maps being built (a batch job's) */
 	bool map_has_box = false;              /* the grid box of the maps being built (a batch job's scene */
 	Box map_box;                           /* over its own interval), else the frame octree's root box */
-	const std::vector<uint32_t> *map_bits = nullptr;   /* a batch job's projection maps, built beforehand */
-	const std::vector<float> *map_cov = nullptr;
 	void batch_projmaps(std::vector<std::vector<uint32_t>> &bits, std::vector<std::vector<float>> &cov);
-	/* the photon job of a batch job: its scene's lights and its photon counts (-1: all lights, the options') */
-	int map_light0 = 0, map_nlight = -1, map_counts[2] = {-1, -1}, map_obj0 = 0, map_nobj = -1;
+	/* the photon wavefront's tables (photon.cu): jobs, per-light prefix sums
+	 * and scales, projection maps and coverages, the photons' job table for
+	 * the traversal, stored photons and their flags by global index */
+	DevBuf pw_jobs, pw_prefix, pw_scale, pw_bits, pw_cov, pw_pix, pw_out, pw_valid;
 	std::vector<int> batch_scene, batch_caust, batch_gi;   /* jobs' scenes and photon counts (0: the options') */
 	/* a scene set: its scene descriptors on the device */
 	DevBuf dscenes;
@@ -288,7 +288,21 @@ struct Renderer {
 int launch_trace(Renderer &R, const DScene &D, const RayQueue &q, int n, const char *name, cudaStream_t s);
 
 /* photon.cu: both maps traced with the scene view `base` */
-int photon_shoot_maps(Renderer &R, const DScene &base, cudaStream_t s, int *caust_stored, int *gi_stored);
+/* a frame's photon maps as a job of the photon wavefront (photon.cu) */
+struct PhotonJobSpec {
+	int num[2] = {0, 0};          /* photons asked for: caustic, global map */
+	int light0 = 0, nlights = 0;  /* its scene's lights */
+	int t0 = 0, t1 = 0;           /* its interval */
+	int scene = -1;               /* its scene in a scene set (-1: the view's own) */
+	const std::vector<uint32_t> *bits = nullptr;   /* its projection maps, 128 words per light */
+	const std::vector<float> *cov = nullptr;       /* their coverages, 2 per light */
+};
+struct PJobOut { int base = 0; int total[2] = {0, 0}; };   /* a job's photons: first global index, counts per map */
+int photon_trace_jobs(Renderer &R, const DScene &base, const std::vector<PhotonJobSpec> &spec, std::vector<PJobOut> &out,
+		cudaStream_t s);
+int photon_finalize(Renderer &R, int global, const int *valid, const DevPhoton *in, int total, cudaStream_t s, int *stored);
+int photon_shoot_maps(Renderer &R, const DScene &base, const std::vector<uint32_t> &bits, const std::vector<float> &cov,
+		cudaStream_t s, int *caust_stored, int *gi_stored);
 /* photon.cu: map `global` (0 caustic, 1 global) over the n photons in its buffer / from host photons */
 int photon_map_build(Renderer &R, int global, int n, cudaStream_t s);
 int photon_map_restore(Renderer &R, int global, const std::vector<DevPhoton> &h, cudaStream_t s);
