@@ -810,19 +810,12 @@ int photon_shoot_maps(Renderer &R, const DScene &base, const std::vector<uint32_
 	return photon_finalize(R, 1, valid + o1, ph + o1, out[0].total[1], s, ng);
 }
 
-/* the map over the n photons in P.ph: grid, Morton sort, cell table */
-int photon_map_build(Renderer &R, int global, int n, cudaStream_t s)
+/* A map's grid over box rb for gathers of radius rad (k nearest, or all
+ * within rad when k = 0): cells twice the radius, so that a query cube
+ * overlaps at most 2x2x2, at most 2^26 of them; the map's range constants.
+ * Morton keys when every dimension fits 10 bits. */
+static void map_grid(int k, double rad, const Box &rb, DPhotonMap &M, bool *morton, size_t *ncells)
 {
-	PhotonBufs &P = global ? R.gi : R.caust;
-	const sray_opts &opt = R.opt;
-	if(R.sc.oct.nodes.empty()) return R.fail(SRAY_ESTATE, "no scene bounds (build the frame first)");
-	/* grid over the scene bounds (a batch job's: its scene over its own
-	 * interval, the box its frame alone would have): cells of the gather radius */
-	const Box &rb = R.map_has_box ? R.map_box : R.sc.oct.nodes[0].box;
-	int k = global ? opt.gi_k : opt.caust_k;
-	/* a job of a batch gathers with the radius of its own interval */
-	double rad = k > 0 ? (double)opt.gather_rcap : (R.map_gather_dist >= 0.0 ? R.map_gather_dist : R.sc.gather_dist);
-	/* cells twice the gather radius: a query cube overlaps at most 2x2x2 */
 	double cell = rad > 0.0 ? 2.0 * rad : 1.0;
 	double ext[3];
 	for(int a = 0; a < 3; a++) ext[a] = rb.mx[a] - rb.mn[a];
@@ -836,8 +829,6 @@ int photon_map_build(Renderer &R, int global, int n, cudaStream_t s)
 		if(total_cells <= (double)(1 << 26)) break;
 		cell *= 1.25;
 	}
-	DPhotonMap &M = P.map;
-	M.n = n;
 	M.k = k;
 	M.cell = (float)cell;
 	while((double)M.cell < cell) M.cell = nextafterf(M.cell, INFINITY);
@@ -852,8 +843,27 @@ int photon_map_build(Renderer &R, int global, int n, cudaStream_t s)
 		M.r2_lo = (float)(r2 - (double)M.r2_hi);
 		M.screen = (float)(r2 * (1.0 + 1.0 / 1048576.0));
 	}
-	bool morton = dims[0] <= 1024 && dims[1] <= 1024 && dims[2] <= 1024;
-	size_t ncells = (size_t)dims[0] * dims[1] * dims[2];
+	*morton = dims[0] <= 1024 && dims[1] <= 1024 && dims[2] <= 1024;
+	*ncells = (size_t)dims[0] * dims[1] * dims[2];
+}
+
+/* the map over the n photons in P.ph: grid, Morton sort, cell table */
+int photon_map_build(Renderer &R, int global, int n, cudaStream_t s)
+{
+	PhotonBufs &P = global ? R.gi : R.caust;
+	const sray_opts &opt = R.opt;
+	if(R.sc.oct.nodes.empty()) return R.fail(SRAY_ESTATE, "no scene bounds (build the frame first)");
+	/* grid over the scene bounds (a batch job's: its scene over its own
+	 * interval, the box its frame alone would have) */
+	const Box &rb = R.map_has_box ? R.map_box : R.sc.oct.nodes[0].box;
+	int k = global ? opt.gi_k : opt.caust_k;
+	/* a job of a batch gathers with the radius of its own interval */
+	double rad = k > 0 ? (double)opt.gather_rcap : (R.map_gather_dist >= 0.0 ? R.map_gather_dist : R.sc.gather_dist);
+	DPhotonMap &M = P.map;
+	bool morton;
+	size_t ncells;
+	map_grid(k, rad, rb, M, &morton, &ncells);
+	M.n = n;
 	PCK(P.keys.ensure((size_t)n * 4), "keys");
 	PCK(P.keys2.ensure((size_t)n * 4), "keys");
 	PCK(P.vals.ensure((size_t)n * 4), "vals");
@@ -885,6 +895,237 @@ int photon_map_build(Renderer &R, int global, int n, cudaStream_t s)
 	std::swap(P.ph, P.tmp_ph);
 	M.ph = P.ph.as<DevPhoton>();
 	M.cells = P.cells.as<uint2>();
+	PCK(cudaStreamSynchronize(s), "photon map build");
+	R.prof_collect();
+	return 0;
+}
+
+/* ---------------- the maps of many jobs at once (a batch) ----------------
+ * The wavefront's output holds every job's two maps as segments (job-major,
+ * caustic then global).  One compaction keeps the stored photons of all
+ * segments in emission order; each photon's key is its cell in its own
+ * map's grid; a stable LSD radix sort by key and then by segment leaves the
+ * segments in order, each sorted by cell with ties in emission order -- the
+ * order a map sorted alone gets -- and each segment's cell table indexes
+ * its own photons. */
+
+#define SCAN_PART 8192   /* entries per block of the long scan */
+
+/* exclusive scan of each SCAN_PART-entry part in place (1024 threads, 8
+ * entries each); the part's total into sums */
+__global__ void k_scan_part(unsigned *data, int m, unsigned *sums)
+{
+	__shared__ unsigned part[1024];
+	int t = threadIdx.x;
+	int b = blockIdx.x * SCAN_PART + t * 8;
+	unsigned v[8], sum = 0;
+	#pragma unroll
+	for(int k = 0; k < 8; k++) {
+		v[k] = b + k < m ? data[b + k] : 0u;
+		sum += v[k];
+	}
+	part[t] = sum;
+	__syncthreads();
+	for(int off = 1; off < 1024; off <<= 1) {
+		unsigned u = t >= off ? part[t - off] : 0u;
+		__syncthreads();
+		part[t] += u;
+		__syncthreads();
+	}
+	unsigned run = part[t] - sum;
+	#pragma unroll
+	for(int k = 0; k < 8; k++) {
+		if(b + k < m) data[b + k] = run;
+		run += v[k];
+	}
+	if(t == 1023) sums[blockIdx.x] = part[1023];
+}
+
+__global__ void k_scan_add(unsigned *data, int m, const unsigned *offs)
+{
+	unsigned o = offs[blockIdx.x];
+	int b = blockIdx.x * SCAN_PART;
+	for(int i = b + threadIdx.x; i < b + SCAN_PART && i < m; i += blockDim.x) data[i] += o;
+}
+
+/* the segment holding compacted index i: the last s with offs[s] <= i */
+__device__ __forceinline__ int seg_of(const unsigned *offs, int nseg, unsigned i)
+{
+	int lo = 0, hi = nseg - 1;
+	while(lo < hi) {
+		int mid = (lo + hi + 1) >> 1;
+		if(offs[mid] <= i) lo = mid;
+		else hi = mid - 1;
+	}
+	return lo;
+}
+
+/* compacted index of each segment boundary: the tile's offset plus the
+ * stored photons of the tile before it (one block per boundary) */
+__global__ void k_seg_offsets(const int *valid, const unsigned *tile_offs, const int *bounds, unsigned *offs)
+{
+	__shared__ int red[256];
+	int b = bounds[blockIdx.x], tile = b / TILE, c = 0;
+	for(int i = tile * TILE + threadIdx.x; i < b; i += blockDim.x) c += valid[i];
+	red[threadIdx.x] = c;
+	__syncthreads();
+	for(int off = 128; off > 0; off >>= 1) {
+		if(threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+		__syncthreads();
+	}
+	if(threadIdx.x == 0) offs[blockIdx.x] = tile_offs[tile] + (unsigned)red[0];
+}
+
+/* cell keys of the compacted photons, each in its segment's grid */
+__global__ void k_keys_seg(const DevPhoton *ph, int n, const DPhotonMap *grids, const int *morton, const unsigned *offs, int nseg,
+		unsigned *keys, unsigned *vals, unsigned *lin)
+{
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		const DPhotonMap &M = grids[seg_of(offs, nseg, (unsigned)i)];
+		int c[3];
+		for(int a = 0; a < 3; a++) {
+			double v = floor(((double)ph[i].p[a] - (double)M.org[a]) / (double)M.cell);
+			c[a] = v < 0.0 ? 0 : (v > (double)(M.dims[a] - 1) ? M.dims[a] - 1 : (int)v);
+		}
+		unsigned l = (unsigned)(((size_t)c[2] * M.dims[1] + c[1]) * M.dims[0] + c[0]);
+		keys[i] = morton[seg_of(offs, nseg, (unsigned)i)] ? (spread3(c[0]) | (spread3(c[1]) << 1) | (spread3(c[2]) << 2)) : l;
+		vals[i] = (unsigned)i;
+		lin[i] = l;
+	}
+}
+
+/* the segment of each entry (by its compacted index) as the next pass's key */
+__global__ void k_seg_keys(const unsigned *vals, int n, const unsigned *offs, int nseg, unsigned *keys)
+{
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) keys[i] = (unsigned)seg_of(offs, nseg, vals[i]);
+}
+
+/* (first, end) of every occupied cell of every segment, relative to the
+ * segment's first photon, in the segment's own cell table */
+__global__ void k_cells_seg(const unsigned *lin, int n, const unsigned *offs, int nseg, const unsigned long long *cell_base, uint2 *cells)
+{
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		int sg = seg_of(offs, nseg, (unsigned)i);
+		unsigned i0 = offs[sg], i1 = offs[sg + 1];
+		unsigned l = lin[i];
+		uint2 *c = cells + cell_base[sg];
+		if((unsigned)i == i0 || lin[i - 1] != l) c[l].x = (unsigned)i - i0;
+		if((unsigned)i + 1 == i1 || lin[i + 1] != l) c[l].y = (unsigned)i + 1 - i0;
+	}
+}
+
+/* exclusive scan of m entries; the total into *total when given */
+static int scan_long(Renderer &R, unsigned *data, int m, unsigned *total, cudaStream_t s)
+{
+	if(m <= 65536) {
+		LAUNCH(R, "photon_sort", s, k_scan_excl<<<1, 1024, 0, s>>>(data, m, total));
+		return 0;
+	}
+	int parts = (m + SCAN_PART - 1) / SCAN_PART;
+	PCK(R.pw_part.ensure((size_t)(parts + 4) * sizeof(unsigned)), "scan parts");
+	unsigned *sums = R.pw_part.as<unsigned>();
+	LAUNCH(R, "photon_sort", s, k_scan_part<<<parts, 1024, 0, s>>>(data, m, sums));
+	LAUNCH(R, "photon_sort", s, k_scan_excl<<<1, 1024, 0, s>>>(sums, parts, total));
+	LAUNCH(R, "photon_sort", s, k_scan_add<<<parts, 256, 0, s>>>(data, m, sums));
+	return 0;
+}
+
+/* every job's two maps from the wavefront's output: maps[2j] caustic,
+ * maps[2j + 1] global, over the boxes and range radii of the jobs' own
+ * frames.  Returns 1 (nothing done) when the maps' cell tables together
+ * would pass 2^28 cells, for the map-by-map build to take over. */
+int photon_finalize_jobs(Renderer &R, const std::vector<PJobOut> &jobs, const std::vector<Box> &boxes,
+		const std::vector<double> &gather_dist, std::vector<DPhotonMap> &maps, cudaStream_t s)
+{
+	const sray_opts &opt = R.opt;
+	int nj = (int)jobs.size(), nseg = 2 * nj;
+	maps.assign(nseg, DPhotonMap());
+	std::vector<int> morton(nseg);
+	std::vector<unsigned long long> cell_base(nseg + 1, 0);
+	for(int sg = 0; sg < nseg; sg++) {
+		int k = (sg & 1) ? opt.gi_k : opt.caust_k;
+		double rad = k > 0 ? (double)opt.gather_rcap : gather_dist[sg >> 1];
+		bool mo;
+		size_t nc;
+		map_grid(k, rad, boxes[sg >> 1], maps[sg], &mo, &nc);
+		morton[sg] = mo ? 1 : 0;
+		cell_base[sg + 1] = cell_base[sg] + nc;
+	}
+	if(cell_base[nseg] > (1ull << 28)) return 1;
+	const PJobOut &last = jobs[nj - 1];
+	int total = last.base + last.total[0] + last.total[1];
+	if(total == 0) return 0;
+	const int *valid = R.pw_valid.as<int>();
+	int nb = (total + TILE - 1) / TILE;
+	PCK(R.pw_tiles.ensure((size_t)(nb + 4) * sizeof(unsigned)), "scan");
+	unsigned *bc = R.pw_tiles.as<unsigned>();
+	LAUNCH(R, "photon_compact", s, k_count_valid<<<nb, 256, 0, s>>>(valid, total, bc));
+	if(scan_long(R, bc, nb, bc + nb, s)) return SRAY_ECUDA;
+	std::vector<int> bounds(nseg + 1);
+	for(int j = 0; j < nj; j++) {
+		bounds[2 * j] = jobs[j].base;
+		bounds[2 * j + 1] = jobs[j].base + jobs[j].total[0];
+	}
+	bounds[nseg] = total;
+	PCK(R.pw_bounds.upload(bounds, s), "segment bounds");
+	PCK(R.pw_offs.ensure((size_t)(nseg + 1) * sizeof(unsigned)), "segment offsets");
+	unsigned *offs = R.pw_offs.as<unsigned>();
+	LAUNCH(R, "photon_compact", s, k_seg_offsets<<<nseg + 1, 256, 0, s>>>(valid, bc, R.pw_bounds.as<int>(), offs));
+	std::vector<unsigned> h_offs(nseg + 1);
+	PCK(cudaMemcpyAsync(h_offs.data(), offs, (nseg + 1) * sizeof(unsigned), cudaMemcpyDeviceToHost, s), "segment offsets");
+	PCK(cudaStreamSynchronize(s), "photon compaction");
+	R.d2h += (int64_t)(nseg + 1) * sizeof(unsigned);
+	R.h2d += (int64_t)bounds.size() * sizeof(int);
+	R.prof_collect();
+	int n = (int)h_offs[nseg];
+	for(int sg = 0; sg < nseg; sg++) maps[sg].n = (int)(h_offs[sg + 1] - h_offs[sg]);
+	if(n == 0) return 0;
+	PCK(R.pw_ph.ensure((size_t)n * sizeof(DevPhoton)), "photon maps");
+	PCK(R.pw_sorted.ensure((size_t)n * sizeof(DevPhoton)), "photon maps");
+	LAUNCH(R, "photon_compact", s, k_compact<<<nb, 256, 0, s>>>(valid, R.pw_out.as<DevPhoton>(), total, bc, R.pw_ph.as<DevPhoton>()));
+	PCK(R.pw_grids.upload(maps, s), "map grids");
+	PCK(R.pw_morton.upload(morton, s), "map keys");
+	PCK(R.pw_cellbase.upload(cell_base, s), "cell tables");
+	R.h2d += (int64_t)(maps.size() * sizeof(DPhotonMap) + morton.size() * 4 + cell_base.size() * 8);
+	PCK(R.pw_keys.ensure((size_t)n * 16), "keys");
+	PCK(R.pw_lin.ensure((size_t)n * 8), "cell ids");
+	PCK(R.pw_cells.ensure((size_t)cell_base[nseg] * sizeof(uint2) + 16), "cell tables");
+	unsigned *keys = R.pw_keys.as<unsigned>(), *vals = keys + n, *keys2 = keys + 2 * (size_t)n, *vals2 = keys + 3 * (size_t)n;
+	unsigned *lin = R.pw_lin.as<unsigned>(), *lin2 = lin + n;
+	LAUNCH(R, "photon_sort", s, k_keys_seg<<<grid_n(n, 256), 256, 0, s>>>(R.pw_ph.as<DevPhoton>(), n, R.pw_grids.as<DPhotonMap>(),
+			R.pw_morton.as<int>(), offs, nseg, keys, vals, lin));
+	int key_bits = 0;
+	for(int sg = 0; sg < nseg; sg++) {
+		unsigned long long maxkey = morton[sg] ? (1ull << 30) - 1ull : cell_base[sg + 1] - cell_base[sg] - 1ull;
+		int b = 0;
+		while(b < 32 && (maxkey >> b)) b++;
+		key_bits = std::max(key_bits, b);
+	}
+	int seg_bits = 0;
+	while(seg_bits < 32 && ((unsigned)(nseg - 1) >> seg_bits)) seg_bits++;
+	int nbr = (n + TILE - 1) / TILE;
+	PCK(R.pw_hist.ensure((size_t)256 * nbr * sizeof(unsigned) + 16), "radix histogram");
+	unsigned *hist = R.pw_hist.as<unsigned>();
+	int key_passes = (key_bits + 7) / 8, seg_passes = (seg_bits + 7) / 8;
+	for(int ps = 0; ps < key_passes + seg_passes; ps++) {
+		if(ps == key_passes)
+			LAUNCH(R, "photon_sort", s, k_seg_keys<<<grid_n(n, 256), 256, 0, s>>>(vals, n, offs, nseg, keys));
+		int shift = (ps < key_passes ? ps : ps - key_passes) * 8;
+		LAUNCH(R, "photon_sort", s, k_rs_hist<<<nbr, RS_THREADS, 0, s>>>(keys, n, shift, hist, nbr));
+		if(scan_long(R, hist, 256 * nbr, nullptr, s)) return SRAY_ECUDA;
+		LAUNCH(R, "photon_sort", s, k_rs_scatter<<<nbr, RS_THREADS, 0, s>>>(keys, vals, n, shift, hist, nbr, keys2, vals2));
+		std::swap(keys, keys2);
+		std::swap(vals, vals2);
+	}
+	LAUNCH(R, "photon_sort", s, k_permute<<<grid_n(n, 256), 256, 0, s>>>(R.pw_ph.as<DevPhoton>(), vals, lin, n, R.pw_sorted.as<DevPhoton>(),
+			lin2));
+	PCK(cudaMemsetAsync(R.pw_cells.p, 0, (size_t)cell_base[nseg] * sizeof(uint2), s), "cell tables");
+	LAUNCH(R, "photon_sort", s, k_cells_seg<<<grid_n(n, 256), 256, 0, s>>>(lin2, n, offs, nseg, R.pw_cellbase.as<unsigned long long>(),
+			R.pw_cells.as<uint2>()));
+	for(int sg = 0; sg < nseg; sg++) {
+		maps[sg].ph = R.pw_sorted.as<DevPhoton>() + h_offs[sg];
+		maps[sg].cells = R.pw_cells.as<uint2>() + cell_base[sg];
+	}
 	PCK(cudaStreamSynchronize(s), "photon map build");
 	R.prof_collect();
 	return 0;

@@ -2160,13 +2160,33 @@ int Renderer::photon_job(DScene base)
 	std::vector<PJobOut> out;
 	int r = photon_trace_jobs(*this, base, spec, out, ps);
 	if(r) return r;
+	/* the maps of all jobs together: grids over the jobs' own boxes with
+	 * their own range radii (the batch's tree spans every job's interval) */
+	std::vector<Box> boxes(n);
+	std::vector<double> gdist(n);
+	for(size_t j = 0; j < n; j++) {
+		boxes[j] = sc.box_at(batch_t0[j], batch_t1[j], o0[j], no[j]);
+		gdist[j] = sc.gather_dist_at(batch_t0[j], batch_t1[j], opt, o0[j], no[j]);
+	}
+	r = photon_finalize_jobs(*this, out, boxes, gdist, hm, ps);
+	if(r == 0) {
+		caust.map.n = 0;
+		gi.map.n = 0;
+		CK(dmaps.upload(hm, ps), "job photon maps");
+		CK(cudaStreamSynchronize(ps), "job photon maps");
+		h2d += (int64_t)(hm.size() * sizeof(DPhotonMap));
+		return 0;
+	}
+	if(r != 1) return r;
+	/* cell tables too large to hold together: map by map */
+	hm.assign(2 * n, DPhotonMap());
 	const DevPhoton *ph = pw_out.as<DevPhoton>();
 	const int *valid = pw_valid.as<int>();
 	for(size_t j = 0; j < n; j++) {
 		/* the radius and grid box Scene::build_tree gives the job's own
 		 * frame: the batch's tree spans every job's interval */
-		map_gather_dist = sc.gather_dist_at(batch_t0[j], batch_t1[j], opt, o0[j], no[j]);
-		map_box = sc.box_at(batch_t0[j], batch_t1[j], o0[j], no[j]);
+		map_gather_dist = gdist[j];
+		map_box = boxes[j];
 		map_has_box = true;
 		std::swap(caust, job_maps[j].caust);
 		std::swap(gi, job_maps[j].gi);
@@ -3945,6 +3965,8 @@ void sray_gpu_shutdown(void)
 		&R.active[0], &R.active[1], &R.spp, &R.fbdev, &R.ctr, &R.counts, &R.bnodes, &R.btris, &R.bprim, &R.bhome,
 		&R.fbl, &R.tnodes, &R.ohome, &R.pool_ready, &R.pqbuf[0], &R.pqbuf[1], &R.phits, &R.pfbl, &R.pcounts, &R.pctr,
 		&R.pw_jobs, &R.pw_prefix, &R.pw_scale, &R.pw_bits, &R.pw_cov, &R.pw_pix, &R.pw_out, &R.pw_valid,
+		&R.pw_part, &R.pw_tiles, &R.pw_bounds, &R.pw_offs, &R.pw_ph, &R.pw_sorted, &R.pw_grids, &R.pw_morton, &R.pw_cellbase,
+		&R.pw_keys, &R.pw_lin, &R.pw_cells, &R.pw_hist,
 		&R.nrc_qx, &R.nrc_qw, &R.nrc_rx, &R.nrc_rt, &R.nrc_ry, &R.nrc_regions};
 	if(R.ps) cudaStreamSynchronize(R.ps);
 	for(DevBuf *b : bufs) b->release();

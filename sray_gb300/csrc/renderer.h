@@ -203,6 +203,10 @@ struct Renderer {
 	 * and scales, projection maps and coverages, the photons' job table for
 	 * the traversal, stored photons and their flags by global index */
 	DevBuf pw_jobs, pw_prefix, pw_scale, pw_bits, pw_cov, pw_pix, pw_out, pw_valid;
+	/* a batch's maps built together (photon_finalize_jobs): scan scratch,
+	 * segment bounds and offsets, compacted and sorted photons, grids, keys,
+	 * cell tables */
+	DevBuf pw_part, pw_tiles, pw_bounds, pw_offs, pw_ph, pw_sorted, pw_grids, pw_morton, pw_cellbase, pw_keys, pw_lin, pw_cells, pw_hist;
 	std::vector<int> batch_scene, batch_caust, batch_gi;   /* jobs' scenes and photon counts (0: the options') */
 	/* a scene set: its scene descriptors on the device */
 	DevBuf dscenes;
@@ -301,6 +305,8 @@ struct PJobOut { int base = 0; int total[2] = {0, 0}; };   /* a job's photons: f
 int photon_trace_jobs(Renderer &R, const DScene &base, const std::vector<PhotonJobSpec> &spec, std::vector<PJobOut> &out,
 		cudaStream_t s);
 int photon_finalize(Renderer &R, int global, const int *valid, const DevPhoton *in, int total, cudaStream_t s, int *stored);
+int photon_finalize_jobs(Renderer &R, const std::vector<PJobOut> &jobs, const std::vector<Box> &boxes,
+		const std::vector<double> &gather_dist, std::vector<DPhotonMap> &maps, cudaStream_t s);
 int photon_shoot_maps(Renderer &R, const DScene &base, const std::vector<uint32_t> &bits, const std::vector<float> &cov,
 		cudaStream_t s, int *caust_stored, int *gi_stored);
 /* photon.cu: map `global` (0 caustic, 1 global) over the n photons in its buffer / from host photons */
