@@ -598,10 +598,13 @@ __global__ void k_cells(const unsigned *lin, int n, uint2 *cells)
 	}
 }
 
+/* Photon launches run beside the frame's higher-priority stream: a block
+ * per `block` items, so that blocks are short-lived and the frame's kernels
+ * get SMs as they free, instead of a capped grid whose blocks stride over
+ * the whole launch and hold their SMs until it ends. */
 static int grid_n(int n, int block)
 {
 	int g = (n + block - 1) / block;
-	if(g > 152 * 16) g = 152 * 16;
 	return g < 1 ? 1 : g;
 }
 

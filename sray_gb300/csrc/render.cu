@@ -2941,11 +2941,14 @@ int Renderer::queue_overflow(int count, int cap)
  * rays of q into hits: the hierarchy pass, then the octree pass over the
  * rays it listed */
 int Renderer::trace_rays_with(const DScene &D, const RayQueue &qq, int n, const char *name, bool count, cudaStream_t s,
-		int4 *hit_out, DevBuf &fb, DevCounters *c)
+		int4 *hit_out, DevBuf &fb, DevCounters *c, bool short_blocks)
 {
 	CK(fb.ensure(((size_t)n + 1) * sizeof(int)), "fallback list");
 	CK(cudaMemsetAsync(fb.p, 0, sizeof(int), s), "reset fallback list");
-	int g = grid_for(n, 128);
+	/* short_blocks (the photon stream's passes): a block per 128 rays
+	 * instead of a capped grid that strides, so that its blocks free their
+	 * SMs for the frame's stream as they finish */
+	int g = short_blocks ? std::max(1, (n + 127) / 128) : grid_for(n, 128);
 	if(!count && n <= tune.warp_rays) {
 		/* a pass of few rays: one warp per ray */
 		LAUNCH(*this, name, s, k_trace_warp<<<grid_for(n, 4), 128, 0, s>>>(D, qq, hit_out, fb.as<int>()));
@@ -2994,7 +2997,7 @@ int Renderer::trace_rays(const RayQueue &qq, int n, const char *name, bool count
 /* photon passes: the photon buffers and counters */
 int launch_trace(Renderer &R, const DScene &D, const RayQueue &q, int n, const char *name, cudaStream_t s)
 {
-	return R.trace_rays_with(D, q, n, name, false, s, R.phits.as<int4>(), R.pfbl, R.pctr.as<DevCounters>());
+	return R.trace_rays_with(D, q, n, name, false, s, R.phits.as<int4>(), R.pfbl, R.pctr.as<DevCounters>(), true);
 }
 
 int Renderer::photon_stream()

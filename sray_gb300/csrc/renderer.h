@@ -276,7 +276,7 @@ struct Renderer {
 	int queue_alloc(DevBuf &buf, RayQueue &Q, int &qc, int cap);
 	int trace_rays(const RayQueue &q, int n, const char *name, bool count, cudaStream_t s);
 	int trace_rays_with(const DScene &D, const RayQueue &q, int n, const char *name, bool count, cudaStream_t s, int4 *hit_out,
-			DevBuf &fb, DevCounters *c);
+			DevBuf &fb, DevCounters *c, bool short_blocks = false);
 	int photon_stream();
 	void fill_scene_desc();
 };
