@@ -44,7 +44,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="production",
-                    choices=["production", "small", "learned", "stress", "batch", "stress-batch"])
+                    choices=["production", "small", "learned", "stress", "batch", "stress-batch", "nrc-infer"])
+    ap.add_argument("--nrc-samples", type=int, default=1 << 20, help="samples per launch of the nrc-infer configuration")
     ap.add_argument("--batch-frames", type=int, default=16, help="frames per batch of the stress-batch configuration")
     ap.add_argument("--batch-jobs", type=int, default=64, help="jobs of the batch configuration")
     ap.add_argument("--batch-scenes", type=int, default=16, help="scenes of the batch configuration's scene set")
@@ -1108,10 +1109,51 @@ def run_ours(args):
     return 0
 
 
+def run_nrc_infer(args):
+    """The radiance cache's tensor-core inference alone: `--nrc-samples`
+    uniform inputs, `--warmup` untimed calls, then `--steps` calls timed with
+    CUDA events (sray_nrc_infer: one k_nrc_forward_tc launch and a read of
+    its error word each); TFLOP/s of the 2 x 26,304 FLOP per sample against
+    the measured bf16 peak."""
+    import torch
+    from sray_gb300 import build as gbuild, gpu
+    torch.cuda.set_device(0)
+    gbuild.build()
+    n = args.nrc_samples
+    cache = gpu.RadianceCache(seed=1)
+    gen = torch.Generator(device="cuda").manual_seed(3)
+    x = torch.rand((n, 9), device="cuda", generator=gen)
+    y = torch.empty((n, 3), device="cuda")
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        cache.infer(x, y, stream=stream)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        cache.infer(x, y, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    tflops = 2 * 26304 * n / (ms / 1e3) / 1e12
+    peak = bf16_peak()
+    print(json.dumps({"metric": "radiance-cache inference (k_nrc_forward_tc)", "value": tflops, "unit": "TFLOP/s",
+                      "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+                      "higher_is_better": True, "dtype": "bf16", "data": "synthetic (uniform inputs)",
+                      "config": {"workload": "nrc-infer: %d samples per launch" % n},
+                      "roofline": {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s",
+                                   "frac": tflops / peak if peak else None},
+                      "finite": bool(torch.isfinite(y).all())}))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == "nrc-infer":
+        return run_nrc_infer(args)
     if args.config == "batch":
         return run_batch(args)
     if args.config == "stress-batch":

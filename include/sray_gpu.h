@@ -453,12 +453,17 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
  *  - pool_spin_limit > 0: polls of a slot before the persistent shading
  *    pool (sray_tuning.render_tail) gives up waiting for work (default
  *    about half a second); a frame whose wait runs out returns
- *    SRAY_EDEVICE. */
+ *    SRAY_EDEVICE.
+ *  - photon_group > 0: a batch's photon maps are traced in wavefronts of
+ *    at most about that many photons (whole jobs; default 2^26), each
+ *    group's maps copied out of the wavefront's buffers before the next;
+ *    the images do not change. */
 typedef struct sray_faults {
 	int fail_alloc_after;
 	int queue_cap;
 	int pool_spin_limit;
-	int reserved[5];
+	int photon_group;
+	int reserved[4];
 } sray_faults;
 
 int sray_gpu_set_faults(const sray_faults *f);

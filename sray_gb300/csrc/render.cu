@@ -1450,6 +1450,9 @@ __global__ void k_primary_hits(DScene S, RayQueue q, const int4 *hits, int *obj,
 /* ================================================================ */
 /* host side                                                          */
 /* ================================================================ */
+/* photons of one wavefront of a batch's photon maps (jobs beyond it go to the next) */
+#define PW_MAX_PHOTONS ((int64_t)1 << 26)
+
 /* at most this many gather requests wait for the photon maps across waves */
 #define DEFER_MAX_REQS ((int64_t)1 << 28)
 
@@ -2157,49 +2160,82 @@ int Renderer::photon_job(DScene base)
 		J.bits = &jbits[j];
 		J.cov = &jcov[j];
 	}
-	std::vector<PJobOut> out;
-	int r = photon_trace_jobs(*this, base, spec, out, ps);
-	if(r) return r;
-	/* the maps of all jobs together: grids over the jobs' own boxes with
-	 * their own range radii (the batch's tree spans every job's interval) */
+	/* the grids of the jobs' own frames: boxes and range radii over their
+	 * own intervals (the batch's tree spans every job's interval) */
 	std::vector<Box> boxes(n);
 	std::vector<double> gdist(n);
 	for(size_t j = 0; j < n; j++) {
 		boxes[j] = sc.box_at(batch_t0[j], batch_t1[j], o0[j], no[j]);
 		gdist[j] = sc.gather_dist_at(batch_t0[j], batch_t1[j], opt, o0[j], no[j]);
 	}
-	r = photon_finalize_jobs(*this, out, boxes, gdist, hm, ps);
-	if(r == 0) {
-		caust.map.n = 0;
-		gi.map.n = 0;
-		CK(dmaps.upload(hm, ps), "job photon maps");
-		CK(cudaStreamSynchronize(ps), "job photon maps");
-		h2d += (int64_t)(hm.size() * sizeof(DPhotonMap));
-		return 0;
-	}
-	if(r != 1) return r;
-	/* cell tables too large to hold together: map by map */
-	hm.assign(2 * n, DPhotonMap());
-	const DevPhoton *ph = pw_out.as<DevPhoton>();
-	const int *valid = pw_valid.as<int>();
+	/* jobs in groups of at most PW_MAX_PHOTONS photons per wavefront, so that
+	 * the wavefront's memory follows the group and not the batch; when the
+	 * batch takes more than one group, each map is copied out to its job's
+	 * own buffers before the next group reuses the wavefront's */
+	const int64_t gcap = g_faults.photon_group.load() > 0 ? (int64_t)g_faults.photon_group.load() : PW_MAX_PHOTONS;
+	std::vector<size_t> group0(1, 0);
+	int64_t acc = 0;
 	for(size_t j = 0; j < n; j++) {
-		/* the radius and grid box Scene::build_tree gives the job's own
-		 * frame: the batch's tree spans every job's interval */
-		map_gather_dist = gdist[j];
-		map_box = boxes[j];
-		map_has_box = true;
-		std::swap(caust, job_maps[j].caust);
-		std::swap(gi, job_maps[j].gi);
-		int b = out[j].base, t0 = out[j].total[0];
-		r = photon_finalize(*this, 0, valid + b, ph + b, t0, ps, &c);
-		if(!r) r = photon_finalize(*this, 1, valid + b + t0, ph + b + t0, out[j].total[1], ps, &g);
-		std::swap(caust, job_maps[j].caust);
-		std::swap(gi, job_maps[j].gi);
-		map_gather_dist = -1.0;
-		map_has_box = false;
+		int64_t pj = (int64_t)spec[j].num[0] + spec[j].num[1] + 2 * spec[j].nlights;
+		if(j > group0.back() && acc + pj > gcap) {
+			group0.push_back(j);
+			acc = 0;
+		}
+		acc += pj;
+	}
+	group0.push_back(n);
+	bool copy_out = group0.size() > 2;
+	for(size_t gi0 = 0; gi0 + 1 < group0.size(); gi0++) {
+		size_t a = group0[gi0], b = group0[gi0 + 1];
+		std::vector<PhotonJobSpec> gspec(spec.begin() + a, spec.begin() + b);
+		std::vector<Box> gbox(boxes.begin() + a, boxes.begin() + b);
+		std::vector<double> gd(gdist.begin() + a, gdist.begin() + b);
+		std::vector<PJobOut> out;
+		int r = photon_trace_jobs(*this, base, gspec, out, ps);
 		if(r) return r;
-		hm[2 * j] = job_maps[j].caust.map;
-		hm[2 * j + 1] = job_maps[j].gi.map;
+		std::vector<DPhotonMap> gm;
+		r = photon_finalize_jobs(*this, out, gbox, gd, gm, ps);
+		if(r == 0) {
+			for(size_t k = 0; k < gm.size(); k++) {
+				DPhotonMap &M = gm[k];
+				if(copy_out && M.n > 0) {
+					/* out of the wavefront's buffers into the job's own */
+					PhotonBufs &P = (k & 1) ? job_maps[a + k / 2].gi : job_maps[a + k / 2].caust;
+					size_t ncells = (size_t)M.dims[0] * M.dims[1] * M.dims[2];
+					CK(P.ph.ensure((size_t)M.n * sizeof(DevPhoton)), "job photon map");
+					CK(P.cells.ensure(ncells * sizeof(uint2)), "job cell table");
+					CK(cudaMemcpyAsync(P.ph.p, M.ph, (size_t)M.n * sizeof(DevPhoton), cudaMemcpyDeviceToDevice, ps), "job photon map");
+					CK(cudaMemcpyAsync(P.cells.p, M.cells, ncells * sizeof(uint2), cudaMemcpyDeviceToDevice, ps), "job cell table");
+					M.ph = P.ph.as<DevPhoton>();
+					M.cells = P.cells.as<uint2>();
+				}
+				hm[2 * a + k] = M;
+			}
+			continue;
+		}
+		if(r != 1) return r;
+		/* cell tables too large to hold together: map by map, into the
+		 * jobs' own buffers */
+		const DevPhoton *ph = pw_out.as<DevPhoton>();
+		const int *valid = pw_valid.as<int>();
+		for(size_t j = a; j < b; j++) {
+			map_gather_dist = gdist[j];
+			map_box = boxes[j];
+			map_has_box = true;
+			std::swap(caust, job_maps[j].caust);
+			std::swap(gi, job_maps[j].gi);
+			const PJobOut &o = out[j - a];
+			int t0 = o.total[0];
+			r = photon_finalize(*this, 0, valid + o.base, ph + o.base, t0, ps, &c);
+			if(!r) r = photon_finalize(*this, 1, valid + o.base + t0, ph + o.base + t0, o.total[1], ps, &g);
+			std::swap(caust, job_maps[j].caust);
+			std::swap(gi, job_maps[j].gi);
+			map_gather_dist = -1.0;
+			map_has_box = false;
+			if(r) return r;
+			hm[2 * j] = job_maps[j].caust.map;
+			hm[2 * j + 1] = job_maps[j].gi.map;
+		}
 	}
 	caust.map.n = 0;
 	gi.map.n = 0;
@@ -3930,10 +3966,14 @@ int sray_gpu_kernel_times(char *names, size_t names_cap, double *ms, int64_t *la
 int sray_gpu_set_faults(const sray_faults *f)
 {
 	if(!f) { g_err = "null fault settings"; return SRAY_EINVAL; }
-	if(f->fail_alloc_after < -1 || f->queue_cap < 0 || f->pool_spin_limit < 0) { g_err = "bad fault settings"; return SRAY_EINVAL; }
+	if(f->fail_alloc_after < -1 || f->queue_cap < 0 || f->pool_spin_limit < 0 || f->photon_group < 0) {
+		g_err = "bad fault settings";
+		return SRAY_EINVAL;
+	}
 	g_faults.alloc_left.store(f->fail_alloc_after);
 	g_faults.queue_cap.store(f->queue_cap);
 	g_faults.spin_limit.store(f->pool_spin_limit);
+	g_faults.photon_group.store(f->photon_group);
 	return 0;
 }
 

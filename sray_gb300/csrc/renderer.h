@@ -23,6 +23,7 @@ struct FaultState {
 	std::atomic<int> alloc_left{-1};
 	std::atomic<int> queue_cap{0};
 	std::atomic<int> spin_limit{0};
+	std::atomic<int> photon_group{0};
 };
 extern FaultState g_faults;
 

@@ -58,7 +58,7 @@ class SrayJob(ctypes.Structure):
 
 class SrayFaults(ctypes.Structure):
     _fields_ = [("fail_alloc_after", ctypes.c_int), ("queue_cap", ctypes.c_int), ("pool_spin_limit", ctypes.c_int),
-                ("reserved", ctypes.c_int * 5)]
+                ("photon_group", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
 
 
 class SrayTuning(ctypes.Structure):
@@ -381,10 +381,10 @@ class GpuRenderer:
         """Re-initialise the network and forget the regions' validation history."""
         self._chk(self.L.sray_gpu_nrc_reset(self.opts.seed if seed is None else seed))
 
-    def set_faults(self, fail_alloc_after=-1, queue_cap=0, pool_spin_limit=0):
+    def set_faults(self, fail_alloc_after=-1, queue_cap=0, pool_spin_limit=0, photon_group=0):
         """Host-side fault injection for tests (sray_gpu_set_faults); the
         defaults turn it off."""
-        f = SrayFaults(fail_alloc_after, queue_cap, pool_spin_limit)
+        f = SrayFaults(fail_alloc_after, queue_cap, pool_spin_limit, photon_group)
         self._chk(self.L.sray_gpu_set_faults(ctypes.byref(f)))
 
     def tuning(self):

@@ -547,3 +547,28 @@ def test_scene_set_batch_matches_oracle(gpu_lib, oracle_lib, tuning):
         img_o = o.render(ms)
         assert _compare(fb.cpu().numpy(), img_o, "scene %d job %dx%d at %d ms (pixel base %d)" % (k, w, h, ms, base)) <= 1e-3
         base += w * h
+
+
+def test_batch_photon_groups_keep_images(gpu_lib):
+    # a batch's photon maps traced in groups of jobs (each group its own
+    # wavefront, its maps copied out before the next) give the images of
+    # the batch traced as one wavefront
+    opts = dict(width=96, height=72, min_samples=1, max_samples=3, max_var=0.01, caust_photons=10000, gi_photons=20000,
+                iter=5, shadow_samples=2, diffuse_samples=1, mblur=1, shutter=40, gather_dist=0.02)
+    paths = [scenegen.write_scene("small"), scenegen.write_scene("feature")]
+    jobs = [(0, 96, 72, 0, {}), (40, 64, 48, 1, dict(caust_photons=5000, gi_photons=30000)), (100, 96, 72, 1, {}),
+            (0, 48, 36, 0, dict(caust_photons=20000))]
+    imgs = []
+    for group in (0, 40000):
+        g = gpu_lib.GpuRenderer(**opts)
+        g.load_scene_set(paths)
+        g.set_faults(photon_group=group)
+        fbs = [torch.zeros((h, w, 4), dtype=torch.float32, device="cuda") for _, w, h, _, _ in jobs]
+        g.render_batch([(ms, fb, dict(extra, scene=k)) for (ms, _, _, k, extra), fb in zip(jobs, fbs)])
+        g.set_faults()
+        imgs.append([fb.cpu().numpy() for fb in fbs])
+        g.close()
+    for a, b in zip(*imgs):
+        rel = np.abs(a - b) / np.maximum(np.abs(a), 1e-3)
+        print("photon groups: max rel difference %.3g" % rel.max())
+        assert rel.max() <= 1e-5
