@@ -420,6 +420,10 @@ typedef struct sray_tuning {
 	                             the remaining bounces; 2: the same, the render loop
 	                             waiting for the maps at the second bounce (a check of
 	                             that path independent of timing) (0) */
+	int sort_rays;            /* secondary closest-hit passes of at least this many rays are
+	                             first sorted by direction octant and origin cell, so that a
+	                             warp's rays start close together and head the same way
+	                             (0: never) (0) */
 } sray_tuning;
 
 typedef struct sray_tune_trial {

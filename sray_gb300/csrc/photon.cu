@@ -1017,19 +1017,40 @@ __global__ void k_cells_seg(const unsigned *lin, int n, const unsigned *offs, in
 	}
 }
 
-/* exclusive scan of m entries; the total into *total when given */
-static int scan_long(Renderer &R, unsigned *data, int m, unsigned *total, cudaStream_t s)
+/* exclusive scan of m entries (scratch `part` for the parts' totals); the
+ * total into *total when given */
+static int scan_long(Renderer &R, unsigned *data, int m, unsigned *total, DevBuf &part, const char *name, cudaStream_t s)
 {
 	if(m <= 65536) {
-		LAUNCH(R, "photon_sort", s, k_scan_excl<<<1, 1024, 0, s>>>(data, m, total));
+		LAUNCH(R, name, s, k_scan_excl<<<1, 1024, 0, s>>>(data, m, total));
 		return 0;
 	}
 	int parts = (m + SCAN_PART - 1) / SCAN_PART;
-	PCK(R.pw_part.ensure((size_t)(parts + 4) * sizeof(unsigned)), "scan parts");
-	unsigned *sums = R.pw_part.as<unsigned>();
-	LAUNCH(R, "photon_sort", s, k_scan_part<<<parts, 1024, 0, s>>>(data, m, sums));
-	LAUNCH(R, "photon_sort", s, k_scan_excl<<<1, 1024, 0, s>>>(sums, parts, total));
-	LAUNCH(R, "photon_sort", s, k_scan_add<<<parts, 256, 0, s>>>(data, m, sums));
+	PCK(part.ensure((size_t)(parts + 4) * sizeof(unsigned)), "scan parts");
+	unsigned *sums = part.as<unsigned>();
+	LAUNCH(R, name, s, k_scan_part<<<parts, 1024, 0, s>>>(data, m, sums));
+	LAUNCH(R, name, s, k_scan_excl<<<1, 1024, 0, s>>>(sums, parts, total));
+	LAUNCH(R, name, s, k_scan_add<<<parts, 256, 0, s>>>(data, m, sums));
+	return 0;
+}
+
+/* stable LSD radix sort of n (key, value) pairs over the low `bits` bits of
+ * the keys, ping-ponging with keys2 / vals2; *vals_out is the buffer that
+ * holds the sorted values (scratch: hist, part) */
+int sort_pairs(Renderer &R, unsigned *keys, unsigned *vals, unsigned *keys2, unsigned *vals2, int n, int bits, DevBuf &hist,
+		DevBuf &part, const char *name, cudaStream_t s, unsigned **vals_out)
+{
+	int nbr = (n + TILE - 1) / TILE;
+	PCK(hist.ensure((size_t)256 * nbr * sizeof(unsigned) + 16), "radix histogram");
+	unsigned *h = hist.as<unsigned>();
+	for(int shift = 0; shift < bits; shift += 8) {
+		LAUNCH(R, name, s, k_rs_hist<<<nbr, RS_THREADS, 0, s>>>(keys, n, shift, h, nbr));
+		if(scan_long(R, h, 256 * nbr, nullptr, part, name, s)) return SRAY_ECUDA;
+		LAUNCH(R, name, s, k_rs_scatter<<<nbr, RS_THREADS, 0, s>>>(keys, vals, n, shift, h, nbr, keys2, vals2));
+		std::swap(keys, keys2);
+		std::swap(vals, vals2);
+	}
+	*vals_out = vals;
 	return 0;
 }
 
@@ -1063,7 +1084,7 @@ int photon_finalize_jobs(Renderer &R, const std::vector<PJobOut> &jobs, const st
 	PCK(R.pw_tiles.ensure((size_t)(nb + 4) * sizeof(unsigned)), "scan");
 	unsigned *bc = R.pw_tiles.as<unsigned>();
 	LAUNCH(R, "photon_compact", s, k_count_valid<<<nb, 256, 0, s>>>(valid, total, bc));
-	if(scan_long(R, bc, nb, bc + nb, s)) return SRAY_ECUDA;
+	if(scan_long(R, bc, nb, bc + nb, R.pw_part, "photon_compact", s)) return SRAY_ECUDA;
 	std::vector<int> bounds(nseg + 1);
 	for(int j = 0; j < nj; j++) {
 		bounds[2 * j] = jobs[j].base;
@@ -1115,7 +1136,7 @@ int photon_finalize_jobs(Renderer &R, const std::vector<PJobOut> &jobs, const st
 			LAUNCH(R, "photon_sort", s, k_seg_keys<<<grid_n(n, 256), 256, 0, s>>>(vals, n, offs, nseg, keys));
 		int shift = (ps < key_passes ? ps : ps - key_passes) * 8;
 		LAUNCH(R, "photon_sort", s, k_rs_hist<<<nbr, RS_THREADS, 0, s>>>(keys, n, shift, hist, nbr));
-		if(scan_long(R, hist, 256 * nbr, nullptr, s)) return SRAY_ECUDA;
+		if(scan_long(R, hist, 256 * nbr, nullptr, R.pw_part, "photon_sort", s)) return SRAY_ECUDA;
 		LAUNCH(R, "photon_sort", s, k_rs_scatter<<<nbr, RS_THREADS, 0, s>>>(keys, vals, n, shift, hist, nbr, keys2, vals2));
 		std::swap(keys, keys2);
 		std::swap(vals, vals2);

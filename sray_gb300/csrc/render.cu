@@ -95,6 +95,46 @@ __global__ void k_camera(DScene S, const int *active, int a0, int na, int s0, in
 	}
 }
 
+/* ---------------------------------------------------------------- */
+/* sorting a pass before it is traced: key = direction octant over the
+ * Morton code of the origin's cell in a 128^3 grid over the scene box */
+__device__ __forceinline__ unsigned spread7(unsigned v)
+{
+	v &= 0x7f;
+	v = (v | (v << 8)) & 0x0000F00Fu;
+	v = (v | (v << 4)) & 0x000C30C3u;
+	v = (v | (v << 2)) & 0x00249249u;
+	return v;
+}
+
+__global__ void k_ray_keys(RayQueue q, int n, float lx, float ly, float lz, float sx, float sy, float sz, unsigned *keys, unsigned *vals)
+{
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		float4 o = q.o[i], d = q.d[i];
+		int cx = (int)((o.x - lx) * sx), cy = (int)((o.y - ly) * sy), cz = (int)((o.z - lz) * sz);
+		cx = cx < 0 ? 0 : (cx > 127 ? 127 : cx);
+		cy = cy < 0 ? 0 : (cy > 127 ? 127 : cy);
+		cz = cz < 0 ? 0 : (cz > 127 ? 127 : cz);
+		unsigned oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+		keys[i] = (oct << 21) | spread7((unsigned)cx) | (spread7((unsigned)cy) << 1) | (spread7((unsigned)cz) << 2);
+		vals[i] = (unsigned)i;
+	}
+}
+
+/* the pass's entries in sorted order */
+__global__ void k_ray_permute(RayQueue in, const unsigned *vals, int n, RayQueue out)
+{
+	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		unsigned v = vals[i];
+		out.o[i] = in.o[v];
+		out.d[i] = in.d[v];
+		out.w[i] = in.w[v];
+		out.meta[i] = in.meta[v];
+		out.stk[i] = in.stk[v];
+		out.ext[i] = in.ext[v];
+	}
+}
+
 /* Closest hits.  HYB = true traces through the mesh hierarchies and lists
  * the rays whose result the octree must decide in fb (count in fb[0], ray
  * indices from fb + 1); HYB = false traces the listed rays with the octree
@@ -2323,6 +2363,35 @@ int Renderer::ensure_pqueue(int which, int cap)
 	return queue_alloc(pqbuf[which], pq[which], pqcap[which], cap);
 }
 
+/* the n rays of q[cur], sorted by direction octant and origin cell into the
+ * spare queue, which then becomes q[cur] (the pass's queue and its
+ * allocation swapped with the spare's) */
+int Renderer::sort_pass(int cur, int n, cudaStream_t s)
+{
+	if(n < 2 || sc.oct.nodes.empty()) return 0;
+	if(int r = queue_alloc(qsbuf, qs, qscap, q[cur].cap)) return r;
+	CK(rs_keys.ensure((size_t)n * 16), "ray sort keys");
+	unsigned *keys = rs_keys.as<unsigned>(), *vals = keys + n, *keys2 = keys + 2 * (size_t)n, *vals2 = keys + 3 * (size_t)n;
+	const Box &b = sc.oct.nodes[0].box;
+	float ext[3], lo[3];
+	for(int a = 0; a < 3; a++) {
+		lo[a] = (float)b.mn[a];
+		double e = b.mx[a] - b.mn[a];
+		ext[a] = e > 0.0 ? (float)(128.0 / e) : 0.0f;
+	}
+	LAUNCH(*this, "ray_sort", s, k_ray_keys<<<grid_for(n, 256), 256, 0, s>>>(q[cur], n, lo[0], lo[1], lo[2], ext[0], ext[1], ext[2],
+			keys, vals));
+	unsigned *sorted = nullptr;
+	if(int r = sort_pairs(*this, keys, vals, keys2, vals2, n, 24, rs_hist, rs_part, "ray_sort", s, &sorted)) return r;
+	LAUNCH(*this, "ray_sort", s, k_ray_permute<<<grid_for(n, 256), 256, 0, s>>>(q[cur], sorted, n, qs));
+	int *count = q[cur].count;
+	std::swap(q[cur], qs);
+	std::swap(qbuf[cur], qsbuf);
+	std::swap(qcap[cur], qscap);
+	q[cur].count = count;
+	return 0;
+}
+
 /* ---------------------------------------------------------------- */
 /* radiance cache: records, validation and training (host driver below) */
 
@@ -2861,6 +2930,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			CK(cudaMemsetAsync(q[cur ^ 1].count, 0, sizeof(int), s), "reset queue");
 			CK(cudaMemsetAsync(cnt + 5, 0, sizeof(int), s), "reset shadow queue");
 			CK(sq.ensure((size_t)n_rays * shadow_per_ray * sizeof(ShadowReq)), "shadow queue");
+			if(depth >= 1 && tune.sort_rays > 0 && n_rays >= tune.sort_rays && (r = sort_pass(cur, n_rays, s))) return r;
 			r = trace_rays(q[cur], n_rays, "trace", (prof_flags & 2) != 0, s);
 			if(r) return r;
 			ShadeOut so;
@@ -3480,6 +3550,7 @@ static int check_tuning(const sray_tuning *t)
 	if(t->warp_rays < 0 || t->warp_rays > (1 << 24)) { g_err = "warp_rays must be 0..2^24"; return SRAY_EINVAL; }
 	if(t->warp_segments < 0 || t->warp_segments > (1 << 24)) { g_err = "warp_segments must be 0..2^24"; return SRAY_EINVAL; }
 	if(t->side_gather < 0 || t->side_gather > 2) { g_err = "side_gather must be 0, 1 or 2"; return SRAY_EINVAL; }
+	if(t->sort_rays < 0) { g_err = "sort_rays must be >= 0"; return SRAY_EINVAL; }
 	if(t->queue_depth != 0 && (t->queue_depth < 1024 || t->queue_depth > (1 << 27))) {
 		g_err = "queue_depth must be 0 or 1024..2^27";
 		return SRAY_EINVAL;
@@ -4009,7 +4080,7 @@ void sray_gpu_shutdown(void)
 		&R.fbl, &R.tnodes, &R.ohome, &R.pool_ready, &R.pqbuf[0], &R.pqbuf[1], &R.phits, &R.pfbl, &R.pcounts, &R.pctr,
 		&R.pw_jobs, &R.pw_prefix, &R.pw_scale, &R.pw_bits, &R.pw_cov, &R.pw_pix, &R.pw_out, &R.pw_valid,
 		&R.pw_part, &R.pw_tiles, &R.pw_bounds, &R.pw_offs, &R.pw_ph, &R.pw_sorted, &R.pw_grids, &R.pw_morton, &R.pw_cellbase,
-		&R.pw_keys, &R.pw_lin, &R.pw_cells, &R.pw_hist,
+		&R.pw_keys, &R.pw_lin, &R.pw_cells, &R.pw_hist, &R.qsbuf, &R.rs_keys, &R.rs_hist, &R.rs_part,
 		&R.nrc_qx, &R.nrc_qw, &R.nrc_rx, &R.nrc_rt, &R.nrc_ry, &R.nrc_regions};
 	if(R.ps) cudaStreamSynchronize(R.ps);
 	for(DevBuf *b : bufs) b->release();

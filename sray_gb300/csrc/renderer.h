@@ -147,6 +147,12 @@ struct Renderer {
 	DevBuf qbuf[2], hits, gq, sq, acc, hist, sums, active[2], spp, fbdev, ctr, counts, fbl, pool_ready;
 	RayQueue q[2];
 	int qcap[2] = {0, 0};
+	/* a pass sorted before it is traced (sray_tuning.sort_rays): the sorted
+	 * copy's queue (swapped with the pass's), keys and values, scratch */
+	DevBuf qsbuf, rs_keys, rs_hist, rs_part;
+	RayQueue qs = {};
+	int qscap = 0;
+	int sort_pass(int cur, int n, cudaStream_t s);
 	/* photon tracing has buffers and a stream of its own, so that it can run
 	 * beside the first bounce of a frame */
 	DevBuf pqbuf[2], phits, pfbl, pcounts, pctr;
@@ -306,6 +312,8 @@ struct PJobOut { int base = 0; int total[2] = {0, 0}; };   /* a job's photons: f
 int photon_trace_jobs(Renderer &R, const DScene &base, const std::vector<PhotonJobSpec> &spec, std::vector<PJobOut> &out,
 		cudaStream_t s);
 int photon_finalize(Renderer &R, int global, const int *valid, const DevPhoton *in, int total, cudaStream_t s, int *stored);
+int sort_pairs(Renderer &R, unsigned *keys, unsigned *vals, unsigned *keys2, unsigned *vals2, int n, int bits, DevBuf &hist,
+		DevBuf &part, const char *name, cudaStream_t s, unsigned **vals_out);
 int photon_finalize_jobs(Renderer &R, const std::vector<PJobOut> &jobs, const std::vector<Box> &boxes,
 		const std::vector<double> &gather_dist, std::vector<DPhotonMap> &maps, cudaStream_t s);
 int photon_shoot_maps(Renderer &R, const DScene &base, const std::vector<uint32_t> &bits, const std::vector<float> &cov,

@@ -100,7 +100,8 @@ def test_image_small_scene(small_pair):
 @pytest.mark.parametrize("tuning", [dict(shadow_order=1), dict(stream_priority=1), dict(stream_priority=2),
                                     dict(warp_rays=1 << 24, warp_segments=1 << 24), dict(warp_rays=0, warp_segments=0),
                                     dict(side_gather=1), dict(side_gather=2), dict(queue_depth=4096),
-                                    dict(queue_depth=1024, warp_rays=1 << 24, warp_segments=1 << 24)])
+                                    dict(queue_depth=1024, warp_rays=1 << 24, warp_segments=1 << 24),
+                                    dict(sort_rays=1), dict(sort_rays=1, queue_depth=4096, warp_rays=0)])
 def test_tuning_keeps_the_image(small_pair, tuning):
     # light samples' any-hit traversal in node order instead of nearest
     # first; the photon stream or the frame's own stream given priority;
