@@ -494,6 +494,15 @@ def nrc_vs_plain(args, reference):
             tf = st["cached"] * 2 * 26304 / (q_ms / 1e3) / 1e12
             res["query_roofline"] = {"bound": "tensor", "achieved": tf, "peak": bf16_peak(), "unit": "TFLOP/s",
                                      "frac": tf / bf16_peak(), "queries_per_frame": st["cached"], "ms_per_frame": q_ms}
+        # and of the frame's training steps: forward, backward and weight
+        # gradients, about 3 x 2 x 26,304 FLOP per training sample
+        t_ms = kt.get("nrc_train", (0.0, 0))[0] / steps
+        if t_ms > 0 and st["train_samples"] > 0:
+            tf = st["train_samples"] * 3 * 2 * 26304 / (t_ms / 1e3) / 1e12
+            res["train_roofline"] = {"bound": "tensor", "achieved": tf, "peak": bf16_peak(), "unit": "TFLOP/s",
+                                     "frac": tf / bf16_peak(), "samples_per_frame": st["train_samples"], "ms_per_frame": t_ms,
+                                     "kernels": "warp-level mma.sync forward, backward and weight-gradient kernels and Adam, "
+                                                "one CUDA graph per frame"}
         if res["rmse"] is not None:
             pts = [(p["diffuse_samples"], p["ms_per_frame"], p["rmse"]) for p in ladder]
             pms, pds, ok = equal_rmse_time(pts, res["rmse"])
