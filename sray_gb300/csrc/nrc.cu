@@ -363,13 +363,15 @@ __global__ void __launch_bounds__(NRC_FWD_THREADS) k_nrc_forward(NrcDev net, int
  * threads per sample (row): its threads write the tile's encoded inputs
  * (half of a row's features each) into shared memory, one elected thread
  * issues the layer's MMAs (M = 128, N = 64, K = 16 each; 14 for the
- * 224-wide first layer, 4 for the others, N = 16 for the output layer) and
- * commits them to the group's mbarrier, and the threads read their rows of
- * the accumulator back from TMEM (tcgen05.ld, 32x32b: warp w its lanes
- * 32 (w mod 4) on; the two warps of a lane quarter take 32 columns each) for
- * the bias, ReLU and BF16 rounding that make the next layer's operand.  The two groups of a CTA
- * interleave, so one group's encoding and epilogues overlap the other's
- * MMAs.  The weights (BF16, 54 KB) are copied once per CTA into the
+ * 224-wide first layer, 5 for the 80-wide others, N = 16 for the output
+ * layer) and commits them to the group's mbarrier, and the threads read
+ * their rows of the accumulator back from TMEM (tcgen05.ld, 32x32b: warp w
+ * its lanes 32 (w mod 4) on; the two warps of a lane quarter take 32
+ * columns each) for the ReLU and BF16 rounding that make the next layer's
+ * operand; the biases come with the products (a BF16 pair per row of each
+ * weight tile against a constant pair in the operand).  The two groups of a
+ * CTA interleave, so one group's encoding and epilogues overlap the other's
+ * MMAs.  The weights (BF16, 62 KB) are copied once per CTA into the
  * canonical K-major layout without swizzle: 8-row x 16-byte core matrices,
  * the two of a K = 16 step 128 bytes apart (leading byte offset), 8-row
  * groups K/8 x 128 bytes apart (stride byte offset).  Every wait on an
