@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--batch-frames", type=int, default=16, help="frames per batch of the stress-batch configuration")
     ap.add_argument("--batch-jobs", type=int, default=64, help="jobs of the batch configuration")
     ap.add_argument("--batch-scenes", type=int, default=16, help="scenes of the batch configuration's scene set")
+    ap.add_argument("--queue-depth", type=int, default=1 << 20,
+                    help="primary rays per wave of the batch configuration before (or without) autotuning")
     ap.add_argument("--no-nrc", action="store_true", help="skip the radiance-cache comparison")
     ap.add_argument("--method", default="plain", choices=["plain", "cache", "cache-everywhere"],
                     help="final gather of the headline frames: the plain gather, the radiance cache with its "
@@ -578,7 +580,7 @@ def run_batch(args):
         return rays_of(g.stats())
 
 
-    g.set_tuning(queue_depth=1 << 20)      # bounded queues from the first batch on
+    g.set_tuning(queue_depth=args.queue_depth)      # bounded queues from the first batch on
     batch()
     tuning = None
     if not args.no_autotune:

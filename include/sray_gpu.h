@@ -476,7 +476,8 @@ int sray_gpu_set_faults(const sray_faults *f);
 int sray_gpu_last_error(char *buf, size_t cap);
 
 /* The autotuner for batches (sray_gpu_render_batch): the queue depth
- * (65,536, 262,144 or 1,048,576 primary rays per wave) against the
+ * (65,536, 262,144, 1,048,576, 4,194,304 or 16,777,216 primary rays per
+ * wave; device memory grows with it) against the
  * traversal mode (thread per ray; one warp per ray in passes of at most
  * 16,384 rays or segments; one warp per ray in every pass), then the best
  * pair with the shading tree's tail in the persistent pool launch (below

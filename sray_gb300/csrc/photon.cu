@@ -731,8 +731,9 @@ int photon_trace_jobs(Renderer &R, const DScene &base, const std::vector<PhotonJ
 			PCK(cudaMemsetAsync(cnt + 2, 0, sizeof(int), s), "reset photon tail counter");
 			LAUNCH(R, "photon_finish", s, k_photon_finish<<<grid_n(n_live, 128), 128, 0, s>>>(PS, PSet, R.pq[cur], cnt + 2,
 					R.pq[cur ^ 1], pctr));
-			PCK(cudaMemcpyAsync(&n_live, R.pq[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "photon queue count");
+			PCK(cudaMemcpyAsync(R.pin + 8, R.pq[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "photon queue count");
 			PCK(cudaStreamSynchronize(s), "photon tail");
+			n_live = R.pin[8];
 			R.d2h += sizeof(int);
 			R.prof_collect();
 			cur ^= 1;
@@ -741,8 +742,9 @@ int photon_trace_jobs(Renderer &R, const DScene &base, const std::vector<PhotonJ
 		if(launch_trace(R, PS, R.pq[cur], n_live, "photon_trace", s)) return SRAY_ECUDA;
 		LAUNCH(R, "photon_bounce", s, k_photon_bounce<<<grid_n(n_live, 128), 128, 0, s>>>(PS, PSet, R.pq[cur], R.phits.as<int4>(),
 				R.pq[cur ^ 1]));
-		PCK(cudaMemcpyAsync(&n_live, R.pq[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "photon queue count");
+		PCK(cudaMemcpyAsync(R.pin + 8, R.pq[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "photon queue count");
 		PCK(cudaStreamSynchronize(s), "photon pass");
+		n_live = R.pin[8];
 		R.d2h += sizeof(int);
 		R.prof_collect();
 		cur ^= 1;

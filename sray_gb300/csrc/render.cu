@@ -2899,10 +2899,10 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 				if(int r = shadow_rays(so.sq_cap, s)) return r;
 				LAUNCH(*this, "gather", s, k_gather<<<grid_for(so.gq_cap, GATHER_WARPS), GATHER_WARPS * 32, 0, s>>>(S,
 						gq.as<GatherReq>(), cnt + 2, acc.as<float4>(), ctr.as<DevCounters>()));
-				int h_cnt = 0, h_err = 0;
-				CK(cudaMemcpyAsync(&h_cnt, q[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "read queue count");
-				CK(cudaMemcpyAsync(&h_err, ctl + 3, sizeof(int), cudaMemcpyDeviceToHost, s), "read pool error");
+				CK(cudaMemcpyAsync(pin, q[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "read queue count");
+				CK(cudaMemcpyAsync(pin + 1, ctl + 3, sizeof(int), cudaMemcpyDeviceToHost, s), "read pool error");
 				CK(cudaStreamSynchronize(s), "shading tail");
+				int h_cnt = pin[0], h_err = pin[1];
 				d2h += 2 * sizeof(int);
 				prof_collect();
 				if(h_err) return fail(SRAY_EDEVICE, "shading pool: a wait for work ran out");
@@ -2951,11 +2951,11 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 				LAUNCH(*this, "gather", s, k_gather<<<grid_for(n_rays, GATHER_WARPS), GATHER_WARPS * 32, 0, s>>>(S, gq.as<GatherReq>(),
 						cnt + 2, acc.as<float4>(), ctr.as<DevCounters>()));
 			stats.secondary_rays += depth ? n_rays : 0;
-			int h_cnt = 0;
-			CK(cudaMemcpyAsync(&h_cnt, q[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "read queue count");
+			CK(cudaMemcpyAsync(pin, q[cur ^ 1].count, sizeof(int), cudaMemcpyDeviceToHost, s), "read queue count");
 			double tw = host_now_ms();
 			CK(cudaStreamSynchronize(s), "bounce");
 			host_time("host.bounce_wait", tw);
+			int h_cnt = pin[0];
 			d2h += sizeof(int);
 			prof_collect();
 			/* children beyond the queue were dropped (the count kept going):
@@ -2982,12 +2982,11 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 				hist.as<float4>(), sums.as<float4>(), maxs, opt.min_samples, opt.max_var, next_list, next_count, fbd,
 				spp.as<int>()));
 		stats.samples += (int64_t)n_active * width;
-		int h_next = 0;
-		CK(cudaMemcpyAsync(&h_next, next_count, sizeof(int), cudaMemcpyDeviceToHost, s), "read active count");
+		CK(cudaMemcpyAsync(pin + 2, next_count, sizeof(int), cudaMemcpyDeviceToHost, s), "read active count");
 		CK(cudaStreamSynchronize(s), "sample pass");
 		d2h += sizeof(int);
 		prof_collect();
-		n_active = h_next;
+		n_active = pin[2];
 	}
 	if(photons_pending) {
 		/* no sample batch ran: the maps are still the frame's */
@@ -3315,7 +3314,11 @@ int sray_gpu_init(const sray_opts *opt)
 	std::lock_guard<std::mutex> lk(g_mu);
 	int r = check_opts(opt);
 	if(r) return r;
-	if(g_R) { delete g_R; g_R = nullptr; }
+	if(g_R) {
+		if(g_R->pin) cudaFreeHost(g_R->pin);
+		delete g_R;
+		g_R = nullptr;
+	}
 	int dev = 0;
 	cudaError_t e = cudaGetDevice(&dev);
 	if(e != cudaSuccess) { g_err = std::string("no CUDA device: ") + cudaGetErrorString(e); return SRAY_ECUDA; }
@@ -3324,6 +3327,14 @@ int sray_gpu_init(const sray_opts *opt)
 	g_R->device = dev;
 	if(cudaDeviceGetAttribute(&g_R->nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || g_R->nsm <= 0) g_R->nsm = 152;
 	memset(&g_R->stats, 0, sizeof g_R->stats);
+	e = cudaMallocHost(&g_R->pin, 16 * sizeof(int));
+	if(e != cudaSuccess) {
+		g_R->pin = nullptr;
+		delete g_R;
+		g_R = nullptr;
+		g_err = std::string("pinned host words: ") + cudaGetErrorString(e);
+		return SRAY_ECUDA;
+	}
 	return 0;
 }
 
@@ -3661,7 +3672,10 @@ int sray_gpu_autotune_batch(const sray_job *jobs, int n, int frames, void *strea
 	if(!R.loaded) { g_err = "no scene loaded"; return SRAY_ESTATE; }
 	if(!jobs || n < 1 || frames < 1) { g_err = "bad arguments"; return SRAY_EINVAL; }
 	cudaStream_t s = as_stream(stream);
-	static const int depths[] = {1 << 16, 1 << 18, 1 << 20};
+	/* the configuration's sweep (64k, 256k, 1M primary rays per wave), then
+	 * deeper waves for batches whose memory allows them */
+	static const int depths[] = {1 << 16, 1 << 18, 1 << 20, 1 << 22, 1 << 24};
+	const int nd = (int)(sizeof depths / sizeof depths[0]);
 	/* thread per ray; warp per ray in the tails; warp per ray everywhere */
 	static const int modes[] = {0, 16384, 1 << 24};
 	std::vector<sray_tune_trial> done;
@@ -3670,18 +3684,19 @@ int sray_gpu_autotune_batch(const sray_job *jobs, int n, int frames, void *strea
 	sray_tuning base = R.tune, cur = R.tune;
 	float cur_ms = 0.0f;
 	int r = 0;
-	/* the nine pairs, then the best pair with the shading tree's tail in the
-	 * persistent pool launch (below 32k and 128k rays in flight) */
+	/* the pairs of depth and mode, then the best pair with the shading
+	 * tree's tail in the persistent pool launch (below 32k and 128k rays in
+	 * flight) */
 	static const int tails[] = {1 << 15, 1 << 17};
-	for(int k = 0; k < 9 + 2 && !r; k++) {
+	for(int k = 0; k < nd * 3 + 2 && !r; k++) {
 		sray_tuning t = base;
-		if(k < 9) {
+		if(k < nd * 3) {
 			t.queue_depth = depths[k / 3];
 			t.warp_rays = t.warp_segments = modes[k % 3];
 			t.render_tail = 0;
 		} else {
 			t = cur;
-			t.render_tail = tails[k - 9];
+			t.render_tail = tails[k - nd * 3];
 		}
 		R.tune = t;
 		r = R.render_batch(jobs, n, s);
@@ -4089,6 +4104,8 @@ void sray_gpu_shutdown(void)
 		DevBuf *pbufs[] = {&p->ph, &p->cells, &p->tmp_ph, &p->keys, &p->keys2, &p->vals, &p->vals2, &p->lin, &p->hist, &p->scan};
 		for(DevBuf *b : pbufs) b->release();
 	}
+	if(R.pin) cudaFreeHost(R.pin);
+	R.pin = nullptr;
 	if(R.ps_done) cudaEventDestroy(R.ps_done);
 	if(R.ps) cudaStreamDestroy(R.ps);
 	if(R.gs) {

@@ -150,6 +150,10 @@ struct Renderer {
 	/* a pass sorted before it is traced (sray_tuning.sort_rays): the sorted
 	 * copy's queue (swapped with the pass's), keys and values, scratch */
 	DevBuf qsbuf, rs_keys, rs_hist, rs_part;
+	/* pinned host words the per-pass counts are read into (a read into
+	 * pageable memory is staged and waits inside the copy call): [0..7] the
+	 * render loop's, [8..15] the photon thread's */
+	int *pin = nullptr;
 	RayQueue qs = {};
 	int qscap = 0;
 	int sort_pass(int cur, int n, cudaStream_t s);
