@@ -49,8 +49,9 @@ def parse():
     ap.add_argument("--batch-frames", type=int, default=16, help="frames per batch of the stress-batch configuration")
     ap.add_argument("--batch-jobs", type=int, default=64, help="jobs of the batch configuration")
     ap.add_argument("--batch-scenes", type=int, default=16, help="scenes of the batch configuration's scene set")
-    ap.add_argument("--queue-depth", type=int, default=1 << 20,
-                    help="primary rays per wave of the batch configuration before (or without) autotuning")
+    ap.add_argument("--queue-depth", type=int, default=None,
+                    help="primary rays per wave: of the batch configuration before (or without) autotuning "
+                         "(default 2^20), of the stress-batch configuration (default 2^24)")
     ap.add_argument("--no-nrc", action="store_true", help="skip the radiance-cache comparison")
     ap.add_argument("--method", default="plain", choices=["plain", "cache", "cache-everywhere"],
                     help="final gather of the headline frames: the plain gather, the radiance cache with its "
@@ -580,7 +581,7 @@ def run_batch(args):
         return rays_of(g.stats())
 
 
-    g.set_tuning(queue_depth=args.queue_depth)      # bounded queues from the first batch on
+    g.set_tuning(queue_depth=args.queue_depth or 1 << 20)      # bounded queues from the first batch on
     batch()
     tuning = None
     if not args.no_autotune:
@@ -659,7 +660,7 @@ def run_stress_batch(args):
     """The combined stress configuration: the stress scene (10M triangles,
     2,000 instances, 24M photons, 3840x2160, adaptive 1-16 spp, motion blur)
     as batches of `--batch-frames` motion-blurred frames 2 ms apart, each
-    batch one wavefront (waves of 4M primary rays), first with the plain
+    batch one wavefront (waves of 16M primary rays), first with the plain
     gather, then with the radiance cache trained online across the batches:
     ms/frame, Mrays/s and device memory of both, and both images' RMSE
     against the FP64 oracle's converged final gather (64 rays per vertex) on
@@ -683,7 +684,7 @@ def run_stress_batch(args):
     nf = args.batch_frames
     fbs = [torch.zeros((H, W, 4), dtype=torch.float32, device="cuda") for _ in range(nf)]
     jobs = [(2 * j, fb) for j, fb in enumerate(fbs)]
-    g.set_tuning(queue_depth=1 << 22)
+    g.set_tuning(queue_depth=args.queue_depth or 1 << 24)
 
     def timed(n):
         e0 = torch.cuda.Event(enable_timing=True)
@@ -738,7 +739,7 @@ def run_stress_batch(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_cache, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator, no dataset)",
         "config": {"workload": workload_desc("stress") + "; %d frames 2 ms apart per batch, one wavefront per batch "
-                                                         "(waves of 4M primary rays)" % nf,
+                                                         "(waves of %d primary rays)" % (nf, args.queue_depth or 1 << 24),
                    "method": "radiance cache with per-region fallback, trained online across batches"},
         "stress_batch": {"frames_per_batch": nf,
                          "plain": {"ms_per_batch": ms_plain, "ms_per_frame": ms_plain / nf,
