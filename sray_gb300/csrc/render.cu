@@ -1344,7 +1344,7 @@ __device__ void gather_one(const DScene &S, int kind, V3 pos, V3 n, unsigned *ke
 	out[2] = sum[2] * inv_area;
 }
 
-__global__ void __launch_bounds__(GATHER_WARPS * 32, 3) k_gather(DScene S, const GatherReq *gq, const int *gq_count,
+__global__ void __launch_bounds__(GATHER_WARPS * 32, 4) k_gather(DScene S, const GatherReq *gq, const int *gq_count,
 		float4 *acc, DevCounters *ctr)
 {
 	__shared__ unsigned keys[GATHER_WARPS][KEY_CAP];
