@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default scheduler tuning")
     ap.add_argument("--tuning", default=None,
                     help="render_tail,pool_blocks_per_sm,photon_tail[,shadow_order[,stream_priority[,warp_rays"
-                         "[,warp_segments[,side_gather[,sort_rays]]]]]]: set the scheduler tuning instead "
+                         "[,warp_segments[,side_gather[,sort_rays[,side_shadow]]]]]]]: set the scheduler tuning instead "
                          "of autotuning")
     ap.add_argument("--nrc-burn-in", type=int, default=600, help="frames of online training before the cache is timed")
     ap.add_argument("--nrc-ladder", default="1,2,4,8,16,32,64,128",
@@ -895,7 +895,7 @@ def run_ours(args):
     if args.tuning:
         vals = [int(v) for v in args.tuning.split(",")]
         g.set_tuning(**dict(zip(("render_tail", "pool_blocks_per_sm", "photon_tail", "shadow_order", "stream_priority",
-                                 "warp_rays", "warp_segments", "side_gather", "sort_rays"), vals)))
+                                 "warp_rays", "warp_segments", "side_gather", "sort_rays", "side_shadow"), vals)))
     tuning = {"chosen": g.tuning(), "autotuned": False}
     if not args.no_autotune and not args.tuning:
         best, best_ms, trials = g.autotune(fb, frames=3, stream=stream)

@@ -2803,6 +2803,26 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 		gq_defer_cap = cap;
 		return true;
 	};
+	/* side_shadow: light samples on their own stream (not in the counting
+	 * pass, whose kernels count on the frame's stream); the render loop
+	 * joins it at a wave's end, before the persistent pool, and, whatever
+	 * the return, before this function's buffers are touched again */
+	const bool sides = tune.side_shadow != 0 && !(prof_flags & 2);
+	if(sides && side_stream()) return SRAY_ECUDA;
+	bool side_busy[2] = {false, false};
+	struct ShadowJoin {
+		Renderer *R;
+		bool *busy;
+		~ShadowJoin() { if(busy[0] || busy[1]) cudaStreamSynchronize(R->xs); }
+	} shadow_join{this, side_busy};
+	auto join_shadows = [&]() -> int {
+		for(int k = 0; k < 2; k++) {
+			if(!side_busy[k]) continue;
+			CK(cudaStreamWaitEvent(s, xs_done[k], 0), "light-sample join");
+			side_busy[k] = false;
+		}
+		return 0;
+	};
 	auto join_side = [&]() -> int {
 		if(!side_pending) return 0;
 		side_pending = false;
@@ -2870,6 +2890,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			if(depth >= 1 && !tail_done && n_rays <= tune.render_tail && (int64_t)n_rays * POOL_HEADROOM <= q[cur].cap) {
 				/* the rest of the shading tree in one launch (k_render_pool) */
 				tail_done = true;
+				if(int r = join_shadows()) return r;
 				if(int r = flush_gathers()) return r;
 				q[0].count = cnt + 0;
 				q[1].count = cnt + 1;
@@ -2928,8 +2949,17 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			q[0].count = cnt + 0;
 			q[1].count = cnt + 1;
 			CK(cudaMemsetAsync(q[cur ^ 1].count, 0, sizeof(int), s), "reset queue");
-			CK(cudaMemsetAsync(cnt + 5, 0, sizeof(int), s), "reset shadow queue");
-			CK(sq.ensure((size_t)n_rays * shadow_per_ray * sizeof(ShadowReq)), "shadow queue");
+			/* side_shadow: this bounce's light samples go to the buffer of its
+			 * parity, once the bounce before last has finished with it */
+			const int par = depth & 1;
+			DevBuf &sqb = sides && par ? sq2 : sq;
+			int *sqc = sides ? cnt + 40 + par : cnt + 5;
+			if(sides && side_busy[par]) {
+				CK(cudaStreamWaitEvent(s, xs_done[par], 0), "light-sample buffer");
+				side_busy[par] = false;
+			}
+			CK(cudaMemsetAsync(sqc, 0, sizeof(int), s), "reset shadow queue");
+			CK(sqb.ensure((size_t)n_rays * shadow_per_ray * sizeof(ShadowReq)), "shadow queue");
 			if(depth >= 1 && tune.sort_rays > 0 && n_rays >= tune.sort_rays && (r = sort_pass(cur, n_rays, s))) return r;
 			r = trace_rays(q[cur], n_rays, "trace", (prof_flags & 2) != 0, s);
 			if(r) return r;
@@ -2939,12 +2969,21 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			so.gq = gq.as<GatherReq>();
 			so.gq_count = cnt + 2;
 			so.gq_cap = deferring ? (int)gq_defer_cap : n_rays;
-			so.sq = sq.as<ShadowReq>();
-			so.sq_count = cnt + 5;
+			so.sq = sqb.as<ShadowReq>();
+			so.sq_count = sqc;
 			so.sq_cap = n_rays * shadow_per_ray;
 			LAUNCH(*this, "shade", s, k_shade<<<grid_for(n_rays, 128), 128, 0, s>>>(S, q[cur], hits.as<int4>(), so, acc.as<float4>(), depth,
 					ctr.as<DevCounters>()));
-			if(int r = shadow_rays(n_rays * shadow_per_ray, s)) return r;
+			if(sides) {
+				/* traced beside the next bounce's closest hits and shading */
+				CK(cudaEventRecord(xs_fork, s), "light-sample fork");
+				CK(cudaStreamWaitEvent(xs, xs_fork, 0), "light-sample fork");
+				if(int r = shadow_rays_on(sqb.as<ShadowReq>(), sqc, n_rays * shadow_per_ray, fbs[par], xs)) return r;
+				CK(cudaEventRecord(xs_done[par], xs), "light-sample done");
+				side_busy[par] = true;
+			} else if(int r = shadow_rays(n_rays * shadow_per_ray, s)) {
+				return r;
+			}
 			if(deferring)
 				gq_upper += n_rays;
 			else
@@ -2964,6 +3003,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			n_rays = h_cnt;
 			cur ^= 1;
 		}
+		if(int r = join_shadows()) return r;
 		/* the wave's gathers and radiance-cache queries; while the photon
 		 * maps are still being traced and more waves follow, the gathers stay
 		 * queued (the radiance cache, whose records are gather estimates,
@@ -3074,23 +3114,39 @@ int Renderer::trace_rays_with(const DScene &D, const RayQueue &qq, int n, const 
  * the tuning's kernel, then the octree retrace of the undecided ones */
 int Renderer::shadow_rays(int cap, cudaStream_t s)
 {
-	int *cnt = counts.as<int>();
-	CK(fbl.ensure(((size_t)cap + 1) * sizeof(int)), "fallback list");
-	CK(cudaMemsetAsync(fbl.p, 0, sizeof(int), s), "reset fallback list");
+	return shadow_rays_on(sq.as<ShadowReq>(), counts.as<int>() + 5, cap, fbl, s);
+}
+
+/* the light samples q (count at *count, at most cap) on stream st, with the
+ * fallback list fb */
+int Renderer::shadow_rays_on(const ShadowReq *q, int *count, int cap, DevBuf &fb, cudaStream_t st)
+{
+	CK(fb.ensure(((size_t)cap + 1) * sizeof(int)), "fallback list");
+	CK(cudaMemsetAsync(fb.p, 0, sizeof(int), st), "reset fallback list");
 	int g = grid_for(cap, 128);
-	const ShadowReq *q = sq.as<ShadowReq>();
 	float4 *a = acc.as<float4>();
 	DevCounters *c = ctr.as<DevCounters>();
-	int *f = fbl.as<int>();
+	int *f = fb.as<int>();
 	if(prof_flags & 2)   /* counting the traversal work: every pass thread per segment */
-		LAUNCH(*this, "shadow", s, k_shadow<true, true, true><<<g, 128, 0, s>>>(S, q, cnt + 5, a, c, f));
+		LAUNCH(*this, "shadow", st, k_shadow<true, true, true><<<g, 128, 0, st>>>(S, q, count, a, c, f));
 	else if(cap <= tune.warp_segments)
-		LAUNCH(*this, "shadow", s, k_shadow_warp<<<grid_for(cap, 4), 128, 0, s>>>(S, q, cnt + 5, a, c, f));
+		LAUNCH(*this, "shadow", st, k_shadow_warp<<<grid_for(cap, 4), 128, 0, st>>>(S, q, count, a, c, f));
 	else if(tune.shadow_order)
-		LAUNCH(*this, "shadow", s, k_shadow<true, false><<<g, 128, 0, s>>>(S, q, cnt + 5, a, c, f));
+		LAUNCH(*this, "shadow", st, k_shadow<true, false><<<g, 128, 0, st>>>(S, q, count, a, c, f));
 	else
-		LAUNCH(*this, "shadow", s, k_shadow<true><<<g, 128, 0, s>>>(S, q, cnt + 5, a, c, f));
-	LAUNCH(*this, "octree_retrace", s, k_shadow<false><<<retrace_grid(), 128, 0, s>>>(S, q, cnt + 5, a, c, f));
+		LAUNCH(*this, "shadow", st, k_shadow<true><<<g, 128, 0, st>>>(S, q, count, a, c, f));
+	LAUNCH(*this, "octree_retrace", st, k_shadow<false><<<retrace_grid(), 128, 0, st>>>(S, q, count, a, c, f));
+	return 0;
+}
+
+int Renderer::side_stream()
+{
+	if(xs) return 0;
+	int least = 0, greatest = 0;
+	CK(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
+	CK(cudaStreamCreateWithPriority(&xs, cudaStreamNonBlocking, greatest), "light-sample stream");
+	CK(cudaEventCreateWithFlags(&xs_fork, cudaEventDisableTiming), "light-sample stream event");
+	for(int k = 0; k < 2; k++) CK(cudaEventCreateWithFlags(&xs_done[k], cudaEventDisableTiming), "light-sample stream event");
 	return 0;
 }
 
@@ -3562,6 +3618,7 @@ static int check_tuning(const sray_tuning *t)
 	if(t->warp_segments < 0 || t->warp_segments > (1 << 24)) { g_err = "warp_segments must be 0..2^24"; return SRAY_EINVAL; }
 	if(t->side_gather < 0 || t->side_gather > 2) { g_err = "side_gather must be 0, 1 or 2"; return SRAY_EINVAL; }
 	if(t->sort_rays < 0) { g_err = "sort_rays must be >= 0"; return SRAY_EINVAL; }
+	if(t->side_shadow != 0 && t->side_shadow != 1) { g_err = "side_shadow must be 0 or 1"; return SRAY_EINVAL; }
 	if(t->queue_depth != 0 && (t->queue_depth < 1024 || t->queue_depth > (1 << 27))) {
 		g_err = "queue_depth must be 0 or 1024..2^27";
 		return SRAY_EINVAL;
@@ -3608,7 +3665,7 @@ int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tunin
 	const Knob knobs[] = {{&sray_tuning::render_tail, tails, 5}, {&sray_tuning::pool_blocks_per_sm, pools, 4},
 		{&sray_tuning::photon_tail, ptails, 4}, {&sray_tuning::shadow_order, binary, 2}, {&sray_tuning::stream_priority, prios, 3},
 		{&sray_tuning::warp_rays, wrays, 5}, {&sray_tuning::warp_segments, wrays, 5}, {&sray_tuning::queue_depth, depths, 4},
-		{&sray_tuning::side_gather, binary, 2}};
+		{&sray_tuning::side_gather, binary, 2}, {&sray_tuning::side_shadow, binary, 2}};
 	std::vector<sray_tune_trial> done;
 	cudaEvent_t e0, e1;
 	if(cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) { g_err = "autotune events"; return SRAY_ECUDA; }
@@ -4095,9 +4152,10 @@ void sray_gpu_shutdown(void)
 		&R.fbl, &R.tnodes, &R.ohome, &R.pool_ready, &R.pqbuf[0], &R.pqbuf[1], &R.phits, &R.pfbl, &R.pcounts, &R.pctr,
 		&R.pw_jobs, &R.pw_prefix, &R.pw_scale, &R.pw_bits, &R.pw_cov, &R.pw_pix, &R.pw_out, &R.pw_valid,
 		&R.pw_part, &R.pw_tiles, &R.pw_bounds, &R.pw_offs, &R.pw_ph, &R.pw_sorted, &R.pw_grids, &R.pw_morton, &R.pw_cellbase,
-		&R.pw_keys, &R.pw_lin, &R.pw_cells, &R.pw_hist, &R.qsbuf, &R.rs_keys, &R.rs_hist, &R.rs_part,
+		&R.pw_keys, &R.pw_lin, &R.pw_cells, &R.pw_hist, &R.qsbuf, &R.rs_keys, &R.rs_hist, &R.rs_part, &R.sq2, &R.fbs[0], &R.fbs[1],
 		&R.nrc_qx, &R.nrc_qw, &R.nrc_rx, &R.nrc_rt, &R.nrc_ry, &R.nrc_regions};
 	if(R.ps) cudaStreamSynchronize(R.ps);
+	if(R.xs) cudaStreamSynchronize(R.xs);
 	for(DevBuf *b : bufs) b->release();
 	PhotonBufs *pb[] = {&R.caust, &R.gi};
 	for(PhotonBufs *p : pb) {
@@ -4113,6 +4171,13 @@ void sray_gpu_shutdown(void)
 		cudaStreamDestroy(R.gs);
 		cudaEventDestroy(R.gs_fork);
 		cudaEventDestroy(R.gs_done);
+	}
+	if(R.xs) {
+		cudaStreamSynchronize(R.xs);
+		cudaStreamDestroy(R.xs);
+		cudaEventDestroy(R.xs_fork);
+		cudaEventDestroy(R.xs_done[0]);
+		cudaEventDestroy(R.xs_done[1]);
 	}
 	R.gq_side.release();
 	if(R.hs) {

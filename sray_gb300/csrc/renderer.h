@@ -167,6 +167,13 @@ struct Renderer {
 	cudaStream_t hs = nullptr; /* the frame's stream under stream_priority 2 */
 	cudaStream_t gs = nullptr; /* the gather stream under side_gather */
 	cudaEvent_t gs_fork = nullptr, gs_done = nullptr;
+	/* side_shadow: the light-sample stream, its requests double-buffered
+	 * by bounce parity (sq for even bounces, sq2 for odd), its fallback lists */
+	cudaStream_t xs = nullptr;
+	cudaEvent_t xs_fork = nullptr, xs_done[2] = {nullptr, nullptr};
+	DevBuf sq2, fbs[2];
+	int side_stream();
+	int shadow_rays_on(const ShadowReq *q, int *count, int cap, DevBuf &fb, cudaStream_t st);
 	DevBuf gq_side;            /* its copy of the accumulated gather requests */
 	std::atomic<bool> photon_finished{false};   /* the photon thread has returned */
 	int gather_stream();
@@ -177,7 +184,7 @@ struct Renderer {
 	cudaEvent_t ps_done = nullptr;
 	sray_stats stats;
 	/* the autotuner's choice on the production frame */
-	sray_tuning tune = {0, 4, 65536, 0, 2, 16384, 16384, 0, 0};
+	sray_tuning tune = {0, 4, 65536, 0, 2, 16384, 16384, 0, 0, 0, 1};
 	int nsm = 0;                  /* multiprocessors of the device */
 	/* Octree retraces follow every hierarchy pass and nearly always find no
 	 * ray listed (a couple a frame).  Their grid-stride launches are sized

@@ -65,7 +65,7 @@ class SrayTuning(ctypes.Structure):
     _fields_ = [("render_tail", ctypes.c_int), ("pool_blocks_per_sm", ctypes.c_int), ("photon_tail", ctypes.c_int),
                 ("shadow_order", ctypes.c_int), ("stream_priority", ctypes.c_int), ("warp_rays", ctypes.c_int),
                 ("warp_segments", ctypes.c_int), ("queue_depth", ctypes.c_int), ("side_gather", ctypes.c_int),
-                ("sort_rays", ctypes.c_int)]
+                ("sort_rays", ctypes.c_int), ("side_shadow", ctypes.c_int)]
 
 
 class SrayTuneTrial(ctypes.Structure):

@@ -101,7 +101,9 @@ def test_image_small_scene(small_pair):
                                     dict(warp_rays=1 << 24, warp_segments=1 << 24), dict(warp_rays=0, warp_segments=0),
                                     dict(side_gather=1), dict(side_gather=2), dict(queue_depth=4096),
                                     dict(queue_depth=1024, warp_rays=1 << 24, warp_segments=1 << 24),
-                                    dict(sort_rays=1), dict(sort_rays=1, queue_depth=4096, warp_rays=0)])
+                                    dict(sort_rays=1), dict(sort_rays=1, queue_depth=4096, warp_rays=0),
+                                    dict(side_shadow=1), dict(side_shadow=1, queue_depth=4096, warp_segments=0),
+                                    dict(side_shadow=1, render_tail=1 << 20)])
 def test_tuning_keeps_the_image(small_pair, tuning):
     # light samples' any-hit traversal in node order instead of nearest
     # first; the photon stream or the frame's own stream given priority;
