@@ -439,9 +439,10 @@ int sray_gpu_set_tuning(const sray_tuning *t);
 
 /* The autotuner: renders frame `msec` into the device framebuffer `fb` on
  * `stream` under candidate tunings (coordinate descent over the fields of
- * sray_tuning, one warm-up and `frames` timed frames each, CUDA-event
- * timing), keeps the fastest and returns it with its time.  Every trial goes
- * into `log` (up to `log_cap`, count through `n_log`). */
+ * sray_tuning, one warm-up and two groups of `frames` timed frames each,
+ * CUDA-event timing, the slower group counting), keeps the fastest and
+ * returns it with its time.  Every trial goes into `log` (up to `log_cap`,
+ * count through `n_log`). */
 int sray_gpu_autotune(long msec, float *fb, int frames, void *stream, sray_tuning *best, float *best_ms,
 		sray_tune_trial *log, int log_cap, int *n_log);
 

@@ -170,6 +170,7 @@ struct Renderer {
 	/* side_shadow: the light-sample stream, its requests double-buffered
 	 * by bounce parity (sq for even bounces, sq2 for odd), its fallback lists */
 	cudaStream_t xs = nullptr;
+	int xs_priority = -1;      /* 1 when xs has the greatest priority */
 	cudaEvent_t xs_fork = nullptr, xs_done[2] = {nullptr, nullptr};
 	DevBuf sq2, fbs[2];
 	int side_stream();
