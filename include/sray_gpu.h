@@ -424,8 +424,9 @@ typedef struct sray_tuning {
 	                             first sorted by direction octant and origin cell, so that a
 	                             warp's rays start close together and head the same way
 	                             (0: never) (0) */
-	int side_shadow;          /* 1: a bounce's light samples are traced on a stream of their
-	                             own beside the next bounce's closest hits and shading (1) */
+	int side_shadow;          /* 1: a bounce's light samples and photon-map gathers run on a
+	                             stream of their own beside the next bounce's closest hits
+	                             and shading (1) */
 } sray_tuning;
 
 typedef struct sray_tune_trial {

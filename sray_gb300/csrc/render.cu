@@ -2942,21 +2942,24 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 				bool grown = !photon_finished.load() && !S.nrc.mode && grow_deferred(gq_upper + n_rays);
 				if(!grown && (r = flush_gathers())) return r;
 			}
-			if(!deferring) {
-				CK(gq.ensure((size_t)n_rays * sizeof(GatherReq)), "gather queue");
-				CK(cudaMemsetAsync(cnt + 2, 0, sizeof(int), s), "reset gather queue");
-			}
 			q[0].count = cnt + 0;
 			q[1].count = cnt + 1;
 			CK(cudaMemsetAsync(q[cur ^ 1].count, 0, sizeof(int), s), "reset queue");
-			/* side_shadow: this bounce's light samples go to the buffer of its
-			 * parity, once the bounce before last has finished with it */
+			/* side_shadow: this bounce's light samples (and, once the photon
+			 * maps exist, its gathers) go to the buffers of its parity, once
+			 * the bounce before last has finished with them */
 			const int par = depth & 1;
 			DevBuf &sqb = sides && par ? sq2 : sq;
 			int *sqc = sides ? cnt + 40 + par : cnt + 5;
+			DevBuf &gqb = sides && par ? gq2 : gq;
+			int *gqc = sides ? cnt + 42 + par : cnt + 2;
 			if(sides && side_busy[par]) {
 				CK(cudaStreamWaitEvent(s, xs_done[par], 0), "light-sample buffer");
 				side_busy[par] = false;
+			}
+			if(!deferring) {
+				CK(gqb.ensure((size_t)n_rays * sizeof(GatherReq)), "gather queue");
+				CK(cudaMemsetAsync(gqc, 0, sizeof(int), s), "reset gather queue");
 			}
 			CK(cudaMemsetAsync(sqc, 0, sizeof(int), s), "reset shadow queue");
 			CK(sqb.ensure((size_t)n_rays * shadow_per_ray * sizeof(ShadowReq)), "shadow queue");
@@ -2966,8 +2969,8 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			ShadeOut so;
 			so.qo = q[cur ^ 1];
 			so.qo.cap = child_cap(so.qo.cap);
-			so.gq = gq.as<GatherReq>();
-			so.gq_count = cnt + 2;
+			so.gq = deferring ? gq.as<GatherReq>() : gqb.as<GatherReq>();
+			so.gq_count = deferring ? cnt + 2 : gqc;
 			so.gq_cap = deferring ? (int)gq_defer_cap : n_rays;
 			so.sq = sqb.as<ShadowReq>();
 			so.sq_count = sqc;
@@ -2979,6 +2982,9 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 				CK(cudaEventRecord(xs_fork, s), "light-sample fork");
 				CK(cudaStreamWaitEvent(xs, xs_fork, 0), "light-sample fork");
 				if(int r = shadow_rays_on(sqb.as<ShadowReq>(), sqc, n_rays * shadow_per_ray, fbs[par], xs)) return r;
+				if(!deferring)
+					LAUNCH(*this, "gather", xs, k_gather<<<grid_for(n_rays, GATHER_WARPS), GATHER_WARPS * 32, 0, xs>>>(S,
+							gqb.as<GatherReq>(), gqc, acc.as<float4>(), ctr.as<DevCounters>()));
 				CK(cudaEventRecord(xs_done[par], xs), "light-sample done");
 				side_busy[par] = true;
 			} else if(int r = shadow_rays(n_rays * shadow_per_ray, s)) {
@@ -2986,7 +2992,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			}
 			if(deferring)
 				gq_upper += n_rays;
-			else
+			else if(!sides)
 				LAUNCH(*this, "gather", s, k_gather<<<grid_for(n_rays, GATHER_WARPS), GATHER_WARPS * 32, 0, s>>>(S, gq.as<GatherReq>(),
 						cnt + 2, acc.as<float4>(), ctr.as<DevCounters>()));
 			stats.secondary_rays += depth ? n_rays : 0;
@@ -4171,7 +4177,7 @@ void sray_gpu_shutdown(void)
 		&R.fbl, &R.tnodes, &R.ohome, &R.pool_ready, &R.pqbuf[0], &R.pqbuf[1], &R.phits, &R.pfbl, &R.pcounts, &R.pctr,
 		&R.pw_jobs, &R.pw_prefix, &R.pw_scale, &R.pw_bits, &R.pw_cov, &R.pw_pix, &R.pw_out, &R.pw_valid,
 		&R.pw_part, &R.pw_tiles, &R.pw_bounds, &R.pw_offs, &R.pw_ph, &R.pw_sorted, &R.pw_grids, &R.pw_morton, &R.pw_cellbase,
-		&R.pw_keys, &R.pw_lin, &R.pw_cells, &R.pw_hist, &R.qsbuf, &R.rs_keys, &R.rs_hist, &R.rs_part, &R.sq2, &R.fbs[0], &R.fbs[1],
+		&R.pw_keys, &R.pw_lin, &R.pw_cells, &R.pw_hist, &R.qsbuf, &R.rs_keys, &R.rs_hist, &R.rs_part, &R.sq2, &R.gq2, &R.fbs[0], &R.fbs[1],
 		&R.nrc_qx, &R.nrc_qw, &R.nrc_rx, &R.nrc_rt, &R.nrc_ry, &R.nrc_regions};
 	if(R.ps) cudaStreamSynchronize(R.ps);
 	if(R.xs) cudaStreamSynchronize(R.xs);

@@ -168,11 +168,12 @@ struct Renderer {
 	cudaStream_t gs = nullptr; /* the gather stream under side_gather */
 	cudaEvent_t gs_fork = nullptr, gs_done = nullptr;
 	/* side_shadow: the light-sample stream, its requests double-buffered
-	 * by bounce parity (sq for even bounces, sq2 for odd), its fallback lists */
+	 * by bounce parity (sq / gq for even bounces, sq2 / gq2 for odd), its
+	 * fallback lists */
 	cudaStream_t xs = nullptr;
 	int xs_priority = -1;      /* 1 when xs has the greatest priority */
 	cudaEvent_t xs_fork = nullptr, xs_done[2] = {nullptr, nullptr};
-	DevBuf sq2, fbs[2];
+	DevBuf sq2, gq2, fbs[2];
 	int side_stream();
 	int shadow_rays_on(const ShadowReq *q, int *count, int cap, DevBuf &fb, cudaStream_t st);
 	DevBuf gq_side;            /* its copy of the accumulated gather requests */
