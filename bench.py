@@ -1008,7 +1008,9 @@ def run_ours(args):
                      "around every launch on its own stream); traffic = DRAM bytes per unit from the committed ncu capture "
                      "of a smaller frame, times this frame's units per launch: the hierarchies and photon maps are "
                      "re-read from L1/L2, so DRAM traffic is a small fraction of the algorithmic bytes and the kernels "
-                     "are bound by instruction issue at the SIMT efficiency beside each")
+                     "are bound by instruction issue at the SIMT efficiency beside each; with side_shadow the light "
+                     "samples and gathers run beside the closest-hit launches, whose event time then includes the SMs "
+                     "they share")
     roof["node_records_per_ray"] = st_count["node_visits"] / max(st_count["primary_rays"] + st_count["secondary_rays"], 1)
     roof["prim_tests_per_ray"] = st_count["prim_tests"] / max(st_count["primary_rays"] + st_count["secondary_rays"], 1)
     if not scaled:
