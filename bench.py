@@ -45,7 +45,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="production",
                     choices=["production", "small", "learned", "stress", "batch", "stress-batch", "nrc-infer"])
-    ap.add_argument("--nrc-samples", type=int, default=1 << 20, help="samples per launch of the nrc-infer configuration")
+    ap.add_argument("--nrc-samples", type=int, default=1 << 22,
+                    help="samples per launch of the nrc-infer configuration (the default's 151 MB of inputs exceed the L2)")
     ap.add_argument("--batch-frames", type=int, default=16, help="frames per batch of the stress-batch configuration")
     ap.add_argument("--batch-jobs", type=int, default=64, help="jobs of the batch configuration")
     ap.add_argument("--batch-scenes", type=int, default=16, help="scenes of the batch configuration's scene set")
@@ -1143,10 +1144,13 @@ def run_ours(args):
 
 def run_nrc_infer(args):
     """The radiance cache's tensor-core inference alone: `--nrc-samples`
-    uniform inputs, `--warmup` untimed calls, then `--steps` calls timed with
-    CUDA events (sray_nrc_infer: one k_nrc_forward_tc launch and a read of
-    its error word each); TFLOP/s of the 2 x 26,304 FLOP per sample against
-    the measured bf16 peak."""
+    uniform inputs, `--warmup` untimed calls, then `--steps` launches
+    enqueued back to back (sray_nrc_infer_async: one k_nrc_forward_tc launch
+    each, the error word read once after them by sray_nrc_check) timed with
+    CUDA events -- the kernel's rate -- and `--steps` synchronous calls
+    (sray_nrc_infer: the launch, a wait and a read of the error word each);
+    TFLOP/s of the 2 x 26,304 FLOP per sample against the measured bf16
+    peak."""
     import torch
     from sray_gb300 import build as gbuild, gpu
     torch.cuda.set_device(0)
@@ -1160,20 +1164,29 @@ def run_nrc_infer(args):
     for _ in range(args.warmup):
         cache.infer(x, y, stream=stream)
     torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        cache.infer(x, y, stream=stream)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
+
+    def timed(sync):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            cache.infer(x, y, stream=stream, sync=sync)
+        e1.record(stream)
+        cache.check(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    ms = timed(False)
+    ms_sync = timed(True)
     tflops = 2 * 26304 * n / (ms / 1e3) / 1e12
     peak = bf16_peak()
     print(json.dumps({"metric": "radiance-cache inference (k_nrc_forward_tc)", "value": tflops, "unit": "TFLOP/s",
                       "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+                      "ms_per_synchronous_call": ms_sync,
+                      "tflops_synchronous_calls": 2 * 26304 * n / (ms_sync / 1e3) / 1e12,
                       "higher_is_better": True, "dtype": "bf16", "data": "synthetic (uniform inputs)",
-                      "config": {"workload": "nrc-infer: %d samples per launch" % n},
+                      "config": {"workload": "nrc-infer: %d samples per launch" % n,
+                                 "l2": "inputs of %.0f MB per launch%s" % (n * 36 / 1e6, " (larger than L2)" if n * 36 > 129e6 else "")},
                       "roofline": {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s",
                                    "frac": tflops / peak if peak else None},
                       "finite": bool(torch.isfinite(y).all())}))

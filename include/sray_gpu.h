@@ -357,7 +357,7 @@ int sray_gpu_nrc_reset(uint64_t seed);
  * A small MLP standing in for the final gather of indirect light
  * (shade_phong's diffuse rays + PhotonMap::radiance_est, src/shader.cc:154-187,
  * src/pmap.cc:143-178).  Inputs x[n][9]: position scaled to the scene box,
- * unit normal, unit direction; outputs y[n][3].  12-band sin/cos encoding,
+ * unit normal, unit direction (each within [-4096, 4096]); outputs y[n][3].  12-band sin/cos encoding,
  * 216 -> 64 -> 64 -> 64 -> 64 -> 3 (ReLU), BF16 weights on tensor cores with
  * FP32 accumulation, relative L2 loss, Adam (lr 1e-3).  Parameters are
  * exchanged as SRAY_NRC_PARAMS floats in the order W1 (64x216, row-major),
@@ -369,6 +369,13 @@ int sray_nrc_reset(uint64_t seed);
 int sray_nrc_set_params(const float *params, int n);
 int sray_nrc_get_params(float *params, int n);
 int sray_nrc_infer(int n, const float *x, float *y, void *stream);
+/* the same inference enqueued on `stream` without waiting for it; a
+ * tensor-core wait that ran out (SRAY_EDEVICE) is reported by the next
+ * sray_nrc_check or sray_nrc_infer */
+int sray_nrc_infer_async(int n, const float *x, float *y, void *stream);
+/* waits for `stream`; SRAY_EDEVICE when an inference's bounded wait ran out
+ * since the last check */
+int sray_nrc_check(void *stream);
 /* gradient of the loss over the batch (no update) */
 int sray_nrc_gradients(int n, const float *x, const float *targets, float *grad, float *loss, void *stream);
 /* one Adam step on the batch; *loss (device, optional) = the batch loss before the step */

@@ -357,49 +357,67 @@ __global__ void __launch_bounds__(NRC_FWD_THREADS) k_nrc_forward(NrcDev net, int
 }
 
 /* ---- The inference and query forward on the 5th-generation tensor cores ----
- * tcgen05.mma with the operands in shared memory and the accumulators in
- * tensor memory (TMEM).  A CTA of 512 threads is two groups of eight warps;
- * each group carries a tile of 128 samples through the five layers, two
- * threads per sample (row): its threads write the tile's encoded inputs
- * (half of a row's features each) into shared memory, one elected thread
- * issues the layer's MMAs (M = 128, N = 64, K = 16 each; 14 for the
- * 224-wide first layer, 5 for the 80-wide others, N = 16 for the output
- * layer) and commits them to the group's mbarrier, and the threads read
- * their rows of the accumulator back from TMEM (tcgen05.ld, 32x32b: warp w
- * its lanes 32 (w mod 4) on; the two warps of a lane quarter take 32
- * columns each) for the ReLU and BF16 rounding that make the next layer's
- * operand; the biases come with the products (a BF16 pair per row of each
- * weight tile against a constant pair in the operand).  The two groups of a
- * CTA interleave, so one group's encoding and epilogues overlap the other's
- * MMAs.  The weights (BF16, 62 KB) are copied once per CTA into the
- * canonical K-major layout without swizzle: 8-row x 16-byte core matrices,
- * the two of a K = 16 step 128 bytes apart (leading byte offset), 8-row
- * groups K/8 x 128 bytes apart (stride byte offset).  Every wait on an
- * mbarrier is bounded; one that runs out sets the error word and the group
- * stops (TMEM is released as usual). */
-#define TC_THREADS 512
+ * tcgen05.mma with the accumulators in tensor memory (TMEM).  A CTA of 768
+ * threads is three groups of eight warps; each group carries a tile of 128
+ * samples through the five layers, two threads per sample (row): its threads
+ * write the tile's encoded inputs (half of a row's features each) into
+ * shared memory, one elected thread issues the layer's MMAs (M = 128, N = 64,
+ * K = 16 each; 14 for the 224-wide first layer, 5 for the 80-wide others,
+ * N = 16 for the output layer) and commits them to the group's mbarrier, and
+ * the threads read their rows of the accumulator back from TMEM (tcgen05.ld,
+ * 32x32b: warp w its lanes 32 (w mod 4) on; the two warps of a lane quarter
+ * take 32 columns each) for the ReLU and BF16 rounding that make the next
+ * layer's operand, which stays in TMEM (tcgen05.st; the MMA's A operand
+ * there, two BF16 per column); the biases come with the products (a BF16 pair
+ * per row of each weight tile against a constant pair in the operand).  The
+ * features are read only by the first layer, so a group encodes its next
+ * tile while the MMAs of the current one's layers 2-5 run (a quarter of the
+ * encoding after each of their issues), and the three groups interleave.
+ *
+ * Shared memory, canonical K-major layouts without swizzle (8-row x 16-byte
+ * core matrices; a descriptor's leading byte offset steps along K, its
+ * stride byte offset along the rows):
+ *   weights   W1 64 x 224, W2-W4 64 x 80, W5 its first 8 rows x 80 (rows 3-7
+ *             zero; the MMA's rows 8-15 read the bytes that follow and land in
+ *             output columns that are never read), row-group-major: the core
+ *             matrices of a row group 128 bytes apart, row groups K/8 x 128
+ *   per group the tile's 27 feature chunks, chunk-major: chunk c, row r at
+ *             c x 2048 + r x 16 (leading byte offset 2048, stride 128)
+ *   constant  2 KB of rows (1, 1, 0 ...), the features' bias pair (chunk 27),
+ *             reached by the first layer's last K step through its leading
+ *             byte offset
+ * 228,648 bytes.  TMEM: 128 columns per group (the hidden accumulator, the
+ * hidden operand, the output accumulator).  Every wait on an mbarrier is
+ * bounded; one that runs out sets the error word and the group stops at its
+ * next barrier (TMEM is released as usual). */
+#define TC_NG 3                 /* groups (tiles in flight) per CTA */
 #define TC_GROUP_THREADS 256
+#define TC_THREADS (TC_NG * TC_GROUP_THREADS)
 #define TC_WAIT_LIMIT (1 << 20)
+#define TC_XH 5                 /* inputs a half of the encoding reads: 0-4 or 4-8 */
 
 enum {
 	TC_KH = 80,                         /* K of layers 2-5: 64 activations, the bias pair, zeros */
+	TC_CHUNK = 128 * 16,                /* one 8-element K chunk of a 128-row operand */
 	TC_W1 = 0,                          /* 64 x 224: 8 row groups x 28 K-chunks x 128 B */
 	TC_W2 = TC_W1 + 64 * NRC_FP * 2,    /* 64 x 80 each */
 	TC_W3 = TC_W2 + 64 * TC_KH * 2,
 	TC_W4 = TC_W3 + 64 * TC_KH * 2,
-	TC_W5 = TC_W4 + 64 * TC_KH * 2,     /* 16 x 80 (rows 3..15 zero) */
-	TC_GROUP0 = (TC_W5 + 16 * TC_KH * 2 + 127) & ~127,
-	TC_A1 = 0,                          /* per group: 128 x 224 encoded inputs */
-	TC_H = TC_A1 + 128 * NRC_FP * 2,    /* 128 x 80 hidden activations */
-	TC_MBAR = TC_H + 128 * TC_KH * 2,
-	TC_GROUP_BYTES = TC_MBAR + 128,
-	TC_TMEM_SLOT = TC_GROUP0 + 2 * TC_GROUP_BYTES,
+	TC_W5 = TC_W4 + 64 * TC_KH * 2,     /* 8 x 80 */
+	TC_GROUP0 = TC_W5 + 8 * TC_KH * 2,
+	TC_GROUP_BYTES = (NRC_F / 8) * TC_CHUNK,        /* the 27 feature chunks */
+	TC_CONST = TC_GROUP0 + TC_NG * TC_GROUP_BYTES,
+	TC_MBAR = TC_CONST + TC_CHUNK,
+	TC_TMEM_SLOT = TC_MBAR + 8 * TC_NG,
 	TC_SMEM = TC_TMEM_SLOT + 16,
-	TC_TMEM_COLS = 256                  /* per group: 64 hidden + 16 output columns, at 128 g */
+	TC_TMEM_COLS = 512,                 /* a power of two >= 128 per group */
+	/* a group's TMEM columns, from 128 g: the hidden layers' accumulator,
+	 * the hidden operand (80 BF16 = 40 columns), the output layer's
+	 * accumulator */
+	TC_TD = 0, TC_TA = 64, TC_TO = 112
 };
-
-/* byte offset of element row r, 8-element K-chunk c in the canonical layout of a tile with kc chunks */
-__device__ __forceinline__ uint32_t tc_canon(int r, int c, int kc) { return (uint32_t)(((r >> 3) * kc + c) * 128 + (r & 7) * 16); }
+static_assert(TC_SMEM <= 232448, "shared memory of the tensor-core forward");
+static_assert(TC_GROUP0 % 128 == 0 && TC_CONST % 128 == 0 && TC_MBAR % 8 == 0, "operand alignment");
 
 /* shared-memory matrix descriptor: start, leading and stride byte offsets, the
  * descriptor version of sm_100, no swizzle */
@@ -425,6 +443,14 @@ __device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t adesc, uint64_t
 			:: "r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate) : "memory");
 }
 
+/* the same with the A operand in TMEM (M = 128 lanes, two BF16 per column) */
+__device__ __forceinline__ void tc_mma_ta(uint32_t tmem_d, uint32_t tmem_a, uint64_t bdesc, uint32_t idesc, int accumulate)
+{
+	asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+			"tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}\n"
+			:: "r"(tmem_d), "r"(tmem_a), "l"(bdesc), "r"(idesc), "r"(accumulate) : "memory");
+}
+
 __device__ __forceinline__ void tc_commit(uint32_t mbar)
 {
 	asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" :: "r"(mbar) : "memory");
@@ -444,7 +470,6 @@ __device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity)
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void proxy_fence() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void group_sync(int g) { asm volatile("bar.sync %0, %1;" :: "r"(1 + g), "n"(TC_GROUP_THREADS) : "memory"); }
 
 /* true when v holds in every thread of group g (its named barrier): a wait
  * that ran out in one thread stops the whole group together */
@@ -484,34 +509,111 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16])
 	for(int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
-/* K-chunk c of a sample's encoded inputs: the (sin, cos) pairs of bands
- * 4k .. 4k + 3 of input v (c = 3v + k; chunk 27 is padding).  Band 4k is
- * evaluated (sincospif, exact argument scaling), the next three by angle
- * doubling, sin 2a = 2 sin a cos a and cos 2a = 1 - 2 sin^2 a: a few units in
- * the last place of FP32 after three steps, below the BF16 rounding that
- * follows. */
-__device__ __forceinline__ uint4 tc_encode_chunk(const float *xv, int c)
+/* 16 columns of the calling thread's TMEM lane (its warp's 32 lanes), then
+ * the wait for them */
+__device__ __forceinline__ void tc_st16(uint32_t taddr, const uint32_t (&r)[16])
 {
-	/* 9 inputs x 3 chunks; chunk 27 the constant pair (1, 1) of the bias */
-	if(c >= NRC_F / 8) return make_uint4(pack_bf16(1.0f, 1.0f), 0u, 0u, 0u);
-	int v = c / 3, k = c - 3 * v;
-	float sn, cs;
-	sincospif(xv[v] * (float)(1 << (4 * k)), &sn, &cs);
-	uint32_t q[4];
-	#pragma unroll
-	for(int b = 0; b < 4; b++) {
-		q[b] = pack_bf16(sn, cs);
-		float s2 = 2.0f * (sn * cs);
-		cs = fmaf(-2.0f * sn, sn, 1.0f);
-		sn = s2;
-	}
-	return make_uint4(q[0], q[1], q[2], q[3]);
+	asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"
+			:: "r"(taddr), "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+			   "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]) : "memory");
+	asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
-/* a weight image [rows][ld] (BF16) into the canonical layout of kc K-chunks:
- * its first ks chunks, then in chunk ks the row's bias as a BF16 pair (hi,
- * lo: b = hi + lo to 2^-17) that multiplies the operand's constant pair
- * (1, 1), the rest zero; rows beyond `rows` up to `rows_pad` zero */
+/* (sin, cos) of a + q quarter turns from (sin a, cos a); q mod 4 in the low bits of q */
+__device__ __forceinline__ void quarter_turns(float &s, float &c, uint32_t q)
+{
+	float s1 = (q & 1u) ? c : s, c1 = (q & 1u) ? s : c;
+	s = __uint_as_float(__float_as_uint(s1) ^ ((q << 30) & 0x80000000u));
+	c = __uint_as_float(__float_as_uint(c1) ^ (((q + 1u) << 30) & 0x80000000u));
+}
+
+/* sin(pi t) and cos(pi t) of two arguments at once in packed FP32 (the
+ * .f32x2 operations of sm_100 on), for |t| < 2^20.  Reduction: n = rint(2t)
+ * by adding 1.5 x 2^23 (which rounds to an integer and leaves n in the low
+ * bits of the sum), r = t - n/2 in [-1/4, 1/4] exactly (one FMA); then
+ * sin(pi r) = r P(r^2) and cos(pi r) = 1 + r^2 Q(r^2) with P, Q of degree 3,
+ * their coefficients fitted for this kernel by weighted least squares on 4000
+ * Chebyshev nodes of [0, 1/4] (relative error of the sine, absolute of the
+ * cosine), and n quarter turns.  Error within 8e-8 (against float64 sin and
+ * cos of pi t over |t| <= 300, six million points). */
+__device__ __forceinline__ void sincospi2(float2 t, float2 &sn, float2 &cs)
+{
+	const float MAGIC = 12582912.0f;
+	const float2 u = __fadd2_rn(__fadd2_rn(t, t), make_float2(MAGIC, MAGIC));
+	const float2 n = __fadd2_rn(u, make_float2(-MAGIC, -MAGIC));
+	const float2 r = __ffma2_rn(n, make_float2(-0.5f, -0.5f), t);
+	const float2 z = __fmul2_rn(r, r);
+	float2 p = __ffma2_rn(z, make_float2(-0.5890136361122131f, -0.5890136361122131f),
+			make_float2(2.5497612953186035f, 2.5497612953186035f));
+	p = __ffma2_rn(p, z, make_float2(-5.167707920074463f, -5.167707920074463f));
+	p = __ffma2_rn(p, z, make_float2(3.1415927410125732f, 3.1415927410125732f));
+	float2 q = __ffma2_rn(z, make_float2(0.2314295470714569f, 0.2314295470714569f),
+			make_float2(-1.3350584506988525f, -1.3350584506988525f));
+	q = __ffma2_rn(q, z, make_float2(4.0587077140808105f, 4.0587077140808105f));
+	q = __ffma2_rn(q, z, make_float2(-4.934802055358887f, -4.934802055358887f));
+	sn = __fmul2_rn(p, r);
+	cs = __ffma2_rn(q, z, make_float2(1.0f, 1.0f));
+	quarter_turns(sn.x, cs.x, __float_as_uint(u.x));
+	quarter_turns(sn.y, cs.y, __float_as_uint(u.y));
+}
+
+/* Pairs P0 .. P1 - 1 of this thread's half of a sample's encoded inputs:
+ * the half is chunks C0 .. C0 + 13 of the 27 (chunk c = 3v + k holds the
+ * (sin, cos) pairs of bands 4k .. 4k + 3 of input v; the bias pair, chunk
+ * 27, is the constant block), from inputs C0/3 .. C0/3 + 4 (xv), two chunks
+ * (a pair) at a time in packed FP32.  Band 4k from sincospi2 (exact
+ * argument scaling), the next three by angle doubling, sin 2a = 2 sin a cos
+ * a and cos 2a = 1 - 2 sin^2 a: 0.011 % of the features then round to
+ * another BF16 value than the exact ones' (0.009 % from correctly rounded
+ * bases). */
+template <int C0, int P0, int P1>
+__device__ __forceinline__ void tc_encode_pairs(unsigned char *A1, int row, const float (&xv)[TC_XH])
+{
+	const int v0 = C0 / 3;      /* the first input of this half: 0 or 4 */
+	#pragma unroll
+	for(int p = P0; p < P1; p++) {
+		const int ca = C0 + 2 * p, cb = ca + 1 < NRC_F / 8 ? ca + 1 : ca;
+		float2 sn, cs;
+		sincospi2(__fmul2_rn(make_float2(xv[ca / 3 - v0], xv[cb / 3 - v0]),
+				make_float2((float)(1 << (4 * (ca % 3))), (float)(1 << (4 * (cb % 3))))), sn, cs);
+		uint32_t qa[4], qb[4];
+		#pragma unroll
+		for(int b = 0; b < 4; b++) {
+			qa[b] = pack_bf16(sn.x, cs.x);
+			qb[b] = pack_bf16(sn.y, cs.y);
+			if(b < 3) {
+				const float2 m = __fmul2_rn(sn, make_float2(-2.0f, -2.0f));
+				const float2 s2 = __fmul2_rn(__fadd2_rn(sn, sn), cs);
+				cs = __ffma2_rn(m, sn, make_float2(1.0f, 1.0f));
+				sn = s2;
+			}
+		}
+		*reinterpret_cast<uint4 *>(A1 + ca * TC_CHUNK + row * 16) = make_uint4(qa[0], qa[1], qa[2], qa[3]);
+		if(cb != ca) *reinterpret_cast<uint4 *>(A1 + cb * TC_CHUNK + row * 16) = make_uint4(qb[0], qb[1], qb[2], qb[3]);
+	}
+}
+
+template <int P0, int P1>
+__device__ __forceinline__ void tc_encode_part(int hf, unsigned char *A1, int row, const float (&xv)[TC_XH])
+{
+	if(hf) tc_encode_pairs<NRC_FP / 16, P0, P1>(A1, row, xv);
+	else tc_encode_pairs<0, P0, P1>(A1, row, xv);
+}
+
+/* the inputs of half hf of row `row` (zeros past n) */
+__device__ __forceinline__ void tc_inputs(float (&xv)[TC_XH], const float *x, int n, int row, int hf)
+{
+	#pragma unroll
+	for(int k = 0; k < TC_XH; k++) xv[k] = row < n ? x[(size_t)row * 9 + 4 * hf + k] : 0.0f;
+}
+
+/* byte offset of element row r, 8-element K-chunk c in the row-group-major layout of a tile with kc chunks */
+__device__ __forceinline__ uint32_t tc_canon(int r, int c, int kc) { return (uint32_t)(((r >> 3) * kc + c) * 128 + (r & 7) * 16); }
+
+/* a weight image [rows][ld] (BF16) into the row-group-major layout of kc
+ * K-chunks: its first ks chunks, then in chunk ks the row's bias as a BF16
+ * pair (hi, lo: b = hi + lo to 2^-17) that multiplies the operand's constant
+ * pair (1, 1), the rest zero; rows beyond `rows` up to `rows_pad` zero */
 __device__ __forceinline__ void tc_weights(unsigned char *dst, const __nv_bfloat16 *src, int rows, int rows_pad, int ld, int ks, int kc,
 		const float *bias)
 {
@@ -537,19 +639,15 @@ __device__ __forceinline__ uint32_t relu_bf16x2(float lo, float hi)
 }
 
 /* half `hf` (32 columns) of the hidden activations of the calling thread's
- * row (the bias came with the product): ReLU, BF16, canonical layout (10
- * K-chunks, this half's 4) */
-__device__ __forceinline__ void tc_hidden(unsigned char *H, int row, int hf, const float (&v)[32])
+ * row (the bias came with the product): ReLU and BF16, into columns 16 hf ..
+ * 16 hf + 15 of the next layer's operand in TMEM (ta: the operand's first
+ * column in the thread's lane quarter) */
+__device__ __forceinline__ void tc_hidden(uint32_t ta, int hf, const float (&v)[32])
 {
+	uint32_t q[16];
 	#pragma unroll
-	for(int c = 0; c < 4; c++) {
-		uint4 q;
-		q.x = relu_bf16x2(v[8 * c + 0], v[8 * c + 1]);
-		q.y = relu_bf16x2(v[8 * c + 2], v[8 * c + 3]);
-		q.z = relu_bf16x2(v[8 * c + 4], v[8 * c + 5]);
-		q.w = relu_bf16x2(v[8 * c + 6], v[8 * c + 7]);
-		*reinterpret_cast<uint4 *>(H + tc_canon(row, hf * 4 + c, TC_KH / 8)) = q;
-	}
+	for(int i = 0; i < 16; i++) q[i] = relu_bf16x2(v[2 * i], v[2 * i + 1]);
+	tc_st16(ta + (uint32_t)(hf * 16), q);
 }
 
 template <int MODE>
@@ -566,89 +664,92 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_nrc_forward_tc(NrcDev net, in
 	tc_weights(tsm + TC_W2, net.w2, 64, 64, LDH, 8, TC_KH / 8, net.bias + 64);
 	tc_weights(tsm + TC_W3, net.w3, 64, 64, LDH, 8, TC_KH / 8, net.bias + 128);
 	tc_weights(tsm + TC_W4, net.w4, 64, 64, LDH, 8, TC_KH / 8, net.bias + 192);
-	tc_weights(tsm + TC_W5, net.w5, NRC_O, 16, LDH, 8, TC_KH / 8, net.bias + 256);
+	tc_weights(tsm + TC_W5, net.w5, NRC_O, 8, LDH, 8, TC_KH / 8, net.bias + 256);
+	for(int i = threadIdx.x; i < TC_CHUNK / 16; i += blockDim.x)
+		*reinterpret_cast<uint4 *>(tsm + TC_CONST + i * 16) = make_uint4(pack_bf16(1.0f, 1.0f), 0u, 0u, 0u);
 	/* group g: warps 8g .. 8g + 7; a warp's lane quarter (warp mod 4) gives
 	 * its rows, its half (hf) the features and accumulator columns it takes */
 	const int warp = threadIdx.x >> 5, g = warp >> 3, hf = (warp >> 2) & 1;
 	const int tid = ((warp & 3) << 5) | (threadIdx.x & 31);
 	const bool leader = (threadIdx.x & (TC_GROUP_THREADS - 1)) == 0;
-	unsigned char *gbase = tsm + TC_GROUP0 + g * TC_GROUP_BYTES;
-	const uint32_t mbar = sbase + TC_GROUP0 + g * TC_GROUP_BYTES + TC_MBAR;
-	uint32_t *tslot = reinterpret_cast<uint32_t *>(tsm + TC_TMEM_SLOT);
+	unsigned char *A1 = tsm + TC_GROUP0 + g * TC_GROUP_BYTES;
+	const uint32_t sA1 = sbase + TC_GROUP0 + g * TC_GROUP_BYTES;
+	const uint32_t mbar = sbase + TC_MBAR + 8 * g;
 	if(leader) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(mbar) : "memory");
-	/* the hidden operand's chunks 8 and 9: the bias pair (1, 1), then zeros */
-	*reinterpret_cast<uint4 *>(gbase + TC_H + tc_canon(tid, 8 + hf, TC_KH / 8)) =
-			make_uint4(hf ? 0u : pack_bf16(1.0f, 1.0f), 0u, 0u, 0u);
 	if(warp == 0) {
 		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
 				:: "r"(sbase + TC_TMEM_SLOT), "r"((uint32_t)TC_TMEM_COLS) : "memory");
 		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
 	}
-	/* the weights are read by the tensor cores (async proxy) */
+	/* the weights and constants are read by the tensor cores (async proxy) */
 	proxy_fence();
 	tc_fence_before();
 	__syncthreads();
 	tc_fence_after();
-	const uint32_t tmem = *tslot;
-	const uint32_t tD = tmem + (uint32_t)(g * 128), tO = tD + 64;
+	const uint32_t tmem = *reinterpret_cast<const uint32_t *>(tsm + TC_TMEM_SLOT);
 	const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
-	const uint32_t sA1 = sbase + TC_GROUP0 + g * TC_GROUP_BYTES + TC_A1, sH = sA1 + (TC_H - TC_A1);
-	const uint32_t sW1 = sbase + TC_W1, sW5 = sbase + TC_W5;
-	unsigned char *A1 = gbase + TC_A1, *H = gbase + TC_H;
+	const uint32_t tD = tmem + (uint32_t)(g * 128) + TC_TD, tA = tmem + (uint32_t)(g * 128) + TC_TA, tO = tmem + (uint32_t)(g * 128) + TC_TO;
+	const uint32_t sW1 = sbase + TC_W1, sW5 = sbase + TC_W5, sK = sbase + TC_CONST;
 	const uint32_t id64 = tc_idesc(128, 64), id16 = tc_idesc(128, 16);
-	uint32_t phase = 0;
-	bool ok = true;
-	int ntiles = (n + 127) >> 7;
-	/* the inputs of this thread's sample in its group's next tile, loaded one
-	 * tile ahead so that the loads wait under the current tile's layers */
-	float xn[9];
-	{
-		int row = (blockIdx.x * 2 + g) * 128 + tid;
-		#pragma unroll
-		for(int k = 0; k < 9; k++) xn[k] = row < n ? x[(size_t)row * 9 + k] : 0.0f;
+	if(hf == 0) {
+		/* the hidden operand's last K step: the bias pair (1, 1), then zeros */
+		uint32_t q[16] = {pack_bf16(1.0f, 1.0f)};
+		tc_st16(tA + lane_off + 32, q);
 	}
-	for(int tile = blockIdx.x * 2 + g; tile < ntiles && ok; tile += gridDim.x * 2) {
-		int row = tile * 128 + tid;
-		float xv[9];
+	uint32_t phase = 0;
+	bool ok = true;        /* this thread's waits so far */
+	bool agreed = true;    /* the group's, at its last barrier */
+	const int ntiles = (n + 127) >> 7, stride = gridDim.x * TC_NG;
+	/* The encoding of a group's next tile runs under the MMAs of the
+	 * current tile's layers 2-5 (which read the hidden operand, not the
+	 * features): a quarter of it after each of their issues.  xv holds the
+	 * inputs of the tile to encode next. */
+	int tile = blockIdx.x * TC_NG + g;
+	float xv[TC_XH];
+	tc_inputs(xv, x, n, tile * 128 + tid, hf);
+	if(tile < ntiles) tc_encode_part<0, 7>(hf, A1, tid, xv);
+	for(; tile < ntiles; tile += stride) {
+		const int row = tile * 128 + tid;
+		const bool more = tile + stride < ntiles;
+		tc_inputs(xv, x, n, row + stride * 128, hf);
 		#pragma unroll
-		for(int k = 0; k < 9; k++) xv[k] = xn[k];
-		{
-			int nrow = row + gridDim.x * 2 * 128;
-			#pragma unroll
-			for(int k = 0; k < 9; k++) xn[k] = nrow < n ? x[(size_t)nrow * 9 + k] : 0.0f;
-		}
-		/* encoded inputs of this thread's sample: its half of the 28 chunks
-		 * of 4 (sin, cos) pairs */
-		for(int c = hf * (NRC_FP / 16); c < (hf + 1) * (NRC_FP / 16); c++)
-			*reinterpret_cast<uint4 *>(A1 + tc_canon(tid, c, NRC_FP / 8)) = tc_encode_chunk(xv, c);
-		/* five layers: MMAs by one thread, epilogues by all */
-		for(int l = 0; l < 5 && ok; l++) {
+		for(int l = 0; l < 5; l++) {
 			proxy_fence();
 			tc_fence_before();
-			group_sync(g);
+			agreed = group_all(g, ok);
+			if(!agreed) break;
 			if(leader) {
 				tc_fence_after();
 				if(l == 0) {
-					for(int j = 0; j < NRC_FP / 16; j++)
-						tc_mma(tD, tc_desc(sA1 + j * 256, 128, (NRC_FP / 8) * 128), tc_desc(sW1 + j * 256, 128, (NRC_FP / 8) * 128), id64, j);
-				} else if(l < 4) {
-					const uint32_t sW = sbase + TC_W2 + (uint32_t)(l - 1) * (TC_W3 - TC_W2);   /* W2, W3, W4 back to back */
-					for(int j = 0; j < TC_KH / 16; j++)
-						tc_mma(tD, tc_desc(sH + j * 256, 128, TC_KH / 8 * 128), tc_desc(sW + j * 256, 128, TC_KH / 8 * 128), id64, j);
+					for(int j = 0; j < NRC_FP / 16 - 1; j++)
+						tc_mma(tD, tc_desc(sA1 + 2 * j * TC_CHUNK, TC_CHUNK, 128), tc_desc(sW1 + j * 256, 128, (NRC_FP / 8) * 128), id64, j);
+					/* the last K step: chunk 26, then the constant block's bias pairs */
+					const uint32_t a = sA1 + (NRC_F / 8 - 1) * TC_CHUNK;
+					tc_mma(tD, tc_desc(a, sK - a, 128), tc_desc(sW1 + (NRC_FP / 16 - 1) * 256, 128, (NRC_FP / 8) * 128), id64, 1);
 				} else {
+					const uint32_t sW = l < 4 ? sbase + TC_W2 + (uint32_t)(l - 1) * (TC_W3 - TC_W2) : sW5;   /* W2, W3, W4 back to back */
+					const uint32_t td = l < 4 ? tD : tO, id = l < 4 ? id64 : id16;
 					for(int j = 0; j < TC_KH / 16; j++)
-						tc_mma(tO, tc_desc(sH + j * 256, 128, TC_KH / 8 * 128), tc_desc(sW5 + j * 256, 128, TC_KH / 8 * 128), id16, j);
+						tc_mma_ta(td, tA + (uint32_t)(8 * j), tc_desc(sW + j * 256, 128, TC_KH / 8 * 128), id, j);
 				}
 				tc_commit(mbar);
 			}
-			ok = group_all(g, tc_wait(mbar, phase));
-			if(!ok) break;      /* phase stays the one still outstanding */
+			if(more) {
+				if(l == 1) tc_encode_part<0, 2>(hf, A1, tid, xv);
+				else if(l == 2) tc_encode_part<2, 4>(hf, A1, tid, xv);
+				else if(l == 3) tc_encode_part<4, 6>(hf, A1, tid, xv);
+				else if(l == 4) tc_encode_part<6, 7>(hf, A1, tid, xv);
+			}
+			if(!tc_wait(mbar, phase)) {
+				ok = false;     /* phase stays the one still outstanding */
+				continue;
+			}
 			phase ^= 1u;
 			tc_fence_after();
 			if(l < 4) {
 				float v[32];
 				tc_ld32(tD + lane_off + (uint32_t)(hf * 32), v);
-				tc_hidden(H, tid, hf, v);
+				tc_hidden(tA + lane_off, hf, v);
 			} else if(hf == 0) {
 				float v[16];
 				tc_ld16(tO + lane_off, v);
@@ -668,11 +769,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_nrc_forward_tc(NrcDev net, in
 				}
 			}
 		}
+		if(!agreed) break;
 	}
-	if(!ok) {
-		atomicOr(err, 1u);
-		/* what was committed may still be running: a last bounded wait */
-		tc_wait(mbar, phase);
+	/* the waits of the group's last layer */
+	if(agreed) agreed = group_all(g, ok);
+	if(!agreed) {
+		if(leader) atomicOr(err, 1u);
+		/* what was committed may still be running: a last bounded wait by
+		 * the threads whose wait ran out (they hold its phase) */
+		if(!ok) tc_wait(mbar, phase);
 	}
 	tc_fence_before();
 	__syncthreads();
@@ -1066,11 +1171,11 @@ int nrc_ensure_ready(uint64_t seed, cudaStream_t s)
 }
 
 /* CTAs of the tensor-core forward for up to n samples: one per SM at
- * most, two 128-sample tiles in flight each */
+ * most, TC_NG 128-sample tiles in flight each */
 static int tc_grid(int n)
 {
 	int tiles = (n + 127) / 128;
-	int blocks = (tiles + 1) / 2;
+	int blocks = (tiles + TC_NG - 1) / TC_NG;
 	int cap = g_nrc.nsm > 0 ? g_nrc.nsm : 152;
 	if(blocks > cap) blocks = cap;
 	return blocks < 1 ? 1 : blocks;
@@ -1224,6 +1329,26 @@ int sray_nrc_infer(int n, const float *x, float *y, void *stream)
 	cudaStream_t s = (cudaStream_t)stream;
 	int r = nrc_infer(n, x, y, s);
 	if(!r) { cudaError_t e = cudaStreamSynchronize(s); if(e != cudaSuccess) r = nrc_fail(e, "inference"); }
+	if(!r) r = nrc_device_error(s);
+	return nrc_err_ret(r);
+}
+
+int sray_nrc_infer_async(int n, const float *x, float *y, void *stream)
+{
+	std::lock_guard<std::mutex> lk(g_nrc_mu);
+	if(n < 0 || (n > 0 && (!x || !y))) { g_nrc.err = "bad arguments"; return nrc_err_ret(SRAY_EINVAL); }
+	if(!g_nrc.ready) { g_nrc.err = "radiance cache not initialised"; return nrc_err_ret(SRAY_ESTATE); }
+	return nrc_err_ret(nrc_infer(n, x, y, (cudaStream_t)stream));
+}
+
+int sray_nrc_check(void *stream)
+{
+	std::lock_guard<std::mutex> lk(g_nrc_mu);
+	if(!g_nrc.ready) return 0;
+	cudaStream_t s = (cudaStream_t)stream;
+	int r = 0;
+	cudaError_t e = cudaStreamSynchronize(s);
+	if(e != cudaSuccess) r = nrc_fail(e, "inference");
 	if(!r) r = nrc_device_error(s);
 	return nrc_err_ret(r);
 }

@@ -9,7 +9,8 @@ namespace sray {
 
 /* allocate and, the first time, initialise the network from `seed` */
 int nrc_ensure_ready(uint64_t seed, cudaStream_t s);
-/* y[n][3] = network(x[n][9]); x = position scaled to the scene box, normal, direction */
+/* y[n][3] = network(x[n][9]); x = position scaled to the scene box, normal,
+ * direction (the encoding's argument reduction holds for |x| <= 4096) */
 int nrc_infer(int n, const float *x, float *y, cudaStream_t s);
 /* the renderer's queries: acc[slot] += w.rgb * max(network(x[i]), 0) for
  * i < *count (at most cap), slot = the int in w[i].w */

@@ -23,7 +23,7 @@ EXPORTS = ["sray_default_opts", "sray_gpu_init", "sray_gpu_set_opts", "sray_gpu_
            "sray_gpu_set_tuning", "sray_gpu_autotune", "sray_gpu_set_profiling", "sray_gpu_kernel_times", "sray_gpu_last_error",
            "sray_gpu_shutdown", "sray_gpu_set_faults", "sray_gpu_upload_scene", "sray_gpu_load_scene_set",
            "sray_gpu_autotune_batch", "sray_nrc_reset", "sray_nrc_set_params", "sray_nrc_get_params", "sray_nrc_infer",
-           "sray_nrc_gradients", "sray_nrc_train", "sray_nrc_last_error"]
+           "sray_nrc_infer_async", "sray_nrc_check", "sray_nrc_gradients", "sray_nrc_train", "sray_nrc_last_error"]
 
 NRC_PARAMS = 26563
 
@@ -144,6 +144,8 @@ def load_library():
     L.sray_nrc_set_params.argtypes = [vp, ip]
     L.sray_nrc_get_params.argtypes = [vp, ip]
     L.sray_nrc_infer.argtypes = [ip, vp, vp, vp]
+    L.sray_nrc_infer_async.argtypes = [ip, vp, vp, vp]
+    L.sray_nrc_check.argtypes = [vp]
     L.sray_nrc_gradients.argtypes = [ip, vp, vp, vp, vp, vp]
     L.sray_nrc_train.argtypes = [ip, vp, vp, vp, vp]
     L.sray_nrc_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
@@ -177,8 +179,14 @@ class RadianceCache:
         self._chk(self.L.sray_nrc_get_params(_ptr(p), p.size))
         return p
 
-    def infer(self, x, y, stream=None):
-        self._chk(self.L.sray_nrc_infer(x.shape[0], _ptr(x), _ptr(y), _stream(stream)))
+    def infer(self, x, y, stream=None, sync=True):
+        """y = network(x); with sync=False the launch is only enqueued and
+        check() reports a device-side failure."""
+        f = self.L.sray_nrc_infer if sync else self.L.sray_nrc_infer_async
+        self._chk(f(x.shape[0], _ptr(x), _ptr(y), _stream(stream)))
+
+    def check(self, stream=None):
+        self._chk(self.L.sray_nrc_check(_stream(stream)))
 
     def gradients(self, x, t, grad, loss, stream=None):
         self._chk(self.L.sray_nrc_gradients(x.shape[0], _ptr(x), _ptr(t), _ptr(grad), _ptr(loss), _stream(stream)))

@@ -52,6 +52,18 @@ def test_forward_matches_oracle(cache):
         assert np.sqrt(np.mean((got - ref) ** 2)) / scale < 2e-3
 
 
+def test_async_inference_matches_synchronous(cache):
+    rng = np.random.default_rng(14)
+    cache.set_params(nrc.init_params(24))
+    x = torch.tensor(inputs(rng, 50000), device="cuda")
+    y0 = torch.empty((50000, 3), dtype=torch.float32, device="cuda")
+    y1 = torch.full((50000, 3), float("nan"), dtype=torch.float32, device="cuda")
+    cache.infer(x, y0)
+    cache.infer(x, y1, sync=False)
+    cache.check()
+    assert torch.equal(y0, y1)
+
+
 def test_gradients_match_oracle(cache):
     rng = np.random.default_rng(12)
     p = nrc.init_params(22)
