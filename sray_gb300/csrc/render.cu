@@ -47,6 +47,20 @@ static __device__ __forceinline__ int warp_alloc(int *counter, int n)
 /* ---------------------------------------------------------------- */
 /* primary rays of samples [s0, s0 + width) of every active pixel; the ray's
  * accumulator slot is (active index * width + sample - s0) */
+/* The pixel of active slot a: the batch's list when there is one, else --
+ * the first batch -- for a single frame of tw x th pixels the pixels in
+ * bands of four rows, column-major within a band, so that the 32 rays of a
+ * warp leave from an 8 x 4 patch (and the rays they spawn keep that
+ * order); tw = 0: slot a is pixel a (a batch of jobs) */
+__device__ __forceinline__ int slot_pixel(const int *active, int a, int tw, int th)
+{
+	if(active) return active[a];
+	if(tw <= 0) return a;
+	const int band = a / (4 * tw), r = a - band * 4 * tw;
+	const int hb = th - 4 * band < 4 ? th - 4 * band : 4;
+	return (4 * band + r % hb) * tw + r / hb;
+}
+
 __global__ void k_camera(DScene S, const int *active, int a0, int na, int s0, int width, RayQueue q, float4 *acc,
 		DevCounters *ctr)
 {
@@ -55,7 +69,7 @@ __global__ void k_camera(DScene S, const int *active, int a0, int na, int s0, in
 	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 		int a = a0 + i / width, j = i - (i / width) * width;
 		int slot = a0 * width + i;
-		int p = active ? active[a] : a;
+		int p = slot_pixel(active, a, S.njobs > 0 ? 0 : S.width, S.height);
 		int sample = s0 + j;
 		int W = S.width, Hh = S.height, lp = p, t0 = S.t0, cam_base = 0;
 		float cam_f = S.cam_f, xsz = S.cam_xsz, ysz = S.cam_ysz;
@@ -1412,12 +1426,12 @@ __global__ void __launch_bounds__(GATHER_WARPS * 32, 3) k_gather_points(DScene S
  * (src/render.cc:199-244): after sample i (counting from 1), if i >= min
  * and i > 1 and the sample variance is below max_var the pixel stops; later
  * samples of the batch were speculative and are discarded */
-__global__ void k_finish(const int *active, const int *n_active_p, int s0, int width, const float4 *acc, float4 *hist,
+__global__ void k_finish(const int *active, int tw, int th, const int *n_active_p, int s0, int width, const float4 *acc, float4 *hist,
 		float4 *sums, int max_samples, int min_samples, float max_var, int *next, int *next_count, float4 *fb, int *spp)
 {
 	int n = *n_active_p;
 	for(int a = blockIdx.x * blockDim.x + threadIdx.x; a < n; a += gridDim.x * blockDim.x) {
-		int p = active ? active[a] : a;
+		int p = slot_pixel(active, a, tw, th);
 		float4 sum = s0 == 0 ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : sums[p];
 		bool done = false;
 		int i1 = s0;
@@ -3024,7 +3038,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 		if(int r = join_side()) return r;
 		if(int r = nrc_batch_done(b, s)) return r;
 		CK(cudaMemsetAsync(next_count, 0, sizeof(int), s), "reset next active");
-		LAUNCH(*this, "finish", s, k_finish<<<grid_for(n_active, 256), 256, 0, s>>>(act, act_count, s0, width, acc.as<float4>(),
+		LAUNCH(*this, "finish", s, k_finish<<<grid_for(n_active, 256), 256, 0, s>>>(act, S.njobs > 0 ? 0 : S.width, S.height, act_count, s0, width, acc.as<float4>(),
 				hist.as<float4>(), sums.as<float4>(), maxs, opt.min_samples, opt.max_var, next_list, next_count, fbd,
 				spp.as<int>()));
 		stats.samples += (int64_t)n_active * width;
