@@ -183,6 +183,231 @@ __global__ void __launch_bounds__(SRAY_TRACE_THREADS, 8) k_trace(DScene S, RayQu
 	if(!HYB && n > 0 && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ctr->bvh_fallbacks, (unsigned long long)n);
 }
 
+/* Closest hits of coherent rays -- a pass of camera rays, the 32 of a warp
+ * from an 8 x 4 pixel patch -- by one traversal per warp: the warp walks the
+ * two-level hierarchy together, opening a node when any lane's widened box
+ * test reaches one of its children and taking the reached children nearest
+ * first by their smallest entry distance over the lanes; each lane tests its
+ * own ray against the boxes, objects and faces the warp visits, and enters
+ * an instance only when its own ray enters the instance's mesh box within
+ * its best distance.  A lane's result equals the thread-per-ray
+ * traversal's: a box, object or face its own traversal would not have
+ * reached holds no candidate within the lane's best distance (the box tests
+ * are conservative and bounded by the best so far), so the candidates at
+ * the final distance, the tie flag and the octree confirmation are the
+ * same; a ray that traversal hands to the octrees (a tie, an unconfirmed
+ * hit, a mesh without a hierarchy) goes to the octree retrace here too.  The
+ * warp's stack (entries and their smallest entry distance) is in shared
+ * memory; every branch around a warp vote is the same for all lanes.
+ * Returns 0 when the octrees must decide, else 1 with the closest hit in h
+ * (h.obj -1: none). */
+__device__ __forceinline__ int ford(float x)
+{
+	int b = __float_as_int(x);
+	return b >= 0 ? b : b ^ 0x7fffffff;
+}
+
+__device__ __forceinline__ float ford_inv(int b) { return __int_as_float(b >= 0 ? b : b ^ 0x7fffffff); }
+
+__device__ __forceinline__ int packet_trace(const DScene &S, bool valid, V3 wo, V3 wd, int time, int *st_node, float *st_te,
+		Hit &h, int *overflow)
+{
+	const unsigned FULL = 0xffffffffu;
+	const int lane = threadIdx.x & 31;
+	h.t = FLT_MAX;
+	h.obj = -1;
+	h.prim = -1;
+	h.tie = 0;
+	const int2 roots = scene_roots(S, -1);
+	if(roots.x < 0) return 1;
+	if(roots.y < 0) return 0;
+	const int ti = time_index(S, time);
+	const RayT wr = make_ray(wo, wd);
+	const DevNode &sroot = S.snodes[roots.x];
+	const RayC wc = make_rayc(wr, box_bound(sroot.mn, sroot.mx));
+	RayT r = wr;
+	RayC rc = wc;
+	float best = FLT_MAX;
+	int bobj = -1, bprim = -1, bslot = -1;
+	bool eq = false, undecided = false;
+	bool live = valid;     /* the lane takes part in the current instance (or the object level) */
+	int sp = 0, inst_base = 0, iobj = -1;
+	bool inst = false;
+	int cur = roots.y;
+	for(;;) {
+		if(cur == BVH_NONE) {
+			bool found = false;
+			while(sp > 0) {
+				const int k = sp - 1;
+				if(inst && k < inst_base) {   /* the instance's entries are done */
+					inst = false;
+					iobj = -1;
+					r = wr;
+					rc = wc;
+					live = valid;
+				}
+				sp = k;
+				if(__any_sync(FULL, live && st_te[k] <= best)) {
+					cur = st_node[k];
+					found = true;
+					break;
+				}
+			}
+			if(!found) break;
+		}
+		if(!inst && cur < 0) {
+			/* object ~cur */
+			const int o = ~cur;
+			cur = BVH_NONE;
+			const DevObj ob = S.objs[o];
+			const RayT orr = object_ray(S, o, ti, wo, wd);
+			if(ob.type != 2) {
+				float t;
+				if(valid && (ob.type == 0 ? sphere_hit(orr, ob.rad, S.eps, t) : cylinder_hit(orr, ob.rad, ob.start, ob.end, S.eps, t))
+						&& t <= best) {
+					if(t < best) {
+						best = t;
+						bobj = o;
+						bprim = 0;
+						bslot = -1;
+						eq = false;
+					} else if(o != bobj || bprim != 0) {
+						eq = true;
+					}
+				}
+				continue;
+			}
+			if(ob.mesh_root < 0) continue;
+			if(ob.bvh_root < 0) {
+				undecided = undecided || valid;
+				continue;
+			}
+			float te = 0.0f;
+			const DevNode &rn = S.mnodes[ob.mesh_root];
+			const bool enter = valid && box_hit(rn.mn, rn.mx, orr, te) && !SRAY_PRUNE(te, best);
+			if(!__any_sync(FULL, enter)) continue;
+			r = orr;
+			rc = make_rayc(orr, box_bound(rn.mn, rn.mx));
+			inst = true;
+			inst_base = sp;
+			iobj = o;
+			live = enter;
+			cur = ob.bvh_root;
+			continue;
+		}
+		if(inst && cur < 0) {
+			/* a leaf of the mesh hierarchy: its faces, for the lanes in the instance */
+			const unsigned v = ~(unsigned)cur;
+			cur = BVH_NONE;
+			const int start = (int)(v >> 4), cnt = (int)(v & 15u);
+			const float4 *tp = reinterpret_cast<const float4 *>(S.btris + start);
+			for(int k = 0; k < cnt; k++) {
+				const float4 a = __ldg(tp + 3 * k), b = __ldg(tp + 3 * k + 1), c = __ldg(tp + 3 * k + 2);
+				float t;
+				if(!live || !tri_hit(a, b, c, r, S.eps, best, t)) continue;
+				const int prim = __ldg(S.bprim + start + k);
+				if(t < best) {
+					best = t;
+					bobj = iobj;
+					bprim = prim;
+					bslot = start + k;
+					eq = false;
+				} else if(iobj != bobj || prim != bprim) {
+					eq = true;
+				}
+			}
+			continue;
+		}
+		/* a node: the lanes' box tests, then the warp's smallest entry distance per child */
+		const float4 *np = reinterpret_cast<const float4 *>((inst ? S.bnodes : S.tnodes) + cur);
+		const NodePlanes pl = node_planes(np, rc);
+		const int4 ch = __ldg(reinterpret_cast<const int4 *>(np) + 6);
+		const float lim = fminf(best, 1.0f);
+		int ref[4] = {ch.x, ch.y, ch.z, ch.w};
+		float tn;
+		float key[4];
+		key[0] = (live && ref[0] != BVH_NONE && wide_box(rc, pl.nx.x, pl.ny.x, pl.nz.x, pl.fx.x, pl.fy.x, pl.fz.x, lim, tn)) ? tn : INFINITY;
+		key[1] = (live && ref[1] != BVH_NONE && wide_box(rc, pl.nx.y, pl.ny.y, pl.nz.y, pl.fx.y, pl.fy.y, pl.fz.y, lim, tn)) ? tn : INFINITY;
+		key[2] = (live && ref[2] != BVH_NONE && wide_box(rc, pl.nx.z, pl.ny.z, pl.nz.z, pl.fx.z, pl.fy.z, pl.fz.z, lim, tn)) ? tn : INFINITY;
+		key[3] = (live && ref[3] != BVH_NONE && wide_box(rc, pl.nx.w, pl.ny.w, pl.nz.w, pl.fx.w, pl.fy.w, pl.fz.w, lim, tn)) ? tn : INFINITY;
+		#pragma unroll
+		for(int k = 0; k < 4; k++) key[k] = ford_inv(__reduce_min_sync(FULL, ford(key[k])));
+#define SRAY_CSWAP(i, j) do { if(key[j] < key[i]) { float tk = key[i]; key[i] = key[j]; key[j] = tk; int tr_ = ref[i]; ref[i] = ref[j]; ref[j] = tr_; } } while(0)
+		SRAY_CSWAP(0, 1);
+		SRAY_CSWAP(2, 3);
+		SRAY_CSWAP(0, 2);
+		SRAY_CSWAP(1, 3);
+		SRAY_CSWAP(1, 2);
+#undef SRAY_CSWAP
+		if(key[0] == INFINITY) {
+			cur = BVH_NONE;
+			continue;
+		}
+		#pragma unroll
+		for(int k = 3; k >= 1; k--) {
+			if(key[k] == INFINITY) continue;
+			if(sp >= SRAY_STACK) {
+				*overflow = 1;
+				return 1;
+			}
+			if(lane == 0) {
+				st_node[sp] = ref[k];
+				st_te[sp] = key[k];
+			}
+			sp++;
+		}
+		__syncwarp(FULL);
+		cur = ref[0];
+	}
+	if(!valid) return 1;
+	if(undecided) return 0;
+	if(bobj < 0) return 1;
+	if(eq) return 0;
+	/* confirm against the octrees */
+	if(bslot >= 0 && !octree_reaches(S.mnodes, S.mprim, __ldg(S.bhome + bslot), object_ray(S, bobj, ti, wo, wd), bprim, best, true))
+		return 0;
+	if(!octree_reaches(S.snodes, S.sslots, __ldg(S.ohome + bobj), wr, bobj, best, true)) return 0;
+	h.t = best;
+	h.obj = bobj;
+	h.prim = bprim;
+	h.tie = 0;
+	return 1;
+}
+
+/* a pass of coherent closest-hit rays (one scene), a warp per 32 rays; the
+ * rays the octrees must decide are listed in fb as by k_trace */
+#ifndef SRAY_PACKET_BLOCKS
+#define SRAY_PACKET_BLOCKS 6     /* resident blocks per SM: 80 registers */
+#endif
+__global__ void __launch_bounds__(SRAY_TRACE_THREADS, SRAY_PACKET_BLOCKS) k_trace_packet(DScene S, RayQueue q, int4 *hits, DevCounters *ctr, int *fb)
+{
+	__shared__ int st_node[SRAY_TRACE_THREADS / 32][SRAY_STACK];
+	__shared__ float st_te[SRAY_TRACE_THREADS / 32][SRAY_STACK];
+	const int n = *q.count;
+	const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	int overflow = 0;
+	for(int base = (blockIdx.x * (SRAY_TRACE_THREADS / 32) + w) * 32; base < n; base += gridDim.x * SRAY_TRACE_THREADS) {
+		const int ri = base + lane;
+		const bool valid = ri < n;
+		float4 o = make_float4(0.0f, 0.0f, 0.0f, 0.0f), d = make_float4(0.0f, 0.0f, 1.0f, 0.0f);
+		int time = S.t0;
+		if(valid) {
+			o = q.o[ri];
+			d = q.d[ri];
+			time = q.meta[ri].w;
+		}
+		Hit h;
+		const int res = packet_trace(S, valid, mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), time, st_node[w], st_te[w], h, &overflow);
+		if(!valid) continue;
+		if(res == 0) {
+			fb[1 + atomicAdd(fb, 1)] = ri;
+			continue;
+		}
+		hits[ri] = make_int4(__float_as_int(h.t), h.obj, h.prim, h.tie);
+	}
+	if(overflow) atomicOr(&ctr->overflow, 1);
+}
+
 /* Closest hits with one warp per ray, for passes of few rays (the tails of
  * the shading tree: long mirror and glass chains, grazing rays), whose
  * launches otherwise last as long as one thread's chain of dependent node
@@ -2978,7 +3203,7 @@ int Renderer::render_pixels(long msec, float *fb, int fb_is_device, cudaStream_t
 			CK(cudaMemsetAsync(sqc, 0, sizeof(int), s), "reset shadow queue");
 			CK(sqb.ensure((size_t)n_rays * shadow_per_ray * sizeof(ShadowReq)), "shadow queue");
 			if(depth >= 1 && tune.sort_rays > 0 && n_rays >= tune.sort_rays && (r = sort_pass(cur, n_rays, s))) return r;
-			r = trace_rays(q[cur], n_rays, "trace", (prof_flags & 2) != 0, s);
+			r = trace_rays(q[cur], n_rays, "trace", (prof_flags & 2) != 0, s, depth == 0);
 			if(r) return r;
 			ShadeOut so;
 			so.qo = q[cur ^ 1];
@@ -3106,7 +3331,7 @@ int Renderer::queue_overflow(int count, int cap)
  * rays of q into hits: the hierarchy pass, then the octree pass over the
  * rays it listed */
 int Renderer::trace_rays_with(const DScene &D, const RayQueue &qq, int n, const char *name, bool count, cudaStream_t s,
-		int4 *hit_out, DevBuf &fb, DevCounters *c, bool short_blocks)
+		int4 *hit_out, DevBuf &fb, DevCounters *c, bool short_blocks, bool coherent)
 {
 	CK(fb.ensure(((size_t)n + 1) * sizeof(int)), "fallback list");
 	CK(cudaMemsetAsync(fb.p, 0, sizeof(int), s), "reset fallback list");
@@ -3114,6 +3339,11 @@ int Renderer::trace_rays_with(const DScene &D, const RayQueue &qq, int n, const 
 	 * instead of a capped grid that strides, so that its blocks free their
 	 * SMs for the frame's stream as they finish */
 	int g = short_blocks ? std::max(1, (n + 127) / 128) : grid_for(n, 128);
+	if(!count && coherent && D.nscenes <= 1 && n > tune.warp_rays) {
+		LAUNCH(*this, name, s, k_trace_packet<<<g, SRAY_TRACE_THREADS, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
+		LAUNCH(*this, "octree_retrace", s, k_trace<false, false><<<retrace_grid(), 128, 0, s>>>(D, qq, hit_out, c, fb.as<int>()));
+		return 0;
+	}
 	if(!count && n <= tune.warp_rays) {
 		/* a pass of few rays: one warp per ray */
 		LAUNCH(*this, name, s, k_trace_warp<<<grid_for(n, 4), 128, 0, s>>>(D, qq, hit_out, fb.as<int>()));
@@ -3182,9 +3412,9 @@ int Renderer::side_stream()
 	return 0;
 }
 
-int Renderer::trace_rays(const RayQueue &qq, int n, const char *name, bool count, cudaStream_t s)
+int Renderer::trace_rays(const RayQueue &qq, int n, const char *name, bool count, cudaStream_t s, bool coherent)
 {
-	return trace_rays_with(S, qq, n, name, count, s, hits.as<int4>(), fbl, ctr.as<DevCounters>());
+	return trace_rays_with(S, qq, n, name, count, s, hits.as<int4>(), fbl, ctr.as<DevCounters>(), false, coherent);
 }
 
 /* photon passes: the photon buffers and counters */
@@ -3886,7 +4116,7 @@ int sray_gpu_primary_hits(long msec, int *obj, int *prim, float *t, unsigned cha
 	if(e != cudaSuccess) { g_err = cudaGetErrorString(e); return SRAY_ECUDA; }
 	R.q[0].count = cnt + 0;
 	k_camera<<<grid_for(npix, 256), 256, 0, s>>>(R.S, nullptr, 0, npix, 0, 1, R.q[0], R.acc.as<float4>(), R.ctr.as<DevCounters>());
-	if(R.trace_rays(R.q[0], npix, "trace", false, s)) { g_err = R.err; return SRAY_ECUDA; }
+	if(R.trace_rays(R.q[0], npix, "trace", false, s, true)) { g_err = R.err; return SRAY_ECUDA; }
 	k_primary_hits<<<grid_for(npix, 256), 256, 0, s>>>(R.S, R.q[0], R.hits.as<int4>(), obj, prim, t, tie);
 	DevCounters hc;
 	e = cudaMemcpyAsync(&hc, R.ctr.p, sizeof hc, cudaMemcpyDeviceToHost, s);

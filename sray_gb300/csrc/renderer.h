@@ -294,9 +294,10 @@ struct Renderer {
 	int queue_overflow(int count, int cap);
 	int ensure_pqueue(int which, int cap);
 	int queue_alloc(DevBuf &buf, RayQueue &Q, int &qc, int cap);
-	int trace_rays(const RayQueue &q, int n, const char *name, bool count, cudaStream_t s);
+	/* coherent: a pass of camera rays (traced as warp packets when it is large) */
+	int trace_rays(const RayQueue &q, int n, const char *name, bool count, cudaStream_t s, bool coherent = false);
 	int trace_rays_with(const DScene &D, const RayQueue &q, int n, const char *name, bool count, cudaStream_t s, int4 *hit_out,
-			DevBuf &fb, DevCounters *c, bool short_blocks = false);
+			DevBuf &fb, DevCounters *c, bool short_blocks = false, bool coherent = false);
 	int photon_stream();
 	void fill_scene_desc();
 };
