@@ -3,7 +3,8 @@
  * One pixel sample of every active pixel is rendered per pass:
  *   k_camera    primary rays            Camera::get_primary_ray (src/camera.cc:119-142)
  *   k_trace     closest hits            Scene::cast_ray / Octree::intersect (src/scene.cc:764,
- *                                        src/octree.inl:201-241) with the intersectors
+ *                                        src/octree.inl:201-241) with the intersectors;
+ *                                        camera rays by k_trace_packet, a warp per 8 x 4 patch
  *   k_shade     Phong + shadows + spawn shade_phong / calc_lighting / shade_undef
  *                                        (src/shader.cc:36-283)
  *   k_gather    photon-map estimates    PhotonMap::irradiance_est / radiance_est (src/pmap.cc:109-178)
