@@ -207,6 +207,7 @@ __device__ bool gen_dir(const uint32_t *bits, sray_rng *s, V3 *out)
  * caustic map, map 1 the global one. */
 
 #define PHOTON_GUARD 4096   /* interactions per phase (loop bound of the oracle's tracer) */
+#define PHOTON_SORT_MIN (1 << 20)   /* photon passes of at least this many are sorted before they are traced */
 
 /* A job of the photon wavefront: one frame's two maps (a batch traces the
  * maps of all its jobs in one wavefront).  Its photons are the global
@@ -719,8 +720,13 @@ int photon_trace_jobs(Renderer &R, const DScene &base, const std::vector<PhotonJ
 	PS.njobs = PS.nscenes > 1 ? n : 0;
 	DevCounters *pctr = R.pctr.as<DevCounters>();
 	LAUNCH(R, "photon_emit", s, k_photon_emit<<<grid_n((int)all, 128), 128, 0, s>>>(PS, PSet, R.pq[0], pctr));
+	/* the emitted count (a photon whose direction sampling fails is not queued) */
+	PCK(cudaMemcpyAsync(R.pin + 8, R.pq[0].count, sizeof(int), cudaMemcpyDeviceToHost, s), "photon queue count");
+	PCK(cudaStreamSynchronize(s), "photon emission");
 	int cur = 0;
-	int n_live = (int)all;   /* upper bound until the first count is read */
+	int n_live = R.pin[8];
+	R.d2h += sizeof(int);
+	R.prof_collect();
 	bool finished = false;
 	for(int pass = 0; n_live > 0; pass++) {
 		if(pass >= 2 * PHOTON_GUARD + 4) return R.fail(SRAY_EDEVICE, "photon paths did not terminate");
@@ -739,6 +745,12 @@ int photon_trace_jobs(Renderer &R, const DScene &base, const std::vector<PhotonJ
 			cur ^= 1;
 			continue;
 		}
+		/* a large pass in the order of direction octant and origin cell: the
+		 * photons of a warp then leave from nearby points in similar
+		 * directions (the queue's order is arbitrary anyway: its slots come
+		 * from atomics, and each entry carries its photon's identity) */
+		if(n_live >= PHOTON_SORT_MIN)
+			if(int r = R.sort_photon_pass(cur, n_live, s)) return r;
 		if(launch_trace(R, PS, R.pq[cur], n_live, "photon_trace", s)) return SRAY_ECUDA;
 		LAUNCH(R, "photon_bounce", s, k_photon_bounce<<<grid_n(n_live, 128), 128, 0, s>>>(PS, PSet, R.pq[cur], R.phits.as<int4>(),
 				R.pq[cur ^ 1]));

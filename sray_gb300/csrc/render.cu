@@ -122,7 +122,8 @@ __device__ __forceinline__ unsigned spread7(unsigned v)
 	return v;
 }
 
-__global__ void k_ray_keys(RayQueue q, int n, float lx, float ly, float lz, float sx, float sy, float sz, unsigned *keys, unsigned *vals)
+__global__ void k_ray_keys(RayQueue q, int n, float lx, float ly, float lz, float sx, float sy, float sz, int kshift, unsigned *keys,
+		unsigned *vals)
 {
 	for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 		float4 o = q.o[i], d = q.d[i];
@@ -131,7 +132,7 @@ __global__ void k_ray_keys(RayQueue q, int n, float lx, float ly, float lz, floa
 		cy = cy < 0 ? 0 : (cy > 127 ? 127 : cy);
 		cz = cz < 0 ? 0 : (cz > 127 ? 127 : cz);
 		unsigned oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
-		keys[i] = (oct << 21) | spread7((unsigned)cx) | (spread7((unsigned)cy) << 1) | (spread7((unsigned)cz) << 2);
+		keys[i] = ((oct << 21) | spread7((unsigned)cx) | (spread7((unsigned)cy) << 1) | (spread7((unsigned)cz) << 2)) >> kshift;
 		vals[i] = (unsigned)i;
 	}
 }
@@ -2606,12 +2607,13 @@ int Renderer::ensure_pqueue(int which, int cap)
 /* the n rays of q[cur], sorted by direction octant and origin cell into the
  * spare queue, which then becomes q[cur] (the pass's queue and its
  * allocation swapped with the spare's) */
-int Renderer::sort_pass(int cur, int n, cudaStream_t s)
+int Renderer::sort_queue(RayQueue &Q, DevBuf &Qbuf, int &Qcap, RayQueue &T, DevBuf &Tbuf, int &Tcap, DevBuf &keysb, DevBuf &hist,
+		DevBuf &part, int n, int bits, const char *name, cudaStream_t s)
 {
 	if(n < 2 || sc.oct.nodes.empty()) return 0;
-	if(int r = queue_alloc(qsbuf, qs, qscap, q[cur].cap)) return r;
-	CK(rs_keys.ensure((size_t)n * 16), "ray sort keys");
-	unsigned *keys = rs_keys.as<unsigned>(), *vals = keys + n, *keys2 = keys + 2 * (size_t)n, *vals2 = keys + 3 * (size_t)n;
+	if(int r = queue_alloc(Tbuf, T, Tcap, Q.cap)) return r;
+	CK(keysb.ensure((size_t)n * 16), "ray sort keys");
+	unsigned *keys = keysb.as<unsigned>(), *vals = keys + n, *keys2 = keys + 2 * (size_t)n, *vals2 = keys + 3 * (size_t)n;
 	const Box &b = sc.oct.nodes[0].box;
 	float ext[3], lo[3];
 	for(int a = 0; a < 3; a++) {
@@ -2619,17 +2621,29 @@ int Renderer::sort_pass(int cur, int n, cudaStream_t s)
 		double e = b.mx[a] - b.mn[a];
 		ext[a] = e > 0.0 ? (float)(128.0 / e) : 0.0f;
 	}
-	LAUNCH(*this, "ray_sort", s, k_ray_keys<<<grid_for(n, 256), 256, 0, s>>>(q[cur], n, lo[0], lo[1], lo[2], ext[0], ext[1], ext[2],
-			keys, vals));
+	LAUNCH(*this, name, s, k_ray_keys<<<grid_for(n, 256), 256, 0, s>>>(Q, n, lo[0], lo[1], lo[2], ext[0], ext[1], ext[2],
+			24 - bits, keys, vals));
 	unsigned *sorted = nullptr;
-	if(int r = sort_pairs(*this, keys, vals, keys2, vals2, n, 24, rs_hist, rs_part, "ray_sort", s, &sorted)) return r;
-	LAUNCH(*this, "ray_sort", s, k_ray_permute<<<grid_for(n, 256), 256, 0, s>>>(q[cur], sorted, n, qs));
-	int *count = q[cur].count;
-	std::swap(q[cur], qs);
-	std::swap(qbuf[cur], qsbuf);
-	std::swap(qcap[cur], qscap);
-	q[cur].count = count;
+	if(int r = sort_pairs(*this, keys, vals, keys2, vals2, n, bits, hist, part, name, s, &sorted)) return r;
+	LAUNCH(*this, name, s, k_ray_permute<<<grid_for(n, 256), 256, 0, s>>>(Q, sorted, n, T));
+	int *count = Q.count;
+	std::swap(Q, T);
+	std::swap(Qbuf, Tbuf);
+	std::swap(Qcap, Tcap);
+	Q.count = count;
 	return 0;
+}
+
+int Renderer::sort_pass(int cur, int n, cudaStream_t s)
+{
+	return sort_queue(q[cur], qbuf[cur], qcap[cur], qs, qsbuf, qscap, rs_keys, rs_hist, rs_part, n, 24, "ray_sort", s);
+}
+
+int Renderer::sort_photon_pass(int cur, int n, cudaStream_t s)
+{
+	/* one radix pass: the direction octant and the origin's cell in a coarse
+	 * grid (the first pass's photons leave from the lights) */
+	return sort_queue(pq[cur], pqbuf[cur], pqcap[cur], pqs, pqsbuf, pqscap, ps_keys, ps_hist, ps_part, n, 8, "photon_ray_sort", s);
 }
 
 /* ---------------------------------------------------------------- */
@@ -4423,6 +4437,7 @@ void sray_gpu_shutdown(void)
 		&R.pw_jobs, &R.pw_prefix, &R.pw_scale, &R.pw_bits, &R.pw_cov, &R.pw_pix, &R.pw_out, &R.pw_valid,
 		&R.pw_part, &R.pw_tiles, &R.pw_bounds, &R.pw_offs, &R.pw_ph, &R.pw_sorted, &R.pw_grids, &R.pw_morton, &R.pw_cellbase,
 		&R.pw_keys, &R.pw_lin, &R.pw_cells, &R.pw_hist, &R.qsbuf, &R.rs_keys, &R.rs_hist, &R.rs_part, &R.sq2, &R.gq2, &R.fbs[0], &R.fbs[1],
+		&R.pqsbuf, &R.ps_keys, &R.ps_hist, &R.ps_part,
 		&R.nrc_qx, &R.nrc_qw, &R.nrc_rx, &R.nrc_rt, &R.nrc_ry, &R.nrc_regions};
 	if(R.ps) cudaStreamSynchronize(R.ps);
 	if(R.xs) cudaStreamSynchronize(R.xs);

@@ -157,11 +157,24 @@ struct Renderer {
 	RayQueue qs = {};
 	int qscap = 0;
 	int sort_pass(int cur, int n, cudaStream_t s);
+	/* queue Q's first n entries in the order of the top `bits` of their
+	 * 24-bit keys (direction octant over the Morton code of the origin's cell
+	 * in a 128^3 grid), through the scratch queue T (swapped with Q) and the
+	 * key, histogram and partial-sum buffers */
+	int sort_queue(RayQueue &Q, DevBuf &Qbuf, int &Qcap, RayQueue &T, DevBuf &Tbuf, int &Tcap, DevBuf &keysb, DevBuf &hist,
+			DevBuf &part, int n, int bits, const char *name, cudaStream_t s);
 	/* photon tracing has buffers and a stream of its own, so that it can run
 	 * beside the first bounce of a frame */
 	DevBuf pqbuf[2], phits, pfbl, pcounts, pctr;
 	RayQueue pq[2];
 	int pqcap[2] = {0, 0};
+	/* photon passes of at least PHOTON_SORT_MIN photons are sorted before
+	 * they are traced, with scratch of their own (the photon stream runs
+	 * beside the frame's) */
+	DevBuf pqsbuf, ps_keys, ps_hist, ps_part;
+	RayQueue pqs = {};
+	int pqscap = 0;
+	int sort_photon_pass(int cur, int n, cudaStream_t s);
 	cudaStream_t ps = nullptr;
 	int ps_priority = -1;      /* 1 when ps has the greatest priority */
 	cudaStream_t hs = nullptr; /* the frame's stream under stream_priority 2 */
