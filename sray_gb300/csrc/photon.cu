@@ -207,7 +207,7 @@ __device__ bool gen_dir(const uint32_t *bits, sray_rng *s, V3 *out)
  * caustic map, map 1 the global one. */
 
 #define PHOTON_GUARD 4096   /* interactions per phase (loop bound of the oracle's tracer) */
-#define PHOTON_SORT_MIN (1 << 20)   /* photon passes of at least this many are sorted before they are traced */
+#define PHOTON_SORT_MIN (1 << 20)   /* an emission pass of at least this many photons is sorted before it is traced */
 
 /* A job of the photon wavefront: one frame's two maps (a batch traces the
  * maps of all its jobs in one wavefront).  Its photons are the global
@@ -745,11 +745,12 @@ int photon_trace_jobs(Renderer &R, const DScene &base, const std::vector<PhotonJ
 			cur ^= 1;
 			continue;
 		}
-		/* a large pass in the order of direction octant and origin cell: the
-		 * photons of a warp then leave from nearby points in similar
-		 * directions (the queue's order is arbitrary anyway: its slots come
-		 * from atomics, and each entry carries its photon's identity) */
-		if(n_live >= PHOTON_SORT_MIN)
+		/* a large emission pass in the order of direction octant and origin
+		 * cell: the photons of a warp then leave one light into one octant
+		 * (the queue's order is arbitrary anyway: its slots come from
+		 * atomics, and each entry carries its photon's identity); the
+		 * bounced passes gain less than their sort costs */
+		if(pass == 0 && n_live >= PHOTON_SORT_MIN)
 			if(int r = R.sort_photon_pass(cur, n_live, s)) return r;
 		if(launch_trace(R, PS, R.pq[cur], n_live, "photon_trace", s)) return SRAY_ECUDA;
 		LAUNCH(R, "photon_bounce", s, k_photon_bounce<<<grid_n(n_live, 128), 128, 0, s>>>(PS, PSet, R.pq[cur], R.phits.as<int4>(),

@@ -168,9 +168,9 @@ struct Renderer {
 	DevBuf pqbuf[2], phits, pfbl, pcounts, pctr;
 	RayQueue pq[2];
 	int pqcap[2] = {0, 0};
-	/* photon passes of at least PHOTON_SORT_MIN photons are sorted before
-	 * they are traced, with scratch of their own (the photon stream runs
-	 * beside the frame's) */
+	/* an emission pass of at least PHOTON_SORT_MIN photons is sorted before
+	 * it is traced, with scratch of its own (the photon stream runs beside
+	 * the frame's) */
 	DevBuf pqsbuf, ps_keys, ps_hist, ps_part;
 	RayQueue pqs = {};
 	int pqscap = 0;
