@@ -24,7 +24,7 @@ CU_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-prec-div=true", "
 CC_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-I/usr/local/cuda/include"]
 
 SOURCES = ["render.cu", "photon.cu", "nrc.cu", "scene_host.cc", "bvh_host.cc"]
-HEADERS = ["dev_common.cuh", "renderer.h", "scene_host.h", "sray_device.h", "range_ff.h", "nrc.h", "anim_eval.h"]
+HEADERS = ["dev_common.cuh", "renderer.h", "scene_host.h", "sray_device.h", "range_ff.h", "nrc.h", "anim_eval.h", "slot_order.h"]
 
 
 def _deps():

@@ -28,6 +28,7 @@
 #include "renderer.h"
 #include "nrc.h"
 #include "range_ff.h"
+#include "slot_order.h"
 
 namespace cg = cooperative_groups;
 
@@ -48,20 +49,6 @@ static __device__ __forceinline__ int warp_alloc(int *counter, int n)
 /* ---------------------------------------------------------------- */
 /* primary rays of samples [s0, s0 + width) of every active pixel; the ray's
  * accumulator slot is (active index * width + sample - s0) */
-/* The pixel of active slot a: the batch's list when there is one, else --
- * the first batch -- for a single frame of tw x th pixels the pixels in
- * bands of four rows, column-major within a band, so that the 32 rays of a
- * warp leave from an 8 x 4 patch (and the rays they spawn keep that
- * order); tw = 0: slot a is pixel a (a batch of jobs) */
-__device__ __forceinline__ int slot_pixel(const int *active, int a, int tw, int th)
-{
-	if(active) return active[a];
-	if(tw <= 0) return a;
-	const int band = a / (4 * tw), r = a - band * 4 * tw;
-	const int hb = th - 4 * band < 4 ? th - 4 * band : 4;
-	return (4 * band + r % hb) * tw + r / hb;
-}
-
 __global__ void k_camera(DScene S, const int *active, int a0, int na, int s0, int width, RayQueue q, float4 *acc,
 		DevCounters *ctr)
 {
