@@ -32,3 +32,16 @@ def test_reference_bands_cover_the_image():
     assert all(0 <= a < b <= 1080 and b - a == 8 for a, b in bands)
     assert bands[0][0] < 68 and bands[-1][1] > 1000
     assert all(b0[1] <= b1[0] for b0, b1 in zip(bands, bands[1:]))
+
+
+def test_committed_profile_figures_are_read():
+    # the machine-read lines of the committed ncu summary the roofline quotes
+    for kind in ("trace", "shadow", "gather", "trace_packet"):
+        prof = bench.committed_profile(kind)
+        assert prof["source"] == os.path.join("profiles", "roofline_kernels_960x540.md")
+        assert 1.0 <= prof["threads_per_instruction"] <= 32.0, kind
+        assert 0.0 < prof["issue_active"] <= 100.0, kind
+    assert bench.committed_profile("trace_packet")["dram_bytes_per_unit"] is None
+    assert bench.committed_profile("trace")["dram_bytes_per_unit"] > 0.0
+    # the camera rays' packets run at a higher SIMT efficiency than the thread-per-ray kernel
+    assert bench.committed_profile("trace_packet")["threads_per_instruction"] > bench.committed_profile("trace")["threads_per_instruction"]
