@@ -7,14 +7,16 @@
  * Network: 9 inputs (position scaled to the scene box, normal, direction),
  * 12-band sin/cos encoding (216 features), 4 hidden layers of 64 ReLU units,
  * 3 linear outputs; relative L2 loss; Adam.  Weights are kept in FP32 (the
- * Adam master copy) and used as BF16 by warp-level tensor-core MMAs
- * (mma.sync m16n8k16, FP32 accumulation): a warp carries 16 samples through
- * all five layers with the activations in registers, the accumulator tile of
- * one layer becoming the operand tile of the next.
+ * Adam master copy) and used as BF16 with FP32 accumulation: inference and
+ * queries on the 5th-generation tensor cores (tcgen05.mma, a 128-sample tile
+ * per MMA); the training step by warp-level MMAs (mma.sync m16n8k16: a warp
+ * carries 16 samples through all five layers with the activations in
+ * registers, the accumulator tile of one layer becoming the operand tile of
+ * the next).
  *
  *   k_nrc_forward_tc<FWD_INFER>  inference: encode + 5 layers on the
- *                         5th-generation tensor cores (tcgen05.mma, TMEM
- *                         accumulators), a 128-sample tile per MMA
+ *                         5th-generation tensor cores (TMEM accumulators
+ *                         and hidden operands, three tiles in flight per SM)
  *   k_nrc_forward_tc<FWD_QUERY>  the renderer's queries: the same, the output
  *                         weighted into the pixel's accumulator
  *   k_nrc_forward<FWD_TRAIN>  training forward (warp-level MMA): also stores
