@@ -282,8 +282,9 @@ int sray_gpu_photon_gather(int which, int n, const float *pos, const float *norm
  * held on every GPU that loads the library until the process exits).
  *  - n > SRAY_NOALLOC_MAX_POINTS is rejected with SRAY_EINVAL.
  *  - The first call on a device looks up the array's device address on that
- *    device (the renderer's, which must be current); make that first call
- *    before any stream capture.
+ *    device (the renderer's, which must be current).  No call may be made
+ *    while a stream is being captured into a graph: every call waits for its
+ *    stream (below).
  *  - All calls share the one array and it keeps the previous call's
  *    requests; each call writes all the requests it reads, so nothing needs
  *    clearing, but calls that overlap on the GPU (several host threads or
